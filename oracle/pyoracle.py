@@ -1,0 +1,192 @@
+"""ORACLE / TEST INFRASTRUCTURE ONLY: ctypes bindings of the two CPU checkers.
+
+* ``Oracle``    -- liborb_oracle.so, this repository's CPU restatement of the
+  reference path (orb_oracle.cpp).  Builds anywhere.
+* ``RefOracle`` -- oracle/_ref/libref_orb.so, the reference's own sources
+  compiled against the cv stand-in (only where those sources are present).
+Both expose the same methods so tests can run one against the other.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liborb_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_orb.so")
+
+KP_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("size", "<f4"), ("angle", "<f4"), ("response", "<f4"),
+                     ("octave", "<i4"), ("class_id", "<i4")])
+MP_DTYPE = np.dtype([("proj_x", "<f4"), ("proj_y", "<f4"), ("proj_xr", "<f4"), ("view_cos", "<f4"),
+                     ("track_scale_level", "<i4"), ("track_in_view", "<i4"), ("bad", "<i4"), ("pad", "<i4")])
+
+
+class Params(C.Structure):
+    _fields_ = [("nfeatures", C.c_int), ("scale_factor", C.c_float), ("nlevels", C.c_int),
+                ("ini_th_fast", C.c_int), ("min_th_fast", C.c_int)]
+
+
+@dataclass
+class ExtractResult:
+    keypoints: np.ndarray  # KP_DTYPE
+    descriptors: np.ndarray  # N x 32 uint8
+    pyramid: list  # unblurred levels (uint8 2-D arrays)
+
+
+def build(ref: bool = False) -> None:
+    """Compile the restatement (and, with ref=True, the reference harness)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"] + (["ref"] if ref else []), check=True)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def level_sizes(w: int, h: int, nlevels: int, scale_factor: float):
+    """Level dimensions exactly as src/ORBextractor.cc:1661-1663 computes them."""
+    inv = scale_tables(nlevels, scale_factor)[1]
+    return [(int(np.rint(np.float32(w) * inv[l])), int(np.rint(np.float32(h) * inv[l]))) for l in range(nlevels)]
+
+
+def scale_tables(nlevels: int, scale_factor: float):
+    """mvScaleFactor / mvInvScaleFactor (src/ORBextractor.cc:478-500): the
+    running product is taken in double (scaleFactor is a double member) and
+    stored as float."""
+    sf = np.float64(np.float32(scale_factor))
+    s = [np.float32(1.0)]
+    for _ in range(1, nlevels):
+        s.append(np.float32(np.float64(s[-1]) * sf))
+    inv = [np.float32(np.float32(1.0) / x) for x in s]
+    return s, inv
+
+
+class _Base:
+    def __init__(self, path: str):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        self.prefix = "ref_" if "ref_orb" in path else "orc_"
+
+    def fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def extract(self, img: np.ndarray, nfeatures=1000, scale_factor=1.2, nlevels=8, ini_th=20, min_th=7,
+                want_pyramid=True) -> ExtractResult:
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape
+        p = Params(nfeatures, scale_factor, nlevels, ini_th, min_th)
+        cap = max(4 * nfeatures + 64, 256)
+        kps = np.zeros(cap, KP_DTYPE)
+        desc = np.zeros((cap, 32), np.uint8)
+        n = C.c_int(0)
+        sizes = level_sizes(w, h, nlevels, scale_factor)
+        tot = sum(a * b for a, b in sizes)
+        pyr = np.zeros(tot, np.uint8) if want_pyramid else None
+        rc = self.fn("extract")(_p(img), w, h, C.c_size_t(w), C.byref(p), _p(kps), _p(desc), cap, C.byref(n),
+                                _p(pyr), C.c_size_t(tot))
+        if rc != 0:
+            raise RuntimeError(f"extract rc={rc}")
+        levels = []
+        if want_pyramid:
+            off = 0
+            for lw, lh in sizes:
+                levels.append(pyr[off:off + lw * lh].reshape(lh, lw))
+                off += lw * lh
+        return ExtractResult(kps[:n.value].copy(), desc[:n.value].copy(), levels)
+
+    def descriptor_distance(self, a: np.ndarray, b: np.ndarray) -> int:
+        a = np.ascontiguousarray(a, np.uint8)
+        b = np.ascontiguousarray(b, np.uint8)
+        return int(self.fn("descriptor_distance")(_p(a), _p(b)))
+
+    def features_in_area(self, kps, w, h, x, y, r, min_level=-1, max_level=-1, nlevels=8, scale_factor=1.2):
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        out = np.zeros(max(len(kps), 1), np.int32)
+        f = self.fn("features_in_area")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                      C.c_int, C.c_int, C.c_void_p, C.c_int]
+        n = f(C.byref(p), _p(kps), len(kps), w, h, x, y, r, min_level, max_level, _p(out), len(out))
+        return out[:n].copy()
+
+    def search_for_initialization(self, kps1, desc1, kps2, desc2, w, h, prev_xy=None, window=100, nnratio=0.9,
+                                  check_ori=True, nlevels=8, scale_factor=1.2):
+        kps1 = np.ascontiguousarray(kps1, KP_DTYPE)
+        kps2 = np.ascontiguousarray(kps2, KP_DTYPE)
+        desc1 = np.ascontiguousarray(desc1, np.uint8)
+        desc2 = np.ascontiguousarray(desc2, np.uint8)
+        if prev_xy is None:
+            prev_xy = np.stack([kps1["x"], kps1["y"]], axis=1)
+        prev = np.ascontiguousarray(prev_xy, np.float32).copy()
+        m12 = np.zeros(max(len(kps1), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("search_for_initialization")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                      C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_void_p]
+        nm = f(C.byref(p), _p(kps1), _p(desc1), len(kps1), _p(kps2), _p(desc2), len(kps2), w, h, _p(prev),
+               window, nnratio, int(check_ori), _p(m12))
+        return int(nm), m12[:len(kps1)].copy(), prev
+
+    def search_by_projection(self, kps, desc, w, h, mps, mp_desc, th=1.0, nnratio=0.8, uright=None, claimed=None,
+                             nlevels=8, scale_factor=1.2):
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        desc = np.ascontiguousarray(desc, np.uint8)
+        mps = np.ascontiguousarray(mps, MP_DTYPE)
+        mp_desc = np.ascontiguousarray(mp_desc, np.uint8)
+        ur = None if uright is None else np.ascontiguousarray(uright, np.float32)
+        cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
+        out = np.zeros(max(len(kps), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("search_by_projection")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                      C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
+        nm = f(C.byref(p), _p(kps), _p(desc), _p(ur), len(kps), w, h, _p(mps), _p(mp_desc), len(mps), th, nnratio,
+               _p(cl), _p(out))
+        return int(nm), out[:len(kps)].copy()
+
+    def compute_stereo_matches(self, kpsL, descL, kpsR, descR, pyrL, pyrR, w, h, bf, fx, nlevels=8,
+                               scale_factor=1.2):
+        kpsL = np.ascontiguousarray(kpsL, KP_DTYPE)
+        kpsR = np.ascontiguousarray(kpsR, KP_DTYPE)
+        descL = np.ascontiguousarray(descL, np.uint8)
+        descR = np.ascontiguousarray(descR, np.uint8)
+        lw = np.array([l.shape[1] for l in pyrL], np.int32)
+        lh = np.array([l.shape[0] for l in pyrL], np.int32)
+        pl = np.ascontiguousarray(np.concatenate([l.ravel() for l in pyrL]))
+        pr = np.ascontiguousarray(np.concatenate([l.ravel() for l in pyrR]))
+        ur = np.zeros(max(len(kpsL), 1), np.float32)
+        dp = np.zeros(max(len(kpsL), 1), np.float32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("compute_stereo_matches")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p,
+                      C.c_void_p]
+        f(C.byref(p), _p(kpsL), _p(descL), len(kpsL), _p(kpsR), _p(descR), len(kpsR), _p(pl), _p(pr), _p(lw),
+          _p(lh), w, h, bf, fx, _p(ur), _p(dp))
+        return ur[:len(kpsL)].copy(), dp[:len(kpsL)].copy()
+
+    def knn2(self, q, t):
+        q = np.ascontiguousarray(q, np.uint8)
+        t = np.ascontiguousarray(t, np.uint8)
+        nq = len(q)
+        outs = [np.zeros(max(nq, 1), np.int32) for _ in range(4)]
+        self.fn("knn2")(_p(q), nq, _p(t), len(t), *[_p(o) for o in outs])
+        return tuple(o[:nq].copy() for o in outs)
+
+
+class Oracle(_Base):
+    def __init__(self, path: str = ORACLE_SO):
+        super().__init__(path)
+
+
+class RefOracle(_Base):
+    def __init__(self, path: str = REF_SO):
+        super().__init__(path)
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)

@@ -1,0 +1,386 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// C entry points around the reference's own, unmodified ORB-SLAM2 sources
+// (src/ORBextractor.cc, src/ORBmatcher.cc, src/Frame.cc), compiled against the
+// cv stand-in in ../cvshim.  Used to pin the oracle restatement
+// (../orb_oracle.cpp) and to generate the golden fixtures under tests/golden.
+//
+// Determinism of DistributeOctTree: src/ORBextractor.cc:926 sorts
+// (size, ExtractorNode*) pairs, so equal-size nodes are ordered by heap
+// address.  This library replaces the global allocator with a monotonic arena,
+// which makes address order equal allocation order, i.e. the order in which
+// the std::list nodes were created.  The restatement and the CUDA kernels use
+// that creation order explicitly.
+#include <algorithm>
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <list>
+#include <map>
+#include <mutex>
+#include <new>
+#include <set>
+#include <string>
+#include <thread>
+#include <vector>
+#include <sys/mman.h>
+
+#include <opencv2/core/core.hpp>
+
+// The harness needs Frame::AssignFeaturesToGrid (private) and
+// MapPoint::mDescriptor (protected) to build frames and map points from
+// recorded keypoints; the reference files themselves are compiled unchanged.
+#define private public
+#define protected public
+#include "Frame.h"
+#include "MapPoint.h"
+#include "ORBextractor.h"
+#include "ORBmatcher.h"
+#undef private
+#undef protected
+
+#include "../orb_types.h"
+
+// ------------------------------------------------------------------ arena
+namespace {
+struct Arena {
+    char* base = nullptr;
+    size_t cap = 0;
+    size_t top = 0;
+    size_t mark = 0;
+    long live_since_mark = 0;
+    Arena() {
+        cap = (size_t)64 << 30;
+        void* p = mmap(nullptr, cap, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS | MAP_NORESERVE, -1, 0);
+        if (p == MAP_FAILED) { std::fprintf(stderr, "ref arena: mmap failed\n"); std::abort(); }
+        base = (char*)p;
+    }
+    void* alloc(size_t n) {
+        n = (n + 15) & ~(size_t)15;
+        if (n == 0) n = 16;
+        if (top + n > cap) { std::fprintf(stderr, "ref arena exhausted\n"); std::abort(); }
+        void* p = base + top;
+        top += n;
+        live_since_mark++;
+        return p;
+    }
+    bool owns(void* p) const { return (char*)p >= base && (char*)p < base + cap; }
+    void release(void* p) {
+        if ((size_t)((char*)p - base) >= mark) live_since_mark--;
+    }
+};
+Arena& arena() {
+    static Arena* a = new (std::malloc(sizeof(Arena))) Arena();
+    return *a;
+}
+// Scope of one harness call: everything allocated inside and freed before the
+// end is reclaimed, so repeated calls do not grow the arena.
+struct ArenaScope {
+    size_t saved_mark;
+    long saved_live;
+    ArenaScope() {
+        Arena& a = arena();
+        saved_mark = a.mark;
+        saved_live = a.live_since_mark;
+        a.mark = a.top;
+        a.live_since_mark = 0;
+    }
+    ~ArenaScope() {
+        Arena& a = arena();
+        if (a.live_since_mark == 0) {
+            const size_t page = 4096;
+            size_t lo = (a.mark + page - 1) & ~(page - 1);
+            if (a.top > lo) madvise(a.base + lo, a.top - lo, MADV_DONTNEED);
+            a.top = a.mark;
+        }
+        a.mark = saved_mark;
+        a.live_since_mark = saved_live + a.live_since_mark;
+    }
+};
+}  // namespace
+
+void* operator new(size_t n) { return arena().alloc(n); }
+void* operator new[](size_t n) { return arena().alloc(n); }
+void* operator new(size_t n, const std::nothrow_t&) noexcept { return arena().alloc(n); }
+void* operator new[](size_t n, const std::nothrow_t&) noexcept { return arena().alloc(n); }
+void operator delete(void* p) noexcept {
+    if (!p) return;
+    if (arena().owns(p)) arena().release(p);
+    else std::free(p);
+}
+void operator delete[](void* p) noexcept { operator delete(p); }
+void operator delete(void* p, size_t) noexcept { operator delete(p); }
+void operator delete[](void* p, size_t) noexcept { operator delete(p); }
+
+using namespace ORB_SLAM2;
+
+namespace {
+
+void copy_kps_out(const std::vector<cv::KeyPoint>& kps, orc_kp* out) {
+    for (size_t i = 0; i < kps.size(); i++) {
+        out[i].x = kps[i].pt.x;
+        out[i].y = kps[i].pt.y;
+        out[i].size = kps[i].size;
+        out[i].angle = kps[i].angle;
+        out[i].response = kps[i].response;
+        out[i].octave = kps[i].octave;
+        out[i].class_id = kps[i].class_id;
+    }
+}
+
+std::vector<cv::KeyPoint> kps_in(const orc_kp* kps, int n) {
+    std::vector<cv::KeyPoint> v(n);
+    for (int i = 0; i < n; i++)
+        v[i] = cv::KeyPoint(kps[i].x, kps[i].y, kps[i].size, kps[i].angle, kps[i].response, kps[i].octave,
+                            kps[i].class_id);
+    return v;
+}
+
+// A Frame as the reference's constructors leave it (src/Frame.cc:313-393 for
+// an image without distortion), built from recorded keypoints/descriptors.
+Frame* make_frame(ORBextractor* ext, const orc_kp* kps, const uint8_t* desc, int n, int w, int h, const float* uright) {
+    Frame* F = new Frame();
+    F->mpORBextractorLeft = ext;
+    F->mpORBextractorRight = nullptr;
+    F->N = n;
+    F->mvKeys = kps_in(kps, n);
+    F->mvKeysUn = F->mvKeys;
+    F->mDescriptors = cv::Mat(n, 32, CV_8U);
+    if (n) std::memcpy(F->mDescriptors.data, desc, (size_t)n * 32);
+    F->mvuRight = std::vector<float>(n, -1.f);
+    if (uright)
+        for (int i = 0; i < n; i++) F->mvuRight[i] = uright[i];
+    F->mvDepth = std::vector<float>(n, -1.f);
+    F->mvpMapPoints = std::vector<MapPoint*>(n, static_cast<MapPoint*>(NULL));
+    F->mvbOutlier = std::vector<bool>(n, false);
+    F->mnScaleLevels = ext->GetLevels();
+    F->mfScaleFactor = ext->GetScaleFactor();
+    F->mvScaleFactors = ext->GetScaleFactors();
+    F->mvInvScaleFactors = ext->GetInverseScaleFactors();
+    F->mvLevelSigma2 = ext->GetScaleSigmaSquares();
+    F->mvInvLevelSigma2 = ext->GetInverseScaleSigmaSquares();
+    // ComputeImageBounds without distortion + the grid constants
+    // (src/Frame.cc:783-819, :372-388).
+    Frame::mnMinX = 0.0f;
+    Frame::mnMaxX = w;
+    Frame::mnMinY = 0.0f;
+    Frame::mnMaxY = h;
+    Frame::mfGridElementWidthInv = static_cast<float>(FRAME_GRID_COLS) / static_cast<float>(Frame::mnMaxX - Frame::mnMinX);
+    Frame::mfGridElementHeightInv = static_cast<float>(FRAME_GRID_ROWS) / static_cast<float>(Frame::mnMaxY - Frame::mnMinY);
+    F->AssignFeaturesToGrid();
+    return F;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ORBextractor(...)(image, Mat(), keypoints, descriptors) -- src/ORBextractor.cc:1533.
+// pyr (optional) receives the unblurred pyramid levels back to back.
+int ref_extract(const uint8_t* img, int w, int h, size_t step, const orc_params* p, orc_kp* kps, uint8_t* desc,
+                int cap, int* n_out, uint8_t* pyr, size_t pyr_cap) {
+    ArenaScope scope;
+    int rc = 0;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        cv::Mat image(h, w, CV_8UC1, (void*)img, step);
+        std::vector<cv::KeyPoint> keys;
+        cv::Mat descriptors;
+        ext(image, cv::Mat(), keys, descriptors);
+        *n_out = (int)keys.size();
+        if ((int)keys.size() > cap) rc = -1;
+        else {
+            copy_kps_out(keys, kps);
+            if (!keys.empty()) std::memcpy(desc, descriptors.data, keys.size() * 32);
+        }
+        if (pyr) {
+            size_t off = 0;
+            for (int l = 0; l < p->nlevels && rc == 0; l++) {
+                const cv::Mat& L = ext.mvImagePyramid[l];
+                if (off + (size_t)L.rows * L.cols > pyr_cap) { rc = -2; break; }
+                for (int y = 0; y < L.rows; y++) std::memcpy(pyr + off + (size_t)y * L.cols, L.ptr(y), L.cols);
+                off += (size_t)L.rows * L.cols;
+            }
+        }
+    }
+    return rc;
+}
+
+// Scale tables and per-level budgets of the ORBextractor constructor
+// (src/ORBextractor.cc:469-571).
+int ref_extractor_tables(const orc_params* p, float* scale, float* inv_scale, float* sigma2, float* inv_sigma2,
+                         int* features_per_level, int* umax16) {
+    ArenaScope scope;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        for (int l = 0; l < p->nlevels; l++) {
+            scale[l] = ext.mvScaleFactor[l];
+            inv_scale[l] = ext.mvInvScaleFactor[l];
+            sigma2[l] = ext.mvLevelSigma2[l];
+            inv_sigma2[l] = ext.mvInvLevelSigma2[l];
+            features_per_level[l] = ext.mnFeaturesPerLevel[l];
+        }
+        for (int v = 0; v < 16; v++) umax16[v] = ext.umax[v];
+    }
+    return 0;
+}
+
+int ref_descriptor_distance(const uint8_t* a, const uint8_t* b) {
+    ArenaScope scope;
+    int d;
+    {
+        cv::Mat A(1, 32, CV_8U, (void*)a), B(1, 32, CV_8U, (void*)b);
+        d = ORBmatcher::DescriptorDistance(A, B);
+    }
+    return d;
+}
+
+// Frame::GetFeaturesInArea (src/Frame.cc:590) on a frame built from keypoints.
+int ref_features_in_area(const orc_params* p, const orc_kp* kps, int n, int w, int h, float x, float y, float r,
+                         int minLevel, int maxLevel, int* out, int cap) {
+    ArenaScope scope;
+    int cnt;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        std::vector<uint8_t> desc((size_t)n * 32 + 32, 0);
+        Frame* F = make_frame(&ext, kps, desc.data(), n, w, h, nullptr);
+        std::vector<size_t> v = F->GetFeaturesInArea(x, y, r, minLevel, maxLevel);
+        cnt = (int)v.size();
+        for (int i = 0; i < cnt && i < cap; i++) out[i] = (int)v[i];
+        delete F;
+    }
+    return cnt;
+}
+
+// ORBmatcher(nnratio, checkOri).SearchForInitialization(F1, F2, vbPrevMatched,
+// vnMatches12, windowSize) -- src/ORBmatcher.cc:573-717.
+int ref_search_for_initialization(const orc_params* p, const orc_kp* kps1, const uint8_t* desc1, int n1,
+                                  const orc_kp* kps2, const uint8_t* desc2, int n2, int w, int h,
+                                  float* prev_matched_xy, int window, float nnratio, int check_ori,
+                                  int* matches12) {
+    ArenaScope scope;
+    int nm;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame* F1 = make_frame(&ext, kps1, desc1, n1, w, h, nullptr);
+        Frame* F2 = make_frame(&ext, kps2, desc2, n2, w, h, nullptr);
+        std::vector<cv::Point2f> prev(n1);
+        for (int i = 0; i < n1; i++) prev[i] = cv::Point2f(prev_matched_xy[2 * i], prev_matched_xy[2 * i + 1]);
+        std::vector<int> m12;
+        ORBmatcher matcher(nnratio, check_ori != 0);
+        nm = matcher.SearchForInitialization(*F1, *F2, prev, m12, window);
+        for (int i = 0; i < n1; i++) {
+            matches12[i] = m12[i];
+            prev_matched_xy[2 * i] = prev[i].x;
+            prev_matched_xy[2 * i + 1] = prev[i].y;
+        }
+        delete F1;
+        delete F2;
+    }
+    return nm;
+}
+
+// ORBmatcher(nnratio).SearchByProjection(F, vpMapPoints, th) -- src/ORBmatcher.cc:72-183.
+// claimed[i] != 0 marks frame keypoints that already hold a map point with
+// observations (skipped by :128-130).  match_out[i] receives the index of the
+// map point now assigned to keypoint i, -2 for a pre-claimed keypoint, -1 for none.
+int ref_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright,
+                             int n, int w, int h, const orc_mappoint* mps, const uint8_t* mp_desc, int m,
+                             float th, float nnratio, const uint8_t* claimed, int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame* F = make_frame(&ext, kps, desc, n, w, h, uright);
+        cv::Mat pos = cv::Mat::zeros(3, 1, CV_32F);
+        MapPoint* preclaimed = new MapPoint(pos, nullptr, nullptr);
+        std::vector<MapPoint*> vmp(m);
+        std::map<MapPoint*, int> index;
+        for (int i = 0; i < m; i++) {
+            MapPoint* mp = new MapPoint(pos, nullptr, nullptr);
+            mp->mTrackProjX = mps[i].proj_x;
+            mp->mTrackProjY = mps[i].proj_y;
+            mp->mTrackProjXR = mps[i].proj_xr;
+            mp->mTrackViewCos = mps[i].view_cos;
+            mp->mnTrackScaleLevel = mps[i].track_scale_level;
+            mp->mbTrackInView = mps[i].track_in_view != 0;
+            mp->mbBad = mps[i].bad != 0;
+            mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+            std::memcpy(mp->mDescriptor.data, mp_desc + (size_t)i * 32, 32);
+            vmp[i] = mp;
+            index[mp] = i;
+        }
+        for (int i = 0; i < n; i++)
+            if (claimed && claimed[i]) F->mvpMapPoints[i] = preclaimed;
+        ORBmatcher matcher(nnratio, true);
+        nm = matcher.SearchByProjection(*F, vmp, th);
+        for (int i = 0; i < n; i++) {
+            MapPoint* mp = F->mvpMapPoints[i];
+            match_out[i] = mp == nullptr ? -1 : (mp == preclaimed ? -2 : index[mp]);
+        }
+        for (int i = 0; i < m; i++) delete vmp[i];
+        delete preclaimed;
+        delete F;
+    }
+    return nm;
+}
+
+// Frame::ComputeStereoMatches -- src/Frame.cc:831-1082, on frames built from
+// recorded keypoints and the unblurred pyramids (levels back to back).  mb is
+// set to mbf/fx first: the stereo constructor reads it before assigning it
+// (src/Frame.cc:154 vs :202), and mbf/fx is its value for every later frame.
+int ref_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
+                               const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,
+                               const uint8_t* pyrR, const int* level_w, const int* level_h, int w, int h, float bf,
+                               float fx, float* uright, float* depth) {
+    ArenaScope scope;
+    {
+        ORBextractor extL(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        ORBextractor extR(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        size_t off = 0;
+        for (int l = 0; l < p->nlevels; l++) {
+            extL.mvImagePyramid[l] = cv::Mat(level_h[l], level_w[l], CV_8UC1, (void*)(pyrL + off));
+            extR.mvImagePyramid[l] = cv::Mat(level_h[l], level_w[l], CV_8UC1, (void*)(pyrR + off));
+            off += (size_t)level_w[l] * level_h[l];
+        }
+        Frame* F = make_frame(&extL, kpsL, descL, nL, w, h, nullptr);
+        F->mpORBextractorRight = &extR;
+        F->mvKeysRight = kps_in(kpsR, nR);
+        F->mDescriptorsRight = cv::Mat(nR, 32, CV_8U);
+        if (nR) std::memcpy(F->mDescriptorsRight.data, descR, (size_t)nR * 32);
+        F->mbf = bf;
+        Frame::fx = fx;
+        F->mb = F->mbf / Frame::fx;
+        F->ComputeStereoMatches();
+        for (int i = 0; i < nL; i++) {
+            uright[i] = F->mvuRight[i];
+            depth[i] = F->mvDepth[i];
+        }
+        delete F;
+    }
+    return 0;
+}
+
+// Brute-force k=2 over ORBmatcher::DescriptorDistance (src/ORBmatcher.cc:2083):
+// for each query, best and second-best train rows, ties to the lower index.
+int ref_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int* d1, int* idx2, int* d2) {
+    ArenaScope scope;
+    {
+        for (int i = 0; i < nq; i++) {
+            cv::Mat Q(1, 32, CV_8U, (void*)(q + (size_t)i * 32));
+            int b1 = INT_MAX, b2 = INT_MAX, i1 = -1, i2 = -1;
+            for (int j = 0; j < nt; j++) {
+                cv::Mat T(1, 32, CV_8U, (void*)(t + (size_t)j * 32));
+                int d = ORBmatcher::DescriptorDistance(Q, T);
+                if (d < b1) { b2 = b1; i2 = i1; b1 = d; i1 = j; }
+                else if (d < b2) { b2 = d; i2 = j; }
+            }
+            idx1[i] = i1; d1[i] = b1; idx2[i] = i2; d2[i] = b2;
+        }
+    }
+    return 0;
+}
+
+}  // extern "C"

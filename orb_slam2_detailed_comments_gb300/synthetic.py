@@ -1,0 +1,131 @@
+"""Seeded synthetic inputs for the ORB front-end workloads.
+
+No public dataset is used: every image is generated from a seed with the
+shapes, sizes and value distributions of the benchmark workloads --
+200 filled rectangles / ellipses with uniform intensities 0-255 over a random
+background, plus a 3x3-smoothed Gaussian noise layer (sigma 8), clipped to
+uint8.  Second views are homography warps (rotation <= 3 deg, translation <=
+10 px, + noise sigma 2); stereo right views shift each pixel by a
+piecewise-planar disparity in 5-80 px (+ noise sigma 2).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _smooth3(a: np.ndarray) -> np.ndarray:
+    p = np.pad(a, 1, mode="edge")
+    h, w = a.shape
+    s = np.zeros_like(a)
+    for dy in range(3):
+        for dx in range(3):
+            s += p[dy:dy + h, dx:dx + w]
+    return s / 9.0
+
+
+def scene(w: int, h: int, seed: int, n_shapes: int = 200, noise_sigma: float = 8.0) -> np.ndarray:
+    """A w x h uint8 scene of random filled rectangles and ellipses."""
+    rng = np.random.default_rng(seed)
+    img = np.full((h, w), float(rng.integers(0, 256)), dtype=np.float32)
+    yy, xx = np.mgrid[0:h, 0:w]
+    max_half = max(8, min(w, h) // 6)
+    for _ in range(n_shapes):
+        cx, cy = rng.uniform(0, w), rng.uniform(0, h)
+        ax, ay = rng.uniform(3, max_half), rng.uniform(3, max_half)
+        val = float(rng.integers(0, 256))
+        x0, x1 = max(0, int(cx - ax) - 1), min(w, int(cx + ax) + 2)
+        y0, y1 = max(0, int(cy - ay) - 1), min(h, int(cy + ay) + 2)
+        if x0 >= x1 or y0 >= y1:
+            continue
+        sx, sy = xx[y0:y1, x0:x1], yy[y0:y1, x0:x1]
+        if rng.random() < 0.5:
+            m = (np.abs(sx - cx) <= ax) & (np.abs(sy - cy) <= ay)
+        else:
+            m = ((sx - cx) / ax) ** 2 + ((sy - cy) / ay) ** 2 <= 1.0
+        img[y0:y1, x0:x1][m] = val
+    noise = _smooth3(rng.normal(0.0, noise_sigma, size=(h, w)).astype(np.float32))
+    return np.clip(np.rint(img + noise), 0, 255).astype(np.uint8)
+
+
+def _bilinear(img: np.ndarray, sx: np.ndarray, sy: np.ndarray) -> np.ndarray:
+    h, w = img.shape
+    sx = np.clip(sx, 0, w - 1.0001)
+    sy = np.clip(sy, 0, h - 1.0001)
+    x0, y0 = np.floor(sx).astype(np.int64), np.floor(sy).astype(np.int64)
+    fx, fy = sx - x0, sy - y0
+    a = img.astype(np.float32)
+    return ((a[y0, x0] * (1 - fx) + a[y0, x0 + 1] * fx) * (1 - fy)
+            + (a[y0 + 1, x0] * (1 - fx) + a[y0 + 1, x0 + 1] * fx) * fy)
+
+
+def random_homography(w: int, h: int, rng: np.random.Generator, max_rot_deg: float = 3.0,
+                      max_shift: float = 10.0) -> np.ndarray:
+    """Rotation about the image centre plus a translation, as a 3x3 matrix."""
+    th = np.deg2rad(rng.uniform(-max_rot_deg, max_rot_deg))
+    tx, ty = rng.uniform(-max_shift, max_shift, size=2)
+    c, s = np.cos(th), np.sin(th)
+    cx, cy = w / 2.0, h / 2.0
+    return np.array([[c, -s, cx - c * cx + s * cy + tx],
+                     [s, c, cy - s * cx - c * cy + ty],
+                     [0.0, 0.0, 1.0]])
+
+
+def warp(img: np.ndarray, H: np.ndarray, seed: int, noise_sigma: float = 2.0) -> np.ndarray:
+    """img warped by H (destination pixel p samples source H^-1 p) plus noise."""
+    rng = np.random.default_rng(seed)
+    h, w = img.shape
+    Hi = np.linalg.inv(H)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    den = Hi[2, 0] * xx + Hi[2, 1] * yy + Hi[2, 2]
+    sx = (Hi[0, 0] * xx + Hi[0, 1] * yy + Hi[0, 2]) / den
+    sy = (Hi[1, 0] * xx + Hi[1, 1] * yy + Hi[1, 2]) / den
+    out = _bilinear(img, sx, sy) + rng.normal(0.0, noise_sigma, size=(h, w))
+    return np.clip(np.rint(out), 0, 255).astype(np.uint8)
+
+
+def frame_pair(w: int, h: int, seed: int):
+    """(frame1, frame2, H): frame2 is frame1 under a small homography + noise."""
+    f1 = scene(w, h, seed)
+    rng = np.random.default_rng(seed + 7919)
+    H = random_homography(w, h, rng)
+    return f1, warp(f1, H, seed + 104729), H
+
+
+def disparity_map(w: int, h: int, rng: np.random.Generator, dmin: float = 5.0, dmax: float = 80.0) -> np.ndarray:
+    """Piecewise-planar disparity: a few vertical bands, each its own plane."""
+    d = np.empty((h, w), dtype=np.float64)
+    nb = int(rng.integers(3, 7))
+    cuts = np.sort(rng.uniform(0, w, size=nb - 1)).astype(int)
+    edges = [0, *cuts.tolist(), w]
+    yy, xx = np.mgrid[0:h, 0:w]
+    for i in range(nb):
+        a = rng.uniform(dmin, dmax)
+        gx, gy = rng.uniform(-0.03, 0.03), rng.uniform(-0.05, 0.05)
+        sl = slice(edges[i], edges[i + 1])
+        d[:, sl] = a + gx * (xx[:, sl] - edges[i]) + gy * (yy[:, sl] - h / 2)
+    return np.clip(d, dmin, dmax)
+
+
+def stereo_pair(w: int, h: int, seed: int, noise_sigma: float = 2.0):
+    """(left, right, disparity): right(x, y) = left(x + d(x, y), y) + noise."""
+    left = scene(w, h, seed)
+    rng = np.random.default_rng(seed + 31337)
+    d = disparity_map(w, h, rng)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    right = _bilinear(left, xx + d, yy) + rng.normal(0.0, noise_sigma, size=(h, w))
+    return left, np.clip(np.rint(right), 0, 255).astype(np.uint8), d
+
+
+def random_descriptors(n: int, seed: int) -> np.ndarray:
+    """n x 32 uint8 descriptors with independent Bernoulli(0.5) bits."""
+    return np.random.default_rng(seed).integers(0, 256, size=(n, 32), dtype=np.uint8)
+
+
+def clustered_descriptors(n: int, n_centres: int, flip_p: float, seed: int) -> np.ndarray:
+    """n descriptors, each a random centre XOR Bernoulli(flip_p) bit flips."""
+    rng = np.random.default_rng(seed)
+    centres = rng.integers(0, 256, size=(n_centres, 32), dtype=np.uint8)
+    pick = rng.integers(0, n_centres, size=n)
+    bits = rng.random(size=(n, 256)) < flip_p
+    flips = np.packbits(bits, axis=1, bitorder="little")
+    return centres[pick] ^ flips
