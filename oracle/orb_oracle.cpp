@@ -1,0 +1,755 @@
+// orb_oracle.cpp -- ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of ORB-SLAM2's feature front-end (see orb_oracle.h).  The
+// code is this repository's own; each function names the reference lines it
+// restates.  OpenCV primitives come from cvshim/cvshim_prims.h.
+//
+// DistributeOctTree is restated with explicit node creation numbers instead of
+// list node addresses: the reference's list only ever grows at the front
+// after the initial nodes are appended, so list order is "non-initial nodes by
+// creation number descending, then initial nodes ascending", and the
+// (size, node*) sort at src/ORBextractor.cc:926 breaks size ties by creation
+// order once allocation order is made monotonic.
+#include "orb_oracle.h"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "cvshim/cvshim_prims.h"
+#include "orb_pattern_table.h"
+
+namespace {
+
+const int kEdgeThreshold = 19;
+const int kHalfPatch = 15;
+const int kPatchSize = 31;
+const int kGridCols = 64;
+const int kGridRows = 48;
+const int kThHigh = 100;
+const int kThLow = 50;
+const int kHistoLength = 30;
+
+struct Tables {
+    int nlevels;
+    std::vector<float> scale, inv_scale, sigma2, inv_sigma2;
+    std::vector<int> nfeat;
+    int umax[kHalfPatch + 1];
+};
+
+// ORBextractor::ORBextractor, src/ORBextractor.cc:469-571.
+Tables make_tables(const orc_params* p) {
+    Tables t;
+    t.nlevels = p->nlevels;
+    const double sf = (double)p->scale_factor;  // scaleFactor is a double member
+    t.scale.assign(p->nlevels, 1.0f);
+    t.sigma2.assign(p->nlevels, 1.0f);
+    for (int i = 1; i < p->nlevels; i++) {
+        t.scale[i] = (float)(t.scale[i - 1] * sf);
+        t.sigma2[i] = t.scale[i] * t.scale[i];
+    }
+    t.inv_scale.resize(p->nlevels);
+    t.inv_sigma2.resize(p->nlevels);
+    for (int i = 0; i < p->nlevels; i++) {
+        t.inv_scale[i] = 1.0f / t.scale[i];
+        t.inv_sigma2[i] = 1.0f / t.sigma2[i];
+    }
+    t.nfeat.assign(p->nlevels, 0);
+    const float factor = (float)(1.0f / sf);
+    float per_scale = p->nfeatures * (1 - factor) / (1 - (float)std::pow((double)factor, (double)p->nlevels));
+    int sum = 0;
+    for (int l = 0; l < p->nlevels - 1; l++) {
+        t.nfeat[l] = shim_cvround_f(per_scale);
+        sum += t.nfeat[l];
+        per_scale *= factor;
+    }
+    t.nfeat[p->nlevels - 1] = std::max(p->nfeatures - sum, 0);
+    const int vmax = (int)std::floor(kHalfPatch * std::sqrt(2.f) / 2 + 1);
+    const int vmin = (int)std::ceil(kHalfPatch * std::sqrt(2.f) / 2);
+    const double hp2 = kHalfPatch * kHalfPatch;
+    for (int v = 0; v <= vmax; ++v) t.umax[v] = shim_cvround_d(std::sqrt(hp2 - v * v));
+    for (int v = kHalfPatch, v0 = 0; v >= vmin; --v) {
+        while (t.umax[v0] == t.umax[v0 + 1]) ++v0;
+        t.umax[v] = v0;
+        ++v0;
+    }
+    return t;
+}
+
+struct Level {
+    int w, h;
+    std::vector<uint8_t> px;
+    const uint8_t* at(int x, int y) const { return &px[(size_t)y * w + x]; }
+};
+
+// ComputePyramid, src/ORBextractor.cc:1655-1724 (the padded border is never
+// read on the path, so only the level interiors are kept).
+std::vector<Level> build_pyramid(const uint8_t* img, int w, int h, size_t step, const Tables& t) {
+    std::vector<Level> pyr(t.nlevels);
+    for (int l = 0; l < t.nlevels; l++) {
+        const float s = t.inv_scale[l];
+        Level& L = pyr[l];
+        L.w = shim_cvround_f((float)w * s);
+        L.h = shim_cvround_f((float)h * s);
+        L.px.resize((size_t)L.w * L.h);
+        if (l == 0) {
+            for (int y = 0; y < h; y++) std::memcpy(&L.px[(size_t)y * w], img + (size_t)y * step, w);
+        } else {
+            const Level& P = pyr[l - 1];
+            shim_resize_linear_u8(P.px.data(), P.w, P.w, P.h, L.px.data(), L.w, L.w, L.h);
+        }
+    }
+    return pyr;
+}
+
+// The per-cell FAST loop of ComputeKeyPointsOctTree, src/ORBextractor.cc:1069-1142.
+std::vector<orc_kp> fast_level(const Level& L, int ini_th, int min_th) {
+    std::vector<orc_kp> out;
+    const int minBorderX = kEdgeThreshold - 3, minBorderY = minBorderX;
+    const int maxBorderX = L.w - kEdgeThreshold + 3, maxBorderY = L.h - kEdgeThreshold + 3;
+    const float W = 30;
+    const float width = (float)(maxBorderX - minBorderX), height = (float)(maxBorderY - minBorderY);
+    const int nCols = (int)(width / W), nRows = (int)(height / W);
+    if (nCols <= 0 || nRows <= 0) return out;
+    const int wCell = (int)std::ceil(width / nCols), hCell = (int)std::ceil(height / nRows);
+    std::vector<shim_corner> buf;
+    for (int i = 0; i < nRows; i++) {
+        const float iniY = (float)(minBorderY + i * hCell);
+        float maxY = iniY + hCell + 6;
+        if (iniY >= maxBorderY - 3) continue;
+        if (maxY > maxBorderY) maxY = (float)maxBorderY;
+        for (int j = 0; j < nCols; j++) {
+            const float iniX = (float)(minBorderX + j * wCell);
+            float maxX = iniX + wCell + 6;
+            if (iniX >= maxBorderX - 6) continue;
+            if (maxX > maxBorderX) maxX = (float)maxBorderX;
+            const int y0 = (int)iniY, y1 = (int)maxY, x0 = (int)iniX, x1 = (int)maxX;
+            const int rw = x1 - x0, rh = y1 - y0;
+            buf.resize((size_t)rw * rh / 4 + 16);
+            const uint8_t* roi = L.at(x0, y0);
+            int n = shim_fast9_u8(roi, L.w, rw, rh, ini_th, buf.data(), (int)buf.size());
+            if (n == 0) n = shim_fast9_u8(roi, L.w, rw, rh, min_th, buf.data(), (int)buf.size());
+            for (int k = 0; k < n; k++) {
+                orc_kp kp;
+                kp.x = (float)buf[k].x + (float)(j * wCell);
+                kp.y = (float)buf[k].y + (float)(i * hCell);
+                kp.size = 7.f;
+                kp.angle = -1.f;
+                kp.response = (float)buf[k].score;
+                kp.octave = 0;
+                kp.class_id = -1;
+                out.push_back(kp);
+            }
+        }
+    }
+    return out;
+}
+
+struct Node {
+    int x0, x1, y0, y1;     // UL.x, UR.x, UL.y, BR.y
+    std::vector<int> keys;  // indices into the candidate list, in list order
+    bool no_more = false;
+    bool alive = true;
+    bool root = false;
+    long id = 0;
+};
+
+// ExtractorNode::DivideNode, src/ORBextractor.cc:602-674.
+void divide(const Node& p, const std::vector<orc_kp>& c, Node ch[4]) {
+    const int halfX = (int)std::ceil(static_cast<float>(p.x1 - p.x0) / 2);
+    const int halfY = (int)std::ceil(static_cast<float>(p.y1 - p.y0) / 2);
+    const int xm = p.x0 + halfX, ym = p.y0 + halfY;
+    ch[0].x0 = p.x0; ch[0].x1 = xm;   ch[0].y0 = p.y0; ch[0].y1 = ym;
+    ch[1].x0 = xm;   ch[1].x1 = p.x1; ch[1].y0 = p.y0; ch[1].y1 = ym;
+    ch[2].x0 = p.x0; ch[2].x1 = xm;   ch[2].y0 = ym;   ch[2].y1 = p.y1;
+    ch[3].x0 = xm;   ch[3].x1 = p.x1; ch[3].y0 = ym;   ch[3].y1 = p.y1;
+    for (int k : p.keys) {
+        const orc_kp& kp = c[k];
+        int q;
+        if (kp.x < (float)xm) q = kp.y < (float)ym ? 0 : 2;
+        else q = kp.y < (float)ym ? 1 : 3;
+        ch[q].keys.push_back(k);
+    }
+    for (int q = 0; q < 4; q++)
+        if (ch[q].keys.size() == 1) ch[q].no_more = true;
+}
+
+// DistributeOctTree, src/ORBextractor.cc:688-1033.
+std::vector<orc_kp> distribute(const std::vector<orc_kp>& cand, int minX, int maxX, int minY, int maxY, int N) {
+    const int nIni = (int)std::round(static_cast<float>(maxX - minX) / (maxY - minY));
+    const float hX = static_cast<float>(maxX - minX) / nIni;
+    std::vector<Node> nodes;
+    long next_id = 0;
+    for (int i = 0; i < nIni; i++) {
+        Node n;
+        n.x0 = (int)(hX * static_cast<float>(i));
+        n.x1 = (int)(hX * static_cast<float>(i + 1));
+        n.y0 = 0;
+        n.y1 = maxY - minY;
+        n.root = true;
+        n.id = next_id++;
+        nodes.push_back(n);
+    }
+    for (size_t i = 0; i < cand.size(); i++) nodes[(size_t)(cand[i].x / hX)].keys.push_back((int)i);
+    for (Node& n : nodes) {
+        if (n.keys.size() == 1) n.no_more = true;
+        else if (n.keys.empty()) n.alive = false;
+    }
+    int alive = 0;
+    for (const Node& n : nodes) alive += n.alive;
+
+    auto list_order = [&]() {
+        std::vector<int> ord;
+        for (int i = 0; i < (int)nodes.size(); i++)
+            if (nodes[i].alive) ord.push_back(i);
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+            const Node &A = nodes[a], &B = nodes[b];
+            if (A.root != B.root) return !A.root;
+            return A.root ? A.id < B.id : A.id > B.id;
+        });
+        return ord;
+    };
+    // Splits node idx, creating its non-empty children in n1..n4 order;
+    // returns the indices of the children holding more than one key.
+    auto split = [&](int idx, std::vector<int>& big) {
+        Node ch[4];
+        divide(nodes[idx], cand, ch);
+        nodes[idx].alive = false;
+        alive--;
+        for (int q = 0; q < 4; q++) {
+            if (ch[q].keys.empty()) continue;
+            ch[q].id = next_id++;
+            nodes.push_back(ch[q]);
+            alive++;
+            if (nodes.back().keys.size() > 1) big.push_back((int)nodes.size() - 1);
+        }
+    };
+
+    bool finish = false;
+    std::vector<int> expand;
+    while (!finish) {
+        int prev = alive;
+        std::vector<int> ord = list_order();
+        expand.clear();
+        for (int idx : ord) {
+            if (nodes[idx].no_more) continue;
+            split(idx, expand);
+        }
+        const int nToExpand = (int)expand.size();
+        if (alive >= N || alive == prev) {
+            finish = true;
+        } else if (alive + nToExpand * 3 > N) {
+            while (!finish) {
+                prev = alive;
+                std::vector<int> vprev = expand;
+                expand.clear();
+                std::sort(vprev.begin(), vprev.end(), [&](int a, int b) {
+                    if (nodes[a].keys.size() != nodes[b].keys.size()) return nodes[a].keys.size() < nodes[b].keys.size();
+                    return nodes[a].id < nodes[b].id;
+                });
+                for (int j = (int)vprev.size() - 1; j >= 0; j--) {
+                    split(vprev[j], expand);
+                    if (alive >= N) break;
+                }
+                if (alive >= N || alive == prev) finish = true;
+            }
+        }
+    }
+    std::vector<orc_kp> res;
+    for (int idx : list_order()) {
+        const Node& n = nodes[idx];
+        int best = n.keys[0];
+        float maxr = cand[best].response;
+        for (size_t k = 1; k < n.keys.size(); k++)
+            if (cand[n.keys[k]].response > maxr) {
+                best = n.keys[k];
+                maxr = cand[best].response;
+            }
+        res.push_back(cand[best]);
+    }
+    return res;
+}
+
+// IC_Angle, src/ORBextractor.cc:94-141.
+float ic_angle(const Level& L, float px, float py, const int* umax) {
+    int m_01 = 0, m_10 = 0;
+    const uint8_t* center = L.at(shim_cvround_f(px), shim_cvround_f(py));
+    for (int u = -kHalfPatch; u <= kHalfPatch; ++u) m_10 += u * center[u];
+    const int step = L.w;
+    for (int v = 1; v <= kHalfPatch; ++v) {
+        int v_sum = 0;
+        const int d = umax[v];
+        for (int u = -d; u <= d; ++u) {
+            const int vp = center[u + v * step], vm = center[u - v * step];
+            v_sum += vp - vm;
+            m_10 += u * (vp + vm);
+        }
+        m_01 += v * v_sum;
+    }
+    return shim_fast_atan2((float)m_01, (float)m_10);
+}
+
+// computeOrbDescriptor, src/ORBextractor.cc:153-204 (on the blurred level).
+void orb_descriptor(const orc_kp& kp, const uint8_t* blurred, int w, uint8_t* desc) {
+    const float factorPI = (float)(3.1415926535897932384626433832795 / 180.f);
+    const float angle = (float)kp.angle * factorPI;
+    const float a = (float)cosf(angle), b = (float)sinf(angle);
+    const uint8_t* center = blurred + (size_t)shim_cvround_f(kp.y) * w + shim_cvround_f(kp.x);
+    const int step = w;
+    for (int i = 0; i < 32; ++i) {
+        int val = 0;
+        for (int k = 0; k < 8; k++) {
+            const signed char* pp = &kOracleBriefPattern[(i * 16 + 2 * k) * 2];
+            int t[2];
+            for (int e = 0; e < 2; e++) {
+                const float x = (float)pp[2 * e], y = (float)pp[2 * e + 1];
+                t[e] = center[shim_cvround_f(x * b + y * a) * step + shim_cvround_f(x * a - y * b)];
+            }
+            val |= (t[0] < t[1]) << k;
+        }
+        desc[i] = (uint8_t)val;
+    }
+}
+
+struct Grid {
+    float minX, maxX, minY, maxY, invW, invH;
+    std::vector<int> cells[kGridCols][kGridRows];
+};
+
+// ComputeImageBounds (no distortion) + grid constants + AssignFeaturesToGrid,
+// src/Frame.cc:783-819, :372-388, :399-423, PosInGrid :682-698.
+void build_grid(Grid& g, const orc_kp* kps, int n, int w, int h) {
+    g.minX = 0.0f;
+    g.maxX = (float)w;
+    g.minY = 0.0f;
+    g.maxY = (float)h;
+    g.invW = static_cast<float>(kGridCols) / static_cast<float>(g.maxX - g.minX);
+    g.invH = static_cast<float>(kGridRows) / static_cast<float>(g.maxY - g.minY);
+    for (int i = 0; i < n; i++) {
+        const int px = (int)std::round((kps[i].x - g.minX) * g.invW);
+        const int py = (int)std::round((kps[i].y - g.minY) * g.invH);
+        if (px < 0 || px >= kGridCols || py < 0 || py >= kGridRows) continue;
+        g.cells[px][py].push_back(i);
+    }
+}
+
+// Frame::GetFeaturesInArea, src/Frame.cc:590-670.
+std::vector<int> features_in_area(const Grid& g, const orc_kp* kps, float x, float y, float r, int minLevel,
+                                  int maxLevel) {
+    std::vector<int> v;
+    const int nMinCellX = std::max(0, (int)std::floor((x - g.minX - r) * g.invW));
+    if (nMinCellX >= kGridCols) return v;
+    const int nMaxCellX = std::min(kGridCols - 1, (int)std::ceil((x - g.minX + r) * g.invW));
+    if (nMaxCellX < 0) return v;
+    const int nMinCellY = std::max(0, (int)std::floor((y - g.minY - r) * g.invH));
+    if (nMinCellY >= kGridRows) return v;
+    const int nMaxCellY = std::min(kGridRows - 1, (int)std::ceil((y - g.minY + r) * g.invH));
+    if (nMaxCellY < 0) return v;
+    const bool check = (minLevel > 0) || (maxLevel >= 0);
+    for (int ix = nMinCellX; ix <= nMaxCellX; ix++)
+        for (int iy = nMinCellY; iy <= nMaxCellY; iy++)
+            for (int idx : g.cells[ix][iy]) {
+                const orc_kp& kp = kps[idx];
+                if (check) {
+                    if (kp.octave < minLevel) continue;
+                    if (maxLevel >= 0 && kp.octave > maxLevel) continue;
+                }
+                const float dx = kp.x - x, dy = kp.y - y;
+                if (dx * dx + dy * dy < r * r) v.push_back(idx);
+            }
+    return v;
+}
+
+// ORBmatcher::DescriptorDistance, src/ORBmatcher.cc:2083-2103.
+int hamming(const uint8_t* a, const uint8_t* b) {
+    int d = 0;
+    for (int i = 0; i < 8; i++) {
+        uint32_t x, y;
+        std::memcpy(&x, a + 4 * i, 4);
+        std::memcpy(&y, b + 4 * i, 4);
+        d += __builtin_popcount(x ^ y);
+    }
+    return d;
+}
+
+// ORBmatcher::ComputeThreeMaxima, src/ORBmatcher.cc:2035-2077.
+void three_maxima(const std::vector<int>* histo, int L, int& ind1, int& ind2, int& ind3) {
+    int max1 = 0, max2 = 0, max3 = 0;
+    for (int i = 0; i < L; i++) {
+        const int s = (int)histo[i].size();
+        if (s > max1) {
+            max3 = max2; max2 = max1; max1 = s;
+            ind3 = ind2; ind2 = ind1; ind1 = i;
+        } else if (s > max2) {
+            max3 = max2; max2 = s;
+            ind3 = ind2; ind2 = i;
+        } else if (s > max3) {
+            max3 = s;
+            ind3 = i;
+        }
+    }
+    if (max2 < 0.1f * (float)max1) {
+        ind2 = -1;
+        ind3 = -1;
+    } else if (max3 < 0.1f * (float)max1) {
+        ind3 = -1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// ORBextractor::operator(), src/ORBextractor.cc:1533-1649.
+int orc_extract(const uint8_t* img, int w, int h, size_t step, const orc_params* p, orc_kp* kps, uint8_t* desc,
+                int cap, int* n_out, uint8_t* pyr_out, size_t pyr_cap) {
+    *n_out = 0;
+    if (img == nullptr || w <= 0 || h <= 0) return 0;
+    const Tables t = make_tables(p);
+    const std::vector<Level> pyr = build_pyramid(img, w, h, step, t);
+    std::vector<std::vector<orc_kp> > all(t.nlevels);
+    for (int l = 0; l < t.nlevels; l++) {
+        const Level& L = pyr[l];
+        std::vector<orc_kp> cand = fast_level(L, p->ini_th_fast, p->min_th_fast);
+        const int minBorderX = kEdgeThreshold - 3, minBorderY = minBorderX;
+        const int maxBorderX = L.w - kEdgeThreshold + 3, maxBorderY = L.h - kEdgeThreshold + 3;
+        std::vector<orc_kp> keys = distribute(cand, minBorderX, maxBorderX, minBorderY, maxBorderY, t.nfeat[l]);
+        const int scaledPatchSize = (int)(kPatchSize * t.scale[l]);
+        for (orc_kp& k : keys) {
+            k.x += minBorderX;
+            k.y += minBorderY;
+            k.octave = l;
+            k.size = (float)scaledPatchSize;
+        }
+        for (orc_kp& k : keys) k.angle = ic_angle(L, k.x, k.y, t.umax);
+        all[l] = keys;
+    }
+    int total = 0;
+    for (auto& v : all) total += (int)v.size();
+    *n_out = total;
+    if (total > cap) return -1;
+    int off = 0;
+    for (int l = 0; l < t.nlevels; l++) {
+        std::vector<orc_kp>& keys = all[l];
+        if (keys.empty()) continue;
+        const Level& L = pyr[l];
+        std::vector<uint8_t> blurred(L.px.size());
+        shim_gauss7_u8(L.px.data(), L.w, L.w, L.h, blurred.data(), L.w);
+        for (size_t i = 0; i < keys.size(); i++) orb_descriptor(keys[i], blurred.data(), L.w, desc + (size_t)(off + i) * 32);
+        if (l != 0) {
+            const float s = t.scale[l];
+            for (orc_kp& k : keys) {
+                k.x *= s;
+                k.y *= s;
+            }
+        }
+        for (size_t i = 0; i < keys.size(); i++) kps[off + i] = keys[i];
+        off += (int)keys.size();
+    }
+    if (pyr_out) {
+        size_t o = 0;
+        for (const Level& L : pyr) {
+            if (o + L.px.size() > pyr_cap) return -2;
+            std::memcpy(pyr_out + o, L.px.data(), L.px.size());
+            o += L.px.size();
+        }
+    }
+    return 0;
+}
+
+int orc_extractor_tables(const orc_params* p, float* scale, float* inv_scale, float* sigma2, float* inv_sigma2,
+                         int* features_per_level, int* umax16) {
+    const Tables t = make_tables(p);
+    for (int l = 0; l < p->nlevels; l++) {
+        scale[l] = t.scale[l];
+        inv_scale[l] = t.inv_scale[l];
+        sigma2[l] = t.sigma2[l];
+        inv_sigma2[l] = t.inv_sigma2[l];
+        features_per_level[l] = t.nfeat[l];
+    }
+    for (int v = 0; v < 16; v++) umax16[v] = t.umax[v];
+    return 0;
+}
+
+int orc_descriptor_distance(const uint8_t* a, const uint8_t* b) { return hamming(a, b); }
+
+int orc_features_in_area(const orc_params* p, const orc_kp* kps, int n, int w, int h, float x, float y, float r,
+                         int minLevel, int maxLevel, int* out, int cap) {
+    (void)p;
+    Grid* g = new Grid();
+    build_grid(*g, kps, n, w, h);
+    std::vector<int> v = features_in_area(*g, kps, x, y, r, minLevel, maxLevel);
+    delete g;
+    for (int i = 0; i < (int)v.size() && i < cap; i++) out[i] = v[i];
+    return (int)v.size();
+}
+
+// ORBmatcher::SearchForInitialization, src/ORBmatcher.cc:573-717.
+int orc_search_for_initialization(const orc_params* p, const orc_kp* kps1, const uint8_t* desc1, int n1,
+                                  const orc_kp* kps2, const uint8_t* desc2, int n2, int w, int h,
+                                  float* prev_matched_xy, int window, float nnratio, int check_ori, int* matches12) {
+    (void)p;
+    Grid* g2 = new Grid();
+    build_grid(*g2, kps2, n2, w, h);
+    int nmatches = 0;
+    for (int i = 0; i < n1; i++) matches12[i] = -1;
+    std::vector<int> rotHist[kHistoLength];
+    const float factor = kHistoLength / 360.0f;
+    std::vector<int> matchedDistance(n2, INT_MAX), matches21(n2, -1);
+    for (int i1 = 0; i1 < n1; i1++) {
+        const orc_kp kp1 = kps1[i1];
+        const int level1 = kp1.octave;
+        if (level1 > 0) continue;
+        std::vector<int> idx2 = features_in_area(*g2, kps2, prev_matched_xy[2 * i1], prev_matched_xy[2 * i1 + 1],
+                                                 (float)window, level1, level1);
+        if (idx2.empty()) continue;
+        int bestDist = INT_MAX, bestDist2 = INT_MAX, bestIdx2 = -1;
+        for (int i2 : idx2) {
+            const int dist = hamming(desc1 + (size_t)i1 * 32, desc2 + (size_t)i2 * 32);
+            if (matchedDistance[i2] <= dist) continue;
+            if (dist < bestDist) {
+                bestDist2 = bestDist;
+                bestDist = dist;
+                bestIdx2 = i2;
+            } else if (dist < bestDist2) {
+                bestDist2 = dist;
+            }
+        }
+        if (bestDist <= kThLow && bestDist < (float)bestDist2 * nnratio) {
+            if (matches21[bestIdx2] >= 0) {
+                matches12[matches21[bestIdx2]] = -1;
+                nmatches--;
+            }
+            matches12[i1] = bestIdx2;
+            matches21[bestIdx2] = i1;
+            matchedDistance[bestIdx2] = bestDist;
+            nmatches++;
+            if (check_ori) {
+                float rot = kps1[i1].angle - kps2[bestIdx2].angle;
+                if (rot < 0.0) rot += 360.0f;
+                int bin = (int)std::round(rot * factor);
+                if (bin == kHistoLength) bin = 0;
+                rotHist[bin].push_back(i1);
+            }
+        }
+    }
+    if (check_ori) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        three_maxima(rotHist, kHistoLength, ind1, ind2, ind3);
+        for (int i = 0; i < kHistoLength; i++) {
+            if (i == ind1 || i == ind2 || i == ind3) continue;
+            for (int idx1 : rotHist[i])
+                if (matches12[idx1] >= 0) {
+                    matches12[idx1] = -1;
+                    nmatches--;
+                }
+        }
+    }
+    for (int i1 = 0; i1 < n1; i1++)
+        if (matches12[i1] >= 0) {
+            prev_matched_xy[2 * i1] = kps2[matches12[i1]].x;
+            prev_matched_xy[2 * i1 + 1] = kps2[matches12[i1]].y;
+        }
+    delete g2;
+    return nmatches;
+}
+
+// ORBmatcher::SearchByProjection(Frame&, const vector<MapPoint*>&, th),
+// src/ORBmatcher.cc:72-183, with RadiusByViewingCos :186-193.
+int orc_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright, int n,
+                             int w, int h, const orc_mappoint* mps, const uint8_t* mp_desc, int m, float th,
+                             float nnratio, const uint8_t* claimed, int* match_out) {
+    const Tables t = make_tables(p);
+    Grid* g = new Grid();
+    build_grid(*g, kps, n, w, h);
+    for (int i = 0; i < n; i++) match_out[i] = (claimed && claimed[i]) ? -2 : -1;
+    int nmatches = 0;
+    const bool bFactor = th != 1.0;
+    for (int imp = 0; imp < m; imp++) {
+        const orc_mappoint& mp = mps[imp];
+        if (!mp.track_in_view || mp.bad) continue;
+        const int level = mp.track_scale_level;
+        float r = mp.view_cos > 0.998 ? 2.5f : 4.0f;
+        if (bFactor) r *= th;
+        const float radius = r * t.scale[level];
+        std::vector<int> idx = features_in_area(*g, kps, mp.proj_x, mp.proj_y, radius, level - 1, level);
+        if (idx.empty()) continue;
+        int bestDist = 256, bestLevel = -1, bestDist2 = 256, bestLevel2 = -1, bestIdx = -1;
+        for (int i : idx) {
+            if (match_out[i] != -1) continue;
+            if (uright && uright[i] > 0) {
+                const float er = std::fabs(mp.proj_xr - uright[i]);
+                if (er > r * t.scale[level]) continue;
+            }
+            const int dist = hamming(mp_desc + (size_t)imp * 32, desc + (size_t)i * 32);
+            if (dist < bestDist) {
+                bestDist2 = bestDist;
+                bestDist = dist;
+                bestLevel2 = bestLevel;
+                bestLevel = kps[i].octave;
+                bestIdx = i;
+            } else if (dist < bestDist2) {
+                bestLevel2 = kps[i].octave;
+                bestDist2 = dist;
+            }
+        }
+        if (bestDist <= kThHigh) {
+            if (bestLevel == bestLevel2 && bestDist > nnratio * bestDist2) continue;
+            match_out[bestIdx] = imp;
+            nmatches++;
+        }
+    }
+    delete g;
+    return nmatches;
+}
+
+// Frame::ComputeStereoMatches, src/Frame.cc:831-1082 (mb = mbf/fx).
+int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
+                               const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,
+                               const uint8_t* pyrR, const int* level_w, const int* level_h, int w, int h, float bf,
+                               float fx, float* uright, float* depth) {
+    (void)w;
+    const Tables t = make_tables(p);
+    std::vector<size_t> off(p->nlevels, 0);
+    for (int l = 1; l < p->nlevels; l++) off[l] = off[l - 1] + (size_t)level_w[l - 1] * level_h[l - 1];
+    for (int i = 0; i < nL; i++) uright[i] = depth[i] = -1.0f;
+    const int thOrbDist = (kThHigh + kThLow) / 2;
+    const int nRows = level_h[0];
+    (void)h;
+    std::vector<std::vector<int> > rows(nRows);
+    for (int iR = 0; iR < nR; iR++) {
+        const float kpY = kpsR[iR].y;
+        const float r = 2.0f * t.scale[kpsR[iR].octave];
+        const int maxr = (int)std::ceil(kpY + r), minr = (int)std::floor(kpY - r);
+        for (int yi = minr; yi <= maxr; yi++) rows[yi].push_back(iR);
+    }
+    const float mb = bf / fx;
+    const float minZ = mb, minD = 0, maxD = bf / minZ;
+    std::vector<std::pair<int, int> > distIdx;
+    for (int iL = 0; iL < nL; iL++) {
+        const orc_kp& kpL = kpsL[iL];
+        const int levelL = kpL.octave;
+        const float vL = kpL.y, uL = kpL.x;
+        const std::vector<int>& cands = rows[(size_t)vL];
+        if (cands.empty()) continue;
+        const float minU = uL - maxD, maxU = uL - minD;
+        if (maxU < 0) continue;
+        int bestDist = kThHigh;
+        int bestIdxR = 0;
+        for (int iR : cands) {
+            const orc_kp& kpR = kpsR[iR];
+            if (kpR.octave < levelL - 1 || kpR.octave > levelL + 1) continue;
+            const float uR = kpR.x;
+            if (uR >= minU && uR <= maxU) {
+                const int dist = hamming(descL + (size_t)iL * 32, descR + (size_t)iR * 32);
+                if (dist < bestDist) {
+                    bestDist = dist;
+                    bestIdxR = iR;
+                }
+            }
+        }
+        if (bestDist >= thOrbDist) continue;
+        const float uR0 = kpsR[bestIdxR].x;
+        const float sf = t.inv_scale[levelL];
+        const float scaleduL = std::round(kpL.x * sf), scaledvL = std::round(kpL.y * sf);
+        const float scaleduR0 = std::round(uR0 * sf);
+        const int W = 5, L = 5;
+        const int lw = level_w[levelL];
+        const uint8_t* left = pyrL + off[levelL];
+        const uint8_t* right = pyrR + off[levelL];
+        const int ly0 = (int)(scaledvL - W), lx0 = (int)(scaleduL - W);
+        const float cl = (float)left[(size_t)(ly0 + W) * lw + lx0 + W];
+        const float iniu = scaleduR0 - L - W, endu = scaleduR0 + L + W + 1;
+        if (iniu < 0 || endu >= lw) continue;
+        int bestSad = INT_MAX, bestincR = 0;
+        float dists[2 * L + 1];
+        for (int incR = -L; incR <= L; incR++) {
+            const int rx0 = (int)(scaleduR0 + incR - W);
+            const float cr = (float)right[(size_t)(ly0 + W) * lw + rx0 + W];
+            double s = 0;
+            for (int yy = 0; yy < 2 * W + 1; yy++)
+                for (int xx = 0; xx < 2 * W + 1; xx++) {
+                    const float a = (float)left[(size_t)(ly0 + yy) * lw + lx0 + xx] - cl;
+                    const float b = (float)right[(size_t)(ly0 + yy) * lw + rx0 + xx] - cr;
+                    s += std::fabs((double)(a - b));
+                }
+            const float dist = (float)s;
+            if (dist < bestSad) {
+                bestSad = (int)dist;
+                bestincR = incR;
+            }
+            dists[L + incR] = dist;
+        }
+        if (bestincR == -L || bestincR == L) continue;
+        const float d1 = dists[L + bestincR - 1], d2 = dists[L + bestincR], d3 = dists[L + bestincR + 1];
+        const float deltaR = (d1 - d3) / (2.0f * (d1 + d3 - 2.0f * d2));
+        if (deltaR < -1 || deltaR > 1) continue;
+        float bestuR = t.scale[levelL] * ((float)scaleduR0 + (float)bestincR + deltaR);
+        float disparity = uL - bestuR;
+        if (disparity >= minD && disparity < maxD) {
+            if (disparity <= 0) {
+                disparity = 0.01;
+                bestuR = uL - 0.01;
+            }
+            depth[iL] = bf / disparity;
+            uright[iL] = bestuR;
+            distIdx.push_back(std::make_pair(bestSad, iL));
+        }
+    }
+    if (distIdx.empty()) return 0;
+    std::sort(distIdx.begin(), distIdx.end());
+    const float median = distIdx[distIdx.size() / 2].first;
+    const float thDist = 1.5f * 1.4f * median;
+    for (int i = (int)distIdx.size() - 1; i >= 0; i--) {
+        if (distIdx[i].first < thDist) break;
+        uright[distIdx[i].second] = -1;
+        depth[distIdx[i].second] = -1;
+    }
+    return (int)distIdx.size();
+}
+
+int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int* d1, int* idx2, int* d2) {
+    for (int i = 0; i < nq; i++) {
+        int b1 = INT_MAX, b2 = INT_MAX, i1 = -1, i2 = -1;
+        for (int j = 0; j < nt; j++) {
+            const int d = hamming(q + (size_t)i * 32, t + (size_t)j * 32);
+            if (d < b1) {
+                b2 = b1; i2 = i1; b1 = d; i1 = j;
+            } else if (d < b2) {
+                b2 = d; i2 = j;
+            }
+        }
+        idx1[i] = i1; d1[i] = b1; idx2[i] = i2; d2[i] = b2;
+    }
+    return 0;
+}
+
+void orc_blur_level(const uint8_t* src, int w, int h, uint8_t* dst) { shim_gauss7_u8(src, w, w, h, dst, w); }
+
+int orc_fast_level(const uint8_t* level, int w, int h, int ini_th, int min_th, orc_kp* out, int cap) {
+    Level L;
+    L.w = w;
+    L.h = h;
+    L.px.assign(level, level + (size_t)w * h);
+    std::vector<orc_kp> v = fast_level(L, ini_th, min_th);
+    for (int i = 0; i < (int)v.size() && i < cap; i++) out[i] = v[i];
+    return (int)v.size();
+}
+
+int orc_distribute(const orc_kp* cand, int n, int minX, int maxX, int minY, int maxY, int N, orc_kp* out, int cap) {
+    std::vector<orc_kp> c(cand, cand + n);
+    std::vector<orc_kp> r = distribute(c, minX, maxX, minY, maxY, N);
+    for (int i = 0; i < (int)r.size() && i < cap; i++) out[i] = r[i];
+    return (int)r.size();
+}
+
+void orc_sincos_table(const float* x, int n, float* c, float* s) {
+    for (int i = 0; i < n; i++) {
+        c[i] = cosf(x[i]);
+        s[i] = sinf(x[i]);
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+/*
+ * orb_oracle.h -- ORACLE / TEST INFRASTRUCTURE ONLY.
+ *
+ * This repository's CPU restatement of ORB-SLAM2's feature front-end, written
+ * from the reference's behaviour (each function cites the reference lines it
+ * follows).  It is the checker the GPU path is compared with: only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.  It is
+ * pinned against the reference's own sources (refbuild/, built where they are
+ * present) and through them against the committed golden fixtures.
+ *
+ * Every entry point mirrors the harness entry point of the same name with a
+ * ref_ prefix (refbuild/ref_harness.cpp).
+ */
+#ifndef ORB_ORACLE_H
+#define ORB_ORACLE_H
+#include "orb_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int orc_extract(const uint8_t* img, int w, int h, size_t step, const orc_params* p, orc_kp* kps, uint8_t* desc,
+                int cap, int* n_out, uint8_t* pyr, size_t pyr_cap);
+int orc_extractor_tables(const orc_params* p, float* scale, float* inv_scale, float* sigma2, float* inv_sigma2,
+                         int* features_per_level, int* umax16);
+int orc_descriptor_distance(const uint8_t* a, const uint8_t* b);
+int orc_features_in_area(const orc_params* p, const orc_kp* kps, int n, int w, int h, float x, float y, float r,
+                         int minLevel, int maxLevel, int* out, int cap);
+int orc_search_for_initialization(const orc_params* p, const orc_kp* kps1, const uint8_t* desc1, int n1,
+                                  const orc_kp* kps2, const uint8_t* desc2, int n2, int w, int h,
+                                  float* prev_matched_xy, int window, float nnratio, int check_ori, int* matches12);
+int orc_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright, int n,
+                             int w, int h, const orc_mappoint* mps, const uint8_t* mp_desc, int m, float th,
+                             float nnratio, const uint8_t* claimed, int* match_out);
+int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
+                               const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,
+                               const uint8_t* pyrR, const int* level_w, const int* level_h, int w, int h, float bf,
+                               float fx, float* uright, float* depth);
+int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int* d1, int* idx2, int* d2);
+
+/* Stage-level checkers for the kernel tests. */
+/* 7x7 sigma-2 blur of one level (GaussianBlur, src/ORBextractor.cc:1607-1615). */
+void orc_blur_level(const uint8_t* src, int w, int h, uint8_t* dst);
+/* FAST candidates of one level in the order the cell loop of
+ * src/ORBextractor.cc:1069-1142 emits them (coordinates relative to the
+ * 16-pixel border, as handed to DistributeOctTree); returns the count. */
+int orc_fast_level(const uint8_t* level, int w, int h, int ini_th, int min_th, orc_kp* out, int cap);
+/* DistributeOctTree (src/ORBextractor.cc:688-1033) on given candidates. */
+int orc_distribute(const orc_kp* cand, int n, int minX, int maxX, int minY, int maxY, int N, orc_kp* out, int cap);
+/* glibc cosf/sinf of the descriptor angle, for the GPU's rotation check. */
+void orc_sincos_table(const float* x, int n, float* c, float* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,112 @@
+"""Generate the golden fixtures of the ORB front-end path.
+
+The outputs come from the reference's own src/ORBextractor.cc,
+src/ORBmatcher.cc and src/Frame.cc, compiled unmodified against the cv
+stand-in (oracle/Makefile target ``ref``; needs the reference sources, so this
+script runs only where they are present).  Inputs are stored with the outputs,
+so the fixtures do not depend on the generator's random streams.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import pyoracle  # noqa: E402
+from oracle.pyoracle import MP_DTYPE, RefOracle  # noqa: E402
+from orb_slam2_detailed_comments_gb300 import synthetic as syn  # noqa: E402
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print(f"{name}: {os.path.getsize(path) // 1024} KiB")
+
+
+def main():
+    pyoracle.build(ref=True)
+    R = RefOracle()
+
+    # 1. extraction, 640x480, nFeatures 1000 (and the pyramid, as level digests)
+    f1, f2, H = syn.frame_pair(640, 480, seed=0)
+    a = R.extract(f1, nfeatures=1000)
+    b = R.extract(f2, nfeatures=1000)
+    save("extract_640x480.npz", image=f1, keypoints=a.keypoints, descriptors=a.descriptors,
+         level_shapes=np.array([l.shape for l in a.pyramid]),
+         level_sums=np.array([int(l.astype(np.int64).sum()) for l in a.pyramid]),
+         level7=a.pyramid[7])
+
+    # 2. SearchForInitialization between the warped pair (window 100, ratio 0.9, rotation check)
+    nm, m12, prev = R.search_for_initialization(a.keypoints, a.descriptors, b.keypoints, b.descriptors, 640, 480,
+                                                window=100, nnratio=0.9, check_ori=True)
+    save("init_640x480.npz", image2=f2, keypoints1=a.keypoints, descriptors1=a.descriptors,
+         keypoints2=b.keypoints, descriptors2=b.descriptors, nmatches=np.array(nm), matches12=m12,
+         prev_matched=prev)
+
+    # 3. ComputeStereoMatches on a rectified 640x240 pair, bf 386.1, fx 718.856
+    left, right, _ = syn.stereo_pair(640, 240, seed=3)
+    L = R.extract(left, nfeatures=1000)
+    Rr = R.extract(right, nfeatures=1000)
+    ur, depth = R.compute_stereo_matches(L.keypoints, L.descriptors, Rr.keypoints, Rr.descriptors, L.pyramid,
+                                         Rr.pyramid, 640, 240, 386.1, 718.856)
+    save("stereo_640x240.npz", left=left, right=right, keypoints_left=L.keypoints, descriptors_left=L.descriptors,
+         keypoints_right=Rr.keypoints, descriptors_right=Rr.descriptors, uright=ur, depth=depth,
+         bf=np.float32(386.1), fx=np.float32(718.856))
+
+    # 4. SearchByProjection(Frame, map points, th) with 1000 map points
+    rng = np.random.default_rng(11)
+    n = len(a.keypoints)
+    M = 1000
+    src = rng.integers(0, n, M)
+    mpd = a.descriptors[src] ^ np.packbits(rng.random((M, 256)) < 0.1, axis=1, bitorder="little")
+    mps = np.zeros(M, MP_DTYPE)
+    mps["proj_x"] = a.keypoints["x"][src] + rng.normal(0, 2, M)
+    mps["proj_y"] = a.keypoints["y"][src] + rng.normal(0, 2, M)
+    mps["proj_xr"] = np.where(rng.random(M) < 0.3, mps["proj_x"] - rng.uniform(5, 50, M), -1)
+    mps["view_cos"] = rng.uniform(0.99, 1.0, M)
+    mps["track_scale_level"] = a.keypoints["octave"][src]
+    mps["track_in_view"] = rng.random(M) < 0.95
+    mps["bad"] = rng.random(M) < 0.02
+    claimed = (rng.random(n) < 0.05).astype(np.uint8)
+    uright = np.where(rng.random(n) < 0.3, a.keypoints["x"] - rng.uniform(5, 50, n), -1).astype(np.float32)
+    out = {}
+    for th in (1.0, 3.75):
+        nmp, match = R.search_by_projection(a.keypoints, a.descriptors, 640, 480, mps, mpd, th=th, nnratio=0.8,
+                                            uright=uright, claimed=claimed)
+        out[f"nmatches_th{th}"] = np.array(nmp)
+        out[f"match_th{th}"] = match
+    save("projection_640x480.npz", mappoints=mps, mp_descriptors=mpd, claimed=claimed, uright=uright, **out)
+
+    # 5. brute-force k=2 over DescriptorDistance
+    q = syn.clustered_descriptors(200, 20, 0.1, seed=5)
+    t = syn.clustered_descriptors(3000, 20, 0.1, seed=6)
+    i1, d1, i2, d2 = R.knn2(q, t)
+    save("knn_200x3000.npz", query=q, train=t, idx1=i1, d1=d1, idx2=i2, d2=d2)
+
+    # 6. DescriptorDistance known answers on crafted bit patterns
+    pats = [np.zeros(32, np.uint8), np.full(32, 255, np.uint8), np.tile(np.array([0x55], np.uint8), 32),
+            np.tile(np.array([0xAA], np.uint8), 32), np.arange(32, dtype=np.uint8),
+            np.array([1 << (i % 8) for i in range(32)], np.uint8)]
+    pa = np.stack(pats)
+    dist = np.array([[R.descriptor_distance(x, y) for y in pats] for x in pats], np.int32)
+    save("hamming_kat.npz", patterns=pa, distance=dist)
+
+    # 7. tables of the ORBextractor constructor
+    import ctypes as C
+    for nf in (1000, 2000):
+        p = pyoracle.Params(nf, 1.2, 8, 20, 7)
+        arrs = [np.zeros(8, np.float32) for _ in range(4)] + [np.zeros(8, np.int32), np.zeros(16, np.int32)]
+        R.fn("extractor_tables")(C.byref(p), *[x.ctypes.data_as(C.c_void_p) for x in arrs])
+        save(f"tables_{nf}.npz", scale=arrs[0], inv_scale=arrs[1], sigma2=arrs[2], inv_sigma2=arrs[3],
+             features_per_level=arrs[4], umax=arrs[5])
+
+
+if __name__ == "__main__":
+    main()

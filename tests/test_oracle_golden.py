@@ -1,0 +1,98 @@
+"""The CPU restatement (oracle/orb_oracle.cpp) against the golden fixtures,
+which were produced by the reference's own sources (tests/golden/make_golden.py)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+
+def test_extractor_tables(oracle, golden):
+    for nf in (1000, 2000):
+        g = golden(f"tables_{nf}.npz")
+        p = pyoracle.Params(nf, 1.2, 8, 20, 7)
+        arrs = [np.zeros(8, np.float32) for _ in range(4)] + [np.zeros(8, np.int32), np.zeros(16, np.int32)]
+        oracle.fn("extractor_tables")(C.byref(p), *[x.ctypes.data_as(C.c_void_p) for x in arrs])
+        for name, a in zip(["scale", "inv_scale", "sigma2", "inv_sigma2", "features_per_level", "umax"], arrs):
+            assert np.array_equal(a, g[name]), name
+    s, inv = pyoracle.scale_tables(8, 1.2)
+    assert np.array_equal(np.array(s, np.float32), golden("tables_1000.npz")["scale"])
+
+
+def test_extract_640x480(oracle, golden):
+    g = golden("extract_640x480.npz")
+    r = oracle.extract(g["image"], nfeatures=1000)
+    assert len(r.keypoints) == len(g["keypoints"])
+    assert r.keypoints.tobytes() == g["keypoints"].tobytes()
+    assert np.array_equal(r.descriptors, g["descriptors"])
+    assert [l.shape for l in r.pyramid] == [tuple(s) for s in g["level_shapes"]]
+    assert [int(l.astype(np.int64).sum()) for l in r.pyramid] == list(g["level_sums"])
+    assert np.array_equal(r.pyramid[7], g["level7"])
+
+
+def test_search_for_initialization(oracle, golden):
+    g = golden("init_640x480.npz")
+    nm, m12, prev = oracle.search_for_initialization(g["keypoints1"], g["descriptors1"], g["keypoints2"],
+                                                     g["descriptors2"], 640, 480, window=100, nnratio=0.9,
+                                                     check_ori=True)
+    assert nm == int(g["nmatches"])
+    assert np.array_equal(m12, g["matches12"])
+    assert np.array_equal(prev, g["prev_matched"])
+
+
+def test_stereo(oracle, golden):
+    g = golden("stereo_640x240.npz")
+    L = oracle.extract(g["left"], nfeatures=1000)
+    R = oracle.extract(g["right"], nfeatures=1000)
+    assert L.keypoints.tobytes() == g["keypoints_left"].tobytes()
+    assert R.keypoints.tobytes() == g["keypoints_right"].tobytes()
+    ur, depth = oracle.compute_stereo_matches(L.keypoints, L.descriptors, R.keypoints, R.descriptors, L.pyramid,
+                                              R.pyramid, 640, 240, float(g["bf"]), float(g["fx"]))
+    assert np.array_equal(ur, g["uright"])
+    assert np.array_equal(depth, g["depth"])
+    assert (ur > 0).sum() > 50
+
+
+def test_search_by_projection(oracle, golden):
+    e = golden("extract_640x480.npz")
+    g = golden("projection_640x480.npz")
+    for th in (1.0, 3.75):
+        nm, match = oracle.search_by_projection(e["keypoints"], e["descriptors"], 640, 480, g["mappoints"],
+                                                g["mp_descriptors"], th=th, nnratio=0.8, uright=g["uright"],
+                                                claimed=g["claimed"])
+        assert nm == int(g[f"nmatches_th{th}"])
+        assert np.array_equal(match, g[f"match_th{th}"])
+
+
+def test_knn(oracle, golden):
+    g = golden("knn_200x3000.npz")
+    i1, d1, i2, d2 = oracle.knn2(g["query"], g["train"])
+    for a, name in zip((i1, d1, i2, d2), ("idx1", "d1", "idx2", "d2")):
+        assert np.array_equal(a, g[name]), name
+
+
+def test_hamming_kat(oracle, golden):
+    g = golden("hamming_kat.npz")
+    pats = g["patterns"]
+    for i in range(len(pats)):
+        for j in range(len(pats)):
+            assert oracle.descriptor_distance(pats[i], pats[j]) == g["distance"][i, j]
+    assert g["distance"][0, 1] == 256 and g["distance"][2, 3] == 256 and g["distance"][0, 0] == 0
+
+
+def test_constant_image_has_no_keypoints(oracle):
+    r = oracle.extract(np.full((480, 640), 77, np.uint8))
+    assert len(r.keypoints) == 0 and r.descriptors.shape == (0, 32)
+
+
+@pytest.mark.skipif(not pyoracle.ref_available(), reason="reference sources not built here")
+def test_oracle_matches_reference_on_fresh_seeds(oracle):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    R = pyoracle.RefOracle()
+    for seed, (w, h, nf) in enumerate([(752, 480, 1500), (1241, 376, 2000)]):
+        img = syn.scene(w, h, 100 + seed)
+        a = R.extract(img, nfeatures=nf)
+        b = oracle.extract(img, nfeatures=nf)
+        assert a.keypoints.tobytes() == b.keypoints.tobytes()
+        assert np.array_equal(a.descriptors, b.descriptors)
