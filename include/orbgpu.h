@@ -1,0 +1,180 @@
+/*
+ * orbgpu.h -- C ABI of the GB300 ORB front-end (liborbgpu.so).
+ *
+ * Drop-in boundary for ORB-SLAM2's feature hot path: each entry point names
+ * the reference interface it replaces (file:line in the reference tree).
+ * Plain pointers and sizes only.  Every call is asynchronous on the handle's
+ * CUDA stream unless it says otherwise; calls that return host results
+ * synchronise that stream before returning.
+ *
+ * Memory flags: ORBGPU_MEM_HOST means the pointer is host memory (pageable or
+ * pinned) and the library copies through its own device buffers;
+ * ORBGPU_MEM_DEVICE means the pointer is device memory of the current device.
+ *
+ * Error convention: every function returns an orbgpu_status; 0 is success.
+ * orbgpu_last_error() returns a thread-local description of the last failure.
+ * There is no CPU fallback: without a usable CUDA device every call fails
+ * with ORBGPU_ERR_CUDA.
+ */
+#ifndef ORBGPU_H
+#define ORBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    ORBGPU_OK = 0,
+    ORBGPU_ERR_BAD_ARG = 1,  /* invalid argument (the reference asserts or has undefined behaviour) */
+    ORBGPU_ERR_OOM = 2,      /* device allocation failed */
+    ORBGPU_ERR_CUDA = 3,     /* CUDA runtime error (no device, launch failure, ...) */
+    ORBGPU_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+    ORBGPU_ERR_CAPACITY = 5  /* caller's output capacity too small; *n_* holds the needed size */
+} orbgpu_status;
+
+enum { ORBGPU_MEM_HOST = 0, ORBGPU_MEM_DEVICE = 1 };
+
+/* Field for field the layout of cv::KeyPoint: pt.x, pt.y, size, angle,
+ * response, octave, class_id (28 bytes). */
+typedef struct {
+    float x, y, size, angle, response;
+    int32_t octave, class_id;
+} orbgpu_keypoint;
+
+const char* orbgpu_last_error(void);
+int orbgpu_version(void);
+
+/* ------------------------------------------------------------ extractor */
+typedef struct orbgpu_extractor orbgpu_extractor;
+
+/* ORBextractor::ORBextractor(int nfeatures, float scaleFactor, int nlevels,
+ *                            int iniThFAST, int minThFAST)
+ * -- include/ORBextractor.h:93, src/ORBextractor.cc:469-571.
+ * max_width/max_height bound the images this handle accepts (device buffers
+ * are sized for them once).  stream: a cudaStream_t, or NULL for a stream the
+ * handle creates and owns. */
+int orbgpu_extractor_create(int nfeatures, float scale_factor, int nlevels, int ini_th_fast, int min_th_fast,
+                            int max_width, int max_height, void* stream, orbgpu_extractor** out);
+int orbgpu_extractor_destroy(orbgpu_extractor* ex);
+
+/* ORBextractor::operator()(InputArray image, InputArray mask,
+ *                          vector<KeyPoint>& keypoints, OutputArray descriptors)
+ * -- include/ORBextractor.h:111, src/ORBextractor.cc:1533-1649.
+ * image: width x height uint8, row pitch 'step' bytes, host or device per
+ * image_mem.  keypoints (capacity entries) and descriptors (capacity x 32
+ * bytes, row-major) are host or device per out_mem.  The mask is ignored by
+ * the reference and has no parameter here.  An empty image (width or height
+ * 0) returns OK with *n_keypoints = 0.  Output order is the reference's:
+ * level-major, each level in DistributeOctTree's list order; coordinates
+ * scaled to level 0.  Synchronises the handle's stream. */
+int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int width, int height, size_t step, int image_mem,
+                   orbgpu_keypoint* keypoints, uint8_t* descriptors, int capacity, int out_mem, int* n_keypoints);
+
+/* GetLevels / GetScaleFactors / GetInverseScaleFactors / GetScaleSigmaSquares
+ * / GetInverseScaleSigmaSquares -- include/ORBextractor.h:119-159.
+ * Arrays receive nlevels floats each (any may be NULL). */
+int orbgpu_extractor_tables(const orbgpu_extractor* ex, int* nlevels, float* scale_factors, float* inv_scale_factors,
+                            float* sigma2, float* inv_sigma2, int* features_per_level);
+
+/* mvImagePyramid[level] of the last extraction -- include/ORBextractor.h:162.
+ * Returns the device pointer of the unblurred level, its size and row pitch. */
+int orbgpu_extractor_pyramid_level(const orbgpu_extractor* ex, int level, const uint8_t** dev_ptr, int* width,
+                                   int* height, size_t* pitch);
+
+/* The CUDA stream of the handle (a cudaStream_t). */
+void* orbgpu_extractor_stream(const orbgpu_extractor* ex);
+
+/* ------------------------------------------------------------ batched extraction */
+/* Many frames of uneven size through one pipeline: a ragged list of
+ * (frame, level) and (frame, level, cell) work items processed by one launch
+ * per stage, replayed as a CUDA graph when the frame list repeats.
+ * images: device pointers (one per frame), widths/heights/steps per frame.
+ * Output for frame f starts at keypoints + f * per_frame_capacity (and the
+ * same row of descriptors); n_keypoints[f] receives its count (device or
+ * host per out_mem). */
+typedef struct orbgpu_batch orbgpu_batch;
+int orbgpu_batch_create(int max_frames, int max_width, int max_height, int max_nfeatures, void* stream,
+                        orbgpu_batch** out);
+int orbgpu_batch_destroy(orbgpu_batch* b);
+int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t* const* images, const int* widths,
+                         const int* heights, const size_t* steps, const int* nfeatures, float scale_factor,
+                         int nlevels, int ini_th_fast, int min_th_fast, orbgpu_keypoint* keypoints,
+                         uint8_t* descriptors, int per_frame_capacity, int out_mem, int* n_keypoints);
+
+/* ------------------------------------------------------------ matcher */
+typedef struct orbgpu_matcher orbgpu_matcher;
+
+/* A frame as the matchers read it (the fields of ORB_SLAM2::Frame that the
+ * searches use): undistorted keypoints, descriptors (n x 32), optional
+ * mvuRight (n floats, NULL = none), image bounds for the 64 x 48 grid
+ * (src/Frame.cc:783-819 without distortion: [0, width] x [0, height]) and the
+ * scale factors of its extractor.  All pointers share one memory flag. */
+typedef struct {
+    const orbgpu_keypoint* keypoints;
+    const uint8_t* descriptors;
+    const float* uright;
+    int n;
+    int width, height;
+    int nlevels;
+    float scale_factors[16];
+    int mem;
+} orbgpu_frame;
+
+/* ORBmatcher::ORBmatcher(float nnratio, bool checkOri) -- include/ORBmatcher.h. */
+int orbgpu_matcher_create(float nnratio, int check_orientation, void* stream, orbgpu_matcher** out);
+int orbgpu_matcher_destroy(orbgpu_matcher* m);
+
+/* ORBmatcher::SearchForInitialization(Frame& F1, Frame& F2,
+ *     vector<Point2f>& vbPrevMatched, vector<int>& vnMatches12, int windowSize)
+ * -- src/ORBmatcher.cc:573-717.  prev_matched: n1 x 2 floats (in/out),
+ * matches12: n1 ints (out), both host memory.  Returns OK and *nmatches. */
+int orbgpu_search_for_initialization(orbgpu_matcher* m, const orbgpu_frame* f1, const orbgpu_frame* f2,
+                                     float* prev_matched, int* matches12, int window_size, int* nmatches);
+
+/* One map point of ORBmatcher::SearchByProjection(Frame&, vector<MapPoint*>, th)
+ * as Frame::isInFrustum leaves it (src/Frame.cc:491-578). */
+typedef struct {
+    float proj_x, proj_y, proj_xr, view_cos;
+    int32_t track_scale_level;
+    int32_t track_in_view;
+    int32_t bad;
+    int32_t pad;
+} orbgpu_mappoint;
+
+/* ORBmatcher::SearchByProjection(Frame& F, const vector<MapPoint*>& vpMapPoints,
+ *     const float th) -- src/ORBmatcher.cc:72-183.
+ * mappoints/mp_descriptors: m records and m x 32 bytes.  claimed: n bytes,
+ * non-zero where F.mvpMapPoints[i] already holds a map point with
+ * observations (NULL = none).  match_out: n ints, receives the index of the
+ * map point assigned to keypoint i, -2 where claimed, -1 otherwise.
+ * Host memory (mem = ORBGPU_MEM_HOST) or device memory. */
+int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame* f, const orbgpu_mappoint* mappoints,
+                                const uint8_t* mp_descriptors, int n_mappoints, float th, const uint8_t* claimed,
+                                int* match_out, int mem, int* nmatches);
+
+/* Frame::ComputeStereoMatches() -- src/Frame.cc:831-1082.
+ * left/right: the two extractor handles that produced the frames (their
+ * pyramids are read in place).  bf = mbf, fx = K(0,0); mb = bf/fx.
+ * uright/depth: nL floats each (host or device per 'mem'). */
+int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* left, const orbgpu_extractor* right,
+                                  const orbgpu_frame* fl, const orbgpu_frame* fr, float bf, float fx, float* uright,
+                                  float* depth, int mem);
+
+/* Brute-force k = 2 Hamming nearest neighbours over ORBmatcher::DescriptorDistance
+ * semantics (src/ORBmatcher.cc:2083): for each query row, the best and the
+ * second-best train rows, ties to the lower train index.  Not a reference
+ * function: the build's batched matcher.  algo: 0 = popcount kernel.
+ * All arrays on the device. */
+int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
+                int* idx2, int* d2, int algo);
+
+/* ORBmatcher::DescriptorDistance for n row pairs (device arrays). */
+int orbgpu_descriptor_distance(const uint8_t* a, const uint8_t* b, int n, int* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -38,8 +38,18 @@ class ExtractResult:
 
 
 def build(ref: bool = False) -> None:
-    """Compile the restatement (and, with ref=True, the reference harness)."""
-    subprocess.run(["make", "-s", "-C", HERE, "oracle"] + (["ref"] if ref else []), check=True)
+    """Compile the restatement (and, with ref=True, the reference harness via
+    oracle/Makefile; the reference sources are only present where they were
+    mounted)."""
+    srcs = [os.path.join(HERE, "orb_oracle.cpp"), os.path.join(HERE, "cvshim", "cvshim_prims.cpp")]
+    deps = srcs + [os.path.join(HERE, f) for f in ("orb_oracle.h", "orb_types.h", "orb_pattern_table.h")]
+    deps.append(os.path.join(HERE, "cvshim", "cvshim_prims.h"))
+    if not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(d) for d in deps):
+        os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
+        subprocess.run(["g++", "-O3", "-std=c++11", "-ffp-contract=off", "-fPIC", "-shared", "-o", ORACLE_SO, *srcs,
+                        "-lm", "-pthread"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 
 def _p(a):

@@ -1,0 +1,10 @@
+"""GB300-native ORB-SLAM2 feature front-end.
+
+The compute path is liborbgpu.so (hand-written CUDA kernels for sm_103a
+behind the C ABI in include/orbgpu.h); this package mirrors the reference's
+ORBextractor / ORBmatcher / Frame interfaces on top of it.  There is no CPU
+fallback: without the built library or a CUDA device every call raises.
+"""
+from ._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE, OrbGpuError, lib  # noqa: F401
+from .extractor import ORBextractor  # noqa: F401
+from .matcher import ORBmatcher, FrameView, compute_stereo_matches  # noqa: F401

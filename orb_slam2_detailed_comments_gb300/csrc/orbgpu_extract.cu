@@ -1,0 +1,608 @@
+// orbgpu_extract.cu -- host side of the extractor: level geometry, device
+// buffers, work lists and the C ABI of include/orbgpu.h for extraction.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "orbgpu_extract_kernels.cuh"
+#include "orbgpu_host.h"
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void orbgpu_set_last_error(const char* msg, const char* file, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s (%s:%d)", msg, file, line);
+    g_last_error = buf;
+}
+
+extern "C" const char* orbgpu_last_error(void) { return g_last_error.c_str(); }
+extern "C" int orbgpu_version(void) { return 1; }
+
+namespace orbgpu {
+
+// ---------------------------------------------------------------- tables
+// ORBextractor::ORBextractor, src/ORBextractor.cc:469-571.
+ExtractorTables make_tables(int nfeatures, float scale_factor, int nlevels) {
+    ExtractorTables t;
+    t.nlevels = nlevels;
+    const double sf = (double)scale_factor;  // scaleFactor is a double member
+    t.scale.assign(nlevels, 1.0f);
+    t.sigma2.assign(nlevels, 1.0f);
+    for (int i = 1; i < nlevels; i++) {
+        t.scale[i] = (float)(t.scale[i - 1] * sf);
+        t.sigma2[i] = t.scale[i] * t.scale[i];
+    }
+    t.inv_scale.resize(nlevels);
+    t.inv_sigma2.resize(nlevels);
+    for (int i = 0; i < nlevels; i++) {
+        t.inv_scale[i] = 1.0f / t.scale[i];
+        t.inv_sigma2[i] = 1.0f / t.sigma2[i];
+    }
+    t.nfeat.assign(nlevels, 0);
+    const float factor = (float)(1.0f / sf);
+    float per_scale = nfeatures * (1 - factor) / (1 - (float)std::pow((double)factor, (double)nlevels));
+    int sum = 0;
+    for (int l = 0; l < nlevels - 1; l++) {
+        t.nfeat[l] = (int)std::lrint(per_scale);
+        sum += t.nfeat[l];
+        per_scale *= factor;
+    }
+    t.nfeat[nlevels - 1] = std::max(nfeatures - sum, 0);
+    const int hp = ORBGPU_HALF_PATCH;
+    const int vmax = (int)std::floor(hp * std::sqrt(2.f) / 2 + 1);
+    const int vmin = (int)std::ceil(hp * std::sqrt(2.f) / 2);
+    const double hp2 = hp * hp;
+    for (int v = 0; v <= vmax; ++v) t.umax[v] = (int)std::lrint(std::sqrt(hp2 - v * v));
+    for (int v = hp, v0 = 0; v >= vmin; --v) {
+        while (t.umax[v0] == t.umax[v0 + 1]) ++v0;
+        t.umax[v] = v0;
+        ++v0;
+    }
+    // getGaussianKernel(7, 2, CV_32F) in 8-bit fixed point
+    {
+        float cf[7];
+        double s = 0;
+        for (int i = 0; i < 7; i++) {
+            const double x = i - 3.0;
+            cf[i] = (float)std::exp(-0.125 * x * x);
+            s += cf[i];
+        }
+        s = 1. / s;
+        for (int i = 0; i < 7; i++) cf[i] = (float)(cf[i] * s);
+        for (int i = 0; i < 7; i++) t.taps[i] = (int)std::lrint(cf[i] * 256.f);
+    }
+    return t;
+}
+
+static inline short sat_short_round(float v) {
+    long r = std::lrint(v);
+    return (short)std::min(32767L, std::max(-32768L, r));
+}
+static inline int floor_f(float v) {
+    int i = (int)v;
+    return i - (i > v);
+}
+
+// cv::resize INTER_LINEAR coefficient tables (the fixed-point path).
+void resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int* yofs, short* ybeta) {
+    const double scale_x = 1. / ((double)dw / sw), scale_y = 1. / ((double)dh / sh);
+    int xmax = dw;
+    for (int dx = 0; dx < dw; dx++) {
+        float fx = (float)((dx + 0.5) * scale_x - 0.5);
+        int sx = floor_f(fx);
+        fx -= sx;
+        if (sx < 0) { fx = 0.f; sx = 0; }
+        if (sx + 1 >= sw) {
+            if (dx < xmax) xmax = dx;
+            if (sx >= sw - 1) { fx = 0.f; sx = sw - 1; }
+        }
+        xofs[dx] = sx;
+        xalpha[2 * dx] = sat_short_round((1.f - fx) * 2048);
+        xalpha[2 * dx + 1] = sat_short_round(fx * 2048);
+    }
+    // past xmax the horizontal pass uses the left sample alone (weight 2048)
+    for (int dx = xmax; dx < dw; dx++) {
+        xalpha[2 * dx] = 2048;
+        xalpha[2 * dx + 1] = 0;
+    }
+    for (int dy = 0; dy < dh; dy++) {
+        float fy = (float)((dy + 0.5) * scale_y - 0.5);
+        int sy = floor_f(fy);
+        fy -= sy;
+        yofs[dy] = sy;
+        ybeta[2 * dy] = sat_short_round((1.f - fy) * 2048);
+        ybeta[2 * dy + 1] = sat_short_round(fy * 2048);
+    }
+}
+
+// Level geometry of one image (src/ORBextractor.cc:1037-1063, 1661-1663).
+int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom>& g) {
+    g.resize(t.nlevels);
+    for (int l = 0; l < t.nlevels; l++) {
+        LevelGeom& L = g[l];
+        L.w = (int)std::lrint((float)w * t.inv_scale[l]);
+        L.h = (int)std::lrint((float)h * t.inv_scale[l]);
+        if (L.w < 1 || L.h < 1) return ORBGPU_ERR_BAD_ARG;
+        L.pitch = (L.w + 63) & ~63;
+        const int minB = ORBGPU_EDGE_THRESHOLD - 3;
+        L.maxBorderX = L.w - ORBGPU_EDGE_THRESHOLD + 3;
+        L.maxBorderY = L.h - ORBGPU_EDGE_THRESHOLD + 3;
+        const float width = (float)(L.maxBorderX - minB), height = (float)(L.maxBorderY - minB);
+        L.nCols = (int)(width / 30.f);
+        L.nRows = (int)(height / 30.f);
+        if (L.nCols <= 0 || L.nRows <= 0 || width <= 0 || height <= 0) {
+            // no cell fits: the level yields no keypoints
+            L.nCols = L.nRows = 0;
+            L.wCell = L.hCell = 0;
+            L.nIni = 0;
+            L.cell_cap = 0;
+        } else {
+            L.wCell = (int)std::ceil(width / L.nCols);
+            L.hCell = (int)std::ceil(height / L.nRows);
+            L.nIni = (int)std::round(static_cast<float>(L.maxBorderX - minB) / (float)(L.maxBorderY - minB));
+            // DistributeOctTree would index an empty vector (aspect below 0.5)
+            if (L.nIni < 1 || L.nIni > 64) return ORBGPU_ERR_BAD_ARG;
+            L.cell_cap = ((L.wCell + 1) / 2) * ((L.hCell + 1) / 2);
+            if (L.wCell + 6 > 72 || L.hCell + 6 > 72) return ORBGPU_ERR_BAD_ARG;
+        }
+        L.ncells = L.nCols * L.nRows;
+        L.cand_cap = L.ncells * L.cell_cap;
+        L.nfeat = t.nfeat[l];
+        L.node_cap = std::max(L.nfeat + 8, 4 * L.nIni + 8);
+        L.node_cap = (L.node_cap + 31) & ~31;
+        if (L.node_cap > 60000) return ORBGPU_ERR_BAD_ARG;
+    }
+    return ORBGPU_OK;
+}
+
+// ---------------------------------------------------------------- arena
+size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
+    size_t off = base;
+    auto take = [&](size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        size_t r = off;
+        off += bytes;
+        return r;
+    };
+    lv.resize(g.size());
+    for (size_t l = 0; l < g.size(); l++) {
+        const LevelGeom& L = g[l];
+        LevelOffsets& o = lv[l];
+        o.pyr = take((size_t)L.pitch * L.h);
+        o.blur = take((size_t)L.pitch * L.h);
+        o.xofs = take(sizeof(int) * L.w);
+        o.xalpha = take(sizeof(short) * 2 * L.w);
+        o.yofs = take(sizeof(int) * L.h);
+        o.ybeta = take(sizeof(short) * 2 * L.h);
+        o.slots = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
+        o.cell_count = take(sizeof(int) * std::max(1, L.ncells));
+        o.cand = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
+        o.node_of = take(sizeof(int) * std::max(1, L.cand_cap));
+        o.quad = take(std::max(1, L.cand_cap));
+        o.nodes_a = take(sizeof(DNode) * L.node_cap);
+        o.nodes_b = take(sizeof(DNode) * L.node_cap);
+        o.cnt4 = take(sizeof(int4) * L.node_cap);
+        o.childpos = take(sizeof(int4) * L.node_cap);
+        o.aux0 = take(sizeof(int) * L.node_cap);
+        o.aux1 = take(sizeof(int) * L.node_cap);
+        o.aux2 = take(sizeof(int) * L.node_cap);
+        o.best = take(sizeof(uint32_t) * L.node_cap);
+        o.kept = take(sizeof(uint32_t) * L.node_cap);
+    }
+    level_counts = take(sizeof(int) * 16);
+    frame_total = take(sizeof(int) * 4);
+    bytes = off - base;
+    return off;
+}
+
+void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const FrameLayout& lay, uint8_t* arena,
+                int frame, int ini_th, int min_th, int out_base, int out_cap, LevelDesc* out) {
+    for (size_t l = 0; l < g.size(); l++) {
+        const LevelGeom& L = g[l];
+        const LevelOffsets& o = lay.lv[l];
+        LevelDesc& d = out[l];
+        std::memset(&d, 0, sizeof(d));
+        if (l > 0) {
+            const LevelGeom& P = g[l - 1];
+            d.src = arena + lay.lv[l - 1].pyr;
+            d.sw = P.w;
+            d.sh = P.h;
+            d.spitch = P.pitch;
+        }
+        d.dst = arena + o.pyr;
+        d.blur = arena + o.blur;
+        d.w = L.w;
+        d.h = L.h;
+        d.pitch = L.pitch;
+        d.xofs = (const int*)(arena + o.xofs);
+        d.xalpha = (const short*)(arena + o.xalpha);
+        d.yofs = (const int*)(arena + o.yofs);
+        d.ybeta = (const short*)(arena + o.ybeta);
+        d.nCols = L.nCols;
+        d.nRows = L.nRows;
+        d.wCell = L.wCell;
+        d.hCell = L.hCell;
+        d.maxBorderX = L.maxBorderX;
+        d.maxBorderY = L.maxBorderY;
+        d.cell_cap = L.cell_cap;
+        d.slots = (uint32_t*)(arena + o.slots);
+        d.cell_count = (int*)(arena + o.cell_count);
+        d.ini_th = ini_th;
+        d.min_th = min_th;
+        d.nfeat = L.nfeat;
+        d.nIni = L.nIni;
+        d.cand_cap = L.cand_cap;
+        d.node_cap = L.node_cap;
+        d.cand = (uint32_t*)(arena + o.cand);
+        d.node_of = (int*)(arena + o.node_of);
+        d.quad = arena + o.quad;
+        d.nodes_a = arena + o.nodes_a;
+        d.nodes_b = arena + o.nodes_b;
+        d.cnt4 = (int4*)(arena + o.cnt4);
+        d.childpos = (int4*)(arena + o.childpos);
+        d.aux0 = (int*)(arena + o.aux0);
+        d.aux1 = (int*)(arena + o.aux1);
+        d.aux2 = (int*)(arena + o.aux2);
+        d.best = (uint32_t*)(arena + o.best);
+        d.kept = (uint32_t*)(arena + o.kept);
+        d.level_counts = (int*)(arena + lay.level_counts);
+        d.kept_count = d.level_counts + l;
+        d.level = (int)l;
+        d.frame = frame;
+        d.scale = t.scale[l];
+        d.nlevels = (int)g.size();
+        d.out_base = out_base;
+        d.out_cap = out_cap;
+        d.frame_total = (int*)(arena + lay.frame_total);
+    }
+}
+
+// Host-side resize tables of every level, written at their arena offsets.
+void fill_tables(const std::vector<LevelGeom>& g, const FrameLayout& lay, std::vector<uint8_t>& host_img, size_t base) {
+    for (size_t l = 1; l < g.size(); l++) {
+        const LevelGeom& P = g[l - 1];
+        const LevelGeom& L = g[l];
+        const LevelOffsets& o = lay.lv[l];
+        resize_tables(P.w, P.h, L.w, L.h, (int*)&host_img[o.xofs - base], (short*)&host_img[o.xalpha - base],
+                      (int*)&host_img[o.yofs - base], (short*)&host_img[o.ybeta - base]);
+    }
+}
+
+// ---------------------------------------------------------------- sin/cos exceptions
+// The descriptor angle's cos/sin must equal the host C library's
+// cosf/sinf (what std::cos(float) / std::sin(float) call in
+// computeOrbDescriptor, src/ORBextractor.cc:157).  The device evaluates
+// sincos_taylor and corrects the inputs listed in an exception table built
+// here from the host library.  The table covers every float in
+// [0, 360 * pi/180] and is cached on disk next to the library.
+static std::once_flag g_exc_once;
+static int g_exc_status = ORBGPU_OK;
+static uint32_t* g_exc_dev = nullptr;
+
+int load_sincos_exceptions(const char* path) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return ORBGPU_ERR_BAD_ARG;
+    int32_t hdr[4];
+    if (std::fread(hdr, sizeof(int32_t), 4, f) != 4 || hdr[0] != 0x4f524258) {
+        std::fclose(f);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    const int cn = hdr[1], sn = hdr[2];
+    std::vector<uint32_t> buf((size_t)2 * (cn + sn));
+    if (std::fread(buf.data(), sizeof(uint32_t), buf.size(), f) != buf.size()) {
+        std::fclose(f);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    std::fclose(f);
+    if (cudaMalloc(&g_exc_dev, std::max<size_t>(4, buf.size() * 4)) != cudaSuccess) return ORBGPU_ERR_OOM;
+    cudaMemcpy(g_exc_dev, buf.data(), buf.size() * 4, cudaMemcpyHostToDevice);
+    const uint32_t* ck = g_exc_dev;
+    const float* cv = (const float*)(g_exc_dev + cn);
+    const uint32_t* sk = g_exc_dev + 2 * cn;
+    const float* sv = (const float*)(g_exc_dev + 2 * cn + sn);
+    set_sincos_exceptions(ck, cv, cn, sk, sv, sn);
+    return ORBGPU_OK;
+}
+
+int ensure_sincos_exceptions() {
+    std::call_once(g_exc_once, []() {
+        const char* p = std::getenv("ORBGPU_SINCOS_TABLE");
+        std::string path = p ? p : default_sincos_table_path();
+        g_exc_status = load_sincos_exceptions(path.c_str());
+        if (g_exc_status != ORBGPU_OK) {
+            std::string msg = "sin/cos exception table not found or invalid: " + path;
+            orbgpu_set_last_error(msg.c_str(), __FILE__, __LINE__);
+        }
+    });
+    return g_exc_status;
+}
+
+}  // namespace orbgpu
+
+using namespace orbgpu;
+
+struct orbgpu_extractor {
+    int nfeatures, nlevels, ini_th, min_th;
+    float scale_factor;
+    int max_w, max_h;
+    ExtractorTables tables;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // current geometry
+    int cur_w = -1, cur_h = -1;
+    std::vector<LevelGeom> geom;
+    FrameLayout layout;
+    uint8_t* arena = nullptr;
+    size_t arena_bytes = 0;
+    LevelDesc* d_descs = nullptr;
+    WorkItem* d_items = nullptr;
+    size_t items_cap = 0;
+    std::vector<int> rb_first, rb_count;  // resize/blur items per level
+    int fast_first = 0, fast_count = 0;
+    int max_kept = 0, sort_cap = 0;
+    int* d_status = nullptr;
+    // output staging
+    orbgpu_keypoint* d_kps = nullptr;
+    uint8_t* d_desc = nullptr;
+    int out_cap = 0;
+    int* h_pinned = nullptr;  // status + counts
+};
+
+static int setup_geometry(orbgpu_extractor* ex, int w, int h) {
+    if (w == ex->cur_w && h == ex->cur_h) return ORBGPU_OK;
+    std::vector<LevelGeom> g;
+    int rc = level_geometry(ex->tables, w, h, g);
+    if (rc != ORBGPU_OK) {
+        orbgpu_set_last_error("image size not supported by the level geometry", __FILE__, __LINE__);
+        return rc;
+    }
+    FrameLayout lay;
+    lay.plan(g, 0);
+    if (lay.bytes > ex->arena_bytes) {
+        if (ex->arena) cudaFree(ex->arena);
+        ex->arena = nullptr;
+        ORBGPU_CUDA_TRY(cudaMalloc(&ex->arena, lay.bytes));
+        ex->arena_bytes = lay.bytes;
+    }
+    // resize tables
+    std::vector<uint8_t> host(lay.bytes, 0);
+    fill_tables(g, lay, host, 0);
+    for (size_t l = 1; l < g.size(); l++) {
+        const LevelOffsets& o = lay.lv[l];
+        const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * g[l].h;
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->arena + lo, host.data() + lo, hi - lo, cudaMemcpyHostToDevice, ex->stream));
+    }
+    // work lists
+    std::vector<WorkItem> items;
+    ex->rb_first.assign(g.size(), 0);
+    ex->rb_count.assign(g.size(), 0);
+    for (size_t l = 0; l < g.size(); l++) {
+        ex->rb_first[l] = (int)items.size();
+        const int tiles = ((g[l].w + 63) / 64) * ((g[l].h + 15) / 16);
+        for (int i = 0; i < tiles; i++) items.push_back({(int)l, i});
+        ex->rb_count[l] = tiles;
+    }
+    ex->fast_first = (int)items.size();
+    for (size_t l = 0; l < g.size(); l++)
+        for (int c = 0; c < g[l].ncells; c++) items.push_back({(int)l, c});
+    ex->fast_count = (int)items.size() - ex->fast_first;
+    if (items.size() > ex->items_cap) {
+        if (ex->d_items) cudaFree(ex->d_items);
+        ex->d_items = nullptr;
+        ORBGPU_CUDA_TRY(cudaMalloc(&ex->d_items, items.size() * sizeof(WorkItem)));
+        ex->items_cap = items.size();
+    }
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                                    ex->stream));
+    ex->max_kept = 0;
+    ex->sort_cap = 1;
+    for (auto& L : g) {
+        ex->max_kept = std::max(ex->max_kept, L.node_cap);
+        while (ex->sort_cap < L.node_cap) ex->sort_cap <<= 1;
+    }
+    ex->geom = g;
+    ex->layout = lay;
+    ex->cur_w = w;
+    ex->cur_h = h;
+    return ORBGPU_OK;
+}
+
+static int ensure_out(orbgpu_extractor* ex, int cap) {
+    if (cap <= ex->out_cap) return ORBGPU_OK;
+    if (ex->d_kps) cudaFree(ex->d_kps);
+    if (ex->d_desc) cudaFree(ex->d_desc);
+    ex->d_kps = nullptr;
+    ex->d_desc = nullptr;
+    ORBGPU_CUDA_TRY(cudaMalloc(&ex->d_kps, sizeof(orbgpu_keypoint) * (size_t)cap));
+    ORBGPU_CUDA_TRY(cudaMalloc(&ex->d_desc, 32 * (size_t)cap));
+    ex->out_cap = cap;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_extractor_create(int nfeatures, float scale_factor, int nlevels, int ini_th_fast,
+                                       int min_th_fast, int max_width, int max_height, void* stream,
+                                       orbgpu_extractor** out) {
+    if (!out || nfeatures < 0 || nlevels < 1 || nlevels > ORBGPU_MAX_LEVELS || !(scale_factor > 1.0f) ||
+        max_width < 0 || max_height < 0 || max_width > ORBGPU_MAX_DIM || max_height > ORBGPU_MAX_DIM) {
+        orbgpu_set_last_error("invalid extractor parameters", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    int dev = 0;
+    ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
+    int rc = ensure_sincos_exceptions();
+    if (rc != ORBGPU_OK) return rc;
+    orbgpu_extractor* ex = new orbgpu_extractor();
+    ex->nfeatures = nfeatures;
+    ex->scale_factor = scale_factor;
+    ex->nlevels = nlevels;
+    ex->ini_th = ini_th_fast;
+    ex->min_th = min_th_fast;
+    ex->max_w = max_width;
+    ex->max_h = max_height;
+    ex->tables = make_tables(nfeatures, scale_factor, nlevels);
+    if (stream) ex->stream = (cudaStream_t)stream;
+    else {
+        cudaError_t e = cudaStreamCreateWithFlags(&ex->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete ex;
+            orbgpu_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+            return ORBGPU_ERR_CUDA;
+        }
+        ex->own_stream = true;
+    }
+    cudaError_t e1 = cudaMalloc(&ex->d_descs, sizeof(LevelDesc) * ORBGPU_MAX_LEVELS);
+    cudaError_t e2 = cudaMalloc(&ex->d_status, sizeof(int) * 4);
+    cudaError_t e3 = cudaMallocHost(&ex->h_pinned, sizeof(int) * 32);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+        orbgpu_set_last_error("device allocation failed", __FILE__, __LINE__);
+        orbgpu_extractor_destroy(ex);
+        return ORBGPU_ERR_OOM;
+    }
+    upload_constants(ex->stream, ex->tables.taps, ex->tables.umax);
+    if (max_width > 0 && max_height > 0) {
+        rc = setup_geometry(ex, max_width, max_height);
+        if (rc != ORBGPU_OK) {
+            orbgpu_extractor_destroy(ex);
+            return rc;
+        }
+    }
+    *out = ex;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_extractor_destroy(orbgpu_extractor* ex) {
+    if (!ex) return ORBGPU_OK;
+    if (ex->stream) cudaStreamSynchronize(ex->stream);
+    cudaFree(ex->arena);
+    cudaFree(ex->d_descs);
+    cudaFree(ex->d_items);
+    cudaFree(ex->d_status);
+    cudaFree(ex->d_kps);
+    cudaFree(ex->d_desc);
+    cudaFreeHost(ex->h_pinned);
+    if (ex->own_stream) cudaStreamDestroy(ex->stream);
+    delete ex;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int width, int height, size_t step,
+                              int image_mem, orbgpu_keypoint* keypoints, uint8_t* descriptors, int capacity,
+                              int out_mem, int* n_keypoints) {
+    if (!ex || !n_keypoints) {
+        orbgpu_set_last_error("null handle or count pointer", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    *n_keypoints = 0;
+    // an empty image returns without output (src/ORBextractor.cc:1537)
+    if (image == nullptr || width == 0 || height == 0) return ORBGPU_OK;
+    if (width < 0 || height < 0 || width > ORBGPU_MAX_DIM || height > ORBGPU_MAX_DIM || step < (size_t)width ||
+        capacity < 0 || (capacity > 0 && (!keypoints || !descriptors)) ||
+        (ex->max_w > 0 && (width > ex->max_w || height > ex->max_h))) {
+        orbgpu_set_last_error("invalid image or output arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    int rc = setup_geometry(ex, width, height);
+    if (rc != ORBGPU_OK) return rc;
+    const std::vector<LevelGeom>& g = ex->geom;
+    const int nl = (int)g.size();
+    // descriptors of this call (outputs go to the caller's device arrays or
+    // to the staging buffers)
+    orbgpu_keypoint* okps;
+    uint8_t* odesc;
+    if (out_mem == ORBGPU_MEM_DEVICE) {
+        okps = keypoints;
+        odesc = descriptors;
+    } else {
+        rc = ensure_out(ex, std::max(capacity, 1));
+        if (rc != ORBGPU_OK) return rc;
+        okps = ex->d_kps;
+        odesc = ex->d_desc;
+    }
+    LevelDesc hd[ORBGPU_MAX_LEVELS];
+    fill_descs(g, ex->tables, ex->layout, ex->arena, 0, ex->ini_th, ex->min_th, 0, capacity, hd);
+    cudaStream_t st = ex->stream;
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_descs, hd, sizeof(LevelDesc) * nl, cudaMemcpyHostToDevice, st));
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(ex->d_status, 0, sizeof(int) * 4, st));
+    // level 0 = the image
+    ORBGPU_CUDA_TRY(cudaMemcpy2DAsync(hd[0].dst, hd[0].pitch, image, step, width, height,
+                                      image_mem == ORBGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice
+                                                                     : cudaMemcpyHostToDevice,
+                                      st));
+    for (int l = 0; l < nl; l++)
+        launch_resize_blur(ex->d_descs, ex->d_items + ex->rb_first[l], ex->rb_count[l], l == 0, st);
+    launch_fast(ex->d_descs, ex->d_items + ex->fast_first, ex->fast_count, ex->d_status, st);
+    launch_distribute(ex->d_descs, nl, ex->sort_cap, ex->d_status, st);
+    launch_describe(ex->d_descs, nl, ex->max_kept, okps, odesc, ex->d_status, st);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->h_pinned, ex->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->h_pinned + 4, hd[0].frame_total, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    const int status = ex->h_pinned[0];
+    const int total = ex->h_pinned[4];
+    *n_keypoints = total;
+    if (status & ~16) {
+        char msg[128];
+        std::snprintf(msg, sizeof(msg), "device-side capacity check failed (status 0x%x)", status);
+        orbgpu_set_last_error(msg, __FILE__, __LINE__);
+        return ORBGPU_ERR_CUDA;
+    }
+    if (total > capacity) {
+        orbgpu_set_last_error("output capacity too small", __FILE__, __LINE__);
+        return ORBGPU_ERR_CAPACITY;
+    }
+    if (out_mem != ORBGPU_MEM_DEVICE && total > 0) {
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(keypoints, okps, sizeof(orbgpu_keypoint) * total, cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(descriptors, odesc, 32 * (size_t)total, cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_extractor_tables(const orbgpu_extractor* ex, int* nlevels, float* scale_factors,
+                                       float* inv_scale_factors, float* sigma2, float* inv_sigma2,
+                                       int* features_per_level) {
+    if (!ex) return ORBGPU_ERR_BAD_ARG;
+    const ExtractorTables& t = ex->tables;
+    if (nlevels) *nlevels = t.nlevels;
+    for (int l = 0; l < t.nlevels; l++) {
+        if (scale_factors) scale_factors[l] = t.scale[l];
+        if (inv_scale_factors) inv_scale_factors[l] = t.inv_scale[l];
+        if (sigma2) sigma2[l] = t.sigma2[l];
+        if (inv_sigma2) inv_sigma2[l] = t.inv_sigma2[l];
+        if (features_per_level) features_per_level[l] = t.nfeat[l];
+    }
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_extractor_pyramid_level(const orbgpu_extractor* ex, int level, const uint8_t** dev_ptr,
+                                              int* width, int* height, size_t* pitch) {
+    if (!ex || level < 0 || level >= ex->nlevels || ex->cur_w < 0) return ORBGPU_ERR_BAD_ARG;
+    const LevelGeom& L = ex->geom[level];
+    if (dev_ptr) *dev_ptr = ex->arena + ex->layout.lv[level].pyr;
+    if (width) *width = L.w;
+    if (height) *height = L.h;
+    if (pitch) *pitch = L.pitch;
+    return ORBGPU_OK;
+}
+
+extern "C" void* orbgpu_extractor_stream(const orbgpu_extractor* ex) { return ex ? (void*)ex->stream : nullptr; }
+
+// blurred level accessor used by the kernel tests
+extern "C" int orbgpu_extractor_blurred_level(const orbgpu_extractor* ex, int level, const uint8_t** dev_ptr) {
+    if (!ex || level < 0 || level >= ex->nlevels || ex->cur_w < 0) return ORBGPU_ERR_BAD_ARG;
+    *dev_ptr = ex->arena + ex->layout.lv[level].blur;
+    return ORBGPU_OK;
+}
+
+// Synchronous device-to-host copy of library-owned buffers (tests, tools).
+extern "C" int orbgpu_copy_to_host(void* dst, const void* src, size_t bytes) {
+    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
+    ORBGPU_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return ORBGPU_OK;
+}

@@ -1,0 +1,724 @@
+// orbgpu_extract_kernels.cu -- the ORB extraction stages (see the .cuh).
+#include "orbgpu_extract_kernels.cuh"
+#include "orb_pattern.h"
+#include "orbgpu_host.h"
+
+namespace orbgpu {
+
+__constant__ int c_gauss_taps[7];
+__constant__ int c_umax[ORBGPU_HALF_PATCH + 1];
+__constant__ signed char c_pattern[256 * 4];
+
+// Exception table of the descriptor rotation: sorted float bit patterns x for
+// which the host C library's cosf(x)/sinf(x) differ from the rounded
+// sincos_taylor(x) value, with the library's results.
+__device__ const uint32_t* g_cos_exc_key = nullptr;
+__device__ const float* g_cos_exc_val = nullptr;
+__device__ int g_cos_exc_n = 0;
+__device__ const uint32_t* g_sin_exc_key = nullptr;
+__device__ const float* g_sin_exc_val = nullptr;
+__device__ int g_sin_exc_n = 0;
+
+__device__ __forceinline__ int reflect101(int p, int len) {
+    if (len == 1) return 0;
+    while (p < 0 || p >= len) p = p < 0 ? -p : 2 * len - 2 - p;
+    return p;
+}
+
+// ---------------------------------------------------------------- pyramid
+#define RB_TW 64
+#define RB_TH 16
+#define RB_HALO 3
+
+__device__ __forceinline__ int resize_pixel(const LevelDesc& d, int x, int y) {
+    const int sx = d.xofs[x];
+    const int sx1 = min(sx + 1, d.sw - 1);
+    const int a0 = d.xalpha[2 * x], a1 = d.xalpha[2 * x + 1];
+    const int sy = d.yofs[y];
+    const int r0 = min(max(sy, 0), d.sh - 1), r1 = min(max(sy + 1, 0), d.sh - 1);
+    const int b0 = d.ybeta[2 * y], b1 = d.ybeta[2 * y + 1];
+    const uint8_t* S0 = d.src + (size_t)r0 * d.spitch;
+    const uint8_t* S1 = d.src + (size_t)r1 * d.spitch;
+    const int h0 = S0[sx] * a0 + S0[sx1] * a1;
+    const int h1 = S1[sx] * a0 + S1[sx1] * a1;
+    const int v = (h0 * b0 + h1 * b1 + (1 << 21)) >> 22;
+    return v < 0 ? 0 : (v > 255 ? 255 : v);
+}
+
+// Level l (l >= 1) by resizing level l-1, then the blur of level l; at
+// level 0 only the blur.  One 64x16 tile per block.
+__global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* descs, const WorkItem* items, int level0) {
+    const WorkItem it = items[blockIdx.x];
+    const LevelDesc& d = descs[it.desc];
+    const int tiles_x = (d.w + RB_TW - 1) / RB_TW;
+    const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH;
+    __shared__ uint8_t tile[RB_TH + 2 * RB_HALO][RB_TW + 2 * RB_HALO];
+    __shared__ int rows[RB_TH + 2 * RB_HALO][RB_TW];
+    const int TW = RB_TW + 2 * RB_HALO, TH = RB_TH + 2 * RB_HALO;
+    for (int i = threadIdx.x; i < TW * TH; i += blockDim.x) {
+        const int ty = i / TW, tx = i % TW;
+        const int x = reflect101(ox - RB_HALO + tx, d.w), y = reflect101(oy - RB_HALO + ty, d.h);
+        int v;
+        if (level0) v = d.dst[(size_t)y * d.pitch + x];
+        else v = resize_pixel(d, x, y);
+        tile[ty][tx] = (uint8_t)v;
+        const int gx = ox - RB_HALO + tx, gy = oy - RB_HALO + ty;
+        if (!level0 && tx >= RB_HALO && tx < RB_HALO + RB_TW && ty >= RB_HALO && ty < RB_HALO + RB_TH && gx < d.w && gy < d.h)
+            d.dst[(size_t)gy * d.pitch + gx] = (uint8_t)v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < RB_TW * TH; i += blockDim.x) {
+        const int ty = i / RB_TW, tx = i % RB_TW;
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < 7; k++) s += c_gauss_taps[k] * tile[ty][tx + k];
+        rows[ty][tx] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < RB_TW * RB_TH; i += blockDim.x) {
+        const int ty = i / RB_TW, tx = i % RB_TW;
+        const int gx = ox + tx, gy = oy + ty;
+        if (gx >= d.w || gy >= d.h) continue;
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < 7; k++) s += c_gauss_taps[k] * rows[ty + k][tx];
+        s = (s + (1 << 15)) >> 16;
+        d.blur[(size_t)gy * d.pitch + gx] = (uint8_t)(s < 0 ? 0 : (s > 255 ? 255 : s));
+    }
+}
+
+// ---------------------------------------------------------------- FAST
+// Circle of radius 3 in cyclic order (dx, dy).
+__constant__ int8_t c_circle[16][2] = {{0, 3},  {1, 3},   {2, 2},   {3, 1},   {3, 0},  {3, -1},
+                                       {2, -2}, {1, -3},  {0, -3},  {-1, -3}, {-2, -2}, {-3, -1},
+                                       {-3, 0}, {-3, 1},  {-2, 2},  {-1, 3}};
+
+__device__ __forceinline__ bool has_run9(uint32_t m) {
+    uint32_t m32 = m | (m << 16);
+    uint32_t r = m32 & (m32 >> 1);
+    r &= r >> 2;
+    r &= r >> 4;
+    r &= m32 >> 8;
+    return (r & 0xFFFFu) != 0;
+}
+
+// Largest arc threshold (max over the 16 nine-pixel arcs of the smallest
+// absolute difference of consistent sign) if the pixel is a FAST corner at
+// threshold t, else 0.
+__device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw, int r, int c, int t) {
+    const uint8_t* cp = roi + r * rw + c;
+    const int v = cp[0];
+    const int p0 = cp[3 * rw], p4 = cp[3], p8 = cp[-3 * rw], p12 = cp[-3];
+    const int hi = v + t, lo = v - t;
+    const bool b0 = p0 > hi, b4 = p4 > hi, b8 = p8 > hi, b12 = p12 > hi;
+    const bool d0 = p0 < lo, d4 = p4 < lo, d8 = p8 < lo, d12 = p12 < lo;
+    const bool maybe_b = (b0 & b4) | (b4 & b8) | (b8 & b12) | (b12 & b0);
+    const bool maybe_d = (d0 & d4) | (d4 & d8) | (d8 & d12) | (d12 & d0);
+    if (!maybe_b && !maybe_d) return 0;
+    int dd[16];
+    uint32_t bm = 0, dm = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int p = cp[c_circle[k][0] + c_circle[k][1] * rw];
+        dd[k] = v - p;
+        bm |= (uint32_t)(p > hi) << k;
+        dm |= (uint32_t)(p < lo) << k;
+    }
+    if (!has_run9(bm) && !has_run9(dm)) return 0;
+    int best = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        int mn = dd[k], mx = dd[k];
+#pragma unroll
+        for (int j = 1; j < 9; j++) {
+            const int e = dd[(k + j) & 15];
+            mn = min(mn, e);
+            mx = max(mx, e);
+        }
+        best = max(best, max(mn, -mx));
+    }
+    return best;
+}
+
+#define FAST_MAX_ROI 72
+__global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, const WorkItem* items, int* status) {
+    const WorkItem it = items[blockIdx.x];
+    const LevelDesc& d = descs[it.desc];
+    const int cell = it.index;
+    const int i = cell / d.nCols, j = cell % d.nCols;
+    const int minB = ORBGPU_EDGE_THRESHOLD - 3;
+    const int iniY = minB + i * d.hCell, iniX = minB + j * d.wCell;
+    int maxY = iniY + d.hCell + 6, maxX = iniX + d.wCell + 6;
+    const bool skip = (iniY >= d.maxBorderY - 3) || (iniX >= d.maxBorderX - 6);
+    if (maxY > d.maxBorderY) maxY = d.maxBorderY;
+    if (maxX > d.maxBorderX) maxX = d.maxBorderX;
+    const int rw = maxX - iniX, rh = maxY - iniY;
+    if (skip || rw < 7 || rh < 7 || rw > FAST_MAX_ROI || rh > FAST_MAX_ROI) {
+        if (threadIdx.x == 0) {
+            d.cell_count[cell] = 0;
+            if (!skip && (rw > FAST_MAX_ROI || rh > FAST_MAX_ROI)) atomicOr(status, 1);
+        }
+        return;
+    }
+    __shared__ uint8_t roi[FAST_MAX_ROI * FAST_MAX_ROI];
+    __shared__ uint8_t mstr[(FAST_MAX_ROI - 6) * (FAST_MAX_ROI - 6)];
+    __shared__ int s_scan[32];
+    for (int k = threadIdx.x; k < rw * rh; k += blockDim.x) {
+        const int r = k / rw, c = k % rw;
+        roi[k] = d.dst[(size_t)(iniY + r) * d.pitch + iniX + c];
+    }
+    __syncthreads();
+    const int dw = rw - 6, dh = rh - 6, nd = dw * dh;
+    const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
+    const int t_lo = min(ini_th, min_th);
+    for (int k = threadIdx.x; k < nd; k += blockDim.x) {
+        const int r = k / dw + 3, c = k % dw + 3;
+        mstr[k] = (uint8_t)arc_strength(roi, rw, r, c, t_lo);
+    }
+    __syncthreads();
+    const int chunk = (nd + blockDim.x - 1) / blockDim.x;
+    const int k0 = threadIdx.x * chunk, k1 = min(nd, k0 + chunk);
+    for (int pass = 0; pass < 2; pass++) {
+        const int th = pass == 0 ? ini_th : min_th;
+        int cnt = 0;
+        for (int k = k0; k < k1; k++) {
+            const int m = mstr[k];
+            if (m <= th) continue;
+            const int s = m - 1;
+            const int r = k / dw, c = k % dw;
+            bool keep = true;
+            for (int dy = -1; dy <= 1 && keep; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (!dx && !dy) continue;
+                    const int rr = r + dy, cc = c + dx;
+                    if (rr < 0 || rr >= dh || cc < 0 || cc >= dw) continue;
+                    const int mq = mstr[rr * dw + cc];
+                    const int nb = mq > th ? mq - 1 : 0;
+                    if (!(s > nb)) { keep = false; break; }
+                }
+            cnt += keep;
+        }
+        int total;
+        int pos = block_exclusive_scan(cnt, s_scan, &total);
+        if (total == 0 && pass == 0) continue;
+        if (total > d.cell_cap) {
+            if (threadIdx.x == 0) atomicOr(status, 2);
+            total = d.cell_cap;
+        }
+        uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
+        for (int k = k0; k < k1 && cnt > 0; k++) {
+            const int m = mstr[k];
+            if (m <= th) continue;
+            const int s = m - 1;
+            const int r = k / dw, c = k % dw;
+            bool keep = true;
+            for (int dy = -1; dy <= 1 && keep; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (!dx && !dy) continue;
+                    const int rr = r + dy, cc = c + dx;
+                    if (rr < 0 || rr >= dh || cc < 0 || cc >= dw) continue;
+                    const int mq = mstr[rr * dw + cc];
+                    const int nb = mq > th ? mq - 1 : 0;
+                    if (!(s > nb)) { keep = false; break; }
+                }
+            if (keep) {
+                if (pos < total)
+                    out[pos] = (uint32_t)(iniX + 3 + c) | ((uint32_t)(iniY + 3 + r) << 12) | ((uint32_t)s << 24);
+                pos++;
+            }
+        }
+        if (threadIdx.x == 0) d.cell_count[cell] = total;
+        return;
+    }
+    if (threadIdx.x == 0) d.cell_count[cell] = 0;
+}
+
+// ---------------------------------------------------------------- DistributeOctTree
+// List order of the reference's std::list<ExtractorNode>: after the initial
+// nodes are appended, nodes are only ever pushed to the front, so the list
+// is "children by creation number descending, then the initial nodes".  A
+// split step therefore rebuilds the list as: the children created in this
+// step in reverse creation order, followed by the nodes that were not split,
+// in their previous order.  Node arrays are indexed by list position.
+
+__device__ __forceinline__ int quadrant_of(uint32_t p, const DNode& n) {
+    const float x = (float)((int)(p & 0xFFF) - (ORBGPU_EDGE_THRESHOLD - 3));
+    const float y = (float)((int)((p >> 12) & 0xFFF) - (ORBGPU_EDGE_THRESHOLD - 3));
+    const int halfX = (int)ceilf(__fdiv_rn((float)(n.x1 - n.x0), 2.f));
+    const int halfY = (int)ceilf(__fdiv_rn((float)(n.y1 - n.y0), 2.f));
+    const int xm = n.x0 + halfX, ym = n.y0 + halfY;
+    if (x < (float)xm) return y < (float)ym ? 0 : 2;
+    return y < (float)ym ? 1 : 3;
+}
+
+__device__ __forceinline__ DNode child_rect(const DNode& n, int q) {
+    const int halfX = (int)ceilf(__fdiv_rn((float)(n.x1 - n.x0), 2.f));
+    const int halfY = (int)ceilf(__fdiv_rn((float)(n.y1 - n.y0), 2.f));
+    const int xm = n.x0 + halfX, ym = n.y0 + halfY;
+    DNode c;
+    c.x0 = (int16_t)((q & 1) ? xm : n.x0);
+    c.x1 = (int16_t)((q & 1) ? n.x1 : xm);
+    c.y0 = (int16_t)((q & 2) ? ym : n.y0);
+    c.y1 = (int16_t)((q & 2) ? n.y1 : ym);
+    return c;
+}
+
+// Applies one split step.  split_rank[n] >= 0 is node n's rank in creation
+// order (nsplit nodes split), -1 for nodes kept.  order[rank] = node.
+// Returns (through smem) the new alive count and the number of children with
+// more than one key.
+__device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive, int K, int nsplit, int& next_id,
+                           int& n_big, int* s_scan, int* s_vars) {
+    int* split_rank = d.aux0;
+    int* order = d.aux1;
+    int* base = d.aux2;
+    // 1. quadrant counts for keys of split nodes
+    for (int n = threadIdx.x; n < alive; n += blockDim.x) d.cnt4[n] = make_int4(0, 0, 0, 0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const int n = d.node_of[k];
+        if (split_rank[n] < 0) continue;
+        const int q = quadrant_of(d.cand[k], A[n]);
+        d.quad[k] = (uint8_t)q;
+        atomicAdd(&((int*)&d.cnt4[n])[q], 1);
+    }
+    __syncthreads();
+    // 2. children per split node, in creation order -> creation base
+    int E = 0;
+    const int U_count = alive - nsplit;
+    for (int b0 = 0; b0 < nsplit; b0 += blockDim.x) {
+        const int rk = b0 + threadIdx.x;
+        int c = 0;
+        if (rk < nsplit) {
+            const int4 q = d.cnt4[order[rk]];
+            c = (q.x > 0) + (q.y > 0) + (q.z > 0) + (q.w > 0);
+        }
+        int tot;
+        const int ex = block_exclusive_scan(c, s_scan, &tot);
+        if (rk < nsplit) base[rk] = E + ex;
+        E += tot;
+    }
+    __syncthreads();
+    if (E + U_count > d.node_cap) {  // node arrays too small: report and stop
+        if (threadIdx.x == 0) s_vars[15] = 1;
+        __syncthreads();
+        n_big = 0;
+        return;
+    }
+    // 3. unsplit nodes keep their order after the E children
+    int U = 0;
+    for (int b0 = 0; b0 < alive; b0 += blockDim.x) {
+        const int n = b0 + threadIdx.x;
+        const int u = (n < alive && split_rank[n] < 0) ? 1 : 0;
+        int tot;
+        const int ex = block_exclusive_scan(u, s_scan, &tot);
+        if (u) {
+            B[E + U + ex] = A[n];
+            d.childpos[n] = make_int4(E + U + ex, 0, 0, 0);
+        }
+        U += tot;
+    }
+    // 4. children
+    int big = 0;
+    for (int rk = threadIdx.x; rk < nsplit; rk += blockDim.x) {
+        const int n = order[rk];
+        const int4 q4 = d.cnt4[n];
+        const int cq[4] = {q4.x, q4.y, q4.z, q4.w};
+        int pos4[4] = {-1, -1, -1, -1};
+        int r = 0;
+        for (int q = 0; q < 4; q++) {
+            if (cq[q] == 0) continue;
+            const int e = base[rk] + r++;
+            const int pos = E - 1 - e;
+            DNode c = child_rect(A[n], q);
+            c.cnt = cq[q];
+            c.id = next_id + e;
+            c.flags = cq[q] == 1 ? 1 : 0;
+            B[pos] = c;
+            pos4[q] = pos;
+            big += cq[q] > 1;
+        }
+        d.childpos[n] = make_int4(pos4[0], pos4[1], pos4[2], pos4[3]);
+    }
+    __syncthreads();
+    // 5. keys follow their nodes
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const int n = d.node_of[k];
+        const int4 cp = d.childpos[n];
+        if (split_rank[n] < 0) d.node_of[k] = cp.x;
+        else {
+            const int q = d.quad[k];
+            d.node_of[k] = q == 0 ? cp.x : (q == 1 ? cp.y : (q == 2 ? cp.z : cp.w));
+        }
+    }
+    // block sum of 'big'
+    int tot_big;
+    block_exclusive_scan(big, s_scan, &tot_big);
+    DNode* t = A;
+    A = B;
+    B = t;
+    next_id += E;
+    alive = E + U;
+    n_big = tot_big;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int* status) {
+    const LevelDesc& d = descs[blockIdx.x];
+    __shared__ int s_scan[32];
+    __shared__ int s_vars[16];
+    __shared__ int s_root_cnt[64];
+    __shared__ int s_root_pos[64];
+    extern __shared__ unsigned long long s_sort[];
+    const int ncells = d.nCols * d.nRows;
+    // 1. candidates in the reference's emission order: cell rows, cell
+    //    columns, then the detector's row-major order inside each cell.
+    int K = 0;
+    for (int b0 = 0; b0 < ncells; b0 += blockDim.x) {
+        const int c = b0 + threadIdx.x;
+        const int cnt = c < ncells ? d.cell_count[c] : 0;
+        int tot;
+        const int ex = block_exclusive_scan(cnt, s_scan, &tot);
+        for (int k = 0; k < cnt; k++) d.cand[K + ex + k] = d.slots[(size_t)c * d.cell_cap + k];
+        K += tot;
+    }
+    __syncthreads();
+    if (K == 0 || d.nIni <= 0) {
+        if (threadIdx.x == 0) *d.kept_count = 0;
+        return;
+    }
+    DNode* A = (DNode*)d.nodes_a;
+    DNode* B = (DNode*)d.nodes_b;
+    const int minB = ORBGPU_EDGE_THRESHOLD - 3;
+    const int Wd = d.maxBorderX - minB, Hd = d.maxBorderY - minB;
+    const int nIni = d.nIni;
+    const float hX = __fdiv_rn((float)Wd, (float)nIni);
+    // 2. initial nodes
+    if (threadIdx.x < 64) s_root_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const float x = (float)((int)(d.cand[k] & 0xFFF) - minB);
+        int r = (int)__fdiv_rn(x, hX);
+        if (r >= nIni) { atomicOr(status, 4); r = nIni - 1; }
+        d.node_of[k] = r;
+        atomicAdd(&s_root_cnt[r], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int a = 0;
+        for (int r = 0; r < nIni; r++) {
+            s_root_pos[r] = -1;
+            if (s_root_cnt[r] == 0) continue;
+            DNode n;
+            n.x0 = (int16_t)(int)__fmul_rn(hX, (float)r);
+            n.x1 = (int16_t)(int)__fmul_rn(hX, (float)(r + 1));
+            n.y0 = 0;
+            n.y1 = (int16_t)Hd;
+            n.cnt = s_root_cnt[r];
+            n.id = r;
+            n.flags = 2 | (s_root_cnt[r] == 1 ? 1 : 0);
+            A[a] = n;
+            s_root_pos[r] = a++;
+        }
+        s_vars[0] = a;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) d.node_of[k] = s_root_pos[d.node_of[k]];
+    if (threadIdx.x == 0) s_vars[15] = 0;
+    int alive = s_vars[0];
+    int next_id = nIni;
+    const int N = d.nfeat;
+    __syncthreads();
+    // 3. full passes (src/ORBextractor.cc:759-904)
+    bool final_phase = false;
+    for (int guard = 0; guard < 64; guard++) {
+        const int prev = alive;
+        // every node without bNoMore splits, in list order
+        int nsplit = 0;
+        for (int b0 = 0; b0 < alive; b0 += blockDim.x) {
+            const int n = b0 + threadIdx.x;
+            const int s = (n < alive && !(A[n].flags & 1)) ? 1 : 0;
+            int tot;
+            const int ex = block_exclusive_scan(s, s_scan, &tot);
+            if (n < alive) {
+                d.aux0[n] = s ? nsplit + ex : -1;
+                if (s) d.aux1[nsplit + ex] = n;
+            }
+            nsplit += tot;
+        }
+        __syncthreads();
+        int n_big = 0;
+        split_step(d, A, B, alive, K, nsplit, next_id, n_big, s_scan, s_vars);
+        if (s_vars[15]) break;
+        if (alive >= N || alive == prev) break;
+        if (alive + n_big * 3 > N) { final_phase = true; break; }
+        if (guard == 63) atomicOr(status, 8);
+    }
+    // 4. final phase (src/ORBextractor.cc:908-991): split the largest nodes
+    //    first, ties broken by later creation first, until N is reached.
+    if (final_phase) {
+        for (int guard = 0; guard < 64; guard++) {
+            const int prev = alive;
+            // nodes with more than one key (all created by the last step)
+            int nv = 0;
+            for (int b0 = 0; b0 < alive; b0 += blockDim.x) {
+                const int n = b0 + threadIdx.x;
+                const int s = (n < alive && A[n].cnt > 1) ? 1 : 0;
+                int tot;
+                const int ex = block_exclusive_scan(s, s_scan, &tot);
+                if (s) s_sort[nv + ex] = ((unsigned long long)A[n].cnt << 40) | ((unsigned long long)A[n].id << 16) | (unsigned long long)n;
+                nv += tot;
+            }
+            __syncthreads();
+            if (nv == 0) break;
+            int np2 = 1;
+            while (np2 < nv) np2 <<= 1;
+            for (int k = nv + threadIdx.x; k < np2; k += blockDim.x) s_sort[k] = 0ull;
+            __syncthreads();
+            // bitonic sort, descending
+            for (int size = 2; size <= np2; size <<= 1)
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int t = threadIdx.x; t < np2 / 2; t += blockDim.x) {
+                        const int lo = 2 * t - (t & (stride - 1));
+                        const int hi = lo + stride;
+                        const bool desc = ((lo & size) == 0);
+                        const unsigned long long a = s_sort[lo], b = s_sort[hi];
+                        if ((a < b) == desc) {
+                            s_sort[lo] = b;
+                            s_sort[hi] = a;
+                        }
+                    }
+                    __syncthreads();
+                }
+            // children count of each candidate node -> how many to split
+            for (int n = threadIdx.x; n < alive; n += blockDim.x) d.cnt4[n] = make_int4(0, 0, 0, 0);
+            for (int n = threadIdx.x; n < alive; n += blockDim.x) d.aux0[n] = -1;
+            __syncthreads();
+            for (int j = threadIdx.x; j < nv; j += blockDim.x) d.aux0[(int)(s_sort[j] & 0xFFFF)] = j;
+            __syncthreads();
+            for (int k = threadIdx.x; k < K; k += blockDim.x) {
+                const int n = d.node_of[k];
+                if (d.aux0[n] < 0) continue;
+                const int q = quadrant_of(d.cand[k], A[n]);
+                atomicAdd(&((int*)&d.cnt4[n])[q], 1);
+            }
+            __syncthreads();
+            // prefix of (children - 1) in processing order; first j reaching N
+            int acc = 0;
+            int J = nv - 1;
+            if (threadIdx.x == 0) s_vars[1] = nv - 1;
+            __syncthreads();
+            for (int b0 = 0; b0 < nv; b0 += blockDim.x) {
+                const int j = b0 + threadIdx.x;
+                int g = 0;
+                if (j < nv) {
+                    const int4 q = d.cnt4[(int)(s_sort[j] & 0xFFFF)];
+                    g = (q.x > 0) + (q.y > 0) + (q.z > 0) + (q.w > 0) - 1;
+                }
+                int tot;
+                const int ex = block_exclusive_scan(g, s_scan, &tot);
+                if (j < nv && alive + acc + ex + g >= N) atomicMin(&s_vars[1], j);
+                acc += tot;
+            }
+            __syncthreads();
+            J = s_vars[1];
+            const int nsplit = J + 1;
+            for (int n = threadIdx.x; n < alive; n += blockDim.x) d.aux0[n] = -1;
+            __syncthreads();
+            for (int j = threadIdx.x; j < nsplit; j += blockDim.x) {
+                const int n = (int)(s_sort[j] & 0xFFFF);
+                d.aux0[n] = j;
+                d.aux1[j] = n;
+            }
+            __syncthreads();
+            int n_big = 0;
+            split_step(d, A, B, alive, K, nsplit, next_id, n_big, s_scan, s_vars);
+            if (s_vars[15]) break;
+            if (alive >= N || alive == prev) break;
+            if (guard == 63) atomicOr(status, 8);
+        }
+    }
+    if (s_vars[15]) {
+        if (threadIdx.x == 0) {
+            atomicOr(status, 32);
+            *d.kept_count = 0;
+        }
+        return;
+    }
+    // 5. per node the key with the largest response, first in key order
+    for (int n = threadIdx.x; n < alive; n += blockDim.x) d.best[n] = 0u;
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const uint32_t p = d.cand[k];
+        const uint32_t key = ((p >> 24) << 20) | (uint32_t)(0xFFFFF - k);
+        atomicMax(&d.best[d.node_of[k]], key);
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < alive; n += blockDim.x) {
+        const int k = 0xFFFFF - (int)(d.best[n] & 0xFFFFF);
+        d.kept[n] = d.cand[k];
+    }
+    if (threadIdx.x == 0) *d.kept_count = alive;
+}
+
+// ---------------------------------------------------------------- describe
+__device__ __forceinline__ float lookup_exception(const uint32_t* keys, const float* vals, int n, uint32_t xb,
+                                                  float v) {
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const uint32_t k = keys[mid];
+        if (k == xb) return vals[mid];
+        if (k < xb) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, orbgpu_keypoint* out_kps, uint8_t* out_desc,
+                                                  int* status) {
+    const LevelDesc& d = descs[blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && d.level == 0) {
+        int t = 0;
+        for (int l = 0; l < d.nlevels; l++) t += d.level_counts[l];
+        *d.frame_total = t;
+    }
+    const int cnt = *d.kept_count;
+    if (k >= cnt) return;
+    int off = 0;
+    for (int l = 0; l < d.level; l++) off += d.level_counts[l];
+    if (off + k >= d.out_cap) {
+        if (lane == 0) atomicOr(status, 16);
+        return;
+    }
+    const int o = d.out_base + off + k;
+    const uint32_t p = d.kept[k];
+    const int x = (int)(p & 0xFFF), y = (int)((p >> 12) & 0xFFF), score = (int)(p >> 24);
+    // keypoints lie at least EDGE_THRESHOLD pixels inside their level
+    if (x < ORBGPU_EDGE_THRESHOLD || y < ORBGPU_EDGE_THRESHOLD || x > d.w - ORBGPU_EDGE_THRESHOLD - 1 ||
+        y > d.h - ORBGPU_EDGE_THRESHOLD - 1) {
+        if (lane == 0) atomicOr(status, 64);
+        return;
+    }
+    // IC_Angle on the unblurred level (src/ORBextractor.cc:94-141)
+    int m10 = 0, m01 = 0;
+    if (lane < 2 * ORBGPU_HALF_PATCH + 1) {
+        const int v = lane - ORBGPU_HALF_PATCH;
+        const int dlim = c_umax[v < 0 ? -v : v];
+        const uint8_t* row = d.dst + (size_t)(y + v) * d.pitch + x;
+        int rs = 0;
+        for (int u = -dlim; u <= dlim; u++) {
+            const int val = row[u];
+            rs += val;
+            m10 += u * val;
+        }
+        m01 = v * rs;
+    }
+    m10 = warp_sum(m10);
+    m01 = warp_sum(m01);
+    const float angle = fast_atan2_deg((float)m01, (float)m10);
+    // computeOrbDescriptor on the blurred level (src/ORBextractor.cc:153-204)
+    const float factorPI = (float)(3.1415926535897932384626433832795 / 180.f);
+    const float ar = __fmul_rn(angle, factorPI);
+    double sd, cd;
+    sincos_taylor(ar, &sd, &cd);
+    float a = __double2float_rn(cd), b = __double2float_rn(sd);
+    const uint32_t xb = __float_as_uint(ar);
+    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_n, xb, a);
+    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_n, xb, b);
+    const uint8_t* center = d.blur + (size_t)y * d.pitch + x;
+    const int step = d.pitch;
+    int val = 0;
+#pragma unroll
+    for (int kk = 0; kk < 8; kk++) {
+        const signed char* pp = &c_pattern[(lane * 16 + 2 * kk) * 2];
+        int t[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            const float px = (float)pp[2 * e], py = (float)pp[2 * e + 1];
+            const int ry = cv_round(__fadd_rn(__fmul_rn(px, b), __fmul_rn(py, a)));
+            const int rx = cv_round(__fsub_rn(__fmul_rn(px, a), __fmul_rn(py, b)));
+            t[e] = center[ry * step + rx];
+        }
+        val |= (t[0] < t[1]) << kk;
+    }
+    out_desc[(size_t)o * 32 + lane] = (uint8_t)val;
+    if (lane == 0) {
+        orbgpu_keypoint kp;
+        const float s = d.scale;
+        kp.x = d.level == 0 ? (float)x : __fmul_rn((float)x, s);
+        kp.y = d.level == 0 ? (float)y : __fmul_rn((float)y, s);
+        kp.size = (float)(int)__fmul_rn((float)ORBGPU_PATCH_SIZE, s);
+        kp.angle = angle;
+        kp.response = (float)score;
+        kp.octave = d.level;
+        kp.class_id = -1;
+        out_kps[o] = kp;
+    }
+}
+
+// ---------------------------------------------------------------- host access
+void upload_constants(cudaStream_t st, const int* taps, const int* umax) {
+    cudaMemcpyToSymbolAsync(c_gauss_taps, taps, 7 * sizeof(int), 0, cudaMemcpyHostToDevice, st);
+    cudaMemcpyToSymbolAsync(c_umax, umax, (ORBGPU_HALF_PATCH + 1) * sizeof(int), 0, cudaMemcpyHostToDevice, st);
+    cudaMemcpyToSymbolAsync(c_pattern, kBriefPattern, sizeof(kBriefPattern), 0, cudaMemcpyHostToDevice, st);
+}
+
+void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn) {
+    cudaMemcpyToSymbol(g_cos_exc_key, &ck, sizeof(ck));
+    cudaMemcpyToSymbol(g_cos_exc_val, &cv, sizeof(cv));
+    cudaMemcpyToSymbol(g_cos_exc_n, &cn, sizeof(cn));
+    cudaMemcpyToSymbol(g_sin_exc_key, &sk, sizeof(sk));
+    cudaMemcpyToSymbol(g_sin_exc_val, &sv, sizeof(sv));
+    cudaMemcpyToSymbol(g_sin_exc_n, &sn, sizeof(sn));
+}
+
+void launch_resize_blur(const LevelDesc* descs, const WorkItem* items, int nitems, int level0, cudaStream_t st) {
+    if (nitems > 0) k_level_resize_blur<<<nitems, 256, 0, st>>>(descs, items, level0);
+}
+void launch_fast(const LevelDesc* descs, const WorkItem* items, int nitems, int* status, cudaStream_t st) {
+    if (nitems > 0) k_fast_cells<<<nitems, 128, 0, st>>>(descs, items, status);
+}
+void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {
+    const size_t smem = (size_t)sort_cap * sizeof(unsigned long long);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_distribute, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (ndescs > 0) k_distribute<<<ndescs, 512, smem, st>>>(descs, status);
+}
+void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
+                     cudaStream_t st) {
+    const int wpb = 8;
+    dim3 grid((max_kept + wpb - 1) / wpb, ndescs);
+    if (ndescs > 0 && max_kept > 0) k_describe<<<grid, 256, 0, st>>>(descs, kps, desc, status);
+}
+
+}  // namespace orbgpu
+
+namespace orbgpu {
+// The descriptor rotation exactly as k_describe evaluates it (Taylor value
+// corrected by the exception table), for the rotation tests.
+__global__ void k_sincos_probe(const float* x, int n, float* c, float* s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sd, cd;
+    sincos_taylor(x[i], &sd, &cd);
+    float a = __double2float_rn(cd), b = __double2float_rn(sd);
+    const uint32_t xb = __float_as_uint(x[i]);
+    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_n, xb, a);
+    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_n, xb, b);
+    c[i] = a;
+    s[i] = b;
+}
+}  // namespace orbgpu
+
+// Device arrays x (n floats) -> the descriptor rotation's cos and sin.
+extern "C" int orbgpu_descriptor_sincos(const float* x, int n, float* c, float* s) {
+    int rc = orbgpu::ensure_sincos_exceptions();
+    if (rc != ORBGPU_OK) return rc;
+    if (n <= 0) return ORBGPU_OK;
+    orbgpu::k_sincos_probe<<<(n + 255) / 256, 256>>>(x, n, c, s);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
+    return ORBGPU_OK;
+}

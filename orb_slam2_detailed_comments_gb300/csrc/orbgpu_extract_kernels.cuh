@@ -1,0 +1,93 @@
+// orbgpu_extract_kernels.cuh -- the ORB extraction stages as CUDA kernels.
+//
+// Each kernel walks a list of work items, so the same kernels serve one frame
+// (the drop-in path) and a ragged batch of frames of different sizes.
+//
+//   k_level_resize_blur  level l from level l-1 (cv::resize INTER_LINEAR,
+//                        8-bit fixed point) and the 7x7 sigma-2 blur of level l
+//                        (REFLECT_101), one 64x16 output tile per block, the
+//                        3-pixel blur halo recomputed in shared memory.
+//   k_fast_cells         one 30-px cell per block: FAST-9 arc strength for
+//                        every pixel of the cell's ROI interior, per-ROI
+//                        non-max suppression at iniThFAST, retried at
+//                        minThFAST when nothing survives, ordered compaction.
+//   k_distribute         one (frame, level) per block: DistributeOctTree as a
+//                        sequence of parallel split steps over node creation
+//                        numbers.
+//   k_describe           one warp per keypoint: IC_Angle, fastAtan2, rBRIEF.
+#pragma once
+
+#include "orbgpu_common.cuh"
+
+namespace orbgpu {
+
+// Per-(frame, level) description shared by all stages.
+struct LevelDesc {
+    // pyramid
+    const uint8_t* src;  // level l-1 (unused at level 0)
+    int sw, sh, spitch;
+    uint8_t* dst;  // level l (unblurred)
+    uint8_t* blur; // level l blurred (same pitch)
+    int w, h, pitch;
+    const int* xofs;      // resize tables of this level: source column per output column
+    const short* xalpha;  // 2 weights per output column
+    const int* yofs;      // source row per output row (unclamped)
+    const short* ybeta;   // 2 weights per output row
+    // FAST cells
+    int nCols, nRows, wCell, hCell;
+    int maxBorderX, maxBorderY;
+    int cell_cap;
+    uint32_t* slots;  // nCols*nRows*cell_cap packed (x | y << 12 | score << 24), level coordinates
+    int* cell_count;  // nCols*nRows
+    int ini_th, min_th;
+    // distribute
+    int nfeat;
+    int nIni;
+    int cand_cap;     // nCols*nRows*cell_cap
+    int node_cap;
+    uint32_t* cand;   // cand_cap
+    int* node_of;     // cand_cap
+    uint8_t* quad;    // cand_cap
+    void* nodes_a;    // node_cap DNode
+    void* nodes_b;    // node_cap DNode
+    int4* cnt4;       // node_cap
+    int4* childpos;   // node_cap
+    int* aux0;        // node_cap (split rank / order)
+    int* aux1;        // node_cap
+    int* aux2;        // node_cap
+    uint32_t* best;   // node_cap
+    uint32_t* kept;   // node_cap: distributed keypoints, packed like slots
+    int* kept_count;  // one int
+    // describe
+    int level;
+    int frame;
+    float scale;          // mvScaleFactor[level]
+    int* level_counts;    // the frame's kept_count of every level (nlevels ints)
+    int nlevels;
+    int out_base;         // first output row of the frame
+    int out_cap;          // output rows available to the frame
+    int* frame_total;     // the frame's keypoint count
+};
+
+struct DNode {
+    int16_t x0, x1, y0, y1;
+    int32_t cnt;
+    int32_t id;
+    int32_t flags;  // 1 = bNoMore, 2 = initial node
+};
+
+// One tile of k_level_resize_blur / one cell of k_fast_cells.
+struct WorkItem {
+    int desc;
+    int index;
+};
+
+void upload_constants(cudaStream_t st, const int* taps, const int* umax);
+void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn);
+void launch_resize_blur(const LevelDesc* descs, const WorkItem* items, int nitems, int level0, cudaStream_t st);
+void launch_fast(const LevelDesc* descs, const WorkItem* items, int nitems, int* status, cudaStream_t st);
+void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);
+void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
+                     cudaStream_t st);
+
+}  // namespace orbgpu

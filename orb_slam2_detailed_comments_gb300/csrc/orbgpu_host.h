@@ -1,0 +1,61 @@
+// orbgpu_host.h -- host-side structures shared by the extractor, the batch
+// pipeline and the matchers.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "orbgpu_extract_kernels.cuh"
+
+namespace orbgpu {
+
+// Scale tables, per-level budgets, the IC_Angle row bounds and the Gaussian
+// taps of one ORBextractor configuration (src/ORBextractor.cc:469-571).
+struct ExtractorTables {
+    int nlevels = 0;
+    std::vector<float> scale, inv_scale, sigma2, inv_sigma2;
+    std::vector<int> nfeat;
+    int umax[ORBGPU_HALF_PATCH + 1];
+    int taps[7];
+};
+
+// Geometry of one pyramid level of one image.
+struct LevelGeom {
+    int w, h, pitch;
+    int maxBorderX, maxBorderY;
+    int nCols, nRows, wCell, hCell, ncells;
+    int nIni;
+    int cell_cap, cand_cap, node_cap;
+    int nfeat;
+};
+
+struct LevelOffsets {
+    size_t pyr, blur, xofs, xalpha, yofs, ybeta, slots, cell_count, cand, node_of, quad, nodes_a, nodes_b, cnt4,
+        childpos, aux0, aux1, aux2, best, kept;
+};
+
+// Byte offsets of one frame's buffers inside a device arena.
+struct FrameLayout {
+    std::vector<LevelOffsets> lv;
+    size_t level_counts = 0, frame_total = 0;
+    size_t bytes = 0;
+    size_t plan(const std::vector<LevelGeom>& g, size_t base);
+};
+
+ExtractorTables make_tables(int nfeatures, float scale_factor, int nlevels);
+void resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int* yofs, short* ybeta);
+int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom>& g);
+void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const FrameLayout& lay, uint8_t* arena,
+                int frame, int ini_th, int min_th, int out_base, int out_cap, LevelDesc* out);
+void fill_tables(const std::vector<LevelGeom>& g, const FrameLayout& lay, std::vector<uint8_t>& host_img,
+                 size_t base);
+
+int ensure_sincos_exceptions();
+std::string default_sincos_table_path();
+// Builds the table of descriptor-angle inputs whose host cosf/sinf differ
+// from the rounded sincos_taylor value, and writes it to 'path'.
+int build_sincos_table(const char* path, int threads);
+
+}  // namespace orbgpu

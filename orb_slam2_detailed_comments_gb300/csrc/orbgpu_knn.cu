@@ -1,0 +1,111 @@
+// orbgpu_knn.cu -- brute-force k = 2 Hamming nearest neighbours.
+//
+// Popcount path: every thread owns one query (its 256 bits in registers) and
+// streams tiles of train rows through shared memory; the train set is split
+// into slices across blocks so the grid covers the GPU, and a merge kernel
+// combines the per-slice (best, second) pairs.  Ties go to the lower train
+// index, the rule of a sequential scan over DescriptorDistance
+// (src/ORBmatcher.cc:2083-2103).
+#include <algorithm>
+
+#include "orbgpu_host.h"
+
+cudaStream_t orbgpu_matcher_stream_internal(orbgpu_matcher* m);
+
+namespace orbgpu {
+
+#define KNN_QPB 128
+#define KNN_TILE 256
+
+__global__ void __launch_bounds__(KNN_QPB) k_knn_popc(const uint4* __restrict__ q, int nq, const uint4* __restrict__ t,
+                                                     int nt, int slice, int4* __restrict__ partial) {
+    __shared__ uint4 tile[KNN_TILE * 2];
+    const int qi = blockIdx.x * KNN_QPB + threadIdx.x;
+    const int t0 = blockIdx.y * slice, t1 = min(nt, t0 + slice);
+    uint4 a0 = make_uint4(0, 0, 0, 0), a1 = a0;
+    if (qi < nq) {
+        a0 = q[2 * (size_t)qi];
+        a1 = q[2 * (size_t)qi + 1];
+    }
+    int b1 = 0x7fffffff, b2 = 0x7fffffff, i1 = -1, i2 = -1;
+    for (int base = t0; base < t1; base += KNN_TILE) {
+        const int nb = min(KNN_TILE, t1 - base);
+        __syncthreads();
+        for (int k = threadIdx.x; k < 2 * nb; k += KNN_QPB) tile[k] = t[2 * (size_t)base + k];
+        __syncthreads();
+        for (int j = 0; j < nb; j++) {
+            const int d = hamming256(a0, a1, tile[2 * j], tile[2 * j + 1]);
+            if (d < b1) {
+                b2 = b1;
+                i2 = i1;
+                b1 = d;
+                i1 = base + j;
+            } else if (d < b2) {
+                b2 = d;
+                i2 = base + j;
+            }
+        }
+    }
+    if (qi < nq) partial[(size_t)blockIdx.y * nq + qi] = make_int4(i1, b1, i2, b2);
+}
+
+__global__ void k_knn_merge(const int4* __restrict__ partial, int nq, int nslices, int* idx1, int* d1, int* idx2,
+                            int* d2) {
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    // slices are in increasing train order, so strict comparisons keep the
+    // lower index on ties
+    int b1 = 0x7fffffff, b2 = 0x7fffffff, i1 = -1, i2 = -1;
+    for (int s = 0; s < nslices; s++) {
+        const int4 p = partial[(size_t)s * nq + qi];
+        if (p.x >= 0) {
+            if (p.y < b1) {
+                b2 = b1; i2 = i1; b1 = p.y; i1 = p.x;
+            } else if (p.y < b2) {
+                b2 = p.y; i2 = p.x;
+            }
+        }
+        if (p.z >= 0) {
+            if (p.w < b1) {
+                b2 = b1; i2 = i1; b1 = p.w; i1 = p.z;
+            } else if (p.w < b2) {
+                b2 = p.w; i2 = p.z;
+            }
+        }
+    }
+    idx1[qi] = i1;
+    d1[qi] = b1;
+    idx2[qi] = i2;
+    d2[qi] = b2;
+}
+
+}  // namespace orbgpu
+
+using namespace orbgpu;
+
+extern "C" int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1,
+                           int* d1, int* idx2, int* d2, int algo) {
+    if (!m || nq < 0 || nt < 0 || (nq > 0 && (!query || !idx1 || !d1 || !idx2 || !d2)) || (nt > 0 && !train) ||
+        algo != 0)
+        return ORBGPU_ERR_BAD_ARG;
+    if (nq == 0) return ORBGPU_OK;
+    cudaStream_t st = orbgpu_matcher_stream_internal(m);
+    int dev, nsm;
+    ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
+    ORBGPU_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int qblocks = (nq + KNN_QPB - 1) / KNN_QPB;
+    // enough slices for ~8 resident blocks per SM, each slice a whole number of tiles
+    int nslices = std::max(1, std::min((nt + KNN_TILE - 1) / KNN_TILE, (8 * nsm + qblocks - 1) / qblocks));
+    int slice = (nt + nslices - 1) / nslices;
+    slice = ((slice + KNN_TILE - 1) / KNN_TILE) * KNN_TILE;
+    nslices = std::max(1, (nt + slice - 1) / std::max(1, slice));
+    int4* partial = nullptr;
+    ORBGPU_CUDA_TRY(cudaMallocAsync((void**)&partial, sizeof(int4) * (size_t)nq * nslices, st));
+    dim3 grid(qblocks, nslices);
+    k_knn_popc<<<grid, KNN_QPB, 0, st>>>((const uint4*)query, nq, (const uint4*)train, nt, slice, partial);
+    k_knn_merge<<<(nq + 255) / 256, 256, 0, st>>>(partial, nq, nslices, idx1, d1, idx2, d2);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaFreeAsync(partial, st));
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    return ORBGPU_OK;
+}

@@ -1,0 +1,963 @@
+// orbgpu_match.cu -- the windowed descriptor searches and stereo matching.
+//
+// Distances and candidate windows are computed in parallel (one warp per
+// query); the parts of the reference that are sequential by construction --
+// a later query seeing the matches of earlier ones (vMatchedDistance in
+// SearchForInitialization, claimed keypoints in SearchByProjection) -- are
+// replayed in order by one warp over the precomputed candidate lists.
+//
+// Candidate order: Frame::GetFeaturesInArea (src/Frame.cc:590-670) visits
+// grid cells column by column and each cell in keypoint-index order, so a
+// candidate's position in that order is (cell x * 48 + cell y, index).  The
+// searches compare candidates lexicographically on (distance, position),
+// which reproduces the reference's "first strictly smaller wins" loops.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "orbgpu_host.h"
+
+namespace orbgpu {
+
+struct GridDev {
+    const orbgpu_keypoint* kps;
+    const uint8_t* desc;
+    const float* uright;
+    int n;
+    float minX, minY, invW, invH;
+    const int* cell_start;  // 64*48 + 1
+    const int* cell_keys;   // n
+    const int* key_cell;    // n, -1 if outside the grid
+    float scale[16];
+};
+
+// PosInGrid (src/Frame.cc:682-698).
+__device__ __forceinline__ int pos_in_grid(const orbgpu_keypoint& kp, float minX, float minY, float invW, float invH) {
+    const int px = (int)roundf(__fmul_rn(__fsub_rn(kp.x, minX), invW));
+    const int py = (int)roundf(__fmul_rn(__fsub_rn(kp.y, minY), invH));
+    if (px < 0 || px >= ORBGPU_GRID_COLS || py < 0 || py >= ORBGPU_GRID_ROWS) return -1;
+    return px * ORBGPU_GRID_ROWS + py;
+}
+
+__global__ void k_grid_count(const orbgpu_keypoint* kps, int n, float minX, float minY, float invW, float invH,
+                             int* key_cell, int* cell_count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = pos_in_grid(kps[i], minX, minY, invW, invH);
+    key_cell[i] = c;
+    if (c >= 0) atomicAdd(&cell_count[c], 1);
+}
+
+__global__ void k_grid_scan(const int* cell_count, int* cell_start, int* cursor) {
+    __shared__ int s_scan[32];
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    int base = 0;
+    for (int b0 = 0; b0 < ncell; b0 += blockDim.x) {
+        const int c = b0 + threadIdx.x;
+        const int v = c < ncell ? cell_count[c] : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (c < ncell) {
+            cell_start[c] = base + ex;
+            cursor[c] = base + ex;
+        }
+        base += tot;
+    }
+    if (threadIdx.x == 0) cell_start[ncell] = base;
+}
+
+__global__ void k_grid_fill(const int* key_cell, int n, int* cursor, int* cell_keys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = key_cell[i];
+    if (c >= 0) cell_keys[atomicAdd(&cursor[c], 1)] = i;
+}
+
+// Frame::GetFeaturesInArea cell range; false when the window misses the grid.
+__device__ __forceinline__ bool area_cells(const GridDev& g, float x, float y, float r, int& x0, int& x1, int& y0,
+                                           int& y1) {
+    x0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(x, g.minX), r), g.invW)));
+    if (x0 >= ORBGPU_GRID_COLS) return false;
+    x1 = min(ORBGPU_GRID_COLS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(x, g.minX), r), g.invW)));
+    if (x1 < 0) return false;
+    y0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(y, g.minY), r), g.invH)));
+    if (y0 >= ORBGPU_GRID_ROWS) return false;
+    y1 = min(ORBGPU_GRID_ROWS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(y, g.minY), r), g.invH)));
+    if (y1 < 0) return false;
+    return true;
+}
+
+__device__ __forceinline__ bool in_area(const GridDev& g, int idx, float x, float y, float r, int minLevel,
+                                        int maxLevel) {
+    const orbgpu_keypoint kp = g.kps[idx];
+    const bool check = (minLevel > 0) || (maxLevel >= 0);
+    if (check) {
+        if (kp.octave < minLevel) return false;
+        if (maxLevel >= 0 && kp.octave > maxLevel) return false;
+    }
+    const float dx = __fsub_rn(kp.x, x), dy = __fsub_rn(kp.y, y);
+    return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < __fmul_rn(r, r);
+}
+
+// Candidate record: distance, GetFeaturesInArea position, keypoint index, octave.
+struct Cand {
+    int dist;
+    int idx;
+    uint32_t order;  // cell << 16 | rank-free tie key: index
+    int octave;
+};
+
+__device__ __forceinline__ uint64_t cand_key(int dist, int cell, int idx) {
+    return ((uint64_t)(uint32_t)dist << 40) | ((uint64_t)(uint32_t)cell << 20) | (uint64_t)(uint32_t)idx;
+}
+
+// ----------------------------------------------------------------- SearchForInitialization
+// Pass 1: count (fill == 0) or write (fill == 1) the candidates of every
+// level-0 keypoint of F1 in the window around prev[i1] (src/ORBmatcher.cc:603-640).
+__global__ void k_init_candidates(GridDev g2, const orbgpu_keypoint* kps1, const uint8_t* desc1, int n1,
+                                  const float* prev, float window, const int* cand_start, int* cand_count,
+                                  uint64_t* cand_out, int fill) {
+    const int lane = threadIdx.x & 31;
+    const int i1 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i1 >= n1) return;
+    const orbgpu_keypoint kp1 = kps1[i1];
+    int total = 0;
+    int x0, x1, y0, y1;
+    if (kp1.octave <= 0 && area_cells(g2, prev[2 * i1], prev[2 * i1 + 1], window, x0, x1, y0, y1)) {
+        const uint8_t* d1 = desc1 + (size_t)i1 * 32;
+        for (int ix = x0; ix <= x1; ix++)
+            for (int iy = y0; iy <= y1; iy++) {
+                const int c = ix * ORBGPU_GRID_ROWS + iy;
+                const int s = g2.cell_start[c], e = g2.cell_start[c + 1];
+                for (int b = s; b < e; b += 32) {
+                    const int j = b + lane;
+                    bool ok = false;
+                    int idx = -1;
+                    if (j < e) {
+                        idx = g2.cell_keys[j];
+                        ok = in_area(g2, idx, prev[2 * i1], prev[2 * i1 + 1], window, kp1.octave, kp1.octave);
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, ok);
+                    if (fill && ok) {
+                        const int pos = cand_start[i1] + total + __popc(m & ((1u << lane) - 1));
+                        const int dist = hamming256_ptr(d1, g2.desc + (size_t)idx * 32);
+                        cand_out[pos] = cand_key(dist, c, idx);
+                    }
+                    total += __popc(m);
+                }
+            }
+    }
+    if (!fill && lane == 0) cand_count[i1] = total;
+}
+
+__global__ void k_exclusive_scan(const int* in, int n, int* out, int* total) {
+    __shared__ int s_scan[32];
+    int base = 0;
+    for (int b0 = 0; b0 < n; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const int v = i < n ? in[i] : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (i < n) out[i] = base + ex;
+        base += tot;
+    }
+    if (threadIdx.x == 0) *total = base;
+}
+
+// Pass 2: the in-order resolution of src/ORBmatcher.cc:600-677 by one warp.
+__global__ void k_init_resolve(const orbgpu_keypoint* kps1, int n1, const orbgpu_keypoint* kps2, int n2,
+                               const int* cand_start, const int* cand_count, const uint64_t* cands, float nnratio,
+                               int check_ori, int* matched_dist, int* matches21, int* matches12, int* bin_of,
+                               int* nmatches_out) {
+    const int lane = threadIdx.x;
+    __shared__ int hist[ORBGPU_HISTO_LENGTH];
+    if (lane < ORBGPU_HISTO_LENGTH) hist[lane] = 0;
+    for (int i = lane; i < n2; i += 32) {
+        matched_dist[i] = 0x7fffffff;
+        matches21[i] = -1;
+    }
+    for (int i = lane; i < n1; i += 32) {
+        matches12[i] = -1;
+        bin_of[i] = -1;
+    }
+    __syncwarp();
+    int nmatches = 0;
+    const float factor = __fdiv_rn((float)ORBGPU_HISTO_LENGTH, 360.0f);
+    for (int i1 = 0; i1 < n1; i1++) {
+        const int s = cand_start[i1], cnt = cand_count[i1];
+        if (cnt == 0) continue;
+        // best: lexicographic (dist, position); second: smallest dist of the others
+        uint64_t best = ~0ull;
+        int second = 0x7fffffff;
+        for (int b = 0; b < cnt; b += 32) {
+            uint64_t key = ~0ull;
+            if (b + lane < cnt) {
+                key = cands[s + b + lane];
+                const int dist = (int)(key >> 40);
+                const int i2 = (int)(key & 0xFFFFF);
+                if (matched_dist[i2] <= dist) key = ~0ull;
+            }
+            // merge (best, second) with this lane's key
+            if (key < best) {
+                if (best != ~0ull) second = min(second, (int)(best >> 40));
+                best = key;
+            } else if (key != ~0ull) {
+                second = min(second, (int)(key >> 40));
+            }
+        }
+        // warp merge of (best, second)
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int os = __shfl_xor_sync(0xffffffffu, second, o);
+            if (ob < best) {
+                second = min(os, best == ~0ull ? 0x7fffffff : (int)(best >> 40));
+                best = ob;
+            } else {
+                second = min(second, min(os, ob == ~0ull ? 0x7fffffff : (int)(ob >> 40)));
+            }
+        }
+        if (best == ~0ull) continue;
+        const int bestDist = (int)(best >> 40);
+        const int bestIdx2 = (int)(best & 0xFFFFF);
+        if (bestDist <= ORBGPU_TH_LOW && (float)bestDist < __fmul_rn((float)second, nnratio)) {
+            if (lane == 0) {
+                const int prev = matches21[bestIdx2];
+                if (prev >= 0) {
+                    matches12[prev] = -1;
+                    nmatches--;
+                }
+                matches12[i1] = bestIdx2;
+                matches21[bestIdx2] = i1;
+                matched_dist[bestIdx2] = bestDist;
+                nmatches++;
+                if (check_ori) {
+                    float rot = __fsub_rn(kps1[i1].angle, kps2[bestIdx2].angle);
+                    if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
+                    int bin = (int)roundf(__fmul_rn(rot, factor));
+                    if (bin == ORBGPU_HISTO_LENGTH) bin = 0;
+                    bin_of[i1] = bin;
+                    hist[bin]++;
+                }
+            }
+            nmatches = __shfl_sync(0xffffffffu, nmatches, 0);
+        }
+        __syncwarp();
+    }
+    if (check_ori) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        int max1 = 0, max2 = 0, max3 = 0;
+        for (int i = 0; i < ORBGPU_HISTO_LENGTH; i++) {  // ComputeThreeMaxima, src/ORBmatcher.cc:2035-2077
+            const int sz = hist[i];
+            if (sz > max1) {
+                max3 = max2; max2 = max1; max1 = sz;
+                ind3 = ind2; ind2 = ind1; ind1 = i;
+            } else if (sz > max2) {
+                max3 = max2; max2 = sz;
+                ind3 = ind2; ind2 = i;
+            } else if (sz > max3) {
+                max3 = sz;
+                ind3 = i;
+            }
+        }
+        if ((float)max2 < __fmul_rn(0.1f, (float)max1)) {
+            ind2 = -1;
+            ind3 = -1;
+        } else if ((float)max3 < __fmul_rn(0.1f, (float)max1)) {
+            ind3 = -1;
+        }
+        int removed = 0;
+        for (int i1 = lane; i1 < n1; i1 += 32) {
+            const int b = bin_of[i1];
+            if (b < 0 || b == ind1 || b == ind2 || b == ind3) continue;
+            if (matches12[i1] >= 0) {
+                matches12[i1] = -1;
+                removed++;
+            }
+        }
+        nmatches -= warp_sum(removed);
+    }
+    if (lane == 0) *nmatches_out = nmatches;
+}
+
+// ----------------------------------------------------------------- SearchByProjection(Frame, MapPoints)
+// Pass 1 (warp per map point): candidates in the scaled window over levels
+// [L-1, L] that pass the stereo gate, with their distances (src/ORBmatcher.cc:84-145).
+__global__ void k_proj_candidates(GridDev g, const orbgpu_mappoint* mps, const uint8_t* mp_desc, int m, float th,
+                                  const int* cand_start, int* cand_count, uint64_t* cand_out, int fill) {
+    const int lane = threadIdx.x & 31;
+    const int imp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (imp >= m) return;
+    const orbgpu_mappoint mp = mps[imp];
+    int total = 0;
+    if (mp.track_in_view && !mp.bad && mp.track_scale_level >= 0 && mp.track_scale_level < 16) {
+        const int level = mp.track_scale_level;
+        float r = mp.view_cos > 0.998f ? 2.5f : 4.0f;  // RadiusByViewingCos, src/ORBmatcher.cc:186-193
+        if (th != 1.0f) r = __fmul_rn(r, th);
+        const float radius = __fmul_rn(r, g.scale[level]);
+        int x0, x1, y0, y1;
+        if (area_cells(g, mp.proj_x, mp.proj_y, radius, x0, x1, y0, y1)) {
+            const uint8_t* dmp = mp_desc + (size_t)imp * 32;
+            for (int ix = x0; ix <= x1; ix++)
+                for (int iy = y0; iy <= y1; iy++) {
+                    const int c = ix * ORBGPU_GRID_ROWS + iy;
+                    const int s = g.cell_start[c], e = g.cell_start[c + 1];
+                    for (int b = s; b < e; b += 32) {
+                        const int j = b + lane;
+                        bool ok = false;
+                        int idx = -1;
+                        if (j < e) {
+                            idx = g.cell_keys[j];
+                            ok = in_area(g, idx, mp.proj_x, mp.proj_y, radius, level - 1, level);
+                            if (ok && g.uright && g.uright[idx] > 0) {
+                                const float er = fabsf(__fsub_rn(mp.proj_xr, g.uright[idx]));
+                                if (er > radius) ok = false;
+                            }
+                        }
+                        const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                        if (fill && ok) {
+                            const int pos = cand_start[imp] + total + __popc(msk & ((1u << lane) - 1));
+                            const int dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
+                            cand_out[pos] = cand_key(dist, c, idx);
+                        }
+                        total += __popc(msk);
+                    }
+                }
+        }
+    }
+    if (!fill && lane == 0) cand_count[imp] = total;
+}
+
+// Pass 2: in-order resolution (src/ORBmatcher.cc:117-180) by one warp.
+// claimed[] starts with the caller's pre-claimed keypoints.
+__global__ void k_proj_resolve(GridDev g, int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
+                               float nnratio, int* match_out, int* nmatches_out) {
+    const int lane = threadIdx.x;
+    int nmatches = 0;
+    for (int imp = 0; imp < m; imp++) {
+        const int s = cand_start[imp], cnt = cand_count[imp];
+        if (cnt == 0) continue;
+        uint64_t best = ~0ull, second = ~0ull;
+        for (int b = 0; b < cnt; b += 32) {
+            uint64_t key = ~0ull;
+            if (b + lane < cnt) {
+                key = cands[s + b + lane];
+                const int idx = (int)(key & 0xFFFFF);
+                if (match_out[idx] != -1 || (int)(key >> 40) >= 256) key = ~0ull;
+            }
+            if (key < best) {
+                second = best;
+                best = key;
+            } else if (key < second) {
+                second = key;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
+            if (ob < best) {
+                second = min(best, os);
+                best = ob;
+            } else {
+                second = min(second, ob);
+            }
+        }
+        if (best == ~0ull) continue;
+        const int bestDist = (int)(best >> 40);
+        const int bestIdx = (int)(best & 0xFFFFF);
+        const int bestLevel = g.kps[bestIdx].octave;
+        const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
+        const int bestLevel2 = second == ~0ull ? -1 : g.kps[(int)(second & 0xFFFFF)].octave;
+        if (bestDist <= ORBGPU_TH_HIGH) {
+            if (bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)) continue;
+            if (lane == 0) match_out[bestIdx] = imp;
+            nmatches++;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) *nmatches_out = nmatches;
+}
+
+__global__ void k_init_match_out(const uint8_t* claimed, int n, int* match_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) match_out[i] = (claimed && claimed[i]) ? -2 : -1;
+}
+
+// ----------------------------------------------------------------- stereo
+struct StereoLevels {
+    const uint8_t* left[16];
+    const uint8_t* right[16];
+    int w[16], h[16], pitch[16];
+    float scale[16], inv_scale[16];
+    int nlevels;
+};
+
+__global__ void k_stereo_rows_count(const orbgpu_keypoint* kpsR, int nR, StereoLevels lv, int nRows, int* row_count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nR) return;
+    const orbgpu_keypoint kp = kpsR[i];
+    if (kp.octave < 0 || kp.octave >= lv.nlevels) return;
+    const float r = __fmul_rn(2.0f, lv.scale[kp.octave]);
+    const int maxr = (int)ceilf(__fadd_rn(kp.y, r)), minr = (int)floorf(__fsub_rn(kp.y, r));
+    for (int yi = max(minr, 0); yi <= min(maxr, nRows - 1); yi++) atomicAdd(&row_count[yi], 1);
+}
+
+__global__ void k_stereo_rows_fill(const orbgpu_keypoint* kpsR, int nR, StereoLevels lv, int nRows, int* cursor,
+                                   int* row_keys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nR) return;
+    const orbgpu_keypoint kp = kpsR[i];
+    if (kp.octave < 0 || kp.octave >= lv.nlevels) return;
+    const float r = __fmul_rn(2.0f, lv.scale[kp.octave]);
+    const int maxr = (int)ceilf(__fadd_rn(kp.y, r)), minr = (int)floorf(__fsub_rn(kp.y, r));
+    for (int yi = max(minr, 0); yi <= min(maxr, nRows - 1); yi++) row_keys[atomicAdd(&cursor[yi], 1)] = i;
+}
+
+// Frame::ComputeStereoMatches per left keypoint (src/Frame.cc:884-1064), one warp each.
+__global__ void k_stereo_match(const orbgpu_keypoint* kpsL, const uint8_t* descL, int nL, const orbgpu_keypoint* kpsR,
+                               const uint8_t* descR, StereoLevels lv, int nRows, const int* row_start,
+                               const int* row_keys, float bf, float fx, float* uright, float* depth, int* sad_out,
+                               int* status) {
+    const int lane = threadIdx.x & 31;
+    const int iL = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (iL >= nL) return;
+    if (lane == 0) {
+        uright[iL] = -1.0f;
+        depth[iL] = -1.0f;
+        sad_out[iL] = -1;
+    }
+    const orbgpu_keypoint kpL = kpsL[iL];
+    const int levelL = kpL.octave;
+    if (levelL < 0 || levelL >= lv.nlevels) return;
+    const float vL = kpL.y, uL = kpL.x;
+    const int row = (int)vL;
+    if (row < 0 || row >= nRows) return;
+    const int rs = row_start[row], re = row_start[row + 1];
+    if (rs == re) return;
+    const float mb = __fdiv_rn(bf, fx);
+    const float minZ = mb, minD = 0.f, maxD = __fdiv_rn(bf, minZ);
+    const float minU = __fsub_rn(uL, maxD), maxU = __fsub_rn(uL, minD);
+    if (maxU < 0) return;
+    // best over the row band: lexicographic (distance, right index), distance < TH_HIGH
+    uint64_t best = ~0ull;
+    const uint8_t* dL = descL + (size_t)iL * 32;
+    for (int b = rs; b < re; b += 32) {
+        const int j = b + lane;
+        if (j < re) {
+            const int iR = row_keys[j];
+            const orbgpu_keypoint kpR = kpsR[iR];
+            if (kpR.octave >= levelL - 1 && kpR.octave <= levelL + 1 && kpR.x >= minU && kpR.x <= maxU) {
+                const int dist = hamming256_ptr(dL, descR + (size_t)iR * 32);
+                if (dist < ORBGPU_TH_HIGH) {
+                    const uint64_t key = ((uint64_t)dist << 32) | (uint32_t)iR;
+                    best = key < best ? key : best;
+                }
+            }
+        }
+    }
+    best = warp_min_u64(best);
+    if (best == ~0ull) return;
+    const int bestDist = (int)(best >> 32);
+    const int thOrbDist = (ORBGPU_TH_HIGH + ORBGPU_TH_LOW) / 2;
+    if (bestDist >= thOrbDist) return;
+    const int bestIdxR = (int)(best & 0xFFFFFFFFu);
+    // SAD refinement on the unblurred level (src/Frame.cc:951-1020)
+    const float uR0 = kpsR[bestIdxR].x;
+    const float sf = lv.inv_scale[levelL];
+    const float scaleduL = roundf(__fmul_rn(kpL.x, sf));
+    const float scaledvL = roundf(__fmul_rn(kpL.y, sf));
+    const float scaleduR0 = roundf(__fmul_rn(uR0, sf));
+    const int W = 5, L = 5;
+    const int lw = lv.w[levelL], lh = lv.h[levelL], lp = lv.pitch[levelL];
+    const float iniu = __fsub_rn(__fsub_rn(scaleduR0, (float)L), (float)W);
+    const float endu = __fadd_rn(__fadd_rn(__fadd_rn(scaleduR0, (float)L), (float)W), 1.0f);
+    if (iniu < 0 || endu >= (float)lw) return;
+    const int ly0 = (int)(scaledvL - W), lx0 = (int)(scaleduL - W);
+    if (ly0 < 0 || ly0 + 2 * W + 1 > lh || lx0 < 0 || lx0 + 2 * W + 1 > lw) {
+        if (lane == 0) atomicOr(status, 1);
+        return;
+    }
+    const uint8_t* left = lv.left[levelL];
+    const uint8_t* right = lv.right[levelL];
+    int sad = 0x7fffffff;
+    if (lane < 2 * L + 1) {
+        const int incR = lane - L;
+        const int rx0 = (int)(scaleduR0 + incR - W);
+        const int cl = left[(size_t)(ly0 + W) * lp + lx0 + W];
+        const int cr = right[(size_t)(ly0 + W) * lp + rx0 + W];
+        int s = 0;
+        for (int yy = 0; yy < 2 * W + 1; yy++) {
+            const uint8_t* lr = left + (size_t)(ly0 + yy) * lp + lx0;
+            const uint8_t* rr = right + (size_t)(ly0 + yy) * lp + rx0;
+#pragma unroll
+            for (int xx = 0; xx < 2 * W + 1; xx++) s += abs((lr[xx] - cl) - (rr[xx] - cr));
+        }
+        sad = s;
+    }
+    // first minimum over incR = -L..L (ascending lanes)
+    int bestSad = 0x7fffffff, bestinc = 0;
+    float dists[2 * 5 + 1];
+#pragma unroll
+    for (int t = 0; t < 2 * L + 1; t++) {
+        const int v = __shfl_sync(0xffffffffu, sad, t);
+        dists[t] = (float)v;
+        if ((float)v < (float)bestSad) {
+            bestSad = v;
+            bestinc = t - L;
+        }
+    }
+    if (lane != 0) return;
+    if (bestinc == -L || bestinc == L) return;
+    const float d1 = dists[L + bestinc - 1], d2 = dists[L + bestinc], d3 = dists[L + bestinc + 1];
+    const float deltaR = __fdiv_rn(__fsub_rn(d1, d3), __fmul_rn(2.0f, __fsub_rn(__fadd_rn(d1, d3), __fmul_rn(2.0f, d2))));
+    if (deltaR < -1 || deltaR > 1) return;
+    float bestuR = __fmul_rn(lv.scale[levelL], __fadd_rn(__fadd_rn(scaleduR0, (float)bestinc), deltaR));
+    float disparity = __fsub_rn(uL, bestuR);
+    if (disparity >= minD && disparity < maxD) {
+        if (disparity <= 0) {
+            disparity = 0.01f;
+            bestuR = (float)((double)uL - 0.01);
+        }
+        depth[iL] = __fdiv_rn(bf, disparity);
+        uright[iL] = bestuR;
+        sad_out[iL] = bestSad;
+    }
+}
+
+// Median cut (src/Frame.cc:1069-1081): one block; sorts the SAD values of the
+// accepted matches and discards those at or above 1.5*1.4*median.
+__global__ void k_stereo_median(int nL, const int* sad, float* uright, float* depth, int* sort_buf, int cap,
+                                int* n_valid) {
+    __shared__ int s_scan[32];
+    int cnt = 0;
+    for (int b0 = 0; b0 < nL; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const int v = (i < nL && sad[i] >= 0) ? 1 : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (v && cnt + ex < cap) sort_buf[cnt + ex] = sad[i];
+        cnt += tot;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *n_valid = cnt;
+    if (cnt == 0 || cnt > cap) return;
+    int np2 = 1;
+    while (np2 < cnt) np2 <<= 1;
+    for (int i = cnt + threadIdx.x; i < np2; i += blockDim.x) sort_buf[i] = 0x7fffffff;
+    __syncthreads();
+    for (int size = 2; size <= np2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < np2 / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool asc = ((lo & size) == 0);
+                const int a = sort_buf[lo], b = sort_buf[hi];
+                if ((a > b) == asc) {
+                    sort_buf[lo] = b;
+                    sort_buf[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    const float median = (float)sort_buf[cnt / 2];
+    const float thDist = __fmul_rn(1.5f * 1.4f, median);
+    for (int i = threadIdx.x; i < nL; i += blockDim.x)
+        if (sad[i] >= 0 && !((float)sad[i] < thDist)) {
+            uright[i] = -1.0f;
+            depth[i] = -1.0f;
+        }
+}
+
+// ----------------------------------------------------------------- distance batch
+__global__ void k_descriptor_distance(const uint8_t* a, const uint8_t* b, int n, int* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = hamming256_ptr(a + (size_t)i * 32, b + (size_t)i * 32);
+}
+
+}  // namespace orbgpu
+
+using namespace orbgpu;
+
+// ----------------------------------------------------------------- host side
+struct orbgpu_matcher {
+    float nnratio;
+    int check_ori;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // scratch (grown on demand)
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int* h_pinned = nullptr;
+};
+
+namespace {
+
+struct Staged {
+    const orbgpu_keypoint* kps = nullptr;
+    const uint8_t* desc = nullptr;
+    const float* uright = nullptr;
+};
+
+struct Bump {
+    uint8_t* base;
+    size_t off = 0, cap;
+    template <typename T> T* take(size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = (T*)(base + off);
+        off += n * sizeof(T);
+        return p;
+    }
+};
+
+int ensure_scratch(orbgpu_matcher* m, size_t bytes) {
+    if (bytes <= m->scratch_bytes) return ORBGPU_OK;
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+    if (m->scratch) cudaFree(m->scratch);
+    m->scratch = nullptr;
+    m->scratch_bytes = 0;
+    ORBGPU_CUDA_TRY(cudaMalloc(&m->scratch, bytes));
+    m->scratch_bytes = bytes;
+    return ORBGPU_OK;
+}
+
+// Device copies of a frame's arrays (or the caller's device pointers).
+int stage_frame(orbgpu_matcher* m, const orbgpu_frame* f, Bump& b, Staged& s) {
+    if (f->mem == ORBGPU_MEM_DEVICE) {
+        s.kps = f->keypoints;
+        s.desc = f->descriptors;
+        s.uright = f->uright;
+        return ORBGPU_OK;
+    }
+    orbgpu_keypoint* k = b.take<orbgpu_keypoint>(std::max(1, f->n));
+    uint8_t* d = b.take<uint8_t>((size_t)std::max(1, f->n) * 32);
+    if (f->n > 0) {
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(k, f->keypoints, sizeof(orbgpu_keypoint) * f->n, cudaMemcpyHostToDevice, m->stream));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(d, f->descriptors, 32 * (size_t)f->n, cudaMemcpyHostToDevice, m->stream));
+    }
+    s.kps = k;
+    s.desc = d;
+    s.uright = nullptr;
+    if (f->uright) {
+        float* u = b.take<float>(std::max(1, f->n));
+        if (f->n > 0) ORBGPU_CUDA_TRY(cudaMemcpyAsync(u, f->uright, sizeof(float) * f->n, cudaMemcpyHostToDevice, m->stream));
+        s.uright = u;
+    }
+    return ORBGPU_OK;
+}
+
+size_t frame_stage_bytes(const orbgpu_frame* f) {
+    if (f->mem == ORBGPU_MEM_DEVICE) return 0;
+    return (size_t)std::max(1, f->n) * (sizeof(orbgpu_keypoint) + 32 + 4) + 1024;
+}
+
+size_t grid_bytes(int n) { return (size_t)(3 * 3072 + 8 + 2 * std::max(1, n)) * sizeof(int) + 2048; }
+
+// AssignFeaturesToGrid (src/Frame.cc:399-423) on the device.
+int build_grid(orbgpu_matcher* m, const orbgpu_frame* f, const Staged& s, Bump& b, GridDev& g) {
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    int* cell_count = b.take<int>(ncell);
+    int* cell_start = b.take<int>(ncell + 1);
+    int* cursor = b.take<int>(ncell);
+    int* key_cell = b.take<int>(std::max(1, f->n));
+    int* cell_keys = b.take<int>(std::max(1, f->n));
+    g.kps = s.kps;
+    g.desc = s.desc;
+    g.uright = s.uright;
+    g.n = f->n;
+    g.minX = 0.0f;
+    g.minY = 0.0f;
+    g.invW = static_cast<float>(ORBGPU_GRID_COLS) / static_cast<float>((float)f->width - 0.0f);
+    g.invH = static_cast<float>(ORBGPU_GRID_ROWS) / static_cast<float>((float)f->height - 0.0f);
+    g.cell_start = cell_start;
+    g.cell_keys = cell_keys;
+    g.key_cell = key_cell;
+    for (int l = 0; l < 16; l++) g.scale[l] = l < f->nlevels ? f->scale_factors[l] : 1.0f;
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(cell_count, 0, sizeof(int) * ncell, m->stream));
+    if (f->n > 0) k_grid_count<<<(f->n + 255) / 256, 256, 0, m->stream>>>(s.kps, f->n, g.minX, g.minY, g.invW, g.invH, key_cell, cell_count);
+    k_grid_scan<<<1, 1024, 0, m->stream>>>(cell_count, cell_start, cursor);
+    if (f->n > 0) k_grid_fill<<<(f->n + 255) / 256, 256, 0, m->stream>>>(key_cell, f->n, cursor, cell_keys);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    return ORBGPU_OK;
+}
+
+bool frame_ok(const orbgpu_frame* f) {
+    return f && f->n >= 0 && f->n < (1 << 20) && f->width > 0 && f->height > 0 && f->nlevels >= 1 &&
+           f->nlevels <= 16 && (f->n == 0 || (f->keypoints && f->descriptors));
+}
+
+}  // namespace
+
+extern "C" int orbgpu_matcher_create(float nnratio, int check_orientation, void* stream, orbgpu_matcher** out) {
+    if (!out) return ORBGPU_ERR_BAD_ARG;
+    int dev;
+    ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
+    orbgpu_matcher* m = new orbgpu_matcher();
+    m->nnratio = nnratio;
+    m->check_ori = check_orientation;
+    if (stream) m->stream = (cudaStream_t)stream;
+    else {
+        if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete m;
+            return ORBGPU_ERR_CUDA;
+        }
+        m->own_stream = true;
+    }
+    if (cudaMallocHost(&m->h_pinned, 64) != cudaSuccess) {
+        orbgpu_matcher_destroy(m);
+        return ORBGPU_ERR_OOM;
+    }
+    *out = m;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_matcher_destroy(orbgpu_matcher* m) {
+    if (!m) return ORBGPU_OK;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    cudaFree(m->scratch);
+    cudaFreeHost(m->h_pinned);
+    if (m->own_stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return ORBGPU_OK;
+}
+
+// Runs the two-pass candidate listing: count, scan, fill.  Returns the
+// device candidate arrays in (start, count, keys).
+template <typename Launch>
+static int candidate_lists(orbgpu_matcher* m, int nq, Bump& b, Launch launch, int*& start, int*& count,
+                           uint64_t*& keys, int& total) {
+    count = b.take<int>(std::max(1, nq));
+    start = b.take<int>(std::max(1, nq));
+    int* d_total = b.take<int>(1);
+    launch((const int*)nullptr, count, (uint64_t*)nullptr, 0);
+    k_exclusive_scan<<<1, 1024, 0, m->stream>>>(count, nq, start, d_total);
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, d_total, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+    total = m->h_pinned[0];
+    const size_t need = b.off + 256 + sizeof(uint64_t) * (size_t)std::max(1, total);
+    if (need > b.cap) return ORBGPU_ERR_CAPACITY;
+    keys = b.take<uint64_t>(std::max(1, total));
+    launch((const int*)start, count, keys, 1);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_search_for_initialization(orbgpu_matcher* m, const orbgpu_frame* f1, const orbgpu_frame* f2,
+                                                float* prev_matched, int* matches12, int window_size, int* nmatches) {
+    if (!m || !frame_ok(f1) || !frame_ok(f2) || !prev_matched || !matches12 || !nmatches) return ORBGPU_ERR_BAD_ARG;
+    const int n1 = f1->n, n2 = f2->n;
+    *nmatches = 0;
+    for (int i = 0; i < n1; i++) matches12[i] = -1;
+    if (n1 == 0) return ORBGPU_OK;
+    // generous scratch: every F1 key may see every F2 key
+    size_t est = frame_stage_bytes(f1) + frame_stage_bytes(f2) + grid_bytes(n2) +
+                 (size_t)n1 * 2 * 3 * sizeof(int) + (size_t)n2 * 2 * sizeof(int) + 64 * 1024 +
+                 sizeof(uint64_t) * (size_t)n1 * std::max(1, std::min(n2, 4096));
+    for (int attempt = 0; attempt < 2; attempt++) {
+        int rc = ensure_scratch(m, est);
+        if (rc) return rc;
+        Bump b{(uint8_t*)m->scratch, 0, m->scratch_bytes};
+        Staged s1, s2;
+        if ((rc = stage_frame(m, f1, b, s1)) || (rc = stage_frame(m, f2, b, s2))) return rc;
+        GridDev g2;
+        if ((rc = build_grid(m, f2, s2, b, g2))) return rc;
+        float* d_prev = b.take<float>(2 * n1);
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_prev, prev_matched, sizeof(float) * 2 * n1, cudaMemcpyHostToDevice, m->stream));
+        int *start, *count, total;
+        uint64_t* keys;
+        const float window = (float)window_size;
+        auto launch = [&](const int* st, int* cnt, uint64_t* out, int fill) {
+            const int wpb = 8;
+            k_init_candidates<<<(n1 + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g2, s1.kps, s1.desc, n1, d_prev, window,
+                                                                             st, cnt, out, fill);
+        };
+        rc = candidate_lists(m, n1, b, launch, start, count, keys, total);
+        if (rc == ORBGPU_ERR_CAPACITY) {
+            est = est + sizeof(uint64_t) * (size_t)total * 2;
+            continue;
+        }
+        if (rc) return rc;
+        int* matched_dist = b.take<int>(std::max(1, n2));
+        int* m21 = b.take<int>(std::max(1, n2));
+        int* m12 = b.take<int>(n1);
+        int* bin_of = b.take<int>(n1);
+        int* d_nm = b.take<int>(1);
+        k_init_resolve<<<1, 32, 0, m->stream>>>(s1.kps, n1, s2.kps, n2, start, count, keys, m->nnratio, m->check_ori,
+                                                matched_dist, m21, m12, bin_of, d_nm);
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(matches12, m12, sizeof(int) * n1, cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, d_nm, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+        *nmatches = m->h_pinned[0];
+        // vbPrevMatched update (src/ORBmatcher.cc:712-714)
+        std::vector<orbgpu_keypoint> k2;
+        if (f2->mem == ORBGPU_MEM_DEVICE) {
+            k2.resize(n2);
+            if (n2) ORBGPU_CUDA_TRY(cudaMemcpy(k2.data(), f2->keypoints, sizeof(orbgpu_keypoint) * n2, cudaMemcpyDeviceToHost));
+        }
+        const orbgpu_keypoint* K2 = f2->mem == ORBGPU_MEM_DEVICE ? k2.data() : f2->keypoints;
+        for (int i1 = 0; i1 < n1; i1++)
+            if (matches12[i1] >= 0) {
+                prev_matched[2 * i1] = K2[matches12[i1]].x;
+                prev_matched[2 * i1 + 1] = K2[matches12[i1]].y;
+            }
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
+}
+
+extern "C" int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame* f, const orbgpu_mappoint* mappoints,
+                                           const uint8_t* mp_descriptors, int n_mappoints, float th,
+                                           const uint8_t* claimed, int* match_out, int mem, int* nmatches) {
+    if (!m || !frame_ok(f) || n_mappoints < 0 || (n_mappoints > 0 && (!mappoints || !mp_descriptors)) || !match_out ||
+        !nmatches)
+        return ORBGPU_ERR_BAD_ARG;
+    const int n = f->n, M = n_mappoints;
+    *nmatches = 0;
+    size_t est = frame_stage_bytes(f) + grid_bytes(n) + (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint) + 32 + 16) +
+                 (size_t)n * 8 + 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 64;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        int rc = ensure_scratch(m, est);
+        if (rc) return rc;
+        Bump b{(uint8_t*)m->scratch, 0, m->scratch_bytes};
+        Staged s;
+        if ((rc = stage_frame(m, f, b, s))) return rc;
+        GridDev g;
+        if ((rc = build_grid(m, f, s, b, g))) return rc;
+        const orbgpu_mappoint* d_mps = mappoints;
+        const uint8_t* d_mpd = mp_descriptors;
+        const uint8_t* d_claimed = claimed;
+        int* d_match = match_out;
+        if (mem != ORBGPU_MEM_DEVICE) {
+            orbgpu_mappoint* a = b.take<orbgpu_mappoint>(std::max(1, M));
+            uint8_t* dd = b.take<uint8_t>((size_t)std::max(1, M) * 32);
+            if (M) {
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(a, mappoints, sizeof(orbgpu_mappoint) * M, cudaMemcpyHostToDevice, m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(dd, mp_descriptors, 32 * (size_t)M, cudaMemcpyHostToDevice, m->stream));
+            }
+            d_mps = a;
+            d_mpd = dd;
+            if (claimed) {
+                uint8_t* c = b.take<uint8_t>(std::max(1, n));
+                if (n) ORBGPU_CUDA_TRY(cudaMemcpyAsync(c, claimed, n, cudaMemcpyHostToDevice, m->stream));
+                d_claimed = c;
+            }
+            d_match = b.take<int>(std::max(1, n));
+        }
+        if (n > 0) k_init_match_out<<<(n + 255) / 256, 256, 0, m->stream>>>(d_claimed, n, d_match);
+        int *start, *count, total = 0;
+        uint64_t* keys = nullptr;
+        auto launch = [&](const int* st, int* cnt, uint64_t* out, int fill) {
+            const int wpb = 8;
+            if (M > 0)
+                k_proj_candidates<<<(M + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, d_mps, d_mpd, M, th, st, cnt, out,
+                                                                                fill);
+        };
+        rc = candidate_lists(m, M, b, launch, start, count, keys, total);
+        if (rc == ORBGPU_ERR_CAPACITY) {
+            est = est + sizeof(uint64_t) * (size_t)total * 2;
+            continue;
+        }
+        if (rc) return rc;
+        int* d_nm = b.take<int>(1);
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(d_nm, 0, sizeof(int), m->stream));
+        if (M > 0) k_proj_resolve<<<1, 32, 0, m->stream>>>(g, M, start, count, keys, m->nnratio, d_match, d_nm);
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        if (mem != ORBGPU_MEM_DEVICE && n > 0)
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(match_out, d_match, sizeof(int) * n, cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, d_nm, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+        *nmatches = m->h_pinned[0];
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
+}
+
+extern "C" int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* left,
+                                             const orbgpu_extractor* right, const orbgpu_frame* fl,
+                                             const orbgpu_frame* fr, float bf, float fx, float* uright, float* depth,
+                                             int mem) {
+    if (!m || !left || !right || !frame_ok(fl) || !frame_ok(fr) || !uright || !depth) return ORBGPU_ERR_BAD_ARG;
+    const int nL = fl->n, nR = fr->n;
+    if (nL == 0) return ORBGPU_OK;
+    StereoLevels lv;
+    std::memset(&lv, 0, sizeof(lv));
+    int nlev = fl->nlevels;
+    for (int l = 0; l < nlev; l++) {
+        const uint8_t *pl, *pr;
+        int w, h, w2, h2;
+        size_t pitch, pitch2;
+        if (orbgpu_extractor_pyramid_level(left, l, &pl, &w, &h, &pitch) ||
+            orbgpu_extractor_pyramid_level(right, l, &pr, &w2, &h2, &pitch2) || w != w2 || h != h2 || pitch != pitch2)
+            return ORBGPU_ERR_BAD_ARG;
+        lv.left[l] = pl;
+        lv.right[l] = pr;
+        lv.w[l] = w;
+        lv.h[l] = h;
+        lv.pitch[l] = (int)pitch;
+        lv.scale[l] = fl->scale_factors[l];
+        lv.inv_scale[l] = 1.0f / fl->scale_factors[l];
+    }
+    lv.nlevels = nlev;
+    const int nRows = lv.h[0];
+    float maxscale = 1.0f;
+    for (int l = 0; l < nlev; l++) maxscale = std::max(maxscale, lv.scale[l]);
+    const int rows_per_key = 2 * (int)std::ceil(2.0f * maxscale) + 4;
+    int sort_cap = 1;
+    while (sort_cap < nL) sort_cap <<= 1;
+    const size_t est = frame_stage_bytes(fl) + frame_stage_bytes(fr) + (size_t)(2 * nRows + 8) * sizeof(int) +
+                       (size_t)nR * rows_per_key * sizeof(int) + (size_t)nL * 3 * sizeof(float) + sort_cap * sizeof(int) +
+                       64 * 1024;
+    int rc = ensure_scratch(m, est);
+    if (rc) return rc;
+    Bump b{(uint8_t*)m->scratch, 0, m->scratch_bytes};
+    Staged sl, sr;
+    if ((rc = stage_frame(m, fl, b, sl)) || (rc = stage_frame(m, fr, b, sr))) return rc;
+    int* row_count = b.take<int>(nRows + 1);
+    int* row_start = b.take<int>(nRows + 1);
+    int* cursor = b.take<int>(nRows + 1);
+    int* row_keys = b.take<int>((size_t)std::max(1, nR) * rows_per_key);
+    int* d_total = b.take<int>(1);
+    float* d_ur = uright;
+    float* d_dp = depth;
+    if (mem != ORBGPU_MEM_DEVICE) {
+        d_ur = b.take<float>(nL);
+        d_dp = b.take<float>(nL);
+    }
+    int* sad = b.take<int>(nL);
+    int* sort_buf = b.take<int>(sort_cap);
+    int* status = b.take<int>(2);
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(row_count, 0, sizeof(int) * (nRows + 1), m->stream));
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * 2, m->stream));
+    if (nR > 0) k_stereo_rows_count<<<(nR + 255) / 256, 256, 0, m->stream>>>(sr.kps, nR, lv, nRows, row_count);
+    k_exclusive_scan<<<1, 1024, 0, m->stream>>>(row_count, nRows + 1, row_start, d_total);
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(cursor, row_start, sizeof(int) * (nRows + 1), cudaMemcpyDeviceToDevice, m->stream));
+    if (nR > 0) k_stereo_rows_fill<<<(nR + 255) / 256, 256, 0, m->stream>>>(sr.kps, nR, lv, nRows, cursor, row_keys);
+    const int wpb = 8;
+    k_stereo_match<<<(nL + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(sl.kps, sl.desc, nL, sr.kps, sr.desc, lv, nRows,
+                                                                   row_start, row_keys, bf, fx, d_ur, d_dp, sad, status);
+    k_stereo_median<<<1, 1024, 0, m->stream>>>(nL, sad, d_ur, d_dp, sort_buf, sort_cap, status + 1);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    if (mem != ORBGPU_MEM_DEVICE) {
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(uright, d_ur, sizeof(float) * nL, cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(depth, d_dp, sizeof(float) * nL, cudaMemcpyDeviceToHost, m->stream));
+    }
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+    if (m->h_pinned[0]) {
+        orbgpu_set_last_error("stereo patch outside its level", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_descriptor_distance(const uint8_t* a, const uint8_t* b, int n, int* out, void* stream) {
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return ORBGPU_ERR_BAD_ARG;
+    if (n == 0) return ORBGPU_OK;
+    k_descriptor_distance<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a, b, n, out);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    return ORBGPU_OK;
+}
+
+// ---------------------------------------------------------------- internal access for the kNN file
+cudaStream_t orbgpu_matcher_stream_internal(orbgpu_matcher* m) { return m->stream; }

@@ -1,0 +1,159 @@
+"""ORBmatcher and Frame::ComputeStereoMatches on the GPU, with the
+reference's interfaces (include/ORBmatcher.h, src/Frame.cc:831)."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE, MEM_DEVICE, MEM_HOST, FrameStruct, check, lib, ptr
+
+
+def _is_cuda(a) -> bool:
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+@dataclass
+class FrameView:
+    """The fields of ORB_SLAM2::Frame that the searches read.
+
+    keypoints: structured KEYPOINT_DTYPE array (host) or an (n, 7) float32
+    CUDA tensor with the same 28-byte records; descriptors: n x 32 uint8.
+    width/height: image bounds of the 64 x 48 grid (no distortion).
+    """
+    keypoints: object
+    descriptors: object
+    width: int
+    height: int
+    scale_factors: object
+    uright: object = None
+    _keep: list = field(default_factory=list, repr=False)
+
+    def struct(self) -> FrameStruct:
+        dev = _is_cuda(self.descriptors)
+        kps = self.keypoints
+        desc = self.descriptors
+        ur = self.uright
+        if not dev:
+            kps = np.ascontiguousarray(kps, KEYPOINT_DTYPE)
+            desc = np.ascontiguousarray(desc, np.uint8)
+            ur = None if ur is None else np.ascontiguousarray(ur, np.float32)
+        self._keep = [kps, desc, ur]
+        s = FrameStruct()
+        s.keypoints = ptr(kps).value
+        s.descriptors = ptr(desc).value
+        s.uright = ptr(ur).value if ur is not None else None
+        s.n = int(kps.shape[0])
+        s.width = int(self.width)
+        s.height = int(self.height)
+        sf = np.asarray(self.scale_factors, np.float32)
+        s.nlevels = int(len(sf))
+        for i, v in enumerate(sf[:16]):
+            s.scale_factors[i] = float(v)
+        s.mem = MEM_DEVICE if dev else MEM_HOST
+        return s
+
+
+class ORBmatcher:
+    """ORB_SLAM2::ORBmatcher(nnratio=0.6, checkOri=true)."""
+
+    TH_HIGH = 100
+    TH_LOW = 50
+    HISTO_LENGTH = 30
+
+    def __init__(self, nnratio: float = 0.6, checkOri: bool = True, stream=None):
+        self._h = C.c_void_p()
+        st = C.c_void_p(0 if stream is None else int(stream))
+        check(lib().orbgpu_matcher_create(C.c_float(nnratio), int(bool(checkOri)), st, C.byref(self._h)),
+              "orbgpu_matcher_create")
+        self.mfNNratio = nnratio
+        self.mbCheckOrientation = checkOri
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            try:
+                lib().orbgpu_matcher_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def SearchForInitialization(self, F1: FrameView, F2: FrameView, vbPrevMatched, windowSize: int = 10):
+        """Returns (nmatches, vnMatches12, vbPrevMatched updated) -- src/ORBmatcher.cc:573-717."""
+        s1, s2 = F1.struct(), F2.struct()
+        prev = np.ascontiguousarray(vbPrevMatched, np.float32).copy()
+        m12 = np.full(max(s1.n, 1), -1, np.int32)
+        nm = C.c_int(0)
+        check(lib().orbgpu_search_for_initialization(self._h, C.byref(s1), C.byref(s2), ptr(prev), ptr(m12),
+                                                     int(windowSize), C.byref(nm)),
+              "orbgpu_search_for_initialization")
+        return nm.value, m12[:s1.n], prev
+
+    def SearchByProjection(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0, claimed=None):
+        """SearchByProjection(Frame&, vector<MapPoint*>, th) -- src/ORBmatcher.cc:72-183.
+
+        Returns (nmatches, match) with match[i] the map point index assigned
+        to keypoint i (-2 pre-claimed, -1 none)."""
+        s = F.struct()
+        dev = s.mem == MEM_DEVICE
+        nm = C.c_int(0)
+        if dev:
+            import torch
+            out = torch.empty(max(s.n, 1), dtype=torch.int32, device="cuda")
+            mps, mpd, cl = mappoints, mp_descriptors, claimed
+        else:
+            out = np.zeros(max(s.n, 1), np.int32)
+            mps = np.ascontiguousarray(mappoints, MAPPOINT_DTYPE)
+            mpd = np.ascontiguousarray(mp_descriptors, np.uint8)
+            cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
+        check(lib().orbgpu_search_by_projection(self._h, C.byref(s), ptr(mps), ptr(mpd), int(len(mps)),
+                                                C.c_float(th), ptr(cl), ptr(out), MEM_DEVICE if dev else MEM_HOST,
+                                                C.byref(nm)),
+              "orbgpu_search_by_projection")
+        return nm.value, out[:s.n]
+
+    def knn2(self, query, train):
+        """Brute-force k=2 over DescriptorDistance (device tensors) -> (idx1, d1, idx2, d2)."""
+        import torch
+        nq = int(query.shape[0])
+        outs = [torch.empty(max(nq, 1), dtype=torch.int32, device=query.device) for _ in range(4)]
+        check(lib().orbgpu_knn2(self._h, ptr(query), nq, ptr(train), int(train.shape[0]), *[ptr(o) for o in outs], 0),
+              "orbgpu_knn2")
+        return tuple(o[:nq] for o in outs)
+
+    @staticmethod
+    def DescriptorDistance(a, b):
+        """ORBmatcher::DescriptorDistance over rows of two device tensors."""
+        import torch
+        n = int(a.shape[0])
+        out = torch.empty(max(n, 1), dtype=torch.int32, device=a.device)
+        check(lib().orbgpu_descriptor_distance(ptr(a), ptr(b), n, ptr(out), C.c_void_p(0)), "orbgpu_descriptor_distance")
+        torch.cuda.synchronize()
+        return out[:n]
+
+
+def compute_stereo_matches(matcher: ORBmatcher, left_extractor, right_extractor, FL: FrameView, FR: FrameView,
+                           bf: float, fx: float):
+    """Frame::ComputeStereoMatches (src/Frame.cc:831-1082): (mvuRight, mvDepth).
+
+    The extractors must be the ones that produced FL / FR (their pyramids are
+    read in place)."""
+    sl, sr = FL.struct(), FR.struct()
+    dev = sl.mem == MEM_DEVICE
+    if dev:
+        import torch
+        ur = torch.empty(max(sl.n, 1), dtype=torch.float32, device="cuda")
+        dp = torch.empty(max(sl.n, 1), dtype=torch.float32, device="cuda")
+    else:
+        ur = np.zeros(max(sl.n, 1), np.float32)
+        dp = np.zeros(max(sl.n, 1), np.float32)
+    check(lib().orbgpu_compute_stereo_matches(matcher.handle, left_extractor.handle, right_extractor.handle,
+                                              C.byref(sl), C.byref(sr), C.c_float(bf), C.c_float(fx), ptr(ur), ptr(dp),
+                                              MEM_DEVICE if dev else MEM_HOST),
+          "orbgpu_compute_stereo_matches")
+    return ur[:sl.n], dp[:sl.n]

@@ -1,0 +1,119 @@
+"""GPU extraction through the C ABI against the oracle and the golden fixtures."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from tests.gpu_util import assert_kps_equal, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return require_gpu()
+
+
+def extractor(nf, w=0, h=0):
+    from orb_slam2_detailed_comments_gb300 import ORBextractor
+    return ORBextractor(nf, 1.2, 8, 20, 7, w, h)
+
+
+def test_golden_640x480(torch, golden):
+    g = golden("extract_640x480.npz")
+    ex = extractor(1000)
+    kps, desc = ex(g["image"])
+    assert_kps_equal(kps, g["keypoints"], "keypoints")
+    assert np.array_equal(desc, g["descriptors"])
+    levels = ex.pyramid_numpy()
+    assert [l.shape for l in levels] == [tuple(s) for s in g["level_shapes"]]
+    assert [int(l.astype(np.int64).sum()) for l in levels] == list(g["level_sums"])
+    assert np.array_equal(levels[7], g["level7"])
+
+
+@pytest.mark.parametrize("w,h,nf,seed", [(640, 480, 1000, 1), (752, 480, 1500, 2), (1241, 376, 2000, 3),
+                                         (1280, 720, 2000, 4), (320, 240, 500, 5), (1024, 768, 3000, 6)])
+def test_vs_oracle(torch, oracle, w, h, nf, seed):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    img = syn.scene(w, h, seed)
+    ex = extractor(nf)
+    kps, desc = ex(img)
+    ref = oracle.extract(img, nfeatures=nf)
+    levels = ex.pyramid_numpy()
+    for l, (a, b) in enumerate(zip(levels, ref.pyramid)):
+        assert a.shape == b.shape and np.array_equal(a, b), f"pyramid level {l}"
+    blurred = ex.pyramid_numpy(blurred=True)
+    for l, (a, b) in enumerate(zip(blurred, ref.pyramid)):
+        bb = np.zeros_like(b)
+        oracle.lib.orc_blur_level(b.ctypes.data_as(pyoracle.C.c_void_p), b.shape[1], b.shape[0],
+                                  bb.ctypes.data_as(pyoracle.C.c_void_p))
+        assert np.array_equal(a, bb), f"blurred level {l}"
+    assert_kps_equal(kps, ref.keypoints, f"{w}x{h}")
+    assert np.array_equal(desc, ref.descriptors)
+
+
+def test_repeated_calls_and_sizes(torch, oracle):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    ex = extractor(1000)
+    for seed, (w, h) in enumerate([(640, 480), (320, 240), (640, 480), (800, 600)]):
+        img = syn.scene(w, h, 50 + seed)
+        kps, desc = ex(img)
+        ref = oracle.extract(img, nfeatures=1000)
+        assert_kps_equal(kps, ref.keypoints)
+        assert np.array_equal(desc, ref.descriptors)
+
+
+def test_device_in_device_out(torch, oracle):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    img = syn.scene(640, 480, 9)
+    ex = extractor(1000)
+    t = torch.from_numpy(img).cuda()
+    kps, desc = ex(t, device_out=True)
+    ref = oracle.extract(img, nfeatures=1000)
+    k = kps.cpu().numpy().view(pyoracle.KP_DTYPE).reshape(-1)
+    assert_kps_equal(k, ref.keypoints)
+    assert np.array_equal(desc.cpu().numpy(), ref.descriptors)
+
+
+def test_edge_cases(torch):
+    from orb_slam2_detailed_comments_gb300 import OrbGpuError
+    ex = extractor(1000)
+    kps, desc = ex(np.full((480, 640), 77, np.uint8))
+    assert len(kps) == 0 and desc.shape == (0, 32)
+    kps, desc = ex(np.zeros((0, 0), np.uint8))
+    assert len(kps) == 0
+    # portrait images make DistributeOctTree index an empty vector in the reference
+    with pytest.raises(OrbGpuError):
+        ex(np.zeros((800, 200), np.uint8))
+    # a capacity that is too small is reported, not truncated
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    import ctypes as C
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, lib, ptr
+    img = syn.scene(640, 480, 3)
+    k = np.zeros(10, KEYPOINT_DTYPE)
+    d = np.zeros((10, 32), np.uint8)
+    n = C.c_int(0)
+    rc = lib().orbgpu_extract(ex.handle, ptr(img), 640, 480, C.c_size_t(640), 0, ptr(k), ptr(d), 10, 0, C.byref(n))
+    assert rc == 5 and n.value > 10
+
+
+def test_descriptor_rotation_matches_host_libm(torch, oracle):
+    """cos/sin of the descriptor angle equal the host C library's cosf/sinf."""
+    import ctypes as C
+    from orb_slam2_detailed_comments_gb300._lib import lib, ptr
+    rng = np.random.default_rng(0)
+    hi = np.float32(360.0) * np.float32(np.pi / 180.0)
+    xs = [rng.uniform(0, hi, 1 << 22).astype(np.float32),
+          rng.uniform(0, 1e-3, 1 << 20).astype(np.float32),
+          np.arange(0, 1 << 20, dtype=np.uint32).view(np.float32)]
+    # every input the rotation of a keypoint at an integer-moment angle can take near 0, 90, 180, 270 degrees
+    x = np.ascontiguousarray(np.concatenate(xs))
+    xd = torch.from_numpy(x).cuda()
+    c = torch.empty_like(xd)
+    s = torch.empty_like(xd)
+    assert lib().orbgpu_descriptor_sincos(ptr(xd), len(x), ptr(c), ptr(s)) == 0
+    hc = np.zeros_like(x)
+    hs = np.zeros_like(x)
+    oracle.lib.orc_sincos_table(x.ctypes.data_as(C.c_void_p), len(x), hc.ctypes.data_as(C.c_void_p),
+                                hs.ctypes.data_as(C.c_void_p))
+    assert np.array_equal(c.cpu().numpy().view(np.uint32), hc.view(np.uint32))
+    assert np.array_equal(s.cpu().numpy().view(np.uint32), hs.view(np.uint32))

@@ -1,0 +1,156 @@
+"""GPU matchers through the C ABI against the oracle and the golden fixtures."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from tests.gpu_util import require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return require_gpu()
+
+
+def frame(kps, desc, w, h, uright=None):
+    from orb_slam2_detailed_comments_gb300 import FrameView
+    s, _ = pyoracle.scale_tables(8, 1.2)
+    return FrameView(kps, desc, w, h, np.array(s, np.float32), uright)
+
+
+def test_init_golden(torch, golden):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    g = golden("init_640x480.npz")
+    m = ORBmatcher(0.9, True)
+    F1 = frame(g["keypoints1"], g["descriptors1"], 640, 480)
+    F2 = frame(g["keypoints2"], g["descriptors2"], 640, 480)
+    prev = np.stack([g["keypoints1"]["x"], g["keypoints1"]["y"]], 1)
+    nm, m12, prev2 = m.SearchForInitialization(F1, F2, prev, 100)
+    assert nm == int(g["nmatches"])
+    assert np.array_equal(m12, g["matches12"])
+    assert np.array_equal(prev2, g["prev_matched"])
+
+
+@pytest.mark.parametrize("seed,ori,window", [(1, True, 100), (2, False, 100), (3, True, 50), (4, True, 200)])
+def test_init_vs_oracle(torch, oracle, seed, ori, window):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    f1, f2, _ = syn.frame_pair(640, 480, seed)
+    a = oracle.extract(f1, nfeatures=2000)
+    b = oracle.extract(f2, nfeatures=2000)
+    r = oracle.search_for_initialization(a.keypoints, a.descriptors, b.keypoints, b.descriptors, 640, 480,
+                                         window=window, nnratio=0.9, check_ori=ori)
+    m = ORBmatcher(0.9, ori)
+    prev = np.stack([a.keypoints["x"], a.keypoints["y"]], 1)
+    nm, m12, prev2 = m.SearchForInitialization(frame(a.keypoints, a.descriptors, 640, 480),
+                                               frame(b.keypoints, b.descriptors, 640, 480), prev, window)
+    assert nm == r[0]
+    assert np.array_equal(m12, r[1])
+    assert np.array_equal(prev2, r[2])
+
+
+def test_projection_golden(torch, golden):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    e = golden("extract_640x480.npz")
+    g = golden("projection_640x480.npz")
+    m = ORBmatcher(0.8, True)
+    F = frame(e["keypoints"], e["descriptors"], 640, 480, g["uright"])
+    for th in (1.0, 3.75):
+        nm, match = m.SearchByProjection(F, g["mappoints"], g["mp_descriptors"], th, g["claimed"])
+        assert nm == int(g[f"nmatches_th{th}"])
+        assert np.array_equal(match, g[f"match_th{th}"])
+
+
+def make_mappoints(kps, desc, M, rng):
+    n = len(kps)
+    src = rng.integers(0, n, M)
+    mpd = desc[src] ^ np.packbits(rng.random((M, 256)) < 0.1, axis=1, bitorder="little")
+    mps = np.zeros(M, pyoracle.MP_DTYPE)
+    mps["proj_x"] = kps["x"][src] + rng.normal(0, 2, M)
+    mps["proj_y"] = kps["y"][src] + rng.normal(0, 2, M)
+    mps["proj_xr"] = -1
+    mps["view_cos"] = 1.0
+    mps["track_scale_level"] = kps["octave"][src]
+    mps["track_in_view"] = 1
+    return mps, mpd
+
+
+@pytest.mark.parametrize("w,h,nf,seed", [(1280, 720, 2000, 1), (752, 480, 1500, 2)])
+def test_projection_vs_oracle(torch, oracle, w, h, nf, seed):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    rng = np.random.default_rng(seed)
+    a = oracle.extract(syn.scene(w, h, seed), nfeatures=nf)
+    mps, mpd = make_mappoints(a.keypoints, a.descriptors, 3000, rng)
+    th = 15.0 / 2.5
+    r = oracle.search_by_projection(a.keypoints, a.descriptors, w, h, mps, mpd, th=th, nnratio=0.8)
+    m = ORBmatcher(0.8, True)
+    nm, match = m.SearchByProjection(frame(a.keypoints, a.descriptors, w, h), mps, mpd, th)
+    assert nm == r[0]
+    assert np.array_equal(match, r[1])
+
+
+def test_stereo_golden(torch, golden, oracle):
+    from orb_slam2_detailed_comments_gb300 import ORBextractor, ORBmatcher, compute_stereo_matches
+    g = golden("stereo_640x240.npz")
+    exL = ORBextractor(1000, 1.2, 8, 20, 7)
+    exR = ORBextractor(1000, 1.2, 8, 20, 7)
+    kL, dL = exL(g["left"])
+    kR, dR = exR(g["right"])
+    assert kL.tobytes() == g["keypoints_left"].tobytes()
+    assert kR.tobytes() == g["keypoints_right"].tobytes()
+    m = ORBmatcher(0.75, True)
+    ur, dp = compute_stereo_matches(m, exL, exR, frame(kL, dL, 640, 240), frame(kR, dR, 640, 240),
+                                    float(g["bf"]), float(g["fx"]))
+    # bit-exact in practice; the contract is |delta| <= 1e-4 px
+    np.testing.assert_allclose(ur, g["uright"], atol=1e-4, rtol=0)
+    np.testing.assert_allclose(dp, g["depth"], atol=1e-4, rtol=1e-6)
+    assert np.array_equal(ur > 0, g["uright"] > 0)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_stereo_vs_oracle_1241x376(torch, oracle, seed):
+    from orb_slam2_detailed_comments_gb300 import ORBextractor, ORBmatcher, compute_stereo_matches
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    left, right, _ = syn.stereo_pair(1241, 376, seed)
+    exL = ORBextractor(2000, 1.2, 8, 20, 7)
+    exR = ORBextractor(2000, 1.2, 8, 20, 7)
+    kL, dL = exL(left)
+    kR, dR = exR(right)
+    L = oracle.extract(left, nfeatures=2000)
+    R = oracle.extract(right, nfeatures=2000)
+    u1, d1 = oracle.compute_stereo_matches(L.keypoints, L.descriptors, R.keypoints, R.descriptors, L.pyramid,
+                                           R.pyramid, 1241, 376, 386.1, 718.856)
+    m = ORBmatcher(0.75, True)
+    u2, d2 = compute_stereo_matches(m, exL, exR, frame(kL, dL, 1241, 376), frame(kR, dR, 1241, 376), 386.1, 718.856)
+    np.testing.assert_allclose(u2, u1, atol=1e-4, rtol=0)
+    np.testing.assert_allclose(d2, d1, atol=1e-4, rtol=1e-6)
+    assert np.array_equal(u1 > 0, u2 > 0) and (u1 > 0).sum() > 200
+
+
+def test_knn_golden_and_oracle(torch, golden, oracle):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    m = ORBmatcher()
+    g = golden("knn_200x3000.npz")
+    out = m.knn2(torch.from_numpy(g["query"]).cuda(), torch.from_numpy(g["train"]).cuda())
+    for a, name in zip(out, ("idx1", "d1", "idx2", "d2")):
+        assert np.array_equal(a.cpu().numpy(), g[name]), name
+    q = syn.random_descriptors(1000, 3)
+    t = syn.random_descriptors(20000, 4)
+    ref = oracle.knn2(q, t)
+    out = m.knn2(torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda())
+    for a, b in zip(out, ref):
+        assert np.array_equal(a.cpu().numpy(), b)
+
+
+def test_descriptor_distance_kat(torch, golden):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    g = golden("hamming_kat.npz")
+    p = g["patterns"]
+    n = len(p)
+    a = np.repeat(p, n, axis=0)
+    b = np.tile(p, (n, 1))
+    d = ORBmatcher.DescriptorDistance(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
+    assert np.array_equal(d.cpu().numpy().reshape(n, n), g["distance"])
