@@ -606,3 +606,31 @@ extern "C" int orbgpu_copy_to_host(void* dst, const void* src, size_t bytes) {
     ORBGPU_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
     return ORBGPU_OK;
 }
+
+// Internal per-level arrays of the last extraction, for stage-level tests:
+// what = 0 cell counts (ncells ints), 1 cell slots (ncells*cell_cap uint32),
+// 2 distributed keypoints (node_cap uint32), 3 geometry (8 ints: nCols,
+// nRows, wCell, hCell, cell_cap, nIni, node_cap, level count).
+extern "C" int orbgpu_extractor_debug_level(const orbgpu_extractor* ex, int level, int what, void* dst, size_t cap) {
+    if (!ex || level < 0 || level >= ex->nlevels || ex->cur_w < 0) return ORBGPU_ERR_BAD_ARG;
+    const LevelGeom& L = ex->geom[level];
+    const LevelOffsets& o = ex->layout.lv[level];
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(ex->stream));
+    size_t bytes = 0;
+    const void* src = nullptr;
+    if (what == 0) { src = ex->arena + o.cell_count; bytes = sizeof(int) * L.ncells; }
+    else if (what == 1) { src = ex->arena + o.slots; bytes = sizeof(uint32_t) * (size_t)L.cand_cap; }
+    else if (what == 2) { src = ex->arena + o.kept; bytes = sizeof(uint32_t) * (size_t)L.node_cap; }
+    else if (what == 3) {
+        int cnt = 0;
+        ORBGPU_CUDA_TRY(cudaMemcpy(&cnt, ex->arena + ex->layout.level_counts + sizeof(int) * level, sizeof(int),
+                                   cudaMemcpyDeviceToHost));
+        const int g[8] = {L.nCols, L.nRows, L.wCell, L.hCell, L.cell_cap, L.nIni, L.node_cap, cnt};
+        if (cap < sizeof(g)) return ORBGPU_ERR_CAPACITY;
+        std::memcpy(dst, g, sizeof(g));
+        return ORBGPU_OK;
+    } else return ORBGPU_ERR_BAD_ARG;
+    if (bytes > cap) return ORBGPU_ERR_CAPACITY;
+    ORBGPU_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return ORBGPU_OK;
+}

@@ -88,10 +88,28 @@ __global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* desc
 }
 
 // ---------------------------------------------------------------- FAST
-// Circle of radius 3 in cyclic order (dx, dy).
-__constant__ int8_t c_circle[16][2] = {{0, 3},  {1, 3},   {2, 2},   {3, 1},   {3, 0},  {3, -1},
-                                       {2, -2}, {1, -3},  {0, -3},  {-1, -3}, {-2, -2}, {-3, -1},
-                                       {-3, 0}, {-3, 1},  {-2, 2},  {-1, 3}};
+// The 16 pixels of the radius-3 Bresenham circle in cyclic order, as
+// offsets from the centre for a row stride 'rw': (dx, dy) = (0,3) (1,3)
+// (2,2) (3,1) (3,0) (3,-1) (2,-2) (1,-3) (0,-3) (-1,-3) (-2,-2) (-3,-1)
+// (-3,0) (-3,1) (-2,2) (-1,3).
+__device__ __forceinline__ void load_circle(const uint8_t* cp, int rw, int p[16]) {
+    p[0] = cp[3 * rw];
+    p[1] = cp[3 * rw + 1];
+    p[2] = cp[2 * rw + 2];
+    p[3] = cp[rw + 3];
+    p[4] = cp[3];
+    p[5] = cp[-rw + 3];
+    p[6] = cp[-2 * rw + 2];
+    p[7] = cp[-3 * rw + 1];
+    p[8] = cp[-3 * rw];
+    p[9] = cp[-3 * rw - 1];
+    p[10] = cp[-2 * rw - 2];
+    p[11] = cp[-rw - 3];
+    p[12] = cp[-3];
+    p[13] = cp[rw - 3];
+    p[14] = cp[2 * rw - 2];
+    p[15] = cp[3 * rw - 1];
+}
 
 __device__ __forceinline__ bool has_run9(uint32_t m) {
     uint32_t m32 = m | (m << 16);
@@ -115,11 +133,12 @@ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw, int r, i
     const bool maybe_b = (b0 & b4) | (b4 & b8) | (b8 & b12) | (b12 & b0);
     const bool maybe_d = (d0 & d4) | (d4 & d8) | (d8 & d12) | (d12 & d0);
     if (!maybe_b && !maybe_d) return 0;
-    int dd[16];
+    int pc[16], dd[16];
+    load_circle(cp, rw, pc);
     uint32_t bm = 0, dm = 0;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-        const int p = cp[c_circle[k][0] + c_circle[k][1] * rw];
+        const int p = pc[k];
         dd[k] = v - p;
         bm |= (uint32_t)(p > hi) << k;
         dm |= (uint32_t)(p < lo) << k;
@@ -231,6 +250,16 @@ __global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, cons
         return;
     }
     if (threadIdx.x == 0) d.cell_count[cell] = 0;
+}
+
+// Arc strength of every interior pixel of an image (pixels closer than 3 to
+// the border get 0), for the stage tests of the detector.
+__global__ void k_fast_strength_map(const uint8_t* img, int pitch, int w, int h, int t, uint8_t* out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= w || y >= h) return;
+    int m = 0;
+    if (x >= 3 && x < w - 3 && y >= 3 && y < h - 3) m = arc_strength(img + (size_t)y * pitch, pitch, 0, x, t);
+    out[(size_t)y * w + x] = (uint8_t)m;
 }
 
 // ---------------------------------------------------------------- DistributeOctTree
@@ -718,6 +747,15 @@ extern "C" int orbgpu_descriptor_sincos(const float* x, int n, float* c, float* 
     if (rc != ORBGPU_OK) return rc;
     if (n <= 0) return ORBGPU_OK;
     orbgpu::k_sincos_probe<<<(n + 255) / 256, 256>>>(x, n, c, s);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
+    return ORBGPU_OK;
+}
+
+// Device image (pitch bytes per row) -> w*h arc strengths at threshold t.
+extern "C" int orbgpu_debug_fast_strength(const uint8_t* img, int pitch, int w, int h, int t, uint8_t* out) {
+    dim3 grid((w + 127) / 128, h);
+    orbgpu::k_fast_strength_map<<<grid, 128>>>(img, pitch, w, h, t, out);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
     return ORBGPU_OK;
