@@ -1,0 +1,389 @@
+"""Benchmark of the GB300 ORB front-end.
+
+Workload (one "step"): the batched extraction + windowed matching workload --
+64 synthetic frames per batch with resolutions drawn uniformly from
+{640x480, 752x480, 1241x376, 1280x720} and nFeatures from {1000, 1500, 2000},
+8 levels, scale 1.2, FAST 20/7; then, for every frame, SearchByProjection of
+3000 map points (a frame descriptor with 10 % of its bits flipped, projected to
+its keypoint position + N(0, 2 px)) within radius 15 * scale, TH_HIGH 100,
+ratio 0.8.  Inputs are seeded synthetic images (no dataset is available).
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+Prints one JSON line.  value = frames/s over the timed steps (device-resident
+inputs); e2e = frames/s through the C ABI with host buffers (host->device
+image copies and device->host keypoints/descriptors/matches inside the timed
+region).  The reference arm times the CPU restatement of the reference path
+(oracle/) on the host cores with a thread pool.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RESOLUTIONS = [(640, 480), (752, 480), (1241, 376), (1280, 720)]
+NFEATURES = [1000, 1500, 2000]
+NFRAMES = 64
+NMAPPOINTS = 3000
+METRIC = "ORB frames/s (batched extraction + windowed matching, 64 mixed frames)"
+
+
+def workload(seed: int = 2024):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    rng = np.random.default_rng(seed)
+    frames = []
+    for f in range(NFRAMES):
+        w, h = RESOLUTIONS[rng.integers(0, len(RESOLUTIONS))]
+        nf = NFEATURES[rng.integers(0, len(NFEATURES))]
+        frames.append((syn.scene(w, h, seed * 1000 + f), int(nf)))
+    return frames
+
+
+def make_mappoints(kps, desc, rng):
+    from orb_slam2_detailed_comments_gb300._lib import MAPPOINT_DTYPE
+    n = len(kps)
+    src = rng.integers(0, n, NMAPPOINTS)
+    mpd = desc[src] ^ np.packbits(rng.random((NMAPPOINTS, 256)) < 0.1, axis=1, bitorder="little")
+    mps = np.zeros(NMAPPOINTS, MAPPOINT_DTYPE)
+    mps["proj_x"] = kps["x"][src] + rng.normal(0, 2, NMAPPOINTS)
+    mps["proj_y"] = kps["y"][src] + rng.normal(0, 2, NMAPPOINTS)
+    mps["proj_xr"] = -1
+    mps["view_cos"] = 1.0  # RadiusByViewingCos -> 2.5; th = 6 gives radius 15 * scale
+    mps["track_scale_level"] = kps["octave"][src]
+    mps["track_in_view"] = 1
+    return mps, np.ascontiguousarray(mpd)
+
+
+TH = 6.0  # 2.5 * 6 = 15 px at level 0
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle samples while the timed region runs."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, nm in enumerate(names):
+                if len(s) > 4 + i and s[4 + i].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def _level_sizes(w, h):
+    # mvInvScaleFactor and cvRound((float)W * inv) of src/ORBextractor.cc:1661-1663
+    s = [np.float32(1.0)]
+    for _ in range(7):
+        s.append(np.float32(np.float64(s[-1]) * np.float64(np.float32(1.2))))
+    inv = [np.float32(np.float32(1.0) / x) for x in s]
+    return [(int(np.rint(np.float32(w) * i)), int(np.rint(np.float32(h) * i))) for i in inv]
+
+
+def fast_bytes(frames):
+    """Algorithmic bytes of the FAST stage: every pixel of every level read once
+    plus the candidate words written (counted as read bytes only; the
+    candidates are a few KB per frame)."""
+    tot = 0
+    for img, _ in frames:
+        h, w = img.shape
+        tot += sum(a * b for a, b in _level_sizes(w, h))
+    return tot
+
+
+def run_ours(args):
+    import torch
+    from orb_slam2_detailed_comments_gb300 import build
+    build.build()
+    from orb_slam2_detailed_comments_gb300 import FrameView, ORBextractor, ORBmatcher
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE, check, lib, ptr
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchProjection
+
+    dev = torch.device("cuda", 0)
+    frames = workload()
+    imgs_dev = [torch.from_numpy(img).to(dev) for img, _ in frames]
+    nfs = [nf for _, nf in frames]
+    batch = BatchExtractor(NFRAMES, 1280, 720, 2000)
+    cap = batch.per_frame_capacity
+    # map points from the frames' own features (generated once)
+    kps, desc, counts = batch.extract(imgs_dev, nfs)
+    rng = np.random.default_rng(7)
+    mps_list, mpd_list = [], []
+    kps_h = kps.cpu().numpy().view(KEYPOINT_DTYPE).reshape(NFRAMES, cap)
+    desc_h = desc.cpu().numpy().reshape(NFRAMES, cap, 32)
+    cnt_h = counts.cpu().numpy()
+    for f in range(NFRAMES):
+        n = int(cnt_h[f])
+        m, d = make_mappoints(kps_h[f, :n], desc_h[f, :n], rng)
+        mps_list.append(m)
+        mpd_list.append(d)
+    proj = BatchProjection(batch, nnratio=0.8)
+    mps_dev = torch.from_numpy(np.concatenate(mps_list).view(np.uint8)).to(dev)
+    mpd_dev = torch.from_numpy(np.concatenate(mpd_list)).to(dev)
+    sizes = [(img.shape[1], img.shape[0]) for img, _ in frames]
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.ExternalStream(batch.stream)
+
+    def step():
+        k, d, c = batch.extract(imgs_dev, nfs)
+        match, nm = proj.search(mps_dev, mpd_dev, [NMAPPOINTS] * NFRAMES, TH)
+        return nm
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    stage_ms = {}
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (outside the events)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            for kname, v in batch.stage_times().items():
+                stage_ms[kname] = stage_ms.get(kname, 0.0) + v
+    total_ms = sum(times)
+    value = NFRAMES * args.steps / (total_ms / 1e3)
+
+    # e2e: host images in pinned memory, copies inside the timed region
+    pinned = [torch.from_numpy(img).pin_memory() for img, _ in frames]
+    staging = [torch.empty_like(t, device=dev) for t in pinned]
+    kps_host = torch.empty((NFRAMES * cap, 7), dtype=torch.float32).pin_memory()
+    desc_host = torch.empty((NFRAMES * cap, 32), dtype=torch.uint8).pin_memory()
+    match_host = torch.empty(NFRAMES * cap, dtype=torch.int32).pin_memory()
+    mps_host = torch.from_numpy(np.concatenate(mps_list).view(np.uint8)).pin_memory()
+    mpd_host = torch.from_numpy(np.concatenate(mpd_list)).pin_memory()
+    mps_stage = torch.empty_like(mps_dev)
+    mpd_stage = torch.empty_like(mpd_dev)
+    h2d = sum(t.numel() for t in pinned) + mps_host.numel() + mpd_host.numel()
+    d2h = kps_host.numel() * 4 + desc_host.numel() + match_host.numel() * 4
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for s, p in zip(staging, pinned):
+                s.copy_(p, non_blocking=True)
+            mps_stage.copy_(mps_host, non_blocking=True)
+            mpd_stage.copy_(mpd_host, non_blocking=True)
+        k, d, c = batch.extract(staging, nfs)
+        match, nm = proj.search(mps_stage, mpd_stage, [NMAPPOINTS] * NFRAMES, TH)
+        with torch.cuda.stream(stream):
+            kps_host.copy_(k.view(-1, 7), non_blocking=True)
+            desc_host.copy_(d.view(-1, 32), non_blocking=True)
+            match_host.copy_(match.view(-1), non_blocking=True)
+        torch.cuda.current_stream().wait_stream(stream)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = NFRAMES * args.steps / sum(e2e_times)
+
+    # per-frame plain path on the same frames (the drop-in path), for the batching gain
+    ex = ORBextractor(2000, 1.2, 8, 20, 7, 1280, 720)
+    matcher = ORBmatcher(0.8, True)
+    sc = ex.GetScaleFactors()
+    per_frame_ms = []
+    exs = {nf: ORBextractor(nf, 1.2, 8, 20, 7, 1280, 720) for nf in NFEATURES}
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for f, (img, nf) in enumerate(frames):
+            k, d = exs[nf](imgs_dev[f], device_out=True)
+            F = FrameView(k, d, img.shape[1], img.shape[0], sc)
+            matcher.SearchByProjection(F, torch.from_numpy(mps_list[f].view(np.uint8)).to(dev),
+                                       torch.from_numpy(mpd_list[f]).to(dev), TH)
+        torch.cuda.synchronize()
+        per_frame_ms.append((time.perf_counter() - t0) * 1e3)
+    per_frame_fps = NFRAMES / (min(per_frame_ms) / 1e3)
+
+    # roofline of the dominant stage
+    pk, pk_src = peaks()
+    dom = max(stage_ms, key=stage_ms.get) if stage_ms else None
+    dom_ms = stage_ms.get(dom, 0.0) / max(1, args.steps)
+    alg = {"fast": fast_bytes(frames), "resize_blur": 3 * fast_bytes(frames)}
+    achieved = alg.get(dom, fast_bytes(frames)) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
+                "peak_source": pk_src, "stage_ms_per_step": {k: v / max(1, args.steps) for k, v in stage_ms.items()}}
+
+    # CPU baseline: the oracle restatement on a bounded sample, one thread
+    cpu = cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1)
+
+    launches = (batch.launches_per_extract() + proj.launches_per_search()) * args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded scenes, no dataset)",
+        "config": {"workload": "batched extraction + SearchByProjection, 64 frames mixed 640x480/752x480/1241x376/"
+                               "1280x720, nFeatures 1000/1500/2000, 3000 map points per frame, radius 15*scale",
+                   "frames_per_step": NFRAMES, "l2": "flushed (256 MiB write) between timed steps"},
+        "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "per_frame_path_fps": per_frame_fps, "batched_over_per_frame": value / per_frame_fps,
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
+    }
+    print(json.dumps(line))
+
+
+def cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1):
+    """Frames/s of the CPU restatement (extraction + projection search) on a
+    bounded sample of the workload."""
+    from oracle import pyoracle
+    pyoracle.build()
+    done = [0]
+    t_end = time.perf_counter() + budget_s
+    lock = threading.Lock()
+    order = list(range(len(frames)))
+
+    def worker(tid):
+        o = pyoracle.Oracle()
+        i = tid
+        while time.perf_counter() < t_end:
+            f = order[i % len(order)]
+            img, nf = frames[f]
+            r = o.extract(img, nfeatures=nf, want_pyramid=False)
+            mps = mps_list[f] if mps_list is not None else None
+            if mps is not None:
+                o.search_by_projection(r.keypoints, r.descriptors, img.shape[1], img.shape[0],
+                                       mps.view(pyoracle.MP_DTYPE), mpd_list[f], th=TH, nnratio=0.8)
+            with lock:
+                done[0] += 1
+            i += threads
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    el = time.perf_counter() - t0
+    return {"value": done[0] / el, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{done[0]} frames of the workload (extraction + SearchByProjection) in {el:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    frames = workload()
+    # map points need keypoints: generate them from the restatement's own extraction of each frame used
+    from oracle import pyoracle
+    pyoracle.build()
+    o = pyoracle.Oracle()
+    rng = np.random.default_rng(7)
+    mps_list, mpd_list = [], []
+    nsample = min(len(frames), 16)
+    for f in range(nsample):
+        img, nf = frames[f]
+        r = o.extract(img, nfeatures=nf, want_pyramid=False)
+        kp = r.keypoints.view(pyoracle.KP_DTYPE)
+        from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
+        m, d = make_mappoints(kp.view(KEYPOINT_DTYPE), r.descriptors, rng)
+        mps_list.append(m)
+        mpd_list.append(d)
+    frames = frames[:nsample]
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(frames, mps_list, mpd_list, budget_s=2.0, threads=threads)
+    for _ in range(args.steps):
+        vals.append(cpu_sample(frames, mps_list, mpd_list, budget_s=8.0, threads=threads))
+    fps = sum(v["value"] for v in vals) / len(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * NFRAMES / fps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded scenes, no dataset)",
+            "config": {"workload": "batched extraction + SearchByProjection, 64 frames mixed 640x480/752x480/"
+                                   "1241x376/1280x720, nFeatures 1000/1500/2000, 3000 map points per frame"},
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": f"first {nsample} frames of the workload, 8 s per step on {threads} threads"},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        # replicas only: every rank runs the same single-GPU workload on its own GPU
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if rank == 0 or world == 1:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* desc
 // offsets from the centre for a row stride 'rw': (dx, dy) = (0,3) (1,3)
 // (2,2) (3,1) (3,0) (3,-1) (2,-2) (1,-3) (0,-3) (-1,-3) (-2,-2) (-3,-1)
 // (-3,0) (-3,1) (-2,2) (-1,3).
-__device__ __forceinline__ void load_circle(const uint8_t* cp, int rw, int p[16]) {
+__host__ __device__ __forceinline__ void load_circle(const uint8_t* cp, int rw, int p[16]) {
     p[0] = cp[3 * rw];
     p[1] = cp[3 * rw + 1];
     p[2] = cp[2 * rw + 2];
@@ -111,7 +111,7 @@ __device__ __forceinline__ void load_circle(const uint8_t* cp, int rw, int p[16]
     p[15] = cp[3 * rw - 1];
 }
 
-__device__ __forceinline__ bool has_run9(uint32_t m) {
+__host__ __device__ __forceinline__ bool has_run9(uint32_t m) {
     uint32_t m32 = m | (m << 16);
     uint32_t r = m32 & (m32 >> 1);
     r &= r >> 2;
@@ -120,10 +120,37 @@ __device__ __forceinline__ bool has_run9(uint32_t m) {
     return (r & 0xFFFFu) != 0;
 }
 
+// Max over the 16 cyclic nine-element windows of the window minimum of a
+// (by doubling: windows of 2, 4, 8, then 9).  Only min/max of the values
+// themselves: the darker- and brighter-centre cases are evaluated on two
+// arrays (v - p and p - v) instead of negating inside a max.
+__host__ __device__ __forceinline__ int best_window_min9(const int a[16]) {
+    int m2[16], m4[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int x = a[k], y = a[(k + 1) & 15];
+        m2[k] = x < y ? x : y;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int x = m2[k], y = m2[(k + 2) & 15];
+        m4[k] = x < y ? x : y;
+    }
+    int best = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int x = m4[k], y = m4[(k + 4) & 15], z = a[(k + 8) & 15];
+        int m = x < y ? x : y;
+        m = m < z ? m : z;
+        best = best > m ? best : m;
+    }
+    return best;
+}
+
 // Largest arc threshold (max over the 16 nine-pixel arcs of the smallest
 // absolute difference of consistent sign) if the pixel is a FAST corner at
 // threshold t, else 0.
-__device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw, int r, int c, int t) {
+__host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw, int r, int c, int t) {
     const uint8_t* cp = roi + r * rw + c;
     const int v = cp[0];
     const int p0 = cp[3 * rw], p4 = cp[3], p8 = cp[-3 * rw], p12 = cp[-3];
@@ -133,30 +160,20 @@ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw, int r, i
     const bool maybe_b = (b0 & b4) | (b4 & b8) | (b8 & b12) | (b12 & b0);
     const bool maybe_d = (d0 & d4) | (d4 & d8) | (d8 & d12) | (d12 & d0);
     if (!maybe_b && !maybe_d) return 0;
-    int pc[16], dd[16];
+    int pc[16], dark[16], bright[16];
     load_circle(cp, rw, pc);
     uint32_t bm = 0, dm = 0;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
         const int p = pc[k];
-        dd[k] = v - p;
+        dark[k] = v - p;    // circle darker than the centre
+        bright[k] = p - v;  // circle brighter than the centre
         bm |= (uint32_t)(p > hi) << k;
         dm |= (uint32_t)(p < lo) << k;
     }
     if (!has_run9(bm) && !has_run9(dm)) return 0;
-    int best = 0;
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-        int mn = dd[k], mx = dd[k];
-#pragma unroll
-        for (int j = 1; j < 9; j++) {
-            const int e = dd[(k + j) & 15];
-            mn = min(mn, e);
-            mx = max(mx, e);
-        }
-        best = max(best, max(mn, -mx));
-    }
-    return best;
+    const int a = best_window_min9(dark), b = best_window_min9(bright);
+    return a > b ? a : b;
 }
 
 #define FAST_MAX_ROI 72
@@ -756,6 +773,81 @@ extern "C" int orbgpu_descriptor_sincos(const float* x, int n, float* c, float* 
 extern "C" int orbgpu_debug_fast_strength(const uint8_t* img, int pitch, int w, int h, int t, uint8_t* out) {
     dim3 grid((w + 127) / 128, h);
     orbgpu::k_fast_strength_map<<<grid, 128>>>(img, pitch, w, h, t, out);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
+    return ORBGPU_OK;
+}
+
+// The same arc strengths computed by the host compiler (stage tests).
+extern "C" void orbgpu_debug_fast_strength_host(const uint8_t* img, int pitch, int w, int h, int t, uint8_t* out) {
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            out[(size_t)y * w + x] =
+                (x >= 3 && x < w - 3 && y >= 3 && y < h - 3) ? (uint8_t)orbgpu::arc_strength(img + (size_t)y * pitch, pitch, 0, x, t) : 0;
+}
+
+namespace orbgpu {
+// Per pixel (x, y): v, the 16 circle values, the bright/dark masks at t and
+// the arc strength, as the device reads and computes them (stage tests).
+__global__ void k_fast_probe(const uint8_t* img, int pitch, const int* xy, int n, int t, int* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t* cp = img + (size_t)xy[2 * i + 1] * pitch + xy[2 * i];
+    int pc[16];
+    load_circle(cp, pitch, pc);
+    int* o = out + (size_t)i * 21;
+    o[0] = cp[0];
+    uint32_t bm = 0, dm = 0;
+    for (int k = 0; k < 16; k++) {
+        o[1 + k] = pc[k];
+        bm |= (uint32_t)(pc[k] > cp[0] + t) << k;
+        dm |= (uint32_t)(pc[k] < cp[0] - t) << k;
+    }
+    o[17] = (int)bm;
+    o[18] = (int)dm;
+    o[19] = arc_strength(img + (size_t)xy[2 * i + 1] * pitch, pitch, 0, xy[2 * i], t);
+    o[20] = (int)has_run9(bm) + 2 * (int)has_run9(dm);
+}
+}  // namespace orbgpu
+extern "C" int orbgpu_debug_fast_probe(const uint8_t* img, int pitch, const int* xy, int n, int t, int* out) {
+    orbgpu::k_fast_probe<<<(n + 127) / 128, 128>>>(img, pitch, xy, n, t, out);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
+    return ORBGPU_OK;
+}
+
+namespace orbgpu {
+// arc_strength's internals for one pixel: v, hi, lo, dd[16], bm, dm, result
+__global__ void k_fast_probe2(const uint8_t* img, int pitch, int x, int y, int t, int* out) {
+    const uint8_t* cp = img + (size_t)y * pitch + x;
+    const int v = cp[0];
+    const int hi = v + t, lo = v - t;
+    int pc[16], dd[16];
+    load_circle(cp, pitch, pc);
+    uint32_t bm = 0, dm = 0;
+    for (int k = 0; k < 16; k++) {
+        const int p = pc[k];
+        dd[k] = v - p;
+        bm |= (uint32_t)(p > hi) << k;
+        dm |= (uint32_t)(p < lo) << k;
+    }
+    out[0] = v; out[1] = hi; out[2] = lo;
+    for (int k = 0; k < 16; k++) out[3 + k] = dd[k];
+    out[19] = (int)bm; out[20] = (int)dm;
+    out[21] = 0;
+    out[22] = arc_strength(img + (size_t)y * pitch, pitch, 0, x, t);
+    int best = 0;
+    for (int k = 0; k < 16; k++) {
+        int mn = dd[k], mx = dd[k];
+        for (int j = 1; j < 9; j++) { const int e = dd[(k + j) & 15]; mn = min(mn, e); mx = max(mx, e); }
+        out[23 + 2 * k] = mn; out[24 + 2 * k] = mx;
+        best = max(best, max(mn, -mx));
+    }
+    out[55] = best;
+}
+}  // namespace orbgpu
+extern "C" int orbgpu_debug_fast_probe2(const uint8_t* img, int pitch, int x, int y, int t, int* out) {
+    orbgpu::k_fast_probe2<<<1, 1>>>(img, pitch, x, y, t, out);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
     return ORBGPU_OK;
