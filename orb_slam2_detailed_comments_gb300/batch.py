@@ -1,0 +1,108 @@
+"""Batched extraction and projection matching over ragged frame lists
+(orbgpu_batch_* in include/orbgpu.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import MEM_DEVICE, check, lib, ptr
+
+STAGES = ("gather", "resize_blur", "fast", "distribute", "describe")
+
+
+class BatchExtractor:
+    """Extraction of many frames of uneven size per call (device images)."""
+
+    def __init__(self, max_frames: int, max_width: int, max_height: int, max_nfeatures: int,
+                 scale_factor: float = 1.2, nlevels: int = 8, ini_th: int = 20, min_th: int = 7, stream=None):
+        import torch
+        self._h = C.c_void_p()
+        st = C.c_void_p(0 if stream is None else int(stream))
+        check(lib().orbgpu_batch_create(int(max_frames), int(max_width), int(max_height), int(max_nfeatures), st,
+                                        C.byref(self._h)), "orbgpu_batch_create")
+        lib().orbgpu_batch_stream.restype = C.c_void_p
+        self.scale_factor = scale_factor
+        self.nlevels = nlevels
+        self.ini_th = ini_th
+        self.min_th = min_th
+        self.max_frames = max_frames
+        self.per_frame_capacity = int(max_nfeatures) + 64 * nlevels + 64
+        cap = self.per_frame_capacity
+        self.kps = torch.empty((max_frames * cap, 7), dtype=torch.float32, device="cuda")
+        self.desc = torch.empty((max_frames * cap, 32), dtype=torch.uint8, device="cuda")
+        self.counts = torch.zeros(max_frames, dtype=torch.int32, device="cuda")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            try:
+                lib().orbgpu_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return int(lib().orbgpu_batch_stream(self._h) or 0)
+
+    def extract(self, images, nfeatures):
+        """images: list of 2-D uint8 CUDA tensors; nfeatures: list of ints.
+        Returns (keypoints (F*cap, 7) float32 records, descriptors (F*cap, 32),
+        counts (F,)) -- frame f's rows start at f * per_frame_capacity."""
+        n = len(images)
+        ptrs = (C.c_void_p * n)(*[t.data_ptr() for t in images])
+        ws = np.array([t.shape[1] for t in images], np.int32)
+        hs = np.array([t.shape[0] for t in images], np.int32)
+        steps = np.array([t.stride(0) for t in images], np.uint64)
+        nf = np.array(nfeatures, np.int32)
+        self._keep = (ptrs, ws, hs, steps, nf)
+        check(lib().orbgpu_batch_extract(self._h, n, ptrs, ptr(ws), ptr(hs), ptr(steps), ptr(nf),
+                                         C.c_float(self.scale_factor), self.nlevels, self.ini_th, self.min_th,
+                                         ptr(self.kps), ptr(self.desc), self.per_frame_capacity, MEM_DEVICE,
+                                         ptr(self.counts)),
+              "orbgpu_batch_extract")
+        return self.kps[: n * self.per_frame_capacity], self.desc[: n * self.per_frame_capacity], self.counts[:n]
+
+    def stage_times(self) -> dict:
+        ms = np.zeros(5, np.float32)
+        check(lib().orbgpu_batch_stage_times(self._h, ptr(ms), 5), "orbgpu_batch_stage_times")
+        return dict(zip(STAGES, ms.tolist()))
+
+    def launches_per_extract(self) -> int:
+        return int(lib().orbgpu_batch_launch_count(self._h))
+
+
+class BatchProjection:
+    """SearchByProjection(Frame&, vector<MapPoint*>, th) for every frame of the
+    batch's last extraction."""
+
+    def __init__(self, batch: BatchExtractor, nnratio: float = 0.8):
+        import torch
+        self.batch = batch
+        self.nnratio = nnratio
+        self.match = torch.empty(batch.max_frames * batch.per_frame_capacity, dtype=torch.int32, device="cuda")
+        self.nm = torch.zeros(batch.max_frames, dtype=torch.int32, device="cuda")
+
+    def search(self, mappoints_u8, mp_descriptors, counts_per_frame, th: float):
+        """mappoints_u8: all frames' orbgpu_mappoint records (as uint8 CUDA
+        tensor), mp_descriptors: (M, 32) CUDA tensor; counts_per_frame: map
+        points per frame.  Returns (match (F*cap,), nmatches (F,))."""
+        b = self.batch
+        off = np.zeros(len(counts_per_frame) + 1, np.int32)
+        off[1:] = np.cumsum(counts_per_frame)
+        self._keep = off
+        check(lib().orbgpu_batch_search_by_projection(b.handle, ptr(b.kps), ptr(b.desc), ptr(b.counts),
+                                                      ptr(mappoints_u8), ptr(mp_descriptors), ptr(off),
+                                                      C.c_float(th), C.c_float(self.nnratio), ptr(self.match),
+                                                      ptr(self.nm)),
+              "orbgpu_batch_search_by_projection")
+        n = len(counts_per_frame)
+        return self.match[: n * b.per_frame_capacity], self.nm[:n]
+
+    def launches_per_search(self) -> int:
+        return int(lib().orbgpu_batch_search_launch_count())

@@ -80,6 +80,7 @@ struct orbgpu_batch {
     uint8_t* graph_desc = nullptr;
     int graph_cap = 0;
     int launches_per_run = 0;
+    cudaEvent_t ev[6] = {};
 };
 
 static void destroy_graph(orbgpu_batch* b) {
@@ -118,6 +119,11 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
         return ORBGPU_ERR_OOM;
     }
     b->src_cap = max_frames;
+    for (int i = 0; i < 6; i++)
+        if (cudaEventCreate(&b->ev[i]) != cudaSuccess) {
+            orbgpu_batch_destroy(b);
+            return ORBGPU_ERR_CUDA;
+        }
     *out = b;
     return ORBGPU_OK;
 }
@@ -134,6 +140,8 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     cudaFree(b->d_src);
     cudaFreeHost(b->h_src);
     cudaFreeHost(b->h_pinned);
+    for (int i = 0; i < 6; i++)
+        if (b->ev[i]) cudaEventDestroy(b->ev[i]);
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
     return ORBGPU_OK;
@@ -241,12 +249,20 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     int maxh = 0;
     for (int f = 0; f < b->nframes; f++) maxh = std::max(maxh, b->geoms[f][0].h);
     dim3 g((maxh + 7) / 8, b->nframes);
+    // stage boundaries are recorded as events (event nodes in the graph) so
+    // the per-stage device time of every replay can be read back
+    cudaEventRecord(b->ev[0], st);
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
+    cudaEventRecord(b->ev[1], st);
     for (int l = 0; l < b->nlevels; l++)
         launch_resize_blur(b->d_descs, b->d_items + b->rb_first[l], b->rb_count[l], l == 0, st);
+    cudaEventRecord(b->ev[2], st);
     launch_fast(b->d_descs, b->d_items + b->fast_first, b->fast_count, b->d_status, st);
+    cudaEventRecord(b->ev[3], st);
     launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->d_status, st);
+    cudaEventRecord(b->ev[4], st);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
+    cudaEventRecord(b->ev[5], st);
     b->launches_per_run = 1 + b->nlevels + 3;
 }
 
@@ -307,6 +323,288 @@ extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t*
     return ORBGPU_OK;
 }
 
+// Device time of the stages of the last orbgpu_batch_extract call (ms):
+// gather, resize+blur (all levels), FAST cells, DistributeOctTree, describe.
+extern "C" int orbgpu_batch_stage_times(orbgpu_batch* b, float* ms, int n) {
+    if (!b || !ms || n < 5) return ORBGPU_ERR_BAD_ARG;
+    ORBGPU_CUDA_TRY(cudaEventSynchronize(b->ev[5]));
+    for (int i = 0; i < 5; i++) ORBGPU_CUDA_TRY(cudaEventElapsedTime(&ms[i], b->ev[i], b->ev[i + 1]));
+    return ORBGPU_OK;
+}
+
 // Kernels launched by one orbgpu_batch_extract call.
 extern "C" int orbgpu_batch_launch_count(const orbgpu_batch* b) { return b ? b->launches_per_run : 0; }
 extern "C" void* orbgpu_batch_stream(const orbgpu_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+// ---------------------------------------------------------------- batched SearchByProjection
+// SearchByProjection(Frame&, vector<MapPoint*>, th) (src/ORBmatcher.cc:72-183)
+// for every frame of the last batch at once: grid build, candidate listing
+// (warp per map point, fixed-capacity slots) and the in-order resolution
+// (one warp per frame), five launches for the whole batch.
+namespace orbgpu {
+
+struct BatchFrameInfo {
+    float invW, invH;
+    int n_cap;
+    float scale[16];
+};
+
+__global__ void k_bgrid_count(const orbgpu_keypoint* kps, const int* counts, int cap, const BatchFrameInfo* info,
+                              int* key_cell, int* cell_count) {
+    const int f = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(counts[f], cap)) return;
+    const orbgpu_keypoint kp = kps[(size_t)f * cap + i];
+    const int px = (int)roundf(__fmul_rn(__fsub_rn(kp.x, 0.0f), info[f].invW));
+    const int py = (int)roundf(__fmul_rn(__fsub_rn(kp.y, 0.0f), info[f].invH));
+    int c = -1;
+    if (px >= 0 && px < ORBGPU_GRID_COLS && py >= 0 && py < ORBGPU_GRID_ROWS) c = px * ORBGPU_GRID_ROWS + py;
+    key_cell[(size_t)f * cap + i] = c;
+    if (c >= 0) atomicAdd(&cell_count[f * (ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS) + c], 1);
+}
+
+__global__ void k_bgrid_scan(const int* cell_count, int* cell_start, int* cursor) {
+    __shared__ int s_scan[32];
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    const int f = blockIdx.x;
+    const int* cc = cell_count + (size_t)f * ncell;
+    int* cs = cell_start + (size_t)f * (ncell + 1);
+    int* cu = cursor + (size_t)f * ncell;
+    int base = 0;
+    for (int b0 = 0; b0 < ncell; b0 += blockDim.x) {
+        const int c = b0 + threadIdx.x;
+        const int v = c < ncell ? cc[c] : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (c < ncell) {
+            cs[c] = base + ex;
+            cu[c] = base + ex;
+        }
+        base += tot;
+    }
+    if (threadIdx.x == 0) cs[ncell] = base;
+}
+
+__global__ void k_bgrid_fill(const int* counts, int cap, const int* key_cell, int* cursor, int* cell_keys) {
+    const int f = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(counts[f], cap)) return;
+    const int c = key_cell[(size_t)f * cap + i];
+    if (c >= 0) cell_keys[(size_t)f * cap + atomicAdd(&cursor[f * (ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS) + c], 1)] = i;
+}
+
+__global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* desc, int cap, const BatchFrameInfo* info,
+                                   const int* cell_start, const int* cell_keys, const orbgpu_mappoint* mps,
+                                   const uint8_t* mp_desc, const int* mp_off, float th, int slot_cap, uint64_t* slots,
+                                   int* slot_count, int* status) {
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    const int f = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int imp = mp_off[f] + local;
+    if (imp >= mp_off[f + 1]) return;
+    const orbgpu_mappoint mp = mps[imp];
+    const BatchFrameInfo& I = info[f];
+    const orbgpu_keypoint* K = kps + (size_t)f * cap;
+    const uint8_t* D = desc + (size_t)f * cap * 32;
+    const int* cs = cell_start + (size_t)f * (ncell + 1);
+    const int* ck = cell_keys + (size_t)f * cap;
+    int total = 0;
+    if (mp.track_in_view && !mp.bad && mp.track_scale_level >= 0 && mp.track_scale_level < 16) {
+        const int level = mp.track_scale_level;
+        float r = mp.view_cos > 0.998f ? 2.5f : 4.0f;
+        if (th != 1.0f) r = __fmul_rn(r, th);
+        const float radius = __fmul_rn(r, I.scale[level]);
+        const float x = mp.proj_x, y = mp.proj_y;
+        const int x0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(x, 0.0f), radius), I.invW)));
+        const int x1 = min(ORBGPU_GRID_COLS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(x, 0.0f), radius), I.invW)));
+        const int y0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(y, 0.0f), radius), I.invH)));
+        const int y1 = min(ORBGPU_GRID_ROWS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(y, 0.0f), radius), I.invH)));
+        if (x0 < ORBGPU_GRID_COLS && x1 >= 0 && y0 < ORBGPU_GRID_ROWS && y1 >= 0) {
+            const uint8_t* dmp = mp_desc + (size_t)imp * 32;
+            const float rr = __fmul_rn(radius, radius);
+            for (int ix = x0; ix <= x1; ix++)
+                for (int iy = y0; iy <= y1; iy++) {
+                    const int c = ix * ORBGPU_GRID_ROWS + iy;
+                    const int s = cs[c], e = cs[c + 1];
+                    for (int b = s; b < e; b += 32) {
+                        const int j = b + lane;
+                        bool ok = false;
+                        int idx = -1;
+                        if (j < e) {
+                            idx = ck[j];
+                            const orbgpu_keypoint kp = K[idx];
+                            ok = kp.octave >= level - 1 && kp.octave <= level;
+                            if (ok) {
+                                const float dx = __fsub_rn(kp.x, x), dy = __fsub_rn(kp.y, y);
+                                ok = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < rr;
+                            }
+                        }
+                        const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                        if (ok) {
+                            const int pos = total + __popc(msk & ((1u << lane) - 1));
+                            if (pos < slot_cap) {
+                                const int dist = hamming256_ptr(dmp, D + (size_t)idx * 32);
+                                slots[(size_t)imp * slot_cap + pos] = ((uint64_t)(uint32_t)dist << 40) |
+                                                                      ((uint64_t)(uint32_t)c << 20) | (uint64_t)(uint32_t)idx;
+                            }
+                        }
+                        total += __popc(msk);
+                    }
+                }
+        }
+    }
+    if (lane == 0) {
+        slot_count[imp] = total;
+        if (total > slot_cap) atomicMax(status, total);
+    }
+}
+
+__global__ void k_bproj_resolve(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off, int slot_cap,
+                                const uint64_t* slots, const int* slot_count, float nnratio, int* match_out,
+                                int* nmatches) {
+    const int f = blockIdx.x;
+    const int lane = threadIdx.x;
+    const orbgpu_keypoint* K = kps + (size_t)f * cap;
+    int* M = match_out + (size_t)f * cap;
+    const int n = min(counts[f], cap);
+    for (int i = lane; i < cap; i += 32) M[i] = i < n ? -1 : -3;
+    __syncwarp();
+    int nm = 0;
+    for (int imp = mp_off[f]; imp < mp_off[f + 1]; imp++) {
+        const int cnt = min(slot_count[imp], slot_cap);
+        if (cnt == 0) continue;
+        const uint64_t* S = slots + (size_t)imp * slot_cap;
+        uint64_t best = ~0ull, second = ~0ull;
+        for (int b = 0; b < cnt; b += 32) {
+            uint64_t key = ~0ull;
+            if (b + lane < cnt) {
+                key = S[b + lane];
+                if (M[(int)(key & 0xFFFFF)] != -1 || (int)(key >> 40) >= 256) key = ~0ull;
+            }
+            if (key < best) {
+                second = best;
+                best = key;
+            } else if (key < second) {
+                second = key;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
+            if (ob < best) {
+                second = best < os ? best : os;
+                best = ob;
+            } else {
+                second = second < ob ? second : ob;
+            }
+        }
+        if (best == ~0ull) continue;
+        const int bestDist = (int)(best >> 40);
+        const int bestIdx = (int)(best & 0xFFFFF);
+        const int bestLevel = K[bestIdx].octave;
+        const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
+        const int bestLevel2 = second == ~0ull ? -1 : K[(int)(second & 0xFFFFF)].octave;
+        if (bestDist <= ORBGPU_TH_HIGH) {
+            if (bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)) continue;
+            if (lane == 0) M[bestIdx] = imp - mp_off[f];
+            nm++;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) nmatches[f] = nm;
+}
+
+}  // namespace orbgpu
+
+struct orbgpu_batch_proj {
+    uint8_t* scratch = nullptr;
+    size_t bytes = 0;
+    int slot_cap = 64;
+    int* h_pinned = nullptr;
+};
+
+// Projection search over the frames of the last orbgpu_batch_extract call.
+// kps/desc/counts: that call's outputs (device); mappoints / mp_descriptors:
+// all frames' map points back to back (device), frame f owning
+// [mp_offsets[f], mp_offsets[f+1]) (host array).  match_out: device,
+// nframes * per_frame_capacity ints (map point index within the frame, -1
+// none, -3 past the frame's keypoints); nmatches: device, nframes ints.
+extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_keypoint* kps, const uint8_t* desc,
+                                                 const int* counts, const orbgpu_mappoint* mappoints,
+                                                 const uint8_t* mp_descriptors, const int* mp_offsets, float th,
+                                                 float nnratio, int* match_out, int* nmatches) {
+    if (!b || b->nframes <= 0 || !kps || !desc || !counts || !mp_offsets || !match_out || !nmatches)
+        return ORBGPU_ERR_BAD_ARG;
+    const int nf = b->nframes;
+    const int cap = b->sig[4];
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    const int total_mp = mp_offsets[nf];
+    int max_mp = 0;
+    for (int f = 0; f < nf; f++) max_mp = std::max(max_mp, mp_offsets[f + 1] - mp_offsets[f]);
+    static thread_local orbgpu_batch_proj P;
+    if (!P.h_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_pinned, 64));
+    cudaStream_t st = b->stream;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        const size_t need = sizeof(BatchFrameInfo) * nf + sizeof(int) * ((size_t)nf * ncell * 2 + (size_t)nf * (ncell + 1) +
+                                                                      (size_t)nf * cap * 2 + (nf + 1) + total_mp + 8) +
+                            sizeof(uint64_t) * (size_t)std::max(1, total_mp) * P.slot_cap + 8 * 256;
+        if (need > P.bytes) {
+            ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+            if (P.scratch) cudaFree(P.scratch);
+            P.scratch = nullptr;
+            ORBGPU_CUDA_TRY(cudaMalloc(&P.scratch, need));
+            P.bytes = need;
+        }
+        size_t off = 0;
+        auto take = [&](size_t n) {
+            off = (off + 255) & ~(size_t)255;
+            uint8_t* p = P.scratch + off;
+            off += n;
+            return p;
+        };
+        BatchFrameInfo* info = (BatchFrameInfo*)take(sizeof(BatchFrameInfo) * nf);
+        int* cell_count = (int*)take(sizeof(int) * (size_t)nf * ncell);
+        int* cursor = (int*)take(sizeof(int) * (size_t)nf * ncell);
+        int* cell_start = (int*)take(sizeof(int) * (size_t)nf * (ncell + 1));
+        int* key_cell = (int*)take(sizeof(int) * (size_t)nf * cap);
+        int* cell_keys = (int*)take(sizeof(int) * (size_t)nf * cap);
+        int* d_off = (int*)take(sizeof(int) * (nf + 1));
+        int* slot_count = (int*)take(sizeof(int) * std::max(1, total_mp));
+        int* status = (int*)take(sizeof(int) * 4);
+        uint64_t* slots = (uint64_t*)take(sizeof(uint64_t) * (size_t)std::max(1, total_mp) * P.slot_cap);
+        std::vector<BatchFrameInfo> hi(nf);
+        for (int f = 0; f < nf; f++) {
+            const int w = b->sig[6 + 3 * f], h = b->sig[7 + 3 * f];
+            hi[f].invW = static_cast<float>(ORBGPU_GRID_COLS) / static_cast<float>((float)w - 0.0f);
+            hi[f].invH = static_cast<float>(ORBGPU_GRID_ROWS) / static_cast<float>((float)h - 0.0f);
+            hi[f].n_cap = cap;
+            for (int l = 0; l < 16; l++) hi[f].scale[l] = l < b->nlevels ? b->tables[f].scale[l] : 1.0f;
+        }
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(info, hi.data(), sizeof(BatchFrameInfo) * nf, cudaMemcpyHostToDevice, st));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_off, mp_offsets, sizeof(int) * (nf + 1), cudaMemcpyHostToDevice, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(cell_count, 0, sizeof(int) * (size_t)nf * ncell, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * 4, st));
+        dim3 gk((cap + 255) / 256, nf);
+        k_bgrid_count<<<gk, 256, 0, st>>>(kps, counts, cap, info, key_cell, cell_count);
+        k_bgrid_scan<<<nf, 1024, 0, st>>>(cell_count, cell_start, cursor);
+        k_bgrid_fill<<<gk, 256, 0, st>>>(counts, cap, key_cell, cursor, cell_keys);
+        const int wpb = 8;
+        dim3 gc((std::max(1, max_mp) + wpb - 1) / wpb, nf);
+        k_bproj_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, mappoints,
+                                                   mp_descriptors, d_off, th, P.slot_cap, slots, slot_count, status);
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (P.h_pinned[0] > P.slot_cap) {  // a window held more candidates than the slots: widen and redo
+            P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
+            continue;
+        }
+        k_bproj_resolve<<<nf, 32, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, match_out,
+                                          nmatches);
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
+}
+
+extern "C" int orbgpu_batch_search_launch_count(void) { return 5; }

@@ -1,0 +1,91 @@
+"""Batched (ragged, graph-replayed) extraction and projection matching
+against the per-frame oracle."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from tests.gpu_util import assert_kps_equal, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(640, 480), (752, 480), (1241, 376), (1280, 720), (320, 240)]
+NF = [1000, 1500, 2000, 500]
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return require_gpu()
+
+
+def frames(seed, n):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    rng = np.random.default_rng(seed)
+    out = []
+    for f in range(n):
+        w, h = SIZES[rng.integers(0, len(SIZES))]
+        out.append((syn.scene(w, h, seed * 100 + f), int(NF[rng.integers(0, len(NF))])))
+    return out
+
+
+def test_batch_extract_vs_oracle(torch, oracle):
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
+    b = BatchExtractor(16, 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    for rep, seed in enumerate([1, 1, 2]):  # same list twice (graph replay), then a new list
+        fr = frames(seed, 12)
+        imgs = [torch.from_numpy(img).cuda() for img, _ in fr]
+        if rep == 1:  # same sizes, different pixels: the replayed graph reads the new images
+            from orb_slam2_detailed_comments_gb300 import synthetic as syn
+            fr = [(syn.scene(img.shape[1], img.shape[0], 999 + i), nf) for i, (img, nf) in enumerate(fr)]
+            imgs = [torch.from_numpy(img).cuda() for img, _ in fr]
+        k, d, c = b.extract(imgs, [nf for _, nf in fr])
+        k = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+        d = d.cpu().numpy().reshape(len(fr), cap, 32)
+        c = c.cpu().numpy()
+        for f, (img, nf) in enumerate(fr):
+            ref = oracle.extract(img, nfeatures=nf, want_pyramid=False)
+            assert c[f] == len(ref.keypoints), f"frame {f}"
+            assert_kps_equal(k[f, :c[f]], ref.keypoints, f"frame {f}")
+            assert np.array_equal(d[f, :c[f]], ref.descriptors)
+
+
+def test_batch_projection_vs_oracle(torch, oracle):
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchProjection
+    b = BatchExtractor(8, 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    fr = frames(5, 6)
+    imgs = [torch.from_numpy(img).cuda() for img, _ in fr]
+    k, d, c = b.extract(imgs, [nf for _, nf in fr])
+    kh = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    dh = d.cpu().numpy().reshape(len(fr), cap, 32)
+    ch = c.cpu().numpy()
+    rng = np.random.default_rng(3)
+    mps_all, mpd_all, counts = [], [], []
+    for f in range(len(fr)):
+        n = int(ch[f])
+        M = 3000
+        src = rng.integers(0, n, M)
+        mpd = dh[f, src] ^ np.packbits(rng.random((M, 256)) < 0.1, axis=1, bitorder="little")
+        mps = np.zeros(M, MAPPOINT_DTYPE)
+        mps["proj_x"] = kh[f, src]["x"] + rng.normal(0, 2, M)
+        mps["proj_y"] = kh[f, src]["y"] + rng.normal(0, 2, M)
+        mps["proj_xr"] = -1
+        mps["view_cos"] = 1.0
+        mps["track_scale_level"] = kh[f, src]["octave"]
+        mps["track_in_view"] = 1
+        mps_all.append(mps)
+        mpd_all.append(mpd)
+        counts.append(M)
+    p = BatchProjection(b, 0.8)
+    match, nm = p.search(torch.from_numpy(np.concatenate(mps_all).view(np.uint8)).cuda(),
+                         torch.from_numpy(np.ascontiguousarray(np.concatenate(mpd_all))).cuda(), counts, 6.0)
+    match = match.cpu().numpy().reshape(len(fr), cap)
+    nm = nm.cpu().numpy()
+    for f, (img, _) in enumerate(fr):
+        n = int(ch[f])
+        r = oracle.search_by_projection(kh[f, :n], dh[f, :n], img.shape[1], img.shape[0],
+                                        mps_all[f].view(pyoracle.MP_DTYPE), mpd_all[f], th=6.0, nnratio=0.8)
+        assert nm[f] == r[0], f"frame {f}"
+        assert np.array_equal(match[f, :n], r[1]), f"frame {f}"
