@@ -97,6 +97,8 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
     ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
     int rc = ensure_sincos_exceptions();
     if (rc != ORBGPU_OK) return rc;
+    rc = ensure_constants();
+    if (rc != ORBGPU_OK) return rc;
     orbgpu_batch* b = new orbgpu_batch();
     b->max_frames = max_frames;
     b->max_w = max_width;
@@ -602,6 +604,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         k_bproj_resolve<<<nf, 32, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, match_out,
                                           nmatches);
         ORBGPU_CUDA_TRY(cudaGetLastError());
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
         return ORBGPU_OK;
     }
     return ORBGPU_ERR_CAPACITY;

@@ -310,6 +310,19 @@ int load_sincos_exceptions(const char* path) {
     return ORBGPU_OK;
 }
 
+// The constant tables every kernel shares (Gaussian taps, IC_Angle row
+// bounds, rBRIEF pattern): the same for every configuration, uploaded once.
+static std::once_flag g_const_once;
+static int g_const_status = ORBGPU_OK;
+int ensure_constants() {
+    std::call_once(g_const_once, []() {
+        const ExtractorTables t = make_tables(1000, 1.2f, 8);
+        upload_constants(0, t.taps, t.umax);
+        g_const_status = cudaStreamSynchronize(0) == cudaSuccess ? ORBGPU_OK : ORBGPU_ERR_CUDA;
+    });
+    return g_const_status;
+}
+
 int ensure_sincos_exceptions() {
     std::call_once(g_exc_once, []() {
         const char* p = std::getenv("ORBGPU_SINCOS_TABLE");
@@ -464,7 +477,11 @@ extern "C" int orbgpu_extractor_create(int nfeatures, float scale_factor, int nl
         orbgpu_extractor_destroy(ex);
         return ORBGPU_ERR_OOM;
     }
-    upload_constants(ex->stream, ex->tables.taps, ex->tables.umax);
+    rc = ensure_constants();
+    if (rc != ORBGPU_OK) {
+        orbgpu_extractor_destroy(ex);
+        return rc;
+    }
     if (max_width > 0 && max_height > 0) {
         rc = setup_geometry(ex, max_width, max_height);
         if (rc != ORBGPU_OK) {

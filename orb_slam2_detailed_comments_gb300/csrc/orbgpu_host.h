@@ -53,6 +53,7 @@ void fill_tables(const std::vector<LevelGeom>& g, const FrameLayout& lay, std::v
                  size_t base);
 
 int ensure_sincos_exceptions();
+int ensure_constants();
 std::string default_sincos_table_path();
 // Builds the table of descriptor-angle inputs whose host cosf/sinf differ
 // from the rounded sincos_taylor value, and writes it to 'path'.
