@@ -251,20 +251,21 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     int maxh = 0;
     for (int f = 0; f < b->nframes; f++) maxh = std::max(maxh, b->geoms[f][0].h);
     dim3 g((maxh + 7) / 8, b->nframes);
-    // stage boundaries are recorded as events (event nodes in the graph) so
-    // the per-stage device time of every replay can be read back
-    cudaEventRecord(b->ev[0], st);
+    // stage boundaries are recorded as external events (event record nodes
+    // in the graph that the host can time), so the per-stage device time of
+    // every replay can be read back
+    cudaEventRecordWithFlags(b->ev[0], st, cudaEventRecordExternal);
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
-    cudaEventRecord(b->ev[1], st);
+    cudaEventRecordWithFlags(b->ev[1], st, cudaEventRecordExternal);
     for (int l = 0; l < b->nlevels; l++)
         launch_resize_blur(b->d_descs, b->d_items + b->rb_first[l], b->rb_count[l], l == 0, st);
-    cudaEventRecord(b->ev[2], st);
+    cudaEventRecordWithFlags(b->ev[2], st, cudaEventRecordExternal);
     launch_fast(b->d_descs, b->d_items + b->fast_first, b->fast_count, b->d_status, st);
-    cudaEventRecord(b->ev[3], st);
+    cudaEventRecordWithFlags(b->ev[3], st, cudaEventRecordExternal);
     launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->d_status, st);
-    cudaEventRecord(b->ev[4], st);
+    cudaEventRecordWithFlags(b->ev[4], st, cudaEventRecordExternal);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
-    cudaEventRecord(b->ev[5], st);
+    cudaEventRecordWithFlags(b->ev[5], st, cudaEventRecordExternal);
     b->launches_per_run = 1 + b->nlevels + 3;
 }
 
