@@ -171,6 +171,25 @@ int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* lef
 int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
                 int* idx2, int* d2, int algo);
 
+/* The same k = 2 search as orbgpu_knn2 (popcount kernel), for callers that
+ * cannot allocate device memory: processes whose device memory is reserved up
+ * front by their own allocator (a library cudaMalloc would fail or fragment
+ * it) and real-time paths where cudaMalloc/cudaFree's implicit device-wide
+ * synchronisation would stall other streams.  No counterpart in the
+ * reference.
+ * It allocates nothing: its scratch is a fixed 16 MiB device array inside
+ * the library, one (best, second) pair per query row per train slice, so nq
+ * is limited to 1048576 (ORBGPU_ERR_BAD_ARG beyond).  Every GPU that loads
+ * the library holds that array until the process exits.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, or host threads) race and give wrong results; serialise them.
+ * Asynchronous on 'stream' (NULL = the legacy default stream); all arrays on
+ * the device. */
+int orbgpu_knn2_noalloc(const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1, int* idx2,
+                        int* d2, void* stream);
+
 /* ORBmatcher::DescriptorDistance for n row pairs (device arrays). */
 int orbgpu_descriptor_distance(const uint8_t* a, const uint8_t* b, int n, int* out, void* stream);
 

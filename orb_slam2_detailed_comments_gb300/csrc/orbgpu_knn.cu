@@ -7,6 +7,7 @@
 // index, the rule of a sequential scan over DescriptorDistance
 // (src/ORBmatcher.cc:2083-2103).
 #include <algorithm>
+#include <mutex>
 
 #include "orbgpu_host.h"
 
@@ -107,5 +108,61 @@ extern "C" int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, cons
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaFreeAsync(partial, st));
     ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    return ORBGPU_OK;
+}
+
+// ---------------------------------------------------------------- allocation-free variant
+// orbgpu_knn2_noalloc keeps its per-slice (best, second) pairs in this
+// file-scope device array instead of memory it allocates.  Each GPU that
+// loads the library holds the array (16 MiB) until the process exits.
+#define ORBGPU_KNN_NOALLOC_MAX_PARTIAL (1 << 20)
+static __device__ __align__(256) int4 g_knn_noalloc_partial[ORBGPU_KNN_NOALLOC_MAX_PARTIAL];
+
+namespace {
+std::mutex g_noalloc_mutex;
+int4* g_noalloc_partial[256] = {};  // device address of the array, per device ordinal
+}  // namespace
+
+extern "C" int orbgpu_knn2_noalloc(const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
+                                   int* idx2, int* d2, void* stream) {
+    if (nq < 0 || nt < 0 || (nq > 0 && (!query || !idx1 || !d1 || !idx2 || !d2)) || (nt > 0 && !train)) {
+        orbgpu_set_last_error("invalid kNN arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (nq > ORBGPU_KNN_NOALLOC_MAX_PARTIAL) {
+        orbgpu_set_last_error("orbgpu_knn2_noalloc: more than 1048576 query rows (its fixed scratch holds one "
+                              "(best, second) pair per query per train slice)", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (nq == 0) return ORBGPU_OK;
+    int dev = 0, nsm = 0;
+    ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return ORBGPU_ERR_BAD_ARG;
+    int4* partial = nullptr;
+    {
+        // first call on a device: look up the array's device address with
+        // that device current (the host-side symbol is not a device address)
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_partial[dev]) {
+            void* p = nullptr;
+            ORBGPU_CUDA_TRY(cudaGetSymbolAddress(&p, g_knn_noalloc_partial));
+            g_noalloc_partial[dev] = (int4*)p;
+        }
+        partial = g_noalloc_partial[dev];
+    }
+    ORBGPU_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int qblocks = (nq + KNN_QPB - 1) / KNN_QPB;
+    int nslices = std::max(1, std::min((nt + KNN_TILE - 1) / KNN_TILE, (8 * nsm + qblocks - 1) / qblocks));
+    nslices = std::max(1, std::min(nslices, ORBGPU_KNN_NOALLOC_MAX_PARTIAL / nq));
+    int slice = (nt + nslices - 1) / nslices;
+    slice = ((slice + KNN_TILE - 1) / KNN_TILE) * KNN_TILE;
+    nslices = std::max(1, (nt + slice - 1) / std::max(1, slice));
+    // every partial entry read by the merge is written by the popcount
+    // kernel of the same call, so nothing is cleared between calls
+    dim3 grid(qblocks, nslices);
+    k_knn_popc<<<grid, KNN_QPB, 0, st>>>((const uint4*)query, nq, (const uint4*)train, nt, slice, partial);
+    k_knn_merge<<<(nq + 255) / 256, 256, 0, st>>>(partial, nq, nslices, idx1, d1, idx2, d2);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
     return ORBGPU_OK;
 }
