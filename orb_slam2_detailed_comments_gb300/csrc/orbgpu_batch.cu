@@ -463,14 +463,106 @@ __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* de
     }
 }
 
-__global__ void k_bproj_resolve(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off, int slot_cap,
-                                const uint64_t* slots, const int* slot_count, float nnratio, int* match_out,
-                                int* nmatches) {
+// Parallel resolution by fixed-point rounds.  In the reference a map point
+// sees a keypoint as claimed iff an earlier map point of the same call took
+// it.  Round r evaluates every map point against the claims made by the
+// results of round r-1 (claim owner = smallest map point index that took the
+// keypoint); once a round changes no result, every map point's result is
+// consistent with the results of the map points before it, which by
+// induction over the map point order is the sequential result.  Three claim
+// arrays rotate: read (round r-1's claims), write (round r's), and the one
+// cleared for round r+1.  A frame that has not converged after the last
+// round is replayed serially by k_bproj_resolve.
+#define BPROJ_ROUNDS 12
+#define BPROJ_NONE 0x7f7f7f7f
+
+__global__ void k_bproj_round(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off,
+                              int slot_cap, const uint64_t* slots, const int* slot_count, float nnratio, int round,
+                              int* claims3, int* res, int* changed, int* nwarp_frame) {
+    const int f = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int n_mp = mp_off[f + 1] - mp_off[f];
+    if (round > 0 && changed[(round - 1) * gridDim.y + f] == 0) return;  // converged
+    int* claims_r = claims3 + (size_t)((round + 0) % 3) * gridDim.y * cap + (size_t)f * cap;
+    int* claims_w = claims3 + (size_t)((round + 1) % 3) * gridDim.y * cap + (size_t)f * cap;
+    int* claims_z = claims3 + (size_t)((round + 2) % 3) * gridDim.y * cap + (size_t)f * cap;
+    // clear the array the next round writes into
+    for (int i = local * 32 + lane; i < cap; i += (*nwarp_frame) * 32) claims_z[i] = BPROJ_NONE;
+    if (local >= n_mp) return;
+    const int imp = mp_off[f] + local;
+    const orbgpu_keypoint* K = kps + (size_t)f * cap;
+    const int cnt = min(slot_count[imp], slot_cap);
+    const uint64_t* S = slots + (size_t)imp * slot_cap;
+    uint64_t best = ~0ull, second = ~0ull;
+    for (int b = 0; b < cnt; b += 32) {
+        uint64_t key = ~0ull;
+        if (b + lane < cnt) {
+            key = S[b + lane];
+            if (claims_r[(int)(key & 0xFFFFF)] < local || (int)(key >> 40) >= 256) key = ~0ull;
+        }
+        if (key < best) {
+            second = best;
+            best = key;
+        } else if (key < second) {
+            second = key;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
+        if (ob < best) {
+            second = best < os ? best : os;
+            best = ob;
+        } else {
+            second = second < ob ? second : ob;
+        }
+    }
+    int r = -1;
+    if (best != ~0ull) {
+        const int bestDist = (int)(best >> 40);
+        const int bestIdx = (int)(best & 0xFFFFF);
+        const int bestLevel = K[bestIdx].octave;
+        const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
+        const int bestLevel2 = second == ~0ull ? -1 : K[(int)(second & 0xFFFFF)].octave;
+        if (bestDist <= ORBGPU_TH_HIGH &&
+            !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
+            r = bestIdx;
+    }
+    if (lane == 0) {
+        if (res[imp] != r) changed[round * gridDim.y + f] = 1;
+        res[imp] = r;
+        if (r >= 0) atomicMin(&claims_w[r], local);
+    }
+}
+
+// Writes match_out / nmatches from the converged results; frames that did
+// not converge are replayed serially (same code as k_bproj_resolve).
+__global__ void k_bproj_finish(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off, int slot_cap,
+                               const uint64_t* slots, const int* slot_count, float nnratio, const int* changed,
+                               const int* res, int* match_out, int* nmatches, int* status) {
     const int f = blockIdx.x;
     const int lane = threadIdx.x;
-    const orbgpu_keypoint* K = kps + (size_t)f * cap;
     int* M = match_out + (size_t)f * cap;
     const int n = min(counts[f], cap);
+    if (changed[(BPROJ_ROUNDS - 1) * gridDim.x + f] == 0) {
+        for (int i = lane; i < cap; i += 32) M[i] = i < n ? -1 : -3;
+        __syncwarp();
+        int nm = 0;
+        for (int imp = mp_off[f] + lane; imp < mp_off[f + 1]; imp += 32) {
+            const int r = res[imp];
+            if (r >= 0) {
+                M[r] = imp - mp_off[f];
+                nm++;
+            }
+        }
+        nm = warp_sum(nm);
+        if (lane == 0) nmatches[f] = nm;
+        return;
+    }
+    if (lane == 0) atomicAdd(status + 1, 1);
+    // serial replay
+    const orbgpu_keypoint* K = kps + (size_t)f * cap;
     for (int i = lane; i < cap; i += 32) M[i] = i < n ? -1 : -3;
     __syncwarp();
     int nm = 0;
@@ -525,6 +617,7 @@ struct orbgpu_batch_proj {
     size_t bytes = 0;
     int slot_cap = 64;
     int* h_pinned = nullptr;
+    int last_serial_frames = 0;
 };
 
 // Projection search over the frames of the last orbgpu_batch_extract call.
@@ -550,7 +643,8 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
     cudaStream_t st = b->stream;
     for (int attempt = 0; attempt < 3; attempt++) {
         const size_t need = sizeof(BatchFrameInfo) * nf + sizeof(int) * ((size_t)nf * ncell * 2 + (size_t)nf * (ncell + 1) +
-                                                                      (size_t)nf * cap * 2 + (nf + 1) + total_mp + 8) +
+                                                                      (size_t)nf * cap * 5 + (nf + 1) + 2 * total_mp +
+                                                                      BPROJ_ROUNDS * nf + 16) +
                             sizeof(uint64_t) * (size_t)std::max(1, total_mp) * P.slot_cap + 8 * 256;
         if (need > P.bytes) {
             ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
@@ -576,6 +670,10 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         int* slot_count = (int*)take(sizeof(int) * std::max(1, total_mp));
         int* status = (int*)take(sizeof(int) * 4);
         uint64_t* slots = (uint64_t*)take(sizeof(uint64_t) * (size_t)std::max(1, total_mp) * P.slot_cap);
+        int* claims3 = (int*)take(sizeof(int) * (size_t)3 * nf * cap);
+        int* res = (int*)take(sizeof(int) * std::max(1, total_mp));
+        int* changed = (int*)take(sizeof(int) * BPROJ_ROUNDS * nf);
+        int* nwarp = (int*)take(sizeof(int) * 2);
         std::vector<BatchFrameInfo> hi(nf);
         for (int f = 0; f < nf; f++) {
             const int w = b->sig[6 + 3 * f], h = b->sig[7 + 3 * f];
@@ -602,13 +700,27 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
             P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
             continue;
         }
-        k_bproj_resolve<<<nf, 32, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, match_out,
-                                          nmatches);
+        // fixed-point rounds, then the result write-out (serial replay for any
+        // frame that did not converge)
+        const int warps = std::max((std::max(1, max_mp) + wpb - 1) / wpb * wpb, ((cap + 31) / 32 + wpb - 1) / wpb * wpb);
+        P.h_pinned[1] = warps;
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(nwarp, &P.h_pinned[1], sizeof(int), cudaMemcpyHostToDevice, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(claims3, 0x7f, sizeof(int) * (size_t)3 * nf * cap, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(res, 0xfe, sizeof(int) * std::max(1, total_mp), st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(changed, 0, sizeof(int) * BPROJ_ROUNDS * nf, st));
+        dim3 gr(warps / wpb, nf);
+        for (int r = 0; r < BPROJ_ROUNDS; r++)
+            k_bproj_round<<<gr, 32 * wpb, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, r,
+                                                  claims3, res, changed, nwarp);
+        k_bproj_finish<<<nf, 32, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, changed, res,
+                                         match_out, nmatches, status);
         ORBGPU_CUDA_TRY(cudaGetLastError());
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned + 2, status + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
         ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        P.last_serial_frames = P.h_pinned[2];
         return ORBGPU_OK;
     }
     return ORBGPU_ERR_CAPACITY;
 }
 
-extern "C" int orbgpu_batch_search_launch_count(void) { return 5; }
+extern "C" int orbgpu_batch_search_launch_count(void) { return 4 + BPROJ_ROUNDS + 1; }

@@ -340,6 +340,21 @@ int ensure_sincos_exceptions() {
 
 using namespace orbgpu;
 
+// Everything that depends on the image size: level geometry, the device
+// arena with the resize tables, the work lists.  An extractor keeps the plans
+// of the last few sizes it saw, so alternating sizes cost no re-planning.
+struct SizePlan {
+    int w = -1, h = -1;
+    std::vector<LevelGeom> geom;
+    FrameLayout layout;
+    uint8_t* arena = nullptr;
+    WorkItem* d_items = nullptr;
+    std::vector<int> rb_first, rb_count;
+    int fast_first = 0, fast_count = 0;
+    int max_kept = 0, sort_cap = 0;
+    uint64_t last_use = 0;
+};
+
 struct orbgpu_extractor {
     int nfeatures, nlevels, ini_th, min_th;
     float scale_factor;
@@ -347,18 +362,12 @@ struct orbgpu_extractor {
     ExtractorTables tables;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    // current geometry
+    std::vector<SizePlan*> plans;
+    SizePlan* cur = nullptr;
+    uint64_t use_clock = 0;
+    // current geometry (mirrors cur)
     int cur_w = -1, cur_h = -1;
-    std::vector<LevelGeom> geom;
-    FrameLayout layout;
-    uint8_t* arena = nullptr;
-    size_t arena_bytes = 0;
     LevelDesc* d_descs = nullptr;
-    WorkItem* d_items = nullptr;
-    size_t items_cap = 0;
-    std::vector<int> rb_first, rb_count;  // resize/blur items per level
-    int fast_first = 0, fast_count = 0;
-    int max_kept = 0, sort_cap = 0;
     int* d_status = nullptr;
     // output staging
     orbgpu_keypoint* d_kps = nullptr;
@@ -367,60 +376,93 @@ struct orbgpu_extractor {
     int* h_pinned = nullptr;  // status + counts
 };
 
-static int setup_geometry(orbgpu_extractor* ex, int w, int h) {
-    if (w == ex->cur_w && h == ex->cur_h) return ORBGPU_OK;
-    std::vector<LevelGeom> g;
-    int rc = level_geometry(ex->tables, w, h, g);
+static void free_plan(SizePlan* p) {
+    if (!p) return;
+    cudaFree(p->arena);
+    cudaFree(p->d_items);
+    delete p;
+}
+
+static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
+    SizePlan* P = new SizePlan();
+    int rc = level_geometry(ex->tables, w, h, P->geom);
     if (rc != ORBGPU_OK) {
+        delete P;
         orbgpu_set_last_error("image size not supported by the level geometry", __FILE__, __LINE__);
         return rc;
     }
-    FrameLayout lay;
-    lay.plan(g, 0);
-    if (lay.bytes > ex->arena_bytes) {
-        if (ex->arena) cudaFree(ex->arena);
-        ex->arena = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&ex->arena, lay.bytes));
-        ex->arena_bytes = lay.bytes;
+    const std::vector<LevelGeom>& g = P->geom;
+    P->layout.plan(g, 0);
+    if (cudaMalloc(&P->arena, P->layout.bytes) != cudaSuccess) {
+        delete P;
+        orbgpu_set_last_error("device allocation failed", __FILE__, __LINE__);
+        return ORBGPU_ERR_OOM;
     }
-    // resize tables
-    std::vector<uint8_t> host(lay.bytes, 0);
-    fill_tables(g, lay, host, 0);
+    // resize tables, level by level
     for (size_t l = 1; l < g.size(); l++) {
-        const LevelOffsets& o = lay.lv[l];
+        const LevelOffsets& o = P->layout.lv[l];
         const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * g[l].h;
-        ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->arena + lo, host.data() + lo, hi - lo, cudaMemcpyHostToDevice, ex->stream));
+        std::vector<uint8_t> host(hi - lo, 0);
+        resize_tables(g[l - 1].w, g[l - 1].h, g[l].w, g[l].h, (int*)&host[o.xofs - lo], (short*)&host[o.xalpha - lo],
+                      (int*)&host[o.yofs - lo], (short*)&host[o.ybeta - lo]);
+        if (cudaMemcpy(P->arena + lo, host.data(), hi - lo, cudaMemcpyHostToDevice) != cudaSuccess) {
+            free_plan(P);
+            return ORBGPU_ERR_CUDA;
+        }
     }
-    // work lists
     std::vector<WorkItem> items;
-    ex->rb_first.assign(g.size(), 0);
-    ex->rb_count.assign(g.size(), 0);
+    P->rb_first.assign(g.size(), 0);
+    P->rb_count.assign(g.size(), 0);
     for (size_t l = 0; l < g.size(); l++) {
-        ex->rb_first[l] = (int)items.size();
+        P->rb_first[l] = (int)items.size();
         const int tiles = ((g[l].w + 63) / 64) * ((g[l].h + 15) / 16);
         for (int i = 0; i < tiles; i++) items.push_back({(int)l, i});
-        ex->rb_count[l] = tiles;
+        P->rb_count[l] = tiles;
     }
-    ex->fast_first = (int)items.size();
+    P->fast_first = (int)items.size();
     for (size_t l = 0; l < g.size(); l++)
         for (int c = 0; c < g[l].ncells; c++) items.push_back({(int)l, c});
-    ex->fast_count = (int)items.size() - ex->fast_first;
-    if (items.size() > ex->items_cap) {
-        if (ex->d_items) cudaFree(ex->d_items);
-        ex->d_items = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&ex->d_items, items.size() * sizeof(WorkItem)));
-        ex->items_cap = items.size();
+    P->fast_count = (int)items.size() - P->fast_first;
+    if (cudaMalloc(&P->d_items, std::max<size_t>(1, items.size()) * sizeof(WorkItem)) != cudaSuccess ||
+        cudaMemcpy(P->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice) != cudaSuccess) {
+        free_plan(P);
+        return ORBGPU_ERR_OOM;
     }
-    ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
-                                    ex->stream));
-    ex->max_kept = 0;
-    ex->sort_cap = 1;
+    P->max_kept = 0;
+    P->sort_cap = 1;
     for (auto& L : g) {
-        ex->max_kept = std::max(ex->max_kept, L.node_cap);
-        while (ex->sort_cap < L.node_cap) ex->sort_cap <<= 1;
+        P->max_kept = std::max(P->max_kept, L.node_cap);
+        while (P->sort_cap < L.node_cap) P->sort_cap <<= 1;
     }
-    ex->geom = g;
-    ex->layout = lay;
+    P->w = w;
+    P->h = h;
+    *out = P;
+    return ORBGPU_OK;
+}
+
+static int setup_geometry(orbgpu_extractor* ex, int w, int h) {
+    ex->use_clock++;
+    if (ex->cur && ex->cur->w == w && ex->cur->h == h) {
+        ex->cur->last_use = ex->use_clock;
+        return ORBGPU_OK;
+    }
+    SizePlan* found = nullptr;
+    for (SizePlan* p : ex->plans)
+        if (p->w == w && p->h == h) found = p;
+    if (!found) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(ex->stream));
+        if (ex->plans.size() >= 8) {  // drop the least recently used plan
+            auto it = std::min_element(ex->plans.begin(), ex->plans.end(),
+                                       [](SizePlan* a, SizePlan* b) { return a->last_use < b->last_use; });
+            free_plan(*it);
+            ex->plans.erase(it);
+        }
+        int rc = build_plan(ex, w, h, &found);
+        if (rc != ORBGPU_OK) return rc;
+        ex->plans.push_back(found);
+    }
+    found->last_use = ex->use_clock;
+    ex->cur = found;
     ex->cur_w = w;
     ex->cur_h = h;
     return ORBGPU_OK;
@@ -496,9 +538,9 @@ extern "C" int orbgpu_extractor_create(int nfeatures, float scale_factor, int nl
 extern "C" int orbgpu_extractor_destroy(orbgpu_extractor* ex) {
     if (!ex) return ORBGPU_OK;
     if (ex->stream) cudaStreamSynchronize(ex->stream);
-    cudaFree(ex->arena);
+    for (SizePlan* p : ex->plans) free_plan(p);
+    ex->plans.clear();
     cudaFree(ex->d_descs);
-    cudaFree(ex->d_items);
     cudaFree(ex->d_status);
     cudaFree(ex->d_kps);
     cudaFree(ex->d_desc);
@@ -526,7 +568,8 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
     }
     int rc = setup_geometry(ex, width, height);
     if (rc != ORBGPU_OK) return rc;
-    const std::vector<LevelGeom>& g = ex->geom;
+    const SizePlan& P = *ex->cur;
+    const std::vector<LevelGeom>& g = P.geom;
     const int nl = (int)g.size();
     // descriptors of this call (outputs go to the caller's device arrays or
     // to the staging buffers)
@@ -542,7 +585,7 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
         odesc = ex->d_desc;
     }
     LevelDesc hd[ORBGPU_MAX_LEVELS];
-    fill_descs(g, ex->tables, ex->layout, ex->arena, 0, ex->ini_th, ex->min_th, 0, capacity, hd);
+    fill_descs(g, ex->tables, P.layout, P.arena, 0, ex->ini_th, ex->min_th, 0, capacity, hd);
     cudaStream_t st = ex->stream;
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_descs, hd, sizeof(LevelDesc) * nl, cudaMemcpyHostToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(ex->d_status, 0, sizeof(int) * 4, st));
@@ -552,10 +595,10 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                                                      : cudaMemcpyHostToDevice,
                                       st));
     for (int l = 0; l < nl; l++)
-        launch_resize_blur(ex->d_descs, ex->d_items + ex->rb_first[l], ex->rb_count[l], l == 0, st);
-    launch_fast(ex->d_descs, ex->d_items + ex->fast_first, ex->fast_count, ex->d_status, st);
-    launch_distribute(ex->d_descs, nl, ex->sort_cap, ex->d_status, st);
-    launch_describe(ex->d_descs, nl, ex->max_kept, okps, odesc, ex->d_status, st);
+        launch_resize_blur(ex->d_descs, P.d_items + P.rb_first[l], P.rb_count[l], l == 0, st);
+    launch_fast(ex->d_descs, P.d_items + P.fast_first, P.fast_count, ex->d_status, st);
+    launch_distribute(ex->d_descs, nl, P.sort_cap, ex->d_status, st);
+    launch_describe(ex->d_descs, nl, P.max_kept, okps, odesc, ex->d_status, st);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->h_pinned, ex->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->h_pinned + 4, hd[0].frame_total, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -600,8 +643,8 @@ extern "C" int orbgpu_extractor_tables(const orbgpu_extractor* ex, int* nlevels,
 extern "C" int orbgpu_extractor_pyramid_level(const orbgpu_extractor* ex, int level, const uint8_t** dev_ptr,
                                               int* width, int* height, size_t* pitch) {
     if (!ex || level < 0 || level >= ex->nlevels || ex->cur_w < 0) return ORBGPU_ERR_BAD_ARG;
-    const LevelGeom& L = ex->geom[level];
-    if (dev_ptr) *dev_ptr = ex->arena + ex->layout.lv[level].pyr;
+    const LevelGeom& L = ex->cur->geom[level];
+    if (dev_ptr) *dev_ptr = ex->cur->arena + ex->cur->layout.lv[level].pyr;
     if (width) *width = L.w;
     if (height) *height = L.h;
     if (pitch) *pitch = L.pitch;
@@ -613,7 +656,7 @@ extern "C" void* orbgpu_extractor_stream(const orbgpu_extractor* ex) { return ex
 // blurred level accessor used by the kernel tests
 extern "C" int orbgpu_extractor_blurred_level(const orbgpu_extractor* ex, int level, const uint8_t** dev_ptr) {
     if (!ex || level < 0 || level >= ex->nlevels || ex->cur_w < 0) return ORBGPU_ERR_BAD_ARG;
-    *dev_ptr = ex->arena + ex->layout.lv[level].blur;
+    *dev_ptr = ex->cur->arena + ex->cur->layout.lv[level].blur;
     return ORBGPU_OK;
 }
 
@@ -630,17 +673,18 @@ extern "C" int orbgpu_copy_to_host(void* dst, const void* src, size_t bytes) {
 // nRows, wCell, hCell, cell_cap, nIni, node_cap, level count).
 extern "C" int orbgpu_extractor_debug_level(const orbgpu_extractor* ex, int level, int what, void* dst, size_t cap) {
     if (!ex || level < 0 || level >= ex->nlevels || ex->cur_w < 0) return ORBGPU_ERR_BAD_ARG;
-    const LevelGeom& L = ex->geom[level];
-    const LevelOffsets& o = ex->layout.lv[level];
+    const LevelGeom& L = ex->cur->geom[level];
+    const LevelOffsets& o = ex->cur->layout.lv[level];
+    uint8_t* arena = ex->cur->arena;
     ORBGPU_CUDA_TRY(cudaStreamSynchronize(ex->stream));
     size_t bytes = 0;
     const void* src = nullptr;
-    if (what == 0) { src = ex->arena + o.cell_count; bytes = sizeof(int) * L.ncells; }
-    else if (what == 1) { src = ex->arena + o.slots; bytes = sizeof(uint32_t) * (size_t)L.cand_cap; }
-    else if (what == 2) { src = ex->arena + o.kept; bytes = sizeof(uint32_t) * (size_t)L.node_cap; }
+    if (what == 0) { src = arena + o.cell_count; bytes = sizeof(int) * L.ncells; }
+    else if (what == 1) { src = arena + o.slots; bytes = sizeof(uint32_t) * (size_t)L.cand_cap; }
+    else if (what == 2) { src = arena + o.kept; bytes = sizeof(uint32_t) * (size_t)L.node_cap; }
     else if (what == 3) {
         int cnt = 0;
-        ORBGPU_CUDA_TRY(cudaMemcpy(&cnt, ex->arena + ex->layout.level_counts + sizeof(int) * level, sizeof(int),
+        ORBGPU_CUDA_TRY(cudaMemcpy(&cnt, arena + ex->cur->layout.level_counts + sizeof(int) * level, sizeof(int),
                                    cudaMemcpyDeviceToHost));
         const int g[8] = {L.nCols, L.nRows, L.wCell, L.hCell, L.cell_cap, L.nIni, L.node_cap, cnt};
         if (cap < sizeof(g)) return ORBGPU_ERR_CAPACITY;
