@@ -48,44 +48,63 @@ __global__ void k_gather_images(const ImageSrc* src, int nframes) {
 
 using namespace orbgpu;
 
+// Everything about one frame configuration (size, feature budget) that the
+// batch needs: geometry, relative arena layout, the resize tables as a host
+// blob per level, and the block counts of its stages.
+struct FramePlan {
+    int w, h, nf;
+    ExtractorTables tables;
+    std::vector<LevelGeom> geom;
+    FrameLayout layout;  // offsets relative to the frame's slot
+    std::vector<std::vector<uint8_t>> table_blob;  // per level (l >= 1): xofs..ybeta region
+    std::vector<int> tiles;                         // resize/blur blocks per level
+};
+
 struct orbgpu_batch {
     int max_frames, max_w, max_h, max_nf;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    // plan of the last frame list
-    std::vector<int> sig;
-    int nframes = 0, nlevels = 0;
-    std::vector<ExtractorTables> tables;  // per frame
-    std::vector<std::vector<LevelGeom>> geoms;
-    std::vector<FrameLayout> layouts;
-    std::vector<size_t> frame_base;
+    int nlevels = 0;
+    float scale_factor = 0.f;
+    int ini_th = 0, min_th = 0;
+    std::vector<FramePlan*> plans;   // cache of frame configurations
+    // one arena slot per frame position; slot_plan[f] is what its tables hold
     uint8_t* arena = nullptr;
-    size_t arena_bytes = 0;
+    size_t slot_bytes = 0;
+    std::vector<const FramePlan*> slot_plan;
+    // current batch
+    std::vector<const FramePlan*> cur;
+    int nframes = 0;
+    std::vector<int> sig;
+    std::vector<int> h_prefix;  // host copy of the block-range prefix arrays
+    int* d_prefix = nullptr;
+    size_t prefix_cap = 0;
+    std::vector<int> rb_off, rb_count;
+    int fast_off = 0, fast_count = 0;
     LevelDesc* d_descs = nullptr;
     size_t descs_cap = 0;
-    WorkItem* d_items = nullptr;
-    size_t items_cap = 0;
-    std::vector<int> rb_first, rb_count;
-    int fast_first = 0, fast_count = 0;
+    int ndesc = 0;
     int max_kept = 0, sort_cap = 0;
     ImageSrc* d_src = nullptr;
     ImageSrc* h_src = nullptr;  // pinned
-    int src_cap = 0;
     int* d_status = nullptr;
     int* d_totals = nullptr;  // per frame
     int* h_pinned = nullptr;
-    int ndesc = 0;
     cudaGraphExec_t graph = nullptr;
+    std::vector<int> graph_sig;
     orbgpu_keypoint* graph_kps = nullptr;
     uint8_t* graph_desc = nullptr;
-    int graph_cap = 0;
+    int same_sig_runs = 0;
     int launches_per_run = 0;
     cudaEvent_t ev[6] = {};
+    // frame configuration handed to the accessors of the last batch
+    std::vector<float> frame_scale;  // nframes * 16
 };
 
 static void destroy_graph(orbgpu_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
+    b->graph_sig.clear();
 }
 
 extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height, int max_nfeatures, void* stream,
@@ -120,12 +139,12 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
         orbgpu_batch_destroy(b);
         return ORBGPU_ERR_OOM;
     }
-    b->src_cap = max_frames;
     for (int i = 0; i < 6; i++)
         if (cudaEventCreate(&b->ev[i]) != cudaSuccess) {
             orbgpu_batch_destroy(b);
             return ORBGPU_ERR_CUDA;
         }
+    b->slot_plan.assign(max_frames, nullptr);
     *out = b;
     return ORBGPU_OK;
 }
@@ -136,7 +155,7 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     destroy_graph(b);
     cudaFree(b->arena);
     cudaFree(b->d_descs);
-    cudaFree(b->d_items);
+    cudaFree(b->d_prefix);
     cudaFree(b->d_status);
     cudaFree(b->d_totals);
     cudaFree(b->d_src);
@@ -144,12 +163,50 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     cudaFreeHost(b->h_pinned);
     for (int i = 0; i < 6; i++)
         if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    for (FramePlan* p : b->plans) delete p;
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
     return ORBGPU_OK;
 }
 
-// Builds the plan (geometry, arena, descriptors, work lists) of a frame list.
+static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out) {
+    for (FramePlan* p : b->plans)
+        if (p->w == w && p->h == h && p->nf == nf) {
+            *out = p;
+            return ORBGPU_OK;
+        }
+    FramePlan* P = new FramePlan();
+    P->w = w;
+    P->h = h;
+    P->nf = nf;
+    P->tables = make_tables(nf, b->scale_factor, b->nlevels);
+    int rc = level_geometry(P->tables, w, h, P->geom);
+    if (rc != ORBGPU_OK) {
+        delete P;
+        orbgpu_set_last_error("frame size not supported by the level geometry", __FILE__, __LINE__);
+        return rc;
+    }
+    P->layout.plan(P->geom, 0);
+    P->table_blob.assign(b->nlevels, {});
+    P->tiles.assign(b->nlevels, 0);
+    for (int l = 0; l < b->nlevels; l++) {
+        const LevelGeom& L = P->geom[l];
+        P->tiles[l] = ((L.w + 63) / 64) * ((L.h + 15) / 16);
+        if (l == 0) continue;
+        const LevelOffsets& o = P->layout.lv[l];
+        const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * L.h;
+        std::vector<uint8_t>& blob = P->table_blob[l];
+        blob.assign(hi - lo, 0);
+        resize_tables(P->geom[l - 1].w, P->geom[l - 1].h, L.w, L.h, (int*)&blob[o.xofs - lo], (short*)&blob[o.xalpha - lo],
+                      (int*)&blob[o.yofs - lo], (short*)&blob[o.ybeta - lo]);
+    }
+    b->plans.push_back(P);
+    *out = P;
+    return ORBGPU_OK;
+}
+
+// Plans the batch: frame configurations, arena slots (tables written only
+// where a slot changes configuration), descriptors and block ranges.
 static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int* heights, const int* nfeatures,
                       float scale_factor, int nlevels, int ini_th, int min_th, int per_frame_cap) {
     std::vector<int> sig = {nframes, nlevels, ini_th, min_th, per_frame_cap};
@@ -161,95 +218,123 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         sig.push_back(heights[f]);
         sig.push_back(nfeatures[f]);
     }
-    if (sig == b->sig) return ORBGPU_OK;
-    destroy_graph(b);
-    b->sig.clear();
-    b->nframes = nframes;
-    b->nlevels = nlevels;
-    b->tables.clear();
-    b->geoms.assign(nframes, {});
-    b->layouts.assign(nframes, {});
-    b->frame_base.assign(nframes, 0);
-    size_t off = 0;
-    for (int f = 0; f < nframes; f++) {
-        b->tables.push_back(make_tables(nfeatures[f], scale_factor, nlevels));
-        int rc = level_geometry(b->tables.back(), widths[f], heights[f], b->geoms[f]);
-        if (rc != ORBGPU_OK) {
-            orbgpu_set_last_error("frame size not supported by the level geometry", __FILE__, __LINE__);
-            return rc;
-        }
-        b->frame_base[f] = off;
-        off = b->layouts[f].plan(b->geoms[f], off);
+    if (sig == b->sig) {
+        b->same_sig_runs++;
+        return ORBGPU_OK;
     }
-    if (off > b->arena_bytes) {
+    b->same_sig_runs = 0;
+    if (nlevels != b->nlevels || scale_factor != b->scale_factor) {  // configuration cache is per pyramid shape
         ORBGPU_CUDA_TRY(cudaStreamSynchronize(b->stream));
+        for (FramePlan* p : b->plans) delete p;
+        b->plans.clear();
+        std::fill(b->slot_plan.begin(), b->slot_plan.end(), nullptr);
+        b->nlevels = nlevels;
+        b->scale_factor = scale_factor;
+    }
+    b->ini_th = ini_th;
+    b->min_th = min_th;
+    b->cur.assign(nframes, nullptr);
+    size_t need = b->slot_bytes;
+    for (int f = 0; f < nframes; f++) {
+        int rc = get_plan(b, widths[f], heights[f], nfeatures[f], &b->cur[f]);
+        if (rc != ORBGPU_OK) return rc;
+        need = std::max(need, (b->cur[f]->layout.bytes + 4095) & ~(size_t)4095);
+    }
+    cudaStream_t st = b->stream;
+    if (need > b->slot_bytes || !b->arena) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        destroy_graph(b);
         if (b->arena) cudaFree(b->arena);
         b->arena = nullptr;
-        b->arena_bytes = 0;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->arena, off));
-        b->arena_bytes = off;
+        ORBGPU_CUDA_TRY(cudaMalloc(&b->arena, need * b->max_frames));
+        b->slot_bytes = need;
+        std::fill(b->slot_plan.begin(), b->slot_plan.end(), nullptr);
     }
-    // resize tables of every frame
-    std::vector<uint8_t> host(off, 0);
-    for (int f = 0; f < nframes; f++) fill_tables(b->geoms[f], b->layouts[f], host, 0);
-    ORBGPU_CUDA_TRY(cudaMemcpy(b->arena, host.data(), off, cudaMemcpyHostToDevice));
+    // resize tables of slots whose configuration changed
+    for (int f = 0; f < nframes; f++) {
+        const FramePlan* P = b->cur[f];
+        if (b->slot_plan[f] == P) continue;
+        uint8_t* base = b->arena + (size_t)f * b->slot_bytes;
+        for (int l = 1; l < nlevels; l++)
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(base + P->layout.lv[l].xofs, P->table_blob[l].data(), P->table_blob[l].size(),
+                                            cudaMemcpyHostToDevice, st));
+        b->slot_plan[f] = P;
+    }
     // descriptors
     const int ndesc = nframes * nlevels;
     if ((size_t)ndesc > b->descs_cap) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
         if (b->d_descs) cudaFree(b->d_descs);
         b->d_descs = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_descs, sizeof(LevelDesc) * ndesc));
-        b->descs_cap = ndesc;
+        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_descs, sizeof(LevelDesc) * b->max_frames * nlevels));
+        b->descs_cap = (size_t)b->max_frames * nlevels;
     }
     std::vector<LevelDesc> hd(ndesc);
+    b->frame_scale.assign((size_t)nframes * 16, 1.0f);
     for (int f = 0; f < nframes; f++) {
-        fill_descs(b->geoms[f], b->tables[f], b->layouts[f], b->arena, f, ini_th, min_th, f * per_frame_cap,
-                   per_frame_cap, &hd[(size_t)f * nlevels]);
-        for (int l = 0; l < nlevels; l++) hd[(size_t)f * nlevels + l].frame_total = b->d_totals + f;
+        const FramePlan* P = b->cur[f];
+        fill_descs(P->geom, P->tables, P->layout, b->arena + (size_t)f * b->slot_bytes, f, ini_th, min_th,
+                   f * per_frame_cap, per_frame_cap, &hd[(size_t)f * nlevels]);
+        for (int l = 0; l < nlevels; l++) {
+            hd[(size_t)f * nlevels + l].frame_total = b->d_totals + f;
+            b->frame_scale[(size_t)f * 16 + l] = P->tables.scale[l];
+        }
     }
-    ORBGPU_CUDA_TRY(cudaMemcpy(b->d_descs, hd.data(), sizeof(LevelDesc) * ndesc, cudaMemcpyHostToDevice));
-    // work lists: resize/blur tiles per level (all frames), then all cells
-    std::vector<WorkItem> items;
-    b->rb_first.assign(nlevels, 0);
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->d_descs, hd.data(), sizeof(LevelDesc) * ndesc, cudaMemcpyHostToDevice, st));
+    // block ranges: per level the tiles of every frame, then the cells of
+    // every (frame, level) pair
+    std::vector<int>& pre = b->h_prefix;
+    pre.clear();
+    b->rb_off.assign(nlevels, 0);
     b->rb_count.assign(nlevels, 0);
     for (int l = 0; l < nlevels; l++) {
-        b->rb_first[l] = (int)items.size();
+        b->rb_off[l] = (int)pre.size();
+        int acc = 0;
         for (int f = 0; f < nframes; f++) {
-            const LevelGeom& L = b->geoms[f][l];
-            const int tiles = ((L.w + 63) / 64) * ((L.h + 15) / 16);
-            for (int i = 0; i < tiles; i++) items.push_back({f * nlevels + l, i});
+            pre.push_back(acc);
+            acc += b->cur[f]->tiles[l];
         }
-        b->rb_count[l] = (int)items.size() - b->rb_first[l];
+        pre.push_back(acc);
+        b->rb_count[l] = acc;
     }
-    b->fast_first = (int)items.size();
-    // larger levels first so the long blocks start early
-    for (int l = 0; l < nlevels; l++)
-        for (int f = 0; f < nframes; f++)
-            for (int c = 0; c < b->geoms[f][l].ncells; c++) items.push_back({f * nlevels + l, c});
-    b->fast_count = (int)items.size() - b->fast_first;
-    if (items.size() > b->items_cap) {
-        if (b->d_items) cudaFree(b->d_items);
-        b->d_items = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_items, items.size() * sizeof(WorkItem)));
-        b->items_cap = items.size();
+    b->fast_off = (int)pre.size();
+    int acc = 0;
+    for (int f = 0; f < nframes; f++)
+        for (int l = 0; l < nlevels; l++) {
+            pre.push_back(acc);
+            acc += b->cur[f]->geom[l].ncells;
+        }
+    pre.push_back(acc);
+    b->fast_count = acc;
+    if (pre.size() > b->prefix_cap) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (b->d_prefix) cudaFree(b->d_prefix);
+        b->d_prefix = nullptr;
+        const size_t cap = (size_t)(b->max_frames + 1) * nlevels + (size_t)b->max_frames * nlevels + 1;
+        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_prefix, sizeof(int) * std::max(cap, pre.size())));
+        b->prefix_cap = std::max(cap, pre.size());
     }
-    ORBGPU_CUDA_TRY(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->d_prefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, st));
     b->max_kept = 0;
     b->sort_cap = 1;
-    for (auto& g : b->geoms)
-        for (auto& L : g) {
+    for (int f = 0; f < nframes; f++)
+        for (auto& L : b->cur[f]->geom) {
             b->max_kept = std::max(b->max_kept, L.node_cap);
             while (b->sort_cap < L.node_cap) b->sort_cap <<= 1;
         }
+    b->nframes = nframes;
     b->ndesc = ndesc;
     b->sig = sig;
+    // the block-range and descriptor uploads above read pageable host
+    // memory: complete them before the host vectors change
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
     return ORBGPU_OK;
 }
 
 static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* desc) {
     cudaStream_t st = b->stream;
     int maxh = 0;
-    for (int f = 0; f < b->nframes; f++) maxh = std::max(maxh, b->geoms[f][0].h);
+    for (int f = 0; f < b->nframes; f++) maxh = std::max(maxh, b->cur[f]->geom[0].h);
     dim3 g((maxh + 7) / 8, b->nframes);
     // stage boundaries are recorded as external events (event record nodes
     // in the graph that the host can time), so the per-stage device time of
@@ -258,9 +343,10 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
     cudaEventRecordWithFlags(b->ev[1], st, cudaEventRecordExternal);
     for (int l = 0; l < b->nlevels; l++)
-        launch_resize_blur(b->d_descs, b->d_items + b->rb_first[l], b->rb_count[l], l == 0, st);
+        launch_resize_blur(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels}, b->rb_count[l],
+                           l == 0, st);
     cudaEventRecordWithFlags(b->ev[2], st, cudaEventRecordExternal);
-    launch_fast(b->d_descs, b->d_items + b->fast_first, b->fast_count, b->d_status, st);
+    launch_fast(b->d_descs, RangeMap{b->d_prefix + b->fast_off, b->ndesc, 0, 1}, b->fast_count, b->d_status, st);
     cudaEventRecordWithFlags(b->ev[3], st, cudaEventRecordExternal);
     launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->d_status, st);
     cudaEventRecordWithFlags(b->ev[4], st, cudaEventRecordExternal);
@@ -286,19 +372,24 @@ extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t*
             orbgpu_set_last_error("invalid frame in batch", __FILE__, __LINE__);
             return ORBGPU_ERR_BAD_ARG;
         }
+    cudaStream_t st = b->stream;
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));  // h_src is rewritten below
     int rc = plan_batch(b, nframes, widths, heights, nfeatures, scale_factor, nlevels, ini_th_fast, min_th_fast,
                         per_frame_capacity);
     if (rc != ORBGPU_OK) return rc;
-    cudaStream_t st = b->stream;
     // image sources of this call (read by the gather kernel at run time)
-    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
     for (int f = 0; f < nframes; f++) {
-        const LevelGeom& L0 = b->geoms[f][0];
-        b->h_src[f] = {images[f], widths[f], heights[f], (int)steps[f], b->arena + b->layouts[f].lv[0].pyr, L0.pitch};
+        const LevelGeom& L0 = b->cur[f]->geom[0];
+        b->h_src[f] = {images[f], widths[f], heights[f], (int)steps[f],
+                       b->arena + (size_t)f * b->slot_bytes + b->cur[f]->layout.lv[0].pyr, L0.pitch};
     }
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->d_src, b->h_src, sizeof(ImageSrc) * nframes, cudaMemcpyHostToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(b->d_status, 0, sizeof(int) * 4, st));
-    if (!b->graph || b->graph_kps != keypoints || b->graph_desc != descriptors) {
+    const bool graph_ok = b->graph && b->graph_sig == b->sig && b->graph_kps == keypoints && b->graph_desc == descriptors;
+    if (graph_ok) {
+        ORBGPU_CUDA_TRY(cudaGraphLaunch(b->graph, st));
+    } else if (b->same_sig_runs >= 1) {
+        // the same frame list came again: capture it once and replay from now on
         destroy_graph(b);
         cudaGraph_t g;
         ORBGPU_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -306,10 +397,13 @@ extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t*
         ORBGPU_CUDA_TRY(cudaStreamEndCapture(st, &g));
         ORBGPU_CUDA_TRY(cudaGraphInstantiate(&b->graph, g, 0));
         cudaGraphDestroy(g);
+        b->graph_sig = b->sig;
         b->graph_kps = keypoints;
         b->graph_desc = descriptors;
+        ORBGPU_CUDA_TRY(cudaGraphLaunch(b->graph, st));
+    } else {
+        enqueue_pipeline(b, keypoints, descriptors);
     }
-    ORBGPU_CUDA_TRY(cudaGraphLaunch(b->graph, st));
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(n_keypoints, b->d_totals, sizeof(int) * nframes, cudaMemcpyDeviceToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->h_pinned, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
@@ -680,7 +774,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
             hi[f].invW = static_cast<float>(ORBGPU_GRID_COLS) / static_cast<float>((float)w - 0.0f);
             hi[f].invH = static_cast<float>(ORBGPU_GRID_ROWS) / static_cast<float>((float)h - 0.0f);
             hi[f].n_cap = cap;
-            for (int l = 0; l < 16; l++) hi[f].scale[l] = l < b->nlevels ? b->tables[f].scale[l] : 1.0f;
+            for (int l = 0; l < 16; l++) hi[f].scale[l] = b->frame_scale[(size_t)f * 16 + l];
         }
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(info, hi.data(), sizeof(BatchFrameInfo) * nf, cudaMemcpyHostToDevice, st));
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_off, mp_offsets, sizeof(int) * (nf + 1), cudaMemcpyHostToDevice, st));

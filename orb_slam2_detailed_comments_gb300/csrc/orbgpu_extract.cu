@@ -300,13 +300,29 @@ int load_sincos_exceptions(const char* path) {
         return ORBGPU_ERR_BAD_ARG;
     }
     std::fclose(f);
+    // bucket offsets: first entry of every 4096-wide range of input bits
+    const uint32_t hi_bits = 0x40C90FDCu;  // just above 360 * pi / 180 as a float
+    const int nb = (int)(hi_bits >> 12) + 1;
+    std::vector<uint32_t> bk((size_t)2 * (nb + 1));
+    auto fill_buckets = [&](const uint32_t* keys, int n, uint32_t* out) {
+        int j = 0;
+        for (int b = 0; b <= nb; b++) {
+            while (j < n && (keys[j] >> 12) < (uint32_t)b) j++;
+            out[b] = (uint32_t)j;
+        }
+    };
+    fill_buckets(buf.data(), cn, bk.data());
+    fill_buckets(buf.data() + 2 * cn, sn, bk.data() + nb + 1);
+    buf.insert(buf.end(), bk.begin(), bk.end());
     if (cudaMalloc(&g_exc_dev, std::max<size_t>(4, buf.size() * 4)) != cudaSuccess) return ORBGPU_ERR_OOM;
     cudaMemcpy(g_exc_dev, buf.data(), buf.size() * 4, cudaMemcpyHostToDevice);
     const uint32_t* ck = g_exc_dev;
     const float* cv = (const float*)(g_exc_dev + cn);
     const uint32_t* sk = g_exc_dev + 2 * cn;
     const float* sv = (const float*)(g_exc_dev + 2 * cn + sn);
-    set_sincos_exceptions(ck, cv, cn, sk, sv, sn);
+    const int* cb = (const int*)(g_exc_dev + 2 * (cn + sn));
+    const int* sb = cb + nb + 1;
+    set_sincos_exceptions(ck, cv, cn, sk, sv, sn, cb, sb, nb);
     return ORBGPU_OK;
 }
 
@@ -348,7 +364,7 @@ struct SizePlan {
     std::vector<LevelGeom> geom;
     FrameLayout layout;
     uint8_t* arena = nullptr;
-    WorkItem* d_items = nullptr;
+    int* d_items = nullptr;  // block-range prefix arrays
     std::vector<int> rb_first, rb_count;
     int fast_first = 0, fast_count = 0;
     int max_kept = 0, sort_cap = 0;
@@ -410,21 +426,28 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
             return ORBGPU_ERR_CUDA;
         }
     }
-    std::vector<WorkItem> items;
+    // block ranges: per level the resize/blur tiles (one entry), then the
+    // cells of every level (one entry per level)
+    std::vector<int> pre;
     P->rb_first.assign(g.size(), 0);
     P->rb_count.assign(g.size(), 0);
     for (size_t l = 0; l < g.size(); l++) {
-        P->rb_first[l] = (int)items.size();
+        P->rb_first[l] = (int)pre.size();
         const int tiles = ((g[l].w + 63) / 64) * ((g[l].h + 15) / 16);
-        for (int i = 0; i < tiles; i++) items.push_back({(int)l, i});
+        pre.push_back(0);
+        pre.push_back(tiles);
         P->rb_count[l] = tiles;
     }
-    P->fast_first = (int)items.size();
-    for (size_t l = 0; l < g.size(); l++)
-        for (int c = 0; c < g[l].ncells; c++) items.push_back({(int)l, c});
-    P->fast_count = (int)items.size() - P->fast_first;
-    if (cudaMalloc(&P->d_items, std::max<size_t>(1, items.size()) * sizeof(WorkItem)) != cudaSuccess ||
-        cudaMemcpy(P->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice) != cudaSuccess) {
+    P->fast_first = (int)pre.size();
+    int acc = 0;
+    for (size_t l = 0; l < g.size(); l++) {
+        pre.push_back(acc);
+        acc += g[l].ncells;
+    }
+    pre.push_back(acc);
+    P->fast_count = acc;
+    if (cudaMalloc(&P->d_items, pre.size() * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(P->d_items, pre.data(), pre.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
         free_plan(P);
         return ORBGPU_ERR_OOM;
     }
@@ -595,8 +618,8 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                                                      : cudaMemcpyHostToDevice,
                                       st));
     for (int l = 0; l < nl; l++)
-        launch_resize_blur(ex->d_descs, P.d_items + P.rb_first[l], P.rb_count[l], l == 0, st);
-    launch_fast(ex->d_descs, P.d_items + P.fast_first, P.fast_count, ex->d_status, st);
+        launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, st);
+    launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, st);
     launch_distribute(ex->d_descs, nl, P.sort_cap, ex->d_status, st);
     launch_describe(ex->d_descs, nl, P.max_kept, okps, odesc, ex->d_status, st);
     ORBGPU_CUDA_TRY(cudaGetLastError());

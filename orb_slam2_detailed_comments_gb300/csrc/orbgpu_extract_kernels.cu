@@ -18,6 +18,12 @@ __device__ int g_cos_exc_n = 0;
 __device__ const uint32_t* g_sin_exc_key = nullptr;
 __device__ const float* g_sin_exc_val = nullptr;
 __device__ int g_sin_exc_n = 0;
+// bucket index (input bits >> ORBGPU_EXC_SHIFT) -> first table entry, one
+// array per table, nbuckets + 1 entries each
+#define ORBGPU_EXC_SHIFT 12
+__device__ const int* g_cos_exc_bucket = nullptr;
+__device__ const int* g_sin_exc_bucket = nullptr;
+__device__ int g_exc_nbuckets = 0;
 
 __device__ __forceinline__ int reflect101(int p, int len) {
     if (len == 1) return 0;
@@ -47,8 +53,20 @@ __device__ __forceinline__ int resize_pixel(const LevelDesc& d, int x, int y) {
 
 // Level l (l >= 1) by resizing level l-1, then the blur of level l; at
 // level 0 only the blur.  One 64x16 tile per block.
-__global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* descs, const WorkItem* items, int level0) {
-    const WorkItem it = items[blockIdx.x];
+__device__ __forceinline__ void map_item(const RangeMap& rm, int b, int& desc, int& index) {
+    int lo = 0, hi = rm.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (rm.prefix[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    desc = rm.desc0 + lo * rm.desc_stride;
+    index = b - rm.prefix[lo];
+}
+
+__global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* descs, RangeMap rm, int level0) {
+    WorkItem it;
+    map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int tiles_x = (d.w + RB_TW - 1) / RB_TW;
     const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH;
@@ -147,6 +165,18 @@ __host__ __device__ __forceinline__ int best_window_min9(const int a[16]) {
     return best;
 }
 
+// Necessary condition for a FAST corner at threshold t: two compass points
+// (dy = +3, dx = +3, dy = -3, dx = -3) four apart on the circle are both
+// brighter than v + t or both darker than v - t.
+__device__ __forceinline__ bool compass_test(const uint8_t* cp, int rw, int t) {
+    const int v = cp[0];
+    const int p0 = cp[3 * rw], p4 = cp[3], p8 = cp[-3 * rw], p12 = cp[-3];
+    const int hi = v + t, lo = v - t;
+    const bool b0 = p0 > hi, b4 = p4 > hi, b8 = p8 > hi, b12 = p12 > hi;
+    const bool d0 = p0 < lo, d4 = p4 < lo, d8 = p8 < lo, d12 = p12 < lo;
+    return ((b0 & b4) | (b4 & b8) | (b8 & b12) | (b12 & b0)) | ((d0 & d4) | (d4 & d8) | (d8 & d12) | (d12 & d0));
+}
+
 // Largest arc threshold (max over the 16 nine-pixel arcs of the smallest
 // absolute difference of consistent sign) if the pixel is a FAST corner at
 // threshold t, else 0.
@@ -177,8 +207,9 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 }
 
 #define FAST_MAX_ROI 72
-__global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, const WorkItem* items, int* status) {
-    const WorkItem it = items[blockIdx.x];
+__global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
+    WorkItem it;
+    map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int cell = it.index;
     const int i = cell / d.nCols, j = cell % d.nCols;
@@ -198,6 +229,7 @@ __global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, cons
     }
     __shared__ uint8_t roi[FAST_MAX_ROI * FAST_MAX_ROI];
     __shared__ uint8_t mstr[(FAST_MAX_ROI - 6) * (FAST_MAX_ROI - 6)];
+    __shared__ uint16_t s_queue[(FAST_MAX_ROI - 6) * (FAST_MAX_ROI - 6)];
     __shared__ int s_scan[32];
     for (int k = threadIdx.x; k < rw * rh; k += blockDim.x) {
         const int r = k / rw, c = k % rw;
@@ -207,7 +239,31 @@ __global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, cons
     const int dw = rw - 6, dh = rh - 6, nd = dw * dh;
     const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
     const int t_lo = min(ini_th, min_th);
-    for (int k = threadIdx.x; k < nd; k += blockDim.x) {
+    // Phase 1: the compass-point test (a nine-pixel arc always contains two
+    // compass points four apart) for every pixel; survivors are queued.
+    __shared__ int s_nq;
+    if (threadIdx.x == 0) s_nq = 0;
+    __syncthreads();
+    for (int k0 = 0; k0 < nd; k0 += blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        bool cand = false;
+        if (k < nd) {
+            mstr[k] = 0;
+            const int r = k / dw + 3, c = k % dw + 3;
+            cand = compass_test(roi + r * rw + c, rw, t_lo);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        int base = 0;
+        if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(&s_nq, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (cand) s_queue[base + __popc(m & ((1u << (threadIdx.x & 31)) - 1))] = (uint16_t)k;
+    }
+    __syncthreads();
+    // Phase 2: full segment test and arc strength for the queued pixels only,
+    // with every lane busy.
+    const int nq = s_nq;
+    for (int j = threadIdx.x; j < nq; j += blockDim.x) {
+        const int k = s_queue[j];
         const int r = k / dw + 3, c = k % dw + 3;
         mstr[k] = (uint8_t)arc_strength(roi, rw, r, c, t_lo);
     }
@@ -608,16 +664,15 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
 }
 
 // ---------------------------------------------------------------- describe
-__device__ __forceinline__ float lookup_exception(const uint32_t* keys, const float* vals, int n, uint32_t xb,
+// The host library's value for input bits xb if the table lists xb, else v.
+// The bucket of xb bounds the search to a handful of entries.
+__device__ __forceinline__ float lookup_exception(const uint32_t* keys, const float* vals, const int* bucket, uint32_t xb,
                                                   float v) {
-    int lo = 0, hi = n - 1;
-    while (lo <= hi) {
-        const int mid = (lo + hi) >> 1;
-        const uint32_t k = keys[mid];
-        if (k == xb) return vals[mid];
-        if (k < xb) lo = mid + 1;
-        else hi = mid - 1;
-    }
+    const uint32_t b = xb >> ORBGPU_EXC_SHIFT;
+    if (bucket == nullptr || b >= (uint32_t)g_exc_nbuckets) return v;
+    const int lo = bucket[b], hi = bucket[b + 1];
+    for (int i = lo; i < hi; i++)
+        if (keys[i] == xb) return vals[i];
     return v;
 }
 
@@ -672,8 +727,8 @@ __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, orbgpu
     sincos_taylor(ar, &sd, &cd);
     float a = __double2float_rn(cd), b = __double2float_rn(sd);
     const uint32_t xb = __float_as_uint(ar);
-    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_n, xb, a);
-    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_n, xb, b);
+    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, xb, a);
+    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, xb, b);
     const uint8_t* center = d.blur + (size_t)y * d.pitch + x;
     const int step = d.pitch;
     int val = 0;
@@ -712,7 +767,11 @@ void upload_constants(cudaStream_t st, const int* taps, const int* umax) {
     cudaMemcpyToSymbolAsync(c_pattern, kBriefPattern, sizeof(kBriefPattern), 0, cudaMemcpyHostToDevice, st);
 }
 
-void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn) {
+void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
+                           const int* cb, const int* sb, int nbuckets) {
+    cudaMemcpyToSymbol(g_cos_exc_bucket, &cb, sizeof(cb));
+    cudaMemcpyToSymbol(g_sin_exc_bucket, &sb, sizeof(sb));
+    cudaMemcpyToSymbol(g_exc_nbuckets, &nbuckets, sizeof(nbuckets));
     cudaMemcpyToSymbol(g_cos_exc_key, &ck, sizeof(ck));
     cudaMemcpyToSymbol(g_cos_exc_val, &cv, sizeof(cv));
     cudaMemcpyToSymbol(g_cos_exc_n, &cn, sizeof(cn));
@@ -721,11 +780,11 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
     cudaMemcpyToSymbol(g_sin_exc_n, &sn, sizeof(sn));
 }
 
-void launch_resize_blur(const LevelDesc* descs, const WorkItem* items, int nitems, int level0, cudaStream_t st) {
-    if (nitems > 0) k_level_resize_blur<<<nitems, 256, 0, st>>>(descs, items, level0);
+void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
+    if (nitems > 0) k_level_resize_blur<<<nitems, 256, 0, st>>>(descs, rm, level0);
 }
-void launch_fast(const LevelDesc* descs, const WorkItem* items, int nitems, int* status, cudaStream_t st) {
-    if (nitems > 0) k_fast_cells<<<nitems, 128, 0, st>>>(descs, items, status);
+void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st) {
+    if (nitems > 0) k_fast_cells<<<nitems, 128, 0, st>>>(descs, rm, status);
 }
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {
     const size_t smem = (size_t)sort_cap * sizeof(unsigned long long);
@@ -751,8 +810,8 @@ __global__ void k_sincos_probe(const float* x, int n, float* c, float* s) {
     sincos_taylor(x[i], &sd, &cd);
     float a = __double2float_rn(cd), b = __double2float_rn(sd);
     const uint32_t xb = __float_as_uint(x[i]);
-    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_n, xb, a);
-    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_n, xb, b);
+    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, xb, a);
+    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, xb, b);
     c[i] = a;
     s[i] = b;
 }

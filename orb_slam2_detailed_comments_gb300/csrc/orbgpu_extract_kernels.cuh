@@ -82,10 +82,22 @@ struct WorkItem {
     int index;
 };
 
+// The work of one launch over a list of n entries (frames, or (frame,
+// level) pairs): entry e owns blocks [prefix[e], prefix[e+1]) and uses level
+// descriptor desc0 + e * desc_stride.  Blocks find their entry by binary
+// search, so the host uploads n + 1 ints per launch instead of a block list.
+struct RangeMap {
+    const int* prefix;
+    int n;
+    int desc0;
+    int desc_stride;
+};
+
 void upload_constants(cudaStream_t st, const int* taps, const int* umax);
-void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn);
-void launch_resize_blur(const LevelDesc* descs, const WorkItem* items, int nitems, int level0, cudaStream_t st);
-void launch_fast(const LevelDesc* descs, const WorkItem* items, int nitems, int* status, cudaStream_t st);
+void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
+                           const int* cb, const int* sb, int nbuckets);
+void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st);
+void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st);
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st);

@@ -21,6 +21,9 @@
 
 namespace orbgpu {
 
+#define PROJ_ROUNDS 12
+#define PROJ_NONE 0x7f7f7f7f
+
 struct GridDev {
     const orbgpu_keypoint* kps;
     const uint8_t* desc;
@@ -332,7 +335,8 @@ __global__ void k_proj_candidates(GridDev g, const orbgpu_mappoint* mps, const u
 // Pass 2: in-order resolution (src/ORBmatcher.cc:117-180) by one warp.
 // claimed[] starts with the caller's pre-claimed keypoints.
 __global__ void k_proj_resolve(GridDev g, int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
-                               float nnratio, int* match_out, int* nmatches_out) {
+                               float nnratio, int* match_out, int* nmatches_out, const int* converged_flags) {
+    if (converged_flags && converged_flags[PROJ_ROUNDS - 1] == 0) return;
     const int lane = threadIdx.x;
     int nmatches = 0;
     for (int imp = 0; imp < m; imp++) {
@@ -377,6 +381,82 @@ __global__ void k_proj_resolve(GridDev g, int m, const int* cand_start, const in
         __syncwarp();
     }
     if (lane == 0) *nmatches_out = nmatches;
+}
+
+// Parallel resolution of the same search by fixed-point rounds (the scheme
+// of the batched search): round r evaluates every map point against the
+// claims of round r-1's results; when a round changes nothing the results
+// equal the sequential ones.  Pre-claimed keypoints (match_out == -2) are
+// always excluded.  k_proj_resolve replays serially if no round converged.
+__global__ void k_proj_round(GridDev g, int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
+                             float nnratio, int round, int* claims3, int* res, int* changed, const int* pre) {
+    const int lane = threadIdx.x & 31;
+    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    if (round > 0 && changed[round - 1] == 0) return;
+    const int n = g.n;
+    int* claims_r = claims3 + (size_t)((round + 0) % 3) * n;
+    int* claims_w = claims3 + (size_t)((round + 1) % 3) * n;
+    int* claims_z = claims3 + (size_t)((round + 2) % 3) * n;
+    for (int i = local * 32 + lane; i < n; i += nwarps * 32) claims_z[i] = PROJ_NONE;
+    if (local >= m) return;
+    const int s = cand_start[local], cnt = cand_count[local];
+    uint64_t best = ~0ull, second = ~0ull;
+    for (int b = 0; b < cnt; b += 32) {
+        uint64_t key = ~0ull;
+        if (b + lane < cnt) {
+            key = cands[s + b + lane];
+            const int idx = (int)(key & 0xFFFFF);
+            if (pre[idx] == -2 || claims_r[idx] < local || (int)(key >> 40) >= 256) key = ~0ull;
+        }
+        if (key < best) {
+            second = best;
+            best = key;
+        } else if (key < second) {
+            second = key;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
+        if (ob < best) {
+            second = best < os ? best : os;
+            best = ob;
+        } else {
+            second = second < ob ? second : ob;
+        }
+    }
+    int r = -1;
+    if (best != ~0ull) {
+        const int bestDist = (int)(best >> 40);
+        const int bestIdx = (int)(best & 0xFFFFF);
+        const int bestLevel = g.kps[bestIdx].octave;
+        const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
+        const int bestLevel2 = second == ~0ull ? -1 : g.kps[(int)(second & 0xFFFFF)].octave;
+        if (bestDist <= ORBGPU_TH_HIGH &&
+            !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
+            r = bestIdx;
+    }
+    if (lane == 0) {
+        if (res[local] != r) changed[round] = 1;
+        res[local] = r;
+        if (r >= 0) atomicMin(&claims_w[r], local);
+    }
+}
+
+// Converged rounds: write the matches; otherwise leave match_out for the
+// serial replay.
+__global__ void k_proj_finish(int m, const int* changed, const int* res, int* match_out, int* nmatches_out) {
+    if (changed[PROJ_ROUNDS - 1] != 0) return;
+    int nm = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int r = res[i];
+        if (r >= 0) {
+            match_out[r] = i;
+            nm++;
+        }
+    }
+    atomicAdd(nmatches_out, nm);
 }
 
 __global__ void k_init_match_out(const uint8_t* claimed, int n, int* match_out) {
@@ -814,8 +894,8 @@ extern "C" int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame
         return ORBGPU_ERR_BAD_ARG;
     const int n = f->n, M = n_mappoints;
     *nmatches = 0;
-    size_t est = frame_stage_bytes(f) + grid_bytes(n) + (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint) + 32 + 16) +
-                 (size_t)n * 8 + 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 64;
+    size_t est = frame_stage_bytes(f) + grid_bytes(n) + (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint) + 32 + 24) +
+                 (size_t)n * 24 + 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 64;
     for (int attempt = 0; attempt < 2; attempt++) {
         int rc = ensure_scratch(m, est);
         if (rc) return rc;
@@ -860,8 +940,22 @@ extern "C" int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame
         }
         if (rc) return rc;
         int* d_nm = b.take<int>(1);
+        int* claims3 = b.take<int>((size_t)3 * std::max(1, n));
+        int* res = b.take<int>(std::max(1, M));
+        int* changed = b.take<int>(PROJ_ROUNDS);
         ORBGPU_CUDA_TRY(cudaMemsetAsync(d_nm, 0, sizeof(int), m->stream));
-        if (M > 0) k_proj_resolve<<<1, 32, 0, m->stream>>>(g, M, start, count, keys, m->nnratio, d_match, d_nm);
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(claims3, 0x7f, sizeof(int) * (size_t)3 * std::max(1, n), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(res, 0xfe, sizeof(int) * std::max(1, M), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(changed, 0, sizeof(int) * PROJ_ROUNDS, m->stream));
+        if (M > 0) {
+            const int wpb = 8;
+            const int warps = std::max(M, (n + 31) / 32);
+            for (int r = 0; r < PROJ_ROUNDS; r++)
+                k_proj_round<<<(warps + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, M, start, count, keys, m->nnratio, r,
+                                                                                claims3, res, changed, d_match);
+            k_proj_finish<<<1, 256, 0, m->stream>>>(M, changed, res, d_match, d_nm);
+            k_proj_resolve<<<1, 32, 0, m->stream>>>(g, M, start, count, keys, m->nnratio, d_match, d_nm, changed);
+        }
         ORBGPU_CUDA_TRY(cudaGetLastError());
         if (mem != ORBGPU_MEM_DEVICE && n > 0)
             ORBGPU_CUDA_TRY(cudaMemcpyAsync(match_out, d_match, sizeof(int) * n, cudaMemcpyDeviceToHost, m->stream));

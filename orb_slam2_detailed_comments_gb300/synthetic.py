@@ -129,3 +129,16 @@ def clustered_descriptors(n: int, n_centres: int, flip_p: float, seed: int) -> n
     bits = rng.random(size=(n, 256)) < flip_p
     flips = np.packbits(bits, axis=1, bitorder="little")
     return centres[pick] ^ flips
+
+
+def stream_frames(w: int, h: int, seed: int, nframes: int, noise_sigma: float = 2.0):
+    """A camera stream: frame k is the stream's scene under a drifting
+    homography (random walk of small rotations / translations) + noise."""
+    base = scene(w, h, seed)
+    rng = np.random.default_rng(seed + 4242)
+    H = np.eye(3)
+    out = []
+    for k in range(nframes):
+        out.append(warp(base, H, seed * 7919 + k, noise_sigma))
+        H = random_homography(w, h, rng, max_rot_deg=1.0, max_shift=3.0) @ H
+    return out
