@@ -245,22 +245,43 @@ def run_ours(args):
     e2e_value = NFRAMES * args.steps / sum(e2e_times)
 
     # per-frame plain path on the same frames (the drop-in path), for the batching gain
-    ex = ORBextractor(2000, 1.2, 8, 20, 7, 1280, 720)
     matcher = ORBmatcher(0.8, True)
-    sc = ex.GetScaleFactors()
-    per_frame_ms = []
     exs = {nf: ORBextractor(nf, 1.2, 8, 20, 7, 1280, 720) for nf in NFEATURES}
-    for rep in range(2):
+    sc = exs[NFEATURES[0]].GetScaleFactors()
+    mps_d = [torch.from_numpy(m.view(np.uint8)).to(dev) for m in mps_list]
+    mpd_d = [torch.from_numpy(m).to(dev) for m in mpd_list]
+    per_frame_ms, ext_ms = [], []
+    for rep in range(3):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        te = 0.0
         for f, (img, nf) in enumerate(frames):
+            a = time.perf_counter()
             k, d = exs[nf](imgs_dev[f], device_out=True)
+            te += time.perf_counter() - a
             F = FrameView(k, d, img.shape[1], img.shape[0], sc)
-            matcher.SearchByProjection(F, torch.from_numpy(mps_list[f].view(np.uint8)).to(dev),
-                                       torch.from_numpy(mpd_list[f]).to(dev), TH)
+            matcher.SearchByProjection(F, mps_d[f], mpd_d[f], TH)
         torch.cuda.synchronize()
         per_frame_ms.append((time.perf_counter() - t0) * 1e3)
-    per_frame_fps = NFRAMES / (min(per_frame_ms) / 1e3)
+        ext_ms.append(te * 1e3)
+    best = int(np.argmin(per_frame_ms))
+    per_frame_fps = NFRAMES / (per_frame_ms[best] / 1e3)
+    per_frame_split = {"extract_ms_per_frame": ext_ms[best] / NFRAMES,
+                       "match_ms_per_frame": (per_frame_ms[best] - ext_ms[best]) / NFRAMES}
+
+    extra = {}
+    try:
+        extra["stereo_1241x376"] = bench_stereo(dev)
+    except Exception as e:  # reported, not fatal
+        extra["stereo_1241x376"] = {"error": repr(e)}
+    try:
+        extra["knn_50kx200k"] = bench_knn(dev)
+    except Exception as e:
+        extra["knn_50kx200k"] = {"error": repr(e)}
+    try:
+        extra["serving_32_streams"] = bench_serving(dev)
+    except Exception as e:
+        extra["serving_32_streams"] = {"error": repr(e)}
 
     # roofline of the dominant stage
     pk, pk_src = peaks()
@@ -284,10 +305,93 @@ def run_ours(args):
                                "1280x720, nFeatures 1000/1500/2000, 3000 map points per frame, radius 15*scale",
                    "frames_per_step": NFRAMES, "l2": "flushed (256 MiB write) between timed steps"},
         "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "per_frame_path_fps": per_frame_fps, "batched_over_per_frame": value / per_frame_fps,
+        "per_frame_path_fps": per_frame_fps, "per_frame_split": per_frame_split,
+        "batched_over_per_frame": value / per_frame_fps, "other_configs": extra,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
     }
     print(json.dumps(line))
+
+
+def bench_stereo(dev):
+    """Stereo plain path (1241x376, nFeatures 2000): left + right extraction and
+    ComputeStereoMatches per frame pair, bf 386.1, fx 718.856."""
+    import torch
+    from orb_slam2_detailed_comments_gb300 import ORBextractor, ORBmatcher, FrameView, compute_stereo_matches
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    left, right, _ = syn.stereo_pair(1241, 376, 1)
+    L, R = torch.from_numpy(left).to(dev), torch.from_numpy(right).to(dev)
+    exL, exR = ORBextractor(2000, 1.2, 8, 20, 7, 1241, 376), ORBextractor(2000, 1.2, 8, 20, 7, 1241, 376)
+    m = ORBmatcher(0.75, True)
+    sc = exL.GetScaleFactors()
+
+    def once():
+        kl, dl = exL(L, device_out=True)
+        kr, dr = exR(R, device_out=True)
+        return compute_stereo_matches(m, exL, exR, FrameView(kl, dl, 1241, 376, sc), FrameView(kr, dr, 1241, 376, sc),
+                                      386.1, 718.856)
+    for _ in range(3):
+        once()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n = 30
+    for _ in range(n):
+        ur, _ = once()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    return {"frames_per_s": n / el, "ms_per_frame": el / n * 1e3, "matched": int((ur > 0).sum().item())}
+
+
+def bench_knn(dev):
+    """Brute-force k=2 Hamming kNN, 50,000 x 200,000 (uniform and clustered bits)."""
+    import torch
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    m = ORBmatcher()
+    out = {}
+    for name, q, t in (("uniform", syn.random_descriptors(50000, 1), syn.random_descriptors(200000, 2)),
+                       ("clustered", syn.clustered_descriptors(50000, 2000, 0.1, 3),
+                        syn.clustered_descriptors(200000, 2000, 0.1, 4))):
+        qd, td = torch.from_numpy(q).to(dev), torch.from_numpy(t).to(dev)
+        m.knn2(qd, td)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        reps = 3
+        for _ in range(reps):
+            m.knn2(qd, td)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"ms": ms, "pairs_per_s": 5e4 * 2e5 / (ms / 1e3), "algo": "popc"}
+    return out
+
+
+def bench_serving(dev, duration_s=3.0):
+    """32 camera streams, Poisson 30 Hz each, mixed 640x480/1241x376/1280x720,
+    nFeatures 1000-2000, extraction + frame-to-previous-frame matching,
+    continuous batching, 40 GB admission budget."""
+    import torch
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    from orb_slam2_detailed_comments_gb300.serving import ServingEngine, latency_stats, poisson_arrivals
+    rng = np.random.default_rng(5)
+    res_opts = [(640, 480), (1241, 376), (1280, 720)]
+    e = ServingEngine(max_batch=64, hbm_budget_bytes=40 << 30)
+    frames = {}
+    for s in range(32):
+        w, h = res_opts[rng.integers(0, 3)]
+        nf = int(rng.choice([1000, 1500, 2000]))
+        if e.admit(s, w, h, nf):
+            frames[s] = [torch.from_numpy(f).to(dev) for f in syn.stream_frames(w, h, 700 + s, 2)]
+    arr = poisson_arrivals(32, 30.0, duration_s, seed=9)
+    # warm-up pass (plans, graphs)
+    e.serve(arr[:64], lambda s, k: frames[s][k % 2], 0.3)
+    t0 = time.perf_counter()
+    res = e.serve(arr, lambda s, k: frames[s][k % 2], duration_s)
+    el = time.perf_counter() - t0
+    st = latency_stats(res)
+    st.update({"frames_per_s": len(res) / el, "offered_frames_per_s": 32 * 30.0, "streams_admitted": len(frames),
+               "hbm_budget_gb": 40})
+    return st
 
 
 def cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1):
