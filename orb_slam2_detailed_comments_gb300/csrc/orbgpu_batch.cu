@@ -331,27 +331,33 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     return ORBGPU_OK;
 }
 
-static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* desc) {
+static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* desc, bool capturing) {
     cudaStream_t st = b->stream;
+    // inside a capture the stage events become external event nodes (timed by
+    // the host on every replay); outside, plain records
+    auto mark = [&](int i) {
+        if (capturing) cudaEventRecordWithFlags(b->ev[i], st, cudaEventRecordExternal);
+        else cudaEventRecord(b->ev[i], st);
+    };
     int maxh = 0;
     for (int f = 0; f < b->nframes; f++) maxh = std::max(maxh, b->cur[f]->geom[0].h);
     dim3 g((maxh + 7) / 8, b->nframes);
     // stage boundaries are recorded as external events (event record nodes
     // in the graph that the host can time), so the per-stage device time of
     // every replay can be read back
-    cudaEventRecordWithFlags(b->ev[0], st, cudaEventRecordExternal);
+    mark(0);
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
-    cudaEventRecordWithFlags(b->ev[1], st, cudaEventRecordExternal);
+    mark(1);
     for (int l = 0; l < b->nlevels; l++)
         launch_resize_blur(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels}, b->rb_count[l],
                            l == 0, st);
-    cudaEventRecordWithFlags(b->ev[2], st, cudaEventRecordExternal);
+    mark(2);
     launch_fast(b->d_descs, RangeMap{b->d_prefix + b->fast_off, b->ndesc, 0, 1}, b->fast_count, b->d_status, st);
-    cudaEventRecordWithFlags(b->ev[3], st, cudaEventRecordExternal);
+    mark(3);
     launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->d_status, st);
-    cudaEventRecordWithFlags(b->ev[4], st, cudaEventRecordExternal);
+    mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
-    cudaEventRecordWithFlags(b->ev[5], st, cudaEventRecordExternal);
+    mark(5);
     b->launches_per_run = 1 + b->nlevels + 3;
 }
 
@@ -393,7 +399,7 @@ extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t*
         destroy_graph(b);
         cudaGraph_t g;
         ORBGPU_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        enqueue_pipeline(b, keypoints, descriptors);
+        enqueue_pipeline(b, keypoints, descriptors, true);
         ORBGPU_CUDA_TRY(cudaStreamEndCapture(st, &g));
         ORBGPU_CUDA_TRY(cudaGraphInstantiate(&b->graph, g, 0));
         cudaGraphDestroy(g);
@@ -402,8 +408,9 @@ extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t*
         b->graph_desc = descriptors;
         ORBGPU_CUDA_TRY(cudaGraphLaunch(b->graph, st));
     } else {
-        enqueue_pipeline(b, keypoints, descriptors);
+        enqueue_pipeline(b, keypoints, descriptors, false);
     }
+    ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(n_keypoints, b->d_totals, sizeof(int) * nframes, cudaMemcpyDeviceToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->h_pinned, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
