@@ -191,7 +191,7 @@ static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out
     P->tiles.assign(b->nlevels, 0);
     for (int l = 0; l < b->nlevels; l++) {
         const LevelGeom& L = P->geom[l];
-        P->tiles[l] = ((L.w + 63) / 64) * ((L.h + 15) / 16);
+        P->tiles[l] = resize_blur_tiles(L.w, L.h);
         if (l == 0) continue;
         const LevelOffsets& o = P->layout.lv[l];
         const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * L.h;

@@ -433,7 +433,7 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     P->rb_count.assign(g.size(), 0);
     for (size_t l = 0; l < g.size(); l++) {
         P->rb_first[l] = (int)pre.size();
-        const int tiles = ((g[l].w + 63) / 64) * ((g[l].h + 15) / 16);
+        const int tiles = resize_blur_tiles(g[l].w, g[l].h);
         pre.push_back(0);
         pre.push_back(tiles);
         P->rb_count[l] = tiles;

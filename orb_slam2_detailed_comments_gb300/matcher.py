@@ -111,7 +111,12 @@ class ORBmatcher:
             mps = np.ascontiguousarray(mappoints, MAPPOINT_DTYPE)
             mpd = np.ascontiguousarray(mp_descriptors, np.uint8)
             cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
-        check(lib().orbgpu_search_by_projection(self._h, C.byref(s), ptr(mps), ptr(mpd), int(len(mps)),
+        # the map point count comes from the descriptor rows (M x 32), so a raw
+        # byte view of the records cannot be mistaken for more map points
+        n_mp = int(mpd.shape[0])
+        if (mps.nbytes if isinstance(mps, np.ndarray) else mps.numel() * mps.element_size()) < n_mp * 32:
+            raise ValueError("mappoints buffer holds fewer records than mp_descriptors rows")
+        check(lib().orbgpu_search_by_projection(self._h, C.byref(s), ptr(mps), ptr(mpd), n_mp,
                                                 C.c_float(th), ptr(cl), ptr(out), MEM_DEVICE if dev else MEM_HOST,
                                                 C.byref(nm)),
               "orbgpu_search_by_projection")

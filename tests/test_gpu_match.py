@@ -154,3 +154,22 @@ def test_descriptor_distance_kat(torch, golden):
     b = np.tile(p, (n, 1))
     d = ORBmatcher.DescriptorDistance(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
     assert np.array_equal(d.cpu().numpy().reshape(n, n), g["distance"])
+
+
+def test_projection_device_inputs(torch, oracle):
+    """Device-resident frame, map point records as raw bytes and descriptors."""
+    from orb_slam2_detailed_comments_gb300 import ORBextractor, ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    rng = np.random.default_rng(21)
+    img = syn.scene(1241, 376, 21)
+    ex = ORBextractor(2000, 1.2, 8, 20, 7)
+    k, d = ex(torch.from_numpy(img).cuda(), device_out=True)
+    kh = k.cpu().numpy().view(pyoracle.KP_DTYPE).reshape(-1)
+    dh = d.cpu().numpy()
+    mps, mpd = make_mappoints(kh, dh, 2500, rng)
+    r = oracle.search_by_projection(kh, dh, 1241, 376, mps, mpd, th=6.0, nnratio=0.8)
+    m = ORBmatcher(0.8, True)
+    nm, match = m.SearchByProjection(frame(k, d, 1241, 376), torch.from_numpy(mps.view(np.uint8)).cuda(),
+                                     torch.from_numpy(mpd).cuda(), 6.0)
+    assert nm == r[0]
+    assert np.array_equal(match.cpu().numpy(), r[1])
