@@ -383,7 +383,11 @@ def bench_serving(dev, duration_s=3.0):
         if e.admit(s, w, h, nf):
             frames[s] = [torch.from_numpy(f).to(dev) for f in syn.stream_frames(w, h, 700 + s, 2)]
     arr = poisson_arrivals(32, 30.0, duration_s, seed=9)
-    # warm-up pass (plans, graphs)
+    # warm-up: every (resolution, nFeatures) configuration is planned once,
+    # then a short replay
+    for (w, h) in res_opts:
+        for nf in (1000, 1500, 2000):
+            e.warm(w, h, nf)
     e.serve(arr[:64], lambda s, k: frames[s][k % 2], 0.3)
     t0 = time.perf_counter()
     res = e.serve(arr, lambda s, k: frames[s][k % 2], duration_s)

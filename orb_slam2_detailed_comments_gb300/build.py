@@ -31,6 +31,7 @@ SOURCES = [
     "orbgpu_batch.cu",
     "orbgpu_match.cu",
     "orbgpu_knn.cu",
+    "orbgpu_knn_tc.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -105,136 +105,6 @@ __global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* desc
     }
 }
 
-// Row-cached variant: one 128x32 output tile per block.  The source rows and
-// columns the tile (plus the 3-pixel blur halo) needs are staged once in
-// shared memory; the horizontal pass is computed once per staged source row,
-// the vertical pass per tile row, then the separable blur.  Falls back to
-// the per-pixel kernel above when the staged window would not fit (scale
-// factors above ~1.5).
-#define RB2_TW 128
-#define RB2_TH 32
-#define RB2_CW (RB2_TW + 2 * RB_HALO)   // 134 tile columns with halo
-#define RB2_CH (RB2_TH + 2 * RB_HALO)   // 38 tile rows with halo
-#define RB2_SW 208                      // staged source columns
-#define RB2_SH 64                       // staged source rows
-
-struct RB2Smem {
-    int sxofs[RB2_CW];
-    short sa0[RB2_CW], sa1[RB2_CW];
-    int syofs[RB2_CH];
-    short sb0[RB2_CH], sb1[RB2_CH];
-    int xlo, xhi, ylo, yhi, fit;
-    uint8_t tile[RB2_CH][RB2_CW];
-    union {
-        uint8_t src[RB2_SH][RB2_SW];
-        int rows[RB2_CH][RB2_TW];
-    } u;
-    int hpass[RB2_SH][RB2_CW];
-};
-
-__global__ void __launch_bounds__(256) k_level_resize_blur2(const LevelDesc* descs, RangeMap rm, int level0) {
-    extern __shared__ __align__(16) unsigned char rb2_raw[];
-    RB2Smem& S = *reinterpret_cast<RB2Smem*>(rb2_raw);
-    WorkItem it;
-    map_item(rm, blockIdx.x, it.desc, it.index);
-    const LevelDesc& d = descs[it.desc];
-    const int tiles_x = (d.w + RB2_TW - 1) / RB2_TW;
-    const int ox = (it.index % tiles_x) * RB2_TW, oy = (it.index / tiles_x) * RB2_TH;
-    const int tid = threadIdx.x;
-    if (level0) {
-        for (int i = tid; i < RB2_CW * RB2_CH; i += blockDim.x) {
-            const int ty = i / RB2_CW, tx = i % RB2_CW;
-            const int x = reflect101(ox - RB_HALO + tx, d.w), y = reflect101(oy - RB_HALO + ty, d.h);
-            S.tile[ty][tx] = d.dst[(size_t)y * d.pitch + x];
-        }
-        __syncthreads();
-    } else {
-        if (tid == 0) {
-            S.xlo = 0x7fffffff; S.xhi = -1; S.ylo = 0x7fffffff; S.yhi = -1;
-        }
-        __syncthreads();
-        // per-column and per-row coefficients of the (reflected) tile coordinates
-        for (int j = tid; j < RB2_CW; j += blockDim.x) {
-            const int x = reflect101(ox - RB_HALO + j, d.w);
-            const int sx = d.xofs[x];
-            S.sxofs[j] = sx;
-            S.sa0[j] = d.xalpha[2 * x];
-            S.sa1[j] = d.xalpha[2 * x + 1];
-            atomicMin(&S.xlo, sx);
-            atomicMax(&S.xhi, min(sx + 1, d.sw - 1));
-        }
-        for (int i = tid; i < RB2_CH; i += blockDim.x) {
-            const int y = reflect101(oy - RB_HALO + i, d.h);
-            const int sy = d.yofs[y];
-            S.syofs[i] = sy;
-            S.sb0[i] = d.ybeta[2 * y];
-            S.sb1[i] = d.ybeta[2 * y + 1];
-            atomicMin(&S.ylo, min(max(sy, 0), d.sh - 1));
-            atomicMax(&S.yhi, min(max(sy + 1, 0), d.sh - 1));
-        }
-        __syncthreads();
-        const int xlo = S.xlo, ylo = S.ylo;
-        const int sw = S.xhi - xlo + 1, sh = S.yhi - ylo + 1;
-        if (sw > RB2_SW || sh > RB2_SH) {
-            // window too large for the staging buffers: per-pixel path
-            for (int i = tid; i < RB2_CW * RB2_CH; i += blockDim.x) {
-                const int ty = i / RB2_CW, tx = i % RB2_CW;
-                S.tile[ty][tx] = (uint8_t)resize_pixel(d, reflect101(ox - RB_HALO + tx, d.w), reflect101(oy - RB_HALO + ty, d.h));
-            }
-            __syncthreads();
-        } else {
-            // stage the source window (row segments, coalesced)
-            for (int i = tid; i < sw * sh; i += blockDim.x) {
-                const int r = i / sw, c = i % sw;
-                S.u.src[r][c] = d.src[(size_t)(ylo + r) * d.spitch + xlo + c];
-            }
-            __syncthreads();
-            // horizontal pass once per staged source row
-            for (int i = tid; i < sh * RB2_CW; i += blockDim.x) {
-                const int r = i / RB2_CW, j = i % RB2_CW;
-                const int sx = S.sxofs[j] - xlo;
-                const int sx1 = min(S.sxofs[j] + 1, d.sw - 1) - xlo;
-                S.hpass[r][j] = S.u.src[r][sx] * S.sa0[j] + S.u.src[r][sx1] * S.sa1[j];
-            }
-            __syncthreads();
-            // vertical pass per tile row
-            for (int i = tid; i < RB2_CH * RB2_CW; i += blockDim.x) {
-                const int ty = i / RB2_CW, tx = i % RB2_CW;
-                const int sy = S.syofs[ty];
-                const int r0 = min(max(sy, 0), d.sh - 1) - ylo, r1 = min(max(sy + 1, 0), d.sh - 1) - ylo;
-                const int v = (S.hpass[r0][tx] * S.sb0[ty] + S.hpass[r1][tx] * S.sb1[ty] + (1 << 21)) >> 22;
-                S.tile[ty][tx] = (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
-            }
-            __syncthreads();
-        }
-        // the level itself
-        for (int i = tid; i < RB2_TW * RB2_TH; i += blockDim.x) {
-            const int ty = i / RB2_TW, tx = i % RB2_TW;
-            const int gx = ox + tx, gy = oy + ty;
-            if (gx < d.w && gy < d.h) d.dst[(size_t)gy * d.pitch + gx] = S.tile[ty + RB_HALO][tx + RB_HALO];
-        }
-    }
-    // separable 7x7 blur of the tile (taps from constant memory)
-    for (int i = tid; i < RB2_TW * RB2_CH; i += blockDim.x) {
-        const int ty = i / RB2_TW, tx = i % RB2_TW;
-        int acc = 0;
-#pragma unroll
-        for (int k = 0; k < 7; k++) acc += c_gauss_taps[k] * S.tile[ty][tx + k];
-        S.u.rows[ty][tx] = acc;
-    }
-    __syncthreads();
-    for (int i = tid; i < RB2_TW * RB2_TH; i += blockDim.x) {
-        const int ty = i / RB2_TW, tx = i % RB2_TW;
-        const int gx = ox + tx, gy = oy + ty;
-        if (gx >= d.w || gy >= d.h) continue;
-        int acc = 0;
-#pragma unroll
-        for (int k = 0; k < 7; k++) acc += c_gauss_taps[k] * S.u.rows[ty + k][tx];
-        acc = (acc + (1 << 15)) >> 16;
-        d.blur[(size_t)gy * d.pitch + gx] = (uint8_t)(acc < 0 ? 0 : (acc > 255 ? 255 : acc));
-    }
-}
-
 // ---------------------------------------------------------------- FAST
 // The 16 pixels of the radius-3 Bresenham circle in cyclic order, as
 // offsets from the centre for a row stride 'rw': (dx, dy) = (0,3) (1,3)
@@ -920,17 +790,11 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
 }
 
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
-    static bool attr_set = false;
-    const size_t smem = sizeof(RB2Smem);
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_level_resize_blur2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
-    if (nitems > 0) k_level_resize_blur2<<<nitems, 256, smem, st>>>(descs, rm, level0);
+    if (nitems > 0) k_level_resize_blur<<<nitems, 256, 0, st>>>(descs, rm, level0);
 }
 
-// Blocks of k_level_resize_blur2 for a w x h level.
-int resize_blur_tiles(int w, int h) { return ((w + RB2_TW - 1) / RB2_TW) * ((h + RB2_TH - 1) / RB2_TH); }
+// Blocks of k_level_resize_blur for a w x h level.
+int resize_blur_tiles(int w, int h) { return ((w + RB_TW - 1) / RB_TW) * ((h + RB_TH - 1) / RB_TH); }
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st) {
     if (nitems > 0) k_fast_cells<<<nitems, 128, 0, st>>>(descs, rm, status);
 }

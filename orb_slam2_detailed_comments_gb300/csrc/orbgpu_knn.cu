@@ -84,12 +84,21 @@ __global__ void k_knn_merge(const int4* __restrict__ partial, int nq, int nslice
 
 using namespace orbgpu;
 
+void knn_merge_launch(const int4* partial, int nq, int nslices, int* idx1, int* d1, int* idx2, int* d2,
+                      cudaStream_t st) {
+    k_knn_merge<<<(nq + 255) / 256, 256, 0, st>>>(partial, nq, nslices, idx1, d1, idx2, d2);
+}
+
+int orbgpu_knn2_tc(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
+                   int* idx2, int* d2);
+
 extern "C" int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1,
                            int* d1, int* idx2, int* d2, int algo) {
     if (!m || nq < 0 || nt < 0 || (nq > 0 && (!query || !idx1 || !d1 || !idx2 || !d2)) || (nt > 0 && !train) ||
-        algo != 0)
+        (algo != 0 && algo != 1))
         return ORBGPU_ERR_BAD_ARG;
     if (nq == 0) return ORBGPU_OK;
+    if (algo == 1) return orbgpu_knn2_tc(m, query, nq, train, nt, idx1, d1, idx2, d2);
     cudaStream_t st = orbgpu_matcher_stream_internal(m);
     int dev, nsm;
     ORBGPU_CUDA_TRY(cudaGetDevice(&dev));

@@ -48,10 +48,16 @@ class Result:
 
 
 class ServingEngine:
-    """Admission by HBM budget, per-stream device state, continuous batching."""
+    """Admission by HBM budget, per-stream device state, continuous batching.
+
+    Every admitted stream owns a row block of two device arrays that hold its
+    previous frame's keypoints and descriptors; after each batch one
+    index_copy moves the batch's outputs into the streams' blocks, and the
+    next batch's map points are gathered from them with one index_select."""
 
     def __init__(self, max_batch: int = 64, max_width: int = 1280, max_height: int = 720, max_nfeatures: int = 2000,
-                 hbm_budget_bytes: int = 40 << 30, th: float = 6.0, nnratio: float = 0.8, keep_outputs: bool = False):
+                 hbm_budget_bytes: int = 40 << 30, th: float = 6.0, nnratio: float = 0.8, keep_outputs: bool = False,
+                 max_streams: int = 64):
         import torch
         self.torch = torch
         self.batch = BatchExtractor(max_batch, max_width, max_height, max_nfeatures)
@@ -64,23 +70,32 @@ class ServingEngine:
         self.streams: dict[int, StreamState] = {}
         self.keep_outputs = keep_outputs
         self.rejected: list[int] = []
+        self.max_streams = max_streams
+        self.free_slots = list(range(max_streams))
+        self.slot_of: dict[int, int] = {}
+        # previous-frame state of every stream slot, as map point records and descriptors
+        self.state_rec = torch.zeros((max_streams * self.cap, 8), dtype=torch.int32, device="cuda")
+        self.state_desc = torch.zeros((max_streams * self.cap, 32), dtype=torch.uint8, device="cuda")
+        self.prev_n = np.zeros(max_streams, np.int64)
+        self._col = torch.arange(self.cap, device="cuda", dtype=torch.int64)
+        self._bstream = torch.cuda.ExternalStream(self.batch.stream)
 
     # ---------------------------------------------------------------- admission
     def stream_bytes(self, w: int, h: int) -> int:
-        # previous keypoints + descriptors, staging of one image and its share
-        # of the batch arena (pyramid + blurred pyramid, ~2 * 3.1 * w * h)
-        return self.cap * (28 + 32) + w * h + int(2 * 3.1 * w * h) + 64 * 1024
+        # previous keypoints (as records) + descriptors, staging of one image and
+        # its share of the batch arena (pyramid + blurred pyramid, ~2 * 3.1 * w * h)
+        return self.cap * (32 + 32) + w * h + int(2 * 3.1 * w * h) + 64 * 1024
 
     def admit(self, sid: int, width: int, height: int, nfeatures: int) -> bool:
         need = self.stream_bytes(width, height)
-        if self.used + need > self.budget:
+        if self.used + need > self.budget or not self.free_slots:
             self.rejected.append(sid)
             return False
-        t = self.torch
         st = StreamState(sid, width, height, nfeatures, need)
-        st.prev_kps = t.zeros((self.cap, 7), dtype=t.float32, device="cuda")
-        st.prev_desc = t.zeros((self.cap, 32), dtype=t.uint8, device="cuda")
         self.streams[sid] = st
+        slot = self.free_slots.pop(0)
+        self.slot_of[sid] = slot
+        self.prev_n[slot] = 0
         self.used += need
         return True
 
@@ -88,43 +103,56 @@ class ServingEngine:
         st = self.streams.pop(sid, None)
         if st:
             self.used -= st.resident_bytes
+            slot = self.slot_of.pop(sid)
+            self.free_slots.append(slot)
+
+    def warm(self, width: int, height: int, nfeatures: int, reps: int = 2) -> None:
+        """Runs one frame of a configuration through the pipeline so its plan
+        exists before requests arrive."""
+        t = self.torch
+        img = t.zeros((height, width), dtype=t.uint8, device="cuda")
+        for _ in range(reps):
+            self.batch.extract([img], [nfeatures])
 
     # ---------------------------------------------------------------- one batch
-    def _mappoints(self, st: StreamState):
-        """The previous frame's keypoints as map-point records (device)."""
-        t = self.torch
-        n = st.prev_n
-        rec = t.zeros((n, 8), dtype=t.int32, device="cuda")
-        k = st.prev_kps[:n]
-        rec[:, 0] = k[:, 0].contiguous().view(t.int32)
-        rec[:, 1] = k[:, 1].contiguous().view(t.int32)
-        rec[:, 2] = t.full((n,), -1.0, dtype=t.float32, device="cuda").view(t.int32)
-        rec[:, 3] = t.ones((n,), dtype=t.float32, device="cuda").view(t.int32)
-        rec[:, 4] = k[:, 5].contiguous().view(t.int32)  # octave
-        rec[:, 5] = 1  # in view
-        return rec, st.prev_desc[:n]
-
     def run_batch(self, requests):
-        """requests: list of (sid, image CUDA tensor, arrival time).  Returns Results."""
+        """requests: list of (sid, image CUDA tensor, arrival time), at most one
+        per stream.  Returns Results."""
         t = self.torch
+        cap = self.cap
         imgs = [img for _, img, _ in requests]
         nfs = [self.streams[sid].nfeatures for sid, _, _ in requests]
+        slots = np.array([self.slot_of[sid] for sid, _, _ in requests], np.int64)
         kps, desc, counts = self.batch.extract(imgs, nfs)
-        # frame-to-previous-frame matching for frames whose stream has a previous frame
-        recs, descs, mcount = [], [], []
-        for sid, _, _ in requests:
-            st = self.streams[sid]
-            if st.prev_n > 0:
-                r, d = self._mappoints(st)
-            else:
-                r = t.zeros((0, 8), dtype=t.int32, device="cuda")
-                d = t.zeros((0, 32), dtype=t.uint8, device="cuda")
-            recs.append(r)
-            descs.append(d)
-            mcount.append(int(r.shape[0]))
-        mp = t.cat(recs).view(t.uint8).contiguous() if sum(mcount) else t.zeros(8 * 4, dtype=t.uint8, device="cuda")
-        md = t.cat(descs).contiguous() if sum(mcount) else t.zeros((1, 32), dtype=t.uint8, device="cuda")
+        # map points of every frame: its stream's previous keypoints (identity motion)
+        mcount = [int(self.prev_n[s]) for s in slots]
+        rows = np.concatenate([s * cap + np.arange(n, dtype=np.int64) for s, n in zip(slots, mcount)]) \
+            if sum(mcount) else np.zeros(0, np.int64)
+        if len(rows):
+            ridx = t.from_numpy(rows).to("cuda", non_blocking=True)
+            mp = t.index_select(self.state_rec, 0, ridx).view(t.uint8).contiguous()
+            md = t.index_select(self.state_desc, 0, ridx).contiguous()
+        else:
+            mp = t.zeros(32, dtype=t.uint8, device="cuda")
+            md = t.zeros((1, 32), dtype=t.uint8, device="cuda")
+        # the gathers above run on torch's stream, the search on the batch's
+        ev = t.cuda.Event()
+        ev.record()
+        self._bstream.wait_event(ev)
         match, nm = self.proj.search(mp, md, mcount, self.th)
+        # this batch's keypoints become the streams' map point records
+        nb = len(requests)
+        k = kps[: nb * cap]
+        rec = t.empty((nb * cap, 8), dtype=t.int32, device="cuda")
+        rec[:, 0:2] = k[:, 0:2].contiguous().view(t.int32)
+        rec[:, 2] = -1082130432  # -1.0f: no right coordinate
+        rec[:, 3] = 1065353216   # 1.0f: viewing cosine
+        rec[:, 4] = k[:, 5].contiguous().view(t.int32)  # octave -> predicted level
+        rec[:, 5] = 1
+        rec[:, 6:8] = 0
+        dst = (t.from_numpy(slots).to("cuda", non_blocking=True)[:, None] * cap + self._col[None, :]).reshape(-1)
+        self.state_rec.index_copy_(0, dst, rec)
+        self.state_desc.index_copy_(0, dst, desc[: nb * cap])
         counts_h = counts.cpu().numpy()
         nm_h = nm.cpu().numpy()
         done = time.perf_counter()
@@ -132,13 +160,11 @@ class ServingEngine:
         for f, (sid, _, arrival) in enumerate(requests):
             st = self.streams[sid]
             n = int(counts_h[f])
-            lo = f * self.cap
-            st.prev_kps[:n].copy_(kps[lo:lo + n])
-            st.prev_desc[:n].copy_(desc[lo:lo + n])
-            st.prev_n = n
+            self.prev_n[slots[f]] = n
             st.frames += 1
             r = Result(sid, arrival, done, n, int(nm_h[f]) if mcount[f] else 0)
             if self.keep_outputs:
+                lo = f * cap
                 r.keypoints = kps[lo:lo + n].cpu().numpy().view(KEYPOINT_DTYPE).reshape(-1)
                 r.descriptors = desc[lo:lo + n].cpu().numpy()
                 r.matches = match[lo:lo + n].cpu().numpy()
@@ -174,12 +200,10 @@ class ServingEngine:
                         batch.append(r)
                 pending = rest
                 results.extend(self.run_batch(batch))
-            elif i >= len(arrivals) or now > duration_s:
+            elif i >= len(arrivals):
                 break
             else:
-                time.sleep(max(0.0, min(0.0005, arrivals[i][0] - now)))
-            if now > duration_s and not pending and i >= len(arrivals):
-                break
+                time.sleep(max(0.0, min(0.0002, arrivals[i][0] - now)))
         return results
 
 
