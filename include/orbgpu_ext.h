@@ -1,0 +1,77 @@
+/* orbgpu_ext.h -- entry points of liborbgpu.so beyond the reference's
+ * interfaces: the batched projection search that follows
+ * orbgpu_batch_extract, batch instrumentation, and the stage accessors and
+ * kernels that the stage tests drive.  None of these has a counterpart in
+ * ORB-SLAM2; the reference-facing entry points are in orbgpu.h.
+ * Return codes are orbgpu_status values. */
+#ifndef ORBGPU_EXT_H
+#define ORBGPU_EXT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "orbgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ batched projection search */
+/* SearchByProjection(Frame&, vector<MapPoint*>, th) (src/ORBmatcher.cc:72-183)
+ * for every frame of the last orbgpu_batch_extract call, in one pass.
+ * kps / desc / counts: that call's device outputs.  mappoints /
+ * mp_descriptors: all frames' map points back to back (device), frame f
+ * owning [mp_offsets[f], mp_offsets[f + 1]) (host array of nframes + 1).
+ * match_out: device, nframes * per_frame_capacity ints (map point index
+ * within the frame, -1 none, -3 past the frame's keypoints); nmatches:
+ * device, nframes ints.  Returns after the results are complete. */
+int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_keypoint* kps, const uint8_t* desc,
+                                      const int* counts, const orbgpu_mappoint* mappoints,
+                                      const uint8_t* mp_descriptors, const int* mp_offsets, float th, float nnratio,
+                                      int* match_out, int* nmatches);
+/* Kernel launches of one orbgpu_batch_search_by_projection call. */
+int orbgpu_batch_search_launch_count(void);
+
+/* ------------------------------------------------------------ batch instrumentation */
+/* Device milliseconds of the five stages of the last orbgpu_batch_extract
+ * (gather, resize + blur, FAST, octree, orientation + descriptor); n >= 5. */
+int orbgpu_batch_stage_times(orbgpu_batch* b, float* ms, int n);
+/* Kernel launches of one orbgpu_batch_extract of the last frame list. */
+int orbgpu_batch_launch_count(const orbgpu_batch* b);
+/* The batch's CUDA stream (cudaStream_t). */
+void* orbgpu_batch_stream(const orbgpu_batch* b);
+
+/* ------------------------------------------------------------ stage accessors (tests) */
+/* Device pointer of blurred level 'level' of the last extraction (same
+ * geometry as orbgpu_extractor_pyramid_level). */
+int orbgpu_extractor_blurred_level(const orbgpu_extractor* ex, int level, const uint8_t** dev_ptr);
+/* Per-level internals of the last extraction, copied to the host dst
+ * (cap bytes): what = 0 cell counts (ncells ints), 1 cell slots (ncells *
+ * cell_cap uint32: x | y << 12 | score << 24, level coordinates), 2
+ * distributed keypoints (node_cap uint32), 3 geometry (8 ints: nCols,
+ * nRows, wCell, hCell, cell_cap, nIni, node_cap, keypoints kept). */
+int orbgpu_extractor_debug_level(const orbgpu_extractor* ex, int level, int what, void* dst, size_t cap);
+/* Synchronous device-to-host copy (device-wide synchronize first). */
+int orbgpu_copy_to_host(void* dst, const void* src, size_t bytes);
+/* Arc strength (FAST score + 1, 0 = no corner) of every pixel of a device
+ * image at threshold t, into out (w * h bytes, device). */
+int orbgpu_debug_fast_strength(const uint8_t* img, int pitch, int w, int h, int t, uint8_t* out);
+/* The descriptor rotation's cos / sin of n device floats (device outputs). */
+int orbgpu_descriptor_sincos(const float* x, int n, float* c, float* s);
+/* One 128 x 256 x 256 FP8 tensor-core MMA group of +-1 expansions of host
+ * descriptors (128 and 256 rows) with the given operand strides; dots:
+ * host 128 x 256 floats. */
+int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots, int* status_out, int lbo, int sbo);
+
+/* ------------------------------------------------------------ rotation table */
+/* Builds the descriptor-rotation exception table (path NULL = next to the
+ * library) with 'threads' host threads. */
+int orbgpu_build_sincos_table(const char* path, int threads);
+/* Where the library looks for that table. */
+const char* orbgpu_sincos_table_path(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ORBGPU_EXT_H */

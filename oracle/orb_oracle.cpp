@@ -605,6 +605,111 @@ int orc_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8
     return nmatches;
 }
 
+// cv::Mat products of the reference's pose algebra: the 3 x 3 float product
+// accumulates in double and is stored as float (gemm), an added vector is a
+// float addition.
+static float mat_row_dot(const float* row, int stride, const float* x) {
+    double s = 0.0;
+    for (int k = 0; k < 3; k++) s += (double)row[k * stride] * (double)x[k];
+    return (float)s;
+}
+
+// ORBmatcher::SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame,
+// th, bMono), src/ORBmatcher.cc:1710-1879.
+int orc_search_by_projection_frame(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright,
+                                   int n, int w, int h, const orc_kp* last_kps, int n_last,
+                                   const orc_frame_mappoint* last_mps, const uint8_t* last_mp_desc,
+                                   const orc_frame_motion* mo, float th, int mono, int check_ori,
+                                   const uint8_t* claimed, int* match_out) {
+    const Tables t = make_tables(p);
+    Grid* g = new Grid();
+    build_grid(*g, kps, n, w, h);
+    // mvpMapPoints of the current frame: -1 none, -2 pre-claimed (observed), >= 0 LastFrame index
+    std::vector<int> owner(n);
+    for (int i = 0; i < n; i++) owner[i] = (claimed && claimed[i]) ? -2 : -1;
+    std::vector<char> touched(n, 0);
+    std::vector<int> rotHist[kHistoLength];
+    const float factor = kHistoLength / 360.0f;
+    // twc = -Rcw' tcw, tlc = Rlw twc + tlw (src/ORBmatcher.cc:1724-1737)
+    const float* T = mo->Tcw;
+    const float tcw[3] = {T[3], T[7], T[11]};
+    float twc[3];
+    for (int r = 0; r < 3; r++) {
+        const float col[3] = {-T[r], -T[4 + r], -T[8 + r]};  // row r of -Rcw'
+        twc[r] = mat_row_dot(col, 1, tcw);
+    }
+    const float* L = mo->Tlw;
+    const float tlcz = mat_row_dot(L + 8, 1, twc) + L[11];
+    const bool bForward = tlcz > mo->b && !mono;
+    const bool bBackward = -tlcz > mo->b && !mono;
+    int nmatches = 0;
+    for (int i = 0; i < n_last; i++) {
+        const orc_frame_mappoint& mp = last_mps[i];
+        if (!(mp.flags & ORC_MP_PRESENT) || (mp.flags & ORC_MP_OUTLIER)) continue;
+        const float X[3] = {mp.x, mp.y, mp.z};
+        float c[3];
+        for (int r = 0; r < 3; r++) c[r] = mat_row_dot(T + 4 * r, 1, X) + T[4 * r + 3];
+        const float xc = c[0], yc = c[1];
+        const float invzc = 1.0 / c[2];
+        if (invzc < 0) continue;
+        const float u = mo->fx * xc * invzc + mo->cx;
+        const float v = mo->fy * yc * invzc + mo->cy;
+        // a non-finite projection finds no cell in the reference (x86 float->int of NaN)
+        if (!std::isfinite(u) || !std::isfinite(v)) continue;
+        if (u < g->minX || u > g->maxX) continue;
+        if (v < g->minY || v > g->maxY) continue;
+        const int nLastOctave = last_kps[i].octave;
+        const float radius = th * t.scale[nLastOctave];
+        std::vector<int> idx2;
+        if (bForward) idx2 = features_in_area(*g, kps, u, v, radius, nLastOctave, -1);
+        else if (bBackward) idx2 = features_in_area(*g, kps, u, v, radius, 0, nLastOctave);
+        else idx2 = features_in_area(*g, kps, u, v, radius, nLastOctave - 1, nLastOctave + 1);
+        if (idx2.empty()) continue;
+        int bestDist = 256, bestIdx2 = -1;
+        for (int i2 : idx2) {
+            // an owner with observations blocks (src/ORBmatcher.cc:1800-1802)
+            if (owner[i2] == -2 || (owner[i2] >= 0 && (last_mps[owner[i2]].flags & ORC_MP_OBSERVED))) continue;
+            if (uright && uright[i2] > 0) {
+                const float ur = u - mo->bf * invzc;
+                const float er = std::fabs(ur - uright[i2]);
+                if (er > radius) continue;
+            }
+            const int dist = hamming(last_mp_desc + (size_t)i * 32, desc + (size_t)i2 * 32);
+            if (dist < bestDist) {
+                bestDist = dist;
+                bestIdx2 = i2;
+            }
+        }
+        if (bestDist <= kThHigh) {
+            owner[bestIdx2] = i;
+            touched[bestIdx2] = 1;
+            nmatches++;
+            if (check_ori) {
+                float rot = last_kps[i].angle - kps[bestIdx2].angle;
+                if (rot < 0.0) rot += 360.0f;
+                int bin = (int)std::round(rot * factor);
+                if (bin == kHistoLength) bin = 0;
+                rotHist[bin].push_back(bestIdx2);
+            }
+        }
+    }
+    std::vector<char> nulled(n, 0);
+    if (check_ori) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        three_maxima(rotHist, kHistoLength, ind1, ind2, ind3);
+        for (int b = 0; b < kHistoLength; b++) {
+            if (b == ind1 || b == ind2 || b == ind3) continue;
+            for (int i2 : rotHist[b]) {
+                nulled[i2] = 1;
+                nmatches--;
+            }
+        }
+    }
+    for (int i = 0; i < n; i++) match_out[i] = nulled[i] ? -4 : owner[i];
+    delete g;
+    return nmatches;
+}
+
 // Frame::ComputeStereoMatches, src/Frame.cc:831-1082 (mb = mbf/fx).
 int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
                                const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,

@@ -32,6 +32,14 @@ int orc_search_for_initialization(const orc_params* p, const orc_kp* kps1, const
 int orc_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright, int n,
                              int w, int h, const orc_mappoint* mps, const uint8_t* mp_desc, int m, float th,
                              float nnratio, const uint8_t* claimed, int* match_out);
+/* match_out per current keypoint: >= 0 the LastFrame keypoint whose map point
+ * now fills CurrentFrame.mvpMapPoints[i2]; -1 untouched; -2 claimed before the
+ * call (untouched); -4 assigned, then reset to NULL by the rotation check. */
+int orc_search_by_projection_frame(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright,
+                                   int n, int w, int h, const orc_kp* last_kps, int n_last,
+                                   const orc_frame_mappoint* last_mps, const uint8_t* last_mp_desc,
+                                   const orc_frame_motion* mo, float th, int mono, int check_ori,
+                                   const uint8_t* claimed, int* match_out);
 int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
                                const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,
                                const uint8_t* pyrR, const int* level_w, const int* level_h, int w, int h, float bf,

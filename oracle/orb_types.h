@@ -38,6 +38,25 @@ typedef struct {
     int32_t pad;
 } orc_mappoint;
 
+/* One entry of LastFrame.mvpMapPoints for ORBmatcher::SearchByProjection(
+ * Frame& CurrentFrame, const Frame& LastFrame, th, bMono)
+ * (src/ORBmatcher.cc:1710-1879), indexed like LastFrame's keypoints. */
+typedef struct {
+    float x, y, z;  /* MapPoint::GetWorldPos() */
+    int32_t flags;  /* ORC_MP_PRESENT | ORC_MP_OUTLIER | ORC_MP_OBSERVED */
+} orc_frame_mappoint;
+#define ORC_MP_PRESENT 1  /* LastFrame.mvpMapPoints[i] != NULL */
+#define ORC_MP_OUTLIER 2  /* LastFrame.mvbOutlier[i] */
+#define ORC_MP_OBSERVED 4 /* MapPoint::Observations() > 0 */
+
+/* Camera data of that search: rows 0-2 of both frames' mTcw (row-major
+ * 3 x 4) and the current frame's fx, fy, cx, cy, mbf, mb. */
+typedef struct {
+    float Tcw[12];
+    float Tlw[12];
+    float fx, fy, cx, cy, bf, b;
+} orc_frame_motion;
+
 #ifdef __cplusplus
 }
 #endif

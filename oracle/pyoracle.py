@@ -25,6 +25,26 @@ MP_DTYPE = np.dtype([("proj_x", "<f4"), ("proj_y", "<f4"), ("proj_xr", "<f4"), (
                      ("track_scale_level", "<i4"), ("track_in_view", "<i4"), ("bad", "<i4"), ("pad", "<i4")])
 
 
+FMP_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("flags", "<i4")])
+MP_PRESENT, MP_OUTLIER, MP_OBSERVED = 1, 2, 4
+
+
+class Motion(C.Structure):
+    """Rows 0-2 of both frames' Tcw (row-major 3 x 4) and fx, fy, cx, cy, mbf, mb."""
+    _fields_ = [("Tcw", C.c_float * 12), ("Tlw", C.c_float * 12), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("bf", C.c_float), ("b", C.c_float)]
+
+
+def make_motion(Tcw, Tlw, fx, fy, cx, cy, bf=0.0, b=0.0) -> Motion:
+    m = Motion()
+    for i, v in enumerate(np.asarray(Tcw, np.float32).reshape(-1)[:12]):
+        m.Tcw[i] = float(v)
+    for i, v in enumerate(np.asarray(Tlw, np.float32).reshape(-1)[:12]):
+        m.Tlw[i] = float(v)
+    m.fx, m.fy, m.cx, m.cy, m.bf, m.b = (float(np.float32(v)) for v in (fx, fy, cx, cy, bf, b))
+    return m
+
+
 class Params(C.Structure):
     _fields_ = [("nfeatures", C.c_int), ("scale_factor", C.c_float), ("nlevels", C.c_int),
                 ("ini_th_fast", C.c_int), ("min_th_fast", C.c_int)]
@@ -156,6 +176,26 @@ class _Base:
                       C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
         nm = f(C.byref(p), _p(kps), _p(desc), _p(ur), len(kps), w, h, _p(mps), _p(mp_desc), len(mps), th, nnratio,
                _p(cl), _p(out))
+        return int(nm), out[:len(kps)].copy()
+
+    def search_by_projection_frame(self, kps, desc, w, h, last_kps, last_mps, last_mp_desc, motion, th=7.0,
+                                   mono=True, check_ori=True, uright=None, claimed=None, nlevels=8,
+                                   scale_factor=1.2):
+        """SearchByProjection(CurrentFrame, LastFrame, th, bMono) -> (nmatches, match_out)."""
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        desc = np.ascontiguousarray(desc, np.uint8)
+        last_kps = np.ascontiguousarray(last_kps, KP_DTYPE)
+        last_mps = np.ascontiguousarray(last_mps, FMP_DTYPE)
+        last_mp_desc = np.ascontiguousarray(last_mp_desc, np.uint8)
+        ur = None if uright is None else np.ascontiguousarray(uright, np.float32)
+        cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
+        out = np.zeros(max(len(kps), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("search_by_projection_frame")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        nm = f(C.byref(p), _p(kps), _p(desc), _p(ur), len(kps), w, h, _p(last_kps), len(last_kps), _p(last_mps),
+               _p(last_mp_desc), C.byref(motion), th, int(bool(mono)), int(bool(check_ori)), _p(cl), _p(out))
         return int(nm), out[:len(kps)].copy()
 
     def compute_stereo_matches(self, kpsL, descL, kpsR, descR, pyrL, pyrR, w, h, bf, fx, nlevels=8,

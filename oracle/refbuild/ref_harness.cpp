@@ -327,6 +327,76 @@ int ref_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8
     return nm;
 }
 
+// ORBmatcher::SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame,
+// th, bMono) -- src/ORBmatcher.cc:1710-1879.  Current keypoints without a
+// pre-claimed map point start with a sentinel map point that has no
+// observations (it blocks nothing, exactly like NULL), so that an entry the
+// rotation check resets to NULL can be told from an untouched one.
+int ref_search_by_projection_frame(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright,
+                                   int n, int w, int h, const orc_kp* last_kps, int n_last,
+                                   const orc_frame_mappoint* last_mps, const uint8_t* last_mp_desc,
+                                   const orc_frame_motion* mo, float th, int mono, int check_ori,
+                                   const uint8_t* claimed, int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        std::vector<uint8_t> no_desc((size_t)std::max(1, n_last) * 32, 0);
+        Frame* LF = make_frame(&ext, last_kps, no_desc.data(), n_last, w, h, nullptr);
+        Frame* CF = make_frame(&ext, kps, desc, n, w, h, uright);
+        CF->mTcw = cv::Mat::eye(4, 4, CV_32F);
+        LF->mTcw = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) {
+                CF->mTcw.at<float>(r, c) = mo->Tcw[4 * r + c];
+                LF->mTcw.at<float>(r, c) = mo->Tlw[4 * r + c];
+            }
+        Frame::fx = mo->fx;
+        Frame::fy = mo->fy;
+        Frame::cx = mo->cx;
+        Frame::cy = mo->cy;
+        Frame::invfx = 1.0f / mo->fx;
+        Frame::invfy = 1.0f / mo->fy;
+        CF->mbf = mo->bf;
+        CF->mb = mo->b;
+        cv::Mat zero = cv::Mat::zeros(3, 1, CV_32F);
+        MapPoint* preclaimed = new MapPoint(zero, nullptr, nullptr);
+        MapPoint* sentinel = new MapPoint(zero, nullptr, nullptr);
+        sentinel->nObs = 0;
+        std::vector<MapPoint*> owned;
+        std::map<MapPoint*, int> index;
+        for (int i = 0; i < n_last; i++) {
+            const orc_frame_mappoint& q = last_mps[i];
+            LF->mvbOutlier[i] = (q.flags & ORC_MP_OUTLIER) != 0;
+            if (!(q.flags & ORC_MP_PRESENT)) continue;
+            cv::Mat pos(3, 1, CV_32F);
+            pos.at<float>(0) = q.x;
+            pos.at<float>(1) = q.y;
+            pos.at<float>(2) = q.z;
+            MapPoint* mp = new MapPoint(pos, nullptr, nullptr);
+            mp->nObs = (q.flags & ORC_MP_OBSERVED) ? 1 : 0;
+            mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+            std::memcpy(mp->mDescriptor.data, last_mp_desc + (size_t)i * 32, 32);
+            LF->mvpMapPoints[i] = mp;
+            owned.push_back(mp);
+            index[mp] = i;
+        }
+        for (int i = 0; i < n; i++) CF->mvpMapPoints[i] = (claimed && claimed[i]) ? preclaimed : sentinel;
+        ORBmatcher matcher(0.9f, check_ori != 0);
+        nm = matcher.SearchByProjection(*CF, *LF, th, mono != 0);
+        for (int i = 0; i < n; i++) {
+            MapPoint* mp = CF->mvpMapPoints[i];
+            match_out[i] = mp == nullptr ? -4 : mp == sentinel ? -1 : mp == preclaimed ? -2 : index[mp];
+        }
+        for (MapPoint* mp : owned) delete mp;
+        delete preclaimed;
+        delete sentinel;
+        delete CF;
+        delete LF;
+    }
+    return nm;
+}
+
 // Frame::ComputeStereoMatches -- src/Frame.cc:831-1082, on frames built from
 // recorded keypoints and the unblurred pyramids (levels back to back).  mb is
 // set to mbf/fx first: the stereo constructor reads it before assigning it

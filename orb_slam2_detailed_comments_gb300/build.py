@@ -53,7 +53,7 @@ def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
     srcp = os.path.join(CSRC, src)
     deps = [srcp] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    deps.append(os.path.join(ROOT, "include", "orbgpu.h"))
+    deps += [os.path.join(ROOT, "include", h) for h in ("orbgpu.h", "orbgpu_ext.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), *flags(), "-c", srcp, "-o", obj]

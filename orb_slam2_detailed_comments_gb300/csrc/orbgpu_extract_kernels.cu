@@ -207,12 +207,39 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 }
 
 #define FAST_MAX_ROI 72
+#define FAST_MAX_DET (FAST_MAX_ROI - 6)
+
+// Per-ROI 3x3 suppression of detection pixel (r, c) at threshold th: the
+// pixel is a corner (strength > th) whose score beats every neighbour's
+// (neighbours that are not corners, or lie outside the ROI's detection
+// region, count as 0).
+__device__ __forceinline__ bool fast_keep(const uint8_t* mstr, int dw, int dh, int r, int c, int th) {
+    const int m = mstr[r * dw + c];
+    if (m <= th) return false;
+    const int s = m - 1;
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++) {
+            if (!dx && !dy) continue;
+            const int rr = r + dy, cc = c + dx;
+            if (rr < 0 || rr >= dh || cc < 0 || cc >= dw) continue;
+            const int mq = mstr[rr * dw + cc];
+            const int nb = mq > th ? mq - 1 : 0;
+            if (!(s > nb)) return false;
+        }
+    return true;
+}
+
+// Rows are spread over warps and columns over lanes, so no index needs a
+// division; the row-major emission order of the detector is rebuilt from
+// per-row counts.
 __global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int cell = it.index;
-    const int i = cell / d.nCols, j = cell % d.nCols;
+    const int i = cell / d.nCols, j = cell - (cell / d.nCols) * d.nCols;
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
     const int iniY = minB + i * d.hCell, iniX = minB + j * d.wCell;
     int maxY = iniY + d.hCell + 6, maxX = iniX + d.wCell + 6;
@@ -228,95 +255,88 @@ __global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, Rang
         return;
     }
     __shared__ uint8_t roi[FAST_MAX_ROI * FAST_MAX_ROI];
-    __shared__ uint8_t mstr[(FAST_MAX_ROI - 6) * (FAST_MAX_ROI - 6)];
-    __shared__ uint16_t s_queue[(FAST_MAX_ROI - 6) * (FAST_MAX_ROI - 6)];
-    __shared__ int s_scan[32];
-    for (int k = threadIdx.x; k < rw * rh; k += blockDim.x) {
-        const int r = k / rw, c = k % rw;
-        roi[k] = d.dst[(size_t)(iniY + r) * d.pitch + iniX + c];
-    }
-    __syncthreads();
-    const int dw = rw - 6, dh = rh - 6, nd = dw * dh;
-    const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
-    const int t_lo = min(ini_th, min_th);
-    // Phase 1: the compass-point test (a nine-pixel arc always contains two
-    // compass points four apart) for every pixel; survivors are queued.
+    __shared__ uint8_t mstr[FAST_MAX_DET * FAST_MAX_DET];
+    __shared__ uint16_t s_queue[FAST_MAX_DET * FAST_MAX_DET];
+    __shared__ int s_rowoff[FAST_MAX_DET + 1];
     __shared__ int s_nq;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const unsigned lt = (1u << lane) - 1;
+    for (int r = warp; r < rh; r += nw) {
+        const uint8_t* src = d.dst + (size_t)(iniY + r) * d.pitch + iniX;
+        for (int c = lane; c < rw; c += 32) roi[r * rw + c] = src[c];
+    }
     if (threadIdx.x == 0) s_nq = 0;
     __syncthreads();
-    for (int k0 = 0; k0 < nd; k0 += blockDim.x) {
-        const int k = k0 + threadIdx.x;
-        bool cand = false;
-        if (k < nd) {
-            mstr[k] = 0;
-            const int r = k / dw + 3, c = k % dw + 3;
-            cand = compass_test(roi + r * rw + c, rw, t_lo);
+    const int dw = rw - 6, dh = rh - 6;
+    const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
+    const int t_lo = min(ini_th, min_th);
+    // Phase 1: compass-point test for every pixel; survivors are queued.
+    for (int r = warp; r < dh; r += nw)
+        for (int c0 = 0; c0 < dw; c0 += 32) {
+            const int c = c0 + lane;
+            bool cand = false;
+            if (c < dw) {
+                mstr[r * dw + c] = 0;
+                cand = compass_test(roi + (r + 3) * rw + c + 3, rw, t_lo);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, cand);
+            if (m) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&s_nq, __popc(m));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (cand) s_queue[base + __popc(m & lt)] = (uint16_t)(r * dw + c);
+            }
         }
-        const unsigned m = __ballot_sync(0xffffffffu, cand);
-        int base = 0;
-        if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(&s_nq, __popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (cand) s_queue[base + __popc(m & ((1u << (threadIdx.x & 31)) - 1))] = (uint16_t)k;
-    }
     __syncthreads();
-    // Phase 2: full segment test and arc strength for the queued pixels only,
-    // with every lane busy.
+    // Phase 2: full segment test and arc strength for the queued pixels.
     const int nq = s_nq;
-    for (int j = threadIdx.x; j < nq; j += blockDim.x) {
-        const int k = s_queue[j];
-        const int r = k / dw + 3, c = k % dw + 3;
-        mstr[k] = (uint8_t)arc_strength(roi, rw, r, c, t_lo);
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        const int k = s_queue[q];
+        const int r = k / dw, c = k - (k / dw) * dw;
+        mstr[k] = (uint8_t)arc_strength(roi, rw, r + 3, c + 3, t_lo);
     }
     __syncthreads();
-    const int chunk = (nd + blockDim.x - 1) / blockDim.x;
-    const int k0 = threadIdx.x * chunk, k1 = min(nd, k0 + chunk);
+    uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
     for (int pass = 0; pass < 2; pass++) {
         const int th = pass == 0 ? ini_th : min_th;
-        int cnt = 0;
-        for (int k = k0; k < k1; k++) {
-            const int m = mstr[k];
-            if (m <= th) continue;
-            const int s = m - 1;
-            const int r = k / dw, c = k % dw;
-            bool keep = true;
-            for (int dy = -1; dy <= 1 && keep; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    if (!dx && !dy) continue;
-                    const int rr = r + dy, cc = c + dx;
-                    if (rr < 0 || rr >= dh || cc < 0 || cc >= dw) continue;
-                    const int mq = mstr[rr * dw + cc];
-                    const int nb = mq > th ? mq - 1 : 0;
-                    if (!(s > nb)) { keep = false; break; }
-                }
-            cnt += keep;
+        // survivors per detection row
+        for (int r = warp; r < dh; r += nw) {
+            int cnt = 0;
+            for (int c0 = 0; c0 < dw; c0 += 32) {
+                const int c = c0 + lane;
+                const bool keep = c < dw && fast_keep(mstr, dw, dh, r, c, th);
+                cnt += __popc(__ballot_sync(0xffffffffu, keep));
+            }
+            if (lane == 0) s_rowoff[r + 1] = cnt;
         }
-        int total;
-        int pos = block_exclusive_scan(cnt, s_scan, &total);
-        if (total == 0 && pass == 0) continue;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_rowoff[0] = 0;
+            for (int r = 0; r < dh; r++) s_rowoff[r + 1] += s_rowoff[r];
+        }
+        __syncthreads();
+        int total = s_rowoff[dh];
+        if (total == 0 && pass == 0) {
+            __syncthreads();
+            continue;
+        }
         if (total > d.cell_cap) {
             if (threadIdx.x == 0) atomicOr(status, 2);
             total = d.cell_cap;
         }
-        uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
-        for (int k = k0; k < k1 && cnt > 0; k++) {
-            const int m = mstr[k];
-            if (m <= th) continue;
-            const int s = m - 1;
-            const int r = k / dw, c = k % dw;
-            bool keep = true;
-            for (int dy = -1; dy <= 1 && keep; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    if (!dx && !dy) continue;
-                    const int rr = r + dy, cc = c + dx;
-                    if (rr < 0 || rr >= dh || cc < 0 || cc >= dw) continue;
-                    const int mq = mstr[rr * dw + cc];
-                    const int nb = mq > th ? mq - 1 : 0;
-                    if (!(s > nb)) { keep = false; break; }
+        for (int r = warp; r < dh; r += nw) {
+            int base = s_rowoff[r];
+            for (int c0 = 0; c0 < dw; c0 += 32) {
+                const int c = c0 + lane;
+                const bool keep = c < dw && fast_keep(mstr, dw, dh, r, c, th);
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int pos = base + __popc(m & lt);
+                    if (pos < total)
+                        out[pos] = (uint32_t)(iniX + 3 + c) | ((uint32_t)(iniY + 3 + r) << 12) |
+                                   ((uint32_t)(mstr[r * dw + c] - 1) << 24);
                 }
-            if (keep) {
-                if (pos < total)
-                    out[pos] = (uint32_t)(iniX + 3 + c) | ((uint32_t)(iniY + 3 + r) << 12) | ((uint32_t)s << 24);
-                pos++;
+                base += __popc(m);
             }
         }
         if (threadIdx.x == 0) d.cell_count[cell] = total;
@@ -849,77 +869,3 @@ extern "C" int orbgpu_debug_fast_strength(const uint8_t* img, int pitch, int w, 
     return ORBGPU_OK;
 }
 
-// The same arc strengths computed by the host compiler (stage tests).
-extern "C" void orbgpu_debug_fast_strength_host(const uint8_t* img, int pitch, int w, int h, int t, uint8_t* out) {
-    for (int y = 0; y < h; y++)
-        for (int x = 0; x < w; x++)
-            out[(size_t)y * w + x] =
-                (x >= 3 && x < w - 3 && y >= 3 && y < h - 3) ? (uint8_t)orbgpu::arc_strength(img + (size_t)y * pitch, pitch, 0, x, t) : 0;
-}
-
-namespace orbgpu {
-// Per pixel (x, y): v, the 16 circle values, the bright/dark masks at t and
-// the arc strength, as the device reads and computes them (stage tests).
-__global__ void k_fast_probe(const uint8_t* img, int pitch, const int* xy, int n, int t, int* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint8_t* cp = img + (size_t)xy[2 * i + 1] * pitch + xy[2 * i];
-    int pc[16];
-    load_circle(cp, pitch, pc);
-    int* o = out + (size_t)i * 21;
-    o[0] = cp[0];
-    uint32_t bm = 0, dm = 0;
-    for (int k = 0; k < 16; k++) {
-        o[1 + k] = pc[k];
-        bm |= (uint32_t)(pc[k] > cp[0] + t) << k;
-        dm |= (uint32_t)(pc[k] < cp[0] - t) << k;
-    }
-    o[17] = (int)bm;
-    o[18] = (int)dm;
-    o[19] = arc_strength(img + (size_t)xy[2 * i + 1] * pitch, pitch, 0, xy[2 * i], t);
-    o[20] = (int)has_run9(bm) + 2 * (int)has_run9(dm);
-}
-}  // namespace orbgpu
-extern "C" int orbgpu_debug_fast_probe(const uint8_t* img, int pitch, const int* xy, int n, int t, int* out) {
-    orbgpu::k_fast_probe<<<(n + 127) / 128, 128>>>(img, pitch, xy, n, t, out);
-    ORBGPU_CUDA_TRY(cudaGetLastError());
-    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
-    return ORBGPU_OK;
-}
-
-namespace orbgpu {
-// arc_strength's internals for one pixel: v, hi, lo, dd[16], bm, dm, result
-__global__ void k_fast_probe2(const uint8_t* img, int pitch, int x, int y, int t, int* out) {
-    const uint8_t* cp = img + (size_t)y * pitch + x;
-    const int v = cp[0];
-    const int hi = v + t, lo = v - t;
-    int pc[16], dd[16];
-    load_circle(cp, pitch, pc);
-    uint32_t bm = 0, dm = 0;
-    for (int k = 0; k < 16; k++) {
-        const int p = pc[k];
-        dd[k] = v - p;
-        bm |= (uint32_t)(p > hi) << k;
-        dm |= (uint32_t)(p < lo) << k;
-    }
-    out[0] = v; out[1] = hi; out[2] = lo;
-    for (int k = 0; k < 16; k++) out[3 + k] = dd[k];
-    out[19] = (int)bm; out[20] = (int)dm;
-    out[21] = 0;
-    out[22] = arc_strength(img + (size_t)y * pitch, pitch, 0, x, t);
-    int best = 0;
-    for (int k = 0; k < 16; k++) {
-        int mn = dd[k], mx = dd[k];
-        for (int j = 1; j < 9; j++) { const int e = dd[(k + j) & 15]; mn = min(mn, e); mx = max(mx, e); }
-        out[23 + 2 * k] = mn; out[24 + 2 * k] = mx;
-        best = max(best, max(mn, -mx));
-    }
-    out[55] = best;
-}
-}  // namespace orbgpu
-extern "C" int orbgpu_debug_fast_probe2(const uint8_t* img, int pitch, int x, int y, int t, int* out) {
-    orbgpu::k_fast_probe2<<<1, 1>>>(img, pitch, x, y, t, out);
-    ORBGPU_CUDA_TRY(cudaGetLastError());
-    ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
-    return ORBGPU_OK;
-}

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "orbgpu_extract_kernels.cuh"
+#include "orbgpu_ext.h"
 
 namespace orbgpu {
 

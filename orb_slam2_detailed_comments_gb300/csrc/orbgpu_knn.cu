@@ -98,7 +98,7 @@ extern "C" int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, cons
         (algo != 0 && algo != 1))
         return ORBGPU_ERR_BAD_ARG;
     if (nq == 0) return ORBGPU_OK;
-    if (algo == 1) return orbgpu_knn2_tc(m, query, nq, train, nt, idx1, d1, idx2, d2);
+    if (algo == 1 && nt > 0) return orbgpu_knn2_tc(m, query, nq, train, nt, idx1, d1, idx2, d2);
     cudaStream_t st = orbgpu_matcher_stream_internal(m);
     int dev, nsm;
     ORBGPU_CUDA_TRY(cudaGetDevice(&dev));

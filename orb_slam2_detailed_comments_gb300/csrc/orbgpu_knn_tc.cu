@@ -39,6 +39,7 @@ namespace orbgpu {
 #define TC_EPI_WARPS 16
 #define TC_THREADS (32 * (TC_EPI_WARPS + 2))  // + producer warp + MMA warp
 #define TC_SPIN_LIMIT (1u << 26)
+#define TC_WAIT_NS 1000000000ull  // one second
 
 // ---------------------------------------------------------------- operand layout
 // Byte offset of element (row r, k) inside a tile stored K-major without
@@ -73,9 +74,16 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// Bounded wait on phase 'parity'; false on timeout.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait on phase 'parity': false after about one second (or
+// TC_SPIN_LIMIT polls), whichever comes first.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t a = smem_u32(bar);
+    uint64_t t0 = 0;
     for (uint32_t i = 0; i < TC_SPIN_LIMIT; i++) {
         uint32_t done;
         asm volatile(
@@ -86,6 +94,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((i & 31) == 31) {
+            const uint64_t t = global_ns();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > TC_WAIT_NS) return false;
+        }
     }
     return false;
 }
@@ -245,6 +258,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int ntile = max(0, t1 - t0);
     if (warp == producer) {
         if (lane == 0) {
+            int issued = 0;
             mbar_expect_tx(&bar_a, TC_QTILE_BYTES);
             bulk_g2s(sA, qa + (size_t)qtile * TC_QTILE_BYTES, TC_QTILE_BYTES, &bar_a);
             for (int i = 0; i < ntile; i++) {
@@ -256,12 +270,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 mbar_expect_tx(&bar_full[s], TC_TTILE_BYTES);
                 bulk_g2s(sB0 + s * TC_TTILE_BYTES, tb + (size_t)(t0 + i) * TC_TTILE_BYTES, TC_TTILE_BYTES, &bar_full[s]);
+                issued = i + 1;
             }
+            // no copy may still be writing shared memory when the CTA ends:
+            // wait (bounded) for the last phase issued on every barrier
+            bool drained = mbar_wait(&bar_a, 0);
+            for (int i = max(0, issued - 2); i < issued; i++) drained &= mbar_wait(&bar_full[i & 1], (i >> 1) & 1);
+            if (!drained) atomicOr(status, 32);
         }
     } else if (warp == issuer) {
         if (lane == 0) {
             const uint32_t idesc = idesc_e4m3(TC_M, TC_N);
             bool ok = mbar_wait(&bar_a, 0);
+            int issued = 0;
             for (int i = 0; ok && i < ntile; i++) {
                 const int s = i & 1;
                 ok = mbar_wait(&bar_full[s], (i >> 1) & 1);
@@ -275,11 +296,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     tc_mma(d, smem_desc(sA + ks * 256, 128, 2048), smem_desc(sB + ks * 256, 128, 2048), idesc, ks > 0);
                 tc_commit(&bar_empty[s]);  // train buffer s reusable when these MMAs are done
                 tc_commit(&bar_acc[s]);    // accumulator s ready
+                issued = i + 1;
             }
             if (!ok) {
                 atomicOr(status, 8);
                 s_abort = 1;
             }
+            // TMEM is freed below: wait (bounded) until the last MMAs issued on
+            // both accumulators have completed
+            bool drained = true;
+            for (int i = max(0, issued - 2); i < issued; i++) drained &= mbar_wait(&bar_acc[i & 1], (i >> 1) & 1);
+            if (!drained) atomicOr(status, 64);
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32*(w%4).. and columns 64*(w/4)..
@@ -288,7 +315,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         int b1 = 0x7fffffff, b2 = 0x7fffffff, i1 = -1, i2 = -1;
         for (int i = 0; i < ntile; i++) {
             const int s = i & 1;
-            if (!mbar_wait(&bar_acc[s], (i >> 1) & 1)) {
+            // warp-uniform outcome: tcgen05.ld below is a whole-warp instruction
+            if (!__all_sync(0xffffffffu, mbar_wait(&bar_acc[s], (i >> 1) & 1))) {
                 if (lane == 0) atomicOr(status, 16);
                 s_abort = 1;
                 break;
@@ -388,6 +416,7 @@ extern "C" int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, f
 // The tensor-core kNN (algo 1 of orbgpu_knn2); see orbgpu.h.
 int orbgpu_knn2_tc(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
                    int* idx2, int* d2) {
+    if (nq <= 0 || nt <= 0) return ORBGPU_ERR_BAD_ARG;  // the caller answers empty sets
     cudaStream_t st = orbgpu_matcher_stream_internal(m);
     int dev, nsm;
     ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
@@ -409,11 +438,7 @@ int orbgpu_knn2_tc(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_
     k_expand_fp8<<<qt * TC_M, 256, 0, st>>>(query, nq, TC_M, eq);
     k_expand_fp8<<<tt * TC_N, 256, 0, st>>>(train, nt, TC_N, et);
     const size_t smem = TC_QTILE_BYTES + 2 * TC_TTILE_BYTES;
-    static bool attr = false;
-    if (!attr) {
-        ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
+    ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(qt, nslices);
     k_knn_tc<<<grid, TC_THREADS, smem, st>>>(eq, et, nq, nt, per, partial, status);
     knn_merge_launch(partial, nq, nslices, idx1, d1, idx2, d2, st);

@@ -119,13 +119,3 @@ extern "C" const char* orbgpu_sincos_table_path(void) {
     return p.c_str();
 }
 
-// The rounded device evaluation and the table-corrected value for n inputs
-// (host arrays), for tests of the rotation.
-extern "C" void orbgpu_sincos_host(const float* x, int n, float* c_taylor, float* s_taylor) {
-    for (int i = 0; i < n; i++) {
-        double sd, cd;
-        orbgpu::sincos_taylor(x[i], &sd, &cd);
-        c_taylor[i] = (float)cd;
-        s_taylor[i] = (float)sd;
-    }
-}

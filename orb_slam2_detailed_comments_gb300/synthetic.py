@@ -142,3 +142,89 @@ def stream_frames(w: int, h: int, seed: int, nframes: int, noise_sigma: float = 
         out.append(warp(base, H, seed * 7919 + k, noise_sigma))
         H = random_homography(w, h, rng, max_rot_deg=1.0, max_shift=3.0) @ H
     return out
+
+
+FRAME_MAPPOINT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("flags", "<i4")])
+MP_PRESENT, MP_OUTLIER, MP_OBSERVED = 1, 2, 4
+
+
+def _rot(rx: float, ry: float, rz: float) -> np.ndarray:
+    cx_, sx = np.cos(rx), np.sin(rx)
+    cy_, sy = np.cos(ry), np.sin(ry)
+    cz, sz = np.cos(rz), np.sin(rz)
+    Rx = np.array([[1, 0, 0], [0, cx_, -sx], [0, sx, cx_]])
+    Ry = np.array([[cy_, 0, sy], [0, 1, 0], [-sy, 0, cy_]])
+    Rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx
+
+
+def motion_case(kps: np.ndarray, desc: np.ndarray, w: int, h: int, seed: int, n_last: int | None = None,
+                stereo: bool = False, dz: float = 0.0, rot_offset_deg: float = 8.0, flip_p: float = 0.08,
+                claimed_p: float = 0.05):
+    """A LastFrame for SearchByProjection(CurrentFrame, LastFrame, th, bMono)
+    whose map points project near the given current keypoints.
+
+    kps / desc: the current frame (structured 28-byte keypoints, n x 32).
+    dz: the current camera's displacement along the last camera's optical
+    axis (metres; > baseline = forward, < -baseline = backward).
+    Returns a dict with last_kps, last_mps (FRAME_MAPPOINT_DTYPE),
+    last_mp_desc, Tcw, Tlw (3 x 4 float32), fx, fy, cx, cy, bf, b, uright
+    (current frame, stereo only) and claimed (current frame)."""
+    rng = np.random.default_rng(seed)
+    n = len(kps)
+    if n_last is None:
+        n_last = max(1, int(n * 1.1))
+    fx = fy = 718.856
+    cx, cy = w / 2.0, h / 2.0
+    bf = 386.1
+    b = bf / fx
+    Rcw = _rot(*rng.normal(0, 0.02, 3))
+    tcw = rng.normal(0, 0.3, 3)
+    twc = -Rcw.T @ tcw
+    Rlw = Rcw @ _rot(*rng.normal(0, 0.005, 3))
+    Cl = twc - Rlw.T @ np.array([0.0, 0.0, dz])  # last camera centre in the world
+    tlw = -Rlw @ Cl
+    Tcw = np.hstack([Rcw, tcw[:, None]]).astype(np.float32)
+    Tlw = np.hstack([Rlw, tlw[:, None]]).astype(np.float32)
+    zj = rng.uniform(3.0, 40.0, size=max(n, 1))
+    uright = None
+    if stereo:
+        uright = np.full(n, -1.0, np.float32)
+        has = rng.random(n) < 0.7
+        uright[has] = (kps["x"][has] - bf / zj[:n][has] + rng.normal(0, 0.5, has.sum())).astype(np.float32)
+    last_kps = np.zeros(n_last, kps.dtype)
+    mps = np.zeros(n_last, FRAME_MAPPOINT_DTYPE)
+    mpd = rng.integers(0, 256, size=(n_last, 32), dtype=np.uint8)
+    for i in range(n_last):
+        if n > 0 and rng.random() < 0.85:
+            j = int(rng.integers(0, n))
+            u = float(kps["x"][j]) + rng.normal(0, 1.0)
+            v = float(kps["y"][j]) + rng.normal(0, 1.0)
+            z = zj[j] * (1 + rng.normal(0, 0.01))
+            octv = int(np.clip(int(kps["octave"][j]) + rng.choice([-1, 0, 0, 0, 1]), 0, 7))
+            ang = float(kps["angle"][j]) + rot_offset_deg + rng.normal(0, 3.0)
+            if rng.random() < 0.1:
+                ang = rng.uniform(0, 360)
+            flips = np.packbits(rng.random(256) < flip_p, bitorder="little")
+            mpd[i] = desc[j] ^ flips
+        else:
+            u, v = rng.uniform(-20, w + 20), rng.uniform(-20, h + 20)
+            z = rng.uniform(3.0, 40.0) * (-1 if rng.random() < 0.05 else 1)
+            octv = int(rng.integers(0, 8))
+            ang = rng.uniform(0, 360)
+        Xc = np.array([(u - cx) * z / fx, (v - cy) * z / fy, z])
+        Xw = Rcw.T @ (Xc - tcw)
+        mps[i] = (Xw[0], Xw[1], Xw[2], 0)
+        r = rng.random()
+        flags = MP_PRESENT if r < 0.9 else 0
+        if flags and rng.random() < 0.05:
+            flags |= MP_OUTLIER
+        if flags and rng.random() < 0.85:
+            flags |= MP_OBSERVED
+        mps["flags"][i] = flags
+        last_kps[i]["octave"] = octv
+        last_kps[i]["angle"] = np.float32(ang % 360.0)
+        last_kps[i]["class_id"] = -1
+    claimed = (rng.random(n) < claimed_p).astype(np.uint8)
+    return dict(last_kps=last_kps, last_mps=mps, last_mp_desc=mpd, Tcw=Tcw, Tlw=Tlw, fx=fx, fy=fy, cx=cx, cy=cy,
+                bf=bf, b=b, uright=uright, claimed=claimed)

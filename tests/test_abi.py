@@ -1,0 +1,67 @@
+"""The C ABI without a GPU: the headers compile as plain C, the library
+loads, and it exports every function the headers declare."""
+import ctypes as C
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("orbgpu.h", "orbgpu_ext.h")]
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(orbgpu_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def library():
+    from orb_slam2_detailed_comments_gb300 import _lib, build
+    if not os.path.exists(_lib.LIB_PATH):
+        if not (os.path.exists("/usr/local/cuda/bin/nvcc") or shutil.which("nvcc")):
+            pytest.skip("library not built and no nvcc")
+        build.build()
+    return _lib.lib()
+
+
+def test_headers_compile_as_c():
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    for h in HEADERS:
+        r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-x", "c", h,
+                            "-I" + os.path.join(ROOT, "include")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
+def test_every_declared_symbol_is_exported(library):
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(library, n)]
+    assert not missing, missing
+
+
+def test_version_and_error_string_without_gpu(library):
+    assert library.orbgpu_version() > 0
+    library.orbgpu_last_error.restype = C.c_char_p
+    assert isinstance(library.orbgpu_last_error(), bytes)
+
+
+def test_bad_arguments_are_rejected_before_any_device_work(library):
+    """Argument checks run on the host: they answer BAD_ARG with or without a GPU."""
+    h = C.c_void_p()
+    # nfeatures < 0, scale factor <= 1, nlevels out of range
+    assert library.orbgpu_extractor_create(-1, C.c_float(1.2), 8, 20, 7, 0, 0, None, C.byref(h)) == 1
+    assert library.orbgpu_extractor_create(1000, C.c_float(1.0), 8, 20, 7, 0, 0, None, C.byref(h)) == 1
+    assert library.orbgpu_extractor_create(1000, C.c_float(1.2), 0, 20, 7, 0, 0, None, C.byref(h)) == 1
+    assert library.orbgpu_knn2(None, None, 1, None, 1, None, None, None, None, 0) == 1
+    assert library.orbgpu_knn2_noalloc(None, -1, None, 0, None, None, None, None, None) == 1
+    assert library.orbgpu_batch_create(0, 640, 480, 1000, None, C.byref(h)) == 1

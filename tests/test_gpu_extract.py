@@ -117,3 +117,44 @@ def test_descriptor_rotation_matches_host_libm(torch, oracle):
                                 hs.ctypes.data_as(C.c_void_p))
     assert np.array_equal(c.cpu().numpy().view(np.uint32), hc.view(np.uint32))
     assert np.array_equal(s.cpu().numpy().view(np.uint32), hs.view(np.uint32))
+
+
+def test_fast_stage_per_level(torch, oracle):
+    """The detector stage alone: per level, the GPU's per-cell FAST output (in
+    cell order, retry threshold applied) equals the oracle's cell loop on the
+    same pyramid level, and every candidate's score is its arc strength - 1."""
+    import ctypes as C
+    from orb_slam2_detailed_comments_gb300._lib import lib, ptr
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    img = syn.scene(1241, 376, 77)
+    ex = extractor(2000)
+    ex(img)
+    levels = ex.pyramid_numpy()
+    fn = oracle.fn("fast_level")
+    for lvl, li in enumerate(levels):
+        h, w = li.shape
+        cap = 200000
+        ref = np.zeros(cap, pyoracle.KP_DTYPE)
+        nref = fn(np.ascontiguousarray(li).ctypes.data_as(C.c_void_p), w, h, 20, 7, ref.ctypes.data_as(C.c_void_p), cap)
+        ref = ref[:nref]
+        geom = np.zeros(8, np.int32)
+        assert lib().orbgpu_extractor_debug_level(ex.handle, lvl, 3, ptr(geom), C.c_size_t(geom.nbytes)) == 0
+        ncols, nrows, _, _, cell_cap = (int(v) for v in geom[:5])
+        counts = np.zeros(ncols * nrows, np.int32)
+        slots = np.zeros(ncols * nrows * cell_cap, np.uint32)
+        assert lib().orbgpu_extractor_debug_level(ex.handle, lvl, 0, ptr(counts), C.c_size_t(counts.nbytes)) == 0
+        assert lib().orbgpu_extractor_debug_level(ex.handle, lvl, 1, ptr(slots), C.c_size_t(slots.nbytes)) == 0
+        got = np.concatenate([slots[c * cell_cap: c * cell_cap + counts[c]] for c in range(len(counts))])
+        gx = (got & 0xFFF).astype(np.int64) - 16
+        gy = ((got >> 12) & 0xFFF).astype(np.int64) - 16
+        gs = (got >> 24).astype(np.int64)
+        assert len(got) == nref, lvl
+        assert np.array_equal(gx, ref["x"].astype(np.int64)), lvl
+        assert np.array_equal(gy, ref["y"].astype(np.int64)), lvl
+        assert np.array_equal(gs, ref["response"].astype(np.int64)), lvl
+        # arc strengths of the whole level at the threshold each cell used
+        dimg = torch.from_numpy(li).cuda()
+        smap = torch.empty((h, w), dtype=torch.uint8, device="cuda")
+        assert lib().orbgpu_debug_fast_strength(ptr(dimg), w, w, h, 7, ptr(smap)) == 0
+        sm = smap.cpu().numpy().astype(np.int64)
+        assert np.array_equal(sm[gy + 16, gx + 16] - 1, gs), lvl

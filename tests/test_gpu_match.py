@@ -173,3 +173,52 @@ def test_projection_device_inputs(torch, oracle):
                                      torch.from_numpy(mpd).cuda(), 6.0)
     assert nm == r[0]
     assert np.array_equal(match.cpu().numpy(), r[1])
+
+
+def test_tc_operand_layout(torch):
+    """One 128 x 256 x 256 tensor-core MMA group on +-1 FP8 expansions equals
+    the integer dot products (the shared-memory operand layout self-test)."""
+    import ctypes as C
+    from orb_slam2_detailed_comments_gb300._lib import lib
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    q = syn.random_descriptors(128, 1)
+    t = syn.random_descriptors(256, 2)
+    bq = 1 - 2 * np.unpackbits(q, axis=1, bitorder="little").astype(np.int32)
+    bt = 1 - 2 * np.unpackbits(t, axis=1, bitorder="little").astype(np.int32)
+    dots = np.zeros((128, 256), np.float32)
+    st = np.zeros(1, np.int32)
+    rc = lib().orbgpu_debug_tc_probe(q.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                                     dots.ctypes.data_as(C.c_void_p), st.ctypes.data_as(C.c_void_p), 128, 2048)
+    assert rc == 0 and st[0] == 0
+    assert np.array_equal(dots, (bq @ bt.T).astype(np.float32))
+
+
+@pytest.mark.parametrize("nq,nt", [(1, 1), (129, 257), (1000, 20000)])
+def test_knn_tensor_cores_oracle(torch, oracle, nq, nt):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    q = syn.random_descriptors(nq, 5)
+    t = syn.random_descriptors(nt, 6)
+    ref = oracle.knn2(q, t)
+    out = ORBmatcher().knn2(torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda(), algo=1)
+    for a, b, name in zip(out, ref, ("idx1", "d1", "idx2", "d2")):
+        assert np.array_equal(a.cpu().numpy(), b), name
+
+
+def test_knn_tensor_cores_golden_and_ties(torch, golden):
+    """Golden vectors, then clustered descriptors (many equal distances) against
+    the popcount kernel at a size with many slices."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    m = ORBmatcher()
+    g = golden("knn_200x3000.npz")
+    out = m.knn2(torch.from_numpy(g["query"]).cuda(), torch.from_numpy(g["train"]).cuda(), algo=1)
+    for a, name in zip(out, ("idx1", "d1", "idx2", "d2")):
+        assert np.array_equal(a.cpu().numpy(), g[name]), name
+    # the same seed gives both sets the same 200 centres: many equal distances
+    q = torch.from_numpy(syn.clustered_descriptors(5000, 200, 0.05, 8)).cuda()
+    t = torch.from_numpy(syn.clustered_descriptors(60000, 200, 0.05, 8)).cuda()
+    a = m.knn2(q, t, algo=0)
+    b = m.knn2(q, t, algo=1)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
