@@ -155,6 +155,46 @@ int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame* f, const 
                                 const uint8_t* mp_descriptors, int n_mappoints, float th, const uint8_t* claimed,
                                 int* match_out, int mem, int* nmatches);
 
+/* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
+ * indexed like LastFrame's keypoints. */
+typedef struct {
+    float x, y, z; /* MapPoint::GetWorldPos() */
+    int32_t flags; /* ORBGPU_MP_* */
+} orbgpu_frame_mappoint;
+#define ORBGPU_MP_PRESENT 1  /* LastFrame.mvpMapPoints[i] != NULL */
+#define ORBGPU_MP_OUTLIER 2  /* LastFrame.mvbOutlier[i] */
+#define ORBGPU_MP_OBSERVED 4 /* MapPoint::Observations() > 0 */
+
+/* Camera data of that search: rows 0-2 of CurrentFrame.mTcw and
+ * LastFrame.mTcw (row-major 3 x 4), Frame::fx, fy, cx, cy and the current
+ * frame's mbf and mb. */
+typedef struct {
+    float Tcw[12];
+    float Tlw[12];
+    float fx, fy, cx, cy;
+    float bf, b;
+} orbgpu_frame_motion;
+
+/* ORBmatcher::SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame,
+ *     const float th, const bool bMono) -- src/ORBmatcher.cc:1710-1879,
+ * with the matcher's checkOri for the rotation check.
+ * current: the frame searched (keypoints, descriptors, optional mvuRight);
+ * last: LastFrame's keypoints (octave and angle are read; descriptors may be
+ * NULL); last_mappoints / last_mp_descriptors: last->n records and
+ * last->n x 32 bytes (MapPoint::GetDescriptor()).  claimed: current->n bytes,
+ * non-zero where CurrentFrame.mvpMapPoints[i] already holds a map point with
+ * observations (NULL = none).  match_out: current->n ints: >= 0 the LastFrame
+ * keypoint whose map point now fills CurrentFrame.mvpMapPoints[i]; -1 not
+ * assigned by this call; -2 claimed; -4 assigned and then reset to NULL by
+ * the rotation check.  *nmatches: the reference's return value (it counts
+ * reassignments, as the reference does).  last_mappoints, last_mp_descriptors,
+ * claimed and match_out are host or device memory per 'mem'; the frames
+ * carry their own flag. */
+int orbgpu_search_by_projection_frame(orbgpu_matcher* m, const orbgpu_frame* current, const orbgpu_frame* last,
+                                      const orbgpu_frame_mappoint* last_mappoints, const uint8_t* last_mp_descriptors,
+                                      const orbgpu_frame_motion* motion, float th, int mono, const uint8_t* claimed,
+                                      int* match_out, int mem, int* nmatches);
+
 /* Frame::ComputeStereoMatches() -- src/Frame.cc:831-1082.
  * left/right: the two extractor handles that produced the frames (their
  * pyramids are read in place).  bf = mbf, fx = K(0,0); mb = bf/fx.

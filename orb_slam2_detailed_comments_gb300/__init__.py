@@ -5,6 +5,6 @@ behind the C ABI in include/orbgpu.h); this package mirrors the reference's
 ORBextractor / ORBmatcher / Frame interfaces on top of it.  There is no CPU
 fallback: without the built library or a CUDA device every call raises.
 """
-from ._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE, OrbGpuError, lib  # noqa: F401
+from ._lib import FRAME_MAPPOINT_DTYPE, KEYPOINT_DTYPE, MAPPOINT_DTYPE, OrbGpuError, lib  # noqa: F401
 from .extractor import ORBextractor  # noqa: F401
 from .matcher import ORBmatcher, FrameView, compute_stereo_matches  # noqa: F401

@@ -14,6 +14,9 @@ KEYPOINT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("size", "<f4"), ("angle"
 MAPPOINT_DTYPE = np.dtype([("proj_x", "<f4"), ("proj_y", "<f4"), ("proj_xr", "<f4"), ("view_cos", "<f4"),
                            ("track_scale_level", "<i4"), ("track_in_view", "<i4"), ("bad", "<i4"), ("pad", "<i4")])
 
+FRAME_MAPPOINT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("flags", "<i4")])
+MP_PRESENT, MP_OUTLIER, MP_OBSERVED = 1, 2, 4
+
 MEM_HOST = 0
 MEM_DEVICE = 1
 
@@ -30,6 +33,13 @@ class FrameStruct(C.Structure):
     _fields_ = [("keypoints", C.c_void_p), ("descriptors", C.c_void_p), ("uright", C.c_void_p), ("n", C.c_int),
                 ("width", C.c_int), ("height", C.c_int), ("nlevels", C.c_int), ("scale_factors", C.c_float * 16),
                 ("mem", C.c_int)]
+
+
+class MotionStruct(C.Structure):
+    """orbgpu_frame_motion: rows 0-2 of CurrentFrame.mTcw and LastFrame.mTcw,
+    fx, fy, cx, cy, mbf, mb."""
+    _fields_ = [("Tcw", C.c_float * 12), ("Tlw", C.c_float * 12), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("bf", C.c_float), ("b", C.c_float)]
 
 
 _lib = None

@@ -464,6 +464,246 @@ __global__ void k_init_match_out(const uint8_t* claimed, int n, int* match_out) 
     if (i < n) match_out[i] = (claimed && claimed[i]) ? -2 : -1;
 }
 
+// ----------------------------------------------------------------- SearchByProjection(Frame, LastFrame)
+// src/ORBmatcher.cc:1710-1879.  Per LastFrame map point (one warp): the pose
+// algebra with the reference's rounding (3 x 3 float product accumulated in
+// double and stored as float, then a float addition; 1.0 / z in double), the
+// window over the current grid with the motion-dependent level range, the
+// stereo gate, and the candidates whose distance can be accepted
+// (<= TH_HIGH: with no ratio test the first minimum is the answer, and a
+// minimum above TH_HIGH is rejected either way).
+struct FrameMotionDev {
+    float T[12];
+    float fx, fy, cx, cy, bf;
+    float maxX, maxY;
+    int level_mode;  // 1 forward, 2 backward, 0 neither
+};
+
+__device__ __forceinline__ float pose_row(const float* row, float X0, float X1, float X2) {
+    double s = __dadd_rn(0.0, __dmul_rn((double)row[0], (double)X0));
+    s = __dadd_rn(s, __dmul_rn((double)row[1], (double)X1));
+    s = __dadd_rn(s, __dmul_rn((double)row[2], (double)X2));
+    return __fadd_rn(__double2float_rn(s), row[3]);
+}
+
+__global__ void k_pf_candidates(GridDev g, FrameMotionDev mo, const orbgpu_keypoint* last_kps,
+                                const orbgpu_frame_mappoint* mps, const uint8_t* mp_desc, int m, float th,
+                                const int* cand_start, int* cand_count, uint64_t* cand_out, int fill) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= m) return;
+    const orbgpu_frame_mappoint mp = mps[i];
+    int total = 0;
+    const int oct = last_kps[i].octave;
+    bool live = (mp.flags & ORBGPU_MP_PRESENT) && !(mp.flags & ORBGPU_MP_OUTLIER) && oct >= 0 && oct < 16;
+    float u = 0.f, v = 0.f, invzc = 0.f;
+    if (live) {
+        const float xc = pose_row(mo.T, mp.x, mp.y, mp.z);
+        const float yc = pose_row(mo.T + 4, mp.x, mp.y, mp.z);
+        const float zc = pose_row(mo.T + 8, mp.x, mp.y, mp.z);
+        invzc = __double2float_rn(__ddiv_rn(1.0, (double)zc));
+        u = __fadd_rn(__fmul_rn(__fmul_rn(mo.fx, xc), invzc), mo.cx);
+        v = __fadd_rn(__fmul_rn(__fmul_rn(mo.fy, yc), invzc), mo.cy);
+        // a non-finite projection finds no grid cell in the reference
+        live = !(invzc < 0.f) && isfinite(u) && isfinite(v) && !(u < g.minX || u > mo.maxX) &&
+               !(v < g.minY || v > mo.maxY);
+    }
+    if (live) {
+        const float radius = __fmul_rn(th, g.scale[oct]);
+        int minL, maxL;
+        if (mo.level_mode == 1) {
+            minL = oct;
+            maxL = -1;
+        } else if (mo.level_mode == 2) {
+            minL = 0;
+            maxL = oct;
+        } else {
+            minL = oct - 1;
+            maxL = oct + 1;
+        }
+        int x0, x1, y0, y1;
+        if (area_cells(g, u, v, radius, x0, x1, y0, y1)) {
+            const uint8_t* dmp = mp_desc + (size_t)i * 32;
+            const float ur = __fsub_rn(u, __fmul_rn(mo.bf, invzc));
+            for (int ix = x0; ix <= x1; ix++)
+                for (int iy = y0; iy <= y1; iy++) {
+                    const int c = ix * ORBGPU_GRID_ROWS + iy;
+                    const int s = g.cell_start[c], e = g.cell_start[c + 1];
+                    for (int b = s; b < e; b += 32) {
+                        const int j = b + lane;
+                        bool ok = false;
+                        int idx = -1, dist = 256;
+                        if (j < e) {
+                            idx = g.cell_keys[j];
+                            ok = in_area(g, idx, u, v, radius, minL, maxL);
+                            if (ok && g.uright && g.uright[idx] > 0) {
+                                const float er = fabsf(__fsub_rn(ur, g.uright[idx]));
+                                if (er > radius) ok = false;
+                            }
+                            if (ok) {
+                                dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
+                                ok = dist <= ORBGPU_TH_HIGH;
+                            }
+                        }
+                        const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                        if (fill && ok) {
+                            const int pos = cand_start[i] + total + __popc(msk & ((1u << lane) - 1));
+                            cand_out[pos] = cand_key(dist, c, idx);
+                        }
+                        total += __popc(msk);
+                    }
+                }
+        }
+    }
+    if (!fill && lane == 0) cand_count[i] = total;
+}
+
+// Fixed-point round r of the in-order assignment: map point i takes its
+// first minimum among candidates not held by an observed map point j < i of
+// round r-1's results (an owner without observations blocks nothing,
+// src/ORBmatcher.cc:1800-1802).  A round that changes nothing equals the
+// sequential result.
+__global__ void k_pf_round(int n, int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
+                           const orbgpu_frame_mappoint* mps, int round, int* claims3, int* res, int* changed,
+                           const int* pre) {
+    const int lane = threadIdx.x & 31;
+    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    if (round > 0 && changed[round - 1] == 0) return;
+    int* claims_r = claims3 + (size_t)((round + 0) % 3) * n;
+    int* claims_w = claims3 + (size_t)((round + 1) % 3) * n;
+    int* claims_z = claims3 + (size_t)((round + 2) % 3) * n;
+    for (int k = local * 32 + lane; k < n; k += nwarps * 32) claims_z[k] = PROJ_NONE;
+    if (local >= m) return;
+    const int s = cand_start[local], cnt = cand_count[local];
+    uint64_t best = ~0ull;
+    for (int b = lane; b < cnt; b += 32) {
+        const uint64_t key = cands[s + b];
+        const int idx = (int)(key & 0xFFFFF);
+        if (pre[idx] != -2 && !(claims_r[idx] < local) && key < best) best = key;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+        best = ob < best ? ob : best;
+    }
+    const int r = best == ~0ull ? -1 : (int)(best & 0xFFFFF);
+    if (lane == 0) {
+        if (res[local] != r) changed[round] = 1;
+        res[local] = r;
+        if (r >= 0 && (mps[local].flags & ORBGPU_MP_OBSERVED)) atomicMin(&claims_w[r], local);
+    }
+}
+
+// Sequential assignment when no round converged (one warp).
+__global__ void k_pf_serial(int n, int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
+                            const orbgpu_frame_mappoint* mps, const int* changed, int* res, int* blocked,
+                            const int* pre) {
+    if (changed[PROJ_ROUNDS - 1] == 0) return;
+    const int lane = threadIdx.x;
+    for (int k = lane; k < n; k += 32) blocked[k] = pre[k] == -2;
+    __syncwarp();
+    for (int i = 0; i < m; i++) {
+        const int s = cand_start[i], cnt = cand_count[i];
+        uint64_t best = ~0ull;
+        for (int b = lane; b < cnt; b += 32) {
+            const uint64_t key = cands[s + b];
+            if (!blocked[(int)(key & 0xFFFFF)] && key < best) best = key;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+            best = ob < best ? ob : best;
+        }
+        const int r = best == ~0ull ? -1 : (int)(best & 0xFFFFF);
+        if (lane == 0) {
+            res[i] = r;
+            if (r >= 0 && (mps[i].flags & ORBGPU_MP_OBSERVED)) blocked[r] = 1;
+        }
+        __syncwarp();
+    }
+}
+
+// Owners (the last map point that assigned each keypoint), the rotation
+// histogram of every assignment (src/ORBmatcher.cc:1847-1857), the three
+// maxima and the resets (:1862-1876), and the output codes.  One block.
+__global__ void __launch_bounds__(1024) k_pf_finish(int n, int m, const int* res, const orbgpu_keypoint* last_kps,
+                                                    const orbgpu_keypoint* cur_kps, int check_ori, int* owner,
+                                                    int* bin_of, int* nulled, int* match_out, int* nmatches_out) {
+    __shared__ int hist[ORBGPU_HISTO_LENGTH];
+    __shared__ int s_nm, s_ind[3];
+    if (threadIdx.x < ORBGPU_HISTO_LENGTH) hist[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_nm = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        owner[k] = -1;
+        nulled[k] = 0;
+    }
+    __syncthreads();
+    const float factor = __fdiv_rn((float)ORBGPU_HISTO_LENGTH, 360.0f);
+    int nm = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int r = res[i];
+        int bin = -1;
+        if (r >= 0) {
+            nm++;
+            atomicMax(&owner[r], i);
+            if (check_ori) {
+                float rot = __fsub_rn(last_kps[i].angle, cur_kps[r].angle);
+                if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
+                bin = (int)roundf(__fmul_rn(rot, factor));
+                if (bin == ORBGPU_HISTO_LENGTH) bin = 0;
+                atomicAdd(&hist[bin], 1);
+            }
+        }
+        bin_of[i] = bin;
+    }
+    atomicAdd(&s_nm, nm);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        if (check_ori) {
+            int max1 = 0, max2 = 0, max3 = 0;
+            for (int b = 0; b < ORBGPU_HISTO_LENGTH; b++) {  // ComputeThreeMaxima, src/ORBmatcher.cc:2035-2077
+                const int sz = hist[b];
+                if (sz > max1) {
+                    max3 = max2; max2 = max1; max1 = sz;
+                    ind3 = ind2; ind2 = ind1; ind1 = b;
+                } else if (sz > max2) {
+                    max3 = max2; max2 = sz;
+                    ind3 = ind2; ind2 = b;
+                } else if (sz > max3) {
+                    max3 = sz;
+                    ind3 = b;
+                }
+            }
+            if ((float)max2 < __fmul_rn(0.1f, (float)max1)) {
+                ind2 = -1;
+                ind3 = -1;
+            } else if ((float)max3 < __fmul_rn(0.1f, (float)max1)) {
+                ind3 = -1;
+            }
+        }
+        s_ind[0] = ind1;
+        s_ind[1] = ind2;
+        s_ind[2] = ind3;
+    }
+    __syncthreads();
+    if (check_ori) {
+        int removed = 0;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int b = bin_of[i];
+            if (b < 0 || b == s_ind[0] || b == s_ind[1] || b == s_ind[2]) continue;
+            nulled[res[i]] = 1;
+            removed++;
+        }
+        atomicSub(&s_nm, removed);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int pre = match_out[k];
+        match_out[k] = nulled[k] ? -4 : owner[k] >= 0 ? owner[k] : pre;
+    }
+    if (threadIdx.x == 0) *nmatches_out = s_nm;
+}
+
 // ----------------------------------------------------------------- stereo
 struct StereoLevels {
     const uint8_t* left[16];
@@ -955,6 +1195,137 @@ extern "C" int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame
                                                                                 claims3, res, changed, d_match);
             k_proj_finish<<<1, 256, 0, m->stream>>>(M, changed, res, d_match, d_nm);
             k_proj_resolve<<<1, 32, 0, m->stream>>>(g, M, start, count, keys, m->nnratio, d_match, d_nm, changed);
+        }
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        if (mem != ORBGPU_MEM_DEVICE && n > 0)
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(match_out, d_match, sizeof(int) * n, cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, d_nm, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+        *nmatches = m->h_pinned[0];
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
+}
+
+// The reference's bForward / bBackward decision (src/ORBmatcher.cc:1724-1741):
+// twc = -Rcw' tcw and tlc = Rlw twc + tlw with cv::Mat rounding (products
+// accumulated in double, stored as float, then a float addition).
+static int motion_level_mode(const orbgpu_frame_motion& mo, int mono) {
+    const float* T = mo.Tcw;
+    const float tcw[3] = {T[3], T[7], T[11]};
+    float twc[3];
+    for (int r = 0; r < 3; r++) {
+        const float col[3] = {-T[r], -T[4 + r], -T[8 + r]};
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (double)col[k] * (double)tcw[k];
+        twc[r] = (float)s;
+    }
+    const float* L = mo.Tlw;
+    double s = 0.0;
+    for (int k = 0; k < 3; k++) s += (double)L[8 + k] * (double)twc[k];
+    const float tlcz = (float)s + L[11];
+    const bool fwd = tlcz > mo.b && !mono;
+    const bool bwd = -tlcz > mo.b && !mono;
+    return fwd ? 1 : bwd ? 2 : 0;
+}
+
+extern "C" int orbgpu_search_by_projection_frame(orbgpu_matcher* m, const orbgpu_frame* current,
+                                                 const orbgpu_frame* last, const orbgpu_frame_mappoint* last_mappoints,
+                                                 const uint8_t* last_mp_descriptors, const orbgpu_frame_motion* motion,
+                                                 float th, int mono, const uint8_t* claimed, int* match_out, int mem,
+                                                 int* nmatches) {
+    if (!m || !frame_ok(current) || !last || last->n < 0 || last->n >= (1 << 20) || (last->n > 0 && !last->keypoints) ||
+        !motion || !match_out || !nmatches || (last->n > 0 && (!last_mappoints || !last_mp_descriptors)))
+        return ORBGPU_ERR_BAD_ARG;
+    const int n = current->n, M = last->n;
+    *nmatches = 0;
+    const int mode = motion_level_mode(*motion, mono);
+    FrameMotionDev mo;
+    std::memcpy(mo.T, motion->Tcw, sizeof(mo.T));
+    mo.fx = motion->fx;
+    mo.fy = motion->fy;
+    mo.cx = motion->cx;
+    mo.cy = motion->cy;
+    mo.bf = motion->bf;
+    mo.maxX = (float)current->width;
+    mo.maxY = (float)current->height;
+    mo.level_mode = mode;
+    size_t est = frame_stage_bytes(current) + grid_bytes(n) +
+                 (size_t)std::max(1, M) * (sizeof(orbgpu_frame_mappoint) + sizeof(orbgpu_keypoint) + 32 + 32) +
+                 (size_t)std::max(1, n) * 32 + 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 32;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        int rc = ensure_scratch(m, est);
+        if (rc) return rc;
+        Bump b{(uint8_t*)m->scratch, 0, m->scratch_bytes};
+        Staged s;
+        if ((rc = stage_frame(m, current, b, s))) return rc;
+        GridDev g;
+        if ((rc = build_grid(m, current, s, b, g))) return rc;
+        const orbgpu_keypoint* d_lk = last->keypoints;
+        if (last->mem != ORBGPU_MEM_DEVICE) {
+            orbgpu_keypoint* k = b.take<orbgpu_keypoint>(std::max(1, M));
+            if (M)
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(k, last->keypoints, sizeof(orbgpu_keypoint) * M, cudaMemcpyHostToDevice,
+                                                m->stream));
+            d_lk = k;
+        }
+        const orbgpu_frame_mappoint* d_mps = last_mappoints;
+        const uint8_t* d_mpd = last_mp_descriptors;
+        const uint8_t* d_claimed = claimed;
+        int* d_match = match_out;
+        if (mem != ORBGPU_MEM_DEVICE) {
+            orbgpu_frame_mappoint* a = b.take<orbgpu_frame_mappoint>(std::max(1, M));
+            uint8_t* dd = b.take<uint8_t>((size_t)std::max(1, M) * 32);
+            if (M) {
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(a, last_mappoints, sizeof(orbgpu_frame_mappoint) * M,
+                                                cudaMemcpyHostToDevice, m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(dd, last_mp_descriptors, 32 * (size_t)M, cudaMemcpyHostToDevice,
+                                                m->stream));
+            }
+            d_mps = a;
+            d_mpd = dd;
+            if (claimed) {
+                uint8_t* c = b.take<uint8_t>(std::max(1, n));
+                if (n) ORBGPU_CUDA_TRY(cudaMemcpyAsync(c, claimed, n, cudaMemcpyHostToDevice, m->stream));
+                d_claimed = c;
+            }
+            d_match = b.take<int>(std::max(1, n));
+        }
+        if (n > 0) k_init_match_out<<<(n + 255) / 256, 256, 0, m->stream>>>(d_claimed, n, d_match);
+        int *start, *count, total = 0;
+        uint64_t* keys = nullptr;
+        auto launch = [&](const int* st, int* cnt, uint64_t* out, int fill) {
+            const int wpb = 8;
+            if (M > 0)
+                k_pf_candidates<<<(M + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, mo, d_lk, d_mps, d_mpd, M, th, st,
+                                                                              cnt, out, fill);
+        };
+        rc = candidate_lists(m, M, b, launch, start, count, keys, total);
+        if (rc == ORBGPU_ERR_CAPACITY) {
+            est = est + sizeof(uint64_t) * (size_t)total * 2;
+            continue;
+        }
+        if (rc) return rc;
+        int* d_nm = b.take<int>(1);
+        int* claims3 = b.take<int>((size_t)3 * std::max(1, n));
+        int* res = b.take<int>(std::max(1, M));
+        int* changed = b.take<int>(PROJ_ROUNDS);
+        int* owner = b.take<int>(std::max(1, n));
+        int* nulled = b.take<int>(std::max(1, n));
+        int* bin_of = b.take<int>(std::max(1, M));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(d_nm, 0, sizeof(int), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(claims3, 0x7f, sizeof(int) * (size_t)3 * std::max(1, n), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(res, 0xfe, sizeof(int) * std::max(1, M), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(changed, 0, sizeof(int) * PROJ_ROUNDS, m->stream));
+        if (M > 0 && n > 0) {
+            const int wpb = 8;
+            const int warps = std::max(M, (n + 31) / 32);
+            for (int r = 0; r < PROJ_ROUNDS; r++)
+                k_pf_round<<<(warps + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(n, M, start, count, keys, d_mps, r,
+                                                                              claims3, res, changed, d_match);
+            k_pf_serial<<<1, 32, 0, m->stream>>>(n, M, start, count, keys, d_mps, changed, res, claims3, d_match);
+            k_pf_finish<<<1, 1024, 0, m->stream>>>(n, M, res, d_lk, s.kps, m->check_ori, owner, bin_of, nulled, d_match,
+                                                   d_nm);
         }
         ORBGPU_CUDA_TRY(cudaGetLastError());
         if (mem != ORBGPU_MEM_DEVICE && n > 0)

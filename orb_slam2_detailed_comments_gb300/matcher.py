@@ -7,11 +7,16 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE, MEM_DEVICE, MEM_HOST, FrameStruct, check, lib, ptr
+from ._lib import (FRAME_MAPPOINT_DTYPE, KEYPOINT_DTYPE, MAPPOINT_DTYPE, MEM_DEVICE, MEM_HOST, FrameStruct,
+                   MotionStruct, check, lib, ptr)
 
 
 def _is_cuda(a) -> bool:
     return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+def _cpu(a):
+    return a.cpu().numpy() if _is_cuda(a) else a
 
 
 @dataclass
@@ -28,6 +33,20 @@ class FrameView:
     height: int
     scale_factors: object
     uright: object = None
+    # read by SearchByProjection(CurrentFrame, LastFrame, th, bMono) only:
+    # pose (rows 0-2 of mTcw), intrinsics and stereo constants of the frame,
+    # its map points (FRAME_MAPPOINT_DTYPE records, one per keypoint) with
+    # their descriptors, and which keypoints already hold an observed map point
+    Tcw: object = None
+    fx: float = 0.0
+    fy: float = 0.0
+    cx: float = 0.0
+    cy: float = 0.0
+    mbf: float = 0.0
+    mb: float = 0.0
+    mappoints: object = None
+    mp_descriptors: object = None
+    claimed: object = None
     _keep: list = field(default_factory=list, repr=False)
 
     def struct(self) -> FrameStruct:
@@ -94,11 +113,54 @@ class ORBmatcher:
               "orbgpu_search_for_initialization")
         return nm.value, m12[:s1.n], prev
 
-    def SearchByProjection(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0, claimed=None):
-        """SearchByProjection(Frame&, vector<MapPoint*>, th) -- src/ORBmatcher.cc:72-183.
+    def SearchByProjection(self, F: FrameView, second, *args, **kw):
+        """The two SearchByProjection overloads on a Frame:
 
-        Returns (nmatches, match) with match[i] the map point index assigned
-        to keypoint i (-2 pre-claimed, -1 none)."""
+        SearchByProjection(F, mappoints, mp_descriptors, th=1.0, claimed=None)
+            -- (Frame&, vector<MapPoint*>, th), src/ORBmatcher.cc:72-183;
+            match[i] = map point index assigned to keypoint i (-2 pre-claimed,
+            -1 none).
+        SearchByProjection(CurrentFrame, LastFrame, th, bMono)
+            -- (Frame&, const Frame&, th, bMono), src/ORBmatcher.cc:1710-1879;
+            match[i] = LastFrame keypoint whose map point fills
+            CurrentFrame.mvpMapPoints[i] (-1 not assigned, -2 pre-claimed, -4
+            reset by the rotation check).
+        Both return (nmatches, match)."""
+        if isinstance(second, FrameView):
+            return self._search_by_projection_frame(F, second, *args, **kw)
+        return self._search_by_projection_mappoints(F, second, *args, **kw)
+
+    def _search_by_projection_frame(self, CF: FrameView, LF: FrameView, th: float, bMono: bool):
+        sc, sl = CF.struct(), LF.struct()
+        dev = sc.mem == MEM_DEVICE
+        mo = MotionStruct()
+        for i, v in enumerate(np.asarray(_cpu(CF.Tcw), np.float32).reshape(-1)[:12]):
+            mo.Tcw[i] = float(v)
+        for i, v in enumerate(np.asarray(_cpu(LF.Tcw), np.float32).reshape(-1)[:12]):
+            mo.Tlw[i] = float(v)
+        mo.fx, mo.fy, mo.cx, mo.cy, mo.bf, mo.b = (float(np.float32(v)) for v in
+                                                   (CF.fx, CF.fy, CF.cx, CF.cy, CF.mbf, CF.mb))
+        nm = C.c_int(0)
+        if dev:
+            import torch
+            out = torch.empty(max(sc.n, 1), dtype=torch.int32, device="cuda")
+            mps, mpd, cl = LF.mappoints, LF.mp_descriptors, CF.claimed
+        else:
+            out = np.zeros(max(sc.n, 1), np.int32)
+            mps = np.ascontiguousarray(LF.mappoints, FRAME_MAPPOINT_DTYPE)
+            mpd = np.ascontiguousarray(LF.mp_descriptors, np.uint8)
+            cl = None if CF.claimed is None else np.ascontiguousarray(CF.claimed, np.uint8)
+        if sl.n and (int(mpd.shape[0]) < sl.n or
+                     (mps.nbytes if isinstance(mps, np.ndarray) else mps.numel() * mps.element_size()) < sl.n * 16):
+            raise ValueError("LastFrame needs one map point record and descriptor per keypoint")
+        check(lib().orbgpu_search_by_projection_frame(self._h, C.byref(sc), C.byref(sl), ptr(mps), ptr(mpd),
+                                                      C.byref(mo), C.c_float(th), int(bool(bMono)), ptr(cl), ptr(out),
+                                                      MEM_DEVICE if dev else MEM_HOST, C.byref(nm)),
+              "orbgpu_search_by_projection_frame")
+        return nm.value, out[:sc.n]
+
+    def _search_by_projection_mappoints(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0,
+                                        claimed=None):
         s = F.struct()
         dev = s.mem == MEM_DEVICE
         nm = C.c_int(0)

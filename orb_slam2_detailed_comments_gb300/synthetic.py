@@ -144,8 +144,7 @@ def stream_frames(w: int, h: int, seed: int, nframes: int, noise_sigma: float = 
     return out
 
 
-FRAME_MAPPOINT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("flags", "<i4")])
-MP_PRESENT, MP_OUTLIER, MP_OBSERVED = 1, 2, 4
+from ._lib import FRAME_MAPPOINT_DTYPE, MP_OBSERVED, MP_OUTLIER, MP_PRESENT  # noqa: E402
 
 
 def _rot(rx: float, ry: float, rz: float) -> np.ndarray:
@@ -228,3 +227,44 @@ def motion_case(kps: np.ndarray, desc: np.ndarray, w: int, h: int, seed: int, n_
     claimed = (rng.random(n) < claimed_p).astype(np.uint8)
     return dict(last_kps=last_kps, last_mps=mps, last_mp_desc=mpd, Tcw=Tcw, Tlw=Tlw, fx=fx, fy=fy, cx=cx, cy=cy,
                 bf=bf, b=b, uright=uright, claimed=claimed)
+
+
+def chain_case(k: int = 30, seed: int = 0, observed_every: int = 1):
+    """k current keypoints on one spot whose descriptors sit 0, 1, 2, ... bits
+    from a common descriptor D, and k LastFrame map points with descriptor D
+    projecting onto that spot (identity poses): in reference order map point i
+    takes keypoint i, so a parallel resolution needs k rounds.  Every
+    observed_every-th map point has observations (the others block nothing).
+    Returns (kps, desc, case dict as motion_case, w, h)."""
+    rng = np.random.default_rng(seed)
+    w, h = 640, 480
+    from ._lib import KEYPOINT_DTYPE
+    kps = np.zeros(k, KEYPOINT_DTYPE)
+    kps["x"] = 320.0 + rng.uniform(-1, 1, k).astype(np.float32)
+    kps["y"] = 240.0 + rng.uniform(-1, 1, k).astype(np.float32)
+    kps["size"] = 31.0
+    kps["angle"] = rng.uniform(0, 360, k).astype(np.float32)
+    kps["octave"] = 0
+    kps["class_id"] = -1
+    D = rng.integers(0, 256, 32, dtype=np.uint8)
+    desc = np.zeros((k, 32), np.uint8)
+    for j in range(k):
+        bits = np.zeros(256, bool)
+        bits[:j] = True
+        desc[j] = D ^ np.packbits(bits, bitorder="little")
+    fx = fy = 500.0
+    cx, cy = 320.0, 240.0
+    last_kps = np.zeros(k, KEYPOINT_DTYPE)
+    last_kps["octave"] = 0
+    last_kps["angle"] = (kps["angle"] + 5.0) % 360.0
+    mps = np.zeros(k, FRAME_MAPPOINT_DTYPE)
+    z = 10.0
+    mps["x"] = (320.0 - cx) * z / fx
+    mps["y"] = (240.0 - cy) * z / fy
+    mps["z"] = z
+    mps["flags"] = MP_PRESENT
+    mps["flags"][::observed_every] |= MP_OBSERVED
+    T = np.hstack([np.eye(3), np.zeros((3, 1))]).astype(np.float32)
+    case = dict(last_kps=last_kps, last_mps=mps, last_mp_desc=np.tile(D, (k, 1)), Tcw=T, Tlw=T, fx=fx, fy=fy, cx=cx,
+                cy=cy, bf=0.0, b=0.0, uright=None, claimed=np.zeros(k, np.uint8))
+    return kps, desc, case, w, h

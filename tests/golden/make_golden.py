@@ -6,7 +6,8 @@ stand-in (oracle/Makefile target ``ref``; needs the reference sources, so this
 script runs only where they are present).  Inputs are stored with the outputs,
 so the fixtures do not depend on the generator's random streams.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py projframe  # only the named groups
 """
 from __future__ import annotations
 
@@ -30,10 +31,26 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-def main():
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe")
+
+
+def main(groups=GROUPS):
     pyoracle.build(ref=True)
     R = RefOracle()
+    if any(g in groups for g in ("extract", "projection")):
+        base_fixtures(R, groups)
+    if "knn" in groups:
+        knn_fixture(R)
+    if "kat" in groups:
+        kat_fixture(R)
+    if "tables" in groups:
+        tables_fixture(R)
+    if "projframe" in groups:
+        projframe_fixture(R)
 
+
+def base_fixtures(R, groups):
+    # (extract, init, stereo and projection share their inputs)
     # 1. extraction, 640x480, nFeatures 1000 (and the pyramid, as level digests)
     f1, f2, H = syn.frame_pair(640, 480, seed=0)
     a = R.extract(f1, nfeatures=1000)
@@ -84,12 +101,16 @@ def main():
         out[f"match_th{th}"] = match
     save("projection_640x480.npz", mappoints=mps, mp_descriptors=mpd, claimed=claimed, uright=uright, **out)
 
+
+def knn_fixture(R):
     # 5. brute-force k=2 over DescriptorDistance
     q = syn.clustered_descriptors(200, 20, 0.1, seed=5)
     t = syn.clustered_descriptors(3000, 20, 0.1, seed=6)
     i1, d1, i2, d2 = R.knn2(q, t)
     save("knn_200x3000.npz", query=q, train=t, idx1=i1, d1=d1, idx2=i2, d2=d2)
 
+
+def kat_fixture(R):
     # 6. DescriptorDistance known answers on crafted bit patterns
     pats = [np.zeros(32, np.uint8), np.full(32, 255, np.uint8), np.tile(np.array([0x55], np.uint8), 32),
             np.tile(np.array([0xAA], np.uint8), 32), np.arange(32, dtype=np.uint8),
@@ -98,6 +119,8 @@ def main():
     dist = np.array([[R.descriptor_distance(x, y) for y in pats] for x in pats], np.int32)
     save("hamming_kat.npz", patterns=pa, distance=dist)
 
+
+def tables_fixture(R):
     # 7. tables of the ORBextractor constructor
     import ctypes as C
     for nf in (1000, 2000):
@@ -108,5 +131,34 @@ def main():
              features_per_level=arrs[4], umax=arrs[5])
 
 
+def projframe_fixture(R):
+    # 8. SearchByProjection(CurrentFrame, LastFrame, th, bMono): a stereo pair
+    # moving forward (th 15) and a monocular pair (th 7), rotation check on
+    from oracle.pyoracle import make_motion
+    cases = {}
+    for name, (w, h, nf, stereo, dz, th) in {"stereo_fwd_1241x376": (1241, 376, 2000, True, 2.0, 15.0),
+                                             "mono_640x480": (640, 480, 1000, False, 0.0, 7.0)}.items():
+        img = syn.scene(w, h, 40 + len(cases))
+        cur = R.extract(img, nfeatures=nf)
+        c = syn.motion_case(cur.keypoints, cur.descriptors, w, h, seed=50 + len(cases), stereo=stereo, dz=dz)
+        mo = make_motion(c["Tcw"], c["Tlw"], c["fx"], c["fy"], c["cx"], c["cy"], c["bf"], c["b"])
+        nm, match = R.search_by_projection_frame(cur.keypoints, cur.descriptors, w, h, c["last_kps"], c["last_mps"],
+                                                 c["last_mp_desc"], mo, th=th, mono=not stereo, check_ori=True,
+                                                 uright=c["uright"], claimed=c["claimed"])
+        ur = c["uright"] if c["uright"] is not None else np.zeros(0, np.float32)
+        cases[name] = dict(keypoints=cur.keypoints, descriptors=cur.descriptors, uright=ur, claimed=c["claimed"],
+                           last_keypoints=c["last_kps"], last_mappoints=c["last_mps"],
+                           last_mp_descriptors=c["last_mp_desc"], Tcw=c["Tcw"], Tlw=c["Tlw"],
+                           camera=np.array([c["fx"], c["fy"], c["cx"], c["cy"], c["bf"], c["b"]], np.float32),
+                           size=np.array([w, h]), th=np.float32(th), mono=np.array(not stereo),
+                           nmatches=np.array(nm), match=match)
+    for name, arrays in cases.items():
+        save(f"projframe_{name}.npz", **arrays)
+
+
 if __name__ == "__main__":
-    main()
+    sel = tuple(sys.argv[1:]) or GROUPS
+    bad = [g for g in sel if g not in GROUPS]
+    if bad:
+        raise SystemExit(f"unknown fixture groups {bad}; known: {GROUPS}")
+    main(sel)

@@ -222,3 +222,101 @@ def test_knn_tensor_cores_golden_and_ties(torch, golden):
     b = m.knn2(q, t, algo=1)
     for x, y in zip(a, b):
         assert torch.equal(x, y)
+
+
+# ----------------------------------------------------------------- SearchByProjection(CurrentFrame, LastFrame)
+def frame_pair_views(kps, desc, w, h, c, dev=False, torch=None):
+    """(CurrentFrame, LastFrame) views of a motion case (host or device arrays)."""
+    from orb_slam2_detailed_comments_gb300 import FrameView
+    s, _ = pyoracle.scale_tables(8, 1.2)
+    sf = np.array(s, np.float32)
+    ur = c["uright"]
+    lk, mps, mpd, cl = c["last_kps"], c["last_mps"], c["last_mp_desc"], c["claimed"]
+    if dev:
+        kps = torch.from_numpy(np.ascontiguousarray(kps).view(np.float32).reshape(-1, 7)).cuda()
+        desc = torch.from_numpy(np.ascontiguousarray(desc)).cuda()
+        ur = None if ur is None else torch.from_numpy(np.ascontiguousarray(ur)).cuda()
+        lk = torch.from_numpy(np.ascontiguousarray(lk).view(np.float32).reshape(-1, 7)).cuda()
+        mps = torch.from_numpy(np.ascontiguousarray(mps).view(np.uint8)).cuda()
+        mpd = torch.from_numpy(np.ascontiguousarray(mpd)).cuda()
+        cl = None if cl is None else torch.from_numpy(np.ascontiguousarray(cl)).cuda()
+    CF = FrameView(kps, desc, w, h, sf, ur, Tcw=c["Tcw"], fx=c["fx"], fy=c["fy"], cx=c["cx"], cy=c["cy"],
+                   mbf=c["bf"], mb=c["b"], claimed=cl)
+    LF = FrameView(lk, mpd, w, h, sf, None, Tcw=c["Tlw"], mappoints=mps, mp_descriptors=mpd)
+    return CF, LF
+
+
+@pytest.mark.parametrize("name", ["stereo_fwd_1241x376", "mono_640x480"])
+def test_projection_frame_golden(torch, golden, name):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    g = golden(f"projframe_{name}.npz")
+    w, h = (int(v) for v in g["size"])
+    cam = [float(v) for v in g["camera"]]
+    c = dict(uright=g["uright"] if len(g["uright"]) else None, last_kps=g["last_keypoints"],
+             last_mps=g["last_mappoints"], last_mp_desc=g["last_mp_descriptors"], claimed=g["claimed"],
+             Tcw=g["Tcw"], Tlw=g["Tlw"], fx=cam[0], fy=cam[1], cx=cam[2], cy=cam[3], bf=cam[4], b=cam[5])
+    for dev in (False, True):
+        CF, LF = frame_pair_views(g["keypoints"], g["descriptors"], w, h, c, dev=dev, torch=torch)
+        nm, match = ORBmatcher(0.9, True).SearchByProjection(CF, LF, float(g["th"]), bool(g["mono"]))
+        match = match.cpu().numpy() if dev else match
+        assert nm == int(g["nmatches"])
+        assert np.array_equal(match, g["match"])
+
+
+@pytest.mark.parametrize("stereo,dz,mono,th,ori,dev", [(True, 2.0, False, 15.0, True, True),
+                                                      (True, -2.0, False, 15.0, True, False),
+                                                      (True, 0.2, False, 15.0, False, True),
+                                                      (False, 0.0, True, 7.0, True, True),
+                                                      (False, 0.0, True, 7.0, False, False)])
+def test_projection_frame_vs_oracle(torch, oracle, stereo, dz, mono, th, ori, dev):
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    img = syn.scene(1280, 720, 81)
+    cur = oracle.extract(img, nfeatures=2000)
+    c = syn.motion_case(cur.keypoints, cur.descriptors, 1280, 720, seed=int(10 * dz) + 90, stereo=stereo, dz=dz)
+    mo = pyoracle.make_motion(c["Tcw"], c["Tlw"], c["fx"], c["fy"], c["cx"], c["cy"], c["bf"], c["b"])
+    ref = oracle.search_by_projection_frame(cur.keypoints, cur.descriptors, 1280, 720, c["last_kps"], c["last_mps"],
+                                            c["last_mp_desc"], mo, th=th, mono=mono, check_ori=ori,
+                                            uright=c["uright"], claimed=c["claimed"])
+    CF, LF = frame_pair_views(cur.keypoints, cur.descriptors, 1280, 720, c, dev=dev, torch=torch)
+    nm, match = ORBmatcher(0.9, ori).SearchByProjection(CF, LF, th, mono)
+    match = match.cpu().numpy() if dev else match
+    assert nm == ref[0]
+    assert np.array_equal(match, ref[1])
+
+
+@pytest.mark.parametrize("every", [1, 3])
+def test_projection_frame_deep_chain(torch, oracle, every):
+    """A 30-deep assignment chain: more than the parallel rounds, so the
+    sequential fallback decides; observed_every 3 mixes owners that block
+    nothing (they are overwritten, and counted, as in the reference)."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    kps, desc, c, w, h = syn.chain_case(30, seed=every, observed_every=every)
+    mo = pyoracle.make_motion(c["Tcw"], c["Tlw"], c["fx"], c["fy"], c["cx"], c["cy"], c["bf"], c["b"])
+    ref = oracle.search_by_projection_frame(kps, desc, w, h, c["last_kps"], c["last_mps"], c["last_mp_desc"], mo,
+                                            th=7.0, mono=True, check_ori=False)
+    CF, LF = frame_pair_views(kps, desc, w, h, c)
+    nm, match = ORBmatcher(0.9, False).SearchByProjection(CF, LF, 7.0, True)
+    assert nm == ref[0]
+    assert np.array_equal(match, ref[1])
+
+
+def test_projection_frame_edges(torch, oracle):
+    """No LastFrame keypoints; LastFrame without map points; no current keypoints."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    kps, desc, c, w, h = syn.chain_case(8, seed=5)
+    m = ORBmatcher(0.9, True)
+    empty = dict(c, last_kps=c["last_kps"][:0], last_mps=c["last_mps"][:0], last_mp_desc=c["last_mp_desc"][:0])
+    CF, LF = frame_pair_views(kps, desc, w, h, empty)
+    nm, match = m.SearchByProjection(CF, LF, 7.0, True)
+    assert nm == 0 and np.array_equal(match, np.full(8, -1))
+    none = dict(c, last_mps=c["last_mps"].copy())
+    none["last_mps"]["flags"] = 0
+    CF, LF = frame_pair_views(kps, desc, w, h, none)
+    nm, match = m.SearchByProjection(CF, LF, 7.0, True)
+    assert nm == 0 and np.array_equal(match, np.full(8, -1))
+    CF, LF = frame_pair_views(kps[:0], desc[:0], w, h, dict(c, claimed=c["claimed"][:0]))
+    nm, match = m.SearchByProjection(CF, LF, 7.0, True)
+    assert nm == 0 and len(match) == 0

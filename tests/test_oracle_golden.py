@@ -96,3 +96,52 @@ def test_oracle_matches_reference_on_fresh_seeds(oracle):
         b = oracle.extract(img, nfeatures=nf)
         assert a.keypoints.tobytes() == b.keypoints.tobytes()
         assert np.array_equal(a.descriptors, b.descriptors)
+
+
+def _projframe_args(g):
+    w, h = (int(v) for v in g["size"])
+    mo = pyoracle.make_motion(g["Tcw"], g["Tlw"], *[float(v) for v in g["camera"]])
+    ur = g["uright"] if len(g["uright"]) else None
+    return w, h, mo, ur
+
+
+@pytest.mark.parametrize("name", ["stereo_fwd_1241x376", "mono_640x480"])
+def test_search_by_projection_frame(oracle, golden, name):
+    g = golden(f"projframe_{name}.npz")
+    w, h, mo, ur = _projframe_args(g)
+    nm, match = oracle.search_by_projection_frame(g["keypoints"], g["descriptors"], w, h, g["last_keypoints"],
+                                                  g["last_mappoints"], g["last_mp_descriptors"], mo,
+                                                  th=float(g["th"]), mono=bool(g["mono"]), check_ori=True,
+                                                  uright=ur, claimed=g["claimed"])
+    assert nm == int(g["nmatches"])
+    assert np.array_equal(match, g["match"])
+    assert (match == -4).any() and (match >= 0).any()
+
+
+@pytest.mark.skipif(not pyoracle.ref_available(), reason="reference sources not built here")
+def test_search_by_projection_frame_reference_cases(oracle):
+    """Oracle against the reference build: forward / backward / static stereo,
+    monocular, rotation check on and off, and the k-deep assignment chain."""
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    R = pyoracle.RefOracle()
+    img = syn.scene(752, 480, 61)
+    cur = oracle.extract(img, nfeatures=1500)
+    for seed, (stereo, dz, mono, th) in enumerate([(True, 2.0, False, 15.0), (True, -2.0, False, 15.0),
+                                                    (True, 0.2, False, 15.0), (False, 0.0, True, 7.0)]):
+        c = syn.motion_case(cur.keypoints, cur.descriptors, 752, 480, seed=70 + seed, stereo=stereo, dz=dz)
+        mo = pyoracle.make_motion(c["Tcw"], c["Tlw"], c["fx"], c["fy"], c["cx"], c["cy"], c["bf"], c["b"])
+        for co in (True, False):
+            args = (cur.keypoints, cur.descriptors, 752, 480, c["last_kps"], c["last_mps"], c["last_mp_desc"], mo)
+            kw = dict(th=th, mono=mono, check_ori=co, uright=c["uright"], claimed=c["claimed"])
+            a = R.search_by_projection_frame(*args, **kw)
+            b = oracle.search_by_projection_frame(*args, **kw)
+            assert a[0] == b[0] and np.array_equal(a[1], b[1]), (seed, co)
+    for every in (1, 3):
+        kps, desc, c, w, h = syn.chain_case(30, seed=every, observed_every=every)
+        mo = pyoracle.make_motion(c["Tcw"], c["Tlw"], c["fx"], c["fy"], c["cx"], c["cy"], c["bf"], c["b"])
+        args = (kps, desc, w, h, c["last_kps"], c["last_mps"], c["last_mp_desc"], mo)
+        a = R.search_by_projection_frame(*args, th=7.0, mono=True, check_ori=False)
+        b = oracle.search_by_projection_frame(*args, th=7.0, mono=True, check_ori=False)
+        assert a[0] == b[0] and np.array_equal(a[1], b[1])
+        if every == 1:
+            assert np.array_equal(b[1], np.arange(30))
