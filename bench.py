@@ -206,7 +206,33 @@ def run_ours(args):
     total_ms = sum(times)
     value = NFRAMES * args.steps / (total_ms / 1e3)
 
-    # e2e: host images in pinned memory, copies inside the timed region
+    legs = LEGS if args.legs == "all" else set(args.legs.split(","))
+    e2e_value, h2d, d2h = None, 0, 0
+    if "e2e" in legs:
+        e2e_value, h2d, d2h = run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev,
+                                      nfs, cap)
+    per_frame_fps, per_frame_split = None, None
+    if "perframe" in legs:
+        per_frame_fps, per_frame_split = run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev)
+    extra = {}
+    for leg, fn in (("stereo", bench_stereo), ("knn", bench_knn), ("serving", bench_serving)):
+        if leg in legs:
+            try:
+                extra[LEG_KEYS[leg]] = fn(dev)
+            except Exception as e:  # reported, not fatal
+                extra[LEG_KEYS[leg]] = {"error": repr(e)}
+    return finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, per_frame_fps, per_frame_split,
+                  extra, mps_list, mpd_list, clk, batch, proj)
+
+
+LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "cpu"}
+LEG_KEYS = {"stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams"}
+
+
+def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev, nfs, cap):
+    """Host images in pinned memory, copies inside the timed region."""
+    import torch
+    dev = mps_dev.device
     pinned = [torch.from_numpy(img).pin_memory() for img, _ in frames]
     staging = [torch.empty_like(t, device=dev) for t in pinned]
     kps_host = torch.empty((NFRAMES * cap, 7), dtype=torch.float32).pin_memory()
@@ -244,9 +270,13 @@ def run_ours(args):
         e2e_step()
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_value = NFRAMES * args.steps / sum(e2e_times)
+    return NFRAMES * args.steps / sum(e2e_times), h2d, d2h
 
-    # per-frame plain path on the same frames (the drop-in path), for the batching gain
+
+def run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev):
+    """The plain per-frame path on the same frames (the drop-in path), for the batching gain."""
+    import torch
+    from orb_slam2_detailed_comments_gb300 import FrameView, ORBextractor, ORBmatcher
     matcher = ORBmatcher(0.8, True)
     exs = {nf: ORBextractor(nf, 1.2, 8, 20, 7, 1280, 720) for nf in NFEATURES}
     sc = exs[NFEATURES[0]].GetScaleFactors()
@@ -270,21 +300,11 @@ def run_ours(args):
     per_frame_fps = NFRAMES / (per_frame_ms[best] / 1e3)
     per_frame_split = {"extract_ms_per_frame": ext_ms[best] / NFRAMES,
                        "match_ms_per_frame": (per_frame_ms[best] - ext_ms[best]) / NFRAMES}
+    return per_frame_fps, per_frame_split
 
-    extra = {}
-    try:
-        extra["stereo_1241x376"] = bench_stereo(dev)
-    except Exception as e:  # reported, not fatal
-        extra["stereo_1241x376"] = {"error": repr(e)}
-    try:
-        extra["knn_50kx200k"] = bench_knn(dev)
-    except Exception as e:
-        extra["knn_50kx200k"] = {"error": repr(e)}
-    try:
-        extra["serving_32_streams"] = bench_serving(dev)
-    except Exception as e:
-        extra["serving_32_streams"] = {"error": repr(e)}
 
+def finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, per_frame_fps, per_frame_split,
+           extra, mps_list, mpd_list, clk, batch, proj):
     # roofline of the dominant stage
     pk, pk_src = peaks()
     dom = max(stage_ms, key=stage_ms.get) if stage_ms else None
@@ -296,7 +316,7 @@ def run_ours(args):
                 "peak_source": pk_src, "stage_ms_per_step": {k: v / max(1, args.steps) for k, v in stage_ms.items()}}
 
     # CPU baseline: the oracle restatement on a bounded sample, one thread
-    cpu = cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1)
+    cpu = cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1) if "cpu" in legs else None
 
     launches = (batch.launches_per_extract() + proj.launches_per_search()) * args.steps
     line = {
@@ -308,7 +328,7 @@ def run_ours(args):
                    "frames_per_step": NFRAMES, "l2": "flushed (256 MiB write) between timed steps"},
         "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "per_frame_path_fps": per_frame_fps, "per_frame_split": per_frame_split,
-        "batched_over_per_frame": value / per_frame_fps, "other_configs": extra,
+        "batched_over_per_frame": value / per_frame_fps if per_frame_fps else None, "other_configs": extra,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
     }
     print(json.dumps(line))
@@ -482,12 +502,18 @@ def run_reference(args):
 
 
 def main():
+    global NFRAMES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=NFRAMES,
+                    help="frames per step (the reported workload is 64; other values are for profiling)")
+    ap.add_argument("--legs", default="all",
+                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,cpu) or 'all'")
     args = ap.parse_args()
+    NFRAMES = args.frames
     if args.impl == "reference":
         run_reference(args)
         return

@@ -302,7 +302,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     for (int f = 0; f < nframes; f++)
         for (int l = 0; l < nlevels; l++) {
             pre.push_back(acc);
-            acc += b->cur[f]->geom[l].ncells;
+            acc += (b->cur[f]->geom[l].ncells + ORBGPU_FAST_CELLS_PER_BLOCK - 1) / ORBGPU_FAST_CELLS_PER_BLOCK;
         }
     pre.push_back(acc);
     b->fast_count = acc;
@@ -579,62 +579,66 @@ __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* de
 
 __global__ void k_bproj_round(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off,
                               int slot_cap, const uint64_t* slots, const int* slot_count, float nnratio, int round,
-                              int* claims3, int* res, int* changed, int* nwarp_frame) {
+                              int* claims3, int* res, int* changed) {
     const int f = blockIdx.y;
     const int lane = threadIdx.x & 31;
-    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int wpf = gridDim.x * (blockDim.x >> 5);  // warps of this frame
+    const int w0 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int n_mp = mp_off[f + 1] - mp_off[f];
     if (round > 0 && changed[(round - 1) * gridDim.y + f] == 0) return;  // converged
     int* claims_r = claims3 + (size_t)((round + 0) % 3) * gridDim.y * cap + (size_t)f * cap;
     int* claims_w = claims3 + (size_t)((round + 1) % 3) * gridDim.y * cap + (size_t)f * cap;
     int* claims_z = claims3 + (size_t)((round + 2) % 3) * gridDim.y * cap + (size_t)f * cap;
     // clear the array the next round writes into
-    for (int i = local * 32 + lane; i < cap; i += (*nwarp_frame) * 32) claims_z[i] = BPROJ_NONE;
-    if (local >= n_mp) return;
-    const int imp = mp_off[f] + local;
+    for (int i = w0 * 32 + lane; i < cap; i += wpf * 32) claims_z[i] = BPROJ_NONE;
     const orbgpu_keypoint* K = kps + (size_t)f * cap;
-    const int cnt = min(slot_count[imp], slot_cap);
-    const uint64_t* S = slots + (size_t)imp * slot_cap;
-    uint64_t best = ~0ull, second = ~0ull;
-    for (int b = 0; b < cnt; b += 32) {
-        uint64_t key = ~0ull;
-        if (b + lane < cnt) {
-            key = S[b + lane];
-            if (claims_r[(int)(key & 0xFFFFF)] < local || (int)(key >> 40) >= 256) key = ~0ull;
+    bool any_change = false;
+    for (int local = w0; local < n_mp; local += wpf) {
+        const int imp = mp_off[f] + local;
+        const int cnt = min(slot_count[imp], slot_cap);
+        const uint64_t* S = slots + (size_t)imp * slot_cap;
+        uint64_t best = ~0ull, second = ~0ull;
+        for (int b = 0; b < cnt; b += 32) {
+            uint64_t key = ~0ull;
+            if (b + lane < cnt) {
+                key = S[b + lane];
+                if (claims_r[(int)(key & 0xFFFFF)] < local || (int)(key >> 40) >= 256) key = ~0ull;
+            }
+            if (key < best) {
+                second = best;
+                best = key;
+            } else if (key < second) {
+                second = key;
+            }
         }
-        if (key < best) {
-            second = best;
-            best = key;
-        } else if (key < second) {
-            second = key;
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
+            if (ob < best) {
+                second = best < os ? best : os;
+                best = ob;
+            } else {
+                second = second < ob ? second : ob;
+            }
+        }
+        int r = -1;
+        if (best != ~0ull) {
+            const int bestDist = (int)(best >> 40);
+            const int bestIdx = (int)(best & 0xFFFFF);
+            const int bestLevel = K[bestIdx].octave;
+            const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
+            const int bestLevel2 = second == ~0ull ? -1 : K[(int)(second & 0xFFFFF)].octave;
+            if (bestDist <= ORBGPU_TH_HIGH &&
+                !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
+                r = bestIdx;
+        }
+        if (lane == 0) {
+            if (res[imp] != r) any_change = true;
+            res[imp] = r;
+            if (r >= 0) atomicMin(&claims_w[r], local);
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
-        if (ob < best) {
-            second = best < os ? best : os;
-            best = ob;
-        } else {
-            second = second < ob ? second : ob;
-        }
-    }
-    int r = -1;
-    if (best != ~0ull) {
-        const int bestDist = (int)(best >> 40);
-        const int bestIdx = (int)(best & 0xFFFFF);
-        const int bestLevel = K[bestIdx].octave;
-        const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
-        const int bestLevel2 = second == ~0ull ? -1 : K[(int)(second & 0xFFFFF)].octave;
-        if (bestDist <= ORBGPU_TH_HIGH &&
-            !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
-            r = bestIdx;
-    }
-    if (lane == 0) {
-        if (res[imp] != r) changed[round * gridDim.y + f] = 1;
-        res[imp] = r;
-        if (r >= 0) atomicMin(&claims_w[r], local);
-    }
+    if (lane == 0 && any_change) changed[round * gridDim.y + f] = 1;
 }
 
 // Writes match_out / nmatches from the converged results; frames that did
@@ -774,7 +778,6 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         int* claims3 = (int*)take(sizeof(int) * (size_t)3 * nf * cap);
         int* res = (int*)take(sizeof(int) * std::max(1, total_mp));
         int* changed = (int*)take(sizeof(int) * BPROJ_ROUNDS * nf);
-        int* nwarp = (int*)take(sizeof(int) * 2);
         std::vector<BatchFrameInfo> hi(nf);
         for (int f = 0; f < nf; f++) {
             const int w = b->sig[6 + 3 * f], h = b->sig[7 + 3 * f];
@@ -803,16 +806,16 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         }
         // fixed-point rounds, then the result write-out (serial replay for any
         // frame that did not converge)
-        const int warps = std::max((std::max(1, max_mp) + wpb - 1) / wpb * wpb, ((cap + 31) / 32 + wpb - 1) / wpb * wpb);
-        P.h_pinned[1] = warps;
-        ORBGPU_CUDA_TRY(cudaMemcpyAsync(nwarp, &P.h_pinned[1], sizeof(int), cudaMemcpyHostToDevice, st));
+        // one warp per map point (a round is a chain of dependent loads per
+        // map point, so width beats a grid-stride loop)
+        const int per_frame_blocks = std::max(1, (std::max(1, max_mp) + wpb - 1) / wpb);
         ORBGPU_CUDA_TRY(cudaMemsetAsync(claims3, 0x7f, sizeof(int) * (size_t)3 * nf * cap, st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(res, 0xfe, sizeof(int) * std::max(1, total_mp), st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(changed, 0, sizeof(int) * BPROJ_ROUNDS * nf, st));
-        dim3 gr(warps / wpb, nf);
+        dim3 gr(per_frame_blocks, nf);
         for (int r = 0; r < BPROJ_ROUNDS; r++)
             k_bproj_round<<<gr, 32 * wpb, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, r,
-                                                  claims3, res, changed, nwarp);
+                                                  claims3, res, changed);
         k_bproj_finish<<<nf, 32, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, changed, res,
                                          match_out, nmatches, status);
         ORBGPU_CUDA_TRY(cudaGetLastError());

@@ -176,6 +176,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         LevelOffsets& o = lv[l];
         o.pyr = take((size_t)L.pitch * L.h);
         o.blur = take((size_t)L.pitch * L.h);
+        o.strength = take((size_t)L.pitch * L.h);
         o.xofs = take(sizeof(int) * L.w);
         o.xalpha = take(sizeof(short) * 2 * L.w);
         o.yofs = take(sizeof(int) * L.h);
@@ -217,6 +218,7 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         }
         d.dst = arena + o.pyr;
         d.blur = arena + o.blur;
+        d.strength = arena + o.strength;
         d.w = L.w;
         d.h = L.h;
         d.pitch = L.pitch;
@@ -442,7 +444,7 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     int acc = 0;
     for (size_t l = 0; l < g.size(); l++) {
         pre.push_back(acc);
-        acc += g[l].ncells;
+        acc += (g[l].ncells + ORBGPU_FAST_CELLS_PER_BLOCK - 1) / ORBGPU_FAST_CELLS_PER_BLOCK;
     }
     pre.push_back(acc);
     P->fast_count = acc;

@@ -1,4 +1,6 @@
 // orbgpu_extract_kernels.cu -- the ORB extraction stages (see the .cuh).
+#include <algorithm>
+
 #include "orbgpu_extract_kernels.cuh"
 #include "orb_pattern.h"
 #include "orbgpu_host.h"
@@ -62,47 +64,6 @@ __device__ __forceinline__ void map_item(const RangeMap& rm, int b, int& desc, i
     }
     desc = rm.desc0 + lo * rm.desc_stride;
     index = b - rm.prefix[lo];
-}
-
-__global__ void __launch_bounds__(256) k_level_resize_blur(const LevelDesc* descs, RangeMap rm, int level0) {
-    WorkItem it;
-    map_item(rm, blockIdx.x, it.desc, it.index);
-    const LevelDesc& d = descs[it.desc];
-    const int tiles_x = (d.w + RB_TW - 1) / RB_TW;
-    const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH;
-    __shared__ uint8_t tile[RB_TH + 2 * RB_HALO][RB_TW + 2 * RB_HALO];
-    __shared__ int rows[RB_TH + 2 * RB_HALO][RB_TW];
-    const int TW = RB_TW + 2 * RB_HALO, TH = RB_TH + 2 * RB_HALO;
-    for (int i = threadIdx.x; i < TW * TH; i += blockDim.x) {
-        const int ty = i / TW, tx = i % TW;
-        const int x = reflect101(ox - RB_HALO + tx, d.w), y = reflect101(oy - RB_HALO + ty, d.h);
-        int v;
-        if (level0) v = d.dst[(size_t)y * d.pitch + x];
-        else v = resize_pixel(d, x, y);
-        tile[ty][tx] = (uint8_t)v;
-        const int gx = ox - RB_HALO + tx, gy = oy - RB_HALO + ty;
-        if (!level0 && tx >= RB_HALO && tx < RB_HALO + RB_TW && ty >= RB_HALO && ty < RB_HALO + RB_TH && gx < d.w && gy < d.h)
-            d.dst[(size_t)gy * d.pitch + gx] = (uint8_t)v;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < RB_TW * TH; i += blockDim.x) {
-        const int ty = i / RB_TW, tx = i % RB_TW;
-        int s = 0;
-#pragma unroll
-        for (int k = 0; k < 7; k++) s += c_gauss_taps[k] * tile[ty][tx + k];
-        rows[ty][tx] = s;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < RB_TW * RB_TH; i += blockDim.x) {
-        const int ty = i / RB_TW, tx = i % RB_TW;
-        const int gx = ox + tx, gy = oy + ty;
-        if (gx >= d.w || gy >= d.h) continue;
-        int s = 0;
-#pragma unroll
-        for (int k = 0; k < 7; k++) s += c_gauss_taps[k] * rows[ty + k][tx];
-        s = (s + (1 << 15)) >> 16;
-        d.blur[(size_t)gy * d.pitch + gx] = (uint8_t)(s < 0 ? 0 : (s > 255 ? 255 : s));
-    }
 }
 
 // ---------------------------------------------------------------- FAST
@@ -206,6 +167,225 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
     return a > b ? a : b;
 }
 
+// ---------------------------------------------------------------- resize + blur + FAST strength
+// One 64 x 16 tile of level l per block of 256 threads.  Shared memory holds
+// the level pixels of the tile with a 3-pixel ring (REFLECT_101 outside the
+// level) in rows of 72 bytes covering columns [ox - 4, ox + 68), so every
+// 4-pixel group of the core is one aligned 32-bit word:
+//  * fill: level 0 copies the image (aligned words for interior tiles);
+//    levels >= 1 stage the source block of level l-1 that the tile's
+//    bilinear taps touch, with per-column and per-row tap tables, and
+//    resize from shared memory (the fixed-point INTER_LINEAR formula);
+//  * the core is written to the level plane, blurred with the 7x7
+//    fixed-point Gaussian (horizontal pass 4 outputs per thread from three
+//    words, vertical pass 4 outputs per thread from seven int4 rows) into
+//    the blurred plane, and scored with the FAST arc strength at the lower
+//    threshold into the strength plane: a byte-SIMD compass-point test of 4
+//    pixels per thread queues the candidates, the full segment test scores
+//    them.  The ring is exactly the radius-3 circle, so every pixel whose
+//    circle lies inside the level is scored (others get 0 and are never
+//    read by the cell stage).
+#define RB_SW 72                       // shared row: columns [ox - 4, ox + 68)
+#define RB_SH (RB_TH + 2 * RB_HALO)    // 22 rows: [oy - 3, oy + 19)
+#define RB_SRC_W 96                    // staged source columns (72 taps x 1.25 + 2, word aligned)
+#define RB_SRC_H 32                    // staged source rows (22 taps x 1.25 + 2)
+
+__device__ __forceinline__ int byte_of(uint32_t w, int j) { return (int)((w >> (8 * j)) & 0xFFu); }
+
+__global__ void __launch_bounds__(256, 5) k_level_resize_blur(const LevelDesc* descs, RangeMap rm, int level0) {
+    WorkItem it;
+    map_item(rm, blockIdx.x, it.desc, it.index);
+    const LevelDesc& d = descs[it.desc];
+    const int tiles_x = (d.w + RB_TW - 1) / RB_TW;
+    const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH;
+    __shared__ __align__(16) uint8_t tile[RB_SH][RB_SW];
+    __shared__ __align__(16) int rows[RB_SH][RB_TW];
+    __shared__ __align__(16) uint8_t s_str[RB_TH][RB_TW];
+    __shared__ __align__(16) uint8_t src_s[RB_SRC_H][RB_SRC_W];
+    __shared__ uint16_t s_q[RB_TH * RB_TW];
+    __shared__ short c_sx[RB_SW], c_sx1[RB_SW], c_a0[RB_SW], c_a1[RB_SW];
+    __shared__ short r_r0[RB_SH], r_r1[RB_SH], r_b0[RB_SH], r_b1[RB_SH];
+    __shared__ int s_rng[4];
+    __shared__ int s_nq;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_nq = 0;
+    if (level0) {
+        if (ox >= 4 && ox + 68 <= d.w && oy >= 3 && oy + RB_TH + 3 <= d.h) {
+            for (int i = tid; i < RB_SH * (RB_SW / 4); i += blockDim.x) {
+                const int ty = i / (RB_SW / 4), wx = i - ty * (RB_SW / 4);
+                *reinterpret_cast<uint32_t*>(&tile[ty][4 * wx]) =
+                    *reinterpret_cast<const uint32_t*>(d.dst + (size_t)(oy - 3 + ty) * d.pitch + ox - 4 + 4 * wx);
+            }
+        } else {
+            for (int i = tid; i < RB_SH * RB_SW; i += blockDim.x) {
+                const int ty = i / RB_SW, tx = i - ty * RB_SW;
+                tile[ty][tx] = d.dst[(size_t)reflect101(oy - 3 + ty, d.h) * d.pitch + reflect101(ox - 4 + tx, d.w)];
+            }
+        }
+        __syncthreads();
+    } else {
+        if (tid < 4) s_rng[tid] = (tid & 1) ? -1 : 0x7fffffff;
+        __syncthreads();
+        if (tid < RB_SW) {
+            const int x = reflect101(ox - 4 + tid, d.w);
+            const int sx = d.xofs[x];
+            const int sx1 = min(sx + 1, d.sw - 1);
+            c_sx[tid] = (short)sx;
+            c_sx1[tid] = (short)sx1;
+            c_a0[tid] = d.xalpha[2 * x];
+            c_a1[tid] = d.xalpha[2 * x + 1];
+            atomicMin(&s_rng[0], sx);
+            atomicMax(&s_rng[1], sx1);
+        } else if (tid >= 128 && tid < 128 + RB_SH) {
+            const int ty = tid - 128;
+            const int y = reflect101(oy - 3 + ty, d.h);
+            const int sy = d.yofs[y];
+            const int r0 = min(max(sy, 0), d.sh - 1), r1 = min(max(sy + 1, 0), d.sh - 1);
+            r_r0[ty] = (short)r0;
+            r_r1[ty] = (short)r1;
+            r_b0[ty] = d.ybeta[2 * y];
+            r_b1[ty] = d.ybeta[2 * y + 1];
+            atomicMin(&s_rng[2], r0);
+            atomicMax(&s_rng[3], r1);
+        }
+        __syncthreads();
+        const int cx0 = s_rng[0] & ~3, ry0 = s_rng[2];
+        const int nwc = (s_rng[1] - cx0) / 4 + 1, nr = s_rng[3] - ry0 + 1;
+        if (nwc * 4 <= RB_SRC_W && nr <= RB_SRC_H) {
+            // the words end at the multiple of 4 above the last tap column, inside the row's pitch
+            for (int i = tid; i < nr * nwc; i += blockDim.x) {
+                const int r = i / nwc, wc = i - r * nwc;
+                *reinterpret_cast<uint32_t*>(&src_s[r][4 * wc]) =
+                    *reinterpret_cast<const uint32_t*>(d.src + (size_t)(ry0 + r) * d.spitch + cx0 + 4 * wc);
+            }
+            __syncthreads();
+            for (int i = tid; i < RB_SH * RB_SW; i += blockDim.x) {
+                const int ty = i / RB_SW, tx = i - ty * RB_SW;
+                const uint8_t* S0 = src_s[r_r0[ty] - ry0];
+                const uint8_t* S1 = src_s[r_r1[ty] - ry0];
+                const int sx = c_sx[tx] - cx0, sx1 = c_sx1[tx] - cx0, a0 = c_a0[tx], a1 = c_a1[tx];
+                const int h0 = S0[sx] * a0 + S0[sx1] * a1;
+                const int h1 = S1[sx] * a0 + S1[sx1] * a1;
+                const int v = (h0 * r_b0[ty] + h1 * r_b1[ty] + (1 << 21)) >> 22;
+                tile[ty][tx] = (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
+            }
+        } else {
+            // a source block larger than the staging area (not met by 1.2 scale steps)
+            for (int i = tid; i < RB_SH * RB_SW; i += blockDim.x) {
+                const int ty = i / RB_SW, tx = i - ty * RB_SW;
+                tile[ty][tx] = (uint8_t)resize_pixel(d, reflect101(ox - 4 + tx, d.w), reflect101(oy - 3 + ty, d.h));
+            }
+        }
+        __syncthreads();
+        // the core into the level plane (bytes past the level width land in the row padding)
+        {
+            const int ty = tid >> 4, g = tid & 15;
+            if (oy + ty < d.h)
+                *reinterpret_cast<uint32_t*>(d.dst + (size_t)(oy + ty) * d.pitch + ox + 4 * g) =
+                    *reinterpret_cast<const uint32_t*>(&tile[ty + RB_HALO][4 + 4 * g]);
+        }
+    }
+    int taps[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) taps[k] = c_gauss_taps[k];
+    // horizontal pass: output x = ox + 4g + j reads columns 4g + 1 + j + k
+    for (int i = tid; i < RB_SH * (RB_TW / 4); i += blockDim.x) {
+        const int ty = i >> 4, g = i & 15;
+        const uint32_t* R = reinterpret_cast<const uint32_t*>(&tile[ty][0]);
+        const uint32_t w0 = R[g], w1 = R[g + 1], w2 = R[g + 2];
+        int bb[12];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            bb[j] = byte_of(w0, j);
+            bb[4 + j] = byte_of(w1, j);
+            bb[8 + j] = byte_of(w2, j);
+        }
+        int4 o;
+        int acc[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int sacc = 0;
+#pragma unroll
+            for (int k = 0; k < 7; k++) sacc += taps[k] * bb[1 + j + k];
+            acc[j] = sacc;
+        }
+        o.x = acc[0];
+        o.y = acc[1];
+        o.z = acc[2];
+        o.w = acc[3];
+        *reinterpret_cast<int4*>(&rows[ty][4 * g]) = o;
+    }
+    // FAST, phase 1: byte-SIMD compass-point test of 4 pixels per thread
+    const int t_lo = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
+    const int lane = tid & 31;
+    {
+        const int ty = tid >> 4, g = tid & 15;
+        const uint32_t* R = reinterpret_cast<const uint32_t*>(&tile[ty + RB_HALO][0]);
+        const uint32_t c = R[g + 1], left = R[g], right = R[g + 2];
+        const uint32_t p0 = reinterpret_cast<const uint32_t*>(&tile[ty + 2 * RB_HALO][0])[g + 1];  // row + 3
+        const uint32_t p8 = reinterpret_cast<const uint32_t*>(&tile[ty][0])[g + 1];               // row - 3
+        const uint32_t p4 = __funnelshift_r(c, right, 24);                                        // column + 3
+        const uint32_t p12 = __funnelshift_r(left, c, 8);                                         // column - 3
+        const uint32_t t4 = (uint32_t)t_lo * 0x01010101u;
+        const uint32_t hi = __vaddus4(c, t4), lo = __vsubus4(c, t4);
+        const uint32_t b0 = __vcmpgtu4(p0, hi), b4 = __vcmpgtu4(p4, hi), b8 = __vcmpgtu4(p8, hi), b12 = __vcmpgtu4(p12, hi);
+        const uint32_t d0 = __vcmpltu4(p0, lo), d4 = __vcmpltu4(p4, lo), d8 = __vcmpltu4(p8, lo), d12 = __vcmpltu4(p12, lo);
+        const uint32_t cand = (b0 & b4) | (b4 & b8) | (b8 & b12) | (b12 & b0) | (d0 & d4) | (d4 & d8) | (d8 & d12) |
+                              (d12 & d0);
+        const int gy = oy + ty;
+        const bool row_ok = gy >= 3 && gy < d.h - 3;
+        *reinterpret_cast<uint32_t*>(&s_str[ty][4 * g]) = 0u;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int gx = ox + 4 * g + j;
+            const bool cj = row_ok && gx >= 3 && gx < d.w - 3 && byte_of(cand, j) != 0;
+            const unsigned m = __ballot_sync(0xffffffffu, cj);
+            if (m) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&s_nq, __popc(m));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (cj) s_q[base + __popc(m & ((1u << lane) - 1))] = (uint16_t)(ty * RB_TW + 4 * g + j);
+            }
+        }
+    }
+    __syncthreads();
+    // vertical pass: 4 outputs of one row per thread
+    {
+        const int ty = tid >> 4, g = tid & 15;
+        int acc[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 7; k++) {
+            const int4 r = *reinterpret_cast<const int4*>(&rows[ty + k][4 * g]);
+            acc[0] += taps[k] * r.x;
+            acc[1] += taps[k] * r.y;
+            acc[2] += taps[k] * r.z;
+            acc[3] += taps[k] * r.w;
+        }
+        uint32_t packed = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int v = (acc[j] + (1 << 15)) >> 16;
+            v = v < 0 ? 0 : (v > 255 ? 255 : v);
+            packed |= (uint32_t)v << (8 * j);
+        }
+        if (oy + ty < d.h) *reinterpret_cast<uint32_t*>(d.blur + (size_t)(oy + ty) * d.pitch + ox + 4 * g) = packed;
+    }
+    // FAST, phase 2: full segment test and strength of the queued pixels
+    const int nq = s_nq;
+    for (int q = tid; q < nq; q += blockDim.x) {
+        const int i = s_q[q];
+        const int ty = i / RB_TW, tx = i % RB_TW;
+        s_str[ty][tx] = (uint8_t)arc_strength(&tile[0][0], RB_SW, ty + RB_HALO, tx + 4, t_lo);
+    }
+    __syncthreads();
+    {
+        const int ty = tid >> 4, g = tid & 15;
+        if (oy + ty < d.h)
+            *reinterpret_cast<uint32_t*>(d.strength + (size_t)(oy + ty) * d.pitch + ox + 4 * g) =
+                *reinterpret_cast<const uint32_t*>(&s_str[ty][4 * g]);
+    }
+}
+
 #define FAST_MAX_ROI 72
 #define FAST_MAX_DET (FAST_MAX_ROI - 6)
 
@@ -231,14 +411,23 @@ __device__ __forceinline__ bool fast_keep(const uint8_t* mstr, int dw, int dh, i
     return true;
 }
 
-// Rows are spread over warps and columns over lanes, so no index needs a
-// division; the row-major emission order of the detector is rebuilt from
-// per-row counts.
-__global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
+// The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142)
+// on the strength plane: one warp per cell.  The cell's detection region
+// (its ROI minus the 3-pixel ring) is staged in shared memory, suppressed at
+// iniThFAST and, when that leaves nothing, at minThFAST; survivors are
+// written row by row in the detector's row-major order with a running warp
+// count (no block-wide scan).
+__global__ void __launch_bounds__(32 * ORBGPU_FAST_CELLS_PER_BLOCK)
+    k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
-    const int cell = it.index;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
+    const int cell = it.index * ORBGPU_FAST_CELLS_PER_BLOCK + warp;
+    if (cell >= d.nCols * d.nRows) return;
+    __shared__ uint8_t s_m[ORBGPU_FAST_CELLS_PER_BLOCK][FAST_MAX_DET * FAST_MAX_DET];
+    uint8_t* mstr = s_m[warp];
     const int i = cell / d.nCols, j = cell - (cell / d.nCols) * d.nCols;
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
     const int iniY = minB + i * d.hCell, iniX = minB + j * d.wCell;
@@ -248,101 +437,44 @@ __global__ void __launch_bounds__(128) k_fast_cells(const LevelDesc* descs, Rang
     if (maxX > d.maxBorderX) maxX = d.maxBorderX;
     const int rw = maxX - iniX, rh = maxY - iniY;
     if (skip || rw < 7 || rh < 7 || rw > FAST_MAX_ROI || rh > FAST_MAX_ROI) {
-        if (threadIdx.x == 0) {
+        if (lane == 0) {
             d.cell_count[cell] = 0;
             if (!skip && (rw > FAST_MAX_ROI || rh > FAST_MAX_ROI)) atomicOr(status, 1);
         }
         return;
     }
-    __shared__ uint8_t roi[FAST_MAX_ROI * FAST_MAX_ROI];
-    __shared__ uint8_t mstr[FAST_MAX_DET * FAST_MAX_DET];
-    __shared__ uint16_t s_queue[FAST_MAX_DET * FAST_MAX_DET];
-    __shared__ int s_rowoff[FAST_MAX_DET + 1];
-    __shared__ int s_nq;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const unsigned lt = (1u << lane) - 1;
-    for (int r = warp; r < rh; r += nw) {
-        const uint8_t* src = d.dst + (size_t)(iniY + r) * d.pitch + iniX;
-        for (int c = lane; c < rw; c += 32) roi[r * rw + c] = src[c];
-    }
-    if (threadIdx.x == 0) s_nq = 0;
-    __syncthreads();
     const int dw = rw - 6, dh = rh - 6;
-    const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
-    const int t_lo = min(ini_th, min_th);
-    // Phase 1: compass-point test for every pixel; survivors are queued.
-    for (int r = warp; r < dh; r += nw)
-        for (int c0 = 0; c0 < dw; c0 += 32) {
-            const int c = c0 + lane;
-            bool cand = false;
-            if (c < dw) {
-                mstr[r * dw + c] = 0;
-                cand = compass_test(roi + (r + 3) * rw + c + 3, rw, t_lo);
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, cand);
-            if (m) {
-                int base = 0;
-                if (lane == 0) base = atomicAdd(&s_nq, __popc(m));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (cand) s_queue[base + __popc(m & lt)] = (uint16_t)(r * dw + c);
-            }
-        }
-    __syncthreads();
-    // Phase 2: full segment test and arc strength for the queued pixels.
-    const int nq = s_nq;
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-        const int k = s_queue[q];
-        const int r = k / dw, c = k - (k / dw) * dw;
-        mstr[k] = (uint8_t)arc_strength(roi, rw, r + 3, c + 3, t_lo);
+    for (int r = 0; r < dh; r++) {
+        const uint8_t* src = d.strength + (size_t)(iniY + 3 + r) * d.pitch + iniX + 3;
+        for (int c = lane; c < dw; c += 32) mstr[r * dw + c] = src[c];
     }
-    __syncthreads();
+    __syncwarp();
+    const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
     uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
     for (int pass = 0; pass < 2; pass++) {
         const int th = pass == 0 ? ini_th : min_th;
-        // survivors per detection row
-        for (int r = warp; r < dh; r += nw) {
-            int cnt = 0;
-            for (int c0 = 0; c0 < dw; c0 += 32) {
-                const int c = c0 + lane;
-                const bool keep = c < dw && fast_keep(mstr, dw, dh, r, c, th);
-                cnt += __popc(__ballot_sync(0xffffffffu, keep));
-            }
-            if (lane == 0) s_rowoff[r + 1] = cnt;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            s_rowoff[0] = 0;
-            for (int r = 0; r < dh; r++) s_rowoff[r + 1] += s_rowoff[r];
-        }
-        __syncthreads();
-        int total = s_rowoff[dh];
-        if (total == 0 && pass == 0) {
-            __syncthreads();
-            continue;
-        }
-        if (total > d.cell_cap) {
-            if (threadIdx.x == 0) atomicOr(status, 2);
-            total = d.cell_cap;
-        }
-        for (int r = warp; r < dh; r += nw) {
-            int base = s_rowoff[r];
+        int total = 0;
+        for (int r = 0; r < dh; r++)
             for (int c0 = 0; c0 < dw; c0 += 32) {
                 const int c = c0 + lane;
                 const bool keep = c < dw && fast_keep(mstr, dw, dh, r, c, th);
                 const unsigned m = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
-                    const int pos = base + __popc(m & lt);
-                    if (pos < total)
+                    const int pos = total + __popc(m & lt);
+                    if (pos < d.cell_cap)
                         out[pos] = (uint32_t)(iniX + 3 + c) | ((uint32_t)(iniY + 3 + r) << 12) |
                                    ((uint32_t)(mstr[r * dw + c] - 1) << 24);
                 }
-                base += __popc(m);
+                total += __popc(m);
             }
+        if (total == 0 && pass == 0) continue;
+        if (lane == 0) {
+            if (total > d.cell_cap) atomicOr(status, 2);
+            d.cell_count[cell] = min(total, d.cell_cap);
         }
-        if (threadIdx.x == 0) d.cell_count[cell] = total;
         return;
     }
-    if (threadIdx.x == 0) d.cell_count[cell] = 0;
+    if (lane == 0) d.cell_count[cell] = 0;
 }
 
 // Arc strength of every interior pixel of an image (pixels closer than 3 to
@@ -696,96 +828,156 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, orbgpu_keypoint* out_kps, uint8_t* out_desc,
-                                                  int* status) {
-    const LevelDesc& d = descs[blockIdx.y];
+// Orientation and descriptor of the kept keypoints, DESC_GROUP keypoints per
+// warp: phase A computes the IC_Angle moments of each keypoint with one lane
+// per patch column (every row read is one coalesced segment); phase B
+// evaluates fastAtan2 and the double-precision rotation of the whole group
+// at once (one keypoint per lane: the FP64 pipe is narrow on this GPU, and a
+// one-lane evaluation per keypoint occupied it for a whole warp); phase C
+// builds each rBRIEF descriptor with one descriptor byte per lane.  The
+// group size trades FP64 lane use against the serial chain of phases A and
+// C inside a warp.
+// Each block scans the levels' kept counts into shared memory (descriptors
+// are frame-major with levels ascending, so a level's offset inside its
+// frame is a difference of two prefix entries); keypoint g of the flattened
+// list finds its level by binary search.
+#define DESC_GROUP 8
+__global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
+                                                  uint8_t* out_desc, int* status) {
+    extern __shared__ int s_pre[];  // ndescs + 1
+    __shared__ int s_scan[32];
     const int lane = threadIdx.x & 31;
-    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (blockIdx.x == 0 && threadIdx.x == 0 && d.level == 0) {
-        int t = 0;
-        for (int l = 0; l < d.nlevels; l++) t += d.level_counts[l];
-        *d.frame_total = t;
+    int base = 0;
+    for (int e0 = 0; e0 < ndescs; e0 += blockDim.x) {
+        const int e = e0 + threadIdx.x;
+        const int v = e < ndescs ? *descs[e].kept_count : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (e < ndescs) s_pre[e] = base + ex;
+        base += tot;
     }
-    const int cnt = *d.kept_count;
-    if (k >= cnt) return;
-    int off = 0;
-    for (int l = 0; l < d.level; l++) off += d.level_counts[l];
-    if (off + k >= d.out_cap) {
-        if (lane == 0) atomicOr(status, 16);
-        return;
-    }
-    const int o = d.out_base + off + k;
-    const uint32_t p = d.kept[k];
-    const int x = (int)(p & 0xFFF), y = (int)((p >> 12) & 0xFFF), score = (int)(p >> 24);
-    // keypoints lie at least EDGE_THRESHOLD pixels inside their level
-    if (x < ORBGPU_EDGE_THRESHOLD || y < ORBGPU_EDGE_THRESHOLD || x > d.w - ORBGPU_EDGE_THRESHOLD - 1 ||
-        y > d.h - ORBGPU_EDGE_THRESHOLD - 1) {
-        if (lane == 0) atomicOr(status, 64);
-        return;
-    }
-    // IC_Angle on the unblurred level (src/ORBextractor.cc:94-141)
-    int m10 = 0, m01 = 0;
-    if (lane < 2 * ORBGPU_HALF_PATCH + 1) {
-        const int v = lane - ORBGPU_HALF_PATCH;
-        const int dlim = c_umax[v < 0 ? -v : v];
-        const uint8_t* row = d.dst + (size_t)(y + v) * d.pitch + x;
-        int rs = 0;
-        for (int u = -dlim; u <= dlim; u++) {
-            const int val = row[u];
-            rs += val;
-            m10 += u * val;
+    if (threadIdx.x == 0) s_pre[ndescs] = base;
+    __syncthreads();
+    const int total = base;
+    if (blockIdx.x == 0)
+        for (int e = threadIdx.x; e < ndescs; e += blockDim.x) {
+            const LevelDesc& d = descs[e];
+            if (d.level == 0) *d.frame_total = s_pre[min(ndescs, e + d.nlevels)] - s_pre[e];
         }
-        m01 = v * rs;
-    }
-    m10 = warp_sum(m10);
-    m01 = warp_sum(m01);
-    // angle and rotation on one lane (the double-precision series is the
-    // costly part on this GPU), then broadcast
-    float angle = 0.f, a = 0.f, b = 0.f;
-    if (lane == 0) {
-        angle = fast_atan2_deg((float)m01, (float)m10);
-        // computeOrbDescriptor on the blurred level (src/ORBextractor.cc:153-204)
-        const float factorPI = (float)(3.1415926535897932384626433832795 / 180.f);
-        const float ar = __fmul_rn(angle, factorPI);
-        double sd, cd;
-        sincos_taylor(ar, &sd, &cd);
-        a = __double2float_rn(cd);
-        b = __double2float_rn(sd);
-        const uint32_t xb = __float_as_uint(ar);
-        if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, xb, a);
-        if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, xb, b);
-    }
-    angle = __shfl_sync(0xffffffffu, angle, 0);
-    a = __shfl_sync(0xffffffffu, a, 0);
-    b = __shfl_sync(0xffffffffu, b, 0);
-    const uint8_t* center = d.blur + (size_t)y * d.pitch + x;
-    const int step = d.pitch;
-    int val = 0;
-#pragma unroll
-    for (int kk = 0; kk < 8; kk++) {
-        const signed char* pp = &c_pattern[(lane * 16 + 2 * kk) * 2];
-        int t[2];
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-            const float px = (float)pp[2 * e], py = (float)pp[2 * e + 1];
-            const int ry = cv_round(__fadd_rn(__fmul_rn(px, b), __fmul_rn(py, a)));
-            const int rx = cv_round(__fsub_rn(__fmul_rn(px, a), __fmul_rn(py, b)));
-            t[e] = center[ry * step + rx];
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    const int u = lane - ORBGPU_HALF_PATCH;  // patch column of this lane in phase A
+    const int au = u < 0 ? -u : u;
+    for (int g0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * DESC_GROUP; g0 < total;
+         g0 += nwarps * DESC_GROUP) {
+        // this lane's keypoint (lanes < DESC_GROUP): level, position, output row, validity
+        const int g = g0 + lane;
+        int e = 0, x = 0, y = 0, score = 0, o = 0;
+        bool valid = false;
+        if (lane < DESC_GROUP && g < total) {
+            int lo = 0, hi = ndescs - 1;  // last e with s_pre[e] <= g
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_pre[mid] <= g) lo = mid;
+                else hi = mid - 1;
+            }
+            e = lo;
+            const LevelDesc& d = descs[e];
+            const int k = g - s_pre[e], off = s_pre[e] - s_pre[e - d.level];
+            const uint32_t p = d.kept[k];
+            x = (int)(p & 0xFFF);
+            y = (int)((p >> 12) & 0xFFF);
+            score = (int)(p >> 24);
+            o = d.out_base + off + k;
+            valid = true;
+            if (off + k >= d.out_cap) {
+                atomicOr(status, 16);
+                valid = false;
+            } else if (x < ORBGPU_EDGE_THRESHOLD || y < ORBGPU_EDGE_THRESHOLD || x > d.w - ORBGPU_EDGE_THRESHOLD - 1 ||
+                       y > d.h - ORBGPU_EDGE_THRESHOLD - 1) {
+                // keypoints lie at least EDGE_THRESHOLD pixels inside their level
+                atomicOr(status, 64);
+                valid = false;
+            }
         }
-        val |= (t[0] < t[1]) << kk;
-    }
-    out_desc[(size_t)o * 32 + lane] = (uint8_t)val;
-    if (lane == 0) {
-        orbgpu_keypoint kp;
-        const float s = d.scale;
-        kp.x = d.level == 0 ? (float)x : __fmul_rn((float)x, s);
-        kp.y = d.level == 0 ? (float)y : __fmul_rn((float)y, s);
-        kp.size = (float)(int)__fmul_rn((float)ORBGPU_PATCH_SIZE, s);
-        kp.angle = angle;
-        kp.response = (float)score;
-        kp.octave = d.level;
-        kp.class_id = -1;
-        out_kps[o] = kp;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        // phase A: IC_Angle moments (src/ORBextractor.cc:94-141), integer exact
+        int my_m01 = 0, my_m10 = 0;
+        for (unsigned rest = vmask; rest; rest &= rest - 1) {
+            const int k = __ffs(rest) - 1;
+            const int ek = __shfl_sync(0xffffffffu, e, k);
+            const int xk = __shfl_sync(0xffffffffu, x, k), yk = __shfl_sync(0xffffffffu, y, k);
+            const LevelDesc& d = descs[ek];
+            const uint8_t* col = d.dst + (size_t)yk * d.pitch + xk + u;
+            int m10 = 0, m01 = 0;
+            if (lane < 2 * ORBGPU_HALF_PATCH + 1) {
+#pragma unroll
+                for (int v = -ORBGPU_HALF_PATCH; v <= ORBGPU_HALF_PATCH; v++) {
+                    if (c_umax[v < 0 ? -v : v] >= au) {
+                        const int val = col[v * d.pitch];
+                        m10 += u * val;
+                        m01 += v * val;
+                    }
+                }
+            }
+            m10 = warp_sum(m10);
+            m01 = warp_sum(m01);
+            if (lane == k) {
+                my_m10 = m10;
+                my_m01 = m01;
+            }
+        }
+        // phase B: angle and rotation, one keypoint per lane
+        float angle = 0.f, ca = 0.f, sb = 0.f;
+        if (valid) {
+            angle = fast_atan2_deg((float)my_m01, (float)my_m10);
+            // computeOrbDescriptor on the blurred level (src/ORBextractor.cc:153-204)
+            const float factorPI = (float)(3.1415926535897932384626433832795 / 180.f);
+            const float ar = __fmul_rn(angle, factorPI);
+            double sd, cd;
+            sincos_taylor(ar, &sd, &cd);
+            ca = __double2float_rn(cd);
+            sb = __double2float_rn(sd);
+            const uint32_t xb = __float_as_uint(ar);
+            if (g_cos_exc_n > 0) ca = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, xb, ca);
+            if (g_sin_exc_n > 0) sb = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, xb, sb);
+            const LevelDesc& d = descs[e];
+            orbgpu_keypoint kp;
+            const float sc = d.scale;
+            kp.x = d.level == 0 ? (float)x : __fmul_rn((float)x, sc);
+            kp.y = d.level == 0 ? (float)y : __fmul_rn((float)y, sc);
+            kp.size = (float)(int)__fmul_rn((float)ORBGPU_PATCH_SIZE, sc);
+            kp.angle = angle;
+            kp.response = (float)score;
+            kp.octave = d.level;
+            kp.class_id = -1;
+            out_kps[o] = kp;
+        }
+        // phase C: rBRIEF, one descriptor byte per lane
+        for (unsigned rest = vmask; rest; rest &= rest - 1) {
+            const int k = __ffs(rest) - 1;
+            const int ek = __shfl_sync(0xffffffffu, e, k);
+            const int xk = __shfl_sync(0xffffffffu, x, k), yk = __shfl_sync(0xffffffffu, y, k);
+            const int ok = __shfl_sync(0xffffffffu, o, k);
+            const float a = __shfl_sync(0xffffffffu, ca, k), b = __shfl_sync(0xffffffffu, sb, k);
+            const LevelDesc& d = descs[ek];
+            const uint8_t* center = d.blur + (size_t)yk * d.pitch + xk;
+            const int step = d.pitch;
+            int val = 0;
+#pragma unroll
+            for (int kk = 0; kk < 8; kk++) {
+                const signed char* pp = &c_pattern[(lane * 16 + 2 * kk) * 2];
+                int t[2];
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const float px = (float)pp[2 * q], py = (float)pp[2 * q + 1];
+                    const int ry = cv_round(__fadd_rn(__fmul_rn(px, b), __fmul_rn(py, a)));
+                    const int rx = cv_round(__fsub_rn(__fmul_rn(px, a), __fmul_rn(py, b)));
+                    t[q] = center[ry * step + rx];
+                }
+                val |= (t[0] < t[1]) << kk;
+            }
+            out_desc[(size_t)ok * 32 + lane] = (uint8_t)val;
+        }
     }
 }
 
@@ -816,7 +1008,7 @@ void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int lev
 // Blocks of k_level_resize_blur for a w x h level.
 int resize_blur_tiles(int w, int h) { return ((w + RB_TW - 1) / RB_TW) * ((h + RB_TH - 1) / RB_TH); }
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st) {
-    if (nitems > 0) k_fast_cells<<<nitems, 128, 0, st>>>(descs, rm, status);
+    if (nitems > 0) k_fast_cells<<<nitems, 32 * ORBGPU_FAST_CELLS_PER_BLOCK, 0, st>>>(descs, rm, status);
 }
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {
     const size_t smem = (size_t)sort_cap * sizeof(unsigned long long);
@@ -825,9 +1017,14 @@ void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* st
 }
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st) {
-    const int wpb = 8;
-    dim3 grid((max_kept + wpb - 1) / wpb, ndescs);
-    if (ndescs > 0 && max_kept > 0) k_describe<<<grid, 256, 0, st>>>(descs, kps, desc, status);
+    if (ndescs <= 0 || max_kept <= 0) return;
+    const int nsm = nsm_of_current_device();
+    // DESC_GROUP keypoints per warp, 8 warps per block; max_kept (the node
+    // capacity) overestimates a level's keypoints about twice; at most 8
+    // resident blocks per SM
+    const long want = ((long)ndescs * max_kept / 2 + 8 * DESC_GROUP - 1) / (8 * DESC_GROUP);
+    const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 8));
+    k_describe<<<blocks, 256, sizeof(int) * (ndescs + 1), st>>>(descs, ndescs, kps, desc, status);
 }
 
 }  // namespace orbgpu

@@ -28,6 +28,7 @@ struct LevelDesc {
     int sw, sh, spitch;
     uint8_t* dst;  // level l (unblurred)
     uint8_t* blur; // level l blurred (same pitch)
+    uint8_t* strength;  // FAST arc strength of every pixel at the lower threshold (same pitch)
     int w, h, pitch;
     const int* xofs;      // resize tables of this level: source column per output column
     const short* xalpha;  // 2 weights per output column
@@ -68,6 +69,9 @@ struct LevelDesc {
     int out_cap;          // output rows available to the frame
     int* frame_total;     // the frame's keypoint count
 };
+
+// FAST cells handled by one block of k_fast_cells (one warp each).
+#define ORBGPU_FAST_CELLS_PER_BLOCK 4
 
 struct DNode {
     int16_t x0, x1, y0, y1;

@@ -33,7 +33,7 @@ struct LevelGeom {
 };
 
 struct LevelOffsets {
-    size_t pyr, blur, xofs, xalpha, yofs, ybeta, slots, cell_count, cand, node_of, quad, nodes_a, nodes_b, cnt4,
+    size_t pyr, blur, strength, xofs, xalpha, yofs, ybeta, slots, cell_count, cand, node_of, quad, nodes_a, nodes_b, cnt4,
         childpos, aux0, aux1, aux2, best, kept;
 };
 
@@ -59,5 +59,18 @@ std::string default_sincos_table_path();
 // Builds the table of descriptor-angle inputs whose host cosf/sinf differ
 // from the rounded sincos_taylor value, and writes it to 'path'.
 int build_sincos_table(const char* path, int threads);
+
+// SM count of the current device, cached per device ordinal.
+inline int nsm_of_current_device() {
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 132;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 132;
+    }
+    return cache[dev];
+}
 
 }  // namespace orbgpu

@@ -83,8 +83,9 @@ class ServingEngine:
     # ---------------------------------------------------------------- admission
     def stream_bytes(self, w: int, h: int) -> int:
         # previous keypoints (as records) + descriptors, staging of one image and
-        # its share of the batch arena (pyramid + blurred pyramid, ~2 * 3.1 * w * h)
-        return self.cap * (32 + 32) + w * h + int(2 * 3.1 * w * h) + 64 * 1024
+        # its share of the batch arena (pyramid, blurred pyramid and FAST
+        # strength planes, ~3 * 3.1 * w * h)
+        return self.cap * (32 + 32) + w * h + int(3 * 3.1 * w * h) + 64 * 1024
 
     def admit(self, sid: int, width: int, height: int, nfeatures: int) -> bool:
         need = self.stream_bytes(width, height)
