@@ -29,8 +29,15 @@ int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_keypoint* kp
                                       const int* counts, const orbgpu_mappoint* mappoints,
                                       const uint8_t* mp_descriptors, const int* mp_offsets, float th, float nnratio,
                                       int* match_out, int* nmatches);
-/* Kernel launches of one orbgpu_batch_search_by_projection call. */
+/* Kernel launches of the last orbgpu_batch_search_by_projection call of the
+ * calling thread (5 when every frame is resolved in shared memory, 17 with
+ * the global-memory rounds). */
 int orbgpu_batch_search_launch_count(void);
+/* Resolution of the batched search on the calling thread: 0 (default) one
+ * block per frame in shared memory when every frame fits, else the
+ * global-memory rounds; 1 always the global-memory rounds.  Both give the
+ * same results. */
+int orbgpu_batch_search_mode(int mode);
 
 /* ------------------------------------------------------------ batch instrumentation */
 /* Device milliseconds of the five stages of the last orbgpu_batch_extract

@@ -500,7 +500,7 @@ __global__ void k_bgrid_fill(const int* counts, int cap, const int* key_cell, in
 __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* desc, int cap, const BatchFrameInfo* info,
                                    const int* cell_start, const int* cell_keys, const orbgpu_mappoint* mps,
                                    const uint8_t* mp_desc, const int* mp_off, float th, int slot_cap, uint64_t* slots,
-                                   int* slot_count, int* status) {
+                                   int* slot_count, int* status, int* frame_cands) {
     const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
     const int f = blockIdx.y;
     const int lane = threadIdx.x & 31;
@@ -561,6 +561,7 @@ __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* de
     if (lane == 0) {
         slot_count[imp] = total;
         if (total > slot_cap) atomicMax(status, total);
+        if (total > 0) atomicAdd(&frame_cands[f], total);
     }
 }
 
@@ -579,66 +580,180 @@ __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* de
 
 __global__ void k_bproj_round(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off,
                               int slot_cap, const uint64_t* slots, const int* slot_count, float nnratio, int round,
-                              int* claims3, int* res, int* changed) {
+                              int* claims3, int* res, int* changed, int* nwarp_frame) {
     const int f = blockIdx.y;
     const int lane = threadIdx.x & 31;
-    const int wpf = gridDim.x * (blockDim.x >> 5);  // warps of this frame
-    const int w0 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int n_mp = mp_off[f + 1] - mp_off[f];
     if (round > 0 && changed[(round - 1) * gridDim.y + f] == 0) return;  // converged
     int* claims_r = claims3 + (size_t)((round + 0) % 3) * gridDim.y * cap + (size_t)f * cap;
     int* claims_w = claims3 + (size_t)((round + 1) % 3) * gridDim.y * cap + (size_t)f * cap;
     int* claims_z = claims3 + (size_t)((round + 2) % 3) * gridDim.y * cap + (size_t)f * cap;
     // clear the array the next round writes into
-    for (int i = w0 * 32 + lane; i < cap; i += wpf * 32) claims_z[i] = BPROJ_NONE;
+    for (int i = local * 32 + lane; i < cap; i += (*nwarp_frame) * 32) claims_z[i] = BPROJ_NONE;
+    if (local >= n_mp) return;
+    const int imp = mp_off[f] + local;
     const orbgpu_keypoint* K = kps + (size_t)f * cap;
-    bool any_change = false;
-    for (int local = w0; local < n_mp; local += wpf) {
-        const int imp = mp_off[f] + local;
-        const int cnt = min(slot_count[imp], slot_cap);
-        const uint64_t* S = slots + (size_t)imp * slot_cap;
-        uint64_t best = ~0ull, second = ~0ull;
-        for (int b = 0; b < cnt; b += 32) {
-            uint64_t key = ~0ull;
-            if (b + lane < cnt) {
-                key = S[b + lane];
-                if (claims_r[(int)(key & 0xFFFFF)] < local || (int)(key >> 40) >= 256) key = ~0ull;
-            }
-            if (key < best) {
-                second = best;
-                best = key;
-            } else if (key < second) {
-                second = key;
-            }
+    const int cnt = min(slot_count[imp], slot_cap);
+    const uint64_t* S = slots + (size_t)imp * slot_cap;
+    uint64_t best = ~0ull, second = ~0ull;
+    for (int b = 0; b < cnt; b += 32) {
+        uint64_t key = ~0ull;
+        if (b + lane < cnt) {
+            key = S[b + lane];
+            if (claims_r[(int)(key & 0xFFFFF)] < local || (int)(key >> 40) >= 256) key = ~0ull;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
-            const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
-            if (ob < best) {
-                second = best < os ? best : os;
-                best = ob;
-            } else {
-                second = second < ob ? second : ob;
-            }
-        }
-        int r = -1;
-        if (best != ~0ull) {
-            const int bestDist = (int)(best >> 40);
-            const int bestIdx = (int)(best & 0xFFFFF);
-            const int bestLevel = K[bestIdx].octave;
-            const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
-            const int bestLevel2 = second == ~0ull ? -1 : K[(int)(second & 0xFFFFF)].octave;
-            if (bestDist <= ORBGPU_TH_HIGH &&
-                !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
-                r = bestIdx;
-        }
-        if (lane == 0) {
-            if (res[imp] != r) any_change = true;
-            res[imp] = r;
-            if (r >= 0) atomicMin(&claims_w[r], local);
+        if (key < best) {
+            second = best;
+            best = key;
+        } else if (key < second) {
+            second = key;
         }
     }
-    if (lane == 0 && any_change) changed[round * gridDim.y + f] = 1;
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const uint64_t os = __shfl_xor_sync(0xffffffffu, second, o);
+        if (ob < best) {
+            second = best < os ? best : os;
+            best = ob;
+        } else {
+            second = second < ob ? second : ob;
+        }
+    }
+    int r = -1;
+    if (best != ~0ull) {
+        const int bestDist = (int)(best >> 40);
+        const int bestIdx = (int)(best & 0xFFFFF);
+        const int bestLevel = K[bestIdx].octave;
+        const int bestDist2 = second == ~0ull ? 256 : (int)(second >> 40);
+        const int bestLevel2 = second == ~0ull ? -1 : K[(int)(second & 0xFFFFF)].octave;
+        if (bestDist <= ORBGPU_TH_HIGH &&
+            !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
+            r = bestIdx;
+    }
+    if (lane == 0) {
+        if (res[imp] != r) changed[round * gridDim.y + f] = 1;
+        res[imp] = r;
+        if (r >= 0) atomicMin(&claims_w[r], local);
+    }
+}
+
+// The same fixed-point resolution with one block per frame and the whole
+// frame in shared memory: the map points' candidate keys (32 bits: distance,
+// GetFeaturesInArea cell, keypoint index -- the lexicographic order of the
+// 64-bit keys), the keypoints' octaves, the results and two claim arrays.
+// A thread evaluates its map points with the reference's best / second-best
+// loop over the candidates not claimed by an earlier map point of the
+// previous round; rounds repeat until one changes nothing (at most M + 1
+// rounds: round r fixes the first r + 1 map points).  Used when every frame
+// fits; the global-memory rounds above handle the rest.
+__global__ void __launch_bounds__(1024)
+    k_bproj_resolve_smem(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off, int slot_cap,
+                         const uint64_t* slots, const int* slot_count, float nnratio, int t_cap, int* match_out,
+                         int* nmatches, int* status) {
+    extern __shared__ __align__(16) int s_dyn[];
+    __shared__ int s_scan[32];
+    __shared__ int s_flag[3];
+    const int f = blockIdx.x;
+    const int tid = threadIdx.x;
+    const int mp0 = mp_off[f], M = mp_off[f + 1] - mp0;
+    const int n = min(counts[f], cap);
+    int* s_start = s_dyn;                 // M + 1
+    int* s_res = s_start + (M + 1);       // M
+    int* cr = s_res + M;                  // cap: claims of the previous round
+    int* cw = cr + cap;                   // cap: claims of this round
+    uint32_t* s_key = reinterpret_cast<uint32_t*>(cw + cap);  // t_cap
+    uint8_t* s_oct = reinterpret_cast<uint8_t*>(s_key + t_cap);  // cap
+    int base = 0;
+    for (int i0 = 0; i0 < M; i0 += blockDim.x) {
+        const int i = i0 + tid;
+        const int v = i < M ? min(slot_count[mp0 + i], slot_cap) : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (i < M) s_start[i] = base + ex;
+        base += tot;
+    }
+    if (base > t_cap) {  // the host sized t_cap from these counts
+        if (tid == 0) atomicOr(status + 2, 1);
+        return;
+    }
+    if (tid == 0) s_start[M] = base;
+    if (tid < 3) s_flag[tid] = 0;
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    for (int i = warp; i < M; i += nw) {
+        const int s0 = s_start[i], cnt = s_start[i + 1] - s0;
+        const uint64_t* S = slots + (size_t)(mp0 + i) * slot_cap;
+        for (int b = lane; b < cnt; b += 32) {
+            const uint64_t key = S[b];
+            const uint32_t dist = (uint32_t)(key >> 40), cell = (uint32_t)(key >> 20) & 0xFFFFFu,
+                           idx = (uint32_t)key & 0xFFFFFu;
+            s_key[s0 + b] = dist >= 256 ? 0xFFFFFFFFu : (dist << 24) | (cell << 12) | idx;
+        }
+    }
+    for (int k = tid; k < n; k += blockDim.x) s_oct[k] = (uint8_t)kps[(size_t)f * cap + k].octave;
+    for (int i = tid; i < M; i += blockDim.x) s_res[i] = -2;
+    for (int k = tid; k < cap; k += blockDim.x) {
+        cr[k] = 0x7fffffff;
+        cw[k] = 0x7fffffff;
+    }
+    bool converged = M == 0;
+    for (int round = 0; round <= M + 1 && !converged; round++) {
+        if (tid == 0) s_flag[(round + 1) % 3] = 0;
+        __syncthreads();
+        for (int i = tid; i < M; i += blockDim.x) {
+            uint32_t best = 0xFFFFFFFFu, second = 0xFFFFFFFFu;
+            for (int e = s_start[i]; e < s_start[i + 1]; e++) {
+                const uint32_t key = s_key[e];
+                if (key == 0xFFFFFFFFu || cr[key & 0xFFFu] < i) continue;
+                if (key < best) {
+                    second = best;
+                    best = key;
+                } else if (key < second) {
+                    second = key;
+                }
+            }
+            int r = -1;
+            if (best != 0xFFFFFFFFu) {
+                const int bestDist = (int)(best >> 24);
+                const int bestIdx = (int)(best & 0xFFFu);
+                const int bestLevel = s_oct[bestIdx];
+                const int bestDist2 = second == 0xFFFFFFFFu ? 256 : (int)(second >> 24);
+                const int bestLevel2 = second == 0xFFFFFFFFu ? -1 : s_oct[second & 0xFFFu];
+                if (bestDist <= ORBGPU_TH_HIGH &&
+                    !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
+                    r = bestIdx;
+            }
+            if (r != s_res[i]) {
+                s_res[i] = r;
+                s_flag[round % 3] = 1;
+            }
+            if (r >= 0) atomicMin(&cw[r], i);
+        }
+        __syncthreads();
+        converged = s_flag[round % 3] == 0;
+        // this round's claims are read by the next; the array read now is cleared for writing
+        int* t = cr;
+        cr = cw;
+        cw = t;
+        if (!converged)
+            for (int k = tid; k < cap; k += blockDim.x) cw[k] = 0x7fffffff;
+    }
+    if (!converged && tid == 0) atomicOr(status + 2, 2);
+    int* Mo = match_out + (size_t)f * cap;
+    for (int k = tid; k < cap; k += blockDim.x) Mo[k] = k < n ? -1 : -3;
+    __syncthreads();
+    int nm = 0;
+    for (int i = tid; i < M; i += blockDim.x) {
+        const int r = s_res[i];
+        if (r >= 0) {
+            Mo[r] = i;
+            nm++;
+        }
+    }
+    int tot;
+    block_exclusive_scan(nm, s_scan, &tot);
+    if (tid == 0) nmatches[f] = tot;
 }
 
 // Writes match_out / nmatches from the converged results; frames that did
@@ -722,8 +837,22 @@ struct orbgpu_batch_proj {
     size_t bytes = 0;
     int slot_cap = 64;
     int* h_pinned = nullptr;
+    int* h_cands = nullptr;  // per-frame candidate totals (pinned)
+    int h_cands_cap = 0;
     int last_serial_frames = 0;
+    int last_launches = 0;
+    int mode = 0;  // 0: shared-memory resolution when the frames fit; 1: global-memory rounds
 };
+// one scratch per host thread (the search is synchronous)
+static thread_local orbgpu_batch_proj g_bproj;
+
+static int orbgpu_batch_search_last_launches() { return g_bproj.last_launches; }
+
+extern "C" int orbgpu_batch_search_mode(int mode) {
+    if (mode != 0 && mode != 1) return ORBGPU_ERR_BAD_ARG;
+    g_bproj.mode = mode;
+    return ORBGPU_OK;
+}
 
 // Projection search over the frames of the last orbgpu_batch_extract call.
 // kps/desc/counts: that call's outputs (device); mappoints / mp_descriptors:
@@ -743,13 +872,19 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
     const int total_mp = mp_offsets[nf];
     int max_mp = 0;
     for (int f = 0; f < nf; f++) max_mp = std::max(max_mp, mp_offsets[f + 1] - mp_offsets[f]);
-    static thread_local orbgpu_batch_proj P;
+    orbgpu_batch_proj& P = g_bproj;
     if (!P.h_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_pinned, 64));
+    if (P.h_cands_cap < nf) {
+        if (P.h_cands) cudaFreeHost(P.h_cands);
+        P.h_cands = nullptr;
+        ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_cands, sizeof(int) * nf));
+        P.h_cands_cap = nf;
+    }
     cudaStream_t st = b->stream;
     for (int attempt = 0; attempt < 3; attempt++) {
         const size_t need = sizeof(BatchFrameInfo) * nf + sizeof(int) * ((size_t)nf * ncell * 2 + (size_t)nf * (ncell + 1) +
                                                                       (size_t)nf * cap * 5 + (nf + 1) + 2 * total_mp +
-                                                                      BPROJ_ROUNDS * nf + 16) +
+                                                                      BPROJ_ROUNDS * nf + nf + 16) +
                             sizeof(uint64_t) * (size_t)std::max(1, total_mp) * P.slot_cap + 8 * 256;
         if (need > P.bytes) {
             ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
@@ -778,6 +913,8 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         int* claims3 = (int*)take(sizeof(int) * (size_t)3 * nf * cap);
         int* res = (int*)take(sizeof(int) * std::max(1, total_mp));
         int* changed = (int*)take(sizeof(int) * BPROJ_ROUNDS * nf);
+        int* nwarp = (int*)take(sizeof(int) * 2);
+        int* frame_cands = (int*)take(sizeof(int) * nf);
         std::vector<BatchFrameInfo> hi(nf);
         for (int f = 0; f < nf; f++) {
             const int w = b->sig[6 + 3 * f], h = b->sig[7 + 3 * f];
@@ -790,6 +927,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_off, mp_offsets, sizeof(int) * (nf + 1), cudaMemcpyHostToDevice, st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(cell_count, 0, sizeof(int) * (size_t)nf * ncell, st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * 4, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(frame_cands, 0, sizeof(int) * nf, st));
         dim3 gk((cap + 255) / 256, nf);
         k_bgrid_count<<<gk, 256, 0, st>>>(kps, counts, cap, info, key_cell, cell_count);
         k_bgrid_scan<<<nf, 1024, 0, st>>>(cell_count, cell_start, cursor);
@@ -797,25 +935,48 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         const int wpb = 8;
         dim3 gc((std::max(1, max_mp) + wpb - 1) / wpb, nf);
         k_bproj_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, mappoints,
-                                                   mp_descriptors, d_off, th, P.slot_cap, slots, slot_count, status);
+                                                   mp_descriptors, d_off, th, P.slot_cap, slots, slot_count, status,
+                                                   frame_cands);
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_cands, frame_cands, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
         ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
         if (P.h_pinned[0] > P.slot_cap) {  // a window held more candidates than the slots: widen and redo
             P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
             continue;
         }
-        // fixed-point rounds, then the result write-out (serial replay for any
-        // frame that did not converge)
-        // one warp per map point (a round is a chain of dependent loads per
-        // map point, so width beats a grid-stride loop)
-        const int per_frame_blocks = std::max(1, (std::max(1, max_mp) + wpb - 1) / wpb);
+        // every frame in shared memory when it fits (one launch), else the
+        // global-memory fixed-point rounds and the result write-out (serial
+        // replay for any frame that did not converge)
+        int t_max = 0;
+        for (int f = 0; f < nf; f++) t_max = std::max(t_max, P.h_cands[f]);
+        const size_t smem = sizeof(int) * ((size_t)2 * max_mp + 1 + 2 * (size_t)cap + (size_t)t_max) + (size_t)cap + 16;
+        if (P.mode == 0 && cap < 4096 && smem <= 200 * 1024) {
+            ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bproj_resolve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem));
+            k_bproj_resolve_smem<<<nf, 1024, smem, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio,
+                                                         t_max, match_out, nmatches, status);
+            ORBGPU_CUDA_TRY(cudaGetLastError());
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned + 2, status + 1, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+            ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+            P.last_serial_frames = 0;
+            P.last_launches = 4 + 1;
+            if (P.h_pinned[3] != 0) {
+                orbgpu_set_last_error("batched projection: shared-memory resolution failed", __FILE__, __LINE__);
+                return ORBGPU_ERR_CUDA;
+            }
+            return ORBGPU_OK;
+        }
+        P.last_launches = 4 + BPROJ_ROUNDS + 1;
+        const int warps = std::max((std::max(1, max_mp) + wpb - 1) / wpb * wpb, ((cap + 31) / 32 + wpb - 1) / wpb * wpb);
+        P.h_pinned[1] = warps;
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(nwarp, &P.h_pinned[1], sizeof(int), cudaMemcpyHostToDevice, st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(claims3, 0x7f, sizeof(int) * (size_t)3 * nf * cap, st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(res, 0xfe, sizeof(int) * std::max(1, total_mp), st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(changed, 0, sizeof(int) * BPROJ_ROUNDS * nf, st));
-        dim3 gr(per_frame_blocks, nf);
+        dim3 gr(warps / wpb, nf);
         for (int r = 0; r < BPROJ_ROUNDS; r++)
             k_bproj_round<<<gr, 32 * wpb, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, r,
-                                                  claims3, res, changed);
+                                                  claims3, res, changed, nwarp);
         k_bproj_finish<<<nf, 32, 0, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio, changed, res,
                                          match_out, nmatches, status);
         ORBGPU_CUDA_TRY(cudaGetLastError());
@@ -827,4 +988,6 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
     return ORBGPU_ERR_CAPACITY;
 }
 
-extern "C" int orbgpu_batch_search_launch_count(void) { return 4 + BPROJ_ROUNDS + 1; }
+extern "C" int orbgpu_batch_search_launch_count(void) {
+    return orbgpu_batch_search_last_launches();
+}

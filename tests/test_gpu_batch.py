@@ -78,14 +78,26 @@ def test_batch_projection_vs_oracle(torch, oracle):
         mps_all.append(mps)
         mpd_all.append(mpd)
         counts.append(M)
+    from orb_slam2_detailed_comments_gb300._lib import lib
     p = BatchProjection(b, 0.8)
-    match, nm = p.search(torch.from_numpy(np.concatenate(mps_all).view(np.uint8)).cuda(),
-                         torch.from_numpy(np.ascontiguousarray(np.concatenate(mpd_all))).cuda(), counts, 6.0)
-    match = match.cpu().numpy().reshape(len(fr), cap)
-    nm = nm.cpu().numpy()
+    refs = []
     for f, (img, _) in enumerate(fr):
         n = int(ch[f])
-        r = oracle.search_by_projection(kh[f, :n], dh[f, :n], img.shape[1], img.shape[0],
-                                        mps_all[f].view(pyoracle.MP_DTYPE), mpd_all[f], th=6.0, nnratio=0.8)
-        assert nm[f] == r[0], f"frame {f}"
-        assert np.array_equal(match[f, :n], r[1]), f"frame {f}"
+        refs.append(oracle.search_by_projection(kh[f, :n], dh[f, :n], img.shape[1], img.shape[0],
+                                                mps_all[f].view(pyoracle.MP_DTYPE), mpd_all[f], th=6.0, nnratio=0.8))
+    # both resolutions: frames in shared memory (default) and the global-memory rounds
+    for mode, launches in ((0, 5), (1, 17)):
+        assert lib().orbgpu_batch_search_mode(mode) == 0
+        try:
+            match, nm = p.search(torch.from_numpy(np.concatenate(mps_all).view(np.uint8)).cuda(),
+                                 torch.from_numpy(np.ascontiguousarray(np.concatenate(mpd_all))).cuda(), counts, 6.0)
+            assert p.launches_per_search() == launches
+        finally:
+            lib().orbgpu_batch_search_mode(0)
+        match = match.cpu().numpy().reshape(len(fr), cap)
+        nm = nm.cpu().numpy()
+        for f in range(len(fr)):
+            n = int(ch[f])
+            assert nm[f] == refs[f][0], f"mode {mode} frame {f}"
+            assert np.array_equal(match[f, :n], refs[f][1]), f"mode {mode} frame {f}"
+            assert (match[f, n:] == -3).all()
