@@ -499,8 +499,12 @@ __global__ void k_bgrid_fill(const int* counts, int cap, const int* key_cell, in
 
 __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* desc, int cap, const BatchFrameInfo* info,
                                    const int* cell_start, const int* cell_keys, const orbgpu_mappoint* mps,
-                                   const uint8_t* mp_desc, const int* mp_off, float th, int slot_cap, uint64_t* slots,
-                                   int* slot_count, int* status, int* frame_cands) {
+                                   const uint8_t* mp_desc, const int* mp_off, float th, float nnratio, int slot_cap,
+                                   uint64_t* slots, int* slot_count, int* status, int* frame_cands) {
+    // A candidate with nnratio * dist > TH_HIGH (nnratio <= 1) can neither be
+    // accepted (dist > TH_HIGH) nor make an accepted best fail the ratio test
+    // (best <= TH_HIGH < nnratio * dist), so the lists leave it out.
+    const bool drop_far = nnratio <= 1.0f;
     const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
     const int f = blockIdx.y;
     const int lane = threadIdx.x & 31;
@@ -527,35 +531,30 @@ __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* de
         if (x0 < ORBGPU_GRID_COLS && x1 >= 0 && y0 < ORBGPU_GRID_ROWS && y1 >= 0) {
             const uint8_t* dmp = mp_desc + (size_t)imp * 32;
             const float rr = __fmul_rn(radius, radius);
-            for (int ix = x0; ix <= x1; ix++)
-                for (int iy = y0; iy <= y1; iy++) {
-                    const int c = ix * ORBGPU_GRID_ROWS + iy;
-                    const int s = cs[c], e = cs[c + 1];
-                    for (int b = s; b < e; b += 32) {
-                        const int j = b + lane;
-                        bool ok = false;
-                        int idx = -1;
-                        if (j < e) {
-                            idx = ck[j];
-                            const orbgpu_keypoint kp = K[idx];
-                            ok = kp.octave >= level - 1 && kp.octave <= level;
-                            if (ok) {
-                                const float dx = __fsub_rn(kp.x, x), dy = __fsub_rn(kp.y, y);
-                                ok = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < rr;
-                            }
-                        }
-                        const unsigned msk = __ballot_sync(0xffffffffu, ok);
-                        if (ok) {
-                            const int pos = total + __popc(msk & ((1u << lane) - 1));
-                            if (pos < slot_cap) {
-                                const int dist = hamming256_ptr(dmp, D + (size_t)idx * 32);
-                                slots[(size_t)imp * slot_cap + pos] = ((uint64_t)(uint32_t)dist << 40) |
-                                                                      ((uint64_t)(uint32_t)c << 20) | (uint64_t)(uint32_t)idx;
-                            }
-                        }
-                        total += __popc(msk);
+            warp_window_keys(cs, ck, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+                bool ok = false;
+                int dist = 256;
+                if (valid) {
+                    const orbgpu_keypoint kp = K[idx];
+                    ok = kp.octave >= level - 1 && kp.octave <= level;
+                    if (ok) {
+                        const float dx = __fsub_rn(kp.x, x), dy = __fsub_rn(kp.y, y);
+                        ok = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < rr;
+                    }
+                    if (ok) {
+                        dist = hamming256_ptr(dmp, D + (size_t)idx * 32);
+                        ok = !(drop_far && __fmul_rn(nnratio, (float)dist) > (float)ORBGPU_TH_HIGH);
                     }
                 }
+                const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    const int pos = total + __popc(msk & ((1u << lane) - 1));
+                    if (pos < slot_cap)
+                        slots[(size_t)imp * slot_cap + pos] = ((uint64_t)(uint32_t)dist << 40) |
+                                                              ((uint64_t)(uint32_t)c << 20) | (uint64_t)(uint32_t)idx;
+                }
+                total += __popc(msk);
+            });
         }
     }
     if (lane == 0) {
@@ -935,8 +934,8 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         const int wpb = 8;
         dim3 gc((std::max(1, max_mp) + wpb - 1) / wpb, nf);
         k_bproj_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, mappoints,
-                                                   mp_descriptors, d_off, th, P.slot_cap, slots, slot_count, status,
-                                                   frame_cands);
+                                                   mp_descriptors, d_off, th, nnratio, P.slot_cap, slots, slot_count,
+                                                   status, frame_cands);
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_cands, frame_cands, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
         ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));

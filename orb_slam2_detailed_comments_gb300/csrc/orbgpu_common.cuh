@@ -86,6 +86,54 @@ __device__ __forceinline__ int warp_min_i(int v) {
     return v;
 }
 
+// The keypoint indices of the grid cells [x0, x1] x [y0, y1] (cell c =
+// ix * rows + iy, lists in CSR form: cell_start / cell_keys), 32 per step in
+// Frame::GetFeaturesInArea's order (cells by ix then iy, each cell's list in
+// order).  The lanes read up to 32 cells' bounds at once and prefix-sum their
+// sizes, so a window costs one pass instead of one dependent round trip per
+// cell.  visit(idx, cell, valid) is called by every lane once per step
+// (valid is false past the window's last entry).
+template <typename Visit>
+__device__ __forceinline__ void warp_window_keys(const int* cell_start, const int* cell_keys, int rows, int x0,
+                                                 int x1, int y0, int y1, Visit visit) {
+    const int lane = threadIdx.x & 31;
+    const int ncy = y1 - y0 + 1;
+    const int ncell = (x1 - x0 + 1) * ncy;
+    for (int c0 = 0; c0 < ncell; c0 += 32) {
+        const int ci = c0 + lane;
+        int s = 0, n = 0, cell = 0;
+        if (ci < ncell) {
+            const int qx = ci / ncy;
+            cell = (x0 + qx) * rows + y0 + (ci - qx * ncy);
+            s = cell_start[cell];
+            n = cell_start[cell + 1] - s;
+        }
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int excl = incl - n;
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            // the last lane whose list starts at or before t holds entry t
+            int k = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int e = __shfl_sync(0xffffffffu, excl, k + step);
+                if (e <= t) k += step;
+            }
+            const int sk = __shfl_sync(0xffffffffu, s, k);
+            const int ek = __shfl_sync(0xffffffffu, excl, k);
+            const int ck = __shfl_sync(0xffffffffu, cell, k);
+            const bool valid = t < total;
+            visit(valid ? cell_keys[sk + t - ek] : -1, ck, valid);
+        }
+    }
+}
+
 // Block-wide exclusive scan of one int per thread; returns the block total.
 // 'smem' must hold 32 ints.  All threads of the block must call it.
 __device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int* total) {

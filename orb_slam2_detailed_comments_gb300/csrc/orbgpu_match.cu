@@ -130,27 +130,17 @@ __global__ void k_init_candidates(GridDev g2, const orbgpu_keypoint* kps1, const
     int x0, x1, y0, y1;
     if (kp1.octave <= 0 && area_cells(g2, prev[2 * i1], prev[2 * i1 + 1], window, x0, x1, y0, y1)) {
         const uint8_t* d1 = desc1 + (size_t)i1 * 32;
-        for (int ix = x0; ix <= x1; ix++)
-            for (int iy = y0; iy <= y1; iy++) {
-                const int c = ix * ORBGPU_GRID_ROWS + iy;
-                const int s = g2.cell_start[c], e = g2.cell_start[c + 1];
-                for (int b = s; b < e; b += 32) {
-                    const int j = b + lane;
-                    bool ok = false;
-                    int idx = -1;
-                    if (j < e) {
-                        idx = g2.cell_keys[j];
-                        ok = in_area(g2, idx, prev[2 * i1], prev[2 * i1 + 1], window, kp1.octave, kp1.octave);
-                    }
-                    const unsigned m = __ballot_sync(0xffffffffu, ok);
-                    if (fill && ok) {
-                        const int pos = cand_start[i1] + total + __popc(m & ((1u << lane) - 1));
-                        const int dist = hamming256_ptr(d1, g2.desc + (size_t)idx * 32);
-                        cand_out[pos] = cand_key(dist, c, idx);
-                    }
-                    total += __popc(m);
-                }
+        const float px = prev[2 * i1], py = prev[2 * i1 + 1];
+        warp_window_keys(g2.cell_start, g2.cell_keys, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+            const bool ok = valid && in_area(g2, idx, px, py, window, kp1.octave, kp1.octave);
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (fill && ok) {
+                const int pos = cand_start[i1] + total + __popc(m & ((1u << lane) - 1));
+                const int dist = hamming256_ptr(d1, g2.desc + (size_t)idx * 32);
+                cand_out[pos] = cand_key(dist, c, idx);
             }
+            total += __popc(m);
+        });
     }
     if (!fill && lane == 0) cand_count[i1] = total;
 }
@@ -287,8 +277,12 @@ __global__ void k_init_resolve(const orbgpu_keypoint* kps1, int n1, const orbgpu
 // ----------------------------------------------------------------- SearchByProjection(Frame, MapPoints)
 // Pass 1 (warp per map point): candidates in the scaled window over levels
 // [L-1, L] that pass the stereo gate, with their distances (src/ORBmatcher.cc:84-145).
+// A candidate with nnratio * dist > TH_HIGH (nnratio <= 1) can neither be
+// accepted nor make an accepted best fail the ratio test, so it is left out.
 __global__ void k_proj_candidates(GridDev g, const orbgpu_mappoint* mps, const uint8_t* mp_desc, int m, float th,
-                                  const int* cand_start, int* cand_count, uint64_t* cand_out, int fill) {
+                                  float nnratio, const int* cand_start, int* cand_count, uint64_t* cand_out,
+                                  int fill) {
+    const bool drop_far = nnratio <= 1.0f;
     const int lane = threadIdx.x & 31;
     const int imp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (imp >= m) return;
@@ -302,31 +296,24 @@ __global__ void k_proj_candidates(GridDev g, const orbgpu_mappoint* mps, const u
         int x0, x1, y0, y1;
         if (area_cells(g, mp.proj_x, mp.proj_y, radius, x0, x1, y0, y1)) {
             const uint8_t* dmp = mp_desc + (size_t)imp * 32;
-            for (int ix = x0; ix <= x1; ix++)
-                for (int iy = y0; iy <= y1; iy++) {
-                    const int c = ix * ORBGPU_GRID_ROWS + iy;
-                    const int s = g.cell_start[c], e = g.cell_start[c + 1];
-                    for (int b = s; b < e; b += 32) {
-                        const int j = b + lane;
-                        bool ok = false;
-                        int idx = -1;
-                        if (j < e) {
-                            idx = g.cell_keys[j];
-                            ok = in_area(g, idx, mp.proj_x, mp.proj_y, radius, level - 1, level);
-                            if (ok && g.uright && g.uright[idx] > 0) {
-                                const float er = fabsf(__fsub_rn(mp.proj_xr, g.uright[idx]));
-                                if (er > radius) ok = false;
-                            }
-                        }
-                        const unsigned msk = __ballot_sync(0xffffffffu, ok);
-                        if (fill && ok) {
-                            const int pos = cand_start[imp] + total + __popc(msk & ((1u << lane) - 1));
-                            const int dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
-                            cand_out[pos] = cand_key(dist, c, idx);
-                        }
-                        total += __popc(msk);
-                    }
+            warp_window_keys(g.cell_start, g.cell_keys, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+                bool ok = valid && in_area(g, idx, mp.proj_x, mp.proj_y, radius, level - 1, level);
+                if (ok && g.uright && g.uright[idx] > 0) {
+                    const float er = fabsf(__fsub_rn(mp.proj_xr, g.uright[idx]));
+                    if (er > radius) ok = false;
                 }
+                int dist = 256;
+                if (ok) {
+                    dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
+                    ok = !(drop_far && __fmul_rn(nnratio, (float)dist) > (float)ORBGPU_TH_HIGH);
+                }
+                const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                if (fill && ok) {
+                    const int pos = cand_start[imp] + total + __popc(msk & ((1u << lane) - 1));
+                    cand_out[pos] = cand_key(dist, c, idx);
+                }
+                total += __popc(msk);
+            });
         }
     }
     if (!fill && lane == 0) cand_count[imp] = total;
@@ -525,34 +512,24 @@ __global__ void k_pf_candidates(GridDev g, FrameMotionDev mo, const orbgpu_keypo
         if (area_cells(g, u, v, radius, x0, x1, y0, y1)) {
             const uint8_t* dmp = mp_desc + (size_t)i * 32;
             const float ur = __fsub_rn(u, __fmul_rn(mo.bf, invzc));
-            for (int ix = x0; ix <= x1; ix++)
-                for (int iy = y0; iy <= y1; iy++) {
-                    const int c = ix * ORBGPU_GRID_ROWS + iy;
-                    const int s = g.cell_start[c], e = g.cell_start[c + 1];
-                    for (int b = s; b < e; b += 32) {
-                        const int j = b + lane;
-                        bool ok = false;
-                        int idx = -1, dist = 256;
-                        if (j < e) {
-                            idx = g.cell_keys[j];
-                            ok = in_area(g, idx, u, v, radius, minL, maxL);
-                            if (ok && g.uright && g.uright[idx] > 0) {
-                                const float er = fabsf(__fsub_rn(ur, g.uright[idx]));
-                                if (er > radius) ok = false;
-                            }
-                            if (ok) {
-                                dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
-                                ok = dist <= ORBGPU_TH_HIGH;
-                            }
-                        }
-                        const unsigned msk = __ballot_sync(0xffffffffu, ok);
-                        if (fill && ok) {
-                            const int pos = cand_start[i] + total + __popc(msk & ((1u << lane) - 1));
-                            cand_out[pos] = cand_key(dist, c, idx);
-                        }
-                        total += __popc(msk);
-                    }
+            warp_window_keys(g.cell_start, g.cell_keys, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+                bool ok = valid && in_area(g, idx, u, v, radius, minL, maxL);
+                if (ok && g.uright && g.uright[idx] > 0) {
+                    const float er = fabsf(__fsub_rn(ur, g.uright[idx]));
+                    if (er > radius) ok = false;
                 }
+                int dist = 256;
+                if (ok) {
+                    dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
+                    ok = dist <= ORBGPU_TH_HIGH;
+                }
+                const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                if (fill && ok) {
+                    const int pos = cand_start[i] + total + __popc(msk & ((1u << lane) - 1));
+                    cand_out[pos] = cand_key(dist, c, idx);
+                }
+                total += __popc(msk);
+            });
         }
     }
     if (!fill && lane == 0) cand_count[i] = total;
@@ -1170,8 +1147,8 @@ extern "C" int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame
         auto launch = [&](const int* st, int* cnt, uint64_t* out, int fill) {
             const int wpb = 8;
             if (M > 0)
-                k_proj_candidates<<<(M + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, d_mps, d_mpd, M, th, st, cnt, out,
-                                                                                fill);
+                k_proj_candidates<<<(M + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, d_mps, d_mpd, M, th, m->nnratio, st,
+                                                                                cnt, out, fill);
         };
         rc = candidate_lists(m, M, b, launch, start, count, keys, total);
         if (rc == ORBGPU_ERR_CAPACITY) {
