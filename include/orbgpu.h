@@ -206,8 +206,10 @@ int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* lef
 /* Brute-force k = 2 Hamming nearest neighbours over ORBmatcher::DescriptorDistance
  * semantics (src/ORBmatcher.cc:2083): for each query row, the best and the
  * second-best train rows, ties to the lower train index.  Not a reference
- * function: the build's batched matcher.  algo: 0 = popcount kernel.
- * All arrays on the device. */
+ * function: the build's batched matcher.  algo: 0 = popcount kernel, 1 =
+ * tensor cores (+-1 FP8 dot products, tcgen05), -1 = automatic (the tensor
+ * cores from the tuned problem size on, see orbgpu_tune_set); all give the
+ * same results.  All arrays on the device. */
 int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
                 int* idx2, int* d2, int algo);
 

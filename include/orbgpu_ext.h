@@ -70,6 +70,17 @@ int orbgpu_descriptor_sincos(const float* x, int n, float* c, float* s);
  * host 128 x 256 floats. */
 int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots, int* status_out, int lbo, int sbo);
 
+/* ------------------------------------------------------------ autotuner parameters */
+/* Launch shapes the autotuner chooses (orb_slam2_detailed_comments_gb300.autotune):
+ *   "resize_rows"          tile rows of the resize / blur / FAST-strength kernel: 8, 16, 32
+ *   "fast_cells_per_block" FAST cells (one warp each) per block: 1, 2, 4, 8
+ *   "describe_group"       keypoints per warp of the descriptor kernel: 4, 8, 16, 32
+ *   "knn_tc_min_pairs"     query x train size from which orbgpu_knn2(algo -1) uses tcgen05
+ * Process-wide; a change makes extractors and batches re-plan (and re-capture
+ * their graphs) on their next call.  Results do not depend on these values. */
+int orbgpu_tune_set(const char* name, long long value);
+int orbgpu_tune_get(const char* name, long long* value);
+
 /* ------------------------------------------------------------ rotation table */
 /* Builds the descriptor-rotation exception table (path NULL = next to the
  * library) with 'threads' host threads. */

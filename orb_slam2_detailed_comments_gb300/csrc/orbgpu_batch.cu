@@ -58,6 +58,7 @@ struct FramePlan {
     FrameLayout layout;  // offsets relative to the frame's slot
     std::vector<std::vector<uint8_t>> table_blob;  // per level (l >= 1): xofs..ybeta region
     std::vector<int> tiles;                         // resize/blur blocks per level
+    int gen = -1;                                   // tuning generation the tiles were counted for
 };
 
 struct orbgpu_batch {
@@ -99,6 +100,8 @@ struct orbgpu_batch {
     cudaEvent_t ev[6] = {};
     // frame configuration handed to the accessors of the last batch
     std::vector<float> frame_scale;  // nframes * 16
+    std::vector<int> frame_w, frame_h;
+    int frame_cap = 0;
 };
 
 static void destroy_graph(orbgpu_batch* b) {
@@ -172,6 +175,10 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
 static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out) {
     for (FramePlan* p : b->plans)
         if (p->w == w && p->h == h && p->nf == nf) {
+            if (p->gen != tune_generation()) {
+                for (int l = 0; l < b->nlevels; l++) p->tiles[l] = resize_blur_tiles(p->geom[l].w, p->geom[l].h);
+                p->gen = tune_generation();
+            }
             *out = p;
             return ORBGPU_OK;
         }
@@ -200,6 +207,7 @@ static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out
         resize_tables(P->geom[l - 1].w, P->geom[l - 1].h, L.w, L.h, (int*)&blob[o.xofs - lo], (short*)&blob[o.xalpha - lo],
                       (int*)&blob[o.yofs - lo], (short*)&blob[o.ybeta - lo]);
     }
+    P->gen = tune_generation();
     b->plans.push_back(P);
     *out = P;
     return ORBGPU_OK;
@@ -218,11 +226,16 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         sig.push_back(heights[f]);
         sig.push_back(nfeatures[f]);
     }
+    // launch shapes: a new tuning makes a new signature
+    sig.push_back(tune_generation());
     if (sig == b->sig) {
         b->same_sig_runs++;
         return ORBGPU_OK;
     }
     b->same_sig_runs = 0;
+    b->frame_w.assign(widths, widths + nframes);
+    b->frame_h.assign(heights, heights + nframes);
+    b->frame_cap = per_frame_cap;
     if (nlevels != b->nlevels || scale_factor != b->scale_factor) {  // configuration cache is per pyramid shape
         ORBGPU_CUDA_TRY(cudaStreamSynchronize(b->stream));
         for (FramePlan* p : b->plans) delete p;
@@ -302,7 +315,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     for (int f = 0; f < nframes; f++)
         for (int l = 0; l < nlevels; l++) {
             pre.push_back(acc);
-            acc += (b->cur[f]->geom[l].ncells + ORBGPU_FAST_CELLS_PER_BLOCK - 1) / ORBGPU_FAST_CELLS_PER_BLOCK;
+            acc += fast_blocks(b->cur[f]->geom[l].ncells);
         }
     pre.push_back(acc);
     b->fast_count = acc;
@@ -866,7 +879,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
     if (!b || b->nframes <= 0 || !kps || !desc || !counts || !mp_offsets || !match_out || !nmatches)
         return ORBGPU_ERR_BAD_ARG;
     const int nf = b->nframes;
-    const int cap = b->sig[4];
+    const int cap = b->frame_cap;
     const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
     const int total_mp = mp_offsets[nf];
     int max_mp = 0;
@@ -916,7 +929,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         int* frame_cands = (int*)take(sizeof(int) * nf);
         std::vector<BatchFrameInfo> hi(nf);
         for (int f = 0; f < nf; f++) {
-            const int w = b->sig[6 + 3 * f], h = b->sig[7 + 3 * f];
+            const int w = b->frame_w[f], h = b->frame_h[f];
             hi[f].invW = static_cast<float>(ORBGPU_GRID_COLS) / static_cast<float>((float)w - 0.0f);
             hi[f].invH = static_cast<float>(ORBGPU_GRID_ROWS) / static_cast<float>((float)h - 0.0f);
             hi[f].n_cap = cap;

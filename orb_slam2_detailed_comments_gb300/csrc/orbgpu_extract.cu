@@ -1,6 +1,7 @@
 // orbgpu_extract.cu -- host side of the extractor: level geometry, device
 // buffers, work lists and the C ABI of include/orbgpu.h for extraction.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -23,6 +24,44 @@ void orbgpu_set_last_error(const char* msg, const char* file, int line) {
 
 extern "C" const char* orbgpu_last_error(void) { return g_last_error.c_str(); }
 extern "C" int orbgpu_version(void) { return 1; }
+
+namespace orbgpu {
+static Tunables g_tunables;
+static std::atomic<int> g_tune_gen{0};
+const Tunables& tunables() { return g_tunables; }
+int tune_generation() { return g_tune_gen.load(); }
+}  // namespace orbgpu
+
+// Autotuner parameters; see orbgpu_ext.h.
+extern "C" int orbgpu_tune_set(const char* name, long long value) {
+    if (!name) return ORBGPU_ERR_BAD_ARG;
+    orbgpu::Tunables& t = orbgpu::g_tunables;
+    const std::string n(name);
+    if (n == "resize_rows" && (value == 8 || value == 16 || value == 32)) t.resize_rows = (int)value;
+    else if (n == "fast_cells_per_block" && (value == 1 || value == 2 || value == 4 || value == 8))
+        t.fast_cells_per_block = (int)value;
+    else if (n == "describe_group" && (value == 4 || value == 8 || value == 16 || value == 32))
+        t.describe_group = (int)value;
+    else if (n == "knn_tc_min_pairs" && value >= 0) t.knn_tc_min_pairs = value;
+    else {
+        orbgpu_set_last_error("unknown tuning parameter or value", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    orbgpu::g_tune_gen++;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_tune_get(const char* name, long long* value) {
+    if (!name || !value) return ORBGPU_ERR_BAD_ARG;
+    const orbgpu::Tunables& t = orbgpu::g_tunables;
+    const std::string n(name);
+    if (n == "resize_rows") *value = t.resize_rows;
+    else if (n == "fast_cells_per_block") *value = t.fast_cells_per_block;
+    else if (n == "describe_group") *value = t.describe_group;
+    else if (n == "knn_tc_min_pairs") *value = t.knn_tc_min_pairs;
+    else return ORBGPU_ERR_BAD_ARG;
+    return ORBGPU_OK;
+}
 
 namespace orbgpu {
 
@@ -371,6 +410,7 @@ struct SizePlan {
     int fast_first = 0, fast_count = 0;
     int max_kept = 0, sort_cap = 0;
     uint64_t last_use = 0;
+    int gen = -1;  // tuning generation of the work lists
 };
 
 struct orbgpu_extractor {
@@ -444,7 +484,7 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     int acc = 0;
     for (size_t l = 0; l < g.size(); l++) {
         pre.push_back(acc);
-        acc += (g[l].ncells + ORBGPU_FAST_CELLS_PER_BLOCK - 1) / ORBGPU_FAST_CELLS_PER_BLOCK;
+        acc += fast_blocks(g[l].ncells);
     }
     pre.push_back(acc);
     P->fast_count = acc;
@@ -467,9 +507,18 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
 
 static int setup_geometry(orbgpu_extractor* ex, int w, int h) {
     ex->use_clock++;
-    if (ex->cur && ex->cur->w == w && ex->cur->h == h) {
+    if (ex->cur && ex->cur->w == w && ex->cur->h == h && ex->cur->gen == tune_generation()) {
         ex->cur->last_use = ex->use_clock;
         return ORBGPU_OK;
+    }
+    // work lists counted for other launch shapes are rebuilt
+    bool stale = false;
+    for (SizePlan* p : ex->plans) stale |= p->gen != tune_generation();
+    if (stale) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(ex->stream));
+        for (SizePlan* p : ex->plans) free_plan(p);
+        ex->plans.clear();
+        ex->cur = nullptr;
     }
     SizePlan* found = nullptr;
     for (SizePlan* p : ex->plans)
@@ -484,6 +533,7 @@ static int setup_geometry(orbgpu_extractor* ex, int w, int h) {
         }
         int rc = build_plan(ex, w, h, &found);
         if (rc != ORBGPU_OK) return rc;
+        found->gen = tune_generation();
         ex->plans.push_back(found);
     }
     found->last_use = ex->use_clock;

@@ -70,8 +70,19 @@ struct LevelDesc {
     int* frame_total;     // the frame's keypoint count
 };
 
-// FAST cells handled by one block of k_fast_cells (one warp each).
-#define ORBGPU_FAST_CELLS_PER_BLOCK 4
+// Launch shapes chosen by the autotuner (orbgpu_tune_set): tile rows of the
+// resize / blur / strength kernel, FAST cells per block, keypoints per warp of
+// the descriptor kernel, and the query x train size from which orbgpu_knn2's
+// automatic choice uses the tensor cores.  Changing one bumps the generation,
+// so cached frame plans and captured graphs are rebuilt.
+struct Tunables {
+    int resize_rows = 16;
+    int fast_cells_per_block = 4;
+    int describe_group = 8;
+    long long knn_tc_min_pairs = 1LL << 28;
+};
+const Tunables& tunables();
+int tune_generation();
 
 struct DNode {
     int16_t x0, x1, y0, y1;
@@ -103,6 +114,7 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st);
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st);
 int resize_blur_tiles(int w, int h);
+int fast_blocks(int ncells);
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st);

@@ -95,9 +95,11 @@ int orbgpu_knn2_tc(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_
 extern "C" int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1,
                            int* d1, int* idx2, int* d2, int algo) {
     if (!m || nq < 0 || nt < 0 || (nq > 0 && (!query || !idx1 || !d1 || !idx2 || !d2)) || (nt > 0 && !train) ||
-        (algo != 0 && algo != 1))
+        (algo != 0 && algo != 1 && algo != -1))
         return ORBGPU_ERR_BAD_ARG;
     if (nq == 0) return ORBGPU_OK;
+    if (algo == -1)  // automatic: the tensor cores from the tuned problem size on
+        algo = (long long)nq * nt >= tunables().knn_tc_min_pairs ? 1 : 0;
     if (algo == 1 && nt > 0) return orbgpu_knn2_tc(m, query, nq, train, nt, idx1, d1, idx2, d2);
     cudaStream_t st = orbgpu_matcher_stream_internal(m);
     int dev, nsm;
