@@ -35,7 +35,6 @@ __device__ __forceinline__ int reflect101(int p, int len) {
 
 // ---------------------------------------------------------------- pyramid
 #define RB_TW 64
-#define RB_TH 16
 #define RB_HALO 3
 
 __device__ __forceinline__ int resize_pixel(const LevelDesc& d, int x, int y) {
@@ -186,23 +185,28 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 //    circle lies inside the level is scored (others get 0 and are never
 //    read by the cell stage).
 #define RB_SW 72                       // shared row: columns [ox - 4, ox + 68)
-#define RB_SH (RB_TH + 2 * RB_HALO)    // 22 rows: [oy - 3, oy + 19)
 #define RB_SRC_W 96                    // staged source columns (72 taps x 1.25 + 2, word aligned)
-#define RB_SRC_H 32                    // staged source rows (22 taps x 1.25 + 2)
 
 __device__ __forceinline__ int byte_of(uint32_t w, int j) { return (int)((w >> (8 * j)) & 0xFFu); }
 
-__global__ void __launch_bounds__(256, 5) k_level_resize_blur(const LevelDesc* descs, RangeMap rm, int level0) {
+// TH (tile rows, 8 / 16 / 32) is chosen by the autotuner; the block has
+// 16 * TH threads (one 4-pixel group of the core each).
+template <int TH>
+__global__ void __launch_bounds__(16 * TH, 1280 / (16 * TH))
+    k_level_resize_blur(const LevelDesc* descs, RangeMap rm, int level0) {
+    constexpr int RB_TH_ = TH;
+    constexpr int RB_SH = TH + 2 * RB_HALO;          // rows [oy - 3, oy + TH + 3)
+    constexpr int RB_SRC_H = (RB_SH * 5) / 4 + 4;    // staged source rows (RB_SH taps x 1.25 + 2)
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int tiles_x = (d.w + RB_TW - 1) / RB_TW;
-    const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH;
+    const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH_;
     __shared__ __align__(16) uint8_t tile[RB_SH][RB_SW];
     __shared__ __align__(16) int rows[RB_SH][RB_TW];
-    __shared__ __align__(16) uint8_t s_str[RB_TH][RB_TW];
+    __shared__ __align__(16) uint8_t s_str[RB_TH_][RB_TW];
     __shared__ __align__(16) uint8_t src_s[RB_SRC_H][RB_SRC_W];
-    __shared__ uint16_t s_q[RB_TH * RB_TW];
+    __shared__ uint16_t s_q[RB_TH_ * RB_TW];
     __shared__ short c_sx[RB_SW], c_sx1[RB_SW], c_a0[RB_SW], c_a1[RB_SW];
     __shared__ short r_r0[RB_SH], r_r1[RB_SH], r_b0[RB_SH], r_b1[RB_SH];
     __shared__ int s_rng[4];
@@ -210,7 +214,7 @@ __global__ void __launch_bounds__(256, 5) k_level_resize_blur(const LevelDesc* d
     const int tid = threadIdx.x;
     if (tid == 0) s_nq = 0;
     if (level0) {
-        if (ox >= 4 && ox + 68 <= d.w && oy >= 3 && oy + RB_TH + 3 <= d.h) {
+        if (ox >= 4 && ox + 68 <= d.w && oy >= 3 && oy + RB_TH_ + 3 <= d.h) {
             for (int i = tid; i < RB_SH * (RB_SW / 4); i += blockDim.x) {
                 const int ty = i / (RB_SW / 4), wx = i - ty * (RB_SW / 4);
                 *reinterpret_cast<uint32_t*>(&tile[ty][4 * wx]) =
@@ -236,8 +240,8 @@ __global__ void __launch_bounds__(256, 5) k_level_resize_blur(const LevelDesc* d
             c_a1[tid] = d.xalpha[2 * x + 1];
             atomicMin(&s_rng[0], sx);
             atomicMax(&s_rng[1], sx1);
-        } else if (tid >= 128 && tid < 128 + RB_SH) {
-            const int ty = tid - 128;
+        } else if (tid >= RB_SW && tid < RB_SW + RB_SH) {
+            const int ty = tid - RB_SW;
             const int y = reflect101(oy - 3 + ty, d.h);
             const int sy = d.yofs[y];
             const int r0 = min(max(sy, 0), d.sh - 1), r1 = min(max(sy + 1, 0), d.sh - 1);
@@ -417,16 +421,17 @@ __device__ __forceinline__ bool fast_keep(const uint8_t* mstr, int dw, int dh, i
 // iniThFAST and, when that leaves nothing, at minThFAST; survivors are
 // written row by row in the detector's row-major order with a running warp
 // count (no block-wide scan).
-__global__ void __launch_bounds__(32 * ORBGPU_FAST_CELLS_PER_BLOCK)
-    k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
+// CPB (cells per block, 1 / 2 / 4 / 8) is chosen by the autotuner.
+template <int CPB>
+__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1;
-    const int cell = it.index * ORBGPU_FAST_CELLS_PER_BLOCK + warp;
+    const int cell = it.index * CPB + warp;
     if (cell >= d.nCols * d.nRows) return;
-    __shared__ uint8_t s_m[ORBGPU_FAST_CELLS_PER_BLOCK][FAST_MAX_DET * FAST_MAX_DET];
+    __shared__ uint8_t s_m[CPB][FAST_MAX_DET * FAST_MAX_DET];
     uint8_t* mstr = s_m[warp];
     const int i = cell / d.nCols, j = cell - (cell / d.nCols) * d.nCols;
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
@@ -444,9 +449,24 @@ __global__ void __launch_bounds__(32 * ORBGPU_FAST_CELLS_PER_BLOCK)
         return;
     }
     const int dw = rw - 6, dh = rh - 6;
-    for (int r = 0; r < dh; r++) {
-        const uint8_t* src = d.strength + (size_t)(iniY + 3 + r) * d.pitch + iniX + 3;
-        for (int c = lane; c < dw; c += 32) mstr[r * dw + c] = src[c];
+    // staged 8 rows at a time with every load in flight before the stores
+    const uint8_t* src = d.strength + (size_t)(iniY + 3) * d.pitch + iniX + 3;
+    for (int r0 = 0; r0 < dh; r0 += 8) {
+        uint8_t v[8][3];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const int r = r0 + u, c = lane + 32 * k;
+                v[u][k] = (r < dh && c < dw) ? src[(size_t)r * d.pitch + c] : (uint8_t)0;
+            }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const int r = r0 + u, c = lane + 32 * k;
+                if (r < dh && c < dw) mstr[r * dw + c] = v[u][k];
+            }
     }
     __syncwarp();
     const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
@@ -841,7 +861,8 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
 // are frame-major with levels ascending, so a level's offset inside its
 // frame is a difference of two prefix entries); keypoint g of the flattened
 // list finds its level by binary search.
-#define DESC_GROUP 8
+// DESC_GROUP (keypoints per warp, 4 / 8 / 16 / 32) is chosen by the autotuner.
+template <int DESC_GROUP>
 __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
                                                   uint8_t* out_desc, int* status) {
     extern __shared__ int s_pre[];  // ndescs + 1
@@ -1002,13 +1023,31 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
 }
 
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
-    if (nitems > 0) k_level_resize_blur<<<nitems, 256, 0, st>>>(descs, rm, level0);
+    if (nitems <= 0) return;
+    switch (tunables().resize_rows) {
+        case 8: k_level_resize_blur<8><<<nitems, 16 * 8, 0, st>>>(descs, rm, level0); break;
+        case 32: k_level_resize_blur<32><<<nitems, 16 * 32, 0, st>>>(descs, rm, level0); break;
+        default: k_level_resize_blur<16><<<nitems, 16 * 16, 0, st>>>(descs, rm, level0); break;
+    }
 }
 
 // Blocks of k_level_resize_blur for a w x h level.
-int resize_blur_tiles(int w, int h) { return ((w + RB_TW - 1) / RB_TW) * ((h + RB_TH - 1) / RB_TH); }
+int resize_blur_tiles(int w, int h) {
+    const int th = tunables().resize_rows;
+    return ((w + RB_TW - 1) / RB_TW) * ((h + th - 1) / th);
+}
+int fast_blocks(int ncells) {
+    const int cpb = tunables().fast_cells_per_block;
+    return (ncells + cpb - 1) / cpb;
+}
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st) {
-    if (nitems > 0) k_fast_cells<<<nitems, 32 * ORBGPU_FAST_CELLS_PER_BLOCK, 0, st>>>(descs, rm, status);
+    if (nitems <= 0) return;
+    switch (tunables().fast_cells_per_block) {
+        case 1: k_fast_cells<1><<<nitems, 32, 0, st>>>(descs, rm, status); break;
+        case 2: k_fast_cells<2><<<nitems, 64, 0, st>>>(descs, rm, status); break;
+        case 8: k_fast_cells<8><<<nitems, 256, 0, st>>>(descs, rm, status); break;
+        default: k_fast_cells<4><<<nitems, 128, 0, st>>>(descs, rm, status); break;
+    }
 }
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {
     const size_t smem = (size_t)sort_cap * sizeof(unsigned long long);
@@ -1019,12 +1058,19 @@ void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_ke
                      cudaStream_t st) {
     if (ndescs <= 0 || max_kept <= 0) return;
     const int nsm = nsm_of_current_device();
-    // DESC_GROUP keypoints per warp, 8 warps per block; max_kept (the node
+    const int group = tunables().describe_group;
+    // 'group' keypoints per warp, 8 warps per block; max_kept (the node
     // capacity) overestimates a level's keypoints about twice; at most 8
     // resident blocks per SM
-    const long want = ((long)ndescs * max_kept / 2 + 8 * DESC_GROUP - 1) / (8 * DESC_GROUP);
+    const long want = ((long)ndescs * max_kept / 2 + 8 * group - 1) / (8 * group);
     const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 8));
-    k_describe<<<blocks, 256, sizeof(int) * (ndescs + 1), st>>>(descs, ndescs, kps, desc, status);
+    const size_t smem = sizeof(int) * (ndescs + 1);
+    switch (group) {
+        case 4: k_describe<4><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+        case 16: k_describe<16><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+        case 32: k_describe<32><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+        default: k_describe<8><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+    }
 }
 
 }  // namespace orbgpu
