@@ -39,6 +39,23 @@ int orbgpu_batch_search_launch_count(void);
  * same results. */
 int orbgpu_batch_search_mode(int mode);
 
+/* SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame, th, bMono)
+ * (src/ORBmatcher.cc:1710-1879) for every frame of the last
+ * orbgpu_batch_extract call: CurrentFrame f is the batch's frame f (its
+ * mvpMapPoints empty beforehand, as TrackWithMotionModel leaves them), and
+ * LastFrame f owns rows [last_offsets[f], last_offsets[f + 1]) of last_kps /
+ * last_mps / last_desc (device; last_offsets and motions are host arrays of
+ * nframes + 1 and nframes).  check_ori is the matcher's checkOri.
+ * match_out: device, nframes * per_frame_capacity ints (LastFrame row within
+ * the frame whose map point now fills the keypoint, -1 none, -4 reset by the
+ * rotation check, -3 past the frame's keypoints); nmatches: device, nframes
+ * ints (the reference's return value).  Per-frame capacity below 4096. */
+int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const orbgpu_keypoint* kps, const uint8_t* desc,
+                                            const int* counts, const orbgpu_keypoint* last_kps,
+                                            const orbgpu_frame_mappoint* last_mps, const uint8_t* last_desc,
+                                            const int* last_offsets, const orbgpu_frame_motion* motions, float th,
+                                            int mono, int check_ori, int* match_out, int* nmatches);
+
 /* ------------------------------------------------------------ batch instrumentation */
 /* Device milliseconds of the five stages of the last orbgpu_batch_extract
  * (gather, resize + blur, FAST, octree, orientation + descriptor); n >= 5. */

@@ -106,3 +106,48 @@ class BatchProjection:
 
     def launches_per_search(self) -> int:
         return int(lib().orbgpu_batch_search_launch_count())
+
+
+def motion_struct(Tcw, Tlw, fx, fy, cx, cy, bf=0.0, b=0.0):
+    """orbgpu_frame_motion from rows 0-2 of CurrentFrame.mTcw / LastFrame.mTcw."""
+    from ._lib import MotionStruct
+    m = MotionStruct()
+    for i, v in enumerate(np.asarray(Tcw, np.float32).reshape(-1)[:12]):
+        m.Tcw[i] = float(v)
+    for i, v in enumerate(np.asarray(Tlw, np.float32).reshape(-1)[:12]):
+        m.Tlw[i] = float(v)
+    m.fx, m.fy, m.cx, m.cy, m.bf, m.b = (float(np.float32(v)) for v in (fx, fy, cx, cy, bf, b))
+    return m
+
+
+class BatchFrameProjection:
+    """SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame, th, bMono)
+    for every frame of the batch's last extraction, each against its own
+    LastFrame (orbgpu_batch_search_by_projection_frame)."""
+
+    def __init__(self, batch: BatchExtractor, check_ori: bool = True):
+        import torch
+        self.batch = batch
+        self.check_ori = check_ori
+        self.match = torch.empty(batch.max_frames * batch.per_frame_capacity, dtype=torch.int32, device="cuda")
+        self.nm = torch.zeros(batch.max_frames, dtype=torch.int32, device="cuda")
+
+    def search(self, last_kps, last_mps_u8, last_desc, last_counts, motions, th: float, mono: bool):
+        """last_kps: (R, 7) float32 CUDA tensor of all frames' LastFrame
+        keypoints back to back; last_mps_u8: their orbgpu_frame_mappoint
+        records (uint8 CUDA tensor, 16 bytes each); last_desc: (R, 32) CUDA
+        tensor of the map points' descriptors; last_counts: rows per frame;
+        motions: one motion_struct per frame.  Returns (match (F*cap,),
+        nmatches (F,))."""
+        from ._lib import MotionStruct
+        b = self.batch
+        n = len(last_counts)
+        off = np.zeros(n + 1, np.int32)
+        off[1:] = np.cumsum(last_counts)
+        mo = (MotionStruct * n)(*motions)
+        self._keep = (off, mo)
+        check(lib().orbgpu_batch_search_by_projection_frame(
+            b.handle, ptr(b.kps), ptr(b.desc), ptr(b.counts), ptr(last_kps), ptr(last_mps_u8), ptr(last_desc),
+            ptr(off), mo, C.c_float(th), int(bool(mono)), int(bool(self.check_ori)), ptr(self.match), ptr(self.nm)),
+            "orbgpu_batch_search_by_projection_frame")
+        return self.match[: n * b.per_frame_capacity], self.nm[:n]

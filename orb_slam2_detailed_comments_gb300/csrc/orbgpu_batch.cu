@@ -1003,3 +1003,407 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
 extern "C" int orbgpu_batch_search_launch_count(void) {
     return orbgpu_batch_search_last_launches();
 }
+
+// ---------------------------------------------------------------- batched SearchByProjection(Frame, LastFrame)
+// ORBmatcher::SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame,
+// th, bMono) (src/ORBmatcher.cc:1710-1879) for every frame of the last batch:
+// CurrentFrame f is the batch's frame f, LastFrame f comes with its own
+// keypoints, map points and pose.  Candidate keys are 32 bits (distance,
+// GetFeaturesInArea cell, keypoint index), only those at or below TH_HIGH
+// (no ratio test: the first minimum wins).  One block per frame resolves the
+// in-order assignment (owners without observations block nothing), the
+// owners, the rotation histogram, the three maxima and the resets.
+namespace orbgpu {
+
+struct BatchMotion {
+    float T[12];
+    float fx, fy, cx, cy, bf;
+    float maxX, maxY;
+    int level_mode;
+};
+
+__device__ __forceinline__ float bpose_row(const float* row, float X0, float X1, float X2) {
+    double s = __dadd_rn(0.0, __dmul_rn((double)row[0], (double)X0));
+    s = __dadd_rn(s, __dmul_rn((double)row[1], (double)X1));
+    s = __dadd_rn(s, __dmul_rn((double)row[2], (double)X2));
+    return __fadd_rn(__double2float_rn(s), row[3]);
+}
+
+__global__ void k_bpf_candidates(const orbgpu_keypoint* kps, const uint8_t* desc, int cap, const BatchFrameInfo* info,
+                                 const int* cell_start, const int* cell_keys, const BatchMotion* motions,
+                                 const orbgpu_keypoint* last_kps, const orbgpu_frame_mappoint* last_mps,
+                                 const uint8_t* last_desc, const int* last_off, float th, int slot_cap,
+                                 uint32_t* slots, int* slot_count, int* status, int* frame_cands) {
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    const int f = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int i = last_off[f] + local;
+    if (i >= last_off[f + 1]) return;
+    const orbgpu_frame_mappoint mp = last_mps[i];
+    const BatchMotion& mo = motions[f];
+    const BatchFrameInfo& I = info[f];
+    const orbgpu_keypoint* K = kps + (size_t)f * cap;
+    const uint8_t* D = desc + (size_t)f * cap * 32;
+    const int* cs = cell_start + (size_t)f * (ncell + 1);
+    const int* ck = cell_keys + (size_t)f * cap;
+    const int oct = last_kps[i].octave;
+    int total = 0;
+    bool live = (mp.flags & ORBGPU_MP_PRESENT) && !(mp.flags & ORBGPU_MP_OUTLIER) && oct >= 0 && oct < 16;
+    float u = 0.f, v = 0.f;
+    if (live) {
+        const float xc = bpose_row(mo.T, mp.x, mp.y, mp.z);
+        const float yc = bpose_row(mo.T + 4, mp.x, mp.y, mp.z);
+        const float zc = bpose_row(mo.T + 8, mp.x, mp.y, mp.z);
+        const float invzc = __double2float_rn(__ddiv_rn(1.0, (double)zc));
+        u = __fadd_rn(__fmul_rn(__fmul_rn(mo.fx, xc), invzc), mo.cx);
+        v = __fadd_rn(__fmul_rn(__fmul_rn(mo.fy, yc), invzc), mo.cy);
+        live = !(invzc < 0.f) && isfinite(u) && isfinite(v) && !(u < 0.0f || u > mo.maxX) && !(v < 0.0f || v > mo.maxY);
+    }
+    if (live) {
+        const float radius = __fmul_rn(th, I.scale[oct]);
+        int minL, maxL;
+        if (mo.level_mode == 1) {
+            minL = oct;
+            maxL = -1;
+        } else if (mo.level_mode == 2) {
+            minL = 0;
+            maxL = oct;
+        } else {
+            minL = oct - 1;
+            maxL = oct + 1;
+        }
+        const bool check = (minL > 0) || (maxL >= 0);  // GetFeaturesInArea's level test (src/Frame.cc:628)
+        const int x0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(u, 0.0f), radius), I.invW)));
+        const int x1 = min(ORBGPU_GRID_COLS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(u, 0.0f), radius), I.invW)));
+        const int y0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(v, 0.0f), radius), I.invH)));
+        const int y1 = min(ORBGPU_GRID_ROWS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(v, 0.0f), radius), I.invH)));
+        if (x0 < ORBGPU_GRID_COLS && x1 >= 0 && y0 < ORBGPU_GRID_ROWS && y1 >= 0) {
+            const uint8_t* dmp = last_desc + (size_t)i * 32;
+            const float rr = __fmul_rn(radius, radius);
+            warp_window_keys(cs, ck, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+                bool ok = false;
+                int dist = 256;
+                if (valid) {
+                    const orbgpu_keypoint kp = K[idx];
+                    ok = !(check && (kp.octave < minL || (maxL >= 0 && kp.octave > maxL)));
+                    if (ok) {
+                        const float dx = __fsub_rn(kp.x, u), dy = __fsub_rn(kp.y, v);
+                        ok = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < rr;
+                    }
+                    if (ok) {
+                        dist = hamming256_ptr(dmp, D + (size_t)idx * 32);
+                        ok = dist <= ORBGPU_TH_HIGH;
+                    }
+                }
+                const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    const int pos = total + __popc(msk & ((1u << lane) - 1));
+                    if (pos < slot_cap)
+                        slots[(size_t)i * slot_cap + pos] = ((uint32_t)dist << 24) | ((uint32_t)c << 12) | (uint32_t)idx;
+                }
+                total += __popc(msk);
+            });
+        }
+    }
+    if (lane == 0) {
+        slot_count[i] = total;
+        if (total > slot_cap) atomicMax(status, total);
+        if (total > 0) atomicAdd(&frame_cands[f], min(total, slot_cap));
+    }
+}
+
+// One block per frame.  Shared memory: list starts (M + 1), results (M),
+// two claim arrays (cap), observed flags and histogram bins (M bytes each),
+// and the keys when t_cap > 0 (else they are read from the global slots).
+__global__ void __launch_bounds__(1024)
+    k_bpf_resolve(const orbgpu_keypoint* kps, int cap, const int* counts, const orbgpu_keypoint* last_kps,
+                  const orbgpu_frame_mappoint* last_mps, const int* last_off, int slot_cap, const uint32_t* slots,
+                  const int* slot_count, int check_ori, int t_cap, int* match_out, int* nmatches, int* status) {
+    extern __shared__ __align__(16) int s_dyn[];
+    __shared__ int s_scan[32];
+    __shared__ int s_flag[3];
+    __shared__ int hist[ORBGPU_HISTO_LENGTH];
+    __shared__ int s_ind[3];
+    const int f = blockIdx.x;
+    const int tid = threadIdx.x;
+    const int mp0 = last_off[f], M = last_off[f + 1] - mp0;
+    const int n = min(counts[f], cap);
+    int* s_start = s_dyn;               // M + 1
+    int* s_res = s_start + (M + 1);     // M
+    int* cr = s_res + M;                // cap
+    int* cw = cr + cap;                 // cap
+    uint32_t* s_key = reinterpret_cast<uint32_t*>(cw + cap);            // t_cap
+    uint8_t* s_obs = reinterpret_cast<uint8_t*>(s_key + t_cap);         // M
+    uint8_t* s_bin = s_obs + M;                                         // M
+    int base = 0;
+    for (int i0 = 0; i0 < M; i0 += blockDim.x) {
+        const int i = i0 + tid;
+        const int v = i < M ? min(slot_count[mp0 + i], slot_cap) : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (i < M) s_start[i] = base + ex;
+        base += tot;
+    }
+    const bool in_smem = t_cap > 0;
+    if (in_smem && base > t_cap) {
+        if (tid == 0) atomicOr(status + 2, 1);
+        return;
+    }
+    if (tid == 0) s_start[M] = base;
+    if (tid < 3) s_flag[tid] = 0;
+    if (tid < ORBGPU_HISTO_LENGTH) hist[tid] = 0;
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    if (in_smem)
+        for (int i = warp; i < M; i += nw) {
+            const int s0 = s_start[i], cnt = s_start[i + 1] - s0;
+            const uint32_t* S = slots + (size_t)(mp0 + i) * slot_cap;
+            for (int b = lane; b < cnt; b += 32) s_key[s0 + b] = S[b];
+        }
+    for (int i = tid; i < M; i += blockDim.x) {
+        s_res[i] = -2;
+        s_obs[i] = (last_mps[mp0 + i].flags & ORBGPU_MP_OBSERVED) ? 1 : 0;
+    }
+    for (int k = tid; k < cap; k += blockDim.x) {
+        cr[k] = 0x7fffffff;
+        cw[k] = 0x7fffffff;
+    }
+    bool converged = M == 0;
+    for (int round = 0; round <= M + 1 && !converged; round++) {
+        if (tid == 0) s_flag[(round + 1) % 3] = 0;
+        __syncthreads();
+        for (int i = tid; i < M; i += blockDim.x) {
+            const int cnt = s_start[i + 1] - s_start[i];
+            const uint32_t* L = in_smem ? s_key + s_start[i] : slots + (size_t)(mp0 + i) * slot_cap;
+            uint32_t best = 0xFFFFFFFFu;
+            for (int e = 0; e < cnt; e++) {
+                const uint32_t key = L[e];
+                if (!(cr[key & 0xFFFu] < i) && key < best) best = key;
+            }
+            const int r = best == 0xFFFFFFFFu ? -1 : (int)(best & 0xFFFu);
+            if (r != s_res[i]) {
+                s_res[i] = r;
+                s_flag[round % 3] = 1;
+            }
+            if (r >= 0 && s_obs[i]) atomicMin(&cw[r], i);
+        }
+        __syncthreads();
+        converged = s_flag[round % 3] == 0;
+        int* t = cr;
+        cr = cw;
+        cw = t;
+        if (!converged)
+            for (int k = tid; k < cap; k += blockDim.x) cw[k] = 0x7fffffff;
+    }
+    if (!converged && tid == 0) atomicOr(status + 2, 2);
+    // owners (the last map point that assigned each keypoint), rotation histogram
+    int* owner = cr;
+    int* nulled = cw;
+    __syncthreads();
+    for (int k = tid; k < cap; k += blockDim.x) {
+        owner[k] = -1;
+        nulled[k] = 0;
+    }
+    __syncthreads();
+    const orbgpu_keypoint* K = kps + (size_t)f * cap;
+    const float factor = __fdiv_rn((float)ORBGPU_HISTO_LENGTH, 360.0f);
+    int nm = 0;
+    for (int i = tid; i < M; i += blockDim.x) {
+        const int r = s_res[i];
+        uint8_t bin = 0xFF;
+        if (r >= 0) {
+            nm++;
+            atomicMax(&owner[r], i);
+            if (check_ori) {
+                float rot = __fsub_rn(last_kps[mp0 + i].angle, K[r].angle);
+                if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
+                int bb = (int)roundf(__fmul_rn(rot, factor));
+                if (bb == ORBGPU_HISTO_LENGTH) bb = 0;
+                bin = (uint8_t)bb;
+                atomicAdd(&hist[bb], 1);
+            }
+        }
+        s_bin[i] = bin;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        if (check_ori) {
+            int max1 = 0, max2 = 0, max3 = 0;
+            for (int b = 0; b < ORBGPU_HISTO_LENGTH; b++) {  // ComputeThreeMaxima, src/ORBmatcher.cc:2035-2077
+                const int sz = hist[b];
+                if (sz > max1) {
+                    max3 = max2; max2 = max1; max1 = sz;
+                    ind3 = ind2; ind2 = ind1; ind1 = b;
+                } else if (sz > max2) {
+                    max3 = max2; max2 = sz;
+                    ind3 = ind2; ind2 = b;
+                } else if (sz > max3) {
+                    max3 = sz;
+                    ind3 = b;
+                }
+            }
+            if ((float)max2 < __fmul_rn(0.1f, (float)max1)) {
+                ind2 = -1;
+                ind3 = -1;
+            } else if ((float)max3 < __fmul_rn(0.1f, (float)max1)) {
+                ind3 = -1;
+            }
+        }
+        s_ind[0] = ind1;
+        s_ind[1] = ind2;
+        s_ind[2] = ind3;
+    }
+    __syncthreads();
+    int removed = 0;
+    if (check_ori)
+        for (int i = tid; i < M; i += blockDim.x) {
+            const int b = s_bin[i];
+            if (b == 0xFF || b == s_ind[0] || b == s_ind[1] || b == s_ind[2]) continue;
+            nulled[s_res[i]] = 1;
+            removed++;
+        }
+    __syncthreads();
+    int* Mo = match_out + (size_t)f * cap;
+    for (int k = tid; k < cap; k += blockDim.x) Mo[k] = k >= n ? -3 : nulled[k] ? -4 : (owner[k] >= 0 ? owner[k] : -1);
+    int tot;
+    block_exclusive_scan(nm - removed, s_scan, &tot);
+    if (tid == 0) nmatches[f] = tot;
+}
+
+}  // namespace orbgpu
+
+extern "C" int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const orbgpu_keypoint* kps, const uint8_t* desc,
+                                                       const int* counts, const orbgpu_keypoint* last_kps,
+                                                       const orbgpu_frame_mappoint* last_mps,
+                                                       const uint8_t* last_desc, const int* last_offsets,
+                                                       const orbgpu_frame_motion* motions, float th, int mono,
+                                                       int check_ori, int* match_out, int* nmatches) {
+    if (!b || b->nframes <= 0 || !kps || !desc || !counts || !last_offsets || !motions || !match_out || !nmatches)
+        return ORBGPU_ERR_BAD_ARG;
+    const int nf = b->nframes;
+    const int cap = b->frame_cap;
+    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
+    const int total_mp = last_offsets[nf];
+    if (cap >= 4096 || total_mp < 0 || (total_mp > 0 && (!last_kps || !last_mps || !last_desc))) {
+        orbgpu_set_last_error("batched frame search: per-frame capacity must be below 4096", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    int max_mp = 0;
+    for (int f = 0; f < nf; f++) {
+        if (last_offsets[f + 1] < last_offsets[f]) return ORBGPU_ERR_BAD_ARG;
+        max_mp = std::max(max_mp, last_offsets[f + 1] - last_offsets[f]);
+    }
+    orbgpu_batch_proj& P = g_bproj;
+    if (!P.h_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_pinned, 64));
+    if (P.h_cands_cap < nf) {
+        if (P.h_cands) cudaFreeHost(P.h_cands);
+        P.h_cands = nullptr;
+        ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_cands, sizeof(int) * nf));
+        P.h_cands_cap = nf;
+    }
+    std::vector<BatchMotion> hm(nf);
+    std::vector<BatchFrameInfo> hi(nf);
+    for (int f = 0; f < nf; f++) {
+        const orbgpu_frame_motion& m = motions[f];
+        std::memcpy(hm[f].T, m.Tcw, sizeof(hm[f].T));
+        hm[f].fx = m.fx;
+        hm[f].fy = m.fy;
+        hm[f].cx = m.cx;
+        hm[f].cy = m.cy;
+        hm[f].bf = m.bf;
+        hm[f].maxX = (float)b->frame_w[f];
+        hm[f].maxY = (float)b->frame_h[f];
+        hm[f].level_mode = motion_level_mode(m, mono);
+        const int w = b->frame_w[f], h = b->frame_h[f];
+        hi[f].invW = static_cast<float>(ORBGPU_GRID_COLS) / static_cast<float>((float)w - 0.0f);
+        hi[f].invH = static_cast<float>(ORBGPU_GRID_ROWS) / static_cast<float>((float)h - 0.0f);
+        hi[f].n_cap = cap;
+        for (int l = 0; l < 16; l++) hi[f].scale[l] = b->frame_scale[(size_t)f * 16 + l];
+    }
+    cudaStream_t st = b->stream;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        const size_t need = sizeof(BatchFrameInfo) * nf + sizeof(BatchMotion) * nf +
+                            sizeof(int) * ((size_t)nf * ncell * 2 + (size_t)nf * (ncell + 1) + (size_t)nf * cap * 2 +
+                                           (nf + 1) + (size_t)std::max(1, total_mp) + nf + 16) +
+                            sizeof(uint32_t) * (size_t)std::max(1, total_mp) * P.slot_cap + 16 * 256;
+        if (need > P.bytes) {
+            ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+            if (P.scratch) cudaFree(P.scratch);
+            P.scratch = nullptr;
+            ORBGPU_CUDA_TRY(cudaMalloc(&P.scratch, need));
+            P.bytes = need;
+        }
+        size_t off = 0;
+        auto take = [&](size_t n) {
+            off = (off + 255) & ~(size_t)255;
+            uint8_t* p = P.scratch + off;
+            off += n;
+            return p;
+        };
+        BatchFrameInfo* info = (BatchFrameInfo*)take(sizeof(BatchFrameInfo) * nf);
+        BatchMotion* mot = (BatchMotion*)take(sizeof(BatchMotion) * nf);
+        int* cell_count = (int*)take(sizeof(int) * (size_t)nf * ncell);
+        int* cursor = (int*)take(sizeof(int) * (size_t)nf * ncell);
+        int* cell_start = (int*)take(sizeof(int) * (size_t)nf * (ncell + 1));
+        int* key_cell = (int*)take(sizeof(int) * (size_t)nf * cap);
+        int* cell_keys = (int*)take(sizeof(int) * (size_t)nf * cap);
+        int* d_off = (int*)take(sizeof(int) * (nf + 1));
+        int* slot_count = (int*)take(sizeof(int) * std::max(1, total_mp));
+        int* status = (int*)take(sizeof(int) * 4);
+        int* frame_cands = (int*)take(sizeof(int) * nf);
+        uint32_t* slots = (uint32_t*)take(sizeof(uint32_t) * (size_t)std::max(1, total_mp) * P.slot_cap);
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(info, hi.data(), sizeof(BatchFrameInfo) * nf, cudaMemcpyHostToDevice, st));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(mot, hm.data(), sizeof(BatchMotion) * nf, cudaMemcpyHostToDevice, st));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_off, last_offsets, sizeof(int) * (nf + 1), cudaMemcpyHostToDevice, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(cell_count, 0, sizeof(int) * (size_t)nf * ncell, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * 4, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(frame_cands, 0, sizeof(int) * nf, st));
+        dim3 gk((cap + 255) / 256, nf);
+        k_bgrid_count<<<gk, 256, 0, st>>>(kps, counts, cap, info, key_cell, cell_count);
+        k_bgrid_scan<<<nf, 1024, 0, st>>>(cell_count, cell_start, cursor);
+        k_bgrid_fill<<<gk, 256, 0, st>>>(counts, cap, key_cell, cursor, cell_keys);
+        const int wpb = 8;
+        if (max_mp > 0) {
+            dim3 gc((max_mp + wpb - 1) / wpb, nf);
+            k_bpf_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, mot, last_kps,
+                                                      last_mps, last_desc, d_off, th, P.slot_cap, slots, slot_count,
+                                                      status, frame_cands);
+        }
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_cands, frame_cands, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (P.h_pinned[0] > P.slot_cap) {  // a window held more candidates than the slots: widen and redo
+            P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
+            continue;
+        }
+        int t_max = 0;
+        for (int f = 0; f < nf; f++) t_max = std::max(t_max, P.h_cands[f]);
+        const size_t fixed = sizeof(int) * ((size_t)2 * max_mp + 1 + 2 * (size_t)cap) + 2 * (size_t)max_mp + 64;
+        size_t smem = fixed + sizeof(uint32_t) * (size_t)t_max;
+        int t_cap = std::max(1, t_max);
+        if (smem > 200 * 1024) {  // keys stay in global memory
+            smem = fixed;
+            t_cap = 0;
+        }
+        if (smem > 200 * 1024) {
+            orbgpu_set_last_error("batched frame search: a frame's map points exceed shared memory", __FILE__, __LINE__);
+            return ORBGPU_ERR_CAPACITY;
+        }
+        ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bpf_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_bpf_resolve<<<nf, 1024, smem, st>>>(kps, cap, counts, last_kps, last_mps, d_off, P.slot_cap, slots, slot_count,
+                                               check_ori, t_cap, match_out, nmatches, status);
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned + 2, status + 1, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        P.last_launches = 5;
+        if (P.h_pinned[3] != 0) {
+            orbgpu_set_last_error("batched frame search: resolution failed", __FILE__, __LINE__);
+            return ORBGPU_ERR_CUDA;
+        }
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
+}

@@ -60,6 +60,10 @@ std::string default_sincos_table_path();
 // from the rounded sincos_taylor value, and writes it to 'path'.
 int build_sincos_table(const char* path, int threads);
 
+// The reference's bForward / bBackward decision of SearchByProjection(Frame&,
+// const Frame&) (src/ORBmatcher.cc:1724-1741): 1 forward, 2 backward, 0 neither.
+int motion_level_mode(const orbgpu_frame_motion& mo, int mono);
+
 // SM count of the current device, cached per device ordinal.
 inline int nsm_of_current_device() {
     static int cache[64] = {};

@@ -1187,7 +1187,7 @@ extern "C" int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame
 // The reference's bForward / bBackward decision (src/ORBmatcher.cc:1724-1741):
 // twc = -Rcw' tcw and tlc = Rlw twc + tlw with cv::Mat rounding (products
 // accumulated in double, stored as float, then a float addition).
-static int motion_level_mode(const orbgpu_frame_motion& mo, int mono) {
+int orbgpu::motion_level_mode(const orbgpu_frame_motion& mo, int mono) {
     const float* T = mo.Tcw;
     const float tcw[3] = {T[3], T[7], T[11]};
     float twc[3];

@@ -268,3 +268,74 @@ def chain_case(k: int = 30, seed: int = 0, observed_every: int = 1):
     case = dict(last_kps=last_kps, last_mps=mps, last_mp_desc=np.tile(D, (k, 1)), Tcw=T, Tlw=T, fx=fx, fy=fy, cx=cx,
                 cy=cy, bf=0.0, b=0.0, uright=None, claimed=np.zeros(k, np.uint8))
     return kps, desc, case, w, h
+
+
+def _plane_points(u, v, Tcw, K, depth):
+    """World points of the plane Z = depth seen at pixels (u, v) from pose
+    Tcw (3 x 4): ray from the camera centre through the pixel."""
+    fx, fy, cx, cy = K
+    R, t = Tcw[:, :3].astype(np.float64), Tcw[:, 3].astype(np.float64)
+    C = -R.T @ t
+    d = np.stack([(u - cx) / fx, (v - cy) / fy, np.ones_like(u)], -1) @ R  # rows: R^T d_c
+    lam = (depth - C[2]) / d[..., 2]
+    return C + lam[..., None] * d
+
+
+def camera_stream(w: int, h: int, seed: int, nframes: int, depth: float = 8.0, noise_sigma: float = 2.0):
+    """A camera moving in front of a textured plane Z = depth (world frame).
+
+    Frame k is the plane seen from pose Tcw_k, rendered by casting each
+    pixel's ray onto the plane and sampling the texture bilinearly, plus
+    N(0, noise_sigma).  The poses follow a smooth random walk (rotations of a
+    few tenths of a degree and translations of about 1 % of the depth per
+    frame).  Returns (frames, poses (3 x 4 float32 each), K = (fx, fy, cx,
+    cy), depth)."""
+    rng = np.random.default_rng(seed)
+    fx = fy = 0.9 * w
+    cx, cy = w / 2.0, h / 2.0
+    K = (fx, fy, cx, cy)
+    tw, th_ = int(w * 1.6), int(h * 1.6)
+    tex = scene(tw, th_, seed).astype(np.float64)
+    s = depth / fx  # world units per texel: the first view maps texels about 1:1 to pixels
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    R = np.eye(3)
+    t = np.zeros(3)
+    w_rot = np.zeros(3)
+    v_tr = np.zeros(3)
+    frames, poses = [], []
+    for _ in range(nframes):
+        Tcw = np.hstack([R, t[:, None]])
+        P = _plane_points(xx, yy, Tcw, K, depth)
+        a = P[..., 0] / s + tw / 2.0
+        b = P[..., 1] / s + th_ / 2.0
+        img = _bilinear(tex, a, b) + rng.normal(0.0, noise_sigma, size=(h, w))
+        frames.append(np.clip(np.rint(img), 0, 255).astype(np.uint8))
+        poses.append(Tcw.astype(np.float32))
+        w_rot = 0.8 * w_rot + rng.normal(0, 0.0015, 3)
+        v_tr = 0.8 * v_tr + rng.normal(0, 0.004 * depth, 3)
+        R = _rot(*w_rot) @ R
+        t = t + v_tr
+    return frames, poses, K, depth
+
+
+def plane_mappoints(kps, Tcw, K, depth):
+    """orbgpu_frame_mappoint records (present and observed) of keypoints seen
+    from pose Tcw on the plane Z = depth (level-0 coordinates)."""
+    P = _plane_points(np.asarray(kps["x"], np.float64), np.asarray(kps["y"], np.float64), np.asarray(Tcw), K, depth)
+    out = np.zeros(len(kps), FRAME_MAPPOINT_DTYPE)
+    out["x"], out["y"], out["z"] = P[:, 0], P[:, 1], P[:, 2]
+    out["flags"] = MP_PRESENT | MP_OBSERVED
+    return out
+
+
+def predict_pose(T_last, T_lastlast):
+    """Constant-velocity prediction mVelocity * LastFrame.mTcw with
+    mVelocity = Tcw_last * Twc_lastlast (src/Tracking.cc, TrackWithMotionModel)."""
+    def h(T):
+        M = np.eye(4)
+        M[:3, :4] = T
+        return M
+    if T_lastlast is None:
+        return np.asarray(T_last, np.float32)
+    V = h(T_last) @ np.linalg.inv(h(T_lastlast))
+    return (V @ h(T_last))[:3, :4].astype(np.float32)

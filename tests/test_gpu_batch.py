@@ -101,3 +101,44 @@ def test_batch_projection_vs_oracle(torch, oracle):
             assert nm[f] == refs[f][0], f"mode {mode} frame {f}"
             assert np.array_equal(match[f, :n], refs[f][1]), f"mode {mode} frame {f}"
             assert (match[f, n:] == -3).all()
+
+
+@pytest.mark.parametrize("dz,mono,ori", [(0.0, True, True), (2.0, False, True), (-2.0, False, False)])
+def test_batch_frame_projection_vs_oracle(torch, oracle, dz, mono, ori):
+    """SearchByProjection(CurrentFrame, LastFrame) for every frame of a batch,
+    each against its own LastFrame and pose, equals the oracle frame by frame."""
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchFrameProjection, motion_struct
+    b = BatchExtractor(8, 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    fr = frames(11, 5)
+    k, d, c = b.extract([torch.from_numpy(img).cuda() for img, _ in fr], [nf for _, nf in fr])
+    kh = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    dh = d.cpu().numpy().reshape(len(fr), cap, 32)
+    ch = c.cpu().numpy()
+    cases, motions, refs = [], [], []
+    for f, (img, _) in enumerate(fr):
+        n = int(ch[f])
+        h, w = img.shape
+        cs = syn.motion_case(kh[f, :n], dh[f, :n], w, h, seed=40 + f, dz=dz, claimed_p=0.0)
+        cases.append(cs)
+        motions.append(motion_struct(cs["Tcw"], cs["Tlw"], cs["fx"], cs["fy"], cs["cx"], cs["cy"], cs["bf"], cs["b"]))
+        mo = pyoracle.make_motion(cs["Tcw"], cs["Tlw"], cs["fx"], cs["fy"], cs["cx"], cs["cy"], cs["bf"], cs["b"])
+        refs.append(oracle.search_by_projection_frame(kh[f, :n], dh[f, :n], w, h, cs["last_kps"], cs["last_mps"],
+                                                      cs["last_mp_desc"], mo, th=7.0 if mono else 15.0, mono=mono,
+                                                      check_ori=ori))
+    lk = np.concatenate([cs["last_kps"] for cs in cases])
+    lm = np.concatenate([cs["last_mps"] for cs in cases])
+    ld = np.concatenate([cs["last_mp_desc"] for cs in cases])
+    p = BatchFrameProjection(b, check_ori=ori)
+    match, nm = p.search(torch.from_numpy(lk.view(np.float32).reshape(-1, 7)).cuda(),
+                         torch.from_numpy(lm.view(np.uint8)).cuda(), torch.from_numpy(np.ascontiguousarray(ld)).cuda(),
+                         [len(cs["last_kps"]) for cs in cases], motions, 7.0 if mono else 15.0, mono)
+    match = match.cpu().numpy().reshape(len(fr), cap)
+    nm = nm.cpu().numpy()
+    for f in range(len(fr)):
+        n = int(ch[f])
+        assert nm[f] == refs[f][0], f"frame {f}"
+        assert np.array_equal(match[f, :n], refs[f][1]), f"frame {f}"
+        assert (match[f, n:] == -3).all()

@@ -15,33 +15,67 @@ def torch():
     return require_gpu()
 
 
-def test_alone_equals_mixed(torch):
+def stream(torch, s, w, h, n, seed0=100):
     from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    frames, poses, K, depth = syn.camera_stream(w, h, seed0 + s, n)
+    return [torch.from_numpy(f).cuda() for f in frames], poses, K, depth
+
+
+def test_alone_equals_mixed(torch):
     from orb_slam2_detailed_comments_gb300.serving import ServingEngine
     nfr = 4
-    frames = {s: [torch.from_numpy(f).cuda() for f in syn.stream_frames(w, h, 100 + s, nfr)]
-              for s, (w, h, _) in enumerate(STREAMS)}
+    data = {s: stream(torch, s, w, h, nfr) for s, (w, h, _) in enumerate(STREAMS)}
     mixed = ServingEngine(max_batch=8, keep_outputs=True)
     for s, (w, h, nf) in enumerate(STREAMS):
-        assert mixed.admit(s, w, h, nf)
+        assert mixed.admit(s, w, h, nf, K=data[s][2], depth=data[s][3])
     got = {}
     for k in range(nfr):
         # a mixed batch: every stream's k-th frame, in a rotating order
         order = [(s + k) % len(STREAMS) for s in range(len(STREAMS))]
-        for r in mixed.run_batch([(s, frames[s][k], 0.0) for s in order]):
+        for r in mixed.run_batch([(s, data[s][0][k], 0.0, data[s][1][k]) for s in order]):
             got[(r.sid, k)] = r
     for s, (w, h, nf) in enumerate(STREAMS):
         alone = ServingEngine(max_batch=1, keep_outputs=True)
-        assert alone.admit(s, w, h, nf)
+        assert alone.admit(s, w, h, nf, K=data[s][2], depth=data[s][3])
         for k in range(nfr):
-            (r,) = alone.run_batch([(s, frames[s][k], 0.0)])
+            (r,) = alone.run_batch([(s, data[s][0][k], 0.0, data[s][1][k])])
             m = got[(s, k)]
             assert r.nkeypoints == m.nkeypoints and r.nmatches == m.nmatches, (s, k)
             assert r.keypoints.tobytes() == m.keypoints.tobytes()
             assert np.array_equal(r.descriptors, m.descriptors)
             assert np.array_equal(r.matches, m.matches)
             if k > 0:
-                assert r.nmatches > 0.2 * r.nkeypoints  # consecutive frames of a slow drift match
+                assert r.nmatches > 0.2 * r.nkeypoints  # neighbouring views of the plane match
+
+
+def test_frame_search_equals_oracle(torch, oracle):
+    """The engine's frame-to-frame search of one stream equals the oracle's
+    SearchByProjection(CurrentFrame, LastFrame) on the same keypoints, map
+    points (the engine's resident rows) and predicted pose."""
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import FRAME_MAPPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    from orb_slam2_detailed_comments_gb300.serving import ServingEngine
+    w, h, nf = 1280, 720, 2000
+    imgs, poses, K, depth = stream(torch, 7, w, h, 3, seed0=500)
+    e = ServingEngine(max_batch=2, keep_outputs=True)
+    assert e.admit(0, w, h, nf, K=K, depth=depth)
+    slot = e.slot_of[0]
+    prev = None
+    for k in range(3):
+        n_prev = int(e.prev_n[slot])
+        last_mps = e.state_mps[slot * e.cap: slot * e.cap + n_prev].cpu().numpy().view(FRAME_MAPPOINT_DTYPE).reshape(-1)
+        (cur,) = e.run_batch([(0, imgs[k], 0.0, poses[k])])
+        if k > 0:
+            T = syn.predict_pose(poses[k - 1], poses[k - 2] if k >= 2 else None)
+            mo = pyoracle.make_motion(T, poses[k - 1], *K, 0.0, 0.0)
+            nm, match = oracle.search_by_projection_frame(cur.keypoints, cur.descriptors, w, h, prev.keypoints,
+                                                          last_mps, prev.descriptors, mo, th=15.0, mono=True,
+                                                          check_ori=True)
+            assert nm == cur.nmatches, k
+            assert np.array_equal(match, cur.matches), k
+            assert nm > 0.3 * len(cur.keypoints)
+        prev = cur
 
 
 def test_admission_budget(torch):
@@ -58,15 +92,14 @@ def test_admission_budget(torch):
 
 
 def test_serve_loop_latency(torch):
-    from orb_slam2_detailed_comments_gb300 import synthetic as syn
-    from orb_slam2_detailed_comments_gb300.serving import ServingEngine, latency_stats, poisson_arrivals
+    from orb_slam2_detailed_comments_gb300.serving import ServingEngine, latency_stats, pingpong, poisson_arrivals
     e = ServingEngine(max_batch=16)
-    frames = {}
+    data = {}
     for s, (w, h, nf) in enumerate(STREAMS * 2):
-        assert e.admit(s, w, h, nf)
-        frames[s] = [torch.from_numpy(f).cuda() for f in syn.stream_frames(w, h, 300 + s, 3)]
-    arr = poisson_arrivals(len(frames), 30.0, 0.5, seed=1)
-    res = e.serve(arr, lambda s, k: frames[s][k % 3], 0.5)
+        data[s] = stream(torch, s, w, h, 3, seed0=300)
+        assert e.admit(s, w, h, nf, K=data[s][2], depth=data[s][3])
+    arr = poisson_arrivals(len(data), 30.0, 0.5, seed=1)
+    res = e.serve(arr, lambda s, k: (data[s][0][pingpong(k, 3)], data[s][1][pingpong(k, 3)]), 0.5)
     st = latency_stats(res)
     assert st["frames"] == len(arr)
     assert st["p99_ms"] is not None and st["p99_ms"] < 1000.0
