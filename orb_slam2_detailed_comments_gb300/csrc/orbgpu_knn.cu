@@ -100,6 +100,7 @@ extern "C" int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, cons
     if (nq == 0) return ORBGPU_OK;
     if (algo == -1)  // automatic: the tensor cores from the tuned problem size on
         algo = (long long)nq * nt >= tunables().knn_tc_min_pairs ? 1 : 0;
+    if (nt >= (1 << 23)) algo = 0;  // the tensor-core epilogue packs train indices in 23 bits
     if (algo == 1 && nt > 0) return orbgpu_knn2_tc(m, query, nq, train, nt, idx1, d1, idx2, d2);
     cudaStream_t st = orbgpu_matcher_stream_internal(m);
     int dev, nsm;

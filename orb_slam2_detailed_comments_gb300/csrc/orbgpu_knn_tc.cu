@@ -52,14 +52,24 @@ __host__ __device__ __forceinline__ uint32_t tc_offset(int r, int k) {
 }
 
 // Expands n descriptors (32 bytes) into tiled FP8 +-1 rows; rows past n are
-// +1 everywhere (their distances are discarded by the index bound).
+// +1 everywhere (their distances are discarded by the index bound).  One
+// thread per 16 bits: the 16 FP8 values of one core-matrix row, one 16-byte
+// store.
 __global__ void k_expand_fp8(const uint8_t* __restrict__ desc, int n, int tile_rows, uint8_t* __restrict__ out) {
-    const int row = blockIdx.x;  // one block per row, 256 threads = 256 bits
-    const int bit = threadIdx.x;
-    uint8_t v = 0x38;  // +1.0 in E4M3
-    if (row < n) v = ((desc[(size_t)row * 32 + (bit >> 3)] >> (bit & 7)) & 1) ? 0xB8 : 0x38;  // 1 bit -> -1.0
-    const int tile = row / tile_rows, r = row % tile_rows;
-    out[(size_t)tile * tile_rows * TC_K + tc_offset(r, bit)] = v;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = (int)(t >> 4), c = (int)(t & 15);  // bits 16c .. 16c + 15 of the row
+    const int tile = row / tile_rows, r = row - tile * tile_rows;
+    uint32_t bits = 0;
+    if (row < n) bits = (uint32_t)desc[(size_t)row * 32 + 2 * c] | ((uint32_t)desc[(size_t)row * 32 + 2 * c + 1] << 8);
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) v |= (((bits >> (4 * q + b)) & 1u) ? 0xB8u : 0x38u) << (8 * b);  // 1 bit -> -1.0
+        w[q] = v;
+    }
+    *reinterpret_cast<uint4*>(out + (size_t)tile * tile_rows * TC_K + tc_offset(r, 16 * c)) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 // ---------------------------------------------------------------- PTX wrappers
@@ -136,6 +146,19 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive 32-bit columns of this warp's 32 TMEM lanes, without the
+// wait (the caller issues tcgen05.wait::ld before reading r).
+__device__ __forceinline__ void tc_ld32_raw(uint32_t taddr, uint32_t* r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
 
 // 32 consecutive FP32 columns of this warp's 32 TMEM lanes.
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
@@ -310,9 +333,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32*(w%4).. and columns 64*(w/4)..
+        // Keys pack (distance << 23 | train index), so the lexicographic
+        // (distance, index) top-2 is three min/max operations per value.  The
+        // dot products are exact integers in [-256, 256]: adding 1.5 * 2^23
+        // puts them in the low mantissa bits, and 256 - dot = 2 * Hamming.
         const int quad = warp & 3, part = warp >> 2;
         const int row = quad * 32 + lane;
-        int b1 = 0x7fffffff, b2 = 0x7fffffff, i1 = -1, i2 = -1;
+        uint32_t k1 = 0xFFFFFFFFu, k2 = 0xFFFFFFFFu;
         for (int i = 0; i < ntile; i++) {
             const int s = i & 1;
             // warp-uniform outcome: tcgen05.ld below is a whole-warp instruction
@@ -322,29 +349,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            const int tbase = (t0 + i) * TC_N;
-#pragma unroll 1
-            for (int c = 0; c < 64; c += 32) {
-                float v[32];
-                const int col = part * 64 + c;
-                tc_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(s * TC_N + col), v);
+            const int jbase = (t0 + i) * TC_N + part * 64;
+            uint32_t r[64];
+            const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(s * TC_N + part * 64);
+            tc_ld32_raw(ta, r);
+            tc_ld32_raw(ta + 32, r + 32);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            tc_fence_before();
+            mbar_arrive(&bar_acc_free[s]);  // the accumulator is in registers: the next MMAs may overwrite it
+            const int valid = nt - jbase;    // columns of this part that are real train rows
+            // a value can enter the top 2 only if its dot product reaches the
+            // second best's (Hamming <= the second's): groups of 8 whose
+            // largest dot falls short are skipped with 8 float max/compares
+            float thr = k2 == 0xFFFFFFFFu ? -1.0e30f : (float)(256 - 2 * (int)(k2 >> 23));
 #pragma unroll
-                for (int k = 0; k < 32; k++) {
-                    const int j = tbase + col + k;
-                    const int dist = (256 - (int)v[k]) >> 1;
-                    if (j < nt) {
-                        if (dist < b1) {
-                            b2 = b1; i2 = i1; b1 = dist; i1 = j;
-                        } else if (dist < b2) {
-                            b2 = dist; i2 = j;
-                        }
+            for (int c8 = 0; c8 < 64; c8 += 8) {
+                float m = __uint_as_float(r[c8]);
+#pragma unroll
+                for (int k = 1; k < 8; k++) m = fmaxf(m, __uint_as_float(r[c8 + k]));
+                if (m >= thr) {
+#pragma unroll
+                    for (int k = c8; k < c8 + 8; k++) {
+                        const uint32_t twice =
+                            (uint32_t)(0x4B400000 + 256) - __float_as_uint(__uint_as_float(r[k]) + 12582912.0f);
+                        uint32_t key = (twice << 22) | (uint32_t)(jbase + k);
+                        key = k < valid ? key : 0xFFFFFFFFu;
+                        const uint32_t hi = max(k1, key);
+                        k1 = min(k1, key);
+                        k2 = min(k2, hi);
                     }
+                    thr = k2 == 0xFFFFFFFFu ? -1.0e30f : (float)(256 - 2 * (int)(k2 >> 23));
                 }
             }
-            tc_fence_before();
-            mbar_arrive(&bar_acc_free[s]);
         }
-        s_part[part][row] = make_int4(i1, b1, i2, b2);
+        s_part[part][row] = make_int4(k1 == 0xFFFFFFFFu ? -1 : (int)(k1 & 0x7FFFFF), (int)(k1 >> 23),
+                                      k2 == 0xFFFFFFFFu ? -1 : (int)(k2 & 0x7FFFFF), (int)(k2 >> 23));
     }
     tc_fence_before();
     __syncthreads();
@@ -395,8 +434,8 @@ extern "C" int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, f
     ORBGPU_CUDA_TRY(cudaMemcpy(dt, t256, 256 * 32, cudaMemcpyHostToDevice));
     ORBGPU_CUDA_TRY(cudaMemset(st, 0, sizeof(int)));
     ORBGPU_CUDA_TRY(cudaMemset(dd, 0, sizeof(float) * 128 * 256));
-    k_expand_fp8<<<128, 256>>>(dq, 128, TC_M, eq);
-    k_expand_fp8<<<256, 256>>>(dt, 256, TC_N, et);
+    k_expand_fp8<<<128 * 16 / 256, 256>>>(dq, 128, TC_M, eq);
+    k_expand_fp8<<<256 * 16 / 256, 256>>>(dt, 256, TC_N, et);
     const size_t smem = TC_QTILE_BYTES + TC_TTILE_BYTES;
     ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_tc_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_tc_probe<<<1, 128, smem>>>(eq, et, dd, st, (uint32_t)lbo, (uint32_t)sbo);
@@ -435,8 +474,8 @@ int orbgpu_knn2_tc(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_
     ORBGPU_CUDA_TRY(cudaMallocAsync((void**)&partial, sizeof(int4) * (size_t)nq * nslices, st));
     ORBGPU_CUDA_TRY(cudaMallocAsync((void**)&status, sizeof(int), st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
-    k_expand_fp8<<<qt * TC_M, 256, 0, st>>>(query, nq, TC_M, eq);
-    k_expand_fp8<<<tt * TC_N, 256, 0, st>>>(train, nt, TC_N, et);
+    k_expand_fp8<<<qt * TC_M * 16 / 256, 256, 0, st>>>(query, nq, TC_M, eq);
+    k_expand_fp8<<<tt * TC_N * 16 / 256, 256, 0, st>>>(train, nt, TC_N, et);
     const size_t smem = TC_QTILE_BYTES + 2 * TC_TTILE_BYTES;
     ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(qt, nslices);
