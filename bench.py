@@ -206,9 +206,16 @@ def run_ours(args):
         match, nm = proj.search(mps_dev, mpd_dev, [NMAPPOINTS] * NFRAMES, TH)
         return nm
 
-    # launch shapes chosen by the autotuner on this device for this workload (untimed)
+    # launch shapes chosen by the autotuner on this device for this workload
+    # (untimed), or pinned by --shapes (profiling runs: timings under a
+    # profiler would steer the tuner)
     from orb_slam2_detailed_comments_gb300 import autotune
-    tuning = autotune.tune_batch(batch, imgs_dev, nfs, reps=3)
+    if args.shapes:
+        vals = [int(v) for v in args.shapes.split(",")]
+        tuning = {name: {"value": v} for name, v in zip(autotune.PARAMS, vals)}
+        autotune.apply(tuning)
+    else:
+        tuning = autotune.tune_batch(batch, imgs_dev, nfs, reps=3)
 
     for _ in range(args.warmup):
         step()
@@ -357,7 +364,8 @@ def finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, p
                                "1280x720, nFeatures 1000/1500/2000, 3000 map points per frame, radius 15*scale",
                    "frames_per_step": NFRAMES, "l2": "flushed (256 MiB write) between timed steps",
                    "launch_shapes": {k: v["value"] for k, v in tuning.items()},
-                   "launch_shapes_by": "autotuner (stage events, this device and workload)"},
+                   "launch_shapes_by": "pinned (--shapes)" if args.shapes else
+                   "autotuner (stage events, this device and workload)"},
         "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "per_frame_path_fps": per_frame_fps, "per_frame_split": per_frame_split,
         "batched_over_per_frame": value / per_frame_fps if per_frame_fps else None, "other_configs": extra,
@@ -553,6 +561,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames per step (the reported workload is 64; other values are for profiling)")
+    ap.add_argument("--shapes", default="",
+                    help="pin the launch shapes resize_rows,fast_cells_per_block,describe_group (no tuning)")
     ap.add_argument("--legs", default="all",
                     help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,cpu) or 'all'")
     args = ap.parse_args()

@@ -213,6 +213,12 @@ int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* lef
 int orbgpu_knn2(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
                 int* idx2, int* d2, int algo);
 
+/* The ratio test of a k = 2 result in the reference's form
+ * (src/ORBmatcher.cc:647: bestDist < bestDist2 * nnratio, as floats):
+ * accept[i] = 1 where d1[i] < ratio * d2[i] (a query without a second
+ * neighbour is rejected).  Device arrays; returns after the stream finished. */
+int orbgpu_knn2_accept(const int* d1, const int* d2, int n, float ratio, uint8_t* accept, void* stream);
+
 /* The same k = 2 search as orbgpu_knn2 (popcount kernel), for callers that
  * cannot allocate device memory: processes whose device memory is reserved up
  * front by their own allocator (a library cudaMalloc would fail or fragment

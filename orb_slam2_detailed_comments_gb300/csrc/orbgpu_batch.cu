@@ -73,6 +73,7 @@ struct orbgpu_batch {
     uint8_t* arena = nullptr;
     size_t slot_bytes = 0;
     std::vector<const FramePlan*> slot_plan;
+    std::vector<int> slot_gen;  // tuning generation of the tables in each slot
     // current batch
     std::vector<const FramePlan*> cur;
     int nframes = 0;
@@ -148,6 +149,7 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
             return ORBGPU_ERR_CUDA;
         }
     b->slot_plan.assign(max_frames, nullptr);
+    b->slot_gen.assign(max_frames, -1);
     *out = b;
     return ORBGPU_OK;
 }
@@ -175,8 +177,15 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
 static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out) {
     for (FramePlan* p : b->plans)
         if (p->w == w && p->h == h && p->nf == nf) {
-            if (p->gen != tune_generation()) {
-                for (int l = 0; l < b->nlevels; l++) p->tiles[l] = resize_blur_tiles(p->geom[l].w, p->geom[l].h);
+            if (p->gen != tune_generation()) {  // launch shapes changed: tile counts and source blocks
+                for (int l = 0; l < b->nlevels; l++) {
+                    p->tiles[l] = resize_blur_tiles(p->geom[l].w, p->geom[l].h);
+                    if (l == 0) continue;
+                    const LevelOffsets& o = p->layout.lv[l];
+                    std::vector<uint8_t>& blob = p->table_blob[l];
+                    fill_source_blocks(p->geom[l - 1], p->geom[l], (const int*)&blob[0],
+                                       (const int*)&blob[o.yofs - o.xofs], (int2*)&blob[o.srcb - o.xofs]);
+                }
                 p->gen = tune_generation();
             }
             *out = p;
@@ -201,11 +210,13 @@ static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out
         P->tiles[l] = resize_blur_tiles(L.w, L.h);
         if (l == 0) continue;
         const LevelOffsets& o = P->layout.lv[l];
-        const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * L.h;
+        const size_t lo = o.xofs, hi = o.srcb + sizeof(int2) * srcb_entries(L);
         std::vector<uint8_t>& blob = P->table_blob[l];
         blob.assign(hi - lo, 0);
         resize_tables(P->geom[l - 1].w, P->geom[l - 1].h, L.w, L.h, (int*)&blob[o.xofs - lo], (short*)&blob[o.xalpha - lo],
                       (int*)&blob[o.yofs - lo], (short*)&blob[o.ybeta - lo]);
+        fill_source_blocks(P->geom[l - 1], L, (const int*)&blob[o.xofs - lo], (const int*)&blob[o.yofs - lo],
+                           (int2*)&blob[o.srcb - lo]);
     }
     P->gen = tune_generation();
     b->plans.push_back(P);
@@ -266,12 +277,13 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     // resize tables of slots whose configuration changed
     for (int f = 0; f < nframes; f++) {
         const FramePlan* P = b->cur[f];
-        if (b->slot_plan[f] == P) continue;
+        if (b->slot_plan[f] == P && b->slot_gen[f] == P->gen) continue;
         uint8_t* base = b->arena + (size_t)f * b->slot_bytes;
         for (int l = 1; l < nlevels; l++)
             ORBGPU_CUDA_TRY(cudaMemcpyAsync(base + P->layout.lv[l].xofs, P->table_blob[l].data(), P->table_blob[l].size(),
                                             cudaMemcpyHostToDevice, st));
         b->slot_plan[f] = P;
+        b->slot_gen[f] = P->gen;
     }
     // descriptors
     const int ndesc = nframes * nlevels;

@@ -220,6 +220,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         o.xalpha = take(sizeof(short) * 2 * L.w);
         o.yofs = take(sizeof(int) * L.h);
         o.ybeta = take(sizeof(short) * 2 * L.h);
+        o.srcb = take(sizeof(int2) * srcb_entries(L));
         o.slots = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
         o.cell_count = take(sizeof(int) * std::max(1, L.ncells));
         o.cand = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
@@ -265,6 +266,7 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.xalpha = (const short*)(arena + o.xalpha);
         d.yofs = (const int*)(arena + o.yofs);
         d.ybeta = (const short*)(arena + o.ybeta);
+        d.srcb = (const int2*)(arena + o.srcb);
         d.nCols = L.nCols;
         d.nRows = L.nRows;
         d.wCell = L.wCell;
@@ -305,13 +307,36 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
 }
 
 // Host-side resize tables of every level, written at their arena offsets.
-void fill_tables(const std::vector<LevelGeom>& g, const FrameLayout& lay, std::vector<uint8_t>& host_img, size_t base) {
-    for (size_t l = 1; l < g.size(); l++) {
-        const LevelGeom& P = g[l - 1];
-        const LevelGeom& L = g[l];
-        const LevelOffsets& o = lay.lv[l];
-        resize_tables(P.w, P.h, L.w, L.h, (int*)&host_img[o.xofs - base], (short*)&host_img[o.xalpha - base],
-                      (int*)&host_img[o.yofs - base], (short*)&host_img[o.ybeta - base]);
+static int reflect101_host(int p, int len) {
+    if (len == 1) return 0;
+    while (p < 0 || p >= len) p = p < 0 ? -p : 2 * len - 2 - p;
+    return p;
+}
+
+// Room for the tile columns and for the tile rows of the smallest tile height (8).
+int srcb_entries(const LevelGeom& L) { return (L.w + 63) / 64 + (L.h + 7) / 8; }
+
+void fill_source_blocks(const LevelGeom& P, const LevelGeom& L, const int* xofs, const int* yofs, int2* out) {
+    const int th = tunables().resize_rows;
+    const int tiles_x = (L.w + 63) / 64, tiles_y = (L.h + th - 1) / th;
+    for (int tc = 0; tc < tiles_x; tc++) {  // columns [ox - 4, ox + 68) reflected
+        int lo = 1 << 30, hi = -1;
+        for (int i = 0; i < 72; i++) {
+            const int sx = xofs[reflect101_host(64 * tc - 4 + i, L.w)];
+            lo = std::min(lo, sx);
+            hi = std::max(hi, std::min(sx + 1, P.w - 1));
+        }
+        lo &= ~3;
+        out[tc] = make_int2(lo, (hi - lo) / 4 + 1);
+    }
+    for (int tr = 0; tr < tiles_y; tr++) {  // rows [oy - 3, oy + th + 3) reflected
+        int lo = 1 << 30, hi = -1;
+        for (int i = 0; i < th + 6; i++) {
+            const int sy = yofs[reflect101_host(th * tr - 3 + i, L.h)];
+            lo = std::min(lo, std::min(std::max(sy, 0), P.h - 1));
+            hi = std::max(hi, std::min(std::max(sy + 1, 0), P.h - 1));
+        }
+        out[tiles_x + tr] = make_int2(lo, hi - lo + 1);
     }
 }
 
@@ -459,10 +484,12 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     // resize tables, level by level
     for (size_t l = 1; l < g.size(); l++) {
         const LevelOffsets& o = P->layout.lv[l];
-        const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * g[l].h;
+        const size_t lo = o.xofs, hi = o.srcb + sizeof(int2) * srcb_entries(g[l]);
         std::vector<uint8_t> host(hi - lo, 0);
         resize_tables(g[l - 1].w, g[l - 1].h, g[l].w, g[l].h, (int*)&host[o.xofs - lo], (short*)&host[o.xalpha - lo],
                       (int*)&host[o.yofs - lo], (short*)&host[o.ybeta - lo]);
+        fill_source_blocks(g[l - 1], g[l], (const int*)&host[o.xofs - lo], (const int*)&host[o.yofs - lo],
+                           (int2*)&host[o.srcb - lo]);
         if (cudaMemcpy(P->arena + lo, host.data(), hi - lo, cudaMemcpyHostToDevice) != cudaSuccess) {
             free_plan(P);
             return ORBGPU_ERR_CUDA;

@@ -209,7 +209,6 @@ __global__ void __launch_bounds__(16 * TH, 1280 / (16 * TH))
     __shared__ uint16_t s_q[RB_TH_ * RB_TW];
     __shared__ short c_sx[RB_SW], c_sx1[RB_SW], c_a0[RB_SW], c_a1[RB_SW];
     __shared__ short r_r0[RB_SH], r_r1[RB_SH], r_b0[RB_SH], r_b1[RB_SH];
-    __shared__ int s_rng[4];
     __shared__ int s_nq;
     const int tid = threadIdx.x;
     if (tid == 0) s_nq = 0;
@@ -228,34 +227,28 @@ __global__ void __launch_bounds__(16 * TH, 1280 / (16 * TH))
         }
         __syncthreads();
     } else {
-        if (tid < 4) s_rng[tid] = (tid & 1) ? -1 : 0x7fffffff;
-        __syncthreads();
-        if (tid < RB_SW) {
-            const int x = reflect101(ox - 4 + tid, d.w);
-            const int sx = d.xofs[x];
-            const int sx1 = min(sx + 1, d.sw - 1);
-            c_sx[tid] = (short)sx;
-            c_sx1[tid] = (short)sx1;
-            c_a0[tid] = d.xalpha[2 * x];
-            c_a1[tid] = d.xalpha[2 * x + 1];
-            atomicMin(&s_rng[0], sx);
-            atomicMax(&s_rng[1], sx1);
-        } else if (tid >= RB_SW && tid < RB_SW + RB_SH) {
-            const int ty = tid - RB_SW;
-            const int y = reflect101(oy - 3 + ty, d.h);
-            const int sy = d.yofs[y];
-            const int r0 = min(max(sy, 0), d.sh - 1), r1 = min(max(sy + 1, 0), d.sh - 1);
-            r_r0[ty] = (short)r0;
-            r_r1[ty] = (short)r1;
-            r_b0[ty] = d.ybeta[2 * y];
-            r_b1[ty] = d.ybeta[2 * y + 1];
-            atomicMin(&s_rng[2], r0);
-            atomicMax(&s_rng[3], r1);
-        }
-        __syncthreads();
-        const int cx0 = s_rng[0] & ~3, ry0 = s_rng[2];
-        const int nwc = (s_rng[1] - cx0) / 4 + 1, nr = s_rng[3] - ry0 + 1;
+        // the source block the tile's taps touch (precomputed per tile
+        // column and row); it and the tap tables load in one phase
+        const int2 bx = d.srcb[ox / RB_TW];
+        const int2 by = d.srcb[tiles_x + oy / RB_TH_];
+        const int cx0 = bx.x, nwc = bx.y, ry0 = by.x, nr = by.y;
         if (nwc * 4 <= RB_SRC_W && nr <= RB_SRC_H) {
+            if (tid < RB_SW) {
+                const int x = reflect101(ox - 4 + tid, d.w);
+                const int sx = d.xofs[x];
+                c_sx[tid] = (short)sx;
+                c_sx1[tid] = (short)min(sx + 1, d.sw - 1);
+                c_a0[tid] = d.xalpha[2 * x];
+                c_a1[tid] = d.xalpha[2 * x + 1];
+            } else if (tid >= RB_SW && tid < RB_SW + RB_SH) {
+                const int ty = tid - RB_SW;
+                const int y = reflect101(oy - 3 + ty, d.h);
+                const int sy = d.yofs[y];
+                r_r0[ty] = (short)min(max(sy, 0), d.sh - 1);
+                r_r1[ty] = (short)min(max(sy + 1, 0), d.sh - 1);
+                r_b0[ty] = d.ybeta[2 * y];
+                r_b1[ty] = d.ybeta[2 * y + 1];
+            }
             // the words end at the multiple of 4 above the last tap column, inside the row's pitch
             for (int i = tid; i < nr * nwc; i += blockDim.x) {
                 const int r = i / nwc, wc = i - r * nwc;

@@ -34,6 +34,9 @@ struct LevelDesc {
     const short* xalpha;  // 2 weights per output column
     const int* yofs;      // source row per output row (unclamped)
     const short* ybeta;   // 2 weights per output row
+    // source block of every resize tile: (first column rounded down to 4,
+    // words per row) per tile column, then (first row, rows) per tile row
+    const int2* srcb;
     // FAST cells
     int nCols, nRows, wCell, hCell;
     int maxBorderX, maxBorderY;

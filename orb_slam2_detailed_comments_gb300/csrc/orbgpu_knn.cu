@@ -80,9 +80,28 @@ __global__ void k_knn_merge(const int4* __restrict__ partial, int nq, int nslice
     d2[qi] = b2;
 }
 
+// Lowe's ratio test in the reference's form (src/ORBmatcher.cc:647:
+// bestDist < (float)bestDist2 * nnratio); no second neighbour rejects.
+__global__ void k_knn_accept(const int* d1, const int* d2, int n, float ratio, uint8_t* accept) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = d1[i], s = d2[i];
+    accept[i] = (s != 0x7fffffff && (float)b < __fmul_rn((float)s, ratio)) ? 1 : 0;
+}
+
 }  // namespace orbgpu
 
 using namespace orbgpu;
+
+extern "C" int orbgpu_knn2_accept(const int* d1, const int* d2, int n, float ratio, uint8_t* accept, void* stream) {
+    if (n < 0 || (n > 0 && (!d1 || !d2 || !accept))) return ORBGPU_ERR_BAD_ARG;
+    if (n == 0) return ORBGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_knn_accept<<<(n + 255) / 256, 256, 0, st>>>(d1, d2, n, ratio, accept);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    return ORBGPU_OK;
+}
 
 void knn_merge_launch(const int4* partial, int nq, int nslices, int* idx1, int* d1, int* idx2, int* d2,
                       cudaStream_t st) {

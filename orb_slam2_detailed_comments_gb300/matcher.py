@@ -184,18 +184,27 @@ class ORBmatcher:
               "orbgpu_search_by_projection")
         return nm.value, out[:s.n]
 
-    def knn2(self, query, train, algo: int = 0):
-        """Brute-force k=2 over DescriptorDistance (device tensors) -> (idx1, d1, idx2, d2).
+    def knn2(self, query, train, algo: int = 0, ratio: float | None = None):
+        """Brute-force k=2 over DescriptorDistance (device tensors) -> (idx1, d1, idx2, d2),
+        plus the ratio test's accept mask (uint8) when 'ratio' is given.
 
-        algo 0: popcount kernel; algo 1: tensor cores (+-1 FP8 dot products).
-        Both give the same (distance, lower index first) results."""
+        algo 0: popcount kernel; 1: tensor cores (+-1 FP8 dot products); -1:
+        automatic (tuned crossover).  All give the same (distance, lower index
+        first) results."""
         import torch
         nq = int(query.shape[0])
         outs = [torch.empty(max(nq, 1), dtype=torch.int32, device=query.device) for _ in range(4)]
         check(lib().orbgpu_knn2(self._h, ptr(query), nq, ptr(train), int(train.shape[0]), *[ptr(o) for o in outs],
                                 int(algo)),
               "orbgpu_knn2")
-        return tuple(o[:nq] for o in outs)
+        res = tuple(o[:nq] for o in outs)
+        if ratio is None:
+            return res
+        accept = torch.empty(max(nq, 1), dtype=torch.uint8, device=query.device)
+        check(lib().orbgpu_knn2_accept(ptr(outs[1]), ptr(outs[3]), nq, C.c_float(ratio), ptr(accept),
+                                       C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+              "orbgpu_knn2_accept")
+        return res + (accept[:nq],)
 
     @staticmethod
     def DescriptorDistance(a, b):

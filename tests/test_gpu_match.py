@@ -320,3 +320,18 @@ def test_projection_frame_edges(torch, oracle):
     CF, LF = frame_pair_views(kps[:0], desc[:0], w, h, dict(c, claimed=c["claimed"][:0]))
     nm, match = m.SearchByProjection(CF, LF, 7.0, True)
     assert nm == 0 and len(match) == 0
+
+
+def test_knn_ratio_accept(torch, oracle):
+    """The accept mask is the reference's float test bestDist < bestDist2 * ratio."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    q = syn.clustered_descriptors(3000, 50, 0.1, 12)
+    t = syn.clustered_descriptors(20000, 50, 0.1, 12)
+    i1, d1, i2, d2 = oracle.knn2(q, t)
+    out = ORBmatcher().knn2(torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda(), algo=-1, ratio=0.8)
+    for a, b in zip(out[:4], (i1, d1, i2, d2)):
+        assert np.array_equal(a.cpu().numpy(), b)
+    want = (d1.astype(np.float32) < d2.astype(np.float32) * np.float32(0.8)).astype(np.uint8)
+    assert np.array_equal(out[4].cpu().numpy(), want)
+    assert 0 < want.sum() < len(want)
