@@ -1,6 +1,6 @@
 """Autotuner of the launch shapes.
 
-Chooses, on the device at hand, the tile rows of the resize / blur / FAST
+Chooses, on the device at hand, the strip rows of the resize / blur / FAST
 strength kernel, the FAST cells per block, the keypoints per warp of the
 descriptor kernel (each timed on the pipeline stage it shapes, from the
 stage events of a batch extraction) and the problem size from which the kNN
@@ -28,7 +28,7 @@ from ._lib import check, lib
 
 # parameter -> (candidate values, pipeline stage it shapes)
 PARAMS = {
-    "resize_rows": ((8, 16, 32), "resize_blur"),
+    "resize_rows": ((8, 22, 36, 64), "resize_blur"),
     "fast_cells_per_block": ((1, 2, 4, 8), "fast"),
     "describe_group": ((4, 8, 16, 32), "describe"),
 }

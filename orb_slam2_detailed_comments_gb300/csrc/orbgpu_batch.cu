@@ -177,15 +177,8 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
 static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out) {
     for (FramePlan* p : b->plans)
         if (p->w == w && p->h == h && p->nf == nf) {
-            if (p->gen != tune_generation()) {  // launch shapes changed: tile counts and source blocks
-                for (int l = 0; l < b->nlevels; l++) {
-                    p->tiles[l] = resize_blur_tiles(p->geom[l].w, p->geom[l].h);
-                    if (l == 0) continue;
-                    const LevelOffsets& o = p->layout.lv[l];
-                    std::vector<uint8_t>& blob = p->table_blob[l];
-                    fill_source_blocks(p->geom[l - 1], p->geom[l], (const int*)&blob[0],
-                                       (const int*)&blob[o.yofs - o.xofs], (int2*)&blob[o.srcb - o.xofs]);
-                }
+            if (p->gen != tune_generation()) {  // launch shapes changed: tile counts
+                for (int l = 0; l < b->nlevels; l++) p->tiles[l] = resize_blur_tiles(p->geom[l].w, p->geom[l].h);
                 p->gen = tune_generation();
             }
             *out = p;
@@ -210,13 +203,15 @@ static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out
         P->tiles[l] = resize_blur_tiles(L.w, L.h);
         if (l == 0) continue;
         const LevelOffsets& o = P->layout.lv[l];
-        const size_t lo = o.xofs, hi = o.srcb + sizeof(int2) * srcb_entries(L);
+        const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * L.h;
         std::vector<uint8_t>& blob = P->table_blob[l];
         blob.assign(hi - lo, 0);
-        resize_tables(P->geom[l - 1].w, P->geom[l - 1].h, L.w, L.h, (int*)&blob[o.xofs - lo], (short*)&blob[o.xalpha - lo],
-                      (int*)&blob[o.yofs - lo], (short*)&blob[o.ybeta - lo]);
-        fill_source_blocks(P->geom[l - 1], L, (const int*)&blob[o.xofs - lo], (const int*)&blob[o.yofs - lo],
-                           (int2*)&blob[o.srcb - lo]);
+        if (!resize_tables(P->geom[l - 1].w, P->geom[l - 1].h, L.w, L.h, (int*)&blob[o.xofs - lo],
+                           (short*)&blob[o.xalpha - lo], (int*)&blob[o.yofs - lo], (short*)&blob[o.ybeta - lo])) {
+            delete P;
+            orbgpu_set_last_error("resize weights out of range", __FILE__, __LINE__);
+            return ORBGPU_ERR_BAD_ARG;
+        }
     }
     P->gen = tune_generation();
     b->plans.push_back(P);

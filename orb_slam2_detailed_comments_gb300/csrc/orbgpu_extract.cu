@@ -37,7 +37,7 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
     if (!name) return ORBGPU_ERR_BAD_ARG;
     orbgpu::Tunables& t = orbgpu::g_tunables;
     const std::string n(name);
-    if (n == "resize_rows" && (value == 8 || value == 16 || value == 32)) t.resize_rows = (int)value;
+    if (n == "resize_rows" && (value == 8 || value == 22 || value == 36 || value == 64)) t.resize_rows = (int)value;
     else if (n == "fast_cells_per_block" && (value == 1 || value == 2 || value == 4 || value == 8))
         t.fast_cells_per_block = (int)value;
     else if (n == "describe_group" && (value == 4 || value == 8 || value == 16 || value == 32))
@@ -129,7 +129,7 @@ static inline int floor_f(float v) {
 }
 
 // cv::resize INTER_LINEAR coefficient tables (the fixed-point path).
-void resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int* yofs, short* ybeta) {
+bool resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int* yofs, short* ybeta) {
     const double scale_x = 1. / ((double)dw / sw), scale_y = 1. / ((double)dh / sh);
     int xmax = dw;
     for (int dx = 0; dx < dw; dx++) {
@@ -158,6 +158,12 @@ void resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int
         ybeta[2 * dy] = sat_short_round((1.f - fy) * 2048);
         ybeta[2 * dy + 1] = sat_short_round(fy * 2048);
     }
+    auto fits = [](const short* wt, int n) {
+        for (int i = 0; i < n; i++)
+            if (wt[2 * i] < 0 || wt[2 * i + 1] < 0 || wt[2 * i] + wt[2 * i + 1] > 2049) return false;
+        return true;
+    };
+    return fits(xalpha, dw) && fits(ybeta, dh);
 }
 
 // Level geometry of one image (src/ORBextractor.cc:1037-1063, 1661-1663).
@@ -220,7 +226,6 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         o.xalpha = take(sizeof(short) * 2 * L.w);
         o.yofs = take(sizeof(int) * L.h);
         o.ybeta = take(sizeof(short) * 2 * L.h);
-        o.srcb = take(sizeof(int2) * srcb_entries(L));
         o.slots = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
         o.cell_count = take(sizeof(int) * std::max(1, L.ncells));
         o.cand = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
@@ -266,7 +271,6 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.xalpha = (const short*)(arena + o.xalpha);
         d.yofs = (const int*)(arena + o.yofs);
         d.ybeta = (const short*)(arena + o.ybeta);
-        d.srcb = (const int2*)(arena + o.srcb);
         d.nCols = L.nCols;
         d.nRows = L.nRows;
         d.wCell = L.wCell;
@@ -303,40 +307,6 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.out_base = out_base;
         d.out_cap = out_cap;
         d.frame_total = (int*)(arena + lay.frame_total);
-    }
-}
-
-// Host-side resize tables of every level, written at their arena offsets.
-static int reflect101_host(int p, int len) {
-    if (len == 1) return 0;
-    while (p < 0 || p >= len) p = p < 0 ? -p : 2 * len - 2 - p;
-    return p;
-}
-
-// Room for the tile columns and for the tile rows of the smallest tile height (8).
-int srcb_entries(const LevelGeom& L) { return (L.w + 63) / 64 + (L.h + 7) / 8; }
-
-void fill_source_blocks(const LevelGeom& P, const LevelGeom& L, const int* xofs, const int* yofs, int2* out) {
-    const int th = tunables().resize_rows;
-    const int tiles_x = (L.w + 63) / 64, tiles_y = (L.h + th - 1) / th;
-    for (int tc = 0; tc < tiles_x; tc++) {  // columns [ox - 4, ox + 68) reflected
-        int lo = 1 << 30, hi = -1;
-        for (int i = 0; i < 72; i++) {
-            const int sx = xofs[reflect101_host(64 * tc - 4 + i, L.w)];
-            lo = std::min(lo, sx);
-            hi = std::max(hi, std::min(sx + 1, P.w - 1));
-        }
-        lo &= ~3;
-        out[tc] = make_int2(lo, (hi - lo) / 4 + 1);
-    }
-    for (int tr = 0; tr < tiles_y; tr++) {  // rows [oy - 3, oy + th + 3) reflected
-        int lo = 1 << 30, hi = -1;
-        for (int i = 0; i < th + 6; i++) {
-            const int sy = yofs[reflect101_host(th * tr - 3 + i, L.h)];
-            lo = std::min(lo, std::min(std::max(sy, 0), P.h - 1));
-            hi = std::max(hi, std::min(std::max(sy + 1, 0), P.h - 1));
-        }
-        out[tiles_x + tr] = make_int2(lo, hi - lo + 1);
     }
 }
 
@@ -484,12 +454,14 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     // resize tables, level by level
     for (size_t l = 1; l < g.size(); l++) {
         const LevelOffsets& o = P->layout.lv[l];
-        const size_t lo = o.xofs, hi = o.srcb + sizeof(int2) * srcb_entries(g[l]);
+        const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * g[l].h;
         std::vector<uint8_t> host(hi - lo, 0);
-        resize_tables(g[l - 1].w, g[l - 1].h, g[l].w, g[l].h, (int*)&host[o.xofs - lo], (short*)&host[o.xalpha - lo],
-                      (int*)&host[o.yofs - lo], (short*)&host[o.ybeta - lo]);
-        fill_source_blocks(g[l - 1], g[l], (const int*)&host[o.xofs - lo], (const int*)&host[o.yofs - lo],
-                           (int2*)&host[o.srcb - lo]);
+        if (!resize_tables(g[l - 1].w, g[l - 1].h, g[l].w, g[l].h, (int*)&host[o.xofs - lo],
+                           (short*)&host[o.xalpha - lo], (int*)&host[o.yofs - lo], (short*)&host[o.ybeta - lo])) {
+            free_plan(P);
+            orbgpu_set_last_error("resize weights out of range", __FILE__, __LINE__);
+            return ORBGPU_ERR_BAD_ARG;
+        }
         if (cudaMemcpy(P->arena + lo, host.data(), hi - lo, cudaMemcpyHostToDevice) != cudaSuccess) {
             free_plan(P);
             return ORBGPU_ERR_CUDA;

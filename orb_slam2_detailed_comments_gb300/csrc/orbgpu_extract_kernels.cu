@@ -33,27 +33,7 @@ __device__ __forceinline__ int reflect101(int p, int len) {
     return p;
 }
 
-// ---------------------------------------------------------------- pyramid
-#define RB_TW 64
-#define RB_HALO 3
-
-__device__ __forceinline__ int resize_pixel(const LevelDesc& d, int x, int y) {
-    const int sx = d.xofs[x];
-    const int sx1 = min(sx + 1, d.sw - 1);
-    const int a0 = d.xalpha[2 * x], a1 = d.xalpha[2 * x + 1];
-    const int sy = d.yofs[y];
-    const int r0 = min(max(sy, 0), d.sh - 1), r1 = min(max(sy + 1, 0), d.sh - 1);
-    const int b0 = d.ybeta[2 * y], b1 = d.ybeta[2 * y + 1];
-    const uint8_t* S0 = d.src + (size_t)r0 * d.spitch;
-    const uint8_t* S1 = d.src + (size_t)r1 * d.spitch;
-    const int h0 = S0[sx] * a0 + S0[sx1] * a1;
-    const int h1 = S1[sx] * a0 + S1[sx1] * a1;
-    const int v = (h0 * b0 + h1 * b1 + (1 << 21)) >> 22;
-    return v < 0 ? 0 : (v > 255 ? 255 : v);
-}
-
-// Level l (l >= 1) by resizing level l-1, then the blur of level l; at
-// level 0 only the blur.  One 64x16 tile per block.
+// Entry and index of block b within a launch over a RangeMap.
 __device__ __forceinline__ void map_item(const RangeMap& rm, int b, int& desc, int& index) {
     int lo = 0, hi = rm.n - 1;
     while (lo < hi) {
@@ -167,219 +147,317 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 }
 
 // ---------------------------------------------------------------- resize + blur + FAST strength
-// One 64 x 16 tile of level l per block of 256 threads.  Shared memory holds
-// the level pixels of the tile with a 3-pixel ring (REFLECT_101 outside the
-// level) in rows of 72 bytes covering columns [ox - 4, ox + 68), so every
-// 4-pixel group of the core is one aligned 32-bit word:
-//  * fill: level 0 copies the image (aligned words for interior tiles);
-//    levels >= 1 stage the source block of level l-1 that the tile's
-//    bilinear taps touch, with per-column and per-row tap tables, and
-//    resize from shared memory (the fixed-point INTER_LINEAR formula);
-//  * the core is written to the level plane, blurred with the 7x7
-//    fixed-point Gaussian (horizontal pass 4 outputs per thread from three
-//    words, vertical pass 4 outputs per thread from seven int4 rows) into
-//    the blurred plane, and scored with the FAST arc strength at the lower
-//    threshold into the strength plane: a byte-SIMD compass-point test of 4
-//    pixels per thread queues the candidates, the full segment test scores
-//    them.  The ring is exactly the radius-3 circle, so every pixel whose
-//    circle lies inside the level is scored (others get 0 and are never
-//    read by the cell stage).
-#define RB_SW 72                       // shared row: columns [ox - 4, ox + 68)
-#define RB_SRC_W 96                    // staged source columns (72 taps x 1.25 + 2, word aligned)
+// One warp per strip of 120 columns x TH rows of level l.  Lane k holds the
+// four pixels of columns [x0 - 4 + 4k, x0 + 4k) of a row as one 32-bit word:
+// lanes 1..30 own the strip's columns, lanes 0 and 31 the 4-column halos
+// (REFLECT_101 outside the level).  The warp walks the TH + 6 rows
+// [y0 - 3, y0 + TH + 3) top to bottom with the last seven rows in registers:
+//  * the row's pixels: level 0 loads them; levels >= 1 resize from level l-1
+//    (cv::resize INTER_LINEAR, 11-bit fixed point): a source row is
+//    interpolated horizontally once for the (on average 1.2) output rows that
+//    use it, one dp2a per pixel on the two source bytes a prmt picks from the
+//    lane's source words, which are loaded one row ahead;
+//  * the 7x7 Gaussian (8-bit fixed point): horizontal sums by two dp4a per
+//    pixel from the lane's word and its neighbours' (shuffles), the vertical
+//    pass over seven rows of sums held in registers;
+//  * FAST at the lower threshold t: the compass-point pre-test (two circle
+//    points among 0, 4, 8, 12 that are adjacent on the circle both brighter
+//    than v + t or both darker than v - t; every nine-pixel arc contains such
+//    a pair) in 16-bit lanes gives a candidate bitmap; after every seven rows
+//    the warp compacts the candidates and scores them from a 16-row ring of
+//    level rows in shared memory.
+// The warps of a block share nothing: no block-level synchronisation.
+#define RS_COLS 120       // level columns per strip (lanes 1..30)
+#define RS_WPB 2          // strips (warps) per block
+#define RS_CAND (30 * 28) // candidates of one 7-row block at most
 
-__device__ __forceinline__ int byte_of(uint32_t w, int j) { return (int)((w >> (8 * j)) & 0xFFu); }
-
-// TH (tile rows, 8 / 16 / 32) is chosen by the autotuner; the block has
-// 16 * TH threads (one 4-pixel group of the core each).
 template <int TH>
-__global__ void __launch_bounds__(16 * TH, 1280 / (16 * TH))
-    k_level_resize_blur(const LevelDesc* descs, RangeMap rm, int level0) {
-    constexpr int RB_TH_ = TH;
-    constexpr int RB_SH = TH + 2 * RB_HALO;          // rows [oy - 3, oy + TH + 3)
-    constexpr int RB_SRC_H = (RB_SH * 5) / 4 + 4;    // staged source rows (RB_SH taps x 1.25 + 2)
+struct StripShared {
+    uint32_t ring[16][32];  // level rows: input row i at i & 15
+    int4 rows[TH + 7];      // input row i: reflected level row, source rows r0, r1, 4 b0 | 4 b1 << 16
+    uint16_t cand[RS_CAND]; // (row within the 7-row block) << 7 | byte column of the ring
+};
+
+// Even (bytes 0, 2) and odd (bytes 1, 3) pixels of a word in 16-bit lanes.
+__device__ __forceinline__ uint32_t rs_even(uint32_t w) { return w & 0x00FF00FFu; }
+__device__ __forceinline__ uint32_t rs_odd(uint32_t w) { return __byte_perm(w, 0u, 0x4341); }
+
+// Compass pre-test of the two pixels in the 16-bit lanes of c (centres) and
+// p0, p4, p8, p12 (circle points), K = (0x8000 - t - 1) in both lanes: every
+// lane sum stays within [0x7E01, 0x80FE], so no borrow crosses lanes and bit
+// 15 of a lane is set exactly when p - c > t (or c - p > t).  Returns bit 15 /
+// bit 31 set for candidates.
+__device__ __forceinline__ uint32_t rs_compass(uint32_t c, uint32_t p0, uint32_t p4, uint32_t p8, uint32_t p12,
+                                               uint32_t K) {
+    const uint32_t b0 = p0 + K - c, b4 = p4 + K - c, b8 = p8 + K - c, b12 = p12 + K - c;
+    const uint32_t d0 = c + K - p0, d4 = c + K - p4, d8 = c + K - p8, d12 = c + K - p12;
+    // adjacent pairs (0,4) (4,8) (8,12) (12,0) == (0 | 8) & (4 | 12)
+    return (((b0 | b8) & (b4 | b12)) | ((d0 | d8) & (d4 | d12))) & 0x80008000u;
+}
+
+// Largest arc threshold of the pixel at byte column 'col' of input row 'ic'
+// of the ring: max over the sixteen nine-pixel arcs of the arc's smallest
+// difference, for the darker-centre (v - p) and brighter-centre (p - v)
+// differences clipped at 0, which travel together in the 16-bit halves of one
+// word.  Above t exactly when the pixel is a FAST corner at threshold t.
+__device__ __forceinline__ int rs_arc_strength(const uint8_t* ring, int ic, int col) {
+    const uint8_t* R[7];
+#pragma unroll
+    for (int dy = -3; dy <= 3; dy++) R[dy + 3] = ring + (((ic + dy) & 15) << 7) + col;
+    const uint32_t v = R[3][0];
+    const uint32_t p[16] = {R[6][0], R[6][1], R[5][2],  R[4][3],  R[3][3],  R[2][3],  R[1][2],  R[0][1],
+                            R[0][0], R[0][-1], R[1][-2], R[2][-3], R[3][-3], R[4][-3], R[5][-2], R[6][-1]};
+    uint32_t a[16], m2[16], m4[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const uint32_t x = p[k] | (v << 16), y = v | (p[k] << 16);
+        a[k] = __vmaxu2(x, y) - x;  // (v - p)+ | (p - v)+ << 16
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) m2[k] = __vminu2(a[k], a[(k + 1) & 15]);
+#pragma unroll
+    for (int k = 0; k < 16; k++) m4[k] = __vminu2(m2[k], m2[(k + 2) & 15]);
+    uint32_t best = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) best = __vmaxu2(best, __vminu2(__vminu2(m4[k], m4[(k + 4) & 15]), a[(k + 8) & 15]));
+    return (int)max(best & 0xFFFFu, best >> 16);
+}
+
+template <int TH, bool LEVEL0>
+__global__ void __launch_bounds__(32 * RS_WPB) k_level_strip(const LevelDesc* descs, RangeMap rm) {
+    static_assert((TH + 6) % 7 == 0, "TH + 6 rows must be whole blocks of 7");
+    constexpr int NB = (TH + 6) / 7;
+    __shared__ __align__(16) StripShared<TH> sh_all[RS_WPB];
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
-    const int tiles_x = (d.w + RB_TW - 1) / RB_TW;
-    const int ox = (it.index % tiles_x) * RB_TW, oy = (it.index / tiles_x) * RB_TH_;
-    __shared__ __align__(16) uint8_t tile[RB_SH][RB_SW];
-    __shared__ __align__(16) int rows[RB_SH][RB_TW];
-    __shared__ __align__(16) uint8_t s_str[RB_TH_][RB_TW];
-    __shared__ __align__(16) uint8_t src_s[RB_SRC_H][RB_SRC_W];
-    __shared__ uint16_t s_q[RB_TH_ * RB_TW];
-    __shared__ short c_sx[RB_SW], c_sx1[RB_SW], c_a0[RB_SW], c_a1[RB_SW];
-    __shared__ short r_r0[RB_SH], r_r1[RB_SH], r_b0[RB_SH], r_b1[RB_SH];
-    __shared__ int s_nq;
-    const int tid = threadIdx.x;
-    if (tid == 0) s_nq = 0;
-    if (level0) {
-        if (ox >= 4 && ox + 68 <= d.w && oy >= 3 && oy + RB_TH_ + 3 <= d.h) {
-            for (int i = tid; i < RB_SH * (RB_SW / 4); i += blockDim.x) {
-                const int ty = i / (RB_SW / 4), wx = i - ty * (RB_SW / 4);
-                *reinterpret_cast<uint32_t*>(&tile[ty][4 * wx]) =
-                    *reinterpret_cast<const uint32_t*>(d.dst + (size_t)(oy - 3 + ty) * d.pitch + ox - 4 + 4 * wx);
-            }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = d.w, h = d.h, pitch = d.pitch;
+    const int tiles_x = (w + RS_COLS - 1) / RS_COLS;
+    const int tile = it.index * RS_WPB + warp;
+    if (tile >= tiles_x * ((h + TH - 1) / TH)) return;
+    StripShared<TH>& S = sh_all[warp];
+    const uint8_t* ring8 = reinterpret_cast<const uint8_t*>(&S.ring[0][0]);
+    const int x0 = (tile % tiles_x) * RS_COLS, y0 = (tile / tiles_x) * TH;
+    const int X = x0 - 4 + 4 * lane;
+    const bool writer = lane >= 1 && lane <= 30 && X < w;
+    uint32_t colmask = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (writer && X + j >= 3 && X + j < w - 3) colmask |= 1u << j;
+    const int t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
+    const uint32_t K = (0x8000u - (uint32_t)t - 1u) * 0x00010001u;
+
+    // per input row: reflected level row and (levels >= 1) source rows and weights
+    for (int i = lane; i < TH + 7; i += 32) {
+        const int rr = reflect101(y0 - 3 + min(i, TH + 5), h);
+        int4 e = make_int4(rr, 0, 0, 0);
+        if (!LEVEL0) {
+            const int sy = d.yofs[rr];
+            e.y = min(max(sy, 0), d.sh - 1);
+            e.z = min(max(sy + 1, 0), d.sh - 1);
+            e.w = (4 * (int)d.ybeta[2 * rr]) | ((4 * (int)d.ybeta[2 * rr + 1]) << 16);
+        }
+        S.rows[i] = e;
+    }
+
+    // level 0: the lane's columns (reflected at the edges)
+    int xr[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) xr[j] = reflect101(X + j, w);
+    const bool interior = X >= 0 && X + 3 < w;
+    // levels >= 1: per pixel the packed weights (a0 | a1 << 16) and the
+    // byte selector of (sx, sx1) among the 8 source bytes from bmin
+    uint32_t coef[4] = {0, 0, 0, 0}, sel[4] = {0, 0, 0, 0};
+    int sbase = 0, nwords = 0;
+    uint32_t sshift = 0;
+    bool fastcols = true;
+    if (!LEVEL0) {
+        int sxs[4], sx1s[4], bmin = 1 << 30, bmax = -1;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            sxs[j] = d.xofs[xr[j]];
+            sx1s[j] = min(sxs[j] + 1, d.sw - 1);
+            coef[j] = (uint32_t)(uint16_t)d.xalpha[2 * xr[j]] | ((uint32_t)(uint16_t)d.xalpha[2 * xr[j] + 1] << 16);
+            bmin = min(bmin, sxs[j]);
+            bmax = max(bmax, sx1s[j]);
+        }
+        fastcols = bmax - bmin <= 7;
+        sbase = bmin & ~3;
+        sshift = 8u * (uint32_t)(bmin & 3);
+        nwords = fastcols ? (bmax - sbase) / 4 + 1 : 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) sel[j] = (uint32_t)(sxs[j] - bmin) | ((uint32_t)(sx1s[j] - bmin) << 4);
+    }
+    __syncwarp();
+
+    const uint32_t TA = (uint32_t)c_gauss_taps[0] | ((uint32_t)c_gauss_taps[1] << 8) |
+                        ((uint32_t)c_gauss_taps[2] << 16) | ((uint32_t)c_gauss_taps[3] << 24);
+    const uint32_t TB = (uint32_t)c_gauss_taps[4] | ((uint32_t)c_gauss_taps[5] << 8) | ((uint32_t)c_gauss_taps[6] << 16);
+
+    // one level word of row rr (level 0)
+    auto level_word = [&](int rr) -> uint32_t {
+        const uint8_t* row = d.dst + (size_t)rr * pitch;
+        if (interior) return *reinterpret_cast<const uint32_t*>(row + X);
+        return (uint32_t)row[xr[0]] | ((uint32_t)row[xr[1]] << 8) | ((uint32_t)row[xr[2]] << 16) |
+               ((uint32_t)row[xr[3]] << 24);
+    };
+    // the lane's source words of source row s (levels >= 1)
+    auto source_words = [&](int s, uint32_t& w0, uint32_t& w1, uint32_t& w2) {
+        const uint8_t* p = d.src + (size_t)s * d.spitch + sbase;
+        w0 = nwords > 0 ? *reinterpret_cast<const uint32_t*>(p) : 0u;
+        w1 = nwords > 1 ? *reinterpret_cast<const uint32_t*>(p + 4) : 0u;
+        w2 = nwords > 2 ? *reinterpret_cast<const uint32_t*>(p + 8) : 0u;
+    };
+    // horizontal interpolation of source row s at the lane's 4 columns
+    auto hinterp = [&](int s, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t* hv) {
+        if (fastcols) {
+            const uint32_t W0 = __funnelshift_r(w0, w1, sshift), W1 = __funnelshift_r(w1, w2, sshift);
+#pragma unroll
+            for (int j = 0; j < 4; j++) hv[j] = __dp2a_lo(coef[j], __byte_perm(W0, W1, sel[j]), 0u);
         } else {
-            for (int i = tid; i < RB_SH * RB_SW; i += blockDim.x) {
-                const int ty = i / RB_SW, tx = i - ty * RB_SW;
-                tile[ty][tx] = d.dst[(size_t)reflect101(oy - 3 + ty, d.h) * d.pitch + reflect101(ox - 4 + tx, d.w)];
-            }
-        }
-        __syncthreads();
-    } else {
-        // the source block the tile's taps touch (precomputed per tile
-        // column and row); it and the tap tables load in one phase
-        const int2 bx = d.srcb[ox / RB_TW];
-        const int2 by = d.srcb[tiles_x + oy / RB_TH_];
-        const int cx0 = bx.x, nwc = bx.y, ry0 = by.x, nr = by.y;
-        if (nwc * 4 <= RB_SRC_W && nr <= RB_SRC_H) {
-            if (tid < RB_SW) {
-                const int x = reflect101(ox - 4 + tid, d.w);
-                const int sx = d.xofs[x];
-                c_sx[tid] = (short)sx;
-                c_sx1[tid] = (short)min(sx + 1, d.sw - 1);
-                c_a0[tid] = d.xalpha[2 * x];
-                c_a1[tid] = d.xalpha[2 * x + 1];
-            } else if (tid >= RB_SW && tid < RB_SW + RB_SH) {
-                const int ty = tid - RB_SW;
-                const int y = reflect101(oy - 3 + ty, d.h);
-                const int sy = d.yofs[y];
-                r_r0[ty] = (short)min(max(sy, 0), d.sh - 1);
-                r_r1[ty] = (short)min(max(sy + 1, 0), d.sh - 1);
-                r_b0[ty] = d.ybeta[2 * y];
-                r_b1[ty] = d.ybeta[2 * y + 1];
-            }
-            // the words end at the multiple of 4 above the last tap column, inside the row's pitch
-            for (int i = tid; i < nr * nwc; i += blockDim.x) {
-                const int r = i / nwc, wc = i - r * nwc;
-                *reinterpret_cast<uint32_t*>(&src_s[r][4 * wc]) =
-                    *reinterpret_cast<const uint32_t*>(d.src + (size_t)(ry0 + r) * d.spitch + cx0 + 4 * wc);
-            }
-            __syncthreads();
-            for (int i = tid; i < RB_SH * RB_SW; i += blockDim.x) {
-                const int ty = i / RB_SW, tx = i - ty * RB_SW;
-                const uint8_t* S0 = src_s[r_r0[ty] - ry0];
-                const uint8_t* S1 = src_s[r_r1[ty] - ry0];
-                const int sx = c_sx[tx] - cx0, sx1 = c_sx1[tx] - cx0, a0 = c_a0[tx], a1 = c_a1[tx];
-                const int h0 = S0[sx] * a0 + S0[sx1] * a1;
-                const int h1 = S1[sx] * a0 + S1[sx1] * a1;
-                const int v = (h0 * r_b0[ty] + h1 * r_b1[ty] + (1 << 21)) >> 22;
-                tile[ty][tx] = (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
-            }
-        } else {
-            // a source block larger than the staging area (not met by 1.2 scale steps)
-            for (int i = tid; i < RB_SH * RB_SW; i += blockDim.x) {
-                const int ty = i / RB_SW, tx = i - ty * RB_SW;
-                tile[ty][tx] = (uint8_t)resize_pixel(d, reflect101(ox - 4 + tx, d.w), reflect101(oy - 3 + ty, d.h));
-            }
-        }
-        __syncthreads();
-        // the core into the level plane (bytes past the level width land in the row padding)
-        {
-            const int ty = tid >> 4, g = tid & 15;
-            if (oy + ty < d.h)
-                *reinterpret_cast<uint32_t*>(d.dst + (size_t)(oy + ty) * d.pitch + ox + 4 * g) =
-                    *reinterpret_cast<const uint32_t*>(&tile[ty + RB_HALO][4 + 4 * g]);
-        }
-    }
-    int taps[7];
+            // source columns more than 7 apart (scale factors above about 1.6)
+            const uint8_t* row = d.src + (size_t)s * d.spitch;
 #pragma unroll
-    for (int k = 0; k < 7; k++) taps[k] = c_gauss_taps[k];
-    // horizontal pass: output x = ox + 4g + j reads columns 4g + 1 + j + k
-    for (int i = tid; i < RB_SH * (RB_TW / 4); i += blockDim.x) {
-        const int ty = i >> 4, g = i & 15;
-        const uint32_t* R = reinterpret_cast<const uint32_t*>(&tile[ty][0]);
-        const uint32_t w0 = R[g], w1 = R[g + 1], w2 = R[g + 2];
-        int bb[12];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            bb[j] = byte_of(w0, j);
-            bb[4 + j] = byte_of(w1, j);
-            bb[8 + j] = byte_of(w2, j);
+            for (int j = 0; j < 4; j++) {
+                const int sx = d.xofs[xr[j]], sx1 = min(sx + 1, d.sw - 1);
+                hv[j] = (uint32_t)row[sx] * (coef[j] & 0xFFFFu) + (uint32_t)row[sx1] * (coef[j] >> 16);
+            }
         }
-        int4 o;
-        int acc[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            int sacc = 0;
-#pragma unroll
-            for (int k = 0; k < 7; k++) sacc += taps[k] * bb[1 + j + k];
-            acc[j] = sacc;
-        }
-        o.x = acc[0];
-        o.y = acc[1];
-        o.z = acc[2];
-        o.w = acc[3];
-        *reinterpret_cast<int4*>(&rows[ty][4 * g]) = o;
-    }
-    // FAST, phase 1: byte-SIMD compass-point test of 4 pixels per thread
-    const int t_lo = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
-    const int lane = tid & 31;
+    };
+
+    uint32_t cw[7], lw[7], rw[7], hs[7][4];
+    uint32_t ha[4] = {0, 0, 0, 0}, hb[4] = {0, 0, 0, 0};
+    int ca = -1, cb = -1;
+    uint32_t pc = 0, pa0 = 0, pa1 = 0, pa2 = 0, pb0 = 0, pb1 = 0, pb2 = 0;
     {
-        const int ty = tid >> 4, g = tid & 15;
-        const uint32_t* R = reinterpret_cast<const uint32_t*>(&tile[ty + RB_HALO][0]);
-        const uint32_t c = R[g + 1], left = R[g], right = R[g + 2];
-        const uint32_t p0 = reinterpret_cast<const uint32_t*>(&tile[ty + 2 * RB_HALO][0])[g + 1];  // row + 3
-        const uint32_t p8 = reinterpret_cast<const uint32_t*>(&tile[ty][0])[g + 1];               // row - 3
-        const uint32_t p4 = __funnelshift_r(c, right, 24);                                        // column + 3
-        const uint32_t p12 = __funnelshift_r(left, c, 8);                                         // column - 3
-        const uint32_t t4 = (uint32_t)t_lo * 0x01010101u;
-        const uint32_t hi = __vaddus4(c, t4), lo = __vsubus4(c, t4);
-        const uint32_t b0 = __vcmpgtu4(p0, hi), b4 = __vcmpgtu4(p4, hi), b8 = __vcmpgtu4(p8, hi), b12 = __vcmpgtu4(p12, hi);
-        const uint32_t d0 = __vcmpltu4(p0, lo), d4 = __vcmpltu4(p4, lo), d8 = __vcmpltu4(p8, lo), d12 = __vcmpltu4(p12, lo);
-        const uint32_t cand = (b0 & b4) | (b4 & b8) | (b8 & b12) | (b12 & b0) | (d0 & d4) | (d4 & d8) | (d8 & d12) |
-                              (d12 & d0);
-        const int gy = oy + ty;
-        const bool row_ok = gy >= 3 && gy < d.h - 3;
-        *reinterpret_cast<uint32_t*>(&s_str[ty][4 * g]) = 0u;
+        const int4 e = S.rows[0];
+        if (LEVEL0) pc = level_word(e.x);
+        else {
+            source_words(e.y, pa0, pa1, pa2);
+            source_words(e.z, pb0, pb1, pb2);
+        }
+    }
+    for (int blk = 0; blk < NB; blk++) {
+        uint32_t bmw = 0;  // candidates of this block: bit 4u + j
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int gx = ox + 4 * g + j;
-            const bool cj = row_ok && gx >= 3 && gx < d.w - 3 && byte_of(cand, j) != 0;
-            const unsigned m = __ballot_sync(0xffffffffu, cj);
-            if (m) {
-                int base = 0;
-                if (lane == 0) base = atomicAdd(&s_nq, __popc(m));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (cj) s_q[base + __popc(m & ((1u << lane) - 1))] = (uint16_t)(ty * RB_TW + 4 * g + j);
+        for (int u = 0; u < 7; u++) {
+            const int i = 7 * blk + u;
+            const int4 e = S.rows[i];
+            const int4 e1 = S.rows[i + 1];
+            uint32_t c;
+            if (LEVEL0) {
+                c = pc;
+                pc = level_word(e1.x);
+            } else {
+                uint32_t na[4], nb[4];
+                if (e.y == ca) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) na[j] = ha[j];
+                } else if (e.y == cb) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) na[j] = hb[j];
+                } else {
+                    hinterp(e.y, pa0, pa1, pa2, na);
+                }
+                if (e.z == cb) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) nb[j] = hb[j];
+                } else if (e.z == ca) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) nb[j] = ha[j];
+                } else if (e.z == e.y) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) nb[j] = na[j];
+                } else {
+                    hinterp(e.z, pb0, pb1, pb2, nb);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    ha[j] = na[j];
+                    hb[j] = nb[j];
+                }
+                ca = e.y;
+                cb = e.z;
+                source_words(e1.y, pa0, pa1, pa2);
+                source_words(e1.z, pb0, pb1, pb2);
+                // (h0 b0 + h1 b1 + 2^21) >> 22 == byte 3 of 4 h0 b0 + 4 h1 b1 + 2^23 (below 2^32 for
+                // weights summing to at most 2049)
+                const uint32_t B0 = (uint32_t)e.w & 0xFFFFu, B1 = (uint32_t)e.w >> 16;
+                uint32_t v[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[j] = ha[j] * B0 + hb[j] * B1 + (1u << 23);
+                c = __byte_perm(__byte_perm(v[0], v[1], 0x0073), __byte_perm(v[2], v[3], 0x0073), 0x5410);
+                const int yl = y0 - 3 + i;
+                if (writer && i >= 3 && i < TH + 3 && yl < h)
+                    *reinterpret_cast<uint32_t*>(d.dst + (size_t)yl * pitch + X) = c;
+            }
+            S.ring[i & 15][lane] = c;
+            const uint32_t l = __shfl_up_sync(0xffffffffu, c, 1), r = __shfl_down_sync(0xffffffffu, c, 1);
+            cw[u] = c;
+            lw[u] = l;
+            rw[u] = r;
+            // horizontal Gaussian sums of the lane's 4 pixels: columns X + j - 3 .. X + j + 3
+            hs[u][0] = __dp4a(__funnelshift_r(l, c, 8), TA, __dp4a(__funnelshift_r(c, r, 8), TB, 0u));
+            hs[u][1] = __dp4a(__funnelshift_r(l, c, 16), TA, __dp4a(__funnelshift_r(c, r, 16), TB, 0u));
+            hs[u][2] = __dp4a(__funnelshift_r(l, c, 24), TA, __dp4a(__funnelshift_r(c, r, 24), TB, 0u));
+            hs[u][3] = __dp4a(c, TA, __dp4a(r, TB, 0u));
+            if (blk > 0 || u == 6) {
+                const int y = y0 + i - 6;  // output row: input rows i - 6 .. i
+                if (y < h) {
+                    // vertical pass; (acc + 2^15) >> 16 clamped to 255 == byte 2 of min(acc + 2^15, 2^24 - 1)
+                    uint32_t acc[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        uint32_t s = 1u << 15;
+#pragma unroll
+                        for (int k = 0; k < 7; k++) s += (uint32_t)c_gauss_taps[k] * hs[(u + 1 + k) % 7][j];
+                        acc[j] = min(s, 0xFFFFFFu);
+                    }
+                    const uint32_t blurw =
+                        __byte_perm(__byte_perm(acc[0], acc[1], 0x0062), __byte_perm(acc[2], acc[3], 0x0062), 0x5410);
+                    if (writer) {
+                        *reinterpret_cast<uint32_t*>(d.blur + (size_t)y * pitch + X) = blurw;
+                        *reinterpret_cast<uint32_t*>(d.strength + (size_t)y * pitch + X) = 0u;
+                    }
+                    if (y >= 3 && y < h - 3) {
+                        const int cc = (u + 4) % 7, up = (u + 1) % 7;
+                        const uint32_t cm = cw[cc];
+                        const uint32_t p4 = __funnelshift_r(cm, rw[cc], 24), p12 = __funnelshift_r(lw[cc], cm, 8);
+                        const uint32_t E = rs_compass(rs_even(cm), rs_even(cw[u]), rs_even(p4), rs_even(cw[up]),
+                                                      rs_even(p12), K);
+                        const uint32_t O =
+                            rs_compass(rs_odd(cm), rs_odd(cw[u]), rs_odd(p4), rs_odd(cw[up]), rs_odd(p12), K);
+                        const uint32_t m = (E >> 15) | (O >> 14);  // pixels 0, 1 at bits 0, 1; 2, 3 at bits 16, 17
+                        bmw |= ((m | (m >> 14)) & colmask & 0xFu) << (4 * u);
+                    }
+                }
             }
         }
-    }
-    __syncthreads();
-    // vertical pass: 4 outputs of one row per thread
-    {
-        const int ty = tid >> 4, g = tid & 15;
-        int acc[4] = {0, 0, 0, 0};
+        // score this block's candidates (their circles lie within input rows 7 blk - 6 .. 7 blk + 6)
+        if (__any_sync(0xffffffffu, bmw != 0)) {
+            const int cnt = __popc(bmw);
+            int incl = cnt;
 #pragma unroll
-        for (int k = 0; k < 7; k++) {
-            const int4 r = *reinterpret_cast<const int4*>(&rows[ty + k][4 * g]);
-            acc[0] += taps[k] * r.x;
-            acc[1] += taps[k] * r.y;
-            acc[2] += taps[k] * r.z;
-            acc[3] += taps[k] * r.w;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int n = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += n;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            int pos = incl - cnt;
+            for (uint32_t m = bmw; m; m &= m - 1) {
+                const int b = __ffs(m) - 1;
+                S.cand[pos++] = (uint16_t)(((b >> 2) << 7) | (4 * lane + (b & 3)));
+            }
+            __syncwarp();
+            for (int q = lane; q < total; q += 32) {
+                const int e = S.cand[q];
+                const int ic = 7 * blk + (e >> 7) - 3, col = e & 127;  // centre input row, ring byte column
+                const int s = rs_arc_strength(ring8, ic, col);
+                if (s > t) d.strength[(size_t)(y0 + ic - 3) * pitch + x0 - 4 + col] = (uint8_t)s;
+            }
         }
-        uint32_t packed = 0;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            int v = (acc[j] + (1 << 15)) >> 16;
-            v = v < 0 ? 0 : (v > 255 ? 255 : v);
-            packed |= (uint32_t)v << (8 * j);
-        }
-        if (oy + ty < d.h) *reinterpret_cast<uint32_t*>(d.blur + (size_t)(oy + ty) * d.pitch + ox + 4 * g) = packed;
-    }
-    // FAST, phase 2: full segment test and strength of the queued pixels
-    const int nq = s_nq;
-    for (int q = tid; q < nq; q += blockDim.x) {
-        const int i = s_q[q];
-        const int ty = i / RB_TW, tx = i % RB_TW;
-        s_str[ty][tx] = (uint8_t)arc_strength(&tile[0][0], RB_SW, ty + RB_HALO, tx + 4, t_lo);
-    }
-    __syncthreads();
-    {
-        const int ty = tid >> 4, g = tid & 15;
-        if (oy + ty < d.h)
-            *reinterpret_cast<uint32_t*>(d.strength + (size_t)(oy + ty) * d.pitch + ox + 4 * g) =
-                *reinterpret_cast<const uint32_t*>(&s_str[ty][4 * g]);
+        __syncwarp();
     }
 }
 
@@ -1015,19 +1093,26 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
     cudaMemcpyToSymbol(g_sin_exc_n, &sn, sizeof(sn));
 }
 
+template <int TH>
+static void launch_strip(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
+    if (level0) k_level_strip<TH, true><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
+    else k_level_strip<TH, false><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
+}
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
     if (nitems <= 0) return;
     switch (tunables().resize_rows) {
-        case 8: k_level_resize_blur<8><<<nitems, 16 * 8, 0, st>>>(descs, rm, level0); break;
-        case 32: k_level_resize_blur<32><<<nitems, 16 * 32, 0, st>>>(descs, rm, level0); break;
-        default: k_level_resize_blur<16><<<nitems, 16 * 16, 0, st>>>(descs, rm, level0); break;
+        case 8: launch_strip<8>(descs, rm, nitems, level0, st); break;
+        case 22: launch_strip<22>(descs, rm, nitems, level0, st); break;
+        case 64: launch_strip<64>(descs, rm, nitems, level0, st); break;
+        default: launch_strip<36>(descs, rm, nitems, level0, st); break;
     }
 }
 
-// Blocks of k_level_resize_blur for a w x h level.
+// Blocks of k_level_strip for a w x h level (RS_WPB strips per block).
 int resize_blur_tiles(int w, int h) {
     const int th = tunables().resize_rows;
-    return ((w + RB_TW - 1) / RB_TW) * ((h + th - 1) / th);
+    const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + th - 1) / th);
+    return (strips + RS_WPB - 1) / RS_WPB;
 }
 int fast_blocks(int ncells) {
     const int cpb = tunables().fast_cells_per_block;

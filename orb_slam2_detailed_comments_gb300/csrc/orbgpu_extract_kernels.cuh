@@ -34,9 +34,6 @@ struct LevelDesc {
     const short* xalpha;  // 2 weights per output column
     const int* yofs;      // source row per output row (unclamped)
     const short* ybeta;   // 2 weights per output row
-    // source block of every resize tile: (first column rounded down to 4,
-    // words per row) per tile column, then (first row, rows) per tile row
-    const int2* srcb;
     // FAST cells
     int nCols, nRows, wCell, hCell;
     int maxBorderX, maxBorderY;
@@ -79,7 +76,7 @@ struct LevelDesc {
 // automatic choice uses the tensor cores.  Changing one bumps the generation,
 // so cached frame plans and captured graphs are rebuilt.
 struct Tunables {
-    int resize_rows = 16;
+    int resize_rows = 36;
     int fast_cells_per_block = 4;
     int describe_group = 8;
     long long knn_tc_min_pairs = 1LL << 28;

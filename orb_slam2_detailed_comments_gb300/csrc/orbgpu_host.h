@@ -33,7 +33,7 @@ struct LevelGeom {
 };
 
 struct LevelOffsets {
-    size_t pyr, blur, strength, xofs, srcb, xalpha, yofs, ybeta, slots, cell_count, cand, node_of, quad, nodes_a, nodes_b, cnt4,
+    size_t pyr, blur, strength, xofs, xalpha, yofs, ybeta, slots, cell_count, cand, node_of, quad, nodes_a, nodes_b, cnt4,
         childpos, aux0, aux1, aux2, best, kept;
 };
 
@@ -46,14 +46,13 @@ struct FrameLayout {
 };
 
 ExtractorTables make_tables(int nfeatures, float scale_factor, int nlevels);
-void resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int* yofs, short* ybeta);
+// Returns false if a weight pair is negative or sums above 2049 (the
+// resize kernel's 32-bit vertical sum relies on both; the rounding of
+// (1 - f) * 2048 and f * 2048 keeps every pair within [2047, 2049]).
+bool resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int* yofs, short* ybeta);
 int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom>& g);
 void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const FrameLayout& lay, uint8_t* arena,
                 int frame, int ini_th, int min_th, int out_base, int out_cap, LevelDesc* out);
-// The source block of every resize tile of level L (from level P) for the
-// current tile rows: int2 per tile column then per tile row (srcb_entries).
-void fill_source_blocks(const LevelGeom& P, const LevelGeom& L, const int* xofs, const int* yofs, int2* out);
-int srcb_entries(const LevelGeom& L);
 
 int ensure_sincos_exceptions();
 int ensure_constants();

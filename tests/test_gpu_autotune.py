@@ -13,7 +13,7 @@ def torch():
     t = require_gpu()
     yield t
     from orb_slam2_detailed_comments_gb300 import autotune
-    autotune.apply({"resize_rows": 16, "fast_cells_per_block": 4, "describe_group": 8, "knn_tc_min_pairs": 1 << 28})
+    autotune.apply({"resize_rows": 36, "fast_cells_per_block": 4, "describe_group": 8, "knn_tc_min_pairs": 1 << 28})
 
 
 def frames():
@@ -26,7 +26,7 @@ def refs(oracle):
     return [oracle.extract(img, nfeatures=nf, want_pyramid=False) for img, nf in frames()]
 
 
-@pytest.mark.parametrize("name,value", [("resize_rows", 8), ("resize_rows", 32), ("fast_cells_per_block", 1),
+@pytest.mark.parametrize("name,value", [("resize_rows", 8), ("resize_rows", 22), ("resize_rows", 64), ("fast_cells_per_block", 1),
                                         ("fast_cells_per_block", 2), ("fast_cells_per_block", 8),
                                         ("describe_group", 4), ("describe_group", 16), ("describe_group", 32)])
 def test_batch_shapes_match_oracle(torch, refs, name, value):
