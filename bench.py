@@ -149,11 +149,12 @@ def resize_blur_bytes(frames):
 
 
 # DRAM bytes (read + write) of the resize / blur / strength stage measured by
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum over its eight launches)
-# on this workload at 128 frames per step, per frame: the stage's traffic
-# scales with the frames of a step.  Below the algorithmic bytes because a
-# level written by one launch is still in L2 when the next launch reads it.
-RESIZE_BLUR_DRAM_BYTES_PER_FRAME = 544.0e6 / 128
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum over its fifteen launches:
+# the strip kernel of every level, the resize kernel of levels 1-7) on this
+# workload at 128 frames per step, per frame: the stage's traffic scales with
+# the frames of a step.  Below the algorithmic bytes because a level written
+# by one launch is still partly in L2 when the next launch reads it.
+RESIZE_BLUR_DRAM_BYTES_PER_FRAME = 572.8e6 / 128
 
 
 def fast_bytes(frames):

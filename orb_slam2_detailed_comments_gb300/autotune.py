@@ -29,7 +29,7 @@ from ._lib import check, lib
 # parameter -> (candidate values, pipeline stage it shapes)
 PARAMS = {
     "resize_rows": ((8, 22, 36, 64), "resize_blur"),
-    "fast_cells_per_block": ((1, 2, 4, 8), "fast"),
+    "fast_cells_per_block": ((1, 2, 4), "fast"),
     "describe_group": ((4, 8, 16, 32), "describe"),
 }
 KNN_PARAM = "knn_tc_min_pairs"

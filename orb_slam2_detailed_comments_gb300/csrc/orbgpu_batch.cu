@@ -3,7 +3,8 @@
 //
 // Frames of different sizes and feature budgets go through the same stage
 // kernels as the per-frame path, but each stage is ONE launch over the work
-// items of every frame: 8 resize/blur launches (one per level), one FAST
+// items of every frame: per level one resize launch (levels >= 1) and one
+// blur / FAST-strength launch, one FAST
 // launch over all cells of all levels of all frames, one DistributeOctTree
 // launch over all (frame, level) pairs, one describe launch.  The launch
 // sequence for a given frame list is captured once in a CUDA graph and
@@ -378,7 +379,7 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
     mark(5);
-    b->launches_per_run = 1 + b->nlevels + 3;
+    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 3;  // gather, strip per level, resize per level >= 1, 3 stages
 }
 
 extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t* const* images, const int* widths,

@@ -38,7 +38,7 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
     orbgpu::Tunables& t = orbgpu::g_tunables;
     const std::string n(name);
     if (n == "resize_rows" && (value == 8 || value == 22 || value == 36 || value == 64)) t.resize_rows = (int)value;
-    else if (n == "fast_cells_per_block" && (value == 1 || value == 2 || value == 4 || value == 8))
+    else if (n == "fast_cells_per_block" && (value == 1 || value == 2 || value == 4))
         t.fast_cells_per_block = (int)value;
     else if (n == "describe_group" && (value == 4 || value == 8 || value == 16 || value == 32))
         t.describe_group = (int)value;

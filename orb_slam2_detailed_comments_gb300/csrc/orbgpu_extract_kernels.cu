@@ -146,20 +146,154 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
     return a > b ? a : b;
 }
 
-// ---------------------------------------------------------------- resize + blur + FAST strength
-// One warp per strip of 120 columns x TH rows of level l.  Lane k holds the
-// four pixels of columns [x0 - 4 + 4k, x0 + 4k) of a row as one 32-bit word:
-// lanes 1..30 own the strip's columns, lanes 0 and 31 the 4-column halos
-// (REFLECT_101 outside the level).  The warp walks the TH + 6 rows
-// [y0 - 3, y0 + TH + 3) top to bottom with the last seven rows in registers:
-//  * the row's pixels: level 0 loads them; levels >= 1 resize from level l-1
-//    (cv::resize INTER_LINEAR, 11-bit fixed point): a source row is
-//    interpolated horizontally once for the (on average 1.2) output rows that
-//    use it, one dp2a per pixel on the two source bytes a prmt picks from the
-//    lane's source words, which are loaded one row ahead;
-//  * the 7x7 Gaussian (8-bit fixed point): horizontal sums by two dp4a per
-//    pixel from the lane's word and its neighbours' (shuffles), the vertical
-//    pass over seven rows of sums held in registers;
+// ---------------------------------------------------------------- resize, blur + FAST strength
+// Both kernels tile a level in strips of 120 columns x TH rows, RS_WPB strips
+// (one warp each) per block, so they share one block count per level.
+#define RS_COLS 120       // level columns per strip
+#define RS_WPB 2          // strips (warps) per block
+#define RS_CAND (30 * 28) // FAST candidates of one 7-row block at most
+
+// Level l (l >= 1) from level l-1: cv::resize INTER_LINEAR in 11-bit fixed
+// point.  Lane k (k < 30) of the strip's warp produces columns
+// [x0 + 4k, x0 + 4k + 4) of the strip's rows.  A source row is interpolated
+// horizontally once for the (on average 1.2) output rows that use it: one
+// dp2a per pixel on the two source bytes that a prmt picks from the lane's
+// source words, which are loaded one row ahead.  Weights come in pairs
+// summing to 2047..2049 (checked when the tables are built), so the
+// vertical sum 4 (h0 b0 + h1 b1) + 2^23 stays below 2^32 and its byte 3 is
+// (h0 b0 + h1 b1 + 2^21) >> 22.
+template <int TH>
+__global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* descs, RangeMap rm) {
+    __shared__ int4 s_rows[RS_WPB][TH + 1];  // output row i: source rows r0, r1, 4 b0 | 4 b1 << 16
+    WorkItem it;
+    map_item(rm, blockIdx.x, it.desc, it.index);
+    const LevelDesc& d = descs[it.desc];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = d.w, h = d.h;
+    const int tiles_x = (w + RS_COLS - 1) / RS_COLS;
+    const int tile = it.index * RS_WPB + warp;
+    if (tile >= tiles_x * ((h + TH - 1) / TH)) return;
+    const int x0 = (tile % tiles_x) * RS_COLS, y0 = (tile / tiles_x) * TH;
+    const int X = x0 + 4 * lane;
+    const bool writer = lane < RS_COLS / 4 && X < w;
+    int4* rows = s_rows[warp];
+    for (int i = lane; i <= TH; i += 32) {
+        const int y = min(y0 + i, h - 1);
+        const int sy = d.yofs[y];
+        rows[i] = make_int4(min(max(sy, 0), d.sh - 1), min(max(sy + 1, 0), d.sh - 1),
+                            (4 * (int)d.ybeta[2 * y]) | ((4 * (int)d.ybeta[2 * y + 1]) << 16), 0);
+    }
+    // per pixel the packed weights (a0 | a1 << 16) and the byte selector of
+    // (sx, sx1) among the 8 source bytes from bmin; columns past the level
+    // width repeat the last one (their bytes land in the row padding)
+    uint32_t coef[4], sel[4];
+    int sxs[4], sx1s[4], bmin = 1 << 30, bmax = -1;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int x = min(X + j, w - 1);
+        sxs[j] = d.xofs[x];
+        sx1s[j] = min(sxs[j] + 1, d.sw - 1);
+        coef[j] = (uint32_t)(uint16_t)d.xalpha[2 * x] | ((uint32_t)(uint16_t)d.xalpha[2 * x + 1] << 16);
+        bmin = min(bmin, sxs[j]);
+        bmax = max(bmax, sx1s[j]);
+    }
+    const bool fastcols = bmax - bmin <= 7;
+    const int sbase = bmin & ~3;
+    const uint32_t sshift = 8u * (uint32_t)(bmin & 3);
+    const int nwords = writer && fastcols ? (bmax - sbase) / 4 + 1 : 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) sel[j] = (uint32_t)(sxs[j] - bmin) | ((uint32_t)(sx1s[j] - bmin) << 4);
+    __syncwarp();
+
+    auto source_words = [&](int s, uint32_t& w0, uint32_t& w1, uint32_t& w2) {
+        const uint8_t* p = d.src + (size_t)s * d.spitch + sbase;
+        w0 = nwords > 0 ? *reinterpret_cast<const uint32_t*>(p) : 0u;
+        w1 = nwords > 1 ? *reinterpret_cast<const uint32_t*>(p + 4) : 0u;
+        w2 = nwords > 2 ? *reinterpret_cast<const uint32_t*>(p + 8) : 0u;
+    };
+    auto hinterp = [&](int s, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t* hv) {
+        if (fastcols) {
+            const uint32_t W0 = __funnelshift_r(w0, w1, sshift), W1 = __funnelshift_r(w1, w2, sshift);
+#pragma unroll
+            for (int j = 0; j < 4; j++) hv[j] = __dp2a_lo(coef[j], __byte_perm(W0, W1, sel[j]), 0u);
+        } else {
+            // source columns more than 7 apart (scale factors above about 1.6)
+            const uint8_t* row = d.src + (size_t)s * d.spitch;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                hv[j] = (uint32_t)row[sxs[j]] * (coef[j] & 0xFFFFu) + (uint32_t)row[sx1s[j]] * (coef[j] >> 16);
+        }
+    };
+
+    const int nrows = min(TH, h - y0);
+    uint32_t ha[4] = {0, 0, 0, 0}, hb[4] = {0, 0, 0, 0};
+    int ca = -1, cb = -1;
+    // source words of output rows i (set i & 1) and i + 1, loaded two rows ahead
+    uint32_t pw[2][6];
+    {
+        const int4 e0 = rows[0], e1 = rows[min(1, TH)];
+        source_words(e0.x, pw[0][0], pw[0][1], pw[0][2]);
+        source_words(e0.y, pw[0][3], pw[0][4], pw[0][5]);
+        source_words(e1.x, pw[1][0], pw[1][1], pw[1][2]);
+        source_words(e1.y, pw[1][3], pw[1][4], pw[1][5]);
+    }
+    uint8_t* out = d.dst + (size_t)y0 * d.pitch + X;
+    auto row_step = [&](int i, uint32_t* cur) {
+        const int4 e = rows[i];
+        uint32_t na[4], nb[4];
+        if (e.x == ca) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) na[j] = ha[j];
+        } else if (e.x == cb) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) na[j] = hb[j];
+        } else {
+            hinterp(e.x, cur[0], cur[1], cur[2], na);
+        }
+        if (e.y == cb) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) nb[j] = hb[j];
+        } else if (e.y == ca) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) nb[j] = ha[j];
+        } else if (e.y == e.x) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) nb[j] = na[j];
+        } else {
+            hinterp(e.y, cur[3], cur[4], cur[5], nb);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            ha[j] = na[j];
+            hb[j] = nb[j];
+        }
+        ca = e.x;
+        cb = e.y;
+        const int4 e2 = rows[min(i + 2, TH)];
+        source_words(e2.x, cur[0], cur[1], cur[2]);
+        source_words(e2.y, cur[3], cur[4], cur[5]);
+        const uint32_t B0 = (uint32_t)e.z & 0xFFFFu, B1 = (uint32_t)e.z >> 16;
+        uint32_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = ha[j] * B0 + hb[j] * B1 + (1u << 23);
+        if (writer)
+            *reinterpret_cast<uint32_t*>(out + (size_t)i * d.pitch) =
+                __byte_perm(__byte_perm(v[0], v[1], 0x0073), __byte_perm(v[2], v[3], 0x0073), 0x5410);
+    };
+    for (int i = 0; i < nrows; i += 2) {
+        row_step(i, pw[0]);
+        if (i + 1 < nrows) row_step(i + 1, pw[1]);
+    }
+}
+
+// The 7x7 Gaussian (8-bit fixed point, REFLECT_101) and the FAST arc strength
+// of every pixel of level l.  Lane k holds the four pixels of columns
+// [x0 - 4 + 4k, x0 + 4k) of a row as one 32-bit word: lanes 1..30 own the
+// strip's columns, lanes 0 and 31 the 4-column halos (reflected outside the
+// level).  The warp walks the TH + 6 rows [y0 - 3, y0 + TH + 3) top to
+// bottom with the last seven rows in registers:
+//  * horizontal sums by two dp4a per pixel from the lane's word and its
+//    neighbours' (shuffles), the vertical pass over seven rows of sums;
 //  * FAST at the lower threshold t: the compass-point pre-test (two circle
 //    points among 0, 4, 8, 12 that are adjacent on the circle both brighter
 //    than v + t or both darker than v - t; every nine-pixel arc contains such
@@ -167,14 +301,10 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 //    the warp compacts the candidates and scores them from a 16-row ring of
 //    level rows in shared memory.
 // The warps of a block share nothing: no block-level synchronisation.
-#define RS_COLS 120       // level columns per strip (lanes 1..30)
-#define RS_WPB 2          // strips (warps) per block
-#define RS_CAND (30 * 28) // candidates of one 7-row block at most
-
 template <int TH>
 struct StripShared {
     uint32_t ring[16][32];  // level rows: input row i at i & 15
-    int4 rows[TH + 7];      // input row i: reflected level row, source rows r0, r1, 4 b0 | 4 b1 << 16
+    int rows[TH + 7];       // input row i: reflected level row
     uint16_t cand[RS_CAND]; // (row within the 7-row block) << 7 | byte column of the ring
 };
 
@@ -223,8 +353,8 @@ __device__ __forceinline__ int rs_arc_strength(const uint8_t* ring, int ic, int 
     return (int)max(best & 0xFFFFu, best >> 16);
 }
 
-template <int TH, bool LEVEL0>
-__global__ void __launch_bounds__(32 * RS_WPB) k_level_strip(const LevelDesc* descs, RangeMap rm) {
+template <int TH>
+__global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc* descs, RangeMap rm) {
     static_assert((TH + 6) % 7 == 0, "TH + 6 rows must be whole blocks of 7");
     constexpr int NB = (TH + 6) / 7;
     __shared__ __align__(16) StripShared<TH> sh_all[RS_WPB];
@@ -247,171 +377,63 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_strip(const LevelDesc* de
         if (writer && X + j >= 3 && X + j < w - 3) colmask |= 1u << j;
     const int t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
     const uint32_t K = (0x8000u - (uint32_t)t - 1u) * 0x00010001u;
-
-    // per input row: reflected level row and (levels >= 1) source rows and weights
-    for (int i = lane; i < TH + 7; i += 32) {
-        const int rr = reflect101(y0 - 3 + min(i, TH + 5), h);
-        int4 e = make_int4(rr, 0, 0, 0);
-        if (!LEVEL0) {
-            const int sy = d.yofs[rr];
-            e.y = min(max(sy, 0), d.sh - 1);
-            e.z = min(max(sy + 1, 0), d.sh - 1);
-            e.w = (4 * (int)d.ybeta[2 * rr]) | ((4 * (int)d.ybeta[2 * rr + 1]) << 16);
-        }
-        S.rows[i] = e;
-    }
-
-    // level 0: the lane's columns (reflected at the edges)
+    for (int i = lane; i < TH + 7; i += 32) S.rows[i] = reflect101(y0 - 3 + min(i, TH + 5), h);
+    // the lane's columns, reflected at the level edges
     int xr[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) xr[j] = reflect101(X + j, w);
     const bool interior = X >= 0 && X + 3 < w;
-    // levels >= 1: per pixel the packed weights (a0 | a1 << 16) and the
-    // byte selector of (sx, sx1) among the 8 source bytes from bmin
-    uint32_t coef[4] = {0, 0, 0, 0}, sel[4] = {0, 0, 0, 0};
-    int sbase = 0, nwords = 0;
-    uint32_t sshift = 0;
-    bool fastcols = true;
-    if (!LEVEL0) {
-        int sxs[4], sx1s[4], bmin = 1 << 30, bmax = -1;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            sxs[j] = d.xofs[xr[j]];
-            sx1s[j] = min(sxs[j] + 1, d.sw - 1);
-            coef[j] = (uint32_t)(uint16_t)d.xalpha[2 * xr[j]] | ((uint32_t)(uint16_t)d.xalpha[2 * xr[j] + 1] << 16);
-            bmin = min(bmin, sxs[j]);
-            bmax = max(bmax, sx1s[j]);
-        }
-        fastcols = bmax - bmin <= 7;
-        sbase = bmin & ~3;
-        sshift = 8u * (uint32_t)(bmin & 3);
-        nwords = fastcols ? (bmax - sbase) / 4 + 1 : 0;
-#pragma unroll
-        for (int j = 0; j < 4; j++) sel[j] = (uint32_t)(sxs[j] - bmin) | ((uint32_t)(sx1s[j] - bmin) << 4);
-    }
     __syncwarp();
-
     const uint32_t TA = (uint32_t)c_gauss_taps[0] | ((uint32_t)c_gauss_taps[1] << 8) |
                         ((uint32_t)c_gauss_taps[2] << 16) | ((uint32_t)c_gauss_taps[3] << 24);
     const uint32_t TB = (uint32_t)c_gauss_taps[4] | ((uint32_t)c_gauss_taps[5] << 8) | ((uint32_t)c_gauss_taps[6] << 16);
-
-    // one level word of row rr (level 0)
+    // tap pairs of the vertical pass (bytes 0, 1 for dp2a)
+    const uint32_t T01 = (uint32_t)c_gauss_taps[0] | ((uint32_t)c_gauss_taps[1] << 8);
+    const uint32_t T23 = (uint32_t)c_gauss_taps[2] | ((uint32_t)c_gauss_taps[3] << 8);
+    const uint32_t T45 = (uint32_t)c_gauss_taps[4] | ((uint32_t)c_gauss_taps[5] << 8);
+    const uint32_t T6 = (uint32_t)c_gauss_taps[6];
     auto level_word = [&](int rr) -> uint32_t {
         const uint8_t* row = d.dst + (size_t)rr * pitch;
         if (interior) return *reinterpret_cast<const uint32_t*>(row + X);
         return (uint32_t)row[xr[0]] | ((uint32_t)row[xr[1]] << 8) | ((uint32_t)row[xr[2]] << 16) |
                ((uint32_t)row[xr[3]] << 24);
     };
-    // the lane's source words of source row s (levels >= 1)
-    auto source_words = [&](int s, uint32_t& w0, uint32_t& w1, uint32_t& w2) {
-        const uint8_t* p = d.src + (size_t)s * d.spitch + sbase;
-        w0 = nwords > 0 ? *reinterpret_cast<const uint32_t*>(p) : 0u;
-        w1 = nwords > 1 ? *reinterpret_cast<const uint32_t*>(p + 4) : 0u;
-        w2 = nwords > 2 ? *reinterpret_cast<const uint32_t*>(p + 8) : 0u;
-    };
-    // horizontal interpolation of source row s at the lane's 4 columns
-    auto hinterp = [&](int s, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t* hv) {
-        if (fastcols) {
-            const uint32_t W0 = __funnelshift_r(w0, w1, sshift), W1 = __funnelshift_r(w1, w2, sshift);
-#pragma unroll
-            for (int j = 0; j < 4; j++) hv[j] = __dp2a_lo(coef[j], __byte_perm(W0, W1, sel[j]), 0u);
-        } else {
-            // source columns more than 7 apart (scale factors above about 1.6)
-            const uint8_t* row = d.src + (size_t)s * d.spitch;
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int sx = d.xofs[xr[j]], sx1 = min(sx + 1, d.sw - 1);
-                hv[j] = (uint32_t)row[sx] * (coef[j] & 0xFFFFu) + (uint32_t)row[sx1] * (coef[j] >> 16);
-            }
-        }
-    };
 
-    uint32_t cw[7], lw[7], rw[7], hs[7][4];
-    uint32_t ha[4] = {0, 0, 0, 0}, hb[4] = {0, 0, 0, 0};
-    int ca = -1, cb = -1;
-    uint32_t pc = 0, pa0 = 0, pa1 = 0, pa2 = 0, pb0 = 0, pb1 = 0, pb2 = 0;
-    {
-        const int4 e = S.rows[0];
-        if (LEVEL0) pc = level_word(e.x);
-        else {
-            source_words(e.y, pa0, pa1, pa2);
-            source_words(e.z, pb0, pb1, pb2);
-        }
-    }
+    uint32_t cw[7], pr[7][4], hprev[4] = {0, 0, 0, 0};
+    uint32_t pc = level_word(S.rows[0]);
     for (int blk = 0; blk < NB; blk++) {
         uint32_t bmw = 0;  // candidates of this block: bit 4u + j
 #pragma unroll
         for (int u = 0; u < 7; u++) {
             const int i = 7 * blk + u;
-            const int4 e = S.rows[i];
-            const int4 e1 = S.rows[i + 1];
-            uint32_t c;
-            if (LEVEL0) {
-                c = pc;
-                pc = level_word(e1.x);
-            } else {
-                uint32_t na[4], nb[4];
-                if (e.y == ca) {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) na[j] = ha[j];
-                } else if (e.y == cb) {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) na[j] = hb[j];
-                } else {
-                    hinterp(e.y, pa0, pa1, pa2, na);
-                }
-                if (e.z == cb) {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) nb[j] = hb[j];
-                } else if (e.z == ca) {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) nb[j] = ha[j];
-                } else if (e.z == e.y) {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) nb[j] = na[j];
-                } else {
-                    hinterp(e.z, pb0, pb1, pb2, nb);
-                }
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    ha[j] = na[j];
-                    hb[j] = nb[j];
-                }
-                ca = e.y;
-                cb = e.z;
-                source_words(e1.y, pa0, pa1, pa2);
-                source_words(e1.z, pb0, pb1, pb2);
-                // (h0 b0 + h1 b1 + 2^21) >> 22 == byte 3 of 4 h0 b0 + 4 h1 b1 + 2^23 (below 2^32 for
-                // weights summing to at most 2049)
-                const uint32_t B0 = (uint32_t)e.w & 0xFFFFu, B1 = (uint32_t)e.w >> 16;
-                uint32_t v[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) v[j] = ha[j] * B0 + hb[j] * B1 + (1u << 23);
-                c = __byte_perm(__byte_perm(v[0], v[1], 0x0073), __byte_perm(v[2], v[3], 0x0073), 0x5410);
-                const int yl = y0 - 3 + i;
-                if (writer && i >= 3 && i < TH + 3 && yl < h)
-                    *reinterpret_cast<uint32_t*>(d.dst + (size_t)yl * pitch + X) = c;
-            }
+            const uint32_t c = pc;
+            pc = level_word(S.rows[i + 1]);  // one row ahead
             S.ring[i & 15][lane] = c;
             const uint32_t l = __shfl_up_sync(0xffffffffu, c, 1), r = __shfl_down_sync(0xffffffffu, c, 1);
             cw[u] = c;
-            lw[u] = l;
-            rw[u] = r;
-            // horizontal Gaussian sums of the lane's 4 pixels: columns X + j - 3 .. X + j + 3
-            hs[u][0] = __dp4a(__funnelshift_r(l, c, 8), TA, __dp4a(__funnelshift_r(c, r, 8), TB, 0u));
-            hs[u][1] = __dp4a(__funnelshift_r(l, c, 16), TA, __dp4a(__funnelshift_r(c, r, 16), TB, 0u));
-            hs[u][2] = __dp4a(__funnelshift_r(l, c, 24), TA, __dp4a(__funnelshift_r(c, r, 24), TB, 0u));
-            hs[u][3] = __dp4a(c, TA, __dp4a(r, TB, 0u));
+            // horizontal Gaussian sums of the lane's 4 pixels (columns X + j - 3 .. X + j + 3; at most
+            // 255 * 257 = 65535), paired with the previous row's in 16-bit halves
+            uint32_t hcur[4];
+            hcur[0] = __dp4a(__funnelshift_r(l, c, 8), TA, __dp4a(__funnelshift_r(c, r, 8), TB, 0u));
+            hcur[1] = __dp4a(__funnelshift_r(l, c, 16), TA, __dp4a(__funnelshift_r(c, r, 16), TB, 0u));
+            hcur[2] = __dp4a(__funnelshift_r(l, c, 24), TA, __dp4a(__funnelshift_r(c, r, 24), TB, 0u));
+            hcur[3] = __dp4a(c, TA, __dp4a(r, TB, 0u));
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                pr[u][j] = __byte_perm(hprev[j], hcur[j], 0x5410);  // rows i - 1 | i << 16
+                hprev[j] = hcur[j];
+            }
             if (blk > 0 || u == 6) {
                 const int y = y0 + i - 6;  // output row: input rows i - 6 .. i
                 if (y < h) {
-                    // vertical pass; (acc + 2^15) >> 16 clamped to 255 == byte 2 of min(acc + 2^15, 2^24 - 1)
+                    // vertical pass over rows i - 6 .. i as three row pairs and row i;
+                    // (acc + 2^15) >> 16 clamped to 255 == byte 2 of min(acc + 2^15, 2^24 - 1)
                     uint32_t acc[4];
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
-                        uint32_t s = 1u << 15;
-#pragma unroll
-                        for (int k = 0; k < 7; k++) s += (uint32_t)c_gauss_taps[k] * hs[(u + 1 + k) % 7][j];
+                        uint32_t s = __dp2a_lo(pr[(u + 2) % 7][j], T01, (1u << 15) + T6 * hcur[j]);
+                        s = __dp2a_lo(pr[(u + 4) % 7][j], T23, s);
+                        s = __dp2a_lo(pr[(u + 6) % 7][j], T45, s);
                         acc[j] = min(s, 0xFFFFFFu);
                     }
                     const uint32_t blurw =
@@ -423,7 +445,8 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_strip(const LevelDesc* de
                     if (y >= 3 && y < h - 3) {
                         const int cc = (u + 4) % 7, up = (u + 1) % 7;
                         const uint32_t cm = cw[cc];
-                        const uint32_t p4 = __funnelshift_r(cm, rw[cc], 24), p12 = __funnelshift_r(lw[cc], cm, 8);
+                        const uint32_t lm = __shfl_up_sync(0xffffffffu, cm, 1), rm_ = __shfl_down_sync(0xffffffffu, cm, 1);
+                        const uint32_t p4 = __funnelshift_r(cm, rm_, 24), p12 = __funnelshift_r(lm, cm, 8);
                         const uint32_t E = rs_compass(rs_even(cm), rs_even(cw[u]), rs_even(p4), rs_even(cw[up]),
                                                       rs_even(p12), K);
                         const uint32_t O =
@@ -463,46 +486,34 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_strip(const LevelDesc* de
 
 #define FAST_MAX_ROI 72
 #define FAST_MAX_DET (FAST_MAX_ROI - 6)
-
-// Per-ROI 3x3 suppression of detection pixel (r, c) at threshold th: the
-// pixel is a corner (strength > th) whose score beats every neighbour's
-// (neighbours that are not corners, or lie outside the ROI's detection
-// region, count as 0).
-__device__ __forceinline__ bool fast_keep(const uint8_t* mstr, int dw, int dh, int r, int c, int th) {
-    const int m = mstr[r * dw + c];
-    if (m <= th) return false;
-    const int s = m - 1;
-#pragma unroll
-    for (int dy = -1; dy <= 1; dy++)
-#pragma unroll
-        for (int dx = -1; dx <= 1; dx++) {
-            if (!dx && !dy) continue;
-            const int rr = r + dy, cc = c + dx;
-            if (rr < 0 || rr >= dh || cc < 0 || cc >= dw) continue;
-            const int mq = mstr[rr * dw + cc];
-            const int nb = mq > th ? mq - 1 : 0;
-            if (!(s > nb)) return false;
-        }
-    return true;
-}
+#define FAST_ROW 80                 // staged row: 20 words
+#define FAST_MIN_CAP (33 * 33)      // survivors of a 66 x 66 region at most
 
 // The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142)
-// on the strength plane: one warp per cell.  The cell's detection region
-// (its ROI minus the 3-pixel ring) is staged in shared memory, suppressed at
-// iniThFAST and, when that leaves nothing, at minThFAST; survivors are
-// written row by row in the detector's row-major order with a running warp
-// count (no block-wide scan).
-// CPB (cells per block, 1 / 2 / 4 / 8) is chosen by the autotuner.
+// on the strength plane: one warp per cell.  FAST's per-ROI 3x3 suppression
+// keeps pixel p at threshold th when its score beats every neighbour's score
+// (a neighbour that is not a corner at th, or lies outside the ROI's
+// detection region, scores 0).  On the arc strength m (score + 1) that is
+// m > th' and m > m(q) for the 8 neighbours q (0 outside the region), with
+// th' = max(th, 1) unless the region is a single pixel: a neighbour at or
+// below th is below m already, and a pixel of score 0 (m = 1) loses to any
+// neighbour.  The neighbour test does not depend on th, so one pass over the
+// region yields the survivors at iniThFAST and at minThFAST; the latter are
+// used when the former are none.  The region is staged in shared memory as
+// aligned words with a zero ring; words without a corner are skipped whole.
+// Survivors are written in the detector's row-major order (lane order is
+// row-major order within an iteration).
+// CPB (cells per block, 1 / 2 / 4) is chosen by the autotuner.
 template <int CPB>
 __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1;
     const int cell = it.index * CPB + warp;
     if (cell >= d.nCols * d.nRows) return;
-    __shared__ uint8_t s_m[CPB][FAST_MAX_DET * FAST_MAX_DET];
+    __shared__ __align__(16) uint8_t s_m[CPB][(FAST_MAX_DET + 2) * FAST_ROW];
+    __shared__ uint16_t s_min[CPB][FAST_MIN_CAP];
     uint8_t* mstr = s_m[warp];
     const int i = cell / d.nCols, j = cell - (cell / d.nCols) * d.nCols;
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
@@ -520,52 +531,119 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         return;
     }
     const int dw = rw - 6, dh = rh - 6;
-    // staged 8 rows at a time with every load in flight before the stores
-    const uint8_t* src = d.strength + (size_t)(iniY + 3) * d.pitch + iniX + 3;
-    for (int r0 = 0; r0 < dh; r0 += 8) {
-        uint8_t v[8][3];
+    const int gx0 = iniX + 3, gy0 = iniY + 3;  // level coordinates of region pixel (0, 0)
+    // staged row: byte b <-> region column b - off - 4; words 1..nwr hold region bytes
+    const int off = gx0 & 3;
+    const int nwr = (off + 3 + dw) >> 2, nws = nwr + 2;
+    {
+        const uint8_t* g = d.strength + (size_t)gy0 * d.pitch + (gx0 - off);
+        const int rpi = 32 / nws, lr = lane / nws, lk = lane - lr * nws;
+        // keep the bytes of region columns: byte j <-> column c0 + j, c0 in [-3, dw - 1]
+        const int c0 = 4 * lk - off - 4;
+        uint32_t keep = 0;
+        if (lk >= 1 && lk <= nwr) {
+            keep = 0xFFFFFFFFu;
+            if (c0 < 0) keep <<= -8 * c0;
+            if (c0 + 4 > dw) keep &= 0xFFFFFFFFu >> (8 * (c0 + 4 - dw));
+        }
+        if (lr < rpi)
+            for (int r0 = lr - 1; r0 <= dh; r0 += 8 * rpi) {  // 8 rows of loads in flight
+                uint32_t v[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+                for (int u = 0; u < 8; u++) {
+                    const int r = r0 + u * rpi;
+                    v[u] = (keep && r >= 0 && r < dh)
+                               ? *reinterpret_cast<const uint32_t*>(g + (size_t)r * d.pitch + 4 * (lk - 1)) & keep
+                               : 0u;
+                }
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const int r = r0 + u, c = lane + 32 * k;
-                v[u][k] = (r < dh && c < dw) ? src[(size_t)r * d.pitch + c] : (uint8_t)0;
-            }
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const int r = r0 + u, c = lane + 32 * k;
-                if (r < dh && c < dw) mstr[r * dw + c] = v[u][k];
+                for (int u = 0; u < 8; u++) {
+                    const int r = r0 + u * rpi;
+                    if (r <= dh) *reinterpret_cast<uint32_t*>(mstr + (r + 1) * FAST_ROW + 4 * lk) = v[u];
+                }
             }
     }
     __syncwarp();
-    const int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
+    const int single = dw * dh == 1;
+    int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
+    if (!single) {
+        ini_th = max(ini_th, 1);
+        min_th = max(min_th, 1);
+    }
+    const int lo_th = min(ini_th, min_th);
     uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
-    for (int pass = 0; pass < 2; pass++) {
-        const int th = pass == 0 ? ini_th : min_th;
-        int total = 0;
-        for (int r = 0; r < dh; r++)
-            for (int c0 = 0; c0 < dw; c0 += 32) {
-                const int c = c0 + lane;
-                const bool keep = c < dw && fast_keep(mstr, dw, dh, r, c, th);
-                const unsigned m = __ballot_sync(0xffffffffu, keep);
-                if (keep) {
-                    const int pos = total + __popc(m & lt);
-                    if (pos < d.cell_cap)
-                        out[pos] = (uint32_t)(iniX + 3 + c) | ((uint32_t)(iniY + 3 + r) << 12) |
-                                   ((uint32_t)(mstr[r * dw + c] - 1) << 24);
+    uint16_t* smin = s_min[warp];
+    int total_ini = 0, total_min = 0;
+    const int rpi = 32 / nwr, lr = lane / nwr, lk = lane - lr * nwr + 1;
+    for (int rb = 0; rb < dh; rb += rpi) {
+        const int r = rb + lr;
+        uint32_t kini = 0, kmin = 0;  // survivors among the lane's 4 pixels
+        const uint8_t* row = mstr + (r + 1) * FAST_ROW + 4 * lk;
+        if (lr < rpi && r < dh) {
+            const uint32_t B = *reinterpret_cast<const uint32_t*>(row);
+            if (B) {
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const int m = (int)((B >> (8 * jj)) & 0xFFu);
+                    if (m > lo_th) {
+                        const uint8_t* p = row + jj;
+                        int nb = max(max(p[-1], p[1]), max(max(p[-FAST_ROW - 1], p[-FAST_ROW]), p[-FAST_ROW + 1]));
+                        nb = max(nb, max(max(p[FAST_ROW - 1], p[FAST_ROW]), p[FAST_ROW + 1]));
+                        if (m > nb) {
+                            kini |= (uint32_t)(m > ini_th) << jj;
+                            kmin |= (uint32_t)(m > min_th) << jj;
+                        }
+                    }
                 }
-                total += __popc(m);
             }
-        if (total == 0 && pass == 0) continue;
+        }
+        if (__any_sync(0xffffffffu, (kini | kmin) != 0)) {
+            const int ci = __popc(kini), cm = __popc(kmin);
+            int ii = ci, im = cm;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int ni = __shfl_up_sync(0xffffffffu, ii, o), nm = __shfl_up_sync(0xffffffffu, im, o);
+                if (lane >= o) {
+                    ii += ni;
+                    im += nm;
+                }
+            }
+            int pi = total_ini + ii - ci, pm = total_min + im - cm;
+            const int c4 = 4 * lk - off - 4;  // region column of the lane's byte 0
+            for (uint32_t b = kini; b; b &= b - 1) {
+                const int jj = __ffs(b) - 1;
+                if (pi < d.cell_cap)
+                    out[pi] = (uint32_t)(gx0 + c4 + jj) | ((uint32_t)(gy0 + r) << 12) |
+                              ((uint32_t)(row[jj] - 1) << 24);
+                pi++;
+            }
+            for (uint32_t b = kmin; b; b &= b - 1) {
+                const int jj = __ffs(b) - 1;
+                if (pm < FAST_MIN_CAP) smin[pm] = (uint16_t)((r << 8) | (c4 + jj));
+                pm++;
+            }
+            total_ini += __shfl_sync(0xffffffffu, ii, 31);
+            total_min += __shfl_sync(0xffffffffu, im, 31);
+        }
+    }
+    if (total_ini > 0) {
         if (lane == 0) {
-            if (total > d.cell_cap) atomicOr(status, 2);
-            d.cell_count[cell] = min(total, d.cell_cap);
+            if (total_ini > d.cell_cap) atomicOr(status, 2);
+            d.cell_count[cell] = min(total_ini, d.cell_cap);
         }
         return;
     }
-    if (lane == 0) d.cell_count[cell] = 0;
+    __syncwarp();
+    const int n = min(min(total_min, d.cell_cap), FAST_MIN_CAP);
+    for (int q = lane; q < n; q += 32) {
+        const int e = smin[q], r = e >> 8, c = e & 255;
+        out[q] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
+                 ((uint32_t)(mstr[(r + 1) * FAST_ROW + c + off + 4] - 1) << 24);
+    }
+    if (lane == 0) {
+        if (total_min > d.cell_cap) atomicOr(status, 2);
+        d.cell_count[cell] = n;
+    }
 }
 
 // Arc strength of every interior pixel of an image (pixels closer than 3 to
@@ -1095,8 +1173,8 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
 
 template <int TH>
 static void launch_strip(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
-    if (level0) k_level_strip<TH, true><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
-    else k_level_strip<TH, false><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
+    if (!level0) k_level_resize<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
+    k_level_strip<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
 }
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
     if (nitems <= 0) return;
@@ -1108,7 +1186,7 @@ void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int lev
     }
 }
 
-// Blocks of k_level_strip for a w x h level (RS_WPB strips per block).
+// Blocks of k_level_resize / k_level_strip for a w x h level (RS_WPB strips per block).
 int resize_blur_tiles(int w, int h) {
     const int th = tunables().resize_rows;
     const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + th - 1) / th);
@@ -1123,7 +1201,6 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, c
     switch (tunables().fast_cells_per_block) {
         case 1: k_fast_cells<1><<<nitems, 32, 0, st>>>(descs, rm, status); break;
         case 2: k_fast_cells<2><<<nitems, 64, 0, st>>>(descs, rm, status); break;
-        case 8: k_fast_cells<8><<<nitems, 256, 0, st>>>(descs, rm, status); break;
         default: k_fast_cells<4><<<nitems, 128, 0, st>>>(descs, rm, status); break;
     }
 }

@@ -3,14 +3,15 @@
 // Each kernel walks a list of work items, so the same kernels serve one frame
 // (the drop-in path) and a ragged batch of frames of different sizes.
 //
-//   k_level_resize_blur  level l from level l-1 (cv::resize INTER_LINEAR,
-//                        8-bit fixed point) and the 7x7 sigma-2 blur of level l
-//                        (REFLECT_101), one 64x16 output tile per block, the
-//                        3-pixel blur halo recomputed in shared memory.
-//   k_fast_cells         one 30-px cell per block: FAST-9 arc strength for
-//                        every pixel of the cell's ROI interior, per-ROI
-//                        non-max suppression at iniThFAST, retried at
-//                        minThFAST when nothing survives, ordered compaction.
+//   k_level_strip        level l from level l-1 (cv::resize INTER_LINEAR,
+//                        11-bit fixed point), the 7x7 sigma-2 blur of level l
+//                        (REFLECT_101) and the FAST arc strength of every
+//                        pixel: one warp per 120-column strip, rows walked
+//                        with a 7-row register window.
+//   k_fast_cells         one 30-px cell per warp: per-ROI non-max suppression
+//                        of the strength plane at iniThFAST and minThFAST in
+//                        one pass (the latter used when the former keeps
+//                        nothing), ordered compaction.
 //   k_distribute         one (frame, level) per block: DistributeOctTree as a
 //                        sequence of parallel split steps over node creation
 //                        numbers.
