@@ -349,7 +349,30 @@ int load_sincos_exceptions(const char* path) {
     };
     fill_buckets(buf.data(), cn, bk.data());
     fill_buckets(buf.data() + 2 * cn, sn, bk.data() + nb + 1);
+    // sub-bucket offsets: inside bucket b, the entries whose next 6 input
+    // bits are below s (64 uint16 per bucket; a bucket holds at most 4096)
+    std::vector<uint16_t> sub((size_t)2 * nb * 64, 0);
+    auto fill_sub = [&](const uint32_t* keys, int n, uint16_t* out) {
+        for (int i = 0; i < n; i++) {
+            const uint32_t b = keys[i] >> 12;
+            if (b < (uint32_t)nb) out[(size_t)b * 64 + ((keys[i] >> 6) & 63)]++;
+        }
+        for (size_t b = 0; b < (size_t)nb; b++) {  // counts -> exclusive prefix
+            uint16_t run = 0;
+            for (int s = 0; s < 64; s++) {
+                const uint16_t c = out[b * 64 + s];
+                out[b * 64 + s] = run;
+                run = (uint16_t)(run + c);
+            }
+        }
+    };
+    fill_sub(buf.data(), cn, sub.data());
+    fill_sub(buf.data() + 2 * cn, sn, sub.data() + (size_t)nb * 64);
     buf.insert(buf.end(), bk.begin(), bk.end());
+    const size_t sub_words = sub.size() / 2;
+    const size_t sub_at = buf.size();
+    buf.resize(buf.size() + sub_words);
+    std::memcpy(&buf[sub_at], sub.data(), sub.size() * sizeof(uint16_t));
     if (cudaMalloc(&g_exc_dev, std::max<size_t>(4, buf.size() * 4)) != cudaSuccess) return ORBGPU_ERR_OOM;
     cudaMemcpy(g_exc_dev, buf.data(), buf.size() * 4, cudaMemcpyHostToDevice);
     const uint32_t* ck = g_exc_dev;
@@ -358,7 +381,9 @@ int load_sincos_exceptions(const char* path) {
     const float* sv = (const float*)(g_exc_dev + 2 * cn + sn);
     const int* cb = (const int*)(g_exc_dev + 2 * (cn + sn));
     const int* sb = cb + nb + 1;
-    set_sincos_exceptions(ck, cv, cn, sk, sv, sn, cb, sb, nb);
+    const uint16_t* csub = (const uint16_t*)(g_exc_dev + sub_at);
+    const uint16_t* ssub = csub + (size_t)nb * 64;
+    set_sincos_exceptions(ck, cv, cn, sk, sv, sn, cb, sb, csub, ssub, nb);
     return ORBGPU_OK;
 }
 

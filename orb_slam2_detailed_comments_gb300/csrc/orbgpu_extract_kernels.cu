@@ -21,10 +21,15 @@ __device__ const uint32_t* g_sin_exc_key = nullptr;
 __device__ const float* g_sin_exc_val = nullptr;
 __device__ int g_sin_exc_n = 0;
 // bucket index (input bits >> ORBGPU_EXC_SHIFT) -> first table entry, one
-// array per table, nbuckets + 1 entries each
+// array per table, nbuckets + 1 entries each; inside bucket b, sub-bucket s
+// (the next ORBGPU_EXC_SUB_BITS input bits) starts sub[b * 64 + s] entries
+// after the bucket's first
 #define ORBGPU_EXC_SHIFT 12
+#define ORBGPU_EXC_SUB_BITS 6
 __device__ const int* g_cos_exc_bucket = nullptr;
 __device__ const int* g_sin_exc_bucket = nullptr;
+__device__ const uint16_t* g_cos_exc_sub = nullptr;
+__device__ const uint16_t* g_sin_exc_sub = nullptr;
 __device__ int g_exc_nbuckets = 0;
 
 __device__ __forceinline__ int reflect101(int p, int len) {
@@ -987,36 +992,47 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
 // ---------------------------------------------------------------- describe
 // The host library's value for input bits xb if the table lists xb, else v.
 // The bucket of xb bounds the search to a handful of entries.
-__device__ __forceinline__ float lookup_exception(const uint32_t* keys, const float* vals, const int* bucket, uint32_t xb,
-                                                  float v) {
+__device__ __forceinline__ float lookup_exception(const uint32_t* keys, const float* vals, const int* bucket,
+                                                  const uint16_t* sub, uint32_t xb, float v) {
     const uint32_t b = xb >> ORBGPU_EXC_SHIFT;
-    if (bucket == nullptr || b >= (uint32_t)g_exc_nbuckets) return v;
-    const int lo = bucket[b], hi = bucket[b + 1];
+    if (bucket == nullptr || sub == nullptr || b >= (uint32_t)g_exc_nbuckets) return v;
+    constexpr uint32_t NS = 1u << ORBGPU_EXC_SUB_BITS;
+    const uint32_t s = (xb >> (ORBGPU_EXC_SHIFT - ORBGPU_EXC_SUB_BITS)) & (NS - 1);
+    // the four loads are independent: one round trip for the entry range
+    const int base = bucket[b];
+    const int lo = base + sub[b * NS + s];
+    const int hi = s + 1 < NS ? base + sub[b * NS + s + 1] : bucket[b + 1];
     for (int i = lo; i < hi; i++)
         if (keys[i] == xb) return vals[i];
     return v;
 }
 
-// Orientation and descriptor of the kept keypoints, DESC_GROUP keypoints per
-// warp: phase A computes the IC_Angle moments of each keypoint with one lane
-// per patch column (every row read is one coalesced segment); phase B
-// evaluates fastAtan2 and the double-precision rotation of the whole group
-// at once (one keypoint per lane: the FP64 pipe is narrow on this GPU, and a
-// one-lane evaluation per keypoint occupied it for a whole warp); phase C
-// builds each rBRIEF descriptor with one descriptor byte per lane.  The
-// group size trades FP64 lane use against the serial chain of phases A and
-// C inside a warp.
+// Orientation and descriptor of the kept keypoints, G keypoints per warp and
+// no block-level synchronisation after the prologue: phase A computes the
+// IC_Angle moments with one lane per patch column (every row read is one
+// coalesced segment), two keypoints' loads in flight; phase B evaluates
+// fastAtan2 and the double-precision rotation of the warp's keypoints at once
+// (one keypoint per lane: the FP64 pipe is narrow on this GPU); phase C
+// builds the rBRIEF descriptors with one descriptor byte per lane, two
+// keypoints at a time, the pattern read from shared memory.  The group size
+// trades FP64 lane use against the serial chain of phases A and C inside a
+// warp.
 // Each block scans the levels' kept counts into shared memory (descriptors
 // are frame-major with levels ascending, so a level's offset inside its
 // frame is a difference of two prefix entries); keypoint g of the flattened
 // list finds its level by binary search.
-// DESC_GROUP (keypoints per warp, 4 / 8 / 16 / 32) is chosen by the autotuner.
-template <int DESC_GROUP>
+// G (keypoints per warp, 4 / 8 / 16 / 32) is chosen by the autotuner.
+template <int G>
 __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
                                                   uint8_t* out_desc, int* status) {
     extern __shared__ int s_pre[];  // ndescs + 1
     __shared__ int s_scan[32];
+    __shared__ float2 s_pat[16][32];  // lane l's pattern point 16 l + p at [p][l]
     const int lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+        const int l = i >> 4, p = i & 15;
+        s_pat[p][l] = make_float2((float)c_pattern[2 * i], (float)c_pattern[2 * i + 1]);
+    }
     int base = 0;
     for (int e0 = 0; e0 < ndescs; e0 += blockDim.x) {
         const int e = e0 + threadIdx.x;
@@ -1037,13 +1053,15 @@ __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int nd
     const int nwarps = gridDim.x * (blockDim.x >> 5);
     const int u = lane - ORBGPU_HALF_PATCH;  // patch column of this lane in phase A
     const int au = u < 0 ? -u : u;
-    for (int g0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * DESC_GROUP; g0 < total;
-         g0 += nwarps * DESC_GROUP) {
-        // this lane's keypoint (lanes < DESC_GROUP): level, position, output row, validity
+    for (int g0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G; g0 < total; g0 += nwarps * G) {
+        // this lane's keypoint (lanes < G): level, position, output row, validity
         const int g = g0 + lane;
         int e = 0, x = 0, y = 0, score = 0, o = 0;
         bool valid = false;
-        if (lane < DESC_GROUP && g < total) {
+        const uint8_t* lvl = nullptr;  // this keypoint's level plane and blurred plane
+        const uint8_t* blr = nullptr;
+        int pitch = 0;
+        if (lane < G && g < total) {
             int lo = 0, hi = ndescs - 1;  // last e with s_pre[e] <= g
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -1058,6 +1076,9 @@ __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int nd
             y = (int)((p >> 12) & 0xFFF);
             score = (int)(p >> 24);
             o = d.out_base + off + k;
+            pitch = d.pitch;
+            lvl = d.dst + (size_t)y * pitch + x;
+            blr = d.blur + (size_t)y * pitch + x;
             valid = true;
             if (off + k >= d.out_cap) {
                 atomicOr(status, 16);
@@ -1070,30 +1091,45 @@ __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int nd
             }
         }
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        // phase A: IC_Angle moments (src/ORBextractor.cc:94-141), integer exact
+        // phase A: IC_Angle moments (src/ORBextractor.cc:94-141), integer exact, two keypoints at a time
         int my_m01 = 0, my_m10 = 0;
-        for (unsigned rest = vmask; rest; rest &= rest - 1) {
-            const int k = __ffs(rest) - 1;
-            const int ek = __shfl_sync(0xffffffffu, e, k);
-            const int xk = __shfl_sync(0xffffffffu, x, k), yk = __shfl_sync(0xffffffffu, y, k);
-            const LevelDesc& d = descs[ek];
-            const uint8_t* col = d.dst + (size_t)yk * d.pitch + xk + u;
-            int m10 = 0, m01 = 0;
+        for (unsigned rest = vmask; rest;) {
+            const int ka = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const int kb = rest ? __ffs(rest) - 1 : -1;
+            if (rest) rest &= rest - 1;
+            const uint8_t* pa = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)lvl, ka) + u;
+            const uint8_t* pb = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)lvl, kb < 0 ? ka : kb) + u;
+            const int sa = __shfl_sync(0xffffffffu, pitch, ka), sb_ = __shfl_sync(0xffffffffu, pitch, kb < 0 ? ka : kb);
+            int a10 = 0, a01 = 0, b10 = 0, b01 = 0;
             if (lane < 2 * ORBGPU_HALF_PATCH + 1) {
 #pragma unroll
                 for (int v = -ORBGPU_HALF_PATCH; v <= ORBGPU_HALF_PATCH; v++) {
                     if (c_umax[v < 0 ? -v : v] >= au) {
-                        const int val = col[v * d.pitch];
-                        m10 += u * val;
-                        m01 += v * val;
+                        const int va = pa[v * sa];
+                        a10 += u * va;
+                        a01 += v * va;
+                        if (kb >= 0) {
+                            const int vb = pb[v * sb_];
+                            b10 += u * vb;
+                            b01 += v * vb;
+                        }
                     }
                 }
             }
-            m10 = warp_sum(m10);
-            m01 = warp_sum(m01);
-            if (lane == k) {
-                my_m10 = m10;
-                my_m01 = m01;
+            a10 = warp_sum(a10);
+            a01 = warp_sum(a01);
+            if (lane == ka) {
+                my_m10 = a10;
+                my_m01 = a01;
+            }
+            if (kb >= 0) {
+                b10 = warp_sum(b10);
+                b01 = warp_sum(b01);
+                if (lane == kb) {
+                    my_m10 = b10;
+                    my_m01 = b01;
+                }
             }
         }
         // phase B: angle and rotation, one keypoint per lane
@@ -1108,8 +1144,8 @@ __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int nd
             ca = __double2float_rn(cd);
             sb = __double2float_rn(sd);
             const uint32_t xb = __float_as_uint(ar);
-            if (g_cos_exc_n > 0) ca = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, xb, ca);
-            if (g_sin_exc_n > 0) sb = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, xb, sb);
+            if (g_cos_exc_n > 0) ca = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, g_cos_exc_sub, xb, ca);
+            if (g_sin_exc_n > 0) sb = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, g_sin_exc_sub, xb, sb);
             const LevelDesc& d = descs[e];
             orbgpu_keypoint kp;
             const float sc = d.scale;
@@ -1122,31 +1158,42 @@ __global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int nd
             kp.class_id = -1;
             out_kps[o] = kp;
         }
-        // phase C: rBRIEF, one descriptor byte per lane
-        for (unsigned rest = vmask; rest; rest &= rest - 1) {
-            const int k = __ffs(rest) - 1;
-            const int ek = __shfl_sync(0xffffffffu, e, k);
-            const int xk = __shfl_sync(0xffffffffu, x, k), yk = __shfl_sync(0xffffffffu, y, k);
-            const int ok = __shfl_sync(0xffffffffu, o, k);
-            const float a = __shfl_sync(0xffffffffu, ca, k), b = __shfl_sync(0xffffffffu, sb, k);
-            const LevelDesc& d = descs[ek];
-            const uint8_t* center = d.blur + (size_t)yk * d.pitch + xk;
-            const int step = d.pitch;
-            int val = 0;
+        // phase C: rBRIEF, one descriptor byte per lane, two keypoints at a time
+        for (unsigned rest = vmask; rest;) {
+            const int ka = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const int kb = rest ? __ffs(rest) - 1 : -1;
+            if (rest) rest &= rest - 1;
+            const int kb_ = kb < 0 ? ka : kb;
+            const uint8_t* cA = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)blr, ka);
+            const uint8_t* cB = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)blr, kb_);
+            const int stA = __shfl_sync(0xffffffffu, pitch, ka), stB = __shfl_sync(0xffffffffu, pitch, kb_);
+            const float aA = __shfl_sync(0xffffffffu, ca, ka), bA = __shfl_sync(0xffffffffu, sb, ka);
+            const float aB = __shfl_sync(0xffffffffu, ca, kb_), bB = __shfl_sync(0xffffffffu, sb, kb_);
+            const int oA = __shfl_sync(0xffffffffu, o, ka), oB = __shfl_sync(0xffffffffu, o, kb_);
+            int valA = 0, valB = 0;
 #pragma unroll
             for (int kk = 0; kk < 8; kk++) {
-                const signed char* pp = &c_pattern[(lane * 16 + 2 * kk) * 2];
-                int t[2];
+                int tA[2], tB[2] = {0, 0};
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
-                    const float px = (float)pp[2 * q], py = (float)pp[2 * q + 1];
-                    const int ry = cv_round(__fadd_rn(__fmul_rn(px, b), __fmul_rn(py, a)));
-                    const int rx = cv_round(__fsub_rn(__fmul_rn(px, a), __fmul_rn(py, b)));
-                    t[q] = center[ry * step + rx];
+                    const float2 pt = s_pat[2 * kk + q][lane];
+                    {
+                        const int ry = cv_round(__fadd_rn(__fmul_rn(pt.x, bA), __fmul_rn(pt.y, aA)));
+                        const int rx = cv_round(__fsub_rn(__fmul_rn(pt.x, aA), __fmul_rn(pt.y, bA)));
+                        tA[q] = cA[ry * stA + rx];
+                    }
+                    if (kb >= 0) {
+                        const int ry = cv_round(__fadd_rn(__fmul_rn(pt.x, bB), __fmul_rn(pt.y, aB)));
+                        const int rx = cv_round(__fsub_rn(__fmul_rn(pt.x, aB), __fmul_rn(pt.y, bB)));
+                        tB[q] = cB[ry * stB + rx];
+                    }
                 }
-                val |= (t[0] < t[1]) << kk;
+                valA |= (tA[0] < tA[1]) << kk;
+                valB |= (tB[0] < tB[1]) << kk;
             }
-            out_desc[(size_t)ok * 32 + lane] = (uint8_t)val;
+            out_desc[(size_t)oA * 32 + lane] = (uint8_t)valA;
+            if (kb >= 0) out_desc[(size_t)oB * 32 + lane] = (uint8_t)valB;
         }
     }
 }
@@ -1159,9 +1206,11 @@ void upload_constants(cudaStream_t st, const int* taps, const int* umax) {
 }
 
 void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
-                           const int* cb, const int* sb, int nbuckets) {
+                           const int* cb, const int* sb, const uint16_t* csub, const uint16_t* ssub, int nbuckets) {
     cudaMemcpyToSymbol(g_cos_exc_bucket, &cb, sizeof(cb));
     cudaMemcpyToSymbol(g_sin_exc_bucket, &sb, sizeof(sb));
+    cudaMemcpyToSymbol(g_cos_exc_sub, &csub, sizeof(csub));
+    cudaMemcpyToSymbol(g_sin_exc_sub, &ssub, sizeof(ssub));
     cudaMemcpyToSymbol(g_exc_nbuckets, &nbuckets, sizeof(nbuckets));
     cudaMemcpyToSymbol(g_cos_exc_key, &ck, sizeof(ck));
     cudaMemcpyToSymbol(g_cos_exc_val, &cv, sizeof(cv));
@@ -1215,16 +1264,16 @@ void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_ke
     const int nsm = nsm_of_current_device();
     const int group = tunables().describe_group;
     // 'group' keypoints per warp, 8 warps per block; max_kept (the node
-    // capacity) overestimates a level's keypoints about twice; at most 8
-    // resident blocks per SM
+    // capacity) overestimates a level's keypoints about twice; warps stride
+    // over the groups, at most 8 blocks per SM
     const long want = ((long)ndescs * max_kept / 2 + 8 * group - 1) / (8 * group);
     const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 8));
     const size_t smem = sizeof(int) * (ndescs + 1);
     switch (group) {
         case 4: k_describe<4><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+        case 8: k_describe<8><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
         case 16: k_describe<16><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
-        case 32: k_describe<32><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
-        default: k_describe<8><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+        default: k_describe<32><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
     }
 }
 
@@ -1240,8 +1289,8 @@ __global__ void k_sincos_probe(const float* x, int n, float* c, float* s) {
     sincos_taylor(x[i], &sd, &cd);
     float a = __double2float_rn(cd), b = __double2float_rn(sd);
     const uint32_t xb = __float_as_uint(x[i]);
-    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, xb, a);
-    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, xb, b);
+    if (g_cos_exc_n > 0) a = lookup_exception(g_cos_exc_key, g_cos_exc_val, g_cos_exc_bucket, g_cos_exc_sub, xb, a);
+    if (g_sin_exc_n > 0) b = lookup_exception(g_sin_exc_key, g_sin_exc_val, g_sin_exc_bucket, g_sin_exc_sub, xb, b);
     c[i] = a;
     s[i] = b;
 }

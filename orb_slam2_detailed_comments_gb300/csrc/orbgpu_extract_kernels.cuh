@@ -15,7 +15,8 @@
 //   k_distribute         one (frame, level) per block: DistributeOctTree as a
 //                        sequence of parallel split steps over node creation
 //                        numbers.
-//   k_describe           one warp per keypoint: IC_Angle, fastAtan2, rBRIEF.
+//   k_describe           4 to 32 keypoints per warp: IC_Angle, fastAtan2,
+//                        rBRIEF.
 #pragma once
 
 #include "orbgpu_common.cuh"
@@ -71,9 +72,9 @@ struct LevelDesc {
     int* frame_total;     // the frame's keypoint count
 };
 
-// Launch shapes chosen by the autotuner (orbgpu_tune_set): tile rows of the
-// resize / blur / strength kernel, FAST cells per block, keypoints per warp of
-// the descriptor kernel, and the query x train size from which orbgpu_knn2's
+// Launch shapes chosen by the autotuner (orbgpu_tune_set): strip rows of the
+// resize and blur / strength kernels, FAST cells per block, keypoints per
+// warp of the descriptor kernel, and the query x train size from which orbgpu_knn2's
 // automatic choice uses the tensor cores.  Changing one bumps the generation,
 // so cached frame plans and captured graphs are rebuilt.
 struct Tunables {
@@ -111,7 +112,7 @@ struct RangeMap {
 
 void upload_constants(cudaStream_t st, const int* taps, const int* umax);
 void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
-                           const int* cb, const int* sb, int nbuckets);
+                           const int* cb, const int* sb, const uint16_t* csub, const uint16_t* ssub, int nbuckets);
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st);
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st);
 int resize_blur_tiles(int w, int h);
