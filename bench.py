@@ -240,6 +240,7 @@ def run_ours(args):
                 stage_ms[kname] = stage_ms.get(kname, 0.0) + v
     total_ms = sum(times)
     value = NFRAMES * args.steps / (total_ms / 1e3)
+    search_rounds = proj.rounds()  # fixed-point rounds of the slowest frame, last timed step
 
     legs = LEGS if args.legs == "all" else set(args.legs.split(","))
     e2e_value, h2d, d2h = None, 0, 0
@@ -256,6 +257,7 @@ def run_ours(args):
                 extra[LEG_KEYS[leg]] = fn(dev)
             except Exception as e:  # reported, not fatal
                 extra[LEG_KEYS[leg]] = {"error": repr(e)}
+    tuning = dict(tuning, search_rounds=search_rounds)
     return finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, per_frame_fps, per_frame_split,
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
 
@@ -364,9 +366,10 @@ def finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, p
         "config": {"workload": "batched extraction + SearchByProjection, 64 frames mixed 640x480/752x480/1241x376/"
                                "1280x720, nFeatures 1000/1500/2000, 3000 map points per frame, radius 15*scale",
                    "frames_per_step": NFRAMES, "l2": "flushed (256 MiB write) between timed steps",
-                   "launch_shapes": {k: v["value"] for k, v in tuning.items()},
+                   "launch_shapes": {k: v["value"] for k, v in tuning.items() if k != "search_rounds"},
                    "launch_shapes_by": "pinned (--shapes)" if args.shapes else
-                   "autotuner (stage events, this device and workload)"},
+                   "autotuner (stage events, this device and workload)",
+                   "search_rounds_slowest_frame": tuning.get("search_rounds")},
         "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "per_frame_path_fps": per_frame_fps, "per_frame_split": per_frame_split,
         "batched_over_per_frame": value / per_frame_fps if per_frame_fps else None, "other_configs": extra,

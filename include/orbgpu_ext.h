@@ -33,6 +33,9 @@ int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_keypoint* kp
  * calling thread (5 when every frame is resolved in shared memory, 17 with
  * the global-memory rounds). */
 int orbgpu_batch_search_launch_count(void);
+/* Fixed-point rounds the slowest frame of the last shared-memory resolution
+ * of orbgpu_batch_search_by_projection took on the calling thread. */
+int orbgpu_batch_search_rounds(void);
 /* Resolution of the batched search on the calling thread: 0 (default) one
  * block per frame in shared memory when every frame fits, else the
  * global-memory rounds; 1 always the global-memory rounds.  Both give the

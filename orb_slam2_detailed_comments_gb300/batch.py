@@ -107,6 +107,10 @@ class BatchProjection:
     def launches_per_search(self) -> int:
         return int(lib().orbgpu_batch_search_launch_count())
 
+    def rounds(self) -> int:
+        """Fixed-point rounds of the slowest frame in the last search."""
+        return int(lib().orbgpu_batch_search_rounds())
+
 
 def motion_struct(Tcw, Tlw, fx, fy, cx, cy, bf=0.0, b=0.0):
     """orbgpu_frame_motion from rows 0-2 of CurrentFrame.mTcw / LastFrame.mTcw."""

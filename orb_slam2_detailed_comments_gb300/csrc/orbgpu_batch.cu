@@ -518,70 +518,87 @@ __global__ void k_bgrid_fill(const int* counts, int cap, const int* key_cell, in
     if (c >= 0) cell_keys[(size_t)f * cap + atomicAdd(&cursor[f * (ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS) + c], 1)] = i;
 }
 
+// BPROJ_SEG lanes per map point (32 / BPROJ_SEG map points per warp): a
+// window covers about a dozen grid cells and a handful of keypoints.
+#define BPROJ_SEG 16
 __global__ void k_bproj_candidates(const orbgpu_keypoint* kps, const uint8_t* desc, int cap, const BatchFrameInfo* info,
-                                   const int* cell_start, const int* cell_keys, const orbgpu_mappoint* mps,
+                                   const int* cell_start, const int* cell_keys, const int* key_cell,
+                                   const orbgpu_mappoint* mps,
                                    const uint8_t* mp_desc, const int* mp_off, float th, float nnratio, int slot_cap,
-                                   uint64_t* slots, int* slot_count, int* status, int* frame_cands) {
+                                   uint64_t* slots, int* slot_count, int* status) {
     // A candidate with nnratio * dist > TH_HIGH (nnratio <= 1) can neither be
     // accepted (dist > TH_HIGH) nor make an accepted best fail the ratio test
     // (best <= TH_HIGH < nnratio * dist), so the lists leave it out.
+    constexpr int W = BPROJ_SEG;
     const bool drop_far = nnratio <= 1.0f;
-    const int ncell = ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS;
     const int f = blockIdx.y;
-    const int lane = threadIdx.x & 31;
-    const int local = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31, sl = lane & (W - 1), sbase = lane & ~(W - 1);
+    const unsigned smask = (W == 32 ? 0xffffffffu : ((1u << W) - 1)) << sbase;
+    const int local = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * (32 / W) + lane / W;
     const int imp = mp_off[f] + local;
-    if (imp >= mp_off[f + 1]) return;
-    const orbgpu_mappoint mp = mps[imp];
+    const bool have = imp < mp_off[f + 1];
+    if (__all_sync(0xffffffffu, !have)) return;
     const BatchFrameInfo& I = info[f];
     const orbgpu_keypoint* K = kps + (size_t)f * cap;
     const uint8_t* D = desc + (size_t)f * cap * 32;
-    const int* cs = cell_start + (size_t)f * (ncell + 1);
+    const int* cs = cell_start + (size_t)f * (ORBGPU_GRID_COLS * ORBGPU_GRID_ROWS + 1);
     const int* ck = cell_keys + (size_t)f * cap;
-    int total = 0;
-    if (mp.track_in_view && !mp.bad && mp.track_scale_level >= 0 && mp.track_scale_level < 16) {
-        const int level = mp.track_scale_level;
+    const int* kc = key_cell + (size_t)f * cap;
+    orbgpu_mappoint mp{};
+    if (have) mp = mps[imp];
+    bool active = have && mp.track_in_view && !mp.bad && mp.track_scale_level >= 0 && mp.track_scale_level < 16;
+    int x0 = 0, x1 = -1, y0 = 0, y1 = -1, level = 0;
+    float x = 0.f, y = 0.f, rr = 0.f;
+    if (active) {
+        level = mp.track_scale_level;
         float r = mp.view_cos > 0.998f ? 2.5f : 4.0f;
         if (th != 1.0f) r = __fmul_rn(r, th);
         const float radius = __fmul_rn(r, I.scale[level]);
-        const float x = mp.proj_x, y = mp.proj_y;
-        const int x0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(x, 0.0f), radius), I.invW)));
-        const int x1 = min(ORBGPU_GRID_COLS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(x, 0.0f), radius), I.invW)));
-        const int y0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(y, 0.0f), radius), I.invH)));
-        const int y1 = min(ORBGPU_GRID_ROWS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(y, 0.0f), radius), I.invH)));
-        if (x0 < ORBGPU_GRID_COLS && x1 >= 0 && y0 < ORBGPU_GRID_ROWS && y1 >= 0) {
-            const uint8_t* dmp = mp_desc + (size_t)imp * 32;
-            const float rr = __fmul_rn(radius, radius);
-            warp_window_keys(cs, ck, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
-                bool ok = false;
-                int dist = 256;
-                if (valid) {
-                    const orbgpu_keypoint kp = K[idx];
-                    ok = kp.octave >= level - 1 && kp.octave <= level;
-                    if (ok) {
-                        const float dx = __fsub_rn(kp.x, x), dy = __fsub_rn(kp.y, y);
-                        ok = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < rr;
-                    }
-                    if (ok) {
-                        dist = hamming256_ptr(dmp, D + (size_t)idx * 32);
-                        ok = !(drop_far && __fmul_rn(nnratio, (float)dist) > (float)ORBGPU_TH_HIGH);
-                    }
-                }
-                const unsigned msk = __ballot_sync(0xffffffffu, ok);
-                if (ok) {
-                    const int pos = total + __popc(msk & ((1u << lane) - 1));
-                    if (pos < slot_cap)
-                        slots[(size_t)imp * slot_cap + pos] = ((uint64_t)(uint32_t)dist << 40) |
-                                                              ((uint64_t)(uint32_t)c << 20) | (uint64_t)(uint32_t)idx;
-                }
-                total += __popc(msk);
-            });
-        }
+        x = mp.proj_x;
+        y = mp.proj_y;
+        x0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(x, 0.0f), radius), I.invW)));
+        x1 = min(ORBGPU_GRID_COLS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(x, 0.0f), radius), I.invW)));
+        y0 = max(0, (int)floorf(__fmul_rn(__fsub_rn(__fsub_rn(y, 0.0f), radius), I.invH)));
+        y1 = min(ORBGPU_GRID_ROWS - 1, (int)ceilf(__fmul_rn(__fadd_rn(__fsub_rn(y, 0.0f), radius), I.invH)));
+        active = x0 < ORBGPU_GRID_COLS && x1 >= 0 && y0 < ORBGPU_GRID_ROWS && y1 >= 0 && x0 <= x1 && y0 <= y1;
+        rr = __fmul_rn(radius, radius);
     }
-    if (lane == 0) {
+    uint4 dm0 = make_uint4(0, 0, 0, 0), dm1 = dm0;  // the map point's descriptor
+    if (active) {
+        const uint4* dp = reinterpret_cast<const uint4*>(mp_desc + (size_t)imp * 32);
+        dm0 = dp[0];
+        dm1 = dp[1];
+    }
+    int total = 0;
+    seg_window_cols<W>(cs, ck, ORBGPU_GRID_ROWS, active, x0, x1, y0, y1, [&](int idx, bool valid) {
+        bool ok = false;
+        int dist = 256, c = 0;
+        if (valid) {
+            c = kc[idx];
+            const orbgpu_keypoint kp = K[idx];
+            ok = kp.octave >= level - 1 && kp.octave <= level;
+            if (ok) {
+                const float dx = __fsub_rn(kp.x, x), dy = __fsub_rn(kp.y, y);
+                ok = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) < rr;
+            }
+            if (ok) {
+                const uint4* kd = reinterpret_cast<const uint4*>(D + (size_t)idx * 32);
+                dist = hamming256(dm0, dm1, kd[0], kd[1]);
+                ok = !(drop_far && __fmul_rn(nnratio, (float)dist) > (float)ORBGPU_TH_HIGH);
+            }
+        }
+        const unsigned msk = __ballot_sync(0xffffffffu, ok) & smask;
+        if (ok) {
+            const int pos = total + __popc(msk & ((1u << lane) - 1));
+            if (pos < slot_cap)
+                slots[(size_t)imp * slot_cap + pos] =
+                    ((uint64_t)(uint32_t)dist << 40) | ((uint64_t)(uint32_t)c << 20) | (uint64_t)(uint32_t)idx;
+        }
+        total += __popc(msk);
+    });
+    if (have && sl == 0) {
         slot_count[imp] = total;
         if (total > slot_cap) atomicMax(status, total);
-        if (total > 0) atomicAdd(&frame_cands[f], total);
     }
 }
 
@@ -700,16 +717,19 @@ __global__ void __launch_bounds__(1024)
     if (tid == 0) s_start[M] = base;
     if (tid < 3) s_flag[tid] = 0;
     __syncthreads();
-    const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    for (int i = warp; i < M; i += nw) {
-        const int s0 = s_start[i], cnt = s_start[i + 1] - s0;
-        const uint64_t* S = slots + (size_t)(mp0 + i) * slot_cap;
-        for (int b = lane; b < cnt; b += 32) {
-            const uint64_t key = S[b];
-            const uint32_t dist = (uint32_t)(key >> 40), cell = (uint32_t)(key >> 20) & 0xFFFFFu,
-                           idx = (uint32_t)key & 0xFFFFFu;
-            s_key[s0 + b] = dist >= 256 ? 0xFFFFFFFFu : (dist << 24) | (cell << 12) | idx;
+    // every candidate entry by one thread (its map point by binary search over
+    // the list starts), so all the slot loads are independent
+    for (int t = tid; t < base; t += blockDim.x) {
+        int lo = 0, hi = M - 1;  // last i with s_start[i] <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_start[mid] <= t) lo = mid;
+            else hi = mid - 1;
         }
+        const uint64_t key = slots[(size_t)(mp0 + lo) * slot_cap + (t - s_start[lo])];
+        const uint32_t dist = (uint32_t)(key >> 40), cell = (uint32_t)(key >> 20) & 0xFFFFFu,
+                       idx = (uint32_t)key & 0xFFFFFu;
+        s_key[t] = dist >= 256 ? 0xFFFFFFFFu : (dist << 24) | (cell << 12) | idx;
     }
     for (int k = tid; k < n; k += blockDim.x) s_oct[k] = (uint8_t)kps[(size_t)f * cap + k].octave;
     for (int i = tid; i < M; i += blockDim.x) s_res[i] = -2;
@@ -718,7 +738,9 @@ __global__ void __launch_bounds__(1024)
         cw[k] = 0x7fffffff;
     }
     bool converged = M == 0;
+    int rounds_run = 0;
     for (int round = 0; round <= M + 1 && !converged; round++) {
+        rounds_run = round + 1;
         if (tid == 0) s_flag[(round + 1) % 3] = 0;
         __syncthreads();
         for (int i = tid; i < M; i += blockDim.x) {
@@ -759,7 +781,10 @@ __global__ void __launch_bounds__(1024)
         if (!converged)
             for (int k = tid; k < cap; k += blockDim.x) cw[k] = 0x7fffffff;
     }
-    if (!converged && tid == 0) atomicOr(status + 2, 2);
+    if (tid == 0) {
+        if (!converged) atomicOr(status + 2, 2);
+        atomicMax(status + 3, rounds_run);
+    }
     int* Mo = match_out + (size_t)f * cap;
     for (int k = tid; k < cap; k += blockDim.x) Mo[k] = k < n ? -1 : -3;
     __syncthreads();
@@ -861,12 +886,19 @@ struct orbgpu_batch_proj {
     int h_cands_cap = 0;
     int last_serial_frames = 0;
     int last_launches = 0;
+    int last_rounds = 0;  // fixed-point rounds of the slowest frame (shared-memory resolution)
     int mode = 0;  // 0: shared-memory resolution when the frames fit; 1: global-memory rounds
+    int smem_attr = 0;  // dynamic shared memory the resolution kernel was last allowed
+    // frame info and map point offsets as last uploaded (skipped when unchanged)
+    std::vector<uint8_t> last_upload;
+    uint8_t* h_stage = nullptr;  // pinned staging of the uploads
+    size_t h_stage_cap = 0;
 };
 // one scratch per host thread (the search is synchronous)
 static thread_local orbgpu_batch_proj g_bproj;
 
 static int orbgpu_batch_search_last_launches() { return g_bproj.last_launches; }
+extern "C" int orbgpu_batch_search_rounds(void) { return g_bproj.last_rounds; }
 
 extern "C" int orbgpu_batch_search_mode(int mode) {
     if (mode != 0 && mode != 1) return ORBGPU_ERR_BAD_ARG;
@@ -894,12 +926,6 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
     for (int f = 0; f < nf; f++) max_mp = std::max(max_mp, mp_offsets[f + 1] - mp_offsets[f]);
     orbgpu_batch_proj& P = g_bproj;
     if (!P.h_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_pinned, 64));
-    if (P.h_cands_cap < nf) {
-        if (P.h_cands) cudaFreeHost(P.h_cands);
-        P.h_cands = nullptr;
-        ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_cands, sizeof(int) * nf));
-        P.h_cands_cap = nf;
-    }
     cudaStream_t st = b->stream;
     for (int attempt = 0; attempt < 3; attempt++) {
         const size_t need = sizeof(BatchFrameInfo) * nf + sizeof(int) * ((size_t)nf * ncell * 2 + (size_t)nf * (ncell + 1) +
@@ -912,6 +938,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
             P.scratch = nullptr;
             ORBGPU_CUDA_TRY(cudaMalloc(&P.scratch, need));
             P.bytes = need;
+            P.last_upload.clear();
         }
         size_t off = 0;
         auto take = [&](size_t n) {
@@ -921,12 +948,12 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
             return p;
         };
         BatchFrameInfo* info = (BatchFrameInfo*)take(sizeof(BatchFrameInfo) * nf);
+        int* d_off = (int*)take(sizeof(int) * (nf + 1));  // uploaded with info in one copy
         int* cell_count = (int*)take(sizeof(int) * (size_t)nf * ncell);
         int* cursor = (int*)take(sizeof(int) * (size_t)nf * ncell);
         int* cell_start = (int*)take(sizeof(int) * (size_t)nf * (ncell + 1));
         int* key_cell = (int*)take(sizeof(int) * (size_t)nf * cap);
         int* cell_keys = (int*)take(sizeof(int) * (size_t)nf * cap);
-        int* d_off = (int*)take(sizeof(int) * (nf + 1));
         int* slot_count = (int*)take(sizeof(int) * std::max(1, total_mp));
         int* status = (int*)take(sizeof(int) * 4);
         uint64_t* slots = (uint64_t*)take(sizeof(uint64_t) * (size_t)std::max(1, total_mp) * P.slot_cap);
@@ -934,7 +961,6 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         int* res = (int*)take(sizeof(int) * std::max(1, total_mp));
         int* changed = (int*)take(sizeof(int) * BPROJ_ROUNDS * nf);
         int* nwarp = (int*)take(sizeof(int) * 2);
-        int* frame_cands = (int*)take(sizeof(int) * nf);
         std::vector<BatchFrameInfo> hi(nf);
         for (int f = 0; f < nf; f++) {
             const int w = b->frame_w[f], h = b->frame_h[f];
@@ -943,48 +969,76 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
             hi[f].n_cap = cap;
             for (int l = 0; l < 16; l++) hi[f].scale[l] = b->frame_scale[(size_t)f * 16 + l];
         }
-        ORBGPU_CUDA_TRY(cudaMemcpyAsync(info, hi.data(), sizeof(BatchFrameInfo) * nf, cudaMemcpyHostToDevice, st));
-        ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_off, mp_offsets, sizeof(int) * (nf + 1), cudaMemcpyHostToDevice, st));
+        {
+            // frame info then offsets, contiguous in the scratch (info is 256-aligned and d_off follows it)
+            const size_t ib = sizeof(BatchFrameInfo) * nf, ob = sizeof(int) * (nf + 1);
+            const size_t gap = (size_t)((uint8_t*)d_off - (uint8_t*)info);
+            std::vector<uint8_t> up(gap + ob, 0);
+            std::memcpy(up.data(), hi.data(), ib);
+            std::memcpy(up.data() + gap, mp_offsets, ob);
+            if (up != P.last_upload) {
+                if (P.h_stage_cap < up.size()) {
+                    if (P.h_stage) cudaFreeHost(P.h_stage);
+                    P.h_stage = nullptr;
+                    ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_stage, up.size()));
+                    P.h_stage_cap = up.size();
+                }
+                std::memcpy(P.h_stage, up.data(), up.size());  // the previous call's copy has completed (it synchronised)
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(info, P.h_stage, up.size(), cudaMemcpyHostToDevice, st));
+                P.last_upload.swap(up);
+            }
+        }
         ORBGPU_CUDA_TRY(cudaMemsetAsync(cell_count, 0, sizeof(int) * (size_t)nf * ncell, st));
         ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * 4, st));
-        ORBGPU_CUDA_TRY(cudaMemsetAsync(frame_cands, 0, sizeof(int) * nf, st));
         dim3 gk((cap + 255) / 256, nf);
         k_bgrid_count<<<gk, 256, 0, st>>>(kps, counts, cap, info, key_cell, cell_count);
         k_bgrid_scan<<<nf, 1024, 0, st>>>(cell_count, cell_start, cursor);
         k_bgrid_fill<<<gk, 256, 0, st>>>(counts, cap, key_cell, cursor, cell_keys);
         const int wpb = 8;
-        dim3 gc((std::max(1, max_mp) + wpb - 1) / wpb, nf);
-        k_bproj_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, mappoints,
+        const int mp_per_block = wpb * (32 / BPROJ_SEG);
+        dim3 gc((std::max(1, max_mp) + mp_per_block - 1) / mp_per_block, nf);
+        k_bproj_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, key_cell, mappoints,
                                                    mp_descriptors, d_off, th, nnratio, P.slot_cap, slots, slot_count,
-                                                   status, frame_cands);
-        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
-        ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_cands, frame_cands, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
-        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
-        if (P.h_pinned[0] > P.slot_cap) {  // a window held more candidates than the slots: widen and redo
-            P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
-            continue;
-        }
-        // every frame in shared memory when it fits (one launch), else the
-        // global-memory fixed-point rounds and the result write-out (serial
-        // replay for any frame that did not converge)
-        int t_max = 0;
-        for (int f = 0; f < nf; f++) t_max = std::max(t_max, P.h_cands[f]);
-        const size_t smem = sizeof(int) * ((size_t)2 * max_mp + 1 + 2 * (size_t)cap + (size_t)t_max) + (size_t)cap + 16;
-        if (P.mode == 0 && cap < 4096 && smem <= 200 * 1024) {
-            ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bproj_resolve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem));
+                                                   status);
+        // every frame in shared memory when it fits (one launch, sized for up
+        // to t_cap candidates per frame; the kernel reports a frame above it),
+        // else the global-memory fixed-point rounds and the result write-out
+        // (serial replay for any frame that did not converge)
+        const size_t fixed = sizeof(int) * ((size_t)2 * max_mp + 1 + 2 * (size_t)cap) + (size_t)cap + 16;
+        const size_t smem_max = 200 * 1024;
+        if (P.mode == 0 && cap < 4096 && fixed + 4 * 1024 <= smem_max) {
+            const int t_cap = (int)((smem_max - fixed) / sizeof(int));
+            const size_t smem = fixed + sizeof(int) * (size_t)t_cap;
+            if (P.smem_attr != (int)smem) {
+                ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bproj_resolve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)smem));
+                P.smem_attr = (int)smem;
+            }
             k_bproj_resolve_smem<<<nf, 1024, smem, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio,
-                                                         t_max, match_out, nmatches, status);
+                                                         t_cap, match_out, nmatches, status);
             ORBGPU_CUDA_TRY(cudaGetLastError());
-            ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned + 2, status + 1, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
             ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+            if (P.h_pinned[0] > P.slot_cap) {  // a window held more candidates than the slots: widen and redo
+                P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
+                continue;
+            }
             P.last_serial_frames = 0;
             P.last_launches = 4 + 1;
-            if (P.h_pinned[3] != 0) {
+            P.last_rounds = P.h_pinned[3];
+            if (P.h_pinned[2] & 2) {
                 orbgpu_set_last_error("batched projection: shared-memory resolution failed", __FILE__, __LINE__);
                 return ORBGPU_ERR_CUDA;
             }
-            return ORBGPU_OK;
+            if (!(P.h_pinned[2] & 1)) return ORBGPU_OK;
+            // a frame above t_cap: the global-memory rounds below
+        } else {
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+            ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+            if (P.h_pinned[0] > P.slot_cap) {
+                P.slot_cap = ((P.h_pinned[0] + 63) / 64) * 64;
+                continue;
+            }
         }
         P.last_launches = 4 + BPROJ_ROUNDS + 1;
         const int warps = std::max((std::max(1, max_mp) + wpb - 1) / wpb * wpb, ((cap + 31) / 32 + wpb - 1) / wpb * wpb);
@@ -1162,12 +1216,15 @@ __global__ void __launch_bounds__(1024)
     if (tid < 3) s_flag[tid] = 0;
     if (tid < ORBGPU_HISTO_LENGTH) hist[tid] = 0;
     __syncthreads();
-    const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    if (in_smem)
-        for (int i = warp; i < M; i += nw) {
-            const int s0 = s_start[i], cnt = s_start[i + 1] - s0;
-            const uint32_t* S = slots + (size_t)(mp0 + i) * slot_cap;
-            for (int b = lane; b < cnt; b += 32) s_key[s0 + b] = S[b];
+    if (in_smem)  // every candidate entry by one thread: the slot loads are independent
+        for (int t = tid; t < base; t += blockDim.x) {
+            int lo = 0, hi = M - 1;  // last i with s_start[i] <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_start[mid] <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            s_key[t] = slots[(size_t)(mp0 + lo) * slot_cap + (t - s_start[lo])];
         }
     for (int i = tid; i < M; i += blockDim.x) {
         s_res[i] = -2;
@@ -1304,6 +1361,7 @@ extern "C" int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const or
         max_mp = std::max(max_mp, last_offsets[f + 1] - last_offsets[f]);
     }
     orbgpu_batch_proj& P = g_bproj;
+    P.last_upload.clear();  // this search reuses the scratch the projection search caches its uploads in
     if (!P.h_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&P.h_pinned, 64));
     if (P.h_cands_cap < nf) {
         if (P.h_cands) cudaFreeHost(P.h_cands);

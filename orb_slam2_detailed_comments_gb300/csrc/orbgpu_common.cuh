@@ -93,6 +93,62 @@ __device__ __forceinline__ int warp_min_i(int v) {
 // sizes, so a window costs one pass instead of one dependent round trip per
 // cell.  visit(idx, cell, valid) is called by every lane once per step
 // (valid is false past the window's last entry).
+// The keypoints of the grid cells [x0, x1] x [y0, y1] for W-lane segments of
+// a warp (W = 8 or 16), each segment with its own window: segment g holds
+// lanes [g W, g W + W).  Cells are stored column-major (cell = x * rows + y)
+// and their key lists back to back, so the window's keys of grid column x
+// are one range of cell_keys: one lane per column instead of one per cell.
+// Keys are visited column by column, cell by cell within a column, in list
+// order within a cell (GetFeaturesInArea's order); the visitor learns a
+// key's cell from the binning.  Every lane of the warp runs the loops to the
+// longest segment's bounds (a segment with active == false, or past its own
+// bounds, visits with valid == false), so the visitor may use full-warp
+// ballots and shuffles.
+template <int W, typename Visit>
+__device__ __forceinline__ void seg_window_cols(const int* cell_start, const int* cell_keys, int rows, bool active,
+                                                int x0, int x1, int y0, int y1, Visit visit) {
+    static_assert(W == 8 || W == 16, "segment width");
+    const int sl = (threadIdx.x & 31) & (W - 1);
+    const int ncol = active && y1 >= y0 ? x1 - x0 + 1 : 0;
+    int nmax = ncol;
+#pragma unroll
+    for (int o = W; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+    for (int c0 = 0; c0 < nmax; c0 += W) {
+        const int cx = c0 + sl;
+        int s = 0, n = 0;
+        if (cx < ncol) {
+            const int base = (x0 + cx) * rows;
+            s = cell_start[base + y0];
+            n = cell_start[base + y1 + 1] - s;
+        }
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < W; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o, W);
+            if (sl >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, W - 1, W);
+        const int excl = incl - n;
+        int tmax = total;
+#pragma unroll
+        for (int o = W; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+        for (int t0 = 0; t0 < tmax; t0 += W) {
+            const int t = t0 + sl;
+            // the last lane of the segment whose range starts at or before t holds entry t
+            int k = 0;
+#pragma unroll
+            for (int step = W / 2; step > 0; step >>= 1) {
+                const int e = __shfl_sync(0xffffffffu, excl, k + step, W);
+                if (e <= t) k += step;
+            }
+            const int sk = __shfl_sync(0xffffffffu, s, k, W);
+            const int ek = __shfl_sync(0xffffffffu, excl, k, W);
+            const bool valid = t < total;
+            visit(valid ? cell_keys[sk + t - ek] : -1, valid);
+        }
+    }
+}
+
 template <typename Visit>
 __device__ __forceinline__ void warp_window_keys(const int* cell_start, const int* cell_keys, int rows, int x0,
                                                  int x1, int y0, int y1, Visit visit) {
