@@ -1092,7 +1092,8 @@ __device__ __forceinline__ float bpose_row(const float* row, float X0, float X1,
 }
 
 __global__ void k_bpf_candidates(const orbgpu_keypoint* kps, const uint8_t* desc, int cap, const BatchFrameInfo* info,
-                                 const int* cell_start, const int* cell_keys, const BatchMotion* motions,
+                                 const int* cell_start, const int* cell_keys, const int* key_cell,
+                                 const BatchMotion* motions,
                                  const orbgpu_keypoint* last_kps, const orbgpu_frame_mappoint* last_mps,
                                  const uint8_t* last_desc, const int* last_off, float th, int slot_cap,
                                  uint32_t* slots, int* slot_count, int* status, int* frame_cands) {
@@ -1109,6 +1110,7 @@ __global__ void k_bpf_candidates(const orbgpu_keypoint* kps, const uint8_t* desc
     const uint8_t* D = desc + (size_t)f * cap * 32;
     const int* cs = cell_start + (size_t)f * (ncell + 1);
     const int* ck = cell_keys + (size_t)f * cap;
+    const int* kc = key_cell + (size_t)f * cap;
     const int oct = last_kps[i].octave;
     int total = 0;
     bool live = (mp.flags & ORBGPU_MP_PRESENT) && !(mp.flags & ORBGPU_MP_OUTLIER) && oct >= 0 && oct < 16;
@@ -1143,7 +1145,7 @@ __global__ void k_bpf_candidates(const orbgpu_keypoint* kps, const uint8_t* desc
         if (x0 < ORBGPU_GRID_COLS && x1 >= 0 && y0 < ORBGPU_GRID_ROWS && y1 >= 0) {
             const uint8_t* dmp = last_desc + (size_t)i * 32;
             const float rr = __fmul_rn(radius, radius);
-            warp_window_keys(cs, ck, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+            warp_window_keys(cs, ck, kc, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
                 bool ok = false;
                 int dist = 256;
                 if (valid) {
@@ -1433,7 +1435,7 @@ extern "C" int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const or
         const int wpb = 8;
         if (max_mp > 0) {
             dim3 gc((max_mp + wpb - 1) / wpb, nf);
-            k_bpf_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, mot, last_kps,
+            k_bpf_candidates<<<gc, 32 * wpb, 0, st>>>(kps, desc, cap, info, cell_start, cell_keys, key_cell, mot, last_kps,
                                                       last_mps, last_desc, d_off, th, P.slot_cap, slots, slot_count,
                                                       status, frame_cands);
         }

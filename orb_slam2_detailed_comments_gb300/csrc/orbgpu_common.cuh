@@ -87,17 +87,13 @@ __device__ __forceinline__ int warp_min_i(int v) {
 }
 
 // The keypoint indices of the grid cells [x0, x1] x [y0, y1] (cell c =
-// ix * rows + iy, lists in CSR form: cell_start / cell_keys), 32 per step in
+// ix * rows + iy, lists in CSR form: cell_start / cell_keys) in
 // Frame::GetFeaturesInArea's order (cells by ix then iy, each cell's list in
-// order).  The lanes read up to 32 cells' bounds at once and prefix-sum their
-// sizes, so a window costs one pass instead of one dependent round trip per
-// cell.  visit(idx, cell, valid) is called by every lane once per step
-// (valid is false past the window's last entry).
-// The keypoints of the grid cells [x0, x1] x [y0, y1] for W-lane segments of
-// a warp (W = 8 or 16), each segment with its own window: segment g holds
-// lanes [g W, g W + W).  Cells are stored column-major (cell = x * rows + y)
-// and their key lists back to back, so the window's keys of grid column x
-// are one range of cell_keys: one lane per column instead of one per cell.
+// order), for W-lane segments of a warp (W = 8, 16 or 32), each segment with
+// its own window: segment g holds lanes [g W, g W + W).  Cells are stored
+// column-major (cell = x * rows + y) and their key lists back to back, so
+// the window's keys of grid column x are one range of cell_keys: one lane per
+// column instead of one per cell.
 // Keys are visited column by column, cell by cell within a column, in list
 // order within a cell (GetFeaturesInArea's order); the visitor learns a
 // key's cell from the binning.  Every lane of the warp runs the loops to the
@@ -107,7 +103,7 @@ __device__ __forceinline__ int warp_min_i(int v) {
 template <int W, typename Visit>
 __device__ __forceinline__ void seg_window_cols(const int* cell_start, const int* cell_keys, int rows, bool active,
                                                 int x0, int x1, int y0, int y1, Visit visit) {
-    static_assert(W == 8 || W == 16, "segment width");
+    static_assert(W == 8 || W == 16 || W == 32, "segment width");
     const int sl = (threadIdx.x & 31) & (W - 1);
     const int ncol = active && y1 >= y0 ? x1 - x0 + 1 : 0;
     int nmax = ncol;
@@ -149,45 +145,15 @@ __device__ __forceinline__ void seg_window_cols(const int* cell_start, const int
     }
 }
 
+// The keypoints of the grid cells [x0, x1] x [y0, y1] for one whole warp
+// (seg_window_cols with one 32-lane segment); the visitor also gets the
+// key's cell (key_cell: the cell of every key from the binning).
 template <typename Visit>
-__device__ __forceinline__ void warp_window_keys(const int* cell_start, const int* cell_keys, int rows, int x0,
-                                                 int x1, int y0, int y1, Visit visit) {
-    const int lane = threadIdx.x & 31;
-    const int ncy = y1 - y0 + 1;
-    const int ncell = (x1 - x0 + 1) * ncy;
-    for (int c0 = 0; c0 < ncell; c0 += 32) {
-        const int ci = c0 + lane;
-        int s = 0, n = 0, cell = 0;
-        if (ci < ncell) {
-            const int qx = ci / ncy;
-            cell = (x0 + qx) * rows + y0 + (ci - qx * ncy);
-            s = cell_start[cell];
-            n = cell_start[cell + 1] - s;
-        }
-        int incl = n;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        const int excl = incl - n;
-        for (int t0 = 0; t0 < total; t0 += 32) {
-            const int t = t0 + lane;
-            // the last lane whose list starts at or before t holds entry t
-            int k = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                const int e = __shfl_sync(0xffffffffu, excl, k + step);
-                if (e <= t) k += step;
-            }
-            const int sk = __shfl_sync(0xffffffffu, s, k);
-            const int ek = __shfl_sync(0xffffffffu, excl, k);
-            const int ck = __shfl_sync(0xffffffffu, cell, k);
-            const bool valid = t < total;
-            visit(valid ? cell_keys[sk + t - ek] : -1, ck, valid);
-        }
-    }
+__device__ __forceinline__ void warp_window_keys(const int* cell_start, const int* cell_keys, const int* key_cell,
+                                                 int rows, int x0, int x1, int y0, int y1, Visit visit) {
+    seg_window_cols<32>(cell_start, cell_keys, rows, true, x0, x1, y0, y1, [&](int idx, bool valid) {
+        visit(idx, valid ? key_cell[idx] : 0, valid);
+    });
 }
 
 // Block-wide exclusive scan of one int per thread; returns the block total.

@@ -131,7 +131,7 @@ __global__ void k_init_candidates(GridDev g2, const orbgpu_keypoint* kps1, const
     if (kp1.octave <= 0 && area_cells(g2, prev[2 * i1], prev[2 * i1 + 1], window, x0, x1, y0, y1)) {
         const uint8_t* d1 = desc1 + (size_t)i1 * 32;
         const float px = prev[2 * i1], py = prev[2 * i1 + 1];
-        warp_window_keys(g2.cell_start, g2.cell_keys, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+        warp_window_keys(g2.cell_start, g2.cell_keys, g2.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
             const bool ok = valid && in_area(g2, idx, px, py, window, kp1.octave, kp1.octave);
             const unsigned m = __ballot_sync(0xffffffffu, ok);
             if (fill && ok) {
@@ -296,7 +296,7 @@ __global__ void k_proj_candidates(GridDev g, const orbgpu_mappoint* mps, const u
         int x0, x1, y0, y1;
         if (area_cells(g, mp.proj_x, mp.proj_y, radius, x0, x1, y0, y1)) {
             const uint8_t* dmp = mp_desc + (size_t)imp * 32;
-            warp_window_keys(g.cell_start, g.cell_keys, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+            warp_window_keys(g.cell_start, g.cell_keys, g.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
                 bool ok = valid && in_area(g, idx, mp.proj_x, mp.proj_y, radius, level - 1, level);
                 if (ok && g.uright && g.uright[idx] > 0) {
                     const float er = fabsf(__fsub_rn(mp.proj_xr, g.uright[idx]));
@@ -512,7 +512,7 @@ __global__ void k_pf_candidates(GridDev g, FrameMotionDev mo, const orbgpu_keypo
         if (area_cells(g, u, v, radius, x0, x1, y0, y1)) {
             const uint8_t* dmp = mp_desc + (size_t)i * 32;
             const float ur = __fsub_rn(u, __fmul_rn(mo.bf, invzc));
-            warp_window_keys(g.cell_start, g.cell_keys, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
+            warp_window_keys(g.cell_start, g.cell_keys, g.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1, [&](int idx, int c, bool valid) {
                 bool ok = valid && in_area(g, idx, u, v, radius, minL, maxL);
                 if (ok && g.uright && g.uright[idx] > 0) {
                     const float er = fabsf(__fsub_rn(ur, g.uright[idx]));
