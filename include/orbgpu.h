@@ -103,6 +103,17 @@ int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t* const* ima
                          const int* heights, const size_t* steps, const int* nfeatures, float scale_factor,
                          int nlevels, int ini_th_fast, int min_th_fast, orbgpu_keypoint* keypoints,
                          uint8_t* descriptors, int per_frame_capacity, int out_mem, int* n_keypoints);
+/* orbgpu_batch_extract without waiting: returns once the work is queued on
+ * the batch's stream (orbgpu_batch_stream), so further work on that stream
+ * (the batched searches) follows it without a host round trip.  The
+ * extraction's status (capacity checks) is returned by orbgpu_batch_wait,
+ * which synchronises the stream; the next extraction on the batch waits for
+ * it first. */
+int orbgpu_batch_extract_async(orbgpu_batch* b, int nframes, const uint8_t* const* images, const int* widths,
+                               const int* heights, const size_t* steps, const int* nfeatures, float scale_factor,
+                               int nlevels, int ini_th_fast, int min_th_fast, orbgpu_keypoint* keypoints,
+                               uint8_t* descriptors, int per_frame_capacity, int out_mem, int* n_keypoints);
+int orbgpu_batch_wait(orbgpu_batch* b);
 
 /* ------------------------------------------------------------ matcher */
 typedef struct orbgpu_matcher orbgpu_matcher;

@@ -50,10 +50,12 @@ class BatchExtractor:
     def stream(self) -> int:
         return int(lib().orbgpu_batch_stream(self._h) or 0)
 
-    def extract(self, images, nfeatures):
+    def extract(self, images, nfeatures, wait: bool = True):
         """images: list of 2-D uint8 CUDA tensors; nfeatures: list of ints.
         Returns (keypoints (F*cap, 7) float32 records, descriptors (F*cap, 32),
-        counts (F,)) -- frame f's rows start at f * per_frame_capacity."""
+        counts (F,)) -- frame f's rows start at f * per_frame_capacity.
+        wait=False returns once the work is queued on the batch's stream
+        (orbgpu_batch_extract_async); wait() then reports its status."""
         n = len(images)
         ptrs = (C.c_void_p * n)(*[t.data_ptr() for t in images])
         ws = np.array([t.shape[1] for t in images], np.int32)
@@ -61,12 +63,17 @@ class BatchExtractor:
         steps = np.array([t.stride(0) for t in images], np.uint64)
         nf = np.array(nfeatures, np.int32)
         self._keep = (ptrs, ws, hs, steps, nf)
-        check(lib().orbgpu_batch_extract(self._h, n, ptrs, ptr(ws), ptr(hs), ptr(steps), ptr(nf),
-                                         C.c_float(self.scale_factor), self.nlevels, self.ini_th, self.min_th,
-                                         ptr(self.kps), ptr(self.desc), self.per_frame_capacity, MEM_DEVICE,
-                                         ptr(self.counts)),
-              "orbgpu_batch_extract")
+        fn = lib().orbgpu_batch_extract if wait else lib().orbgpu_batch_extract_async
+        check(fn(self._h, n, ptrs, ptr(ws), ptr(hs), ptr(steps), ptr(nf), C.c_float(self.scale_factor), self.nlevels,
+                 self.ini_th, self.min_th, ptr(self.kps), ptr(self.desc), self.per_frame_capacity, MEM_DEVICE,
+                 ptr(self.counts)),
+              "orbgpu_batch_extract" if wait else "orbgpu_batch_extract_async")
         return self.kps[: n * self.per_frame_capacity], self.desc[: n * self.per_frame_capacity], self.counts[:n]
+
+    def wait(self):
+        """Synchronises the batch's stream and raises if the last asynchronous
+        extraction failed its capacity checks."""
+        check(lib().orbgpu_batch_wait(self._h), "orbgpu_batch_wait")
 
     def stage_times(self) -> dict:
         ms = np.zeros(5, np.float32)

@@ -29,7 +29,9 @@ struct ImageSrc {
 };
 
 // Copies every frame's image into its level-0 plane: one block row per
-// frame row band.
+// frame row band.  Plane rows are 64-byte aligned; a source row that is
+// 16-byte aligned moves in 16-byte vectors, any other in 4-byte words
+// assembled from bytes.  Bytes past the image width land in the row padding.
 __global__ void k_gather_images(const ImageSrc* src, int nframes) {
     const int f = blockIdx.y;
     if (f >= nframes) return;
@@ -41,7 +43,20 @@ __global__ void k_gather_images(const ImageSrc* src, int nframes) {
     for (int y = y0; y < y1; y++) {
         const uint8_t* a = s.ptr + (size_t)y * s.step;
         uint8_t* b = s.dst + (size_t)y * s.pitch;
-        for (int x = threadIdx.x; x < s.w; x += blockDim.x) b[x] = a[x];
+        if ((reinterpret_cast<uintptr_t>(a) & 15) == 0) {
+            const int nv = s.w >> 4;
+            for (int v = threadIdx.x; v < nv; v += blockDim.x)
+                reinterpret_cast<uint4*>(b)[v] = reinterpret_cast<const uint4*>(a)[v];
+            for (int x = (nv << 4) + threadIdx.x; x < s.w; x += blockDim.x) b[x] = a[x];
+        } else {
+            for (int x = 4 * threadIdx.x; x < s.w; x += 4 * blockDim.x) {
+                uint32_t wv = 0;
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (x + j < s.w) wv |= (uint32_t)a[x + j] << (8 * j);
+                *reinterpret_cast<uint32_t*>(b + x) = wv;
+            }
+        }
     }
 }
 
@@ -90,6 +105,7 @@ struct orbgpu_batch {
     int max_kept = 0, sort_cap = 0;
     ImageSrc* d_src = nullptr;
     ImageSrc* h_src = nullptr;  // pinned
+    bool pending = false;       // an asynchronous extraction whose status has not been read
     int* d_status = nullptr;
     int* d_totals = nullptr;  // per frame
     int* h_pinned = nullptr;
@@ -382,10 +398,37 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     b->launches_per_run = 1 + 2 * b->nlevels - 1 + 3;  // gather, strip per level, resize per level >= 1, 3 stages
 }
 
-extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t* const* images, const int* widths,
-                                    const int* heights, const size_t* steps, const int* nfeatures, float scale_factor,
-                                    int nlevels, int ini_th_fast, int min_th_fast, orbgpu_keypoint* keypoints,
-                                    uint8_t* descriptors, int per_frame_capacity, int out_mem, int* n_keypoints) {
+// The device status of the last extraction (copied to h_pinned[0] at its end)
+// as a return code; the stream must have been synchronised.
+static int batch_status(orbgpu_batch* b) {
+    b->pending = false;
+    if (b->h_pinned[0] & ~16) {
+        char msg[128];
+        std::snprintf(msg, sizeof(msg), "device-side capacity check failed (status 0x%x)", b->h_pinned[0]);
+        orbgpu_set_last_error(msg, __FILE__, __LINE__);
+        return ORBGPU_ERR_CUDA;
+    }
+    if (b->h_pinned[0] & 16) {
+        orbgpu_set_last_error("per-frame output capacity too small", __FILE__, __LINE__);
+        return ORBGPU_ERR_CAPACITY;
+    }
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_batch_wait(orbgpu_batch* b) {
+    if (!b) return ORBGPU_ERR_BAD_ARG;
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return b->pending ? batch_status(b) : ORBGPU_OK;
+}
+
+static int batch_extract(orbgpu_batch* b, int nframes, const uint8_t* const* images, const int* widths,
+                         const int* heights, const size_t* steps, const int* nfeatures, float scale_factor, int nlevels,
+                         int ini_th_fast, int min_th_fast, orbgpu_keypoint* keypoints, uint8_t* descriptors,
+                         int per_frame_capacity, int out_mem, int* n_keypoints, bool wait) {
+    if (b && b->pending) {  // the previous asynchronous extraction's status first
+        const int rc = orbgpu_batch_wait(b);
+        if (rc != ORBGPU_OK) return rc;
+    }
     if (!b || nframes < 0 || nframes > b->max_frames || !images || !widths || !heights || !steps || !nfeatures ||
         nlevels < 1 || nlevels > ORBGPU_MAX_LEVELS || !(scale_factor > 1.0f) || per_frame_capacity < 1 ||
         !keypoints || !descriptors || !n_keypoints || out_mem != ORBGPU_MEM_DEVICE) {
@@ -434,18 +477,29 @@ extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t*
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(n_keypoints, b->d_totals, sizeof(int) * nframes, cudaMemcpyDeviceToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->h_pinned, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (!wait) {
+        b->pending = true;
+        return ORBGPU_OK;
+    }
     ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
-    if (b->h_pinned[0] & ~16) {
-        char msg[128];
-        std::snprintf(msg, sizeof(msg), "device-side capacity check failed (status 0x%x)", b->h_pinned[0]);
-        orbgpu_set_last_error(msg, __FILE__, __LINE__);
-        return ORBGPU_ERR_CUDA;
-    }
-    if (b->h_pinned[0] & 16) {
-        orbgpu_set_last_error("per-frame output capacity too small", __FILE__, __LINE__);
-        return ORBGPU_ERR_CAPACITY;
-    }
-    return ORBGPU_OK;
+    return batch_status(b);
+}
+
+extern "C" int orbgpu_batch_extract(orbgpu_batch* b, int nframes, const uint8_t* const* images, const int* widths,
+                                    const int* heights, const size_t* steps, const int* nfeatures, float scale_factor,
+                                    int nlevels, int ini_th_fast, int min_th_fast, orbgpu_keypoint* keypoints,
+                                    uint8_t* descriptors, int per_frame_capacity, int out_mem, int* n_keypoints) {
+    return batch_extract(b, nframes, images, widths, heights, steps, nfeatures, scale_factor, nlevels, ini_th_fast,
+                         min_th_fast, keypoints, descriptors, per_frame_capacity, out_mem, n_keypoints, true);
+}
+
+extern "C" int orbgpu_batch_extract_async(orbgpu_batch* b, int nframes, const uint8_t* const* images,
+                                          const int* widths, const int* heights, const size_t* steps,
+                                          const int* nfeatures, float scale_factor, int nlevels, int ini_th_fast,
+                                          int min_th_fast, orbgpu_keypoint* keypoints, uint8_t* descriptors,
+                                          int per_frame_capacity, int out_mem, int* n_keypoints) {
+    return batch_extract(b, nframes, images, widths, heights, steps, nfeatures, scale_factor, nlevels, ini_th_fast,
+                         min_th_fast, keypoints, descriptors, per_frame_capacity, out_mem, n_keypoints, false);
 }
 
 // Device time of the stages of the last orbgpu_batch_extract call (ms):

@@ -103,6 +103,49 @@ def test_batch_projection_vs_oracle(torch, oracle):
             assert (match[f, n:] == -3).all()
 
 
+def test_async_extraction_then_search_matches_the_synchronous_path(torch, oracle):
+    """orbgpu_batch_extract_async + the batched search queued behind it on the
+    batch's stream give the synchronous path's results; orbgpu_batch_wait
+    reports a capacity failure of an asynchronous extraction."""
+    import ctypes as C
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, lib, ptr
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
+    b = BatchExtractor(8, 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    fr = frames(9, 5)
+    imgs = [torch.from_numpy(img).cuda() for img, _ in fr]
+    nfs = [nf for _, nf in fr]
+    k, d, c = b.extract(imgs, nfs)
+    ref = (k.cpu().numpy().copy(), d.cpu().numpy().copy(), c.cpu().numpy().copy())
+    rk = ref[0].view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    rd = ref[1].reshape(len(fr), cap, 32)
+    for _ in range(2):  # plain launch, then the captured graph
+        k, d, c = b.extract(imgs, nfs, wait=False)
+        b.wait()
+        assert np.array_equal(c.cpu().numpy(), ref[2])
+        kk = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+        dd = d.cpu().numpy().reshape(len(fr), cap, 32)
+        for f in range(len(fr)):
+            assert np.array_equal(kk[f, :ref[2][f]], rk[f, :ref[2][f]]), f"frame {f}"
+            assert np.array_equal(dd[f, :ref[2][f]], rd[f, :ref[2][f]]), f"frame {f}"
+    kh = rk
+    for f, (img, nf) in enumerate(fr):
+        r = oracle.extract(img, nfeatures=nf, want_pyramid=False)
+        assert_kps_equal(kh[f, :ref[2][f]], r.keypoints, f"frame {f}")
+    # a per-frame capacity of 10 rows: queued fine, reported by the wait
+    n = len(imgs)
+    ptrs = (C.c_void_p * n)(*[t.data_ptr() for t in imgs])
+    ws = np.array([t.shape[1] for t in imgs], np.int32)
+    hs = np.array([t.shape[0] for t in imgs], np.int32)
+    st = np.array([t.stride(0) for t in imgs], np.uint64)
+    nf = np.array(nfs, np.int32)
+    rc = lib().orbgpu_batch_extract_async(b._h, n, ptrs, ptr(ws), ptr(hs), ptr(st), ptr(nf), C.c_float(1.2), 8, 20, 7,
+                                          ptr(b.kps), ptr(b.desc), 10, 1, ptr(b.counts))
+    assert rc == 0
+    assert lib().orbgpu_batch_wait(b._h) == 5
+    assert lib().orbgpu_batch_wait(b._h) == 0  # reported once
+
+
 @pytest.mark.parametrize("dz,mono,ori", [(0.0, True, True), (2.0, False, True), (-2.0, False, False)])
 def test_batch_frame_projection_vs_oracle(torch, oracle, dz, mono, ori):
     """SearchByProjection(CurrentFrame, LastFrame) for every frame of a batch,
