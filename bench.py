@@ -247,10 +247,10 @@ def run_ours(args):
     search_rounds = proj.rounds()  # fixed-point rounds of the slowest frame, last timed step
 
     legs = LEGS if args.legs == "all" else set(args.legs.split(","))
-    e2e_value, h2d, d2h = None, 0, 0
+    e2e_value, h2d, d2h, e2e_ways = None, 0, 0, None
     if "e2e" in legs:
-        e2e_value, h2d, d2h = run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev,
-                                      nfs, cap)
+        e2e_value, h2d, d2h, e2e_ways = run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev,
+                                                mpd_dev, nfs, cap)
     per_frame_fps, per_frame_split = None, None
     if "perframe" in legs:
         per_frame_fps, per_frame_split = run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev)
@@ -261,7 +261,7 @@ def run_ours(args):
                 extra[LEG_KEYS[leg]] = fn(dev)
             except Exception as e:  # reported, not fatal
                 extra[LEG_KEYS[leg]] = {"error": repr(e)}
-    tuning = dict(tuning, search_rounds=search_rounds)
+    tuning = dict(tuning, search_rounds=search_rounds, e2e_ways=e2e_ways)
     return finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, per_frame_fps, per_frame_split,
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
 
@@ -271,7 +271,12 @@ LEG_KEYS = {"stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serv
 
 
 def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev, nfs, cap):
-    """Host images in pinned memory, copies inside the timed region."""
+    """Host images and map points in pinned memory, results read back to
+    pinned memory, all inside the timed region.  Two ways in: the kernels
+    read the page-locked host buffers in place over the host link (the images
+    by the gather kernel, the map points by the search), or one copy per
+    buffer into device staging first.  Returns the faster as the e2e value,
+    with both."""
     import torch
     dev = mps_dev.device
     pinned = [torch.from_numpy(img).pin_memory() for img, _ in frames]
@@ -286,33 +291,47 @@ def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_de
     h2d = sum(t.numel() for t in pinned) + mps_host.numel() + mpd_host.numel()
     d2h = kps_host.numel() * 4 + desc_host.numel() + match_host.numel() * 4
 
-    def e2e_step():
-        with torch.cuda.stream(stream):
-            for s, p in zip(staging, pinned):
-                s.copy_(p, non_blocking=True)
-            mps_stage.copy_(mps_host, non_blocking=True)
-            mpd_stage.copy_(mpd_host, non_blocking=True)
-        k, d, c = batch.extract(staging, nfs, wait=False)
-        match, nm = proj.search(mps_stage, mpd_stage, [NMAPPOINTS] * NFRAMES, TH)
-        batch.wait()
+    def readback(k, d, match):
         with torch.cuda.stream(stream):
             kps_host.copy_(k.view(-1, 7), non_blocking=True)
             desc_host.copy_(d.view(-1, 32), non_blocking=True)
             match_host.copy_(match.view(-1), non_blocking=True)
         torch.cuda.current_stream().wait_stream(stream)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_times = []
-    for _ in range(args.steps):
-        flush.zero_()
+    def step_copies():
+        with torch.cuda.stream(stream):
+            for s_, p_ in zip(staging, pinned):
+                s_.copy_(p_, non_blocking=True)
+            mps_stage.copy_(mps_host, non_blocking=True)
+            mpd_stage.copy_(mpd_host, non_blocking=True)
+        k, d, c = batch.extract(staging, nfs, wait=False)
+        match, nm = proj.search(mps_stage, mpd_stage, [NMAPPOINTS] * NFRAMES, TH)
+        batch.wait()
+        readback(k, d, match)
+
+    def step_inplace():
+        k, d, c = batch.extract(pinned, nfs, wait=False)
+        match, nm = proj.search(mps_host, mpd_host, [NMAPPOINTS] * NFRAMES, TH)
+        batch.wait()
+        readback(k, d, match)
+
+    def timed(step):
+        for _ in range(max(1, args.warmup)):
+            step()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t0)
-    return NFRAMES * args.steps / sum(e2e_times), h2d, d2h
+        t = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step()
+            torch.cuda.synchronize()
+            t.append(time.perf_counter() - t0)
+        return NFRAMES * args.steps / sum(t)
+
+    copies = timed(step_copies)
+    inplace = timed(step_inplace)
+    return max(copies, inplace), h2d, d2h, {"host_buffers_read_in_place": inplace, "one_copy_per_buffer": copies}
 
 
 def run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev):
@@ -371,11 +390,13 @@ def finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, p
         "config": {"workload": "batched extraction + SearchByProjection, 64 frames mixed 640x480/752x480/1241x376/"
                                "1280x720, nFeatures 1000/1500/2000, 3000 map points per frame, radius 15*scale",
                    "frames_per_step": NFRAMES, "l2": "flushed (256 MiB write) between timed steps",
-                   "launch_shapes": {k: v["value"] for k, v in tuning.items() if k != "search_rounds"},
+                   "launch_shapes": {k: v["value"] for k, v in tuning.items() if k not in ("search_rounds", "e2e_ways")},
                    "launch_shapes_by": "pinned (--shapes)" if args.shapes else
                    "autotuner (stage events, this device and workload)",
-                   "search_rounds_slowest_frame": tuning.get("search_rounds")},
-        "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                   "search_rounds_slowest_frame": tuning.get("search_rounds"),
+                   "autotune_stage_ms": {k: v["ms"] for k, v in tuning.items() if isinstance(v, dict) and "ms" in v}},
+        "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ways": tuning.get("e2e_ways")},
         "per_frame_path_fps": per_frame_fps, "per_frame_split": per_frame_split,
         "batched_over_per_frame": value / per_frame_fps if per_frame_fps else None, "other_configs": extra,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,

@@ -91,7 +91,9 @@ void* orbgpu_extractor_stream(const orbgpu_extractor* ex);
 /* Many frames of uneven size through one pipeline: a ragged list of
  * (frame, level) and (frame, level, cell) work items processed by one launch
  * per stage, replayed as a CUDA graph when the frame list repeats.
- * images: device pointers (one per frame), widths/heights/steps per frame.
+ * images: one pointer per frame to device memory or to page-locked host
+ * memory (read in place over the host link by the first kernel of the
+ * pipeline), widths/heights/steps per frame.
  * Output for frame f starts at keypoints + f * per_frame_capacity (and the
  * same row of descriptors); n_keypoints[f] receives its count (device or
  * host per out_mem). */

@@ -20,7 +20,8 @@ extern "C" {
 /* SearchByProjection(Frame&, vector<MapPoint*>, th) (src/ORBmatcher.cc:72-183)
  * for every frame of the last orbgpu_batch_extract call, in one pass.
  * kps / desc / counts: that call's device outputs.  mappoints /
- * mp_descriptors: all frames' map points back to back (device), frame f
+ * mp_descriptors: all frames' map points back to back (device memory or
+ * page-locked host memory, read in place), frame f
  * owning [mp_offsets[f], mp_offsets[f + 1]) (host array of nframes + 1).
  * match_out: device, nframes * per_frame_capacity ints (map point index
  * within the frame, -1 none, -3 past the frame's keypoints); nmatches:
