@@ -160,10 +160,9 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 
 // Level l (l >= 1) from level l-1: cv::resize INTER_LINEAR in 11-bit fixed
 // point.  Lane k (k < 30) of the strip's warp produces columns
-// [x0 + 4k, x0 + 4k + 4) of the strip's rows.  A source row is interpolated
-// horizontally once for the (on average 1.2) output rows that use it: one
+// [x0 + 4k, x0 + 4k + 4) of the strip's rows.  The horizontal pass is one
 // dp2a per pixel on the two source bytes that a prmt picks from the lane's
-// source words, which are loaded one row ahead.  Weights come in pairs
+// source words, which are loaded two rows ahead.  Weights come in pairs
 // summing to 2047..2049 (checked when the tables are built), so the
 // vertical sum 4 (h0 b0 + h1 b1) + 2^23 stays below 2^32 and its byte 3 is
 // (h0 b0 + h1 b1 + 2^21) >> 22.
@@ -231,8 +230,6 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
     };
 
     const int nrows = min(TH, h - y0);
-    uint32_t ha[4] = {0, 0, 0, 0}, hb[4] = {0, 0, 0, 0};
-    int ca = -1, cb = -1;
     // source words of output rows i (set i & 1) and i + 1, loaded two rows ahead
     uint32_t pw[2][6];
     {
@@ -243,37 +240,12 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
         source_words(e1.y, pw[1][3], pw[1][4], pw[1][5]);
     }
     uint8_t* out = d.dst + (size_t)y0 * d.pitch + X;
+    // both source rows interpolated every row: no data-dependent branch
     auto row_step = [&](int i, uint32_t* cur) {
         const int4 e = rows[i];
-        uint32_t na[4], nb[4];
-        if (e.x == ca) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) na[j] = ha[j];
-        } else if (e.x == cb) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) na[j] = hb[j];
-        } else {
-            hinterp(e.x, cur[0], cur[1], cur[2], na);
-        }
-        if (e.y == cb) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) nb[j] = hb[j];
-        } else if (e.y == ca) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) nb[j] = ha[j];
-        } else if (e.y == e.x) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) nb[j] = na[j];
-        } else {
-            hinterp(e.y, cur[3], cur[4], cur[5], nb);
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            ha[j] = na[j];
-            hb[j] = nb[j];
-        }
-        ca = e.x;
-        cb = e.y;
+        uint32_t ha[4], hb[4];
+        hinterp(e.x, cur[0], cur[1], cur[2], ha);
+        hinterp(e.y, cur[3], cur[4], cur[5], hb);
         const int4 e2 = rows[min(i + 2, TH)];
         source_words(e2.x, cur[0], cur[1], cur[2]);
         source_words(e2.y, cur[3], cur[4], cur[5]);

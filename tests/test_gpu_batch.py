@@ -146,6 +146,53 @@ def test_async_extraction_then_search_matches_the_synchronous_path(torch, oracle
     assert lib().orbgpu_batch_wait(b._h) == 0  # reported once
 
 
+def test_pinned_host_images_read_in_place(torch):
+    """Page-locked host images (and map points) go straight into the batch
+    calls: the same keypoints, descriptors and matches as device copies."""
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchProjection
+    b = BatchExtractor(6, 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    fr = frames(13, 4)
+    nfs = [nf for _, nf in fr]
+    dev = [torch.from_numpy(img).cuda() for img, _ in fr]
+    host = [torch.from_numpy(img).pin_memory() for img, _ in fr]
+    k, d, c = b.extract(dev, nfs)
+    ref = (k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap), d.cpu().numpy().reshape(len(fr), cap, 32),
+           c.cpu().numpy().copy())
+    rng = np.random.default_rng(2)
+    mps, mpd, counts = [], [], []
+    for f in range(len(fr)):
+        n = int(ref[2][f])
+        src = rng.integers(0, n, 500)
+        m = np.zeros(500, MAPPOINT_DTYPE)
+        m["proj_x"] = ref[0][f, src]["x"] + rng.normal(0, 2, 500)
+        m["proj_y"] = ref[0][f, src]["y"] + rng.normal(0, 2, 500)
+        m["proj_xr"] = -1
+        m["view_cos"] = 1.0
+        m["track_scale_level"] = ref[0][f, src]["octave"]
+        m["track_in_view"] = 1
+        mps.append(m)
+        mpd.append(ref[1][f, src] ^ np.packbits(rng.random((500, 256)) < 0.1, axis=1, bitorder="little"))
+        counts.append(500)
+    mps_b = np.concatenate(mps).view(np.uint8)
+    mpd_b = np.ascontiguousarray(np.concatenate(mpd))
+    p = BatchProjection(b, 0.8)
+    m_dev, nm_dev = p.search(torch.from_numpy(mps_b).cuda(), torch.from_numpy(mpd_b).cuda(), counts, 6.0)
+    m_dev, nm_dev = m_dev.cpu().numpy().copy(), nm_dev.cpu().numpy().copy()
+    k, d, c = b.extract(host, nfs, wait=False)
+    m_h, nm_h = p.search(torch.from_numpy(mps_b).pin_memory(), torch.from_numpy(mpd_b).pin_memory(), counts, 6.0)
+    b.wait()
+    assert np.array_equal(c.cpu().numpy(), ref[2])
+    kk = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    dd = d.cpu().numpy().reshape(len(fr), cap, 32)
+    for f in range(len(fr)):
+        n = int(ref[2][f])
+        assert np.array_equal(kk[f, :n], ref[0][f, :n]) and np.array_equal(dd[f, :n], ref[1][f, :n]), f"frame {f}"
+    assert np.array_equal(nm_h.cpu().numpy(), nm_dev)
+    assert np.array_equal(m_h.cpu().numpy(), m_dev)
+
+
 @pytest.mark.parametrize("dz,mono,ori", [(0.0, True, True), (2.0, False, True), (-2.0, False, False)])
 def test_batch_frame_projection_vs_oracle(torch, oracle, dz, mono, ori):
     """SearchByProjection(CurrentFrame, LastFrame) for every frame of a batch,
