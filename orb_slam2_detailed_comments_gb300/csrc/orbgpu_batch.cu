@@ -732,31 +732,32 @@ __global__ void k_bproj_round(const orbgpu_keypoint* kps, int cap, const int* co
 // The same fixed-point resolution with one block per frame and the whole
 // frame in shared memory: the map points' candidate keys (32 bits: distance,
 // GetFeaturesInArea cell, keypoint index -- the lexicographic order of the
-// 64-bit keys), the keypoints' octaves, the results and two claim arrays.
-// A thread evaluates its map points with the reference's best / second-best
-// loop over the candidates not claimed by an earlier map point of the
-// previous round; rounds repeat until one changes nothing (at most M + 1
-// rounds: round r fixes the first r + 1 map points).  Used when every frame
-// fits; the global-memory rounds above handle the rest.
+// 64-bit keys, all distinct), the keypoints' octaves, the results and two
+// claim arrays.  A map point's result is the best and second-best of its
+// candidates not claimed by an earlier map point in the previous round, i.e.
+// the first two such in key order: each thread keeps the four smallest keys
+// of its map points in registers and reads the whole list only when fewer
+// than two of them are unclaimed.  Rounds repeat until one changes nothing
+// (at most M + 1 rounds: round r fixes the first r + 1 map points).  Used
+// when every frame's candidates fit (smem_bytes of dynamic shared memory);
+// the global-memory rounds above handle the rest.
+#define BPROJ_MPT 4  // map points per thread with register top-4 lists (1024 threads: M <= 4096)
 __global__ void __launch_bounds__(1024)
     k_bproj_resolve_smem(const orbgpu_keypoint* kps, int cap, const int* counts, const int* mp_off, int slot_cap,
-                         const uint64_t* slots, const int* slot_count, float nnratio, int t_cap, int* match_out,
-                         int* nmatches, int* status) {
+                         const uint64_t* slots, const int* slot_count, float nnratio, int smem_bytes,
+                         int* match_out, int* nmatches, int* status) {
     extern __shared__ __align__(16) int s_dyn[];
     __shared__ int s_scan[32];
     __shared__ int s_flag[3];
     const int f = blockIdx.x;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
     const int mp0 = mp_off[f], M = mp_off[f + 1] - mp0;
     const int n = min(counts[f], cap);
-    int* s_start = s_dyn;                 // M + 1
-    int* s_res = s_start + (M + 1);       // M
-    int* cr = s_res + M;                  // cap: claims of the previous round
-    int* cw = cr + cap;                   // cap: claims of this round
-    uint32_t* s_key = reinterpret_cast<uint32_t*>(cw + cap);  // t_cap
-    uint8_t* s_oct = reinterpret_cast<uint8_t*>(s_key + t_cap);  // cap
+    constexpr int NONE = 0x7fffffff;
+    constexpr uint32_t NOKEY = 0xFFFFFFFFu;
+    int* s_start = s_dyn;  // M + 1: candidate list of map point i
     int base = 0;
-    for (int i0 = 0; i0 < M; i0 += blockDim.x) {
+    for (int i0 = 0; i0 < M; i0 += nt) {
         const int i = i0 + tid;
         const int v = i < M ? min(slot_count[mp0 + i], slot_cap) : 0;
         int tot;
@@ -764,62 +765,134 @@ __global__ void __launch_bounds__(1024)
         if (i < M) s_start[i] = base + ex;
         base += tot;
     }
-    if (base > t_cap) {  // the host sized t_cap from these counts
+    if (4L * (2 * M + 1 + 2 * cap + base) + cap + 16 > smem_bytes) {  // the frame's candidates do not fit
         if (tid == 0) atomicOr(status + 2, 1);
         return;
     }
+    int* s_res = s_start + (M + 1);                          // M
+    int* cr = s_res + M;                                     // cap: claims of the previous round
+    int* cw = cr + cap;                                      // cap: claims of this round
+    uint32_t* s_key = reinterpret_cast<uint32_t*>(cw + cap);  // base
+    uint8_t* s_oct = reinterpret_cast<uint8_t*>(s_key + base);  // cap
     if (tid == 0) s_start[M] = base;
     if (tid < 3) s_flag[tid] = 0;
+    for (int k = tid; k < cap; k += nt) {
+        cr[k] = NONE;
+        cw[k] = NONE;
+    }
+    for (int k = tid; k < n; k += nt) s_oct[k] = (uint8_t)kps[(size_t)f * cap + k].octave;
     __syncthreads();
-    // every candidate entry by one thread (its map point by binary search over
-    // the list starts), so all the slot loads are independent
-    for (int t = tid; t < base; t += blockDim.x) {
-        int lo = 0, hi = M - 1;  // last i with s_start[i] <= t
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_start[mid] <= t) lo = mid;
-            else hi = mid - 1;
+    // keys, one thread per map point (independent loads); the four smallest of
+    // the thread's first BPROJ_MPT map points kept in registers
+    uint32_t top[BPROJ_MPT][4];
+    int tcnt[BPROJ_MPT];
+#pragma unroll
+    for (int q = 0; q < BPROJ_MPT; q++) {
+        tcnt[q] = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) top[q][j] = NOKEY;
+    }
+    for (int i = tid, q = 0; i < M; i += nt, q++) {
+        const int s0 = s_start[i], cnt = s_start[i + 1] - s0;
+        const uint64_t* S = slots + (size_t)(mp0 + i) * slot_cap;
+        uint32_t t0 = NOKEY, t1 = NOKEY, t2 = NOKEY, t3 = NOKEY;
+        for (int b = 0; b < cnt; b++) {
+            const uint64_t key = S[b];
+            const uint32_t dist = (uint32_t)(key >> 40), cell = (uint32_t)(key >> 20) & 0xFFFFFu,
+                           idx = (uint32_t)key & 0xFFFFFu;
+            const uint32_t k32 = dist >= 256 ? NOKEY : (dist << 24) | (cell << 12) | idx;
+            s_key[s0 + b] = k32;
+            // insertion into the sorted four
+            if (k32 < t3) {
+                if (k32 < t2) {
+                    t3 = t2;
+                    if (k32 < t1) {
+                        t2 = t1;
+                        if (k32 < t0) {
+                            t1 = t0;
+                            t0 = k32;
+                        } else {
+                            t1 = k32;
+                        }
+                    } else {
+                        t2 = k32;
+                    }
+                } else {
+                    t3 = k32;
+                }
+            }
         }
-        const uint64_t key = slots[(size_t)(mp0 + lo) * slot_cap + (t - s_start[lo])];
-        const uint32_t dist = (uint32_t)(key >> 40), cell = (uint32_t)(key >> 20) & 0xFFFFFu,
-                       idx = (uint32_t)key & 0xFFFFFu;
-        s_key[t] = dist >= 256 ? 0xFFFFFFFFu : (dist << 24) | (cell << 12) | idx;
+#pragma unroll
+        for (int qq = 0; qq < BPROJ_MPT; qq++)
+            if (qq == q) {
+                top[qq][0] = t0;
+                top[qq][1] = t1;
+                top[qq][2] = t2;
+                top[qq][3] = t3;
+                tcnt[qq] = cnt;
+            }
+        s_res[i] = -2;
     }
-    for (int k = tid; k < n; k += blockDim.x) s_oct[k] = (uint8_t)kps[(size_t)f * cap + k].octave;
-    for (int i = tid; i < M; i += blockDim.x) s_res[i] = -2;
-    for (int k = tid; k < cap; k += blockDim.x) {
-        cr[k] = 0x7fffffff;
-        cw[k] = 0x7fffffff;
-    }
+    // map point i's result from claims cr: the first two candidates in key
+    // order that no earlier map point claimed
+    auto decide = [&](int i, uint32_t best, uint32_t second) -> int {
+        if (best == NOKEY) return -1;
+        const int bestDist = (int)(best >> 24);
+        const int bestIdx = (int)(best & 0xFFFu);
+        const int bestLevel = s_oct[bestIdx];
+        const int bestDist2 = second == NOKEY ? 256 : (int)(second >> 24);
+        const int bestLevel2 = second == NOKEY ? -1 : s_oct[second & 0xFFFu];
+        if (bestDist <= ORBGPU_TH_HIGH && !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
+            return bestIdx;
+        return -1;
+    };
+    auto full_scan = [&](int i, uint32_t& best, uint32_t& second) {
+        best = NOKEY;
+        second = NOKEY;
+        for (int e = s_start[i]; e < s_start[i + 1]; e++) {
+            const uint32_t key = s_key[e];
+            if (key == NOKEY || cr[key & 0xFFFu] < i) continue;
+            if (key < best) {
+                second = best;
+                best = key;
+            } else if (key < second) {
+                second = key;
+            }
+        }
+    };
     bool converged = M == 0;
     int rounds_run = 0;
     for (int round = 0; round <= M + 1 && !converged; round++) {
         rounds_run = round + 1;
         if (tid == 0) s_flag[(round + 1) % 3] = 0;
         __syncthreads();
-        for (int i = tid; i < M; i += blockDim.x) {
-            uint32_t best = 0xFFFFFFFFu, second = 0xFFFFFFFFu;
-            for (int e = s_start[i]; e < s_start[i + 1]; e++) {
-                const uint32_t key = s_key[e];
-                if (key == 0xFFFFFFFFu || cr[key & 0xFFFu] < i) continue;
-                if (key < best) {
-                    second = best;
-                    best = key;
-                } else if (key < second) {
-                    second = key;
+#pragma unroll
+        for (int q = 0; q < BPROJ_MPT; q++) {
+            const int i = tid + q * nt;
+            if (i >= M) continue;
+            uint32_t best = NOKEY, second = NOKEY;
+            int found = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint32_t key = top[q][j];
+                if (found < 2 && key != NOKEY && !(cr[key & 0xFFFu] < i)) {
+                    if (found == 0) best = key;
+                    else second = key;
+                    found++;
                 }
             }
-            int r = -1;
-            if (best != 0xFFFFFFFFu) {
-                const int bestDist = (int)(best >> 24);
-                const int bestIdx = (int)(best & 0xFFFu);
-                const int bestLevel = s_oct[bestIdx];
-                const int bestDist2 = second == 0xFFFFFFFFu ? 256 : (int)(second >> 24);
-                const int bestLevel2 = second == 0xFFFFFFFFu ? -1 : s_oct[second & 0xFFFu];
-                if (bestDist <= ORBGPU_TH_HIGH &&
-                    !(bestLevel == bestLevel2 && (float)bestDist > __fmul_rn(nnratio, (float)bestDist2)))
-                    r = bestIdx;
+            if (found < 2 && tcnt[q] > 4) full_scan(i, best, second);
+            const int r = decide(i, best, second);
+            if (r != s_res[i]) {
+                s_res[i] = r;
+                s_flag[round % 3] = 1;
             }
+            if (r >= 0) atomicMin(&cw[r], i);
+        }
+        for (int i = tid + BPROJ_MPT * nt; i < M; i += nt) {
+            uint32_t best, second;
+            full_scan(i, best, second);
+            const int r = decide(i, best, second);
             if (r != s_res[i]) {
                 s_res[i] = r;
                 s_flag[round % 3] = 1;
@@ -833,17 +906,17 @@ __global__ void __launch_bounds__(1024)
         cr = cw;
         cw = t;
         if (!converged)
-            for (int k = tid; k < cap; k += blockDim.x) cw[k] = 0x7fffffff;
+            for (int k = tid; k < cap; k += nt) cw[k] = NONE;
     }
     if (tid == 0) {
         if (!converged) atomicOr(status + 2, 2);
         atomicMax(status + 3, rounds_run);
     }
     int* Mo = match_out + (size_t)f * cap;
-    for (int k = tid; k < cap; k += blockDim.x) Mo[k] = k < n ? -1 : -3;
+    for (int k = tid; k < cap; k += nt) Mo[k] = k < n ? -1 : -3;
     __syncthreads();
     int nm = 0;
-    for (int i = tid; i < M; i += blockDim.x) {
+    for (int i = tid; i < M; i += nt) {
         const int r = s_res[i];
         if (r >= 0) {
             Mo[r] = i;
@@ -1058,18 +1131,20 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         // to t_cap candidates per frame; the kernel reports a frame above it),
         // else the global-memory fixed-point rounds and the result write-out
         // (serial replay for any frame that did not converge)
-        const size_t fixed = sizeof(int) * ((size_t)2 * max_mp + 1 + 2 * (size_t)cap) + (size_t)cap + 16;
-        const size_t smem_max = 200 * 1024;
+        // s_start, s_res, two claim arrays (ints), octaves and dirty flags
+        // (bytes), then 4 bytes per candidate (6 with the keypoint index):
+        // the kernel lays its frame out once it knows the frame's candidates
+        const size_t fixed = sizeof(int) * ((size_t)2 * max_mp + 1 + 2 * (size_t)cap) + (size_t)cap + (size_t)max_mp + 64;
+        const size_t smem_max = 226 * 1024;  // below the 227 KiB per-block limit with the static part
         if (P.mode == 0 && cap < 4096 && fixed + 4 * 1024 <= smem_max) {
-            const int t_cap = (int)((smem_max - fixed) / sizeof(int));
-            const size_t smem = fixed + sizeof(int) * (size_t)t_cap;
+            const size_t smem = smem_max;
             if (P.smem_attr != (int)smem) {
                 ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bproj_resolve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)smem));
                 P.smem_attr = (int)smem;
             }
             k_bproj_resolve_smem<<<nf, 1024, smem, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio,
-                                                         t_cap, match_out, nmatches, status);
+                                                         (int)smem, match_out, nmatches, status);
             ORBGPU_CUDA_TRY(cudaGetLastError());
             ORBGPU_CUDA_TRY(cudaMemcpyAsync(P.h_pinned, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
             ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
