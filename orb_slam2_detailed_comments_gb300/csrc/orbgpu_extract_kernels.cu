@@ -548,6 +548,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         min_th = max(min_th, 1);
     }
     const int lo_th = min(ini_th, min_th);
+    const uint32_t lo4 = (uint32_t)lo_th * 0x01010101u;
     uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
     uint16_t* smin = s_min[warp];
     int total_ini = 0, total_min = 0;
@@ -558,19 +559,16 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         const uint8_t* row = mstr + (r + 1) * FAST_ROW + 4 * lk;
         if (lr < rpi && r < dh) {
             const uint32_t B = *reinterpret_cast<const uint32_t*>(row);
-            if (B) {
-#pragma unroll
-                for (int jj = 0; jj < 4; jj++) {
-                    const int m = (int)((B >> (8 * jj)) & 0xFFu);
-                    if (m > lo_th) {
-                        const uint8_t* p = row + jj;
-                        int nb = max(max(p[-1], p[1]), max(max(p[-FAST_ROW - 1], p[-FAST_ROW]), p[-FAST_ROW + 1]));
-                        nb = max(nb, max(max(p[FAST_ROW - 1], p[FAST_ROW]), p[FAST_ROW + 1]));
-                        if (m > nb) {
-                            kini |= (uint32_t)(m > ini_th) << jj;
-                            kmin |= (uint32_t)(m > min_th) << jj;
-                        }
-                    }
+            // only the bytes above the lower threshold (about one pixel in 80)
+            for (uint32_t cand = __vcmpgtu4(B, lo4) & 0x80808080u; cand; cand &= cand - 1) {
+                const int jj = (__ffs(cand) - 1) >> 3;
+                const int m = (int)((B >> (8 * jj)) & 0xFFu);
+                const uint8_t* p = row + jj;
+                int nb = max(max(p[-1], p[1]), max(max(p[-FAST_ROW - 1], p[-FAST_ROW]), p[-FAST_ROW + 1]));
+                nb = max(nb, max(max(p[FAST_ROW - 1], p[FAST_ROW]), p[FAST_ROW + 1]));
+                if (m > nb) {
+                    kini |= (uint32_t)(m > ini_th) << jj;
+                    kmin |= (uint32_t)(m > min_th) << jj;
                 }
             }
         }
