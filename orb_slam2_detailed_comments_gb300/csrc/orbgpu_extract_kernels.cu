@@ -331,7 +331,7 @@ __device__ __forceinline__ int rs_arc_strength(const uint8_t* ring, int ic, int 
 }
 
 template <int TH>
-__global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc* descs, RangeMap rm) {
+__global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc* descs, RangeMap rm) {
     static_assert((TH + 6) % 7 == 0, "TH + 6 rows must be whole blocks of 7");
     constexpr int NB = (TH + 6) / 7;
     __shared__ __align__(16) StripShared<TH> sh_all[RS_WPB];
