@@ -507,6 +507,23 @@ def bench_serving(dev, duration_s=3.0):
     return st
 
 
+def host_info():
+    """The host the CPU baseline ran on: CPU model, cores, C library."""
+    import platform
+    model = platform.processor() or platform.machine()
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    lib, ver = platform.libc_ver()
+    return {"cpu": model, "machine": platform.machine(), "nproc": os.cpu_count(), "libc": f"{lib} {ver}".strip()}
+
+
 def cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1):
     """Frames/s of the CPU restatement (extraction + projection search) on a
     bounded sample of the workload."""
@@ -540,7 +557,8 @@ def cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1):
         t.join()
     el = time.perf_counter() - t0
     return {"value": done[0] / el, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"{done[0]} frames of the workload (extraction + SearchByProjection) in {el:.1f} s"}
+            "sample": f"{done[0]} frames of the workload (extraction + SearchByProjection) in {el:.1f} s",
+            "host": host_info()}
 
 
 def run_reference(args):
@@ -577,7 +595,8 @@ def run_reference(args):
             "config": {"workload": "batched extraction + SearchByProjection, 64 frames mixed 640x480/752x480/"
                                    "1241x376/1280x720, nFeatures 1000/1500/2000, 3000 map points per frame"},
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": f"first {nsample} frames of the workload, 8 s per step on {threads} threads"},
+                             "sample": f"first {nsample} frames of the workload, 8 s per step on {threads} threads",
+                             "host": host_info()},
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
