@@ -158,3 +158,45 @@ def test_fast_stage_per_level(torch, oracle):
         assert lib().orbgpu_debug_fast_strength(ptr(dimg), w, w, h, 7, ptr(smap)) == 0
         sm = smap.cpu().numpy().astype(np.int64)
         assert np.array_equal(sm[gy + 16, gx + 16] - 1, gs), lvl
+
+
+# scale factor (2.5: the resize's source span exceeds the 8-byte fast path),
+# level count, iniThFAST / minThFAST (swapped, and zero: the one-pass cell
+# suppression's threshold rule)
+PARAMS = [(2.5, 4, 20, 7), (1.5, 6, 7, 20), (1.2, 8, 20, 0), (1.2, 3, 0, 0)]
+
+
+@pytest.mark.parametrize("scale,nlevels,ini,mn", PARAMS)
+def test_extractor_parameters_vs_oracle(torch, oracle, scale, nlevels, ini, mn):
+    from orb_slam2_detailed_comments_gb300 import ORBextractor
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    for w, h, seed in [(640, 480, 21), (1241, 376, 22)]:
+        img = syn.scene(w, h, seed)
+        ex = ORBextractor(1000, scale, nlevels, ini, mn)
+        kps, desc = ex(img)
+        ref = oracle.extract(img, nfeatures=1000, scale_factor=scale, nlevels=nlevels, ini_th=ini, min_th=mn)
+        levels = ex.pyramid_numpy()
+        for l, (a, b) in enumerate(zip(levels, ref.pyramid)):
+            assert a.shape == b.shape and np.array_equal(a, b), f"{w}x{h} pyramid level {l}"
+        assert_kps_equal(kps, ref.keypoints, f"{w}x{h} scale {scale} th {ini}/{mn}")
+        assert np.array_equal(desc, ref.descriptors)
+
+
+@pytest.mark.parametrize("scale,nlevels,ini,mn", PARAMS)
+def test_batch_parameters_vs_oracle(torch, oracle, scale, nlevels, ini, mn):
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    fr = [(syn.scene(640, 480, 31), 1000), (syn.scene(1241, 376, 32), 1500), (syn.scene(320, 240, 33), 500)]
+    b = BatchExtractor(4, 1280, 720, 2000, scale_factor=scale, nlevels=nlevels, ini_th=ini, min_th=mn)
+    cap = b.per_frame_capacity
+    k, d, c = b.extract([torch.from_numpy(img).cuda() for img, _ in fr], [nf for _, nf in fr])
+    k = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    d = d.cpu().numpy().reshape(len(fr), cap, 32)
+    c = c.cpu().numpy()
+    for f, (img, nf) in enumerate(fr):
+        ref = oracle.extract(img, nfeatures=nf, scale_factor=scale, nlevels=nlevels, ini_th=ini, min_th=mn,
+                             want_pyramid=False)
+        assert c[f] == len(ref.keypoints), f"frame {f}"
+        assert_kps_equal(k[f, :c[f]], ref.keypoints, f"frame {f}")
+        assert np.array_equal(d[f, :c[f]], ref.descriptors)
