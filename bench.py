@@ -255,7 +255,8 @@ def run_ours(args):
     if "perframe" in legs:
         per_frame_fps, per_frame_split = run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev)
     extra = {}
-    for leg, fn in (("stereo", bench_stereo), ("knn", bench_knn), ("serving", bench_serving)):
+    for leg, fn in (("stereo", bench_stereo), ("knn", bench_knn), ("serving", bench_serving),
+                    ("distinctive", bench_distinctive)):
         if leg in legs:
             try:
                 extra[LEG_KEYS[leg]] = fn(dev)
@@ -266,8 +267,9 @@ def run_ours(args):
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
 
 
-LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "cpu"}
-LEG_KEYS = {"stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams"}
+LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "distinctive", "cpu"}
+LEG_KEYS = {"stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams",
+            "distinctive": "distinctive_descriptors_1M_mappoints"}
 
 
 def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev, nfs, cap):
@@ -464,6 +466,87 @@ def bench_knn(dev):
     return out
 
 
+def bench_distinctive(dev, steps=10, warmup=3):
+    """MapPoint::ComputeDistinctiveDescriptors over 1,000,000 map points: lists
+    of 1-64 observations (geometric, mean 6), 5% bad keyframes, 2% empty lists,
+    over a 5.9M-row descriptor pool (every observation a noisy copy of its map
+    point's descriptor, 1/8 of the bits flipped), descriptors written back.
+    Device-resident (kernel events, L2 flushed between launches), end to end
+    from page-locked host buffers, and the oracle on one host core."""
+    import torch
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import compute_distinctive_descriptors
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    m = 1_000_000
+    pool, offsets, rows = syn.observation_case(m, 2024, mean_len=6.0, max_len=64)
+    n_valid = int((rows >= 0).sum())
+    has_valid = np.zeros(m, bool)
+    np.logical_or.at(has_valid, np.repeat(np.arange(m), np.diff(offsets)), rows >= 0)
+    chosen = int(has_valid.sum())
+    # algorithmic bytes: offsets, rows, each valid observation's descriptor once,
+    # best rows, the chosen descriptors
+    alg_bytes = 4 * (m + 1) + 4 * len(rows) + 32 * n_valid + 4 * m + 32 * chosen
+    P, O, R = (torch.from_numpy(a).to(dev) for a in (pool, offsets, rows))
+    D = torch.zeros((m, 32), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        best = compute_distinctive_descriptors(P, O, R, D, validate=False)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        best = compute_distinctive_descriptors(P, O, R, D, validate=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    dev_ms = statistics.median(ms)
+    gpu_best = best.cpu().numpy()
+    # end to end: host arrays in page-locked memory, (a) copied in and the
+    # results copied out, (b) read in place by the kernel (results copied out)
+    hP, hO, hR = (torch.from_numpy(a).pin_memory() for a in (pool, offsets, rows))
+    hB = torch.empty(m, dtype=torch.int32).pin_memory()
+    hD = torch.empty((m, 32), dtype=torch.uint8).pin_memory()
+    ways = {}
+    for way in ("copies", "in_place"):
+        for it in range(warmup + steps):
+            if it == warmup:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+            if way == "copies":
+                P.copy_(hP, non_blocking=True)
+                O.copy_(hO, non_blocking=True)
+                R.copy_(hR, non_blocking=True)
+                b = compute_distinctive_descriptors(P, O, R, D, validate=False)
+            else:
+                b = compute_distinctive_descriptors(hP, hO, hR, D, validate=False)
+            hB.copy_(b, non_blocking=True)
+            hD.copy_(D, non_blocking=True)
+            torch.cuda.current_stream(dev).synchronize()
+        ways[way] = m * steps / (time.perf_counter() - t0)
+    h2d = pool.nbytes + offsets.nbytes + rows.nbytes
+    d2h = 4 * m + 32 * m
+    # the oracle (src/MapPoint.cc:365-447 restated) on the same workload, one core
+    o = pyoracle.Oracle()
+    t0 = time.perf_counter()
+    cpu_best, _ = o.distinctive_descriptors(pool, offsets, rows)
+    cpu_s = time.perf_counter() - t0
+    pk, pk_src = peaks()
+    achieved = alg_bytes / (dev_ms / 1e3) / 1e9
+    return {"metric": "map points/s (ComputeDistinctiveDescriptors)", "map_points": m, "observations": len(rows),
+            "value": m / (dev_ms / 1e3), "ms": dev_ms, "gpu_launches_per_step": 1,
+            "e2e": {"value": max(ways.values()), "unit": "map points/s", "ways": ways,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": "k_distinctive_descriptors", "achieved": achieved,
+                         "peak": pk.get("hbm_gbs"), "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                         "algorithmic_bytes_per_step": alg_bytes, "peak_source": pk_src},
+            "cpu_baseline": {"value": m / cpu_s, "unit": "map points/s", "cores": 1, "kind": "port",
+                             "sample": "the full 1,000,000 map points, oracle restatement"},
+            "equal_to_oracle": bool(np.array_equal(gpu_best, cpu_best))}
+
+
 def bench_serving(dev, duration_s=3.0):
     """32 camera streams, Poisson 30 Hz each, mixed 640x480/1241x376/1280x720,
     nFeatures 1000-2000: every frame is extracted and matched against its
@@ -613,7 +696,8 @@ def main():
     ap.add_argument("--shapes", default="",
                     help="pin the launch shapes resize_rows,fast_cells_per_block,describe_group (no tuning)")
     ap.add_argument("--legs", default="all",
-                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,cpu) or 'all'")
+                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,distinctive,cpu) "
+                         "or 'all'")
     args = ap.parse_args()
     NFRAMES = args.frames
     if args.impl == "reference":

@@ -254,6 +254,33 @@ int orbgpu_knn2_noalloc(const uint8_t* query, int nq, const uint8_t* train, int 
 /* ORBmatcher::DescriptorDistance for n row pairs (device arrays). */
 int orbgpu_descriptor_distance(const uint8_t* a, const uint8_t* b, int n, int* out, void* stream);
 
+/* MapPoint::ComputeDistinctiveDescriptors (src/MapPoint.cc:365-447) for m map
+ * points in one launch.  Each map point's observations are a list of rows of
+ * a descriptor pool (pool_rows x 32 bytes: the observing keyframes'
+ * mDescriptors, e.g. their extraction outputs left resident), given in CSR
+ * form -- map point i owns obs_rows[obs_offsets[i] .. obs_offsets[i + 1]) --
+ * in the order MapPoint::mObservations iterates them; a row of -1 is an
+ * observation whose keyframe is bad (skipped, as KeyFrame::isBad() at
+ * src/MapPoint.cc:391).  For every map point the descriptor with the least
+ * median Hamming distance to the others is chosen, the first such in list
+ * order (the reference's strict '<'), with the median taken as element
+ * (size_t)(0.5 * (N - 1)) of the sorted distance row of the N valid
+ * descriptors.
+ *   best_rows[i]   the chosen pool row; -1 when the list has no valid
+ *                  observation (the reference returns early and keeps
+ *                  mDescriptor); -2 when the list is malformed (a row outside
+ *                  [-1, pool_rows), offsets decreasing, negative or beyond
+ *                  n_obs), where the reference would index out of range.
+ *   descriptors    (nullable, m x 32) the chosen descriptor of every map point
+ *                  with best_rows[i] >= 0; other rows are left unchanged, as
+ *                  mDescriptor is.
+ * No counterpart is needed for the per-map-point call: one list is m = 1.
+ * Arrays may be device memory or page-locked host memory (read in place);
+ * pool and descriptors 16-byte aligned.  Asynchronous on 'stream' (NULL = the
+ * legacy default stream); one kernel launch, no allocation. */
+int orbgpu_distinctive_descriptors(const uint8_t* pool, int pool_rows, const int* obs_offsets, const int* obs_rows,
+                                   int n_obs, int m, int* best_rows, uint8_t* descriptors, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

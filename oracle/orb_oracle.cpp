@@ -850,6 +850,62 @@ int orc_distribute(const orc_kp* cand, int n, int minX, int maxX, int minY, int 
     return (int)r.size();
 }
 
+// MapPoint::ComputeDistinctiveDescriptors, src/MapPoint.cc:365-447, for m
+// map points given as ragged lists of pool rows in observation order (the
+// iteration order of MapPoint::mObservations).  A row of -1 stands for an
+// observation whose keyframe is bad (skipped at :391-394).  The reference
+// collects the valid descriptors, fills the symmetric N x N table of
+// DescriptorDistance values (:403-420), sorts each row, takes element
+// (size_t)(0.5 * (N - 1)) as that descriptor's median (:427-434) and keeps
+// the first descriptor with the least median (:437-441, strict <).
+// best_rows[i] = the chosen pool row, -1 when no observation is valid (the
+// reference returns early and leaves mDescriptor as it was), -2 for an
+// invalid list (a row outside [-1, pool_rows) or a decreasing offset).
+// desc_inout (nullable) receives the chosen row's 32 bytes where
+// best_rows[i] >= 0 and is left unchanged elsewhere.
+int orc_distinctive_descriptors(const uint8_t* pool, int pool_rows, const int* offsets, const int* rows, int m,
+                                int* best_rows, uint8_t* desc_inout) {
+    for (int i = 0; i < m; i++) {
+        const int o0 = offsets[i], o1 = offsets[i + 1];
+        bool bad_input = o1 < o0;
+        std::vector<int> valid;
+        for (int t = o0; t < o1 && !bad_input; t++) {
+            if (rows[t] < -1 || rows[t] >= pool_rows) bad_input = true;
+            else if (rows[t] >= 0) valid.push_back(rows[t]);
+        }
+        if (bad_input) {
+            best_rows[i] = -2;
+            continue;
+        }
+        if (valid.empty()) {
+            best_rows[i] = -1;
+            continue;
+        }
+        const size_t N = valid.size();
+        std::vector<std::vector<int> > dist(N, std::vector<int>(N, 0));
+        for (size_t a = 0; a < N; a++)
+            for (size_t b = a + 1; b < N; b++) {
+                const int d = hamming(pool + (size_t)valid[a] * 32, pool + (size_t)valid[b] * 32);
+                dist[a][b] = d;
+                dist[b][a] = d;
+            }
+        int best_median = INT_MAX;
+        size_t best = 0;
+        for (size_t a = 0; a < N; a++) {
+            std::vector<int> row = dist[a];
+            std::sort(row.begin(), row.end());
+            const int median = row[(size_t)(0.5 * (N - 1))];
+            if (median < best_median) {
+                best_median = median;
+                best = a;
+            }
+        }
+        best_rows[i] = valid[best];
+        if (desc_inout) std::memcpy(desc_inout + (size_t)i * 32, pool + (size_t)valid[best] * 32, 32);
+    }
+    return 0;
+}
+
 void orc_sincos_table(const float* x, int n, float* c, float* s) {
     for (int i = 0; i < n; i++) {
         c[i] = cosf(x[i]);

@@ -45,6 +45,13 @@ int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const ui
                                const uint8_t* pyrR, const int* level_w, const int* level_h, int w, int h, float bf,
                                float fx, float* uright, float* depth);
 int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int* d1, int* idx2, int* d2);
+/* MapPoint::ComputeDistinctiveDescriptors (src/MapPoint.cc:365-447) over
+ * ragged observation lists of pool rows (-1 = observation of a bad keyframe).
+ * best_rows: chosen row, -1 none valid, -2 invalid list (the harness version
+ * reports -3: the reference exposes only the descriptor).  desc_inout
+ * (nullable) gets the chosen descriptor, unchanged where best_rows < 0. */
+int orc_distinctive_descriptors(const uint8_t* pool, int pool_rows, const int* offsets, const int* rows, int m,
+                                int* best_rows, uint8_t* desc_inout);
 
 /* Stage-level checkers for the kernel tests. */
 /* 7x7 sigma-2 blur of one level (GaussianBlur, src/ORBextractor.cc:1607-1615). */

@@ -228,6 +228,22 @@ class _Base:
         return tuple(o[:nq].copy() for o in outs)
 
 
+    def distinctive_descriptors(self, pool, offsets, rows, initial=None):
+        """MapPoint::ComputeDistinctiveDescriptors over ragged observation lists
+        (src/MapPoint.cc:365-447); returns (best_rows, descriptors)."""
+        pool = np.ascontiguousarray(pool, np.uint8).reshape(-1, 32)
+        offsets = np.ascontiguousarray(offsets, np.int32)
+        rows = np.ascontiguousarray(rows, np.int32)
+        m = len(offsets) - 1
+        best = np.zeros(max(m, 1), np.int32)
+        desc = (np.zeros((max(m, 1), 32), np.uint8) if initial is None
+                else np.ascontiguousarray(np.array(initial, np.uint8).reshape(-1, 32)))
+        f = self.fn("distinctive_descriptors")
+        f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        f(_p(pool), len(pool), _p(offsets), _p(rows), m, _p(best), _p(desc))
+        return best[:m].copy(), desc[:m].copy()
+
+
 class Oracle(_Base):
     def __init__(self, path: str = ORACLE_SO):
         super().__init__(path)

@@ -1,7 +1,8 @@
 // ORACLE / TEST INFRASTRUCTURE ONLY.
 //
 // C entry points around the reference's own, unmodified ORB-SLAM2 sources
-// (src/ORBextractor.cc, src/ORBmatcher.cc, src/Frame.cc), compiled against the
+// (src/ORBextractor.cc, src/ORBmatcher.cc, src/Frame.cc, src/MapPoint.cc),
+// compiled against the
 // cv stand-in in ../cvshim.  Used to pin the oracle restatement
 // (../orb_oracle.cpp) and to generate the golden fixtures under tests/golden.
 //
@@ -29,12 +30,15 @@
 
 #include <opencv2/core/core.hpp>
 
-// The harness needs Frame::AssignFeaturesToGrid (private) and
-// MapPoint::mDescriptor (protected) to build frames and map points from
-// recorded keypoints; the reference files themselves are compiled unchanged.
+// The harness needs Frame::AssignFeaturesToGrid (private), MapPoint's
+// protected fields and KeyFrame::mbBad (protected) to build frames, keyframes
+// and map points from recorded data; the reference files themselves are
+// compiled unchanged.
 #define private public
 #define protected public
 #include "Frame.h"
+#include "KeyFrame.h"
+#include "Map.h"
 #include "MapPoint.h"
 #include "ORBextractor.h"
 #include "ORBmatcher.h"
@@ -137,6 +141,32 @@ std::vector<cv::KeyPoint> kps_in(const orc_kp* kps, int n) {
                             kps[i].class_id);
     return v;
 }
+
+// Map points built through the reference's own constructor
+// (src/MapPoint.cc:39-67), which reads its reference keyframe's ids and locks
+// the map's point-creation mutex: one map and one reference keyframe per
+// harness call.  The matchers read only Observations() > 0 of a map point, so
+// make() sets nObs directly.
+struct MapPointMaker {
+    Map* map;
+    Frame* frame;
+    KeyFrame* kf;
+    MapPointMaker() : map(new Map()), frame(new Frame()) {
+        frame->mnId = 0;
+        frame->N = 0;
+        kf = new KeyFrame(*frame, map, nullptr);
+    }
+    ~MapPointMaker() {
+        delete kf;
+        delete frame;
+        delete map;
+    }
+    MapPoint* make(const cv::Mat& pos, int nobs) {
+        MapPoint* mp = new MapPoint(pos, kf, map);
+        mp->nObs = nobs;
+        return mp;
+    }
+};
 
 // A Frame as the reference's constructors leave it (src/Frame.cc:313-393 for
 // an image without distortion), built from recorded keypoints/descriptors.
@@ -295,11 +325,12 @@ int ref_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8
         ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
         Frame* F = make_frame(&ext, kps, desc, n, w, h, uright);
         cv::Mat pos = cv::Mat::zeros(3, 1, CV_32F);
-        MapPoint* preclaimed = new MapPoint(pos, nullptr, nullptr);
+        MapPointMaker maker;
+        MapPoint* preclaimed = maker.make(pos, 1);
         std::vector<MapPoint*> vmp(m);
         std::map<MapPoint*, int> index;
         for (int i = 0; i < m; i++) {
-            MapPoint* mp = new MapPoint(pos, nullptr, nullptr);
+            MapPoint* mp = maker.make(pos, 1);
             mp->mTrackProjX = mps[i].proj_x;
             mp->mTrackProjY = mps[i].proj_y;
             mp->mTrackProjXR = mps[i].proj_xr;
@@ -360,9 +391,9 @@ int ref_search_by_projection_frame(const orc_params* p, const orc_kp* kps, const
         CF->mbf = mo->bf;
         CF->mb = mo->b;
         cv::Mat zero = cv::Mat::zeros(3, 1, CV_32F);
-        MapPoint* preclaimed = new MapPoint(zero, nullptr, nullptr);
-        MapPoint* sentinel = new MapPoint(zero, nullptr, nullptr);
-        sentinel->nObs = 0;
+        MapPointMaker maker;
+        MapPoint* preclaimed = maker.make(zero, 1);
+        MapPoint* sentinel = maker.make(zero, 0);
         std::vector<MapPoint*> owned;
         std::map<MapPoint*, int> index;
         for (int i = 0; i < n_last; i++) {
@@ -373,8 +404,7 @@ int ref_search_by_projection_frame(const orc_params* p, const orc_kp* kps, const
             pos.at<float>(0) = q.x;
             pos.at<float>(1) = q.y;
             pos.at<float>(2) = q.z;
-            MapPoint* mp = new MapPoint(pos, nullptr, nullptr);
-            mp->nObs = (q.flags & ORC_MP_OBSERVED) ? 1 : 0;
+            MapPoint* mp = maker.make(pos, (q.flags & ORC_MP_OBSERVED) ? 1 : 0);
             mp->mDescriptor = cv::Mat(1, 32, CV_8U);
             std::memcpy(mp->mDescriptor.data, last_mp_desc + (size_t)i * 32, 32);
             LF->mvpMapPoints[i] = mp;
@@ -448,6 +478,62 @@ int ref_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
                 else if (d < b2) { b2 = d; i2 = j; }
             }
             idx1[i] = i1; d1[i] = b1; idx2[i] = i2; d2[i] = b2;
+        }
+    }
+    return 0;
+}
+
+// MapPoint::ComputeDistinctiveDescriptors -- src/MapPoint.cc:365-447, run on a
+// real MapPoint whose observations are one keyframe per list entry (each
+// keyframe holding that entry's descriptor as its row 0; a -1 row becomes a
+// keyframe flagged bad).  mObservations is a std::map keyed by KeyFrame*; the
+// arena makes address order equal creation order, so the map iterates in list
+// order.  desc_inout holds each map point's descriptor before the call
+// (zeros when NULL is passed) and receives mDescriptor after it.  best_rows:
+// -2 invalid list (the reference is not run), -1 no valid observation, else
+// -3 (the reference exposes the chosen descriptor, not its index).
+int ref_distinctive_descriptors(const uint8_t* pool, int pool_rows, const int* offsets, const int* rows, int m,
+                                int* best_rows, uint8_t* desc_inout) {
+    ArenaScope scope;
+    {
+        MapPointMaker maker;
+        cv::Mat pos = cv::Mat::zeros(3, 1, CV_32F);
+        for (int i = 0; i < m; i++) {
+            const int o0 = offsets[i], o1 = offsets[i + 1];
+            bool bad_input = o1 < o0, any_valid = false;
+            for (int t = o0; t < o1 && !bad_input; t++) {
+                if (rows[t] < -1 || rows[t] >= pool_rows) bad_input = true;
+                any_valid |= rows[t] >= 0;
+            }
+            if (bad_input) {
+                best_rows[i] = -2;
+                continue;
+            }
+            std::vector<KeyFrame*> kfs;
+            for (int t = o0; t < o1; t++) {
+                Frame f;
+                f.mnId = (long unsigned int)t;
+                f.N = 1;
+                f.mvuRight.assign(1, -1.0f);
+                f.mDescriptors = cv::Mat::zeros(1, 32, CV_8U);
+                if (rows[t] >= 0) std::memcpy(f.mDescriptors.data, pool + (size_t)rows[t] * 32, 32);
+                KeyFrame* kf = new KeyFrame(f, maker.map, nullptr);
+                kf->mbBad = rows[t] < 0;
+                if (!kfs.empty() && kf < kfs.back()) {
+                    std::fprintf(stderr, "ref_distinctive_descriptors: keyframes not in address order\n");
+                    std::abort();
+                }
+                kfs.push_back(kf);
+            }
+            MapPoint* mp = new MapPoint(pos, kfs.empty() ? maker.kf : kfs[0], maker.map);
+            mp->mDescriptor = cv::Mat::zeros(1, 32, CV_8U);
+            if (desc_inout) std::memcpy(mp->mDescriptor.data, desc_inout + (size_t)i * 32, 32);
+            for (KeyFrame* kf : kfs) mp->AddObservation(kf, 0);
+            mp->ComputeDistinctiveDescriptors();
+            if (desc_inout) std::memcpy(desc_inout + (size_t)i * 32, mp->mDescriptor.data, 32);
+            best_rows[i] = any_valid ? -3 : -1;
+            delete mp;
+            for (KeyFrame* kf : kfs) delete kf;
         }
     }
     return 0;

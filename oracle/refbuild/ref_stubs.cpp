@@ -1,13 +1,15 @@
 // ORACLE / TEST INFRASTRUCTURE ONLY.
-// Link stubs for the reference classes that src/ORBmatcher.cc and src/Frame.cc
-// reference but whose own sources (src/MapPoint.cc, src/KeyFrame.cc,
-// src/Converter.cc) need Eigen/g2o/DBoW2 vocabularies and are off the feature
-// path.  The accessors the path does use (MapPoint::isBad, Observations,
-// GetDescriptor, GetWorldPos) return the stored fields exactly as the
-// reference's src/MapPoint.cc does (without its locking); everything else
-// aborts if called.
+// Link stubs for the reference classes that src/ORBmatcher.cc, src/Frame.cc
+// and src/MapPoint.cc reference but whose own sources (src/KeyFrame.cc,
+// src/Map.cc, src/Converter.cc) need Eigen/g2o/DBoW2 vocabularies and are off
+// the feature path.  The keyframe constructor copies only the fields the
+// compiled reference code reads (mnFrameId, mvuRight, mDescriptors) and
+// zeroes the rest; the accessors the path uses (KeyFrame::isBad) return the
+// stored field exactly as src/KeyFrame.cc does (without its locking);
+// everything else aborts if called.
 #include "MapPoint.h"
 #include "KeyFrame.h"
+#include "Map.h"
 #include "Converter.h"
 
 #include <cstdio>
@@ -20,36 +22,25 @@ namespace ORB_SLAM2 {
     std::abort();
 }
 
-long unsigned int MapPoint::nNextId = 0;
-std::mutex MapPoint::mGlobalMutex;
+long unsigned int KeyFrame::nNextId = 0;
 
-// Only the harness constructs map points: a point with one observation
-// (src/MapPoint.cc keeps nObs as the number of keyframe observations).
-MapPoint::MapPoint(const cv::Mat& Pos, KeyFrame* pRefKF, Map* pMap)
-    : mnFirstKFid(0), mnFirstFrame(0), nObs(1), mnTrackReferenceForFrame(0), mnLastFrameSeen(0),
-      mnBALocalForKF(0), mnFuseCandidateForKF(0), mnLoopPointForKF(0), mnCorrectedByKF(0),
-      mnCorrectedReference(0), mnBAGlobalForKF(0), mpRefKF(pRefKF), mnVisible(1), mnFound(1), mbBad(false),
-      mpReplaced(static_cast<MapPoint*>(NULL)), mfMinDistance(0), mfMaxDistance(0), mpMap(pMap) {
-    Pos.copyTo(mWorldPos);
-    mNormalVector = cv::Mat::zeros(3, 1, CV_32F);
+KeyFrame::KeyFrame(Frame& F, Map* pMap, KeyFrameDatabase* pKFDB)
+    : mnFrameId(F.mnId), mTimeStamp(0), mnGridCols(0), mnGridRows(0), mfGridElementWidthInv(0),
+      mfGridElementHeightInv(0), mnTrackReferenceForFrame(0), mnFuseTargetForKF(0), mnBALocalForKF(0),
+      mnBAFixedForKF(0), mnLoopQuery(0), mnLoopWords(0), mLoopScore(0), mnRelocQuery(0), mnRelocWords(0),
+      mRelocScore(0), mnBAGlobalForKF(0), fx(0), fy(0), cx(0), cy(0), invfx(0), invfy(0), mbf(0), mb(0),
+      mThDepth(0), N(F.N), mvuRight(F.mvuRight), mDescriptors(F.mDescriptors.clone()), mnScaleLevels(0),
+      mfScaleFactor(0), mfLogScaleFactor(0), mnMinX(0), mnMinY(0), mnMaxX(0), mnMaxY(0), mpKeyFrameDB(pKFDB),
+      mpORBvocabulary(nullptr), mbFirstConnection(true), mpParent(nullptr), mbNotErase(false),
+      mbToBeErased(false), mbBad(false), mHalfBaseline(0), mpMap(pMap) {
     mnId = nNextId++;
 }
 
-bool MapPoint::isBad() { return mbBad; }
-int MapPoint::Observations() { return nObs; }
-cv::Mat MapPoint::GetDescriptor() { return mDescriptor.clone(); }
-cv::Mat MapPoint::GetWorldPos() { return mWorldPos.clone(); }
-cv::Mat MapPoint::GetNormal() { return mNormalVector.clone(); }
-void MapPoint::AddObservation(KeyFrame*, size_t) { stub_unreachable("MapPoint::AddObservation"); }
-int MapPoint::GetIndexInKeyFrame(KeyFrame*) { stub_unreachable("MapPoint::GetIndexInKeyFrame"); }
-bool MapPoint::IsInKeyFrame(KeyFrame*) { stub_unreachable("MapPoint::IsInKeyFrame"); }
-float MapPoint::GetMinDistanceInvariance() { stub_unreachable("MapPoint::GetMinDistanceInvariance"); }
-float MapPoint::GetMaxDistanceInvariance() { stub_unreachable("MapPoint::GetMaxDistanceInvariance"); }
-int MapPoint::PredictScale(const float&, KeyFrame*) { stub_unreachable("MapPoint::PredictScale"); }
-int MapPoint::PredictScale(const float&, Frame*) { stub_unreachable("MapPoint::PredictScale"); }
-void MapPoint::Replace(MapPoint*) { stub_unreachable("MapPoint::Replace"); }
-
+bool KeyFrame::isBad() { return mbBad; }
 void KeyFrame::AddMapPoint(MapPoint*, const size_t&) { stub_unreachable("KeyFrame::AddMapPoint"); }
+void KeyFrame::EraseMapPointMatch(const size_t&) { stub_unreachable("KeyFrame::EraseMapPointMatch"); }
+void KeyFrame::EraseMapPointMatch(MapPoint*) { stub_unreachable("KeyFrame::EraseMapPointMatch"); }
+void KeyFrame::ReplaceMapPointMatch(const size_t&, MapPoint*) { stub_unreachable("KeyFrame::ReplaceMapPointMatch"); }
 cv::Mat KeyFrame::GetCameraCenter() { stub_unreachable("KeyFrame::GetCameraCenter"); }
 std::vector<size_t> KeyFrame::GetFeaturesInArea(const float&, const float&, const float&) const {
     stub_unreachable("KeyFrame::GetFeaturesInArea");
@@ -60,6 +51,9 @@ std::set<MapPoint*> KeyFrame::GetMapPoints() { stub_unreachable("KeyFrame::GetMa
 cv::Mat KeyFrame::GetRotation() { stub_unreachable("KeyFrame::GetRotation"); }
 cv::Mat KeyFrame::GetTranslation() { stub_unreachable("KeyFrame::GetTranslation"); }
 bool KeyFrame::IsInImage(const float&, const float&) const { stub_unreachable("KeyFrame::IsInImage"); }
+
+Map::Map() : mnMaxKFid(0), mnBigChangeIdx(0) {}
+void Map::EraseMapPoint(MapPoint*) { stub_unreachable("Map::EraseMapPoint"); }
 
 std::vector<cv::Mat> Converter::toDescriptorVector(const cv::Mat&) { stub_unreachable("Converter::toDescriptorVector"); }
 

@@ -8,3 +8,4 @@ fallback: without the built library or a CUDA device every call raises.
 from ._lib import FRAME_MAPPOINT_DTYPE, KEYPOINT_DTYPE, MAPPOINT_DTYPE, OrbGpuError, lib  # noqa: F401
 from .extractor import ORBextractor  # noqa: F401
 from .matcher import ORBmatcher, FrameView, compute_stereo_matches  # noqa: F401
+from .mappoints import compute_distinctive_descriptors, observations_to_csr  # noqa: F401

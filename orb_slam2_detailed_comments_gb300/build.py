@@ -32,6 +32,7 @@ SOURCES = [
     "orbgpu_match.cu",
     "orbgpu_knn.cu",
     "orbgpu_knn_tc.cu",
+    "orbgpu_mappoint.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -339,3 +339,43 @@ def predict_pose(T_last, T_lastlast):
         return np.asarray(T_last, np.float32)
     V = h(T_last) @ np.linalg.inv(h(T_lastlast))
     return (V @ h(T_last))[:3, :4].astype(np.float32)
+
+
+def observation_case(m: int, seed: int, mean_len: float = 6.0, max_len: int = 64, bad_frac: float = 0.05,
+                     empty_frac: float = 0.02, flip_ands: int = 3, extra_rows: int = 0, low_entropy: bool = False):
+    """Map points with observation lists over a keyframe descriptor pool, the
+    input of MapPoint::ComputeDistinctiveDescriptors.
+
+    List lengths are geometric with the given mean (capped at max_len; a
+    fraction empty_frac of the map points has none).  Every observation of a
+    map point is a noisy copy of that map point's base descriptor, each bit
+    flipped with probability 2**-flip_ands; the copies sit at random rows of
+    the pool (extra_rows unrelated rows added), and a fraction bad_frac of the
+    observations is marked -1 (a bad keyframe).  low_entropy keeps only the two
+    low bits of every byte, which makes equal distances and equal medians (the
+    tie rule) common.  Returns (pool (P, 32) uint8, obs_offsets (m + 1,) int32,
+    obs_rows (n,) int32).
+    """
+    rng = np.random.default_rng(seed)
+    lens = np.minimum(rng.geometric(1.0 / max(mean_len, 1.0), m), max_len).astype(np.int64)
+    lens[rng.random(m) < empty_frac] = 0
+    offsets = np.zeros(m + 1, np.int64)
+    np.cumsum(lens, out=offsets[1:])
+    n = int(offsets[-1])
+    base = rng.integers(0, 256, (m, 32), dtype=np.uint8)
+    flips = rng.integers(0, 256, (n, 32), dtype=np.uint8)
+    for _ in range(flip_ands - 1):
+        flips &= rng.integers(0, 256, (n, 32), dtype=np.uint8)
+    obs = base[np.repeat(np.arange(m), lens)] ^ flips
+    pool = np.empty((n + extra_rows, 32), np.uint8)
+    rows = rng.permutation(n + extra_rows)[:n]
+    pool[rows] = obs
+    if extra_rows:
+        free = np.ones(n + extra_rows, bool)
+        free[rows] = False
+        pool[free] = rng.integers(0, 256, (extra_rows, 32), dtype=np.uint8)
+    if low_entropy:
+        pool &= np.uint8(3)
+    rows = rows.astype(np.int32)
+    rows[rng.random(n) < bad_frac] = -1
+    return pool, offsets.astype(np.int32), rows

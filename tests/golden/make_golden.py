@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the ORB front-end path.
 
 The outputs come from the reference's own src/ORBextractor.cc,
-src/ORBmatcher.cc and src/Frame.cc, compiled unmodified against the cv
+src/ORBmatcher.cc, src/Frame.cc and src/MapPoint.cc, compiled unmodified against the cv
 stand-in (oracle/Makefile target ``ref``; needs the reference sources, so this
 script runs only where they are present).  Inputs are stored with the outputs,
 so the fixtures do not depend on the generator's random streams.
@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive")
 
 
 def main(groups=GROUPS):
@@ -47,6 +47,8 @@ def main(groups=GROUPS):
         tables_fixture(R)
     if "projframe" in groups:
         projframe_fixture(R)
+    if "distinctive" in groups:
+        distinctive_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -154,6 +156,55 @@ def projframe_fixture(R):
                            nmatches=np.array(nm), match=match)
     for name, arrays in cases.items():
         save(f"projframe_{name}.npz", **arrays)
+
+
+def distinctive_kats():
+    """Hand-made observation lists for MapPoint::ComputeDistinctiveDescriptors
+    (pool, offsets, rows).  Descriptor b(k) has its first k bits set, so
+    d(b(i), b(j)) = |i - j|."""
+    def b(k):
+        bits = np.zeros(256, np.uint8)
+        bits[:k] = 1
+        return np.packbits(bits, bitorder="little")
+    pool = np.stack([b(k) for k in range(0, 257)])  # row k = b(k)
+    lists = [
+        [5],                      # one observation: chosen
+        [7, 3],                   # two: both medians 0, the first wins
+        [0, 10, 30],              # rows 0/10/30: medians 10, 10, 20 -> row 0
+        [30, 10, 0],              # reversed: medians 20, 10, 10 -> row 10
+        [0, 4, 9, 20],            # N 4, median element 1: 4, 4, 5, 11 -> row 0
+        [20, 9, 4, 0],            # medians 11, 5, 4, 4 -> row 4
+        [-1, -1],                 # every keyframe bad: unchanged
+        [],                       # no observation: unchanged
+        [-1, 40, -1, 42, 100],    # bad entries skipped: 40, 42, 100 -> medians 2, 2, 58 -> row 40
+        [256, 0, 128],            # distances up to 256: medians 128, 128, 128 -> row 256
+        [17] * 40,                # 40 equal descriptors (long list): all medians 0 -> the first
+        list(range(60, 0, -1)),   # rows 60..1, median element 29: rows 16..46 have the least
+                                  # median (15); the first in list order is row 46
+        [-1] * 35 + [8, 9],       # long list, only two valid
+    ]
+    offsets = np.zeros(len(lists) + 1, np.int32)
+    offsets[1:] = np.cumsum([len(x) for x in lists])
+    rows = np.array([r for x in lists for r in x], np.int32)
+    return pool, offsets, rows
+
+
+def distinctive_fixture(R):
+    # 9. MapPoint::ComputeDistinctiveDescriptors: hand-made lists and seeded
+    # synthetic maps (short, long and tie-heavy lists)
+    arrays = {}
+    cases = {"kat": distinctive_kats(),
+             "short": syn.observation_case(1500, 11, mean_len=6.0, max_len=64),
+             "long": syn.observation_case(300, 12, mean_len=40.0, max_len=200),
+             "ties": syn.observation_case(1500, 13, mean_len=5.0, max_len=48, low_entropy=True, extra_rows=64)}
+    rng = np.random.default_rng(14)
+    for name, (pool, offsets, rows) in cases.items():
+        m = len(offsets) - 1
+        initial = rng.integers(0, 256, (m, 32), dtype=np.uint8)
+        _, desc = R.distinctive_descriptors(pool, offsets, rows, initial)
+        arrays.update({f"{name}_pool": pool, f"{name}_offsets": offsets, f"{name}_rows": rows,
+                       f"{name}_initial": initial, f"{name}_descriptors": desc})
+    save("distinctive.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -145,3 +145,45 @@ def test_search_by_projection_frame_reference_cases(oracle):
         assert a[0] == b[0] and np.array_equal(a[1], b[1])
         if every == 1:
             assert np.array_equal(b[1], np.arange(30))
+
+
+# MapPoint::ComputeDistinctiveDescriptors (src/MapPoint.cc:365-447)
+DISTINCTIVE_KAT_ROWS = [5, 7, 0, 10, 0, 4, -1, -1, 40, 256, 17, 46, 8]
+
+
+@pytest.mark.parametrize("case", ["kat", "short", "long", "ties"])
+def test_distinctive_descriptors_golden(oracle, golden, case):
+    g = golden("distinctive.npz")
+    pool, offsets, rows = g[f"{case}_pool"], g[f"{case}_offsets"], g[f"{case}_rows"]
+    best, desc = oracle.distinctive_descriptors(pool, offsets, rows, g[f"{case}_initial"])
+    assert np.array_equal(desc, g[f"{case}_descriptors"])
+    # the chosen row is one of the map point's valid observations
+    for i in range(len(best)):
+        lst = rows[offsets[i]:offsets[i + 1]]
+        if best[i] >= 0:
+            assert best[i] in lst
+        else:
+            assert best[i] == -1 and not (lst >= 0).any()
+    if case == "kat":
+        assert best.tolist() == DISTINCTIVE_KAT_ROWS
+
+
+def test_distinctive_descriptors_malformed_lists(oracle):
+    pool = np.zeros((4, 32), np.uint8)
+    offsets = np.array([0, 2, 1, 3, 5], np.int32)  # map point 1 has a decreasing offset
+    rows = np.array([0, 1, 2, 4, -2], np.int32)    # map point 3 has rows 4 and -2, outside [-1, 4)
+    best, _ = oracle.distinctive_descriptors(pool, offsets, rows)
+    assert best.tolist() == [0, -2, 1, -2]
+
+
+@pytest.mark.skipif(not pyoracle.ref_available(), reason="reference sources not built here")
+def test_distinctive_descriptors_reference_fresh_seeds(oracle):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    R = pyoracle.RefOracle()
+    for seed, kw in ((101, dict(mean_len=8.0)), (102, dict(mean_len=30.0, max_len=120)),
+                     (103, dict(mean_len=5.0, low_entropy=True, extra_rows=32))):
+        pool, offsets, rows = syn.observation_case(800, seed, **kw)
+        init = np.random.default_rng(seed).integers(0, 256, (800, 32), dtype=np.uint8)
+        _, a = oracle.distinctive_descriptors(pool, offsets, rows, init)
+        _, b = R.distinctive_descriptors(pool, offsets, rows, init)
+        assert np.array_equal(a, b), seed
