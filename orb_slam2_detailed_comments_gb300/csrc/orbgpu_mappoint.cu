@@ -62,7 +62,7 @@ struct DDShared {
 // pairs of chunks past jmax are all such entries.
 __device__ __forceinline__ int dd_row_rank32(const unsigned (&p)[16], int k, int jmax) {
     int lo = 0;
-#pragma unroll
+#pragma unroll 1
     for (int step = 256; step >= 1; step >>= 1) {
         const int v = lo + step - 1;
         const unsigned v2 = (unsigned)(0x8000 + v) * 0x10001u;
