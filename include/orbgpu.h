@@ -168,6 +168,59 @@ int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame* f, const 
                                 const uint8_t* mp_descriptors, int n_mappoints, float th, const uint8_t* claimed,
                                 int* match_out, int mem, int* nmatches);
 
+/* The map point fields Frame::isInFrustum reads (src/Frame.cc:491-578). */
+typedef struct {
+    float x, y, z;          /* MapPoint::GetWorldPos() */
+    float nx, ny, nz;       /* MapPoint::GetNormal() */
+    float min_distance;     /* mfMinDistance (GetMinDistanceInvariance() is 0.8f times it) */
+    float max_distance;     /* mfMaxDistance (GetMaxDistanceInvariance() is 1.2f times it) */
+} orbgpu_mappoint_geometry;
+
+/* The frame data isInFrustum and MapPoint::PredictScale(dist, Frame*) read:
+ * mRcw, mtcw and mOw as Frame::UpdatePoseMatrices derives them from mTcw,
+ * Frame::fx, fy, cx, cy, mbf, the image bounds mnMinX, mnMaxX, mnMinY,
+ * mnMaxY, mnScaleLevels, and the predicted-level thresholds: PredictScale
+ * returns #{n < nlevels - 1 : ratio > level_above[n]} (ratio =
+ * mfMaxDistance / dist), the thresholds being where ceil(log(ratio) /
+ * mfLogScaleFactor) steps, found with the host's logf.  Fill it with
+ * orbgpu_frustum_frame_init. */
+typedef struct {
+    float Rcw[9];
+    float tcw[3];
+    float Ow[3];
+    float fx, fy, cx, cy, bf;
+    float min_x, max_x, min_y, max_y;
+    int32_t nlevels;
+    float level_above[15];
+} orbgpu_frustum_frame;
+
+/* Fills *out from rows 0-2 of the frame's mTcw (row-major 3 x 4), the
+ * camera constants, the image bounds and the extractor's scale factor and
+ * level count (Frame::mfScaleFactor, mnScaleLevels; mfLogScaleFactor =
+ * logf(scale_factor) as in the Frame constructors).  Host only; nlevels 1-16,
+ * scale_factor > 1. */
+int orbgpu_frustum_frame_init(const float* Tcw, float fx, float fy, float cx, float cy, float bf, float min_x,
+                              float max_x, float min_y, float max_y, float scale_factor, int nlevels,
+                              orbgpu_frustum_frame* out);
+
+/* Frame::isInFrustum(pMP, viewingCosLimit) -- src/Frame.cc:491-578, with
+ * MapPoint::PredictScale(dist, this) (src/MapPoint.cc:604-619) -- for the map
+ * points of nframes frames in one launch: frame f tests mps[mp_offsets[f] ..
+ * mp_offsets[f + 1]).  For every map point it writes mappoints[i] as the
+ * reference leaves the MapPoint: track_in_view (mbTrackInView), and where it
+ * is 1 also proj_x, proj_y, proj_xr, view_cos and track_scale_level
+ * (mTrackProjX, mTrackProjY, mTrackProjXR, mTrackViewCos,
+ * mnTrackScaleLevel); where it is 0 those fields keep their values, and
+ * 'bad' is never written -- so the records go straight to
+ * orbgpu_search_by_projection / orbgpu_batch_search_by_projection.
+ * in_view (nullable, device, nframes ints) receives the number of map points
+ * in view per frame (Tracking::SearchLocalPoints' nToMatch).  frames,
+ * mp_offsets, mps and mappoints may be device or page-locked host memory.
+ * Asynchronous on 'stream'; one kernel launch (plus a memset of in_view). */
+int orbgpu_is_in_frustum(const orbgpu_frustum_frame* frames, int nframes, const int* mp_offsets,
+                         const orbgpu_mappoint_geometry* mps, float viewing_cos_limit, orbgpu_mappoint* mappoints,
+                         int* in_view, void* stream);
+
 /* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
  * indexed like LastFrame's keypoints. */
 typedef struct {

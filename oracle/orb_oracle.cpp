@@ -850,6 +850,84 @@ int orc_distribute(const orc_kp* cand, int n, int minX, int maxX, int minY, int 
     return (int)r.size();
 }
 
+// Frame::isInFrustum, src/Frame.cc:491-578, as the reference computes it
+// against the cv stand-in: the pose matrices of Frame::UpdatePoseMatrices
+// (:454-470; mOw = -mRcw^T mtcw), Pc = mRcw * P + mtcw with the product
+// accumulated in double and rounded to float before the float add, the
+// projection and bounds in float, GetMin/MaxDistanceInvariance (0.8f / 1.2f
+// times the stored distances, src/MapPoint.cc:542-552), dist = cv::norm(P -
+// mOw) (double sum of squares, double sqrt, to float), viewCos = PO.dot(Pn)
+// (double) / dist, and MapPoint::PredictScale(dist, Frame*)
+// (src/MapPoint.cc:604-619): ceil(logf(mfMaxDistance / dist) /
+// logf(mfScaleFactor)) clamped to [0, nlevels - 1].
+int orc_is_in_frustum(const orc_frustum_camera* cam, const orc_mp_geometry* mps, int m, float cos_limit,
+                      orc_mappoint* out) {
+    float R[3][3], t[3], Ow[3];
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++) R[r][c] = cam->Tcw[4 * r + c];
+        t[r] = cam->Tcw[4 * r + 3];
+    }
+    for (int i = 0; i < 3; i++) {
+        double s = 0;
+        for (int k = 0; k < 3; k++) s += (double)(-R[k][i]) * (double)t[k];
+        Ow[i] = (float)s;
+    }
+    const float log_scale = std::log(cam->scale_factor);
+    int nin = 0;
+    for (int i = 0; i < m; i++) {
+        const orc_mp_geometry& g = mps[i];
+        orc_mappoint& o = out[i];
+        o.track_in_view = 0;
+        const float P[3] = {g.x, g.y, g.z};
+        float Pc[3];
+        for (int r = 0; r < 3; r++) {
+            double s = 0;
+            for (int k = 0; k < 3; k++) s += (double)R[r][k] * (double)P[k];
+            Pc[r] = (float)s + t[r];
+        }
+        if (Pc[2] < 0.0f) continue;
+        const float invz = 1.0f / Pc[2];
+        const float u = cam->fx * Pc[0] * invz + cam->cx;
+        const float v = cam->fy * Pc[1] * invz + cam->cy;
+        if (u < cam->min_x || u > cam->max_x) continue;
+        if (v < cam->min_y || v > cam->max_y) continue;
+        const float max_d = 1.2f * g.max_distance;
+        const float min_d = 0.8f * g.min_distance;
+        const float PO[3] = {P[0] - Ow[0], P[1] - Ow[1], P[2] - Ow[2]};
+        double ss = 0;
+        for (int k = 0; k < 3; k++) ss += (double)PO[k] * (double)PO[k];
+        const float dist = (float)std::sqrt(ss);
+        if (dist < min_d || dist > max_d) continue;
+        const double dot = (double)PO[0] * g.nx + (double)PO[1] * g.ny + (double)PO[2] * g.nz;
+        const float view_cos = (float)(dot / dist);
+        if (view_cos < cos_limit) continue;
+        const float ratio = g.max_distance / dist;
+        int level = (int)std::ceil(std::log(ratio) / log_scale);
+        if (level < 0) level = 0;
+        else if (level >= cam->nlevels) level = cam->nlevels - 1;
+        o.track_in_view = 1;
+        o.proj_x = u;
+        o.proj_xr = u - cam->bf * invz;
+        o.proj_y = v;
+        o.track_scale_level = level;
+        o.view_cos = view_cos;
+        nin++;
+    }
+    return nin;
+}
+
+// MapPoint::PredictScale(currentDist, Frame*), src/MapPoint.cc:604-619, on
+// given ratios mfMaxDistance / currentDist.
+void orc_predict_scale(const float* ratio, int n, float scale_factor, int nlevels, int* out) {
+    const float log_scale = std::log(scale_factor);
+    for (int i = 0; i < n; i++) {
+        int level = (int)std::ceil(std::log(ratio[i]) / log_scale);
+        if (level < 0) level = 0;
+        else if (level >= nlevels) level = nlevels - 1;
+        out[i] = level;
+    }
+}
+
 // MapPoint::ComputeDistinctiveDescriptors, src/MapPoint.cc:365-447, for m
 // map points given as ragged lists of pool rows in observation order (the
 // iteration order of MapPoint::mObservations).  A row of -1 stands for an

@@ -50,6 +50,16 @@ int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
  * best_rows: chosen row, -1 none valid, -2 invalid list (the harness version
  * reports -3: the reference exposes only the descriptor).  desc_inout
  * (nullable) gets the chosen descriptor, unchanged where best_rows < 0. */
+/* Frame::isInFrustum(pMP, cos_limit) (src/Frame.cc:491-578, pose matrices of
+ * Frame::UpdatePoseMatrices :454-470, MapPoint::PredictScale
+ * src/MapPoint.cc:604-619) for m map points of one frame; out holds the map
+ * points' tracking fields before the call and after it (bad untouched).
+ * Returns the number in view. */
+int orc_is_in_frustum(const orc_frustum_camera* cam, const orc_mp_geometry* mps, int m, float cos_limit,
+                      orc_mappoint* out);
+/* MapPoint::PredictScale (src/MapPoint.cc:604-619) on n ratios
+ * mfMaxDistance / currentDist (oracle only; no harness counterpart). */
+void orc_predict_scale(const float* ratio, int n, float scale_factor, int nlevels, int* out);
 int orc_distinctive_descriptors(const uint8_t* pool, int pool_rows, const int* offsets, const int* rows, int m,
                                 int* best_rows, uint8_t* desc_inout);
 

@@ -57,6 +57,25 @@ typedef struct {
     float fx, fy, cx, cy, bf, b;
 } orc_frame_motion;
 
+/* The map point fields Frame::isInFrustum reads (src/Frame.cc:491-578). */
+typedef struct {
+    float x, y, z;       /* GetWorldPos() */
+    float nx, ny, nz;    /* GetNormal() */
+    float min_distance;  /* mfMinDistance */
+    float max_distance;  /* mfMaxDistance */
+} orc_mp_geometry;
+
+/* The frame of isInFrustum: rows 0-2 of mTcw (row-major 3 x 4), Frame::fx,
+ * fy, cx, cy, mbf, mnMinX, mnMaxX, mnMinY, mnMaxY, mfScaleFactor and
+ * mnScaleLevels. */
+typedef struct {
+    float Tcw[12];
+    float fx, fy, cx, cy, bf;
+    float min_x, max_x, min_y, max_y;
+    float scale_factor;
+    int32_t nlevels;
+} orc_frustum_camera;
+
 #ifdef __cplusplus
 }
 #endif

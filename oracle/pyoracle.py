@@ -26,6 +26,8 @@ MP_DTYPE = np.dtype([("proj_x", "<f4"), ("proj_y", "<f4"), ("proj_xr", "<f4"), (
 
 
 FMP_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("flags", "<i4")])
+GEOM_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("nx", "<f4"), ("ny", "<f4"), ("nz", "<f4"),
+                       ("min_distance", "<f4"), ("max_distance", "<f4")])
 MP_PRESENT, MP_OUTLIER, MP_OBSERVED = 1, 2, 4
 
 
@@ -43,6 +45,23 @@ def make_motion(Tcw, Tlw, fx, fy, cx, cy, bf=0.0, b=0.0) -> Motion:
         m.Tlw[i] = float(v)
     m.fx, m.fy, m.cx, m.cy, m.bf, m.b = (float(np.float32(v)) for v in (fx, fy, cx, cy, bf, b))
     return m
+
+
+class FrustumCamera(C.Structure):
+    """Rows 0-2 of mTcw, fx, fy, cx, cy, mbf, image bounds, scale factor, levels."""
+    _fields_ = [("Tcw", C.c_float * 12), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
+                ("cy", C.c_float), ("bf", C.c_float), ("min_x", C.c_float), ("max_x", C.c_float),
+                ("min_y", C.c_float), ("max_y", C.c_float), ("scale_factor", C.c_float), ("nlevels", C.c_int)]
+
+
+def make_frustum_camera(Tcw, fx, fy, cx, cy, bf, min_x, max_x, min_y, max_y, scale_factor=1.2, nlevels=8):
+    c = FrustumCamera()
+    for i, v in enumerate(np.asarray(Tcw, np.float32).reshape(-1)[:12]):
+        c.Tcw[i] = float(v)
+    (c.fx, c.fy, c.cx, c.cy, c.bf, c.min_x, c.max_x, c.min_y, c.max_y,
+     c.scale_factor) = (float(np.float32(v)) for v in (fx, fy, cx, cy, bf, min_x, max_x, min_y, max_y, scale_factor))
+    c.nlevels = int(nlevels)
+    return c
 
 
 class Params(C.Structure):
@@ -228,6 +247,17 @@ class _Base:
         return tuple(o[:nq].copy() for o in outs)
 
 
+    def is_in_frustum(self, cam, mps, cos_limit=0.5, initial=None):
+        """Frame::isInFrustum for every map point (GEOM_DTYPE records) of one
+        frame; returns (MP_DTYPE records after the call, number in view)."""
+        mps = np.ascontiguousarray(mps, GEOM_DTYPE)
+        out = (np.zeros(max(len(mps), 1), MP_DTYPE) if initial is None
+               else np.ascontiguousarray(np.array(initial, MP_DTYPE)))
+        f = self.fn("is_in_frustum")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_void_p]
+        n = f(C.byref(cam), _p(mps), len(mps), C.c_float(cos_limit), _p(out))
+        return out[:len(mps)].copy(), int(n)
+
     def distinctive_descriptors(self, pool, offsets, rows, initial=None):
         """MapPoint::ComputeDistinctiveDescriptors over ragged observation lists
         (src/MapPoint.cc:365-447); returns (best_rows, descriptors)."""
@@ -247,6 +277,15 @@ class _Base:
 class Oracle(_Base):
     def __init__(self, path: str = ORACLE_SO):
         super().__init__(path)
+
+    def predict_scale(self, ratio, scale_factor=1.2, nlevels=8):
+        """MapPoint::PredictScale on ratios mfMaxDistance / currentDist."""
+        r = np.ascontiguousarray(ratio, np.float32)
+        out = np.zeros(max(len(r), 1), np.int32)
+        f = self.lib.orc_predict_scale
+        f.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_void_p]
+        f(_p(r), len(r), C.c_float(scale_factor), nlevels, _p(out))
+        return out[:len(r)].copy()
 
 
 class RefOracle(_Base):

@@ -483,6 +483,66 @@ int ref_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
     return 0;
 }
 
+// Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
+// (UpdatePoseMatrices) and real map points whose tracking fields start from
+// out[i] (the reference leaves them unchanged where it returns false).
+int ref_is_in_frustum(const orc_frustum_camera* cam, const orc_mp_geometry* mps, int m, float cos_limit,
+                      orc_mappoint* out) {
+    ArenaScope scope;
+    int nin = 0;
+    {
+        MapPointMaker maker;
+        Frame* F = new Frame();
+        cv::Mat Tcw = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) Tcw.at<float>(r, c) = cam->Tcw[4 * r + c];
+        F->SetPose(Tcw);
+        Frame::fx = cam->fx;
+        Frame::fy = cam->fy;
+        Frame::cx = cam->cx;
+        Frame::cy = cam->cy;
+        Frame::invfx = 1.0f / cam->fx;
+        Frame::invfy = 1.0f / cam->fy;
+        Frame::mnMinX = cam->min_x;
+        Frame::mnMaxX = cam->max_x;
+        Frame::mnMinY = cam->min_y;
+        Frame::mnMaxY = cam->max_y;
+        F->mbf = cam->bf;
+        F->mnScaleLevels = cam->nlevels;
+        F->mfScaleFactor = cam->scale_factor;
+        F->mfLogScaleFactor = std::log(cam->scale_factor);
+        for (int i = 0; i < m; i++) {
+            cv::Mat pos(3, 1, CV_32F);
+            pos.at<float>(0) = mps[i].x;
+            pos.at<float>(1) = mps[i].y;
+            pos.at<float>(2) = mps[i].z;
+            MapPoint* mp = maker.make(pos, 1);
+            mp->mNormalVector = cv::Mat(3, 1, CV_32F);
+            mp->mNormalVector.at<float>(0) = mps[i].nx;
+            mp->mNormalVector.at<float>(1) = mps[i].ny;
+            mp->mNormalVector.at<float>(2) = mps[i].nz;
+            mp->mfMinDistance = mps[i].min_distance;
+            mp->mfMaxDistance = mps[i].max_distance;
+            mp->mTrackProjX = out[i].proj_x;
+            mp->mTrackProjY = out[i].proj_y;
+            mp->mTrackProjXR = out[i].proj_xr;
+            mp->mTrackViewCos = out[i].view_cos;
+            mp->mnTrackScaleLevel = out[i].track_scale_level;
+            const bool in = F->isInFrustum(mp, cos_limit);
+            nin += in ? 1 : 0;
+            out[i].track_in_view = mp->mbTrackInView ? 1 : 0;
+            out[i].proj_x = mp->mTrackProjX;
+            out[i].proj_y = mp->mTrackProjY;
+            out[i].proj_xr = mp->mTrackProjXR;
+            out[i].view_cos = mp->mTrackViewCos;
+            out[i].track_scale_level = mp->mnTrackScaleLevel;
+            delete mp;
+        }
+        delete F;
+    }
+    return nin;
+}
+
 // MapPoint::ComputeDistinctiveDescriptors -- src/MapPoint.cc:365-447, run on a
 // real MapPoint whose observations are one keyframe per list entry (each
 // keyframe holding that entry's descriptor as its row 0; a -1 row becomes a

@@ -5,7 +5,9 @@ behind the C ABI in include/orbgpu.h); this package mirrors the reference's
 ORBextractor / ORBmatcher / Frame interfaces on top of it.  There is no CPU
 fallback: without the built library or a CUDA device every call raises.
 """
-from ._lib import FRAME_MAPPOINT_DTYPE, KEYPOINT_DTYPE, MAPPOINT_DTYPE, OrbGpuError, lib  # noqa: F401
+from ._lib import (FRAME_MAPPOINT_DTYPE, FRUSTUM_FRAME_DTYPE, KEYPOINT_DTYPE, MAPPOINT_DTYPE,  # noqa: F401
+                   MAPPOINT_GEOMETRY_DTYPE, OrbGpuError, lib)
 from .extractor import ORBextractor  # noqa: F401
 from .matcher import ORBmatcher, FrameView, compute_stereo_matches  # noqa: F401
 from .mappoints import compute_distinctive_descriptors, observations_to_csr  # noqa: F401
+from .frustum import frustum_frame, is_in_frustum  # noqa: F401

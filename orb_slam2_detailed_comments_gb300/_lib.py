@@ -15,6 +15,13 @@ MAPPOINT_DTYPE = np.dtype([("proj_x", "<f4"), ("proj_y", "<f4"), ("proj_xr", "<f
                            ("track_scale_level", "<i4"), ("track_in_view", "<i4"), ("bad", "<i4"), ("pad", "<i4")])
 
 FRAME_MAPPOINT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("flags", "<i4")])
+# orbgpu_mappoint_geometry: the map point fields Frame::isInFrustum reads
+MAPPOINT_GEOMETRY_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("nx", "<f4"), ("ny", "<f4"),
+                                    ("nz", "<f4"), ("min_distance", "<f4"), ("max_distance", "<f4")])
+# orbgpu_frustum_frame (filled by orbgpu_frustum_frame_init)
+FRUSTUM_FRAME_DTYPE = np.dtype([("Rcw", "<f4", 9), ("tcw", "<f4", 3), ("Ow", "<f4", 3), ("fx", "<f4"), ("fy", "<f4"),
+                                ("cx", "<f4"), ("cy", "<f4"), ("bf", "<f4"), ("min_x", "<f4"), ("max_x", "<f4"),
+                                ("min_y", "<f4"), ("max_y", "<f4"), ("nlevels", "<i4"), ("level_above", "<f4", 15)])
 MP_PRESENT, MP_OUTLIER, MP_OBSERVED = 1, 2, 4
 
 MEM_HOST = 0

@@ -379,3 +379,44 @@ def observation_case(m: int, seed: int, mean_len: float = 6.0, max_len: int = 64
     rows = rows.astype(np.int32)
     rows[rng.random(n) < bad_frac] = -1
     return pool, offsets.astype(np.int32), rows
+
+
+def _rotation(a: float, b: float, c: float) -> np.ndarray:
+    ca, sa, cb, sb, cc, sc = np.cos(a), np.sin(a), np.cos(b), np.sin(b), np.cos(c), np.sin(c)
+    rx = np.array([[1, 0, 0], [0, ca, -sa], [0, sa, ca]])
+    ry = np.array([[cb, 0, sb], [0, 1, 0], [-sb, 0, cb]])
+    rz = np.array([[cc, -sc, 0], [sc, cc, 0], [0, 0, 1]])
+    return rz @ ry @ rx
+
+
+def frustum_case(m: int, seed: int, w: int = 640, h: int = 480, fx: float = 500.0, scale_factor: float = 1.2,
+                 nlevels: int = 8):
+    """Local map points around a camera for Frame::isInFrustum.
+
+    The camera has a random pose; map points lie in a box in front of it (a
+    part behind it and beyond the image borders), with normals near the viewing
+    ray (some turned away), and distance invariance limits placed so that the
+    ratio mfMaxDistance / distance falls on and beside the predicted-level
+    boundaries (powers of the scale factor, off by 0 or 1 ulp-sized factors).
+    Returns (Tcw rows 0-2 as float32 (3, 4), geometry records with the fields
+    x, y, z, nx, ny, nz, min_distance, max_distance as a float32 (m, 8) array).
+    """
+    rng = np.random.default_rng(seed)
+    R = _rotation(*rng.normal(0, 0.3, 3))
+    t = rng.normal(0, 1, 3)
+    Tcw = np.hstack([R, t[:, None]]).astype(np.float32)
+    Rwc = R.T
+    Ow = -Rwc @ t
+    zmax = 40.0
+    pc = np.stack([rng.uniform(-0.7, 0.7, m) * w / fx * zmax / 2, rng.uniform(-0.7, 0.7, m) * h / fx * zmax / 2,
+                   rng.uniform(-2.0, zmax, m)], 1)
+    pw = (Rwc @ pc.T).T + Ow
+    nrm = pw - Ow + rng.normal(0, 2.5, (m, 3)) * np.linalg.norm(pw - Ow, axis=1, keepdims=True) / 8
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = np.linalg.norm(pw - Ow, axis=1)
+    lev = rng.integers(-2, nlevels + 2, m)
+    jitter = rng.choice([1.0, 1 + 1e-7, 1 - 1e-7, 1 + 3e-7, 1.0001, 0.9999], m)
+    maxd = (d * scale_factor ** lev * jitter).astype(np.float32)
+    mind = (maxd / scale_factor ** (nlevels - 1) * rng.choice([1.0, 0.5, 2.0, 5.0, 1.25], m)).astype(np.float32)
+    g = np.stack([pw[:, 0], pw[:, 1], pw[:, 2], nrm[:, 0], nrm[:, 1], nrm[:, 2], mind, maxd], 1).astype(np.float32)
+    return Tcw, g

@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum")
 
 
 def main(groups=GROUPS):
@@ -49,6 +49,8 @@ def main(groups=GROUPS):
         projframe_fixture(R)
     if "distinctive" in groups:
         distinctive_fixture(R)
+    if "frustum" in groups:
+        frustum_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -205,6 +207,32 @@ def distinctive_fixture(R):
         arrays.update({f"{name}_pool": pool, f"{name}_offsets": offsets, f"{name}_rows": rows,
                        f"{name}_initial": initial, f"{name}_descriptors": desc})
     save("distinctive.npz", **arrays)
+
+
+FRUSTUM_CAMERAS = {
+    # name: (w, h, fx, fy, cx, cy, bf, scale, nlevels, seed, cos limit)
+    "stereo_1241x376": (1241, 376, 718.856, 718.856, 607.1928, 185.2157, 386.1448, 1.2, 8, 61, 0.5),
+    "mono_640x480": (640, 480, 535.4, 539.2, 320.1, 247.6, 0.0, 1.2, 8, 62, 0.5),
+    "wide_levels_752x480": (752, 480, 458.654, 457.296, 367.215, 248.375, 47.9, 1.5, 12, 63, 0.3),
+}
+
+
+def frustum_fixture(R):
+    # 10. Frame::isInFrustum with MapPoint::PredictScale on three cameras
+    from oracle.pyoracle import GEOM_DTYPE, MP_DTYPE, make_frustum_camera
+    arrays = {}
+    for name, (w, h, fx, fy, cx, cy, bf, sf, nl, seed, lim) in FRUSTUM_CAMERAS.items():
+        Tcw, g = syn.frustum_case(4000, seed, w, h, fx, sf, nl)
+        geom = np.ascontiguousarray(g).view(GEOM_DTYPE).reshape(-1)
+        cam = make_frustum_camera(Tcw, fx, fy, cx, cy, bf, 0.0, w, 0.0, h, sf, nl)
+        init = np.zeros(len(geom), MP_DTYPE)
+        init["proj_x"] = -1.0
+        init["track_scale_level"] = 99
+        out, nin = R.is_in_frustum(cam, geom, lim, init)
+        arrays.update({f"{name}_Tcw": Tcw, f"{name}_camera": np.array([fx, fy, cx, cy, bf, w, h, sf, nl, lim],
+                                                                        np.float32),
+                       f"{name}_geometry": g, f"{name}_initial": init, f"{name}_out": out, f"{name}_nin": np.array(nin)})
+    save("frustum.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -187,3 +187,40 @@ def test_distinctive_descriptors_reference_fresh_seeds(oracle):
         _, a = oracle.distinctive_descriptors(pool, offsets, rows, init)
         _, b = R.distinctive_descriptors(pool, offsets, rows, init)
         assert np.array_equal(a, b), seed
+
+
+# Frame::isInFrustum (src/Frame.cc:491-578) with MapPoint::PredictScale
+FRUSTUM_CASES = ["stereo_1241x376", "mono_640x480", "wide_levels_752x480"]
+
+
+def frustum_inputs(g, name):
+    fx, fy, cx, cy, bf, w, h, sf, nl, lim = (float(v) for v in g[f"{name}_camera"])
+    cam = pyoracle.make_frustum_camera(g[f"{name}_Tcw"], fx, fy, cx, cy, bf, 0.0, w, 0.0, h, sf, int(nl))
+    geom = np.ascontiguousarray(g[f"{name}_geometry"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    return cam, geom, lim
+
+
+@pytest.mark.parametrize("name", FRUSTUM_CASES)
+def test_is_in_frustum_golden(oracle, golden, name):
+    g = golden("frustum.npz")
+    cam, geom, lim = frustum_inputs(g, name)
+    out, nin = oracle.is_in_frustum(cam, geom, lim, g[f"{name}_initial"])
+    assert nin == int(g[f"{name}_nin"])
+    assert out.tobytes() == g[f"{name}_out"].tobytes()
+    # map points out of view keep their earlier fields
+    off = out["track_in_view"] == 0
+    assert np.array_equal(out["proj_x"][off], g[f"{name}_initial"]["proj_x"][off])
+
+
+@pytest.mark.skipif(not pyoracle.ref_available(), reason="reference sources not built here")
+def test_is_in_frustum_reference_fresh_seeds(oracle):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    R = pyoracle.RefOracle()
+    for seed, (w, h, fx, sf, nl) in enumerate([(640, 480, 500.0, 1.2, 8), (1241, 376, 718.9, 1.2, 8),
+                                               (1280, 720, 900.0, 1.3, 10), (640, 480, 400.0, 2.0, 4)]):
+        Tcw, g = syn.frustum_case(3000, 200 + seed, w, h, fx, sf, nl)
+        geom = np.ascontiguousarray(g).view(pyoracle.GEOM_DTYPE).reshape(-1)
+        cam = pyoracle.make_frustum_camera(Tcw, fx, fx, w / 2, h / 2, 40.0, 0.0, w, 0.0, h, sf, nl)
+        a, na = oracle.is_in_frustum(cam, geom, 0.5)
+        b, nb = R.is_in_frustum(cam, geom, 0.5)
+        assert na == nb and a.tobytes() == b.tobytes(), seed
