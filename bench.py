@@ -256,7 +256,7 @@ def run_ours(args):
         per_frame_fps, per_frame_split = run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev)
     extra = {}
     for leg, fn in (("stereo", bench_stereo), ("knn", bench_knn), ("serving", bench_serving),
-                    ("distinctive", bench_distinctive)):
+                    ("distinctive", bench_distinctive), ("frustum", bench_frustum)):
         if leg in legs:
             try:
                 extra[LEG_KEYS[leg]] = fn(dev)
@@ -267,9 +267,9 @@ def run_ours(args):
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
 
 
-LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "distinctive", "cpu"}
+LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "distinctive", "frustum", "cpu"}
 LEG_KEYS = {"stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams",
-            "distinctive": "distinctive_descriptors_1M_mappoints"}
+            "distinctive": "distinctive_descriptors_1M_mappoints", "frustum": "is_in_frustum_64x5000"}
 
 
 def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev, nfs, cap):
@@ -547,6 +547,88 @@ def bench_distinctive(dev, steps=10, warmup=3):
             "equal_to_oracle": bool(np.array_equal(gpu_best, cpu_best))}
 
 
+def bench_frustum(dev, steps=10, warmup=3):
+    """Frame::isInFrustum + PredictScale for 64 frames x 5,000 local map points
+    (320,000 per call; cameras 640x480 / 1241x376 / 752x480 / 1280x720, random
+    poses, ratios on and beside the level boundaries).  Device-resident (kernel
+    events, L2 flushed between calls), end to end from page-locked host
+    buffers (geometry in, records out), and the oracle on one host core."""
+    import torch
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import FRUSTUM_FRAME_DTYPE, frustum_frame, is_in_frustum
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    cams = [(640, 480, 500.0, 1.2, 8), (1241, 376, 718.856, 1.2, 8), (752, 480, 458.7, 1.2, 8),
+            (1280, 720, 900.0, 1.2, 8)]
+    nf, per = 64, 5000
+    frames, geoms, cams_o = [], [], []
+    for f in range(nf):
+        w, h, fx, sf, nl = cams[f % 4]
+        Tcw, g = syn.frustum_case(per, 900 + f, w, h, fx, sf, nl)
+        frames.append(frustum_frame(Tcw, fx, fx, w / 2, h / 2, 40.0, 0.0, w, 0.0, h, sf, nl))
+        geoms.append(g)
+        cams_o.append(pyoracle.make_frustum_camera(Tcw, fx, fx, w / 2, h / 2, 40.0, 0.0, w, 0.0, h, sf, nl))
+    m = nf * per
+    offs = np.arange(0, m + 1, per, dtype=np.int32)
+    geom = np.concatenate(geoms).astype(np.float32)
+    fr = np.array(frames, FRUSTUM_FRAME_DTYPE).view(np.uint8)
+    F, O, G = (torch.from_numpy(a).to(dev) for a in (fr, offs, geom))
+    M = torch.zeros(m * 32, dtype=torch.uint8, device=dev)
+    IV = torch.zeros(nf, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        is_in_frustum(F, O, G, M, 0.5, IV)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        is_in_frustum(F, O, G, M, 0.5, IV)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    dev_ms = statistics.median(ms)
+    gpu = M.cpu().numpy().view(pyoracle.MP_DTYPE)
+    # end to end: geometry in page-locked host memory read in place, the
+    # records and counts copied back
+    hG = torch.from_numpy(geom).pin_memory()
+    hM = torch.empty(m * 32, dtype=torch.uint8).pin_memory()
+    hIV = torch.empty(nf, dtype=torch.int32).pin_memory()
+    for it in range(warmup + steps):
+        if it == warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        is_in_frustum(F, O, hG, M, 0.5, IV)
+        hM.copy_(M, non_blocking=True)
+        hIV.copy_(IV, non_blocking=True)
+        stream.synchronize()
+    e2e = m * steps / (time.perf_counter() - t0)
+    o = pyoracle.Oracle()
+    t0 = time.perf_counter()
+    same = True
+    for f in range(nf):
+        rec, _ = o.is_in_frustum(cams_o[f], np.ascontiguousarray(geoms[f]).view(pyoracle.GEOM_DTYPE).reshape(-1),
+                                 0.5)
+        on = rec["track_in_view"] == 1
+        same &= bool(np.array_equal(on, gpu[f * per:(f + 1) * per]["track_in_view"] == 1))
+    cpu_s = time.perf_counter() - t0
+    pk, pk_src = peaks()
+    alg = m * (32 + 24) + 4 * (nf + 1) + fr.nbytes  # geometry in, fields out
+    return {"metric": "map points/s (isInFrustum + PredictScale)", "frames": nf, "map_points": m,
+            "value": m / (dev_ms / 1e3), "ms": dev_ms, "gpu_launches_per_step": 2,
+            "in_view": int(IV.sum().item()),
+            "e2e": {"value": e2e, "unit": "map points/s", "h2d_bytes_per_step": int(geom.nbytes),
+                    "d2h_bytes_per_step": int(m * 32 + 4 * nf)},
+            "roofline": {"bound": "hbm", "kernel": "k_is_in_frustum", "achieved": alg / (dev_ms / 1e3) / 1e9,
+                         "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": alg / (dev_ms / 1e3) / 1e9 / pk["hbm_gbs"], "algorithmic_bytes_per_step": alg,
+                         "peak_source": pk_src},
+            "cpu_baseline": {"value": m / cpu_s, "unit": "map points/s", "cores": 1, "kind": "port",
+                             "sample": "all 320,000 map points, oracle restatement"},
+            "in_view_equal_to_oracle": same}
+
+
 def bench_serving(dev, duration_s=3.0):
     """32 camera streams, Poisson 30 Hz each, mixed 640x480/1241x376/1280x720,
     nFeatures 1000-2000: every frame is extracted and matched against its
@@ -696,7 +778,7 @@ def main():
     ap.add_argument("--shapes", default="",
                     help="pin the launch shapes resize_rows,fast_cells_per_block,describe_group (no tuning)")
     ap.add_argument("--legs", default="all",
-                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,distinctive,cpu) "
+                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,distinctive,frustum,cpu) "
                          "or 'all'")
     args = ap.parse_args()
     NFRAMES = args.frames
