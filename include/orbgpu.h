@@ -168,6 +168,23 @@ int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame* f, const 
                                 const uint8_t* mp_descriptors, int n_mappoints, float th, const uint8_t* claimed,
                                 int* match_out, int mem, int* nmatches);
 
+/* Frame::UndistortKeyPoints() -- src/Frame.cc:724-776 -- for n keypoints of
+ * one camera: out[i] = kps[i] with x, y through cv::undistortPoints(pts, pts,
+ * mK, mDistCoef, cv::Mat(), mK) (OpenCV 3.2's algorithm: double precision,
+ * five fixed-point rounds).  K4 = fx, fy, cx, cy (mK); dist = mDistCoef, k1
+ * k2 p1 p2 [k3] (ndist 4 or 5); host arrays.  A zero k1 copies the keypoints
+ * unchanged, as the reference does whatever the other coefficients.
+ * kps / out: device or page-locked host memory (out may be kps).
+ * Asynchronous on 'stream'; one kernel launch. */
+int orbgpu_undistort_keypoints(const orbgpu_keypoint* kps, int n, const float* K4, const float* dist, int ndist,
+                               orbgpu_keypoint* out, void* stream);
+
+/* Frame::ComputeImageBounds(imLeft) -- src/Frame.cc:778-819 -- for an image
+ * of cols x rows: bounds = mnMinX, mnMaxX, mnMinY, mnMaxY (the undistorted
+ * corners, or the image rectangle when k1 is zero).  Host only, with the
+ * same arithmetic as orbgpu_undistort_keypoints. */
+int orbgpu_compute_image_bounds(int cols, int rows, const float* K4, const float* dist, int ndist, float* bounds);
+
 /* The map point fields Frame::isInFrustum reads (src/Frame.cc:491-578). */
 typedef struct {
     float x, y, z;          /* MapPoint::GetWorldPos() */

@@ -216,12 +216,15 @@ Mat Mat::cross(const Mat& m) const {
 }
 
 Mat Mat::reshape(int cn, int r) const {
+    // OpenCV's rule: the row count stays unless given; the row width in
+    // scalars (cols x channels) is redistributed over the new channel count
     Mat m = isContinuous() ? *this : clone();
-    int total_elems = m.rows * m.cols * m.channels();
-    int ncn = cn == 0 ? m.channels() : cn;
-    int nrows = r == 0 ? (m.rows * m.cols * m.channels()) / (ncn * m.cols) : r;
-    if (r == 0 && (m.cols * m.channels()) % ncn != 0) nrows = total_elems / ncn;
-    int ncols = total_elems / (ncn * nrows);
+    const int total_elems = m.rows * m.cols * m.channels();
+    const int ncn = cn == 0 ? m.channels() : cn;
+    const int nrows = r == 0 ? m.rows : r;
+    if (nrows <= 0 || total_elems % nrows != 0 || (total_elems / nrows) % ncn != 0)
+        shim_unsupported("reshape to a shape that does not divide the element count");
+    const int ncols = total_elems / nrows / ncn;
     m.flags = CV_MAKETYPE(m.depth(), ncn);
     m.rows = nrows;
     m.cols = ncols;
@@ -386,8 +389,73 @@ void FAST(InputArray _img, std::vector<KeyPoint>& keypoints, int threshold, bool
 void KeyPointsFilter::retainBest(std::vector<KeyPoint>&, int) { shim_unsupported("retainBest"); }
 
 // ---------------------------------------------------------------- calib3d
-void undistortPoints(InputArray, OutputArray, InputArray, InputArray, InputArray, InputArray) {
-    shim_unsupported("undistortPoints (only needed for non-zero distortion)");
+// cv::undistortPoints as OpenCV 3.2's cvUndistortPoints computes it, for the
+// forms ORB-SLAM2 uses (2-channel float points, a 3x3 camera matrix, 4/5/8
+// distortion coefficients k1 k2 p1 p2 [k3 [k4 k5 k6]], no R, P = a 3x3
+// matrix or none).  Everything in double: normalise with 1/fx, 1/fy; with
+// coefficients, 5 fixed-point rounds x = (x0 - delta_x) * icdist; then
+// P * R applied (R the identity) and the result rounded to float.  The
+// thin-prism and tilt terms of later versions are zero for these
+// coefficient counts and leave every value unchanged.
+void undistortPoints(InputArray src_, OutputArray dst_, InputArray K_, InputArray dist_, InputArray R_,
+                     InputArray P_) {
+    const Mat src = src_.getMat();
+    if (src.depth() != CV_32F || src.channels() != 2 || !src.isContinuous())
+        shim_unsupported("undistortPoints: only continuous 2-channel float points");
+    if (!R_.empty()) shim_unsupported("undistortPoints: R");
+    const Mat K = K_.getMat();
+    double A[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) A[i][j] = get_elem(K, i, j);
+    double k[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int iters = 1;
+    if (!dist_.empty()) {
+        const Mat D = dist_.getMat();
+        const int nk = D.rows * D.cols * D.channels();
+        if (nk != 4 && nk != 5 && nk != 8) shim_unsupported("undistortPoints: distortion coefficient count");
+        for (int i = 0; i < nk; i++) k[i] = get_elem(D, D.cols == 1 ? i : 0, D.cols == 1 ? 0 : i);
+        iters = 5;
+    }
+    double RR[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    if (!P_.empty()) {
+        const Mat P = P_.getMat();
+        double PP[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) PP[i][j] = get_elem(P, i, j);
+        double T[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double s = 0;
+                for (int q = 0; q < 3; q++) s += PP[i][q] * RR[q][j];
+                T[i][j] = s;
+            }
+        std::memcpy(RR, T, sizeof(T));
+    }
+    const double fx = A[0][0], fy = A[1][1], ifx = 1. / fx, ify = 1. / fy, cx = A[0][2], cy = A[1][2];
+    const int n = src.rows * src.cols;
+    std::vector<float> out((size_t)n * 2);
+    const float* in = (const float*)src.data;
+    for (int i = 0; i < n; i++) {
+        double x = in[2 * i], y = in[2 * i + 1];
+        double x0 = x = (x - cx) * ifx;
+        double y0 = y = (y - cy) * ify;
+        for (int j = 0; j < iters; j++) {
+            const double r2 = x * x + y * y;
+            const double icdist = (1 + ((k[7] * r2 + k[6]) * r2 + k[5]) * r2) / (1 + ((k[4] * r2 + k[1]) * r2 + k[0]) * r2);
+            const double deltaX = 2 * k[2] * x * y + k[3] * (r2 + 2 * x * x);
+            const double deltaY = k[2] * (r2 + 2 * y * y) + 2 * k[3] * x * y;
+            x = (x0 - deltaX) * icdist;
+            y = (y0 - deltaY) * icdist;
+        }
+        const double xx = RR[0][0] * x + RR[0][1] * y + RR[0][2];
+        const double yy = RR[1][0] * x + RR[1][1] * y + RR[1][2];
+        const double ww = 1. / (RR[2][0] * x + RR[2][1] * y + RR[2][2]);
+        out[2 * i] = (float)(xx * ww);
+        out[2 * i + 1] = (float)(yy * ww);
+    }
+    Mat& dst = dst_.getMatRef();
+    if (dst.data != src.data || dst.type() != src.type()) dst.create(src.rows, src.cols, src.type());
+    std::memcpy(dst.data, out.data(), out.size() * sizeof(float));
 }
 
 }  // namespace cv

@@ -850,6 +850,61 @@ int orc_distribute(const orc_kp* cand, int n, int minX, int maxX, int minY, int 
     return (int)r.size();
 }
 
+// cv::undistortPoints(src, dst, K, dist, noArray(), K) as Frame calls it,
+// restated from OpenCV 3.2's cvUndistortPoints: normalise by the camera
+// matrix in double, 5 rounds of x = (x0 - tangential) / radial, back through
+// K, rounded to float.  k = k1 k2 p1 p2 k3 (k3 = 0 for four coefficients).
+static void undistort_point(double fx, double fy, double cx, double cy, const double* k, float& u, float& v) {
+    const double ifx = 1. / fx, ify = 1. / fy;
+    const double x0 = (u - cx) * ifx, y0 = (v - cy) * ify;
+    double x = x0, y = y0;
+    for (int it = 0; it < 5; it++) {
+        const double r2 = x * x + y * y;
+        const double radial = 1 + ((k[4] * r2 + k[1]) * r2 + k[0]) * r2;
+        const double icdist = 1 / radial;
+        const double dx = 2 * k[2] * x * y + k[3] * (r2 + 2 * x * x);
+        const double dy = k[2] * (r2 + 2 * y * y) + 2 * k[3] * x * y;
+        x = (x0 - dx) * icdist;
+        y = (y0 - dy) * icdist;
+    }
+    u = (float)(fx * x + 0.0 * y + cx);
+    v = (float)(0.0 * x + fy * y + cy);
+}
+
+// Frame::UndistortKeyPoints, src/Frame.cc:724-776: nothing to do when the
+// first coefficient is zero (whatever the others), else every keypoint
+// through undistort_point (the other keypoint fields are copied).
+int orc_undistort_keypoints(const float* K4, const float* dist, int ndist, const orc_kp* kps, int n, orc_kp* out) {
+    double k[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < ndist && i < 5; i++) k[i] = dist[i];
+    for (int i = 0; i < n; i++) {
+        out[i] = kps[i];
+        if (dist[0] != 0.0f) undistort_point(K4[0], K4[1], K4[2], K4[3], k, out[i].x, out[i].y);
+    }
+    return 0;
+}
+
+// Frame::ComputeImageBounds, src/Frame.cc:778-819: the undistorted corners
+// give min over the left / top pair and max over the right / bottom pair.
+int orc_compute_image_bounds(int cols, int rows, const float* K4, const float* dist, int ndist, float* bounds) {
+    if (dist[0] == 0.0f) {
+        bounds[0] = 0.0f;
+        bounds[1] = (float)cols;
+        bounds[2] = 0.0f;
+        bounds[3] = (float)rows;
+        return 0;
+    }
+    double k[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < ndist && i < 5; i++) k[i] = dist[i];
+    float cx[4] = {0.0f, (float)cols, 0.0f, (float)cols}, cy[4] = {0.0f, 0.0f, (float)rows, (float)rows};
+    for (int c = 0; c < 4; c++) undistort_point(K4[0], K4[1], K4[2], K4[3], k, cx[c], cy[c]);
+    bounds[0] = std::min(cx[0], cx[2]);
+    bounds[1] = std::max(cx[1], cx[3]);
+    bounds[2] = std::min(cy[0], cy[1]);
+    bounds[3] = std::max(cy[2], cy[3]);
+    return 0;
+}
+
 // Frame::isInFrustum, src/Frame.cc:491-578, as the reference computes it
 // against the cv stand-in: the pose matrices of Frame::UpdatePoseMatrices
 // (:454-470; mOw = -mRcw^T mtcw), Pc = mRcw * P + mtcw with the product

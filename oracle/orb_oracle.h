@@ -50,6 +50,12 @@ int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
  * best_rows: chosen row, -1 none valid, -2 invalid list (the harness version
  * reports -3: the reference exposes only the descriptor).  desc_inout
  * (nullable) gets the chosen descriptor, unchanged where best_rows < 0. */
+/* Frame::UndistortKeyPoints (src/Frame.cc:724-776) and ComputeImageBounds
+ * (:778-819) with cv::undistortPoints restated from OpenCV 3.2.  K4 = fx, fy,
+ * cx, cy; dist = k1 k2 p1 p2 [k3] (ndist 4 or 5); bounds = mnMinX, mnMaxX,
+ * mnMinY, mnMaxY. */
+int orc_undistort_keypoints(const float* K4, const float* dist, int ndist, const orc_kp* kps, int n, orc_kp* out);
+int orc_compute_image_bounds(int cols, int rows, const float* K4, const float* dist, int ndist, float* bounds);
 /* Frame::isInFrustum(pMP, cos_limit) (src/Frame.cc:491-578, pose matrices of
  * Frame::UpdatePoseMatrices :454-470, MapPoint::PredictScale
  * src/MapPoint.cc:604-619) for m map points of one frame; out holds the map

@@ -247,6 +247,27 @@ class _Base:
         return tuple(o[:nq].copy() for o in outs)
 
 
+    def undistort_keypoints(self, K4, dist, kps):
+        """Frame::UndistortKeyPoints: the keypoints with undistorted x, y."""
+        K = np.ascontiguousarray(K4, np.float32)
+        d = np.ascontiguousarray(dist, np.float32)
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        out = np.zeros(max(len(kps), 1), KP_DTYPE)
+        f = self.fn("undistort_keypoints")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+        f(_p(K), _p(d), len(d), _p(kps), len(kps), _p(out))
+        return out[:len(kps)].copy()
+
+    def compute_image_bounds(self, cols, rows, K4, dist):
+        """Frame::ComputeImageBounds -> (mnMinX, mnMaxX, mnMinY, mnMaxY)."""
+        K = np.ascontiguousarray(K4, np.float32)
+        d = np.ascontiguousarray(dist, np.float32)
+        b = np.zeros(4, np.float32)
+        f = self.fn("compute_image_bounds")
+        f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        f(int(cols), int(rows), _p(K), _p(d), len(d), _p(b))
+        return b
+
     def is_in_frustum(self, cam, mps, cos_limit=0.5, initial=None):
         """Frame::isInFrustum for every map point (GEOM_DTYPE records) of one
         frame; returns (MP_DTYPE records after the call, number in view)."""

@@ -483,6 +483,52 @@ int ref_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
     return 0;
 }
 
+// A frame carrying only the camera of the undistortion functions: mK and
+// mDistCoef as the Frame constructors store them (src/Frame.cc:121-206).
+static Frame* camera_frame(const float* K4, const float* dist, int ndist) {
+    Frame* F = new Frame();
+    F->mK = cv::Mat::eye(3, 3, CV_32F);
+    F->mK.at<float>(0, 0) = K4[0];
+    F->mK.at<float>(1, 1) = K4[1];
+    F->mK.at<float>(0, 2) = K4[2];
+    F->mK.at<float>(1, 2) = K4[3];
+    F->mDistCoef = cv::Mat(ndist, 1, CV_32F);
+    for (int i = 0; i < ndist; i++) F->mDistCoef.at<float>(i) = dist[i];
+    return F;
+}
+
+// Frame::UndistortKeyPoints -- src/Frame.cc:724-776.  K4 = fx, fy, cx, cy;
+// dist = k1 k2 p1 p2 [k3] (ndist 4 or 5).
+int ref_undistort_keypoints(const float* K4, const float* dist, int ndist, const orc_kp* kps, int n, orc_kp* out) {
+    ArenaScope scope;
+    {
+        Frame* F = camera_frame(K4, dist, ndist);
+        F->N = n;
+        F->mvKeys = kps_in(kps, n);
+        F->UndistortKeyPoints();
+        copy_kps_out(F->mvKeysUn, out);
+        delete F;
+    }
+    return 0;
+}
+
+// Frame::ComputeImageBounds -- src/Frame.cc:778-819; bounds = mnMinX,
+// mnMaxX, mnMinY, mnMaxY.
+int ref_compute_image_bounds(int cols, int rows, const float* K4, const float* dist, int ndist, float* bounds) {
+    ArenaScope scope;
+    {
+        Frame* F = camera_frame(K4, dist, ndist);
+        cv::Mat im(rows, cols, CV_8U);
+        F->ComputeImageBounds(im);
+        bounds[0] = Frame::mnMinX;
+        bounds[1] = Frame::mnMaxX;
+        bounds[2] = Frame::mnMinY;
+        bounds[3] = Frame::mnMaxY;
+        delete F;
+    }
+    return 0;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

@@ -10,4 +10,4 @@ from ._lib import (FRAME_MAPPOINT_DTYPE, FRUSTUM_FRAME_DTYPE, KEYPOINT_DTYPE, MA
 from .extractor import ORBextractor  # noqa: F401
 from .matcher import ORBmatcher, FrameView, compute_stereo_matches  # noqa: F401
 from .mappoints import compute_distinctive_descriptors, observations_to_csr  # noqa: F401
-from .frustum import frustum_frame, is_in_frustum  # noqa: F401
+from .frustum import compute_image_bounds, frustum_frame, is_in_frustum, undistort_keypoints  # noqa: F401

@@ -33,7 +33,7 @@ SOURCES = [
     "orbgpu_knn.cu",
     "orbgpu_knn_tc.cu",
     "orbgpu_mappoint.cu",
-    "orbgpu_frustum.cu",
+    "orbgpu_geometry.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,7 +1,14 @@
-// orbgpu_frustum.cu -- Frame::isInFrustum (src/Frame.cc:491-578) with
-// MapPoint::PredictScale(dist, Frame*) (src/MapPoint.cc:604-619) for the map
-// points of many frames in one launch, writing the records the projection
-// searches read.
+// orbgpu_geometry.cu -- per-frame geometry on the device:
+// Frame::UndistortKeyPoints / ComputeImageBounds (src/Frame.cc:724-819) and
+// Frame::isInFrustum (src/Frame.cc:491-578) with MapPoint::PredictScale(dist,
+// Frame*) (src/MapPoint.cc:604-619) for the map points of many frames in one
+// launch, writing the records the projection searches read.
+//
+// Undistortion is cv::undistortPoints as Frame calls it (new camera matrix =
+// the camera matrix, no rectification), restated from OpenCV 3.2's
+// cvUndistortPoints: in double, normalise with 1/fx, 1/fy, five rounds of
+// x = (x0 - tangential) / radial, back through the camera matrix, rounded to
+// float.  The same routine runs on the host for the image bounds.
 //
 // Float semantics follow the compiled reference against the cv stand-in:
 // mRcw * P accumulates in double (float products are exact in double) and is
@@ -13,6 +20,7 @@
 // from per-level thresholds that orbgpu_frustum_frame_init finds with the
 // host's logf (the quotient is monotone in ratio), so no device logarithm is
 // involved.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -22,6 +30,61 @@ namespace orbgpu {
 
 #define FR_THREADS 256
 #define FR_BLOCKS_PER_SM 4
+
+// One camera of the undistortion: the camera matrix entries as doubles,
+// 1/fx and 1/fy, and k1 k2 p1 p2 k3 (k3 = 0 for four coefficients).
+struct UndistortCamera {
+    double fx, fy, cx, cy, ifx, ify;
+    double k[5];
+};
+
+// One point through cv::undistortPoints(src, dst, K, dist, noArray(), K).
+// Plain double operators: device code is compiled without FMA contraction
+// (-fmad=false) and host code with -ffp-contract=off, so both evaluate the
+// same IEEE operations in this order.
+__host__ __device__ inline void undistort_point(const UndistortCamera& c, float& u, float& v) {
+    const double x0 = ((double)u - c.cx) * c.ifx;
+    const double y0 = ((double)v - c.cy) * c.ify;
+    double x = x0, y = y0;
+    for (int it = 0; it < 5; it++) {
+        const double r2 = x * x + y * y;
+        const double icdist = 1.0 / (1 + ((c.k[4] * r2 + c.k[1]) * r2 + c.k[0]) * r2);
+        const double dx = 2 * c.k[2] * x * y + c.k[3] * (r2 + 2 * x * x);
+        const double dy = c.k[2] * (r2 + 2 * y * y) + 2 * c.k[3] * x * y;
+        x = (x0 - dx) * icdist;
+        y = (y0 - dy) * icdist;
+    }
+    u = (float)(c.fx * x + 0.0 * y + c.cx);
+    v = (float)(0.0 * x + c.fy * y + c.cy);
+}
+
+static bool undistort_camera(const float* K4, const float* dist, int ndist, UndistortCamera* c) {
+    if (!K4 || !dist || (ndist != 4 && ndist != 5)) return false;
+    c->fx = K4[0];
+    c->fy = K4[1];
+    c->cx = K4[2];
+    c->cy = K4[3];
+    c->ifx = 1. / c->fx;
+    c->ify = 1. / c->fy;
+    for (int i = 0; i < 5; i++) c->k[i] = i < ndist ? (double)dist[i] : 0.0;
+    return true;
+}
+
+// Keypoint records are 7 words (x, y, size, angle, response, octave,
+// class_id); one thread per keypoint.
+__global__ void __launch_bounds__(FR_THREADS) k_undistort_keypoints(const float* __restrict__ in, int n,
+                                                                    UndistortCamera cam, int copy_only,
+                                                                    float* __restrict__ out) {
+    const int stride = gridDim.x * FR_THREADS;
+    for (int i = blockIdx.x * FR_THREADS + threadIdx.x; i < n; i += stride) {
+        float w[7];
+#pragma unroll
+        for (int q = 0; q < 7; q++) w[q] = in[7 * (size_t)i + q];
+        if (!copy_only) undistort_point(cam, w[0], w[1]);
+#pragma unroll
+        for (int q = 0; q < 7; q++) out[7 * (size_t)i + q] = w[q];
+    }
+}
 
 __global__ void __launch_bounds__(FR_THREADS) k_is_in_frustum(const orbgpu_frustum_frame* __restrict__ frames,
                                                               int nframes, const int* __restrict__ offsets,
@@ -125,6 +188,48 @@ float level_threshold(float log_scale, int n) {
 }  // namespace orbgpu
 
 using namespace orbgpu;
+
+extern "C" int orbgpu_undistort_keypoints(const orbgpu_keypoint* kps, int n, const float* K4, const float* dist,
+                                          int ndist, orbgpu_keypoint* out, void* stream) {
+    UndistortCamera cam;
+    if (n < 0 || (n > 0 && (!kps || !out)) || !undistort_camera(K4, dist, ndist, &cam)) {
+        orbgpu_set_last_error("orbgpu_undistort_keypoints: bad arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (n == 0) return ORBGPU_OK;
+    // the reference returns mvKeys unchanged when mDistCoef(0) == 0
+    const int copy_only = dist[0] == 0.0f ? 1 : 0;
+    const int blocks = (int)std::min<long long>(((long long)n + FR_THREADS - 1) / FR_THREADS,
+                                                (long long)nsm_of_current_device() * FR_BLOCKS_PER_SM * 2);
+    k_undistort_keypoints<<<blocks, FR_THREADS, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float*>(kps), n, cam, copy_only, reinterpret_cast<float*>(out));
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_compute_image_bounds(int cols, int rows, const float* K4, const float* dist, int ndist,
+                                           float* bounds) {
+    UndistortCamera cam;
+    if (cols < 0 || rows < 0 || !bounds || !undistort_camera(K4, dist, ndist, &cam)) {
+        orbgpu_set_last_error("orbgpu_compute_image_bounds: bad arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (dist[0] == 0.0f) {
+        bounds[0] = 0.0f;
+        bounds[1] = (float)cols;
+        bounds[2] = 0.0f;
+        bounds[3] = (float)rows;
+        return ORBGPU_OK;
+    }
+    // corners top-left, top-right, bottom-left, bottom-right
+    float u[4] = {0.0f, (float)cols, 0.0f, (float)cols}, v[4] = {0.0f, 0.0f, (float)rows, (float)rows};
+    for (int c = 0; c < 4; c++) undistort_point(cam, u[c], v[c]);
+    bounds[0] = std::min(u[0], u[2]);
+    bounds[1] = std::max(u[1], u[3]);
+    bounds[2] = std::min(v[0], v[1]);
+    bounds[3] = std::max(v[2], v[3]);
+    return ORBGPU_OK;
+}
 
 extern "C" int orbgpu_frustum_frame_init(const float* Tcw, float fx, float fy, float cx, float cy, float bf,
                                          float min_x, float max_x, float min_y, float max_y, float scale_factor,

@@ -57,3 +57,35 @@ def is_in_frustum(frames, mp_offsets, geometry, mappoints, viewing_cos_limit=0.5
                                      C.c_float(viewing_cos_limit), ptr(mappoints), ptr(in_view), C.c_void_p(st)),
           "orbgpu_is_in_frustum")
     return in_view
+
+
+def undistort_keypoints(keypoints, K4, dist, out=None, stream=None):
+    """Frame::UndistortKeyPoints (src/Frame.cc:724-776) for the keypoints of
+    one camera: keypoints an (n, 7) float32 tensor of KEYPOINT_DTYPE records
+    (device, or page-locked host memory); K4 = fx, fy, cx, cy; dist = k1 k2
+    p1 p2 [k3].  Returns out (a new device tensor unless given; may be the
+    input) with x, y undistorted.  Asynchronous on the current stream."""
+    import torch
+    n = int(keypoints.shape[0])
+    if keypoints.dtype != torch.float32 or keypoints.dim() != 2 or keypoints.shape[1] != 7 \
+            or not keypoints.is_contiguous():
+        raise ValueError("keypoints must be a contiguous (n, 7) float32 tensor")
+    if out is None:
+        out = torch.empty((max(n, 1), 7), dtype=torch.float32, device="cuda")[:n]
+    K = np.ascontiguousarray(K4, np.float32)
+    d = np.ascontiguousarray(dist, np.float32)
+    st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+    check(lib().orbgpu_undistort_keypoints(ptr(keypoints), n, ptr(K), ptr(d), len(d), ptr(out), C.c_void_p(st)),
+          "orbgpu_undistort_keypoints")
+    return out
+
+
+def compute_image_bounds(cols, rows, K4, dist):
+    """Frame::ComputeImageBounds (src/Frame.cc:778-819): (mnMinX, mnMaxX,
+    mnMinY, mnMaxY) of a cols x rows image."""
+    K = np.ascontiguousarray(K4, np.float32)
+    d = np.ascontiguousarray(dist, np.float32)
+    b = np.zeros(4, np.float32)
+    check(lib().orbgpu_compute_image_bounds(int(cols), int(rows), ptr(K), ptr(d), len(d), ptr(b)),
+          "orbgpu_compute_image_bounds")
+    return b

@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort")
 
 
 def main(groups=GROUPS):
@@ -51,6 +51,8 @@ def main(groups=GROUPS):
         distinctive_fixture(R)
     if "frustum" in groups:
         frustum_fixture(R)
+    if "undistort" in groups:
+        undistort_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -233,6 +235,39 @@ def frustum_fixture(R):
                                                                         np.float32),
                        f"{name}_geometry": g, f"{name}_initial": init, f"{name}_out": out, f"{name}_nin": np.array(nin)})
     save("frustum.npz", **arrays)
+
+
+UNDISTORT_CAMERAS = {
+    # name: (fx, fy, cx, cy), (k1 k2 p1 p2 [k3]), width, height
+    "euroc_752x480": ((458.654, 457.296, 367.215, 248.375), (-0.28340811, 0.07395907, 0.00019359, 1.76187114e-05),
+                      752, 480),
+    "tum1_640x480": ((517.306408, 516.469215, 318.643040, 255.313989),
+                     (0.262383, -0.953104, -0.005358, 0.002628, 1.163314), 640, 480),
+    "k1_zero_1241x376": ((718.856, 718.856, 607.1928, 185.2157), (0.0, 0.1, 0.001, 0.0), 1241, 376),
+    "strong_640x480": ((400.0, 400.0, 320.0, 240.0), (-0.4, 0.2, 0.001, -0.002, -0.05), 640, 480),
+}
+
+
+def undistort_fixture(R):
+    # 11. Frame::UndistortKeyPoints and Frame::ComputeImageBounds (the
+    # reference's own functions, cv::undistortPoints restated in the cv stand-in)
+    from oracle.pyoracle import KP_DTYPE
+    rng = np.random.default_rng(71)
+    arrays = {}
+    for name, (K, d, w, h) in UNDISTORT_CAMERAS.items():
+        n = 3000
+        kps = np.zeros(n, KP_DTYPE)
+        kps["x"] = rng.uniform(-4, w + 4, n)
+        kps["y"] = rng.uniform(-4, h + 4, n)
+        kps["size"] = 31.0
+        kps["angle"] = rng.uniform(0, 360, n)
+        kps["response"] = rng.uniform(0, 100, n)
+        kps["octave"] = rng.integers(0, 8, n)
+        arrays.update({f"{name}_K": np.array(K, np.float32), f"{name}_dist": np.array(d, np.float32),
+                       f"{name}_size": np.array([w, h]), f"{name}_keypoints": kps,
+                       f"{name}_undistorted": R.undistort_keypoints(K, d, kps),
+                       f"{name}_bounds": R.compute_image_bounds(w, h, K, d)})
+    save("undistort.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -54,3 +54,13 @@ def test_bad_frame_arguments(init):
         init(np.eye(3, 4), 500, 500, 320, 240, 40, 0, 640, 0, 480, 1.0, 8)
     with pytest.raises(OrbGpuError):
         init(np.eye(3, 4), 500, 500, 320, 240, 40, 0, 640, 0, 480, 1.2, 17)
+
+
+@pytest.mark.parametrize("name", ["euroc_752x480", "tum1_640x480", "k1_zero_1241x376", "strong_640x480"])
+def test_image_bounds_host(init, golden, name):
+    """orbgpu_compute_image_bounds (host) equals the reference's ComputeImageBounds."""
+    from orb_slam2_detailed_comments_gb300 import compute_image_bounds
+    g = golden("undistort.npz")
+    w, h = g[f"{name}_size"]
+    b = compute_image_bounds(int(w), int(h), g[f"{name}_K"], g[f"{name}_dist"])
+    assert b.tobytes() == g[f"{name}_bounds"].tobytes()

@@ -127,3 +127,40 @@ def test_chained_into_search_by_projection(torch, oracle):
                                                          torch.from_numpy(mpd).cuda(), 1.0)
     assert nm == ref_nm
     assert np.array_equal(match.cpu().numpy(), ref_match)
+
+
+UNDISTORT_CASES = ["euroc_752x480", "tum1_640x480", "k1_zero_1241x376", "strong_640x480"]
+
+
+@pytest.mark.parametrize("name", UNDISTORT_CASES)
+@pytest.mark.parametrize("where", ["device", "pinned", "in_place"])
+def test_undistort_golden(torch, golden, name, where):
+    """Frame::UndistortKeyPoints on the GPU equals the reference's (golden)."""
+    from orb_slam2_detailed_comments_gb300 import undistort_keypoints
+    g = golden("undistort.npz")
+    kps = np.ascontiguousarray(g[f"{name}_keypoints"])
+    raw = torch.from_numpy(kps.view(np.float32).reshape(len(kps), 7).copy())
+    if where == "pinned":
+        out = undistort_keypoints(raw.pin_memory(), g[f"{name}_K"], g[f"{name}_dist"])
+    elif where == "in_place":
+        dev = raw.cuda()
+        out = undistort_keypoints(dev, g[f"{name}_K"], g[f"{name}_dist"], out=dev)
+    else:
+        out = undistort_keypoints(raw.cuda(), g[f"{name}_K"], g[f"{name}_dist"])
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tobytes() == g[f"{name}_undistorted"].tobytes()
+
+
+def test_undistort_extractor_output_vs_oracle(torch, oracle):
+    """Keypoints straight from the GPU extractor, undistorted on the device."""
+    from orb_slam2_detailed_comments_gb300 import ORBextractor, undistort_keypoints
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    img = syn.scene(752, 480, 33)
+    ex = ORBextractor(1500, 1.2, 8, 20, 7, 752, 480)
+    kd, _ = ex(torch.from_numpy(img).cuda(), device_out=True)
+    K, d = (458.654, 457.296, 367.215, 248.375), (-0.28340811, 0.07395907, 0.00019359, 1.76187114e-05)
+    out = undistort_keypoints(kd, K, d)
+    torch.cuda.synchronize()
+    host = kd.cpu().numpy().view(pyoracle.KP_DTYPE).reshape(-1)
+    ref = oracle.undistort_keypoints(K, d, host)
+    assert out.cpu().numpy().tobytes() == ref.tobytes()

@@ -224,3 +224,18 @@ def test_is_in_frustum_reference_fresh_seeds(oracle):
         a, na = oracle.is_in_frustum(cam, geom, 0.5)
         b, nb = R.is_in_frustum(cam, geom, 0.5)
         assert na == nb and a.tobytes() == b.tobytes(), seed
+
+
+# Frame::UndistortKeyPoints / ComputeImageBounds (src/Frame.cc:724-819)
+UNDISTORT_CASES = ["euroc_752x480", "tum1_640x480", "k1_zero_1241x376", "strong_640x480"]
+
+
+@pytest.mark.parametrize("name", UNDISTORT_CASES)
+def test_undistort_golden(oracle, golden, name):
+    g = golden("undistort.npz")
+    K, d, (w, h) = g[f"{name}_K"], g[f"{name}_dist"], g[f"{name}_size"]
+    out = oracle.undistort_keypoints(K, d, g[f"{name}_keypoints"])
+    assert out.tobytes() == g[f"{name}_undistorted"].tobytes()
+    assert oracle.compute_image_bounds(w, h, K, d).tobytes() == g[f"{name}_bounds"].tobytes()
+    if name.startswith("k1_zero"):
+        assert out.tobytes() == g[f"{name}_keypoints"].tobytes()
