@@ -13,6 +13,11 @@
 #include "orb_oracle.h"
 
 #include <algorithm>
+#include <array>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -970,6 +975,172 @@ int orc_is_in_frustum(const orc_frustum_camera* cam, const orc_mp_geometry* mps,
     }
     return nin;
 }
+
+// ---------------------------------------------------------------- DBoW2
+// The vocabulary tree of Thirdparty/DBoW2/DBoW2/TemplatedVocabulary.h as
+// loadFromTextFile (:1368-1460) builds it: node 0 the root, then one node per
+// line in file order ("parent is_leaf d0 .. d31 weight"), appended to its
+// parent's children; leaves (by the file flag) numbered as words in file
+// order.  The descent stops at a node without children (Node::isLeaf).
+namespace {
+struct OrcVocab {
+    int k = 0, L = 0, scoring = 0, weighting = 0, nwords = 0;
+    std::vector<std::vector<int> > children;
+    std::vector<std::array<uint8_t, 32> > desc;
+    std::vector<double> weight;
+    std::vector<int> word_id;
+};
+std::map<std::string, OrcVocab> g_vocabs;
+
+bool load_vocab(const std::string& path, OrcVocab& v) {
+    std::ifstream f(path.c_str());
+    if (!f.is_open()) return false;
+    std::string line;
+    if (!std::getline(f, line)) return false;
+    std::stringstream hs(line);
+    int n1 = -1, n2 = -1;
+    hs >> v.k >> v.L >> n1 >> n2;
+    if (v.k < 0 || v.k > 20 || v.L < 1 || v.L > 10 || n1 < 0 || n1 > 5 || n2 < 0 || n2 > 3) return false;
+    v.scoring = n1;
+    v.weighting = n2;
+    v.children.assign(1, std::vector<int>());
+    v.desc.assign(1, std::array<uint8_t, 32>());
+    v.weight.assign(1, 0.0);
+    v.word_id.assign(1, 0);
+    while (std::getline(f, line)) {
+        if (line.empty()) return false;  // the reference would append a node of unset bytes
+        std::stringstream ls(line);
+        const int nid = (int)v.children.size();
+        int pid = -1, leaf = 0;
+        ls >> pid >> leaf;
+        if (ls.fail() || pid < 0 || pid >= nid) return false;
+        std::array<uint8_t, 32> d;
+        for (int i = 0; i < 32; i++) {
+            int b = 0;
+            ls >> b;
+            d[i] = (uint8_t)b;
+        }
+        double w = 0;
+        ls >> w;
+        if (ls.fail()) return false;
+        v.children.push_back(std::vector<int>());
+        v.children[pid].push_back(nid);
+        v.desc.push_back(d);
+        v.weight.push_back(w);
+        v.word_id.push_back(leaf > 0 ? v.nwords++ : 0);
+    }
+    return true;
+}
+
+// TemplatedVocabulary::transform(feature, word_id, weight, nid, levelsup),
+// TemplatedVocabulary.h:1240-1290: from the root, the first child with the
+// least distance at every level (strict <), the node of level L - levelsup
+// kept for the feature vector (the root when that level is <= 0).
+void vocab_descend(const OrcVocab& v, const uint8_t* f, int levelsup, int& word, double& weight, int& nid) {
+    const int nid_level = v.L - levelsup;
+    nid = 0;
+    int node = 0, level = 0;
+    do {
+        ++level;
+        const std::vector<int>& ch = v.children[node];
+        int best = ch[0];
+        int best_d = hamming(f, v.desc[best].data());
+        for (size_t c = 1; c < ch.size(); c++) {
+            const int d = hamming(f, v.desc[ch[c]].data());
+            if (d < best_d) {
+                best_d = d;
+                best = ch[c];
+            }
+        }
+        node = best;
+        if (level == nid_level) nid = node;
+    } while (!v.children[node].empty());
+    word = v.word_id[node];
+    weight = v.weight[node];
+}
+}  // namespace
+
+extern "C" {
+
+int orc_vocabulary_load(const char* path) {
+    OrcVocab v;
+    if (!load_vocab(path, v)) return -1;
+    g_vocabs[path] = v;
+    return v.nwords;
+}
+
+// TemplatedVocabulary::transform(features, BowVector, FeatureVector,
+// levelsup), TemplatedVocabulary.h:1136-1205, with BowVector::addWeight /
+// addIfNotExist / normalize (BowVector.cpp:40-95) and
+// FeatureVector::addFeature (FeatureVector.cpp:37-53), as Frame::ComputeBoW
+// (src/Frame.cc:704-718) calls it with levelsup 4.  Per feature: word, weight
+// and feature-vector node.  BowVector: bow_n (word, value) pairs in ascending
+// word order.  FeatureVector: fv_n nodes in ascending order, node i owning
+// fv_features[fv_offsets[i] .. fv_offsets[i + 1]) in feature order.
+int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup, int* word_ids, double* weights,
+                      int* node_ids, int* bow_n, int* bow_words, double* bow_values, int* fv_n, int* fv_nodes,
+                      int* fv_offsets, int* fv_features) {
+    auto it = g_vocabs.find(path);
+    if (it == g_vocabs.end()) return -1;
+    const OrcVocab& v = it->second;
+    std::map<int, double> bow;
+    std::map<int, std::vector<int> > fv;
+    if (v.nwords > 0) {
+        const bool tf = v.weighting == 0 || v.weighting == 1;  // TF_IDF, TF
+        for (int i = 0; i < n; i++) {
+            int w_id, nid;
+            double w;
+            vocab_descend(v, desc + (size_t)i * 32, levelsup, w_id, w, nid);
+            word_ids[i] = w_id;
+            weights[i] = w;
+            node_ids[i] = nid;
+            if (!(w > 0)) continue;
+            auto b = bow.find(w_id);
+            if (b == bow.end()) bow[w_id] = w;
+            else if (tf) b->second += w;
+            fv[nid].push_back(i);
+        }
+        // L1 for L1 / chi-square / KL / Bhattacharyya, L2 for L2, none for
+        // the dot product (ScoringObject.h:84-89)
+        const bool must = v.scoring != 5;
+        if (tf && !bow.empty() && !must) {
+            const double nd = (double)bow.size();
+            for (auto& e : bow) e.second /= nd;
+        }
+        if (must) {
+            double norm = 0.0;
+            if (v.scoring != 1) {
+                for (auto& e : bow) norm += std::fabs(e.second);
+            } else {
+                for (auto& e : bow) norm += e.second * e.second;
+                norm = std::sqrt(norm);
+            }
+            if (norm > 0.0)
+                for (auto& e : bow) e.second /= norm;
+        }
+    } else {
+        for (int i = 0; i < n; i++) word_ids[i] = node_ids[i] = -1, weights[i] = 0.0;
+    }
+    int b = 0;
+    for (auto& e : bow) {
+        bow_words[b] = e.first;
+        bow_values[b] = e.second;
+        b++;
+    }
+    *bow_n = b;
+    int nn = 0, off = 0;
+    for (auto& e : fv) {
+        fv_nodes[nn] = e.first;
+        fv_offsets[nn] = off;
+        for (int f : e.second) fv_features[off++] = f;
+        nn++;
+    }
+    fv_offsets[nn] = off;
+    *fv_n = nn;
+    return 0;
+}
+
+}  // extern "C"
 
 // MapPoint::PredictScale(currentDist, Frame*), src/MapPoint.cc:604-619, on
 // given ratios mfMaxDistance / currentDist.

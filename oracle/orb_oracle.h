@@ -50,6 +50,15 @@ int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
  * best_rows: chosen row, -1 none valid, -2 invalid list (the harness version
  * reports -3: the reference exposes only the descriptor).  desc_inout
  * (nullable) gets the chosen descriptor, unchanged where best_rows < 0. */
+/* DBoW2 (Thirdparty/DBoW2/DBoW2/TemplatedVocabulary.h): loads a text
+ * vocabulary (loadFromTextFile) under its path, returns its word count or -1;
+ * orc_bow_transform is transform(features, BowVector, FeatureVector,
+ * levelsup) on n descriptors with the vocabulary loaded from path (see
+ * orb_oracle.cpp for the output layout). */
+int orc_vocabulary_load(const char* path);
+int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup, int* word_ids, double* weights,
+                      int* node_ids, int* bow_n, int* bow_words, double* bow_values, int* fv_n, int* fv_nodes,
+                      int* fv_offsets, int* fv_features);
 /* Frame::UndistortKeyPoints (src/Frame.cc:724-776) and ComputeImageBounds
  * (:778-819) with cv::undistortPoints restated from OpenCV 3.2.  K4 = fx, fy,
  * cx, cy; dist = k1 k2 p1 p2 [k3] (ndist 4 or 5); bounds = mnMinX, mnMaxX,

@@ -247,6 +247,35 @@ class _Base:
         return tuple(o[:nq].copy() for o in outs)
 
 
+    def vocabulary_load(self, path):
+        """TemplatedVocabulary::loadFromTextFile; the word count, -1 on failure."""
+        f = self.fn("vocabulary_load")
+        f.argtypes = [C.c_char_p]
+        return int(f(path.encode()))
+
+    def bow_transform(self, path, desc, levelsup=4):
+        """TemplatedVocabulary::transform(features, BowVector, FeatureVector,
+        levelsup) with the vocabulary loaded from path."""
+        desc = np.ascontiguousarray(desc, np.uint8).reshape(-1, 32)
+        n = len(desc)
+        m = max(n, 1)
+        word, node = np.zeros(m, np.int32), np.zeros(m, np.int32)
+        weight = np.zeros(m, np.float64)
+        bw, bv = np.zeros(m, np.int32), np.zeros(m, np.float64)
+        fn, fo, ff = np.zeros(m, np.int32), np.zeros(m + 1, np.int32), np.zeros(m, np.int32)
+        bn, fnn = C.c_int(0), C.c_int(0)
+        f = self.fn("bow_transform")
+        f.argtypes = [C.c_char_p, C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_void_p] * 3 + \
+            [C.c_void_p] * 4
+        rc = f(path.encode(), _p(desc), n, levelsup, _p(word), _p(weight), _p(node), C.byref(bn), _p(bw), _p(bv),
+               C.byref(fnn), _p(fn), _p(fo), _p(ff))
+        if rc != 0:
+            raise RuntimeError("vocabulary not loaded")
+        b, q = bn.value, fnn.value
+        return {"word": word[:n].copy(), "weight": weight[:n].copy(), "node": node[:n].copy(),
+                "bow_words": bw[:b].copy(), "bow_values": bv[:b].copy(), "fv_nodes": fn[:q].copy(),
+                "fv_offsets": fo[:q + 1].copy(), "fv_features": ff[:fo[q]].copy()}
+
     def undistort_keypoints(self, K4, dist, kps):
         """Frame::UndistortKeyPoints: the keypoints with undistorted x, y."""
         K = np.ascontiguousarray(K4, np.float32)

@@ -529,6 +529,63 @@ int ref_compute_image_bounds(int cols, int rows, const float* K4, const float* d
     return 0;
 }
 
+// DBoW2 vocabularies loaded by ORBVocabulary::loadFromTextFile, by path
+// (allocated outside any call's arena scope: they live until exit).
+static std::map<std::string, ORBVocabulary*> g_ref_vocabs;
+
+int ref_vocabulary_load(const char* path) {
+    ORBVocabulary* v = new ORBVocabulary();
+    if (!v->loadFromTextFile(path)) return -1;
+    g_ref_vocabs[path] = v;
+    return (int)v->size();
+}
+
+// ORBVocabulary::transform(features, mBowVec, mFeatVec, levelsup) as
+// Frame::ComputeBoW calls it (src/Frame.cc:704-718), plus the per-feature
+// transform(feature, word, weight, &nid, levelsup) for the word / weight /
+// node of every feature.  Output layout as orc_bow_transform.
+int ref_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup, int* word_ids, double* weights,
+                      int* node_ids, int* bow_n, int* bow_words, double* bow_values, int* fv_n, int* fv_nodes,
+                      int* fv_offsets, int* fv_features) {
+    auto it = g_ref_vocabs.find(path);
+    if (it == g_ref_vocabs.end()) return -1;
+    ORBVocabulary* voc = it->second;
+    ArenaScope scope;
+    {
+        std::vector<cv::Mat> feats;
+        for (int i = 0; i < n; i++) feats.push_back(cv::Mat(1, 32, CV_8U, (void*)(desc + (size_t)i * 32)));
+        DBoW2::BowVector bv;
+        DBoW2::FeatureVector fv;
+        voc->transform(feats, bv, fv, levelsup);
+        for (int i = 0; i < n; i++) {
+            DBoW2::WordId wid = 0;
+            DBoW2::WordValue w = 0;
+            DBoW2::NodeId nid = 0;
+            voc->transform(feats[i], wid, w, &nid, levelsup);
+            word_ids[i] = (int)wid;
+            weights[i] = w;
+            node_ids[i] = (int)nid;
+        }
+        int b = 0;
+        for (auto& e : bv) {
+            bow_words[b] = (int)e.first;
+            bow_values[b] = e.second;
+            b++;
+        }
+        *bow_n = b;
+        int nn = 0, off = 0;
+        for (auto& e : fv) {
+            fv_nodes[nn] = (int)e.first;
+            fv_offsets[nn] = off;
+            for (unsigned f : e.second) fv_features[off++] = (int)f;
+            nn++;
+        }
+        fv_offsets[nn] = off;
+        *fv_n = nn;
+    }
+    return 0;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

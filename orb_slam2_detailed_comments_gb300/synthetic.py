@@ -420,3 +420,54 @@ def frustum_case(m: int, seed: int, w: int = 640, h: int = 480, fx: float = 500.
     mind = (maxd / scale_factor ** (nlevels - 1) * rng.choice([1.0, 0.5, 2.0, 5.0, 1.25], m)).astype(np.float32)
     g = np.stack([pw[:, 0], pw[:, 1], pw[:, 2], nrm[:, 0], nrm[:, 1], nrm[:, 2], mind, maxd], 1).astype(np.float32)
     return Tcw, g
+
+
+def vocabulary(k: int, L: int, seed: int, stop_frac: float = 0.02, scoring: int = 0, weighting: int = 0):
+    """A DBoW2 vocabulary tree standing in for ORBvoc.txt (which is not in the
+    reference tree): the full k-ary tree of depth L in breadth-first order.
+    Level-1 node descriptors are random; every child is its parent's
+    descriptor with each bit flipped with probability 2**-(level + 1), so the
+    tree clusters like a k-means hierarchy.  Leaf weights are idf-like,
+    log(N / n) for a random document count n (a fraction stop_frac of the
+    words get weight 0, DBoW2's stopped words); inner nodes weigh 0.
+    Returns a dict with k, L, scoring, weighting and, for nodes 1..N-1 (node
+    0 is the root), parents, is_leaf, descriptors (N-1, 32) and weights."""
+    rng = np.random.default_rng(seed)
+    sizes = [k ** lvl for lvl in range(1, L + 1)]
+    firsts = np.cumsum([1] + sizes[:-1])  # id of the first node of each level
+    parents, leaves, descs, weights = [], [], [], []
+    prev = np.zeros((1, 32), np.uint8)
+    for lvl, (n, first) in enumerate(zip(sizes, firsts), start=1):
+        par_local = np.arange(n) // k
+        parent_ids = (0 if lvl == 1 else firsts[lvl - 2]) + par_local
+        if lvl == 1:
+            d = rng.integers(0, 256, (n, 32), dtype=np.uint8)
+        else:
+            flips = rng.integers(0, 256, (n, 32), dtype=np.uint8)
+            for _ in range(lvl):
+                flips &= rng.integers(0, 256, (n, 32), dtype=np.uint8)
+            d = prev[par_local] ^ flips
+        leaf = np.full(n, lvl == L)
+        w = np.zeros(n)
+        if lvl == L:
+            w = np.log(n / rng.integers(1, n, n).astype(np.float64))
+            w[rng.random(n) < stop_frac] = 0.0
+        parents.append(parent_ids)
+        leaves.append(leaf)
+        descs.append(d)
+        weights.append(w)
+        prev = d
+    return {"k": k, "L": L, "scoring": scoring, "weighting": weighting,
+            "parents": np.concatenate(parents).astype(np.int32), "is_leaf": np.concatenate(leaves).astype(np.uint8),
+            "descriptors": np.concatenate(descs), "weights": np.concatenate(weights)}
+
+
+def write_vocabulary_text(voc: dict, path: str) -> None:
+    """The vocabulary in the text format TemplatedVocabulary::loadFromTextFile
+    reads: "k L scoring weighting", then one line per node after the root,
+    "parent is_leaf d0 .. d31 weight" (no trailing newline)."""
+    lines = [f"{voc['k']} {voc['L']} {voc['scoring']} {voc['weighting']}"]
+    for p, lf, d, w in zip(voc["parents"], voc["is_leaf"], voc["descriptors"], voc["weights"]):
+        lines.append(f"{int(p)} {int(lf)} " + " ".join(str(int(b)) for b in d) + f" {float(w)!r}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines))
