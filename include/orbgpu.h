@@ -168,6 +168,54 @@ int orbgpu_search_by_projection(orbgpu_matcher* m, const orbgpu_frame* f, const 
                                 const uint8_t* mp_descriptors, int n_mappoints, float th, const uint8_t* claimed,
                                 int* match_out, int mem, int* nmatches);
 
+/* A DBoW2 vocabulary tree (ORBVocabulary, include/ORBVocabulary.h) resident
+ * on the device. */
+typedef struct orbgpu_vocabulary orbgpu_vocabulary;
+
+/* TemplatedVocabulary::loadFromTextFile (Thirdparty/DBoW2/DBoW2/
+ * TemplatedVocabulary.h:1368-1460): "k L scoring weighting", then one line
+ * "parent is_leaf d0 .. d31 weight" per node after the root, in node order.
+ * A line the reference would read only partly (an empty or short line: it
+ * appends a node with unset descriptor bytes) is ORBGPU_ERR_BAD_ARG. */
+int orbgpu_vocabulary_load_text(const char* path, orbgpu_vocabulary** out);
+/* The same tree from arrays: nnodes counts the root; entry i of parents /
+ * is_leaf / descriptors (32 bytes) / weights describes node i + 1, whose
+ * parent must precede it.  scoring: DBoW2::ScoringType (L1_NORM 0 ..
+ * DOT_PRODUCT 5); weighting: DBoW2::WeightingType (TF_IDF 0, TF 1, IDF 2,
+ * BINARY 3).  Host arrays; the tree is copied to the device. */
+int orbgpu_vocabulary_create(int k, int L, int scoring, int weighting, int nnodes, const int* parents,
+                             const uint8_t* is_leaf, const uint8_t* descriptors, const double* weights,
+                             orbgpu_vocabulary** out);
+int orbgpu_vocabulary_destroy(orbgpu_vocabulary* v);
+/* TemplatedVocabulary::size() (words) and the node count. */
+int orbgpu_vocabulary_size(const orbgpu_vocabulary* v, int* nwords, int* nnodes);
+
+/* Frame::ComputeBoW -- src/Frame.cc:704-718 -- i.e.
+ * TemplatedVocabulary::transform(features, BowVector, FeatureVector,
+ * levelsup) (TemplatedVocabulary.h:1136-1290) for the features of nframes
+ * frames: frame f owns descriptor rows [offsets[f], offsets[f + 1]) of desc
+ * (at most 8192 per frame).  Per feature i: word_ids[i], weights[i] (the
+ * word's weight) and node_ids[i] (the node of level L - levelsup on its path;
+ * the root when that level is <= 0).  Per frame f, written from index
+ * offsets[f] on:
+ *   BowVector      bow_counts[f] entries (word, value) in ascending word
+ *                  order in bow_words / bow_values -- the reference's
+ *                  std::map, doubles bit-identical (weights of repeated words
+ *                  summed in sequence, normalised as the vocabulary's scoring
+ *                  requires);
+ *   FeatureVector  fv_counts[f] nodes in ascending order in fv_nodes, node j
+ *                  owning fv_features[fv_starts[j] .. + fv_sizes[j]) (feature
+ *                  indices within the frame, ascending; fv_starts are absolute
+ *                  indices into fv_features).
+ * Features whose word has weight 0 (stopped words) appear in neither, as in
+ * the reference.  A frame of more than 8192 features gets counts of -1.
+ * All arrays device or page-locked host memory (desc 16-byte aligned);
+ * asynchronous on 'stream'; two kernel launches. */
+int orbgpu_bow_transform(const orbgpu_vocabulary* v, const uint8_t* desc, const int* offsets, int nframes,
+                         int levelsup, int* word_ids, double* weights, int* node_ids, int* bow_counts, int* bow_words,
+                         double* bow_values, int* fv_counts, int* fv_nodes, int* fv_starts, int* fv_sizes,
+                         int* fv_features, void* stream);
+
 /* Frame::UndistortKeyPoints() -- src/Frame.cc:724-776 -- for n keypoints of
  * one camera: out[i] = kps[i] with x, y through cv::undistortPoints(pts, pts,
  * mK, mDistCoef, cv::Mat(), mK) (OpenCV 3.2's algorithm: double precision,

@@ -1,0 +1,104 @@
+"""DBoW2's vocabulary on the GPU: ORBVocabulary (include/ORBVocabulary.h) and
+Frame::ComputeBoW (src/Frame.cc:704-718) for many frames at once
+(orbgpu_vocabulary_* / orbgpu_bow_transform in include/orbgpu.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import OrbGpuError, check, lib, ptr
+
+
+class Vocabulary:
+    """A DBoW2 vocabulary tree resident on the device.
+
+    Vocabulary(path) reads the text format of
+    TemplatedVocabulary::loadFromTextFile; Vocabulary.from_arrays builds the
+    same tree from arrays (node i + 1 described by entry i, parents first).
+    """
+
+    def __init__(self, path: str | None = None, _handle=None):
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            check(lib().orbgpu_vocabulary_load_text(str(path).encode(), C.byref(self._h)),
+                  "orbgpu_vocabulary_load_text")
+
+    @classmethod
+    def from_arrays(cls, k, L, scoring, weighting, parents, is_leaf, descriptors, weights):
+        h = C.c_void_p()
+        par = np.ascontiguousarray(parents, np.int32)
+        lf = np.ascontiguousarray(is_leaf, np.uint8)
+        d = np.ascontiguousarray(descriptors, np.uint8).reshape(-1, 32)
+        w = np.ascontiguousarray(weights, np.float64)
+        if not (len(par) == len(lf) == len(d) == len(w)):
+            raise ValueError("parents, is_leaf, descriptors and weights need one entry per node after the root")
+        check(lib().orbgpu_vocabulary_create(int(k), int(L), int(scoring), int(weighting), len(par) + 1, ptr(par),
+                                             ptr(lf), ptr(d), ptr(w), C.byref(h)), "orbgpu_vocabulary_create")
+        return cls(_handle=h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value:
+            try:
+                lib().orbgpu_vocabulary_destroy(h)
+            except Exception:
+                pass
+
+    def size(self) -> int:
+        """TemplatedVocabulary::size(): the number of words."""
+        nw, nn = C.c_int(0), C.c_int(0)
+        check(lib().orbgpu_vocabulary_size(self._h, C.byref(nw), C.byref(nn)), "orbgpu_vocabulary_size")
+        return nw.value
+
+    def transform(self, descriptors, offsets, levelsup: int = 4, stream=None):
+        """TemplatedVocabulary::transform(features, BowVector, FeatureVector,
+        levelsup) for every frame of a batch: descriptors an (n, 32) uint8
+        tensor (device or page-locked host), offsets an (nframes + 1,) int32
+        tensor.  Returns a dict of device tensors (see orbgpu_bow_transform):
+        word, weight, node per feature; bow_counts, bow_words, bow_values,
+        fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features with frame f's
+        entries from offsets[f] on.  Asynchronous on the current stream."""
+        import torch
+        n = int(descriptors.shape[0])
+        nf = int(offsets.shape[0]) - 1
+        dev = torch.device("cuda")
+        m = max(n, 1)
+        out = {"word": torch.empty(m, dtype=torch.int32, device=dev),
+               "weight": torch.empty(m, dtype=torch.float64, device=dev),
+               "node": torch.empty(m, dtype=torch.int32, device=dev),
+               "bow_counts": torch.empty(max(nf, 1), dtype=torch.int32, device=dev),
+               "bow_words": torch.empty(m, dtype=torch.int32, device=dev),
+               "bow_values": torch.empty(m, dtype=torch.float64, device=dev),
+               "fv_counts": torch.empty(max(nf, 1), dtype=torch.int32, device=dev),
+               "fv_nodes": torch.empty(m, dtype=torch.int32, device=dev),
+               "fv_starts": torch.empty(m, dtype=torch.int32, device=dev),
+               "fv_sizes": torch.empty(m, dtype=torch.int32, device=dev),
+               "fv_features": torch.empty(m, dtype=torch.int32, device=dev)}
+        st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+        keys = ("word", "weight", "node", "bow_counts", "bow_words", "bow_values", "fv_counts", "fv_nodes",
+                "fv_starts", "fv_sizes", "fv_features")
+        check(lib().orbgpu_bow_transform(self._h, ptr(descriptors), ptr(offsets), nf, int(levelsup),
+                                         *[ptr(out[k]) for k in keys], C.c_void_p(st)), "orbgpu_bow_transform")
+        return out
+
+    def ComputeBoW(self, descriptors, levelsup: int = 4):
+        """Frame::ComputeBoW for one frame: (BowVector as {word: value},
+        FeatureVector as {node: [feature indices]}) on the host."""
+        import torch
+        n = int(descriptors.shape[0])
+        offs = torch.tensor([0, n], dtype=torch.int32, device="cuda")
+        r = self.transform(descriptors, offs, levelsup)
+        nb, nv = int(r["bow_counts"][0].item()), int(r["fv_counts"][0].item())
+        if nb < 0:
+            raise OrbGpuError(1, "ComputeBoW", "more than 8192 features in one frame")
+        words = r["bow_words"][:nb].cpu().numpy()
+        values = r["bow_values"][:nb].cpu().numpy()
+        nodes = r["fv_nodes"][:nv].cpu().numpy()
+        starts = r["fv_starts"][:nv].cpu().numpy()
+        sizes = r["fv_sizes"][:nv].cpu().numpy()
+        feats = r["fv_features"][:n].cpu().numpy()
+        return ({int(w): float(v) for w, v in zip(words, values)},
+                {int(nd): feats[s:s + z].tolist() for nd, s, z in zip(nodes, starts, sizes)})

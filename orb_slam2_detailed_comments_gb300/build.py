@@ -34,6 +34,7 @@ SOURCES = [
     "orbgpu_knn_tc.cu",
     "orbgpu_mappoint.cu",
     "orbgpu_geometry.cu",
+    "orbgpu_bow.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,377 @@
+// orbgpu_bow.cu -- DBoW2's vocabulary transform (Frame::ComputeBoW,
+// src/Frame.cc:704-718: ORBVocabulary::transform(descriptors, mBowVec,
+// mFeatVec, 4)) for the features of many frames.
+//
+// The vocabulary tree lives in HBM with every node's children contiguous
+// (grouped by parent in node-id order, the order loadFromTextFile appends
+// them), so one descent level reads the k child descriptors of one node as
+// consecutive 32-byte rows.  k_bow_descend: one thread per feature walks the
+// tree (TemplatedVocabulary.h:1240-1290: at every level the first child with
+// the least Hamming distance, strict <; the node of level L - levelsup kept
+// for the feature vector; stop at a node without children) and writes the
+// word, its weight and that node.  k_bow_assemble: one block per frame sorts
+// the kept features (weight > 0) by word and by node in shared memory and
+// writes BowVector (BowVector::addWeight / addIfNotExist, then normalize,
+// BowVector.cpp:40-95) and FeatureVector (FeatureVector::addFeature,
+// FeatureVector.cpp:37-53).  The doubles are the reference's: a word seen c
+// times sums its weight c times in sequence (the reference adds them in
+// feature order, and they are equal), and the norm is one sequential sum in
+// ascending word order, as std::map iterates.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "orbgpu_host.h"
+
+struct orbgpu_vocabulary {
+    int k, L, scoring, weighting, nnodes, nwords;
+    uint4* child_desc;   // one 32-byte row per non-root node, grouped by parent
+    int* child_start;    // nnodes + 1: children of node p at positions [child_start[p], child_start[p + 1])
+    int* pos_node;       // node id at each position
+    int* node_word;      // word id of every node (0 where none, as DBoW2's Node default)
+    double* node_weight;
+};
+
+namespace orbgpu {
+
+#define BOW_THREADS 256
+#define BOW_ASM_THREADS 1024
+#define BOW_MAX_FEATURES 8192  // per frame (the assembly sorts a frame in shared memory)
+
+__global__ void __launch_bounds__(BOW_THREADS) k_bow_descend(const uint4* __restrict__ desc, const int* __restrict__ offsets,
+                                                             int nframes, const uint4* __restrict__ child_desc,
+                                                             const int* __restrict__ child_start,
+                                                             const int* __restrict__ pos_node,
+                                                             const int* __restrict__ node_word,
+                                                             const double* __restrict__ node_weight, int nid_level,
+                                                             int* __restrict__ word_out, double* __restrict__ weight_out,
+                                                             int* __restrict__ node_out) {
+    const int first = __ldg(offsets), last = __ldg(offsets + nframes);
+    if (first < 0) return;
+    for (int i = first + blockIdx.x * BOW_THREADS + threadIdx.x; i < last; i += gridDim.x * BOW_THREADS) {
+        const uint4 f0 = __ldg(desc + 2 * (size_t)i), f1 = __ldg(desc + 2 * (size_t)i + 1);
+        int node = 0, level = 0, nid = 0;
+        int s = __ldg(child_start), e = __ldg(child_start + 1);
+        while (s < e) {
+            ++level;
+            int best = s;
+            int best_d = hamming256(f0, f1, __ldg(child_desc + 2 * (size_t)s), __ldg(child_desc + 2 * (size_t)s + 1));
+            for (int p = s + 1; p < e; p++) {
+                const int d = hamming256(f0, f1, __ldg(child_desc + 2 * (size_t)p), __ldg(child_desc + 2 * (size_t)p + 1));
+                if (d < best_d) {
+                    best_d = d;
+                    best = p;
+                }
+            }
+            node = __ldg(pos_node + best);
+            if (level == nid_level) nid = node;
+            s = __ldg(child_start + node);
+            e = __ldg(child_start + node + 1);
+        }
+        word_out[i] = __ldg(node_word + node);
+        weight_out[i] = __ldg(node_weight + node);
+        node_out[i] = nid;
+    }
+}
+
+// Ascending bitonic sort of n2 (a power of two) 64-bit keys in shared memory.
+__device__ void bow_block_sort(unsigned long long* keys, int n2) {
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = keys[i], b = keys[l];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One block per frame.  Shared memory: BOW_MAX_FEATURES 64-bit keys.
+__global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
+    const int* __restrict__ offsets, const int* __restrict__ word, const double* __restrict__ weight,
+    const int* __restrict__ node, int weighting, int scoring, int* __restrict__ bow_counts,
+    int* __restrict__ bow_words, double* __restrict__ bow_values, int* __restrict__ fv_counts,
+    int* __restrict__ fv_nodes, int* __restrict__ fv_starts, int* __restrict__ fv_sizes,
+    int* __restrict__ fv_features) {
+    extern __shared__ unsigned long long keys[];
+    __shared__ int s_nkept, s_nruns;
+    __shared__ double s_norm;
+    const int f = blockIdx.x;
+    const int o0 = offsets[f], o1 = offsets[f + 1];
+    const int n = o1 - o0;
+    if (o0 < 0 || n < 0 || n > BOW_MAX_FEATURES) {
+        if (threadIdx.x == 0) bow_counts[f] = fv_counts[f] = -1;
+        return;
+    }
+    int n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    const unsigned long long pad = ~0ull;
+    // pass 0: BowVector (keys word << 32 | feature), pass 1: FeatureVector
+    for (int pass = 0; pass < 2; pass++) {
+        for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+            unsigned long long key = pad;
+            if (i < n && weight[o0 + i] > 0.0) {
+                const unsigned hi = pass == 0 ? (unsigned)word[o0 + i] : (unsigned)node[o0 + i];
+                key = ((unsigned long long)hi << 32) | (unsigned)i;
+            }
+            keys[i] = key;
+        }
+        if (threadIdx.x == 0) {
+            s_nkept = 0;
+            s_nruns = 0;
+        }
+        __syncthreads();
+        bow_block_sort(keys, n2);
+        // kept features sort first; runs of equal high words are the entries
+        int kept = 0;
+        for (int i = threadIdx.x; i < n2; i += blockDim.x) kept += keys[i] != pad ? 1 : 0;
+        kept = __reduce_add_sync(0xffffffffu, kept);
+        if ((threadIdx.x & 31) == 0 && kept) atomicAdd(&s_nkept, kept);
+        __syncthreads();
+        const int nk = s_nkept;
+        // run starts in ascending order: a block-wide exclusive scan of the flags
+        __shared__ int s_warp[BOW_ASM_THREADS / 32];
+        for (int base = 0; base < nk; base += blockDim.x) {
+            const int i = base + threadIdx.x;
+            const bool start = i < nk && (i == 0 || (keys[i] >> 32) != (keys[i - 1] >> 32));
+            const unsigned bal = __ballot_sync(0xffffffffu, start);
+            const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+            if (lane == 0) s_warp[w] = __popc(bal);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int acc = s_nruns;
+                for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+                    const int c = s_warp[q];
+                    s_warp[q] = acc;
+                    acc += c;
+                }
+                s_nruns = acc;
+            }
+            __syncthreads();
+            if (start) {
+                const int r = s_warp[w] + __popc(bal & ((1u << lane) - 1u));
+                int end = i + 1;
+                while (end < nk && (keys[end] >> 32) == (keys[i] >> 32)) end++;
+                const unsigned hi = (unsigned)(keys[i] >> 32);
+                if (pass == 0) {
+                    const double w0 = weight[o0 + (int)(keys[i] & 0xffffffffu)];
+                    double v = w0;
+                    if (weighting == 0 || weighting == 1)  // TF_IDF, TF: addWeight per occurrence
+                        for (int q = i + 1; q < end; q++) v = __dadd_rn(v, w0);
+                    bow_words[o0 + r] = (int)hi;
+                    bow_values[o0 + r] = v;
+                } else {
+                    fv_nodes[o0 + r] = (int)hi;
+                    fv_starts[o0 + r] = o0 + i;
+                    fv_sizes[o0 + r] = end - i;
+                }
+            }
+            __syncthreads();
+        }
+        const int nruns = s_nruns;
+        if (pass == 1) {
+            // the features of every node, in feature order (the sort's low words)
+            for (int i = threadIdx.x; i < nk; i += blockDim.x) fv_features[o0 + i] = (int)(keys[i] & 0xffffffffull);
+            if (threadIdx.x == 0) fv_counts[f] = nruns;
+            continue;
+        }
+        // normalisation (ScoringObject.h:84-89: L1 for L1 / chi-square / KL /
+        // Bhattacharyya, L2 for L2, none for the dot product, where TF divides
+        // by the number of words instead)
+        if (threadIdx.x == 0) {
+            double norm = 0.0;
+            if (scoring == 5) {
+                norm = (weighting == 0 || weighting == 1) && nruns > 0 ? (double)nruns : 0.0;
+            } else if (scoring == 1) {
+                for (int r = 0; r < nruns; r++) norm = __dadd_rn(norm, __dmul_rn(bow_values[o0 + r], bow_values[o0 + r]));
+                norm = __dsqrt_rn(norm);
+            } else {
+                for (int r = 0; r < nruns; r++) norm = __dadd_rn(norm, fabs(bow_values[o0 + r]));
+            }
+            s_norm = norm;
+            bow_counts[f] = nruns;
+        }
+        __syncthreads();
+        const double norm = s_norm;
+        if (norm > 0.0)
+            for (int r = threadIdx.x; r < nruns; r += blockDim.x) bow_values[o0 + r] = __ddiv_rn(bow_values[o0 + r], norm);
+        __syncthreads();
+    }
+}
+
+}  // namespace orbgpu
+
+using namespace orbgpu;
+
+extern "C" int orbgpu_vocabulary_create(int k, int L, int scoring, int weighting, int nnodes, const int* parents,
+                                        const uint8_t* is_leaf, const uint8_t* descriptors, const double* weights,
+                                        orbgpu_vocabulary** out) {
+    if (!out || k < 0 || k > 20 || L < 1 || L > 10 || scoring < 0 || scoring > 5 || weighting < 0 || weighting > 3 ||
+        nnodes < 1 || (nnodes > 1 && (!parents || !is_leaf || !descriptors || !weights))) {
+        orbgpu_set_last_error("orbgpu_vocabulary_create: bad arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    const int nc = nnodes - 1;  // nodes after the root; node i + 1 is described by entry i
+    std::vector<int> count(nnodes + 1, 0);
+    for (int i = 0; i < nc; i++) {
+        const int p = parents[i];
+        if (p < 0 || p > i) {  // a parent must precede its child (the reference indexes m_nodes[pid])
+            orbgpu_set_last_error("orbgpu_vocabulary_create: a node's parent does not precede it", __FILE__, __LINE__);
+            return ORBGPU_ERR_BAD_ARG;
+        }
+        count[p + 1]++;
+    }
+    std::vector<int> start(nnodes + 1, 0);
+    for (int p = 0; p < nnodes; p++) start[p + 1] = start[p] + count[p + 1];
+    std::vector<int> fill(start.begin(), start.end() - 1), pos_node(std::max(nc, 1));
+    std::vector<uint8_t> cdesc((size_t)std::max(nc, 1) * 32);
+    std::vector<int> word(nnodes, 0);
+    std::vector<double> w(nnodes, 0.0);
+    int nwords = 0;
+    for (int i = 0; i < nc; i++) {
+        const int node = i + 1, pos = fill[parents[i]]++;
+        pos_node[pos] = node;
+        std::memcpy(&cdesc[(size_t)pos * 32], descriptors + (size_t)i * 32, 32);
+        w[node] = weights[i];
+        if (is_leaf[i]) word[node] = nwords++;
+    }
+    orbgpu_vocabulary* v = new orbgpu_vocabulary();
+    v->k = k;
+    v->L = L;
+    v->scoring = scoring;
+    v->weighting = weighting;
+    v->nnodes = nnodes;
+    v->nwords = nwords;
+    v->child_desc = nullptr;
+    v->child_start = v->pos_node = v->node_word = nullptr;
+    v->node_weight = nullptr;
+    cudaError_t e = cudaMalloc(&v->child_desc, cdesc.size());
+    if (e == cudaSuccess) e = cudaMalloc(&v->child_start, sizeof(int) * (nnodes + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&v->pos_node, sizeof(int) * pos_node.size());
+    if (e == cudaSuccess) e = cudaMalloc(&v->node_word, sizeof(int) * nnodes);
+    if (e == cudaSuccess) e = cudaMalloc(&v->node_weight, sizeof(double) * nnodes);
+    if (e == cudaSuccess) e = cudaMemcpy(v->child_desc, cdesc.data(), cdesc.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(v->child_start, start.data(), sizeof(int) * (nnodes + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(v->pos_node, pos_node.data(), sizeof(int) * pos_node.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(v->node_word, word.data(), sizeof(int) * nnodes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(v->node_weight, w.data(), sizeof(double) * nnodes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        orbgpu_vocabulary_destroy(v);
+        orbgpu_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+        return e == cudaErrorMemoryAllocation ? ORBGPU_ERR_OOM : ORBGPU_ERR_CUDA;
+    }
+    *out = v;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_vocabulary_load_text(const char* path, orbgpu_vocabulary** out) {
+    // TemplatedVocabulary::loadFromTextFile (TemplatedVocabulary.h:1368-1460):
+    // "k L scoring weighting", then "parent is_leaf d0 .. d31 weight" per node
+    std::ifstream f(path ? path : "");
+    std::string line;
+    if (!out || !f.is_open() || !std::getline(f, line)) {
+        orbgpu_set_last_error("orbgpu_vocabulary_load_text: cannot read the file", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    int k = -1, L = -1, n1 = -1, n2 = -1;
+    {
+        std::stringstream hs(line);
+        hs >> k >> L >> n1 >> n2;
+    }
+    std::vector<int> parents;
+    std::vector<uint8_t> leaf, desc;
+    std::vector<double> weights;
+    while (std::getline(f, line)) {
+        std::stringstream ls(line);
+        int pid = -1, lf = 0;
+        ls >> pid >> lf;
+        uint8_t d[32];
+        for (int i = 0; i < 32; i++) {
+            int b = 0;
+            ls >> b;
+            d[i] = (uint8_t)b;
+        }
+        double w = 0;
+        ls >> w;
+        if (line.empty() || ls.fail()) {
+            // an empty or short line: the reference appends a node whose
+            // descriptor bytes are left unset
+            orbgpu_set_last_error("orbgpu_vocabulary_load_text: malformed node line", __FILE__, __LINE__);
+            return ORBGPU_ERR_BAD_ARG;
+        }
+        parents.push_back(pid);
+        leaf.push_back(lf > 0 ? 1 : 0);
+        desc.insert(desc.end(), d, d + 32);
+        weights.push_back(w);
+    }
+    return orbgpu_vocabulary_create(k, L, n1, n2, (int)parents.size() + 1, parents.data(), leaf.data(), desc.data(),
+                                    weights.data(), out);
+}
+
+extern "C" int orbgpu_vocabulary_destroy(orbgpu_vocabulary* v) {
+    if (!v) return ORBGPU_OK;
+    cudaFree(v->child_desc);
+    cudaFree(v->child_start);
+    cudaFree(v->pos_node);
+    cudaFree(v->node_word);
+    cudaFree(v->node_weight);
+    delete v;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_vocabulary_size(const orbgpu_vocabulary* v, int* nwords, int* nnodes) {
+    if (!v) return ORBGPU_ERR_BAD_ARG;
+    if (nwords) *nwords = v->nwords;
+    if (nnodes) *nnodes = v->nnodes;
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_bow_transform(const orbgpu_vocabulary* v, const uint8_t* desc, const int* offsets, int nframes,
+                                    int levelsup, int* word_ids, double* weights, int* node_ids, int* bow_counts,
+                                    int* bow_words, double* bow_values, int* fv_counts, int* fv_nodes, int* fv_starts,
+                                    int* fv_sizes, int* fv_features, void* stream) {
+    if (!v || nframes < 0 ||
+        (nframes > 0 && (!desc || !offsets || !word_ids || !weights || !node_ids || !bow_counts || !bow_words ||
+                         !bow_values || !fv_counts || !fv_nodes || !fv_starts || !fv_sizes || !fv_features)) ||
+        ((uintptr_t)desc & 15)) {
+        orbgpu_set_last_error("orbgpu_bow_transform: bad arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (nframes == 0) return ORBGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (v->nwords == 0) {
+        // TemplatedVocabulary::transform returns empty vectors for an empty vocabulary
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(bow_counts, 0, sizeof(int) * nframes, st));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(fv_counts, 0, sizeof(int) * nframes, st));
+        return ORBGPU_OK;
+    }
+    static bool smem_set = false;
+    if (!smem_set) {
+        ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bow_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             BOW_MAX_FEATURES * 8));
+        smem_set = true;
+    }
+    const int blocks = nsm_of_current_device() * 8;
+    k_bow_descend<<<blocks, BOW_THREADS, 0, st>>>(reinterpret_cast<const uint4*>(desc), offsets, nframes,
+                                                  v->child_desc, v->child_start, v->pos_node, v->node_word,
+                                                  v->node_weight, v->L - levelsup, word_ids, weights, node_ids);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    k_bow_assemble<<<nframes, BOW_ASM_THREADS, BOW_MAX_FEATURES * 8, st>>>(
+        offsets, word_ids, weights, node_ids, v->weighting, v->scoring, bow_counts, bow_words, bow_values, fv_counts,
+        fv_nodes, fv_starts, fv_sizes, fv_features);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    return ORBGPU_OK;
+}

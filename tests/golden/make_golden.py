@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow")
 
 
 def main(groups=GROUPS):
@@ -53,6 +53,8 @@ def main(groups=GROUPS):
         frustum_fixture(R)
     if "undistort" in groups:
         undistort_fixture(R)
+    if "bow" in groups:
+        bow_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -268,6 +270,48 @@ def undistort_fixture(R):
                        f"{name}_undistorted": R.undistort_keypoints(K, d, kps),
                        f"{name}_bounds": R.compute_image_bounds(w, h, K, d)})
     save("undistort.npz", **arrays)
+
+
+BOW_VOCABULARIES = {
+    # name: (k, L, scoring, weighting, seed, levelsup values)
+    "k10_L3_l1_tfidf": (10, 3, 0, 0, 81, (1, 4)),
+    "k6_L4_l2_idf": (6, 4, 1, 2, 82, (2, 4)),
+}
+
+
+def bow_features(voc, n, seed):
+    """Descriptors for the vocabulary transform: noisy copies of random words
+    (about 1 bit in 16 flipped) and some uniform ones."""
+    rng = np.random.default_rng(seed)
+    leaves = np.nonzero(voc["is_leaf"])[0]
+    base = voc["descriptors"][rng.choice(leaves, n - n // 8)]
+    flips = rng.integers(0, 256, base.shape, dtype=np.uint8)
+    for _ in range(3):
+        flips &= rng.integers(0, 256, base.shape, dtype=np.uint8)
+    return np.concatenate([base ^ flips, rng.integers(0, 256, (n // 8, 32), dtype=np.uint8)])
+
+
+def bow_fixture(R):
+    # 12. DBoW2 TemplatedVocabulary::transform (Frame::ComputeBoW) on synthetic
+    # vocabularies written in the loadFromTextFile format
+    import tempfile
+    arrays = {}
+    for name, (k, L, sc, wt, seed, lups) in BOW_VOCABULARIES.items():
+        voc = syn.vocabulary(k, L, seed, scoring=sc, weighting=wt)
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "voc.txt")
+            syn.write_vocabulary_text(voc, path)
+            assert R.vocabulary_load(path) == int(voc["is_leaf"].sum())
+            arrays.update({f"{name}_{key}": np.asarray(voc[key]) for key in
+                           ("k", "L", "scoring", "weighting", "parents", "is_leaf", "descriptors", "weights")})
+            for fi, n in enumerate((1500, 40, 900)):
+                desc = bow_features(voc, n, seed * 10 + fi)
+                arrays[f"{name}_f{fi}_desc"] = desc
+                for lu in lups:
+                    out = R.bow_transform(path, desc, lu)
+                    for key, val in out.items():
+                        arrays[f"{name}_f{fi}_lu{lu}_{key}"] = val
+    save("bow.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -64,6 +64,12 @@ def test_bad_arguments_are_rejected_before_any_device_work(library):
     assert library.orbgpu_extractor_create(1000, C.c_float(1.2), 0, 20, 7, 0, 0, None, C.byref(h)) == 1
     assert library.orbgpu_knn2(None, None, 1, None, 1, None, None, None, None, 0) == 1
     assert library.orbgpu_knn2_noalloc(None, -1, None, 0, None, None, None, None, None) == 1
+    # vocabulary: branching factor out of range, a parent after its child, no file
+    assert library.orbgpu_vocabulary_create(21, 6, 0, 0, 1, None, None, None, None, C.byref(h)) == 1
+    par = (C.c_int * 2)(0, 5)
+    assert library.orbgpu_vocabulary_create(2, 1, 0, 0, 3, par, C.c_void_p(16), C.c_void_p(16), C.c_void_p(16),
+                                            C.byref(h)) == 1
+    assert library.orbgpu_vocabulary_load_text(b"/nonexistent/voc.txt", C.byref(h)) == 1
     # negative map point count; a pool pointer that is not 16-byte aligned
     assert library.orbgpu_distinctive_descriptors(None, 0, None, None, 0, -1, None, None, None) == 1
     assert library.orbgpu_distinctive_descriptors(C.c_void_p(8), 1, C.c_void_p(16), C.c_void_p(16), 1, 1,

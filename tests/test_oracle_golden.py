@@ -239,3 +239,28 @@ def test_undistort_golden(oracle, golden, name):
     assert oracle.compute_image_bounds(w, h, K, d).tobytes() == g[f"{name}_bounds"].tobytes()
     if name.startswith("k1_zero"):
         assert out.tobytes() == g[f"{name}_keypoints"].tobytes()
+
+
+# DBoW2 TemplatedVocabulary::transform (Frame::ComputeBoW)
+BOW_VOCABULARIES = {"k10_L3_l1_tfidf": (1, 4), "k6_L4_l2_idf": (2, 4)}
+
+
+def bow_vocabulary(g, name, path):
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    voc = {key: g[f"{name}_{key}"] for key in ("parents", "is_leaf", "descriptors", "weights")}
+    voc.update({key: int(g[f"{name}_{key}"]) for key in ("k", "L", "scoring", "weighting")})
+    syn.write_vocabulary_text(voc, path)
+    return voc
+
+
+@pytest.mark.parametrize("name", list(BOW_VOCABULARIES))
+def test_bow_transform_golden(oracle, golden, tmp_path, name):
+    g = golden("bow.npz")
+    path = str(tmp_path / "voc.txt")
+    voc = bow_vocabulary(g, name, path)
+    assert oracle.vocabulary_load(path) == int(voc["is_leaf"].sum())
+    for fi in range(3):
+        for lu in BOW_VOCABULARIES[name]:
+            out = oracle.bow_transform(path, g[f"{name}_f{fi}_desc"], lu)
+            for key, val in out.items():
+                assert np.array_equal(val, g[f"{name}_f{fi}_lu{lu}_{key}"]), (fi, lu, key)
