@@ -256,7 +256,7 @@ def run_ours(args):
         per_frame_fps, per_frame_split = run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev)
     extra = {}
     for leg, fn in (("stereo", bench_stereo), ("knn", bench_knn), ("serving", bench_serving),
-                    ("distinctive", bench_distinctive), ("frustum", bench_frustum)):
+                    ("distinctive", bench_distinctive), ("frustum", bench_frustum), ("bow", bench_bow)):
         if leg in legs:
             try:
                 extra[LEG_KEYS[leg]] = fn(dev)
@@ -267,9 +267,10 @@ def run_ours(args):
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
 
 
-LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "distinctive", "frustum", "cpu"}
+LEGS = {"e2e", "perframe", "stereo", "knn", "serving", "distinctive", "frustum", "bow", "cpu"}
 LEG_KEYS = {"stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams",
-            "distinctive": "distinctive_descriptors_1M_mappoints", "frustum": "is_in_frustum_64x5000"}
+            "distinctive": "distinctive_descriptors_1M_mappoints", "frustum": "is_in_frustum_64x5000",
+            "bow": "compute_bow_64x2000_k10L6"}
 
 
 def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev, mpd_dev, nfs, cap):
@@ -629,6 +630,88 @@ def bench_frustum(dev, steps=10, warmup=3):
             "in_view_equal_to_oracle": same}
 
 
+def bench_bow(dev, steps=10, warmup=3):
+    """Frame::ComputeBoW (DBoW2 transform, levelsup 4) for 64 frames x 2,000
+    descriptors with a vocabulary of ORBvoc's shape (k 10, L 6: 1,111,111
+    nodes, 1,000,000 words; synthetic, the reference's vocabulary file is not
+    in its tree), TF-IDF weights, L1 scoring.  Device-resident (events, L2
+    flushed between calls), end to end from page-locked descriptors (results
+    copied back), and the oracle on one host core."""
+    import torch
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import Vocabulary
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    voc = syn.vocabulary(10, 6, 2024)
+    V = Vocabulary.from_arrays(10, 6, 0, 0, voc["parents"], voc["is_leaf"], voc["descriptors"], voc["weights"])
+    nf, per = 64, 2000
+    rng = np.random.default_rng(7)
+    leaves = np.nonzero(voc["is_leaf"])[0]
+    base = voc["descriptors"][rng.choice(leaves, nf * per)]
+    flips = rng.integers(0, 256, base.shape, dtype=np.uint8)
+    for _ in range(2):
+        flips &= rng.integers(0, 256, base.shape, dtype=np.uint8)
+    desc = np.ascontiguousarray(base ^ flips)
+    offs = np.arange(0, nf * per + 1, per, dtype=np.int32)
+    D, O = torch.from_numpy(desc).to(dev), torch.from_numpy(offs).to(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        r = V.transform(D, O, 4)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = V.transform(D, O, 4)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    dev_ms = statistics.median(ms)
+    gpu_words = r["bow_words"].cpu().numpy()
+    gpu_counts = r["bow_counts"].cpu().numpy()
+    hD = torch.from_numpy(desc).pin_memory()
+    host = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in r.items()}
+    for it in range(warmup + steps):
+        if it == warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        r = V.transform(hD, O, 4)
+        for k in ("bow_counts", "bow_words", "bow_values", "fv_counts", "fv_nodes", "fv_starts", "fv_sizes",
+                  "fv_features"):
+            host[k].copy_(r[k], non_blocking=True)
+        stream.synchronize()
+    e2e = nf * per * steps / (time.perf_counter() - t0)
+    d2h = sum(host[k].numel() * host[k].element_size() for k in ("bow_counts", "bow_words", "bow_values",
+                                                                  "fv_counts", "fv_nodes", "fv_starts", "fv_sizes",
+                                                                  "fv_features"))
+    o = pyoracle.Oracle()
+    o.vocabulary_from_arrays("bench", voc)
+    sample = 8
+    t0 = time.perf_counter()
+    same = True
+    for f in range(sample):
+        ref = o.bow_transform("bench", desc[f * per:(f + 1) * per], 4)
+        same &= bool(np.array_equal(ref["bow_words"], gpu_words[f * per:f * per + gpu_counts[f]]))
+    cpu_s = time.perf_counter() - t0
+    pk, pk_src = peaks()
+    # algorithmic bytes: each descriptor read once, 6 levels x 10 child rows,
+    # per-feature outputs, the assembled vectors
+    alg = nf * per * (32 + 6 * 10 * 32 + 16 + 40)
+    return {"metric": "features/s (ComputeBoW, vocabulary k10 L6)", "frames": nf, "features": nf * per,
+            "value": nf * per / (dev_ms / 1e3), "ms": dev_ms, "gpu_launches_per_step": 2,
+            "e2e": {"value": e2e, "unit": "features/s", "h2d_bytes_per_step": int(desc.nbytes),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "l2", "kernel": "k_bow_descend + k_bow_assemble",
+                         "achieved": alg / (dev_ms / 1e3) / 1e9, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": alg / (dev_ms / 1e3) / 1e9 / pk["hbm_gbs"], "algorithmic_bytes_per_step": alg,
+                         "peak_source": pk_src,
+                         "note": "child rows counted at every visit; the upper levels are served by L2"},
+            "cpu_baseline": {"value": sample * per / cpu_s, "unit": "features/s", "cores": 1, "kind": "port",
+                             "sample": f"{sample} frames x {per} descriptors, oracle restatement"},
+            "bow_words_equal_to_oracle": same}
+
+
 def bench_serving(dev, duration_s=3.0):
     """32 camera streams, Poisson 30 Hz each, mixed 640x480/1241x376/1280x720,
     nFeatures 1000-2000: every frame is extracted and matched against its
@@ -778,7 +861,7 @@ def main():
     ap.add_argument("--shapes", default="",
                     help="pin the launch shapes resize_rows,fast_cells_per_block,describe_group (no tuning)")
     ap.add_argument("--legs", default="all",
-                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,distinctive,frustum,cpu) "
+                    help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,distinctive,frustum,bow,cpu) "
                          "or 'all'")
     args = ap.parse_args()
     NFRAMES = args.frames

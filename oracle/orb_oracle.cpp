@@ -1062,6 +1062,32 @@ void vocab_descend(const OrcVocab& v, const uint8_t* f, int levelsup, int& word,
 
 extern "C" {
 
+// The same tree from arrays (entry i describes node i + 1), stored under a
+// name usable as the path argument of orc_bow_transform.
+int orc_vocabulary_from_arrays(const char* name, int k, int L, int scoring, int weighting, int nnodes,
+                               const int* parents, const uint8_t* is_leaf, const uint8_t* descriptors,
+                               const double* weights) {
+    OrcVocab v;
+    v.k = k;
+    v.L = L;
+    v.scoring = scoring;
+    v.weighting = weighting;
+    v.children.assign(nnodes, std::vector<int>());
+    v.desc.assign(nnodes, std::array<uint8_t, 32>());
+    v.weight.assign(nnodes, 0.0);
+    v.word_id.assign(nnodes, 0);
+    for (int i = 0; i + 1 < nnodes; i++) {
+        const int node = i + 1;
+        if (parents[i] < 0 || parents[i] > i) return -1;
+        v.children[parents[i]].push_back(node);
+        std::memcpy(v.desc[node].data(), descriptors + (size_t)i * 32, 32);
+        v.weight[node] = weights[i];
+        v.word_id[node] = is_leaf[i] ? v.nwords++ : 0;
+    }
+    g_vocabs[name] = v;
+    return v.nwords;
+}
+
 int orc_vocabulary_load(const char* path) {
     OrcVocab v;
     if (!load_vocab(path, v)) return -1;

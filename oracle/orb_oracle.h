@@ -56,6 +56,9 @@ int orc_knn2(const uint8_t* q, int nq, const uint8_t* t, int nt, int* idx1, int*
  * levelsup) on n descriptors with the vocabulary loaded from path (see
  * orb_oracle.cpp for the output layout). */
 int orc_vocabulary_load(const char* path);
+int orc_vocabulary_from_arrays(const char* name, int k, int L, int scoring, int weighting, int nnodes,
+                               const int* parents, const uint8_t* is_leaf, const uint8_t* descriptors,
+                               const double* weights);
 int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup, int* word_ids, double* weights,
                       int* node_ids, int* bow_n, int* bow_words, double* bow_values, int* fv_n, int* fv_nodes,
                       int* fv_offsets, int* fv_features);

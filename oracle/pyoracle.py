@@ -253,6 +253,17 @@ class _Base:
         f.argtypes = [C.c_char_p]
         return int(f(path.encode()))
 
+    def vocabulary_from_arrays(self, name, voc):
+        """The tree of a synthetic.vocabulary dict, stored under name (oracle only)."""
+        par = np.ascontiguousarray(voc["parents"], np.int32)
+        lf = np.ascontiguousarray(voc["is_leaf"], np.uint8)
+        d = np.ascontiguousarray(voc["descriptors"], np.uint8)
+        w = np.ascontiguousarray(voc["weights"], np.float64)
+        f = self.lib.orc_vocabulary_from_arrays
+        f.argtypes = [C.c_char_p] + [C.c_int] * 5 + [C.c_void_p] * 4
+        return int(f(name.encode(), int(voc["k"]), int(voc["L"]), int(voc["scoring"]), int(voc["weighting"]),
+                     len(par) + 1, _p(par), _p(lf), _p(d), _p(w)))
+
     def bow_transform(self, path, desc, levelsup=4):
         """TemplatedVocabulary::transform(features, BowVector, FeatureVector,
         levelsup) with the vocabulary loaded from path."""
