@@ -216,6 +216,25 @@ int orbgpu_bow_transform(const orbgpu_vocabulary* v, const uint8_t* desc, const 
                          double* bow_values, int* fv_counts, int* fv_nodes, int* fv_starts, int* fv_sizes,
                          int* fv_features, void* stream);
 
+/* ORBmatcher::SearchByBoW(KeyFrame* pKF, Frame& F, vector<MapPoint*>&
+ * vpMapPointMatches) -- src/ORBmatcher.cc:247-380 -- for npairs (keyframe,
+ * frame) pairs in one launch, with the matcher's nnratio and checkOri.
+ * Keyframes and frames are entries of one set laid out as
+ * orbgpu_bow_transform's inputs and outputs: entry s owns keypoints /
+ * descriptor rows [offsets[s], offsets[s + 1]) (at most 8192) and its
+ * FeatureVector (fv_counts[s] nodes at fv_nodes / fv_starts / fv_sizes from
+ * offsets[s], feature lists in fv_features).  pairs: 2 * npairs ints
+ * (keyframe entry, frame entry).  kf_mappoints: one byte per row, 1 where
+ * the keyframe's GetMapPointMatches()[i] is a map point that is not bad.
+ * match_out: for pair p, the frame's rows at out_offsets[p]: the keyframe
+ * feature whose map point vpMapPointMatches[i] receives, or -1.
+ * nmatches[p]: the reference's return value (-1 for an entry beyond 8192
+ * features).  Device or page-locked host memory; asynchronous; one launch. */
+int orbgpu_search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets, const int* fv_counts,
+                         const int* fv_nodes, const int* fv_starts, const int* fv_sizes, const int* fv_features,
+                         const uint8_t* kf_mappoints, const int* pairs, int npairs, float nnratio, int check_ori,
+                         const int* out_offsets, int* match_out, int* nmatches, void* stream);
+
 /* Frame::UndistortKeyPoints() -- src/Frame.cc:724-776 -- for n keypoints of
  * one camera: out[i] = kps[i] with x, y through cv::undistortPoints(pts, pts,
  * mK, mDistCoef, cv::Mat(), mK) (OpenCV 3.2's algorithm: double precision,

@@ -1168,6 +1168,79 @@ int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup
 
 }  // extern "C"
 
+// ORBmatcher::SearchByBoW(KeyFrame* pKF, Frame& F, vpMapPointMatches),
+// src/ORBmatcher.cc:247-380: the nodes both FeatureVectors hold, in ascending
+// order; in a node every keyframe feature with a map point that is not bad
+// (in list order) takes the frame feature of the node, not yet matched, at
+// the least distance (first in list order; second-best over the rest); kept
+// when best <= TH_LOW and best < nnratio * second; then the rotation check
+// (three_maxima).  kf_mp: 0 no map point, 1 a map point, 2 a bad one.
+// match_out[i]: the keyframe feature whose map point frame feature i got, or -1.
+int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_t* kf_mp, int kf_n, int kf_fv_n,
+                      const int* kf_fv_nodes, const int* kf_fv_offsets, const int* kf_fv_features, const orc_kp* f_kps,
+                      const uint8_t* f_desc, int f_n, int f_fv_n, const int* f_fv_nodes, const int* f_fv_offsets,
+                      const int* f_fv_features, float nnratio, int check_ori, int* match_out) {
+    const int TH_LOW = 50, HISTO = 30;
+    (void)kf_n;
+    for (int i = 0; i < f_n; i++) match_out[i] = -1;
+    std::vector<int> hist[HISTO];
+    const float factor = HISTO / 360.0f;
+    int nmatches = 0;
+    int a = 0, b = 0;
+    while (a < kf_fv_n && b < f_fv_n) {
+        if (kf_fv_nodes[a] < f_fv_nodes[b]) {
+            a++;
+            continue;
+        }
+        if (kf_fv_nodes[a] > f_fv_nodes[b]) {
+            b++;
+            continue;
+        }
+        for (int p = kf_fv_offsets[a]; p < kf_fv_offsets[a + 1]; p++) {
+            const int ikf = kf_fv_features[p];
+            if (kf_mp[ikf] != 1) continue;
+            int best1 = 256, best2 = 256, bestIdx = -1;
+            for (int q = f_fv_offsets[b]; q < f_fv_offsets[b + 1]; q++) {
+                const int jf = f_fv_features[q];
+                if (match_out[jf] >= 0) continue;
+                const int d = hamming(kf_desc + (size_t)ikf * 32, f_desc + (size_t)jf * 32);
+                if (d < best1) {
+                    best2 = best1;
+                    best1 = d;
+                    bestIdx = jf;
+                } else if (d < best2) {
+                    best2 = d;
+                }
+            }
+            if (best1 <= TH_LOW && (float)best1 < nnratio * (float)best2) {
+                match_out[bestIdx] = ikf;
+                if (check_ori) {
+                    float rot = kf_kps[ikf].angle - f_kps[bestIdx].angle;
+                    if (rot < 0.0) rot += 360.0f;
+                    int bin = (int)std::round(rot * factor);
+                    if (bin == HISTO) bin = 0;
+                    hist[bin].push_back(bestIdx);
+                }
+                nmatches++;
+            }
+        }
+        a++;
+        b++;
+    }
+    if (check_ori) {
+        int i1 = -1, i2 = -1, i3 = -1;
+        three_maxima(hist, HISTO, i1, i2, i3);
+        for (int h = 0; h < HISTO; h++) {
+            if (h == i1 || h == i2 || h == i3) continue;
+            for (int jf : hist[h]) {
+                match_out[jf] = -1;
+                nmatches--;
+            }
+        }
+    }
+    return nmatches;
+}
+
 // MapPoint::PredictScale(currentDist, Frame*), src/MapPoint.cc:604-619, on
 // given ratios mfMaxDistance / currentDist.
 void orc_predict_scale(const float* ratio, int n, float scale_factor, int nlevels, int* out) {

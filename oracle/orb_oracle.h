@@ -62,6 +62,15 @@ int orc_vocabulary_from_arrays(const char* name, int k, int L, int scoring, int 
 int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup, int* word_ids, double* weights,
                       int* node_ids, int* bow_n, int* bow_words, double* bow_values, int* fv_n, int* fv_nodes,
                       int* fv_offsets, int* fv_features);
+/* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
+ * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
+ * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:
+ * 0 no map point, 1 a map point, 2 a bad one.  match_out: f_n keyframe
+ * feature indices or -1.  Returns nmatches. */
+int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_t* kf_mp, int kf_n, int kf_fv_n,
+                      const int* kf_fv_nodes, const int* kf_fv_offsets, const int* kf_fv_features, const orc_kp* f_kps,
+                      const uint8_t* f_desc, int f_n, int f_fv_n, const int* f_fv_nodes, const int* f_fv_offsets,
+                      const int* f_fv_features, float nnratio, int check_ori, int* match_out);
 /* Frame::UndistortKeyPoints (src/Frame.cc:724-776) and ComputeImageBounds
  * (:778-819) with cv::undistortPoints restated from OpenCV 3.2.  K4 = fx, fy,
  * cx, cy; dist = k1 k2 p1 p2 [k3] (ndist 4 or 5); bounds = mnMinX, mnMaxX,

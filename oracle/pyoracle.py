@@ -287,6 +287,27 @@ class _Base:
                 "bow_words": bw[:b].copy(), "bow_values": bv[:b].copy(), "fv_nodes": fn[:q].copy(),
                 "fv_offsets": fo[:q + 1].copy(), "fv_features": ff[:fo[q]].copy()}
 
+    def search_by_bow(self, kf_kps, kf_desc, kf_mp, kf_fv, f_kps, f_desc, f_fv, nnratio=0.75, check_ori=True):
+        """ORBmatcher::SearchByBoW(KeyFrame*, Frame&, matches).  *_fv: (nodes,
+        offsets, features) of the FeatureVector (bow_transform's fv_*);
+        kf_mp: 0 none, 1 a map point, 2 a bad one.  -> (nmatches, match_out)."""
+        kf_kps = np.ascontiguousarray(kf_kps, KP_DTYPE)
+        f_kps = np.ascontiguousarray(f_kps, KP_DTYPE)
+        kf_desc = np.ascontiguousarray(kf_desc, np.uint8)
+        f_desc = np.ascontiguousarray(f_desc, np.uint8)
+        kf_mp = np.ascontiguousarray(kf_mp, np.uint8)
+        kn, ko, kfe = (np.ascontiguousarray(a, np.int32) for a in kf_fv)
+        fn_, fo, ffe = (np.ascontiguousarray(a, np.int32) for a in f_fv)
+        out = np.zeros(max(len(f_kps), 1), np.int32)
+        f = self.fn("search_by_bow")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                      C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                      C.c_int, C.c_void_p]
+        nm = f(_p(kf_kps), _p(kf_desc), _p(kf_mp), len(kf_kps), len(kn), _p(kn), _p(ko), _p(kfe), _p(f_kps),
+               _p(f_desc), len(f_kps), len(fn_), _p(fn_), _p(fo), _p(ffe), C.c_float(nnratio), int(bool(check_ori)),
+               _p(out))
+        return int(nm), out[:len(f_kps)].copy()
+
     def undistort_keypoints(self, K4, dist, kps):
         """Frame::UndistortKeyPoints: the keypoints with undistorted x, y."""
         K = np.ascontiguousarray(K4, np.float32)

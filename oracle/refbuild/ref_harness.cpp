@@ -586,6 +586,63 @@ int ref_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup
     return 0;
 }
 
+static DBoW2::FeatureVector feature_vector(int n, const int* nodes, const int* offsets, const int* features) {
+    DBoW2::FeatureVector fv;
+    for (int i = 0; i < n; i++)
+        for (int p = offsets[i]; p < offsets[i + 1]; p++) fv.addFeature((DBoW2::NodeId)nodes[i], (unsigned)features[p]);
+    return fv;
+}
+
+// ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches) --
+// src/ORBmatcher.cc:247-380.  The keyframe is built from a frame holding its
+// keypoints (mvKeysUn) and descriptors; its map points are real MapPoints
+// (kf_mp 1), bad ones (2) or NULL (0).  match_out as orc_search_by_bow.
+int ref_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_t* kf_mp, int kf_n, int kf_fv_n,
+                      const int* kf_fv_nodes, const int* kf_fv_offsets, const int* kf_fv_features, const orc_kp* f_kps,
+                      const uint8_t* f_desc, int f_n, int f_fv_n, const int* f_fv_nodes, const int* f_fv_offsets,
+                      const int* f_fv_features, float nnratio, int check_ori, int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        MapPointMaker maker;
+        cv::Mat pos = cv::Mat::zeros(3, 1, CV_32F);
+        Frame* KFsrc = new Frame();
+        KFsrc->N = kf_n;
+        KFsrc->mvKeys = kps_in(kf_kps, kf_n);
+        KFsrc->mvKeysUn = KFsrc->mvKeys;
+        KFsrc->mvuRight.assign(kf_n, -1.0f);
+        KFsrc->mDescriptors = cv::Mat(kf_n, 32, CV_8U);
+        std::memcpy(KFsrc->mDescriptors.data, kf_desc, (size_t)kf_n * 32);
+        KeyFrame* KF = new KeyFrame(*KFsrc, maker.map, nullptr);
+        KF->mFeatVec = feature_vector(kf_fv_n, kf_fv_nodes, kf_fv_offsets, kf_fv_features);
+        KF->mvpMapPoints.assign(kf_n, static_cast<MapPoint*>(NULL));
+        std::map<MapPoint*, int> index;
+        for (int i = 0; i < kf_n; i++) {
+            if (kf_mp[i] == 0) continue;
+            MapPoint* mp = maker.make(pos, 1);
+            mp->mbBad = kf_mp[i] == 2;
+            KF->mvpMapPoints[i] = mp;
+            index[mp] = i;
+        }
+        Frame* F = new Frame();
+        F->N = f_n;
+        F->mvKeys = kps_in(f_kps, f_n);
+        F->mvKeysUn = F->mvKeys;
+        F->mDescriptors = cv::Mat(f_n, 32, CV_8U);
+        std::memcpy(F->mDescriptors.data, f_desc, (size_t)f_n * 32);
+        F->mFeatVec = feature_vector(f_fv_n, f_fv_nodes, f_fv_offsets, f_fv_features);
+        std::vector<MapPoint*> matches;
+        ORBmatcher matcher(nnratio, check_ori != 0);
+        nm = matcher.SearchByBoW(KF, *F, matches);
+        for (int i = 0; i < f_n; i++) match_out[i] = matches[i] ? index[matches[i]] : -1;
+        for (auto& e : index) delete e.first;
+        delete F;
+        delete KF;
+        delete KFsrc;
+    }
+    return nm;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

@@ -3,9 +3,10 @@
 // and src/MapPoint.cc reference but whose own sources (src/KeyFrame.cc,
 // src/Map.cc, src/Converter.cc) need Eigen/g2o/DBoW2 vocabularies and are off
 // the feature path.  The keyframe constructor copies only the fields the
-// compiled reference code reads (mnFrameId, mvuRight, mDescriptors) and
-// zeroes the rest; the accessors the path uses (KeyFrame::isBad) return the
-// stored field exactly as src/KeyFrame.cc does (without its locking);
+// compiled reference code reads (mnFrameId, mvKeysUn, mvuRight, mDescriptors)
+// and zeroes the rest; the accessors the path uses (KeyFrame::isBad,
+// GetMapPointMatches) return the stored fields exactly as src/KeyFrame.cc
+// does (without its locking);
 // everything else aborts if called.
 #include "MapPoint.h"
 #include "KeyFrame.h"
@@ -29,7 +30,8 @@ KeyFrame::KeyFrame(Frame& F, Map* pMap, KeyFrameDatabase* pKFDB)
       mfGridElementHeightInv(0), mnTrackReferenceForFrame(0), mnFuseTargetForKF(0), mnBALocalForKF(0),
       mnBAFixedForKF(0), mnLoopQuery(0), mnLoopWords(0), mLoopScore(0), mnRelocQuery(0), mnRelocWords(0),
       mRelocScore(0), mnBAGlobalForKF(0), fx(0), fy(0), cx(0), cy(0), invfx(0), invfy(0), mbf(0), mb(0),
-      mThDepth(0), N(F.N), mvuRight(F.mvuRight), mDescriptors(F.mDescriptors.clone()), mnScaleLevels(0),
+      mThDepth(0), N(F.N), mvKeysUn(F.mvKeysUn), mvuRight(F.mvuRight), mDescriptors(F.mDescriptors.clone()),
+      mnScaleLevels(0),
       mfScaleFactor(0), mfLogScaleFactor(0), mnMinX(0), mnMinY(0), mnMaxX(0), mnMaxY(0), mpKeyFrameDB(pKFDB),
       mpORBvocabulary(nullptr), mbFirstConnection(true), mpParent(nullptr), mbNotErase(false),
       mbToBeErased(false), mbBad(false), mHalfBaseline(0), mpMap(pMap) {
@@ -46,7 +48,7 @@ std::vector<size_t> KeyFrame::GetFeaturesInArea(const float&, const float&, cons
     stub_unreachable("KeyFrame::GetFeaturesInArea");
 }
 MapPoint* KeyFrame::GetMapPoint(const size_t&) { stub_unreachable("KeyFrame::GetMapPoint"); }
-std::vector<MapPoint*> KeyFrame::GetMapPointMatches() { stub_unreachable("KeyFrame::GetMapPointMatches"); }
+std::vector<MapPoint*> KeyFrame::GetMapPointMatches() { return mvpMapPoints; }
 std::set<MapPoint*> KeyFrame::GetMapPoints() { stub_unreachable("KeyFrame::GetMapPoints"); }
 cv::Mat KeyFrame::GetRotation() { stub_unreachable("KeyFrame::GetRotation"); }
 cv::Mat KeyFrame::GetTranslation() { stub_unreachable("KeyFrame::GetTranslation"); }

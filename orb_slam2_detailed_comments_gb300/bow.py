@@ -102,3 +102,35 @@ class Vocabulary:
         feats = r["fv_features"][:n].cpu().numpy()
         return ({int(w): float(v) for w, v in zip(words, values)},
                 {int(nd): feats[s:s + z].tolist() for nd, s, z in zip(nodes, starts, sizes)})
+
+
+def search_by_bow(keypoints, descriptors, offsets, bow, kf_mappoints, pairs, nnratio: float = 0.75,
+                  check_orientation: bool = True, stream=None):
+    """ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
+    (src/ORBmatcher.cc:247-380) for many (keyframe, frame) pairs in one launch.
+
+    keypoints (n, 7) float32, descriptors (n, 32) uint8 and offsets (S + 1,)
+    int32 tensors hold a set of S keyframes and frames back to back; bow is
+    Vocabulary.transform's result on that set; kf_mappoints (n,) uint8, 1
+    where a keyframe feature has a map point that is not bad; pairs (P, 2)
+    host ints (keyframe entry, frame entry).  Returns (nmatches (P,), list of
+    P match tensors: per frame feature the keyframe feature whose map point it
+    receives, or -1)."""
+    import torch
+    pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    offs = offsets.cpu().numpy() if offsets.is_cuda else np.asarray(offsets)
+    sizes = offs[pr[:, 1] + 1] - offs[pr[:, 1]]
+    out_off = np.zeros(len(pr) + 1, np.int32)
+    out_off[1:] = np.cumsum(sizes)
+    dev = torch.device("cuda")
+    P = torch.from_numpy(pr.reshape(-1).copy()).to(dev)
+    OO = torch.from_numpy(out_off[:-1].copy()).to(dev)
+    match = torch.empty(max(int(out_off[-1]), 1), dtype=torch.int32, device=dev)
+    nm = torch.empty(max(len(pr), 1), dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+    check(lib().orbgpu_search_by_bow(ptr(keypoints), ptr(descriptors), ptr(offsets), ptr(bow["fv_counts"]),
+                                     ptr(bow["fv_nodes"]), ptr(bow["fv_starts"]), ptr(bow["fv_sizes"]),
+                                     ptr(bow["fv_features"]), ptr(kf_mappoints), ptr(P), len(pr), C.c_float(nnratio),
+                                     int(bool(check_orientation)), ptr(OO), ptr(match), ptr(nm), C.c_void_p(st)),
+          "orbgpu_search_by_bow")
+    return nm[:len(pr)], [match[out_off[i]:out_off[i + 1]] for i in range(len(pr))]

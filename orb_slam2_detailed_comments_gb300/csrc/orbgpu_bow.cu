@@ -211,9 +211,180 @@ __global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
     }
 }
 
+// ORBmatcher::SearchByBoW(KeyFrame* pKF, Frame& F, vpMapPointMatches),
+// src/ORBmatcher.cc:247-380, one block per (keyframe, frame) pair.  A frame
+// feature belongs to one FeatureVector node and so does a keyframe feature:
+// the nodes both vectors hold are independent, and one warp takes one node
+// (found by binary search in the keyframe's sorted node list).  Inside a node
+// the keyframe features run in list order, as in the reference: each takes,
+// among the node's frame features not matched yet (a shared bitmap), the
+// first at the least distance, with the second-best over the rest; kept when
+// best <= TH_LOW and best < nnratio * second.  Then the rotation histogram,
+// ComputeThreeMaxima (src/ORBmatcher.cc:2035-2077) and the resets.
+#define SBB_THREADS 1024
+#define SBB_TH_LOW 50
+
+__global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
+    const orbgpu_keypoint* __restrict__ kps, const uint4* __restrict__ desc, const int* __restrict__ offsets,
+    const int* __restrict__ fv_counts, const int* __restrict__ fv_nodes, const int* __restrict__ fv_starts,
+    const int* __restrict__ fv_sizes, const int* __restrict__ fv_features, const uint8_t* __restrict__ kf_mp,
+    const int* __restrict__ pairs, float nnratio, int check_ori, const int* __restrict__ out_offsets,
+    int* __restrict__ match_out, int* __restrict__ nmatches) {
+    __shared__ unsigned s_taken[BOW_MAX_FEATURES / 32];
+    __shared__ unsigned char s_bin[BOW_MAX_FEATURES];
+    __shared__ int hist[ORBGPU_HISTO_LENGTH];
+    __shared__ int s_ind[3], s_nm;
+    const int p = blockIdx.x;
+    const int kf = pairs[2 * p], fr = pairs[2 * p + 1];
+    const int ok0 = offsets[kf], of0 = offsets[fr];
+    const int fn = offsets[fr + 1] - of0;
+    const int ckf = fv_counts[kf], cf = fv_counts[fr];
+    int* out = match_out + out_offsets[p];
+    if (fn < 0 || fn > BOW_MAX_FEATURES || ckf < 0 || cf < 0) {
+        if (threadIdx.x == 0) nmatches[p] = -1;
+        return;
+    }
+    for (int i = threadIdx.x; i < fn; i += blockDim.x) out[i] = -1;
+    for (int i = threadIdx.x; i < BOW_MAX_FEATURES / 32; i += blockDim.x) s_taken[i] = 0;
+    if (threadIdx.x < ORBGPU_HISTO_LENGTH) hist[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_nm = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const float factor = __fdiv_rn((float)ORBGPU_HISTO_LENGTH, 360.0f);
+    const unsigned INF = 0x7fffffffu;
+    for (int j = warp; j < cf; j += nwarps) {
+        const int node = fv_nodes[of0 + j];
+        int lo = 0, hi = ckf - 1, jk = -1;
+        while (lo <= hi) {
+            const int mid = (lo + hi) >> 1;
+            const int v = fv_nodes[ok0 + mid];
+            if (v == node) {
+                jk = mid;
+                break;
+            }
+            if (v < node) lo = mid + 1;
+            else hi = mid - 1;
+        }
+        if (jk < 0) continue;
+        const int* flist = fv_features + fv_starts[of0 + j];
+        const int fcount = fv_sizes[of0 + j];
+        const int* klist = fv_features + fv_starts[ok0 + jk];
+        const int kcount = fv_sizes[ok0 + jk];
+        for (int t = 0; t < kcount; t++) {
+            const int ikf = klist[t];
+            if (kf_mp[ok0 + ikf] != 1) continue;
+            const uint4 a0 = desc[2 * (size_t)(ok0 + ikf)], a1 = desc[2 * (size_t)(ok0 + ikf) + 1];
+            unsigned b1 = INF;
+            int b2 = 256;
+            for (int c = 0; c < fcount; c += 32) {
+                unsigned key = INF;
+                int d = 256;
+                if (c + lane < fcount) {
+                    const int jf = flist[c + lane];
+                    if (!((s_taken[jf >> 5] >> (jf & 31)) & 1u)) {
+                        d = hamming256(a0, a1, desc[2 * (size_t)(of0 + jf)], desc[2 * (size_t)(of0 + jf) + 1]);
+                        key = ((unsigned)d << 13) | (unsigned)(c + lane);
+                    }
+                }
+                const unsigned c1 = __reduce_min_sync(0xffffffffu, key);
+                const int c2 = (int)__reduce_min_sync(0xffffffffu, (unsigned)(key == c1 ? 256 : d));
+                if (c1 < b1) {
+                    b2 = min(b1 == INF ? 256 : (int)(b1 >> 13), c2);
+                    b1 = c1;
+                } else {
+                    b2 = min(b2, c1 == INF ? 256 : (int)(c1 >> 13));
+                }
+            }
+            const int best1 = b1 == INF ? 256 : (int)(b1 >> 13);
+            if (best1 <= SBB_TH_LOW && (float)best1 < __fmul_rn(nnratio, (float)b2)) {
+                if (lane == 0) {
+                    const int jf = flist[b1 & 8191u];
+                    atomicOr(&s_taken[jf >> 5], 1u << (jf & 31));
+                    out[jf] = ikf;
+                    if (check_ori) {
+                        float rot = __fsub_rn(kps[ok0 + ikf].angle, kps[of0 + jf].angle);
+                        if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
+                        int bin = (int)roundf(__fmul_rn(rot, factor));
+                        if (bin == ORBGPU_HISTO_LENGTH) bin = 0;
+                        s_bin[jf] = (unsigned char)bin;
+                        atomicAdd(&hist[bin], 1);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        if (check_ori) {
+            int max1 = 0, max2 = 0, max3 = 0;
+            for (int b = 0; b < ORBGPU_HISTO_LENGTH; b++) {  // ComputeThreeMaxima, src/ORBmatcher.cc:2035-2077
+                const int sz = hist[b];
+                if (sz > max1) {
+                    max3 = max2; max2 = max1; max1 = sz;
+                    ind3 = ind2; ind2 = ind1; ind1 = b;
+                } else if (sz > max2) {
+                    max3 = max2; max2 = sz;
+                    ind3 = ind2; ind2 = b;
+                } else if (sz > max3) {
+                    max3 = sz;
+                    ind3 = b;
+                }
+            }
+            if ((float)max2 < __fmul_rn(0.1f, (float)max1)) {
+                ind2 = -1;
+                ind3 = -1;
+            } else if ((float)max3 < __fmul_rn(0.1f, (float)max1)) {
+                ind3 = -1;
+            }
+        }
+        s_ind[0] = ind1;
+        s_ind[1] = ind2;
+        s_ind[2] = ind3;
+    }
+    __syncthreads();
+    int kept = 0;
+    for (int i = threadIdx.x; i < fn; i += blockDim.x) {
+        if (out[i] < 0) continue;
+        if (check_ori) {
+            const int b = s_bin[i];
+            if (b != s_ind[0] && b != s_ind[1] && b != s_ind[2]) {
+                out[i] = -1;
+                continue;
+            }
+        }
+        kept++;
+    }
+    kept = __reduce_add_sync(0xffffffffu, kept);
+    if (lane == 0 && kept) atomicAdd(&s_nm, kept);
+    __syncthreads();
+    if (threadIdx.x == 0) nmatches[p] = s_nm;
+}
+
 }  // namespace orbgpu
 
 using namespace orbgpu;
+
+extern "C" int orbgpu_search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
+                                    const int* fv_counts, const int* fv_nodes, const int* fv_starts,
+                                    const int* fv_sizes, const int* fv_features, const uint8_t* kf_mappoints,
+                                    const int* pairs, int npairs, float nnratio, int check_ori,
+                                    const int* out_offsets, int* match_out, int* nmatches, void* stream) {
+    if (npairs < 0 || (npairs > 0 && (!kps || !desc || !offsets || !fv_counts || !fv_nodes || !fv_starts ||
+                                      !fv_sizes || !fv_features || !kf_mappoints || !pairs || !out_offsets ||
+                                      !match_out || !nmatches)) ||
+        ((uintptr_t)desc & 15)) {
+        orbgpu_set_last_error("orbgpu_search_by_bow: bad arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (npairs == 0) return ORBGPU_OK;
+    k_search_by_bow<<<npairs, SBB_THREADS, 0, (cudaStream_t)stream>>>(
+        kps, reinterpret_cast<const uint4*>(desc), offsets, fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features,
+        kf_mappoints, pairs, nnratio, check_ori, out_offsets, match_out, nmatches);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    return ORBGPU_OK;
+}
 
 extern "C" int orbgpu_vocabulary_create(int k, int L, int scoring, int weighting, int nnodes, const int* parents,
                                         const uint8_t* is_leaf, const uint8_t* descriptors, const double* weights,

@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb")
 
 
 def main(groups=GROUPS):
@@ -55,6 +55,8 @@ def main(groups=GROUPS):
         undistort_fixture(R)
     if "bow" in groups:
         bow_fixture(R)
+    if "sbb" in groups:
+        search_by_bow_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -312,6 +314,37 @@ def bow_fixture(R):
                     for key, val in out.items():
                         arrays[f"{name}_f{fi}_lu{lu}_{key}"] = val
     save("bow.npz", **arrays)
+
+
+def search_by_bow_fixture(R):
+    # 13. ORBmatcher::SearchByBoW(KeyFrame*, Frame&) on two scene pairs, the
+    # FeatureVectors from the reference's transform (k 10, L 4, levelsup 2)
+    import tempfile
+    voc = syn.vocabulary(10, 4, 5)
+    arrays = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "voc.txt")
+        syn.write_vocabulary_text(voc, path)
+        R.vocabulary_load(path)
+        for sc in range(2):
+            f1, f2, _ = syn.frame_pair(640, 480, 70 + sc)
+            a, b = R.extract(f1, nfeatures=1500), R.extract(f2, nfeatures=1500)
+            fa, fb = R.bow_transform(path, a.descriptors, 2), R.bow_transform(path, b.descriptors, 2)
+            mp = np.random.default_rng(sc).choice([0, 1, 1, 1, 2], len(a.keypoints)).astype(np.uint8)
+            pre = f"s{sc}_"
+            arrays.update({pre + "kf_kps": a.keypoints, pre + "kf_desc": a.descriptors, pre + "kf_mp": mp,
+                           pre + "f_kps": b.keypoints, pre + "f_desc": b.descriptors})
+            for side, fv in (("kf", fa), ("f", fb)):
+                for key in ("fv_nodes", "fv_offsets", "fv_features"):
+                    arrays[pre + side + "_" + key] = fv[key]
+            for ori, ratio in ((1, 0.75), (0, 0.9)):
+                nm, match = R.search_by_bow(a.keypoints, a.descriptors, mp,
+                                            (fa["fv_nodes"], fa["fv_offsets"], fa["fv_features"]), b.keypoints,
+                                            b.descriptors, (fb["fv_nodes"], fb["fv_offsets"], fb["fv_features"]),
+                                            ratio, bool(ori))
+                arrays[pre + f"nm_{ori}"] = np.array(nm)
+                arrays[pre + f"match_{ori}"] = match
+    save("search_by_bow.npz", **arrays)
 
 
 if __name__ == "__main__":

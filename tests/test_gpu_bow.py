@@ -141,3 +141,43 @@ def test_compute_bow_single_frame(torch, oracle, tmp_path):
     assert list(bv) == ref["bow_words"].tolist() and list(bv.values()) == ref["bow_values"].tolist()
     assert list(fv) == ref["fv_nodes"].tolist()
     assert sum(fv.values(), []) == ref["fv_features"].tolist()
+
+
+@pytest.mark.parametrize("check_ori,ratio", [(True, 0.75), (False, 0.75), (True, 0.9)])
+def test_search_by_bow_vs_oracle(torch, oracle, check_ori, ratio):
+    """SearchByBoW for 8 (keyframe, frame) pairs of 4 scenes in one launch:
+    BoW from the GPU transform, matches and counts against the oracle."""
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import Vocabulary, search_by_bow
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    voc = syn.vocabulary(10, 4, 5)
+    oracle.vocabulary_from_arrays("sbb", voc)
+    V = Vocabulary.from_arrays(10, 4, 0, 0, voc["parents"], voc["is_leaf"], voc["descriptors"], voc["weights"])
+    ents = []
+    for seed in range(4):
+        f1, f2, _ = syn.frame_pair(640, 480, 40 + seed)
+        ents += [oracle.extract(f1, nfeatures=1500), oracle.extract(f2, nfeatures=1500)]
+    offs = np.zeros(len(ents) + 1, np.int32)
+    offs[1:] = np.cumsum([len(e.keypoints) for e in ents])
+    kps = np.concatenate([e.keypoints for e in ents])
+    desc = np.concatenate([e.descriptors for e in ents])
+    mp = np.random.default_rng(2).choice([0, 1, 1, 1, 2], len(kps)).astype(np.uint8)
+    K = torch.from_numpy(kps.view(np.float32).reshape(-1, 7).copy()).cuda()
+    D = torch.from_numpy(desc).cuda()
+    O = torch.from_numpy(offs).cuda()
+    bow = V.transform(D, O, 2)
+    # keyframe = even entry, frame = odd entry, both directions
+    pairs = [(2 * s, 2 * s + 1) for s in range(4)] + [(2 * s + 1, 2 * s) for s in range(4)]
+    nm, matches = search_by_bow(K, D, O, bow, torch.from_numpy(mp).cuda(), pairs, ratio, check_ori)
+    torch.cuda.synchronize()
+    for p, (a, b) in enumerate(pairs):
+        ea, eb = ents[a], ents[b]
+        fa = oracle.bow_transform("sbb", ea.descriptors, 2)
+        fb = oracle.bow_transform("sbb", eb.descriptors, 2)
+        ref_nm, ref = oracle.search_by_bow(ea.keypoints, ea.descriptors, mp[offs[a]:offs[a + 1]],
+                                           (fa["fv_nodes"], fa["fv_offsets"], fa["fv_features"]),
+                                           eb.keypoints, eb.descriptors,
+                                           (fb["fv_nodes"], fb["fv_offsets"], fb["fv_features"]), ratio, check_ori)
+        assert int(nm[p]) == ref_nm, p
+        assert np.array_equal(matches[p].cpu().numpy(), ref), p
+        assert ref_nm > 100

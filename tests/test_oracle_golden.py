@@ -264,3 +264,17 @@ def test_bow_transform_golden(oracle, golden, tmp_path, name):
             out = oracle.bow_transform(path, g[f"{name}_f{fi}_desc"], lu)
             for key, val in out.items():
                 assert np.array_equal(val, g[f"{name}_f{fi}_lu{lu}_{key}"]), (fi, lu, key)
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_search_by_bow_golden(oracle, golden, sc):
+    """ORBmatcher::SearchByBoW(KeyFrame*, Frame&) against the reference's outputs."""
+    g = golden("search_by_bow.npz")
+    pre = f"s{sc}_"
+    fv = {side: tuple(g[pre + side + "_" + k] for k in ("fv_nodes", "fv_offsets", "fv_features"))
+          for side in ("kf", "f")}
+    for ori, ratio in ((1, 0.75), (0, 0.9)):
+        nm, match = oracle.search_by_bow(g[pre + "kf_kps"], g[pre + "kf_desc"], g[pre + "kf_mp"], fv["kf"],
+                                         g[pre + "f_kps"], g[pre + "f_desc"], fv["f"], ratio, bool(ori))
+        assert nm == int(g[pre + f"nm_{ori}"])
+        assert np.array_equal(match, g[pre + f"match_{ori}"])
