@@ -634,7 +634,9 @@ def bench_bow(dev, steps=10, warmup=3):
     """Frame::ComputeBoW (DBoW2 transform, levelsup 4) for 64 frames x 2,000
     descriptors with a vocabulary of ORBvoc's shape (k 10, L 6: 1,111,111
     nodes, 1,000,000 words; synthetic, the reference's vocabulary file is not
-    in its tree), TF-IDF weights, L1 scoring.  Device-resident (events, L2
+    in its tree), TF-IDF weights, L1 scoring; consecutive frames share 70 % of
+    their features.  Then SearchByBoW(KeyFrame*, Frame&) for the 63 pairs of
+    consecutive frames.  Device-resident (events, L2
     flushed between calls), end to end from page-locked descriptors (results
     copied back), and the oracle on one host core."""
     import torch
@@ -651,6 +653,14 @@ def bench_bow(dev, steps=10, warmup=3):
     for _ in range(2):
         flips &= rng.integers(0, 256, base.shape, dtype=np.uint8)
     desc = np.ascontiguousarray(base ^ flips)
+    # consecutive frames share 70 % of their features (noisy copies), so the
+    # SearchByBoW pairs below find matches as tracking frames do
+    for f in range(1, nf):
+        rows = rng.choice(per, int(0.7 * per), replace=False)
+        noise = rng.integers(0, 256, (len(rows), 32), dtype=np.uint8)
+        for _ in range(3):
+            noise &= rng.integers(0, 256, (len(rows), 32), dtype=np.uint8)
+        desc[f * per + rows] = desc[(f - 1) * per + rows] ^ noise
     offs = np.arange(0, nf * per + 1, per, dtype=np.int32)
     D, O = torch.from_numpy(desc).to(dev), torch.from_numpy(offs).to(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -694,6 +704,40 @@ def bench_bow(dev, steps=10, warmup=3):
         ref = o.bow_transform("bench", desc[f * per:(f + 1) * per], 4)
         same &= bool(np.array_equal(ref["bow_words"], gpu_words[f * per:f * per + gpu_counts[f]]))
     cpu_s = time.perf_counter() - t0
+    # SearchByBoW(KeyFrame*, Frame&) on the same set: frame f as the keyframe
+    # of frame f + 1 (63 pairs), every keyframe feature with a map point
+    from orb_slam2_detailed_comments_gb300 import search_by_bow
+    kps = np.zeros((nf * per, 7), np.float32)
+    kps[:, 3] = rng.uniform(0, 360, nf * per)
+    K = torch.from_numpy(kps).to(dev)
+    MP = torch.ones(nf * per, dtype=torch.uint8, device=dev)
+    pairs = [(f, f + 1) for f in range(nf - 1)]
+    r = V.transform(D, O, 4)
+    for _ in range(warmup):
+        search_by_bow(K, D, O, r, MP, pairs)
+    torch.cuda.synchronize()
+    sms = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        nm, _ = search_by_bow(K, D, O, r, MP, pairs)
+        e1.record(stream)
+        e1.synchronize()
+        sms.append(e0.elapsed_time(e1))
+    sbb_ms = statistics.median(sms)
+    gpu_nm = nm.cpu().numpy()
+    t0 = time.perf_counter()
+    sbb_same = True
+    kp_rec = kps.view(pyoracle.KP_DTYPE).reshape(-1)
+    for f in range(4):
+        a = o.bow_transform("bench", desc[f * per:(f + 1) * per], 4)
+        b = o.bow_transform("bench", desc[(f + 1) * per:(f + 2) * per], 4)
+        ref_nm, _ = o.search_by_bow(kp_rec[f * per:(f + 1) * per], desc[f * per:(f + 1) * per],
+                                    np.ones(per, np.uint8), (a["fv_nodes"], a["fv_offsets"], a["fv_features"]),
+                                    kp_rec[(f + 1) * per:(f + 2) * per], desc[(f + 1) * per:(f + 2) * per],
+                                    (b["fv_nodes"], b["fv_offsets"], b["fv_features"]))
+        sbb_same &= ref_nm == int(gpu_nm[f])
+    sbb_cpu_s = time.perf_counter() - t0
     pk, pk_src = peaks()
     # algorithmic bytes: each descriptor read once, 6 levels x 10 child rows,
     # per-feature outputs, the assembled vectors
@@ -709,7 +753,12 @@ def bench_bow(dev, steps=10, warmup=3):
                          "note": "child rows counted at every visit; the upper levels are served by L2"},
             "cpu_baseline": {"value": sample * per / cpu_s, "unit": "features/s", "cores": 1, "kind": "port",
                              "sample": f"{sample} frames x {per} descriptors, oracle restatement"},
-            "bow_words_equal_to_oracle": same}
+            "bow_words_equal_to_oracle": same,
+            "search_by_bow": {"pairs": len(pairs), "ms": sbb_ms, "pairs_per_s": len(pairs) / (sbb_ms / 1e3),
+                              "matches_median": float(np.median(gpu_nm)), "nmatches_equal_to_oracle": bool(sbb_same),
+                              "cpu_baseline": {"value": 4 / sbb_cpu_s, "unit": "pairs/s", "cores": 1,
+                                               "kind": "port",
+                                               "sample": "4 pairs, oracle transform + SearchByBoW"}}}
 
 
 def bench_serving(dev, duration_s=3.0):

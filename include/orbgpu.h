@@ -235,6 +235,18 @@ int orbgpu_search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const 
                          const uint8_t* kf_mappoints, const int* pairs, int npairs, float nnratio, int check_ori,
                          const int* out_offsets, int* match_out, int* nmatches, void* stream);
 
+/* ORBmatcher::SearchByBoW(KeyFrame* pKF1, KeyFrame* pKF2, vector<MapPoint*>&
+ * vpMatches12) -- src/ORBmatcher.cc:729-880 -- for npairs keyframe pairs:
+ * the same set layout; pairs hold (pKF1 entry, pKF2 entry); kf_mappoints is
+ * read for both sides (candidates in pKF2 need a map point that is not bad
+ * too).  match_out: for pair p, pKF1's rows at out_offsets[p]: the pKF2
+ * feature whose map point vpMatches12[i] receives, or -1. */
+int orbgpu_search_by_bow_keyframes(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
+                                   const int* fv_counts, const int* fv_nodes, const int* fv_starts,
+                                   const int* fv_sizes, const int* fv_features, const uint8_t* kf_mappoints,
+                                   const int* pairs, int npairs, float nnratio, int check_ori, const int* out_offsets,
+                                   int* match_out, int* nmatches, void* stream);
+
 /* Frame::UndistortKeyPoints() -- src/Frame.cc:724-776 -- for n keypoints of
  * one camera: out[i] = kps[i] with x, y through cv::undistortPoints(pts, pts,
  * mK, mDistCoef, cv::Mat(), mK) (OpenCV 3.2's algorithm: double precision,

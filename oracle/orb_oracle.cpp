@@ -1176,13 +1176,19 @@ int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup
 // when best <= TH_LOW and best < nnratio * second; then the rotation check
 // (three_maxima).  kf_mp: 0 no map point, 1 a map point, 2 a bad one.
 // match_out[i]: the keyframe feature whose map point frame feature i got, or -1.
-int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_t* kf_mp, int kf_n, int kf_fv_n,
-                      const int* kf_fv_nodes, const int* kf_fv_offsets, const int* kf_fv_features, const orc_kp* f_kps,
-                      const uint8_t* f_desc, int f_n, int f_fv_n, const int* f_fv_nodes, const int* f_fv_offsets,
-                      const int* f_fv_features, float nnratio, int check_ori, int* match_out) {
+// keyframes: SearchByBoW(KeyFrame* pKF1, KeyFrame* pKF2, vpMatches12),
+// src/ORBmatcher.cc:729-880 -- candidates need a map point that is not bad
+// (f_mp), TH_LOW is exclusive, the result is per pKF1 feature.
+static int search_by_bow_impl(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_t* kf_mp, int kf_n,
+                              int kf_fv_n, const int* kf_fv_nodes, const int* kf_fv_offsets,
+                              const int* kf_fv_features, const orc_kp* f_kps, const uint8_t* f_desc,
+                              const uint8_t* f_mp, int f_n, int f_fv_n, const int* f_fv_nodes,
+                              const int* f_fv_offsets, const int* f_fv_features, float nnratio, int check_ori,
+                              bool keyframes, int* match_out) {
     const int TH_LOW = 50, HISTO = 30;
-    (void)kf_n;
-    for (int i = 0; i < f_n; i++) match_out[i] = -1;
+    const int nout = keyframes ? kf_n : f_n;
+    for (int i = 0; i < nout; i++) match_out[i] = -1;
+    std::vector<char> taken(f_n, 0);
     std::vector<int> hist[HISTO];
     const float factor = HISTO / 360.0f;
     int nmatches = 0;
@@ -1202,7 +1208,7 @@ int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_
             int best1 = 256, best2 = 256, bestIdx = -1;
             for (int q = f_fv_offsets[b]; q < f_fv_offsets[b + 1]; q++) {
                 const int jf = f_fv_features[q];
-                if (match_out[jf] >= 0) continue;
+                if (taken[jf] || (keyframes && f_mp[jf] != 1)) continue;
                 const int d = hamming(kf_desc + (size_t)ikf * 32, f_desc + (size_t)jf * 32);
                 if (d < best1) {
                     best2 = best1;
@@ -1212,14 +1218,16 @@ int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_
                     best2 = d;
                 }
             }
-            if (best1 <= TH_LOW && (float)best1 < nnratio * (float)best2) {
-                match_out[bestIdx] = ikf;
+            if ((keyframes ? best1 < TH_LOW : best1 <= TH_LOW) && (float)best1 < nnratio * (float)best2) {
+                taken[bestIdx] = 1;
+                const int slot = keyframes ? ikf : bestIdx;
+                match_out[slot] = keyframes ? bestIdx : ikf;
                 if (check_ori) {
                     float rot = kf_kps[ikf].angle - f_kps[bestIdx].angle;
                     if (rot < 0.0) rot += 360.0f;
                     int bin = (int)std::round(rot * factor);
                     if (bin == HISTO) bin = 0;
-                    hist[bin].push_back(bestIdx);
+                    hist[bin].push_back(slot);
                 }
                 nmatches++;
             }
@@ -1232,13 +1240,31 @@ int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_
         three_maxima(hist, HISTO, i1, i2, i3);
         for (int h = 0; h < HISTO; h++) {
             if (h == i1 || h == i2 || h == i3) continue;
-            for (int jf : hist[h]) {
-                match_out[jf] = -1;
+            for (int slot : hist[h]) {
+                match_out[slot] = -1;
                 nmatches--;
             }
         }
     }
     return nmatches;
+}
+
+int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_t* kf_mp, int kf_n, int kf_fv_n,
+                      const int* kf_fv_nodes, const int* kf_fv_offsets, const int* kf_fv_features, const orc_kp* f_kps,
+                      const uint8_t* f_desc, int f_n, int f_fv_n, const int* f_fv_nodes, const int* f_fv_offsets,
+                      const int* f_fv_features, float nnratio, int check_ori, int* match_out) {
+    return search_by_bow_impl(kf_kps, kf_desc, kf_mp, kf_n, kf_fv_n, kf_fv_nodes, kf_fv_offsets, kf_fv_features,
+                              f_kps, f_desc, nullptr, f_n, f_fv_n, f_fv_nodes, f_fv_offsets, f_fv_features, nnratio,
+                              check_ori, false, match_out);
+}
+
+int orc_search_by_bow_kf(const orc_kp* kps1, const uint8_t* desc1, const uint8_t* mp1, int n1, int fv1_n,
+                         const int* fv1_nodes, const int* fv1_offsets, const int* fv1_features, const orc_kp* kps2,
+                         const uint8_t* desc2, const uint8_t* mp2, int n2, int fv2_n, const int* fv2_nodes,
+                         const int* fv2_offsets, const int* fv2_features, float nnratio, int check_ori,
+                         int* match_out) {
+    return search_by_bow_impl(kps1, desc1, mp1, n1, fv1_n, fv1_nodes, fv1_offsets, fv1_features, kps2, desc2, mp2,
+                              n2, fv2_n, fv2_nodes, fv2_offsets, fv2_features, nnratio, check_ori, true, match_out);
 }
 
 // MapPoint::PredictScale(currentDist, Frame*), src/MapPoint.cc:604-619, on

@@ -71,6 +71,14 @@ int orc_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_
                       const int* kf_fv_nodes, const int* kf_fv_offsets, const int* kf_fv_features, const orc_kp* f_kps,
                       const uint8_t* f_desc, int f_n, int f_fv_n, const int* f_fv_nodes, const int* f_fv_offsets,
                       const int* f_fv_features, float nnratio, int check_ori, int* match_out);
+/* ORBmatcher::SearchByBoW(KeyFrame* pKF1, KeyFrame* pKF2, vpMatches12)
+ * (src/ORBmatcher.cc:729-880): match_out has n1 entries, the pKF2 feature
+ * matched to each pKF1 feature or -1. */
+int orc_search_by_bow_kf(const orc_kp* kps1, const uint8_t* desc1, const uint8_t* mp1, int n1, int fv1_n,
+                         const int* fv1_nodes, const int* fv1_offsets, const int* fv1_features, const orc_kp* kps2,
+                         const uint8_t* desc2, const uint8_t* mp2, int n2, int fv2_n, const int* fv2_nodes,
+                         const int* fv2_offsets, const int* fv2_features, float nnratio, int check_ori,
+                         int* match_out);
 /* Frame::UndistortKeyPoints (src/Frame.cc:724-776) and ComputeImageBounds
  * (:778-819) with cv::undistortPoints restated from OpenCV 3.2.  K4 = fx, fy,
  * cx, cy; dist = k1 k2 p1 p2 [k3] (ndist 4 or 5); bounds = mnMinX, mnMaxX,

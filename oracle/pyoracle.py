@@ -308,6 +308,27 @@ class _Base:
                _p(out))
         return int(nm), out[:len(f_kps)].copy()
 
+    def search_by_bow_kf(self, kps1, desc1, mp1, fv1, kps2, desc2, mp2, fv2, nnratio=0.75, check_ori=True):
+        """ORBmatcher::SearchByBoW(KeyFrame*, KeyFrame*, vpMatches12) ->
+        (nmatches, match_out over pKF1's features: pKF2 feature or -1)."""
+        kps1 = np.ascontiguousarray(kps1, KP_DTYPE)
+        kps2 = np.ascontiguousarray(kps2, KP_DTYPE)
+        d1 = np.ascontiguousarray(desc1, np.uint8)
+        d2 = np.ascontiguousarray(desc2, np.uint8)
+        m1 = np.ascontiguousarray(mp1, np.uint8)
+        m2 = np.ascontiguousarray(mp2, np.uint8)
+        a = [np.ascontiguousarray(x, np.int32) for x in fv1]
+        b = [np.ascontiguousarray(x, np.int32) for x in fv2]
+        out = np.zeros(max(len(kps1), 1), np.int32)
+        f = self.fn("search_by_bow_kf")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                      C.c_float, C.c_int, C.c_void_p]
+        nm = f(_p(kps1), _p(d1), _p(m1), len(kps1), len(a[0]), _p(a[0]), _p(a[1]), _p(a[2]), _p(kps2), _p(d2),
+               _p(m2), len(kps2), len(b[0]), _p(b[0]), _p(b[1]), _p(b[2]), C.c_float(nnratio), int(bool(check_ori)),
+               _p(out))
+        return int(nm), out[:len(kps1)].copy()
+
     def undistort_keypoints(self, K4, dist, kps):
         """Frame::UndistortKeyPoints: the keypoints with undistorted x, y."""
         K = np.ascontiguousarray(K4, np.float32)

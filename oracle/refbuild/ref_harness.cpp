@@ -643,6 +643,64 @@ int ref_search_by_bow(const orc_kp* kf_kps, const uint8_t* kf_desc, const uint8_
     return nm;
 }
 
+// A keyframe built from recorded keypoints / descriptors / FeatureVector with
+// real map points where mp[i] is 1 (bad ones where 2); index maps them back.
+static KeyFrame* make_keyframe(MapPointMaker& maker, const orc_kp* kps, const uint8_t* desc, const uint8_t* mp, int n,
+                               int fv_n, const int* fv_nodes, const int* fv_offsets, const int* fv_features,
+                               std::map<MapPoint*, int>& index, Frame*& src) {
+    cv::Mat pos = cv::Mat::zeros(3, 1, CV_32F);
+    src = new Frame();
+    src->N = n;
+    src->mvKeys = kps_in(kps, n);
+    src->mvKeysUn = src->mvKeys;
+    src->mvuRight.assign(n, -1.0f);
+    src->mDescriptors = cv::Mat(n, 32, CV_8U);
+    std::memcpy(src->mDescriptors.data, desc, (size_t)n * 32);
+    KeyFrame* KF = new KeyFrame(*src, maker.map, nullptr);
+    KF->mFeatVec = feature_vector(fv_n, fv_nodes, fv_offsets, fv_features);
+    KF->mvpMapPoints.assign(n, static_cast<MapPoint*>(NULL));
+    for (int i = 0; i < n; i++) {
+        if (mp[i] == 0) continue;
+        MapPoint* p = maker.make(pos, 1);
+        p->mbBad = mp[i] == 2;
+        KF->mvpMapPoints[i] = p;
+        index[p] = i;
+    }
+    return KF;
+}
+
+// ORBmatcher::SearchByBoW(KeyFrame* pKF1, KeyFrame* pKF2, vpMatches12) --
+// src/ORBmatcher.cc:729-880.  match_out[i]: the pKF2 feature whose map point
+// vpMatches12[i] holds, or -1.
+int ref_search_by_bow_kf(const orc_kp* kps1, const uint8_t* desc1, const uint8_t* mp1, int n1, int fv1_n,
+                         const int* fv1_nodes, const int* fv1_offsets, const int* fv1_features, const orc_kp* kps2,
+                         const uint8_t* desc2, const uint8_t* mp2, int n2, int fv2_n, const int* fv2_nodes,
+                         const int* fv2_offsets, const int* fv2_features, float nnratio, int check_ori,
+                         int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        MapPointMaker maker;
+        std::map<MapPoint*, int> index1, index2;
+        Frame *s1, *s2;
+        KeyFrame* KF1 = make_keyframe(maker, kps1, desc1, mp1, n1, fv1_n, fv1_nodes, fv1_offsets, fv1_features,
+                                      index1, s1);
+        KeyFrame* KF2 = make_keyframe(maker, kps2, desc2, mp2, n2, fv2_n, fv2_nodes, fv2_offsets, fv2_features,
+                                      index2, s2);
+        std::vector<MapPoint*> matches;
+        ORBmatcher matcher(nnratio, check_ori != 0);
+        nm = matcher.SearchByBoW(KF1, KF2, matches);
+        for (int i = 0; i < n1; i++) match_out[i] = matches[i] ? index2[matches[i]] : -1;
+        for (auto& e : index1) delete e.first;
+        for (auto& e : index2) delete e.first;
+        delete KF1;
+        delete KF2;
+        delete s1;
+        delete s2;
+    }
+    return nm;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

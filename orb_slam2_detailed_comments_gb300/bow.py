@@ -105,7 +105,7 @@ class Vocabulary:
 
 
 def search_by_bow(keypoints, descriptors, offsets, bow, kf_mappoints, pairs, nnratio: float = 0.75,
-                  check_orientation: bool = True, stream=None):
+                  check_orientation: bool = True, stream=None, keyframes: bool = False):
     """ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
     (src/ORBmatcher.cc:247-380) for many (keyframe, frame) pairs in one launch.
 
@@ -115,11 +115,15 @@ def search_by_bow(keypoints, descriptors, offsets, bow, kf_mappoints, pairs, nnr
     where a keyframe feature has a map point that is not bad; pairs (P, 2)
     host ints (keyframe entry, frame entry).  Returns (nmatches (P,), list of
     P match tensors: per frame feature the keyframe feature whose map point it
-    receives, or -1)."""
+    receives, or -1).  With keyframes=True it is SearchByBoW(KeyFrame* pKF1,
+    KeyFrame* pKF2, vpMatches12) (src/ORBmatcher.cc:729-880): pairs hold
+    (pKF1, pKF2), kf_mappoints is read for both, and the matches are per pKF1
+    feature (the pKF2 feature or -1)."""
     import torch
     pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
     offs = offsets.cpu().numpy() if offsets.is_cuda else np.asarray(offsets)
-    sizes = offs[pr[:, 1] + 1] - offs[pr[:, 1]]
+    side = 0 if keyframes else 1
+    sizes = offs[pr[:, side] + 1] - offs[pr[:, side]]
     out_off = np.zeros(len(pr) + 1, np.int32)
     out_off[1:] = np.cumsum(sizes)
     dev = torch.device("cuda")
@@ -128,7 +132,8 @@ def search_by_bow(keypoints, descriptors, offsets, bow, kf_mappoints, pairs, nnr
     match = torch.empty(max(int(out_off[-1]), 1), dtype=torch.int32, device=dev)
     nm = torch.empty(max(len(pr), 1), dtype=torch.int32, device=dev)
     st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
-    check(lib().orbgpu_search_by_bow(ptr(keypoints), ptr(descriptors), ptr(offsets), ptr(bow["fv_counts"]),
+    fn = lib().orbgpu_search_by_bow_keyframes if keyframes else lib().orbgpu_search_by_bow
+    check(fn(ptr(keypoints), ptr(descriptors), ptr(offsets), ptr(bow["fv_counts"]),
                                      ptr(bow["fv_nodes"]), ptr(bow["fv_starts"]), ptr(bow["fv_sizes"]),
                                      ptr(bow["fv_features"]), ptr(kf_mappoints), ptr(P), len(pr), C.c_float(nnratio),
                                      int(bool(check_orientation)), ptr(OO), ptr(match), ptr(nm), C.c_void_p(st)),

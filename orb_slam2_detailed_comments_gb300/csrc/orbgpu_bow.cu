@@ -220,7 +220,10 @@ __global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
 // among the node's frame features not matched yet (a shared bitmap), the
 // first at the least distance, with the second-best over the rest; kept when
 // best <= TH_LOW and best < nnratio * second.  Then the rotation histogram,
-// ComputeThreeMaxima (src/ORBmatcher.cc:2035-2077) and the resets.
+// ComputeThreeMaxima (src/ORBmatcher.cc:2035-2077) and the resets.  With
+// 'keyframes' it is SearchByBoW(KeyFrame* pKF1, KeyFrame* pKF2, vpMatches12)
+// (src/ORBmatcher.cc:729-880): candidates need a map point that is not bad,
+// TH_LOW is exclusive, and the result is per pKF1 feature.
 #define SBB_THREADS 1024
 #define SBB_TH_LOW 50
 
@@ -228,7 +231,7 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
     const orbgpu_keypoint* __restrict__ kps, const uint4* __restrict__ desc, const int* __restrict__ offsets,
     const int* __restrict__ fv_counts, const int* __restrict__ fv_nodes, const int* __restrict__ fv_starts,
     const int* __restrict__ fv_sizes, const int* __restrict__ fv_features, const uint8_t* __restrict__ kf_mp,
-    const int* __restrict__ pairs, float nnratio, int check_ori, const int* __restrict__ out_offsets,
+    const int* __restrict__ pairs, float nnratio, int check_ori, int keyframes, const int* __restrict__ out_offsets,
     int* __restrict__ match_out, int* __restrict__ nmatches) {
     __shared__ unsigned s_taken[BOW_MAX_FEATURES / 32];
     __shared__ unsigned char s_bin[BOW_MAX_FEATURES];
@@ -237,10 +240,13 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
     const int p = blockIdx.x;
     const int kf = pairs[2 * p], fr = pairs[2 * p + 1];
     const int ok0 = offsets[kf], of0 = offsets[fr];
-    const int fn = offsets[fr + 1] - of0;
+    const int kn = offsets[kf + 1] - ok0, frn = offsets[fr + 1] - of0;
+    // the output (and bins) are per frame feature, or per first-keyframe
+    // feature for two keyframes (vpMatches12)
+    const int fn = keyframes ? kn : frn;
     const int ckf = fv_counts[kf], cf = fv_counts[fr];
     int* out = match_out + out_offsets[p];
-    if (fn < 0 || fn > BOW_MAX_FEATURES || ckf < 0 || cf < 0) {
+    if (kn < 0 || kn > BOW_MAX_FEATURES || frn < 0 || frn > BOW_MAX_FEATURES || ckf < 0 || cf < 0) {
         if (threadIdx.x == 0) nmatches[p] = -1;
         return;
     }
@@ -281,7 +287,7 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
                 int d = 256;
                 if (c + lane < fcount) {
                     const int jf = flist[c + lane];
-                    if (!((s_taken[jf >> 5] >> (jf & 31)) & 1u)) {
+                    if (!((s_taken[jf >> 5] >> (jf & 31)) & 1u) && (!keyframes || kf_mp[of0 + jf] == 1)) {
                         d = hamming256(a0, a1, desc[2 * (size_t)(of0 + jf)], desc[2 * (size_t)(of0 + jf) + 1]);
                         key = ((unsigned)d << 13) | (unsigned)(c + lane);
                     }
@@ -296,17 +302,20 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
                 }
             }
             const int best1 = b1 == INF ? 256 : (int)(b1 >> 13);
-            if (best1 <= SBB_TH_LOW && (float)best1 < __fmul_rn(nnratio, (float)b2)) {
+            // TH_LOW inclusive for (keyframe, frame), exclusive for two keyframes
+            if ((keyframes ? best1 < SBB_TH_LOW : best1 <= SBB_TH_LOW) &&
+                (float)best1 < __fmul_rn(nnratio, (float)b2)) {
                 if (lane == 0) {
                     const int jf = flist[b1 & 8191u];
                     atomicOr(&s_taken[jf >> 5], 1u << (jf & 31));
-                    out[jf] = ikf;
+                    const int slot = keyframes ? ikf : jf;
+                    out[slot] = keyframes ? jf : ikf;
                     if (check_ori) {
                         float rot = __fsub_rn(kps[ok0 + ikf].angle, kps[of0 + jf].angle);
                         if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
                         int bin = (int)roundf(__fmul_rn(rot, factor));
                         if (bin == ORBGPU_HISTO_LENGTH) bin = 0;
-                        s_bin[jf] = (unsigned char)bin;
+                        s_bin[slot] = (unsigned char)bin;
                         atomicAdd(&hist[bin], 1);
                     }
                 }
@@ -366,11 +375,10 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
 
 using namespace orbgpu;
 
-extern "C" int orbgpu_search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
-                                    const int* fv_counts, const int* fv_nodes, const int* fv_starts,
-                                    const int* fv_sizes, const int* fv_features, const uint8_t* kf_mappoints,
-                                    const int* pairs, int npairs, float nnratio, int check_ori,
-                                    const int* out_offsets, int* match_out, int* nmatches, void* stream) {
+static int search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets, const int* fv_counts,
+                         const int* fv_nodes, const int* fv_starts, const int* fv_sizes, const int* fv_features,
+                         const uint8_t* kf_mappoints, const int* pairs, int npairs, float nnratio, int check_ori,
+                         int keyframes, const int* out_offsets, int* match_out, int* nmatches, void* stream) {
     if (npairs < 0 || (npairs > 0 && (!kps || !desc || !offsets || !fv_counts || !fv_nodes || !fv_starts ||
                                       !fv_sizes || !fv_features || !kf_mappoints || !pairs || !out_offsets ||
                                       !match_out || !nmatches)) ||
@@ -381,9 +389,28 @@ extern "C" int orbgpu_search_by_bow(const orbgpu_keypoint* kps, const uint8_t* d
     if (npairs == 0) return ORBGPU_OK;
     k_search_by_bow<<<npairs, SBB_THREADS, 0, (cudaStream_t)stream>>>(
         kps, reinterpret_cast<const uint4*>(desc), offsets, fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features,
-        kf_mappoints, pairs, nnratio, check_ori, out_offsets, match_out, nmatches);
+        kf_mappoints, pairs, nnratio, check_ori, keyframes, out_offsets, match_out, nmatches);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
+                                    const int* fv_counts, const int* fv_nodes, const int* fv_starts,
+                                    const int* fv_sizes, const int* fv_features, const uint8_t* kf_mappoints,
+                                    const int* pairs, int npairs, float nnratio, int check_ori,
+                                    const int* out_offsets, int* match_out, int* nmatches, void* stream) {
+    return search_by_bow(kps, desc, offsets, fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features, kf_mappoints,
+                         pairs, npairs, nnratio, check_ori, 0, out_offsets, match_out, nmatches, stream);
+}
+
+extern "C" int orbgpu_search_by_bow_keyframes(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
+                                              const int* fv_counts, const int* fv_nodes, const int* fv_starts,
+                                              const int* fv_sizes, const int* fv_features,
+                                              const uint8_t* kf_mappoints, const int* pairs, int npairs,
+                                              float nnratio, int check_ori, const int* out_offsets, int* match_out,
+                                              int* nmatches, void* stream) {
+    return search_by_bow(kps, desc, offsets, fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features, kf_mappoints,
+                         pairs, npairs, nnratio, check_ori, 1, out_offsets, match_out, nmatches, stream);
 }
 
 extern "C" int orbgpu_vocabulary_create(int k, int L, int scoring, int weighting, int nnodes, const int* parents,

@@ -344,6 +344,14 @@ def search_by_bow_fixture(R):
                                             ratio, bool(ori))
                 arrays[pre + f"nm_{ori}"] = np.array(nm)
                 arrays[pre + f"match_{ori}"] = match
+            # SearchByBoW(KeyFrame*, KeyFrame*): the second view as a keyframe
+            mp2 = np.random.default_rng(10 + sc).choice([0, 1, 1, 1, 2], len(b.keypoints)).astype(np.uint8)
+            arrays[pre + "f_mp"] = mp2
+            nm, match = R.search_by_bow_kf(a.keypoints, a.descriptors, mp,
+                                           (fa["fv_nodes"], fa["fv_offsets"], fa["fv_features"]), b.keypoints,
+                                           b.descriptors, mp2, (fb["fv_nodes"], fb["fv_offsets"], fb["fv_features"]))
+            arrays[pre + "kf_nm"] = np.array(nm)
+            arrays[pre + "kf_match"] = match
     save("search_by_bow.npz", **arrays)
 
 

@@ -181,3 +181,40 @@ def test_search_by_bow_vs_oracle(torch, oracle, check_ori, ratio):
         assert int(nm[p]) == ref_nm, p
         assert np.array_equal(matches[p].cpu().numpy(), ref), p
         assert ref_nm > 100
+
+
+@pytest.mark.parametrize("check_ori,ratio", [(True, 0.75), (False, 0.9)])
+def test_search_by_bow_keyframes_vs_oracle(torch, oracle, check_ori, ratio):
+    """SearchByBoW(KeyFrame*, KeyFrame*) for 8 keyframe pairs in one launch."""
+    from orb_slam2_detailed_comments_gb300 import Vocabulary, search_by_bow
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    voc = syn.vocabulary(10, 4, 5)
+    oracle.vocabulary_from_arrays("sbbk", voc)
+    V = Vocabulary.from_arrays(10, 4, 0, 0, voc["parents"], voc["is_leaf"], voc["descriptors"], voc["weights"])
+    ents = []
+    for seed in range(4):
+        f1, f2, _ = syn.frame_pair(640, 480, 50 + seed)
+        ents += [oracle.extract(f1, nfeatures=1500), oracle.extract(f2, nfeatures=1500)]
+    offs = np.zeros(len(ents) + 1, np.int32)
+    offs[1:] = np.cumsum([len(e.keypoints) for e in ents])
+    kps = np.concatenate([e.keypoints for e in ents])
+    desc = np.concatenate([e.descriptors for e in ents])
+    mp = np.random.default_rng(4).choice([0, 1, 1, 1, 2], len(kps)).astype(np.uint8)
+    K = torch.from_numpy(kps.view(np.float32).reshape(-1, 7).copy()).cuda()
+    D = torch.from_numpy(desc).cuda()
+    O = torch.from_numpy(offs).cuda()
+    bow = V.transform(D, O, 2)
+    pairs = [(2 * s, 2 * s + 1) for s in range(4)] + [(2 * s + 1, 2 * s) for s in range(4)]
+    nm, matches = search_by_bow(K, D, O, bow, torch.from_numpy(mp).cuda(), pairs, ratio, check_ori, keyframes=True)
+    torch.cuda.synchronize()
+    for p, (a, b) in enumerate(pairs):
+        ea, eb = ents[a], ents[b]
+        fa = oracle.bow_transform("sbbk", ea.descriptors, 2)
+        fb = oracle.bow_transform("sbbk", eb.descriptors, 2)
+        ref_nm, ref = oracle.search_by_bow_kf(ea.keypoints, ea.descriptors, mp[offs[a]:offs[a + 1]],
+                                              (fa["fv_nodes"], fa["fv_offsets"], fa["fv_features"]), eb.keypoints,
+                                              eb.descriptors, mp[offs[b]:offs[b + 1]],
+                                              (fb["fv_nodes"], fb["fv_offsets"], fb["fv_features"]), ratio, check_ori)
+        assert int(nm[p]) == ref_nm, p
+        assert np.array_equal(matches[p].cpu().numpy(), ref), p
+        assert ref_nm > 50

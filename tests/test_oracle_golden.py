@@ -278,3 +278,16 @@ def test_search_by_bow_golden(oracle, golden, sc):
                                          g[pre + "f_kps"], g[pre + "f_desc"], fv["f"], ratio, bool(ori))
         assert nm == int(g[pre + f"nm_{ori}"])
         assert np.array_equal(match, g[pre + f"match_{ori}"])
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_search_by_bow_keyframes_golden(oracle, golden, sc):
+    """ORBmatcher::SearchByBoW(KeyFrame*, KeyFrame*) against the reference's outputs."""
+    g = golden("search_by_bow.npz")
+    pre = f"s{sc}_"
+    fv = {side: tuple(g[pre + side + "_" + k] for k in ("fv_nodes", "fv_offsets", "fv_features"))
+          for side in ("kf", "f")}
+    nm, match = oracle.search_by_bow_kf(g[pre + "kf_kps"], g[pre + "kf_desc"], g[pre + "kf_mp"], fv["kf"],
+                                        g[pre + "f_kps"], g[pre + "f_desc"], g[pre + "f_mp"], fv["f"])
+    assert nm == int(g[pre + "kf_nm"])
+    assert np.array_equal(match, g[pre + "kf_match"])
