@@ -317,6 +317,27 @@ int orbgpu_is_in_frustum(const orbgpu_frustum_frame* frames, int nframes, const 
                          const orbgpu_mappoint_geometry* mps, float viewing_cos_limit, orbgpu_mappoint* mappoints,
                          int* in_view, void* stream);
 
+/* ORBmatcher::SearchByProjection(Frame& CurrentFrame, KeyFrame* pKF, const
+ * set<MapPoint*>& sAlreadyFound, th, ORBdist) -- src/ORBmatcher.cc:1891-2010
+ * (relocalisation) -- with the matcher's checkOri.  current: the frame
+ * searched; pose: its mTcw / camera / PredictScale thresholds as
+ * orbgpu_frustum_frame_init fills them (the image bounds are the frame's
+ * 0..width x 0..height); per keyframe feature i (n_kf of them):
+ * kf_keypoints[i] (its angle is read), mappoints[i] / mp_descriptors[i] (the
+ * map point's position, distances and GetDescriptor()), usable[i] = 1 where
+ * GetMapPointMatches()[i] is a map point that is not bad and not in
+ * sAlreadyFound.  claimed: current->n bytes, non-zero where
+ * CurrentFrame.mvpMapPoints[i] is already set (NULL = none).  match_out:
+ * current->n ints: >= 0 the keyframe feature whose map point now fills
+ * CurrentFrame.mvpMapPoints[i]; -1 not assigned; -2 claimed before; -4
+ * assigned and reset by the rotation check.  Host or device memory per
+ * 'mem'; returns after the result is complete. */
+int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orbgpu_frame* current,
+                                         const orbgpu_frustum_frame* pose, const orbgpu_keypoint* kf_keypoints,
+                                         const orbgpu_mappoint_geometry* mappoints, const uint8_t* mp_descriptors,
+                                         const uint8_t* usable, int n_kf, float th, int orbdist,
+                                         const uint8_t* claimed, int* match_out, int mem, int* nmatches);
+
 /* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
  * indexed like LastFrame's keypoints. */
 typedef struct {

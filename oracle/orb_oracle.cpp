@@ -715,6 +715,94 @@ int orc_search_by_projection_frame(const orc_params* p, const orc_kp* kps, const
     return nmatches;
 }
 
+// ORBmatcher::SearchByProjection(Frame& CurrentFrame, KeyFrame* pKF,
+// sAlreadyFound, th, ORBdist), src/ORBmatcher.cc:1891-2010.  T: rows 0-2 of
+// CurrentFrame.mTcw; cam = fx, fy, cx, cy.  mp_state: 0 no map point, 1
+// usable, 2 bad, 3 in sAlreadyFound.  match_out as the frame-to-frame search
+// (-4 assigned then reset by the rotation check).
+int orc_search_by_projection_kf(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                                const float* T, const float* cam, const orc_kp* kf_kps, int m,
+                                const orc_mp_geometry* mps, const uint8_t* mp_desc, const uint8_t* mp_state, float th,
+                                int orbdist, int check_ori, const uint8_t* claimed, int* match_out) {
+    const Tables t = make_tables(p);
+    Grid* g = new Grid();
+    build_grid(*g, kps, n, w, h);
+    std::vector<int> owner(n);
+    for (int i = 0; i < n; i++) owner[i] = (claimed && claimed[i]) ? -2 : -1;
+    std::vector<int> rotHist[kHistoLength];
+    const float factor = kHistoLength / 360.0f;
+    // Ow = -Rcw' tcw
+    const float tcw[3] = {T[3], T[7], T[11]};
+    float Ow[3];
+    for (int r = 0; r < 3; r++) {
+        const float col[3] = {-T[r], -T[4 + r], -T[8 + r]};
+        Ow[r] = mat_row_dot(col, 1, tcw);
+    }
+    const float log_scale = std::log(p->scale_factor);
+    int nmatches = 0;
+    for (int i = 0; i < m; i++) {
+        if (mp_state[i] != 1) continue;
+        const orc_mp_geometry& mp = mps[i];
+        const float X[3] = {mp.x, mp.y, mp.z};
+        float c[3];
+        for (int r = 0; r < 3; r++) c[r] = mat_row_dot(T + 4 * r, 1, X) + T[4 * r + 3];
+        const float invzc = 1.0 / c[2];
+        const float u = cam[0] * c[0] * invzc + cam[2];
+        const float v = cam[1] * c[1] * invzc + cam[3];
+        // a non-finite projection finds no cell in the reference
+        if (!std::isfinite(u) || !std::isfinite(v)) continue;
+        if (u < g->minX || u > g->maxX) continue;
+        if (v < g->minY || v > g->maxY) continue;
+        const float PO[3] = {X[0] - Ow[0], X[1] - Ow[1], X[2] - Ow[2]};
+        double ss = 0;
+        for (int k = 0; k < 3; k++) ss += (double)PO[k] * (double)PO[k];
+        const float dist3D = (float)std::sqrt(ss);
+        if (dist3D < 0.8f * mp.min_distance || dist3D > 1.2f * mp.max_distance) continue;
+        const float ratio = mp.max_distance / dist3D;
+        int level = (int)std::ceil(std::log(ratio) / log_scale);
+        if (level < 0) level = 0;
+        else if (level >= p->nlevels) level = p->nlevels - 1;
+        const float radius = th * t.scale[level];
+        const std::vector<int> idx2 = features_in_area(*g, kps, u, v, radius, level - 1, level + 1);
+        if (idx2.empty()) continue;
+        int bestDist = 256, bestIdx2 = -1;
+        for (int i2 : idx2) {
+            if (owner[i2] != -1) continue;  // CurrentFrame.mvpMapPoints[i2] set
+            const int dist = hamming(mp_desc + (size_t)i * 32, desc + (size_t)i2 * 32);
+            if (dist < bestDist) {
+                bestDist = dist;
+                bestIdx2 = i2;
+            }
+        }
+        if (bestDist <= orbdist) {
+            owner[bestIdx2] = i;
+            nmatches++;
+            if (check_ori) {
+                float rot = kf_kps[i].angle - kps[bestIdx2].angle;
+                if (rot < 0.0) rot += 360.0f;
+                int bin = (int)std::round(rot * factor);
+                if (bin == kHistoLength) bin = 0;
+                rotHist[bin].push_back(bestIdx2);
+            }
+        }
+    }
+    std::vector<char> nulled(n, 0);
+    if (check_ori) {
+        int ind1 = -1, ind2 = -1, ind3 = -1;
+        three_maxima(rotHist, kHistoLength, ind1, ind2, ind3);
+        for (int b = 0; b < kHistoLength; b++) {
+            if (b == ind1 || b == ind2 || b == ind3) continue;
+            for (int i2 : rotHist[b]) {
+                nulled[i2] = 1;
+                nmatches--;
+            }
+        }
+    }
+    for (int i = 0; i < n; i++) match_out[i] = nulled[i] ? -4 : owner[i];
+    delete g;
+    return nmatches;
+}
+
 // Frame::ComputeStereoMatches, src/Frame.cc:831-1082 (mb = mbf/fx).
 int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
                                const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,

@@ -62,6 +62,13 @@ int orc_vocabulary_from_arrays(const char* name, int k, int L, int scoring, int 
 int orc_bow_transform(const char* path, const uint8_t* desc, int n, int levelsup, int* word_ids, double* weights,
                       int* node_ids, int* bow_n, int* bow_words, double* bow_values, int* fv_n, int* fv_nodes,
                       int* fv_offsets, int* fv_features);
+/* ORBmatcher::SearchByProjection(Frame&, KeyFrame*, sAlreadyFound, th,
+ * ORBdist) (src/ORBmatcher.cc:1891-2010).  T: rows 0-2 of mTcw; cam: fx, fy,
+ * cx, cy; mp_state: 0 none, 1 usable, 2 bad, 3 already found. */
+int orc_search_by_projection_kf(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                                const float* T, const float* cam, const orc_kp* kf_kps, int m,
+                                const orc_mp_geometry* mps, const uint8_t* mp_desc, const uint8_t* mp_state, float th,
+                                int orbdist, int check_ori, const uint8_t* claimed, int* match_out);
 /* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
  * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
  * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:

@@ -287,6 +287,30 @@ class _Base:
                 "bow_words": bw[:b].copy(), "bow_values": bv[:b].copy(), "fv_nodes": fn[:q].copy(),
                 "fv_offsets": fo[:q + 1].copy(), "fv_features": ff[:fo[q]].copy()}
 
+    def search_by_projection_kf(self, kps, desc, w, h, Tcw, cam, kf_kps, mps, mp_desc, mp_state, th=10.0,
+                                orbdist=100, check_ori=True, claimed=None, nlevels=8, scale_factor=1.2):
+        """SearchByProjection(Frame&, KeyFrame*, sAlreadyFound, th, ORBdist)
+        -> (nmatches, match_out).  mps: GEOM_DTYPE; mp_state 0 none, 1 usable,
+        2 bad, 3 already found; cam: fx, fy, cx, cy."""
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        desc = np.ascontiguousarray(desc, np.uint8)
+        kf_kps = np.ascontiguousarray(kf_kps, KP_DTYPE)
+        mps = np.ascontiguousarray(mps, GEOM_DTYPE)
+        mpd = np.ascontiguousarray(mp_desc, np.uint8)
+        st = np.ascontiguousarray(mp_state, np.uint8)
+        T = np.ascontiguousarray(np.asarray(Tcw, np.float32).reshape(-1)[:12])
+        cm = np.ascontiguousarray(cam, np.float32)
+        cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
+        out = np.zeros(max(len(kps), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("search_by_projection_kf")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                      C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_int,
+                      C.c_void_p, C.c_void_p]
+        nm = f(C.byref(p), _p(kps), _p(desc), len(kps), w, h, _p(T), _p(cm), _p(kf_kps), len(kf_kps), _p(mps),
+               _p(mpd), _p(st), C.c_float(th), int(orbdist), int(bool(check_ori)), _p(cl), _p(out))
+        return int(nm), out[:len(kps)].copy()
+
     def search_by_bow(self, kf_kps, kf_desc, kf_mp, kf_fv, f_kps, f_desc, f_fv, nnratio=0.75, check_ori=True):
         """ORBmatcher::SearchByBoW(KeyFrame*, Frame&, matches).  *_fv: (nodes,
         offsets, features) of the FeatureVector (bow_transform's fv_*);

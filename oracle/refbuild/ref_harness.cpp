@@ -701,6 +701,77 @@ int ref_search_by_bow_kf(const orc_kp* kps1, const uint8_t* desc1, const uint8_t
     return nm;
 }
 
+// ORBmatcher::SearchByProjection(Frame&, KeyFrame*, sAlreadyFound, th,
+// ORBdist) -- src/ORBmatcher.cc:1891-2010.  The keyframe holds real map
+// points (bad ones for mp_state 2, those of state 3 also in sAlreadyFound).
+// match_out: >= 0 the keyframe feature whose map point fills the keypoint,
+// -2 claimed before, -1 otherwise (a reset by the rotation check leaves NULL,
+// like an untouched keypoint).
+int ref_search_by_projection_kf(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                                const float* T, const float* cam, const orc_kp* kf_kps, int m,
+                                const orc_mp_geometry* mps, const uint8_t* mp_desc, const uint8_t* mp_state, float th,
+                                int orbdist, int check_ori, const uint8_t* claimed, int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame* F = make_frame(&ext, kps, desc, n, w, h, nullptr);
+        Frame::fx = cam[0];
+        Frame::fy = cam[1];
+        Frame::cx = cam[2];
+        Frame::cy = cam[3];
+        Frame::invfx = 1.0f / cam[0];
+        Frame::invfy = 1.0f / cam[1];
+        F->mfLogScaleFactor = std::log(F->mfScaleFactor);
+        cv::Mat Tcw = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) Tcw.at<float>(r, c) = T[4 * r + c];
+        F->SetPose(Tcw);
+        MapPointMaker maker;
+        cv::Mat zero = cv::Mat::zeros(3, 1, CV_32F);
+        MapPoint* preclaimed = maker.make(zero, 1);
+        for (int i = 0; i < n; i++)
+            if (claimed && claimed[i]) F->mvpMapPoints[i] = preclaimed;
+        Frame* src = new Frame();
+        src->N = m;
+        src->mvKeys = kps_in(kf_kps, m);
+        src->mvKeysUn = src->mvKeys;
+        src->mvuRight.assign(m, -1.0f);
+        src->mDescriptors = cv::Mat(m, 32, CV_8U);
+        KeyFrame* KF = new KeyFrame(*src, maker.map, nullptr);
+        KF->mvpMapPoints.assign(m, static_cast<MapPoint*>(NULL));
+        std::set<MapPoint*> found;
+        std::map<MapPoint*, int> index;
+        for (int i = 0; i < m; i++) {
+            if (mp_state[i] == 0) continue;
+            cv::Mat pos(3, 1, CV_32F);
+            pos.at<float>(0) = mps[i].x;
+            pos.at<float>(1) = mps[i].y;
+            pos.at<float>(2) = mps[i].z;
+            MapPoint* mp = maker.make(pos, 1);
+            mp->mfMinDistance = mps[i].min_distance;
+            mp->mfMaxDistance = mps[i].max_distance;
+            mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+            std::memcpy(mp->mDescriptor.data, mp_desc + (size_t)i * 32, 32);
+            mp->mbBad = mp_state[i] == 2;
+            if (mp_state[i] == 3) found.insert(mp);
+            KF->mvpMapPoints[i] = mp;
+            index[mp] = i;
+        }
+        ORBmatcher matcher(0.9f, check_ori != 0);
+        nm = matcher.SearchByProjection(*F, KF, found, th, orbdist);
+        for (int i = 0; i < n; i++) {
+            MapPoint* mp = F->mvpMapPoints[i];
+            match_out[i] = mp == nullptr ? -1 : mp == preclaimed ? -2 : index[mp];
+        }
+        for (auto& e : index) delete e.first;
+        delete KF;
+        delete src;
+        delete F;
+    }
+    return nm;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

@@ -535,11 +535,88 @@ __global__ void k_pf_candidates(GridDev g, FrameMotionDev mo, const orbgpu_keypo
     if (!fill && lane == 0) cand_count[i] = total;
 }
 
+// ----------------------------------------------------------------- SearchByProjection(Frame, KeyFrame)
+// src/ORBmatcher.cc:1891-2010 (relocalisation): the keyframe's map points
+// that are usable (not NULL, not bad, not in sAlreadyFound) in keyframe order.
+// Per map point (one warp): Rcw * X + tcw as in the frame-to-frame search
+// (no depth test here), the projection, the distance invariance, the level
+// MapPoint::PredictScale gives (thresholds of orbgpu_frustum_frame_init), the
+// window of levels level - 1 .. level + 1 with radius th * scale[level], and
+// the candidates at distance <= ORBdist (no ratio test: the first minimum is
+// the answer, and a minimum above ORBdist is rejected either way).
+struct KeyframeProjDev {
+    float T[12];
+    float Ow[3];
+    float fx, fy, cx, cy;
+    float maxX, maxY;
+    int nlevels;
+    float level_above[15];
+    int orbdist;
+};
+
+__global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_mappoint_geometry* mps,
+                                 const uint8_t* usable, const uint8_t* mp_desc, int m, float th,
+                                 const int* cand_start, int* cand_count, uint64_t* cand_out, int fill) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= m) return;
+    int total = 0;
+    bool live = usable[i] == 1;
+    float u = 0.f, v = 0.f;
+    int level = 0;
+    if (live) {
+        const orbgpu_mappoint_geometry mp = mps[i];
+        const float xc = pose_row(kp.T, mp.x, mp.y, mp.z);
+        const float yc = pose_row(kp.T + 4, mp.x, mp.y, mp.z);
+        const float zc = pose_row(kp.T + 8, mp.x, mp.y, mp.z);
+        const float invzc = __double2float_rn(__ddiv_rn(1.0, (double)zc));
+        u = __fadd_rn(__fmul_rn(__fmul_rn(kp.fx, xc), invzc), kp.cx);
+        v = __fadd_rn(__fmul_rn(__fmul_rn(kp.fy, yc), invzc), kp.cy);
+        // a non-finite projection finds no grid cell in the reference
+        live = isfinite(u) && isfinite(v) && !(u < g.minX || u > kp.maxX) && !(v < g.minY || v > kp.maxY);
+        if (live) {
+            const float po0 = __fsub_rn(mp.x, kp.Ow[0]), po1 = __fsub_rn(mp.y, kp.Ow[1]),
+                        po2 = __fsub_rn(mp.z, kp.Ow[2]);
+            double ss = __dmul_rn((double)po0, (double)po0);
+            ss = __dadd_rn(ss, __dmul_rn((double)po1, (double)po1));
+            ss = __dadd_rn(ss, __dmul_rn((double)po2, (double)po2));
+            const float dist = (float)__dsqrt_rn(ss);
+            live = !(dist < __fmul_rn(0.8f, mp.min_distance) || dist > __fmul_rn(1.2f, mp.max_distance));
+            const float ratio = __fdiv_rn(mp.max_distance, dist);
+            for (int n = 0; n < kp.nlevels - 1; n++) level += ratio > kp.level_above[n] ? 1 : 0;
+        }
+    }
+    if (live) {
+        const float radius = __fmul_rn(th, g.scale[level]);
+        int x0, x1, y0, y1;
+        if (area_cells(g, u, v, radius, x0, x1, y0, y1)) {
+            const uint8_t* dmp = mp_desc + (size_t)i * 32;
+            warp_window_keys(g.cell_start, g.cell_keys, g.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1,
+                             [&](int idx, int c, bool valid) {
+                bool ok = valid && in_area(g, idx, u, v, radius, level - 1, level + 1);
+                int dist = 256;
+                if (ok) {
+                    dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
+                    ok = dist <= kp.orbdist;
+                }
+                const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                if (fill && ok) {
+                    const int pos = cand_start[i] + total + __popc(msk & ((1u << lane) - 1));
+                    cand_out[pos] = cand_key(dist, c, idx);
+                }
+                total += __popc(msk);
+            });
+        }
+    }
+    if (!fill && lane == 0) cand_count[i] = total;
+}
+
 // Fixed-point round r of the in-order assignment: map point i takes its
 // first minimum among candidates not held by an observed map point j < i of
 // round r-1's results (an owner without observations blocks nothing,
-// src/ORBmatcher.cc:1800-1802).  A round that changes nothing equals the
-// sequential result.
+// src/ORBmatcher.cc:1800-1802; with mps NULL every owner blocks, as in
+// SearchByProjection(Frame&, KeyFrame*, ...)).  A round that changes nothing
+// equals the sequential result.
 __global__ void k_pf_round(int n, int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
                            const orbgpu_frame_mappoint* mps, int round, int* claims3, int* res, int* changed,
                            const int* pre) {
@@ -567,7 +644,7 @@ __global__ void k_pf_round(int n, int m, const int* cand_start, const int* cand_
     if (lane == 0) {
         if (res[local] != r) changed[round] = 1;
         res[local] = r;
-        if (r >= 0 && (mps[local].flags & ORBGPU_MP_OBSERVED)) atomicMin(&claims_w[r], local);
+        if (r >= 0 && (!mps || (mps[local].flags & ORBGPU_MP_OBSERVED))) atomicMin(&claims_w[r], local);
     }
 }
 
@@ -593,7 +670,7 @@ __global__ void k_pf_serial(int n, int m, const int* cand_start, const int* cand
         const int r = best == ~0ull ? -1 : (int)(best & 0xFFFFF);
         if (lane == 0) {
             res[i] = r;
-            if (r >= 0 && (mps[i].flags & ORBGPU_MP_OBSERVED)) blocked[r] = 1;
+            if (r >= 0 && (!mps || (mps[i].flags & ORBGPU_MP_OBSERVED))) blocked[r] = 1;
         }
         __syncwarp();
     }
@@ -1302,6 +1379,124 @@ extern "C" int orbgpu_search_by_projection_frame(orbgpu_matcher* m, const orbgpu
                                                                               claims3, res, changed, d_match);
             k_pf_serial<<<1, 32, 0, m->stream>>>(n, M, start, count, keys, d_mps, changed, res, claims3, d_match);
             k_pf_finish<<<1, 1024, 0, m->stream>>>(n, M, res, d_lk, s.kps, m->check_ori, owner, bin_of, nulled, d_match,
+                                                   d_nm);
+        }
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        if (mem != ORBGPU_MEM_DEVICE && n > 0)
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(match_out, d_match, sizeof(int) * n, cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, d_nm, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+        *nmatches = m->h_pinned[0];
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
+}
+
+extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orbgpu_frame* current,
+                                                    const orbgpu_frustum_frame* pose,
+                                                    const orbgpu_keypoint* kf_keypoints,
+                                                    const orbgpu_mappoint_geometry* mappoints,
+                                                    const uint8_t* mp_descriptors, const uint8_t* usable, int n_kf,
+                                                    float th, int orbdist, const uint8_t* claimed, int* match_out,
+                                                    int mem, int* nmatches) {
+    if (!m || !frame_ok(current) || !pose || n_kf < 0 || n_kf >= (1 << 20) || !match_out || !nmatches ||
+        (n_kf > 0 && (!kf_keypoints || !mappoints || !mp_descriptors || !usable)) || pose->nlevels < 1 ||
+        pose->nlevels > 16)
+        return ORBGPU_ERR_BAD_ARG;
+    const int n = current->n, M = n_kf;
+    *nmatches = 0;
+    KeyframeProjDev kp;
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++) kp.T[4 * r + c] = pose->Rcw[3 * r + c];
+        kp.T[4 * r + 3] = pose->tcw[r];
+        kp.Ow[r] = pose->Ow[r];
+    }
+    kp.fx = pose->fx;
+    kp.fy = pose->fy;
+    kp.cx = pose->cx;
+    kp.cy = pose->cy;
+    kp.maxX = (float)current->width;
+    kp.maxY = (float)current->height;
+    kp.nlevels = pose->nlevels;
+    std::memcpy(kp.level_above, pose->level_above, sizeof(kp.level_above));
+    kp.orbdist = orbdist;
+    size_t est = frame_stage_bytes(current) + grid_bytes(n) +
+                 (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint_geometry) + sizeof(orbgpu_keypoint) + 32 + 1 + 32) +
+                 (size_t)std::max(1, n) * 32 + 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 32;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        int rc = ensure_scratch(m, est);
+        if (rc) return rc;
+        Bump b{(uint8_t*)m->scratch, 0, m->scratch_bytes};
+        Staged s;
+        if ((rc = stage_frame(m, current, b, s))) return rc;
+        GridDev g;
+        if ((rc = build_grid(m, current, s, b, g))) return rc;
+        const orbgpu_keypoint* d_kk = kf_keypoints;
+        const orbgpu_mappoint_geometry* d_mps = mappoints;
+        const uint8_t* d_mpd = mp_descriptors;
+        const uint8_t* d_use = usable;
+        const uint8_t* d_claimed = claimed;
+        int* d_match = match_out;
+        if (mem != ORBGPU_MEM_DEVICE) {
+            orbgpu_keypoint* k = b.take<orbgpu_keypoint>(std::max(1, M));
+            orbgpu_mappoint_geometry* a = b.take<orbgpu_mappoint_geometry>(std::max(1, M));
+            uint8_t* dd = b.take<uint8_t>((size_t)std::max(1, M) * 32);
+            uint8_t* uu = b.take<uint8_t>(std::max(1, M));
+            if (M) {
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(k, kf_keypoints, sizeof(orbgpu_keypoint) * M, cudaMemcpyHostToDevice,
+                                                m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(a, mappoints, sizeof(orbgpu_mappoint_geometry) * M,
+                                                cudaMemcpyHostToDevice, m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(dd, mp_descriptors, 32 * (size_t)M, cudaMemcpyHostToDevice,
+                                                m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(uu, usable, M, cudaMemcpyHostToDevice, m->stream));
+            }
+            d_kk = k;
+            d_mps = a;
+            d_mpd = dd;
+            d_use = uu;
+            if (claimed) {
+                uint8_t* c = b.take<uint8_t>(std::max(1, n));
+                if (n) ORBGPU_CUDA_TRY(cudaMemcpyAsync(c, claimed, n, cudaMemcpyHostToDevice, m->stream));
+                d_claimed = c;
+            }
+            d_match = b.take<int>(std::max(1, n));
+        }
+        if (n > 0) k_init_match_out<<<(n + 255) / 256, 256, 0, m->stream>>>(d_claimed, n, d_match);
+        int *start, *count, total = 0;
+        uint64_t* keys = nullptr;
+        auto launch = [&](const int* st, int* cnt, uint64_t* out, int fill) {
+            const int wpb = 8;
+            if (M > 0)
+                k_pkf_candidates<<<(M + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, kp, d_mps, d_use, d_mpd, M, th,
+                                                                               st, cnt, out, fill);
+        };
+        rc = candidate_lists(m, M, b, launch, start, count, keys, total);
+        if (rc == ORBGPU_ERR_CAPACITY) {
+            est = est + sizeof(uint64_t) * (size_t)total * 2;
+            continue;
+        }
+        if (rc) return rc;
+        int* d_nm = b.take<int>(1);
+        int* claims3 = b.take<int>((size_t)3 * std::max(1, n));
+        int* res = b.take<int>(std::max(1, M));
+        int* changed = b.take<int>(PROJ_ROUNDS);
+        int* owner = b.take<int>(std::max(1, n));
+        int* nulled = b.take<int>(std::max(1, n));
+        int* bin_of = b.take<int>(std::max(1, M));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(d_nm, 0, sizeof(int), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(claims3, 0x7f, sizeof(int) * (size_t)3 * std::max(1, n), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(res, 0xfe, sizeof(int) * std::max(1, M), m->stream));
+        ORBGPU_CUDA_TRY(cudaMemsetAsync(changed, 0, sizeof(int) * PROJ_ROUNDS, m->stream));
+        if (M > 0 && n > 0) {
+            const int wpb = 8;
+            const int warps = std::max(M, (n + 31) / 32);
+            // every assignment blocks (src/ORBmatcher.cc:1951: any map point on the keypoint)
+            for (int r = 0; r < PROJ_ROUNDS; r++)
+                k_pf_round<<<(warps + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(n, M, start, count, keys, nullptr, r,
+                                                                              claims3, res, changed, d_match);
+            k_pf_serial<<<1, 32, 0, m->stream>>>(n, M, start, count, keys, nullptr, changed, res, claims3, d_match);
+            k_pf_finish<<<1, 1024, 0, m->stream>>>(n, M, res, d_kk, s.kps, m->check_ori, owner, bin_of, nulled, d_match,
                                                    d_nm);
         }
         ORBGPU_CUDA_TRY(cudaGetLastError());

@@ -159,6 +159,43 @@ class ORBmatcher:
               "orbgpu_search_by_projection_frame")
         return nm.value, out[:sc.n]
 
+    def SearchByProjectionKeyFrame(self, F: FrameView, pose, kf_keypoints, mappoints, mp_descriptors, usable,
+                                   th: float, orbdist: int, claimed=None):
+        """SearchByProjection(Frame& CurrentFrame, KeyFrame* pKF, const
+        set<MapPoint*>& sAlreadyFound, th, ORBdist) -- src/ORBmatcher.cc:1891-2010.
+
+        pose: CurrentFrame's FRUSTUM_FRAME_DTYPE record (frustum_frame);
+        per keyframe feature: kf_keypoints (KEYPOINT_DTYPE), mappoints
+        (MAPPOINT_GEOMETRY_DTYPE rows), mp_descriptors (m x 32), usable (1
+        where the map point exists, is not bad and not already found).  Host
+        arrays, or CUDA tensors when F is on the device.  Returns (nmatches,
+        match): per keypoint the keyframe feature whose map point it got, -1,
+        -2 claimed before, -4 reset by the rotation check."""
+        from ._lib import FRUSTUM_FRAME_DTYPE
+        s = F.struct()
+        dev = s.mem == MEM_DEVICE
+        nm = C.c_int(0)
+        rec = np.ascontiguousarray(np.array(pose, FRUSTUM_FRAME_DTYPE).reshape(-1)[:1])
+        if dev:
+            import torch
+            out = torch.empty(max(s.n, 1), dtype=torch.int32, device="cuda")
+            kk, mps, mpd, use, cl = kf_keypoints, mappoints, mp_descriptors, usable, claimed
+            m = int(mpd.shape[0])
+        else:
+            out = np.zeros(max(s.n, 1), np.int32)
+            kk = np.ascontiguousarray(kf_keypoints, KEYPOINT_DTYPE)
+            mps = np.ascontiguousarray(np.asarray(mappoints, np.float32).reshape(-1, 8))
+            mpd = np.ascontiguousarray(mp_descriptors, np.uint8)
+            use = np.ascontiguousarray(usable, np.uint8)
+            cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
+            m = len(mpd)
+            assert mps.shape[0] == m and len(kk) == m and len(use) == m
+        check(lib().orbgpu_search_by_projection_keyframe(self._h, C.byref(s), ptr(rec), ptr(kk), ptr(mps), ptr(mpd),
+                                                         ptr(use), m, C.c_float(th), int(orbdist), ptr(cl), ptr(out),
+                                                         MEM_DEVICE if dev else MEM_HOST, C.byref(nm)),
+              "orbgpu_search_by_projection_keyframe")
+        return nm.value, out[:s.n]
+
     def _search_by_projection_mappoints(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0,
                                         claimed=None):
         s = F.struct()

@@ -471,3 +471,50 @@ def write_vocabulary_text(voc: dict, path: str) -> None:
         lines.append(f"{int(p)} {int(lf)} " + " ".join(str(int(b)) for b in d) + f" {float(w)!r}")
     with open(path, "w") as f:
         f.write("\n".join(lines))
+
+
+def relocalisation_case(kps: np.ndarray, desc: np.ndarray, w: int, h: int, seed: int, m: int = 1500,
+                        fx: float = 500.0):
+    """A keyframe's map points for SearchByProjection(Frame&, KeyFrame*, ...)
+    against a frame with keypoints kps / descriptors desc: each map point is
+    the back-projection of a random keypoint at a random depth through a
+    random camera pose (so it projects near that keypoint), its descriptor a
+    copy of the keypoint's with some bits flipped (a fifth get random
+    descriptors), its distance limits placing the predicted level near the
+    keypoint's octave; the keyframe keypoint angles are the frame's rotated by
+    a common 12 degrees (a tenth random).  Some map points sit behind the
+    camera (the search has no depth test), and the states mix usable (1),
+    bad (2), already found (3) and none (0).  Returns (Tcw (3, 4) float32,
+    cam (fx, fy, cx, cy), kf_kps, geometry (m, 8) float32, mp_desc,
+    mp_state, claimed)."""
+    rng = np.random.default_rng(seed)
+    cx, cy = w / 2.0, h / 2.0
+    R = _rotation(*rng.normal(0, 0.2, 3))
+    t = rng.normal(0, 0.5, 3)
+    Tcw = np.hstack([R, t[:, None]]).astype(np.float32)
+    sel = rng.integers(0, len(kps), m)
+    z = rng.uniform(1.5, 25.0, m)
+    z[rng.random(m) < 0.05] *= -1.0
+    pc = np.stack([(kps["x"][sel] + rng.normal(0, 1.0, m) - cx) / fx * z,
+                   (kps["y"][sel] + rng.normal(0, 1.0, m) - cy) / fx * z, z], 1)
+    pw = (R.T @ (pc - t).T).T
+    Ow = -R.T @ t
+    d = np.linalg.norm(pw - Ow, axis=1)
+    maxd = d * 1.2 ** (kps["octave"][sel] + rng.uniform(-0.45, 0.45, m))
+    geom = np.zeros((m, 8), np.float32)
+    geom[:, :3] = pw
+    geom[:, 6] = maxd / 1.2 ** 7
+    geom[:, 7] = maxd
+    flips = rng.integers(0, 256, (m, 32), dtype=np.uint8)
+    for _ in range(3):
+        flips &= rng.integers(0, 256, (m, 32), dtype=np.uint8)
+    mp_desc = desc[sel] ^ flips
+    rnd = rng.random(m) < 0.2
+    mp_desc[rnd] = rng.integers(0, 256, (int(rnd.sum()), 32), dtype=np.uint8)
+    kf_kps = kps[sel].copy()
+    kf_kps["angle"] = (kf_kps["angle"] + 12.0) % 360.0
+    odd = rng.random(m) < 0.1
+    kf_kps["angle"][odd] = rng.uniform(0, 360, int(odd.sum()))
+    mp_state = rng.choice([1, 1, 1, 1, 1, 1, 2, 3, 0], m).astype(np.uint8)
+    claimed = (rng.random(len(kps)) < 0.05).astype(np.uint8)
+    return Tcw, np.array([fx, fx, cx, cy], np.float32), kf_kps, geom, mp_desc, mp_state, claimed

@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc")
 
 
 def main(groups=GROUPS):
@@ -57,6 +57,8 @@ def main(groups=GROUPS):
         bow_fixture(R)
     if "sbb" in groups:
         search_by_bow_fixture(R)
+    if "reloc" in groups:
+        reloc_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -353,6 +355,28 @@ def search_by_bow_fixture(R):
             arrays[pre + "kf_nm"] = np.array(nm)
             arrays[pre + "kf_match"] = match
     save("search_by_bow.npz", **arrays)
+
+
+def reloc_fixture(R):
+    # 14. ORBmatcher::SearchByProjection(Frame&, KeyFrame*, sAlreadyFound, th,
+    # ORBdist) (relocalisation) on two scenes
+    from oracle.pyoracle import GEOM_DTYPE
+    arrays = {}
+    for sc in range(2):
+        img = syn.scene(640, 480, 90 + sc)
+        e = R.extract(img, nfeatures=1500)
+        Tcw, cam, kfk, g, mpd, st, cl = syn.relocalisation_case(e.keypoints, e.descriptors, 640, 480, 90 + sc)
+        geom = np.ascontiguousarray(g).view(GEOM_DTYPE).reshape(-1)
+        pre = f"s{sc}_"
+        arrays.update({pre + "kps": e.keypoints, pre + "desc": e.descriptors, pre + "Tcw": Tcw, pre + "cam": cam,
+                       pre + "kf_kps": kfk, pre + "geometry": g, pre + "mp_desc": mpd, pre + "mp_state": st,
+                       pre + "claimed": cl})
+        for k, (th, od, ori) in enumerate(((10.0, 100, True), (3.0, 50, False))):
+            nm, match = R.search_by_projection_kf(e.keypoints, e.descriptors, 640, 480, Tcw, cam, kfk, geom, mpd, st,
+                                                  th, od, ori, cl)
+            arrays[pre + f"nm_{k}"] = np.array(nm)
+            arrays[pre + f"match_{k}"] = match
+    save("reloc_search.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -335,3 +335,34 @@ def test_knn_ratio_accept(torch, oracle):
     want = (d1.astype(np.float32) < d2.astype(np.float32) * np.float32(0.8)).astype(np.uint8)
     assert np.array_equal(out[4].cpu().numpy(), want)
     assert 0 < want.sum() < len(want)
+
+
+@pytest.mark.parametrize("seed,th,orbdist,ori,dev", [(0, 10.0, 100, True, False), (1, 3.0, 50, False, False),
+                                                     (2, 10.0, 64, True, True), (3, 5.0, 100, True, True)])
+def test_search_by_projection_keyframe_vs_oracle(torch, oracle, seed, th, orbdist, ori, dev):
+    """SearchByProjection(Frame&, KeyFrame*, sAlreadyFound, th, ORBdist), host
+    and device inputs, against the oracle (-4 resets included)."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher, frustum_frame
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    img = syn.scene(640, 480, 120 + seed)
+    e = oracle.extract(img, nfeatures=1500)
+    Tcw, cam, kfk, g, mpd, st, cl = syn.relocalisation_case(e.keypoints, e.descriptors, 640, 480, 120 + seed)
+    geom = np.ascontiguousarray(g).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    ref_nm, ref = oracle.search_by_projection_kf(e.keypoints, e.descriptors, 640, 480, Tcw, cam, kfk, geom, mpd, st,
+                                                 th, orbdist, ori, cl)
+    pose = frustum_frame(Tcw, cam[0], cam[1], cam[2], cam[3], 0.0, 0.0, 640, 0.0, 480, 1.2, 8)
+    usable = (st == 1).astype(np.uint8)
+    m = ORBmatcher(0.9, ori)
+    if dev:
+        kd = torch.from_numpy(e.keypoints.view(np.float32).reshape(-1, 7).copy()).cuda()
+        F = frame(kd, torch.from_numpy(e.descriptors).cuda(), 640, 480)
+        nm, match = m.SearchByProjectionKeyFrame(
+            F, pose, torch.from_numpy(kfk.view(np.float32).reshape(-1, 7).copy()).cuda(), torch.from_numpy(g).cuda(),
+            torch.from_numpy(mpd).cuda(), torch.from_numpy(usable).cuda(), th, orbdist, torch.from_numpy(cl).cuda())
+        match = match.cpu().numpy()
+    else:
+        nm, match = m.SearchByProjectionKeyFrame(frame(e.keypoints, e.descriptors, 640, 480), pose, kfk, g, mpd, usable,
+                                                 th, orbdist, cl)
+    assert nm == ref_nm
+    assert np.array_equal(match, ref)
+    assert ref_nm > 300

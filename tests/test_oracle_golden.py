@@ -291,3 +291,21 @@ def test_search_by_bow_keyframes_golden(oracle, golden, sc):
                                         g[pre + "f_kps"], g[pre + "f_desc"], g[pre + "f_mp"], fv["f"])
     assert nm == int(g[pre + "kf_nm"])
     assert np.array_equal(match, g[pre + "kf_match"])
+
+
+RELOC_PARAMS = ((10.0, 100, True), (3.0, 50, False))
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_search_by_projection_keyframe_golden(oracle, golden, sc):
+    """SearchByProjection(Frame&, KeyFrame*, sAlreadyFound, th, ORBdist) against
+    the reference's outputs (a reset by the rotation check reads as -1 there)."""
+    g = golden("reloc_search.npz")
+    pre = f"s{sc}_"
+    geom = np.ascontiguousarray(g[pre + "geometry"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    for k, (th, od, ori) in enumerate(RELOC_PARAMS):
+        nm, match = oracle.search_by_projection_kf(g[pre + "kps"], g[pre + "desc"], 640, 480, g[pre + "Tcw"],
+                                                   g[pre + "cam"], g[pre + "kf_kps"], geom, g[pre + "mp_desc"],
+                                                   g[pre + "mp_state"], th, od, ori, g[pre + "claimed"])
+        assert nm == int(g[pre + f"nm_{k}"])
+        assert np.array_equal(np.where(match == -4, -1, match), g[pre + f"match_{k}"])
