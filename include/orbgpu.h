@@ -247,6 +247,31 @@ int orbgpu_search_by_bow_keyframes(const orbgpu_keypoint* kps, const uint8_t* de
                                    const int* pairs, int npairs, float nnratio, int check_ori, const int* out_offsets,
                                    int* match_out, int* nmatches, void* stream);
 
+/* ORBmatcher::SearchForTriangulation(pKF1, pKF2, F12, vMatchedPairs,
+ * bOnlyStereo) -- src/ORBmatcher.cc:884-1040, CheckDistEpipolarLine
+ * :205-232 -- for npairs keyframe pairs: the set layout of
+ * orbgpu_search_by_bow; has_mappoint: one byte per row, non-zero where
+ * GetMapPoint(i) is not NULL (such features take no part); uright: one float
+ * per row (mvuRight, >= 0 for stereo); pair_params: 11 floats per pair, F12
+ * row-major then the epipole (ex, ey) in pKF2 (orbgpu_triangulation_epipole);
+ * scale_factors / level_sigma2: pKF2's mvScaleFactors / mvLevelSigma2
+ * (nlevels, host).  match_out: for pair p, pKF1's rows at out_offsets[p]: the
+ * pKF2 feature paired with it (vMatchedPairs), or -1.  nmatches[p]: the
+ * reference's return value.  The candidate a pKF1 feature takes is the last
+ * at the least distance among those passing the tests, as the reference's
+ * "dist > bestDist" skip leaves it. */
+int orbgpu_search_for_triangulation(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
+                                    const int* fv_counts, const int* fv_nodes, const int* fv_starts,
+                                    const int* fv_sizes, const int* fv_features, const uint8_t* has_mappoint,
+                                    const float* uright, const int* pairs, int npairs, const float* pair_params,
+                                    const float* scale_factors, const float* level_sigma2, int nlevels,
+                                    int only_stereo, int check_ori, const int* out_offsets, int* match_out,
+                                    int* nmatches, void* stream);
+/* The epipole of SearchForTriangulation: pKF1's camera centre Cw1 seen by
+ * pKF2 (T2: rows 0-2 of its Tcw; K2: fx, fy, cx, cy), as the reference
+ * computes it (src/ORBmatcher.cc:897-906).  Host only. */
+int orbgpu_triangulation_epipole(const float* Cw1, const float* T2, const float* K2, float* ex, float* ey);
+
 /* Frame::UndistortKeyPoints() -- src/Frame.cc:724-776 -- for n keypoints of
  * one camera: out[i] = kps[i] with x, y through cv::undistortPoints(pts, pts,
  * mK, mDistCoef, cv::Mat(), mK) (OpenCV 3.2's algorithm: double precision,

@@ -803,6 +803,108 @@ int orc_search_by_projection_kf(const orc_params* p, const orc_kp* kps, const ui
     return nmatches;
 }
 
+// ORBmatcher::SearchForTriangulation(pKF1, pKF2, F12, vMatchedPairs,
+// bOnlyStereo), src/ORBmatcher.cc:884-1040, with CheckDistEpipolarLine
+// (:205-232).  Features without a map point only (mp != 0 is a map point,
+// bad or not); in a common node every pKF1 feature takes, among the node's
+// unmatched pKF2 features at distance <= TH_LOW passing the epipole distance
+// (both monocular) and the epipolar line test, the last one at the least
+// distance (the reference's "dist > bestDist" skip keeps equal ones coming
+// later).  Cw1: pKF1's camera centre; T2: rows 0-2 of pKF2's Tcw; K2: pKF2's
+// fx, fy, cx, cy; scale / sigma2: pKF2's mvScaleFactors / mvLevelSigma2.
+// match_out[i1]: the pKF2 feature or -1.
+int orc_search_for_triangulation(const orc_kp* kps1, const uint8_t* desc1, const uint8_t* mp1, const float* ur1, int n1,
+                                  int fv1_n, const int* fv1_nodes, const int* fv1_offsets, const int* fv1_features,
+                                  const orc_kp* kps2, const uint8_t* desc2, const uint8_t* mp2, const float* ur2, int n2,
+                                  int fv2_n, const int* fv2_nodes, const int* fv2_offsets, const int* fv2_features,
+                                  const float* Cw1, const float* T2, const float* K2, const float* F12,
+                                  const float* scale, const float* sigma2, int only_stereo, int check_ori,
+                                  int* match_out) {
+    const int TH_LOW = 50, HISTO = 30;
+    (void)n2;
+    // the epipole: C2 = R2w * Cw + t2w (double-accumulated product), 1.0f / z
+    float C2[3];
+    for (int r = 0; r < 3; r++) C2[r] = mat_row_dot(T2 + 4 * r, 1, Cw1) + T2[4 * r + 3];
+    const float invz = 1.0f / C2[2];
+    const float ex = K2[0] * C2[0] * invz + K2[2];
+    const float ey = K2[1] * C2[1] * invz + K2[3];
+    std::vector<char> matched2(n2, 0);
+    for (int i = 0; i < n1; i++) match_out[i] = -1;
+    std::vector<int> hist[HISTO];
+    const float factor = HISTO / 360.0f;
+    int nmatches = 0, a = 0, b = 0;
+    while (a < fv1_n && b < fv2_n) {
+        if (fv1_nodes[a] < fv2_nodes[b]) {
+            a++;
+            continue;
+        }
+        if (fv1_nodes[a] > fv2_nodes[b]) {
+            b++;
+            continue;
+        }
+        for (int p = fv1_offsets[a]; p < fv1_offsets[a + 1]; p++) {
+            const int i1 = fv1_features[p];
+            if (mp1[i1]) continue;
+            const bool st1 = ur1[i1] >= 0;
+            if (only_stereo && !st1) continue;
+            const orc_kp& k1 = kps1[i1];
+            int bestDist = TH_LOW, best2 = -1;
+            for (int q = fv2_offsets[b]; q < fv2_offsets[b + 1]; q++) {
+                const int i2 = fv2_features[q];
+                if (matched2[i2] || mp2[i2]) continue;
+                const bool st2 = ur2[i2] >= 0;
+                if (only_stereo && !st2) continue;
+                const int dist = hamming(desc1 + (size_t)i1 * 32, desc2 + (size_t)i2 * 32);
+                if (dist > TH_LOW || dist > bestDist) continue;
+                const orc_kp& k2 = kps2[i2];
+                if (!st1 && !st2) {
+                    const float dx = ex - k2.x, dy = ey - k2.y;
+                    if (dx * dx + dy * dy < 100 * scale[k2.octave]) continue;
+                }
+                // CheckDistEpipolarLine: the line of kp1 in pKF2, distance of kp2 to it
+                const float la = k1.x * F12[0] + k1.y * F12[3] + F12[6];
+                const float lb = k1.x * F12[1] + k1.y * F12[4] + F12[7];
+                const float lc = k1.x * F12[2] + k1.y * F12[5] + F12[8];
+                const float num = la * k2.x + lb * k2.y + lc;
+                const float den = la * la + lb * lb;
+                if (den == 0) continue;
+                const float dsqr = num * num / den;
+                if (dsqr < 3.84 * sigma2[k2.octave]) {
+                    best2 = i2;
+                    bestDist = dist;
+                }
+            }
+            if (best2 >= 0) {
+                match_out[i1] = best2;
+                matched2[best2] = 1;
+                nmatches++;
+                if (check_ori) {
+                    float rot = k1.angle - kps2[best2].angle;
+                    if (rot < 0.0) rot += 360.0f;
+                    int bin = (int)std::round(rot * factor);
+                    if (bin == HISTO) bin = 0;
+                    hist[bin].push_back(i1);
+                }
+            }
+        }
+        a++;
+        b++;
+    }
+    if (check_ori) {
+        int i1 = -1, i2 = -1, i3 = -1;
+        three_maxima(hist, HISTO, i1, i2, i3);
+        for (int h = 0; h < HISTO; h++) {
+            if (h == i1 || h == i2 || h == i3) continue;
+            for (int idx1 : hist[h]) {
+                matched2[match_out[idx1]] = 0;
+                match_out[idx1] = -1;
+                nmatches--;
+            }
+        }
+    }
+    return nmatches;
+}
+
 // Frame::ComputeStereoMatches, src/Frame.cc:831-1082 (mb = mbf/fx).
 int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
                                const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,

@@ -69,6 +69,15 @@ int orc_search_by_projection_kf(const orc_params* p, const orc_kp* kps, const ui
                                 const float* T, const float* cam, const orc_kp* kf_kps, int m,
                                 const orc_mp_geometry* mps, const uint8_t* mp_desc, const uint8_t* mp_state, float th,
                                 int orbdist, int check_ori, const uint8_t* claimed, int* match_out);
+/* ORBmatcher::SearchForTriangulation(pKF1, pKF2, F12, pairs, bOnlyStereo)
+ * (src/ORBmatcher.cc:884-1040): see orb_oracle.cpp for the arguments. */
+int orc_search_for_triangulation(const orc_kp* kps1, const uint8_t* desc1, const uint8_t* mp1, const float* ur1, int n1,
+                                  int fv1_n, const int* fv1_nodes, const int* fv1_offsets, const int* fv1_features,
+                                  const orc_kp* kps2, const uint8_t* desc2, const uint8_t* mp2, const float* ur2, int n2,
+                                  int fv2_n, const int* fv2_nodes, const int* fv2_offsets, const int* fv2_features,
+                                  const float* Cw1, const float* T2, const float* K2, const float* F12,
+                                  const float* scale, const float* sigma2, int only_stereo, int check_ori,
+                                  int* match_out);
 /* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
  * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
  * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:

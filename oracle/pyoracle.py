@@ -311,6 +311,30 @@ class _Base:
                _p(mpd), _p(st), C.c_float(th), int(orbdist), int(bool(check_ori)), _p(cl), _p(out))
         return int(nm), out[:len(kps)].copy()
 
+    def search_for_triangulation(self, kps1, desc1, mp1, ur1, fv1, kps2, desc2, mp2, ur2, fv2, Cw1, T2, K2, F12,
+                                 scale, sigma2, only_stereo=False, check_ori=True):
+        """SearchForTriangulation(pKF1, pKF2, F12, pairs, bOnlyStereo) ->
+        (nmatches, match_out over pKF1's features)."""
+        a1 = [np.ascontiguousarray(kps1, KP_DTYPE), np.ascontiguousarray(desc1, np.uint8),
+              np.ascontiguousarray(mp1, np.uint8), np.ascontiguousarray(ur1, np.float32)]
+        a2 = [np.ascontiguousarray(kps2, KP_DTYPE), np.ascontiguousarray(desc2, np.uint8),
+              np.ascontiguousarray(mp2, np.uint8), np.ascontiguousarray(ur2, np.float32)]
+        f1 = [np.ascontiguousarray(x, np.int32) for x in fv1]
+        f2 = [np.ascontiguousarray(x, np.int32) for x in fv2]
+        fl = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1)) for x in (Cw1, T2, K2, F12)]
+        sc = np.zeros(16, np.float32)
+        sg = np.zeros(16, np.float32)
+        sc[:len(scale)] = scale
+        sg[:len(sigma2)] = sigma2
+        out = np.zeros(max(len(a1[0]), 1), np.int32)
+        f = self.fn("search_for_triangulation")
+        f.argtypes = ([C.c_void_p] * 4 + [C.c_int] * 2 + [C.c_void_p] * 3) * 2 + [C.c_void_p] * 6 + \
+            [C.c_int, C.c_int, C.c_void_p]
+        nm = f(*[_p(x) for x in a1], len(a1[0]), len(f1[0]), *[_p(x) for x in f1],
+               *[_p(x) for x in a2], len(a2[0]), len(f2[0]), *[_p(x) for x in f2],
+               *[_p(x) for x in fl], _p(sc), _p(sg), int(bool(only_stereo)), int(bool(check_ori)), _p(out))
+        return int(nm), out[:len(a1[0])].copy()
+
     def search_by_bow(self, kf_kps, kf_desc, kf_mp, kf_fv, f_kps, f_desc, f_fv, nnratio=0.75, check_ori=True):
         """ORBmatcher::SearchByBoW(KeyFrame*, Frame&, matches).  *_fv: (nodes,
         offsets, features) of the FeatureVector (bow_transform's fv_*);

@@ -772,6 +772,69 @@ int ref_search_by_projection_kf(const orc_params* p, const orc_kp* kps, const ui
     return nm;
 }
 
+// ORBmatcher::SearchForTriangulation(pKF1, pKF2, F12, vMatchedPairs,
+// bOnlyStereo) -- src/ORBmatcher.cc:884-1040.  Arguments as
+// orc_search_for_triangulation; pKF1's camera centre and pKF2's pose are set
+// on the keyframes, pKF2's camera constants and scale tables through the
+// frame they are built from.
+int ref_search_for_triangulation(const orc_kp* kps1, const uint8_t* desc1, const uint8_t* mp1, const float* ur1, int n1,
+                                  int fv1_n, const int* fv1_nodes, const int* fv1_offsets, const int* fv1_features,
+                                  const orc_kp* kps2, const uint8_t* desc2, const uint8_t* mp2, const float* ur2, int n2,
+                                  int fv2_n, const int* fv2_nodes, const int* fv2_offsets, const int* fv2_features,
+                                  const float* Cw1, const float* T2, const float* K2, const float* F12,
+                                  const float* scale, const float* sigma2, int only_stereo, int check_ori,
+                                  int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        MapPointMaker maker;
+        Frame::fx = K2[0];
+        Frame::fy = K2[1];
+        Frame::cx = K2[2];
+        Frame::cy = K2[3];
+        std::map<MapPoint*, int> index1, index2;
+        Frame *s1, *s2;
+        KeyFrame* KF1 = make_keyframe(maker, kps1, desc1, mp1, n1, fv1_n, fv1_nodes, fv1_offsets, fv1_features,
+                                      index1, s1);
+        KeyFrame* KF2 = make_keyframe(maker, kps2, desc2, mp2, n2, fv2_n, fv2_nodes, fv2_offsets, fv2_features,
+                                      index2, s2);
+        // stereo flags and pKF2's scale tables live in const members: rebuild
+        // the keyframes from frames carrying them
+        s1->mvuRight.assign(ur1, ur1 + n1);
+        s2->mvuRight.assign(ur2, ur2 + n2);
+        s2->mvScaleFactors.assign(scale, scale + 16);
+        s2->mvLevelSigma2.assign(sigma2, sigma2 + 16);
+        KeyFrame* A = new KeyFrame(*s1, maker.map, nullptr);
+        KeyFrame* B = new KeyFrame(*s2, maker.map, nullptr);
+        A->mFeatVec = KF1->mFeatVec;
+        B->mFeatVec = KF2->mFeatVec;
+        A->mvpMapPoints = KF1->mvpMapPoints;
+        B->mvpMapPoints = KF2->mvpMapPoints;
+        A->Ow = cv::Mat(3, 1, CV_32F);
+        for (int r = 0; r < 3; r++) A->Ow.at<float>(r) = Cw1[r];
+        B->Tcw = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) B->Tcw.at<float>(r, c) = T2[4 * r + c];
+        cv::Mat F(3, 3, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) F.at<float>(r, c) = F12[3 * r + c];
+        std::vector<std::pair<size_t, size_t> > pairs;
+        ORBmatcher matcher(0.6f, check_ori != 0);
+        nm = matcher.SearchForTriangulation(A, B, F, pairs, only_stereo != 0);
+        for (int i = 0; i < n1; i++) match_out[i] = -1;
+        for (auto& pr : pairs) match_out[pr.first] = (int)pr.second;
+        for (auto& e : index1) delete e.first;
+        for (auto& e : index2) delete e.first;
+        delete A;
+        delete B;
+        delete KF1;
+        delete KF2;
+        delete s1;
+        delete s2;
+    }
+    return nm;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

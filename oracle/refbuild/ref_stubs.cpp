@@ -3,10 +3,11 @@
 // and src/MapPoint.cc reference but whose own sources (src/KeyFrame.cc,
 // src/Map.cc, src/Converter.cc) need Eigen/g2o/DBoW2 vocabularies and are off
 // the feature path.  The keyframe constructor copies only the fields the
-// compiled reference code reads (mnFrameId, mvKeysUn, mvuRight, mDescriptors)
-// and zeroes the rest; the accessors the path uses (KeyFrame::isBad,
-// GetMapPointMatches) return the stored fields exactly as src/KeyFrame.cc
-// does (without its locking);
+// compiled reference code reads (mnFrameId, fx, fy, cx, cy, mvKeysUn, mvuRight,
+// mDescriptors, mvScaleFactors, mvLevelSigma2) and zeroes the rest; the
+// accessors the path uses (isBad, GetMapPointMatches, GetMapPoint,
+// GetCameraCenter, GetRotation, GetTranslation) return the stored fields
+// exactly as src/KeyFrame.cc does (without its locking);
 // everything else aborts if called.
 #include "MapPoint.h"
 #include "KeyFrame.h"
@@ -29,9 +30,9 @@ KeyFrame::KeyFrame(Frame& F, Map* pMap, KeyFrameDatabase* pKFDB)
     : mnFrameId(F.mnId), mTimeStamp(0), mnGridCols(0), mnGridRows(0), mfGridElementWidthInv(0),
       mfGridElementHeightInv(0), mnTrackReferenceForFrame(0), mnFuseTargetForKF(0), mnBALocalForKF(0),
       mnBAFixedForKF(0), mnLoopQuery(0), mnLoopWords(0), mLoopScore(0), mnRelocQuery(0), mnRelocWords(0),
-      mRelocScore(0), mnBAGlobalForKF(0), fx(0), fy(0), cx(0), cy(0), invfx(0), invfy(0), mbf(0), mb(0),
+      mRelocScore(0), mnBAGlobalForKF(0), fx(F.fx), fy(F.fy), cx(F.cx), cy(F.cy), invfx(0), invfy(0), mbf(0), mb(0),
       mThDepth(0), N(F.N), mvKeysUn(F.mvKeysUn), mvuRight(F.mvuRight), mDescriptors(F.mDescriptors.clone()),
-      mnScaleLevels(0),
+      mnScaleLevels(0), mvScaleFactors(F.mvScaleFactors), mvLevelSigma2(F.mvLevelSigma2),
       mfScaleFactor(0), mfLogScaleFactor(0), mnMinX(0), mnMinY(0), mnMaxX(0), mnMaxY(0), mpKeyFrameDB(pKFDB),
       mpORBvocabulary(nullptr), mbFirstConnection(true), mpParent(nullptr), mbNotErase(false),
       mbToBeErased(false), mbBad(false), mHalfBaseline(0), mpMap(pMap) {
@@ -43,15 +44,15 @@ void KeyFrame::AddMapPoint(MapPoint*, const size_t&) { stub_unreachable("KeyFram
 void KeyFrame::EraseMapPointMatch(const size_t&) { stub_unreachable("KeyFrame::EraseMapPointMatch"); }
 void KeyFrame::EraseMapPointMatch(MapPoint*) { stub_unreachable("KeyFrame::EraseMapPointMatch"); }
 void KeyFrame::ReplaceMapPointMatch(const size_t&, MapPoint*) { stub_unreachable("KeyFrame::ReplaceMapPointMatch"); }
-cv::Mat KeyFrame::GetCameraCenter() { stub_unreachable("KeyFrame::GetCameraCenter"); }
+cv::Mat KeyFrame::GetCameraCenter() { return Ow.clone(); }
 std::vector<size_t> KeyFrame::GetFeaturesInArea(const float&, const float&, const float&) const {
     stub_unreachable("KeyFrame::GetFeaturesInArea");
 }
-MapPoint* KeyFrame::GetMapPoint(const size_t&) { stub_unreachable("KeyFrame::GetMapPoint"); }
+MapPoint* KeyFrame::GetMapPoint(const size_t& idx) { return mvpMapPoints[idx]; }
 std::vector<MapPoint*> KeyFrame::GetMapPointMatches() { return mvpMapPoints; }
 std::set<MapPoint*> KeyFrame::GetMapPoints() { stub_unreachable("KeyFrame::GetMapPoints"); }
-cv::Mat KeyFrame::GetRotation() { stub_unreachable("KeyFrame::GetRotation"); }
-cv::Mat KeyFrame::GetTranslation() { stub_unreachable("KeyFrame::GetTranslation"); }
+cv::Mat KeyFrame::GetRotation() { return Tcw.rowRange(0, 3).colRange(0, 3).clone(); }
+cv::Mat KeyFrame::GetTranslation() { return Tcw.rowRange(0, 3).col(3).clone(); }
 bool KeyFrame::IsInImage(const float&, const float&) const { stub_unreachable("KeyFrame::IsInImage"); }
 
 Map::Map() : mnMaxKFid(0), mnBigChangeIdx(0) {}

@@ -11,4 +11,4 @@ from .extractor import ORBextractor  # noqa: F401
 from .matcher import ORBmatcher, FrameView, compute_stereo_matches  # noqa: F401
 from .mappoints import compute_distinctive_descriptors, observations_to_csr  # noqa: F401
 from .frustum import compute_image_bounds, frustum_frame, is_in_frustum, undistort_keypoints  # noqa: F401
-from .bow import Vocabulary, search_by_bow  # noqa: F401
+from .bow import Vocabulary, search_by_bow, search_for_triangulation  # noqa: F401

@@ -139,3 +139,49 @@ def search_by_bow(keypoints, descriptors, offsets, bow, kf_mappoints, pairs, nnr
                                      int(bool(check_orientation)), ptr(OO), ptr(match), ptr(nm), C.c_void_p(st)),
           "orbgpu_search_by_bow")
     return nm[:len(pr)], [match[out_off[i]:out_off[i + 1]] for i in range(len(pr))]
+
+
+def search_for_triangulation(keypoints, descriptors, offsets, bow, has_mappoint, uright, pairs, geometry,
+                             scale_factors, level_sigma2, only_stereo: bool = False, check_orientation: bool = True,
+                             stream=None):
+    """ORBmatcher::SearchForTriangulation(pKF1, pKF2, F12, vMatchedPairs,
+    bOnlyStereo) (src/ORBmatcher.cc:884-1040) for many keyframe pairs.
+
+    The set as for search_by_bow; has_mappoint (n,) uint8 (GetMapPoint(i) not
+    NULL), uright (n,) float32 tensors; pairs (P, 2) host ints (pKF1, pKF2);
+    geometry: per pair (Cw1, T2 (3 x 4), K2 (fx, fy, cx, cy), F12 (3 x 3))
+    on the host; scale_factors / level_sigma2: pKF2's tables.  Returns
+    (nmatches (P,), list of P tensors: per pKF1 feature the paired pKF2
+    feature or -1)."""
+    import torch
+    pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    params = np.zeros((len(pr), 11), np.float32)
+    for i, (Cw1, T2, K2, F12) in enumerate(geometry):
+        ex, ey = C.c_float(0), C.c_float(0)
+        c = np.ascontiguousarray(Cw1, np.float32)
+        t = np.ascontiguousarray(np.asarray(T2, np.float32).reshape(-1)[:12])
+        k = np.ascontiguousarray(K2, np.float32)
+        check(lib().orbgpu_triangulation_epipole(ptr(c), ptr(t), ptr(k), C.byref(ex), C.byref(ey)),
+              "orbgpu_triangulation_epipole")
+        params[i, :9] = np.asarray(F12, np.float32).reshape(-1)[:9]
+        params[i, 9], params[i, 10] = ex.value, ey.value
+    offs = offsets.cpu().numpy() if offsets.is_cuda else np.asarray(offsets)
+    sizes = offs[pr[:, 0] + 1] - offs[pr[:, 0]]
+    out_off = np.zeros(len(pr) + 1, np.int32)
+    out_off[1:] = np.cumsum(sizes)
+    dev = torch.device("cuda")
+    P = torch.from_numpy(pr.reshape(-1).copy()).to(dev)
+    PP = torch.from_numpy(params.reshape(-1).copy()).to(dev)
+    OO = torch.from_numpy(out_off[:-1].copy()).to(dev)
+    sc = np.ascontiguousarray(scale_factors, np.float32)
+    sg = np.ascontiguousarray(level_sigma2, np.float32)
+    match = torch.empty(max(int(out_off[-1]), 1), dtype=torch.int32, device=dev)
+    nm = torch.empty(max(len(pr), 1), dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+    check(lib().orbgpu_search_for_triangulation(ptr(keypoints), ptr(descriptors), ptr(offsets), ptr(bow["fv_counts"]),
+                                                ptr(bow["fv_nodes"]), ptr(bow["fv_starts"]), ptr(bow["fv_sizes"]),
+                                                ptr(bow["fv_features"]), ptr(has_mappoint), ptr(uright), ptr(P),
+                                                len(pr), ptr(PP), ptr(sc), ptr(sg), len(sc), int(bool(only_stereo)),
+                                                int(bool(check_orientation)), ptr(OO), ptr(match), ptr(nm),
+                                                C.c_void_p(st)), "orbgpu_search_for_triangulation")
+    return nm[:len(pr)], [match[out_off[i]:out_off[i + 1]] for i in range(len(pr))]

@@ -227,11 +227,20 @@ __global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
 #define SBB_THREADS 1024
 #define SBB_TH_LOW 50
 
+// SearchForTriangulation's per-call constants: pKF2's scale tables (read at
+// the candidate's octave) and bOnlyStereo.
+struct TriangulationDev {
+    float scale[16];
+    float sigma2[16];
+    int only_stereo;
+};
+
 __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
     const orbgpu_keypoint* __restrict__ kps, const uint4* __restrict__ desc, const int* __restrict__ offsets,
     const int* __restrict__ fv_counts, const int* __restrict__ fv_nodes, const int* __restrict__ fv_starts,
     const int* __restrict__ fv_sizes, const int* __restrict__ fv_features, const uint8_t* __restrict__ kf_mp,
-    const int* __restrict__ pairs, float nnratio, int check_ori, int keyframes, const int* __restrict__ out_offsets,
+    const int* __restrict__ pairs, float nnratio, int check_ori, int keyframes, const float* __restrict__ pair_params,
+    const float* __restrict__ uright, TriangulationDev tri, const int* __restrict__ out_offsets,
     int* __restrict__ match_out, int* __restrict__ nmatches) {
     __shared__ unsigned s_taken[BOW_MAX_FEATURES / 32];
     __shared__ unsigned char s_bin[BOW_MAX_FEATURES];
@@ -256,6 +265,15 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
     if (threadIdx.x == 0) s_nm = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    // mode 2: SearchForTriangulation -- F12 (row-major) and the epipole in pKF2
+    const bool triang = keyframes == 2;
+    float F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ex = 0.f, ey = 0.f;
+    if (triang) {
+#pragma unroll
+        for (int q = 0; q < 9; q++) F[q] = pair_params[11 * p + q];
+        ex = pair_params[11 * p + 9];
+        ey = pair_params[11 * p + 10];
+    }
     const float factor = __fdiv_rn((float)ORBGPU_HISTO_LENGTH, 360.0f);
     const unsigned INF = 0x7fffffffu;
     for (int j = warp; j < cf; j += nwarps) {
@@ -278,7 +296,22 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
         const int kcount = fv_sizes[ok0 + jk];
         for (int t = 0; t < kcount; t++) {
             const int ikf = klist[t];
-            if (kf_mp[ok0 + ikf] != 1) continue;
+            bool st1 = false;
+            float x1 = 0.f, y1 = 0.f, la = 0.f, lb = 0.f, lc = 0.f;
+            if (triang) {
+                // features without a map point (bad or not), stereo ones only with bOnlyStereo
+                if (kf_mp[ok0 + ikf] != 0) continue;
+                st1 = uright[ok0 + ikf] >= 0.0f;
+                if (tri.only_stereo && !st1) continue;
+                x1 = kps[ok0 + ikf].x;
+                y1 = kps[ok0 + ikf].y;
+                // CheckDistEpipolarLine (src/ORBmatcher.cc:205-232): the line of kp1 in pKF2
+                la = __fadd_rn(__fadd_rn(__fmul_rn(x1, F[0]), __fmul_rn(y1, F[3])), F[6]);
+                lb = __fadd_rn(__fadd_rn(__fmul_rn(x1, F[1]), __fmul_rn(y1, F[4])), F[7]);
+                lc = __fadd_rn(__fadd_rn(__fmul_rn(x1, F[2]), __fmul_rn(y1, F[5])), F[8]);
+            } else if (kf_mp[ok0 + ikf] != 1) {
+                continue;
+            }
             const uint4 a0 = desc[2 * (size_t)(ok0 + ikf)], a1 = desc[2 * (size_t)(ok0 + ikf) + 1];
             unsigned b1 = INF;
             int b2 = 256;
@@ -287,7 +320,34 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
                 int d = 256;
                 if (c + lane < fcount) {
                     const int jf = flist[c + lane];
-                    if (!((s_taken[jf >> 5] >> (jf & 31)) & 1u) && (!keyframes || kf_mp[of0 + jf] == 1)) {
+                    const bool free2 = !((s_taken[jf >> 5] >> (jf & 31)) & 1u);
+                    if (triang) {
+                        const bool st2 = uright[of0 + jf] >= 0.0f;
+                        if (free2 && kf_mp[of0 + jf] == 0 && (!tri.only_stereo || st2)) {
+                            const int dd = hamming256(a0, a1, desc[2 * (size_t)(of0 + jf)],
+                                                      desc[2 * (size_t)(of0 + jf) + 1]);
+                            const orbgpu_keypoint k2 = kps[of0 + jf];
+                            bool ok = dd <= SBB_TH_LOW && k2.octave >= 0 && k2.octave < 16;
+                            if (ok && !st1 && !st2) {
+                                const float dx = __fsub_rn(ex, k2.x), dy = __fsub_rn(ey, k2.y);
+                                if (__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <
+                                    __fmul_rn(100.0f, tri.scale[k2.octave]))
+                                    ok = false;
+                            }
+                            if (ok) {
+                                const float num = __fadd_rn(__fadd_rn(__fmul_rn(la, k2.x), __fmul_rn(lb, k2.y)), lc);
+                                const float den = __fadd_rn(__fmul_rn(la, la), __fmul_rn(lb, lb));
+                                ok = den != 0.0f &&
+                                     (double)__fdiv_rn(__fmul_rn(num, num), den) <
+                                         __dmul_rn(3.84, (double)tri.sigma2[k2.octave]);
+                            }
+                            if (ok) {
+                                // the last candidate at the least distance wins ("dist > bestDist" skips)
+                                d = dd;
+                                key = ((unsigned)dd << 13) | (unsigned)(8191 - (c + lane));
+                            }
+                        }
+                    } else if (free2 && (!keyframes || kf_mp[of0 + jf] == 1)) {
                         d = hamming256(a0, a1, desc[2 * (size_t)(of0 + jf)], desc[2 * (size_t)(of0 + jf) + 1]);
                         key = ((unsigned)d << 13) | (unsigned)(c + lane);
                     }
@@ -302,14 +362,17 @@ __global__ void __launch_bounds__(SBB_THREADS) k_search_by_bow(
                 }
             }
             const int best1 = b1 == INF ? 256 : (int)(b1 >> 13);
-            // TH_LOW inclusive for (keyframe, frame), exclusive for two keyframes
-            if ((keyframes ? best1 < SBB_TH_LOW : best1 <= SBB_TH_LOW) &&
-                (float)best1 < __fmul_rn(nnratio, (float)b2)) {
+            // TH_LOW inclusive for (keyframe, frame), exclusive for two
+            // keyframes; triangulation: any candidate left (no ratio test)
+            const bool take = triang ? b1 != INF
+                                     : (keyframes ? best1 < SBB_TH_LOW : best1 <= SBB_TH_LOW) &&
+                                           (float)best1 < __fmul_rn(nnratio, (float)b2);
+            if (take) {
                 if (lane == 0) {
-                    const int jf = flist[b1 & 8191u];
+                    const int jf = flist[triang ? 8191u - (b1 & 8191u) : (b1 & 8191u)];
                     atomicOr(&s_taken[jf >> 5], 1u << (jf & 31));
                     const int slot = keyframes ? ikf : jf;
-                    out[slot] = keyframes ? jf : ikf;
+                    out[slot] = keyframes ? jf : ikf;  // modes 1 and 2 report per first-keyframe feature
                     if (check_ori) {
                         float rot = __fsub_rn(kps[ok0 + ikf].angle, kps[of0 + jf].angle);
                         if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
@@ -378,7 +441,9 @@ using namespace orbgpu;
 static int search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets, const int* fv_counts,
                          const int* fv_nodes, const int* fv_starts, const int* fv_sizes, const int* fv_features,
                          const uint8_t* kf_mappoints, const int* pairs, int npairs, float nnratio, int check_ori,
-                         int keyframes, const int* out_offsets, int* match_out, int* nmatches, void* stream) {
+                         int keyframes, const int* out_offsets, int* match_out, int* nmatches, void* stream,
+                         const float* pair_params = nullptr, const float* uright = nullptr,
+                         const TriangulationDev* tri = nullptr) {
     if (npairs < 0 || (npairs > 0 && (!kps || !desc || !offsets || !fv_counts || !fv_nodes || !fv_starts ||
                                       !fv_sizes || !fv_features || !kf_mappoints || !pairs || !out_offsets ||
                                       !match_out || !nmatches)) ||
@@ -389,7 +454,8 @@ static int search_by_bow(const orbgpu_keypoint* kps, const uint8_t* desc, const 
     if (npairs == 0) return ORBGPU_OK;
     k_search_by_bow<<<npairs, SBB_THREADS, 0, (cudaStream_t)stream>>>(
         kps, reinterpret_cast<const uint4*>(desc), offsets, fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features,
-        kf_mappoints, pairs, nnratio, check_ori, keyframes, out_offsets, match_out, nmatches);
+        kf_mappoints, pairs, nnratio, check_ori, keyframes, pair_params, uright, tri ? *tri : TriangulationDev{},
+        out_offsets, match_out, nmatches);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     return ORBGPU_OK;
 }
@@ -572,4 +638,47 @@ extern "C" int orbgpu_bow_transform(const orbgpu_vocabulary* v, const uint8_t* d
         fv_nodes, fv_starts, fv_sizes, fv_features);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_triangulation_epipole(const float* Cw1, const float* T2, const float* K2, float* ex,
+                                            float* ey) {
+    if (!Cw1 || !T2 || !K2 || !ex || !ey) return ORBGPU_ERR_BAD_ARG;
+    // C2 = R2w * Cw + t2w (src/ORBmatcher.cc:897-901): the 3 x 3 product
+    // accumulated in double and rounded to float, then a float add
+    float C2[3];
+    for (int r = 0; r < 3; r++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (double)T2[4 * r + k] * (double)Cw1[k];
+        C2[r] = (float)s + T2[4 * r + 3];
+    }
+    const float invz = 1.0f / C2[2];
+    *ex = K2[0] * C2[0] * invz + K2[2];
+    *ey = K2[1] * C2[1] * invz + K2[3];
+    return ORBGPU_OK;
+}
+
+extern "C" int orbgpu_search_for_triangulation(const orbgpu_keypoint* kps, const uint8_t* desc, const int* offsets,
+                                               const int* fv_counts, const int* fv_nodes, const int* fv_starts,
+                                               const int* fv_sizes, const int* fv_features,
+                                               const uint8_t* has_mappoint, const float* uright, const int* pairs,
+                                               int npairs, const float* pair_params, const float* scale_factors,
+                                               const float* level_sigma2, int nlevels, int only_stereo,
+                                               int check_ori, const int* out_offsets, int* match_out,
+                                               int* nmatches, void* stream) {
+    if (!uright || (npairs > 0 && !pair_params) || !scale_factors || !level_sigma2 || nlevels < 1 || nlevels > 16) {
+        orbgpu_set_last_error("orbgpu_search_for_triangulation: bad arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    TriangulationDev tri;
+    std::memset(&tri, 0, sizeof(tri));
+    for (int l = 0; l < nlevels; l++) {
+        tri.scale[l] = scale_factors[l];
+        tri.sigma2[l] = level_sigma2[l];
+    }
+    // octaves past nlevels read the reference's vectors out of range: they are rejected here
+    for (int l = nlevels; l < 16; l++) tri.scale[l] = tri.sigma2[l] = 0.0f;
+    tri.only_stereo = only_stereo ? 1 : 0;
+    return search_by_bow(kps, desc, offsets, fv_counts, fv_nodes, fv_starts, fv_sizes, fv_features, has_mappoint,
+                         pairs, npairs, 0.0f, check_ori, 2, out_offsets, match_out, nmatches, stream, pair_params,
+                         uright, &tri);
 }

@@ -518,3 +518,31 @@ def relocalisation_case(kps: np.ndarray, desc: np.ndarray, w: int, h: int, seed:
     mp_state = rng.choice([1, 1, 1, 1, 1, 1, 2, 3, 0], m).astype(np.uint8)
     claimed = (rng.random(len(kps)) < 0.05).astype(np.uint8)
     return Tcw, np.array([fx, fx, cx, cy], np.float32), kf_kps, geom, mp_desc, mp_state, claimed
+
+
+def triangulation_case(H: np.ndarray, n1: int, n2: int, seed: int, w: int = 640, h: int = 480):
+    """Inputs of SearchForTriangulation for a frame pair related by the
+    homography H (x2 = H x1): F12 = [e]x H^-1 for a random epipole e, which
+    every true correspondence satisfies (x1^T F12 x2 = 0); pKF1's camera
+    centre and pKF2's pose / camera placing the epipole in pKF2 inside the
+    image; a third of the features carrying map points; a quarter stereo.
+    Returns (Cw1, T2 (3, 4), K2 (fx, fy, cx, cy), F12 (3, 3), mp1, mp2, ur1,
+    ur2) as float32 / uint8 arrays."""
+    rng = np.random.default_rng(seed)
+    e = np.array([rng.uniform(0, w), rng.uniform(0, h), 1.0])
+    ex = np.array([[0, -e[2], e[1]], [e[2], 0, -e[0]], [-e[1], e[0], 0]])
+    F12 = (ex @ np.linalg.inv(H)).astype(np.float64)
+    F12 /= np.abs(F12).max()
+    R2 = _rotation(*rng.normal(0, 0.1, 3))
+    t2 = rng.normal(0, 0.5, 3)
+    T2 = np.hstack([R2, t2[:, None]]).astype(np.float32)
+    K2 = np.array([500.0, 500.0, w / 2, h / 2], np.float32)
+    # pKF1's centre: a point that pKF2 sees at a random pixel, depth 5-20
+    z = rng.uniform(5, 20)
+    pc = np.array([(rng.uniform(0, w) - w / 2) / 500.0 * z, (rng.uniform(0, h) - h / 2) / 500.0 * z, z])
+    Cw1 = (R2.T @ (pc - t2)).astype(np.float32)
+    mp1 = (rng.random(n1) < 0.33).astype(np.uint8)
+    mp2 = (rng.random(n2) < 0.33).astype(np.uint8)
+    ur1 = np.where(rng.random(n1) < 0.25, rng.uniform(0, w, n1), -1.0).astype(np.float32)
+    ur2 = np.where(rng.random(n2) < 0.25, rng.uniform(0, w, n2), -1.0).astype(np.float32)
+    return Cw1, T2, K2, F12.astype(np.float32), mp1, mp2, ur1, ur2

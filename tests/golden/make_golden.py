@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri")
 
 
 def main(groups=GROUPS):
@@ -59,6 +59,8 @@ def main(groups=GROUPS):
         search_by_bow_fixture(R)
     if "reloc" in groups:
         reloc_fixture(R)
+    if "tri" in groups:
+        triangulation_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -377,6 +379,41 @@ def reloc_fixture(R):
             arrays[pre + f"nm_{k}"] = np.array(nm)
             arrays[pre + f"match_{k}"] = match
     save("reloc_search.npz", **arrays)
+
+
+def triangulation_fixture(R):
+    # 15. ORBmatcher::SearchForTriangulation on two scene pairs (F12 from the
+    # pair's homography and a random epipole)
+    import tempfile
+    voc = syn.vocabulary(10, 4, 5)
+    s, _ = pyoracle.scale_tables(8, 1.2)
+    scale = np.array(s, np.float32)
+    sigma2 = (scale * scale).astype(np.float32)
+    arrays = {"scale": scale, "sigma2": sigma2}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "voc.txt")
+        syn.write_vocabulary_text(voc, path)
+        R.vocabulary_load(path)
+        for sc in range(2):
+            f1, f2, H = syn.frame_pair(640, 480, 80 + sc)
+            a, b = R.extract(f1, nfeatures=1500), R.extract(f2, nfeatures=1500)
+            fa, fb = R.bow_transform(path, a.descriptors, 2), R.bow_transform(path, b.descriptors, 2)
+            Cw1, T2, K2, F12, mp1, mp2, ur1, ur2 = syn.triangulation_case(H, len(a.keypoints), len(b.keypoints), sc)
+            pre = f"s{sc}_"
+            arrays.update({pre + "kps1": a.keypoints, pre + "desc1": a.descriptors, pre + "kps2": b.keypoints,
+                           pre + "desc2": b.descriptors, pre + "mp1": mp1, pre + "mp2": mp2, pre + "ur1": ur1,
+                           pre + "ur2": ur2, pre + "Cw1": Cw1, pre + "T2": T2, pre + "K2": K2, pre + "F12": F12})
+            for side, fv in (("1", fa), ("2", fb)):
+                for key in ("fv_nodes", "fv_offsets", "fv_features"):
+                    arrays[pre + key + side] = fv[key]
+            for k, (st, ori) in enumerate(((False, True), (True, False))):
+                nm, match = R.search_for_triangulation(
+                    a.keypoints, a.descriptors, mp1, ur1, (fa["fv_nodes"], fa["fv_offsets"], fa["fv_features"]),
+                    b.keypoints, b.descriptors, mp2, ur2, (fb["fv_nodes"], fb["fv_offsets"], fb["fv_features"]),
+                    Cw1, T2, K2, F12, scale, sigma2, st, ori)
+                arrays[pre + f"nm_{k}"] = np.array(nm)
+                arrays[pre + f"match_{k}"] = match
+    save("triangulation.npz", **arrays)
 
 
 if __name__ == "__main__":

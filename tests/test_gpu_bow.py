@@ -218,3 +218,58 @@ def test_search_by_bow_keyframes_vs_oracle(torch, oracle, check_ori, ratio):
         assert int(nm[p]) == ref_nm, p
         assert np.array_equal(matches[p].cpu().numpy(), ref), p
         assert ref_nm > 50
+
+
+@pytest.mark.parametrize("only_stereo,check_ori", [(False, True), (False, False), (True, True)])
+def test_search_for_triangulation_vs_oracle(torch, oracle, only_stereo, check_ori):
+    """SearchForTriangulation for 6 keyframe pairs (both directions of 3 scenes)."""
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import Vocabulary, search_for_triangulation
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    voc = syn.vocabulary(10, 4, 5)
+    oracle.vocabulary_from_arrays("tri", voc)
+    V = Vocabulary.from_arrays(10, 4, 0, 0, voc["parents"], voc["is_leaf"], voc["descriptors"], voc["weights"])
+    ents, Hs = [], []
+    for seed in range(3):
+        f1, f2, H = syn.frame_pair(640, 480, 60 + seed)
+        ents += [oracle.extract(f1, nfeatures=1500), oracle.extract(f2, nfeatures=1500)]
+        Hs += [H, np.linalg.inv(H)]
+    offs = np.zeros(len(ents) + 1, np.int32)
+    offs[1:] = np.cumsum([len(e.keypoints) for e in ents])
+    kps = np.concatenate([e.keypoints for e in ents])
+    desc = np.concatenate([e.descriptors for e in ents])
+    pairs = [(2 * s, 2 * s + 1) for s in range(3)] + [(2 * s + 1, 2 * s) for s in range(3)]
+    mp = np.zeros(len(kps), np.uint8)
+    ur = np.zeros(len(kps), np.float32)
+    geos = []
+    for p, (a, b) in enumerate(pairs):
+        Cw1, T2, K2, F12, mp1, mp2, ur1, ur2 = syn.triangulation_case(Hs[a], int(offs[a + 1] - offs[a]),
+                                                                      int(offs[b + 1] - offs[b]), 500 + p)
+        if p < 3:  # map points / stereo flags once per entry
+            mp[offs[a]:offs[a + 1]], mp[offs[b]:offs[b + 1]] = mp1, mp2
+            ur[offs[a]:offs[a + 1]], ur[offs[b]:offs[b + 1]] = ur1, ur2
+        geos.append((Cw1, T2, K2, F12))
+    s, _ = pyoracle.scale_tables(8, 1.2)
+    scale = np.array(s, np.float32)
+    sigma2 = scale * scale
+    K = torch.from_numpy(kps.view(np.float32).reshape(-1, 7).copy()).cuda()
+    D = torch.from_numpy(desc).cuda()
+    O = torch.from_numpy(offs).cuda()
+    bow = V.transform(D, O, 2)
+    nm, matches = search_for_triangulation(K, D, O, bow, torch.from_numpy(mp).cuda(), torch.from_numpy(ur).cuda(),
+                                           pairs, geos, scale, sigma2, only_stereo, check_ori)
+    torch.cuda.synchronize()
+    total = 0
+    for p, (a, b) in enumerate(pairs):
+        fa = oracle.bow_transform("tri", ents[a].descriptors, 2)
+        fb = oracle.bow_transform("tri", ents[b].descriptors, 2)
+        Cw1, T2, K2, F12 = geos[p]
+        ref_nm, ref = oracle.search_for_triangulation(
+            ents[a].keypoints, ents[a].descriptors, mp[offs[a]:offs[a + 1]], ur[offs[a]:offs[a + 1]],
+            (fa["fv_nodes"], fa["fv_offsets"], fa["fv_features"]), ents[b].keypoints, ents[b].descriptors,
+            mp[offs[b]:offs[b + 1]], ur[offs[b]:offs[b + 1]], (fb["fv_nodes"], fb["fv_offsets"], fb["fv_features"]),
+            Cw1, T2, K2, F12, scale, sigma2, only_stereo, check_ori)
+        assert int(nm[p]) == ref_nm, p
+        assert np.array_equal(matches[p].cpu().numpy(), ref), p
+        total += ref_nm
+    assert total > 30

@@ -309,3 +309,19 @@ def test_search_by_projection_keyframe_golden(oracle, golden, sc):
                                                    g[pre + "mp_state"], th, od, ori, g[pre + "claimed"])
         assert nm == int(g[pre + f"nm_{k}"])
         assert np.array_equal(np.where(match == -4, -1, match), g[pre + f"match_{k}"])
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_search_for_triangulation_golden(oracle, golden, sc):
+    """ORBmatcher::SearchForTriangulation against the reference's outputs."""
+    g = golden("triangulation.npz")
+    pre = f"s{sc}_"
+    fv1 = tuple(g[pre + k + "1"] for k in ("fv_nodes", "fv_offsets", "fv_features"))
+    fv2 = tuple(g[pre + k + "2"] for k in ("fv_nodes", "fv_offsets", "fv_features"))
+    for k, (st, ori) in enumerate(((False, True), (True, False))):
+        nm, match = oracle.search_for_triangulation(
+            g[pre + "kps1"], g[pre + "desc1"], g[pre + "mp1"], g[pre + "ur1"], fv1, g[pre + "kps2"], g[pre + "desc2"],
+            g[pre + "mp2"], g[pre + "ur2"], fv2, g[pre + "Cw1"], g[pre + "T2"], g[pre + "K2"], g[pre + "F12"],
+            g["scale"], g["sigma2"], st, ori)
+        assert nm == int(g[pre + f"nm_{k}"])
+        assert np.array_equal(match, g[pre + f"match_{k}"])
