@@ -363,6 +363,23 @@ int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orbgpu_frame* 
                                          const uint8_t* usable, int n_kf, float th, int orbdist,
                                          const uint8_t* claimed, int* match_out, int mem, int* nmatches);
 
+/* ORBmatcher::SearchByProjection(KeyFrame* pKF, cv::Mat Scw, const
+ * vector<MapPoint*>& vpPoints, vector<MapPoint*>& vpMatched, int th) --
+ * src/ORBmatcher.cc:423-560 (loop closing).  keyframe: pKF's keypoints and
+ * descriptors (image bounds 0..width x 0..height); Scw: rows 0-2 of the Sim3
+ * (row-major 3 x 4, scale in the rotation block); fx..cy, scale_factor,
+ * nlevels: pKF's camera and pyramid.  points / point_descriptors: vpPoints
+ * (position, normal, distances; GetDescriptor()); usable[i] = 1 where
+ * vpPoints[i] is not bad and not already in vpMatched.  matched:
+ * keyframe->n bytes, non-zero where vpMatched[i] is set before the call
+ * (NULL = none).  match_out: keyframe->n ints: >= 0 the vpPoints index now in
+ * vpMatched[i], -2 set before, -1 none.  Host or device memory per 'mem'. */
+int orbgpu_search_by_projection_sim3(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Scw, float fx,
+                                     float fy, float cx, float cy, float scale_factor, int nlevels,
+                                     const orbgpu_mappoint_geometry* points, const uint8_t* point_descriptors,
+                                     const uint8_t* usable, int npoints, int th, const uint8_t* matched,
+                                     int* match_out, int mem, int* nmatches);
+
 /* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
  * indexed like LastFrame's keypoints. */
 typedef struct {

@@ -78,6 +78,13 @@ int orc_search_for_triangulation(const orc_kp* kps1, const uint8_t* desc1, const
                                   const float* Cw1, const float* T2, const float* K2, const float* F12,
                                   const float* scale, const float* sigma2, int only_stereo, int check_ori,
                                   int* match_out);
+/* ORBmatcher::SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th)
+ * (src/ORBmatcher.cc:423-560).  Scw: rows 0-2 (3 x 4); cam: fx, fy, cx, cy;
+ * pstate: 1 usable, 2 bad. */
+int orc_search_by_projection_sim3(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                                  const float* Scw, const float* cam, const orc_mp_geometry* pts,
+                                  const uint8_t* pdesc, const uint8_t* pstate, int npts, int th,
+                                  const uint8_t* claimed, int* match_out);
 /* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
  * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
  * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:

@@ -311,6 +311,27 @@ class _Base:
                _p(mpd), _p(st), C.c_float(th), int(orbdist), int(bool(check_ori)), _p(cl), _p(out))
         return int(nm), out[:len(kps)].copy()
 
+    def search_by_projection_sim3(self, kps, desc, w, h, Scw, cam, pts, pdesc, pstate, th=10, claimed=None,
+                                  nlevels=8, scale_factor=1.2):
+        """SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th) ->
+        (nmatches, match_out per keyframe keypoint)."""
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        desc = np.ascontiguousarray(desc, np.uint8)
+        S = np.ascontiguousarray(np.asarray(Scw, np.float32).reshape(-1)[:12])
+        cm = np.ascontiguousarray(cam, np.float32)
+        pts = np.ascontiguousarray(pts, GEOM_DTYPE)
+        pd = np.ascontiguousarray(pdesc, np.uint8)
+        ps = np.ascontiguousarray(pstate, np.uint8)
+        cl = None if claimed is None else np.ascontiguousarray(claimed, np.uint8)
+        out = np.zeros(max(len(kps), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("search_by_projection_sim3")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        nm = f(C.byref(p), _p(kps), _p(desc), len(kps), w, h, _p(S), _p(cm), _p(pts), _p(pd), _p(ps), len(pts),
+               int(th), _p(cl), _p(out))
+        return int(nm), out[:len(kps)].copy()
+
     def search_for_triangulation(self, kps1, desc1, mp1, ur1, fv1, kps2, desc2, mp2, ur2, fv2, Cw1, T2, K2, F12,
                                  scale, sigma2, only_stereo=False, check_ori=True):
         """SearchForTriangulation(pKF1, pKF2, F12, pairs, bOnlyStereo) ->

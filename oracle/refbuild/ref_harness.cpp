@@ -835,6 +835,65 @@ int ref_search_for_triangulation(const orc_kp* kps1, const uint8_t* desc1, const
     return nm;
 }
 
+// ORBmatcher::SearchByProjection(KeyFrame* pKF, Scw, vpPoints, vpMatched, th)
+// -- src/ORBmatcher.cc:423-560, on a keyframe built from a frame of the
+// given keypoints (grid, bounds 0..w x 0..h); claimed keypoints hold other
+// map points in vpMatched.  match_out as orc_search_by_projection_sim3.
+int ref_search_by_projection_sim3(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                                  const float* Scw, const float* cam, const orc_mp_geometry* pts,
+                                  const uint8_t* pdesc, const uint8_t* pstate, int npts, int th,
+                                  const uint8_t* claimed, int* match_out) {
+    ArenaScope scope;
+    int nm;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame::fx = cam[0];
+        Frame::fy = cam[1];
+        Frame::cx = cam[2];
+        Frame::cy = cam[3];
+        Frame* F = make_frame(&ext, kps, desc, n, w, h, nullptr);
+        F->mfLogScaleFactor = std::log(F->mfScaleFactor);
+        MapPointMaker maker;
+        KeyFrame* KF = new KeyFrame(*F, maker.map, nullptr);
+        cv::Mat zero = cv::Mat::zeros(3, 1, CV_32F);
+        MapPoint* outside = maker.make(zero, 1);
+        std::vector<MapPoint*> matched(n, static_cast<MapPoint*>(NULL));
+        for (int i = 0; i < n; i++)
+            if (claimed && claimed[i]) matched[i] = outside;
+        std::vector<MapPoint*> points(npts);
+        std::map<MapPoint*, int> index;
+        for (int i = 0; i < npts; i++) {
+            cv::Mat pos(3, 1, CV_32F);
+            pos.at<float>(0) = pts[i].x;
+            pos.at<float>(1) = pts[i].y;
+            pos.at<float>(2) = pts[i].z;
+            MapPoint* mp = maker.make(pos, 1);
+            mp->mNormalVector = cv::Mat(3, 1, CV_32F);
+            mp->mNormalVector.at<float>(0) = pts[i].nx;
+            mp->mNormalVector.at<float>(1) = pts[i].ny;
+            mp->mNormalVector.at<float>(2) = pts[i].nz;
+            mp->mfMinDistance = pts[i].min_distance;
+            mp->mfMaxDistance = pts[i].max_distance;
+            mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+            std::memcpy(mp->mDescriptor.data, pdesc + (size_t)i * 32, 32);
+            mp->mbBad = pstate[i] == 2;
+            points[i] = mp;
+            index[mp] = i;
+        }
+        cv::Mat S = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) S.at<float>(r, c) = Scw[4 * r + c];
+        ORBmatcher matcher(0.9f, true);
+        nm = matcher.SearchByProjection(KF, S, points, matched, th);
+        for (int i = 0; i < n; i++)
+            match_out[i] = matched[i] == nullptr ? -1 : matched[i] == outside ? -2 : index[matched[i]];
+        for (MapPoint* mp : points) delete mp;
+        delete KF;
+        delete F;
+    }
+    return nm;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

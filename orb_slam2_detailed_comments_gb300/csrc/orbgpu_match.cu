@@ -552,6 +552,10 @@ struct KeyframeProjDev {
     int nlevels;
     float level_above[15];
     int orbdist;
+    // 1: SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th)
+    // (src/ORBmatcher.cc:423-560): depth test, IsInImage bounds, viewing angle,
+    // levels level - 1 .. level, u = fx * (x * invz) + cx
+    int sim3;
 };
 
 __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_mappoint_geometry* mps,
@@ -569,11 +573,19 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
         const float xc = pose_row(kp.T, mp.x, mp.y, mp.z);
         const float yc = pose_row(kp.T + 4, mp.x, mp.y, mp.z);
         const float zc = pose_row(kp.T + 8, mp.x, mp.y, mp.z);
-        const float invzc = __double2float_rn(__ddiv_rn(1.0, (double)zc));
-        u = __fadd_rn(__fmul_rn(__fmul_rn(kp.fx, xc), invzc), kp.cx);
-        v = __fadd_rn(__fmul_rn(__fmul_rn(kp.fy, yc), invzc), kp.cy);
-        // a non-finite projection finds no grid cell in the reference
-        live = isfinite(u) && isfinite(v) && !(u < g.minX || u > kp.maxX) && !(v < g.minY || v > kp.maxY);
+        if (kp.sim3) {
+            const float invz = __fdiv_rn(1.0f, zc);
+            u = __fadd_rn(__fmul_rn(kp.fx, __fmul_rn(xc, invz)), kp.cx);
+            v = __fadd_rn(__fmul_rn(kp.fy, __fmul_rn(yc, invz)), kp.cy);
+            // KeyFrame::IsInImage (upper bounds exclusive); NaN fails it
+            live = !(zc < 0.0f) && u >= g.minX && u < kp.maxX && v >= g.minY && v < kp.maxY;
+        } else {
+            const float invzc = __double2float_rn(__ddiv_rn(1.0, (double)zc));
+            u = __fadd_rn(__fmul_rn(__fmul_rn(kp.fx, xc), invzc), kp.cx);
+            v = __fadd_rn(__fmul_rn(__fmul_rn(kp.fy, yc), invzc), kp.cy);
+            // a non-finite projection finds no grid cell in the reference
+            live = isfinite(u) && isfinite(v) && !(u < g.minX || u > kp.maxX) && !(v < g.minY || v > kp.maxY);
+        }
         if (live) {
             const float po0 = __fsub_rn(mp.x, kp.Ow[0]), po1 = __fsub_rn(mp.y, kp.Ow[1]),
                         po2 = __fsub_rn(mp.z, kp.Ow[2]);
@@ -582,6 +594,13 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
             ss = __dadd_rn(ss, __dmul_rn((double)po2, (double)po2));
             const float dist = (float)__dsqrt_rn(ss);
             live = !(dist < __fmul_rn(0.8f, mp.min_distance) || dist > __fmul_rn(1.2f, mp.max_distance));
+            if (live && kp.sim3) {
+                // PO.dot(Pn) < 0.5 * dist, in double
+                double dp = __dmul_rn((double)po0, (double)mp.nx);
+                dp = __dadd_rn(dp, __dmul_rn((double)po1, (double)mp.ny));
+                dp = __dadd_rn(dp, __dmul_rn((double)po2, (double)mp.nz));
+                live = !(dp < __dmul_rn(0.5, (double)dist));
+            }
             const float ratio = __fdiv_rn(mp.max_distance, dist);
             for (int n = 0; n < kp.nlevels - 1; n++) level += ratio > kp.level_above[n] ? 1 : 0;
         }
@@ -593,7 +612,7 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
             const uint8_t* dmp = mp_desc + (size_t)i * 32;
             warp_window_keys(g.cell_start, g.cell_keys, g.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1,
                              [&](int idx, int c, bool valid) {
-                bool ok = valid && in_area(g, idx, u, v, radius, level - 1, level + 1);
+                bool ok = valid && in_area(g, idx, u, v, radius, level - 1, kp.sim3 ? level : level + 1);
                 int dist = 256;
                 if (ok) {
                     dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
@@ -1392,6 +1411,11 @@ extern "C" int orbgpu_search_by_projection_frame(orbgpu_matcher* m, const orbgpu
     return ORBGPU_ERR_CAPACITY;
 }
 
+static int search_projection_keyframe(orbgpu_matcher* m, const orbgpu_frame* current, const KeyframeProjDev& kp,
+                                      const orbgpu_keypoint* kf_keypoints, const orbgpu_mappoint_geometry* mappoints,
+                                      const uint8_t* mp_descriptors, const uint8_t* usable, int n_kf, float th,
+                                      const uint8_t* claimed, int* match_out, int mem, int* nmatches);
+
 extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orbgpu_frame* current,
                                                     const orbgpu_frustum_frame* pose,
                                                     const orbgpu_keypoint* kf_keypoints,
@@ -1403,8 +1427,6 @@ extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orb
         (n_kf > 0 && (!kf_keypoints || !mappoints || !mp_descriptors || !usable)) || pose->nlevels < 1 ||
         pose->nlevels > 16)
         return ORBGPU_ERR_BAD_ARG;
-    const int n = current->n, M = n_kf;
-    *nmatches = 0;
     KeyframeProjDev kp;
     for (int r = 0; r < 3; r++) {
         for (int c = 0; c < 3; c++) kp.T[4 * r + c] = pose->Rcw[3 * r + c];
@@ -1420,6 +1442,19 @@ extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orb
     kp.nlevels = pose->nlevels;
     std::memcpy(kp.level_above, pose->level_above, sizeof(kp.level_above));
     kp.orbdist = orbdist;
+    kp.sim3 = 0;
+    return search_projection_keyframe(m, current, kp, kf_keypoints, mappoints, mp_descriptors, usable, n_kf, th,
+                                      claimed, match_out, mem, nmatches);
+}
+
+// The candidate lists and in-order resolution shared by the relocalisation
+// and the loop-closing projection searches.
+static int search_projection_keyframe(orbgpu_matcher* m, const orbgpu_frame* current, const KeyframeProjDev& kp,
+                                      const orbgpu_keypoint* kf_keypoints, const orbgpu_mappoint_geometry* mappoints,
+                                      const uint8_t* mp_descriptors, const uint8_t* usable, int n_kf, float th,
+                                      const uint8_t* claimed, int* match_out, int mem, int* nmatches) {
+    const int n = current->n, M = n_kf;
+    *nmatches = 0;
     size_t est = frame_stage_bytes(current) + grid_bytes(n) +
                  (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint_geometry) + sizeof(orbgpu_keypoint) + 32 + 1 + 32) +
                  (size_t)std::max(1, n) * 32 + 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 32;
@@ -1443,8 +1478,9 @@ extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orb
             uint8_t* dd = b.take<uint8_t>((size_t)std::max(1, M) * 32);
             uint8_t* uu = b.take<uint8_t>(std::max(1, M));
             if (M) {
-                ORBGPU_CUDA_TRY(cudaMemcpyAsync(k, kf_keypoints, sizeof(orbgpu_keypoint) * M, cudaMemcpyHostToDevice,
-                                                m->stream));
+                if (kf_keypoints)
+                    ORBGPU_CUDA_TRY(cudaMemcpyAsync(k, kf_keypoints, sizeof(orbgpu_keypoint) * M,
+                                                    cudaMemcpyHostToDevice, m->stream));
                 ORBGPU_CUDA_TRY(cudaMemcpyAsync(a, mappoints, sizeof(orbgpu_mappoint_geometry) * M,
                                                 cudaMemcpyHostToDevice, m->stream));
                 ORBGPU_CUDA_TRY(cudaMemcpyAsync(dd, mp_descriptors, 32 * (size_t)M, cudaMemcpyHostToDevice,
@@ -1496,8 +1532,9 @@ extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orb
                 k_pf_round<<<(warps + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(n, M, start, count, keys, nullptr, r,
                                                                               claims3, res, changed, d_match);
             k_pf_serial<<<1, 32, 0, m->stream>>>(n, M, start, count, keys, nullptr, changed, res, claims3, d_match);
-            k_pf_finish<<<1, 1024, 0, m->stream>>>(n, M, res, d_kk, s.kps, m->check_ori, owner, bin_of, nulled, d_match,
-                                                   d_nm);
+            // the loop-closing search has no rotation check
+            k_pf_finish<<<1, 1024, 0, m->stream>>>(n, M, res, d_kk, s.kps, kp.sim3 ? 0 : m->check_ori, owner, bin_of,
+                                                   nulled, d_match, d_nm);
         }
         ORBGPU_CUDA_TRY(cudaGetLastError());
         if (mem != ORBGPU_MEM_DEVICE && n > 0)
@@ -1508,6 +1545,50 @@ extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orb
         return ORBGPU_OK;
     }
     return ORBGPU_ERR_CAPACITY;
+}
+
+extern "C" int orbgpu_search_by_projection_sim3(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Scw,
+                                                float fx, float fy, float cx, float cy, float scale_factor,
+                                                int nlevels, const orbgpu_mappoint_geometry* points,
+                                                const uint8_t* point_descriptors, const uint8_t* usable, int npoints,
+                                                int th, const uint8_t* matched, int* match_out, int mem,
+                                                int* nmatches) {
+    if (!m || !frame_ok(keyframe) || !Scw || npoints < 0 || npoints >= (1 << 20) || !match_out || !nmatches ||
+        (npoints > 0 && (!points || !point_descriptors || !usable)) || nlevels < 1 || nlevels > 16 ||
+        !(scale_factor > 1.0f))
+        return ORBGPU_ERR_BAD_ARG;
+    // Scw = [s R | s t]: s = sqrt(row 0 . row 0) (a double dot product, the
+    // root rounded to float), R and t divided by it as floats, Ow = -R^T t
+    // (src/ORBmatcher.cc:436-442)
+    double d = 0.0;
+    for (int k = 0; k < 3; k++) d += (double)Scw[k] * (double)Scw[k];
+    const float scw = (float)std::sqrt(d);
+    KeyframeProjDev kp;
+    std::memset(&kp, 0, sizeof(kp));
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) kp.T[4 * r + c] = Scw[4 * r + c] / scw;
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (double)(-kp.T[4 * k + i]) * (double)kp.T[4 * k + 3];
+        kp.Ow[i] = (float)s;
+    }
+    kp.fx = fx;
+    kp.fy = fy;
+    kp.cx = cx;
+    kp.cy = cy;
+    kp.maxX = (float)keyframe->width;
+    kp.maxY = (float)keyframe->height;
+    // MapPoint::PredictScale(dist, KeyFrame*): the thresholds of the frame version
+    orbgpu_frustum_frame tmp;
+    const float eye[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    int rc = orbgpu_frustum_frame_init(eye, fx, fy, cx, cy, 0, 0, 1, 0, 1, scale_factor, nlevels, &tmp);
+    if (rc) return rc;
+    kp.nlevels = nlevels;
+    std::memcpy(kp.level_above, tmp.level_above, sizeof(kp.level_above));
+    kp.orbdist = ORBGPU_TH_LOW;
+    kp.sim3 = 1;
+    return search_projection_keyframe(m, keyframe, kp, nullptr, points, point_descriptors, usable, npoints, (float)th,
+                                      matched, match_out, mem, nmatches);
 }
 
 extern "C" int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* left,

@@ -196,6 +196,38 @@ class ORBmatcher:
               "orbgpu_search_by_projection_keyframe")
         return nm.value, out[:s.n]
 
+    def SearchByProjectionSim3(self, KF: FrameView, Scw, fx, fy, cx, cy, points, point_descriptors, usable, th: int,
+                               matched=None, scale_factor: float = 1.2, nlevels: int = 8):
+        """SearchByProjection(KeyFrame* pKF, cv::Mat Scw, vpPoints, vpMatched, th)
+        -- src/ORBmatcher.cc:423-560 (loop closing).  KF: the keyframe's
+        keypoints / descriptors; Scw rows 0-2; points (MAPPOINT_GEOMETRY_DTYPE
+        rows incl. normals), point_descriptors, usable (not bad, not already
+        in vpMatched); matched: keypoints whose vpMatched entry is set.
+        Returns (nmatches, match): per keypoint the point index now in
+        vpMatched, -2 set before, -1 none."""
+        s = KF.struct()
+        dev = s.mem == MEM_DEVICE
+        nm = C.c_int(0)
+        S = np.ascontiguousarray(np.asarray(Scw, np.float32).reshape(-1)[:12])
+        if dev:
+            import torch
+            out = torch.empty(max(s.n, 1), dtype=torch.int32, device="cuda")
+            pts, pd, use, cl = points, point_descriptors, usable, matched
+            m = int(pd.shape[0])
+        else:
+            out = np.zeros(max(s.n, 1), np.int32)
+            pts = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 8))
+            pd = np.ascontiguousarray(point_descriptors, np.uint8)
+            use = np.ascontiguousarray(usable, np.uint8)
+            cl = None if matched is None else np.ascontiguousarray(matched, np.uint8)
+            m = len(pd)
+        check(lib().orbgpu_search_by_projection_sim3(self._h, C.byref(s), ptr(S), C.c_float(fx), C.c_float(fy),
+                                                     C.c_float(cx), C.c_float(cy), C.c_float(scale_factor),
+                                                     int(nlevels), ptr(pts), ptr(pd), ptr(use), m, int(th), ptr(cl),
+                                                     ptr(out), MEM_DEVICE if dev else MEM_HOST, C.byref(nm)),
+              "orbgpu_search_by_projection_sim3")
+        return nm.value, out[:s.n]
+
     def _search_by_projection_mappoints(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0,
                                         claimed=None):
         s = F.struct()

@@ -546,3 +546,27 @@ def triangulation_case(H: np.ndarray, n1: int, n2: int, seed: int, w: int = 640,
     ur1 = np.where(rng.random(n1) < 0.25, rng.uniform(0, w, n1), -1.0).astype(np.float32)
     ur2 = np.where(rng.random(n2) < 0.25, rng.uniform(0, w, n2), -1.0).astype(np.float32)
     return Cw1, T2, K2, F12.astype(np.float32), mp1, mp2, ur1, ur2
+
+
+def sim3_case(kps: np.ndarray, desc: np.ndarray, w: int, h: int, seed: int, m: int = 1500):
+    """Inputs of SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th)
+    for a keyframe with keypoints kps / descriptors desc: the map points of
+    relocalisation_case seen through Scw = [s R | s t] (s in 0.5 .. 2), their
+    normals along the viewing ray with noise (a fifth turned away), states
+    usable (1) or bad (2), and a twentieth of the keypoints already matched.
+    Returns (Scw (3, 4) float32, cam, points (m, 8) float32, descriptors,
+    states, claimed)."""
+    rng = np.random.default_rng(seed)
+    Tcw, cam, _, geom, mp_desc, _, claimed = relocalisation_case(kps, desc, w, h, seed, m)
+    s = rng.uniform(0.5, 2.0)
+    Scw = Tcw.astype(np.float64) * s
+    R, t = Tcw[:, :3].astype(np.float64), Tcw[:, 3].astype(np.float64)
+    Ow = -R.T @ t
+    ray = geom[:, :3] - Ow
+    nrm = ray / np.linalg.norm(ray, axis=1, keepdims=True) + rng.normal(0, 0.3, (m, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm[rng.random(m) < 0.2] *= -1.0
+    geom = geom.copy()
+    geom[:, 3:6] = nrm
+    states = np.where(rng.random(m) < 0.1, 2, 1).astype(np.uint8)
+    return Scw.astype(np.float32), cam, geom, mp_desc, states, claimed

@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri", "sim3")
 
 
 def main(groups=GROUPS):
@@ -61,6 +61,8 @@ def main(groups=GROUPS):
         reloc_fixture(R)
     if "tri" in groups:
         triangulation_fixture(R)
+    if "sim3" in groups:
+        sim3_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -414,6 +416,25 @@ def triangulation_fixture(R):
                 arrays[pre + f"nm_{k}"] = np.array(nm)
                 arrays[pre + f"match_{k}"] = match
     save("triangulation.npz", **arrays)
+
+
+def sim3_fixture(R):
+    # 16. ORBmatcher::SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th)
+    from oracle.pyoracle import GEOM_DTYPE
+    arrays = {}
+    for sc in range(2):
+        e = R.extract(syn.scene(640, 480, 95 + sc), nfeatures=1500)
+        Scw, cam, g, pd, ps, cl = syn.sim3_case(e.keypoints, e.descriptors, 640, 480, 95 + sc)
+        geom = np.ascontiguousarray(g).view(GEOM_DTYPE).reshape(-1)
+        pre = f"s{sc}_"
+        arrays.update({pre + "kps": e.keypoints, pre + "desc": e.descriptors, pre + "Scw": Scw, pre + "cam": cam,
+                       pre + "points": g, pre + "pdesc": pd, pre + "pstate": ps, pre + "claimed": cl})
+        for th in (10, 5):
+            nm, match = R.search_by_projection_sim3(e.keypoints, e.descriptors, 640, 480, Scw, cam, geom, pd, ps, th,
+                                                    cl)
+            arrays[pre + f"nm_{th}"] = np.array(nm)
+            arrays[pre + f"match_{th}"] = match
+    save("sim3_search.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -366,3 +366,30 @@ def test_search_by_projection_keyframe_vs_oracle(torch, oracle, seed, th, orbdis
     assert nm == ref_nm
     assert np.array_equal(match, ref)
     assert ref_nm > 300
+
+
+@pytest.mark.parametrize("seed,th,dev", [(0, 10, False), (1, 5, False), (2, 10, True)])
+def test_search_by_projection_sim3_vs_oracle(torch, oracle, seed, th, dev):
+    """SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th), host and
+    device inputs, against the oracle."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    e = oracle.extract(syn.scene(640, 480, 140 + seed), nfeatures=1500)
+    Scw, cam, g, pd, ps, cl = syn.sim3_case(e.keypoints, e.descriptors, 640, 480, 140 + seed)
+    geom = np.ascontiguousarray(g).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    ref_nm, ref = oracle.search_by_projection_sim3(e.keypoints, e.descriptors, 640, 480, Scw, cam, geom, pd, ps, th,
+                                                   cl)
+    usable = (ps == 1).astype(np.uint8)
+    m = ORBmatcher(0.9, True)
+    if dev:
+        kd = torch.from_numpy(e.keypoints.view(np.float32).reshape(-1, 7).copy()).cuda()
+        KF = frame(kd, torch.from_numpy(e.descriptors).cuda(), 640, 480)
+        nm, match = m.SearchByProjectionSim3(KF, Scw, *cam, torch.from_numpy(g).cuda(), torch.from_numpy(pd).cuda(),
+                                             torch.from_numpy(usable).cuda(), th, torch.from_numpy(cl).cuda())
+        match = match.cpu().numpy()
+    else:
+        nm, match = m.SearchByProjectionSim3(frame(e.keypoints, e.descriptors, 640, 480), Scw, *cam, g, pd, usable, th,
+                                             cl)
+    assert nm == ref_nm
+    assert np.array_equal(match, ref)
+    assert ref_nm > 300

@@ -325,3 +325,17 @@ def test_search_for_triangulation_golden(oracle, golden, sc):
             g["scale"], g["sigma2"], st, ori)
         assert nm == int(g[pre + f"nm_{k}"])
         assert np.array_equal(match, g[pre + f"match_{k}"])
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_search_by_projection_sim3_golden(oracle, golden, sc):
+    """SearchByProjection(KeyFrame*, Scw, vpPoints, vpMatched, th) against the reference."""
+    g = golden("sim3_search.npz")
+    pre = f"s{sc}_"
+    geom = np.ascontiguousarray(g[pre + "points"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    for th in (10, 5):
+        nm, match = oracle.search_by_projection_sim3(g[pre + "kps"], g[pre + "desc"], 640, 480, g[pre + "Scw"],
+                                                     g[pre + "cam"], geom, g[pre + "pdesc"], g[pre + "pstate"], th,
+                                                     g[pre + "claimed"])
+        assert nm == int(g[pre + f"nm_{th}"])
+        assert np.array_equal(match, g[pre + f"match_{th}"])
