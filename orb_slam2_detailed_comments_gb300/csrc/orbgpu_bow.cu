@@ -9,7 +9,7 @@
 // tree (TemplatedVocabulary.h:1240-1290: at every level the first child with
 // the least Hamming distance, strict <; the node of level L - levelsup kept
 // for the feature vector; stop at a node without children) and writes the
-// word, its weight and that node.  k_bow_assemble: one block per frame sorts
+// word, its weight and that node.  k_bow_assemble: two blocks per frame sort
 // the kept features (weight > 0) by word and by node in shared memory and
 // writes BowVector (BowVector::addWeight / addIfNotExist, then normalize,
 // BowVector.cpp:40-95) and FeatureVector (FeatureVector::addFeature,
@@ -108,18 +108,19 @@ __global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
     extern __shared__ unsigned long long keys[];
     __shared__ int s_nkept, s_nruns;
     __shared__ double s_norm;
-    const int f = blockIdx.x;
+    // two blocks per frame: pass 0 the BowVector (keys word << 32 | feature),
+    // pass 1 the FeatureVector (node << 32 | feature)
+    const int f = blockIdx.x >> 1, pass = blockIdx.x & 1;
     const int o0 = offsets[f], o1 = offsets[f + 1];
     const int n = o1 - o0;
     if (o0 < 0 || n < 0 || n > BOW_MAX_FEATURES) {
-        if (threadIdx.x == 0) bow_counts[f] = fv_counts[f] = -1;
+        if (threadIdx.x == 0) (pass == 0 ? bow_counts : fv_counts)[f] = -1;
         return;
     }
     int n2 = 1;
     while (n2 < n) n2 <<= 1;
     const unsigned long long pad = ~0ull;
-    // pass 0: BowVector (keys word << 32 | feature), pass 1: FeatureVector
-    for (int pass = 0; pass < 2; pass++) {
+    {
         for (int i = threadIdx.x; i < n2; i += blockDim.x) {
             unsigned long long key = pad;
             if (i < n && weight[o0 + i] > 0.0) {
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
             // the features of every node, in feature order (the sort's low words)
             for (int i = threadIdx.x; i < nk; i += blockDim.x) fv_features[o0 + i] = (int)(keys[i] & 0xffffffffull);
             if (threadIdx.x == 0) fv_counts[f] = nruns;
-            continue;
+            return;
         }
         // normalisation (ScoringObject.h:84-89: L1 for L1 / chi-square / KL /
         // Bhattacharyya, L2 for L2, none for the dot product, where TF divides
@@ -633,7 +634,7 @@ extern "C" int orbgpu_bow_transform(const orbgpu_vocabulary* v, const uint8_t* d
                                                   v->child_desc, v->child_start, v->pos_node, v->node_word,
                                                   v->node_weight, v->L - levelsup, word_ids, weights, node_ids);
     ORBGPU_CUDA_TRY(cudaGetLastError());
-    k_bow_assemble<<<nframes, BOW_ASM_THREADS, BOW_MAX_FEATURES * 8, st>>>(
+    k_bow_assemble<<<2 * nframes, BOW_ASM_THREADS, BOW_MAX_FEATURES * 8, st>>>(
         offsets, word_ids, weights, node_ids, v->weighting, v->scoring, bow_counts, bow_words, bow_values, fv_counts,
         fv_nodes, fv_starts, fv_sizes, fv_features);
     ORBGPU_CUDA_TRY(cudaGetLastError());

@@ -30,6 +30,7 @@ namespace orbgpu {
 
 #define FR_THREADS 256
 #define FR_BLOCKS_PER_SM 4
+#define FR_SMEM_FRAMES 128  // frames staged in shared memory (160 bytes each)
 
 // One camera of the undistortion: the camera matrix entries as doubles,
 // 1/fx and 1/fy, and k1 k2 p1 p2 k3 (k3 = 0 for four coefficients).
@@ -86,12 +87,26 @@ __global__ void __launch_bounds__(FR_THREADS) k_undistort_keypoints(const float*
     }
 }
 
-__global__ void __launch_bounds__(FR_THREADS) k_is_in_frustum(const orbgpu_frustum_frame* __restrict__ frames,
-                                                              int nframes, const int* __restrict__ offsets,
+__global__ void __launch_bounds__(FR_THREADS) k_is_in_frustum(const orbgpu_frustum_frame* frames,
+                                                              int nframes, const int* offsets,
                                                               const orbgpu_mappoint_geometry* __restrict__ mps,
                                                               float cos_limit, orbgpu_mappoint* __restrict__ out,
                                                               int* __restrict__ in_view) {
-    const int first = __ldg(offsets), last = __ldg(offsets + nframes);
+    // the frames and their offsets staged in shared memory (up to
+    // FR_SMEM_FRAMES of them; larger batches read them from global memory)
+    __shared__ orbgpu_frustum_frame s_frames[FR_SMEM_FRAMES];
+    __shared__ int s_off[FR_SMEM_FRAMES + 1];
+    const bool staged = nframes <= FR_SMEM_FRAMES;
+    if (staged) {
+        const int words = nframes * (int)(sizeof(orbgpu_frustum_frame) / 4);
+        for (int k = threadIdx.x; k < words; k += blockDim.x)
+            reinterpret_cast<float*>(s_frames)[k] = reinterpret_cast<const float*>(frames)[k];
+        for (int k = threadIdx.x; k <= nframes; k += blockDim.x) s_off[k] = offsets[k];
+        __syncthreads();
+        frames = s_frames;
+        offsets = s_off;
+    }
+    const int first = offsets[0], last = offsets[nframes];
     if (first < 0) return;
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * FR_THREADS;
@@ -106,7 +121,7 @@ __global__ void __launch_bounds__(FR_THREADS) k_is_in_frustum(const orbgpu_frust
             int lo = 0, hi = nframes - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (__ldg(offsets + mid) <= i) lo = mid;
+                if (offsets[mid] <= i) lo = mid;
                 else hi = mid - 1;
             }
             f = lo;
