@@ -380,6 +380,28 @@ int orbgpu_search_by_projection_sim3(orbgpu_matcher* m, const orbgpu_frame* keyf
                                      const uint8_t* usable, int npoints, int th, const uint8_t* matched,
                                      int* match_out, int mem, int* nmatches);
 
+/* ORBmatcher::Fuse(KeyFrame* pKF, const vector<MapPoint*>& vpMapPoints,
+ * th) -- src/ORBmatcher.cc:1107-1245 -- the search half: for every map point
+ * the keyframe feature it fuses with (target[i], -1 for none; dist[i] its
+ * distance, nullable), i.e. the first feature at the least distance among
+ * those of its window (levels predicted - 1 .. predicted) that pass the
+ * reprojection gate (chi-square 7.8 with mvuRight, 5.99 without), kept when
+ * <= TH_LOW.  The choice does not depend on the other map points; the map
+ * updates it leads to (MapPoint::Replace when the feature holds a map point
+ * that is not bad, else AddObservation / AddMapPoint; the count nFused)
+ * mutate the map and are applied by the caller in vpMapPoints order,
+ * re-checking isBad() and IsInKeyFrame(pKF) at each step as the reference
+ * does.  keyframe: pKF's keypoints, descriptors and mvuRight (uright);
+ * Tcw: rows 0-2 of its pose; fx..bf: its camera; scale_factor, nlevels,
+ * inv_level_sigma2 (nlevels floats, host): its pyramid.  usable[i] = 1 where
+ * vpMapPoints[i] exists, is not bad and not in pKF at the start of the call.
+ * Host or device memory per 'mem'. */
+int orbgpu_fuse_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Tcw, float fx, float fy,
+                           float cx, float cy, float bf, float scale_factor, int nlevels,
+                           const float* inv_level_sigma2, const orbgpu_mappoint_geometry* mappoints,
+                           const uint8_t* mp_descriptors, const uint8_t* usable, int n_mp, float th, int* target,
+                           int* dist, int mem);
+
 /* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
  * indexed like LastFrame's keypoints. */
 typedef struct {

@@ -85,6 +85,12 @@ int orc_search_by_projection_sim3(const orc_params* p, const orc_kp* kps, const 
                                   const float* Scw, const float* cam, const orc_mp_geometry* pts,
                                   const uint8_t* pdesc, const uint8_t* pstate, int npts, int th,
                                   const uint8_t* claimed, int* match_out);
+/* ORBmatcher::Fuse(KeyFrame*, vpMapPoints, th) (src/ORBmatcher.cc:1107-1220):
+ * the keyframe feature each map point fuses with (target), -1 none; returns
+ * the count.  cam: fx, fy, cx, cy, bf; mp_state 1 usable. */
+int orc_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright, int n,
+                          int w, int h, const float* T, const float* cam, const orc_mp_geometry* mps,
+                          const uint8_t* mp_desc, const uint8_t* mp_state, int m, float th, int* target);
 /* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
  * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
  * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:

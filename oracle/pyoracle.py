@@ -332,6 +332,27 @@ class _Base:
                int(th), _p(cl), _p(out))
         return int(nm), out[:len(kps)].copy()
 
+    def fuse_candidates(self, kps, desc, uright, w, h, Tcw, cam, mps, mp_desc, mp_state, th=3.0, nlevels=8,
+                        scale_factor=1.2):
+        """Fuse(KeyFrame*, vpMapPoints, th): the keyframe feature each map point
+        fuses with -> (count, target).  cam: fx, fy, cx, cy, bf."""
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        desc = np.ascontiguousarray(desc, np.uint8)
+        ur = None if uright is None else np.ascontiguousarray(uright, np.float32)
+        T = np.ascontiguousarray(np.asarray(Tcw, np.float32).reshape(-1)[:12])
+        cm = np.ascontiguousarray(cam, np.float32)
+        mps = np.ascontiguousarray(mps, GEOM_DTYPE)
+        mpd = np.ascontiguousarray(mp_desc, np.uint8)
+        st = np.ascontiguousarray(mp_state, np.uint8)
+        out = np.zeros(max(len(mps), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("fuse_candidates")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_void_p]
+        nf = f(C.byref(p), _p(kps), _p(desc), _p(ur), len(kps), w, h, _p(T), _p(cm), _p(mps), _p(mpd), _p(st),
+               len(mps), C.c_float(th), _p(out))
+        return int(nf), out[:len(mps)].copy()
+
     def search_for_triangulation(self, kps1, desc1, mp1, ur1, fv1, kps2, desc2, mp2, ur2, fv2, Cw1, T2, K2, F12,
                                  scale, sigma2, only_stereo=False, check_ori=True):
         """SearchForTriangulation(pKF1, pKF2, F12, pairs, bOnlyStereo) ->

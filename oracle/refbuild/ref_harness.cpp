@@ -894,6 +894,63 @@ int ref_search_by_projection_sim3(const orc_params* p, const orc_kp* kps, const 
     return nm;
 }
 
+// ORBmatcher::Fuse(KeyFrame*, vpMapPoints, th) -- src/ORBmatcher.cc:1107-1245,
+// run on one map point at a time against the keyframe with no map points (so
+// the reference adds the observation): target[i] is the feature where
+// AddMapPoint put map point i, or -1.
+int ref_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright, int n,
+                          int w, int h, const float* T, const float* cam, const orc_mp_geometry* mps,
+                          const uint8_t* mp_desc, const uint8_t* mp_state, int m, float th, int* target) {
+    ArenaScope scope;
+    int nf = 0;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame::fx = cam[0];
+        Frame::fy = cam[1];
+        Frame::cx = cam[2];
+        Frame::cy = cam[3];
+        Frame* F = make_frame(&ext, kps, desc, n, w, h, uright);
+        F->mfLogScaleFactor = std::log(F->mfScaleFactor);
+        F->mbf = cam[4];
+        MapPointMaker maker;
+        KeyFrame* KF = new KeyFrame(*F, maker.map, nullptr);
+        KF->Tcw = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) KF->Tcw.at<float>(r, c) = T[4 * r + c];
+        // Ow = -Rcw' tcw as KeyFrame::SetPose computes it
+        cv::Mat Rcw = KF->Tcw.rowRange(0, 3).colRange(0, 3);
+        cv::Mat tcw = KF->Tcw.rowRange(0, 3).col(3);
+        KF->Ow = -Rcw.t() * tcw;
+        ORBmatcher matcher(0.6f, true);
+        for (int i = 0; i < m; i++) {
+            target[i] = -1;
+            if (mp_state[i] != 1) continue;
+            cv::Mat pos(3, 1, CV_32F);
+            pos.at<float>(0) = mps[i].x;
+            pos.at<float>(1) = mps[i].y;
+            pos.at<float>(2) = mps[i].z;
+            MapPoint* mp = maker.make(pos, 0);
+            mp->mNormalVector = cv::Mat(3, 1, CV_32F);
+            mp->mNormalVector.at<float>(0) = mps[i].nx;
+            mp->mNormalVector.at<float>(1) = mps[i].ny;
+            mp->mNormalVector.at<float>(2) = mps[i].nz;
+            mp->mfMinDistance = mps[i].min_distance;
+            mp->mfMaxDistance = mps[i].max_distance;
+            mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+            std::memcpy(mp->mDescriptor.data, mp_desc + (size_t)i * 32, 32);
+            KF->mvpMapPoints.assign(n, static_cast<MapPoint*>(NULL));
+            std::vector<MapPoint*> one(1, mp);
+            nf += matcher.Fuse(KF, one, th);
+            for (int k = 0; k < n; k++)
+                if (KF->mvpMapPoints[k] == mp) target[i] = k;
+            delete mp;
+        }
+        delete KF;
+        delete F;
+    }
+    return nf;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

@@ -34,9 +34,10 @@ KeyFrame::KeyFrame(Frame& F, Map* pMap, KeyFrameDatabase* pKFDB)
     : mnFrameId(F.mnId), mTimeStamp(0), mnGridCols(FRAME_GRID_COLS), mnGridRows(FRAME_GRID_ROWS),
       mfGridElementWidthInv(F.mfGridElementWidthInv), mfGridElementHeightInv(F.mfGridElementHeightInv), mnTrackReferenceForFrame(0), mnFuseTargetForKF(0), mnBALocalForKF(0),
       mnBAFixedForKF(0), mnLoopQuery(0), mnLoopWords(0), mLoopScore(0), mnRelocQuery(0), mnRelocWords(0),
-      mRelocScore(0), mnBAGlobalForKF(0), fx(F.fx), fy(F.fy), cx(F.cx), cy(F.cy), invfx(0), invfy(0), mbf(0), mb(0),
+      mRelocScore(0), mnBAGlobalForKF(0), fx(F.fx), fy(F.fy), cx(F.cx), cy(F.cy), invfx(0), invfy(0), mbf(F.mbf), mb(0),
       mThDepth(0), N(F.N), mvKeysUn(F.mvKeysUn), mvuRight(F.mvuRight), mDescriptors(F.mDescriptors.clone()),
       mnScaleLevels(F.mnScaleLevels), mvScaleFactors(F.mvScaleFactors), mvLevelSigma2(F.mvLevelSigma2),
+      mvInvLevelSigma2(F.mvInvLevelSigma2),
       mfScaleFactor(F.mfScaleFactor), mfLogScaleFactor(F.mfLogScaleFactor), mnMinX(F.mnMinX), mnMinY(F.mnMinY),
       mnMaxX(F.mnMaxX), mnMaxY(F.mnMaxY), mpKeyFrameDB(pKFDB),
       mpORBvocabulary(nullptr), mbFirstConnection(true), mpParent(nullptr), mbNotErase(false),
@@ -50,7 +51,8 @@ KeyFrame::KeyFrame(Frame& F, Map* pMap, KeyFrameDatabase* pKFDB)
 }
 
 bool KeyFrame::isBad() { return mbBad; }
-void KeyFrame::AddMapPoint(MapPoint*, const size_t&) { stub_unreachable("KeyFrame::AddMapPoint"); }
+// src/KeyFrame.cc: mvpMapPoints[idx] = pMP
+void KeyFrame::AddMapPoint(MapPoint* pMP, const size_t& idx) { mvpMapPoints[idx] = pMP; }
 void KeyFrame::EraseMapPointMatch(const size_t&) { stub_unreachable("KeyFrame::EraseMapPointMatch"); }
 void KeyFrame::EraseMapPointMatch(MapPoint*) { stub_unreachable("KeyFrame::EraseMapPointMatch"); }
 void KeyFrame::ReplaceMapPointMatch(const size_t&, MapPoint*) { stub_unreachable("KeyFrame::ReplaceMapPointMatch"); }

@@ -556,6 +556,11 @@ struct KeyframeProjDev {
     // (src/ORBmatcher.cc:423-560): depth test, IsInImage bounds, viewing angle,
     // levels level - 1 .. level, u = fx * (x * invz) + cx
     int sim3;
+    // with sim3: Fuse(KeyFrame*, vpMapPoints, th) (src/ORBmatcher.cc:1107-1245)
+    // adds the reprojection-error gate of every candidate (stereo with ur)
+    int fuse;
+    float bf;
+    float inv_sigma2[16];
 };
 
 __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_mappoint_geometry* mps,
@@ -566,7 +571,7 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
     if (i >= m) return;
     int total = 0;
     bool live = usable[i] == 1;
-    float u = 0.f, v = 0.f;
+    float u = 0.f, v = 0.f, ur_f = 0.f;
     int level = 0;
     if (live) {
         const orbgpu_mappoint_geometry mp = mps[i];
@@ -577,6 +582,7 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
             const float invz = __fdiv_rn(1.0f, zc);
             u = __fadd_rn(__fmul_rn(kp.fx, __fmul_rn(xc, invz)), kp.cx);
             v = __fadd_rn(__fmul_rn(kp.fy, __fmul_rn(yc, invz)), kp.cy);
+            ur_f = __fsub_rn(u, __fmul_rn(kp.bf, invz));
             // KeyFrame::IsInImage (upper bounds exclusive); NaN fails it
             live = !(zc < 0.0f) && u >= g.minX && u < kp.maxX && v >= g.minY && v < kp.maxY;
         } else {
@@ -613,6 +619,18 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
             warp_window_keys(g.cell_start, g.cell_keys, g.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1,
                              [&](int idx, int c, bool valid) {
                 bool ok = valid && in_area(g, idx, u, v, radius, level - 1, kp.sim3 ? level : level + 1);
+                if (ok && kp.fuse) {
+                    // chi-square gates of Fuse: 7.8 with the right coordinate, 5.99 without
+                    const orbgpu_keypoint& k = g.kps[idx];
+                    const float ex = __fsub_rn(u, k.x), ey = __fsub_rn(v, k.y);
+                    float e2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+                    const bool stereo = g.uright && g.uright[idx] >= 0.0f;
+                    if (stereo) {
+                        const float er = __fsub_rn(ur_f, g.uright[idx]);
+                        e2 = __fadd_rn(e2, __fmul_rn(er, er));
+                    }
+                    ok = !((double)__fmul_rn(e2, kp.inv_sigma2[k.octave & 15]) > (stereo ? 7.8 : 5.99));
+                }
                 int dist = 256;
                 if (ok) {
                     dist = hamming256_ptr(dmp, g.desc + (size_t)idx * 32);
@@ -1428,6 +1446,7 @@ extern "C" int orbgpu_search_by_projection_keyframe(orbgpu_matcher* m, const orb
         pose->nlevels > 16)
         return ORBGPU_ERR_BAD_ARG;
     KeyframeProjDev kp;
+    std::memset(&kp, 0, sizeof(kp));
     for (int r = 0; r < 3; r++) {
         for (int c = 0; c < 3; c++) kp.T[4 * r + c] = pose->Rcw[3 * r + c];
         kp.T[4 * r + 3] = pose->tcw[r];
@@ -1589,6 +1608,124 @@ extern "C" int orbgpu_search_by_projection_sim3(orbgpu_matcher* m, const orbgpu_
     kp.sim3 = 1;
     return search_projection_keyframe(m, keyframe, kp, nullptr, points, point_descriptors, usable, npoints, (float)th,
                                       matched, match_out, mem, nmatches);
+}
+
+// Fuse's choice per map point: the first least distance of its candidates
+// (candidates are already cut at TH_LOW), with no interaction between map
+// points -- the map updates it leads to are applied in order by the caller.
+__global__ void k_fuse_pick(int m, const int* cand_start, const int* cand_count, const uint64_t* cands,
+                            int* target, int* dist_out) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= m) return;
+    uint64_t best = ~0ull;
+    for (int b = lane; b < cand_count[i]; b += 32) {
+        const uint64_t key = cands[cand_start[i] + b];
+        best = key < best ? key : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+        best = ob < best ? ob : best;
+    }
+    if (lane == 0) {
+        target[i] = best == ~0ull ? -1 : (int)(best & 0xFFFFF);
+        if (dist_out) dist_out[i] = best == ~0ull ? 256 : (int)(best >> 40);
+    }
+}
+
+extern "C" int orbgpu_fuse_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Tcw, float fx,
+                                      float fy, float cx, float cy, float bf, float scale_factor, int nlevels,
+                                      const float* inv_level_sigma2, const orbgpu_mappoint_geometry* mappoints,
+                                      const uint8_t* mp_descriptors, const uint8_t* usable, int n_mp, float th,
+                                      int* target, int* dist, int mem) {
+    if (!m || !frame_ok(keyframe) || !Tcw || !inv_level_sigma2 || n_mp < 0 || n_mp >= (1 << 20) || !target ||
+        (n_mp > 0 && (!mappoints || !mp_descriptors || !usable)) || nlevels < 1 || nlevels > 16 ||
+        !(scale_factor > 1.0f))
+        return ORBGPU_ERR_BAD_ARG;
+    KeyframeProjDev kp;
+    std::memset(&kp, 0, sizeof(kp));
+    std::memcpy(kp.T, Tcw, sizeof(kp.T));
+    // Ow = GetCameraCenter() = -Rcw^T tcw
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (double)(-Tcw[4 * k + i]) * (double)Tcw[4 * k + 3];
+        kp.Ow[i] = (float)s;
+    }
+    kp.fx = fx;
+    kp.fy = fy;
+    kp.cx = cx;
+    kp.cy = cy;
+    kp.bf = bf;
+    kp.maxX = (float)keyframe->width;
+    kp.maxY = (float)keyframe->height;
+    orbgpu_frustum_frame tmp;
+    const float eye[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    int rc = orbgpu_frustum_frame_init(eye, fx, fy, cx, cy, 0, 0, 1, 0, 1, scale_factor, nlevels, &tmp);
+    if (rc) return rc;
+    kp.nlevels = nlevels;
+    std::memcpy(kp.level_above, tmp.level_above, sizeof(kp.level_above));
+    for (int l = 0; l < nlevels; l++) kp.inv_sigma2[l] = inv_level_sigma2[l];
+    kp.orbdist = ORBGPU_TH_LOW;
+    kp.sim3 = 1;
+    kp.fuse = 1;
+    const int n = keyframe->n, M = n_mp;
+    size_t est = frame_stage_bytes(keyframe) + grid_bytes(n) +
+                 (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint_geometry) + 32 + 1 + 2 * sizeof(int) + 32) +
+                 64 * 1024 + sizeof(uint64_t) * (size_t)std::max(1, M) * 32;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        rc = ensure_scratch(m, est);
+        if (rc) return rc;
+        Bump b{(uint8_t*)m->scratch, 0, m->scratch_bytes};
+        Staged s;
+        if ((rc = stage_frame(m, keyframe, b, s))) return rc;
+        GridDev g;
+        if ((rc = build_grid(m, keyframe, s, b, g))) return rc;
+        const orbgpu_mappoint_geometry* d_mps = mappoints;
+        const uint8_t* d_mpd = mp_descriptors;
+        const uint8_t* d_use = usable;
+        int* d_t = target;
+        int* d_d = dist;
+        if (mem != ORBGPU_MEM_DEVICE) {
+            orbgpu_mappoint_geometry* a = b.take<orbgpu_mappoint_geometry>(std::max(1, M));
+            uint8_t* dd = b.take<uint8_t>((size_t)std::max(1, M) * 32);
+            uint8_t* uu = b.take<uint8_t>(std::max(1, M));
+            if (M) {
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(a, mappoints, sizeof(orbgpu_mappoint_geometry) * M,
+                                                cudaMemcpyHostToDevice, m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(dd, mp_descriptors, 32 * (size_t)M, cudaMemcpyHostToDevice,
+                                                m->stream));
+                ORBGPU_CUDA_TRY(cudaMemcpyAsync(uu, usable, M, cudaMemcpyHostToDevice, m->stream));
+            }
+            d_mps = a;
+            d_mpd = dd;
+            d_use = uu;
+            d_t = b.take<int>(std::max(1, M));
+            d_d = dist ? b.take<int>(std::max(1, M)) : nullptr;
+        }
+        int *start, *count, total = 0;
+        uint64_t* keys = nullptr;
+        auto launch = [&](const int* st, int* cnt, uint64_t* out, int fill) {
+            const int wpb = 8;
+            if (M > 0)
+                k_pkf_candidates<<<(M + wpb - 1) / wpb, 32 * wpb, 0, m->stream>>>(g, kp, d_mps, d_use, d_mpd, M, th,
+                                                                               st, cnt, out, fill);
+        };
+        rc = candidate_lists(m, M, b, launch, start, count, keys, total);
+        if (rc == ORBGPU_ERR_CAPACITY) {
+            est = est + sizeof(uint64_t) * (size_t)total * 2;
+            continue;
+        }
+        if (rc) return rc;
+        if (M > 0) k_fuse_pick<<<(M + 7) / 8, 256, 0, m->stream>>>(M, start, count, keys, d_t, d_d);
+        ORBGPU_CUDA_TRY(cudaGetLastError());
+        if (mem != ORBGPU_MEM_DEVICE && M > 0) {
+            ORBGPU_CUDA_TRY(cudaMemcpyAsync(target, d_t, sizeof(int) * M, cudaMemcpyDeviceToHost, m->stream));
+            if (dist) ORBGPU_CUDA_TRY(cudaMemcpyAsync(dist, d_d, sizeof(int) * M, cudaMemcpyDeviceToHost, m->stream));
+        }
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(m->stream));
+        return ORBGPU_OK;
+    }
+    return ORBGPU_ERR_CAPACITY;
 }
 
 extern "C" int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* left,

@@ -228,6 +228,38 @@ class ORBmatcher:
               "orbgpu_search_by_projection_sim3")
         return nm.value, out[:s.n]
 
+    def FuseCandidates(self, KF: FrameView, Tcw, fx, fy, cx, cy, bf, inv_level_sigma2, mappoints, mp_descriptors,
+                       usable, th: float = 3.0, scale_factor: float = 1.2, nlevels: int = 8):
+        """The search half of Fuse(KeyFrame* pKF, vpMapPoints, th) --
+        src/ORBmatcher.cc:1107-1245: per map point the keyframe feature it
+        fuses with (-1 none) and the distance.  KF carries pKF's keypoints,
+        descriptors and mvuRight; the map updates (Replace / AddObservation)
+        are applied by the caller in vpMapPoints order.  Host arrays, or CUDA
+        tensors when KF is on the device.  Returns (target, dist)."""
+        s = KF.struct()
+        dev = s.mem == MEM_DEVICE
+        T = np.ascontiguousarray(np.asarray(Tcw, np.float32).reshape(-1)[:12])
+        isg = np.ascontiguousarray(inv_level_sigma2, np.float32)
+        if dev:
+            import torch
+            mps, mpd, use = mappoints, mp_descriptors, usable
+            m = int(mpd.shape[0])
+            target = torch.empty(max(m, 1), dtype=torch.int32, device="cuda")
+            dist = torch.empty(max(m, 1), dtype=torch.int32, device="cuda")
+        else:
+            mps = np.ascontiguousarray(np.asarray(mappoints, np.float32).reshape(-1, 8))
+            mpd = np.ascontiguousarray(mp_descriptors, np.uint8)
+            use = np.ascontiguousarray(usable, np.uint8)
+            m = len(mpd)
+            target = np.zeros(max(m, 1), np.int32)
+            dist = np.zeros(max(m, 1), np.int32)
+        check(lib().orbgpu_fuse_candidates(self._h, C.byref(s), ptr(T), C.c_float(fx), C.c_float(fy), C.c_float(cx),
+                                           C.c_float(cy), C.c_float(bf), C.c_float(scale_factor), int(nlevels),
+                                           ptr(isg), ptr(mps), ptr(mpd), ptr(use), m, C.c_float(th), ptr(target),
+                                           ptr(dist), MEM_DEVICE if dev else MEM_HOST),
+              "orbgpu_fuse_candidates")
+        return target[:m], dist[:m]
+
     def _search_by_projection_mappoints(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0,
                                         claimed=None):
         s = F.struct()

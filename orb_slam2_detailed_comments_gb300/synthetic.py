@@ -570,3 +570,16 @@ def sim3_case(kps: np.ndarray, desc: np.ndarray, w: int, h: int, seed: int, m: i
     geom[:, 3:6] = nrm
     states = np.where(rng.random(m) < 0.1, 2, 1).astype(np.uint8)
     return Scw.astype(np.float32), cam, geom, mp_desc, states, claimed
+
+
+def fuse_case(kps: np.ndarray, desc: np.ndarray, seed: int, w: int = 640, h: int = 480):
+    """Inputs of Fuse(KeyFrame*, vpMapPoints, th) for a keyframe with keypoints
+    kps / descriptors desc: the sim3_case map points seen through the
+    de-scaled pose, bf 40, a third of the keypoints with a right coordinate.
+    Returns (Tcw (3, 4), cam (fx, fy, cx, cy, bf), points (m, 8), descriptors,
+    states, uright)."""
+    Scw, cam, g, pd, ps, _ = sim3_case(kps, desc, w, h, seed)
+    Tcw = (Scw / np.sqrt((Scw[0, :3].astype(np.float64) ** 2).sum())).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    ur = np.where(rng.random(len(kps)) < 0.3, kps["x"] - rng.uniform(1, 40, len(kps)), -1).astype(np.float32)
+    return Tcw, np.array([cam[0], cam[1], cam[2], cam[3], 40.0], np.float32), g, pd, ps, ur

@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri", "sim3")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri", "sim3", "fuse")
 
 
 def main(groups=GROUPS):
@@ -63,6 +63,8 @@ def main(groups=GROUPS):
         triangulation_fixture(R)
     if "sim3" in groups:
         sim3_fixture(R)
+    if "fuse" in groups:
+        fuse_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -435,6 +437,24 @@ def sim3_fixture(R):
             arrays[pre + f"nm_{th}"] = np.array(nm)
             arrays[pre + f"match_{th}"] = match
     save("sim3_search.npz", **arrays)
+
+
+def fuse_fixture(R):
+    # 17. ORBmatcher::Fuse(KeyFrame*, vpMapPoints, th): each map point's choice
+    from oracle.pyoracle import GEOM_DTYPE
+    arrays = {}
+    for sc in range(2):
+        e = R.extract(syn.scene(640, 480, 97 + sc), nfeatures=1500)
+        Tcw, cam5, g, pd, ps, ur = syn.fuse_case(e.keypoints, e.descriptors, 97 + sc)
+        geom = np.ascontiguousarray(g).view(GEOM_DTYPE).reshape(-1)
+        pre = f"s{sc}_"
+        arrays.update({pre + "kps": e.keypoints, pre + "desc": e.descriptors, pre + "ur": ur, pre + "Tcw": Tcw,
+                       pre + "cam": cam5, pre + "points": g, pre + "pdesc": pd, pre + "pstate": ps})
+        for th in (3.0, 5.0):
+            nf, target = R.fuse_candidates(e.keypoints, e.descriptors, ur, 640, 480, Tcw, cam5, geom, pd, ps, th)
+            arrays[pre + f"nf_{int(th)}"] = np.array(nf)
+            arrays[pre + f"target_{int(th)}"] = target
+    save("fuse.npz", **arrays)
 
 
 if __name__ == "__main__":

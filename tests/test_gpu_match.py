@@ -393,3 +393,29 @@ def test_search_by_projection_sim3_vs_oracle(torch, oracle, seed, th, dev):
     assert nm == ref_nm
     assert np.array_equal(match, ref)
     assert ref_nm > 300
+
+
+@pytest.mark.parametrize("seed,th,dev", [(0, 3.0, False), (1, 5.0, True)])
+def test_fuse_candidates_vs_oracle(torch, oracle, seed, th, dev):
+    """The search half of Fuse(KeyFrame*, vpMapPoints, th) against the oracle."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    e = oracle.extract(syn.scene(640, 480, 150 + seed), nfeatures=1500)
+    Tcw, cam5, g, pd, ps, ur = syn.fuse_case(e.keypoints, e.descriptors, 150 + seed)
+    geom = np.ascontiguousarray(g).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    ref_nf, ref = oracle.fuse_candidates(e.keypoints, e.descriptors, ur, 640, 480, Tcw, cam5, geom, pd, ps, th)
+    s, _ = pyoracle.scale_tables(8, 1.2)
+    inv_sigma2 = (1.0 / (np.array(s, np.float32) ** 2)).astype(np.float32)
+    usable = (ps == 1).astype(np.uint8)
+    m = ORBmatcher(0.6, True)
+    if dev:
+        kd = torch.from_numpy(e.keypoints.view(np.float32).reshape(-1, 7).copy()).cuda()
+        KF = frame(kd, torch.from_numpy(e.descriptors).cuda(), 640, 480, torch.from_numpy(ur).cuda())
+        target, _ = m.FuseCandidates(KF, Tcw, *cam5, inv_sigma2, torch.from_numpy(g).cuda(),
+                                     torch.from_numpy(pd).cuda(), torch.from_numpy(usable).cuda(), th)
+        target = target.cpu().numpy()
+    else:
+        KF = frame(e.keypoints, e.descriptors, 640, 480, ur)
+        target, _ = m.FuseCandidates(KF, Tcw, *cam5, inv_sigma2, g, pd, usable, th)
+    assert np.array_equal(target, ref)
+    assert int((target >= 0).sum()) == ref_nf > 300

@@ -339,3 +339,16 @@ def test_search_by_projection_sim3_golden(oracle, golden, sc):
                                                      g[pre + "claimed"])
         assert nm == int(g[pre + f"nm_{th}"])
         assert np.array_equal(match, g[pre + f"match_{th}"])
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_fuse_candidates_golden(oracle, golden, sc):
+    """ORBmatcher::Fuse(KeyFrame*, vpMapPoints, th): every map point's choice against the reference."""
+    g = golden("fuse.npz")
+    pre = f"s{sc}_"
+    geom = np.ascontiguousarray(g[pre + "points"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    for th in (3.0, 5.0):
+        nf, target = oracle.fuse_candidates(g[pre + "kps"], g[pre + "desc"], g[pre + "ur"], 640, 480, g[pre + "Tcw"],
+                                            g[pre + "cam"], geom, g[pre + "pdesc"], g[pre + "pstate"], th)
+        assert nf == int(g[pre + f"nf_{int(th)}"])
+        assert np.array_equal(target, g[pre + f"target_{int(th)}"])
