@@ -402,6 +402,20 @@ int orbgpu_fuse_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe, cons
                            const uint8_t* mp_descriptors, const uint8_t* usable, int n_mp, float th, int* target,
                            int* dist, int mem);
 
+/* ORBmatcher::Fuse(KeyFrame* pKF, cv::Mat Scw, const vector<MapPoint*>&
+ * vpPoints, float th, vector<MapPoint*>& vpReplacePoint) --
+ * src/ORBmatcher.cc:1290-1380 (loop correction) -- the search half: per
+ * point the keyframe feature it fuses with (target, -1 none; dist
+ * nullable), as orbgpu_fuse_candidates but through the de-scaled Sim3 and
+ * without a reprojection gate.  usable[i] = 1 where vpPoints[i] is not bad
+ * and not among pKF->GetMapPoints() at the start.  The caller applies, in
+ * order, vpReplacePoint[i] = GetMapPoint(target) when that is a map point
+ * not bad, else AddObservation / AddMapPoint.  Scw: rows 0-2 of the Sim3. */
+int orbgpu_fuse_sim3_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Scw, float fx,
+                                float fy, float cx, float cy, float scale_factor, int nlevels,
+                                const orbgpu_mappoint_geometry* points, const uint8_t* point_descriptors,
+                                const uint8_t* usable, int npoints, float th, int* target, int* dist, int mem);
+
 /* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
  * indexed like LastFrame's keypoints. */
 typedef struct {

@@ -1048,6 +1048,70 @@ int orc_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* d
     return nf;
 }
 
+// ORBmatcher::Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint),
+// src/ORBmatcher.cc:1290-1380, the choice of every point: the de-scaled Sim3,
+// invz = 1.0 / z (double), no reprojection gate; pstate 1 usable.
+int orc_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                               const float* Scw, const float* cam, const orc_mp_geometry* pts, const uint8_t* pdesc,
+                               const uint8_t* pstate, int npts, float th, int* target) {
+    const Tables t = make_tables(p);
+    Grid* g = new Grid();
+    build_grid(*g, kps, n, w, h);
+    double d = 0;
+    for (int k = 0; k < 3; k++) d += (double)Scw[k] * (double)Scw[k];
+    const float scw = (float)std::sqrt(d);
+    float T[12];
+    for (int k = 0; k < 12; k++) T[k] = Scw[k] / scw;
+    const float tcw[3] = {T[3], T[7], T[11]};
+    float Ow[3];
+    for (int r = 0; r < 3; r++) {
+        const float col[3] = {-T[r], -T[4 + r], -T[8 + r]};
+        Ow[r] = mat_row_dot(col, 1, tcw);
+    }
+    const float log_scale = std::log(p->scale_factor);
+    int nf = 0;
+    for (int i = 0; i < npts; i++) {
+        target[i] = -1;
+        if (pstate[i] != 1) continue;
+        const orc_mp_geometry& mp = pts[i];
+        const float X[3] = {mp.x, mp.y, mp.z};
+        float c[3];
+        for (int r = 0; r < 3; r++) c[r] = mat_row_dot(T + 4 * r, 1, X) + T[4 * r + 3];
+        if (c[2] < 0.0f) continue;
+        const float invz = 1.0 / c[2];
+        const float x = c[0] * invz, y = c[1] * invz;
+        const float u = cam[0] * x + cam[2], v = cam[1] * y + cam[3];
+        if (!(u >= 0.0f && u < (float)w && v >= 0.0f && v < (float)h)) continue;
+        const float PO[3] = {X[0] - Ow[0], X[1] - Ow[1], X[2] - Ow[2]};
+        double ss = 0;
+        for (int k = 0; k < 3; k++) ss += (double)PO[k] * (double)PO[k];
+        const float dist3D = (float)std::sqrt(ss);
+        if (dist3D < 0.8f * mp.min_distance || dist3D > 1.2f * mp.max_distance) continue;
+        const double dot = (double)PO[0] * mp.nx + (double)PO[1] * mp.ny + (double)PO[2] * mp.nz;
+        if (dot < 0.5 * dist3D) continue;
+        int level = (int)std::ceil(std::log(mp.max_distance / dist3D) / log_scale);
+        if (level < 0) level = 0;
+        else if (level >= p->nlevels) level = p->nlevels - 1;
+        const float radius = th * t.scale[level];
+        const std::vector<int> idx = features_in_area(*g, kps, u, v, radius, -1, -1);
+        int bestDist = INT_MAX, best = -1;
+        for (int k : idx) {
+            if (kps[k].octave < level - 1 || kps[k].octave > level) continue;
+            const int dd = hamming(pdesc + (size_t)i * 32, desc + (size_t)k * 32);
+            if (dd < bestDist) {
+                bestDist = dd;
+                best = k;
+            }
+        }
+        if (bestDist <= 50) {
+            target[i] = best;
+            nf++;
+        }
+    }
+    delete g;
+    return nf;
+}
+
 // Frame::ComputeStereoMatches, src/Frame.cc:831-1082 (mb = mbf/fx).
 int orc_compute_stereo_matches(const orc_params* p, const orc_kp* kpsL, const uint8_t* descL, int nL,
                                const orc_kp* kpsR, const uint8_t* descR, int nR, const uint8_t* pyrL,

@@ -91,6 +91,11 @@ int orc_search_by_projection_sim3(const orc_params* p, const orc_kp* kps, const 
 int orc_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, const float* uright, int n,
                           int w, int h, const float* T, const float* cam, const orc_mp_geometry* mps,
                           const uint8_t* mp_desc, const uint8_t* mp_state, int m, float th, int* target);
+/* ORBmatcher::Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint)
+ * (src/ORBmatcher.cc:1290-1380): each point's choice; cam fx, fy, cx, cy. */
+int orc_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                               const float* Scw, const float* cam, const orc_mp_geometry* pts, const uint8_t* pdesc,
+                               const uint8_t* pstate, int npts, float th, int* target);
 /* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
  * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
  * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:

@@ -353,6 +353,26 @@ class _Base:
                len(mps), C.c_float(th), _p(out))
         return int(nf), out[:len(mps)].copy()
 
+    def fuse_sim3_candidates(self, kps, desc, w, h, Scw, cam, pts, pdesc, pstate, th=4.0, nlevels=8,
+                             scale_factor=1.2):
+        """Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint): each point's
+        choice -> (count, target).  cam: fx, fy, cx, cy."""
+        kps = np.ascontiguousarray(kps, KP_DTYPE)
+        desc = np.ascontiguousarray(desc, np.uint8)
+        S = np.ascontiguousarray(np.asarray(Scw, np.float32).reshape(-1)[:12])
+        cm = np.ascontiguousarray(cam, np.float32)
+        pts = np.ascontiguousarray(pts, GEOM_DTYPE)
+        pd = np.ascontiguousarray(pdesc, np.uint8)
+        ps = np.ascontiguousarray(pstate, np.uint8)
+        out = np.zeros(max(len(pts), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("fuse_sim3_candidates")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_void_p]
+        nf = f(C.byref(p), _p(kps), _p(desc), len(kps), w, h, _p(S), _p(cm), _p(pts), _p(pd), _p(ps), len(pts),
+               C.c_float(th), _p(out))
+        return int(nf), out[:len(pts)].copy()
+
     def search_for_triangulation(self, kps1, desc1, mp1, ur1, fv1, kps2, desc2, mp2, ur2, fv2, Cw1, T2, K2, F12,
                                  scale, sigma2, only_stereo=False, check_ori=True):
         """SearchForTriangulation(pKF1, pKF2, F12, pairs, bOnlyStereo) ->

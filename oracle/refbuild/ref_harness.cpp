@@ -951,6 +951,57 @@ int ref_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* d
     return nf;
 }
 
+// ORBmatcher::Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint) --
+// src/ORBmatcher.cc:1290-1380, one point at a time against the keyframe with
+// no map points: target[i] is where AddMapPoint put point i, or -1.
+int ref_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
+                               const float* Scw, const float* cam, const orc_mp_geometry* pts, const uint8_t* pdesc,
+                               const uint8_t* pstate, int npts, float th, int* target) {
+    ArenaScope scope;
+    int nf = 0;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame::fx = cam[0];
+        Frame::fy = cam[1];
+        Frame::cx = cam[2];
+        Frame::cy = cam[3];
+        Frame* F = make_frame(&ext, kps, desc, n, w, h, nullptr);
+        F->mfLogScaleFactor = std::log(F->mfScaleFactor);
+        MapPointMaker maker;
+        KeyFrame* KF = new KeyFrame(*F, maker.map, nullptr);
+        cv::Mat S = cv::Mat::eye(4, 4, CV_32F);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) S.at<float>(r, c) = Scw[4 * r + c];
+        ORBmatcher matcher(0.6f, true);
+        for (int i = 0; i < npts; i++) {
+            target[i] = -1;
+            if (pstate[i] != 1) continue;
+            cv::Mat pos(3, 1, CV_32F);
+            pos.at<float>(0) = pts[i].x;
+            pos.at<float>(1) = pts[i].y;
+            pos.at<float>(2) = pts[i].z;
+            MapPoint* mp = maker.make(pos, 0);
+            mp->mNormalVector = cv::Mat(3, 1, CV_32F);
+            mp->mNormalVector.at<float>(0) = pts[i].nx;
+            mp->mNormalVector.at<float>(1) = pts[i].ny;
+            mp->mNormalVector.at<float>(2) = pts[i].nz;
+            mp->mfMinDistance = pts[i].min_distance;
+            mp->mfMaxDistance = pts[i].max_distance;
+            mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+            std::memcpy(mp->mDescriptor.data, pdesc + (size_t)i * 32, 32);
+            KF->mvpMapPoints.assign(n, static_cast<MapPoint*>(NULL));
+            std::vector<MapPoint*> one(1, mp), replace(1, static_cast<MapPoint*>(NULL));
+            nf += matcher.Fuse(KF, S, one, th, replace);
+            for (int k = 0; k < n; k++)
+                if (KF->mvpMapPoints[k] == mp) target[i] = k;
+            delete mp;
+        }
+        delete KF;
+        delete F;
+    }
+    return nf;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

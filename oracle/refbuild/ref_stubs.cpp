@@ -79,7 +79,13 @@ std::vector<size_t> KeyFrame::GetFeaturesInArea(const float& x, const float& y, 
 }
 MapPoint* KeyFrame::GetMapPoint(const size_t& idx) { return mvpMapPoints[idx]; }
 std::vector<MapPoint*> KeyFrame::GetMapPointMatches() { return mvpMapPoints; }
-std::set<MapPoint*> KeyFrame::GetMapPoints() { stub_unreachable("KeyFrame::GetMapPoints"); }
+// src/KeyFrame.cc: the map points of the keyframe that are not bad
+std::set<MapPoint*> KeyFrame::GetMapPoints() {
+    std::set<MapPoint*> s;
+    for (MapPoint* pMP : mvpMapPoints)
+        if (pMP && !pMP->isBad()) s.insert(pMP);
+    return s;
+}
 cv::Mat KeyFrame::GetRotation() { return Tcw.rowRange(0, 3).colRange(0, 3).clone(); }
 cv::Mat KeyFrame::GetTranslation() { return Tcw.rowRange(0, 3).col(3).clone(); }
 // src/KeyFrame.cc:832-835

@@ -561,6 +561,9 @@ struct KeyframeProjDev {
     int fuse;
     float bf;
     float inv_sigma2[16];
+    // Fuse(KeyFrame*, Scw, ...) (src/ORBmatcher.cc:1290-1380): invz = 1.0 / z
+    // in double, rounded to float
+    int invz_double;
 };
 
 __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_mappoint_geometry* mps,
@@ -579,7 +582,7 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
         const float yc = pose_row(kp.T + 4, mp.x, mp.y, mp.z);
         const float zc = pose_row(kp.T + 8, mp.x, mp.y, mp.z);
         if (kp.sim3) {
-            const float invz = __fdiv_rn(1.0f, zc);
+            const float invz = kp.invz_double ? __double2float_rn(__ddiv_rn(1.0, (double)zc)) : __fdiv_rn(1.0f, zc);
             u = __fadd_rn(__fmul_rn(kp.fx, __fmul_rn(xc, invz)), kp.cx);
             v = __fadd_rn(__fmul_rn(kp.fy, __fmul_rn(yc, invz)), kp.cy);
             ur_f = __fsub_rn(u, __fmul_rn(kp.bf, invz));
@@ -1633,6 +1636,10 @@ __global__ void k_fuse_pick(int m, const int* cand_start, const int* cand_count,
     }
 }
 
+static int fuse_pick_run(orbgpu_matcher* m, const orbgpu_frame* keyframe, const KeyframeProjDev& kp,
+                         const orbgpu_mappoint_geometry* mappoints, const uint8_t* mp_descriptors,
+                         const uint8_t* usable, int n_mp, float th, int* target, int* dist, int mem);
+
 extern "C" int orbgpu_fuse_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Tcw, float fx,
                                       float fy, float cx, float cy, float bf, float scale_factor, int nlevels,
                                       const float* inv_level_sigma2, const orbgpu_mappoint_geometry* mappoints,
@@ -1668,6 +1675,14 @@ extern "C" int orbgpu_fuse_candidates(orbgpu_matcher* m, const orbgpu_frame* key
     kp.orbdist = ORBGPU_TH_LOW;
     kp.sim3 = 1;
     kp.fuse = 1;
+    return fuse_pick_run(m, keyframe, kp, mappoints, mp_descriptors, usable, n_mp, th, target, dist, mem);
+}
+
+// The candidate lists of a fuse search and the choice of every map point.
+static int fuse_pick_run(orbgpu_matcher* m, const orbgpu_frame* keyframe, const KeyframeProjDev& kp,
+                         const orbgpu_mappoint_geometry* mappoints, const uint8_t* mp_descriptors,
+                         const uint8_t* usable, int n_mp, float th, int* target, int* dist, int mem) {
+    int rc;
     const int n = keyframe->n, M = n_mp;
     size_t est = frame_stage_bytes(keyframe) + grid_bytes(n) +
                  (size_t)std::max(1, M) * (sizeof(orbgpu_mappoint_geometry) + 32 + 1 + 2 * sizeof(int) + 32) +
@@ -1726,6 +1741,46 @@ extern "C" int orbgpu_fuse_candidates(orbgpu_matcher* m, const orbgpu_frame* key
         return ORBGPU_OK;
     }
     return ORBGPU_ERR_CAPACITY;
+}
+
+extern "C" int orbgpu_fuse_sim3_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe, const float* Scw,
+                                           float fx, float fy, float cx, float cy, float scale_factor, int nlevels,
+                                           const orbgpu_mappoint_geometry* points, const uint8_t* point_descriptors,
+                                           const uint8_t* usable, int npoints, float th, int* target, int* dist,
+                                           int mem) {
+    if (!m || !frame_ok(keyframe) || !Scw || npoints < 0 || npoints >= (1 << 20) || !target ||
+        (npoints > 0 && (!points || !point_descriptors || !usable)) || nlevels < 1 || nlevels > 16 ||
+        !(scale_factor > 1.0f))
+        return ORBGPU_ERR_BAD_ARG;
+    // the Sim3 de-scaled as in SearchByProjection(KeyFrame*, Scw, ...)
+    double d = 0.0;
+    for (int k = 0; k < 3; k++) d += (double)Scw[k] * (double)Scw[k];
+    const float scw = (float)std::sqrt(d);
+    KeyframeProjDev kp;
+    std::memset(&kp, 0, sizeof(kp));
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) kp.T[4 * r + c] = Scw[4 * r + c] / scw;
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (double)(-kp.T[4 * k + i]) * (double)kp.T[4 * k + 3];
+        kp.Ow[i] = (float)s;
+    }
+    kp.fx = fx;
+    kp.fy = fy;
+    kp.cx = cx;
+    kp.cy = cy;
+    kp.maxX = (float)keyframe->width;
+    kp.maxY = (float)keyframe->height;
+    orbgpu_frustum_frame tmp;
+    const float eye[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    int rc = orbgpu_frustum_frame_init(eye, fx, fy, cx, cy, 0, 0, 1, 0, 1, scale_factor, nlevels, &tmp);
+    if (rc) return rc;
+    kp.nlevels = nlevels;
+    std::memcpy(kp.level_above, tmp.level_above, sizeof(kp.level_above));
+    kp.orbdist = ORBGPU_TH_LOW;
+    kp.sim3 = 1;
+    kp.invz_double = 1;
+    return fuse_pick_run(m, keyframe, kp, points, point_descriptors, usable, npoints, th, target, dist, mem);
 }
 
 extern "C" int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* left,

@@ -260,6 +260,35 @@ class ORBmatcher:
               "orbgpu_fuse_candidates")
         return target[:m], dist[:m]
 
+    def FuseSim3Candidates(self, KF: FrameView, Scw, fx, fy, cx, cy, points, point_descriptors, usable,
+                           th: float = 4.0, scale_factor: float = 1.2, nlevels: int = 8):
+        """The search half of Fuse(KeyFrame* pKF, cv::Mat Scw, vpPoints, th,
+        vpReplacePoint) -- src/ORBmatcher.cc:1290-1380: per point the keyframe
+        feature it fuses with (-1 none) and the distance; the caller fills
+        vpReplacePoint / adds observations in order.  Returns (target, dist)."""
+        s = KF.struct()
+        dev = s.mem == MEM_DEVICE
+        S = np.ascontiguousarray(np.asarray(Scw, np.float32).reshape(-1)[:12])
+        if dev:
+            import torch
+            pts, pd, use = points, point_descriptors, usable
+            m = int(pd.shape[0])
+            target = torch.empty(max(m, 1), dtype=torch.int32, device="cuda")
+            dist = torch.empty(max(m, 1), dtype=torch.int32, device="cuda")
+        else:
+            pts = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 8))
+            pd = np.ascontiguousarray(point_descriptors, np.uint8)
+            use = np.ascontiguousarray(usable, np.uint8)
+            m = len(pd)
+            target = np.zeros(max(m, 1), np.int32)
+            dist = np.zeros(max(m, 1), np.int32)
+        check(lib().orbgpu_fuse_sim3_candidates(self._h, C.byref(s), ptr(S), C.c_float(fx), C.c_float(fy),
+                                                C.c_float(cx), C.c_float(cy), C.c_float(scale_factor), int(nlevels),
+                                                ptr(pts), ptr(pd), ptr(use), m, C.c_float(th), ptr(target), ptr(dist),
+                                                MEM_DEVICE if dev else MEM_HOST),
+              "orbgpu_fuse_sim3_candidates")
+        return target[:m], dist[:m]
+
     def _search_by_projection_mappoints(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0,
                                         claimed=None):
         s = F.struct()

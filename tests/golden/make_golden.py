@@ -454,6 +454,17 @@ def fuse_fixture(R):
             nf, target = R.fuse_candidates(e.keypoints, e.descriptors, ur, 640, 480, Tcw, cam5, geom, pd, ps, th)
             arrays[pre + f"nf_{int(th)}"] = np.array(nf)
             arrays[pre + f"target_{int(th)}"] = target
+    # Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint)
+    for sc in range(2):
+        e = R.extract(syn.scene(640, 480, 99 + sc), nfeatures=1500)
+        Scw, cam, g, pd, ps, _ = syn.sim3_case(e.keypoints, e.descriptors, 640, 480, 99 + sc)
+        geom = np.ascontiguousarray(g).view(GEOM_DTYPE).reshape(-1)
+        pre = f"sim3_s{sc}_"
+        arrays.update({pre + "kps": e.keypoints, pre + "desc": e.descriptors, pre + "Scw": Scw, pre + "cam": cam,
+                       pre + "points": g, pre + "pdesc": pd, pre + "pstate": ps})
+        nf, target = R.fuse_sim3_candidates(e.keypoints, e.descriptors, 640, 480, Scw, cam, geom, pd, ps, 4.0)
+        arrays[pre + "nf"] = np.array(nf)
+        arrays[pre + "target"] = target
     save("fuse.npz", **arrays)
 
 

@@ -419,3 +419,26 @@ def test_fuse_candidates_vs_oracle(torch, oracle, seed, th, dev):
         target, _ = m.FuseCandidates(KF, Tcw, *cam5, inv_sigma2, g, pd, usable, th)
     assert np.array_equal(target, ref)
     assert int((target >= 0).sum()) == ref_nf > 300
+
+
+@pytest.mark.parametrize("seed,th,dev", [(0, 4.0, False), (1, 8.0, True)])
+def test_fuse_sim3_candidates_vs_oracle(torch, oracle, seed, th, dev):
+    """The search half of Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint) against the oracle."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    e = oracle.extract(syn.scene(640, 480, 160 + seed), nfeatures=1500)
+    Scw, cam, g, pd, ps, _ = syn.sim3_case(e.keypoints, e.descriptors, 640, 480, 160 + seed)
+    geom = np.ascontiguousarray(g).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    ref_nf, ref = oracle.fuse_sim3_candidates(e.keypoints, e.descriptors, 640, 480, Scw, cam, geom, pd, ps, th)
+    usable = (ps == 1).astype(np.uint8)
+    m = ORBmatcher(0.6, True)
+    if dev:
+        kd = torch.from_numpy(e.keypoints.view(np.float32).reshape(-1, 7).copy()).cuda()
+        KF = frame(kd, torch.from_numpy(e.descriptors).cuda(), 640, 480)
+        target, _ = m.FuseSim3Candidates(KF, Scw, *cam, torch.from_numpy(g).cuda(), torch.from_numpy(pd).cuda(),
+                                         torch.from_numpy(usable).cuda(), th)
+        target = target.cpu().numpy()
+    else:
+        target, _ = m.FuseSim3Candidates(frame(e.keypoints, e.descriptors, 640, 480), Scw, *cam, g, pd, usable, th)
+    assert np.array_equal(target, ref)
+    assert int((target >= 0).sum()) == ref_nf > 300

@@ -352,3 +352,15 @@ def test_fuse_candidates_golden(oracle, golden, sc):
                                             g[pre + "cam"], geom, g[pre + "pdesc"], g[pre + "pstate"], th)
         assert nf == int(g[pre + f"nf_{int(th)}"])
         assert np.array_equal(target, g[pre + f"target_{int(th)}"])
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_fuse_sim3_candidates_golden(oracle, golden, sc):
+    """ORBmatcher::Fuse(KeyFrame*, Scw, vpPoints, th, vpReplacePoint): every point's choice."""
+    g = golden("fuse.npz")
+    pre = f"sim3_s{sc}_"
+    geom = np.ascontiguousarray(g[pre + "points"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    nf, target = oracle.fuse_sim3_candidates(g[pre + "kps"], g[pre + "desc"], 640, 480, g[pre + "Scw"],
+                                             g[pre + "cam"], geom, g[pre + "pdesc"], g[pre + "pstate"], 4.0)
+    assert nf == int(g[pre + "nf"])
+    assert np.array_equal(target, g[pre + "target"])
