@@ -416,6 +416,25 @@ int orbgpu_fuse_sim3_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe,
                                 const orbgpu_mappoint_geometry* points, const uint8_t* point_descriptors,
                                 const uint8_t* usable, int npoints, float th, int* target, int* dist, int mem);
 
+/* ORBmatcher::SearchBySim3(KeyFrame* pKF1, KeyFrame* pKF2, vpMatches12,
+ * s12, R12, t12, th) -- src/ORBmatcher.cc:1441-1640: pKF1's map points
+ * projected into pKF2 through the Sim3 and pKF2's into pKF1, each taking the
+ * first least distance in its window (<= TH_HIGH), kept where the two agree.
+ * kf1 / kf2: the keyframes' keypoints and descriptors (image bounds
+ * 0..width x 0..height); T1w / T2w: rows 0-2 of their poses; s12, R12
+ * (row-major 3 x 3), t12: the Sim3; fx..cy: pKF1's camera (the reference
+ * projects into both with it); scale_factor, nlevels: the pyramid.  Per
+ * keyframe feature: mps / mpd (its map point's geometry and descriptor),
+ * usable = 1 where the map point exists, is not bad and is not already in
+ * vpMatches12.  match12 (host, kf1->n ints): the pKF2 feature whose map point
+ * vpMatches12[i] receives, or -1; *nfound the reference's return value.
+ * Host arrays; returns after the result is complete. */
+int orbgpu_search_by_sim3(orbgpu_matcher* m, const orbgpu_frame* kf1, const orbgpu_frame* kf2, const float* T1w,
+                          const float* T2w, float s12, const float* R12, const float* t12, float fx, float fy,
+                          float cx, float cy, float scale_factor, int nlevels, const orbgpu_mappoint_geometry* mps1,
+                          const uint8_t* mpd1, const uint8_t* usable1, const orbgpu_mappoint_geometry* mps2,
+                          const uint8_t* mpd2, const uint8_t* usable2, float th, int* match12, int* nfound);
+
 /* One entry of LastFrame.mvpMapPoints for orbgpu_search_by_projection_frame,
  * indexed like LastFrame's keypoints. */
 typedef struct {

@@ -610,6 +610,26 @@ int orc_search_by_projection(const orc_params* p, const orc_kp* kps, const uint8
     return nmatches;
 }
 
+// KeyFrame::GetFeaturesInArea, src/KeyFrame.cc:785-830: the same cells as
+// the frame's, but a square window (|dx| < r and |dy| < r) where this tree's
+// Frame::GetFeaturesInArea keeps a disc.
+static std::vector<int> kf_features_in_area(const Grid& g, const orc_kp* kps, float x, float y, float r) {
+    std::vector<int> v;
+    const int x0 = std::max(0, (int)std::floor((x - g.minX - r) * g.invW));
+    if (x0 >= kGridCols) return v;
+    const int x1 = std::min(kGridCols - 1, (int)std::ceil((x - g.minX + r) * g.invW));
+    if (x1 < 0) return v;
+    const int y0 = std::max(0, (int)std::floor((y - g.minY - r) * g.invH));
+    if (y0 >= kGridRows) return v;
+    const int y1 = std::min(kGridRows - 1, (int)std::ceil((y - g.minY + r) * g.invH));
+    if (y1 < 0) return v;
+    for (int ix = x0; ix <= x1; ix++)
+        for (int iy = y0; iy <= y1; iy++)
+            for (int idx : g.cells[ix][iy])
+                if (std::fabs(kps[idx].x - x) < r && std::fabs(kps[idx].y - y) < r) v.push_back(idx);
+    return v;
+}
+
 // cv::Mat products of the reference's pose algebra: the 3 x 3 float product
 // accumulates in double and is stored as float (gemm), an added vector is a
 // float addition.
@@ -956,7 +976,7 @@ int orc_search_by_projection_sim3(const orc_params* p, const orc_kp* kps, const 
         if (level < 0) level = 0;
         else if (level >= p->nlevels) level = p->nlevels - 1;
         const float radius = th * t.scale[level];
-        const std::vector<int> idx = features_in_area(*g, kps, u, v, radius, -1, -1);
+        const std::vector<int> idx = kf_features_in_area(*g, kps, u, v, radius);
         int bestDist = 256, best = -1;
         for (int k : idx) {
             if (owner[k] != -1) continue;
@@ -1019,7 +1039,7 @@ int orc_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* d
         if (level < 0) level = 0;
         else if (level >= p->nlevels) level = p->nlevels - 1;
         const float radius = th * t.scale[level];
-        const std::vector<int> idx = features_in_area(*g, kps, u, v, radius, -1, -1);
+        const std::vector<int> idx = kf_features_in_area(*g, kps, u, v, radius);
         int bestDist = 256, best = -1;
         for (int k : idx) {
             const int kl = kps[k].octave;
@@ -1093,7 +1113,7 @@ int orc_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8
         if (level < 0) level = 0;
         else if (level >= p->nlevels) level = p->nlevels - 1;
         const float radius = th * t.scale[level];
-        const std::vector<int> idx = features_in_area(*g, kps, u, v, radius, -1, -1);
+        const std::vector<int> idx = kf_features_in_area(*g, kps, u, v, radius);
         int bestDist = INT_MAX, best = -1;
         for (int k : idx) {
             if (kps[k].octave < level - 1 || kps[k].octave > level) continue;
@@ -1110,6 +1130,84 @@ int orc_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8
     }
     delete g;
     return nf;
+}
+
+// ORBmatcher::SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th),
+// src/ORBmatcher.cc:1441-1640 (vpMatches12 empty on entry): pKF1's map points
+// through R1w, t1w then sR21 = (1/s12) R12^T, t21 = -sR21 t12 into pKF2 and
+// pKF2's through R2w, t2w then sR12 = s12 R12, t12 into pKF1, each the first
+// least distance <= TH_HIGH in its window (levels predicted - 1 .. predicted,
+// depth |p3Dc|, pKF1's camera for both); kept where both agree.  st: 1 usable.
+static int sim3_side(const Tables& t, const Grid& g, const orc_kp* kps, const uint8_t* desc, int w, int h,
+                     const float* Tw, const float* sR, const float* tt, const float* cam, float log_scale,
+                     int nlevels, const orc_mp_geometry& mp, const uint8_t* mpd, float th) {
+    const float X[3] = {mp.x, mp.y, mp.z};
+    float c1[3], c2[3];
+    for (int r = 0; r < 3; r++) c1[r] = mat_row_dot(Tw + 4 * r, 1, X) + Tw[4 * r + 3];
+    for (int r = 0; r < 3; r++) c2[r] = mat_row_dot(sR + 3 * r, 1, c1) + tt[r];
+    if (c2[2] < 0.0) return -1;
+    const float invz = 1.0 / c2[2];
+    const float x = c2[0] * invz, y = c2[1] * invz;
+    const float u = cam[0] * x + cam[2], v = cam[1] * y + cam[3];
+    if (!(u >= 0.0f && u < (float)w && v >= 0.0f && v < (float)h)) return -1;
+    double ss = 0;
+    for (int k = 0; k < 3; k++) ss += (double)c2[k] * (double)c2[k];
+    const float dist3D = (float)std::sqrt(ss);
+    if (dist3D < 0.8f * mp.min_distance || dist3D > 1.2f * mp.max_distance) return -1;
+    int level = (int)std::ceil(std::log(mp.max_distance / dist3D) / log_scale);
+    if (level < 0) level = 0;
+    else if (level >= nlevels) level = nlevels - 1;
+    const float radius = th * t.scale[level];
+    const std::vector<int> idx = kf_features_in_area(g, kps, u, v, radius);
+    int bestDist = INT_MAX, best = -1;
+    for (int k : idx) {
+        if (kps[k].octave < level - 1 || kps[k].octave > level) continue;
+        const int dd = hamming(mpd, desc + (size_t)k * 32);
+        if (dd < bestDist) {
+            bestDist = dd;
+            best = k;
+        }
+    }
+    return bestDist <= kThHigh ? best : -1;
+}
+
+int orc_search_by_sim3(const orc_params* p, const orc_kp* kps1, const uint8_t* desc1, int n1, const orc_kp* kps2,
+                           const uint8_t* desc2, int n2, int w, int h, const float* T1w, const float* T2w, float s12,
+                           const float* R12, const float* t12, const float* cam, const orc_mp_geometry* mps1,
+                           const uint8_t* mpd1, const uint8_t* st1, const orc_mp_geometry* mps2, const uint8_t* mpd2,
+                           const uint8_t* st2, float th, int* match12) {
+    const Tables t = make_tables(p);
+    Grid* g1 = new Grid();
+    Grid* g2 = new Grid();
+    build_grid(*g1, kps1, n1, w, h);
+    build_grid(*g2, kps2, n2, w, h);
+    float sR12[9], sR21[9], nsR21[9], t21[3];
+    const float inv_s = (float)(1.0 / (double)s12);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            sR12[3 * r + c] = R12[3 * r + c] * s12;
+            sR21[3 * r + c] = R12[3 * c + r] * inv_s;
+            nsR21[3 * r + c] = -sR21[3 * r + c];
+        }
+    for (int r = 0; r < 3; r++) t21[r] = mat_row_dot(nsR21 + 3 * r, 1, t12);
+    const float log_scale = std::log(p->scale_factor);
+    std::vector<int> m1(n1, -1), m2(n2, -1);
+    for (int i = 0; i < n1; i++)
+        if (st1[i] == 1)
+            m1[i] = sim3_side(t, *g2, kps2, desc2, w, h, T1w, sR21, t21, cam, log_scale, p->nlevels, mps1[i],
+                              mpd1 + (size_t)i * 32, th);
+    for (int i = 0; i < n2; i++)
+        if (st2[i] == 1)
+            m2[i] = sim3_side(t, *g1, kps1, desc1, w, h, T2w, sR12, t12, cam, log_scale, p->nlevels, mps2[i],
+                              mpd2 + (size_t)i * 32, th);
+    int found = 0;
+    for (int i = 0; i < n1; i++) {
+        match12[i] = (m1[i] >= 0 && m2[m1[i]] == i) ? m1[i] : -1;
+        found += match12[i] >= 0;
+    }
+    delete g1;
+    delete g2;
+    return found;
 }
 
 // Frame::ComputeStereoMatches, src/Frame.cc:831-1082 (mb = mbf/fx).

@@ -96,6 +96,13 @@ int orc_fuse_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* d
 int orc_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8_t* desc, int n, int w, int h,
                                const float* Scw, const float* cam, const orc_mp_geometry* pts, const uint8_t* pdesc,
                                const uint8_t* pstate, int npts, float th, int* target);
+/* ORBmatcher::SearchBySim3 (src/ORBmatcher.cc:1441-1640), vpMatches12 empty
+ * on entry; match12: the pKF2 feature per pKF1 feature or -1. */
+int orc_search_by_sim3(const orc_params* p, const orc_kp* kps1, const uint8_t* desc1, int n1, const orc_kp* kps2,
+                           const uint8_t* desc2, int n2, int w, int h, const float* T1w, const float* T2w, float s12,
+                           const float* R12, const float* t12, const float* cam, const orc_mp_geometry* mps1,
+                           const uint8_t* mpd1, const uint8_t* st1, const orc_mp_geometry* mps2, const uint8_t* mpd2,
+                           const uint8_t* st2, float th, int* match12);
 /* ORBmatcher::SearchByBoW(KeyFrame*, Frame&, vpMapPointMatches)
  * (src/ORBmatcher.cc:247-380) on two FeatureVectors (nodes ascending, node i
  * owning features [offsets[i], offsets[i + 1]) of *_fv_features).  kf_mp:

@@ -373,6 +373,28 @@ class _Base:
                C.c_float(th), _p(out))
         return int(nf), out[:len(pts)].copy()
 
+    def search_by_sim3(self, kps1, desc1, kps2, desc2, w, h, T1w, T2w, s12, R12, t12, cam, mps1, mpd1, st1, mps2,
+                       mpd2, st2, th=7.5, nlevels=8, scale_factor=1.2):
+        """SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) ->
+        (nfound, match12 over pKF1's features)."""
+        a = [np.ascontiguousarray(kps1, KP_DTYPE), np.ascontiguousarray(desc1, np.uint8),
+             np.ascontiguousarray(kps2, KP_DTYPE), np.ascontiguousarray(desc2, np.uint8)]
+        fl = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1)) for x in (T1w, T2w, R12, t12, cam)]
+        g1 = np.ascontiguousarray(mps1, GEOM_DTYPE)
+        g2 = np.ascontiguousarray(mps2, GEOM_DTYPE)
+        d1, d2 = np.ascontiguousarray(mpd1, np.uint8), np.ascontiguousarray(mpd2, np.uint8)
+        s1, s2 = np.ascontiguousarray(st1, np.uint8), np.ascontiguousarray(st2, np.uint8)
+        out = np.zeros(max(len(a[0]), 1), np.int32)
+        p = Params(1000, scale_factor, nlevels, 20, 7)
+        f = self.fn("search_by_sim3")
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                      C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p] + \
+            [C.c_void_p] * 6 + [C.c_float, C.c_void_p]
+        nf = f(C.byref(p), _p(a[0]), _p(a[1]), len(a[0]), _p(a[2]), _p(a[3]), len(a[2]), w, h, _p(fl[0]), _p(fl[1]),
+               C.c_float(s12), _p(fl[2]), _p(fl[3]), _p(fl[4]), _p(g1), _p(d1), _p(s1), _p(g2), _p(d2), _p(s2),
+               C.c_float(th), _p(out))
+        return int(nf), out[:len(a[0])].copy()
+
     def search_for_triangulation(self, kps1, desc1, mp1, ur1, fv1, kps2, desc2, mp2, ur2, fv2, Cw1, T2, K2, F12,
                                  scale, sigma2, only_stereo=False, check_ori=True):
         """SearchForTriangulation(pKF1, pKF2, F12, pairs, bOnlyStereo) ->

@@ -1002,6 +1002,72 @@ int ref_fuse_sim3_candidates(const orc_params* p, const orc_kp* kps, const uint8
     return nf;
 }
 
+// ORBmatcher::SearchBySim3 -- src/ORBmatcher.cc:1441-1640, two keyframes
+// built from frames of the given keypoints, vpMatches12 empty on entry.
+int ref_search_by_sim3(const orc_params* p, const orc_kp* kps1, const uint8_t* desc1, int n1, const orc_kp* kps2,
+                           const uint8_t* desc2, int n2, int w, int h, const float* T1w, const float* T2w, float s12,
+                           const float* R12, const float* t12, const float* cam, const orc_mp_geometry* mps1,
+                           const uint8_t* mpd1, const uint8_t* st1, const orc_mp_geometry* mps2, const uint8_t* mpd2,
+                           const uint8_t* st2, float th, int* match12) {
+    ArenaScope scope;
+    int nf;
+    {
+        ORBextractor ext(p->nfeatures, p->scale_factor, p->nlevels, p->ini_th_fast, p->min_th_fast);
+        Frame::fx = cam[0];
+        Frame::fy = cam[1];
+        Frame::cx = cam[2];
+        Frame::cy = cam[3];
+        MapPointMaker maker;
+        Frame* F1 = make_frame(&ext, kps1, desc1, n1, w, h, nullptr);
+        F1->mfLogScaleFactor = std::log(F1->mfScaleFactor);
+        KeyFrame* K1 = new KeyFrame(*F1, maker.map, nullptr);
+        Frame* F2 = make_frame(&ext, kps2, desc2, n2, w, h, nullptr);
+        F2->mfLogScaleFactor = std::log(F2->mfScaleFactor);
+        KeyFrame* K2 = new KeyFrame(*F2, maker.map, nullptr);
+        std::map<MapPoint*, int> index2;
+        std::vector<MapPoint*> owned;
+        auto fill = [&](KeyFrame* K, const float* T, int n, const orc_mp_geometry* mps, const uint8_t* mpd,
+                        const uint8_t* st, std::map<MapPoint*, int>* index) {
+            K->Tcw = cv::Mat::eye(4, 4, CV_32F);
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 4; c++) K->Tcw.at<float>(r, c) = T[4 * r + c];
+            K->mvpMapPoints.assign(n, static_cast<MapPoint*>(NULL));
+            for (int i = 0; i < n; i++) {
+                if (st[i] == 0) continue;
+                cv::Mat pos(3, 1, CV_32F);
+                pos.at<float>(0) = mps[i].x;
+                pos.at<float>(1) = mps[i].y;
+                pos.at<float>(2) = mps[i].z;
+                MapPoint* mp = maker.make(pos, 1);
+                mp->mfMinDistance = mps[i].min_distance;
+                mp->mfMaxDistance = mps[i].max_distance;
+                mp->mDescriptor = cv::Mat(1, 32, CV_8U);
+                std::memcpy(mp->mDescriptor.data, mpd + (size_t)i * 32, 32);
+                mp->mbBad = st[i] == 2;
+                K->mvpMapPoints[i] = mp;
+                owned.push_back(mp);
+                if (index) (*index)[mp] = i;
+            }
+        };
+        fill(K1, T1w, n1, mps1, mpd1, st1, nullptr);
+        fill(K2, T2w, n2, mps2, mpd2, st2, &index2);
+        cv::Mat R(3, 3, CV_32F), tt(3, 1, CV_32F);
+        for (int k = 0; k < 9; k++) R.at<float>(k / 3, k % 3) = R12[k];
+        for (int k = 0; k < 3; k++) tt.at<float>(k) = t12[k];
+        std::vector<MapPoint*> matches(n1, static_cast<MapPoint*>(NULL));
+        ORBmatcher matcher(0.75f, true);
+        const float s = s12;
+        nf = matcher.SearchBySim3(K1, K2, matches, s, R, tt, th);
+        for (int i = 0; i < n1; i++) match12[i] = matches[i] ? index2[matches[i]] : -1;
+        for (MapPoint* mp : owned) delete mp;
+        delete K1;
+        delete K2;
+        delete F1;
+        delete F2;
+    }
+    return nf;
+}
+
 // Frame::isInFrustum -- src/Frame.cc:491-578, on a Frame posed by SetPose
 // (UpdatePoseMatrices) and real map points whose tracking fields start from
 // out[i] (the reference leaves them unchanged where it returns false).

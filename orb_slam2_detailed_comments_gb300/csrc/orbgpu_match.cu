@@ -564,6 +564,12 @@ struct KeyframeProjDev {
     // Fuse(KeyFrame*, Scw, ...) (src/ORBmatcher.cc:1290-1380): invz = 1.0 / z
     // in double, rounded to float
     int invz_double;
+    // SearchBySim3 (src/ORBmatcher.cc:1441-1640): a second transform T2
+    // applied to the camera coordinates (the Sim3 between the keyframes), the
+    // depth for the distance invariance is |p3Dc| and there is no viewing
+    // angle test
+    int chain;
+    float T2[12];
 };
 
 __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_mappoint_geometry* mps,
@@ -578,9 +584,15 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
     int level = 0;
     if (live) {
         const orbgpu_mappoint_geometry mp = mps[i];
-        const float xc = pose_row(kp.T, mp.x, mp.y, mp.z);
-        const float yc = pose_row(kp.T + 4, mp.x, mp.y, mp.z);
-        const float zc = pose_row(kp.T + 8, mp.x, mp.y, mp.z);
+        float xc = pose_row(kp.T, mp.x, mp.y, mp.z);
+        float yc = pose_row(kp.T + 4, mp.x, mp.y, mp.z);
+        float zc = pose_row(kp.T + 8, mp.x, mp.y, mp.z);
+        if (kp.chain) {
+            const float x1 = xc, y1 = yc, z1 = zc;
+            xc = pose_row(kp.T2, x1, y1, z1);
+            yc = pose_row(kp.T2 + 4, x1, y1, z1);
+            zc = pose_row(kp.T2 + 8, x1, y1, z1);
+        }
         if (kp.sim3) {
             const float invz = kp.invz_double ? __double2float_rn(__ddiv_rn(1.0, (double)zc)) : __fdiv_rn(1.0f, zc);
             u = __fadd_rn(__fmul_rn(kp.fx, __fmul_rn(xc, invz)), kp.cx);
@@ -596,14 +608,16 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
             live = isfinite(u) && isfinite(v) && !(u < g.minX || u > kp.maxX) && !(v < g.minY || v > kp.maxY);
         }
         if (live) {
-            const float po0 = __fsub_rn(mp.x, kp.Ow[0]), po1 = __fsub_rn(mp.y, kp.Ow[1]),
-                        po2 = __fsub_rn(mp.z, kp.Ow[2]);
+            // PO = X - Ow, or the camera coordinates themselves for SearchBySim3
+            const float po0 = kp.chain ? xc : __fsub_rn(mp.x, kp.Ow[0]);
+            const float po1 = kp.chain ? yc : __fsub_rn(mp.y, kp.Ow[1]);
+            const float po2 = kp.chain ? zc : __fsub_rn(mp.z, kp.Ow[2]);
             double ss = __dmul_rn((double)po0, (double)po0);
             ss = __dadd_rn(ss, __dmul_rn((double)po1, (double)po1));
             ss = __dadd_rn(ss, __dmul_rn((double)po2, (double)po2));
             const float dist = (float)__dsqrt_rn(ss);
             live = !(dist < __fmul_rn(0.8f, mp.min_distance) || dist > __fmul_rn(1.2f, mp.max_distance));
-            if (live && kp.sim3) {
+            if (live && kp.sim3 && !kp.chain) {
                 // PO.dot(Pn) < 0.5 * dist, in double
                 double dp = __dmul_rn((double)po0, (double)mp.nx);
                 dp = __dadd_rn(dp, __dmul_rn((double)po1, (double)mp.ny));
@@ -621,7 +635,17 @@ __global__ void k_pkf_candidates(GridDev g, KeyframeProjDev kp, const orbgpu_map
             const uint8_t* dmp = mp_desc + (size_t)i * 32;
             warp_window_keys(g.cell_start, g.cell_keys, g.key_cell, ORBGPU_GRID_ROWS, x0, x1, y0, y1,
                              [&](int idx, int c, bool valid) {
-                bool ok = valid && in_area(g, idx, u, v, radius, level - 1, kp.sim3 ? level : level + 1);
+                bool ok;
+                if (kp.sim3) {
+                    // KeyFrame::GetFeaturesInArea (src/KeyFrame.cc:785-830): a square
+                    // window (|dx| < r and |dy| < r; Frame's is a disc), then the
+                    // levels predicted - 1 .. predicted
+                    const orbgpu_keypoint& kq = g.kps[idx];
+                    ok = valid && kq.octave >= level - 1 && kq.octave <= level &&
+                         fabsf(__fsub_rn(kq.x, u)) < radius && fabsf(__fsub_rn(kq.y, v)) < radius;
+                } else {
+                    ok = valid && in_area(g, idx, u, v, radius, level - 1, level + 1);
+                }
                 if (ok && kp.fuse) {
                     // chi-square gates of Fuse: 7.8 with the right coordinate, 5.99 without
                     const orbgpu_keypoint& k = g.kps[idx];
@@ -1781,6 +1805,83 @@ extern "C" int orbgpu_fuse_sim3_candidates(orbgpu_matcher* m, const orbgpu_frame
     kp.sim3 = 1;
     kp.invz_double = 1;
     return fuse_pick_run(m, keyframe, kp, points, point_descriptors, usable, npoints, th, target, dist, mem);
+}
+
+// SearchBySim3's geometry: cv::Mat products accumulated in double and
+// rounded to float (plus a float add), scalar products of float matrices as
+// float products of the scalar rounded to float.
+static void mat3_times(const float* A, const float* x, float* out) {
+    for (int r = 0; r < 3; r++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (double)A[3 * r + k] * (double)x[k];
+        out[r] = (float)s;
+    }
+}
+
+extern "C" int orbgpu_search_by_sim3(orbgpu_matcher* m, const orbgpu_frame* kf1, const orbgpu_frame* kf2,
+                                     const float* T1w, const float* T2w, float s12, const float* R12,
+                                     const float* t12, float fx, float fy, float cx, float cy, float scale_factor,
+                                     int nlevels, const orbgpu_mappoint_geometry* mps1, const uint8_t* mpd1,
+                                     const uint8_t* usable1, const orbgpu_mappoint_geometry* mps2,
+                                     const uint8_t* mpd2, const uint8_t* usable2, float th, int* match12,
+                                     int* nfound) {
+    if (!m || !frame_ok(kf1) || !frame_ok(kf2) || !T1w || !T2w || !R12 || !t12 || !match12 || !nfound ||
+        nlevels < 1 || nlevels > 16 || !(scale_factor > 1.0f) || kf1->n < 0 || kf2->n < 0 ||
+        (kf1->n > 0 && (!mps1 || !mpd1 || !usable1)) || (kf2->n > 0 && (!mps2 || !mpd2 || !usable2)))
+        return ORBGPU_ERR_BAD_ARG;
+    const int N1 = kf1->n, N2 = kf2->n;
+    // sR12 = s12 * R12, sR21 = (1.0 / s12) * R12^T, t21 = -sR21 * t12
+    // (src/ORBmatcher.cc:1456-1463)
+    const float inv_s = (float)(1.0 / (double)s12);
+    float sR12[9], sR21[9], nsR21[9], t21[3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            sR12[3 * r + c] = R12[3 * r + c] * s12;
+            sR21[3 * r + c] = R12[3 * c + r] * inv_s;
+            nsR21[3 * r + c] = -sR21[3 * r + c];
+        }
+    mat3_times(nsR21, t12, t21);
+    orbgpu_frustum_frame tmp;
+    const float eye[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    int rc = orbgpu_frustum_frame_init(eye, fx, fy, cx, cy, 0, 0, 1, 0, 1, scale_factor, nlevels, &tmp);
+    if (rc) return rc;
+    auto pass = [&](const orbgpu_frame* target_kf, const float* Tw, const float* sR, const float* t,
+                    const orbgpu_mappoint_geometry* mps, const uint8_t* mpd, const uint8_t* use, int n,
+                    std::vector<int>& out) {
+        KeyframeProjDev kp;
+        std::memset(&kp, 0, sizeof(kp));
+        std::memcpy(kp.T, Tw, sizeof(kp.T));
+        for (int r = 0; r < 3; r++) {
+            for (int c = 0; c < 3; c++) kp.T2[4 * r + c] = sR[3 * r + c];
+            kp.T2[4 * r + 3] = t[r];
+        }
+        kp.fx = fx;
+        kp.fy = fy;
+        kp.cx = cx;
+        kp.cy = cy;
+        kp.maxX = (float)target_kf->width;
+        kp.maxY = (float)target_kf->height;
+        kp.nlevels = nlevels;
+        std::memcpy(kp.level_above, tmp.level_above, sizeof(kp.level_above));
+        kp.orbdist = ORBGPU_TH_HIGH;
+        kp.sim3 = 1;
+        kp.invz_double = 1;
+        kp.chain = 1;
+        out.assign(std::max(n, 1), -1);
+        return fuse_pick_run(m, target_kf, kp, mps, mpd, use, n, th, out.data(), nullptr, ORBGPU_MEM_HOST);
+    };
+    // vnMatch1: pKF1's map points into pKF2; vnMatch2: pKF2's into pKF1
+    std::vector<int> match1, match2;
+    if ((rc = pass(kf2, T1w, sR21, t21, mps1, mpd1, usable1, N1, match1))) return rc;
+    if ((rc = pass(kf1, T2w, sR12, t12, mps2, mpd2, usable2, N2, match2))) return rc;
+    int found = 0;
+    for (int i1 = 0; i1 < N1; i1++) {
+        const int i2 = match1[i1];
+        match12[i1] = (i2 >= 0 && i2 < N2 && match2[i2] == i1) ? i2 : -1;
+        found += match12[i1] >= 0;
+    }
+    *nfound = found;
+    return ORBGPU_OK;
 }
 
 extern "C" int orbgpu_compute_stereo_matches(orbgpu_matcher* m, const orbgpu_extractor* left,

@@ -289,6 +289,27 @@ class ORBmatcher:
               "orbgpu_fuse_sim3_candidates")
         return target[:m], dist[:m]
 
+    def SearchBySim3(self, KF1: FrameView, KF2: FrameView, T1w, T2w, s12, R12, t12, fx, fy, cx, cy, mps1, mpd1,
+                     usable1, mps2, mpd2, usable2, th: float = 7.5, scale_factor: float = 1.2, nlevels: int = 8):
+        """SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) --
+        src/ORBmatcher.cc:1441-1640 (host arrays).  Returns (nfound, match12:
+        per pKF1 feature the pKF2 feature whose map point vpMatches12 gets, or
+        -1)."""
+        s1, s2 = KF1.struct(), KF2.struct()
+        out = np.zeros(max(s1.n, 1), np.int32)
+        nf = C.c_int(0)
+        arrs = [np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1)) for a in (T1w, T2w, R12, t12)]
+        g1 = np.ascontiguousarray(np.asarray(mps1, np.float32).reshape(-1, 8))
+        g2 = np.ascontiguousarray(np.asarray(mps2, np.float32).reshape(-1, 8))
+        d1, d2 = np.ascontiguousarray(mpd1, np.uint8), np.ascontiguousarray(mpd2, np.uint8)
+        u1, u2 = np.ascontiguousarray(usable1, np.uint8), np.ascontiguousarray(usable2, np.uint8)
+        check(lib().orbgpu_search_by_sim3(self._h, C.byref(s1), C.byref(s2), ptr(arrs[0]), ptr(arrs[1]),
+                                          C.c_float(s12), ptr(arrs[2]), ptr(arrs[3]), C.c_float(fx), C.c_float(fy),
+                                          C.c_float(cx), C.c_float(cy), C.c_float(scale_factor), int(nlevels), ptr(g1),
+                                          ptr(d1), ptr(u1), ptr(g2), ptr(d2), ptr(u2), C.c_float(th), ptr(out),
+                                          C.byref(nf)), "orbgpu_search_by_sim3")
+        return nf.value, out[:s1.n]
+
     def _search_by_projection_mappoints(self, F: FrameView, mappoints, mp_descriptors, th: float = 1.0,
                                         claimed=None):
         s = F.struct()

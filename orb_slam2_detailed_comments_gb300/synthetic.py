@@ -583,3 +583,46 @@ def fuse_case(kps: np.ndarray, desc: np.ndarray, seed: int, w: int = 640, h: int
     rng = np.random.default_rng(seed)
     ur = np.where(rng.random(len(kps)) < 0.3, kps["x"] - rng.uniform(1, 40, len(kps)), -1).astype(np.float32)
     return Tcw, np.array([cam[0], cam[1], cam[2], cam[3], 40.0], np.float32), g, pd, ps, ur
+
+
+def sim3_pair_case(kps: np.ndarray, desc: np.ndarray, seed: int, w: int = 640, h: int = 480, fx: float = 500.0):
+    """Inputs of SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th): both
+    keyframes are the frame (kps, desc) under one random pose, related by a
+    Sim3 near the identity (s12 1 +- 0.02, rotations of about 0.3 degrees,
+    translations of a few centimetres), so the map points project near their
+    features both ways.  About 60 % of each keyframe's features carry a map
+    point: the back-projection of that feature at a random depth, its
+    descriptor with a few bits flipped, distances placing the predicted level
+    at the feature's octave (a tenth of the map points bad).  Returns (T1w,
+    T2w, s12, R12, t12, cam (fx, fy, cx, cy), geometry1, desc1, usable1,
+    geometry2, desc2, usable2)."""
+    rng = np.random.default_rng(seed)
+    n = len(kps)
+    cx, cy = w / 2.0, h / 2.0
+    R = _rotation(*rng.normal(0, 0.2, 3))
+    t = rng.normal(0, 0.5, 3)
+    T = np.hstack([R, t[:, None]]).astype(np.float32)
+    s12 = np.float32(1.0 + rng.uniform(-0.02, 0.02))
+    R12 = _rotation(*rng.normal(0, 0.005, 3)).astype(np.float32)
+    t12 = rng.normal(0, 0.03, 3).astype(np.float32)
+
+    def side(sd):
+        r = np.random.default_rng(sd)
+        z = r.uniform(2.0, 20.0, n)
+        pc = np.stack([(kps["x"] - cx) / fx * z, (kps["y"] - cy) / fx * z, z], 1)
+        pw = (R.T @ (pc - t).T).T
+        d = np.linalg.norm(pc, axis=1)
+        maxd = d * 1.2 ** (kps["octave"] + r.uniform(-0.3, 0.3, n))
+        g = np.zeros((n, 8), np.float32)
+        g[:, :3] = pw
+        g[:, 6] = maxd / 1.2 ** 7
+        g[:, 7] = maxd
+        flips = r.integers(0, 256, (n, 32), dtype=np.uint8)
+        for _ in range(3):
+            flips &= r.integers(0, 256, (n, 32), dtype=np.uint8)
+        usable = ((r.random(n) < 0.6) & (r.random(n) > 0.1)).astype(np.uint8)
+        return g, desc ^ flips, usable
+
+    g1, d1, u1 = side(seed * 2 + 1)
+    g2, d2, u2 = side(seed * 2 + 2)
+    return (T, T.copy(), s12, R12, t12, np.array([fx, fx, cx, cy], np.float32), g1, d1, u1, g2, d2, u2)

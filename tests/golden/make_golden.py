@@ -31,7 +31,7 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path) // 1024} KiB")
 
 
-GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri", "sim3", "fuse")
+GROUPS = ("extract", "projection", "knn", "kat", "tables", "projframe", "distinctive", "frustum", "undistort", "bow", "sbb", "reloc", "tri", "sim3", "fuse", "bysim3")
 
 
 def main(groups=GROUPS):
@@ -65,6 +65,8 @@ def main(groups=GROUPS):
         sim3_fixture(R)
     if "fuse" in groups:
         fuse_fixture(R)
+    if "bysim3" in groups:
+        by_sim3_fixture(R)
 
 
 def base_fixtures(R, groups):
@@ -466,6 +468,27 @@ def fuse_fixture(R):
         arrays[pre + "nf"] = np.array(nf)
         arrays[pre + "target"] = target
     save("fuse.npz", **arrays)
+
+
+def by_sim3_fixture(R):
+    # 18. ORBmatcher::SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th)
+    from oracle.pyoracle import GEOM_DTYPE
+    arrays = {}
+    for sc in range(2):
+        e = R.extract(syn.scene(640, 480, 110 + sc), nfeatures=1500)
+        T1, T2, s12, R12, t12, cam, g1, d1, u1, g2, d2, u2 = syn.sim3_pair_case(e.keypoints, e.descriptors, 110 + sc)
+        G1 = np.ascontiguousarray(g1).view(GEOM_DTYPE).reshape(-1)
+        G2 = np.ascontiguousarray(g2).view(GEOM_DTYPE).reshape(-1)
+        pre = f"s{sc}_"
+        arrays.update({pre + "kps": e.keypoints, pre + "desc": e.descriptors, pre + "T1": T1, pre + "T2": T2,
+                       pre + "s12": np.float32(s12), pre + "R12": R12, pre + "t12": t12, pre + "cam": cam,
+                       pre + "g1": g1, pre + "d1": d1, pre + "u1": u1, pre + "g2": g2, pre + "d2": d2, pre + "u2": u2})
+        for th in (7.5, 3.0):
+            nf, m12 = R.search_by_sim3(e.keypoints, e.descriptors, e.keypoints, e.descriptors, 640, 480, T1, T2, s12,
+                                       R12, t12, cam, G1, d1, u1, G2, d2, u2, th)
+            arrays[pre + f"nf_{th}"] = np.array(nf)
+            arrays[pre + f"match_{th}"] = m12
+    save("search_by_sim3.npz", **arrays)
 
 
 if __name__ == "__main__":

@@ -442,3 +442,21 @@ def test_fuse_sim3_candidates_vs_oracle(torch, oracle, seed, th, dev):
         target, _ = m.FuseSim3Candidates(frame(e.keypoints, e.descriptors, 640, 480), Scw, *cam, g, pd, usable, th)
     assert np.array_equal(target, ref)
     assert int((target >= 0).sum()) == ref_nf > 300
+
+
+@pytest.mark.parametrize("seed,th", [(0, 7.5), (1, 3.0), (2, 7.5)])
+def test_search_by_sim3_vs_oracle(torch, oracle, seed, th):
+    """SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) against the oracle."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    e = oracle.extract(syn.scene(640, 480, 170 + seed), nfeatures=1500)
+    T1, T2, s12, R12, t12, cam, g1, d1, u1, g2, d2, u2 = syn.sim3_pair_case(e.keypoints, e.descriptors, 170 + seed)
+    G1 = np.ascontiguousarray(g1).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    G2 = np.ascontiguousarray(g2).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    ref_nf, ref = oracle.search_by_sim3(e.keypoints, e.descriptors, e.keypoints, e.descriptors, 640, 480, T1, T2,
+                                        s12, R12, t12, cam, G1, d1, u1, G2, d2, u2, th)
+    KF = frame(e.keypoints, e.descriptors, 640, 480)
+    nf, m12 = ORBmatcher(0.75, True).SearchBySim3(KF, KF, T1, T2, s12, R12, t12, *cam, g1, d1, u1, g2, d2, u2, th)
+    assert nf == ref_nf
+    assert np.array_equal(m12, ref)
+    assert ref_nf > 100

@@ -364,3 +364,22 @@ def test_fuse_sim3_candidates_golden(oracle, golden, sc):
                                              g[pre + "cam"], geom, g[pre + "pdesc"], g[pre + "pstate"], 4.0)
     assert nf == int(g[pre + "nf"])
     assert np.array_equal(target, g[pre + "target"])
+
+
+def sim3_pair_inputs(g, pre):
+    G1 = np.ascontiguousarray(g[pre + "g1"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    G2 = np.ascontiguousarray(g[pre + "g2"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
+    return (g[pre + "kps"], g[pre + "desc"], g[pre + "kps"], g[pre + "desc"], 640, 480, g[pre + "T1"], g[pre + "T2"],
+            float(g[pre + "s12"]), g[pre + "R12"], g[pre + "t12"], g[pre + "cam"], G1, g[pre + "d1"], g[pre + "u1"],
+            G2, g[pre + "d2"], g[pre + "u2"])
+
+
+@pytest.mark.parametrize("sc", [0, 1])
+def test_search_by_sim3_golden(oracle, golden, sc):
+    """ORBmatcher::SearchBySim3 against the reference (its keyframe windows are squares)."""
+    g = golden("search_by_sim3.npz")
+    pre = f"s{sc}_"
+    for th in (7.5, 3.0):
+        nf, m12 = oracle.search_by_sim3(*sim3_pair_inputs(g, pre), th)
+        assert nf == int(g[pre + f"nf_{th}"])
+        assert np.array_equal(m12, g[pre + f"match_{th}"])
