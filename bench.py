@@ -168,6 +168,30 @@ def fast_bytes(frames):
     return tot
 
 
+def _world():
+    return int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def _rank():
+    return int(os.environ.get("RANK", "0"))
+
+
+def _barrier():
+    if _world() > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x):
+    if _world() == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args):
     import torch
     from orb_slam2_detailed_comments_gb300 import build
@@ -176,7 +200,7 @@ def run_ours(args):
     from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE, check, lib, ptr
     from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchProjection
 
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
     frames = workload()
     imgs_dev = [torch.from_numpy(img).to(dev) for img, _ in frames]
     nfs = [nf for _, nf in frames]
@@ -225,6 +249,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    _barrier()
     times = []
     stage_ms = {}
     with ClockSampler() as clk:
@@ -242,11 +267,18 @@ def run_ours(args):
             times.append(e0.elapsed_time(e1))
             for kname, v in batch.stage_times().items():
                 stage_ms[kname] = stage_ms.get(kname, 0.0) + v
-    total_ms = sum(times)
-    value = NFRAMES * args.steps / (total_ms / 1e3)
+    torch.cuda.synchronize()
+    _barrier()
+    # replicas: every rank ran the same step on its own GPU; the job's time is
+    # the slowest rank's and the value counts the frames of all ranks
+    total_ms = _max_over_ranks(sum(times))
+    world = _world()
+    value = world * NFRAMES * args.steps / (total_ms / 1e3)
     search_rounds = proj.rounds()  # fixed-point rounds of the slowest frame, last timed step
 
     legs = LEGS if args.legs == "all" else set(args.legs.split(","))
+    if _rank() != 0:
+        return  # the other measurements (and the JSON line) are rank 0's
     e2e_value, h2d, d2h, e2e_ways = None, 0, 0, None
     if "e2e" in legs:
         e2e_value, h2d, d2h, e2e_ways = run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_dev,
@@ -387,7 +419,7 @@ def finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, p
 
     launches = (batch.launches_per_extract() + proj.launches_per_search()) * args.steps
     line = {
-        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": _world(), "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded scenes, no dataset)",
         "config": {"workload": "batched extraction + SearchByProjection, 64 frames mixed 640x480/752x480/1241x376/"
@@ -917,14 +949,18 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    if world > 1:
-        # replicas only: every rank runs the same single-GPU workload on its own GPU
+    if _world() > 1:
+        # replicas only: every rank runs the same single-GPU workload on its
+        # own GPU (no collective on the data path; a barrier and a max of the
+        # timed region over the ranks)
         import torch
+        import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    if rank == 0 or world == 1:
-        run_ours(args)
+        dist.init_process_group("nccl")
+    run_ours(args)
+    if _world() > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

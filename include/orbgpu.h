@@ -425,9 +425,15 @@ int orbgpu_fuse_sim3_candidates(orbgpu_matcher* m, const orbgpu_frame* keyframe,
  * (row-major 3 x 3), t12: the Sim3; fx..cy: pKF1's camera (the reference
  * projects into both with it); scale_factor, nlevels: the pyramid.  Per
  * keyframe feature: mps / mpd (its map point's geometry and descriptor),
- * usable = 1 where the map point exists, is not bad and is not already in
- * vpMatches12.  match12 (host, kf1->n ints): the pKF2 feature whose map point
- * vpMatches12[i] receives, or -1; *nfound the reference's return value.
+ * usable1[i] = 1 where pKF1's map point i exists, is not bad and
+ * vpMatches12[i] is NULL; usable2[i] = 1 where pKF2's map point i exists, is
+ * not bad and i is not vpMatches12[j]->GetIndexInKeyFrame(pKF2) for any
+ * non-NULL vpMatches12[j] (the reference's vbAlreadyMatched2,
+ * src/ORBmatcher.cc:1478-1490: the pKF2 index of an already matched map
+ * point, not the map point's own slot).  match12 (host, kf1->n ints): the
+ * pKF2 feature whose map point vpMatches12[i] receives, or -1 (also for
+ * entries that were already set); *nfound the reference's return value (new
+ * matches only).
  * Host arrays; returns after the result is complete. */
 int orbgpu_search_by_sim3(orbgpu_matcher* m, const orbgpu_frame* kf1, const orbgpu_frame* kf2, const float* T1w,
                           const float* T2w, float s12, const float* R12, const float* t12, float fx, float fy,
@@ -511,6 +517,9 @@ int orbgpu_knn2_accept(const int* d1, const int* d2, int n, float ratio, uint8_t
  * the library holds that array until the process exits.  The first call on
  * a device looks up the array's device address (cudaGetSymbolAddress) with
  * that device current; make that first call before any stream capture.
+ * The address is kept for the life of the process: after a cudaDeviceReset
+ * of that device (which ends the context the address belongs to) this entry
+ * point must not be called again in the same process.
  * All calls share the one array: calls that overlap on the GPU (different
  * streams, or host threads) race and give wrong results; serialise them.
  * Asynchronous on 'stream' (NULL = the legacy default stream); all arrays on

@@ -76,10 +76,10 @@ class ExtractResult:
     pyramid: list  # unblurred levels (uint8 2-D arrays)
 
 
-def build(ref: bool = False) -> None:
+def build(ref=False) -> None:
     """Compile the restatement (and, with ref=True, the reference harness via
-    oracle/Makefile; the reference sources are only present where they were
-    mounted)."""
+    oracle/Makefile; with ref="if-present", only where the reference sources
+    are mounted -- the Makefile knows where)."""
     srcs = [os.path.join(HERE, "orb_oracle.cpp"), os.path.join(HERE, "cvshim", "cvshim_prims.cpp")]
     deps = srcs + [os.path.join(HERE, f) for f in ("orb_oracle.h", "orb_types.h", "orb_pattern_table.h")]
     deps.append(os.path.join(HERE, "cvshim", "cvshim_prims.h"))
@@ -88,7 +88,7 @@ def build(ref: bool = False) -> None:
         subprocess.run(["g++", "-O3", "-std=c++11", "-ffp-contract=off", "-fPIC", "-shared", "-o", ORACLE_SO, *srcs,
                         "-lm", "-pthread"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present" if ref == "if-present" else "ref"], check=True)
 
 
 def _p(a):

@@ -98,7 +98,8 @@ __device__ void bow_block_sort(unsigned long long* keys, int n2) {
     }
 }
 
-// One block per frame.  Shared memory: BOW_MAX_FEATURES 64-bit keys.
+// Two blocks per frame (block 2f builds frame f's BowVector, block 2f + 1 its
+// FeatureVector).  Shared memory: BOW_MAX_FEATURES 64-bit keys per block.
 __global__ void __launch_bounds__(BOW_ASM_THREADS) k_bow_assemble(
     const int* __restrict__ offsets, const int* __restrict__ word, const double* __restrict__ weight,
     const int* __restrict__ node, int weighting, int scoring, int* __restrict__ bow_counts,

@@ -151,7 +151,10 @@ static __device__ __align__(256) int4 g_knn_noalloc_partial[ORBGPU_KNN_NOALLOC_M
 
 namespace {
 std::mutex g_noalloc_mutex;
-int4* g_noalloc_partial[256] = {};  // device address of the array, per device ordinal
+// device address of the array, per device ordinal, looked up once; a
+// cudaDeviceReset ends the context that address belongs to, so it must not be
+// followed by further calls in the same process
+int4* g_noalloc_partial[256] = {};
 }  // namespace
 
 extern "C" int orbgpu_knn2_noalloc(const uint8_t* query, int nq, const uint8_t* train, int nt, int* idx1, int* d1,
@@ -168,7 +171,10 @@ extern "C" int orbgpu_knn2_noalloc(const uint8_t* query, int nq, const uint8_t* 
     if (nq == 0) return ORBGPU_OK;
     int dev = 0, nsm = 0;
     ORBGPU_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) return ORBGPU_ERR_BAD_ARG;
+    if (dev < 0 || dev >= 256) {
+        orbgpu_set_last_error("orbgpu_knn2_noalloc: device ordinal beyond 255", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
     int4* partial = nullptr;
     {
         // first call on a device: look up the array's device address with
