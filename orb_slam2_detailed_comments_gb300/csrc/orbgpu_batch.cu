@@ -108,6 +108,7 @@ struct orbgpu_batch {
     bool pending = false;       // an asynchronous extraction whose status has not been read
     int* d_status = nullptr;
     int* d_totals = nullptr;  // per frame
+    int* d_fcand = nullptr;   // FAST candidate count per (frame, level)
     int* h_pinned = nullptr;
     cudaGraphExec_t graph = nullptr;
     std::vector<int> graph_sig;
@@ -154,6 +155,7 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
     }
     if (cudaMalloc(&b->d_status, sizeof(int) * 4) != cudaSuccess ||
         cudaMalloc(&b->d_totals, sizeof(int) * max_frames) != cudaSuccess ||
+        cudaMalloc(&b->d_fcand, sizeof(int) * max_frames * ORBGPU_MAX_LEVELS) != cudaSuccess ||
         cudaMallocHost(&b->h_pinned, sizeof(int) * (8 + max_frames)) != cudaSuccess ||
         cudaMalloc(&b->d_src, sizeof(ImageSrc) * max_frames) != cudaSuccess ||
         cudaMallocHost(&b->h_src, sizeof(ImageSrc) * max_frames) != cudaSuccess) {
@@ -180,6 +182,7 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     cudaFree(b->d_prefix);
     cudaFree(b->d_status);
     cudaFree(b->d_totals);
+    cudaFree(b->d_fcand);
     cudaFree(b->d_src);
     cudaFreeHost(b->h_src);
     cudaFreeHost(b->h_pinned);
@@ -314,6 +317,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
                    f * per_frame_cap, per_frame_cap, &hd[(size_t)f * nlevels]);
         for (int l = 0; l < nlevels; l++) {
             hd[(size_t)f * nlevels + l].frame_total = b->d_totals + f;
+            hd[(size_t)f * nlevels + l].fcand_count = b->d_fcand + (size_t)f * nlevels + l;
             b->frame_scale[(size_t)f * 16 + l] = P->tables.scale[l];
         }
     }
@@ -385,9 +389,11 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     mark(0);
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
     mark(1);
+    cudaMemsetAsync(b->d_fcand, 0, sizeof(int) * b->ndesc, st);
     for (int l = 0; l < b->nlevels; l++)
         launch_resize_blur(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels}, b->rb_count[l],
                            l == 0, st);
+    launch_fast_score(b->d_descs, b->ndesc, st);
     mark(2);
     launch_fast(b->d_descs, RangeMap{b->d_prefix + b->fast_off, b->ndesc, 0, 1}, b->fast_count, b->d_status, st);
     mark(3);
@@ -395,7 +401,8 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
     mark(5);
-    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 3;  // gather, strip per level, resize per level >= 1, 3 stages
+    // gather, strip per level, resize per level >= 1, FAST scoring, 3 stages
+    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 1 + 3;
 }
 
 // The device status of the last extraction (copied to h_pinned[0] at its end)

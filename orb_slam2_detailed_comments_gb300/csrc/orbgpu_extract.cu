@@ -175,6 +175,7 @@ int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom
         L.h = (int)std::lrint((float)h * t.inv_scale[l]);
         if (L.w < 1 || L.h < 1) return ORBGPU_ERR_BAD_ARG;
         L.pitch = (L.w + 63) & ~63;
+        L.fcand_cap = std::max(0, L.w - 2 * ORBGPU_EDGE_THRESHOLD) * std::max(0, L.h - 2 * ORBGPU_EDGE_THRESHOLD);
         const int minB = ORBGPU_EDGE_THRESHOLD - 3;
         L.maxBorderX = L.w - ORBGPU_EDGE_THRESHOLD + 3;
         L.maxBorderY = L.h - ORBGPU_EDGE_THRESHOLD + 3;
@@ -226,6 +227,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         o.xalpha = take(sizeof(short) * 2 * L.w);
         o.yofs = take(sizeof(int) * L.h);
         o.ybeta = take(sizeof(short) * 2 * L.h);
+        o.fcand = take(sizeof(uint32_t) * std::max(1, L.fcand_cap));
         o.slots = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
         o.cell_count = take(sizeof(int) * std::max(1, L.ncells));
         o.cand = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
@@ -243,6 +245,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
     }
     level_counts = take(sizeof(int) * 16);
     frame_total = take(sizeof(int) * 4);
+    fcand_counts = take(sizeof(int) * 16);
     bytes = off - base;
     return off;
 }
@@ -282,6 +285,9 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.cell_count = (int*)(arena + o.cell_count);
         d.ini_th = ini_th;
         d.min_th = min_th;
+        d.fcand = (uint32_t*)(arena + o.fcand);
+        d.fcand_count = (int*)(arena + lay.fcand_counts) + l;
+        d.fcand_cap = L.fcand_cap;
         d.nfeat = L.nfeat;
         d.nIni = L.nIni;
         d.cand_cap = L.cand_cap;
@@ -688,6 +694,7 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
     cudaStream_t st = ex->stream;
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_descs, hd, sizeof(LevelDesc) * nl, cudaMemcpyHostToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(ex->d_status, 0, sizeof(int) * 4, st));
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(P.arena + P.layout.fcand_counts, 0, sizeof(int) * 16, st));
     // level 0 = the image
     ORBGPU_CUDA_TRY(cudaMemcpy2DAsync(hd[0].dst, hd[0].pitch, image, step, width, height,
                                       image_mem == ORBGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice
@@ -695,6 +702,7 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                       st));
     for (int l = 0; l < nl; l++)
         launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, st);
+    launch_fast_score(ex->d_descs, nl, st);
     launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, st);
     launch_distribute(ex->d_descs, nl, P.sort_cap, ex->d_status, st);
     launch_describe(ex->d_descs, nl, P.max_kept, okps, odesc, ex->d_status, st);

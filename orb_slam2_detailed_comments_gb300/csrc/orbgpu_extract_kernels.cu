@@ -263,26 +263,30 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
     }
 }
 
-// The 7x7 Gaussian (8-bit fixed point, REFLECT_101) and the FAST arc strength
-// of every pixel of level l.  Lane k holds the four pixels of columns
-// [x0 - 4 + 4k, x0 + 4k) of a row as one 32-bit word: lanes 1..30 own the
-// strip's columns, lanes 0 and 31 the 4-column halos (reflected outside the
-// level).  The warp walks the TH + 6 rows [y0 - 3, y0 + TH + 3) top to
-// bottom with the last seven rows in registers:
+// The 7x7 Gaussian (8-bit fixed point, REFLECT_101) of every pixel of level l
+// and the FAST compass pre-test of every pixel of the cells' detection
+// region.  Lane k holds the four pixels of columns [x0 - 4 + 4k, x0 + 4k) of a
+// row as one 32-bit word: lanes 1..30 own the strip's columns, lanes 0 and 31
+// the 4-column halos (reflected outside the level).  The warp walks the
+// TH + 6 rows [y0 - 3, y0 + TH + 3) top to bottom with the last seven rows in
+// registers:
 //  * horizontal sums by two dp4a per pixel from the lane's word and its
 //    neighbours' (shuffles), the vertical pass over seven rows of sums;
 //  * FAST at the lower threshold t: the compass-point pre-test (two circle
 //    points among 0, 4, 8, 12 that are adjacent on the circle both brighter
 //    than v + t or both darker than v - t; every nine-pixel arc contains such
 //    a pair) in 16-bit lanes gives a candidate bitmap; after every seven rows
-//    the warp compacts the candidates and scores them from a 16-row ring of
-//    level rows in shared memory.
+//    the warp appends its candidates to the level's list (one atomic per
+//    warp), which k_fast_score scores.  The strength plane is cleared here;
+//    only the candidates that are corners get a value there.
+// Only rows and columns [19, dim - 19) are tested: every cell's detection
+// region lies inside them (cells start at EDGE_THRESHOLD - 3 + 3 and end 3
+// before maxBorder = dim - EDGE_THRESHOLD + 3), and k_fast_cells reads
+// nothing else.
 // The warps of a block share nothing: no block-level synchronisation.
 template <int TH>
 struct StripShared {
-    uint32_t ring[16][32];  // level rows: input row i at i & 15
-    int rows[TH + 7];       // input row i: reflected level row
-    uint16_t cand[RS_CAND]; // (row within the 7-row block) << 7 | byte column of the ring
+    int rows[TH + 7];  // input row i: reflected level row
 };
 
 // Even (bytes 0, 2) and odd (bytes 1, 3) pixels of a word in 16-bit lanes.
@@ -302,18 +306,17 @@ __device__ __forceinline__ uint32_t rs_compass(uint32_t c, uint32_t p0, uint32_t
     return (((b0 | b8) & (b4 | b12)) | ((d0 | d8) & (d4 | d12))) & 0x80008000u;
 }
 
-// Largest arc threshold of the pixel at byte column 'col' of input row 'ic'
-// of the ring: max over the sixteen nine-pixel arcs of the arc's smallest
-// difference, for the darker-centre (v - p) and brighter-centre (p - v)
-// differences clipped at 0, which travel together in the 16-bit halves of one
-// word.  Above t exactly when the pixel is a FAST corner at threshold t.
-__device__ __forceinline__ int rs_arc_strength(const uint8_t* ring, int ic, int col) {
-    const uint8_t* R[7];
-#pragma unroll
-    for (int dy = -3; dy <= 3; dy++) R[dy + 3] = ring + (((ic + dy) & 15) << 7) + col;
-    const uint32_t v = R[3][0];
-    const uint32_t p[16] = {R[6][0], R[6][1], R[5][2],  R[4][3],  R[3][3],  R[2][3],  R[1][2],  R[0][1],
-                            R[0][0], R[0][-1], R[1][-2], R[2][-3], R[3][-3], R[4][-3], R[5][-2], R[6][-1]};
+// Largest arc threshold of the level pixel at cp (row pitch rw): max over the
+// sixteen nine-pixel arcs of the arc's smallest difference, for the
+// darker-centre (v - p) and brighter-centre (p - v) differences clipped at 0,
+// which travel together in the 16-bit halves of one word.  Above t exactly
+// when the pixel is a FAST corner at threshold t.
+__device__ __forceinline__ int level_arc_strength(const uint8_t* __restrict__ cp, int rw) {
+    const uint32_t v = __ldg(cp);
+    const uint32_t p[16] = {__ldg(cp + 3 * rw),  __ldg(cp + 3 * rw + 1),  __ldg(cp + 2 * rw + 2), __ldg(cp + rw + 3),
+                            __ldg(cp + 3),       __ldg(cp - rw + 3),      __ldg(cp - 2 * rw + 2), __ldg(cp - 3 * rw + 1),
+                            __ldg(cp - 3 * rw),  __ldg(cp - 3 * rw - 1),  __ldg(cp - 2 * rw - 2), __ldg(cp - rw - 3),
+                            __ldg(cp - 3),       __ldg(cp + rw - 3),      __ldg(cp + 2 * rw - 2), __ldg(cp + 3 * rw - 1)};
     uint32_t a[16], m2[16], m4[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) {
@@ -330,6 +333,46 @@ __device__ __forceinline__ int rs_arc_strength(const uint8_t* ring, int ic, int 
     return (int)max(best & 0xFFFFu, best >> 16);
 }
 
+// The arc strength of every FAST candidate listed by the strips of
+// descs[0 .. ndesc), written to the strength plane where it is above the
+// lower threshold.  One thread per candidate over the concatenated lists
+// (grid-stride); each block rebuilds the lists' prefix in shared memory.
+__global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict__ descs, int ndesc) {
+    extern __shared__ int s_pre[];  // ndesc + 1 prefix entries, then 32 scan words
+    int* s_scan = s_pre + ndesc + 1;
+    int carry = 0;
+    for (int b0 = 0; b0 < ndesc; b0 += blockDim.x) {
+        const int k = b0 + threadIdx.x;
+        const int c = k < ndesc ? min(*descs[k].fcand_count, descs[k].fcand_cap) : 0;
+        int tot;
+        const int ex = block_exclusive_scan(c, s_scan, &tot);
+        if (k < ndesc) s_pre[k] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) s_pre[ndesc] = carry;
+    __syncthreads();
+    const int total = s_pre[ndesc];
+    int dsc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        if (i < s_pre[dsc] || i >= s_pre[dsc + 1]) {  // the last list starting at or before i
+            int lo = 0, hi = ndesc - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_pre[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            dsc = lo;
+        }
+        const LevelDesc& d = descs[dsc];
+        const uint32_t e = d.fcand[i - s_pre[dsc]];
+        const int x = (int)(e & 0xFFFFu), y = (int)(e >> 16);
+        const int t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
+        const size_t at = (size_t)y * d.pitch + x;
+        const int sc = level_arc_strength(d.dst + at, d.pitch);
+        if (sc > t) d.strength[at] = (uint8_t)sc;
+    }
+}
+
 template <int TH>
 __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc* descs, RangeMap rm) {
     static_assert((TH + 6) % 7 == 0, "TH + 6 rows must be whole blocks of 7");
@@ -344,14 +387,14 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
     const int tile = it.index * RS_WPB + warp;
     if (tile >= tiles_x * ((h + TH - 1) / TH)) return;
     StripShared<TH>& S = sh_all[warp];
-    const uint8_t* ring8 = reinterpret_cast<const uint8_t*>(&S.ring[0][0]);
     const int x0 = (tile % tiles_x) * RS_COLS, y0 = (tile / tiles_x) * TH;
     const int X = x0 - 4 + 4 * lane;
     const bool writer = lane >= 1 && lane <= 30 && X < w;
+    // the lane's pixels inside the detection region's columns
     uint32_t colmask = 0;
 #pragma unroll
     for (int j = 0; j < 4; j++)
-        if (writer && X + j >= 3 && X + j < w - 3) colmask |= 1u << j;
+        if (writer && X + j >= ORBGPU_EDGE_THRESHOLD && X + j < w - ORBGPU_EDGE_THRESHOLD) colmask |= 1u << j;
     const int t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
     const uint32_t K = (0x8000u - (uint32_t)t - 1u) * 0x00010001u;
     for (int i = lane; i < TH + 7; i += 32) S.rows[i] = reflect101(y0 - 3 + min(i, TH + 5), h);
@@ -385,7 +428,6 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
             const int i = 7 * blk + u;
             const uint32_t c = pc;
             pc = level_word(S.rows[i + 1]);  // one row ahead
-            S.ring[i & 15][lane] = c;
             const uint32_t l = __shfl_up_sync(0xffffffffu, c, 1), r = __shfl_down_sync(0xffffffffu, c, 1);
             cw[u] = c;
             // horizontal Gaussian sums of the lane's 4 pixels (columns X + j - 3 .. X + j + 3; at most
@@ -419,7 +461,7 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
                         *reinterpret_cast<uint32_t*>(d.blur + (size_t)y * pitch + X) = blurw;
                         *reinterpret_cast<uint32_t*>(d.strength + (size_t)y * pitch + X) = 0u;
                     }
-                    if (y >= 3 && y < h - 3) {
+                    if (y >= ORBGPU_EDGE_THRESHOLD && y < h - ORBGPU_EDGE_THRESHOLD) {
                         const int cc = (u + 4) % 7, up = (u + 1) % 7;
                         const uint32_t cm = cw[cc];
                         const uint32_t lm = __shfl_up_sync(0xffffffffu, cm, 1), rm_ = __shfl_down_sync(0xffffffffu, cm, 1);
@@ -434,7 +476,7 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
                 }
             }
         }
-        // score this block's candidates (their circles lie within input rows 7 blk - 6 .. 7 blk + 6)
+        // append this block's candidates to the level's list: one atomic per warp
         if (__any_sync(0xffffffffu, bmw != 0)) {
             const int cnt = __popc(bmw);
             int incl = cnt;
@@ -443,21 +485,16 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
                 const int n = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += n;
             }
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            int pos = incl - cnt;
+            int base = 0;
+            if (lane == 31) base = atomicAdd(d.fcand_count, incl);
+            int pos = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+            const uint32_t yb = (uint32_t)(y0 + 7 * blk - 6);  // level row of bit group 0
             for (uint32_t m = bmw; m; m &= m - 1) {
                 const int b = __ffs(m) - 1;
-                S.cand[pos++] = (uint16_t)(((b >> 2) << 7) | (4 * lane + (b & 3)));
-            }
-            __syncwarp();
-            for (int q = lane; q < total; q += 32) {
-                const int e = S.cand[q];
-                const int ic = 7 * blk + (e >> 7) - 3, col = e & 127;  // centre input row, ring byte column
-                const int s = rs_arc_strength(ring8, ic, col);
-                if (s > t) d.strength[(size_t)(y0 + ic - 3) * pitch + x0 - 4 + col] = (uint8_t)s;
+                if (pos < d.fcand_cap) d.fcand[pos] = ((yb + (uint32_t)(b >> 2)) << 16) | (uint32_t)(X + (b & 3));
+                pos++;
             }
         }
-        __syncwarp();
     }
 }
 
@@ -1210,6 +1247,12 @@ int resize_blur_tiles(int w, int h) {
     const int th = tunables().resize_rows;
     const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + th - 1) / th);
     return (strips + RS_WPB - 1) / RS_WPB;
+}
+void launch_fast_score(const LevelDesc* descs, int ndesc, cudaStream_t st) {
+    if (ndesc <= 0) return;
+    const size_t smem = sizeof(int) * ((size_t)ndesc + 1 + 32);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_fast_score, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_fast_score<<<nsm_of_current_device() * 8, 256, smem, st>>>(descs, ndesc);
 }
 int fast_blocks(int ncells) {
     const int cpb = tunables().fast_cells_per_block;

@@ -3,11 +3,16 @@
 // Each kernel walks a list of work items, so the same kernels serve one frame
 // (the drop-in path) and a ragged batch of frames of different sizes.
 //
-//   k_level_strip        level l from level l-1 (cv::resize INTER_LINEAR,
-//                        11-bit fixed point), the 7x7 sigma-2 blur of level l
-//                        (REFLECT_101) and the FAST arc strength of every
-//                        pixel: one warp per 120-column strip, rows walked
-//                        with a 7-row register window.
+//   k_level_resize       level l from level l-1 (cv::resize INTER_LINEAR,
+//                        11-bit fixed point).
+//   k_level_strip        the 7x7 sigma-2 blur of level l (REFLECT_101) and the
+//                        FAST compass pre-test of every pixel of the cells'
+//                        detection region (candidates appended to a list):
+//                        one warp per 120-column strip, rows walked with a
+//                        7-row register window.
+//   k_fast_score         the arc strength of every FAST candidate the strips
+//                        listed (one thread per candidate, all levels of all
+//                        frames in one launch).
 //   k_fast_cells         one 30-px cell per warp: per-ROI non-max suppression
 //                        of the strength plane at iniThFAST and minThFAST in
 //                        one pass (the latter used when the former keeps
@@ -43,6 +48,12 @@ struct LevelDesc {
     uint32_t* slots;  // nCols*nRows*cell_cap packed (x | y << 12 | score << 24), level coordinates
     int* cell_count;  // nCols*nRows
     int ini_th, min_th;
+    // FAST candidates (pixels that passed the compass pre-test) appended by
+    // k_level_strip and scored by k_fast_score: y << 16 | x, at most one per
+    // pixel of the detection region
+    uint32_t* fcand;
+    int* fcand_count;
+    int fcand_cap;
     // distribute
     int nfeat;
     int nIni;
@@ -115,6 +126,8 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
                            const int* cb, const int* sb, const uint16_t* csub, const uint16_t* ssub, int nbuckets);
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st);
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st);
+// Scores the FAST candidates of descs[0 .. ndesc) (after every strip launch).
+void launch_fast_score(const LevelDesc* descs, int ndesc, cudaStream_t st);
 int resize_blur_tiles(int w, int h);
 int fast_blocks(int ncells);
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);

@@ -30,17 +30,18 @@ struct LevelGeom {
     int nIni;
     int cell_cap, cand_cap, node_cap;
     int nfeat;
+    int fcand_cap;  // pixels of the cells' detection region [19, w - 19) x [19, h - 19)
 };
 
 struct LevelOffsets {
-    size_t pyr, blur, strength, xofs, xalpha, yofs, ybeta, slots, cell_count, cand, node_of, quad, nodes_a, nodes_b, cnt4,
-        childpos, aux0, aux1, aux2, best, kept;
+    size_t pyr, blur, strength, xofs, xalpha, yofs, ybeta, fcand, slots, cell_count, cand, node_of, quad, nodes_a,
+        nodes_b, cnt4, childpos, aux0, aux1, aux2, best, kept;
 };
 
 // Byte offsets of one frame's buffers inside a device arena.
 struct FrameLayout {
     std::vector<LevelOffsets> lv;
-    size_t level_counts = 0, frame_total = 0;
+    size_t level_counts = 0, frame_total = 0, fcand_counts = 0;
     size_t bytes = 0;
     size_t plan(const std::vector<LevelGeom>& g, size_t base);
 };

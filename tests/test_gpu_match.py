@@ -224,6 +224,31 @@ def test_knn_tensor_cores_golden_and_ties(torch, golden):
         assert torch.equal(x, y)
 
 
+@pytest.mark.parametrize("kind", ["uniform", "clustered"])
+def test_knn_full_size_against_oracle_sample(torch, oracle, kind):
+    """The brute-force kNN at its stated size (50,000 queries x 200,000 train
+    descriptors; uniform bits, or 2,000 centres with 10 % flips): both kernels
+    over the whole problem, equal to each other, and 512 seeded queries against
+    the oracle's loop over DescriptorDistance (src/ORBmatcher.cc:2083-2103)
+    over the full train set.  Integer results: exact equality."""
+    from orb_slam2_detailed_comments_gb300 import ORBmatcher
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    if kind == "uniform":
+        q, t = syn.random_descriptors(50000, 1), syn.random_descriptors(200000, 2)
+    else:
+        q, t = syn.clustered_descriptors(50000, 2000, 0.1, 3), syn.clustered_descriptors(200000, 2000, 0.1, 4)
+    m = ORBmatcher()
+    qd, td = torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda()
+    pop = [a.cpu().numpy() for a in m.knn2(qd, td, algo=0)]
+    tc = [a.cpu().numpy() for a in m.knn2(qd, td, algo=1)]
+    for a, b, name in zip(pop, tc, ("idx1", "d1", "idx2", "d2")):
+        assert np.array_equal(a, b), f"popcount vs tensor cores: {name}"
+    sample = np.sort(np.random.default_rng(2024).choice(len(q), 512, replace=False))
+    ref = oracle.knn2(q[sample], t)
+    for a, b, name in zip(tc, ref, ("idx1", "d1", "idx2", "d2")):
+        assert np.array_equal(a[sample], b), f"tensor cores vs oracle: {name}"
+
+
 # ----------------------------------------------------------------- SearchByProjection(CurrentFrame, LastFrame)
 def frame_pair_views(kps, desc, w, h, c, dev=False, torch=None):
     """(CurrentFrame, LastFrame) views of a motion case (host or device arrays)."""
