@@ -60,6 +60,39 @@ int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const orbgpu_keypoi
                                             const int* last_offsets, const orbgpu_frame_motion* motions, float th,
                                             int mono, int check_ori, int* match_out, int* nmatches);
 
+/* ------------------------------------------------------------ serving state */
+/* The serving loop's per-stream LastFrame state (no reference counterpart:
+ * the reference keeps one Tracking object, with its mLastFrame, per camera).
+ * A store holds max_streams slots of 'cap' rows each: keypoints, map points
+ * (orbgpu_frame_mappoint) and descriptors of the stream's previous frame.
+ * All calls are asynchronous on 'stream' (a cudaStream_t); arrays are device
+ * memory. */
+typedef struct orbgpu_stream_state orbgpu_stream_state;
+int orbgpu_stream_state_create(int max_streams, int cap, orbgpu_stream_state** out);
+int orbgpu_stream_state_destroy(orbgpu_stream_state* s);
+/* LastFrame rows of a batch: frame f's previous frame is slot slots[f]; its
+ * offsets[f + 1] - offsets[f] rows (at most max_rows) are copied to
+ * last_kps / last_mps / last_desc from row offsets[f] -- the inputs of
+ * orbgpu_batch_search_by_projection_frame. */
+int orbgpu_stream_state_gather(orbgpu_stream_state* s, int nframes, const int* slots, const int* offsets,
+                               int max_rows, orbgpu_keypoint* last_kps, orbgpu_frame_mappoint* last_mps,
+                               uint8_t* last_desc, void* stream);
+/* The batch's frames become their streams' previous frames: frame f's
+ * counts[f] keypoints (rows f * cap of kps / desc, the batch's outputs) are
+ * copied to slot slots[f], each with the map point where its ray meets the
+ * plane Z = depth[f]: rays[12 f ..] = R^T K^-1 (row-major 3 x 3) and the camera
+ * centre -R^T t of the frame's pose, doubles; flags = ORBGPU_MP_* of every
+ * new map point. */
+int orbgpu_stream_state_update(orbgpu_stream_state* s, int nframes, const int* slots, const orbgpu_keypoint* kps,
+                               const uint8_t* desc, const int* counts, int cap, const double* rays,
+                               const double* depth, int flags, void* stream);
+/* TrackWithMotionModel's retry (src/Tracking.cc:1347-1353): frames whose
+ * first search found fewer than min_matches take the second search's result
+ * (match2 / nmatches2, run with 2 th); match / nmatches are updated in place
+ * (frame f's rows at f * cap). */
+int orbgpu_serving_retry_select(int* match, int* nmatches, const int* match2, const int* nmatches2, int cap,
+                                int nframes, int min_matches, void* stream);
+
 /* ------------------------------------------------------------ batch instrumentation */
 /* Device milliseconds of the five stages of the last orbgpu_batch_extract
  * (gather, resize + blur, FAST, octree, orientation + descriptor); n >= 5. */

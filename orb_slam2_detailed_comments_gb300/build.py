@@ -35,6 +35,7 @@ SOURCES = [
     "orbgpu_mappoint.cu",
     "orbgpu_geometry.cu",
     "orbgpu_bow.cu",
+    "orbgpu_serving.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

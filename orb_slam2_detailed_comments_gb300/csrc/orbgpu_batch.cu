@@ -109,6 +109,9 @@ struct orbgpu_batch {
     int* d_status = nullptr;
     int* d_totals = nullptr;  // per frame
     int* d_fcand = nullptr;   // FAST candidate count per (frame, level)
+    int* d_ccount = nullptr;  // FAST corner count per (frame, cell): frame f's cells from f * ccount_stride
+    int ccount_stride = 0;
+    size_t ccount_cap = 0;
     int* h_pinned = nullptr;
     cudaGraphExec_t graph = nullptr;
     std::vector<int> graph_sig;
@@ -117,6 +120,11 @@ struct orbgpu_batch {
     int same_sig_runs = 0;
     int launches_per_run = 0;
     cudaEvent_t ev[6] = {};
+    // the resize chain of levels 1.. runs on a second stream beside the
+    // strips (a level's strip waits for its resize only)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_level[ORBGPU_MAX_LEVELS] = {};
     // frame configuration handed to the accessors of the last batch
     std::vector<float> frame_scale;  // nframes * 16
     std::vector<int> frame_w, frame_h;
@@ -167,6 +175,14 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
             orbgpu_batch_destroy(b);
             return ORBGPU_ERR_CUDA;
         }
+    bool side_ok = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) == cudaSuccess &&
+                   cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; side_ok && i < ORBGPU_MAX_LEVELS; i++)
+        side_ok = cudaEventCreateWithFlags(&b->ev_level[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!side_ok) {
+        orbgpu_batch_destroy(b);
+        return ORBGPU_ERR_CUDA;
+    }
     b->slot_plan.assign(max_frames, nullptr);
     b->slot_gen.assign(max_frames, -1);
     *out = b;
@@ -183,11 +199,17 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     cudaFree(b->d_status);
     cudaFree(b->d_totals);
     cudaFree(b->d_fcand);
+    cudaFree(b->d_ccount);
     cudaFree(b->d_src);
     cudaFreeHost(b->h_src);
     cudaFreeHost(b->h_pinned);
     for (int i = 0; i < 6; i++)
         if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    if (b->side) cudaStreamSynchronize(b->side);
+    for (int i = 0; i < ORBGPU_MAX_LEVELS; i++)
+        if (b->ev_level[i]) cudaEventDestroy(b->ev_level[i]);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->side) cudaStreamDestroy(b->side);
     for (FramePlan* p : b->plans) delete p;
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -311,6 +333,18 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     }
     std::vector<LevelDesc> hd(ndesc);
     b->frame_scale.assign((size_t)nframes * 16, 1.0f);
+    // per-cell corner counters of all frames in one array (one memset per run)
+    int stride = 1;
+    for (int f = 0; f < nframes; f++) stride = std::max(stride, b->cur[f]->layout.ncells_total);
+    if ((size_t)stride * b->max_frames > b->ccount_cap) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        destroy_graph(b);
+        if (b->d_ccount) cudaFree(b->d_ccount);
+        b->d_ccount = nullptr;
+        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_ccount, sizeof(int) * (size_t)stride * b->max_frames));
+        b->ccount_cap = (size_t)stride * b->max_frames;
+    }
+    b->ccount_stride = stride;
     for (int f = 0; f < nframes; f++) {
         const FramePlan* P = b->cur[f];
         fill_descs(P->geom, P->tables, P->layout, b->arena + (size_t)f * b->slot_bytes, f, ini_th, min_th,
@@ -318,6 +352,8 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         for (int l = 0; l < nlevels; l++) {
             hd[(size_t)f * nlevels + l].frame_total = b->d_totals + f;
             hd[(size_t)f * nlevels + l].fcand_count = b->d_fcand + (size_t)f * nlevels + l;
+            hd[(size_t)f * nlevels + l].corner_count =
+                b->d_ccount + (size_t)f * stride + b->cur[f]->layout.corner_first[l];
             b->frame_scale[(size_t)f * 16 + l] = P->tables.scale[l];
         }
     }
@@ -390,9 +426,21 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
     mark(1);
     cudaMemsetAsync(b->d_fcand, 0, sizeof(int) * b->ndesc, st);
-    for (int l = 0; l < b->nlevels; l++)
-        launch_resize_blur(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels}, b->rb_count[l],
-                           l == 0, st);
+    cudaMemsetAsync(b->d_ccount, 0, sizeof(int) * (size_t)b->ccount_stride * b->nframes, st);
+    // levels 1.. are resized in a chain on the side stream while the strips
+    // of the levels already resized run on the batch's stream
+    cudaEventRecord(b->ev_fork, st);
+    cudaStreamWaitEvent(b->side, b->ev_fork, 0);
+    for (int l = 1; l < b->nlevels; l++) {
+        launch_level_resize(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
+                            b->rb_count[l], b->side);
+        cudaEventRecord(b->ev_level[l], b->side);
+    }
+    for (int l = 0; l < b->nlevels; l++) {
+        if (l > 0) cudaStreamWaitEvent(st, b->ev_level[l], 0);
+        launch_level_strip(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
+                           b->rb_count[l], st);
+    }
     launch_fast_score(b->d_descs, b->ndesc, st);
     mark(2);
     launch_fast(b->d_descs, RangeMap{b->d_prefix + b->fast_off, b->ndesc, 0, 1}, b->fast_count, b->d_status, st);

@@ -222,12 +222,12 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         LevelOffsets& o = lv[l];
         o.pyr = take((size_t)L.pitch * L.h);
         o.blur = take((size_t)L.pitch * L.h);
-        o.strength = take((size_t)L.pitch * L.h);
         o.xofs = take(sizeof(int) * L.w);
         o.xalpha = take(sizeof(short) * 2 * L.w);
         o.yofs = take(sizeof(int) * L.h);
         o.ybeta = take(sizeof(short) * 2 * L.h);
         o.fcand = take(sizeof(uint32_t) * std::max(1, L.fcand_cap));
+        o.corners = take(sizeof(uint32_t) * std::max<size_t>(1, (size_t)L.ncells * L.wCell * L.hCell));
         o.slots = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
         o.cell_count = take(sizeof(int) * std::max(1, L.ncells));
         o.cand = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
@@ -246,6 +246,13 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
     level_counts = take(sizeof(int) * 16);
     frame_total = take(sizeof(int) * 4);
     fcand_counts = take(sizeof(int) * 16);
+    corner_first.assign(g.size(), 0);
+    ncells_total = 0;
+    for (size_t l = 0; l < g.size(); l++) {
+        corner_first[l] = ncells_total;
+        ncells_total += g[l].ncells;
+    }
+    corner_counts = take(sizeof(int) * std::max(1, ncells_total));
     bytes = off - base;
     return off;
 }
@@ -266,7 +273,6 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         }
         d.dst = arena + o.pyr;
         d.blur = arena + o.blur;
-        d.strength = arena + o.strength;
         d.w = L.w;
         d.h = L.h;
         d.pitch = L.pitch;
@@ -288,6 +294,9 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.fcand = (uint32_t*)(arena + o.fcand);
         d.fcand_count = (int*)(arena + lay.fcand_counts) + l;
         d.fcand_cap = L.fcand_cap;
+        d.corners = (uint32_t*)(arena + o.corners);
+        d.corner_count = (int*)(arena + lay.corner_counts) + lay.corner_first[l];
+        d.corner_cap = L.wCell * L.hCell;
         d.nfeat = L.nfeat;
         d.nIni = L.nIni;
         d.cand_cap = L.cand_cap;
@@ -695,6 +704,8 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_descs, hd, sizeof(LevelDesc) * nl, cudaMemcpyHostToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(ex->d_status, 0, sizeof(int) * 4, st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(P.arena + P.layout.fcand_counts, 0, sizeof(int) * 16, st));
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(P.arena + P.layout.corner_counts, 0,
+                                    sizeof(int) * std::max(1, P.layout.ncells_total), st));
     // level 0 = the image
     ORBGPU_CUDA_TRY(cudaMemcpy2DAsync(hd[0].dst, hd[0].pitch, image, step, width, height,
                                       image_mem == ORBGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice

@@ -277,8 +277,7 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
 //    than v + t or both darker than v - t; every nine-pixel arc contains such
 //    a pair) in 16-bit lanes gives a candidate bitmap; after every seven rows
 //    the warp appends its candidates to the level's list (one atomic per
-//    warp), which k_fast_score scores.  The strength plane is cleared here;
-//    only the candidates that are corners get a value there.
+//    warp), which k_fast_score scores.
 // Only rows and columns [19, dim - 19) are tested: every cell's detection
 // region lies inside them (cells start at EDGE_THRESHOLD - 3 + 3 and end 3
 // before maxBorder = dim - EDGE_THRESHOLD + 3), and k_fast_cells reads
@@ -334,9 +333,15 @@ __device__ __forceinline__ int level_arc_strength(const uint8_t* __restrict__ cp
 }
 
 // The arc strength of every FAST candidate listed by the strips of
-// descs[0 .. ndesc), written to the strength plane where it is above the
-// lower threshold.  One thread per candidate over the concatenated lists
-// (grid-stride); each block rebuilds the lists' prefix in shared memory.
+// descs[0 .. ndesc); a candidate above the lower threshold is a corner and is
+// appended to the list of the cell whose detection region holds it (cell
+// column (x - 19) / wCell, row (y - 19) / hCell: the regions tile
+// [19, w - 19) x [19, h - 19) without overlap).  Each block takes a contiguous
+// range of the concatenated lists (consecutive threads, consecutive
+// candidates: neighbouring pixels of one level, so the circle loads share
+// cache lines) and rebuilds the lists' prefix in shared memory; a thread
+// reloads the level's fields only when its candidates cross into the next
+// level.
 __global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict__ descs, int ndesc) {
     extern __shared__ int s_pre[];  // ndesc + 1 prefix entries, then 32 scan words
     int* s_scan = s_pre + ndesc + 1;
@@ -352,24 +357,49 @@ __global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict_
     if (threadIdx.x == 0) s_pre[ndesc] = carry;
     __syncthreads();
     const int total = s_pre[ndesc];
-    int dsc = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        if (i < s_pre[dsc] || i >= s_pre[dsc + 1]) {  // the last list starting at or before i
-            int lo = 0, hi = ndesc - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (s_pre[mid] <= i) lo = mid;
-                else hi = mid - 1;
+    const int per = (total + gridDim.x - 1) / gridDim.x;
+    const int i0 = blockIdx.x * per, i1 = min(total, i0 + per);
+    int dsc = -1, lo = 0, hi = 0;
+    const uint32_t* fcand = nullptr;
+    const uint8_t* lvl = nullptr;
+    uint32_t* corners = nullptr;
+    int* ccount = nullptr;
+    int pitch = 0, t = 0, ncols = 0, wcell = 1, hcell = 1, ccap = 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        if (i >= hi) {  // the last list starting at or before i
+            int a = dsc < 0 ? 0 : dsc, b = ndesc - 1;
+            while (a < b) {
+                const int mid = (a + b + 1) >> 1;
+                if (s_pre[mid] <= i) a = mid;
+                else b = mid - 1;
             }
-            dsc = lo;
+            dsc = a;
+            lo = s_pre[dsc];
+            hi = s_pre[dsc + 1];
+            const LevelDesc& d = descs[dsc];
+            fcand = d.fcand;
+            lvl = d.dst;
+            pitch = d.pitch;
+            t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
+            corners = d.corners;
+            ccount = d.corner_count;
+            ncols = d.nCols;
+            wcell = max(d.wCell, 1);
+            hcell = max(d.hCell, 1);
+            ccap = d.corner_cap;
         }
-        const LevelDesc& d = descs[dsc];
-        const uint32_t e = d.fcand[i - s_pre[dsc]];
+        const uint32_t e = __ldg(fcand + (i - lo));
         const int x = (int)(e & 0xFFFFu), y = (int)(e >> 16);
-        const int t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
-        const size_t at = (size_t)y * d.pitch + x;
-        const int sc = level_arc_strength(d.dst + at, d.pitch);
-        if (sc > t) d.strength[at] = (uint8_t)sc;
+        const int sc = level_arc_strength(lvl + (size_t)y * pitch + x, pitch);
+        if (sc > t && ncols > 0) {
+            const int rx = x - ORBGPU_EDGE_THRESHOLD, ry = y - ORBGPU_EDGE_THRESHOLD;
+            const int cj = rx / wcell, ci = ry / hcell;
+            const int cell = ci * ncols + cj;
+            const int pos = atomicAdd(ccount + cell, 1);
+            if (pos < ccap)
+                corners[(size_t)cell * ccap + pos] =
+                    ((uint32_t)(ry - ci * hcell) << 16) | ((uint32_t)(rx - cj * wcell) << 8) | (uint32_t)sc;
+        }
     }
 }
 
@@ -457,10 +487,7 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
                     }
                     const uint32_t blurw =
                         __byte_perm(__byte_perm(acc[0], acc[1], 0x0062), __byte_perm(acc[2], acc[3], 0x0062), 0x5410);
-                    if (writer) {
-                        *reinterpret_cast<uint32_t*>(d.blur + (size_t)y * pitch + X) = blurw;
-                        *reinterpret_cast<uint32_t*>(d.strength + (size_t)y * pitch + X) = 0u;
-                    }
+                    if (writer) *reinterpret_cast<uint32_t*>(d.blur + (size_t)y * pitch + X) = blurw;
                     if (y >= ORBGPU_EDGE_THRESHOLD && y < h - ORBGPU_EDGE_THRESHOLD) {
                         const int cc = (u + 4) % 7, up = (u + 1) % 7;
                         const uint32_t cm = cw[cc];
@@ -504,7 +531,7 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
 #define FAST_MIN_CAP (33 * 33)      // survivors of a 66 x 66 region at most
 
 // The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142)
-// on the strength plane: one warp per cell.  FAST's per-ROI 3x3 suppression
+// on the cell's corner list: one warp per cell.  FAST's per-ROI 3x3 suppression
 // keeps pixel p at threshold th when its score beats every neighbour's score
 // (a neighbour that is not a corner at th, or lies outside the ROI's
 // detection region, scores 0).  On the arc strength m (score + 1) that is
@@ -513,8 +540,9 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
 // below th is below m already, and a pixel of score 0 (m = 1) loses to any
 // neighbour.  The neighbour test does not depend on th, so one pass over the
 // region yields the survivors at iniThFAST and at minThFAST; the latter are
-// used when the former are none.  The region is staged in shared memory as
-// aligned words with a zero ring; words without a corner are skipped whole.
+// used when the former are none.  The region is rebuilt in shared memory as
+// words with a zero ring (cleared, then the cell's corners scattered into
+// it); words without a corner are skipped whole.
 // Survivors are written in the detector's row-major order (lane order is
 // row-major order within an iteration).
 // CPB (cells per block, 1 / 2 / 4) is chosen by the autotuner.
@@ -546,36 +574,22 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
     }
     const int dw = rw - 6, dh = rh - 6;
     const int gx0 = iniX + 3, gy0 = iniY + 3;  // level coordinates of region pixel (0, 0)
-    // staged row: byte b <-> region column b - off - 4; words 1..nwr hold region bytes
-    const int off = gx0 & 3;
-    const int nwr = (off + 3 + dw) >> 2, nws = nwr + 2;
+    // staged row: byte b <-> region column b - 4; words 1..nwr hold region
+    // bytes; everything else stays zero (the ring)
+    const int off = 0;
+    const int nwr = (off + 3 + dw) >> 2;
     {
-        const uint8_t* g = d.strength + (size_t)gy0 * d.pitch + (gx0 - off);
-        const int rpi = 32 / nws, lr = lane / nws, lk = lane - lr * nws;
-        // keep the bytes of region columns: byte j <-> column c0 + j, c0 in [-3, dw - 1]
-        const int c0 = 4 * lk - off - 4;
-        uint32_t keep = 0;
-        if (lk >= 1 && lk <= nwr) {
-            keep = 0xFFFFFFFFu;
-            if (c0 < 0) keep <<= -8 * c0;
-            if (c0 + 4 > dw) keep &= 0xFFFFFFFFu >> (8 * (c0 + 4 - dw));
+        uint4* m16 = reinterpret_cast<uint4*>(mstr);
+        for (int k = lane; k < (dh + 2) * (FAST_ROW / 16); k += 32) m16[k] = make_uint4(0u, 0u, 0u, 0u);
+        __syncwarp();
+        // the cell's corners (arc strengths at the lower threshold), in any order
+        const int nc = min(d.corner_count[cell], d.corner_cap);
+        const uint32_t* cl = d.corners + (size_t)cell * d.corner_cap;
+        for (int k = lane; k < nc; k += 32) {
+            const uint32_t e = cl[k];
+            const int r = (int)(e >> 16), c = (int)((e >> 8) & 0xFFu);
+            if (r < dh && c < dw) mstr[(r + 1) * FAST_ROW + c + off + 4] = (uint8_t)(e & 0xFFu);
         }
-        if (lr < rpi)
-            for (int r0 = lr - 1; r0 <= dh; r0 += 8 * rpi) {  // 8 rows of loads in flight
-                uint32_t v[8];
-#pragma unroll
-                for (int u = 0; u < 8; u++) {
-                    const int r = r0 + u * rpi;
-                    v[u] = (keep && r >= 0 && r < dh)
-                               ? *reinterpret_cast<const uint32_t*>(g + (size_t)r * d.pitch + 4 * (lk - 1)) & keep
-                               : 0u;
-                }
-#pragma unroll
-                for (int u = 0; u < 8; u++) {
-                    const int r = r0 + u * rpi;
-                    if (r <= dh) *reinterpret_cast<uint32_t*>(mstr + (r + 1) * FAST_ROW + 4 * lk) = v[u];
-                }
-            }
     }
     __syncwarp();
     const int single = dw * dh == 1;
@@ -1239,6 +1253,33 @@ void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int lev
         case 22: launch_strip<22>(descs, rm, nitems, level0, st); break;
         case 64: launch_strip<64>(descs, rm, nitems, level0, st); break;
         default: launch_strip<36>(descs, rm, nitems, level0, st); break;
+    }
+}
+
+template <int TH>
+static void launch_resize_only(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
+    k_level_resize<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
+}
+template <int TH>
+static void launch_strip_only(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
+    k_level_strip<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
+}
+void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
+    if (nitems <= 0) return;
+    switch (tunables().resize_rows) {
+        case 8: launch_resize_only<8>(descs, rm, nitems, st); break;
+        case 22: launch_resize_only<22>(descs, rm, nitems, st); break;
+        case 64: launch_resize_only<64>(descs, rm, nitems, st); break;
+        default: launch_resize_only<36>(descs, rm, nitems, st); break;
+    }
+}
+void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
+    if (nitems <= 0) return;
+    switch (tunables().resize_rows) {
+        case 8: launch_strip_only<8>(descs, rm, nitems, st); break;
+        case 22: launch_strip_only<22>(descs, rm, nitems, st); break;
+        case 64: launch_strip_only<64>(descs, rm, nitems, st); break;
+        default: launch_strip_only<36>(descs, rm, nitems, st); break;
     }
 }
 

@@ -12,9 +12,10 @@
 //                        7-row register window.
 //   k_fast_score         the arc strength of every FAST candidate the strips
 //                        listed (one thread per candidate, all levels of all
-//                        frames in one launch).
+//                        frames in one launch); corners go to their cell's
+//                        list.
 //   k_fast_cells         one 30-px cell per warp: per-ROI non-max suppression
-//                        of the strength plane at iniThFAST and minThFAST in
+//                        of the cell's corners at iniThFAST and minThFAST in
 //                        one pass (the latter used when the former keeps
 //                        nothing), ordered compaction.
 //   k_distribute         one (frame, level) per block: DistributeOctTree as a
@@ -35,7 +36,6 @@ struct LevelDesc {
     int sw, sh, spitch;
     uint8_t* dst;  // level l (unblurred)
     uint8_t* blur; // level l blurred (same pitch)
-    uint8_t* strength;  // FAST arc strength of every pixel at the lower threshold (same pitch)
     int w, h, pitch;
     const int* xofs;      // resize tables of this level: source column per output column
     const short* xalpha;  // 2 weights per output column
@@ -54,6 +54,13 @@ struct LevelDesc {
     uint32_t* fcand;
     int* fcand_count;
     int fcand_cap;
+    // FAST corners at the lower threshold per cell, appended by k_fast_score
+    // in any order: cell c owns corners[c * corner_cap ..], corner_count[c]
+    // entries of (row << 16 | column << 8 | arc strength) relative to the
+    // cell's detection region; corner_cap = wCell * hCell (every pixel once)
+    uint32_t* corners;
+    int* corner_count;
+    int corner_cap;
     // distribute
     int nfeat;
     int nIni;
@@ -125,6 +132,10 @@ void upload_constants(cudaStream_t st, const int* taps, const int* umax);
 void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
                            const int* cb, const int* sb, const uint16_t* csub, const uint16_t* ssub, int nbuckets);
 void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st);
+// The two halves of launch_resize_blur, for callers that run them on
+// different streams (the strip of level l after the resize of level l).
+void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
+void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st);
 // Scores the FAST candidates of descs[0 .. ndesc) (after every strip launch).
 void launch_fast_score(const LevelDesc* descs, int ndesc, cudaStream_t st);

@@ -34,7 +34,7 @@ struct LevelGeom {
 };
 
 struct LevelOffsets {
-    size_t pyr, blur, strength, xofs, xalpha, yofs, ybeta, fcand, slots, cell_count, cand, node_of, quad, nodes_a,
+    size_t pyr, blur, xofs, xalpha, yofs, ybeta, fcand, corners, slots, cell_count, cand, node_of, quad, nodes_a,
         nodes_b, cnt4, childpos, aux0, aux1, aux2, best, kept;
 };
 
@@ -42,6 +42,11 @@ struct LevelOffsets {
 struct FrameLayout {
     std::vector<LevelOffsets> lv;
     size_t level_counts = 0, frame_total = 0, fcand_counts = 0;
+    // per-cell corner counters of every level, back to back (corner_first[l]
+    // is level l's first cell), ncells_total ints
+    size_t corner_counts = 0;
+    std::vector<int> corner_first;
+    int ncells_total = 0;
     size_t bytes = 0;
     size_t plan(const std::vector<LevelGeom>& g, size_t base);
 };
