@@ -987,47 +987,95 @@ def bench_bow(dev, steps=10, warmup=3):
                                                "sample": "4 pairs, oracle transform + SearchByBoW"}}}
 
 
-def bench_serving(dev, duration_s=3.0):
-    """32 camera streams, Poisson 30 Hz each, mixed 640x480/1241x376/1280x720,
-    nFeatures 1000-2000: every frame is extracted and matched against its
-    stream's previous frame (SearchByProjection(CurrentFrame, LastFrame),
-    monocular th 15, constant-velocity pose) with continuous batching and a
-    40 GB admission budget.  Each stream is a camera moving over a textured
-    plane (4 rendered views replayed forwards and backwards)."""
+def bench_serving(dev, base_s=3.0):
+    """32 camera streams, Poisson arrivals, mixed 640x480/1241x376/1280x720,
+    nFeatures 1000-2000: every frame is extracted (read in place from
+    page-locked host memory) and matched against its stream's previous frame
+    (SearchByProjection(CurrentFrame, LastFrame), monocular th 15,
+    constant-velocity pose, the 2 th retry below 20 matches) with continuous
+    batching, two batches in flight and a 40 GB admission budget.  Each stream
+    is a camera moving over a textured plane (4 rendered views replayed
+    forwards and backwards).  Offered load 30 Hz per stream (the workload) and
+    5x, 20x, 60x that (saturation): p50 / p99 latency from arrival to result
+    and served frames/s; the oracle on the host cores as the CPU baseline."""
     import torch
+    from oracle import pyoracle
     from orb_slam2_detailed_comments_gb300 import synthetic as syn
-    from orb_slam2_detailed_comments_gb300.serving import ServingEngine, latency_stats, pingpong, poisson_arrivals
+    from orb_slam2_detailed_comments_gb300.serving import (ServingEngine, latency_stats, overlapping_batches, pingpong,
+                                                            poisson_arrivals)
     rng = np.random.default_rng(5)
     res_opts = [(640, 480), (1241, 376), (1280, 720)]
-    e = ServingEngine(max_batch=64, hbm_budget_bytes=40 << 30)
-    data = {}
+    e = ServingEngine(max_batch=64, hbm_budget_bytes=40 << 30, inflight=2)
+    data, cams = {}, {}
     nview = 4
     for s in range(32):
         w, h = res_opts[rng.integers(0, 3)]
         nf = int(rng.choice([1000, 1500, 2000]))
         frames, poses, K, depth = syn.camera_stream(w, h, 700 + s, nview)
         if e.admit(s, w, h, nf, K=K, depth=depth):
-            data[s] = ([torch.from_numpy(f).to(dev) for f in frames], poses)
+            data[s] = ([torch.from_numpy(f).pin_memory() for f in frames], poses)
+            cams[s] = (frames, poses, K, nf)
 
     def frames_of(s, k):
         i = pingpong(k, nview)
         return data[s][0][i], data[s][1][i]
-
-    arr = poisson_arrivals(32, 30.0, duration_s, seed=9)
-    # warm-up: every (resolution, nFeatures) configuration is planned once, then a short replay
     for (w, h) in res_opts:
         for nf in (1000, 1500, 2000):
             e.warm(w, h, nf)
-    e.serve(arr[:64], frames_of, 0.3)
+    e.serve(poisson_arrivals(32, 30.0, 0.3, seed=8), frames_of, 0.3)
+    sweep = []
+    for factor in (1, 5, 20, 60):
+        dur = base_s if factor == 1 else max(0.5, base_s / factor * 5)
+        arr = poisson_arrivals(32, 30.0 * factor, dur, seed=9 + factor)
+        t0 = time.perf_counter()
+        res = e.serve(arr, frames_of, dur)
+        el = time.perf_counter() - t0
+        st = latency_stats(res)
+        st.update({"load": f"{factor}x", "offered_frames_per_s": 32 * 30.0 * factor,
+                   "served_frames_per_s": st["frames"] / el, "batches": len(e.batch_spans),
+                   "overlapping_batch_pairs": overlapping_batches(e.batch_spans),
+                   "retried": int(sum(1 for r in res if r.retried)),
+                   "mean_batch": st["frames"] / max(1, len(e.batch_spans))})
+        sweep.append(st)
+    base = sweep[0]
+    ok = [x for x in sweep if x["p99_ms"] is not None and x["p99_ms"] <= 5.0]
+    best = max(ok, key=lambda x: x["served_frames_per_s"]) if ok else None
+    # the oracle (extraction + frame-to-frame search of the same streams) on
+    # the host cores: one stream's consecutive views per task
+    o = pyoracle.Oracle()
+    sids = list(cams)[:4]
     t0 = time.perf_counter()
-    res = e.serve(arr, frames_of, duration_s)
-    el = time.perf_counter() - t0
-    st = latency_stats(res)
-    matched = [r.nmatches / max(1, r.nkeypoints) for r in res if r.nmatches]
-    st.update({"frames_per_s": len(res) / el, "offered_frames_per_s": 32 * 30.0, "streams_admitted": len(data),
-               "hbm_budget_gb": 40, "matched_fraction_median": float(np.median(matched)) if matched else None,
-               "search": "SearchByProjection(CurrentFrame, LastFrame), th 15, monocular, rotation check"})
-    return st
+    nfr = 0
+    for s in sids:
+        frames, poses, K, nf = cams[s]
+        prev = None
+        for k in range(nview):
+            r = o.extract(frames[k], nfeatures=nf, want_pyramid=False)
+            if prev is not None:
+                lm = syn.plane_mappoints(prev.keypoints, poses[k - 1], K, e.streams[s].depth)
+                T = syn.predict_pose(poses[k - 1], poses[k - 2] if k >= 2 else None)
+                mo = pyoracle.make_motion(T, poses[k - 1], *K, 0.0, 0.0)
+                o.search_by_projection_frame(r.keypoints, r.descriptors, frames[k].shape[1], frames[k].shape[0],
+                                             prev.keypoints, lm, prev.descriptors, mo, th=15.0, mono=True,
+                                             check_ori=True)
+            prev = r
+            nfr += 1
+    cpu_s = time.perf_counter() - t0
+    return {"metric": "served frames/s and p50/p99 ms, 32 camera streams (extraction + TrackWithMotionModel search)",
+            "value": base["served_frames_per_s"], "unit": "frames/s", "p50_ms": base["p50_ms"], "p99_ms": base["p99_ms"],
+            "frames": base["frames"], "offered_frames_per_s": base["offered_frames_per_s"],
+            "streams_admitted": len(data), "hbm_budget_gb": 40, "inflight_batches": len(e.workers),
+            "load_sweep": sweep,
+            "highest_load_with_p99_le_5ms": ({"load": best["load"], "served_frames_per_s": best["served_frames_per_s"],
+                                              "p99_ms": best["p99_ms"]} if best else None),
+            "e2e": {"value": base["served_frames_per_s"], "unit": "frames/s",
+                    "note": "images read in place from page-locked host memory inside each frame's latency window; "
+                            "counts and matches copied back before a result is ready"},
+            "cpu_baseline": {"value": nfr / cpu_s, "unit": "frames/s", "cores": 1, "kind": "port",
+                             "sample": f"{nfr} frames of {len(sids)} streams (extraction + frame-to-frame search)",
+                             "host": host_info()},
+            "search": "SearchByProjection(CurrentFrame, LastFrame), th 15 (2 th retry below 20), monocular, "
+                      "rotation check"}
 
 
 def host_info():

@@ -86,6 +86,9 @@ int orbgpu_stream_state_gather(orbgpu_stream_state* s, int nframes, const int* s
 int orbgpu_stream_state_update(orbgpu_stream_state* s, int nframes, const int* slots, const orbgpu_keypoint* kps,
                                const uint8_t* desc, const int* counts, int cap, const double* rays,
                                const double* depth, int flags, void* stream);
+/* Device pointers of slot 'slot''s rows (cap each; any output may be NULL). */
+int orbgpu_stream_state_slot(const orbgpu_stream_state* s, int slot, const orbgpu_keypoint** kps,
+                             const orbgpu_frame_mappoint** mps, const uint8_t** desc);
 /* TrackWithMotionModel's retry (src/Tracking.cc:1347-1353): frames whose
  * first search found fewer than min_matches take the second search's result
  * (match2 / nmatches2, run with 2 th); match / nmatches are updated in place
@@ -128,6 +131,8 @@ int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots,
 /* Launch shapes the autotuner chooses (orb_slam2_detailed_comments_gb300.autotune):
  *   "resize_rows"          strip rows of the resize / blur / FAST-strength kernel: 8, 22, 36, 64
  *   "fast_cells_per_block" FAST cells (one warp each) per block: 1, 2, 4
+ *   "fast_score_per_level" 1: score each level's FAST candidates right after its
+ *                          strip (level still in L2); 0: all levels in one launch
  *   "describe_group"       keypoints per warp of the descriptor kernel: 4, 8, 16, 32
  *   "knn_tc_min_pairs"     query x train size from which orbgpu_knn2(algo -1) uses tcgen05
  * Process-wide; a change makes extractors and batches re-plan (and re-capture

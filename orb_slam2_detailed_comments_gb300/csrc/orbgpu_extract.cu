@@ -42,6 +42,7 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
         t.fast_cells_per_block = (int)value;
     else if (n == "describe_group" && (value == 4 || value == 8 || value == 16 || value == 32))
         t.describe_group = (int)value;
+    else if (n == "fast_score_per_level" && (value == 0 || value == 1)) t.fast_score_per_level = (int)value;
     else if (n == "knn_tc_min_pairs" && value >= 0) t.knn_tc_min_pairs = value;
     else {
         orbgpu_set_last_error("unknown tuning parameter or value", __FILE__, __LINE__);
@@ -58,6 +59,7 @@ extern "C" int orbgpu_tune_get(const char* name, long long* value) {
     if (n == "resize_rows") *value = t.resize_rows;
     else if (n == "fast_cells_per_block") *value = t.fast_cells_per_block;
     else if (n == "describe_group") *value = t.describe_group;
+    else if (n == "fast_score_per_level") *value = t.fast_score_per_level;
     else if (n == "knn_tc_min_pairs") *value = t.knn_tc_min_pairs;
     else return ORBGPU_ERR_BAD_ARG;
     return ORBGPU_OK;
@@ -713,8 +715,13 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                       st));
     for (int l = 0; l < nl; l++)
         launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, st);
-    launch_fast_score(ex->d_descs, nl, st);
-    launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, st);
+    launch_fast_score(ex->d_descs, 0, 1, nl, nsm_of_current_device() * 2, st);
+    int mwc = 1, mhc = 1;
+    for (const LevelGeom& L : g) {
+        mwc = std::max(mwc, L.wCell);
+        mhc = std::max(mhc, L.hCell);
+    }
+    launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, mwc, mhc, st);
     launch_distribute(ex->d_descs, nl, P.sort_cap, ex->d_status, st);
     launch_describe(ex->d_descs, nl, P.max_kept, okps, odesc, ex->d_status, st);
     ORBGPU_CUDA_TRY(cudaGetLastError());

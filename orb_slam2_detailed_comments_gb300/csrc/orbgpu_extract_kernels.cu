@@ -333,7 +333,7 @@ __device__ __forceinline__ int level_arc_strength(const uint8_t* __restrict__ cp
 }
 
 // The arc strength of every FAST candidate listed by the strips of
-// descs[0 .. ndesc); a candidate above the lower threshold is a corner and is
+// descs[desc0 + k * stride], k < ndesc; a candidate above the lower threshold is a corner and is
 // appended to the list of the cell whose detection region holds it (cell
 // column (x - 19) / wCell, row (y - 19) / hCell: the regions tile
 // [19, w - 19) x [19, h - 19) without overlap).  Each block takes a contiguous
@@ -342,13 +342,15 @@ __device__ __forceinline__ int level_arc_strength(const uint8_t* __restrict__ cp
 // cache lines) and rebuilds the lists' prefix in shared memory; a thread
 // reloads the level's fields only when its candidates cross into the next
 // level.
-__global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict__ descs, int ndesc) {
+__global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict__ descs, int desc0, int stride,
+                                                    int ndesc) {
     extern __shared__ int s_pre[];  // ndesc + 1 prefix entries, then 32 scan words
     int* s_scan = s_pre + ndesc + 1;
+    descs += desc0;
     int carry = 0;
     for (int b0 = 0; b0 < ndesc; b0 += blockDim.x) {
         const int k = b0 + threadIdx.x;
-        const int c = k < ndesc ? min(*descs[k].fcand_count, descs[k].fcand_cap) : 0;
+        const int c = k < ndesc ? min(*descs[(size_t)k * stride].fcand_count, descs[(size_t)k * stride].fcand_cap) : 0;
         int tot;
         const int ex = block_exclusive_scan(c, s_scan, &tot);
         if (k < ndesc) s_pre[k] = carry + ex;
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict_
             dsc = a;
             lo = s_pre[dsc];
             hi = s_pre[dsc + 1];
-            const LevelDesc& d = descs[dsc];
+            const LevelDesc& d = descs[(size_t)dsc * stride];
             fcand = d.fcand;
             lvl = d.dst;
             pitch = d.pitch;
@@ -528,7 +530,6 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
 #define FAST_MAX_ROI 72
 #define FAST_MAX_DET (FAST_MAX_ROI - 6)
 #define FAST_ROW 80                 // staged row: 20 words
-#define FAST_MIN_CAP (33 * 33)      // survivors of a 66 x 66 region at most
 
 // The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142)
 // on the cell's corner list: one warp per cell.  FAST's per-ROI 3x3 suppression
@@ -547,16 +548,19 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
 // row-major order within an iteration).
 // CPB (cells per block, 1 / 2 / 4) is chosen by the autotuner.
 template <int CPB>
-__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status) {
+__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status,
+                                                          FastCellsSmem sm) {
     WorkItem it;
     map_item(rm, blockIdx.x, it.desc, it.index);
     const LevelDesc& d = descs[it.desc];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cell = it.index * CPB + warp;
     if (cell >= d.nCols * d.nRows) return;
-    __shared__ __align__(16) uint8_t s_m[CPB][(FAST_MAX_DET + 2) * FAST_ROW];
-    __shared__ uint16_t s_min[CPB][FAST_MIN_CAP];
-    uint8_t* mstr = s_m[warp];
+    // per warp: the region rows (sm.rows of FAST_ROW bytes), then sm.min_cap
+    // minThFAST survivors
+    extern __shared__ __align__(16) uint8_t s_dyn[];
+    uint8_t* mstr = s_dyn + (size_t)warp * sm.warp_bytes;
+    uint16_t* smin = reinterpret_cast<uint16_t*>(mstr + sm.rows * FAST_ROW);
     const int i = cell / d.nCols, j = cell - (cell / d.nCols) * d.nCols;
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
     const int iniY = minB + i * d.hCell, iniX = minB + j * d.wCell;
@@ -565,10 +569,10 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
     if (maxY > d.maxBorderY) maxY = d.maxBorderY;
     if (maxX > d.maxBorderX) maxX = d.maxBorderX;
     const int rw = maxX - iniX, rh = maxY - iniY;
-    if (skip || rw < 7 || rh < 7 || rw > FAST_MAX_ROI || rh > FAST_MAX_ROI) {
+    if (skip || rw < 7 || rh < 7 || rw > FAST_MAX_ROI || rh > FAST_MAX_ROI || rh - 4 > sm.rows) {
         if (lane == 0) {
             d.cell_count[cell] = 0;
-            if (!skip && (rw > FAST_MAX_ROI || rh > FAST_MAX_ROI)) atomicOr(status, 1);
+            if (!skip && (rw > FAST_MAX_ROI || rh > FAST_MAX_ROI || rh - 4 > sm.rows)) atomicOr(status, 1);
         }
         return;
     }
@@ -601,7 +605,6 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
     const int lo_th = min(ini_th, min_th);
     const uint32_t lo4 = (uint32_t)lo_th * 0x01010101u;
     uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
-    uint16_t* smin = s_min[warp];
     int total_ini = 0, total_min = 0;
     const int rpi = 32 / nwr, lr = lane / nwr, lk = lane - lr * nwr + 1;
     for (int rb = 0; rb < dh; rb += rpi) {
@@ -645,7 +648,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
             }
             for (uint32_t b = kmin; b; b &= b - 1) {
                 const int jj = __ffs(b) - 1;
-                if (pm < FAST_MIN_CAP) smin[pm] = (uint16_t)((r << 8) | (c4 + jj));
+                if (pm < sm.min_cap) smin[pm] = (uint16_t)((r << 8) | (c4 + jj));
                 pm++;
             }
             total_ini += __shfl_sync(0xffffffffu, ii, 31);
@@ -660,7 +663,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         return;
     }
     __syncwarp();
-    const int n = min(min(total_min, d.cell_cap), FAST_MIN_CAP);
+    const int n = min(min(total_min, d.cell_cap), sm.min_cap);
     for (int q = lane; q < n; q += 32) {
         const int e = smin[q], r = e >> 8, c = e & 255;
         out[q] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
@@ -1289,22 +1292,32 @@ int resize_blur_tiles(int w, int h) {
     const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + th - 1) / th);
     return (strips + RS_WPB - 1) / RS_WPB;
 }
-void launch_fast_score(const LevelDesc* descs, int ndesc, cudaStream_t st) {
+void launch_fast_score(const LevelDesc* descs, int desc0, int stride, int ndesc, int blocks, cudaStream_t st) {
     if (ndesc <= 0) return;
     const size_t smem = sizeof(int) * ((size_t)ndesc + 1 + 32);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_fast_score, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_fast_score<<<nsm_of_current_device() * 8, 256, smem, st>>>(descs, ndesc);
+    k_fast_score<<<std::max(1, blocks), 256, smem, st>>>(descs, desc0, stride, ndesc);
 }
 int fast_blocks(int ncells) {
     const int cpb = tunables().fast_cells_per_block;
     return (ncells + cpb - 1) / cpb;
 }
-void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st) {
+void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, int max_wcell, int max_hcell,
+                 cudaStream_t st) {
     if (nitems <= 0) return;
-    switch (tunables().fast_cells_per_block) {
-        case 1: k_fast_cells<1><<<nitems, 32, 0, st>>>(descs, rm, status); break;
-        case 2: k_fast_cells<2><<<nitems, 64, 0, st>>>(descs, rm, status); break;
-        default: k_fast_cells<4><<<nitems, 128, 0, st>>>(descs, rm, status); break;
+    // shared memory for the launch's largest cell: its region rows plus the
+    // zero ring, and at most one survivor per 2 x 2 pixels
+    FastCellsSmem sm;
+    sm.rows = std::min(FAST_MAX_DET, std::max(1, max_hcell)) + 2;
+    const int mw = std::min(FAST_MAX_DET, std::max(1, max_wcell)), mh = sm.rows - 2;
+    sm.min_cap = ((mw + 1) / 2) * ((mh + 1) / 2);
+    sm.warp_bytes = ((sm.rows * FAST_ROW + 2 * sm.min_cap) + 15) & ~15;
+    const int cpb = tunables().fast_cells_per_block;
+    const size_t smem = (size_t)cpb * sm.warp_bytes;
+    switch (cpb) {
+        case 1: k_fast_cells<1><<<nitems, 32, smem, st>>>(descs, rm, status, sm); break;
+        case 2: k_fast_cells<2><<<nitems, 64, smem, st>>>(descs, rm, status, sm); break;
+        default: k_fast_cells<4><<<nitems, 128, smem, st>>>(descs, rm, status, sm); break;
     }
 }
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {

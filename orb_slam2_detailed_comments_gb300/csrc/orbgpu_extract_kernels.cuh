@@ -99,6 +99,7 @@ struct Tunables {
     int resize_rows = 36;
     int fast_cells_per_block = 4;
     int describe_group = 8;
+    int fast_score_per_level = 0;  // 1: score each level right after its strip
     long long knn_tc_min_pairs = 1LL << 28;
 };
 const Tunables& tunables();
@@ -136,9 +137,18 @@ void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int lev
 // different streams (the strip of level l after the resize of level l).
 void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
 void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
-void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, cudaStream_t st);
-// Scores the FAST candidates of descs[0 .. ndesc) (after every strip launch).
-void launch_fast_score(const LevelDesc* descs, int ndesc, cudaStream_t st);
+// Shared memory layout of k_fast_cells for one launch (per warp).
+struct FastCellsSmem {
+    int rows;        // staged region rows: the largest detection region + 2
+    int min_cap;     // minThFAST survivors kept
+    int warp_bytes;  // rows * FAST_ROW + 2 * min_cap, 16-byte multiple
+};
+// max_wcell / max_hcell: the largest cell of the launch (sizes its shared memory).
+void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, int max_wcell, int max_hcell,
+                 cudaStream_t st);
+// Scores the FAST candidates of descs[desc0 + k * stride], k < ndesc (after
+// the strips of those levels) with 'blocks' blocks of 256 threads.
+void launch_fast_score(const LevelDesc* descs, int desc0, int stride, int ndesc, int blocks, cudaStream_t st);
 int resize_blur_tiles(int w, int h);
 int fast_blocks(int ncells);
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);

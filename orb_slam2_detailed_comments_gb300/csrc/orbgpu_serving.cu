@@ -177,3 +177,16 @@ extern "C" int orbgpu_serving_retry_select(int* match, int* nmatches, const int*
     ORBGPU_CUDA_TRY(cudaGetLastError());
     return ORBGPU_OK;
 }
+
+extern "C" int orbgpu_stream_state_slot(const orbgpu_stream_state* s, int slot, const orbgpu_keypoint** kps,
+                                        const orbgpu_frame_mappoint** mps, const uint8_t** desc) {
+    if (!s || slot < 0 || slot >= s->max_streams) {
+        orbgpu_set_last_error("invalid stream state slot", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    const size_t r0 = (size_t)slot * s->cap;
+    if (kps) *kps = s->kps + r0;
+    if (mps) *mps = s->mps + r0;
+    if (desc) *desc = s->desc + 32 * r0;
+    return ORBGPU_OK;
+}

@@ -1,35 +1,47 @@
 """Continuous-batching serving loop over many camera streams.
 
-Frames arrive per stream (Poisson arrivals); the loop repeatedly takes every
-frame that has arrived and is admitted (at most one per stream, so each
-stream's frames stay in order), runs ONE batched extraction over all of them
-(orbgpu_batch_extract, graph-replayed) and ONE batched frame-to-frame search
-that matches every frame against its own stream's previous frame --
-SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame, th, bMono)
-(src/ORBmatcher.cc:1710-1879) as TrackWithMotionModel calls it
-(src/Tracking.cc:1335-1346: empty CurrentFrame.mvpMapPoints, monocular th 15,
-the pose predicted by the constant-velocity model).  Requests that arrive
-while a batch is on the GPU join the next batch.
+Frames arrive per stream (Poisson arrivals).  A dispatcher forms batches from
+every arrived frame whose stream has no frame in flight (at most one frame
+per stream per batch, so each stream's frames stay in order) and hands each
+batch to a free worker; ``inflight`` workers (host threads, each with its own
+batch pipeline, CUDA stream and buffers) run their batches concurrently, so
+requests that arrive while others are on the GPU are admitted into the next
+batch and its work overlaps on the device with the batches still running.
 
-Each stream's previous keypoints, map points and descriptors stay resident
-on the device in rows of three engine-wide arrays (one gather and one
-scatter per batch); streams are admitted while their resident state fits an
-HBM budget.  The map points of a frame are its keypoints placed in the world
-by the stream's depth source: the synthetic streams view a textured plane
-Z = depth, so a keypoint's map point is its ray's intersection with that
-plane from the frame's pose (this stands in for the stereo depth or the
-triangulated map points of a real tracker).
+A batch is one batched extraction (orbgpu_batch_extract, graph-replayed, the
+images read in place from page-locked host memory) and TrackWithMotionModel's
+search for every frame against its own stream's previous frame --
+SearchByProjection(Frame& CurrentFrame, const Frame& LastFrame, th, bMono)
+(src/ORBmatcher.cc:1710-1879) as src/Tracking.cc:1321-1353 calls it: empty
+CurrentFrame.mvpMapPoints, monocular th 15, the pose predicted by the
+constant-velocity model, and a second search with 2 th for the frames whose
+first search found fewer than 20 matches.
+
+Each stream's previous keypoints, map points and descriptors stay resident in
+the library's stream state store (orbgpu_stream_state_*: one gather kernel
+before the search, one update kernel after it, both on the batch's stream).
+Streams are admitted while their resident state fits an HBM budget.  The map
+points of a frame are its keypoints placed in the world by the stream's depth
+source: the synthetic streams view a textured plane Z = depth, so a keypoint's
+map point is its ray's intersection with that plane from the frame's pose
+(this stands in for the stereo depth or the triangulated map points of a real
+tracker).
 """
 from __future__ import annotations
 
+import ctypes as C
+import queue
+import threading
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import KEYPOINT_DTYPE, MP_OBSERVED, MP_PRESENT
+from ._lib import KEYPOINT_DTYPE, MP_OBSERVED, MP_PRESENT, check, lib, ptr
 from .batch import BatchExtractor, BatchFrameProjection, motion_struct
 from .synthetic import predict_pose
+
+RETRY_BELOW = 20  # src/Tracking.cc:1347: fewer matches than this -> search again with 2 th
 
 
 @dataclass
@@ -39,10 +51,12 @@ class StreamState:
     height: int
     nfeatures: int
     resident_bytes: int
+    slot: int = 0
     K: tuple = (1.0, 1.0, 0.0, 0.0)  # fx, fy, cx, cy
     depth: float = 1.0
     prev_pose: object = None         # 3 x 4 float32 (LastFrame.mTcw)
     prevprev_pose: object = None
+    prev_n: int = 0                  # LastFrame's keypoints (rows of the stream's slot)
     frames: int = 0
 
 
@@ -53,197 +67,355 @@ class Result:
     done: float
     nkeypoints: int
     nmatches: int
+    retried: bool = False
+    error: str | None = None
+    batch: int = -1
     keypoints: object = field(default=None, repr=False)
     descriptors: object = field(default=None, repr=False)
     matches: object = field(default=None, repr=False)
 
 
+class _Worker:
+    """One batch pipeline: extractor, two frame searches (first and retry),
+    LastFrame staging, device-time events."""
+
+    def __init__(self, engine, idx):
+        t = engine.torch
+        self.idx = idx
+        self.batch = BatchExtractor(engine.max_batch, engine.max_width, engine.max_height, engine.max_nfeatures)
+        self.search1 = BatchFrameProjection(self.batch, check_ori=engine.check_ori)
+        self.search2 = BatchFrameProjection(self.batch, check_ori=engine.check_ori)
+        cap = self.batch.per_frame_capacity
+        rows = engine.max_batch * cap
+        self.lkps = t.zeros((rows, 7), dtype=t.float32, device="cuda")
+        self.lmps = t.zeros((rows, 4), dtype=t.float32, device="cuda")
+        self.ldesc = t.zeros((rows, 32), dtype=t.uint8, device="cuda")
+        self.rkps = t.zeros((rows, 7), dtype=t.float32, device="cuda")
+        self.rmps = t.zeros((rows, 4), dtype=t.float32, device="cuda")
+        self.rdesc = t.zeros((rows, 32), dtype=t.uint8, device="cuda")
+        # per-batch small arrays: slots, offsets (first search, retry), rays, depths
+        self.h_small = t.zeros(4 * (engine.max_batch + 1), dtype=t.int32).pin_memory()
+        self.d_small = t.zeros(4 * (engine.max_batch + 1), dtype=t.int32, device="cuda")
+        self.h_geo = t.zeros(13 * engine.max_batch, dtype=t.float64).pin_memory()
+        self.d_geo = t.zeros(13 * engine.max_batch, dtype=t.float64, device="cuda")
+        self.h_out = t.zeros(2 * engine.max_batch, dtype=t.int32).pin_memory()
+        self.stream = t.cuda.ExternalStream(self.batch.stream)
+        self.ev_start = t.cuda.Event(enable_timing=True)
+        self.ev_end = t.cuda.Event(enable_timing=True)
+
+
 class ServingEngine:
-    """Admission by HBM budget, per-stream device state, continuous batching."""
+    """Admission by HBM budget, per-stream device state, continuous batching
+    with 'inflight' batches on the device at once."""
 
     def __init__(self, max_batch: int = 64, max_width: int = 1280, max_height: int = 720, max_nfeatures: int = 2000,
                  hbm_budget_bytes: int = 40 << 30, th: float = 15.0, mono: bool = True, check_ori: bool = True,
-                 keep_outputs: bool = False, max_streams: int = 64):
+                 keep_outputs: bool = False, max_streams: int = 64, inflight: int = 2):
         import torch
         self.torch = torch
-        self.batch = BatchExtractor(max_batch, max_width, max_height, max_nfeatures)
-        self.search = BatchFrameProjection(self.batch, check_ori=check_ori)
         self.max_batch = max_batch
-        self.cap = self.batch.per_frame_capacity
+        self.max_width, self.max_height, self.max_nfeatures = max_width, max_height, max_nfeatures
+        self.check_ori = check_ori
         self.budget = hbm_budget_bytes
         self.used = 0
         self.th = th
         self.mono = mono
-        self.streams: dict[int, StreamState] = {}
         self.keep_outputs = keep_outputs
+        self.streams: dict[int, StreamState] = {}
         self.rejected: list[int] = []
         self.max_streams = max_streams
         self.free_slots = list(range(max_streams))
-        self.slot_of: dict[int, int] = {}
-        # previous frame of every stream slot: keypoints, map points, descriptors
-        n = max_streams * self.cap
-        self.state_kps = torch.zeros((n, 7), dtype=torch.float32, device="cuda")
-        self.state_mps = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
-        self.state_desc = torch.zeros((n, 32), dtype=torch.uint8, device="cuda")
-        self.prev_n = np.zeros(max_streams, np.int64)
-        self._col = torch.arange(self.cap, device="cuda", dtype=torch.int64)
-        self._bstream = torch.cuda.ExternalStream(self.batch.stream)
-        self._flags = float(np.array([MP_PRESENT | MP_OBSERVED], np.int32).view(np.float32)[0])
+        self.workers = [_Worker(self, i) for i in range(max(1, inflight))]
+        self.cap = self.workers[0].batch.per_frame_capacity
+        self._state = C.c_void_p()
+        check(lib().orbgpu_stream_state_create(max_streams, self.cap, C.byref(self._state)),
+              "orbgpu_stream_state_create")
+        self._flags = MP_PRESENT | MP_OBSERVED
+        self._lock = threading.Lock()
+        self._batches = 0
+        self.batch_spans = []  # (batch id, worker, device ms from the serve start: begin, end)
+        self._t0_event = None
+
+    def __del__(self):
+        st = getattr(self, "_state", None)
+        if st is not None and st.value:
+            try:
+                lib().orbgpu_stream_state_destroy(st)
+            except Exception:
+                pass
+            self._state = None
 
     # ---------------------------------------------------------------- admission
     def stream_bytes(self, w: int, h: int) -> int:
-        # previous keypoints + map points + descriptors, staging of one image
-        # and its share of the batch arena (pyramid, blurred pyramid and FAST
-        # strength planes, ~3 * 3.1 * w * h)
-        return self.cap * (28 + 16 + 32) + w * h + int(3 * 3.1 * w * h) + 64 * 1024
+        # previous keypoints + map points + descriptors, the page-locked image
+        # and its share of a batch arena (pyramid and blurred levels, FAST
+        # candidate and corner lists: ~4 * 3.1 * w * h)
+        return self.cap * (28 + 16 + 32) + w * h + int(4 * 3.1 * w * h) + 64 * 1024
 
     def admit(self, sid: int, width: int, height: int, nfeatures: int, K=None, depth: float = 8.0) -> bool:
         need = self.stream_bytes(width, height)
-        if self.used + need > self.budget or not self.free_slots:
-            self.rejected.append(sid)
-            return False
-        if K is None:
-            K = (0.9 * width, 0.9 * width, width / 2.0, height / 2.0)
-        st = StreamState(sid, width, height, nfeatures, need, tuple(float(v) for v in K), float(depth))
-        self.streams[sid] = st
-        slot = self.free_slots.pop(0)
-        self.slot_of[sid] = slot
-        self.prev_n[slot] = 0
-        self.used += need
+        with self._lock:
+            if self.used + need > self.budget or not self.free_slots:
+                self.rejected.append(sid)
+                return False
+            if K is None:
+                K = (0.9 * width, 0.9 * width, width / 2.0, height / 2.0)
+            slot = self.free_slots.pop(0)
+            self.streams[sid] = StreamState(sid, width, height, nfeatures, need, slot, tuple(float(v) for v in K),
+                                            float(depth))
+            self.used += need
         return True
 
     def release(self, sid: int) -> None:
-        st = self.streams.pop(sid, None)
-        if st:
-            self.used -= st.resident_bytes
-            slot = self.slot_of.pop(sid)
-            self.free_slots.append(slot)
+        """Removes a stream; frames of it that have not been dispatched yet are
+        dropped by the serving loop (a frame already on the device finishes,
+        its result is discarded)."""
+        with self._lock:
+            st = self.streams.pop(sid, None)
+            if st:
+                self.used -= st.resident_bytes
+                self.free_slots.append(st.slot)
 
     def warm(self, width: int, height: int, nfeatures: int, reps: int = 2) -> None:
-        """Runs one frame of a configuration through the extraction so its
-        plan exists before requests arrive."""
+        """Runs one frame of a configuration through every worker's extraction
+        so its plan exists before requests arrive."""
         t = self.torch
         img = t.zeros((height, width), dtype=t.uint8, device="cuda")
-        for _ in range(reps):
-            self.batch.extract([img], [nfeatures])
+        for w in self.workers:
+            for _ in range(reps):
+                w.batch.extract([img], [nfeatures])
+
+    def valid(self, sid: int, img) -> str | None:
+        """Why a request cannot be served (None if it can)."""
+        st = self.streams.get(sid)
+        if st is None:
+            return "stream not admitted"
+        h, w = int(img.shape[0]), int(img.shape[1])
+        if w < 1 or h < 1 or w > self.max_width or h > self.max_height or (w, h) != (st.width, st.height):
+            return f"frame size {w}x{h} not served for this stream"
+        if st.nfeatures < 1 or st.nfeatures > self.max_nfeatures:
+            return "nFeatures out of range"
+        return None
 
     # ---------------------------------------------------------------- one batch
-    def _plane_mappoints(self, kps, poses, Ks, depths):
-        """Map point rows (x, y, z, flags) of the batch's keypoints: each
-        keypoint's ray from its frame's pose meets the plane Z = depth.  The
-        per-frame ray matrix M = R^T K^-1 and camera centre C = -R^T t come
-        from the host; the device does elementwise arithmetic in a fixed
-        order, so a frame's map points do not depend on its batch."""
-        t = self.torch
-        F = len(poses)
-        M = np.zeros((F, 3, 3))
-        C = np.zeros((F, 3))
-        for f, (T, (fx, fy, cx, cy)) in enumerate(zip(poses, Ks)):
-            R = np.asarray(T, np.float64)[:, :3]
-            Kinv = np.array([[1.0 / fx, 0.0, -cx / fx], [0.0, 1.0 / fy, -cy / fy], [0.0, 0.0, 1.0]])
-            M[f] = R.T @ Kinv
-            C[f] = -R.T @ np.asarray(T, np.float64)[:, 3]
-        Md = t.from_numpy(M).cuda()
-        Cd = t.from_numpy(C).cuda()
-        dz = t.tensor(depths, dtype=t.float64, device="cuda")
-        x = kps[:, 0].reshape(F, 1, self.cap).double()
-        y = kps[:, 1].reshape(F, 1, self.cap).double()
-        dw = Md[:, :, 0:1] * x + Md[:, :, 1:2] * y + Md[:, :, 2:3]      # (F, 3, cap): ray directions
-        lam = (dz[:, None] - Cd[:, 2:3]) / dw[:, 2, :]                  # (F, cap)
-        P = Cd[:, :, None] + lam[:, None, :] * dw                        # (F, 3, cap)
-        out = t.empty((F, self.cap, 4), dtype=t.float32, device="cuda")
-        out[:, :, :3] = P.transpose(1, 2).float()
-        out[:, :, 3] = self._flags
-        return out.reshape(-1, 4)
+    def _rays(self, pose, K):
+        T = np.asarray(pose, np.float64)
+        R, tt = T[:, :3], T[:, 3]
+        fx, fy, cx, cy = K
+        Kinv = np.array([[1.0 / fx, 0.0, -cx / fx], [0.0, 1.0 / fy, -cy / fy], [0.0, 0.0, 1.0]])
+        return np.concatenate([(R.T @ Kinv).reshape(-1), -R.T @ tt])
 
-    def run_batch(self, requests):
-        """requests: list of (sid, image CUDA tensor, arrival time, true pose
-        3 x 4), at most one per stream.  Returns Results."""
+    def run_batch(self, requests, worker: int = 0):
+        """requests: list of (sid, image (page-locked host or CUDA tensor),
+        arrival time, true pose 3 x 4), at most one per stream, all valid.
+        Runs on worker 'worker''s pipeline and returns Results."""
         t = self.torch
+        W = self.workers[worker]
         cap = self.cap
         nb = len(requests)
-        sts = [self.streams[sid] for sid, _, _, _ in requests]
-        slots = np.array([self.slot_of[sid] for sid, _, _, _ in requests], np.int64)
-        kps, desc, counts = self.batch.extract([img for _, img, _, _ in requests], [st.nfeatures for st in sts])
-        # LastFrame of every frame: its stream's previous frame
-        lcount = [int(self.prev_n[s]) for s in slots]
-        rows = np.concatenate([s * cap + np.arange(n, dtype=np.int64) for s, n in zip(slots, lcount)]) \
-            if sum(lcount) else np.zeros(1, np.int64)
-        ridx = t.from_numpy(rows).to("cuda", non_blocking=True)
-        lk = t.index_select(self.state_kps, 0, ridx)
-        lm = t.index_select(self.state_mps, 0, ridx)
-        ld = t.index_select(self.state_desc, 0, ridx)
+        with self._lock:
+            sts = [self.streams[sid] for sid, _, _, _ in requests]
+            bid = self._batches
+            self._batches += 1
+        slots = [st.slot for st in sts]
+        lcount = [st.prev_n for st in sts]
+        off1 = np.zeros(nb + 1, np.int32)
+        off1[1:] = np.cumsum(lcount)
+        hs = W.h_small.numpy()
+        hs[:nb] = slots
+        hs[nb + 1:2 * nb + 2] = off1
+        bs = W.stream
+        if self._t0_event is not None:
+            W.ev_start.record(bs)
+        with t.cuda.stream(bs):
+            W.d_small.copy_(W.h_small, non_blocking=True)
+        d_slots = W.d_small[:nb]
+        d_off1 = W.d_small[nb + 1:2 * nb + 2]
+        # extraction, images read in place from page-locked host memory
+        kps, desc, counts = W.batch.extract([img for _, img, _, _ in requests], [st.nfeatures for st in sts],
+                                            wait=False)
+        # LastFrame rows of every frame, then the first search (th)
+        check(lib().orbgpu_stream_state_gather(self._state, nb, ptr(d_slots), ptr(d_off1), max(lcount + [0]),
+                                               ptr(W.lkps), ptr(W.lmps), ptr(W.ldesc), C.c_void_p(W.batch.stream)),
+              "orbgpu_stream_state_gather")
         ident = np.hstack([np.eye(3), np.zeros((3, 1))])
         motions = [motion_struct(ident, ident, *st.K) if st.prev_pose is None else
                    motion_struct(predict_pose(st.prev_pose, st.prevprev_pose), st.prev_pose, *st.K) for st in sts]
-        # the gathers run on torch's stream, the search on the batch's
-        ev = t.cuda.Event()
-        ev.record()
-        self._bstream.wait_event(ev)
-        match, nm = self.search.search(lk, lm.view(t.uint8), ld, lcount, motions, self.th, self.mono)
-        # this batch's keypoints, map points and descriptors become the streams' LastFrames
-        poses = [p for _, _, _, p in requests]
-        Ks = [st.K for st in sts]
-        depths = [st.depth for st in sts]
-        k = kps[: nb * cap]
-        dst = (t.from_numpy(slots).to("cuda", non_blocking=True)[:, None] * cap + self._col[None, :]).reshape(-1)
-        self.state_kps.index_copy_(0, dst, k)
-        self.state_mps.index_copy_(0, dst, self._plane_mappoints(k, poses, Ks, depths))
-        self.state_desc.index_copy_(0, dst, desc[: nb * cap])
-        counts_h = counts.cpu().numpy()
+        W.batch.wait()  # the extraction's status; the search below synchronises the stream anyway
+        match, nm = W.search1.search(W.lkps, W.lmps.view(t.uint8), W.ldesc, lcount, motions, self.th, self.mono)
         nm_h = nm.cpu().numpy()
+        # TrackWithMotionModel's retry: frames below RETRY_BELOW search again with 2 th
+        retry = [bool(nm_h[f] < RETRY_BELOW) for f in range(nb)]
+        if any(retry):
+            lc2 = [lcount[f] if retry[f] else 0 for f in range(nb)]
+            off2 = np.zeros(nb + 1, np.int32)
+            off2[1:] = np.cumsum(lc2)
+            hs[2 * nb + 2:3 * nb + 3] = off2
+            with t.cuda.stream(bs):
+                W.d_small[2 * nb + 2:3 * nb + 3].copy_(W.h_small[2 * nb + 2:3 * nb + 3], non_blocking=True)
+            check(lib().orbgpu_stream_state_gather(self._state, nb, ptr(d_slots), ptr(W.d_small[2 * nb + 2:]),
+                                                   max(lc2 + [0]), ptr(W.rkps), ptr(W.rmps), ptr(W.rdesc),
+                                                   C.c_void_p(W.batch.stream)),
+                  "orbgpu_stream_state_gather (retry)")
+            match2, nm2 = W.search2.search(W.rkps, W.rmps.view(t.uint8), W.rdesc, lc2, motions, 2 * self.th,
+                                           self.mono)
+            check(lib().orbgpu_serving_retry_select(ptr(match), ptr(nm), ptr(match2), ptr(nm2), cap, nb,
+                                                    RETRY_BELOW, C.c_void_p(W.batch.stream)),
+                  "orbgpu_serving_retry_select")
+        # this batch's keypoints, map points and descriptors become the streams' LastFrames
+        geo = W.h_geo.numpy()
+        for f, st in enumerate(sts):
+            geo[12 * f:12 * f + 12] = self._rays(requests[f][3], st.K)
+            geo[12 * nb + f] = st.depth
+        with t.cuda.stream(bs):
+            W.d_geo[:13 * nb].copy_(W.h_geo[:13 * nb], non_blocking=True)
+        check(lib().orbgpu_stream_state_update(self._state, nb, ptr(d_slots), ptr(kps), ptr(desc), ptr(counts), cap,
+                                               ptr(W.d_geo), ptr(W.d_geo[12 * nb:]), self._flags,
+                                               C.c_void_p(W.batch.stream)),
+              "orbgpu_stream_state_update")
+        with t.cuda.stream(bs):
+            W.h_out[:nb].copy_(counts[:nb], non_blocking=True)
+            W.h_out[nb:2 * nb].copy_(nm[:nb], non_blocking=True)
+        if self._t0_event is not None:
+            W.ev_end.record(bs)
+        bs.synchronize()
         done = time.perf_counter()
+        if self._t0_event is not None:
+            self.batch_spans.append((bid, worker, self._t0_event.elapsed_time(W.ev_start),
+                                     self._t0_event.elapsed_time(W.ev_end)))
+        ho = W.h_out.numpy()
         out = []
-        for f, (sid, _, arrival, pose) in enumerate(requests):
-            st = self.streams[sid]
-            n = int(counts_h[f])
-            self.prev_n[slots[f]] = n
-            st.prevprev_pose = st.prev_pose
-            st.prev_pose = np.asarray(pose, np.float32)
-            st.frames += 1
-            r = Result(sid, arrival, done, n, int(nm_h[f]) if lcount[f] else 0)
-            if self.keep_outputs:
-                lo = f * cap
-                r.keypoints = kps[lo:lo + n].cpu().numpy().view(KEYPOINT_DTYPE).reshape(-1)
-                r.descriptors = desc[lo:lo + n].cpu().numpy()
-                r.matches = match[lo:lo + n].cpu().numpy()
-            out.append(r)
+        with self._lock:
+            for f, (sid, _, arrival, pose) in enumerate(requests):
+                st = sts[f]
+                n = int(ho[f])
+                st.prev_n = n
+                st.prevprev_pose = st.prev_pose
+                st.prev_pose = np.asarray(pose, np.float32)
+                st.frames += 1
+                r = Result(sid, arrival, done, n, int(ho[nb + f]) if lcount[f] else 0, retried=retry[f] and lcount[f] > 0,
+                           batch=bid)
+                if self.keep_outputs:
+                    lo = f * cap
+                    r.keypoints = kps[lo:lo + n].cpu().numpy().view(KEYPOINT_DTYPE).reshape(-1)
+                    r.descriptors = desc[lo:lo + n].cpu().numpy()
+                    r.matches = match[lo:lo + n].cpu().numpy()
+                out.append(r)
         return out
 
+    def state_rows(self, sid: int):
+        """Copies of the stream's resident LastFrame rows (keypoints, map
+        points, descriptors), for tests."""
+        st = self.streams[sid]
+        k, m, d = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(lib().orbgpu_stream_state_slot(self._state, st.slot, C.byref(k), C.byref(m), C.byref(d)),
+              "orbgpu_stream_state_slot")
+        n = st.prev_n
+        kh = np.zeros(max(n, 1) * 28, np.uint8)
+        mh = np.zeros(max(n, 1) * 16, np.uint8)
+        dh = np.zeros((max(n, 1), 32), np.uint8)
+        if n:
+            for dst, src in ((kh, k), (mh, m), (dh, d)):
+                check(lib().orbgpu_copy_to_host(ptr(dst), src, C.c_size_t(dst.nbytes)), "orbgpu_copy_to_host")
+        return kh[:28 * n], mh[:16 * n], dh[:n]
+
     # ---------------------------------------------------------------- request loop
-    def serve(self, arrivals, frames_of, duration_s: float):
-        """Replays 'arrivals' (sorted list of (time_s, sid)) in real time for
-        duration_s; frames_of(sid, k) gives stream sid's k-th (image CUDA
-        tensor, true pose 3 x 4).  Returns the list of Results."""
+    def serve(self, arrivals, frames_of, duration_s: float, release_at=None):
+        """Replays 'arrivals' (sorted list of (time_s, sid)) in real time;
+        frames_of(sid, k) gives stream sid's k-th (image, true pose 3 x 4) --
+        page-locked host tensors are read in place by the extraction.
+        release_at: optional {sid: time_s} -- the stream is released then and
+        its frames not yet dispatched are dropped.  Returns the Results
+        (invalid requests come back with .error set; the others are
+        served)."""
+        t = self.torch
+        self._t0_event = t.cuda.Event(enable_timing=True)
+        self._t0_event.record()
+        self.batch_spans = []
         results = []
+        res_lock = threading.Lock()
+        work_q: queue.Queue = queue.Queue()
+        free_q: queue.Queue = queue.Queue()
+        for w in range(len(self.workers)):
+            free_q.put(w)
+        inflight_sids = set()
+        errors = []
+
+        def worker_loop():
+            while True:
+                item = work_q.get()
+                if item is None:
+                    return
+                w, batch = item
+                try:
+                    rs = self.run_batch(batch, worker=w)
+                except Exception as e:  # reported, the loop goes on
+                    errors.append(repr(e))
+                    rs = [Result(sid, arr, time.perf_counter(), 0, 0, error=repr(e)) for sid, _, arr, _ in batch]
+                with res_lock:
+                    for r in rs:
+                        if r.sid in self.streams:  # a stream released meanwhile: result discarded
+                            results.append(r)
+                        inflight_sids.discard(r.sid)
+                free_q.put(w)
+
+        threads = [threading.Thread(target=worker_loop, daemon=True) for _ in self.workers]
+        for th in threads:
+            th.start()
         t0 = time.perf_counter()
         i = 0
         pending = []
         next_frame = {sid: 0 for sid in self.streams}
+        release_at = dict(release_at or {})
         while True:
             now = time.perf_counter() - t0
+            for sid, tr in list(release_at.items()):
+                if tr <= now:
+                    self.release(sid)
+                    del release_at[sid]
+                    pending = [p for p in pending if p[0] != sid]
             while i < len(arrivals) and arrivals[i][0] <= now:
                 ta, sid = arrivals[i]
                 if sid in self.streams:
-                    img, pose = frames_of(sid, next_frame[sid])
-                    pending.append((sid, img, t0 + ta, pose))
-                    next_frame[sid] += 1
+                    img, pose = frames_of(sid, next_frame.get(sid, 0))
+                    next_frame[sid] = next_frame.get(sid, 0) + 1
+                    why = self.valid(sid, img)
+                    if why:
+                        with res_lock:
+                            results.append(Result(sid, t0 + ta, time.perf_counter(), 0, 0, error=why))
+                    else:
+                        pending.append((sid, img, t0 + ta, pose))
                 i += 1
-            if pending:
-                # one frame per stream per batch keeps each stream's frames in order
+            dispatched = False
+            if pending and not free_q.empty():
+                # one frame per stream per batch, none of a stream with a frame in flight
+                with res_lock:
+                    busy = set(inflight_sids)
                 seen, batch, rest = set(), [], []
                 for r in pending:
-                    if r[0] in seen or len(batch) >= self.max_batch:
+                    if r[0] in seen or r[0] in busy or len(batch) >= self.max_batch:
                         rest.append(r)
                     else:
                         seen.add(r[0])
                         batch.append(r)
-                pending = rest
-                results.extend(self.run_batch(batch))
-            elif i >= len(arrivals):
-                break
-            else:
-                time.sleep(max(0.0, min(0.0002, arrivals[i][0] - now)))
+                if batch:
+                    pending = rest
+                    w = free_q.get()
+                    with res_lock:
+                        inflight_sids.update(seen)
+                    work_q.put((w, batch))
+                    dispatched = True
+            if not dispatched:
+                if i >= len(arrivals) and not pending and free_q.qsize() == len(self.workers):
+                    break
+                nxt = arrivals[i][0] - now if i < len(arrivals) else 0.0002
+                time.sleep(max(0.0, min(0.0002, nxt)))
+        for _ in threads:
+            work_q.put(None)
+        for th in threads:
+            th.join()
+        if errors:
+            self.errors = errors
         return results
 
 
@@ -269,8 +441,22 @@ def poisson_arrivals(nstreams: int, rate_hz: float, duration_s: float, seed: int
 
 
 def latency_stats(results):
-    lat = np.array([(r.done - r.arrival) * 1e3 for r in results])
+    ok = [r for r in results if r.error is None]
+    lat = np.array([(r.done - r.arrival) * 1e3 for r in ok])
     if len(lat) == 0:
         return {"p50_ms": None, "p99_ms": None, "frames": 0}
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "frames": int(len(lat))}
+
+
+def overlapping_batches(spans) -> int:
+    """How many pairs of batches ran on different workers with overlapping
+    device time spans (begin, end in ms from the serve start)."""
+    n = 0
+    for a in range(len(spans)):
+        for b in range(a + 1, len(spans)):
+            _, wa, sa, ea = spans[a]
+            _, wb, sb, eb = spans[b]
+            if wa != wb and sa < eb and sb < ea:
+                n += 1
+    return n

@@ -60,11 +60,10 @@ def test_frame_search_equals_oracle(torch, oracle):
     imgs, poses, K, depth = stream(torch, 7, w, h, 3, seed0=500)
     e = ServingEngine(max_batch=2, keep_outputs=True)
     assert e.admit(0, w, h, nf, K=K, depth=depth)
-    slot = e.slot_of[0]
     prev = None
     for k in range(3):
-        n_prev = int(e.prev_n[slot])
-        last_mps = e.state_mps[slot * e.cap: slot * e.cap + n_prev].cpu().numpy().view(FRAME_MAPPOINT_DTYPE).reshape(-1)
+        _, mrows, _ = e.state_rows(0)
+        last_mps = mrows.view(FRAME_MAPPOINT_DTYPE).reshape(-1)
         (cur,) = e.run_batch([(0, imgs[k], 0.0, poses[k])])
         if k > 0:
             T = syn.predict_pose(poses[k - 1], poses[k - 2] if k >= 2 else None)
@@ -103,3 +102,77 @@ def test_serve_loop_latency(torch):
     st = latency_stats(res)
     assert st["frames"] == len(arr)
     assert st["p99_ms"] is not None and st["p99_ms"] < 1000.0
+
+
+def test_batches_overlap_and_results_match_alone(torch):
+    """Two workers: batches run concurrently on the device (their event spans
+    overlap) and every served frame equals the same stream served alone."""
+    from orb_slam2_detailed_comments_gb300.serving import ServingEngine, overlapping_batches, pingpong, poisson_arrivals
+    nfr = 3
+    data = {s: stream(torch, s, w, h, nfr, seed0=900) for s, (w, h, _) in enumerate(STREAMS * 3)}
+    pinned = {s: ([f.cpu().pin_memory() for f in d[0]], d[1]) for s, d in data.items()}
+    e = ServingEngine(max_batch=4, keep_outputs=True, inflight=2)
+    for s, (w, h, nf) in enumerate(STREAMS * 3):
+        assert e.admit(s, w, h, nf, K=data[s][2], depth=data[s][3])
+    # offered far above the engine's rate: batches queue and overlap
+    arr = poisson_arrivals(len(data), 400.0, 0.05, seed=3)
+    seen = {}
+
+    def frames_of(s, k):
+        seen.setdefault(s, []).append(pingpong(k, nfr))
+        i = pingpong(k, nfr)
+        return pinned[s][0][i], pinned[s][1][i]
+    res = e.serve(arr, frames_of, 0.05)
+    assert all(r.error is None for r in res)
+    assert len(res) == len(arr)
+    assert overlapping_batches(e.batch_spans) > 0, e.batch_spans
+    by_sid = {}
+    for r in sorted(res, key=lambda r: (r.sid, r.arrival)):
+        by_sid.setdefault(r.sid, []).append(r)
+    for s, rs in list(by_sid.items())[:5]:
+        w, h, nf = (STREAMS * 3)[s]
+        alone = ServingEngine(max_batch=1, keep_outputs=True, inflight=1)
+        assert alone.admit(s, w, h, nf, K=data[s][2], depth=data[s][3])
+        for r, i in zip(rs, seen[s]):
+            (a,) = alone.run_batch([(s, data[s][0][i], 0.0, data[s][1][i])])
+            assert a.nkeypoints == r.nkeypoints and a.nmatches == r.nmatches, (s, i)
+            assert a.keypoints.tobytes() == r.keypoints.tobytes()
+            assert np.array_equal(a.descriptors, r.descriptors)
+            assert np.array_equal(a.matches, r.matches)
+
+
+def test_bad_frame_release_and_retry(torch):
+    """Host-side failure cases of the serving loop: a frame of the wrong size
+    fails alone (the others are served and equal their alone results); a
+    stream released while it has pending frames loses them and the others are
+    unaffected; a frame with fewer than 20 first-search matches is searched
+    again with 2 th (src/Tracking.cc:1347-1353)."""
+    from orb_slam2_detailed_comments_gb300.serving import ServingEngine, pingpong
+    nfr = 3
+    data = {s: stream(torch, s, w, h, nfr, seed0=700) for s, (w, h, _) in enumerate(STREAMS)}
+    e = ServingEngine(max_batch=8, keep_outputs=True, inflight=2)
+    for s, (w, h, nf) in enumerate(STREAMS):
+        assert e.admit(s, w, h, nf, K=data[s][2], depth=data[s][3])
+    bad = torch.zeros((17, 23), dtype=torch.uint8)
+    arr = [(0.001 * k, s) for k in range(6) for s in range(len(STREAMS))]
+
+    def frames_of(s, k):
+        if s == 1 and k == 2:
+            return bad, data[s][1][0]
+        i = pingpong(k, nfr)
+        return data[s][0][i], data[s][1][i]
+    res = e.serve(arr, frames_of, 0.01, release_at={4: 0.0025})
+    errs = [r for r in res if r.error]
+    assert len(errs) == 1 and errs[0].sid == 1
+    assert all(r.sid != 4 for r in res if r.arrival - min(x.arrival for x in res) > 0.004)
+    served = {s: len([r for r in res if r.sid == s and r.error is None]) for s in range(len(STREAMS))}
+    assert served[0] == served[2] == served[3] == 6 and served[1] == 5
+    # a stream whose next frame is unrelated to the last one: few first-pass
+    # matches, so the second search (2 th) decides, as the reference's retry does
+    r0 = ServingEngine(max_batch=1, keep_outputs=True, inflight=1)
+    w, h, nf = STREAMS[0]
+    other = stream(torch, 11, w, h, 1, seed0=50)
+    assert r0.admit(0, w, h, nf, K=data[0][2], depth=data[0][3])
+    r0.run_batch([(0, data[0][0][0], 0.0, data[0][1][0])])
+    (r,) = r0.run_batch([(0, other[0][0], 0.0, data[0][1][1])])
+    assert r.retried
