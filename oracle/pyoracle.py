@@ -374,9 +374,19 @@ class _Base:
         return int(nf), out[:len(pts)].copy()
 
     def search_by_sim3(self, kps1, desc1, kps2, desc2, w, h, T1w, T2w, s12, R12, t12, cam, mps1, mpd1, st1, mps2,
-                       mpd2, st2, th=7.5, nlevels=8, scale_factor=1.2):
+                       mpd2, st2, th=7.5, nlevels=8, scale_factor=1.2, pre12=None):
         """SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) ->
-        (nfound, match12 over pKF1's features)."""
+        (nfound, match12 over pKF1's features).  st1 / st2: 0 no map point,
+        1 usable, 2 bad.  pre12: vpMatches12 entries already set (pKF2
+        feature index, -1 none) -- the reference build receives them as map
+        points (match12 then reports them), the restatement as skipped
+        features on both sides (match12 -1 there)."""
+        ref = self.prefix == "ref_"
+        if pre12 is not None and not ref:
+            pre = np.asarray(pre12)
+            st1 = np.where(pre >= 0, 0, np.asarray(st1)).astype(np.uint8)
+            st2 = np.asarray(st2).astype(np.uint8).copy()
+            st2[pre[pre >= 0]] = 0
         a = [np.ascontiguousarray(kps1, KP_DTYPE), np.ascontiguousarray(desc1, np.uint8),
              np.ascontiguousarray(kps2, KP_DTYPE), np.ascontiguousarray(desc2, np.uint8)]
         fl = [np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1)) for x in (T1w, T2w, R12, t12, cam)]
@@ -389,10 +399,11 @@ class _Base:
         f = self.fn("search_by_sim3")
         f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                       C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p] + \
-            [C.c_void_p] * 6 + [C.c_float, C.c_void_p]
+            [C.c_void_p] * 6 + [C.c_float] + ([C.c_void_p] if ref else []) + [C.c_void_p]
+        pre = [_p(np.ascontiguousarray(pre12, np.int32)) if pre12 is not None else None] if ref else []
         nf = f(C.byref(p), _p(a[0]), _p(a[1]), len(a[0]), _p(a[2]), _p(a[3]), len(a[2]), w, h, _p(fl[0]), _p(fl[1]),
                C.c_float(s12), _p(fl[2]), _p(fl[3]), _p(fl[4]), _p(g1), _p(d1), _p(s1), _p(g2), _p(d2), _p(s2),
-               C.c_float(th), _p(out))
+               C.c_float(th), *pre, _p(out))
         return int(nf), out[:len(a[0])].copy()
 
     def search_for_triangulation(self, kps1, desc1, mp1, ur1, fv1, kps2, desc2, mp2, ur2, fv2, Cw1, T2, K2, F12,

@@ -1008,7 +1008,7 @@ int ref_search_by_sim3(const orc_params* p, const orc_kp* kps1, const uint8_t* d
                            const uint8_t* desc2, int n2, int w, int h, const float* T1w, const float* T2w, float s12,
                            const float* R12, const float* t12, const float* cam, const orc_mp_geometry* mps1,
                            const uint8_t* mpd1, const uint8_t* st1, const orc_mp_geometry* mps2, const uint8_t* mpd2,
-                           const uint8_t* st2, float th, int* match12) {
+                           const uint8_t* st2, float th, const int* pre12, int* match12) {
     ArenaScope scope;
     int nf;
     {
@@ -1055,6 +1055,15 @@ int ref_search_by_sim3(const orc_params* p, const orc_kp* kps1, const uint8_t* d
         for (int k = 0; k < 9; k++) R.at<float>(k / 3, k % 3) = R12[k];
         for (int k = 0; k < 3; k++) tt.at<float>(k) = t12[k];
         std::vector<MapPoint*> matches(n1, static_cast<MapPoint*>(NULL));
+        // vpMatches12 entries already set: pKF2's map point pre12[i], observed
+        // by pKF2 at that feature (what GetIndexInKeyFrame(pKF2) reports)
+        if (pre12)
+            for (int i = 0; i < n1; i++)
+                if (pre12[i] >= 0 && pre12[i] < n2 && K2->mvpMapPoints[pre12[i]]) {
+                    MapPoint* mp = K2->mvpMapPoints[pre12[i]];
+                    mp->AddObservation(K2, pre12[i]);
+                    matches[i] = mp;
+                }
         ORBmatcher matcher(0.75f, true);
         const float s = s12;
         nf = matcher.SearchBySim3(K1, K2, matches, s, R, tt, th);

@@ -585,31 +585,59 @@ def fuse_case(kps: np.ndarray, desc: np.ndarray, seed: int, w: int = 640, h: int
     return Tcw, np.array([cam[0], cam[1], cam[2], cam[3], 40.0], np.float32), g, pd, ps, ur
 
 
-def sim3_pair_case(kps: np.ndarray, desc: np.ndarray, seed: int, w: int = 640, h: int = 480, fx: float = 500.0):
-    """Inputs of SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th): both
-    keyframes are the frame (kps, desc) under one random pose, related by a
-    Sim3 near the identity (s12 1 +- 0.02, rotations of about 0.3 degrees,
-    translations of a few centimetres), so the map points project near their
-    features both ways.  About 60 % of each keyframe's features carry a map
-    point: the back-projection of that feature at a random depth, its
-    descriptor with a few bits flipped, distances placing the predicted level
-    at the feature's octave (a tenth of the map points bad).  Returns (T1w,
-    T2w, s12, R12, t12, cam (fx, fy, cx, cy), geometry1, desc1, usable1,
-    geometry2, desc2, usable2)."""
-    rng = np.random.default_rng(seed)
-    n = len(kps)
+def sim3_pair_images(seed: int, w: int = 640, h: int = 480, fx: float = 500.0, z0: float = 5.0):
+    """Two views of one fronto-parallel textured plane for SearchBySim3:
+    image 1 is a scene, image 2 the same plane seen by a camera rotated about
+    its optical axis (up to 3 degrees) and shifted (up to 10 px at depth z0)
+    -- image 2 is image 1 under the matching homography plus noise.  Returns
+    (image1, image2, geometry) with geometry = (R21, t21, z0): camera-2
+    coordinates P2 = R21 P1 + t21 of a camera-1 point P1."""
+    img1 = scene(w, h, seed)
+    rng = np.random.default_rng(seed + 7919)
+    H = random_homography(w, h, rng)
+    img2 = warp(img1, H, seed + 104729)
+    c, sn = H[0, 0], H[1, 0]
     cx, cy = w / 2.0, h / 2.0
-    R = _rotation(*rng.normal(0, 0.2, 3))
-    t = rng.normal(0, 0.5, 3)
-    T = np.hstack([R, t[:, None]]).astype(np.float32)
-    s12 = np.float32(1.0 + rng.uniform(-0.02, 0.02))
-    R12 = _rotation(*rng.normal(0, 0.005, 3)).astype(np.float32)
-    t12 = rng.normal(0, 0.03, 3).astype(np.float32)
+    # p2 - c = R(p1 - c) + (tx, ty): recover the pixel translation
+    tx = H[0, 2] - (cx - c * cx + sn * cy)
+    ty = H[1, 2] - (cy - sn * cx - c * cy)
+    R21 = np.array([[c, -sn, 0.0], [sn, c, 0.0], [0.0, 0.0, 1.0]])
+    t21 = np.array([tx * z0 / fx, ty * z0 / fx, 0.0])
+    return img1, img2, (R21, t21, z0)
 
-    def side(sd):
+
+def sim3_pair_case(kps1: np.ndarray, desc1: np.ndarray, kps2: np.ndarray, desc2: np.ndarray, geometry, seed: int,
+                   w: int = 640, h: int = 480, fx: float = 500.0, prematched: float = 0.08):
+    """Inputs of SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) for
+    two keyframes of different poses and feature sets: (kps1, desc1) and
+    (kps2, desc2) are the extractions of sim3_pair_images' two views.  Each
+    keyframe gets its own random world pose (their world frames disagree, as
+    a loop's do); the Sim3 maps camera 2 to camera 1 (s12 1 +- 0.003 around the
+    views' true rigid motion).  About 60 % of each keyframe's features carry a
+    map point (a tenth of them bad): the back-projection of the feature onto
+    the plane, its descriptor with a few bits flipped, distances placing the
+    predicted level at the feature's octave.  vpMatches12 already holds
+    'prematched' of pKF1's usable map points: pre12[i] = the pKF2 feature
+    whose map point it is (the nearest pKF2 keypoint to the feature's
+    projection that has a map point), -1 elsewhere.  Returns (T1w, T2w, s12,
+    R12, t12, cam (fx, fy, cx, cy), geometry1, desc1, state1, geometry2, desc2,
+    state2, pre12) with state 0 no map point, 1 usable, 2 bad."""
+    R21, t21, z0 = geometry
+    rng = np.random.default_rng(seed)
+    cx, cy = w / 2.0, h / 2.0
+    s12 = np.float32(1.0 + rng.uniform(-0.003, 0.003))
+    R12 = R21.T.astype(np.float32)
+    t12 = (-(R21.T @ t21)).astype(np.float32)
+
+    def pose():
+        R = _rotation(*rng.normal(0, 0.2, 3))
+        t = rng.normal(0, 0.5, 3)
+        return R, t, np.hstack([R, t[:, None]]).astype(np.float32)
+
+    def side(kps, desc, R, t, sd):
         r = np.random.default_rng(sd)
-        z = r.uniform(2.0, 20.0, n)
-        pc = np.stack([(kps["x"] - cx) / fx * z, (kps["y"] - cy) / fx * z, z], 1)
+        n = len(kps)
+        pc = np.stack([(kps["x"] - cx) / fx * z0, (kps["y"] - cy) / fx * z0, np.full(n, z0)], 1)
         pw = (R.T @ (pc - t).T).T
         d = np.linalg.norm(pc, axis=1)
         maxd = d * 1.2 ** (kps["octave"] + r.uniform(-0.3, 0.3, n))
@@ -620,9 +648,41 @@ def sim3_pair_case(kps: np.ndarray, desc: np.ndarray, seed: int, w: int = 640, h
         flips = r.integers(0, 256, (n, 32), dtype=np.uint8)
         for _ in range(3):
             flips &= r.integers(0, 256, (n, 32), dtype=np.uint8)
-        usable = ((r.random(n) < 0.6) & (r.random(n) > 0.1)).astype(np.uint8)
-        return g, desc ^ flips, usable
+        u = r.random(n)
+        state = np.where(u < 0.06, 2, np.where(u < 0.6, 1, 0)).astype(np.uint8)
+        return g, desc ^ flips, state
 
-    g1, d1, u1 = side(seed * 2 + 1)
-    g2, d2, u2 = side(seed * 2 + 2)
-    return (T, T.copy(), s12, R12, t12, np.array([fx, fx, cx, cy], np.float32), g1, d1, u1, g2, d2, u2)
+    R1, t1, T1 = pose()
+    R2, t2, T2 = pose()
+    g1, d1, st1 = side(kps1, desc1, R1, t1, seed * 2 + 1)
+    g2, d2, st2 = side(kps2, desc2, R2, t2, seed * 2 + 2)
+    # vpMatches12 entries that are already set
+    pre12 = np.full(len(kps1), -1, np.int32)
+    p1 = np.stack([kps1["x"], kps1["y"]], 1).astype(np.float64)
+    P1 = np.concatenate([(p1 - [cx, cy]) / fx * z0, np.full((len(p1), 1), z0)], 1)
+    P2 = (R21 @ P1.T).T + t21
+    proj = P2[:, :2] / P2[:, 2:3] * fx + [cx, cy]
+    p2 = np.stack([kps2["x"], kps2["y"]], 1).astype(np.float64)
+    taken = set()
+    for i in np.nonzero(st1 == 1)[0]:
+        if rng.random() >= prematched:
+            continue
+        dd = np.hypot(*(p2 - proj[i]).T)
+        for j in np.argsort(dd)[:3]:
+            if st2[j] != 0 and j not in taken and dd[j] < 3.0:
+                pre12[i] = j
+                taken.add(int(j))
+                break
+    return T1, T2, s12, R12, t12, np.array([fx, fx, cx, cy], np.float32), g1, d1, st1, g2, d2, st2, pre12
+
+
+def sim3_usable(state1, state2, pre12):
+    """usable1 / usable2 of orbgpu_search_by_sim3 (and the oracle's states)
+    for pre-set vpMatches12: pKF1 feature i is skipped where vpMatches12[i]
+    is set, pKF2's map point j where j = vpMatches12[i]->GetIndexInKeyFrame(pKF2)
+    for some i (src/ORBmatcher.cc:1478-1490)."""
+    u1 = (np.asarray(state1) == 1) & (np.asarray(pre12) < 0)
+    u2 = np.asarray(state2) == 1
+    u2 = u2.copy()
+    u2[np.asarray(pre12)[np.asarray(pre12) >= 0]] = False
+    return u1.astype(np.uint8), u2.astype(np.uint8)

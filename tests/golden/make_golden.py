@@ -471,21 +471,27 @@ def fuse_fixture(R):
 
 
 def by_sim3_fixture(R):
-    # 18. ORBmatcher::SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th)
+    # 18. ORBmatcher::SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th):
+    # two views of a plane (different poses and feature sets), some
+    # vpMatches12 entries already set
     from oracle.pyoracle import GEOM_DTYPE
     arrays = {}
     for sc in range(2):
-        e = R.extract(syn.scene(640, 480, 110 + sc), nfeatures=1500)
-        T1, T2, s12, R12, t12, cam, g1, d1, u1, g2, d2, u2 = syn.sim3_pair_case(e.keypoints, e.descriptors, 110 + sc)
+        img1, img2, geo = syn.sim3_pair_images(110 + sc)
+        e1 = R.extract(img1, nfeatures=1500)
+        e2 = R.extract(img2, nfeatures=1200)
+        T1, T2, s12, R12, t12, cam, g1, d1, st1, g2, d2, st2, pre12 = syn.sim3_pair_case(
+            e1.keypoints, e1.descriptors, e2.keypoints, e2.descriptors, geo, 110 + sc)
         G1 = np.ascontiguousarray(g1).view(GEOM_DTYPE).reshape(-1)
         G2 = np.ascontiguousarray(g2).view(GEOM_DTYPE).reshape(-1)
         pre = f"s{sc}_"
-        arrays.update({pre + "kps": e.keypoints, pre + "desc": e.descriptors, pre + "T1": T1, pre + "T2": T2,
-                       pre + "s12": np.float32(s12), pre + "R12": R12, pre + "t12": t12, pre + "cam": cam,
-                       pre + "g1": g1, pre + "d1": d1, pre + "u1": u1, pre + "g2": g2, pre + "d2": d2, pre + "u2": u2})
+        arrays.update({pre + "kps1": e1.keypoints, pre + "desc1": e1.descriptors, pre + "kps2": e2.keypoints,
+                       pre + "desc2": e2.descriptors, pre + "T1": T1, pre + "T2": T2, pre + "s12": np.float32(s12),
+                       pre + "R12": R12, pre + "t12": t12, pre + "cam": cam, pre + "g1": g1, pre + "d1": d1,
+                       pre + "st1": st1, pre + "g2": g2, pre + "d2": d2, pre + "st2": st2, pre + "pre12": pre12})
         for th in (7.5, 3.0):
-            nf, m12 = R.search_by_sim3(e.keypoints, e.descriptors, e.keypoints, e.descriptors, 640, 480, T1, T2, s12,
-                                       R12, t12, cam, G1, d1, u1, G2, d2, u2, th)
+            nf, m12 = R.search_by_sim3(e1.keypoints, e1.descriptors, e2.keypoints, e2.descriptors, 640, 480, T1, T2,
+                                       s12, R12, t12, cam, G1, d1, st1, G2, d2, st2, th, pre12=pre12)
             arrays[pre + f"nf_{th}"] = np.array(nf)
             arrays[pre + f"match_{th}"] = m12
     save("search_by_sim3.npz", **arrays)

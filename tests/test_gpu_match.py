@@ -471,17 +471,25 @@ def test_fuse_sim3_candidates_vs_oracle(torch, oracle, seed, th, dev):
 
 @pytest.mark.parametrize("seed,th", [(0, 7.5), (1, 3.0), (2, 7.5)])
 def test_search_by_sim3_vs_oracle(torch, oracle, seed, th):
-    """SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) against the oracle."""
+    """SearchBySim3(pKF1, pKF2, vpMatches12, s12, R12, t12, th) against the
+    oracle: two views of a plane (keyframes of different poses and feature
+    sets), part of vpMatches12 already set and encoded through usable1 /
+    usable2."""
     from orb_slam2_detailed_comments_gb300 import ORBmatcher
     from orb_slam2_detailed_comments_gb300 import synthetic as syn
-    e = oracle.extract(syn.scene(640, 480, 170 + seed), nfeatures=1500)
-    T1, T2, s12, R12, t12, cam, g1, d1, u1, g2, d2, u2 = syn.sim3_pair_case(e.keypoints, e.descriptors, 170 + seed)
+    img1, img2, geo = syn.sim3_pair_images(170 + seed)
+    e1 = oracle.extract(img1, nfeatures=1500)
+    e2 = oracle.extract(img2, nfeatures=1200)
+    T1, T2, s12, R12, t12, cam, g1, d1, st1, g2, d2, st2, pre12 = syn.sim3_pair_case(
+        e1.keypoints, e1.descriptors, e2.keypoints, e2.descriptors, geo, 170 + seed)
     G1 = np.ascontiguousarray(g1).view(pyoracle.GEOM_DTYPE).reshape(-1)
     G2 = np.ascontiguousarray(g2).view(pyoracle.GEOM_DTYPE).reshape(-1)
-    ref_nf, ref = oracle.search_by_sim3(e.keypoints, e.descriptors, e.keypoints, e.descriptors, 640, 480, T1, T2,
-                                        s12, R12, t12, cam, G1, d1, u1, G2, d2, u2, th)
-    KF = frame(e.keypoints, e.descriptors, 640, 480)
-    nf, m12 = ORBmatcher(0.75, True).SearchBySim3(KF, KF, T1, T2, s12, R12, t12, *cam, g1, d1, u1, g2, d2, u2, th)
+    ref_nf, ref = oracle.search_by_sim3(e1.keypoints, e1.descriptors, e2.keypoints, e2.descriptors, 640, 480, T1, T2,
+                                        s12, R12, t12, cam, G1, d1, st1, G2, d2, st2, th, pre12=pre12)
+    u1, u2 = syn.sim3_usable(st1, st2, pre12)
+    nf, m12 = ORBmatcher(0.75, True).SearchBySim3(frame(e1.keypoints, e1.descriptors, 640, 480),
+                                                  frame(e2.keypoints, e2.descriptors, 640, 480), T1, T2, s12, R12,
+                                                  t12, *cam, g1, d1, u1, g2, d2, u2, th)
     assert nf == ref_nf
     assert np.array_equal(m12, ref)
-    assert ref_nf > 100
+    assert ref_nf > 100 and (pre12 >= 0).sum() > 20

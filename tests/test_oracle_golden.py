@@ -369,17 +369,23 @@ def test_fuse_sim3_candidates_golden(oracle, golden, sc):
 def sim3_pair_inputs(g, pre):
     G1 = np.ascontiguousarray(g[pre + "g1"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
     G2 = np.ascontiguousarray(g[pre + "g2"]).view(pyoracle.GEOM_DTYPE).reshape(-1)
-    return (g[pre + "kps"], g[pre + "desc"], g[pre + "kps"], g[pre + "desc"], 640, 480, g[pre + "T1"], g[pre + "T2"],
-            float(g[pre + "s12"]), g[pre + "R12"], g[pre + "t12"], g[pre + "cam"], G1, g[pre + "d1"], g[pre + "u1"],
-            G2, g[pre + "d2"], g[pre + "u2"])
+    return (g[pre + "kps1"], g[pre + "desc1"], g[pre + "kps2"], g[pre + "desc2"], 640, 480, g[pre + "T1"],
+            g[pre + "T2"], float(g[pre + "s12"]), g[pre + "R12"], g[pre + "t12"], g[pre + "cam"], G1, g[pre + "d1"],
+            g[pre + "st1"], G2, g[pre + "d2"], g[pre + "st2"])
 
 
 @pytest.mark.parametrize("sc", [0, 1])
 def test_search_by_sim3_golden(oracle, golden, sc):
-    """ORBmatcher::SearchBySim3 against the reference (its keyframe windows are squares)."""
+    """ORBmatcher::SearchBySim3 against the reference (its keyframe windows are
+    squares): two keyframes with different poses and feature sets, part of
+    vpMatches12 already set (the reference reports those entries; the
+    restatement skips them, as usable1 / usable2 encode)."""
     g = golden("search_by_sim3.npz")
     pre = f"s{sc}_"
+    pre12 = g[pre + "pre12"]
+    assert len(g[pre + "kps1"]) != len(g[pre + "kps2"]) and (pre12 >= 0).sum() > 20
     for th in (7.5, 3.0):
-        nf, m12 = oracle.search_by_sim3(*sim3_pair_inputs(g, pre), th)
-        assert nf == int(g[pre + f"nf_{th}"])
-        assert np.array_equal(m12, g[pre + f"match_{th}"])
+        nf, m12 = oracle.search_by_sim3(*sim3_pair_inputs(g, pre), th, pre12=pre12)
+        assert nf == int(g[pre + f"nf_{th}"]) > 100
+        assert np.array_equal(np.where(pre12 >= 0, pre12, m12), g[pre + f"match_{th}"])
+        assert np.all(m12[pre12 >= 0] == -1)
