@@ -436,17 +436,13 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
                             b->rb_count[l], b->side);
         cudaEventRecord(b->ev_level[l], b->side);
     }
-    const int nsm = nsm_of_current_device();
-    const bool per_level = tunables().fast_score_per_level != 0;
     for (int l = 0; l < b->nlevels; l++) {
         if (l > 0) cudaStreamWaitEvent(st, b->ev_level[l], 0);
         launch_level_strip(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
                            b->rb_count[l], st);
-        // each level's candidates while its plane is still in L2, or all at once
-        if (per_level)
-            launch_fast_score(b->d_descs, l, b->nlevels, b->nframes, std::max(1, (nsm * 8) >> l), st);
     }
-    if (!per_level) launch_fast_score(b->d_descs, 0, 1, b->ndesc, nsm * 8, st);
+    // the candidates of every level of every frame in one launch
+    launch_fast_score(b->d_descs, 0, 1, b->ndesc, nsm_of_current_device() * 8, st);
     mark(2);
     int mwc = 1, mhc = 1;
     for (int f = 0; f < b->nframes; f++)
@@ -461,9 +457,8 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
     mark(5);
-    // gather, strip per level, resize per level >= 1, FAST scoring (per level
-    // or once), 3 stages
-    b->launches_per_run = 1 + 2 * b->nlevels - 1 + (per_level ? b->nlevels : 1) + 3;
+    // gather, strip per level, resize per level >= 1, FAST scoring, 3 stages
+    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 1 + 3;
 }
 
 // The device status of the last extraction (copied to h_pinned[0] at its end)

@@ -361,46 +361,67 @@ __global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict_
     const int total = s_pre[ndesc];
     const int per = (total + gridDim.x - 1) / gridDim.x;
     const int i0 = blockIdx.x * per, i1 = min(total, i0 + per);
+    const int B = blockDim.x;
     int dsc = -1, lo = 0, hi = 0;
     const uint32_t* fcand = nullptr;
     const uint8_t* lvl = nullptr;
     uint32_t* corners = nullptr;
     int* ccount = nullptr;
     int pitch = 0, t = 0, ncols = 0, wcell = 1, hcell = 1, ccap = 0;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        if (i >= hi) {  // the last list starting at or before i
-            int a = dsc < 0 ? 0 : dsc, b = ndesc - 1;
-            while (a < b) {
-                const int mid = (a + b + 1) >> 1;
-                if (s_pre[mid] <= i) a = mid;
-                else b = mid - 1;
-            }
-            dsc = a;
-            lo = s_pre[dsc];
-            hi = s_pre[dsc + 1];
-            const LevelDesc& d = descs[(size_t)dsc * stride];
-            fcand = d.fcand;
-            lvl = d.dst;
-            pitch = d.pitch;
-            t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
-            corners = d.corners;
-            ccount = d.corner_count;
-            ncols = d.nCols;
-            wcell = max(d.wCell, 1);
-            hcell = max(d.hCell, 1);
-            ccap = d.corner_cap;
+    auto resolve = [&](int i) {  // the last list starting at or before i
+        int a = dsc < 0 ? 0 : dsc, b = ndesc - 1;
+        while (a < b) {
+            const int mid = (a + b + 1) >> 1;
+            if (s_pre[mid] <= i) a = mid;
+            else b = mid - 1;
         }
-        const uint32_t e = __ldg(fcand + (i - lo));
-        const int x = (int)(e & 0xFFFFu), y = (int)(e >> 16);
-        const int sc = level_arc_strength(lvl + (size_t)y * pitch + x, pitch);
+        dsc = a;
+        lo = s_pre[dsc];
+        hi = s_pre[dsc + 1];
+        const LevelDesc& d = descs[(size_t)dsc * stride];
+        fcand = d.fcand;
+        lvl = d.dst;
+        pitch = d.pitch;
+        t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
+        corners = d.corners;
+        ccount = d.corner_count;
+        ncols = d.nCols;
+        wcell = max(d.wCell, 1);
+        hcell = max(d.hCell, 1);
+        ccap = d.corner_cap;
+    };
+    auto append = [&](uint32_t e, int sc) {
         if (sc > t && ncols > 0) {
-            const int rx = x - ORBGPU_EDGE_THRESHOLD, ry = y - ORBGPU_EDGE_THRESHOLD;
+            const int rx = (int)(e & 0xFFFFu) - ORBGPU_EDGE_THRESHOLD, ry = (int)(e >> 16) - ORBGPU_EDGE_THRESHOLD;
             const int cj = rx / wcell, ci = ry / hcell;
             const int cell = ci * ncols + cj;
             const int pos = atomicAdd(ccount + cell, 1);
             if (pos < ccap)
                 corners[(size_t)cell * ccap + pos] =
                     ((uint32_t)(ry - ci * hcell) << 16) | ((uint32_t)(rx - cj * wcell) << 8) | (uint32_t)sc;
+        }
+    };
+    // four candidates per thread and pass: their circle loads are in flight
+    // together (the strength computation is latency-bound on them)
+    for (int i = i0 + threadIdx.x; i < i1; i += 4 * B) {
+        if (i >= hi) resolve(i);
+        if (i + 3 * B < min(i1, hi)) {
+            uint32_t e[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) e[k] = __ldg(fcand + (i + k * B - lo));
+            int sc[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                sc[k] = level_arc_strength(lvl + (size_t)(e[k] >> 16) * pitch + (e[k] & 0xFFFFu), pitch);
+#pragma unroll
+            for (int k = 0; k < 4; k++) append(e[k], sc[k]);
+        } else {
+            for (int k = 0; k < 4 && i + k * B < i1; k++) {
+                const int j = i + k * B;
+                if (j >= hi) resolve(j);
+                const uint32_t e = __ldg(fcand + (j - lo));
+                append(e, level_arc_strength(lvl + (size_t)(e >> 16) * pitch + (e & 0xFFFFu), pitch));
+            }
         }
     }
 }

@@ -93,12 +93,16 @@ class _Worker:
         self.rkps = t.zeros((rows, 7), dtype=t.float32, device="cuda")
         self.rmps = t.zeros((rows, 4), dtype=t.float32, device="cuda")
         self.rdesc = t.zeros((rows, 32), dtype=t.uint8, device="cuda")
-        # per-batch small arrays: slots, offsets (first search, retry), rays, depths
-        self.h_small = t.zeros(4 * (engine.max_batch + 1), dtype=t.int32).pin_memory()
+        # per-batch small arrays: slots, offsets (first search, retry), rays,
+        # depths.  Their host sides are ordinary (pageable) memory copied
+        # synchronously: torch's page-locked allocator records events on the
+        # streams a block was copied on when the block is freed, and the
+        # batch's stream belongs to the library, which destroys it first.
+        self.h_small = t.zeros(4 * (engine.max_batch + 1), dtype=t.int32)
         self.d_small = t.zeros(4 * (engine.max_batch + 1), dtype=t.int32, device="cuda")
-        self.h_geo = t.zeros(13 * engine.max_batch, dtype=t.float64).pin_memory()
+        self.h_geo = t.zeros(13 * engine.max_batch, dtype=t.float64)
         self.d_geo = t.zeros(13 * engine.max_batch, dtype=t.float64, device="cuda")
-        self.h_out = t.zeros(2 * engine.max_batch, dtype=t.int32).pin_memory()
+        self.h_out = t.zeros(2 * engine.max_batch, dtype=t.int32)
         self.stream = t.cuda.ExternalStream(self.batch.stream)
         self.ev_start = t.cuda.Event(enable_timing=True)
         self.ev_end = t.cuda.Event(enable_timing=True)
@@ -228,7 +232,7 @@ class ServingEngine:
         if self._t0_event is not None:
             W.ev_start.record(bs)
         with t.cuda.stream(bs):
-            W.d_small.copy_(W.h_small, non_blocking=True)
+            W.d_small.copy_(W.h_small)
         d_slots = W.d_small[:nb]
         d_off1 = W.d_small[nb + 1:2 * nb + 2]
         # extraction, images read in place from page-locked host memory
@@ -252,7 +256,7 @@ class ServingEngine:
             off2[1:] = np.cumsum(lc2)
             hs[2 * nb + 2:3 * nb + 3] = off2
             with t.cuda.stream(bs):
-                W.d_small[2 * nb + 2:3 * nb + 3].copy_(W.h_small[2 * nb + 2:3 * nb + 3], non_blocking=True)
+                W.d_small[2 * nb + 2:3 * nb + 3].copy_(W.h_small[2 * nb + 2:3 * nb + 3])
             check(lib().orbgpu_stream_state_gather(self._state, nb, ptr(d_slots), ptr(W.d_small[2 * nb + 2:]),
                                                    max(lc2 + [0]), ptr(W.rkps), ptr(W.rmps), ptr(W.rdesc),
                                                    C.c_void_p(W.batch.stream)),
@@ -268,16 +272,16 @@ class ServingEngine:
             geo[12 * f:12 * f + 12] = self._rays(requests[f][3], st.K)
             geo[12 * nb + f] = st.depth
         with t.cuda.stream(bs):
-            W.d_geo[:13 * nb].copy_(W.h_geo[:13 * nb], non_blocking=True)
+            W.d_geo[:13 * nb].copy_(W.h_geo[:13 * nb])
         check(lib().orbgpu_stream_state_update(self._state, nb, ptr(d_slots), ptr(kps), ptr(desc), ptr(counts), cap,
                                                ptr(W.d_geo), ptr(W.d_geo[12 * nb:]), self._flags,
                                                C.c_void_p(W.batch.stream)),
               "orbgpu_stream_state_update")
-        with t.cuda.stream(bs):
-            W.h_out[:nb].copy_(counts[:nb], non_blocking=True)
-            W.h_out[nb:2 * nb].copy_(nm[:nb], non_blocking=True)
         if self._t0_event is not None:
             W.ev_end.record(bs)
+        with t.cuda.stream(bs):
+            W.h_out[:nb].copy_(counts[:nb])
+            W.h_out[nb:2 * nb].copy_(nm[:nb])
         bs.synchronize()
         done = time.perf_counter()
         if self._t0_event is not None:
