@@ -287,7 +287,8 @@ def run_ours(args):
     if "perframe" in legs:
         per_frame_fps, per_frame_split = run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev)
     extra = {}
-    for leg, fn in (("mono", bench_plain_mono), ("stereo", bench_stereo), ("knn", bench_knn), ("serving", bench_serving),
+    for leg, fn in (("mono", bench_plain_mono), ("stereo", bench_stereo), ("stereobatch", bench_stereo_batch),
+                    ("knn", bench_knn), ("serving", bench_serving),
                     ("distinctive", bench_distinctive), ("frustum", bench_frustum), ("bow", bench_bow)):
         if leg in legs:
             try:
@@ -299,8 +300,8 @@ def run_ours(args):
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
 
 
-LEGS = {"e2e", "perframe", "mono", "stereo", "knn", "serving", "distinctive", "frustum", "bow", "cpu"}
-LEG_KEYS = {"mono": "plain_640x480_mono_init", "stereo": "stereo_1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams",
+LEGS = {"e2e", "perframe", "mono", "stereo", "stereobatch", "knn", "serving", "distinctive", "frustum", "bow", "cpu"}
+LEG_KEYS = {"mono": "plain_640x480_mono_init", "stereo": "stereo_1241x376", "stereobatch": "stereo_batch_64x1241x376", "knn": "knn_50kx200k", "serving": "serving_32_streams",
             "distinctive": "distinctive_descriptors_1M_mappoints", "frustum": "is_in_frustum_64x5000",
             "bow": "compute_bow_64x2000_k10L6"}
 
@@ -587,6 +588,96 @@ def bench_stereo(dev, reps=30, cpu_reps=8):
             "cpu_baseline": {"value": 1e3 / statistics.median(cpu), "unit": "pairs/s", "cores": 1, "kind": "port",
                              "p50_ms_per_pair": pctl(cpu, 50), "p99_ms_per_pair": pctl(cpu, 99),
                              "sample": f"{cpu_reps} pairs (two extractions + ComputeStereoMatches), one thread",
+                             "host": host_info()},
+            "uR_within_1e-4_of_oracle": same}
+
+
+def bench_stereo_batch(dev, npairs=64, steps=5):
+    """Batched stereo: 64 rectified 1241x376 pairs (nFeatures 2000, 8 distinct
+    pairs each used 8 times) in one batch extraction of 128 frames followed by
+    one batched ComputeStereoMatches over the resident pyramids (bf 386.1, fx
+    718.856).  Device-resident images (value, events) and page-locked host
+    images read in place with uR / depth copied back (e2e); a sample against
+    the oracle."""
+    import torch
+    from oracle import pyoracle
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchStereo
+    uniq = [syn.stereo_pair(1241, 376, 40 + i) for i in range(8)]
+    imgs = []
+    for p in range(npairs):
+        left, right, _ = uniq[p % 8]
+        imgs += [left, right]
+    pairs = [(2 * p, 2 * p + 1) for p in range(npairs)]
+    b = BatchExtractor(2 * npairs, 1241, 376, 2000)
+    bs = BatchStereo(b)
+    dimgs = [torch.from_numpy(i).to(dev) for i in imgs]
+    nfs = [2000] * len(imgs)
+    stream = torch.cuda.ExternalStream(b.stream)
+
+    def step(src):
+        b.extract(src, nfs, wait=False)
+        return bs.compute(pairs, 386.1, 718.856)
+    for _ in range(3):
+        step(dimgs)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(dimgs)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    dev_ms = statistics.median(ms)
+    ur, dp = step(dimgs)
+    counts = b.counts[: 2 * npairs].cpu().numpy()
+    ur_h, dp_h = ur.cpu().numpy(), dp.cpu().numpy()
+    # end to end: page-locked host images read in place, uR / depth copied back
+    pin = [torch.from_numpy(i).pin_memory() for i in imgs]
+    cap = b.per_frame_capacity
+    hu = np.empty((npairs, cap), np.float32)
+    hd = np.empty((npairs, cap), np.float32)
+    for it in range(2 + steps):
+        if it == 2:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        u, d_ = step(pin)
+        hu[:] = u.cpu().numpy()
+        hd[:] = d_.cpu().numpy()
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    # oracle on two distinct pairs
+    o = pyoracle.Oracle()
+    same = True
+    cpu = []
+    for p in range(2):
+        left, right, _ = uniq[p]
+        t0 = time.perf_counter()
+        L = o.extract(left, nfeatures=2000)
+        R = o.extract(right, nfeatures=2000)
+        u1, _ = o.compute_stereo_matches(L.keypoints, L.descriptors, R.keypoints, R.descriptors, L.pyramid, R.pyramid,
+                                         1241, 376, 386.1, 718.856)
+        cpu.append((time.perf_counter() - t0) * 1e3)
+        n = len(L.keypoints)
+        same &= bool(counts[2 * p] == n and np.max(np.abs(ur_h[p, :n] - u1), initial=0.0) <= 1e-4)
+    alg = 0
+    for p in range(npairs):
+        nl, nr = int(counts[2 * p]), int(counts[2 * p + 1])
+        matched = int((ur_h[p, :nl] > 0).sum())
+        alg += extraction_bytes(1241, 376, nl) + extraction_bytes(1241, 376, nr) + matched * 11 * 2 * 121 + 8 * nl
+    pk, pk_src = peaks()
+    return {"metric": "stereo pairs/s (batched: 64 pairs 1241x376/2000, extraction + ComputeStereoMatches)",
+            "value": npairs / (dev_ms / 1e3), "unit": "pairs/s", "ms_per_pair": dev_ms / npairs,
+            "ms_per_batch": dev_ms, "gpu_launches_per_step": b.launches_per_extract() + 5,
+            "e2e": {"value": npairs / (e2e_ms / 1e3), "unit": "pairs/s", "ms_per_pair": e2e_ms / npairs,
+                    "h2d_bytes_per_step": int(sum(i.nbytes for i in imgs)),
+                    "d2h_bytes_per_step": int(2 * 4 * npairs * cap)},
+            "roofline": {"bound": "hbm", "kernel": "batched extraction + stereo (whole step)",
+                         "achieved": alg / (dev_ms / 1e3) / 1e9, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": alg / (dev_ms / 1e3) / 1e9 / pk["hbm_gbs"], "algorithmic_bytes_per_step": alg,
+                         "peak_source": pk_src},
+            "cpu_baseline": {"value": 1e3 / statistics.median(cpu), "unit": "pairs/s", "cores": 1, "kind": "port",
+                             "p50_ms_per_pair": pctl(cpu, 50), "sample": "2 pairs, oracle extraction x 2 + stereo",
                              "host": host_info()},
             "uR_within_1e-4_of_oracle": same}
 

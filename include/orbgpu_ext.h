@@ -60,6 +60,20 @@ int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const orbgpu_keypoi
                                             const int* last_offsets, const orbgpu_frame_motion* motions, float th,
                                             int mono, int check_ori, int* match_out, int* nmatches);
 
+/* Frame::ComputeStereoMatches (src/Frame.cc:831-1082) for npairs (left,
+ * right) frame pairs of the batch's last extraction in one pass, reading the
+ * pyramids the extraction left in the batch's arena.  left_frame[p] /
+ * right_frame[p]: frame indices of that extraction (same image size); bf[p]
+ * (mbf) and fx[p] (K(0,0)): the pair's camera (host arrays).  kps / desc /
+ * counts: the extraction's outputs (device; frame f's rows at f *
+ * per_frame_capacity).  uright / depth: device, npairs * per_frame_capacity
+ * floats; pair p's left keypoint i at p * per_frame_capacity + i (rows past
+ * the left frame's count are not written).  Returns after the stream
+ * finished. */
+int orbgpu_batch_compute_stereo_matches(orbgpu_batch* b, const orbgpu_keypoint* kps, const uint8_t* desc,
+                                        const int* counts, int npairs, const int* left_frame, const int* right_frame,
+                                        const float* bf, const float* fx, float* uright, float* depth);
+
 /* ------------------------------------------------------------ serving state */
 /* The serving loop's per-stream LastFrame state (no reference counterpart:
  * the reference keeps one Tracking object, with its mLastFrame, per camera).

@@ -119,6 +119,37 @@ class BatchProjection:
         return int(lib().orbgpu_batch_search_rounds())
 
 
+class BatchStereo:
+    """Frame::ComputeStereoMatches (src/Frame.cc:831-1082) for (left, right)
+    frame pairs of the batch's last extraction, on its resident pyramids
+    (orbgpu_batch_compute_stereo_matches)."""
+
+    def __init__(self, batch: BatchExtractor):
+        import torch
+        self.batch = batch
+        cap = batch.per_frame_capacity
+        self.uright = torch.empty(batch.max_frames * cap, dtype=torch.float32, device="cuda")
+        self.depth = torch.empty(batch.max_frames * cap, dtype=torch.float32, device="cuda")
+
+    def compute(self, pairs, bf, fx):
+        """pairs: [(left frame, right frame)] indices of the last extraction;
+        bf / fx: per pair or one value.  Returns (uright, depth) as
+        (npairs, per_frame_capacity) CUDA tensors (row p holds the left frame's
+        keypoints in order; entries past its count are unspecified)."""
+        b = self.batch
+        n = len(pairs)
+        lf = np.array([p[0] for p in pairs], np.int32)
+        rf = np.array([p[1] for p in pairs], np.int32)
+        bfa = np.broadcast_to(np.asarray(bf, np.float32), (n,)).copy()
+        fxa = np.broadcast_to(np.asarray(fx, np.float32), (n,)).copy()
+        check(lib().orbgpu_batch_compute_stereo_matches(b.handle, ptr(b.kps), ptr(b.desc), ptr(b.counts), n, ptr(lf),
+                                                        ptr(rf), ptr(bfa), ptr(fxa), ptr(self.uright),
+                                                        ptr(self.depth)),
+              "orbgpu_batch_compute_stereo_matches")
+        cap = b.per_frame_capacity
+        return self.uright[: n * cap].view(n, cap), self.depth[: n * cap].view(n, cap)
+
+
 def motion_struct(Tcw, Tlw, fx, fy, cx, cy, bf=0.0, b=0.0):
     """orbgpu_frame_motion from rows 0-2 of CurrentFrame.mTcw / LastFrame.mTcw."""
     from ._lib import MotionStruct

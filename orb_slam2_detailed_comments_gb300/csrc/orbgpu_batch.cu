@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "orbgpu_host.h"
+#include "orbgpu_stereo.cuh"
 
 namespace orbgpu {
 
@@ -129,6 +130,10 @@ struct orbgpu_batch {
     std::vector<float> frame_scale;  // nframes * 16
     std::vector<int> frame_w, frame_h;
     int frame_cap = 0;
+    // scratch of the batched stereo search (grown on demand)
+    uint8_t* st_scratch = nullptr;
+    size_t st_bytes = 0;
+    int* st_pinned = nullptr;
 };
 
 static void destroy_graph(orbgpu_batch* b) {
@@ -199,6 +204,8 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     cudaFree(b->d_status);
     cudaFree(b->d_totals);
     cudaFree(b->d_fcand);
+    cudaFree(b->st_scratch);
+    if (b->st_pinned) cudaFreeHost(b->st_pinned);
     cudaFree(b->d_ccount);
     cudaFree(b->d_src);
     cudaFreeHost(b->h_src);
@@ -1667,3 +1674,186 @@ extern "C" int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const or
     }
     return ORBGPU_ERR_CAPACITY;
 }
+
+// ---------------------------------------------------------------- batched stereo
+// Frame::ComputeStereoMatches (src/Frame.cc:831-1082) for many (left, right)
+// frame pairs of one batch extraction in one pass: the device functions of
+// orbgpu_stereo.cuh over the pyramids resident in the batch's arena slots,
+// one launch per step for all pairs (grid y = pair).
+namespace orbgpu {
+
+struct StereoPair {
+    StereoLevels lv;
+    int left, right;  // frame indices of the extraction
+    int nRows;        // level-0 rows
+    float bf, fx;
+};
+
+__global__ void k_bstereo_rows_count(const orbgpu_keypoint* kps, const int* counts, int cap, const StereoPair* pairs,
+                                     int rows_stride, int* row_count) {
+    const StereoPair& P = pairs[blockIdx.y];
+    const int nR = min(counts[P.right], cap);
+    int* rc = row_count + (size_t)blockIdx.y * rows_stride;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += gridDim.x * blockDim.x) {
+        int lo, hi;
+        if (!stereo_rows_of(kps[(size_t)P.right * cap + i], P.lv, P.nRows, lo, hi)) continue;
+        for (int yi = lo; yi <= hi; yi++) atomicAdd(&rc[yi], 1);
+    }
+}
+
+// One block per pair: row_start = exclusive prefix of the row counts
+// (nRows + 1 entries), cursor = its copy.
+__global__ void k_bstereo_scan(const int* row_count, const StereoPair* pairs, int rows_stride, int* row_start,
+                               int* cursor) {
+    __shared__ int s_scan[32];
+    const int n = pairs[blockIdx.x].nRows + 1;
+    const size_t o = (size_t)blockIdx.x * rows_stride;
+    int carry = 0;
+    for (int b0 = 0; b0 < n; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const int v = i < n ? row_count[o + i] : 0;
+        int tot;
+        const int ex = block_exclusive_scan(v, s_scan, &tot);
+        if (i < n) {
+            row_start[o + i] = carry + ex;
+            cursor[o + i] = carry + ex;
+        }
+        carry += tot;
+    }
+}
+
+__global__ void k_bstereo_rows_fill(const orbgpu_keypoint* kps, const int* counts, int cap, const StereoPair* pairs,
+                                    int rows_stride, int* cursor, int* row_keys, size_t key_stride) {
+    const StereoPair& P = pairs[blockIdx.y];
+    const int nR = min(counts[P.right], cap);
+    int* cur = cursor + (size_t)blockIdx.y * rows_stride;
+    int* keys = row_keys + blockIdx.y * key_stride;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += gridDim.x * blockDim.x) {
+        int lo, hi;
+        if (!stereo_rows_of(kps[(size_t)P.right * cap + i], P.lv, P.nRows, lo, hi)) continue;
+        for (int yi = lo; yi <= hi; yi++) keys[atomicAdd(&cur[yi], 1)] = i;
+    }
+}
+
+__global__ void k_bstereo_match(const orbgpu_keypoint* kps, const uint8_t* desc, const int* counts, int cap,
+                                const StereoPair* pairs, int rows_stride, const int* row_start, const int* row_keys,
+                                size_t key_stride, float* uright, float* depth, int* sad, int* status) {
+    const StereoPair& P = pairs[blockIdx.y];
+    const int iL = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (iL >= min(counts[P.left], cap)) return;
+    const size_t p = blockIdx.y, l0 = (size_t)P.left * cap, r0 = (size_t)P.right * cap;
+    stereo_match_warp(iL, kps + l0, desc + 32 * l0, kps + r0, desc + 32 * r0, P.lv, P.nRows,
+                      row_start + p * rows_stride, row_keys + p * key_stride, P.bf, P.fx, uright + p * cap,
+                      depth + p * cap, sad + p * cap, status);
+}
+
+__global__ void k_bstereo_median(const int* counts, int cap, const StereoPair* pairs, const int* sad, float* uright,
+                                 float* depth, int* sort_buf, int sort_cap) {
+    const StereoPair& P = pairs[blockIdx.x];
+    const size_t p = blockIdx.x;
+    stereo_median_block(min(counts[P.left], cap), sad + p * cap, uright + p * cap, depth + p * cap,
+                        sort_buf + p * sort_cap, sort_cap, nullptr);
+}
+
+}  // namespace orbgpu
+
+extern "C" int orbgpu_batch_compute_stereo_matches(orbgpu_batch* b, const orbgpu_keypoint* kps, const uint8_t* desc,
+                                                   const int* counts, int npairs, const int* left_frame,
+                                                   const int* right_frame, const float* bf, const float* fx,
+                                                   float* uright, float* depth) {
+    if (!b || b->nframes <= 0 || !kps || !desc || !counts || npairs < 0 || npairs > b->nframes ||
+        (npairs > 0 && (!left_frame || !right_frame || !bf || !fx || !uright || !depth))) {
+        orbgpu_set_last_error("invalid batched stereo arguments", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    if (npairs == 0) return ORBGPU_OK;
+    const int cap = b->frame_cap, nl = b->nlevels;
+    std::vector<StereoPair> hp(npairs);
+    int max_rows = 1;
+    float maxscale = 1.0f;
+    for (int p = 0; p < npairs; p++) {
+        const int lf = left_frame[p], rf = right_frame[p];
+        if (lf < 0 || rf < 0 || lf >= b->nframes || rf >= b->nframes || !(bf[p] > 0.f) || !(fx[p] > 0.f)) {
+            orbgpu_set_last_error("batched stereo: frame index or camera out of range", __FILE__, __LINE__);
+            return ORBGPU_ERR_BAD_ARG;
+        }
+        const FramePlan* L = b->cur[lf];
+        const FramePlan* R = b->cur[rf];
+        if (L->w != R->w || L->h != R->h) {
+            orbgpu_set_last_error("batched stereo: left and right frames differ in size", __FILE__, __LINE__);
+            return ORBGPU_ERR_BAD_ARG;
+        }
+        StereoPair& P = hp[p];
+        std::memset(&P, 0, sizeof(P));
+        for (int l = 0; l < nl; l++) {
+            P.lv.left[l] = b->arena + (size_t)lf * b->slot_bytes + L->layout.lv[l].pyr;
+            P.lv.right[l] = b->arena + (size_t)rf * b->slot_bytes + R->layout.lv[l].pyr;
+            P.lv.w[l] = L->geom[l].w;
+            P.lv.h[l] = L->geom[l].h;
+            P.lv.pitch[l] = L->geom[l].pitch;
+            P.lv.scale[l] = L->tables.scale[l];
+            P.lv.inv_scale[l] = 1.0f / L->tables.scale[l];
+            maxscale = std::max(maxscale, P.lv.scale[l]);
+        }
+        P.lv.nlevels = nl;
+        P.left = lf;
+        P.right = rf;
+        P.nRows = L->geom[0].h;
+        P.bf = bf[p];
+        P.fx = fx[p];
+        max_rows = std::max(max_rows, P.nRows);
+    }
+    const int rows_stride = max_rows + 2;
+    const int rows_per_key = 2 * (int)std::ceil(2.0f * maxscale) + 4;
+    const size_t key_stride = (size_t)cap * rows_per_key;
+    int sort_cap = 1;
+    while (sort_cap < cap) sort_cap <<= 1;
+    cudaStream_t st = b->stream;
+    const size_t need = sizeof(StereoPair) * npairs + 3 * sizeof(int) * (size_t)npairs * rows_stride +
+                        sizeof(int) * npairs * key_stride + sizeof(int) * (size_t)npairs * (cap + sort_cap) +
+                        16 * 256;
+    if (need > b->st_bytes) {
+        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (b->st_scratch) cudaFree(b->st_scratch);
+        b->st_scratch = nullptr;
+        b->st_bytes = 0;
+        ORBGPU_CUDA_TRY(cudaMalloc(&b->st_scratch, need));
+        b->st_bytes = need;
+    }
+    if (!b->st_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&b->st_pinned, 16));
+    size_t off = 0;
+    auto take = [&](size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        uint8_t* q = b->st_scratch + off;
+        off += n;
+        return q;
+    };
+    StereoPair* d_pairs = (StereoPair*)take(sizeof(StereoPair) * npairs);
+    int* row_count = (int*)take(sizeof(int) * (size_t)npairs * rows_stride);
+    int* row_start = (int*)take(sizeof(int) * (size_t)npairs * rows_stride);
+    int* cursor = (int*)take(sizeof(int) * (size_t)npairs * rows_stride);
+    int* row_keys = (int*)take(sizeof(int) * npairs * key_stride);
+    int* sad = (int*)take(sizeof(int) * (size_t)npairs * cap);
+    int* sort_buf = (int*)take(sizeof(int) * (size_t)npairs * sort_cap);
+    int* status = (int*)take(sizeof(int) * 4);
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(d_pairs, hp.data(), sizeof(StereoPair) * npairs, cudaMemcpyHostToDevice, st));
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(row_count, 0, sizeof(int) * (size_t)npairs * rows_stride, st));
+    ORBGPU_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * 4, st));
+    const dim3 gk((cap + 255) / 256, npairs);
+    k_bstereo_rows_count<<<gk, 256, 0, st>>>(kps, counts, cap, d_pairs, rows_stride, row_count);
+    k_bstereo_scan<<<npairs, 1024, 0, st>>>(row_count, d_pairs, rows_stride, row_start, cursor);
+    k_bstereo_rows_fill<<<gk, 256, 0, st>>>(kps, counts, cap, d_pairs, rows_stride, cursor, row_keys, key_stride);
+    const int wpb = 8;
+    k_bstereo_match<<<dim3((cap + wpb - 1) / wpb, npairs), 32 * wpb, 0, st>>>(
+        kps, desc, counts, cap, d_pairs, rows_stride, row_start, row_keys, key_stride, uright, depth, sad, status);
+    k_bstereo_median<<<npairs, 1024, 0, st>>>(counts, cap, d_pairs, sad, uright, depth, sort_buf, sort_cap);
+    ORBGPU_CUDA_TRY(cudaGetLastError());
+    ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->st_pinned, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    if (b->st_pinned[0]) {
+        orbgpu_set_last_error("batched stereo: patch outside its level", __FILE__, __LINE__);
+        return ORBGPU_ERR_BAD_ARG;
+    }
+    return ORBGPU_OK;
+}
+

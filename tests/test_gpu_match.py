@@ -129,6 +129,39 @@ def test_stereo_vs_oracle_1241x376(torch, oracle, seed):
     assert np.array_equal(u1 > 0, u2 > 0) and (u1 > 0).sum() > 200
 
 
+def test_batched_stereo_vs_oracle(torch, oracle):
+    """orbgpu_batch_compute_stereo_matches: four stereo pairs of two sizes in
+    one batch extraction (left and right frames interleaved, one pair listed
+    right-first to exercise the frame indices), every pair against the
+    oracle's Frame::ComputeStereoMatches on the same images, uR / depth within
+    1e-4."""
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchStereo
+    specs = [(1241, 376, 3), (640, 480, 4), (1241, 376, 5), (640, 480, 6)]
+    imgs, pairs, refs = [], [], []
+    for w, h, seed in specs:
+        left, right, _ = syn.stereo_pair(w, h, seed)
+        if seed == 5:  # right frame first in the batch
+            pairs.append((len(imgs) + 1, len(imgs)))
+            imgs += [right, left]
+        else:
+            pairs.append((len(imgs), len(imgs) + 1))
+            imgs += [left, right]
+        L = oracle.extract(left, nfeatures=2000)
+        R = oracle.extract(right, nfeatures=2000)
+        refs.append(oracle.compute_stereo_matches(L.keypoints, L.descriptors, R.keypoints, R.descriptors, L.pyramid,
+                                                  R.pyramid, w, h, 386.1, 718.856) + (len(L.keypoints),))
+    b = BatchExtractor(len(imgs), 1280, 720, 2000)
+    k, d, c = b.extract([torch.from_numpy(i).cuda() for i in imgs], [2000] * len(imgs))
+    ur, dp = BatchStereo(b).compute(pairs, 386.1, 718.856)
+    ur, dp, c = ur.cpu().numpy(), dp.cpu().numpy(), c.cpu().numpy()
+    for p, (u1, d1, n) in enumerate(refs):
+        assert c[pairs[p][0]] == n
+        np.testing.assert_allclose(ur[p, :n], u1, atol=1e-4, rtol=0)
+        np.testing.assert_allclose(dp[p, :n], d1, atol=1e-4, rtol=1e-6)
+        assert np.array_equal(u1 > 0, ur[p, :n] > 0) and (u1 > 0).sum() > 100
+
+
 def test_knn_golden_and_oracle(torch, golden, oracle):
     from orb_slam2_detailed_comments_gb300 import ORBmatcher
     from orb_slam2_detailed_comments_gb300 import synthetic as syn
