@@ -133,39 +133,29 @@ def _level_sizes(w, h):
     return [(int(np.rint(np.float32(w) * i)), int(np.rint(np.float32(h) * i))) for i in inv]
 
 
-def resize_blur_bytes(frames):
-    """Algorithmic bytes of the resize / blur / FAST-strength stage per step:
-    level 0 reads the image and writes the blurred and strength planes;
-    level l >= 1 reads level l-1 and writes its level, blurred and strength
-    planes (each plane once, nothing re-read)."""
-    tot = 0
-    for img, _ in frames:
-        h, w = img.shape
-        sizes = _level_sizes(w, h)
-        tot += 3 * sizes[0][0] * sizes[0][1]
-        for l in range(1, len(sizes)):
-            tot += sizes[l - 1][0] * sizes[l - 1][1] + 3 * sizes[l][0] * sizes[l][1]
-    return tot
+# The issue (instruction) roofline of the stage: its warp instructions per
+# pixel and issue-active share from an ncu capture of the same build
+# (profiles/), None until one was taken.
+ISSUE_ROOFLINE = None
 
 
-# DRAM bytes (read + write) of the resize / blur / strength stage measured by
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum over its fifteen launches:
-# the strip kernel of every level, the resize kernel of levels 1-7) on this
-# workload at 128 frames per step, per frame: the stage's traffic scales with
-# the frames of a step.  Below the algorithmic bytes because a level written
-# by one launch is still partly in L2 when the next launch reads it.
-RESIZE_BLUR_DRAM_BYTES_PER_FRAME = 572.8e6 / 128
+def level_areas(frames):
+    """Per frame, the pixel count of each of the 8 levels (cvRound(W / 1.2^l) x
+    cvRound(H / 1.2^l), src/ORBextractor.cc:1661-1663)."""
+    return [[lw * lh for lw, lh in _level_sizes(img.shape[1], img.shape[0])] for img, _ in frames]
 
 
-def fast_bytes(frames):
-    """Algorithmic bytes of the FAST stage: every pixel of every level read once
-    plus the candidate words written (counted as read bytes only; the
-    candidates are a few KB per frame)."""
-    tot = 0
-    for img, _ in frames:
-        h, w = img.shape
-        tot += sum(a * b for a, b in _level_sizes(w, h))
-    return tot
+def extraction_roofline_bytes(frames, nkps):
+    """Algorithmic bytes of the extraction per step (the path's per-frame
+    model): the image read once, levels 1-7 written (the pyramid is a
+    required output), every level read once for FAST + orientation and once
+    for blur + descriptors, and 28 + 32 bytes per keypoint out -- about
+    9.3 W H + 60 N per frame.  Returns (bytes of the resize / blur / FAST
+    stage = all the level terms, bytes of the whole extraction)."""
+    stage = 0
+    for a in level_areas(frames):
+        stage += a[0] + sum(a[1:]) + 2 * sum(a)
+    return stage, stage + 60 * int(sum(nkps))
 
 
 def _world():
@@ -402,18 +392,27 @@ def run_per_frame(frames, imgs_dev, mps_list, mpd_list, dev):
 
 def finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, per_frame_fps, per_frame_split,
            extra, mps_list, mpd_list, clk, batch, proj, tuning):
-    # roofline of the dominant stage
+    # roofline of the dominant stage against the path's algorithmic bytes
     pk, pk_src = peaks()
-    dom = max(stage_ms, key=stage_ms.get) if stage_ms else None
-    dom_ms = stage_ms.get(dom, 0.0) / max(1, args.steps)
-    alg = {"fast": fast_bytes(frames), "resize_blur": resize_blur_bytes(frames)}
-    achieved = alg.get(dom, fast_bytes(frames)) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
-    traffic = RESIZE_BLUR_DRAM_BYTES_PER_FRAME * len(frames) if dom == "resize_blur" else None
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
-                "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": traffic,
-                "algorithmic_bytes_per_step": alg.get(dom), "peak_source": pk_src,
-                "traffic_source": "ncu dram__bytes_read+write of the stage, 128-frame capture, per frame x frames",
-                "stage_ms_per_step": {k: v / max(1, args.steps) for k, v in stage_ms.items()}}
+    per_step = {k: v / max(1, args.steps) for k, v in stage_ms.items()}
+    dom = max(per_step, key=per_step.get) if per_step else None
+    dom_ms = per_step.get(dom, 0.0)
+    nkps = batch.counts[:len(frames)].cpu().numpy()
+    stage_bytes, total_bytes = extraction_roofline_bytes(frames, nkps)
+    ext_ms = sum(per_step.values())
+    achieved = stage_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    whole = total_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
+    roofline = {"bound": "hbm", "kernel": "resize + blur + FAST (k_level_resize, k_level_strip, k_fast_score)"
+                if dom == "resize_blur" else dom,
+                "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
+                "algorithmic_bytes_per_step": stage_bytes, "peak_source": pk_src,
+                "bytes_model": "per frame: image read + levels 1-7 written + every level read twice (FAST/angle, "
+                               "blur/descriptor); the whole extraction adds 60 bytes per keypoint",
+                "whole_extraction": {"ms": ext_ms, "algorithmic_bytes_per_step": total_bytes, "achieved": whole,
+                                     "frac": (whole / pk["hbm_gbs"]) if whole else None},
+                "stage_ms_per_step": per_step,
+                "issue_bound": ISSUE_ROOFLINE}
 
     # CPU baseline: the oracle restatement on a bounded sample, one thread
     cpu = cpu_sample(frames, mps_list, mpd_list, budget_s=15.0, threads=1) if "cpu" in legs else None

@@ -152,6 +152,13 @@ int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots,
 int orbgpu_tune_set(const char* name, long long value);
 int orbgpu_tune_get(const char* name, long long* value);
 
+/* ------------------------------------------------------------ failure injection (tests) */
+/* The library's next 'count' working-buffer allocations (extractor plans,
+ * batch arenas and scratch, stream state stores) fail as if the device had
+ * no memory left: the call that needed one returns ORBGPU_ERR_OOM and leaves
+ * its handle usable.  0 turns the injection off. */
+int orbgpu_debug_fail_allocations(int count);
+
 /* ------------------------------------------------------------ rotation table */
 /* Builds the descriptor-rotation exception table (path NULL = next to the
  * library) with 'threads' host threads. */

@@ -314,7 +314,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         destroy_graph(b);
         if (b->arena) cudaFree(b->arena);
         b->arena = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->arena, need * b->max_frames));
+        ORBGPU_CUDA_TRY(dev_malloc(&b->arena, need * b->max_frames));
         b->slot_bytes = need;
         std::fill(b->slot_plan.begin(), b->slot_plan.end(), nullptr);
     }
@@ -335,7 +335,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
         if (b->d_descs) cudaFree(b->d_descs);
         b->d_descs = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_descs, sizeof(LevelDesc) * b->max_frames * nlevels));
+        ORBGPU_CUDA_TRY(dev_malloc(&b->d_descs, sizeof(LevelDesc) * b->max_frames * nlevels));
         b->descs_cap = (size_t)b->max_frames * nlevels;
     }
     std::vector<LevelDesc> hd(ndesc);
@@ -348,7 +348,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         destroy_graph(b);
         if (b->d_ccount) cudaFree(b->d_ccount);
         b->d_ccount = nullptr;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_ccount, sizeof(int) * (size_t)stride * b->max_frames));
+        ORBGPU_CUDA_TRY(dev_malloc(&b->d_ccount, sizeof(int) * (size_t)stride * b->max_frames));
         b->ccount_cap = (size_t)stride * b->max_frames;
     }
     b->ccount_stride = stride;
@@ -395,7 +395,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         if (b->d_prefix) cudaFree(b->d_prefix);
         b->d_prefix = nullptr;
         const size_t cap = (size_t)(b->max_frames + 1) * nlevels + (size_t)b->max_frames * nlevels + 1;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->d_prefix, sizeof(int) * std::max(cap, pre.size())));
+        ORBGPU_CUDA_TRY(dev_malloc(&b->d_prefix, sizeof(int) * std::max(cap, pre.size())));
         b->prefix_cap = std::max(cap, pre.size());
     }
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->d_prefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, st));
@@ -1133,7 +1133,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
             ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
             if (P.scratch) cudaFree(P.scratch);
             P.scratch = nullptr;
-            ORBGPU_CUDA_TRY(cudaMalloc(&P.scratch, need));
+            ORBGPU_CUDA_TRY(dev_malloc(&P.scratch, need));
             P.bytes = need;
             P.last_upload.clear();
         }
@@ -1599,7 +1599,7 @@ extern "C" int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const or
             ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
             if (P.scratch) cudaFree(P.scratch);
             P.scratch = nullptr;
-            ORBGPU_CUDA_TRY(cudaMalloc(&P.scratch, need));
+            ORBGPU_CUDA_TRY(dev_malloc(&P.scratch, need));
             P.bytes = need;
         }
         size_t off = 0;
@@ -1817,7 +1817,7 @@ extern "C" int orbgpu_batch_compute_stereo_matches(orbgpu_batch* b, const orbgpu
         if (b->st_scratch) cudaFree(b->st_scratch);
         b->st_scratch = nullptr;
         b->st_bytes = 0;
-        ORBGPU_CUDA_TRY(cudaMalloc(&b->st_scratch, need));
+        ORBGPU_CUDA_TRY(dev_malloc(&b->st_scratch, need));
         b->st_bytes = need;
     }
     if (!b->st_pinned) ORBGPU_CUDA_TRY(cudaMallocHost(&b->st_pinned, 16));

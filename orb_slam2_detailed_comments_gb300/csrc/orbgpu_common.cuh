@@ -252,3 +252,11 @@ __host__ __device__ inline void sincos_taylor(float xf, double* s_out, double* c
     } while (0)
 
 void orbgpu_set_last_error(const char* msg, const char* file, int line);
+
+namespace orbgpu {
+// cudaMalloc of the library's working buffers, except while a test has asked
+// (orbgpu_debug_fail_allocations) for allocations to fail: then it returns
+// cudaErrorMemoryAllocation without allocating.
+cudaError_t dev_malloc(void** p, size_t bytes);
+template <typename T> inline cudaError_t dev_malloc(T** p, size_t bytes) { return dev_malloc((void**)p, bytes); }
+}  // namespace orbgpu

@@ -25,6 +25,21 @@ void orbgpu_set_last_error(const char* msg, const char* file, int line) {
 extern "C" const char* orbgpu_last_error(void) { return g_last_error.c_str(); }
 extern "C" int orbgpu_version(void) { return 1; }
 
+static std::atomic<int> g_fail_allocs{0};
+cudaError_t orbgpu::dev_malloc(void** p, size_t bytes) {
+    int n = g_fail_allocs.load();
+    while (n > 0)
+        if (g_fail_allocs.compare_exchange_weak(n, n - 1)) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+// Test hook; see orbgpu_ext.h.
+extern "C" int orbgpu_debug_fail_allocations(int count) {
+    if (count < 0) return ORBGPU_ERR_BAD_ARG;
+    g_fail_allocs.store(count);
+    return ORBGPU_OK;
+}
+
 namespace orbgpu {
 static Tunables g_tunables;
 static std::atomic<int> g_tune_gen{0};
@@ -486,7 +501,7 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     }
     const std::vector<LevelGeom>& g = P->geom;
     P->layout.plan(g, 0);
-    if (cudaMalloc(&P->arena, P->layout.bytes) != cudaSuccess) {
+    if (dev_malloc(&P->arena, P->layout.bytes) != cudaSuccess) {
         delete P;
         orbgpu_set_last_error("device allocation failed", __FILE__, __LINE__);
         return ORBGPU_ERR_OOM;
@@ -527,7 +542,7 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     }
     pre.push_back(acc);
     P->fast_count = acc;
-    if (cudaMalloc(&P->d_items, pre.size() * sizeof(int)) != cudaSuccess ||
+    if (dev_malloc(&P->d_items, pre.size() * sizeof(int)) != cudaSuccess ||
         cudaMemcpy(P->d_items, pre.data(), pre.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
         free_plan(P);
         return ORBGPU_ERR_OOM;

@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict_
 }
 
 template <int TH>
-__global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc* descs, RangeMap rm) {
+__global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc* descs, RangeMap rm) {
     static_assert((TH + 6) % 7 == 0, "TH + 6 rows must be whole blocks of 7");
     constexpr int NB = (TH + 6) / 7;
     __shared__ __align__(16) StripShared<TH> sh_all[RS_WPB];
@@ -473,14 +473,18 @@ __global__ void __launch_bounds__(32 * RS_WPB, 14) k_level_strip(const LevelDesc
     };
 
     uint32_t cw[7], pr[7][4], hprev[4] = {0, 0, 0, 0};
-    uint32_t pc = level_word(S.rows[0]);
+    // level rows in flight: q[u] holds input row 7 blk + u, loaded one block
+    // (seven rows) ahead
+    uint32_t q[7];
+#pragma unroll
+    for (int u = 0; u < 7; u++) q[u] = level_word(S.rows[u]);
     for (int blk = 0; blk < NB; blk++) {
         uint32_t bmw = 0;  // candidates of this block: bit 4u + j
 #pragma unroll
         for (int u = 0; u < 7; u++) {
             const int i = 7 * blk + u;
-            const uint32_t c = pc;
-            pc = level_word(S.rows[i + 1]);  // one row ahead
+            const uint32_t c = q[u];
+            if (blk + 1 < NB) q[u] = level_word(S.rows[i + 7]);
             const uint32_t l = __shfl_up_sync(0xffffffffu, c, 1), r = __shfl_down_sync(0xffffffffu, c, 1);
             cw[u] = c;
             // horizontal Gaussian sums of the lane's 4 pixels (columns X + j - 3 .. X + j + 3; at most

@@ -112,9 +112,9 @@ extern "C" int orbgpu_stream_state_create(int max_streams, int cap, orbgpu_strea
     s->max_streams = max_streams;
     s->cap = cap;
     const size_t rows = (size_t)max_streams * cap;
-    if (cudaMalloc(&s->kps, sizeof(orbgpu_keypoint) * rows) != cudaSuccess ||
-        cudaMalloc(&s->mps, sizeof(orbgpu_frame_mappoint) * rows) != cudaSuccess ||
-        cudaMalloc(&s->desc, 32 * rows) != cudaSuccess) {
+    if (dev_malloc(&s->kps, sizeof(orbgpu_keypoint) * rows) != cudaSuccess ||
+        dev_malloc(&s->mps, sizeof(orbgpu_frame_mappoint) * rows) != cudaSuccess ||
+        dev_malloc(&s->desc, 32 * rows) != cudaSuccess) {
         orbgpu_stream_state_destroy(s);
         orbgpu_set_last_error("stream state allocation failed", __FILE__, __LINE__);
         return ORBGPU_ERR_OOM;
