@@ -209,8 +209,12 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
     for (int j = 0; j < 4; j++) sel[j] = (uint32_t)(sxs[j] - bmin) | ((uint32_t)(sx1s[j] - bmin) << 4);
     __syncwarp();
 
+    // the level descriptor's fields as locals: the byte stores below could
+    // otherwise alias them and force reloads
+    const uint8_t* const src = d.src;
+    const int spitch = d.spitch;
     auto source_words = [&](int s, uint32_t& w0, uint32_t& w1, uint32_t& w2) {
-        const uint8_t* p = d.src + (size_t)s * d.spitch + sbase;
+        const uint8_t* p = src + (size_t)s * spitch + sbase;
         w0 = nwords > 0 ? *reinterpret_cast<const uint32_t*>(p) : 0u;
         w1 = nwords > 1 ? *reinterpret_cast<const uint32_t*>(p + 4) : 0u;
         w2 = nwords > 2 ? *reinterpret_cast<const uint32_t*>(p + 8) : 0u;
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
             for (int j = 0; j < 4; j++) hv[j] = __dp2a_lo(coef[j], __byte_perm(W0, W1, sel[j]), 0u);
         } else {
             // source columns more than 7 apart (scale factors above about 1.6)
-            const uint8_t* row = d.src + (size_t)s * d.spitch;
+            const uint8_t* row = src + (size_t)s * spitch;
 #pragma unroll
             for (int j = 0; j < 4; j++)
                 hv[j] = (uint32_t)row[sxs[j]] * (coef[j] & 0xFFFFu) + (uint32_t)row[sx1s[j]] * (coef[j] >> 16);
@@ -465,8 +469,15 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
     const uint32_t T23 = (uint32_t)c_gauss_taps[2] | ((uint32_t)c_gauss_taps[3] << 8);
     const uint32_t T45 = (uint32_t)c_gauss_taps[4] | ((uint32_t)c_gauss_taps[5] << 8);
     const uint32_t T6 = (uint32_t)c_gauss_taps[6];
+    // the level descriptor's fields as locals: the stores below could
+    // otherwise alias them and force reloads
+    const uint8_t* const lvl = d.dst;
+    uint8_t* const blur = d.blur;
+    uint32_t* const fcand = d.fcand;
+    int* const fcand_count = d.fcand_count;
+    const int fcand_cap = d.fcand_cap;
     auto level_word = [&](int rr) -> uint32_t {
-        const uint8_t* row = d.dst + (size_t)rr * pitch;
+        const uint8_t* row = lvl + (size_t)rr * pitch;
         if (interior) return *reinterpret_cast<const uint32_t*>(row + X);
         return (uint32_t)row[xr[0]] | ((uint32_t)row[xr[1]] << 8) | ((uint32_t)row[xr[2]] << 16) |
                ((uint32_t)row[xr[3]] << 24);
@@ -514,7 +525,7 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
                     }
                     const uint32_t blurw =
                         __byte_perm(__byte_perm(acc[0], acc[1], 0x0062), __byte_perm(acc[2], acc[3], 0x0062), 0x5410);
-                    if (writer) *reinterpret_cast<uint32_t*>(d.blur + (size_t)y * pitch + X) = blurw;
+                    if (writer) *reinterpret_cast<uint32_t*>(blur + (size_t)y * pitch + X) = blurw;
                     if (y >= ORBGPU_EDGE_THRESHOLD && y < h - ORBGPU_EDGE_THRESHOLD) {
                         const int cc = (u + 4) % 7, up = (u + 1) % 7;
                         const uint32_t cm = cw[cc];
@@ -540,12 +551,12 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
                 if (lane >= o) incl += n;
             }
             int base = 0;
-            if (lane == 31) base = atomicAdd(d.fcand_count, incl);
+            if (lane == 31) base = atomicAdd(fcand_count, incl);
             int pos = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
             const uint32_t yb = (uint32_t)(y0 + 7 * blk - 6);  // level row of bit group 0
             for (uint32_t m = bmw; m; m &= m - 1) {
                 const int b = __ffs(m) - 1;
-                if (pos < d.fcand_cap) d.fcand[pos] = ((yb + (uint32_t)(b >> 2)) << 16) | (uint32_t)(X + (b & 3));
+                if (pos < fcand_cap) fcand[pos] = ((yb + (uint32_t)(b >> 2)) << 16) | (uint32_t)(X + (b & 3));
                 pos++;
             }
         }
@@ -566,11 +577,10 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
 // below th is below m already, and a pixel of score 0 (m = 1) loses to any
 // neighbour.  The neighbour test does not depend on th, so one pass over the
 // region yields the survivors at iniThFAST and at minThFAST; the latter are
-// used when the former are none.  The region is rebuilt in shared memory as
-// words with a zero ring (cleared, then the cell's corners scattered into
-// it); words without a corner are skipped whole.
-// Survivors are written in the detector's row-major order (lane order is
-// row-major order within an iteration).
+// used when the former are none.  The region is rebuilt in shared memory with
+// a zero ring (cleared, then the cell's corners scattered into it); each lane
+// then tests its corners against their 8 neighbours there, and the survivors
+// are written in the detector's row-major order (ranked by row and column).
 // CPB (cells per block, 1 / 2 / 4) is chosen by the autotuner.
 template <int CPB>
 __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status,
@@ -581,8 +591,8 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cell = it.index * CPB + warp;
     if (cell >= d.nCols * d.nRows) return;
-    // per warp: the region rows (sm.rows of FAST_ROW bytes), then sm.min_cap
-    // minThFAST survivors
+    // per warp: the region rows (sm.rows of FAST_ROW bytes), then the
+    // minThFAST and the iniThFAST survivors (sm.min_cap keys each)
     extern __shared__ __align__(16) uint8_t s_dyn[];
     uint8_t* mstr = s_dyn + (size_t)warp * sm.warp_bytes;
     uint16_t* smin = reinterpret_cast<uint16_t*>(mstr + sm.rows * FAST_ROW);
@@ -606,7 +616,6 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
     // staged row: byte b <-> region column b - 4; words 1..nwr hold region
     // bytes; everything else stays zero (the ring)
     const int off = 0;
-    const int nwr = (off + 3 + dw) >> 2;
     {
         uint4* m16 = reinterpret_cast<uint4*>(mstr);
         for (int k = lane; k < (dh + 2) * (FAST_ROW / 16); k += 32) m16[k] = make_uint4(0u, 0u, 0u, 0u);
@@ -627,76 +636,68 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         ini_th = max(ini_th, 1);
         min_th = max(min_th, 1);
     }
-    const int lo_th = min(ini_th, min_th);
-    const uint32_t lo4 = (uint32_t)lo_th * 0x01010101u;
-    uint32_t* out = d.slots + (size_t)cell * d.cell_cap;
+    const int cell_cap = d.cell_cap;
+    uint32_t* const out = d.slots + (size_t)cell * cell_cap;
+    // the survivors at both thresholds, as row-major keys (row << 8 | column)
+    // in two lists of sm.min_cap entries each
+    uint16_t* const sini = smin + sm.min_cap;
     int total_ini = 0, total_min = 0;
-    const int rpi = 32 / nwr, lr = lane / nwr, lk = lane - lr * nwr + 1;
-    for (int rb = 0; rb < dh; rb += rpi) {
-        const int r = rb + lr;
-        uint32_t kini = 0, kmin = 0;  // survivors among the lane's 4 pixels
-        const uint8_t* row = mstr + (r + 1) * FAST_ROW + 4 * lk;
-        if (lr < rpi && r < dh) {
-            const uint32_t B = *reinterpret_cast<const uint32_t*>(row);
-            // only the bytes above the lower threshold (about one pixel in 80)
-            for (uint32_t cand = __vcmpgtu4(B, lo4) & 0x80808080u; cand; cand &= cand - 1) {
-                const int jj = (__ffs(cand) - 1) >> 3;
-                const int m = (int)((B >> (8 * jj)) & 0xFFu);
-                const uint8_t* p = row + jj;
-                int nb = max(max(p[-1], p[1]), max(max(p[-FAST_ROW - 1], p[-FAST_ROW]), p[-FAST_ROW + 1]));
-                nb = max(nb, max(max(p[FAST_ROW - 1], p[FAST_ROW]), p[FAST_ROW + 1]));
-                if (m > nb) {
-                    kini |= (uint32_t)(m > ini_th) << jj;
-                    kmin |= (uint32_t)(m > min_th) << jj;
+    {
+        const int nc = min(d.corner_count[cell], d.corner_cap);
+        const uint32_t* cl = d.corners + (size_t)cell * d.corner_cap;
+        const unsigned below = (1u << lane) - 1u;
+        for (int k0 = 0; k0 < nc; k0 += 32) {
+            const int k = k0 + lane;
+            bool oi = false, om = false;
+            int key = 0;
+            if (k < nc) {
+                const uint32_t e = cl[k];
+                const int r = (int)(e >> 16), c = (int)((e >> 8) & 0xFFu), m = (int)(e & 0xFFu);
+                if (r < dh && c < dw) {
+                    const uint8_t* q = mstr + (r + 1) * FAST_ROW + c + off + 4;
+                    int nb = max(max(q[-1], q[1]), max(max(q[-FAST_ROW - 1], q[-FAST_ROW]), q[-FAST_ROW + 1]));
+                    nb = max(nb, max(max(q[FAST_ROW - 1], q[FAST_ROW]), q[FAST_ROW + 1]));
+                    if (m > nb) {
+                        oi = m > ini_th;
+                        om = m > min_th;
+                    }
+                    key = (r << 8) | c;
                 }
             }
-        }
-        if (__any_sync(0xffffffffu, (kini | kmin) != 0)) {
-            const int ci = __popc(kini), cm = __popc(kmin);
-            int ii = ci, im = cm;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int ni = __shfl_up_sync(0xffffffffu, ii, o), nm = __shfl_up_sync(0xffffffffu, im, o);
-                if (lane >= o) {
-                    ii += ni;
-                    im += nm;
-                }
+            const unsigned bi = __ballot_sync(0xffffffffu, oi), bm = __ballot_sync(0xffffffffu, om);
+            if (oi) {
+                const int pos = total_ini + __popc(bi & below);
+                if (pos < sm.min_cap) sini[pos] = (uint16_t)key;
             }
-            int pi = total_ini + ii - ci, pm = total_min + im - cm;
-            const int c4 = 4 * lk - off - 4;  // region column of the lane's byte 0
-            for (uint32_t b = kini; b; b &= b - 1) {
-                const int jj = __ffs(b) - 1;
-                if (pi < d.cell_cap)
-                    out[pi] = (uint32_t)(gx0 + c4 + jj) | ((uint32_t)(gy0 + r) << 12) |
-                              ((uint32_t)(row[jj] - 1) << 24);
-                pi++;
+            if (om) {
+                const int pos = total_min + __popc(bm & below);
+                if (pos < sm.min_cap) smin[pos] = (uint16_t)key;
             }
-            for (uint32_t b = kmin; b; b &= b - 1) {
-                const int jj = __ffs(b) - 1;
-                if (pm < sm.min_cap) smin[pm] = (uint16_t)((r << 8) | (c4 + jj));
-                pm++;
-            }
-            total_ini += __shfl_sync(0xffffffffu, ii, 31);
-            total_min += __shfl_sync(0xffffffffu, im, 31);
+            total_ini += __popc(bi);
+            total_min += __popc(bm);
         }
-    }
-    if (total_ini > 0) {
-        if (lane == 0) {
-            if (total_ini > d.cell_cap) atomicOr(status, 2);
-            d.cell_count[cell] = min(total_ini, d.cell_cap);
-        }
-        return;
     }
     __syncwarp();
-    const int n = min(min(total_min, d.cell_cap), sm.min_cap);
+    // iniThFAST's survivors if there are any, else minThFAST's, in the
+    // detector's row-major order: a survivor's output row is the number of
+    // smaller keys (keys are distinct)
+    const bool use_ini = total_ini > 0;
+    const uint16_t* L = use_ini ? sini : smin;
+    const int total = use_ini ? total_ini : total_min;
+    const int n = min(total, sm.min_cap);
     for (int q = lane; q < n; q += 32) {
-        const int e = smin[q], r = e >> 8, c = e & 255;
-        out[q] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
-                 ((uint32_t)(mstr[(r + 1) * FAST_ROW + c + off + 4] - 1) << 24);
+        const int key = L[q];
+        int rank = 0;
+        for (int t = 0; t < n; t++) rank += (int)L[t] < key;
+        if (rank < cell_cap) {
+            const int r = key >> 8, c = key & 255;
+            out[rank] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
+                        ((uint32_t)(mstr[(r + 1) * FAST_ROW + c + off + 4] - 1) << 24);
+        }
     }
     if (lane == 0) {
-        if (total_min > d.cell_cap) atomicOr(status, 2);
-        d.cell_count[cell] = n;
+        if (total > cell_cap || total > sm.min_cap) atomicOr(status, 2);
+        d.cell_count[cell] = min(n, cell_cap);
     }
 }
 
@@ -1336,7 +1337,7 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, i
     sm.rows = std::min(FAST_MAX_DET, std::max(1, max_hcell)) + 2;
     const int mw = std::min(FAST_MAX_DET, std::max(1, max_wcell)), mh = sm.rows - 2;
     sm.min_cap = ((mw + 1) / 2) * ((mh + 1) / 2);
-    sm.warp_bytes = ((sm.rows * FAST_ROW + 2 * sm.min_cap) + 15) & ~15;
+    sm.warp_bytes = ((sm.rows * FAST_ROW + 4 * sm.min_cap) + 15) & ~15;
     const int cpb = tunables().fast_cells_per_block;
     const size_t smem = (size_t)cpb * sm.warp_bytes;
     switch (cpb) {

@@ -139,8 +139,8 @@ void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStr
 // Shared memory layout of k_fast_cells for one launch (per warp).
 struct FastCellsSmem {
     int rows;        // staged region rows: the largest detection region + 2
-    int min_cap;     // minThFAST survivors kept
-    int warp_bytes;  // rows * FAST_ROW + 2 * min_cap, 16-byte multiple
+    int min_cap;     // survivors kept per threshold
+    int warp_bytes;  // rows * FAST_ROW + 4 * min_cap (two survivor lists), 16-byte multiple
 };
 // max_wcell / max_hcell: the largest cell of the launch (sizes its shared memory).
 void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, int max_wcell, int max_hcell,
