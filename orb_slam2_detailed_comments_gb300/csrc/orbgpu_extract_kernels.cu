@@ -1073,7 +1073,7 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
 // list finds its level by binary search.
 // G (keypoints per warp, 4 / 8 / 16 / 32) is chosen by the autotuner.
 template <int G>
-__global__ void __launch_bounds__(256) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
+__global__ void __launch_bounds__(256, 6) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
                                                   uint8_t* out_desc, int* status) {
     extern __shared__ int s_pre[];  // ndescs + 1
     __shared__ int s_scan[32];
