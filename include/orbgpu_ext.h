@@ -145,8 +145,6 @@ int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots,
 /* Launch shapes the autotuner chooses (orb_slam2_detailed_comments_gb300.autotune):
  *   "resize_rows"          strip rows of the resize / blur / FAST-strength kernel: 8, 22, 36, 64
  *   "fast_cells_per_block" FAST cells (one warp each) per block: 1, 2, 4
- *   "fast_score_overlap"   1: each level's FAST candidates scored on a side stream
- *                          beside the later levels' strips; 0: all in one launch
  *   "describe_group"       keypoints per warp of the descriptor kernel: 4, 8, 16, 32
  *   "knn_tc_min_pairs"     query x train size from which orbgpu_knn2(algo -1) uses tcgen05
  * Process-wide; a change makes extractors and batches re-plan (and re-capture

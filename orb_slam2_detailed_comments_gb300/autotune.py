@@ -31,7 +31,6 @@ PARAMS = {
     "resize_rows": ((8, 22, 36, 64), "resize_blur"),
     "fast_cells_per_block": ((1, 2, 4), "fast"),
     "describe_group": ((4, 8, 16, 32), "describe"),
-    "fast_score_overlap": ((0, 1), "resize_blur"),
 }
 KNN_PARAM = "knn_tc_min_pairs"
 

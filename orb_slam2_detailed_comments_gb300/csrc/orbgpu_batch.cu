@@ -126,10 +126,7 @@ struct orbgpu_batch {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_level[ORBGPU_MAX_LEVELS] = {};
-    // FAST scoring of a level beside the later strips (tuned option)
-    cudaStream_t side2 = nullptr;
-    cudaEvent_t ev_strip[ORBGPU_MAX_LEVELS] = {};
-    cudaEvent_t ev_join = nullptr;
+
     // frame configuration handed to the accessors of the last batch
     std::vector<float> frame_scale;  // nframes * 16
     std::vector<int> frame_w, frame_h;
@@ -185,12 +182,9 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
             return ORBGPU_ERR_CUDA;
         }
     bool side_ok = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) == cudaSuccess &&
-                   cudaStreamCreateWithFlags(&b->side2, cudaStreamNonBlocking) == cudaSuccess &&
-                   cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
-                   cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) == cudaSuccess;
+                   cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; side_ok && i < ORBGPU_MAX_LEVELS; i++)
-        side_ok = cudaEventCreateWithFlags(&b->ev_level[i], cudaEventDisableTiming) == cudaSuccess &&
-                  cudaEventCreateWithFlags(&b->ev_strip[i], cudaEventDisableTiming) == cudaSuccess;
+        side_ok = cudaEventCreateWithFlags(&b->ev_level[i], cudaEventDisableTiming) == cudaSuccess;
     if (!side_ok) {
         orbgpu_batch_destroy(b);
         return ORBGPU_ERR_CUDA;
@@ -224,11 +218,7 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
         if (b->ev_level[i]) cudaEventDestroy(b->ev_level[i]);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->side) cudaStreamDestroy(b->side);
-    if (b->side2) cudaStreamSynchronize(b->side2);
-    for (int i = 0; i < ORBGPU_MAX_LEVELS; i++)
-        if (b->ev_strip[i]) cudaEventDestroy(b->ev_strip[i]);
-    if (b->ev_join) cudaEventDestroy(b->ev_join);
-    if (b->side2) cudaStreamDestroy(b->side2);
+
     for (FramePlan* p : b->plans) delete p;
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -455,25 +445,15 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
                             b->rb_count[l], b->side);
         cudaEventRecord(b->ev_level[l], b->side);
     }
-    const int nsm = nsm_of_current_device();
-    const bool overlap = tunables().fast_score_overlap != 0;
     for (int l = 0; l < b->nlevels; l++) {
         if (l > 0) cudaStreamWaitEvent(st, b->ev_level[l], 0);
         launch_level_strip(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
                            b->rb_count[l], st);
-        if (overlap) {  // this level's candidates on the second side stream
-            cudaEventRecord(b->ev_strip[l], st);
-            cudaStreamWaitEvent(b->side2, b->ev_strip[l], 0);
-            launch_fast_score(b->d_descs, l, b->nlevels, b->nframes, std::max(8, (nsm * 8) >> l), b->side2);
-        }
     }
-    if (overlap) {
-        cudaEventRecord(b->ev_join, b->side2);
-        cudaStreamWaitEvent(st, b->ev_join, 0);
-    } else {
-        // the candidates of every level of every frame in one launch
-        launch_fast_score(b->d_descs, 0, 1, b->ndesc, nsm * 8, st);
-    }
+    // the candidates of every level of every frame in one launch (scoring
+    // each level apart, right after its strip or on a side stream beside the
+    // later strips, measured 1.6-2x slower)
+    launch_fast_score(b->d_descs, 0, 1, b->ndesc, nsm_of_current_device() * 8, st);
     mark(2);
     int mwc = 1, mhc = 1;
     for (int f = 0; f < b->nframes; f++)
@@ -488,9 +468,8 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
     mark(5);
-    // gather, strip per level, resize per level >= 1, FAST scoring (per level
-    // or once), 3 stages
-    b->launches_per_run = 1 + 2 * b->nlevels - 1 + (overlap ? b->nlevels : 1) + 3;
+    // gather, strip per level, resize per level >= 1, FAST scoring, 3 stages
+    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 1 + 3;
 }
 
 // The device status of the last extraction (copied to h_pinned[0] at its end)

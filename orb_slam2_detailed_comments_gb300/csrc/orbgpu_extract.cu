@@ -57,7 +57,6 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
         t.fast_cells_per_block = (int)value;
     else if (n == "describe_group" && (value == 4 || value == 8 || value == 16 || value == 32))
         t.describe_group = (int)value;
-    else if (n == "fast_score_overlap" && (value == 0 || value == 1)) t.fast_score_overlap = (int)value;
     else if (n == "knn_tc_min_pairs" && value >= 0) t.knn_tc_min_pairs = value;
     else {
         orbgpu_set_last_error("unknown tuning parameter or value", __FILE__, __LINE__);
@@ -74,7 +73,6 @@ extern "C" int orbgpu_tune_get(const char* name, long long* value) {
     if (n == "resize_rows") *value = t.resize_rows;
     else if (n == "fast_cells_per_block") *value = t.fast_cells_per_block;
     else if (n == "describe_group") *value = t.describe_group;
-    else if (n == "fast_score_overlap") *value = t.fast_score_overlap;
     else if (n == "knn_tc_min_pairs") *value = t.knn_tc_min_pairs;
     else return ORBGPU_ERR_BAD_ARG;
     return ORBGPU_OK;

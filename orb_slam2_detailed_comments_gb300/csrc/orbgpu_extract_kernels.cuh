@@ -99,7 +99,6 @@ struct Tunables {
     int resize_rows = 36;
     int fast_cells_per_block = 4;
     int describe_group = 8;
-    int fast_score_overlap = 0;  // 1: score each level on a side stream beside the later strips
     long long knn_tc_min_pairs = 1LL << 28;
 };
 const Tunables& tunables();
