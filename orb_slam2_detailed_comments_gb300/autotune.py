@@ -30,7 +30,7 @@ from ._lib import check, lib
 PARAMS = {
     "resize_rows": ((8, 22, 36, 64), "resize_blur"),
     "fast_cells_per_block": ((1, 2, 4), "fast"),
-    "describe_group": ((4, 8, 16, 32), "describe"),
+    "describe_group": ((1, 2, 4), "describe"),
 }
 KNN_PARAM = "knn_tc_min_pairs"
 

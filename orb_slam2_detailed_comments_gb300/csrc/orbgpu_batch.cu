@@ -328,6 +328,12 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         for (int l = 1; l < nlevels; l++)
             ORBGPU_CUDA_TRY(cudaMemcpyAsync(base + P->layout.lv[l].xofs, P->table_blob[l].data(), P->table_blob[l].size(),
                                             cudaMemcpyHostToDevice, st));
+        // the descriptor kernel's tensor maps of this slot (a pageable
+        // source: the copy has taken the bytes when it returns)
+        std::vector<uint8_t> maps;
+        const int mrc = encode_patch_maps(P->geom, P->layout, base, maps);
+        if (mrc != ORBGPU_OK) return mrc;
+        ORBGPU_CUDA_TRY(cudaMemcpyAsync(base + P->layout.patch_maps, maps.data(), maps.size(), cudaMemcpyHostToDevice, st));
         b->slot_plan[f] = P;
         b->slot_gen[f] = P->gen;
     }

@@ -9,6 +9,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "orbgpu_extract_kernels.cuh"
 #include "orbgpu_host.h"
 
@@ -55,7 +58,7 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
     if (n == "resize_rows" && (value == 8 || value == 22 || value == 36 || value == 64)) t.resize_rows = (int)value;
     else if (n == "fast_cells_per_block" && (value == 1 || value == 2 || value == 4))
         t.fast_cells_per_block = (int)value;
-    else if (n == "describe_group" && (value == 4 || value == 8 || value == 16 || value == 32))
+    else if (n == "describe_group" && (value == 1 || value == 2 || value == 4))
         t.describe_group = (int)value;
     else if (n == "knn_tc_min_pairs" && value >= 0) t.knn_tc_min_pairs = value;
     else {
@@ -268,6 +271,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         ncells_total += g[l].ncells;
     }
     corner_counts = take(sizeof(int) * std::max(1, ncells_total));
+    patch_maps = take((size_t)2 * ORBGPU_TMAP_BYTES * g.size());
     bytes = off - base;
     return off;
 }
@@ -337,7 +341,70 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.out_base = out_base;
         d.out_cap = out_cap;
         d.frame_total = (int*)(arena + lay.frame_total);
+        d.tm_level = arena + lay.patch_maps + (size_t)2 * ORBGPU_TMAP_BYTES * l;
+        d.tm_blur = arena + lay.patch_maps + (size_t)(2 * l + 1) * ORBGPU_TMAP_BYTES;
     }
+}
+
+// ---------------------------------------------------------------- patch tensor maps
+// k_describe copies each keypoint's patches into shared memory with 2-D
+// tensor copies: a DESC_LBOX_W x DESC_LBOX_H box of the level plane
+// (IC_Angle) and a DESC_BBOX_W x DESC_BBOX_H box of the blurred plane
+// (rBRIEF).  The maps span pitch x h bytes of the slot's planes (the pitch is
+// a multiple of 64 and the planes start 256-byte aligned, as the tensor copy
+// requires); box columns past the pitch read as zero and are never used.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, []() {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+int encode_patch_maps(const std::vector<LevelGeom>& g, const FrameLayout& lay, uint8_t* arena,
+                      std::vector<uint8_t>& out) {
+    static_assert(sizeof(CUtensorMap) == ORBGPU_TMAP_BYTES, "tensor map size");
+    auto encode = tensor_map_encoder();
+    if (!encode) {
+        orbgpu_set_last_error("cuTensorMapEncodeTiled is not available", __FILE__, __LINE__);
+        return ORBGPU_ERR_CUDA;
+    }
+    out.assign((size_t)2 * ORBGPU_TMAP_BYTES * g.size(), 0);
+    for (size_t l = 0; l < g.size(); l++) {
+        const LevelGeom& L = g[l];
+        // a level lower than the blurred box holds no describable keypoint
+        // (they lie EDGE_THRESHOLD >= DESC_BBOX_R rows inside): no maps
+        if (L.h < DESC_BBOX_H) continue;
+        for (int plane = 0; plane < 2; plane++) {
+            uint8_t* base = arena + (plane == 0 ? lay.lv[l].pyr : lay.lv[l].blur);
+            const cuuint64_t dims[2] = {(cuuint64_t)L.pitch, (cuuint64_t)L.h};
+            const cuuint64_t strides[1] = {(cuuint64_t)L.pitch};
+            const cuuint32_t box[2] = {plane == 0 ? (cuuint32_t)DESC_LBOX_W : (cuuint32_t)DESC_BBOX_W,
+                                       plane == 0 ? (cuuint32_t)DESC_LBOX_H : (cuuint32_t)DESC_BBOX_H};
+            const cuuint32_t estr[2] = {1, 1};
+            if (((uintptr_t)base & 15) || (L.pitch & 15)) {
+                orbgpu_set_last_error("plane not aligned for tensor copies", __FILE__, __LINE__);
+                return ORBGPU_ERR_CUDA;
+            }
+            CUtensorMap* m = (CUtensorMap*)(out.data() + (size_t)(2 * l + plane) * ORBGPU_TMAP_BYTES);
+            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) {
+                char msg[96];
+                std::snprintf(msg, sizeof(msg), "cuTensorMapEncodeTiled failed (%d)", (int)r);
+                orbgpu_set_last_error(msg, __FILE__, __LINE__);
+                return ORBGPU_ERR_CUDA;
+            }
+        }
+    }
+    return ORBGPU_OK;
 }
 
 // ---------------------------------------------------------------- sin/cos exceptions
@@ -521,6 +588,16 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
             free_plan(P);
             return ORBGPU_ERR_CUDA;
         }
+    }
+    // the descriptor kernel's tensor maps of this arena
+    std::vector<uint8_t> maps;
+    rc = encode_patch_maps(g, P->layout, P->arena, maps);
+    if (rc == ORBGPU_OK &&
+        cudaMemcpy(P->arena + P->layout.patch_maps, maps.data(), maps.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = ORBGPU_ERR_CUDA;
+    if (rc != ORBGPU_OK) {
+        free_plan(P);
+        return rc;
     }
     // block ranges: per level the resize/blur tiles (one entry), then the
     // cells of every level (one entry per level)

@@ -1,6 +1,7 @@
 // orbgpu_extract_kernels.cu -- the ORB extraction stages (see the .cuh).
 #include <algorithm>
 
+#include "orbgpu_async.cuh"
 #include "orbgpu_extract_kernels.cuh"
 #include "orb_pattern.h"
 #include "orbgpu_host.h"
@@ -1057,28 +1058,52 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
     return v;
 }
 
-// Orientation and descriptor of the kept keypoints, G keypoints per warp and
-// no block-level synchronisation after the prologue: phase A computes the
-// IC_Angle moments with one lane per patch column (every row read is one
-// coalesced segment), two keypoints' loads in flight; phase B evaluates
-// fastAtan2 and the double-precision rotation of the warp's keypoints at once
-// (one keypoint per lane: the FP64 pipe is narrow on this GPU); phase C
-// builds the rBRIEF descriptors with one descriptor byte per lane, two
-// keypoints at a time, the pattern read from shared memory.  The group size
-// trades FP64 lane use against the serial chain of phases A and C inside a
-// warp.
+// Orientation and descriptor of the kept keypoints, 32 keypoints per warp
+// task (one per lane) and no block-level synchronisation after the prologue.
+// The task's patches are staged in shared memory by tensor copies in rounds
+// of R keypoints through two buffers of the warp, each with its mbarrier;
+// two rounds are in flight while one is computed:
+//   pass A   the IC_Angle disc of each keypoint from the level plane
+//            (DESC_LBOX_*): moments with one lane per patch column;
+//   pass B   fastAtan2 and the double-precision rotation of all 32 keypoints
+//            at once, one per lane (the FP64 pipe is narrow on this GPU: a
+//            full warp per instruction);
+//   pass C   the rBRIEF disc from the blurred plane (DESC_BBOX_*): one
+//            descriptor byte per lane, two keypoints at a time, the pattern
+//            read from shared memory.
 // Each block scans the levels' kept counts into shared memory (descriptors
 // are frame-major with levels ascending, so a level's offset inside its
 // frame is a difference of two prefix entries); keypoint g of the flattened
-// list finds its level by binary search.
-// G (keypoints per warp, 4 / 8 / 16 / 32) is chosen by the autotuner.
-template <int G>
-__global__ void __launch_bounds__(256, 6) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
-                                                  uint8_t* out_desc, int* status) {
-    extern __shared__ int s_pre[];  // ndescs + 1
+// list finds its level by binary search.  R (1 / 2 / 4 keypoints per round,
+// with WPB = 12 / 6 / 3 warps per block) is chosen by the autotuner.  A copy
+// that does not complete within the bounded wait sets status bit 128 and
+// ends the warp once the copies in flight are drained.
+static_assert(ORBGPU_EDGE_THRESHOLD >= DESC_BBOX_R && ORBGPU_EDGE_THRESHOLD >= ORBGPU_HALF_PATCH,
+              "boxes start inside the plane");
+static_assert(15 + 2 * ORBGPU_HALF_PATCH + 1 <= DESC_LBOX_W && 15 + DESC_BBOX_H <= DESC_BBOX_W,
+              "a box covers its disc from a 16-byte aligned column");
+static_assert(DESC_LBOX_W * DESC_LBOX_H <= DESC_SLOT && DESC_BBOX_W * DESC_BBOX_H <= DESC_SLOT &&
+                  DESC_SLOT % 128 == 0 && DESC_LBOX_W % 16 == 0 && DESC_BBOX_W % 16 == 0,
+              "box slots");
+template <int R, int WPB>
+__global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
+                                                       uint8_t* out_desc, int* status) {
+    extern __shared__ __align__(128) uint8_t s_dyn[];  // boxes (128-byte aligned) | s_pre[ndescs + 1]
     __shared__ int s_scan[32];
-    __shared__ float2 s_pat[16][32];  // lane l's pattern point 16 l + p at [p][l]
-    const int lane = threadIdx.x & 31;
+    __shared__ float2 s_pat[16][32];   // lane l's pattern point 16 l + p at [p][l]
+    __shared__ uint64_t s_bar[2 * WPB];  // per warp: one per buffer
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t dyn0 = smem_u32(s_dyn);
+    uint8_t* boxes = s_dyn + (((dyn0 + 127u) & ~127u) - dyn0);
+    uint8_t* wbuf = boxes + (size_t)warp * 2 * R * DESC_SLOT;
+    int* s_pre = (int*)(boxes + (size_t)WPB * 2 * R * DESC_SLOT);
+    uint64_t* bar = &s_bar[2 * warp];
+    if (lane == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
     for (int i = threadIdx.x; i < 512; i += blockDim.x) {
         const int l = i >> 4, p = i & 15;
         s_pat[p][l] = make_float2((float)c_pattern[2 * i], (float)c_pattern[2 * i + 1]);
@@ -1100,18 +1125,21 @@ __global__ void __launch_bounds__(256, 6) k_describe(const LevelDesc* descs, int
             const LevelDesc& d = descs[e];
             if (d.level == 0) *d.frame_total = s_pre[min(ndescs, e + d.nlevels)] - s_pre[e];
         }
-    const int nwarps = gridDim.x * (blockDim.x >> 5);
-    const int u = lane - ORBGPU_HALF_PATCH;  // patch column of this lane in phase A
+    const int u = lane - ORBGPU_HALF_PATCH;  // patch column of this lane in pass A
     const int au = u < 0 ? -u : u;
-    for (int g0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G; g0 < total; g0 += nwarps * G) {
-        // this lane's keypoint (lanes < G): level, position, output row, validity
-        const int g = g0 + lane;
+    // rows of the disc in this lane's column: |v| <= vmax (umax is non-increasing)
+    int vmax = -1;
+    if (lane < 2 * ORBGPU_HALF_PATCH + 1)
+        for (int v = 0; v <= ORBGPU_HALF_PATCH; v++)
+            if (c_umax[v] >= au) vmax = v;
+    uint32_t par = 0;  // bit b: the phase parity buffer b waits for next
+    const int ntasks = (total + 31) >> 5;
+    for (int t = blockIdx.x * WPB + warp; t < ntasks; t += gridDim.x * WPB) {
+        // this lane's keypoint: level, position, output row, validity
+        const int g = t * 32 + lane;
         int e = 0, x = 0, y = 0, score = 0, o = 0;
         bool valid = false;
-        const uint8_t* lvl = nullptr;  // this keypoint's level plane and blurred plane
-        const uint8_t* blr = nullptr;
-        int pitch = 0;
-        if (lane < G && g < total) {
+        if (g < total) {
             int lo = 0, hi = ndescs - 1;  // last e with s_pre[e] <= g
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -1126,63 +1154,97 @@ __global__ void __launch_bounds__(256, 6) k_describe(const LevelDesc* descs, int
             y = (int)((p >> 12) & 0xFFF);
             score = (int)(p >> 24);
             o = d.out_base + off + k;
-            pitch = d.pitch;
-            lvl = d.dst + (size_t)y * pitch + x;
-            blr = d.blur + (size_t)y * pitch + x;
             valid = true;
             if (off + k >= d.out_cap) {
                 atomicOr(status, 16);
                 valid = false;
             } else if (x < ORBGPU_EDGE_THRESHOLD || y < ORBGPU_EDGE_THRESHOLD || x > d.w - ORBGPU_EDGE_THRESHOLD - 1 ||
                        y > d.h - ORBGPU_EDGE_THRESHOLD - 1) {
-                // keypoints lie at least EDGE_THRESHOLD pixels inside their level
+                // keypoints lie at least EDGE_THRESHOLD pixels inside their
+                // level, so both boxes lie inside the plane's rows and start
+                // at a column >= 0 (EDGE_THRESHOLD >= DESC_BBOX_R)
                 atomicOr(status, 64);
                 valid = false;
             }
         }
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        // phase A: IC_Angle moments (src/ORBextractor.cc:94-141), integer exact, two keypoints at a time
+        const unsigned vmask = __ballot_sync(FULL, valid);
+        if (vmask == 0) continue;
+        const int nv = __popc(vmask);
+        const int rank = __popc(vmask & ((1u << lane) - 1u));  // among the valid lanes
+        const int nr = (nv + R - 1) / R;                         // rounds
+        const void* tm_l = nullptr;
+        const void* tm_b = nullptr;
+        if (valid) {
+            tm_l = descs[e].tm_level;
+            tm_b = descs[e].tm_blur;
+            tensormap_acquire(tm_l);
+            tensormap_acquire(tm_b);
+        }
+        // round i of a pass: the valid lanes of ranks [i R, i R + R) copy
+        // their box into slot rank - i R of buffer i & 1
+        auto issue = [&](int i, bool blurred) {
+            const int b = i & 1;
+            if (lane == 0)
+                mbar_expect_tx(&bar[b], (uint32_t)min(R, nv - i * R) *
+                                            (blurred ? DESC_BBOX_W * DESC_BBOX_H : DESC_LBOX_W * DESC_LBOX_H));
+            __syncwarp();
+            if (valid && rank / R == i) {
+                uint8_t* dst = wbuf + (b * R + rank % R) * DESC_SLOT;
+                if (blurred) tma_load_2d(dst, tm_b, (x - DESC_BBOX_R) & ~15, y - DESC_BBOX_R, &bar[b]);
+                else tma_load_2d(dst, tm_l, (x - ORBGPU_HALF_PATCH) & ~15, y - ORBGPU_HALF_PATCH, &bar[b]);
+            }
+        };
+        // bounded wait for round i; on a timeout the rounds still in flight
+        // (i and i + 1) get one more bounded wait each before the warp leaves
+        auto wait = [&](int i) -> bool {
+            const int b = i & 1;
+            if (__all_sync(FULL, mbar_wait(&bar[b], (par >> b) & 1u))) {
+                par ^= 1u << b;
+                return true;
+            }
+            mbar_wait(&bar[b], (par >> b) & 1u);
+            if (i + 1 < nr) mbar_wait(&bar[b ^ 1], (par >> (b ^ 1)) & 1u);
+            if (lane == 0) atomicOr(status, 128);
+            return false;
+        };
+        // pass A: IC_Angle moments (src/ORBextractor.cc:94-141) from the
+        // staged discs, integer exact: per column u the sum s and the
+        // row-weighted sum sv of the disc's pixels, m_10 = sum u s, m_01 = sum sv
         int my_m01 = 0, my_m10 = 0;
-        for (unsigned rest = vmask; rest;) {
-            const int ka = __ffs(rest) - 1;
-            rest &= rest - 1;
-            const int kb = rest ? __ffs(rest) - 1 : -1;
-            if (rest) rest &= rest - 1;
-            const uint8_t* pa = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)lvl, ka) + u;
-            const uint8_t* pb = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)lvl, kb < 0 ? ka : kb) + u;
-            const int sa = __shfl_sync(0xffffffffu, pitch, ka), sb_ = __shfl_sync(0xffffffffu, pitch, kb < 0 ? ka : kb);
-            int a10 = 0, a01 = 0, b10 = 0, b01 = 0;
-            if (lane < 2 * ORBGPU_HALF_PATCH + 1) {
+        issue(0, false);
+        if (nr > 1) issue(1, false);
+        unsigned rest = vmask;
+        for (int i = 0; i < nr; i++) {
+            if (!wait(i)) return;
+            const uint8_t* buf = wbuf + (i & 1) * R * DESC_SLOT;
+            for (int j = 0; j < R && rest; j++) {
+                const int k = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const int xk = __shfl_sync(FULL, x, k);
+                const uint8_t* col = buf + j * DESC_SLOT + ((xk - ORBGPU_HALF_PATCH) & 15) + lane;
+                int sum = 0, vsum = 0;
 #pragma unroll
                 for (int v = -ORBGPU_HALF_PATCH; v <= ORBGPU_HALF_PATCH; v++) {
-                    if (c_umax[v < 0 ? -v : v] >= au) {
-                        const int va = pa[v * sa];
-                        a10 += u * va;
-                        a01 += v * va;
-                        if (kb >= 0) {
-                            const int vb = pb[v * sb_];
-                            b10 += u * vb;
-                            b01 += v * vb;
-                        }
+                    if ((v < 0 ? -v : v) <= vmax) {
+                        const int val = col[(v + ORBGPU_HALF_PATCH) * DESC_LBOX_W];
+                        sum += val;
+                        vsum += v * val;
                     }
                 }
-            }
-            a10 = warp_sum(a10);
-            a01 = warp_sum(a01);
-            if (lane == ka) {
-                my_m10 = a10;
-                my_m01 = a01;
-            }
-            if (kb >= 0) {
-                b10 = warp_sum(b10);
-                b01 = warp_sum(b01);
-                if (lane == kb) {
-                    my_m10 = b10;
-                    my_m01 = b01;
+                const int m10 = __reduce_add_sync(FULL, u * sum);
+                const int m01 = __reduce_add_sync(FULL, vsum);
+                if (lane == k) {
+                    my_m10 = m10;
+                    my_m01 = m01;
                 }
             }
+            __syncwarp();  // buffer i & 1 is read: round i + 2 may overwrite it
+            if (i + 2 < nr) issue(i + 2, false);
         }
-        // phase B: angle and rotation, one keypoint per lane
+        // the first two rounds of pass C travel during pass B
+        issue(0, true);
+        if (nr > 1) issue(1, true);
+        // pass B: angle and rotation, one keypoint per lane
         float angle = 0.f, ca = 0.f, sb = 0.f;
         if (valid) {
             angle = fast_atan2_deg((float)my_m01, (float)my_m10);
@@ -1208,42 +1270,56 @@ __global__ void __launch_bounds__(256, 6) k_describe(const LevelDesc* descs, int
             kp.class_id = -1;
             out_kps[o] = kp;
         }
-        // phase C: rBRIEF, one descriptor byte per lane, two keypoints at a time
-        for (unsigned rest = vmask; rest;) {
-            const int ka = __ffs(rest) - 1;
-            rest &= rest - 1;
-            const int kb = rest ? __ffs(rest) - 1 : -1;
-            if (rest) rest &= rest - 1;
-            const int kb_ = kb < 0 ? ka : kb;
-            const uint8_t* cA = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)blr, ka);
-            const uint8_t* cB = (const uint8_t*)__shfl_sync(0xffffffffu, (unsigned long long)blr, kb_);
-            const int stA = __shfl_sync(0xffffffffu, pitch, ka), stB = __shfl_sync(0xffffffffu, pitch, kb_);
-            const float aA = __shfl_sync(0xffffffffu, ca, ka), bA = __shfl_sync(0xffffffffu, sb, ka);
-            const float aB = __shfl_sync(0xffffffffu, ca, kb_), bB = __shfl_sync(0xffffffffu, sb, kb_);
-            const int oA = __shfl_sync(0xffffffffu, o, ka), oB = __shfl_sync(0xffffffffu, o, kb_);
-            int valA = 0, valB = 0;
+        // pass C: rBRIEF from the staged blurred discs, one descriptor byte
+        // per lane, two keypoints at a time
+        rest = vmask;
+        for (int i = 0; i < nr; i++) {
+            if (!wait(i)) return;
+            const uint8_t* buf = wbuf + (i & 1) * R * DESC_SLOT;
 #pragma unroll
-            for (int kk = 0; kk < 8; kk++) {
-                int tA[2], tB[2] = {0, 0};
+            for (int j = 0; j < R; j += 2) {
+                if (!rest) break;
+                const int ka = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const int kb = (j + 1 < R && rest) ? __ffs(rest) - 1 : -1;
+                if (kb >= 0) rest &= rest - 1;
+                const int kb_ = kb < 0 ? ka : kb;
+                const int xA = __shfl_sync(FULL, x, ka), xB = __shfl_sync(FULL, x, kb_);
+                // the keypoint's pixel inside its box: row DESC_BBOX_R, column
+                // DESC_BBOX_R + (x - DESC_BBOX_R) mod 16
+                const uint8_t* cA =
+                    buf + j * DESC_SLOT + DESC_BBOX_R * DESC_BBOX_W + DESC_BBOX_R + ((xA - DESC_BBOX_R) & 15);
+                const uint8_t* cB = buf + (kb < 0 ? j : j + 1) * DESC_SLOT + DESC_BBOX_R * DESC_BBOX_W + DESC_BBOX_R +
+                                    ((xB - DESC_BBOX_R) & 15);
+                const float aA = __shfl_sync(FULL, ca, ka), bA = __shfl_sync(FULL, sb, ka);
+                const float aB = __shfl_sync(FULL, ca, kb_), bB = __shfl_sync(FULL, sb, kb_);
+                const int oA = __shfl_sync(FULL, o, ka), oB = __shfl_sync(FULL, o, kb_);
+                int valA = 0, valB = 0;
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    const float2 pt = s_pat[2 * kk + q][lane];
-                    {
-                        const int ry = cv_round(__fadd_rn(__fmul_rn(pt.x, bA), __fmul_rn(pt.y, aA)));
-                        const int rx = cv_round(__fsub_rn(__fmul_rn(pt.x, aA), __fmul_rn(pt.y, bA)));
-                        tA[q] = cA[ry * stA + rx];
+                for (int kk = 0; kk < 8; kk++) {
+                    int tA[2], tB[2] = {0, 0};
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        const float2 pt = s_pat[2 * kk + q][lane];
+                        {
+                            const int ry = cv_round(__fadd_rn(__fmul_rn(pt.x, bA), __fmul_rn(pt.y, aA)));
+                            const int rx = cv_round(__fsub_rn(__fmul_rn(pt.x, aA), __fmul_rn(pt.y, bA)));
+                            tA[q] = cA[ry * DESC_BBOX_W + rx];
+                        }
+                        if (kb >= 0) {
+                            const int ry = cv_round(__fadd_rn(__fmul_rn(pt.x, bB), __fmul_rn(pt.y, aB)));
+                            const int rx = cv_round(__fsub_rn(__fmul_rn(pt.x, aB), __fmul_rn(pt.y, bB)));
+                            tB[q] = cB[ry * DESC_BBOX_W + rx];
+                        }
                     }
-                    if (kb >= 0) {
-                        const int ry = cv_round(__fadd_rn(__fmul_rn(pt.x, bB), __fmul_rn(pt.y, aB)));
-                        const int rx = cv_round(__fsub_rn(__fmul_rn(pt.x, aB), __fmul_rn(pt.y, bB)));
-                        tB[q] = cB[ry * stB + rx];
-                    }
+                    valA |= (tA[0] < tA[1]) << kk;
+                    valB |= (tB[0] < tB[1]) << kk;
                 }
-                valA |= (tA[0] < tA[1]) << kk;
-                valB |= (tB[0] < tB[1]) << kk;
+                out_desc[(size_t)oA * 32 + lane] = (uint8_t)valA;
+                if (kb >= 0) out_desc[(size_t)oB * 32 + lane] = (uint8_t)valB;
             }
-            out_desc[(size_t)oA * 32 + lane] = (uint8_t)valA;
-            if (kb >= 0) out_desc[(size_t)oB * 32 + lane] = (uint8_t)valB;
+            __syncwarp();
+            if (i + 2 < nr) issue(i + 2, true);
         }
     }
 }
@@ -1355,18 +1431,23 @@ void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_ke
                      cudaStream_t st) {
     if (ndescs <= 0 || max_kept <= 0) return;
     const int nsm = nsm_of_current_device();
-    const int group = tunables().describe_group;
-    // 'group' keypoints per warp, 8 warps per block; max_kept (the node
-    // capacity) overestimates a level's keypoints about twice; warps stride
-    // over the groups, at most 8 blocks per SM
-    const long want = ((long)ndescs * max_kept / 2 + 8 * group - 1) / (8 * group);
-    const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 8));
-    const size_t smem = sizeof(int) * (ndescs + 1);
-    switch (group) {
-        case 4: k_describe<4><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
-        case 8: k_describe<8><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
-        case 16: k_describe<16><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
-        default: k_describe<32><<<blocks, 256, smem, st>>>(descs, ndescs, kps, desc, status); break;
+    const int R = tunables().describe_group;
+    // 32-keypoint warp tasks; two buffers of R box slots per warp, 24 slots
+    // (60 KiB) per block: three blocks per SM.
+    // max_kept (the node capacity) overestimates a level's keypoints about
+    // twice; warps stride over the tasks
+    const int wpb = 12 / R;
+    const size_t smem = (size_t)2 * R * wpb * DESC_SLOT + 128 + sizeof(int) * (ndescs + 1);
+    const long want = ((long)ndescs * max_kept / 2 + 32 * wpb - 1) / (32 * wpb);
+    const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 3));
+    auto run = [&](auto kernel) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kernel<<<blocks, 32 * wpb, smem, st>>>(descs, ndescs, kps, desc, status);
+    };
+    switch (R) {
+        case 1: run(k_describe<1, 12>); break;
+        case 4: run(k_describe<4, 3>); break;
+        default: run(k_describe<2, 6>); break;
     }
 }
 

@@ -21,13 +21,28 @@
 //   k_distribute         one (frame, level) per block: DistributeOctTree as a
 //                        sequence of parallel split steps over node creation
 //                        numbers.
-//   k_describe           4 to 32 keypoints per warp: IC_Angle, fastAtan2,
-//                        rBRIEF.
+//   k_describe           32 keypoints per warp, their patches staged in
+//                        shared memory by tensor copies in rounds of 1 to 4:
+//                        IC_Angle, fastAtan2, rBRIEF.
 #pragma once
 
 #include "orbgpu_common.cuh"
 
 namespace orbgpu {
+
+// Patch boxes of the descriptor kernel's tensor copies (bytes x rows): the
+// IC_Angle disc of radius HALF_PATCH_SIZE from a 16-byte aligned column of
+// the level plane, and the rBRIEF samples (rotated pattern points lie within
+// 18.4 pixels of the keypoint) from a 16-byte aligned column of the blurred
+// plane.  Each box has its own 128-byte aligned slot in shared memory, large
+// enough for either box.
+#define ORBGPU_TMAP_BYTES 128
+#define DESC_LBOX_W 48
+#define DESC_LBOX_H (2 * ORBGPU_HALF_PATCH + 1)
+#define DESC_BBOX_R 19
+#define DESC_BBOX_W 64
+#define DESC_BBOX_H (2 * DESC_BBOX_R + 1)
+#define DESC_SLOT 2560  // 64 x 39 = 2496 bytes (the larger box), rounded up to 128
 
 // Per-(frame, level) description shared by all stages.
 struct LevelDesc {
@@ -88,6 +103,10 @@ struct LevelDesc {
     int out_base;         // first output row of the frame
     int out_cap;          // output rows available to the frame
     int* frame_total;     // the frame's keypoint count
+    // tensor maps (CUtensorMap, in the frame's arena) of the level plane and
+    // the blurred plane for the descriptor kernel's patch copies
+    const void* tm_level;
+    const void* tm_blur;
 };
 
 // Launch shapes chosen by the autotuner (orbgpu_tune_set): strip rows of the
@@ -98,7 +117,7 @@ struct LevelDesc {
 struct Tunables {
     int resize_rows = 36;
     int fast_cells_per_block = 4;
-    int describe_group = 8;
+    int describe_group = 2;
     long long knn_tc_min_pairs = 1LL << 28;
 };
 const Tunables& tunables();

@@ -47,6 +47,9 @@ struct FrameLayout {
     size_t corner_counts = 0;
     std::vector<int> corner_first;
     int ncells_total = 0;
+    // two tensor maps per level (unblurred and blurred plane, 128 bytes
+    // each, level-major) for the descriptor kernel's patch copies
+    size_t patch_maps = 0;
     size_t bytes = 0;
     size_t plan(const std::vector<LevelGeom>& g, size_t base);
 };
@@ -59,6 +62,12 @@ bool resize_tables(int sw, int sh, int dw, int dh, int* xofs, short* xalpha, int
 int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom>& g);
 void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const FrameLayout& lay, uint8_t* arena,
                 int frame, int ini_th, int min_th, int out_base, int out_cap, LevelDesc* out);
+
+// Encodes the descriptor kernel's tensor maps of one frame (the layout's
+// patch_maps block: 2 x 128 bytes per level) for the arena slot at 'arena'
+// into 'out'; the caller copies them to arena + lay.patch_maps.
+int encode_patch_maps(const std::vector<LevelGeom>& g, const FrameLayout& lay, uint8_t* arena,
+                      std::vector<uint8_t>& out);
 
 int ensure_sincos_exceptions();
 int ensure_constants();

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <mutex>
 
+#include "orbgpu_async.cuh"
 #include "orbgpu_host.h"
 
 cudaStream_t orbgpu_matcher_stream_internal(orbgpu_matcher* m);
@@ -38,8 +39,6 @@ namespace orbgpu {
 #define TC_TTILE_BYTES (TC_N * TC_K)  // 64 KiB
 #define TC_EPI_WARPS 16
 #define TC_THREADS (32 * (TC_EPI_WARPS + 2))  // + producer warp + MMA warp
-#define TC_SPIN_LIMIT (1u << 26)
-#define TC_WAIT_NS 1000000000ull  // one second
 
 // ---------------------------------------------------------------- operand layout
 // Byte offset of element (row r, k) inside a tile stored K-major without
@@ -73,52 +72,6 @@ __global__ void k_expand_fp8(const uint8_t* __restrict__ desc, int n, int tile_r
 }
 
 // ---------------------------------------------------------------- PTX wrappers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-// Bounded wait on phase 'parity': false after about one second (or
-// TC_SPIN_LIMIT polls), whichever comes first.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    const uint32_t a = smem_u32(bar);
-    uint64_t t0 = 0;
-    for (uint32_t i = 0; i < TC_SPIN_LIMIT; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((i & 31) == 31) {
-            const uint64_t t = global_ns();
-            if (t0 == 0) t0 = t;
-            else if (t - t0 > TC_WAIT_NS) return false;
-        }
-    }
-    return false;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
 // K-major, no swizzle shared-memory operand descriptor.
 __device__ __forceinline__ uint64_t smem_desc(const void* base, uint32_t lbo, uint32_t sbo) {
     const uint64_t a = (uint64_t)((smem_u32(base) >> 4) & 0x3FFF);
