@@ -109,10 +109,6 @@ struct orbgpu_batch {
     bool pending = false;       // an asynchronous extraction whose status has not been read
     int* d_status = nullptr;
     int* d_totals = nullptr;  // per frame
-    int* d_fcand = nullptr;   // FAST candidate count per (frame, level)
-    int* d_ccount = nullptr;  // FAST corner count per (frame, cell): frame f's cells from f * ccount_stride
-    int ccount_stride = 0;
-    size_t ccount_cap = 0;
     int* h_pinned = nullptr;
     cudaGraphExec_t graph = nullptr;
     std::vector<int> graph_sig;
@@ -169,7 +165,6 @@ extern "C" int orbgpu_batch_create(int max_frames, int max_width, int max_height
     }
     if (cudaMalloc(&b->d_status, sizeof(int) * 4) != cudaSuccess ||
         cudaMalloc(&b->d_totals, sizeof(int) * max_frames) != cudaSuccess ||
-        cudaMalloc(&b->d_fcand, sizeof(int) * max_frames * ORBGPU_MAX_LEVELS) != cudaSuccess ||
         cudaMallocHost(&b->h_pinned, sizeof(int) * (8 + max_frames)) != cudaSuccess ||
         cudaMalloc(&b->d_src, sizeof(ImageSrc) * max_frames) != cudaSuccess ||
         cudaMallocHost(&b->h_src, sizeof(ImageSrc) * max_frames) != cudaSuccess) {
@@ -204,10 +199,8 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
     cudaFree(b->d_prefix);
     cudaFree(b->d_status);
     cudaFree(b->d_totals);
-    cudaFree(b->d_fcand);
     cudaFree(b->st_scratch);
     if (b->st_pinned) cudaFreeHost(b->st_pinned);
-    cudaFree(b->d_ccount);
     cudaFree(b->d_src);
     cudaFreeHost(b->h_src);
     cudaFreeHost(b->h_pinned);
@@ -348,27 +341,12 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     }
     std::vector<LevelDesc> hd(ndesc);
     b->frame_scale.assign((size_t)nframes * 16, 1.0f);
-    // per-cell corner counters of all frames in one array (one memset per run)
-    int stride = 1;
-    for (int f = 0; f < nframes; f++) stride = std::max(stride, b->cur[f]->layout.ncells_total);
-    if ((size_t)stride * b->max_frames > b->ccount_cap) {
-        ORBGPU_CUDA_TRY(cudaStreamSynchronize(st));
-        destroy_graph(b);
-        if (b->d_ccount) cudaFree(b->d_ccount);
-        b->d_ccount = nullptr;
-        ORBGPU_CUDA_TRY(dev_malloc(&b->d_ccount, sizeof(int) * (size_t)stride * b->max_frames));
-        b->ccount_cap = (size_t)stride * b->max_frames;
-    }
-    b->ccount_stride = stride;
     for (int f = 0; f < nframes; f++) {
         const FramePlan* P = b->cur[f];
         fill_descs(P->geom, P->tables, P->layout, b->arena + (size_t)f * b->slot_bytes, f, ini_th, min_th,
                    f * per_frame_cap, per_frame_cap, &hd[(size_t)f * nlevels]);
         for (int l = 0; l < nlevels; l++) {
             hd[(size_t)f * nlevels + l].frame_total = b->d_totals + f;
-            hd[(size_t)f * nlevels + l].fcand_count = b->d_fcand + (size_t)f * nlevels + l;
-            hd[(size_t)f * nlevels + l].corner_count =
-                b->d_ccount + (size_t)f * stride + b->cur[f]->layout.corner_first[l];
             b->frame_scale[(size_t)f * 16 + l] = P->tables.scale[l];
         }
     }
@@ -394,7 +372,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
     for (int f = 0; f < nframes; f++)
         for (int l = 0; l < nlevels; l++) {
             pre.push_back(acc);
-            acc += fast_blocks(b->cur[f]->geom[l].ncells);
+            acc += b->cur[f]->geom[l].ncells;
         }
     pre.push_back(acc);
     b->fast_count = acc;
@@ -440,8 +418,6 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     mark(0);
     k_gather_images<<<g, 256, 0, st>>>(b->d_src, b->nframes);
     mark(1);
-    cudaMemsetAsync(b->d_fcand, 0, sizeof(int) * b->ndesc, st);
-    cudaMemsetAsync(b->d_ccount, 0, sizeof(int) * (size_t)b->ccount_stride * b->nframes, st);
     // levels 1.. are resized in a chain on the side stream while the strips
     // of the levels already resized run on the batch's stream
     cudaEventRecord(b->ev_fork, st);
@@ -456,26 +432,24 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
         launch_level_strip(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
                            b->rb_count[l], st);
     }
-    // the candidates of every level of every frame in one launch (scoring
-    // each level apart, right after its strip or on a side stream beside the
-    // later strips, measured 1.6-2x slower)
-    launch_fast_score(b->d_descs, 0, 1, b->ndesc, nsm_of_current_device() * 8, st);
     mark(2);
-    int mwc = 1, mhc = 1;
+    int mwc = 1, mhc = 1, mbox = 0;
     for (int f = 0; f < b->nframes; f++)
         for (const LevelGeom& L : b->cur[f]->geom) {
             mwc = std::max(mwc, L.wCell);
             mhc = std::max(mhc, L.hCell);
+            if (L.ncells > 0) mbox = std::max(mbox, fast_cell_box_w(L.wCell) * (L.hCell + 6));
         }
     launch_fast(b->d_descs, RangeMap{b->d_prefix + b->fast_off, b->ndesc, 0, 1}, b->fast_count, b->d_status, mwc, mhc,
-                st);
+                mbox, st);
     mark(3);
     launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->d_status, st);
     mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
     mark(5);
-    // gather, strip per level, resize per level >= 1, FAST scoring, 3 stages
-    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 1 + 3;
+    // gather, strip per level, resize per level >= 1, FAST cells,
+    // DistributeOctTree, describe
+    b->launches_per_run = 1 + 2 * b->nlevels - 1 + 3;
 }
 
 // The device status of the last extraction (copied to h_pinned[0] at its end)

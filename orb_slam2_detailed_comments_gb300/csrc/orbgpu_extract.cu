@@ -193,7 +193,6 @@ int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom
         L.h = (int)std::lrint((float)h * t.inv_scale[l]);
         if (L.w < 1 || L.h < 1) return ORBGPU_ERR_BAD_ARG;
         L.pitch = (L.w + 63) & ~63;
-        L.fcand_cap = std::max(0, L.w - 2 * ORBGPU_EDGE_THRESHOLD) * std::max(0, L.h - 2 * ORBGPU_EDGE_THRESHOLD);
         const int minB = ORBGPU_EDGE_THRESHOLD - 3;
         L.maxBorderX = L.w - ORBGPU_EDGE_THRESHOLD + 3;
         L.maxBorderY = L.h - ORBGPU_EDGE_THRESHOLD + 3;
@@ -244,8 +243,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
         o.xalpha = take(sizeof(short) * 2 * L.w);
         o.yofs = take(sizeof(int) * L.h);
         o.ybeta = take(sizeof(short) * 2 * L.h);
-        o.fcand = take(sizeof(uint32_t) * std::max(1, L.fcand_cap));
-        o.corners = take(sizeof(uint32_t) * std::max<size_t>(1, (size_t)L.ncells * L.wCell * L.hCell));
+        o.cbits = take((size_t)(L.pitch / 8) * L.h);
         o.slots = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
         o.cell_count = take(sizeof(int) * std::max(1, L.ncells));
         o.cand = take(sizeof(uint32_t) * std::max(1, L.cand_cap));
@@ -263,15 +261,7 @@ size_t FrameLayout::plan(const std::vector<LevelGeom>& g, size_t base) {
     }
     level_counts = take(sizeof(int) * 16);
     frame_total = take(sizeof(int) * 4);
-    fcand_counts = take(sizeof(int) * 16);
-    corner_first.assign(g.size(), 0);
-    ncells_total = 0;
-    for (size_t l = 0; l < g.size(); l++) {
-        corner_first[l] = ncells_total;
-        ncells_total += g[l].ncells;
-    }
-    corner_counts = take(sizeof(int) * std::max(1, ncells_total));
-    patch_maps = take((size_t)2 * ORBGPU_TMAP_BYTES * g.size());
+    patch_maps = take((size_t)3 * ORBGPU_TMAP_BYTES * g.size());
     bytes = off - base;
     return off;
 }
@@ -310,12 +300,9 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.cell_count = (int*)(arena + o.cell_count);
         d.ini_th = ini_th;
         d.min_th = min_th;
-        d.fcand = (uint32_t*)(arena + o.fcand);
-        d.fcand_count = (int*)(arena + lay.fcand_counts) + l;
-        d.fcand_cap = L.fcand_cap;
-        d.corners = (uint32_t*)(arena + o.corners);
-        d.corner_count = (int*)(arena + lay.corner_counts) + lay.corner_first[l];
-        d.corner_cap = L.wCell * L.hCell;
+        d.cbits = arena + o.cbits;
+        d.cbits_stride = L.pitch / 8;
+        d.cell_box_w = fast_cell_box_w(L.wCell);
         d.nfeat = L.nfeat;
         d.nIni = L.nIni;
         d.cand_cap = L.cand_cap;
@@ -341,8 +328,9 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
         d.out_base = out_base;
         d.out_cap = out_cap;
         d.frame_total = (int*)(arena + lay.frame_total);
-        d.tm_level = arena + lay.patch_maps + (size_t)2 * ORBGPU_TMAP_BYTES * l;
-        d.tm_blur = arena + lay.patch_maps + (size_t)(2 * l + 1) * ORBGPU_TMAP_BYTES;
+        d.tm_level = arena + lay.patch_maps + (size_t)(3 * l) * ORBGPU_TMAP_BYTES;
+        d.tm_blur = arena + lay.patch_maps + (size_t)(3 * l + 1) * ORBGPU_TMAP_BYTES;
+        d.tm_cell = arena + lay.patch_maps + (size_t)(3 * l + 2) * ORBGPU_TMAP_BYTES;
     }
 }
 
@@ -350,9 +338,11 @@ void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const
 // k_describe copies each keypoint's patches into shared memory with 2-D
 // tensor copies: a DESC_LBOX_W x DESC_LBOX_H box of the level plane
 // (IC_Angle) and a DESC_BBOX_W x DESC_BBOX_H box of the blurred plane
-// (rBRIEF).  The maps span pitch x h bytes of the slot's planes (the pitch is
-// a multiple of 64 and the planes start 256-byte aligned, as the tensor copy
-// requires); box columns past the pitch read as zero and are never used.
+// (rBRIEF); k_fast_cells copies each cell's ROI, a fast_cell_box_w(wCell) x
+// (hCell + 6) box of the level plane.  The maps span pitch x h bytes of the
+// slot's planes (the pitch is a multiple of 64 and the planes start 256-byte
+// aligned, as the tensor copy requires); box bytes past the pitch or the last
+// row read as zero and are never used.
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
@@ -375,24 +365,29 @@ int encode_patch_maps(const std::vector<LevelGeom>& g, const FrameLayout& lay, u
         orbgpu_set_last_error("cuTensorMapEncodeTiled is not available", __FILE__, __LINE__);
         return ORBGPU_ERR_CUDA;
     }
-    out.assign((size_t)2 * ORBGPU_TMAP_BYTES * g.size(), 0);
+    out.assign((size_t)3 * ORBGPU_TMAP_BYTES * g.size(), 0);
     for (size_t l = 0; l < g.size(); l++) {
         const LevelGeom& L = g[l];
-        // a level lower than the blurred box holds no describable keypoint
-        // (they lie EDGE_THRESHOLD >= DESC_BBOX_R rows inside): no maps
-        if (L.h < DESC_BBOX_H) continue;
-        for (int plane = 0; plane < 2; plane++) {
-            uint8_t* base = arena + (plane == 0 ? lay.lv[l].pyr : lay.lv[l].blur);
+        for (int k = 0; k < 3; k++) {
+            // a level lower than the blurred box holds no describable
+            // keypoint (they lie EDGE_THRESHOLD >= DESC_BBOX_R rows inside),
+            // a level without cells no FAST corner: no maps
+            if (k < 2 ? L.h < DESC_BBOX_H : L.ncells == 0) continue;
+            uint8_t* base = arena + (k == 1 ? lay.lv[l].blur : lay.lv[l].pyr);
             const cuuint64_t dims[2] = {(cuuint64_t)L.pitch, (cuuint64_t)L.h};
             const cuuint64_t strides[1] = {(cuuint64_t)L.pitch};
-            const cuuint32_t box[2] = {plane == 0 ? (cuuint32_t)DESC_LBOX_W : (cuuint32_t)DESC_BBOX_W,
-                                       plane == 0 ? (cuuint32_t)DESC_LBOX_H : (cuuint32_t)DESC_BBOX_H};
+            const cuuint32_t box[2] = {k == 0   ? (cuuint32_t)DESC_LBOX_W
+                                       : k == 1 ? (cuuint32_t)DESC_BBOX_W
+                                                : (cuuint32_t)fast_cell_box_w(L.wCell),
+                                       k == 0   ? (cuuint32_t)DESC_LBOX_H
+                                       : k == 1 ? (cuuint32_t)DESC_BBOX_H
+                                                : (cuuint32_t)(L.hCell + 6)};
             const cuuint32_t estr[2] = {1, 1};
-            if (((uintptr_t)base & 15) || (L.pitch & 15)) {
-                orbgpu_set_last_error("plane not aligned for tensor copies", __FILE__, __LINE__);
+            if (((uintptr_t)base & 15) || (L.pitch & 15) || box[0] > 256 || box[1] > 256) {
+                orbgpu_set_last_error("plane or box not valid for tensor copies", __FILE__, __LINE__);
                 return ORBGPU_ERR_CUDA;
             }
-            CUtensorMap* m = (CUtensorMap*)(out.data() + (size_t)(2 * l + plane) * ORBGPU_TMAP_BYTES);
+            CUtensorMap* m = (CUtensorMap*)(out.data() + (size_t)(3 * l + k) * ORBGPU_TMAP_BYTES);
             const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr,
                                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -615,7 +610,7 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     int acc = 0;
     for (size_t l = 0; l < g.size(); l++) {
         pre.push_back(acc);
-        acc += fast_blocks(g[l].ncells);
+        acc += g[l].ncells;
     }
     pre.push_back(acc);
     P->fast_count = acc;
@@ -795,9 +790,6 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
     cudaStream_t st = ex->stream;
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->d_descs, hd, sizeof(LevelDesc) * nl, cudaMemcpyHostToDevice, st));
     ORBGPU_CUDA_TRY(cudaMemsetAsync(ex->d_status, 0, sizeof(int) * 4, st));
-    ORBGPU_CUDA_TRY(cudaMemsetAsync(P.arena + P.layout.fcand_counts, 0, sizeof(int) * 16, st));
-    ORBGPU_CUDA_TRY(cudaMemsetAsync(P.arena + P.layout.corner_counts, 0,
-                                    sizeof(int) * std::max(1, P.layout.ncells_total), st));
     // level 0 = the image
     ORBGPU_CUDA_TRY(cudaMemcpy2DAsync(hd[0].dst, hd[0].pitch, image, step, width, height,
                                       image_mem == ORBGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice
@@ -805,13 +797,14 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                       st));
     for (int l = 0; l < nl; l++)
         launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, st);
-    launch_fast_score(ex->d_descs, 0, 1, nl, nsm_of_current_device() * 2, st);
-    int mwc = 1, mhc = 1;
+    int mwc = 1, mhc = 1, mbox = 0;
     for (const LevelGeom& L : g) {
         mwc = std::max(mwc, L.wCell);
         mhc = std::max(mhc, L.hCell);
+        if (L.ncells > 0) mbox = std::max(mbox, fast_cell_box_w(L.wCell) * (L.hCell + 6));
     }
-    launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, mwc, mhc, st);
+    launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, mwc, mhc, mbox,
+                st);
     launch_distribute(ex->d_descs, nl, P.sort_cap, ex->d_status, st);
     launch_describe(ex->d_descs, nl, P.max_kept, okps, odesc, ex->d_status, st);
     ORBGPU_CUDA_TRY(cudaGetLastError());

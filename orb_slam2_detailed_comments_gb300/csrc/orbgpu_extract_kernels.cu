@@ -280,9 +280,10 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
 //  * FAST at the lower threshold t: the compass-point pre-test (two circle
 //    points among 0, 4, 8, 12 that are adjacent on the circle both brighter
 //    than v + t or both darker than v - t; every nine-pixel arc contains such
-//    a pair) in 16-bit lanes gives a candidate bitmap; after every seven rows
-//    the warp appends its candidates to the level's list (one atomic per
-//    warp), which k_fast_score scores.
+//    a pair) in 16-bit lanes gives the level's candidate bit map: the lanes of
+//    a pair (odd, even) own the 8 columns of one byte (x0 is a multiple of 8),
+//    so each row costs one shuffle and one byte store per pair; k_fast_cells
+//    scores the candidates.
 // Only rows and columns [19, dim - 19) are tested: every cell's detection
 // region lies inside them (cells start at EDGE_THRESHOLD - 3 + 3 and end 3
 // before maxBorder = dim - EDGE_THRESHOLD + 3), and k_fast_cells reads
@@ -308,127 +309,6 @@ __device__ __forceinline__ uint32_t rs_compass(uint32_t c, uint32_t p0, uint32_t
     const uint32_t d0 = c + K - p0, d4 = c + K - p4, d8 = c + K - p8, d12 = c + K - p12;
     // adjacent pairs (0,4) (4,8) (8,12) (12,0) == (0 | 8) & (4 | 12)
     return (((b0 | b8) & (b4 | b12)) | ((d0 | d8) & (d4 | d12))) & 0x80008000u;
-}
-
-// Largest arc threshold of the level pixel at cp (row pitch rw): max over the
-// sixteen nine-pixel arcs of the arc's smallest difference, for the
-// darker-centre (v - p) and brighter-centre (p - v) differences clipped at 0,
-// which travel together in the 16-bit halves of one word.  Above t exactly
-// when the pixel is a FAST corner at threshold t.
-__device__ __forceinline__ int level_arc_strength(const uint8_t* __restrict__ cp, int rw) {
-    const uint32_t v = __ldg(cp);
-    const uint32_t p[16] = {__ldg(cp + 3 * rw),  __ldg(cp + 3 * rw + 1),  __ldg(cp + 2 * rw + 2), __ldg(cp + rw + 3),
-                            __ldg(cp + 3),       __ldg(cp - rw + 3),      __ldg(cp - 2 * rw + 2), __ldg(cp - 3 * rw + 1),
-                            __ldg(cp - 3 * rw),  __ldg(cp - 3 * rw - 1),  __ldg(cp - 2 * rw - 2), __ldg(cp - rw - 3),
-                            __ldg(cp - 3),       __ldg(cp + rw - 3),      __ldg(cp + 2 * rw - 2), __ldg(cp + 3 * rw - 1)};
-    uint32_t a[16], m2[16], m4[16];
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-        const uint32_t x = p[k] | (v << 16), y = v | (p[k] << 16);
-        a[k] = __vmaxu2(x, y) - x;  // (v - p)+ | (p - v)+ << 16
-    }
-#pragma unroll
-    for (int k = 0; k < 16; k++) m2[k] = __vminu2(a[k], a[(k + 1) & 15]);
-#pragma unroll
-    for (int k = 0; k < 16; k++) m4[k] = __vminu2(m2[k], m2[(k + 2) & 15]);
-    uint32_t best = 0;
-#pragma unroll
-    for (int k = 0; k < 16; k++) best = __vmaxu2(best, __vminu2(__vminu2(m4[k], m4[(k + 4) & 15]), a[(k + 8) & 15]));
-    return (int)max(best & 0xFFFFu, best >> 16);
-}
-
-// The arc strength of every FAST candidate listed by the strips of
-// descs[desc0 + k * stride], k < ndesc; a candidate above the lower threshold is a corner and is
-// appended to the list of the cell whose detection region holds it (cell
-// column (x - 19) / wCell, row (y - 19) / hCell: the regions tile
-// [19, w - 19) x [19, h - 19) without overlap).  Each block takes a contiguous
-// range of the concatenated lists (consecutive threads, consecutive
-// candidates: neighbouring pixels of one level, so the circle loads share
-// cache lines) and rebuilds the lists' prefix in shared memory; a thread
-// reloads the level's fields only when its candidates cross into the next
-// level.
-__global__ void __launch_bounds__(256) k_fast_score(const LevelDesc* __restrict__ descs, int desc0, int stride,
-                                                    int ndesc) {
-    extern __shared__ int s_pre[];  // ndesc + 1 prefix entries, then 32 scan words
-    int* s_scan = s_pre + ndesc + 1;
-    descs += desc0;
-    int carry = 0;
-    for (int b0 = 0; b0 < ndesc; b0 += blockDim.x) {
-        const int k = b0 + threadIdx.x;
-        const int c = k < ndesc ? min(*descs[(size_t)k * stride].fcand_count, descs[(size_t)k * stride].fcand_cap) : 0;
-        int tot;
-        const int ex = block_exclusive_scan(c, s_scan, &tot);
-        if (k < ndesc) s_pre[k] = carry + ex;
-        carry += tot;
-    }
-    if (threadIdx.x == 0) s_pre[ndesc] = carry;
-    __syncthreads();
-    const int total = s_pre[ndesc];
-    const int per = (total + gridDim.x - 1) / gridDim.x;
-    const int i0 = blockIdx.x * per, i1 = min(total, i0 + per);
-    const int B = blockDim.x;
-    int dsc = -1, lo = 0, hi = 0;
-    const uint32_t* fcand = nullptr;
-    const uint8_t* lvl = nullptr;
-    uint32_t* corners = nullptr;
-    int* ccount = nullptr;
-    int pitch = 0, t = 0, ncols = 0, wcell = 1, hcell = 1, ccap = 0;
-    auto resolve = [&](int i) {  // the last list starting at or before i
-        int a = dsc < 0 ? 0 : dsc, b = ndesc - 1;
-        while (a < b) {
-            const int mid = (a + b + 1) >> 1;
-            if (s_pre[mid] <= i) a = mid;
-            else b = mid - 1;
-        }
-        dsc = a;
-        lo = s_pre[dsc];
-        hi = s_pre[dsc + 1];
-        const LevelDesc& d = descs[(size_t)dsc * stride];
-        fcand = d.fcand;
-        lvl = d.dst;
-        pitch = d.pitch;
-        t = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
-        corners = d.corners;
-        ccount = d.corner_count;
-        ncols = d.nCols;
-        wcell = max(d.wCell, 1);
-        hcell = max(d.hCell, 1);
-        ccap = d.corner_cap;
-    };
-    auto append = [&](uint32_t e, int sc) {
-        if (sc > t && ncols > 0) {
-            const int rx = (int)(e & 0xFFFFu) - ORBGPU_EDGE_THRESHOLD, ry = (int)(e >> 16) - ORBGPU_EDGE_THRESHOLD;
-            const int cj = rx / wcell, ci = ry / hcell;
-            const int cell = ci * ncols + cj;
-            const int pos = atomicAdd(ccount + cell, 1);
-            if (pos < ccap)
-                corners[(size_t)cell * ccap + pos] =
-                    ((uint32_t)(ry - ci * hcell) << 16) | ((uint32_t)(rx - cj * wcell) << 8) | (uint32_t)sc;
-        }
-    };
-    // four candidates per thread and pass: their circle loads are in flight
-    // together (the strength computation is latency-bound on them)
-    for (int i = i0 + threadIdx.x; i < i1; i += 4 * B) {
-        if (i >= hi) resolve(i);
-        if (i + 3 * B < min(i1, hi)) {
-            uint32_t e[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) e[k] = __ldg(fcand + (i + k * B - lo));
-            int sc[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                sc[k] = level_arc_strength(lvl + (size_t)(e[k] >> 16) * pitch + (e[k] & 0xFFFFu), pitch);
-#pragma unroll
-            for (int k = 0; k < 4; k++) append(e[k], sc[k]);
-        } else {
-            for (int k = 0; k < 4 && i + k * B < i1; k++) {
-                const int j = i + k * B;
-                if (j >= hi) resolve(j);
-                const uint32_t e = __ldg(fcand + (j - lo));
-                append(e, level_arc_strength(lvl + (size_t)(e >> 16) * pitch + (e & 0xFFFFu), pitch));
-            }
-        }
-    }
 }
 
 template <int TH>
@@ -474,9 +354,10 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
     // otherwise alias them and force reloads
     const uint8_t* const lvl = d.dst;
     uint8_t* const blur = d.blur;
-    uint32_t* const fcand = d.fcand;
-    int* const fcand_count = d.fcand_count;
-    const int fcand_cap = d.fcand_cap;
+    // candidate bytes: the odd writer lane of a pair stores columns X .. X + 7
+    const bool cwriter = writer && (lane & 1);
+    uint8_t* const cbits = d.cbits + (cwriter ? X >> 3 : 0);
+    const int cstride = d.cbits_stride;
     auto level_word = [&](int rr) -> uint32_t {
         const uint8_t* row = lvl + (size_t)rr * pitch;
         if (interior) return *reinterpret_cast<const uint32_t*>(row + X);
@@ -491,7 +372,6 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
 #pragma unroll
     for (int u = 0; u < 7; u++) q[u] = level_word(S.rows[u]);
     for (int blk = 0; blk < NB; blk++) {
-        uint32_t bmw = 0;  // candidates of this block: bit 4u + j
 #pragma unroll
         for (int u = 0; u < 7; u++) {
             const int i = 7 * blk + u;
@@ -537,28 +417,11 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
                         const uint32_t O =
                             rs_compass(rs_odd(cm), rs_odd(cw[u]), rs_odd(p4), rs_odd(cw[up]), rs_odd(p12), K);
                         const uint32_t m = (E >> 15) | (O >> 14);  // pixels 0, 1 at bits 0, 1; 2, 3 at bits 16, 17
-                        bmw |= ((m | (m >> 14)) & colmask & 0xFu) << (4 * u);
+                        const uint32_t nib = (m | (m >> 14)) & colmask & 0xFu;
+                        const uint32_t nib_next = __shfl_down_sync(0xffffffffu, nib, 1);
+                        if (cwriter) cbits[(size_t)y * cstride] = (uint8_t)(nib | (nib_next << 4));
                     }
                 }
-            }
-        }
-        // append this block's candidates to the level's list: one atomic per warp
-        if (__any_sync(0xffffffffu, bmw != 0)) {
-            const int cnt = __popc(bmw);
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int n = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += n;
-            }
-            int base = 0;
-            if (lane == 31) base = atomicAdd(fcand_count, incl);
-            int pos = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
-            const uint32_t yb = (uint32_t)(y0 + 7 * blk - 6);  // level row of bit group 0
-            for (uint32_t m = bmw; m; m &= m - 1) {
-                const int b = __ffs(m) - 1;
-                if (pos < fcand_cap) fcand[pos] = ((yb + (uint32_t)(b >> 2)) << 16) | (uint32_t)(X + (b & 3));
-                pos++;
             }
         }
     }
@@ -567,138 +430,376 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
 #define FAST_MAX_ROI 72
 #define FAST_MAX_DET (FAST_MAX_ROI - 6)
 #define FAST_ROW 80                 // staged row: 20 words
+#define FAST_CHUNK 4                // consecutive cells a warp takes at a time
 
-// The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142)
-// on the cell's corner list: one warp per cell.  FAST's per-ROI 3x3 suppression
-// keeps pixel p at threshold th when its score beats every neighbour's score
-// (a neighbour that is not a corner at th, or lies outside the ROI's
-// detection region, scores 0).  On the arc strength m (score + 1) that is
-// m > th' and m > m(q) for the 8 neighbours q (0 outside the region), with
-// th' = max(th, 1) unless the region is a single pixel: a neighbour at or
-// below th is below m already, and a pixel of score 0 (m = 1) loses to any
-// neighbour.  The neighbour test does not depend on th, so one pass over the
-// region yields the survivors at iniThFAST and at minThFAST; the latter are
-// used when the former are none.  The region is rebuilt in shared memory with
-// a zero ring (cleared, then the cell's corners scattered into it); each lane
-// then tests its corners against their 8 neighbours there, and the survivors
-// are written in the detector's row-major order (ranked by row and column).
-// CPB (cells per block, 1 / 2 / 4) is chosen by the autotuner.
-template <int CPB>
-__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int* status,
-                                                          FastCellsSmem sm) {
-    WorkItem it;
-    map_item(rm, blockIdx.x, it.desc, it.index);
-    const LevelDesc& d = descs[it.desc];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int cell = it.index * CPB + warp;
-    if (cell >= d.nCols * d.nRows) return;
-    // per warp: the region rows (sm.rows of FAST_ROW bytes), then the
-    // minThFAST and the iniThFAST survivors (sm.min_cap keys each)
-    extern __shared__ __align__(16) uint8_t s_dyn[];
-    uint8_t* mstr = s_dyn + (size_t)warp * sm.warp_bytes;
-    uint16_t* smin = reinterpret_cast<uint16_t*>(mstr + sm.rows * FAST_ROW);
-    const int i = cell / d.nCols, j = cell - (cell / d.nCols) * d.nCols;
-    const int minB = ORBGPU_EDGE_THRESHOLD - 3;
-    const int iniY = minB + i * d.hCell, iniX = minB + j * d.wCell;
-    int maxY = iniY + d.hCell + 6, maxX = iniX + d.wCell + 6;
-    const bool skip = (iniY >= d.maxBorderY - 3) || (iniX >= d.maxBorderX - 6);
-    if (maxY > d.maxBorderY) maxY = d.maxBorderY;
-    if (maxX > d.maxBorderX) maxX = d.maxBorderX;
-    const int rw = maxX - iniX, rh = maxY - iniY;
-    if (skip || rw < 7 || rh < 7 || rw > FAST_MAX_ROI || rh > FAST_MAX_ROI || rh - 4 > sm.rows) {
-        if (lane == 0) {
-            d.cell_count[cell] = 0;
-            if (!skip && (rw > FAST_MAX_ROI || rh > FAST_MAX_ROI || rh - 4 > sm.rows)) atomicOr(status, 1);
-        }
-        return;
+// Largest arc threshold of the pixel at cp (row pitch rw, a shared-memory
+// tile): max over the sixteen nine-pixel arcs of the arc's smallest
+// difference, for the darker-centre (v - p) and brighter-centre (p - v)
+// differences clipped at 0, which travel together in the 16-bit halves of one
+// word.  Above t exactly when the pixel is a FAST corner at threshold t.
+__device__ __forceinline__ int tile_arc_strength(const uint8_t* cp, int rw) {
+    const uint32_t v = cp[0];
+    const uint32_t p[16] = {cp[3 * rw],  cp[3 * rw + 1],  cp[2 * rw + 2],  cp[rw + 3],  cp[3],      cp[-rw + 3],
+                            cp[-2 * rw + 2], cp[-3 * rw + 1], cp[-3 * rw], cp[-3 * rw - 1], cp[-2 * rw - 2],
+                            cp[-rw - 3], cp[-3],          cp[rw - 3],      cp[2 * rw - 2], cp[3 * rw - 1]};
+    uint32_t a[16], m2[16], m4[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const uint32_t x = p[k] | (v << 16), y = v | (p[k] << 16);
+        a[k] = __vmaxu2(x, y) - x;  // (v - p)+ | (p - v)+ << 16
     }
-    const int dw = rw - 6, dh = rh - 6;
-    const int gx0 = iniX + 3, gy0 = iniY + 3;  // level coordinates of region pixel (0, 0)
-    // staged row: byte b <-> region column b - 4; words 1..nwr hold region
-    // bytes; everything else stays zero (the ring)
-    const int off = 0;
-    {
-        uint4* m16 = reinterpret_cast<uint4*>(mstr);
-        for (int k = lane; k < (dh + 2) * (FAST_ROW / 16); k += 32) m16[k] = make_uint4(0u, 0u, 0u, 0u);
-        __syncwarp();
-        // the cell's corners (arc strengths at the lower threshold), in any order
-        const int nc = min(d.corner_count[cell], d.corner_cap);
-        const uint32_t* cl = d.corners + (size_t)cell * d.corner_cap;
-        for (int k = lane; k < nc; k += 32) {
-            const uint32_t e = cl[k];
-            const int r = (int)(e >> 16), c = (int)((e >> 8) & 0xFFu);
-            if (r < dh && c < dw) mstr[(r + 1) * FAST_ROW + c + off + 4] = (uint8_t)(e & 0xFFu);
-        }
+#pragma unroll
+    for (int k = 0; k < 16; k++) m2[k] = __vminu2(a[k], a[(k + 1) & 15]);
+#pragma unroll
+    for (int k = 0; k < 16; k++) m4[k] = __vminu2(m2[k], m2[(k + 2) & 15]);
+    uint32_t best = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) best = __vmaxu2(best, __vminu2(__vminu2(m4[k], m4[(k + 4) & 15]), a[(k + 8) & 15]));
+    return (int)max(best & 0xFFFFu, best >> 16);
+}
+
+// FAST-9 segment test of the pixel at cp (row pitch rw, a shared-memory
+// tile) at the threshold of K = (0x8000 - t - 1) in both 16-bit lanes: nine
+// contiguous circle points brighter than v + t or darker than v - t.  Circle
+// points k and k + 8 share a word; as in the compass test no borrow crosses
+// the lanes and bit 15 / 31 of P + K - C is p - v > t (of C + K - P,
+// v - p > t).  Equivalent to tile_arc_strength(cp, rw) > t.
+__device__ __forceinline__ bool tile_is_corner(const uint8_t* cp, int rw, uint32_t K) {
+    const uint32_t v = cp[0];
+    const uint32_t C = v * 0x00010001u;
+    const uint32_t P[8] = {(uint32_t)cp[3 * rw] | ((uint32_t)cp[-3 * rw] << 16),
+                           (uint32_t)cp[3 * rw + 1] | ((uint32_t)cp[-3 * rw - 1] << 16),
+                           (uint32_t)cp[2 * rw + 2] | ((uint32_t)cp[-2 * rw - 2] << 16),
+                           (uint32_t)cp[rw + 3] | ((uint32_t)cp[-rw - 3] << 16),
+                           (uint32_t)cp[3] | ((uint32_t)cp[-3] << 16),
+                           (uint32_t)cp[-rw + 3] | ((uint32_t)cp[rw - 3] << 16),
+                           (uint32_t)cp[-2 * rw + 2] | ((uint32_t)cp[2 * rw - 2] << 16),
+                           (uint32_t)cp[-3 * rw + 1] | ((uint32_t)cp[3 * rw - 1] << 16)};
+    uint32_t br = 0, dk = 0;  // bit k: point k (k < 8) at bit k, point k + 8 at bit 16 + k
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        br |= ((P[k] + K - C) & 0x80008000u) >> (15 - k);
+        dk |= ((C + K - P[k]) & 0x80008000u) >> (15 - k);
+    }
+    br = (br & 0xFFu) | ((br >> 8) & 0xFF00u);
+    dk = (dk & 0xFFu) | ((dk >> 8) & 0xFF00u);
+    return has_run9(br) || has_run9(dk);
+}
+
+// The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142).
+// A persistent kernel: each warp takes chunks of FAST_CHUNK consecutive
+// cells of the launch (work item u = a cell of one (frame, level)), the
+// chunks dealt round-robin over the warps, and per cell
+//   1. lane 0 copies the cell's ROI (the detection region and its 3-pixel
+//      ring) into shared memory with one tensor copy (box cell_box_w x
+//      (hCell + 6) from column iniX rounded down to 16), issued as soon as
+//      the previous cell's scoring is done with the tile (the tensor map is
+//      fenced when the level changes); meanwhile the warp clears the
+//      strength window and lists the region's candidates from the strips'
+//      bit map (one region row per lane, the words loaded a cell ahead, bits
+//      funnel-shifted to the region's first column);
+//   2. the FAST-9 segment test at the lower threshold keeps the candidates
+//      that are corners (about one in eight), and the corners' arc strengths
+//      (score + 1) from the tile go to the window;
+//   3. suppression: FAST's per-ROI 3x3 suppression keeps pixel p at
+//      threshold th when its score beats every neighbour's (a neighbour that
+//      is not a corner at th, or lies outside the ROI's detection region,
+//      scores 0).  On the arc strength m that is m > th' and m > m(q) for the
+//      8 neighbours q (0 outside the region), with th' = max(th, 1) unless
+//      the region is a single pixel: a neighbour at or below th is below m
+//      already, and a pixel of score 0 (m = 1) loses to any neighbour.  The
+//      neighbour test does not depend on th, so one pass over the corners
+//      yields the survivors at iniThFAST and at minThFAST; the latter are
+//      used when the former are none;
+//   4. the survivors are written in the detector's row-major order (ranked
+//      by row and column).
+// CPB (warps per block, 1 / 2 / 4) is chosen by the autotuner.  A copy that
+// does not arrive within the bounded wait sets status bit 128 and ends the
+// warp once the copies in flight are drained.
+struct FastCellGeom {
+    const LevelDesc* d;
+    int cell, iniX, iniY, rw, rh;
+    bool ok;   // the cell is scanned
+    bool bad;  // the cell exceeds the launch's shared memory (status bit 1)
+};
+template <int CPB>
+__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int total, int* status,
+                                                          FastCellsSmem sm) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // per warp (sm.warp_bytes, 128-byte aligned): the ROI tile, the strength
+    // window (sm.rows of FAST_ROW bytes), the candidate list (sm.cand_cap
+    // keys), the minThFAST and the iniThFAST survivors (sm.min_cap keys each)
+    extern __shared__ __align__(128) uint8_t s_dyn[];
+    __shared__ uint64_t s_bar[CPB];
+    const uint32_t dyn0 = smem_u32(s_dyn);
+    uint8_t* const tile = s_dyn + (((dyn0 + 127u) & ~127u) - dyn0) + (size_t)warp * sm.warp_bytes;
+    uint8_t* const mstr = tile + sm.tile_bytes;
+    uint16_t* const cand = reinterpret_cast<uint16_t*>(mstr + sm.rows * FAST_ROW);
+    uint16_t* const smin = cand + sm.cand_cap;
+    uint16_t* const sini = smin + sm.min_cap;
+    uint64_t* const bar = &s_bar[warp];
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        mbar_init_fence();
     }
     __syncwarp();
-    const int single = dw * dh == 1;
-    int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
-    if (!single) {
-        ini_th = max(ini_th, 1);
-        min_th = max(min_th, 1);
+    // work: chunks of FAST_CHUNK consecutive cells (one level, mostly: the
+    // tensor map is fenced once per chunk), chunk c to warp c mod nw, so that
+    // the textured parts of an image spread over the warps
+    const int nw = gridDim.x * CPB, gw = blockIdx.x * CPB + warp;
+    auto next_cell = [&](int u) {  // the warp's cell after u
+        return (u + 1) % FAST_CHUNK != 0 ? u + 1 : u + 1 + (nw - 1) * FAST_CHUNK;
+    };
+    const int minB = ORBGPU_EDGE_THRESHOLD - 3;
+    int ent = -1, ent_lo = 0, ent_hi = 0;  // the entry of the last cell: items [ent_lo, ent_hi)
+    auto geom = [&](int u, FastCellGeom& G) {
+        if (u < ent_lo || u >= ent_hi) {  // the last entry starting at or before u (prefix has n + 1 entries)
+            int lo = ent < 0 ? 0 : ent, hi = rm.n - 1;
+            if (u < ent_lo) lo = 0;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (rm.prefix[mid] <= u) lo = mid;
+                else hi = mid - 1;
+            }
+            ent = lo;
+            ent_lo = rm.prefix[lo];
+            ent_hi = rm.prefix[lo + 1];
+        }
+        const int c = u - ent_lo;
+        const LevelDesc& d = descs[rm.desc0 + ent * rm.desc_stride];
+        G.d = &d;
+        G.cell = c;
+        const int i = c / d.nCols, j = c - i * d.nCols;
+        G.iniY = minB + i * d.hCell;
+        G.iniX = minB + j * d.wCell;
+        int maxY = G.iniY + d.hCell + 6, maxX = G.iniX + d.wCell + 6;
+        const bool skip = (G.iniY >= d.maxBorderY - 3) || (G.iniX >= d.maxBorderX - 6);
+        if (maxY > d.maxBorderY) maxY = d.maxBorderY;
+        if (maxX > d.maxBorderX) maxX = d.maxBorderX;
+        G.rw = maxX - G.iniX;
+        G.rh = maxY - G.iniY;
+        const int bw = d.cell_box_w, bh = d.hCell + 6;
+        G.ok = !skip && G.rw >= 7 && G.rh >= 7;
+        G.bad = G.ok && (G.rw > FAST_MAX_ROI || G.rh > FAST_MAX_ROI || G.rh - 4 > sm.rows ||
+                         (G.rw - 6) * (G.rh - 6) > sm.cand_cap || bw * bh > sm.tile_bytes ||
+                         (G.iniX & 15) + G.rw > bw || G.rh > bh);
+        G.ok = G.ok && !G.bad;
+    };
+    const void* fenced = nullptr;  // lane 0: the tensor map it last acquired
+    auto prefetch = [&](const FastCellGeom& G) {
+        if (lane == 0 && G.ok) {
+            const LevelDesc& d = *G.d;
+            if (d.tm_cell != fenced) {
+                tensormap_acquire(d.tm_cell);
+                fenced = d.tm_cell;
+            }
+            mbar_expect_tx(bar, (uint32_t)(d.cell_box_w * (d.hCell + 6)));
+            tma_load_2d(tile, d.tm_cell, G.iniX & ~15, G.iniY, bar);
+        }
+    };
+    // the bit-map words of region row 'lane' of a cell (rows 32 and up are
+    // read when the cell is processed: regions that high are rare); the
+    // map's rows are 8-byte aligned and a row's last words run into the
+    // next row, which exists (region rows end 19 rows above h)
+    auto load_bits = [&](const FastCellGeom& G, uint32_t (&w)[4]) {
+        w[0] = w[1] = w[2] = w[3] = 0u;
+        if (G.ok && lane < G.rh - 6) {
+            const LevelDesc& d = *G.d;
+            const uint32_t* wr =
+                reinterpret_cast<const uint32_t*>(d.cbits + (size_t)(G.iniY + 3 + lane) * d.cbits_stride) +
+                ((G.iniX + 3) >> 5);
+            w[0] = wr[0];
+            w[1] = wr[1];
+            w[2] = wr[2];
+            if (G.rw - 6 > 64) w[3] = wr[3];
+        }
+    };
+    uint32_t par = 0;  // the phase parity the tile's barrier waits for next
+    FastCellGeom cur, nxt;
+    uint32_t wcur[4], wnxt[4];
+    const int u0 = gw * FAST_CHUNK;
+    if (u0 < total) {
+        geom(u0, cur);
+        prefetch(cur);
+        load_bits(cur, wcur);
     }
-    const int cell_cap = d.cell_cap;
-    uint32_t* const out = d.slots + (size_t)cell * cell_cap;
-    // the survivors at both thresholds, as row-major keys (row << 8 | column)
-    // in two lists of sm.min_cap entries each
-    uint16_t* const sini = smin + sm.min_cap;
-    int total_ini = 0, total_min = 0;
-    {
-        const int nc = min(d.corner_count[cell], d.corner_cap);
-        const uint32_t* cl = d.corners + (size_t)cell * d.corner_cap;
-        const unsigned below = (1u << lane) - 1u;
-        for (int k0 = 0; k0 < nc; k0 += 32) {
-            const int k = k0 + lane;
-            bool oi = false, om = false;
-            int key = 0;
-            if (k < nc) {
-                const uint32_t e = cl[k];
-                const int r = (int)(e >> 16), c = (int)((e >> 8) & 0xFFu), m = (int)(e & 0xFFu);
-                if (r < dh && c < dw) {
-                    const uint8_t* q = mstr + (r + 1) * FAST_ROW + c + off + 4;
-                    int nb = max(max(q[-1], q[1]), max(max(q[-FAST_ROW - 1], q[-FAST_ROW]), q[-FAST_ROW + 1]));
-                    nb = max(nb, max(max(q[FAST_ROW - 1], q[FAST_ROW]), q[FAST_ROW + 1]));
-                    if (m > nb) {
-                        oi = m > ini_th;
-                        om = m > min_th;
+    for (int u = u0; u < total; u = next_cell(u)) {
+        const int un = next_cell(u);
+        const bool more = un < total;
+        if (more) {
+            geom(un, nxt);
+            load_bits(nxt, wnxt);  // in flight while this cell is processed
+        }
+        const LevelDesc& d = *cur.d;
+        const int cell = cur.cell;
+        if (!cur.ok) {
+            if (lane == 0) {
+                d.cell_count[cell] = 0;
+                if (cur.bad) atomicOr(status, 1);
+            }
+            if (more) prefetch(nxt);
+        } else {
+            const int dw = cur.rw - 6, dh = cur.rh - 6, bw = d.cell_box_w;
+            const int gx0 = cur.iniX + 3, gy0 = cur.iniY + 3;  // level coordinates of region pixel (0, 0)
+            // the strength window: byte b of a row <-> region column b - 4,
+            // rows 0 and dh + 1 and everything outside the region stay zero
+            {
+                uint4* m16 = reinterpret_cast<uint4*>(mstr);
+                for (int q = lane; q < (dh + 2) * (FAST_ROW / 16); q += 32) m16[q] = make_uint4(0u, 0u, 0u, 0u);
+            }
+            // the region's candidates, one row per lane (bits of columns gx0
+            // .. gx0 + dw - 1, funnel-shifted from the map's words)
+            int ncand;
+            {
+                const int k0 = gx0 >> 5, sh = gx0 & 31;
+                uint32_t m[3][3];  // [row slot][32-column group]
+                int cnt = 0;
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    const int r = lane + 32 * q;
+                    m[q][0] = m[q][1] = m[q][2] = 0u;
+                    if (r < dh) {
+                        uint32_t w0 = wcur[0], w1 = wcur[1], w2 = wcur[2], w3 = wcur[3];
+                        if (q > 0) {
+                            const uint32_t* wr =
+                                reinterpret_cast<const uint32_t*>(d.cbits + (size_t)(gy0 + r) * d.cbits_stride) + k0;
+                            w0 = wr[0];
+                            w1 = wr[1];
+                            w2 = wr[2];
+                            w3 = dw > 64 ? wr[3] : 0u;
+                        }
+                        m[q][0] = __funnelshift_r(w0, w1, sh);
+                        m[q][1] = __funnelshift_r(w1, w2, sh);
+                        m[q][2] = __funnelshift_r(w2, w3, sh);
+#pragma unroll
+                        for (int g = 0; g < 3; g++) {
+                            const int valid = min(max(dw - 32 * g, 0), 32);
+                            if (valid < 32) m[q][g] &= (1u << valid) - 1u;
+                            cnt += __popc(m[q][g]);
+                        }
                     }
-                    key = (r << 8) | c;
+                }
+                int incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int n = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += n;
+                }
+                ncand = __shfl_sync(0xffffffffu, incl, 31);
+                int pos = incl - cnt;
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+#pragma unroll
+                    for (int g = 0; g < 3; g++)
+                        for (uint32_t bits = m[q][g]; bits; bits &= bits - 1)
+                            cand[pos++] = (uint16_t)(((lane + 32 * q) << 8) | (32 * g + __ffs(bits) - 1));
+            }
+            __syncwarp();  // the cleared window and the candidate list are the warp's
+            if (!__all_sync(0xffffffffu, mbar_wait(bar, par))) {
+                mbar_wait(bar, par);  // the copy gets one more bounded wait before the warp leaves
+                if (lane == 0) {
+                    atomicOr(status, 128);
+                    d.cell_count[cell] = 0;
+                }
+                return;
+            }
+            par ^= 1u;
+            // the candidates that are corners at the lower threshold, by the
+            // segment test, compacted in place (a corner's slot is never
+            // above its candidate's: the list is read before it is written),
+            // then their arc strengths into the window
+            const int tl = min(min(max(d.ini_th, 0), 255), min(max(d.min_th, 0), 255));
+            const uint32_t K = (0x8000u - (uint32_t)tl - 1u) * 0x00010001u;
+            const uint8_t* const org = tile + 3 * bw + (cur.iniX & 15) + 3;  // region pixel (0, 0)
+            const unsigned below = (1u << lane) - 1u;
+            int ncorner = 0;
+            for (int q0 = 0; q0 < ncand; q0 += 32) {
+                const int q = q0 + lane;
+                int key = 0;
+                bool corner = false;
+                if (q < ncand) {
+                    key = cand[q];
+                    corner = tile_is_corner(org + (key >> 8) * bw + (key & 255), bw, K);
+                }
+                const unsigned bc = __ballot_sync(0xffffffffu, corner);
+                if (corner) cand[ncorner + __popc(bc & below)] = (uint16_t)key;
+                ncorner += __popc(bc);
+            }
+            __syncwarp();
+            for (int q = lane; q < ncorner; q += 32) {
+                const int key = cand[q];
+                const int r = key >> 8, c = key & 255;
+                mstr[(r + 1) * FAST_ROW + c + 4] = (uint8_t)tile_arc_strength(org + r * bw + c, bw);
+            }
+            __syncwarp();  // the tile is read: the next cell's copy may land
+            if (more) prefetch(nxt);
+            const int single = dw * dh == 1;
+            int ini_th = min(max(d.ini_th, 0), 255), min_th = min(max(d.min_th, 0), 255);
+            if (!single) {
+                ini_th = max(ini_th, 1);
+                min_th = max(min_th, 1);
+            }
+            const int cell_cap = d.cell_cap;
+            uint32_t* const out = d.slots + (size_t)cell * cell_cap;
+            // the survivors at both thresholds, as row-major keys (row << 8 | column)
+            int total_ini = 0, total_min = 0;
+            {
+                for (int q0 = 0; q0 < ncorner; q0 += 32) {
+                    const int q = q0 + lane;
+                    bool oi = false, om = false;
+                    int key = 0;
+                    if (q < ncorner) {
+                        key = cand[q];
+                        const int r = key >> 8, c = key & 255;
+                        const uint8_t* p = mstr + (r + 1) * FAST_ROW + c + 4;
+                        const int m = p[0];
+                        int nb = max(max(p[-1], p[1]), max(max(p[-FAST_ROW - 1], p[-FAST_ROW]), p[-FAST_ROW + 1]));
+                        nb = max(nb, max(max(p[FAST_ROW - 1], p[FAST_ROW]), p[FAST_ROW + 1]));
+                        if (m > nb) {
+                            oi = m > ini_th;
+                            om = m > min_th;
+                        }
+                    }
+                    const unsigned bi = __ballot_sync(0xffffffffu, oi), bm = __ballot_sync(0xffffffffu, om);
+                    if (oi) {
+                        const int pos = total_ini + __popc(bi & below);
+                        if (pos < sm.min_cap) sini[pos] = (uint16_t)key;
+                    }
+                    if (om) {
+                        const int pos = total_min + __popc(bm & below);
+                        if (pos < sm.min_cap) smin[pos] = (uint16_t)key;
+                    }
+                    total_ini += __popc(bi);
+                    total_min += __popc(bm);
                 }
             }
-            const unsigned bi = __ballot_sync(0xffffffffu, oi), bm = __ballot_sync(0xffffffffu, om);
-            if (oi) {
-                const int pos = total_ini + __popc(bi & below);
-                if (pos < sm.min_cap) sini[pos] = (uint16_t)key;
+            __syncwarp();
+            // iniThFAST's survivors if there are any, else minThFAST's, in the
+            // detector's row-major order: a survivor's output row is the
+            // number of smaller keys (keys are distinct)
+            const bool use_ini = total_ini > 0;
+            const uint16_t* L = use_ini ? sini : smin;
+            const int tot = use_ini ? total_ini : total_min;
+            const int n = min(tot, sm.min_cap);
+            for (int q = lane; q < n; q += 32) {
+                const int key = L[q];
+                int rank = 0;
+                for (int t = 0; t < n; t++) rank += (int)L[t] < key;
+                if (rank < cell_cap) {
+                    const int r = key >> 8, c = key & 255;
+                    out[rank] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
+                                ((uint32_t)(mstr[(r + 1) * FAST_ROW + c + 4] - 1) << 24);
+                }
             }
-            if (om) {
-                const int pos = total_min + __popc(bm & below);
-                if (pos < sm.min_cap) smin[pos] = (uint16_t)key;
+            if (lane == 0) {
+                if (tot > cell_cap || tot > sm.min_cap) atomicOr(status, 2);
+                d.cell_count[cell] = min(n, cell_cap);
             }
-            total_ini += __popc(bi);
-            total_min += __popc(bm);
         }
-    }
-    __syncwarp();
-    // iniThFAST's survivors if there are any, else minThFAST's, in the
-    // detector's row-major order: a survivor's output row is the number of
-    // smaller keys (keys are distinct)
-    const bool use_ini = total_ini > 0;
-    const uint16_t* L = use_ini ? sini : smin;
-    const int total = use_ini ? total_ini : total_min;
-    const int n = min(total, sm.min_cap);
-    for (int q = lane; q < n; q += 32) {
-        const int key = L[q];
-        int rank = 0;
-        for (int t = 0; t < n; t++) rank += (int)L[t] < key;
-        if (rank < cell_cap) {
-            const int r = key >> 8, c = key & 255;
-            out[rank] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
-                        ((uint32_t)(mstr[(r + 1) * FAST_ROW + c + off + 4] - 1) << 24);
-        }
-    }
-    if (lane == 0) {
-        if (total > cell_cap || total > sm.min_cap) atomicOr(status, 2);
-        d.cell_count[cell] = min(n, cell_cap);
+        __syncwarp();  // this cell's window and lists are read
+        cur = nxt;
+#pragma unroll
+        for (int q = 0; q < 4; q++) wcur[q] = wnxt[q];
     }
 }
 
@@ -1394,32 +1495,36 @@ int resize_blur_tiles(int w, int h) {
     const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + th - 1) / th);
     return (strips + RS_WPB - 1) / RS_WPB;
 }
-void launch_fast_score(const LevelDesc* descs, int desc0, int stride, int ndesc, int blocks, cudaStream_t st) {
-    if (ndesc <= 0) return;
-    const size_t smem = sizeof(int) * ((size_t)ndesc + 1 + 32);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_fast_score, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_fast_score<<<std::max(1, blocks), 256, smem, st>>>(descs, desc0, stride, ndesc);
-}
-int fast_blocks(int ncells) {
-    const int cpb = tunables().fast_cells_per_block;
-    return (ncells + cpb - 1) / cpb;
-}
-void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, int max_wcell, int max_hcell,
-                 cudaStream_t st) {
-    if (nitems <= 0) return;
-    // shared memory for the launch's largest cell: its region rows plus the
-    // zero ring, and at most one survivor per 2 x 2 pixels
+void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, int max_wcell, int max_hcell,
+                 int max_box_bytes, cudaStream_t st) {
+    if (ncells <= 0 || max_box_bytes <= 0) return;
+    // shared memory for the launch's largest cell: its ROI box, its region
+    // rows plus the zero ring, a candidate per region pixel and at most one
+    // survivor per 2 x 2 pixels
     FastCellsSmem sm;
+    sm.tile_bytes = (max_box_bytes + 127) & ~127;
     sm.rows = std::min(FAST_MAX_DET, std::max(1, max_hcell)) + 2;
     const int mw = std::min(FAST_MAX_DET, std::max(1, max_wcell)), mh = sm.rows - 2;
+    sm.cand_cap = mw * mh;
     sm.min_cap = ((mw + 1) / 2) * ((mh + 1) / 2);
-    sm.warp_bytes = ((sm.rows * FAST_ROW + 4 * sm.min_cap) + 15) & ~15;
+    sm.warp_bytes = (sm.tile_bytes + sm.rows * FAST_ROW + 2 * sm.cand_cap + 4 * sm.min_cap + 127) & ~127;
     const int cpb = tunables().fast_cells_per_block;
-    const size_t smem = (size_t)cpb * sm.warp_bytes;
+    const size_t smem = (size_t)cpb * sm.warp_bytes + 128;
+    // persistent: as many blocks as fit on the device at once, each warp a
+    // contiguous run of cells
+    const int nsm = nsm_of_current_device();
+    auto run = [&](auto kernel) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * cpb, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        const int blocks = std::max(1, std::min((ncells + cpb - 1) / cpb, nsm * per_sm));
+        kernel<<<blocks, 32 * cpb, smem, st>>>(descs, rm, ncells, status, sm);
+    };
     switch (cpb) {
-        case 1: k_fast_cells<1><<<nitems, 32, smem, st>>>(descs, rm, status, sm); break;
-        case 2: k_fast_cells<2><<<nitems, 64, smem, st>>>(descs, rm, status, sm); break;
-        default: k_fast_cells<4><<<nitems, 128, smem, st>>>(descs, rm, status, sm); break;
+        case 1: run(k_fast_cells<1>); break;
+        case 2: run(k_fast_cells<2>); break;
+        default: run(k_fast_cells<4>); break;
     }
 }
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {

@@ -7,17 +7,15 @@
 //                        11-bit fixed point).
 //   k_level_strip        the 7x7 sigma-2 blur of level l (REFLECT_101) and the
 //                        FAST compass pre-test of every pixel of the cells'
-//                        detection region (candidates appended to a list):
-//                        one warp per 120-column strip, rows walked with a
-//                        7-row register window.
-//   k_fast_score         the arc strength of every FAST candidate the strips
-//                        listed (one thread per candidate, all levels of all
-//                        frames in one launch); corners go to their cell's
-//                        list.
-//   k_fast_cells         one 30-px cell per warp: per-ROI non-max suppression
-//                        of the cell's corners at iniThFAST and minThFAST in
-//                        one pass (the latter used when the former keeps
-//                        nothing), ordered compaction.
+//                        detection region (a candidate bit map): one warp per
+//                        120-column strip, rows walked with a 7-row register
+//                        window.
+//   k_fast_cells         one 30-px cell per warp: the cell's ROI staged in
+//                        shared memory by a tensor copy, the arc strength of
+//                        the cell's candidates, per-ROI non-max suppression
+//                        at iniThFAST and minThFAST in one pass (the latter
+//                        used when the former keeps nothing), ordered
+//                        compaction.
 //   k_distribute         one (frame, level) per block: DistributeOctTree as a
 //                        sequence of parallel split steps over node creation
 //                        numbers.
@@ -63,19 +61,15 @@ struct LevelDesc {
     uint32_t* slots;  // nCols*nRows*cell_cap packed (x | y << 12 | score << 24), level coordinates
     int* cell_count;  // nCols*nRows
     int ini_th, min_th;
-    // FAST candidates (pixels that passed the compass pre-test) appended by
-    // k_level_strip and scored by k_fast_score: y << 16 | x, at most one per
-    // pixel of the detection region
-    uint32_t* fcand;
-    int* fcand_count;
-    int fcand_cap;
-    // FAST corners at the lower threshold per cell, appended by k_fast_score
-    // in any order: cell c owns corners[c * corner_cap ..], corner_count[c]
-    // entries of (row << 16 | column << 8 | arc strength) relative to the
-    // cell's detection region; corner_cap = wCell * hCell (every pixel once)
-    uint32_t* corners;
-    int* corner_count;
-    int corner_cap;
+    // FAST candidates (pixels that passed the compass pre-test), one bit per
+    // pixel: bit x & 7 of byte x >> 3 of row y, written by k_level_strip for
+    // the detection rows and columns [19, dim - 19), read by k_fast_cells
+    uint8_t* cbits;
+    int cbits_stride;  // bytes per row: pitch / 8
+    // tensor map of the level plane for k_fast_cells' copy of a cell's ROI:
+    // box cell_box_w x (hCell + 6) bytes from a 16-byte aligned column
+    const void* tm_cell;
+    int cell_box_w;
     // distribute
     int nfeat;
     int nIni;
@@ -157,18 +151,24 @@ void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, cudaSt
 void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
 // Shared memory layout of k_fast_cells for one launch (per warp).
 struct FastCellsSmem {
-    int rows;        // staged region rows: the largest detection region + 2
+    int tile_bytes;  // the largest ROI box of the launch, 128-byte multiple
+    int rows;        // strength window rows: the largest detection region + 2
+    int cand_cap;    // candidates: the largest detection region's pixels
     int min_cap;     // survivors kept per threshold
-    int warp_bytes;  // rows * FAST_ROW + 4 * min_cap (two survivor lists), 16-byte multiple
+    // tile_bytes + rows * FAST_ROW + 2 * cand_cap + 4 * min_cap (candidate
+    // list and two survivor lists), 128-byte multiple
+    int warp_bytes;
 };
-// max_wcell / max_hcell: the largest cell of the launch (sizes its shared memory).
-void launch_fast(const LevelDesc* descs, RangeMap rm, int nitems, int* status, int max_wcell, int max_hcell,
-                 cudaStream_t st);
-// Scores the FAST candidates of descs[desc0 + k * stride], k < ndesc (after
-// the strips of those levels) with 'blocks' blocks of 256 threads.
-void launch_fast_score(const LevelDesc* descs, int desc0, int stride, int ndesc, int blocks, cudaStream_t st);
+// The cell box width of a level (16-byte multiple covering the ROI from a
+// 16-byte aligned column).
+inline int fast_cell_box_w(int wcell) { return (15 + wcell + 6 + 15) & ~15; }
+// The FAST cells of a launch: rm maps work item u (0 <= u < ncells) to a
+// (frame, level) entry and a cell of it (the prefix counts cells);
+// max_wcell / max_hcell / max_box_bytes: the largest cell and ROI box of the
+// launch (they size its shared memory).
+void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, int max_wcell, int max_hcell,
+                 int max_box_bytes, cudaStream_t st);
 int resize_blur_tiles(int w, int h);
-int fast_blocks(int ncells);
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st);

@@ -30,25 +30,20 @@ struct LevelGeom {
     int nIni;
     int cell_cap, cand_cap, node_cap;
     int nfeat;
-    int fcand_cap;  // pixels of the cells' detection region [19, w - 19) x [19, h - 19)
 };
 
 struct LevelOffsets {
-    size_t pyr, blur, xofs, xalpha, yofs, ybeta, fcand, corners, slots, cell_count, cand, node_of, quad, nodes_a,
+    size_t pyr, blur, xofs, xalpha, yofs, ybeta, cbits, slots, cell_count, cand, node_of, quad, nodes_a,
         nodes_b, cnt4, childpos, aux0, aux1, aux2, best, kept;
 };
 
 // Byte offsets of one frame's buffers inside a device arena.
 struct FrameLayout {
     std::vector<LevelOffsets> lv;
-    size_t level_counts = 0, frame_total = 0, fcand_counts = 0;
-    // per-cell corner counters of every level, back to back (corner_first[l]
-    // is level l's first cell), ncells_total ints
-    size_t corner_counts = 0;
-    std::vector<int> corner_first;
-    int ncells_total = 0;
-    // two tensor maps per level (unblurred and blurred plane, 128 bytes
-    // each, level-major) for the descriptor kernel's patch copies
+    size_t level_counts = 0, frame_total = 0;
+    // three tensor maps per level (128 bytes each, level-major): the
+    // descriptor kernel's level and blurred patch boxes, the FAST cell
+    // kernel's ROI box
     size_t patch_maps = 0;
     size_t bytes = 0;
     size_t plan(const std::vector<LevelGeom>& g, size_t base);
@@ -63,9 +58,9 @@ int level_geometry(const ExtractorTables& t, int w, int h, std::vector<LevelGeom
 void fill_descs(const std::vector<LevelGeom>& g, const ExtractorTables& t, const FrameLayout& lay, uint8_t* arena,
                 int frame, int ini_th, int min_th, int out_base, int out_cap, LevelDesc* out);
 
-// Encodes the descriptor kernel's tensor maps of one frame (the layout's
-// patch_maps block: 2 x 128 bytes per level) for the arena slot at 'arena'
-// into 'out'; the caller copies them to arena + lay.patch_maps.
+// Encodes the tensor maps of one frame (the layout's patch_maps block: 3 x
+// 128 bytes per level) for the arena slot at 'arena' into 'out'; the caller
+// copies them to arena + lay.patch_maps.
 int encode_patch_maps(const std::vector<LevelGeom>& g, const FrameLayout& lay, uint8_t* arena,
                       std::vector<uint8_t>& out);
 
