@@ -186,6 +186,8 @@ int orbgpu_vocabulary_load_text(const char* path, orbgpu_vocabulary** out);
 int orbgpu_vocabulary_create(int k, int L, int scoring, int weighting, int nnodes, const int* parents,
                              const uint8_t* is_leaf, const uint8_t* descriptors, const double* weights,
                              orbgpu_vocabulary** out);
+/* Waits for all device work (transforms run on the callers' streams), then
+ * frees the tree. */
 int orbgpu_vocabulary_destroy(orbgpu_vocabulary* v);
 /* TemplatedVocabulary::size() (words) and the node count. */
 int orbgpu_vocabulary_size(const orbgpu_vocabulary* v, int* nwords, int* nnodes);

@@ -83,6 +83,8 @@ int orbgpu_batch_compute_stereo_matches(orbgpu_batch* b, const orbgpu_keypoint* 
  * memory. */
 typedef struct orbgpu_stream_state orbgpu_stream_state;
 int orbgpu_stream_state_create(int max_streams, int cap, orbgpu_stream_state** out);
+/* Waits for all device work (the calls run on the callers' streams), then
+ * frees the store. */
 int orbgpu_stream_state_destroy(orbgpu_stream_state* s);
 /* LastFrame rows of a batch: frame f's previous frame is slot slots[f]; its
  * offsets[f + 1] - offsets[f] rows (at most max_rows) are copied to

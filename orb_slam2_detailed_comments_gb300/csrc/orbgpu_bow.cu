@@ -589,6 +589,9 @@ extern "C" int orbgpu_vocabulary_load_text(const char* path, orbgpu_vocabulary**
 
 extern "C" int orbgpu_vocabulary_destroy(orbgpu_vocabulary* v) {
     if (!v) return ORBGPU_OK;
+    // transforms run on the caller's streams: all of them are done before the
+    // tree is freed
+    cudaDeviceSynchronize();
     cudaFree(v->child_desc);
     cudaFree(v->child_start);
     cudaFree(v->pos_node);

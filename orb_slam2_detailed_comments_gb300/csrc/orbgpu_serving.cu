@@ -125,6 +125,9 @@ extern "C" int orbgpu_stream_state_create(int max_streams, int cap, orbgpu_strea
 
 extern "C" int orbgpu_stream_state_destroy(orbgpu_stream_state* s) {
     if (!s) return ORBGPU_OK;
+    // gathers and updates run on the callers' streams: all of them are done
+    // before the store is freed
+    cudaDeviceSynchronize();
     cudaFree(s->kps);
     cudaFree(s->mps);
     cudaFree(s->desc);
