@@ -145,9 +145,11 @@ int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots,
 
 /* ------------------------------------------------------------ autotuner parameters */
 /* Launch shapes the autotuner chooses (orb_slam2_detailed_comments_gb300.autotune):
- *   "resize_rows"          strip rows of the resize / blur / FAST-strength kernel: 8, 22, 36, 64
- *   "fast_cells_per_block" FAST cells (one warp each) per block: 1, 2, 4
- *   "describe_group"       keypoints per warp of the descriptor kernel: 4, 8, 16, 32
+ *   "resize_rows"          strip rows of the resize and blur / FAST pre-test kernels: 8, 22, 36, 64
+ *   "fast_cells_per_block" warps per block of the FAST cell kernel: 1, 2, 4
+ *   "describe_group"       keypoints per staging round of the descriptor kernel: 1, 2, 4
+ *   "describe_depth"       staging rounds in flight per warp of the descriptor kernel: 2, 4
+ *                          (with describe_group 4, 2 is used)
  *   "knn_tc_min_pairs"     query x train size from which orbgpu_knn2(algo -1) uses tcgen05
  * Process-wide; a change makes extractors and batches re-plan (and re-capture
  * their graphs) on their next call.  Results do not depend on these values. */

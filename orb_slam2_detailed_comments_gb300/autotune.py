@@ -31,6 +31,7 @@ PARAMS = {
     "resize_rows": ((8, 22, 36, 64), "resize_blur"),
     "fast_cells_per_block": ((1, 2, 4), "fast"),
     "describe_group": ((1, 2, 4), "describe"),
+    "describe_depth": ((2, 4), "describe"),
 }
 KNN_PARAM = "knn_tc_min_pairs"
 

@@ -60,6 +60,7 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
         t.fast_cells_per_block = (int)value;
     else if (n == "describe_group" && (value == 1 || value == 2 || value == 4))
         t.describe_group = (int)value;
+    else if (n == "describe_depth" && (value == 2 || value == 4)) t.describe_depth = (int)value;
     else if (n == "knn_tc_min_pairs" && value >= 0) t.knn_tc_min_pairs = value;
     else {
         orbgpu_set_last_error("unknown tuning parameter or value", __FILE__, __LINE__);
@@ -76,6 +77,7 @@ extern "C" int orbgpu_tune_get(const char* name, long long* value) {
     if (n == "resize_rows") *value = t.resize_rows;
     else if (n == "fast_cells_per_block") *value = t.fast_cells_per_block;
     else if (n == "describe_group") *value = t.describe_group;
+    else if (n == "describe_depth") *value = t.describe_depth;
     else if (n == "knn_tc_min_pairs") *value = t.knn_tc_min_pairs;
     else return ORBGPU_ERR_BAD_ARG;
     return ORBGPU_OK;

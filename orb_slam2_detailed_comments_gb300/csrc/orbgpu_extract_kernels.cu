@@ -1162,8 +1162,8 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
 // Orientation and descriptor of the kept keypoints, 32 keypoints per warp
 // task (one per lane) and no block-level synchronisation after the prologue.
 // The task's patches are staged in shared memory by tensor copies in rounds
-// of R keypoints through two buffers of the warp, each with its mbarrier;
-// two rounds are in flight while one is computed:
+// of R keypoints through D buffers of the warp, each with its mbarrier; D
+// rounds are in flight while one is computed:
 //   pass A   the IC_Angle disc of each keypoint from the level plane
 //            (DESC_LBOX_*): moments with one lane per patch column;
 //   pass B   fastAtan2 and the double-precision rotation of all 32 keypoints
@@ -1175,8 +1175,9 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
 // Each block scans the levels' kept counts into shared memory (descriptors
 // are frame-major with levels ascending, so a level's offset inside its
 // frame is a difference of two prefix entries); keypoint g of the flattened
-// list finds its level by binary search.  R (1 / 2 / 4 keypoints per round,
-// with WPB = 12 / 6 / 3 warps per block) is chosen by the autotuner.  A copy
+// list finds its level by binary search.  R (1 / 2 / 4 keypoints per round)
+// and D (rounds in flight, 2 / 4; WPB = 24 / (R D) warps per block) are
+// chosen by the autotuner.  A copy
 // that does not complete within the bounded wait sets status bit 128 and
 // ends the warp once the copies in flight are drained.
 static_assert(ORBGPU_EDGE_THRESHOLD >= DESC_BBOX_R && ORBGPU_EDGE_THRESHOLD >= ORBGPU_HALF_PATCH,
@@ -1186,23 +1187,23 @@ static_assert(15 + 2 * ORBGPU_HALF_PATCH + 1 <= DESC_LBOX_W && 15 + DESC_BBOX_H 
 static_assert(DESC_LBOX_W * DESC_LBOX_H <= DESC_SLOT && DESC_BBOX_W * DESC_BBOX_H <= DESC_SLOT &&
                   DESC_SLOT % 128 == 0 && DESC_LBOX_W % 16 == 0 && DESC_BBOX_W % 16 == 0,
               "box slots");
-template <int R, int WPB>
+template <int R, int D, int WPB>
 __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
                                                        uint8_t* out_desc, int* status) {
     extern __shared__ __align__(128) uint8_t s_dyn[];  // boxes (128-byte aligned) | s_pre[ndescs + 1]
     __shared__ int s_scan[32];
     __shared__ float2 s_pat[16][32];   // lane l's pattern point 16 l + p at [p][l]
-    __shared__ uint64_t s_bar[2 * WPB];  // per warp: one per buffer
+    __shared__ uint64_t s_bar[D * WPB];  // per warp: one per buffer
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t dyn0 = smem_u32(s_dyn);
     uint8_t* boxes = s_dyn + (((dyn0 + 127u) & ~127u) - dyn0);
-    uint8_t* wbuf = boxes + (size_t)warp * 2 * R * DESC_SLOT;
-    int* s_pre = (int*)(boxes + (size_t)WPB * 2 * R * DESC_SLOT);
-    uint64_t* bar = &s_bar[2 * warp];
+    uint8_t* wbuf = boxes + (size_t)warp * D * R * DESC_SLOT;
+    int* s_pre = (int*)(boxes + (size_t)WPB * D * R * DESC_SLOT);
+    uint64_t* bar = &s_bar[D * warp];
     if (lane == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+#pragma unroll
+        for (int b = 0; b < D; b++) mbar_init(&bar[b], 1);
         mbar_init_fence();
     }
     for (int i = threadIdx.x; i < 512; i += blockDim.x) {
@@ -1282,9 +1283,9 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
             tensormap_acquire(tm_b);
         }
         // round i of a pass: the valid lanes of ranks [i R, i R + R) copy
-        // their box into slot rank - i R of buffer i & 1
+        // their box into slot rank - i R of buffer i mod D
         auto issue = [&](int i, bool blurred) {
-            const int b = i & 1;
+            const int b = i % D;
             if (lane == 0)
                 mbar_expect_tx(&bar[b], (uint32_t)min(R, nv - i * R) *
                                             (blurred ? DESC_BBOX_W * DESC_BBOX_H : DESC_LBOX_W * DESC_LBOX_H));
@@ -1296,15 +1297,14 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
             }
         };
         // bounded wait for round i; on a timeout the rounds still in flight
-        // (i and i + 1) get one more bounded wait each before the warp leaves
+        // (i .. i + D - 1) get one more bounded wait each before the warp leaves
         auto wait = [&](int i) -> bool {
-            const int b = i & 1;
+            const int b = i % D;
             if (__all_sync(FULL, mbar_wait(&bar[b], (par >> b) & 1u))) {
                 par ^= 1u << b;
                 return true;
             }
-            mbar_wait(&bar[b], (par >> b) & 1u);
-            if (i + 1 < nr) mbar_wait(&bar[b ^ 1], (par >> (b ^ 1)) & 1u);
+            for (int j = i; j < min(nr, i + D); j++) mbar_wait(&bar[j % D], (par >> (j % D)) & 1u);
             if (lane == 0) atomicOr(status, 128);
             return false;
         };
@@ -1312,12 +1312,11 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
         // staged discs, integer exact: per column u the sum s and the
         // row-weighted sum sv of the disc's pixels, m_10 = sum u s, m_01 = sum sv
         int my_m01 = 0, my_m10 = 0;
-        issue(0, false);
-        if (nr > 1) issue(1, false);
+        for (int i = 0; i < min(nr, D); i++) issue(i, false);
         unsigned rest = vmask;
         for (int i = 0; i < nr; i++) {
             if (!wait(i)) return;
-            const uint8_t* buf = wbuf + (i & 1) * R * DESC_SLOT;
+            const uint8_t* buf = wbuf + (i % D) * R * DESC_SLOT;
             for (int j = 0; j < R && rest; j++) {
                 const int k = __ffs(rest) - 1;
                 rest &= rest - 1;
@@ -1339,12 +1338,11 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
                     my_m01 = m01;
                 }
             }
-            __syncwarp();  // buffer i & 1 is read: round i + 2 may overwrite it
-            if (i + 2 < nr) issue(i + 2, false);
+            __syncwarp();  // buffer i mod D is read: round i + D may overwrite it
+            if (i + D < nr) issue(i + D, false);
         }
-        // the first two rounds of pass C travel during pass B
-        issue(0, true);
-        if (nr > 1) issue(1, true);
+        // the first D rounds of pass C travel during pass B
+        for (int i = 0; i < min(nr, D); i++) issue(i, true);
         // pass B: angle and rotation, one keypoint per lane
         float angle = 0.f, ca = 0.f, sb = 0.f;
         if (valid) {
@@ -1376,7 +1374,7 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
         rest = vmask;
         for (int i = 0; i < nr; i++) {
             if (!wait(i)) return;
-            const uint8_t* buf = wbuf + (i & 1) * R * DESC_SLOT;
+            const uint8_t* buf = wbuf + (i % D) * R * DESC_SLOT;
 #pragma unroll
             for (int j = 0; j < R; j += 2) {
                 if (!rest) break;
@@ -1420,7 +1418,7 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
                 if (kb >= 0) out_desc[(size_t)oB * 32 + lane] = (uint8_t)valB;
             }
             __syncwarp();
-            if (i + 2 < nr) issue(i + 2, true);
+            if (i + D < nr) issue(i + D, true);
         }
     }
 }
@@ -1536,23 +1534,25 @@ void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_ke
                      cudaStream_t st) {
     if (ndescs <= 0 || max_kept <= 0) return;
     const int nsm = nsm_of_current_device();
-    const int R = tunables().describe_group;
-    // 32-keypoint warp tasks; two buffers of R box slots per warp, 24 slots
+    const int R = tunables().describe_group, D = R * tunables().describe_depth > 8 ? 2 : tunables().describe_depth;
+    // 32-keypoint warp tasks; D buffers of R box slots per warp, 24 slots
     // (60 KiB) per block: three blocks per SM.
     // max_kept (the node capacity) overestimates a level's keypoints about
     // twice; warps stride over the tasks
-    const int wpb = 12 / R;
-    const size_t smem = (size_t)2 * R * wpb * DESC_SLOT + 128 + sizeof(int) * (ndescs + 1);
+    const int wpb = 24 / (R * D);
+    const size_t smem = (size_t)D * R * wpb * DESC_SLOT + 128 + sizeof(int) * (ndescs + 1);
     const long want = ((long)ndescs * max_kept / 2 + 32 * wpb - 1) / (32 * wpb);
     const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 3));
     auto run = [&](auto kernel) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kernel<<<blocks, 32 * wpb, smem, st>>>(descs, ndescs, kps, desc, status);
     };
-    switch (R) {
-        case 1: run(k_describe<1, 12>); break;
-        case 4: run(k_describe<4, 3>); break;
-        default: run(k_describe<2, 6>); break;
+    switch (R * 8 + D) {
+        case 1 * 8 + 2: run(k_describe<1, 2, 12>); break;
+        case 1 * 8 + 4: run(k_describe<1, 4, 6>); break;
+        case 2 * 8 + 4: run(k_describe<2, 4, 3>); break;
+        case 4 * 8 + 2: run(k_describe<4, 2, 3>); break;
+        default: run(k_describe<2, 2, 6>); break;
     }
 }
 

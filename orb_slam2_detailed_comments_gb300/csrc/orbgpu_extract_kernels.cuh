@@ -104,14 +104,16 @@ struct LevelDesc {
 };
 
 // Launch shapes chosen by the autotuner (orbgpu_tune_set): strip rows of the
-// resize and blur / strength kernels, FAST cells per block, keypoints per
-// warp of the descriptor kernel, and the query x train size from which orbgpu_knn2's
-// automatic choice uses the tensor cores.  Changing one bumps the generation,
+// resize and blur / FAST pre-test kernels, warps per block of the FAST cell
+// kernel, keypoints per staging round and rounds in flight of the descriptor
+// kernel, and the query x train size from which orbgpu_knn2's automatic
+// choice uses the tensor cores.  Changing one bumps the generation,
 // so cached frame plans and captured graphs are rebuilt.
 struct Tunables {
     int resize_rows = 36;
     int fast_cells_per_block = 4;
-    int describe_group = 2;
+    int describe_group = 1;
+    int describe_depth = 2;
     long long knn_tc_min_pairs = 1LL << 28;
 };
 const Tunables& tunables();

@@ -22,6 +22,6 @@ def test_table_round_trip_and_merge(tmp_path):
 
 
 def test_parameters_are_the_library_names():
-    assert set(autotune.PARAMS) == {"resize_rows", "fast_cells_per_block", "describe_group"}
+    assert set(autotune.PARAMS) == {"resize_rows", "fast_cells_per_block", "describe_group", "describe_depth"}
     for values, stage in autotune.PARAMS.values():
-        assert stage in ("resize_blur", "fast", "describe") and len(values) >= 3
+        assert stage in ("resize_blur", "fast", "describe") and len(values) >= 2

@@ -13,7 +13,7 @@ def torch():
     t = require_gpu()
     yield t
     from orb_slam2_detailed_comments_gb300 import autotune
-    autotune.apply({"resize_rows": 36, "fast_cells_per_block": 4, "describe_group": 2, "knn_tc_min_pairs": 1 << 28})
+    autotune.apply({"resize_rows": 36, "fast_cells_per_block": 4, "describe_group": 1, "describe_depth": 2, "knn_tc_min_pairs": 1 << 28})
 
 
 def frames():
@@ -28,7 +28,8 @@ def refs(oracle):
 
 @pytest.mark.parametrize("name,value", [("resize_rows", 8), ("resize_rows", 22), ("resize_rows", 64), ("fast_cells_per_block", 1),
                                         ("fast_cells_per_block", 2), ("fast_cells_per_block", 4),
-                                        ("describe_group", 1), ("describe_group", 2), ("describe_group", 4)])
+                                        ("describe_group", 1), ("describe_group", 2), ("describe_group", 4),
+                                        ("describe_depth", 2), ("describe_depth", 4)])
 def test_batch_shapes_match_oracle(torch, refs, name, value):
     from orb_slam2_detailed_comments_gb300 import autotune
     from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
