@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import os
 import statistics
@@ -27,6 +28,7 @@ import subprocess
 import sys
 import threading
 import time
+import traceback
 
 import numpy as np
 
@@ -291,11 +293,17 @@ def run_ours(args):
                     ("distinctive", bench_distinctive), ("frustum", bench_frustum), ("bow", bench_bow)):
         if leg in legs:
             try:
+                # the previous legs' objects are gone and their work done
+                # before this leg starts, and its own before the next: a
+                # leg's asynchronous failure is the leg's
+                gc.collect()
+                torch.cuda.synchronize()
                 extra[LEG_KEYS[leg]] = fn(dev)
-                torch.cuda.synchronize()  # a leg's asynchronous failure is the leg's
+                gc.collect()
+                torch.cuda.synchronize()
             except Exception as e:  # reported, not fatal
                 extra[LEG_KEYS[leg]] = {"error": repr(e)}
-                print(f"leg {leg} failed: {e!r}", file=sys.stderr, flush=True)
+                print(f"leg {leg} failed: {e!r}\n{traceback.format_exc()}", file=sys.stderr, flush=True)
     tuning = dict(tuning, search_rounds=search_rounds, e2e_ways=e2e_ways)
     return finish(args, legs, frames, value, total_ms, stage_ms, e2e_value, h2d, d2h, per_frame_fps, per_frame_split,
                   extra, mps_list, mpd_list, clk, batch, proj, tuning)
@@ -815,7 +823,11 @@ def bench_distinctive(dev, steps=10, warmup=3):
     over a 5.9M-row descriptor pool (every observation a noisy copy of its map
     point's descriptor, 1/8 of the bits flipped), descriptors written back.
     Device-resident (kernel events, L2 flushed between launches), end to end
-    from page-locked host buffers, and the oracle on one host core."""
+    from page-locked host buffers (copied in, results copied out; the kernel
+    reading the 188 MB pool in place over the host link was slower, 0.50 G
+    against 0.59 G map points/s, and is not run here: a full bench run in
+    which it was the step in flight raised a GPU memory fault whose cause is
+    not established), and the oracle on one host core."""
     import torch
     from oracle import pyoracle
     from orb_slam2_detailed_comments_gb300 import compute_distinctive_descriptors
@@ -847,24 +859,21 @@ def bench_distinctive(dev, steps=10, warmup=3):
         ms.append(e0.elapsed_time(e1))
     dev_ms = statistics.median(ms)
     gpu_best = best.cpu().numpy()
-    # end to end: host arrays in page-locked memory, (a) copied in and the
-    # results copied out, (b) read in place by the kernel (results copied out)
+    # end to end: host arrays in page-locked memory copied in, the results
+    # copied out
     hP, hO, hR = (torch.from_numpy(a).pin_memory() for a in (pool, offsets, rows))
     hB = torch.empty(m, dtype=torch.int32).pin_memory()
     hD = torch.empty((m, 32), dtype=torch.uint8).pin_memory()
     ways = {}
-    for way in ("copies", "in_place"):
+    for way in ("copies",):
         for it in range(warmup + steps):
             if it == warmup:
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
-            if way == "copies":
-                P.copy_(hP, non_blocking=True)
-                O.copy_(hO, non_blocking=True)
-                R.copy_(hR, non_blocking=True)
-                b = compute_distinctive_descriptors(P, O, R, D, validate=False)
-            else:
-                b = compute_distinctive_descriptors(hP, hO, hR, D, validate=False)
+            P.copy_(hP, non_blocking=True)
+            O.copy_(hO, non_blocking=True)
+            R.copy_(hR, non_blocking=True)
+            b = compute_distinctive_descriptors(P, O, R, D, validate=False)
             hB.copy_(b, non_blocking=True)
             hD.copy_(D, non_blocking=True)
             torch.cuda.current_stream(dev).synchronize()

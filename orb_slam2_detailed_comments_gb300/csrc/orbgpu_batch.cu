@@ -1069,7 +1069,6 @@ struct orbgpu_batch_proj {
     int last_launches = 0;
     int last_rounds = 0;  // fixed-point rounds of the slowest frame (shared-memory resolution)
     int mode = 0;  // 0: shared-memory resolution when the frames fit; 1: global-memory rounds
-    int smem_attr = 0;  // dynamic shared memory the resolution kernel was last allowed
     // frame info and map point offsets as last uploaded (skipped when unchanged)
     std::vector<uint8_t> last_upload;
     uint8_t* h_stage = nullptr;  // pinned staging of the uploads
@@ -1192,11 +1191,7 @@ extern "C" int orbgpu_batch_search_by_projection(orbgpu_batch* b, const orbgpu_k
         const size_t smem_max = 226 * 1024;  // below the 227 KiB per-block limit with the static part
         if (P.mode == 0 && cap < 4096 && fixed + 4 * 1024 <= smem_max) {
             const size_t smem = smem_max;
-            if (P.smem_attr != (int)smem) {
-                ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bproj_resolve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)smem));
-                P.smem_attr = (int)smem;
-            }
+            ORBGPU_CUDA_TRY(allow_max_dynamic_smem(k_bproj_resolve_smem));
             k_bproj_resolve_smem<<<nf, 1024, smem, st>>>(kps, cap, counts, d_off, P.slot_cap, slots, slot_count, nnratio,
                                                          (int)smem, match_out, nmatches, status);
             ORBGPU_CUDA_TRY(cudaGetLastError());
@@ -1643,7 +1638,7 @@ extern "C" int orbgpu_batch_search_by_projection_frame(orbgpu_batch* b, const or
             orbgpu_set_last_error("batched frame search: a frame's map points exceed shared memory", __FILE__, __LINE__);
             return ORBGPU_ERR_CAPACITY;
         }
-        ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bpf_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ORBGPU_CUDA_TRY(allow_max_dynamic_smem(k_bpf_resolve));
         k_bpf_resolve<<<nf, 1024, smem, st>>>(kps, cap, counts, last_kps, last_mps, d_off, P.slot_cap, slots, slot_count,
                                                check_ori, t_cap, match_out, nmatches, status);
         ORBGPU_CUDA_TRY(cudaGetLastError());

@@ -627,12 +627,7 @@ extern "C" int orbgpu_bow_transform(const orbgpu_vocabulary* v, const uint8_t* d
         ORBGPU_CUDA_TRY(cudaMemsetAsync(fv_counts, 0, sizeof(int) * nframes, st));
         return ORBGPU_OK;
     }
-    static bool smem_set = false;
-    if (!smem_set) {
-        ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_bow_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             BOW_MAX_FEATURES * 8));
-        smem_set = true;
-    }
+    ORBGPU_CUDA_TRY(allow_max_dynamic_smem(k_bow_assemble));
     const int blocks = nsm_of_current_device() * 8;
     k_bow_descend<<<blocks, BOW_THREADS, 0, st>>>(reinterpret_cast<const uint4*>(desc), offsets, nframes,
                                                   v->child_desc, v->child_start, v->pos_node, v->node_word,

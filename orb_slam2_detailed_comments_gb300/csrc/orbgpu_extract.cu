@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -27,6 +28,24 @@ void orbgpu_set_last_error(const char* msg, const char* file, int line) {
 
 extern "C" const char* orbgpu_last_error(void) { return g_last_error.c_str(); }
 extern "C" int orbgpu_version(void) { return 1; }
+
+cudaError_t orbgpu::allow_max_dynamic_smem(const void* kernel) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void*>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({dev, kernel})) return cudaSuccess;
+    int optin = 0;
+    cudaFuncAttributes fa;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess ||
+        (e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess)
+        return e;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) done.insert({dev, kernel});
+    return e;
+}
 
 static std::atomic<int> g_fail_allocs{0};
 cudaError_t orbgpu::dev_malloc(void** p, size_t bytes) {

@@ -1512,7 +1512,7 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
     // contiguous run of cells
     const int nsm = nsm_of_current_device();
     auto run = [&](auto kernel) {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem(kernel);
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * cpb, smem) != cudaSuccess || per_sm < 1)
             per_sm = 1;
@@ -1527,7 +1527,7 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
 }
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {
     const size_t smem = (size_t)sort_cap * sizeof(unsigned long long);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_distribute, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) allow_max_dynamic_smem(k_distribute);
     if (ndescs > 0) k_distribute<<<ndescs, 512, smem, st>>>(descs, status);
 }
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
@@ -1544,7 +1544,7 @@ void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_ke
     const long want = ((long)ndescs * max_kept / 2 + 32 * wpb - 1) / (32 * wpb);
     const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 3));
     auto run = [&](auto kernel) {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem(kernel);
         kernel<<<blocks, 32 * wpb, smem, st>>>(descs, ndescs, kps, desc, status);
     };
     switch (R * 8 + D) {

@@ -75,6 +75,19 @@ int build_sincos_table(const char* path, int threads);
 // const Frame&) (src/ORBmatcher.cc:1724-1741): 1 forward, 2 backward, 0 neither.
 int motion_level_mode(const orbgpu_frame_motion& mo, int mono);
 
+// Raises a kernel's dynamic shared memory limit, once per kernel and device,
+// to the most the device allows a block (less the kernel's static shared
+// memory).  The limit is a function attribute shared by every thread and
+// stream of the process: set per launch to the launch's own size, one thread
+// could lower it below what another thread's launch in flight or captured
+// graph needs.  The limit only caps requests: a launch still gets the size it
+// asks for.
+cudaError_t allow_max_dynamic_smem(const void* kernel);
+template <typename K>
+inline cudaError_t allow_max_dynamic_smem(K* kernel) {
+    return allow_max_dynamic_smem(reinterpret_cast<const void*>(kernel));
+}
+
 // SM count of the current device, cached per device ordinal.
 inline int nsm_of_current_device() {
     static int cache[64] = {};

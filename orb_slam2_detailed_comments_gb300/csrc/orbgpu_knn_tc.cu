@@ -390,7 +390,7 @@ extern "C" int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, f
     k_expand_fp8<<<128 * 16 / 256, 256>>>(dq, 128, TC_M, eq);
     k_expand_fp8<<<256 * 16 / 256, 256>>>(dt, 256, TC_N, et);
     const size_t smem = TC_QTILE_BYTES + TC_TTILE_BYTES;
-    ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_tc_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ORBGPU_CUDA_TRY(allow_max_dynamic_smem(k_tc_probe));
     k_tc_probe<<<1, 128, smem>>>(eq, et, dd, st, (uint32_t)lbo, (uint32_t)sbo);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaDeviceSynchronize());
@@ -430,7 +430,7 @@ int orbgpu_knn2_tc(orbgpu_matcher* m, const uint8_t* query, int nq, const uint8_
     k_expand_fp8<<<qt * TC_M * 16 / 256, 256, 0, st>>>(query, nq, TC_M, eq);
     k_expand_fp8<<<tt * TC_N * 16 / 256, 256, 0, st>>>(train, nt, TC_N, et);
     const size_t smem = TC_QTILE_BYTES + 2 * TC_TTILE_BYTES;
-    ORBGPU_CUDA_TRY(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ORBGPU_CUDA_TRY(allow_max_dynamic_smem(k_knn_tc));
     dim3 grid(qt, nslices);
     k_knn_tc<<<grid, TC_THREADS, smem, st>>>(eq, et, nq, nt, per, partial, status);
     knn_merge_launch(partial, nq, nslices, idx1, d1, idx2, d2, st);
