@@ -139,14 +139,17 @@ def _level_sizes(w, h):
 # pixel and issue-active share from an ncu capture of the same build
 # (profiles/), None until one was taken.
 ISSUE_ROOFLINE = {
-    "kernel": "k_level_strip<22>, level 0 of the 64-frame step",
-    "warp_instructions_per_pixel": 1.78, "issue_active_pct_of_peak": 68.3,
-    "stage_warp_instructions_per_step_M": {"k_level_strip": 185, "k_fast_score": 65, "k_level_resize": 70},
-    "issue_floor_ms_per_step": 0.25,
-    "note": "estimates: the strip at its level-0 rate over all 104 M pixels of a step, the score kernel as "
-            "captured, the resize kernel scaled from a capture of one level; at 4 warp instructions per SM "
-            "cycle (152 SMs, 2.07 GHz) they take about 0.25 ms -- the stage's issue floor; its HBM floor "
-            "(algorithmic bytes at the measured copy bandwidth) is 0.047 ms",
+    "kernels": "k_level_strip<22> (level 0), k_level_resize<22> (level 1), k_fast_cells<4> (all 93,211 cells) "
+               "of the 64-frame step",
+    "strip_warp_instructions_per_level0_pixel": 1.57, "strip_issue_active_pct_of_peak": 75.6,
+    "cells_warp_instructions_per_cell": 1307, "cells_issue_active_pct_of_peak": 61.8,
+    "stage_warp_instructions_per_step_M": {"k_level_strip": 163, "k_fast_cells": 122, "k_level_resize": 57},
+    "issue_floor_ms_per_step": 0.27,
+    "note": "the strip at its level-0 rate over all 104 M pixels of a step, the resize at its level-1 rate over "
+            "the 70 M pixels of levels 1-7, the cell kernel as captured; at 4 warp instructions per SM cycle "
+            "(152 SMs, 2.07 GHz) they take about 0.27 ms -- the stage's issue floor; its HBM floor (algorithmic "
+            "bytes at the measured copy bandwidth) is 0.047 ms, so these instruction counts cap the stage's "
+            "HBM fraction near 0.17",
     "source": "profiles/extract_kernels_64frames.md (ncu --set full, one launch per kernel)"}
 
 
@@ -824,10 +827,9 @@ def bench_distinctive(dev, steps=10, warmup=3):
     point's descriptor, 1/8 of the bits flipped), descriptors written back.
     Device-resident (kernel events, L2 flushed between launches), end to end
     from page-locked host buffers (copied in, results copied out; the kernel
-    reading the 188 MB pool in place over the host link was slower, 0.50 G
-    against 0.59 G map points/s, and is not run here: a full bench run in
-    which it was the step in flight raised a GPU memory fault whose cause is
-    not established), and the oracle on one host core."""
+    reading the 188 MB pool in place over the host link measured slower, 0.50 G
+    against 0.59 G map points/s, and is not repeated here), and the oracle on
+    one host core."""
     import torch
     from oracle import pyoracle
     from orb_slam2_detailed_comments_gb300 import compute_distinctive_descriptors
