@@ -1343,7 +1343,8 @@ def main():
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames per step (the reported workload is 64; other values are for profiling)")
     ap.add_argument("--shapes", default="",
-                    help="pin the launch shapes resize_rows,fast_cells_per_block,describe_group (no tuning)")
+                    help="pin the launch shapes resize_rows,fast_cells_per_block,describe_group,describe_depth "
+                         "(no tuning)")
     ap.add_argument("--legs", default="all",
                     help="comma list of extra measurements (e2e,perframe,stereo,knn,serving,distinctive,frustum,bow,cpu) "
                          "or 'all'")

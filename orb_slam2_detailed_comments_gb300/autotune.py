@@ -1,10 +1,11 @@
 """Autotuner of the launch shapes.
 
-Chooses, on the device at hand, the strip rows of the resize / blur / FAST
-strength kernel, the FAST cells per block, the keypoints per warp of the
-descriptor kernel (each timed on the pipeline stage it shapes, from the
-stage events of a batch extraction) and the problem size from which the kNN
-uses the tensor cores instead of the popcount kernel.  Results never depend
+Chooses, on the device at hand, the strip rows of the resize and blur / FAST
+pre-test kernels, the warps per block of the FAST cell kernel, the keypoints
+per staging round and the rounds in flight of the descriptor kernel (each
+timed on the pipeline stage it shapes, from the stage events of a batch
+extraction) and the problem size from which the kNN uses the tensor cores
+instead of the popcount kernel.  Results never depend
 on these choices; only the time does.
 
 The table is JSON keyed by workload: ``"<W>x<H>/<nFeatures>"`` for a single

@@ -152,9 +152,11 @@ class ServingEngine:
     # ---------------------------------------------------------------- admission
     def stream_bytes(self, w: int, h: int) -> int:
         # previous keypoints + map points + descriptors, the page-locked image
-        # and its share of a batch arena (pyramid and blurred levels, FAST
-        # candidate and corner lists: ~4 * 3.1 * w * h)
-        return self.cap * (28 + 16 + 32) + w * h + int(4 * 3.1 * w * h) + 64 * 1024
+        # and its share of a batch arena: per level the unblurred and blurred
+        # planes and the candidate bit map (~2.2 bytes per level pixel) and
+        # the cell and DistributeOctTree buffers (~3.3), over levels summing
+        # to ~3.3 w h pixels: ~18 w h
+        return self.cap * (28 + 16 + 32) + w * h + 18 * w * h + 64 * 1024
 
     def admit(self, sid: int, width: int, height: int, nfeatures: int, K=None, depth: float = 8.0) -> bool:
         need = self.stream_bytes(width, height)
