@@ -163,7 +163,8 @@ __host__ __device__ __forceinline__ int arc_strength(const uint8_t* roi, int rw,
 // point.  Lane k (k < 30) of the strip's warp produces columns
 // [x0 + 4k, x0 + 4k + 4) of the strip's rows.  The horizontal pass is one
 // dp2a per pixel on the two source bytes that a prmt picks from the lane's
-// source words, which are loaded two rows ahead.  Weights come in pairs
+// source words, which are loaded two rows ahead; a source row shared by two
+// consecutive output rows is loaded and interpolated once.  Weights come in pairs
 // summing to 2047..2049 (checked when the tables are built), so the
 // vertical sum 4 (h0 b0 + h1 b1) + 2^23 stays below 2^32 and its byte 3 is
 // (h0 b0 + h1 b1 + 2^21) >> 22.
@@ -245,14 +246,26 @@ __global__ void __launch_bounds__(32 * RS_WPB) k_level_resize(const LevelDesc* d
         source_words(e1.y, pw[1][3], pw[1][4], pw[1][5]);
     }
     uint8_t* out = d.dst + (size_t)y0 * d.pitch + X;
-    // both source rows interpolated every row: no data-dependent branch
+    // an output row's first source row is usually the previous output row's
+    // second (scale 1.2): its horizontal pass is reused, and its words are
+    // not loaded (the test is the same for every lane of the warp)
+    uint32_t hlast[4] = {0u, 0u, 0u, 0u};
+    int rlast = -1;  // source row of hlast
     auto row_step = [&](int i, uint32_t* cur) {
         const int4 e = rows[i];
         uint32_t ha[4], hb[4];
-        hinterp(e.x, cur[0], cur[1], cur[2], ha);
+        if (e.x == rlast) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) ha[j] = hlast[j];
+        } else {
+            hinterp(e.x, cur[0], cur[1], cur[2], ha);
+        }
         hinterp(e.y, cur[3], cur[4], cur[5], hb);
-        const int4 e2 = rows[min(i + 2, TH)];
-        source_words(e2.x, cur[0], cur[1], cur[2]);
+        rlast = e.y;
+#pragma unroll
+        for (int j = 0; j < 4; j++) hlast[j] = hb[j];
+        const int4 e1 = rows[min(i + 1, TH)], e2 = rows[min(i + 2, TH)];
+        if (e2.x != e1.y) source_words(e2.x, cur[0], cur[1], cur[2]);
         source_words(e2.y, cur[3], cur[4], cur[5]);
         const uint32_t B0 = (uint32_t)e.z & 0xFFFFu, B1 = (uint32_t)e.z >> 16;
         uint32_t v[4];
