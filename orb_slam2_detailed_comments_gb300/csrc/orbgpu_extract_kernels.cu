@@ -442,7 +442,6 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
 
 #define FAST_MAX_ROI 72
 #define FAST_MAX_DET (FAST_MAX_ROI - 6)
-#define FAST_ROW 80                 // staged row: 20 words
 #define FAST_CHUNK 4                // consecutive cells a warp takes at a time
 
 // Largest arc threshold of the pixel at cp (row pitch rw, a shared-memory
@@ -540,16 +539,18 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
                                                           FastCellsSmem sm) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // per warp (sm.warp_bytes, 128-byte aligned): the ROI tile, the strength
-    // window (sm.rows of FAST_ROW bytes), the candidate list (sm.cand_cap
-    // keys), the minThFAST and the iniThFAST survivors (sm.min_cap keys each)
+    // window (sm.rows of ws bytes), the candidate list (sm.cand_cap keys),
+    // which the minThFAST survivors overwrite from its start as the
+    // suppression pass reads it, and the iniThFAST survivors (sm.min_cap keys)
     extern __shared__ __align__(128) uint8_t s_dyn[];
     __shared__ uint64_t s_bar[CPB];
+    const int ws = sm.win_stride;
     const uint32_t dyn0 = smem_u32(s_dyn);
     uint8_t* const tile = s_dyn + (((dyn0 + 127u) & ~127u) - dyn0) + (size_t)warp * sm.warp_bytes;
     uint8_t* const mstr = tile + sm.tile_bytes;
-    uint16_t* const cand = reinterpret_cast<uint16_t*>(mstr + sm.rows * FAST_ROW);
-    uint16_t* const smin = cand + sm.cand_cap;
-    uint16_t* const sini = smin + sm.min_cap;
+    uint16_t* const cand = reinterpret_cast<uint16_t*>(mstr + sm.rows * ws);
+    uint16_t* const smin = cand;
+    uint16_t* const sini = cand + sm.cand_cap;
     uint64_t* const bar = &s_bar[warp];
     if (lane == 0) {
         mbar_init(bar, 1);
@@ -593,7 +594,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         G.rh = maxY - G.iniY;
         const int bw = d.cell_box_w, bh = d.hCell + 6;
         G.ok = !skip && G.rw >= 7 && G.rh >= 7;
-        G.bad = G.ok && (G.rw > FAST_MAX_ROI || G.rh > FAST_MAX_ROI || G.rh - 4 > sm.rows ||
+        G.bad = G.ok && (G.rw > FAST_MAX_ROI || G.rh > FAST_MAX_ROI || G.rh - 4 > sm.rows || G.rw + 2 > sm.win_stride ||
                          (G.rw - 6) * (G.rh - 6) > sm.cand_cap || bw * bh > sm.tile_bytes ||
                          (G.iniX & 15) + G.rw > bw || G.rh > bh);
         G.ok = G.ok && !G.bad;
@@ -658,7 +659,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
             // rows 0 and dh + 1 and everything outside the region stay zero
             {
                 uint4* m16 = reinterpret_cast<uint4*>(mstr);
-                for (int q = lane; q < (dh + 2) * (FAST_ROW / 16); q += 32) m16[q] = make_uint4(0u, 0u, 0u, 0u);
+                for (int q = lane; q < (dh + 2) * (ws / 16); q += 32) m16[q] = make_uint4(0u, 0u, 0u, 0u);
             }
             // the region's candidates, one row per lane (bits of columns gx0
             // .. gx0 + dw - 1, funnel-shifted from the map's words)
@@ -742,7 +743,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
             for (int q = lane; q < ncorner; q += 32) {
                 const int key = cand[q];
                 const int r = key >> 8, c = key & 255;
-                mstr[(r + 1) * FAST_ROW + c + 4] = (uint8_t)tile_arc_strength(org + r * bw + c, bw);
+                mstr[(r + 1) * ws + c + 4] = (uint8_t)tile_arc_strength(org + r * bw + c, bw);
             }
             __syncwarp();  // the tile is read: the next cell's copy may land
             if (more) prefetch(nxt);
@@ -764,10 +765,10 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
                     if (q < ncorner) {
                         key = cand[q];
                         const int r = key >> 8, c = key & 255;
-                        const uint8_t* p = mstr + (r + 1) * FAST_ROW + c + 4;
+                        const uint8_t* p = mstr + (r + 1) * ws + c + 4;
                         const int m = p[0];
-                        int nb = max(max(p[-1], p[1]), max(max(p[-FAST_ROW - 1], p[-FAST_ROW]), p[-FAST_ROW + 1]));
-                        nb = max(nb, max(max(p[FAST_ROW - 1], p[FAST_ROW]), p[FAST_ROW + 1]));
+                        int nb = max(max(p[-1], p[1]), max(max(p[-ws - 1], p[-ws]), p[-ws + 1]));
+                        nb = max(nb, max(max(p[ws - 1], p[ws]), p[ws + 1]));
                         if (m > nb) {
                             oi = m > ini_th;
                             om = m > min_th;
@@ -801,7 +802,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
                 if (rank < cell_cap) {
                     const int r = key >> 8, c = key & 255;
                     out[rank] = (uint32_t)(gx0 + c) | ((uint32_t)(gy0 + r) << 12) |
-                                ((uint32_t)(mstr[(r + 1) * FAST_ROW + c + 4] - 1) << 24);
+                                ((uint32_t)(mstr[(r + 1) * ws + c + 4] - 1) << 24);
                 }
             }
             if (lane == 0) {
@@ -1518,7 +1519,8 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
     const int mw = std::min(FAST_MAX_DET, std::max(1, max_wcell)), mh = sm.rows - 2;
     sm.cand_cap = mw * mh;
     sm.min_cap = ((mw + 1) / 2) * ((mh + 1) / 2);
-    sm.warp_bytes = (sm.tile_bytes + sm.rows * FAST_ROW + 2 * sm.cand_cap + 4 * sm.min_cap + 127) & ~127;
+    sm.win_stride = (mw + 8 + 15) & ~15;
+    sm.warp_bytes = (sm.tile_bytes + sm.rows * sm.win_stride + 2 * sm.cand_cap + 2 * sm.min_cap + 127) & ~127;
     const int cpb = tunables().fast_cells_per_block;
     const size_t smem = (size_t)cpb * sm.warp_bytes + 128;
     // persistent: as many blocks as fit on the device at once, each warp a

@@ -155,10 +155,12 @@ void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStr
 struct FastCellsSmem {
     int tile_bytes;  // the largest ROI box of the launch, 128-byte multiple
     int rows;        // strength window rows: the largest detection region + 2
+    int win_stride;  // strength window row bytes: the largest region width + 8, 16-byte multiple
     int cand_cap;    // candidates: the largest detection region's pixels
     int min_cap;     // survivors kept per threshold
-    // tile_bytes + rows * FAST_ROW + 2 * cand_cap + 4 * min_cap (candidate
-    // list and two survivor lists), 128-byte multiple
+    // tile_bytes + rows * win_stride + 2 * cand_cap + 2 * min_cap (the
+    // candidate list, which the minThFAST survivors reuse, and the iniThFAST
+    // survivors), 128-byte multiple
     int warp_bytes;
 };
 // The cell box width of a level (16-byte multiple covering the ROI from a
