@@ -230,11 +230,15 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.ExternalStream(batch.stream)
 
+    # the frames' argument arrays packed once (the same device buffers every
+    # step)
+    frame_set = batch.frames(imgs_dev, nfs)
+
     def step():
         # the search is queued behind the extraction on the batch's stream
         # (no host round trip between them); wait() reports the extraction's
         # status once the search has synchronised
-        k, d, c = batch.extract(imgs_dev, nfs, wait=False)
+        k, d, c = batch.extract(frame_set, wait=False)
         match, nm = proj.search(mps_dev, mpd_dev, [NMAPPOINTS] * NFRAMES, TH)
         batch.wait()
         return nm
@@ -346,19 +350,21 @@ def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_de
             match_host.copy_(match.view(-1), non_blocking=True)
         torch.cuda.current_stream().wait_stream(stream)
 
+    staging_set, pinned_set = batch.frames(staging, nfs), batch.frames(pinned, nfs)
+
     def step_copies():
         with torch.cuda.stream(stream):
             for s_, p_ in zip(staging, pinned):
                 s_.copy_(p_, non_blocking=True)
             mps_stage.copy_(mps_host, non_blocking=True)
             mpd_stage.copy_(mpd_host, non_blocking=True)
-        k, d, c = batch.extract(staging, nfs, wait=False)
+        k, d, c = batch.extract(staging_set, wait=False)
         match, nm = proj.search(mps_stage, mpd_stage, [NMAPPOINTS] * NFRAMES, TH)
         batch.wait()
         readback(k, d, match)
 
     def step_inplace():
-        k, d, c = batch.extract(pinned, nfs, wait=False)
+        k, d, c = batch.extract(pinned_set, wait=False)
         match, nm = proj.search(mps_host, mpd_host, [NMAPPOINTS] * NFRAMES, TH)
         batch.wait()
         readback(k, d, match)

@@ -11,6 +11,25 @@ from ._lib import MEM_DEVICE, check, lib, ptr
 STAGES = ("gather", "resize_blur", "fast", "distribute", "describe")
 
 
+class FrameSet:
+    """The argument arrays of one list of images (device or page-locked host
+    tensors) and their nFeatures, packed once for repeated extractions of
+    the same buffers (their contents may change between calls; the tensors
+    must not be resized or freed while the set is used: it holds them)."""
+
+    def __init__(self, images, nfeatures):
+        self.images = list(images)
+        n = len(self.images)
+        self.n = n
+        self.ptrs = (C.c_void_p * n)(*[t.data_ptr() for t in self.images])
+        self.ws = np.array([t.shape[1] for t in self.images], np.int32)
+        self.hs = np.array([t.shape[0] for t in self.images], np.int32)
+        self.steps = np.array([t.stride(0) for t in self.images], np.uint64)
+        self.nf = np.array(nfeatures, np.int32)
+        if len(self.nf) != n:
+            raise ValueError("one nFeatures per image")
+
+
 class BatchExtractor:
     """Extraction of many frames of uneven size per call (device images)."""
 
@@ -50,23 +69,27 @@ class BatchExtractor:
     def stream(self) -> int:
         return int(lib().orbgpu_batch_stream(self._h) or 0)
 
-    def extract(self, images, nfeatures, wait: bool = True):
-        """images: list of 2-D uint8 CUDA tensors; nfeatures: list of ints.
-        Returns (keypoints (F*cap, 7) float32 records, descriptors (F*cap, 32),
-        counts (F,)) -- frame f's rows start at f * per_frame_capacity.
-        wait=False returns once the work is queued on the batch's stream
-        (orbgpu_batch_extract_async); wait() then reports its status."""
-        n = len(images)
-        ptrs = (C.c_void_p * n)(*[t.data_ptr() for t in images])
-        ws = np.array([t.shape[1] for t in images], np.int32)
-        hs = np.array([t.shape[0] for t in images], np.int32)
-        steps = np.array([t.stride(0) for t in images], np.uint64)
-        nf = np.array(nfeatures, np.int32)
-        self._keep = (ptrs, ws, hs, steps, nf)
+    @staticmethod
+    def frames(images, nfeatures) -> FrameSet:
+        """The argument arrays of 'images' packed once (see FrameSet), for
+        extract() calls on the same buffers."""
+        return FrameSet(images, nfeatures)
+
+    def extract(self, images, nfeatures=None, wait: bool = True):
+        """images: list of 2-D uint8 CUDA tensors (or page-locked host
+        tensors read in place) with nfeatures a list of ints, or a FrameSet
+        (nfeatures then unused).  Returns (keypoints (F*cap, 7) float32
+        records, descriptors (F*cap, 32), counts (F,)) -- frame f's rows start
+        at f * per_frame_capacity.  wait=False returns once the work is queued
+        on the batch's stream (orbgpu_batch_extract_async); wait() then
+        reports its status."""
+        fs = images if isinstance(images, FrameSet) else FrameSet(images, nfeatures)
+        self._keep = fs
+        n = fs.n
         fn = lib().orbgpu_batch_extract if wait else lib().orbgpu_batch_extract_async
-        check(fn(self._h, n, ptrs, ptr(ws), ptr(hs), ptr(steps), ptr(nf), C.c_float(self.scale_factor), self.nlevels,
-                 self.ini_th, self.min_th, ptr(self.kps), ptr(self.desc), self.per_frame_capacity, MEM_DEVICE,
-                 ptr(self.counts)),
+        check(fn(self._h, n, fs.ptrs, ptr(fs.ws), ptr(fs.hs), ptr(fs.steps), ptr(fs.nf), C.c_float(self.scale_factor),
+                 self.nlevels, self.ini_th, self.min_th, ptr(self.kps), ptr(self.desc), self.per_frame_capacity,
+                 MEM_DEVICE, ptr(self.counts)),
               "orbgpu_batch_extract" if wait else "orbgpu_batch_extract_async")
         return self.kps[: n * self.per_frame_capacity], self.desc[: n * self.per_frame_capacity], self.counts[:n]
 

@@ -50,6 +50,28 @@ def test_batch_extract_vs_oracle(torch, oracle):
             assert np.array_equal(d[f, :c[f]], ref.descriptors)
 
 
+def test_frame_set_equals_the_image_list(torch):
+    """A FrameSet (the argument arrays packed once) extracts what the image
+    list does, also after the buffers' contents change in place."""
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
+    fr = frames(5, 6)
+    imgs = [torch.from_numpy(img).cuda() for img, _ in fr]
+    nfs = [nf for _, nf in fr]
+    b = BatchExtractor(8, 1280, 720, 2000)
+    fs = b.frames(imgs, nfs)
+    for rep in range(3):
+        if rep == 2:  # new pixels in the same buffers
+            for i, t in enumerate(imgs):
+                t.copy_(torch.from_numpy(syn.scene(t.shape[1], t.shape[0], 700 + i)))
+        k1, d1, c1 = (x.clone() for x in b.extract(imgs, nfs))
+        k2, d2, c2 = b.extract(fs)
+        assert torch.equal(c1, c2)
+        for f in range(len(imgs)):
+            n, o = int(c1[f]), f * b.per_frame_capacity
+            assert torch.equal(k1[o:o + n], k2[o:o + n]) and torch.equal(d1[o:o + n], d2[o:o + n])
+
+
 def test_batch_projection_vs_oracle(torch, oracle):
     from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE, MAPPOINT_DTYPE
     from orb_slam2_detailed_comments_gb300.batch import BatchExtractor, BatchProjection
