@@ -84,7 +84,10 @@ class BatchExtractor:
         on the batch's stream (orbgpu_batch_extract_async); wait() then
         reports its status."""
         fs = images if isinstance(images, FrameSet) else FrameSet(images, nfeatures)
-        self._keep = fs
+        # the argument arrays only: the images' owner decides how long they
+        # live (a page-locked tensor held here past this object's stream
+        # would be freed after it)
+        self._keep = (fs.ptrs, fs.ws, fs.hs, fs.steps, fs.nf)
         n = fs.n
         fn = lib().orbgpu_batch_extract if wait else lib().orbgpu_batch_extract_async
         check(fn(self._h, n, fs.ptrs, ptr(fs.ws), ptr(fs.hs), ptr(fs.steps), ptr(fs.nf), C.c_float(self.scale_factor),
