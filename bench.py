@@ -142,8 +142,8 @@ ISSUE_ROOFLINE = {
     "kernels": "k_level_strip<22> (level 0), k_level_resize<22> (level 1), k_fast_cells<4> (all 93,211 cells) "
                "of the 64-frame step",
     "strip_warp_instructions_per_level0_pixel": 1.57, "strip_issue_active_pct_of_peak": 75.6,
-    "cells_warp_instructions_per_cell": 1307, "cells_issue_active_pct_of_peak": 61.8,
-    "stage_warp_instructions_per_step_M": {"k_level_strip": 163, "k_fast_cells": 122, "k_level_resize": 57},
+    "cells_warp_instructions_per_cell": 1323, "cells_issue_active_pct_of_peak": 65.7,
+    "stage_warp_instructions_per_step_M": {"k_level_strip": 163, "k_fast_cells": 123, "k_level_resize": 56},
     "issue_floor_ms_per_step": 0.27,
     "note": "the strip at its level-0 rate over all 104 M pixels of a step, the resize at its level-1 rate over "
             "the 70 M pixels of levels 1-7, the cell kernel as captured; at 4 warp instructions per SM cycle "
