@@ -119,15 +119,13 @@ def test_descriptor_rotation_matches_host_libm(torch, oracle):
     assert np.array_equal(s.cpu().numpy().view(np.uint32), hs.view(np.uint32))
 
 
-def test_fast_stage_per_level(torch, oracle):
-    """The detector stage alone: per level, the GPU's per-cell FAST output (in
-    cell order, retry threshold applied) equals the oracle's cell loop on the
-    same pyramid level, and every candidate's score is its arc strength - 1."""
+def check_fast_levels(torch, oracle, img, nf):
+    """Per level, the GPU's per-cell FAST output (in cell order, retry
+    threshold applied) equals the oracle's cell loop on the same pyramid
+    level, and every candidate's score is its arc strength - 1."""
     import ctypes as C
     from orb_slam2_detailed_comments_gb300._lib import lib, ptr
-    from orb_slam2_detailed_comments_gb300 import synthetic as syn
-    img = syn.scene(1241, 376, 77)
-    ex = extractor(2000)
+    ex = extractor(nf)
     ex(img)
     levels = ex.pyramid_numpy()
     fn = oracle.fn("fast_level")
@@ -158,6 +156,57 @@ def test_fast_stage_per_level(torch, oracle):
         assert lib().orbgpu_debug_fast_strength(ptr(dimg), w, w, h, 7, ptr(smap)) == 0
         sm = smap.cpu().numpy().astype(np.int64)
         assert np.array_equal(sm[gy + 16, gx + 16] - 1, gs), lvl
+
+
+def test_fast_stage_per_level(torch, oracle):
+    """The detector stage alone on a textured scene."""
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    check_fast_levels(torch, oracle, syn.scene(1241, 376, 77), 2000)
+
+
+def dense_textures():
+    """Images whose cells hold far more FAST candidates than one listing batch
+    (256) and, for the noise, more corners than a cell's corner list holds
+    (about 900 candidates and 350 corners per 31 x 32 cell at threshold 7)."""
+    rng = np.random.default_rng(5)
+    noise = rng.integers(0, 256, (480, 640)).astype(np.uint8)
+    yy, xx = np.indices((376, 1241))
+    checker = ((((yy + xx) // 2) % 2) * 200 + rng.integers(0, 40, (376, 1241))).astype(np.uint8)
+    return [("noise", noise), ("checker", checker)]
+
+
+@pytest.mark.parametrize("name", ["noise", "checker"])
+def test_fast_stage_dense_texture(torch, oracle, name):
+    """Cells past the candidate batch and the corner list: the detector stage
+    and the whole extraction equal the oracle's."""
+    img = dict(dense_textures())[name]
+    check_fast_levels(torch, oracle, img, 2000)
+    kps, desc = extractor(2000)(img)
+    ref = oracle.extract(img, nfeatures=2000)
+    assert_kps_equal(kps, ref.keypoints, name)
+    assert np.array_equal(desc, ref.descriptors)
+
+
+def test_batch_dense_texture(torch, oracle):
+    """A batch that mixes dense textures with scenes (the cell kernel's chunks
+    go to whichever warp is free) equals the oracle frame by frame."""
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
+    from orb_slam2_detailed_comments_gb300 import synthetic as syn
+    fr = [(img, 2000) for _, img in dense_textures()] + [(syn.scene(1280, 720, 41), 2000), (syn.scene(640, 480, 42), 1000)]
+    b = BatchExtractor(len(fr), 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    for _ in range(2):
+        k, d, c = b.extract([torch.from_numpy(img).cuda() for img, _ in fr], [nf for _, nf in fr])
+    k = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    d = d.cpu().numpy().reshape(len(fr), cap, 32)
+    c = c.cpu().numpy()
+    for f, (img, nf) in enumerate(fr):
+        ref = oracle.extract(img, nfeatures=nf, want_pyramid=False)
+        n = len(ref.keypoints)
+        assert c[f] == n, f"frame {f}"
+        assert_kps_equal(k[f, :n], ref.keypoints, f"frame {f}")
+        assert np.array_equal(d[f, :n], ref.descriptors), f"frame {f}"
 
 
 # scale factor (2.5: the resize's source span exceeds the 8-byte fast path),
