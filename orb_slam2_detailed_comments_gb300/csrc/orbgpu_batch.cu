@@ -29,35 +29,49 @@ struct ImageSrc {
     int pitch;
 };
 
-// Copies every frame's image into its level-0 plane: one block row per
-// frame row band.  Plane rows are 64-byte aligned; a source row that is
-// 16-byte aligned moves in 16-byte vectors, any other in 4-byte words
-// assembled from bytes.  Bytes past the image width land in the row padding.
-__global__ void k_gather_images(const ImageSrc* src, int nframes) {
+// Copies every frame's image into its level-0 plane: a block takes 8 rows of
+// a frame, one warp per row, and every row moves in 16-byte vectors.  Plane
+// vector j (plane rows are 64-byte aligned) takes source bytes [16 j, 16 j +
+// 16) of the row from the two 16-byte aligned source vectors that hold them,
+// funnel-shifted by the row start's offset.  An aligned 16-byte load that
+// holds a byte of the row cannot leave the row's pages; the second vector is
+// loaded only when it holds one.  Bytes past the image width land in the row
+// padding.
+__device__ __forceinline__ uint4 gather_shift(const uint32_t (&w)[8], int k, int sh) {
+    switch (k) {  // the row start's word offset: uniform over the warp
+        case 0:
+            return make_uint4(__funnelshift_r(w[0], w[1], sh), __funnelshift_r(w[1], w[2], sh),
+                              __funnelshift_r(w[2], w[3], sh), __funnelshift_r(w[3], w[4], sh));
+        case 1:
+            return make_uint4(__funnelshift_r(w[1], w[2], sh), __funnelshift_r(w[2], w[3], sh),
+                              __funnelshift_r(w[3], w[4], sh), __funnelshift_r(w[4], w[5], sh));
+        case 2:
+            return make_uint4(__funnelshift_r(w[2], w[3], sh), __funnelshift_r(w[3], w[4], sh),
+                              __funnelshift_r(w[4], w[5], sh), __funnelshift_r(w[5], w[6], sh));
+        default:
+            return make_uint4(__funnelshift_r(w[3], w[4], sh), __funnelshift_r(w[4], w[5], sh),
+                              __funnelshift_r(w[5], w[6], sh), __funnelshift_r(w[6], w[7], sh));
+    }
+}
+__global__ void __launch_bounds__(256) k_gather_images(const ImageSrc* src, int nframes) {
     const int f = blockIdx.y;
     if (f >= nframes) return;
     const ImageSrc s = src[f];
-    const int rows_per_block = 8;
-    const int y0 = blockIdx.x * rows_per_block;
-    if (y0 >= s.h) return;
-    const int y1 = min(s.h, y0 + rows_per_block);
-    for (int y = y0; y < y1; y++) {
-        const uint8_t* a = s.ptr + (size_t)y * s.step;
-        uint8_t* b = s.dst + (size_t)y * s.pitch;
-        if ((reinterpret_cast<uintptr_t>(a) & 15) == 0) {
-            const int nv = s.w >> 4;
-            for (int v = threadIdx.x; v < nv; v += blockDim.x)
-                reinterpret_cast<uint4*>(b)[v] = reinterpret_cast<const uint4*>(a)[v];
-            for (int x = (nv << 4) + threadIdx.x; x < s.w; x += blockDim.x) b[x] = a[x];
-        } else {
-            for (int x = 4 * threadIdx.x; x < s.w; x += 4 * blockDim.x) {
-                uint32_t wv = 0;
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    if (x + j < s.w) wv |= (uint32_t)a[x + j] << (8 * j);
-                *reinterpret_cast<uint32_t*>(b + x) = wv;
-            }
-        }
+    const int y = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (y >= s.h) return;
+    const uint8_t* a = s.ptr + (size_t)y * s.step;
+    const int off = (int)(reinterpret_cast<uintptr_t>(a) & 15);
+    const uint4* a16 = reinterpret_cast<const uint4*>(a - off);
+    uint4* b16 = reinterpret_cast<uint4*>(s.dst + (size_t)y * s.pitch);
+    const int nv = (s.w + 15) >> 4;  // plane vectors of the row
+    const int span = off + s.w;      // bytes from a16 to the row's end
+    const int k = off >> 2, sh = 8 * (off & 3);
+    for (int j = lane; j < nv; j += 32) {
+        const uint4 v0 = a16[j];
+        uint4 v1 = make_uint4(0u, 0u, 0u, 0u);
+        if (off != 0 && 16 * (j + 1) < span) v1 = a16[j + 1];
+        const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+        b16[j] = gather_shift(w, k, sh);
     }
 }
 

@@ -217,6 +217,36 @@ def test_pinned_host_images_read_in_place(torch):
     assert np.array_equal(m_h.cpu().numpy(), m_dev)
 
 
+@pytest.mark.parametrize("where", ["device", "pinned"])
+def test_strided_images_at_every_row_alignment(torch, oracle, where):
+    """Images as column windows of wider buffers (row steps w + 5 .. w + 13,
+    windows starting 1 .. 7 bytes in), so the rows start at every offset
+    modulo 16: the gather's shifted vector path, against the oracle on the
+    contiguous images."""
+    from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
+    from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
+    fr = frames(17, 5)
+    views = []
+    for f, (img, _) in enumerate(fr):
+        h, w = img.shape
+        off, pad = 1 + (3 * f) % 7, 5 + 2 * f
+        big = torch.zeros((h, w + off + pad), dtype=torch.uint8)
+        big[:, off:off + w] = torch.from_numpy(img)
+        big = big.cuda() if where == "device" else big.pin_memory()
+        views.append(big[:, off:off + w])
+    b = BatchExtractor(len(fr), 1280, 720, 2000)
+    cap = b.per_frame_capacity
+    k, d, c = b.extract(views, [nf for _, nf in fr])
+    k = k.cpu().numpy().view(KEYPOINT_DTYPE).reshape(len(fr), cap)
+    d = d.cpu().numpy().reshape(len(fr), cap, 32)
+    c = c.cpu().numpy()
+    for f, (img, nf) in enumerate(fr):
+        ref = oracle.extract(img, nfeatures=nf, want_pyramid=False)
+        assert c[f] == len(ref.keypoints), f"frame {f}"
+        assert_kps_equal(k[f, :c[f]], ref.keypoints, f"frame {f}")
+        assert np.array_equal(d[f, :c[f]], ref.descriptors)
+
+
 @pytest.mark.parametrize("dz,mono,ori", [(0.0, True, True), (2.0, False, True), (-2.0, False, False)])
 def test_batch_frame_projection_vs_oracle(torch, oracle, dz, mono, ori):
     """SearchByProjection(CurrentFrame, LastFrame) for every frame of a batch,
