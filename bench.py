@@ -330,8 +330,9 @@ def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_de
     into device staging first; or that copy made one step ahead, on a copy
     stream beside the previous step's kernels (two staging sets: every timed
     step holds one step's input copy and its own readback, and the L2 flush
-    between timed steps evicts the inputs copied ahead).  Returns the fastest
-    as the e2e value, with all three."""
+    between timed steps evicts the inputs copied ahead).  The keypoints,
+    descriptors and counts go back while the search runs, the matches after
+    it.  Returns the fastest as the e2e value, with all three."""
     import torch
     dev = mps_dev.device
     pinned = [torch.from_numpy(img).pin_memory() for img, _ in frames]
@@ -339,19 +340,32 @@ def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_de
     kps_host = torch.empty((NFRAMES * cap, 7), dtype=torch.float32).pin_memory()
     desc_host = torch.empty((NFRAMES * cap, 32), dtype=torch.uint8).pin_memory()
     match_host = torch.empty(NFRAMES * cap, dtype=torch.int32).pin_memory()
+    counts_host = torch.empty(2 * NFRAMES, dtype=torch.int32).pin_memory()  # keypoints, then matches per frame
     mps_host = torch.from_numpy(np.concatenate(mps_list).view(np.uint8)).pin_memory()
     mpd_host = torch.from_numpy(np.concatenate(mpd_list)).pin_memory()
     mps_stage = torch.empty_like(mps_dev)
     mpd_stage = torch.empty_like(mpd_dev)
     h2d = sum(t.numel() for t in pinned) + mps_host.numel() + mpd_host.numel()
-    d2h = kps_host.numel() * 4 + desc_host.numel() + match_host.numel() * 4
+    d2h = kps_host.numel() * 4 + desc_host.numel() + match_host.numel() * 4 + counts_host.numel() * 4
+    rb_stream = torch.cuda.Stream(device=dev)
+    extracted = torch.cuda.Event()
 
-    def readback(k, d, match):
-        with torch.cuda.stream(stream):
+    def readback_features(k, d, c):
+        # the extraction's outputs go back on a side stream while the search
+        # (which only reads them) runs
+        extracted.record(stream)
+        rb_stream.wait_event(extracted)
+        with torch.cuda.stream(rb_stream):
             kps_host.copy_(k.view(-1, 7), non_blocking=True)
             desc_host.copy_(d.view(-1, 32), non_blocking=True)
+            counts_host[:NFRAMES].copy_(c, non_blocking=True)
+
+    def readback(match, nm):
+        with torch.cuda.stream(stream):
             match_host.copy_(match.view(-1), non_blocking=True)
+            counts_host[NFRAMES:].copy_(nm, non_blocking=True)
         torch.cuda.current_stream().wait_stream(stream)
+        torch.cuda.current_stream().wait_stream(rb_stream)
 
     staging_set, pinned_set = batch.frames(staging, nfs), batch.frames(pinned, nfs)
 
@@ -362,15 +376,17 @@ def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_de
             mps_stage.copy_(mps_host, non_blocking=True)
             mpd_stage.copy_(mpd_host, non_blocking=True)
         k, d, c = batch.extract(staging_set, wait=False)
+        readback_features(k, d, c)
         match, nm = proj.search(mps_stage, mpd_stage, [NMAPPOINTS] * NFRAMES, TH)
         batch.wait()
-        readback(k, d, match)
+        readback(match, nm)
 
     def step_inplace():
         k, d, c = batch.extract(pinned_set, wait=False)
+        readback_features(k, d, c)
         match, nm = proj.search(mps_host, mpd_host, [NMAPPOINTS] * NFRAMES, TH)
         batch.wait()
-        readback(k, d, match)
+        readback(match, nm)
 
     # two device staging sets: the copy of the next step's inputs runs on a
     # copy stream beside this step's kernels (the set it fills was last read
@@ -395,9 +411,10 @@ def run_e2e(args, frames, batch, proj, stream, flush, mps_list, mpd_list, mps_de
         stream.wait_event(copied[s])  # this step's inputs are in
         k, d, c = batch.extract(sets2[s], wait=False)
         copy_inputs(s ^ 1)  # the next step's, while this step computes
+        readback_features(k, d, c)
         match, nm = proj.search(mps2[s], mpd2[s], [NMAPPOINTS] * NFRAMES, TH)
         batch.wait()
-        readback(k, d, match)
+        readback(match, nm)
         slot[0] = s ^ 1
 
     def timed(step):

@@ -151,6 +151,14 @@ int orbgpu_debug_tc_probe(const uint8_t* q128, const uint8_t* t256, float* dots,
  *   "describe_depth"       staging rounds in flight per warp of the descriptor kernel: 2, 4
  *                          (with describe_group 4, 2 is used)
  *   "knn_tc_min_pairs"     query x train size from which orbgpu_knn2(algo -1) uses tcgen05
+ * and three policies for launches too small to fill the device (one frame, a
+ * few frames), which the autotuner leaves alone:
+ *   "describe_task"        keypoints per descriptor warp task: 0 (by the launch's keypoint
+ *                          count, the default), 8, 16, 32
+ *   "fast_chunk"           consecutive cells per FAST cell warp chunk: 0 (by the launch's
+ *                          cell count, the default), 1, 2, 4
+ *   "strip_rows_small"     strip rows of resize and blur launches whose level-0 strips would
+ *                          not fill the device: 8 (the default), or 0 for resize_rows always
  * Process-wide; a change makes extractors and batches re-plan (and re-capture
  * their graphs) on their next call.  Results do not depend on these values. */
 int orbgpu_tune_set(const char* name, long long value);

@@ -5,8 +5,9 @@ pre-test kernels, the warps per block of the FAST cell kernel, the keypoints
 per staging round and the rounds in flight of the descriptor kernel (each
 timed on the pipeline stage it shapes, from the stage events of a batch
 extraction) and the problem size from which the kNN uses the tensor cores
-instead of the popcount kernel.  Results never depend
-on these choices; only the time does.
+instead of the popcount kernel.  Launches too small to fill the device
+(one frame, a few frames) follow the POLICIES below instead where they
+apply.  Results never depend on these choices; only the time does.
 
 The table is JSON keyed by workload: ``"<W>x<H>/<nFeatures>"`` for a single
 frame configuration, ``"batch:"`` + the sorted distinct configurations for a
@@ -35,6 +36,13 @@ PARAMS = {
     "describe_depth": ((2, 4), "describe"),
 }
 KNN_PARAM = "knn_tc_min_pairs"
+# Launch policies for launches too small to fill the device (not tuned):
+# keypoints per descriptor task and cells per FAST chunk (0: chosen from the
+# launch's size) and the strip rows of short resize / blur launches (8; 0:
+# resize_rows always), with their defaults; FULL_SIZE is what a launch that
+# fills the device uses, which the tuner times the shapes under.
+POLICIES = {"describe_task": 0, "fast_chunk": 0, "strip_rows_small": 8}
+FULL_SIZE = {"describe_task": 32, "fast_chunk": 4, "strip_rows_small": 0}
 
 
 def set_param(name: str, value: int) -> None:
@@ -48,7 +56,7 @@ def get_param(name: str) -> int:
 
 
 def current() -> dict:
-    return {name: get_param(name) for name in list(PARAMS) + [KNN_PARAM]}
+    return {name: get_param(name) for name in list(PARAMS) + list(POLICIES) + [KNN_PARAM]}
 
 
 def workload_key(sizes, nfeatures) -> str:
@@ -61,22 +69,28 @@ def workload_key(sizes, nfeatures) -> str:
 
 def tune_batch(batch, images, nfeatures, reps: int = 5) -> dict:
     """Times every candidate of each parameter on the stage it shapes (median
-    of 'reps' extractions, the other parameters at their current values),
-    leaves the fastest applied and returns {name: {"value", "ms": {v: ms}}}."""
+    of 'reps' extractions, the other parameters at their current values and
+    the small-launch policies at their full-size values), leaves the fastest
+    applied and returns {name: {"value", "ms": {v: ms}}}."""
     out = {}
-    for name, (values, stage) in PARAMS.items():
-        times = {}
-        for v in values:
-            set_param(name, v)
-            batch.extract(images, nfeatures)  # re-plan, capture, warm
-            samples = []
-            for _ in range(reps):
-                batch.extract(images, nfeatures)
-                samples.append(batch.stage_times()[stage])
-            times[v] = statistics.median(samples)
-        best = min(times, key=times.get)
-        set_param(name, best)
-        out[name] = {"value": best, "ms": {str(k): round(t, 5) for k, t in times.items()}}
+    policies = {name: get_param(name) for name in POLICIES}
+    apply(FULL_SIZE)
+    try:
+        for name, (values, stage) in PARAMS.items():
+            times = {}
+            for v in values:
+                set_param(name, v)
+                batch.extract(images, nfeatures)  # re-plan, capture, warm
+                samples = []
+                for _ in range(reps):
+                    batch.extract(images, nfeatures)
+                    samples.append(batch.stage_times()[stage])
+                times[v] = statistics.median(samples)
+            best = min(times, key=times.get)
+            set_param(name, best)
+            out[name] = {"value": best, "ms": {str(k): round(t, 5) for k, t in times.items()}}
+    finally:
+        apply(policies)
     return out
 
 

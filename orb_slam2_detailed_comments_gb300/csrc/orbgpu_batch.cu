@@ -88,8 +88,7 @@ struct FramePlan {
     std::vector<LevelGeom> geom;
     FrameLayout layout;  // offsets relative to the frame's slot
     std::vector<std::vector<uint8_t>> table_blob;  // per level (l >= 1): xofs..ybeta region
-    std::vector<int> tiles;                         // resize/blur blocks per level
-    int gen = -1;                                   // tuning generation the tiles were counted for
+    int gen = -1;                                   // tuning generation when the plan was made
 };
 
 struct orbgpu_batch {
@@ -113,6 +112,7 @@ struct orbgpu_batch {
     int* d_prefix = nullptr;
     size_t prefix_cap = 0;
     std::vector<int> rb_off, rb_count;
+    int rows = 22;  // strip rows of the current batch's resize / blur launches
     int fast_off = 0, fast_count = 0;
     LevelDesc* d_descs = nullptr;
     size_t descs_cap = 0;
@@ -235,10 +235,6 @@ extern "C" int orbgpu_batch_destroy(orbgpu_batch* b) {
 static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out) {
     for (FramePlan* p : b->plans)
         if (p->w == w && p->h == h && p->nf == nf) {
-            if (p->gen != tune_generation()) {  // launch shapes changed: tile counts
-                for (int l = 0; l < b->nlevels; l++) p->tiles[l] = resize_blur_tiles(p->geom[l].w, p->geom[l].h);
-                p->gen = tune_generation();
-            }
             *out = p;
             return ORBGPU_OK;
         }
@@ -255,10 +251,8 @@ static int get_plan(orbgpu_batch* b, int w, int h, int nf, const FramePlan** out
     }
     P->layout.plan(P->geom, 0);
     P->table_blob.assign(b->nlevels, {});
-    P->tiles.assign(b->nlevels, 0);
     for (int l = 0; l < b->nlevels; l++) {
         const LevelGeom& L = P->geom[l];
-        P->tiles[l] = resize_blur_tiles(L.w, L.h);
         if (l == 0) continue;
         const LevelOffsets& o = P->layout.lv[l];
         const size_t lo = o.xofs, hi = o.ybeta + sizeof(short) * 2 * L.h;
@@ -365,8 +359,12 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         }
     }
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(b->d_descs, hd.data(), sizeof(LevelDesc) * ndesc, cudaMemcpyHostToDevice, st));
-    // block ranges: per level the tiles of every frame, then the cells of
-    // every (frame, level) pair
+    // block ranges: per level the tiles of every frame (strips of the rows
+    // that suit the batch's level-0 pixel count), then the cells of every
+    // (frame, level) pair
+    long px = 0;
+    for (int f = 0; f < nframes; f++) px += (long)widths[f] * heights[f];
+    b->rows = strip_rows(px);
     std::vector<int>& pre = b->h_prefix;
     pre.clear();
     b->rb_off.assign(nlevels, 0);
@@ -376,7 +374,7 @@ static int plan_batch(orbgpu_batch* b, int nframes, const int* widths, const int
         int acc = 0;
         for (int f = 0; f < nframes; f++) {
             pre.push_back(acc);
-            acc += b->cur[f]->tiles[l];
+            acc += resize_blur_tiles(b->cur[f]->geom[l].w, b->cur[f]->geom[l].h, b->rows);
         }
         pre.push_back(acc);
         b->rb_count[l] = acc;
@@ -438,13 +436,13 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     cudaStreamWaitEvent(b->side, b->ev_fork, 0);
     for (int l = 1; l < b->nlevels; l++) {
         launch_level_resize(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
-                            b->rb_count[l], b->side);
+                            b->rb_count[l], b->rows, b->side);
         cudaEventRecord(b->ev_level[l], b->side);
     }
     for (int l = 0; l < b->nlevels; l++) {
         if (l > 0) cudaStreamWaitEvent(st, b->ev_level[l], 0);
         launch_level_strip(b->d_descs, RangeMap{b->d_prefix + b->rb_off[l], b->nframes, l, b->nlevels},
-                           b->rb_count[l], st);
+                           b->rb_count[l], b->rows, st);
     }
     mark(2);
     int mwc = 1, mhc = 1, mbox = 0;

@@ -80,6 +80,10 @@ extern "C" int orbgpu_tune_set(const char* name, long long value) {
     else if (n == "describe_group" && (value == 1 || value == 2 || value == 4))
         t.describe_group = (int)value;
     else if (n == "describe_depth" && (value == 2 || value == 4)) t.describe_depth = (int)value;
+    else if (n == "describe_task" && (value == 0 || value == 8 || value == 16 || value == 32))
+        t.describe_task = (int)value;
+    else if (n == "fast_chunk" && (value == 0 || value == 1 || value == 2 || value == 4)) t.fast_chunk = (int)value;
+    else if (n == "strip_rows_small" && (value == 0 || value == 8)) t.strip_rows_small = (int)value;
     else if (n == "knn_tc_min_pairs" && value >= 0) t.knn_tc_min_pairs = value;
     else {
         orbgpu_set_last_error("unknown tuning parameter or value", __FILE__, __LINE__);
@@ -97,6 +101,9 @@ extern "C" int orbgpu_tune_get(const char* name, long long* value) {
     else if (n == "fast_cells_per_block") *value = t.fast_cells_per_block;
     else if (n == "describe_group") *value = t.describe_group;
     else if (n == "describe_depth") *value = t.describe_depth;
+    else if (n == "describe_task") *value = t.describe_task;
+    else if (n == "fast_chunk") *value = t.fast_chunk;
+    else if (n == "strip_rows_small") *value = t.strip_rows_small;
     else if (n == "knn_tc_min_pairs") *value = t.knn_tc_min_pairs;
     else return ORBGPU_ERR_BAD_ARG;
     return ORBGPU_OK;
@@ -540,6 +547,7 @@ struct SizePlan {
     uint8_t* arena = nullptr;
     int* d_items = nullptr;  // block-range prefix arrays
     std::vector<int> rb_first, rb_count;
+    int rows = 22;  // strip rows of the resize / blur launches
     int fast_first = 0, fast_count = 0;
     int max_kept = 0, sort_cap = 0;
     uint64_t last_use = 0;
@@ -620,9 +628,10 @@ static int build_plan(orbgpu_extractor* ex, int w, int h, SizePlan** out) {
     std::vector<int> pre;
     P->rb_first.assign(g.size(), 0);
     P->rb_count.assign(g.size(), 0);
+    P->rows = strip_rows((long)g[0].w * g[0].h);
     for (size_t l = 0; l < g.size(); l++) {
         P->rb_first[l] = (int)pre.size();
-        const int tiles = resize_blur_tiles(g[l].w, g[l].h);
+        const int tiles = resize_blur_tiles(g[l].w, g[l].h, P->rows);
         pre.push_back(0);
         pre.push_back(tiles);
         P->rb_count[l] = tiles;
@@ -817,7 +826,8 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                                                      : cudaMemcpyHostToDevice,
                                       st));
     for (int l = 0; l < nl; l++)
-        launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, st);
+        launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, P.rows,
+                           st);
     int mwc = 1, mhc = 1, mbox = 0;
     for (const LevelGeom& L : g) {
         mwc = std::max(mwc, L.wCell);

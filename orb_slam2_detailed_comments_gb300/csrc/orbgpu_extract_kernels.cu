@@ -442,7 +442,6 @@ __global__ void __launch_bounds__(32 * RS_WPB, 12) k_level_strip(const LevelDesc
 
 #define FAST_MAX_ROI 72
 #define FAST_MAX_DET (FAST_MAX_ROI - 6)
-#define FAST_CHUNK 4                // consecutive cells a warp takes at a time
 
 // Largest arc threshold of the pixel at cp (row pitch rw, a shared-memory
 // tile): max over the sixteen nine-pixel arcs of the arc's smallest
@@ -499,8 +498,9 @@ __device__ __forceinline__ bool tile_is_corner(const uint8_t* cp, int rw, uint32
 }
 
 // The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142).
-// A persistent kernel: each warp takes chunks of FAST_CHUNK consecutive
-// cells of the launch (work item u = a cell of one (frame, level)), the
+// A persistent kernel: each warp takes chunks of 1, 2 or 4 consecutive
+// cells of the launch (work item u = a cell of one (frame, level); four
+// unless the launch has too few cells to give every warp several), the
 // chunks dealt round-robin over the warps, and per cell
 //   1. lane 0 copies the cell's ROI (the detection region and its 3-pixel
 //      ring) into shared memory with one tensor copy (box cell_box_w x
@@ -535,8 +535,8 @@ struct FastCellGeom {
     bool bad;  // the cell exceeds the launch's shared memory (status bit 1)
 };
 template <int CPB>
-__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int total, int* status,
-                                                          FastCellsSmem sm) {
+__global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs, RangeMap rm, int total, int chunk,
+                                                          int* status, FastCellsSmem sm) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // per warp (sm.warp_bytes, 128-byte aligned): the ROI tile, the strength
     // window (sm.rows of ws bytes), the candidate list (sm.cand_cap keys),
@@ -557,12 +557,12 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
         mbar_init_fence();
     }
     __syncwarp();
-    // work: chunks of FAST_CHUNK consecutive cells (one level, mostly: the
-    // tensor map is fenced once per chunk), chunk c to warp c mod nw, so that
-    // the textured parts of an image spread over the warps
+    // work: chunks of 'chunk' (1, 2 or 4) consecutive cells (one level,
+    // mostly: the tensor map is fenced once per chunk), chunk c to warp c mod
+    // nw, so that the textured parts of an image spread over the warps
     const int nw = gridDim.x * CPB, gw = blockIdx.x * CPB + warp;
     auto next_cell = [&](int u) {  // the warp's cell after u
-        return (u + 1) % FAST_CHUNK != 0 ? u + 1 : u + 1 + (nw - 1) * FAST_CHUNK;
+        return ((u + 1) & (chunk - 1)) != 0 ? u + 1 : u + 1 + (nw - 1) * chunk;
     };
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
     int ent = -1, ent_lo = 0, ent_hi = 0;  // the entry of the last cell: items [ent_lo, ent_hi)
@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(32 * CPB) k_fast_cells(const LevelDesc* descs,
     uint32_t par = 0;  // the phase parity the tile's barrier waits for next
     FastCellGeom cur, nxt;
     uint32_t wcur[4], wnxt[4];
-    const int u0 = gw * FAST_CHUNK;
+    const int u0 = gw * chunk;
     if (u0 < total) {
         geom(u0, cur);
         prefetch(cur);
@@ -1173,8 +1173,12 @@ __device__ __forceinline__ float lookup_exception(const uint32_t* keys, const fl
     return v;
 }
 
-// Orientation and descriptor of the kept keypoints, 32 keypoints per warp
-// task (one per lane) and no block-level synchronisation after the prologue.
+// Orientation and descriptor of the kept keypoints, up to 32 keypoints per
+// warp task (one per lane) and no block-level synchronisation after the
+// prologue.  A task holds TS = 8, 16 or 32 keypoints: the smallest size whose
+// tasks fit in one pass of the grid's warps (every block computes the same
+// keypoint total), so a small launch spreads its keypoints over more warps
+// instead of queueing 64 staging rounds on a few ('task' > 0 fixes TS).
 // The task's patches are staged in shared memory by tensor copies in rounds
 // of R keypoints through D buffers of the warp, each with its mbarrier; D
 // rounds are in flight while one is computed:
@@ -1202,8 +1206,8 @@ static_assert(DESC_LBOX_W * DESC_LBOX_H <= DESC_SLOT && DESC_BBOX_W * DESC_BBOX_
                   DESC_SLOT % 128 == 0 && DESC_LBOX_W % 16 == 0 && DESC_BBOX_W % 16 == 0,
               "box slots");
 template <int R, int D, int WPB>
-__global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, int ndescs, orbgpu_keypoint* out_kps,
-                                                       uint8_t* out_desc, int* status) {
+__global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, int ndescs, int task,
+                                                       orbgpu_keypoint* out_kps, uint8_t* out_desc, int* status) {
     extern __shared__ __align__(128) uint8_t s_dyn[];  // boxes (128-byte aligned) | s_pre[ndescs + 1]
     __shared__ int s_scan[32];
     __shared__ float2 s_pat[16][32];   // lane l's pattern point 16 l + p at [p][l]
@@ -1249,13 +1253,15 @@ __global__ void __launch_bounds__(32 * WPB) k_describe(const LevelDesc* descs, i
         for (int v = 0; v <= ORBGPU_HALF_PATCH; v++)
             if (c_umax[v] >= au) vmax = v;
     uint32_t par = 0;  // bit b: the phase parity buffer b waits for next
-    const int ntasks = (total + 31) >> 5;
+    const long grid_warps = (long)gridDim.x * WPB;
+    const int TS = task ? task : total <= 8 * grid_warps ? 8 : total <= 16 * grid_warps ? 16 : 32;
+    const int ntasks = (total + TS - 1) / TS;
     for (int t = blockIdx.x * WPB + warp; t < ntasks; t += gridDim.x * WPB) {
         // this lane's keypoint: level, position, output row, validity
-        const int g = t * 32 + lane;
+        const int g = t * TS + lane;
         int e = 0, x = 0, y = 0, score = 0, o = 0;
         bool valid = false;
-        if (g < total) {
+        if (lane < TS && g < total) {
             int lo = 0, hi = ndescs - 1;  // last e with s_pre[e] <= g
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -1464,9 +1470,9 @@ static void launch_strip(const LevelDesc* descs, RangeMap rm, int nitems, int le
     if (!level0) k_level_resize<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
     k_level_strip<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
 }
-void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
+void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, int rows, cudaStream_t st) {
     if (nitems <= 0) return;
-    switch (tunables().resize_rows) {
+    switch (rows) {
         case 8: launch_strip<8>(descs, rm, nitems, level0, st); break;
         case 22: launch_strip<22>(descs, rm, nitems, level0, st); break;
         case 64: launch_strip<64>(descs, rm, nitems, level0, st); break;
@@ -1482,18 +1488,18 @@ template <int TH>
 static void launch_strip_only(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
     k_level_strip<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
 }
-void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
+void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, int rows, cudaStream_t st) {
     if (nitems <= 0) return;
-    switch (tunables().resize_rows) {
+    switch (rows) {
         case 8: launch_resize_only<8>(descs, rm, nitems, st); break;
         case 22: launch_resize_only<22>(descs, rm, nitems, st); break;
         case 64: launch_resize_only<64>(descs, rm, nitems, st); break;
         default: launch_resize_only<36>(descs, rm, nitems, st); break;
     }
 }
-void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
+void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, int rows, cudaStream_t st) {
     if (nitems <= 0) return;
-    switch (tunables().resize_rows) {
+    switch (rows) {
         case 8: launch_strip_only<8>(descs, rm, nitems, st); break;
         case 22: launch_strip_only<22>(descs, rm, nitems, st); break;
         case 64: launch_strip_only<64>(descs, rm, nitems, st); break;
@@ -1501,11 +1507,23 @@ void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStr
     }
 }
 
-// Blocks of k_level_resize / k_level_strip for a w x h level (RS_WPB strips per block).
-int resize_blur_tiles(int w, int h) {
-    const int th = tunables().resize_rows;
-    const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + th - 1) / th);
+// Blocks of k_level_resize / k_level_strip for a w x h level (RS_WPB strips
+// of 'rows' rows per block).
+int resize_blur_tiles(int w, int h, int rows) {
+    const int strips = ((w + RS_COLS - 1) / RS_COLS) * ((h + rows - 1) / rows);
     return (strips + RS_WPB - 1) / RS_WPB;
+}
+// Strip rows of a launch whose level 0 holds 'px' pixels: the tuned value,
+// or (unless the policy is off) 8 when the tuned strips of level 0 would not
+// fill the device's resident warps one and a half times over (a warp walks
+// its strip's rows one after the other, so a short launch is bound by that
+// walk, not by the work).
+int strip_rows(long px) {
+    const int th = tunables().resize_rows;
+    if (tunables().strip_rows_small == 0 || th <= 8) return th;
+    const long strips = px / ((long)RS_COLS * th);
+    const long resident = (long)nsm_of_current_device() * 12 * RS_WPB;  // k_level_strip: 12 blocks per SM
+    return 2 * strips < 3 * resident ? 8 : th;
 }
 void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, int max_wcell, int max_hcell,
                  int max_box_bytes, cudaStream_t st) {
@@ -1532,7 +1550,15 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * cpb, smem) != cudaSuccess || per_sm < 1)
             per_sm = 1;
         const int blocks = std::max(1, std::min((ncells + cpb - 1) / cpb, nsm * per_sm));
-        kernel<<<blocks, 32 * cpb, smem, st>>>(descs, rm, ncells, status, sm);
+        // chunks of four cells when every warp gets several (the tensor map
+        // is fenced once per chunk), smaller when the launch is short of
+        // cells: a warp's cells run one after the other
+        const long warps = (long)blocks * cpb;
+        const int chunk = tunables().fast_chunk ? tunables().fast_chunk
+                          : ncells >= 4 * warps ? 4
+                          : ncells >= 2 * warps ? 2
+                                                : 1;
+        kernel<<<blocks, 32 * cpb, smem, st>>>(descs, rm, ncells, chunk, status, sm);
     };
     switch (cpb) {
         case 1: run(k_fast_cells<1>); break;
@@ -1550,17 +1576,21 @@ void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_ke
     if (ndescs <= 0 || max_kept <= 0) return;
     const int nsm = nsm_of_current_device();
     const int R = tunables().describe_group, D = R * tunables().describe_depth > 8 ? 2 : tunables().describe_depth;
-    // 32-keypoint warp tasks; D buffers of R box slots per warp, 24 slots
-    // (60 KiB) per block: three blocks per SM.
-    // max_kept (the node capacity) overestimates a level's keypoints about
-    // twice; warps stride over the tasks
+    // D buffers of R box slots per warp, 24 slots (60 KiB) per block: three
+    // blocks per SM.  max_kept (the node capacity) overestimates a level's
+    // keypoints about twice; a grid of 32-keypoint tasks' worth of warps, or
+    // for a launch that would not fill the SMs that way, 8-keypoint tasks'
+    // worth on up to one block per SM (the kernel picks the task size from
+    // the grid and the keypoint count); warps stride over the tasks
     const int wpb = 24 / (R * D);
     const size_t smem = (size_t)D * R * wpb * DESC_SLOT + 128 + sizeof(int) * (ndescs + 1);
-    const long want = ((long)ndescs * max_kept / 2 + 32 * wpb - 1) / (32 * wpb);
+    const long est = (long)ndescs * max_kept / 2;
+    long want = (est + 32 * wpb - 1) / (32 * wpb);
+    if (want < nsm) want = std::min((long)nsm, (est + 8 * wpb - 1) / (8 * wpb));
     const int blocks = (int)std::max(1L, std::min(want, (long)nsm * 3));
     auto run = [&](auto kernel) {
         allow_max_dynamic_smem(kernel);
-        kernel<<<blocks, 32 * wpb, smem, st>>>(descs, ndescs, kps, desc, status);
+        kernel<<<blocks, 32 * wpb, smem, st>>>(descs, ndescs, tunables().describe_task, kps, desc, status);
     };
     switch (R * 8 + D) {
         case 1 * 8 + 2: run(k_describe<1, 2, 12>); break;

@@ -107,13 +107,21 @@ struct LevelDesc {
 // resize and blur / FAST pre-test kernels, warps per block of the FAST cell
 // kernel, keypoints per staging round and rounds in flight of the descriptor
 // kernel, and the query x train size from which orbgpu_knn2's automatic
-// choice uses the tensor cores.  Changing one bumps the generation,
-// so cached frame plans and captured graphs are rebuilt.
+// choice uses the tensor cores.  Three launch policies for launches too
+// small to fill the device (one frame, a few frames): keypoints per
+// descriptor task (0: by the launch's keypoint count, else 8 / 16 / 32),
+// cells per FAST chunk (0: by the launch's cell count, else 1 / 2 / 4) and
+// the strip rows of such launches (8, or 0 for resize_rows always).
+// Changing one bumps the generation, so cached frame plans and captured
+// graphs are rebuilt.
 struct Tunables {
     int resize_rows = 36;
     int fast_cells_per_block = 4;
     int describe_group = 1;
     int describe_depth = 2;
+    int describe_task = 0;
+    int fast_chunk = 0;
+    int strip_rows_small = 8;
     long long knn_tc_min_pairs = 1LL << 28;
 };
 const Tunables& tunables();
@@ -146,11 +154,11 @@ struct RangeMap {
 void upload_constants(cudaStream_t st, const int* taps, const int* umax);
 void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
                            const int* cb, const int* sb, const uint16_t* csub, const uint16_t* ssub, int nbuckets);
-void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st);
+void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, int rows, cudaStream_t st);
 // The two halves of launch_resize_blur, for callers that run them on
 // different streams (the strip of level l after the resize of level l).
-void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
-void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st);
+void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, int rows, cudaStream_t st);
+void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, int rows, cudaStream_t st);
 // Shared memory layout of k_fast_cells for one launch (per warp).
 struct FastCellsSmem {
     int tile_bytes;  // the largest ROI box of the launch, 128-byte multiple
@@ -172,7 +180,8 @@ inline int fast_cell_box_w(int wcell) { return (15 + wcell + 6 + 15) & ~15; }
 // launch (they size its shared memory).
 void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, int max_wcell, int max_hcell,
                  int max_box_bytes, cudaStream_t st);
-int resize_blur_tiles(int w, int h);
+int resize_blur_tiles(int w, int h, int rows);
+int strip_rows(long level0_pixels);
 void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st);

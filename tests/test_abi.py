@@ -75,3 +75,18 @@ def test_bad_arguments_are_rejected_before_any_device_work(library):
     assert library.orbgpu_distinctive_descriptors(C.c_void_p(8), 1, C.c_void_p(16), C.c_void_p(16), 1, 1,
                                                   C.c_void_p(16), None, None) == 1
     assert library.orbgpu_batch_create(0, 640, 480, 1000, None, C.byref(h)) == 1
+
+
+def test_launch_policies_set_and_get_without_gpu(library):
+    """The small-launch policies take exactly their documented values."""
+    import ctypes as C
+    v = C.c_longlong(-1)
+    for name, values in (("describe_task", (0, 8, 16, 32)), ("fast_chunk", (0, 1, 2, 4)), ("strip_rows_small", (0, 8))):
+        assert library.orbgpu_tune_get(name.encode(), C.byref(v)) == 0
+        old = v.value
+        for x in values:
+            assert library.orbgpu_tune_set(name.encode(), C.c_longlong(x)) == 0
+            assert library.orbgpu_tune_get(name.encode(), C.byref(v)) == 0 and v.value == x
+        for bad in (-1, 3, 64):
+            assert library.orbgpu_tune_set(name.encode(), C.c_longlong(bad)) != 0
+        assert library.orbgpu_tune_set(name.encode(), C.c_longlong(old)) == 0

@@ -25,3 +25,9 @@ def test_parameters_are_the_library_names():
     assert set(autotune.PARAMS) == {"resize_rows", "fast_cells_per_block", "describe_group", "describe_depth"}
     for values, stage in autotune.PARAMS.values():
         assert stage in ("resize_blur", "fast", "describe") and len(values) >= 2
+
+
+def test_small_launch_policies():
+    assert set(autotune.POLICIES) == set(autotune.FULL_SIZE) == {"describe_task", "fast_chunk", "strip_rows_small"}
+    assert autotune.POLICIES == {"describe_task": 0, "fast_chunk": 0, "strip_rows_small": 8}
+    assert not set(autotune.POLICIES) & set(autotune.PARAMS)

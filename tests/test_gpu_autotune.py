@@ -14,6 +14,7 @@ def torch():
     yield t
     from orb_slam2_detailed_comments_gb300 import autotune
     autotune.apply({"resize_rows": 36, "fast_cells_per_block": 4, "describe_group": 1, "describe_depth": 2, "knn_tc_min_pairs": 1 << 28})
+    autotune.apply(autotune.POLICIES)
 
 
 def frames():
@@ -26,16 +27,27 @@ def refs(oracle):
     return [oracle.extract(img, nfeatures=nf, want_pyramid=False) for img, nf in frames()]
 
 
-@pytest.mark.parametrize("name,value", [("resize_rows", 8), ("resize_rows", 22), ("resize_rows", 64), ("fast_cells_per_block", 1),
-                                        ("fast_cells_per_block", 2), ("fast_cells_per_block", 4),
-                                        ("describe_group", 1), ("describe_group", 2), ("describe_group", 4),
-                                        ("describe_depth", 2), ("describe_depth", 4)])
+# every tuned shape under the full-size policies (the three-frame batch would
+# otherwise take the small-launch shapes), then every policy value: fixed
+# descriptor task sizes and FAST chunks, 8-row or tuned strips for a short
+# launch, and the automatic choices
+SHAPES = [("resize_rows", 8), ("resize_rows", 22), ("resize_rows", 64), ("fast_cells_per_block", 1),
+          ("fast_cells_per_block", 2), ("fast_cells_per_block", 4), ("describe_group", 1), ("describe_group", 2),
+          ("describe_group", 4), ("describe_depth", 2), ("describe_depth", 4), ("describe_task", 8),
+          ("describe_task", 16), ("describe_task", 32), ("describe_task", 0), ("fast_chunk", 1), ("fast_chunk", 2),
+          ("fast_chunk", 4), ("fast_chunk", 0), ("strip_rows_small", 8), ("strip_rows_small", 0)]
+
+
+@pytest.mark.parametrize("name,value", SHAPES)
 def test_batch_shapes_match_oracle(torch, refs, name, value):
     from orb_slam2_detailed_comments_gb300 import autotune
     from orb_slam2_detailed_comments_gb300._lib import KEYPOINT_DTYPE
     from orb_slam2_detailed_comments_gb300.batch import BatchExtractor
     defaults = autotune.current()
     try:
+        autotune.apply(autotune.FULL_SIZE)
+        if name == "strip_rows_small":
+            autotune.set_param("resize_rows", 22)
         autotune.set_param(name, value)
         fr = frames()
         b = BatchExtractor(4, 1280, 720, 2000)
@@ -76,10 +88,13 @@ def test_tuner_choices_and_knn_auto(torch):
     fr = frames()
     b = BatchExtractor(4, 1280, 720, 2000)
     imgs = [torch.from_numpy(img).cuda() for img, _ in fr]
+    policies = {name: autotune.get_param(name) for name in autotune.POLICIES}
     entry = autotune.tune_batch(b, imgs, [nf for _, nf in fr], reps=2)
     for name, (values, _) in autotune.PARAMS.items():
         assert entry[name]["value"] in values
         assert autotune.get_param(name) == entry[name]["value"]
+    # the small-launch policies are back as they were
+    assert {name: autotune.get_param(name) for name in autotune.POLICIES} == policies
     m = ORBmatcher()
     kn = autotune.tune_knn(m, sizes=((1000, 4000), (4000, 16000)))
     assert kn["value"] > 0 and autotune.get_param("knn_tc_min_pairs") == kn["value"]
