@@ -455,7 +455,7 @@ static void enqueue_pipeline(orbgpu_batch* b, orbgpu_keypoint* kps, uint8_t* des
     launch_fast(b->d_descs, RangeMap{b->d_prefix + b->fast_off, b->ndesc, 0, 1}, b->fast_count, b->d_status, mwc, mhc,
                 mbox, st);
     mark(3);
-    launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->d_status, st);
+    launch_distribute(b->d_descs, b->ndesc, b->sort_cap, b->max_kept, b->d_status, st);
     mark(4);
     launch_describe(b->d_descs, b->ndesc, b->max_kept, kps, desc, b->d_status, st);
     mark(5);

@@ -836,7 +836,7 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
     }
     launch_fast(ex->d_descs, RangeMap{P.d_items + P.fast_first, nl, 0, 1}, P.fast_count, ex->d_status, mwc, mhc, mbox,
                 st);
-    launch_distribute(ex->d_descs, nl, P.sort_cap, ex->d_status, st);
+    launch_distribute(ex->d_descs, nl, P.sort_cap, P.max_kept, ex->d_status, st);
     launch_describe(ex->d_descs, nl, P.max_kept, okps, odesc, ex->d_status, st);
     ORBGPU_CUDA_TRY(cudaGetLastError());
     ORBGPU_CUDA_TRY(cudaMemcpyAsync(ex->h_pinned, ex->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));

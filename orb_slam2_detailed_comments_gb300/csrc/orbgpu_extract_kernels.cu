@@ -857,24 +857,46 @@ __device__ __forceinline__ DNode child_rect(const DNode& n, int q) {
     return c;
 }
 
+// The working arrays of one level's DistributeOctTree: the keys (candidate,
+// node, quadrant) and the nodes (two node lists, quadrant counts, child
+// positions, three scratch ints, best key), each in shared memory when the
+// launch's budget holds it, else in the level's global buffers.
+struct DistArrays {
+    uint32_t* cand;
+    int* node_of;
+    uint8_t* quad;
+    DNode *a, *b;
+    int4 *cnt4, *childpos;
+    int *aux0, *aux1, *aux2;
+    uint32_t* best;
+};
+#define DIST_KEY_BYTES 9  // per key: cand, node_of, quad
+// Shared-memory offsets of the node arrays for nc nodes: a and b, then
+// (16-byte aligned) cnt4 and childpos, then aux0-2 and best; the total is a
+// multiple of 16.
+__host__ __device__ inline size_t dist_nodes_ab(size_t nc) { return (2 * nc * sizeof(DNode) + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t dist_node_bytes(size_t nc) {
+    return (dist_nodes_ab(nc) + 2 * nc * sizeof(int4) + 4 * nc * sizeof(int) + 15) & ~(size_t)15;
+}
+
 // Applies one split step.  split_rank[n] >= 0 is node n's rank in creation
 // order (nsplit nodes split), -1 for nodes kept.  order[rank] = node.
 // Returns (through smem) the new alive count and the number of children with
 // more than one key.
-__device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive, int K, int nsplit, int& next_id,
-                           int& n_big, int* s_scan, int* s_vars) {
-    int* split_rank = d.aux0;
-    int* order = d.aux1;
-    int* base = d.aux2;
+__device__ void split_step(const LevelDesc& d, const DistArrays& m, DNode*& A, DNode*& B, int& alive, int K,
+                           int nsplit, int& next_id, int& n_big, int* s_scan, int* s_vars) {
+    int* split_rank = m.aux0;
+    int* order = m.aux1;
+    int* base = m.aux2;
     // 1. quadrant counts for keys of split nodes
-    for (int n = threadIdx.x; n < alive; n += blockDim.x) d.cnt4[n] = make_int4(0, 0, 0, 0);
+    for (int n = threadIdx.x; n < alive; n += blockDim.x) m.cnt4[n] = make_int4(0, 0, 0, 0);
     __syncthreads();
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        const int n = d.node_of[k];
+        const int n = m.node_of[k];
         if (split_rank[n] < 0) continue;
-        const int q = quadrant_of(d.cand[k], A[n]);
-        d.quad[k] = (uint8_t)q;
-        atomicAdd(&((int*)&d.cnt4[n])[q], 1);
+        const int q = quadrant_of(m.cand[k], A[n]);
+        m.quad[k] = (uint8_t)q;
+        atomicAdd(&((int*)&m.cnt4[n])[q], 1);
     }
     __syncthreads();
     // 2. children per split node, in creation order -> creation base
@@ -884,7 +906,7 @@ __device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive,
         const int rk = b0 + threadIdx.x;
         int c = 0;
         if (rk < nsplit) {
-            const int4 q = d.cnt4[order[rk]];
+            const int4 q = m.cnt4[order[rk]];
             c = (q.x > 0) + (q.y > 0) + (q.z > 0) + (q.w > 0);
         }
         int tot;
@@ -908,7 +930,7 @@ __device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive,
         const int ex = block_exclusive_scan(u, s_scan, &tot);
         if (u) {
             B[E + U + ex] = A[n];
-            d.childpos[n] = make_int4(E + U + ex, 0, 0, 0);
+            m.childpos[n] = make_int4(E + U + ex, 0, 0, 0);
         }
         U += tot;
     }
@@ -916,7 +938,7 @@ __device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive,
     int big = 0;
     for (int rk = threadIdx.x; rk < nsplit; rk += blockDim.x) {
         const int n = order[rk];
-        const int4 q4 = d.cnt4[n];
+        const int4 q4 = m.cnt4[n];
         const int cq[4] = {q4.x, q4.y, q4.z, q4.w};
         int pos4[4] = {-1, -1, -1, -1};
         int r = 0;
@@ -932,17 +954,17 @@ __device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive,
             pos4[q] = pos;
             big += cq[q] > 1;
         }
-        d.childpos[n] = make_int4(pos4[0], pos4[1], pos4[2], pos4[3]);
+        m.childpos[n] = make_int4(pos4[0], pos4[1], pos4[2], pos4[3]);
     }
     __syncthreads();
     // 5. keys follow their nodes
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        const int n = d.node_of[k];
-        const int4 cp = d.childpos[n];
-        if (split_rank[n] < 0) d.node_of[k] = cp.x;
+        const int n = m.node_of[k];
+        const int4 cp = m.childpos[n];
+        if (split_rank[n] < 0) m.node_of[k] = cp.x;
         else {
-            const int q = d.quad[k];
-            d.node_of[k] = q == 0 ? cp.x : (q == 1 ? cp.y : (q == 2 ? cp.z : cp.w));
+            const int q = m.quad[k];
+            m.node_of[k] = q == 0 ? cp.x : (q == 1 ? cp.y : (q == 2 ? cp.z : cp.w));
         }
     }
     // block sum of 'big'
@@ -957,23 +979,66 @@ __device__ void split_step(const LevelDesc& d, DNode*& A, DNode*& B, int& alive,
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int* status) {
+__global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int* status, int sort_cap,
+                                                     int node_smem_cap, int key_smem_cap) {
     const LevelDesc& d = descs[blockIdx.x];
     __shared__ int s_scan[32];
     __shared__ int s_vars[16];
     __shared__ int s_root_cnt[64];
     __shared__ int s_root_pos[64];
-    extern __shared__ unsigned long long s_sort[];
+    // dynamic: the final phase's sort keys (sort_cap), then node arrays for
+    // node_smem_cap nodes (if > 0), then key arrays for key_smem_cap keys
+    extern __shared__ __align__(16) unsigned long long s_sort[];
+    uint8_t* sp = reinterpret_cast<uint8_t*>(s_sort + sort_cap);
+    DistArrays m;
+    if (node_smem_cap >= d.node_cap) {
+        const size_t nc = (size_t)node_smem_cap;
+        m.a = reinterpret_cast<DNode*>(sp);
+        m.b = m.a + nc;
+        m.cnt4 = reinterpret_cast<int4*>(sp + dist_nodes_ab(nc));
+        m.childpos = m.cnt4 + nc;
+        m.aux0 = reinterpret_cast<int*>(m.childpos + nc);
+        m.aux1 = m.aux0 + nc;
+        m.aux2 = m.aux1 + nc;
+        m.best = reinterpret_cast<uint32_t*>(m.aux2 + nc);
+    } else {
+        m.a = (DNode*)d.nodes_a;
+        m.b = (DNode*)d.nodes_b;
+        m.cnt4 = d.cnt4;
+        m.childpos = d.childpos;
+        m.aux0 = d.aux0;
+        m.aux1 = d.aux1;
+        m.aux2 = d.aux2;
+        m.best = d.best;
+    }
+    sp += dist_node_bytes((size_t)node_smem_cap);
     const int ncells = d.nCols * d.nRows;
     // 1. candidates in the reference's emission order: cell rows, cell
-    //    columns, then the detector's row-major order inside each cell.
+    //    columns, then the detector's row-major order inside each cell (the
+    //    count first: it decides where the key arrays live)
     int K = 0;
+    for (int b0 = 0; b0 < ncells; b0 += blockDim.x) {
+        const int c = b0 + threadIdx.x;
+        int tot;
+        block_exclusive_scan(c < ncells ? d.cell_count[c] : 0, s_scan, &tot);
+        K += tot;
+    }
+    if (K <= key_smem_cap) {
+        m.cand = reinterpret_cast<uint32_t*>(sp);
+        m.node_of = reinterpret_cast<int*>(m.cand + key_smem_cap);
+        m.quad = reinterpret_cast<uint8_t*>(m.node_of + key_smem_cap);
+    } else {
+        m.cand = d.cand;
+        m.node_of = d.node_of;
+        m.quad = d.quad;
+    }
+    K = 0;
     for (int b0 = 0; b0 < ncells; b0 += blockDim.x) {
         const int c = b0 + threadIdx.x;
         const int cnt = c < ncells ? d.cell_count[c] : 0;
         int tot;
         const int ex = block_exclusive_scan(cnt, s_scan, &tot);
-        for (int k = 0; k < cnt; k++) d.cand[K + ex + k] = d.slots[(size_t)c * d.cell_cap + k];
+        for (int k = 0; k < cnt; k++) m.cand[K + ex + k] = d.slots[(size_t)c * d.cell_cap + k];
         K += tot;
     }
     __syncthreads();
@@ -981,8 +1046,8 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
         if (threadIdx.x == 0) *d.kept_count = 0;
         return;
     }
-    DNode* A = (DNode*)d.nodes_a;
-    DNode* B = (DNode*)d.nodes_b;
+    DNode* A = m.a;
+    DNode* B = m.b;
     const int minB = ORBGPU_EDGE_THRESHOLD - 3;
     const int Wd = d.maxBorderX - minB, Hd = d.maxBorderY - minB;
     const int nIni = d.nIni;
@@ -991,10 +1056,10 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
     if (threadIdx.x < 64) s_root_cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        const float x = (float)((int)(d.cand[k] & 0xFFF) - minB);
+        const float x = (float)((int)(m.cand[k] & 0xFFF) - minB);
         int r = (int)__fdiv_rn(x, hX);
         if (r >= nIni) { atomicOr(status, 4); r = nIni - 1; }
-        d.node_of[k] = r;
+        m.node_of[k] = r;
         atomicAdd(&s_root_cnt[r], 1);
     }
     __syncthreads();
@@ -1017,7 +1082,7 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
         s_vars[0] = a;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < K; k += blockDim.x) d.node_of[k] = s_root_pos[d.node_of[k]];
+    for (int k = threadIdx.x; k < K; k += blockDim.x) m.node_of[k] = s_root_pos[m.node_of[k]];
     if (threadIdx.x == 0) s_vars[15] = 0;
     int alive = s_vars[0];
     int next_id = nIni;
@@ -1035,14 +1100,14 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
             int tot;
             const int ex = block_exclusive_scan(s, s_scan, &tot);
             if (n < alive) {
-                d.aux0[n] = s ? nsplit + ex : -1;
-                if (s) d.aux1[nsplit + ex] = n;
+                m.aux0[n] = s ? nsplit + ex : -1;
+                if (s) m.aux1[nsplit + ex] = n;
             }
             nsplit += tot;
         }
         __syncthreads();
         int n_big = 0;
-        split_step(d, A, B, alive, K, nsplit, next_id, n_big, s_scan, s_vars);
+        split_step(d, m, A, B, alive, K, nsplit, next_id, n_big, s_scan, s_vars);
         if (s_vars[15]) break;
         if (alive >= N || alive == prev) break;
         if (alive + n_big * 3 > N) { final_phase = true; break; }
@@ -1085,16 +1150,16 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
                     __syncthreads();
                 }
             // children count of each candidate node -> how many to split
-            for (int n = threadIdx.x; n < alive; n += blockDim.x) d.cnt4[n] = make_int4(0, 0, 0, 0);
-            for (int n = threadIdx.x; n < alive; n += blockDim.x) d.aux0[n] = -1;
+            for (int n = threadIdx.x; n < alive; n += blockDim.x) m.cnt4[n] = make_int4(0, 0, 0, 0);
+            for (int n = threadIdx.x; n < alive; n += blockDim.x) m.aux0[n] = -1;
             __syncthreads();
-            for (int j = threadIdx.x; j < nv; j += blockDim.x) d.aux0[(int)(s_sort[j] & 0xFFFF)] = j;
+            for (int j = threadIdx.x; j < nv; j += blockDim.x) m.aux0[(int)(s_sort[j] & 0xFFFF)] = j;
             __syncthreads();
             for (int k = threadIdx.x; k < K; k += blockDim.x) {
-                const int n = d.node_of[k];
-                if (d.aux0[n] < 0) continue;
-                const int q = quadrant_of(d.cand[k], A[n]);
-                atomicAdd(&((int*)&d.cnt4[n])[q], 1);
+                const int n = m.node_of[k];
+                if (m.aux0[n] < 0) continue;
+                const int q = quadrant_of(m.cand[k], A[n]);
+                atomicAdd(&((int*)&m.cnt4[n])[q], 1);
             }
             __syncthreads();
             // prefix of (children - 1) in processing order; first j reaching N
@@ -1106,7 +1171,7 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
                 const int j = b0 + threadIdx.x;
                 int g = 0;
                 if (j < nv) {
-                    const int4 q = d.cnt4[(int)(s_sort[j] & 0xFFFF)];
+                    const int4 q = m.cnt4[(int)(s_sort[j] & 0xFFFF)];
                     g = (q.x > 0) + (q.y > 0) + (q.z > 0) + (q.w > 0) - 1;
                 }
                 int tot;
@@ -1117,16 +1182,16 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
             __syncthreads();
             J = s_vars[1];
             const int nsplit = J + 1;
-            for (int n = threadIdx.x; n < alive; n += blockDim.x) d.aux0[n] = -1;
+            for (int n = threadIdx.x; n < alive; n += blockDim.x) m.aux0[n] = -1;
             __syncthreads();
             for (int j = threadIdx.x; j < nsplit; j += blockDim.x) {
                 const int n = (int)(s_sort[j] & 0xFFFF);
-                d.aux0[n] = j;
-                d.aux1[j] = n;
+                m.aux0[n] = j;
+                m.aux1[j] = n;
             }
             __syncthreads();
             int n_big = 0;
-            split_step(d, A, B, alive, K, nsplit, next_id, n_big, s_scan, s_vars);
+            split_step(d, m, A, B, alive, K, nsplit, next_id, n_big, s_scan, s_vars);
             if (s_vars[15]) break;
             if (alive >= N || alive == prev) break;
             if (guard == 63) atomicOr(status, 8);
@@ -1140,17 +1205,17 @@ __global__ void __launch_bounds__(512) k_distribute(const LevelDesc* descs, int*
         return;
     }
     // 5. per node the key with the largest response, first in key order
-    for (int n = threadIdx.x; n < alive; n += blockDim.x) d.best[n] = 0u;
+    for (int n = threadIdx.x; n < alive; n += blockDim.x) m.best[n] = 0u;
     __syncthreads();
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        const uint32_t p = d.cand[k];
+        const uint32_t p = m.cand[k];
         const uint32_t key = ((p >> 24) << 20) | (uint32_t)(0xFFFFF - k);
-        atomicMax(&d.best[d.node_of[k]], key);
+        atomicMax(&m.best[m.node_of[k]], key);
     }
     __syncthreads();
     for (int n = threadIdx.x; n < alive; n += blockDim.x) {
-        const int k = 0xFFFFF - (int)(d.best[n] & 0xFFFFF);
-        d.kept[n] = d.cand[k];
+        const int k = 0xFFFFF - (int)(m.best[n] & 0xFFFFF);
+        d.kept[n] = m.cand[k];
     }
     if (threadIdx.x == 0) *d.kept_count = alive;
 }
@@ -1566,10 +1631,23 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
         default: run(k_fast_cells<4>); break;
     }
 }
-void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st) {
-    const size_t smem = (size_t)sort_cap * sizeof(unsigned long long);
-    if (smem > 48 * 1024) allow_max_dynamic_smem(k_distribute);
-    if (ndescs > 0) k_distribute<<<ndescs, 512, smem, st>>>(descs, status);
+void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int node_cap, int* status,
+                       cudaStream_t st) {
+    // a 72 KiB budget per block (three 512-thread blocks per SM): the sort
+    // keys, the node arrays of the launch's largest level if they fit, and
+    // the keys of as many candidates as the rest holds (a level with more
+    // keeps them in global memory)
+    const size_t budget = 72 * 1024, sort_b = (size_t)sort_cap * sizeof(unsigned long long);
+    size_t node_b = dist_node_bytes((size_t)node_cap);
+    int node_smem_cap = node_cap;
+    if (sort_b + node_b + 16 * 1024 > budget) {
+        node_b = 0;
+        node_smem_cap = 0;
+    }
+    const int key_smem_cap = (int)(((budget > sort_b + node_b ? budget - sort_b - node_b : 0) / DIST_KEY_BYTES) & ~15);
+    const size_t smem = std::max(budget, sort_b);
+    allow_max_dynamic_smem(k_distribute);
+    if (ndescs > 0) k_distribute<<<ndescs, 512, smem, st>>>(descs, status, sort_cap, node_smem_cap, key_smem_cap);
 }
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st) {

@@ -182,7 +182,10 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
                  int max_box_bytes, cudaStream_t st);
 int resize_blur_tiles(int w, int h, int rows);
 int strip_rows(long level0_pixels);
-void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int* status, cudaStream_t st);
+// DistributeOctTree of every (frame, level); node_cap: the largest level's
+// node capacity (its arrays go to shared memory when they fit).
+void launch_distribute(const LevelDesc* descs, int ndescs, int sort_cap, int node_cap, int* status,
+                       cudaStream_t st);
 void launch_describe(const LevelDesc* descs, int ndescs, int max_kept, orbgpu_keypoint* kps, uint8_t* desc, int* status,
                      cudaStream_t st);
 
