@@ -561,6 +561,11 @@ struct orbgpu_extractor {
     ExtractorTables tables;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // the resize chain of levels 1.. runs on a second stream beside the
+    // strips of the levels already resized (ev_level[l]: level l is written)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_level[ORBGPU_MAX_LEVELS] = {};
     std::vector<SizePlan*> plans;
     SizePlan* cur = nullptr;
     uint64_t use_clock = 0;
@@ -742,6 +747,15 @@ extern "C" int orbgpu_extractor_create(int nfeatures, float scale_factor, int nl
         }
         ex->own_stream = true;
     }
+    bool side_ok = cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking) == cudaSuccess &&
+                   cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 1; i < ORBGPU_MAX_LEVELS && side_ok; i++)
+        side_ok = cudaEventCreateWithFlags(&ex->ev_level[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!side_ok) {
+        orbgpu_set_last_error("stream or event creation failed", __FILE__, __LINE__);
+        orbgpu_extractor_destroy(ex);
+        return ORBGPU_ERR_CUDA;
+    }
     cudaError_t e1 = cudaMalloc(&ex->d_descs, sizeof(LevelDesc) * ORBGPU_MAX_LEVELS);
     cudaError_t e2 = cudaMalloc(&ex->d_status, sizeof(int) * 4);
     cudaError_t e3 = cudaMallocHost(&ex->h_pinned, sizeof(int) * 32);
@@ -769,6 +783,11 @@ extern "C" int orbgpu_extractor_create(int nfeatures, float scale_factor, int nl
 extern "C" int orbgpu_extractor_destroy(orbgpu_extractor* ex) {
     if (!ex) return ORBGPU_OK;
     if (ex->stream) cudaStreamSynchronize(ex->stream);
+    if (ex->side) cudaStreamSynchronize(ex->side);
+    for (int i = 0; i < ORBGPU_MAX_LEVELS; i++)
+        if (ex->ev_level[i]) cudaEventDestroy(ex->ev_level[i]);
+    if (ex->ev_fork) cudaEventDestroy(ex->ev_fork);
+    if (ex->side) cudaStreamDestroy(ex->side);
     for (SizePlan* p : ex->plans) free_plan(p);
     ex->plans.clear();
     cudaFree(ex->d_descs);
@@ -825,9 +844,18 @@ extern "C" int orbgpu_extract(orbgpu_extractor* ex, const uint8_t* image, int wi
                                       image_mem == ORBGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice
                                                                      : cudaMemcpyHostToDevice,
                                       st));
-    for (int l = 0; l < nl; l++)
-        launch_resize_blur(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], l == 0, P.rows,
-                           st);
+    // levels 1.. resized in a chain on the side stream while the strips of
+    // the levels already resized run on the extractor's stream
+    ORBGPU_CUDA_TRY(cudaEventRecord(ex->ev_fork, st));
+    ORBGPU_CUDA_TRY(cudaStreamWaitEvent(ex->side, ex->ev_fork, 0));
+    for (int l = 1; l < nl; l++) {
+        launch_level_resize(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], P.rows, ex->side);
+        ORBGPU_CUDA_TRY(cudaEventRecord(ex->ev_level[l], ex->side));
+    }
+    for (int l = 0; l < nl; l++) {
+        if (l > 0) ORBGPU_CUDA_TRY(cudaStreamWaitEvent(st, ex->ev_level[l], 0));
+        launch_level_strip(ex->d_descs, RangeMap{P.d_items + P.rb_first[l], 1, l, 0}, P.rb_count[l], P.rows, st);
+    }
     int mwc = 1, mhc = 1, mbox = 0;
     for (const LevelGeom& L : g) {
         mwc = std::max(mwc, L.wCell);

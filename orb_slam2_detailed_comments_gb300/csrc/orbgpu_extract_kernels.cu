@@ -499,7 +499,7 @@ __device__ __forceinline__ bool tile_is_corner(const uint8_t* cp, int rw, uint32
 
 // The cell loop of ComputeKeyPointsOctTree (src/ORBextractor.cc:1069-1142).
 // A persistent kernel: each warp takes chunks of 1, 2 or 4 consecutive
-// cells of the launch (work item u = a cell of one (frame, level); four
+// cells of the launch (work item u = a cell of one (frame, level); two
 // unless the launch has too few cells to give every warp several), the
 // chunks dealt round-robin over the warps, and per cell
 //   1. lane 0 copies the cell's ROI (the detection region and its 3-pixel
@@ -1531,21 +1531,6 @@ void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const ui
 }
 
 template <int TH>
-static void launch_strip(const LevelDesc* descs, RangeMap rm, int nitems, int level0, cudaStream_t st) {
-    if (!level0) k_level_resize<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
-    k_level_strip<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
-}
-void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, int rows, cudaStream_t st) {
-    if (nitems <= 0) return;
-    switch (rows) {
-        case 8: launch_strip<8>(descs, rm, nitems, level0, st); break;
-        case 22: launch_strip<22>(descs, rm, nitems, level0, st); break;
-        case 64: launch_strip<64>(descs, rm, nitems, level0, st); break;
-        default: launch_strip<36>(descs, rm, nitems, level0, st); break;
-    }
-}
-
-template <int TH>
 static void launch_resize_only(const LevelDesc* descs, RangeMap rm, int nitems, cudaStream_t st) {
     k_level_resize<TH><<<nitems, 32 * RS_WPB, 0, st>>>(descs, rm);
 }
@@ -1615,14 +1600,12 @@ void launch_fast(const LevelDesc* descs, RangeMap rm, int ncells, int* status, i
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * cpb, smem) != cudaSuccess || per_sm < 1)
             per_sm = 1;
         const int blocks = std::max(1, std::min((ncells + cpb - 1) / cpb, nsm * per_sm));
-        // chunks of four cells when every warp gets several (the tensor map
-        // is fenced once per chunk), smaller when the launch is short of
-        // cells: a warp's cells run one after the other
+        // chunks of two cells when every warp gets several (the tensor map
+        // is fenced once per chunk; on the 64-frame step two measured 2.5 %
+        // faster than four), single cells when the launch is short of cells:
+        // a warp's cells run one after the other
         const long warps = (long)blocks * cpb;
-        const int chunk = tunables().fast_chunk ? tunables().fast_chunk
-                          : ncells >= 4 * warps ? 4
-                          : ncells >= 2 * warps ? 2
-                                                : 1;
+        const int chunk = tunables().fast_chunk ? tunables().fast_chunk : ncells >= 2 * warps ? 2 : 1;
         kernel<<<blocks, 32 * cpb, smem, st>>>(descs, rm, ncells, chunk, status, sm);
     };
     switch (cpb) {

@@ -154,9 +154,9 @@ struct RangeMap {
 void upload_constants(cudaStream_t st, const int* taps, const int* umax);
 void set_sincos_exceptions(const uint32_t* ck, const float* cv, int cn, const uint32_t* sk, const float* sv, int sn,
                            const int* cb, const int* sb, const uint16_t* csub, const uint16_t* ssub, int nbuckets);
-void launch_resize_blur(const LevelDesc* descs, RangeMap rm, int nitems, int level0, int rows, cudaStream_t st);
-// The two halves of launch_resize_blur, for callers that run them on
-// different streams (the strip of level l after the resize of level l).
+// Level l's resize (l >= 1) and its blur / FAST pre-test strips, in strips of
+// 'rows' rows; callers run the resize chain on one stream and the strips on
+// another (the strip of level l after the resize of level l).
 void launch_level_resize(const LevelDesc* descs, RangeMap rm, int nitems, int rows, cudaStream_t st);
 void launch_level_strip(const LevelDesc* descs, RangeMap rm, int nitems, int rows, cudaStream_t st);
 // Shared memory layout of k_fast_cells for one launch (per warp).
