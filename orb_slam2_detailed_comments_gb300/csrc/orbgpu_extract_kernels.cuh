@@ -10,18 +10,19 @@
 //                        detection region (a candidate bit map): one warp per
 //                        120-column strip, rows walked with a 7-row register
 //                        window.
-//   k_fast_cells         one 30-px cell per warp: the cell's ROI staged in
-//                        shared memory by a tensor copy, the arc strength of
-//                        the cell's candidates, per-ROI non-max suppression
-//                        at iniThFAST and minThFAST in one pass (the latter
-//                        used when the former keeps nothing), ordered
-//                        compaction.
+//   k_fast_cells         one 30-px cell at a time per warp (persistent, in
+//                        chunks of 1 or 2 cells): the cell's ROI staged in
+//                        shared memory by a tensor copy, the segment test and
+//                        arc strength of the cell's candidates, per-ROI
+//                        non-max suppression at iniThFAST and minThFAST in
+//                        one pass (the latter used when the former keeps
+//                        nothing), ordered compaction.
 //   k_distribute         one (frame, level) per block: DistributeOctTree as a
 //                        sequence of parallel split steps over node creation
-//                        numbers.
-//   k_describe           32 keypoints per warp, their patches staged in
-//                        shared memory by tensor copies in rounds of 1 to 4:
-//                        IC_Angle, fastAtan2, rBRIEF.
+//                        numbers, its arrays in shared memory when they fit.
+//   k_describe           8, 16 or 32 keypoints per warp task, their patches
+//                        staged in shared memory by tensor copies in rounds
+//                        of 1 to 4: IC_Angle, fastAtan2, rBRIEF.
 #pragma once
 
 #include "orbgpu_common.cuh"
