@@ -161,12 +161,23 @@ __global__ void k_exclusive_scan(const int* in, int n, int* out, int* total) {
 }
 
 // Pass 2: the in-order resolution of src/ORBmatcher.cc:600-677 by one warp.
+// Each keypoint's choice depends on the matched distances the earlier ones
+// left, so the walk is serial and its pace is memory latency: the matched
+// distances and the F2 -> F1 matches live in shared memory when the launch
+// gave 2 * n2 ints of it (smem_n2 >= n2), the candidate ranges are loaded 32
+// keypoints at a time (keypoints without candidates are skipped in order by
+// ballot), and the next keypoint's first 32 candidate keys are loaded while
+// the current one is resolved.
 __global__ void k_init_resolve(const orbgpu_keypoint* kps1, int n1, const orbgpu_keypoint* kps2, int n2,
                                const int* cand_start, const int* cand_count, const uint64_t* cands, float nnratio,
-                               int check_ori, int* matched_dist, int* matches21, int* matches12, int* bin_of,
-                               int* nmatches_out) {
+                               int check_ori, int smem_n2, int* matched_dist_g, int* matches21_g, int* matches12,
+                               int* bin_of, int* nmatches_out) {
+    extern __shared__ int s_init[];
     const int lane = threadIdx.x;
     __shared__ int hist[ORBGPU_HISTO_LENGTH];
+    const bool local = smem_n2 >= n2;
+    int* const matched_dist = local ? s_init : matched_dist_g;
+    int* const matches21 = local ? s_init + n2 : matches21_g;
     if (lane < ORBGPU_HISTO_LENGTH) hist[lane] = 0;
     for (int i = lane; i < n2; i += 32) {
         matched_dist[i] = 0x7fffffff;
@@ -179,65 +190,92 @@ __global__ void k_init_resolve(const orbgpu_keypoint* kps1, int n1, const orbgpu
     __syncwarp();
     int nmatches = 0;
     const float factor = __fdiv_rn((float)ORBGPU_HISTO_LENGTH, 360.0f);
-    for (int i1 = 0; i1 < n1; i1++) {
-        const int s = cand_start[i1], cnt = cand_count[i1];
-        if (cnt == 0) continue;
-        // best: lexicographic (dist, position); second: smallest dist of the others
-        uint64_t best = ~0ull;
-        int second = 0x7fffffff;
-        for (int b = 0; b < cnt; b += 32) {
-            uint64_t key = ~0ull;
-            if (b + lane < cnt) {
-                key = cands[s + b + lane];
-                const int dist = (int)(key >> 40);
-                const int i2 = (int)(key & 0xFFFFF);
-                if (matched_dist[i2] <= dist) key = ~0ull;
+    for (int i0 = 0; i0 < n1; i0 += 32) {
+        // the candidate ranges of keypoints i0 .. i0 + 31, one per lane
+        const int mine = i0 + lane;
+        const int my_s = mine < n1 ? cand_start[mine] : 0, my_c = mine < n1 ? cand_count[mine] : 0;
+        unsigned live = __ballot_sync(0xffffffffu, my_c > 0);
+        if (!live) continue;
+        int j = __ffs(live) - 1;
+        live &= live - 1;
+        int s = __shfl_sync(0xffffffffu, my_s, j), cnt = __shfl_sync(0xffffffffu, my_c, j);
+        uint64_t first = lane < cnt ? cands[s + lane] : ~0ull;  // the keypoint's first 32 keys
+        while (true) {
+            const int i1 = i0 + j;
+            // the next live keypoint's range and first keys, in flight meanwhile
+            const bool more = live != 0;
+            int jn = 0, sn = 0, cn = 0;
+            uint64_t first_n = ~0ull;
+            if (more) {
+                jn = __ffs(live) - 1;
+                live &= live - 1;
             }
-            // merge (best, second) with this lane's key
-            if (key < best) {
-                if (best != ~0ull) second = min(second, (int)(best >> 40));
-                best = key;
-            } else if (key != ~0ull) {
-                second = min(second, (int)(key >> 40));
-            }
-        }
-        // warp merge of (best, second)
-        for (int o = 16; o > 0; o >>= 1) {
-            const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
-            const int os = __shfl_xor_sync(0xffffffffu, second, o);
-            if (ob < best) {
-                second = min(os, best == ~0ull ? 0x7fffffff : (int)(best >> 40));
-                best = ob;
-            } else {
-                second = min(second, min(os, ob == ~0ull ? 0x7fffffff : (int)(ob >> 40)));
-            }
-        }
-        if (best == ~0ull) continue;
-        const int bestDist = (int)(best >> 40);
-        const int bestIdx2 = (int)(best & 0xFFFFF);
-        if (bestDist <= ORBGPU_TH_LOW && (float)bestDist < __fmul_rn((float)second, nnratio)) {
-            if (lane == 0) {
-                const int prev = matches21[bestIdx2];
-                if (prev >= 0) {
-                    matches12[prev] = -1;
-                    nmatches--;
+            sn = __shfl_sync(0xffffffffu, my_s, jn);
+            cn = __shfl_sync(0xffffffffu, my_c, jn);
+            if (more && lane < cn) first_n = cands[sn + lane];
+            // best: lexicographic (dist, position); second: smallest dist of the others
+            uint64_t best = ~0ull;
+            int second = 0x7fffffff;
+            for (int b = 0; b < cnt; b += 32) {
+                uint64_t key = ~0ull;
+                if (b + lane < cnt) {
+                    key = b == 0 ? first : cands[s + b + lane];
+                    const int dist = (int)(key >> 40);
+                    const int i2 = (int)(key & 0xFFFFF);
+                    if (matched_dist[i2] <= dist) key = ~0ull;
                 }
-                matches12[i1] = bestIdx2;
-                matches21[bestIdx2] = i1;
-                matched_dist[bestIdx2] = bestDist;
-                nmatches++;
-                if (check_ori) {
-                    float rot = __fsub_rn(kps1[i1].angle, kps2[bestIdx2].angle);
-                    if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
-                    int bin = (int)roundf(__fmul_rn(rot, factor));
-                    if (bin == ORBGPU_HISTO_LENGTH) bin = 0;
-                    bin_of[i1] = bin;
-                    hist[bin]++;
+                // merge (best, second) with this lane's key
+                if (key < best) {
+                    if (best != ~0ull) second = min(second, (int)(best >> 40));
+                    best = key;
+                } else if (key != ~0ull) {
+                    second = min(second, (int)(key >> 40));
                 }
             }
-            nmatches = __shfl_sync(0xffffffffu, nmatches, 0);
+            // warp merge of (best, second)
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int os = __shfl_xor_sync(0xffffffffu, second, o);
+                if (ob < best) {
+                    second = min(os, best == ~0ull ? 0x7fffffff : (int)(best >> 40));
+                    best = ob;
+                } else {
+                    second = min(second, min(os, ob == ~0ull ? 0x7fffffff : (int)(ob >> 40)));
+                }
+            }
+            if (best != ~0ull) {
+                const int bestDist = (int)(best >> 40);
+                const int bestIdx2 = (int)(best & 0xFFFFF);
+                if (bestDist <= ORBGPU_TH_LOW && (float)bestDist < __fmul_rn((float)second, nnratio)) {
+                    if (lane == 0) {
+                        const int prev = matches21[bestIdx2];
+                        if (prev >= 0) {
+                            matches12[prev] = -1;
+                            nmatches--;
+                        }
+                        matches12[i1] = bestIdx2;
+                        matches21[bestIdx2] = i1;
+                        matched_dist[bestIdx2] = bestDist;
+                        nmatches++;
+                        if (check_ori) {
+                            float rot = __fsub_rn(kps1[i1].angle, kps2[bestIdx2].angle);
+                            if (rot < 0.0f) rot = __fadd_rn(rot, 360.0f);
+                            int bin = (int)roundf(__fmul_rn(rot, factor));
+                            if (bin == ORBGPU_HISTO_LENGTH) bin = 0;
+                            bin_of[i1] = bin;
+                            hist[bin]++;
+                        }
+                    }
+                    nmatches = __shfl_sync(0xffffffffu, nmatches, 0);
+                }
+            }
+            __syncwarp();  // lane 0's updates are seen by the next keypoint's filter
+            if (!more) break;
+            j = jn;
+            s = sn;
+            cnt = cn;
+            first = first_n;
         }
-        __syncwarp();
     }
     if (check_ori) {
         int ind1 = -1, ind2 = -1, ind3 = -1;
@@ -1070,8 +1108,12 @@ extern "C" int orbgpu_search_for_initialization(orbgpu_matcher* m, const orbgpu_
         int* m12 = b.take<int>(n1);
         int* bin_of = b.take<int>(n1);
         int* d_nm = b.take<int>(1);
-        k_init_resolve<<<1, 32, 0, m->stream>>>(s1.kps, n1, s2.kps, n2, start, count, keys, m->nnratio, m->check_ori,
-                                                matched_dist, m21, m12, bin_of, d_nm);
+        // F2's matched distances and matches in shared memory up to 6144
+        // keypoints (48 KiB), else in the scratch buffers
+        const int smem_n2 = n2 <= 6144 ? n2 : 0;
+        k_init_resolve<<<1, 32, sizeof(int) * 2 * (size_t)smem_n2, m->stream>>>(
+            s1.kps, n1, s2.kps, n2, start, count, keys, m->nnratio, m->check_ori, smem_n2, matched_dist, m21, m12,
+            bin_of, d_nm);
         ORBGPU_CUDA_TRY(cudaGetLastError());
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(matches12, m12, sizeof(int) * n1, cudaMemcpyDeviceToHost, m->stream));
         ORBGPU_CUDA_TRY(cudaMemcpyAsync(m->h_pinned, d_nm, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
