@@ -50,3 +50,22 @@ def test_roofline_bytes_of_the_workload():
     assert 9.2 * px < stage < 9.4 * px
     _, whole = bench.extraction_roofline_bytes(frames, [1000] * len(frames))
     assert whole == stage + 60 * 64000
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """Launched as the driver launches N > 1 (torchrun, one process per
+    rank), the reference arm runs on rank 0 alone: one JSON line in all, and
+    every rank exits 0."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+                        "--gpus", "2", "--steps", "1", "--warmup", "0"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d.get("impl") == "reference"
